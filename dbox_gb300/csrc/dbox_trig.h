@@ -1,0 +1,169 @@
+// Portable float sine/cosine used by every rotation update of the step
+// (b2Rot.Set in common/b2math.d:478-488; called from b2Body.SynchronizeTransform
+// b2body.d:1143-1147, b2Sweep.GetTransform b2math.d:556-564 and the position
+// solvers b2contactsolver.d:96-100).
+//
+// The reference calls the C runtime's sinf/cosf, whose results are not
+// correctly rounded (glibc 2.39 differs from the correctly rounded value on
+// about 1% of inputs) and whose algorithm is not part of this project.  This
+// header evaluates sin and cos in IEEE binary64 with only +, -, *, floor-free
+// integer conversions and no fused multiply-add, then rounds once to binary32.
+// The same source compiles for the host (gcc -ffp-contract=off) and for the
+// device (nvcc --fmad=false), so both produce identical bits; the result is the
+// correctly rounded value except when the exact value lies within about 2^-50
+// relative of a binary32 rounding boundary.
+//
+// Method (published, restated here):
+//  * |x| < 2^17: Cody & Waite additive range reduction by pi/2 with a three-part
+//    split of pi/2 (33 + 33 + 53 bits), so k*P1 and k*P2 are exact products.
+//  * |x| >= 2^17: Payne & Hanek reduction: x * (2/pi) mod 4 from 24-bit chunks
+//    of 2/pi (each m*c_i is exact in binary64), summed in double-double.
+//  * Taylor series of sin and cos about 0 for |r| <= pi/4 (Horner form, terms
+//    through r^21 / r^20, truncation error below 2^-60).
+#pragma once
+
+#ifdef __CUDACC__
+#define DBOX_TRIG_HD __host__ __device__ __forceinline__
+#else
+#define DBOX_TRIG_HD static inline
+#endif
+
+#include <stdint.h>
+
+namespace dbox_trig {
+
+// Bits of 2/pi after the binary point, 24 per entry (mpmath, 2000-bit precision).
+#ifdef __CUDACC__
+__host__ __device__
+#endif
+static inline uint32_t two_over_pi_chunk(int i) {
+    // A switch keeps the table out of host/device global memory declarations.
+    switch (i) {
+    case 0: return 0xA2F983u; case 1: return 0x6E4E44u; case 2: return 0x1529FCu;
+    case 3: return 0x2757D1u; case 4: return 0xF534DDu; case 5: return 0xC0DB62u;
+    case 6: return 0x95993Cu; case 7: return 0x439041u; case 8: return 0xFE5163u;
+    case 9: return 0xABDEBBu; case 10: return 0xC561B7u; default: return 0x246E3Au;
+    }
+}
+
+DBOX_TRIG_HD double ldexp_i(double v, int e) {
+    // exact scaling by 2^e for |e| <= 1000 via repeated exact multiplies
+    while (e > 60) { v *= 0x1p60; e -= 60; }      // 2^60
+    while (e < -60) { v *= 0x1p-60; e += 60; }      // 2^-60
+    uint64_t bits = (uint64_t)(e + 1023) << 52;
+    double s;
+    // type pun through a union-free memcpy equivalent
+    union { uint64_t u; double d; } cv; cv.u = bits; s = cv.d;
+    return v * s;
+}
+
+DBOX_TRIG_HD void two_sum(double a, double b, double& s, double& e) {
+    s = a + b;
+    double bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// Reduce |x| (as a float) to r in about [-pi/4, pi/4] and quadrant q in 0..3.
+DBOX_TRIG_HD void reduce(float ax, double& r, int& q) {
+    const double INV_PIO2 = 0x1.45f306dc9c883p-1;
+    const double P1 = 0x1.921fb54400000p+0;
+    const double P2 = 0x1.0b4611a600000p-34;
+    const double P3 = 0x1.3198a2e037073p-69;
+    const double PIO2 = 0x1.921fb54442d18p+0;
+    const double MAGIC = 6755399441055744.0;  // 1.5 * 2^52: round to nearest integer
+    double xd = (double)ax;
+    if (ax < 131072.0f) {
+        double t = xd * INV_PIO2;
+        t = t + MAGIC;
+        t = t - MAGIC;
+        r = ((xd - t * P1) - t * P2) - t * P3;
+        q = ((int)t) & 3;
+        return;
+    }
+    // Payne-Hanek for large arguments: ax = m * 2^e2 with 2^23 <= m < 2^24.
+    union { float f; uint32_t u; } cv; cv.f = ax;
+    int bexp = (int)((cv.u >> 23) & 0xff);
+    uint32_t m = (cv.u & 0x7fffffu) | 0x800000u;
+    int e2 = bexp - 127 - 23;
+    int i0 = (e2 - 2) / 24;  // e2 >= -6 here so e2-2 >= -8; C division truncates toward 0
+    if (e2 - 2 < 0) i0 = 0;
+    double hi = 0.0, lo = 0.0;
+    for (int i = i0; i < i0 + 6; ++i) {
+        double term = ldexp_i((double)((uint64_t)m * (uint64_t)two_over_pi_chunk(i)), e2 - 24 * (i + 1));
+        if (i == i0) {
+            // drop whole multiples of 4 (they do not change sin/cos)
+            double q4 = term * 0.25;
+            q4 = q4 + MAGIC; q4 = q4 - MAGIC;   // nearest integer of term/4
+            if (q4 * 4.0 > term) q4 -= 1.0;     // make it floor
+            term = term - q4 * 4.0;             // exact: both are multiples of the term's ulp
+            hi = term;
+        } else {
+            double s, e;
+            two_sum(hi, term, s, e);
+            hi = s;
+            lo += e;
+        }
+    }
+    double k = hi + MAGIC; k = k - MAGIC;       // nearest integer to hi
+    double f = (hi - k) + lo;
+    r = f * PIO2;
+    q = ((int)k) & 3;
+}
+
+DBOX_TRIG_HD double sin_poly(double r) {
+    const double r2 = r * r;
+    double p = 0x1.71b8ef6dcf572p-66;            //  1/21!
+    p = -0x1.2f49b46814157p-57 + r2 * p;         // -1/19!
+    p =  0x1.952c77030ad4ap-49 + r2 * p;         //  1/17!
+    p = -0x1.ae7f3e733b81fp-41 + r2 * p;         // -1/15!
+    p =  0x1.6124613a86d09p-33 + r2 * p;         //  1/13!
+    p = -0x1.ae64567f544e4p-26 + r2 * p;         // -1/11!
+    p =  0x1.71de3a556c734p-19 + r2 * p;         //  1/9!
+    p = -0x1.a01a01a01a01ap-13 + r2 * p;         // -1/7!
+    p =  0x1.1111111111111p-7 + r2 * p;          //  1/5!
+    p = -0x1.5555555555555p-3 + r2 * p;          // -1/3!
+    return r + (r * r2) * p;
+}
+
+DBOX_TRIG_HD double cos_poly(double r) {
+    const double r2 = r * r;
+    double p = 0x1.e542ba4020225p-62;            //  1/20!
+    p = -0x1.6827863b97d97p-53 + r2 * p;         // -1/18!
+    p =  0x1.ae7f3e733b81fp-45 + r2 * p;         //  1/16!
+    p = -0x1.93974a8c07c9dp-37 + r2 * p;         // -1/14!
+    p =  0x1.1eed8eff8d898p-29 + r2 * p;         //  1/12!
+    p = -0x1.27e4fb7789f5cp-22 + r2 * p;         // -1/10!
+    p =  0x1.a01a01a01a01ap-16 + r2 * p;         //  1/8!
+    p = -0x1.6c16c16c16c17p-10 + r2 * p;         // -1/6!
+    p =  0x1.5555555555555p-5 + r2 * p;          //  1/4!
+    p = -0x1.0000000000000p-1 + r2 * p;          // -1/2!
+    return 1.0 + r2 * p;
+}
+
+}  // namespace dbox_trig
+
+// sin and cos of a binary32 angle, each rounded once from binary64.
+DBOX_TRIG_HD void dbox_sincosf(float x, float* s_out, float* c_out) {
+    union { float f; uint32_t u; } cv; cv.f = x;
+    if ((cv.u & 0x7f800000u) == 0x7f800000u) {  // inf or nan
+        float n = x - x;
+        *s_out = n; *c_out = n;
+        return;
+    }
+    float ax = x < 0.0f ? -x : x;
+    double r; int q;
+    dbox_trig::reduce(ax, r, q);
+    double sr = dbox_trig::sin_poly(r);
+    double cr = dbox_trig::cos_poly(r);
+    double s, c;
+    switch (q) {
+    case 0: s = sr; c = cr; break;
+    case 1: s = cr; c = -sr; break;
+    case 2: s = -sr; c = -cr; break;
+    default: s = -cr; c = sr; break;
+    }
+    if (x < 0.0f) s = -s;
+    if (x == 0.0f) s = (double)x;  // keeps the sign of zero: sin(-0) = -0
+    *s_out = (float)s;
+    *c_out = (float)c;
+}

@@ -1,0 +1,203 @@
+"""Seeded synthetic scenes for the b2World.Step workloads.
+
+Each scene is a dict of plain records (see abi.py): bodies, fixture_body,
+shapes, fixtures, joints, plus gravity.  The same records feed the GPU library
+(dbox_scene_create) and the CPU oracle, so both build identical worlds.
+
+Workloads (sizes as named in the benchmark configuration):
+  pyramid   - static ground box 50x10 half extents at y=-10; 20-row pyramid of
+              210 dynamic SetAsBox(0.5, 0.5) boxes, base row centred at y=0.75,
+              spacing 1.125 m horizontal / 1.0 m vertical, each row shifted by
+              half a spacing (the layout of examples/demo/tests/pyramid.d:51-67
+              with a box ground); density 1, friction 0.6.
+  scatter   - static container of 4 box walls; n dynamic bodies, half circles
+              (r ~ U[0.25,0.5]) and half convex polygons (3..8 points at sorted
+              angles U[0, 2pi), radius U[0.3,0.6], hull by b2PolygonShape.Set) on
+              a jittered grid (spacing 1.3 m, jitter U[-0.1,0.1]), friction
+              U[0.2,0.8], velocity N(0,1) per axis.
+  stacks    - ground box plus columns of unit boxes 1..30 high.
+  batch     - n worlds with body counts log-uniform in [8,512], one third each
+              pyramid / scatter (40 m container) / stacks.
+Random numbers come from numpy's PCG64 generator with the given seed.
+"""
+import math
+
+import numpy as np
+
+from . import abi
+
+F32 = np.float32
+
+
+def _empty():
+    return {
+        "bodies": abi.body_defs(0), "fixture_body": np.zeros(0, np.int32),
+        "shapes": np.zeros(0, abi.SHAPE_DEF), "fixtures": abi.fixture_defs(0),
+        "joints": np.zeros(0, abi.REVOLUTE_DEF), "gravity": (0.0, -10.0), "name": "",
+    }
+
+
+def _concat(parts):
+    """Concatenate scene parts; fixture_body / joint body indices are offset per part."""
+    out = _empty()
+    nb = 0
+    for p in parts:
+        out["bodies"] = np.concatenate([out["bodies"], p["bodies"]])
+        out["fixture_body"] = np.concatenate([out["fixture_body"], p["fixture_body"] + nb]).astype(np.int32)
+        out["shapes"] = np.concatenate([out["shapes"], p["shapes"]])
+        out["fixtures"] = np.concatenate([out["fixtures"], p["fixtures"]])
+        j = p["joints"].copy()
+        j["body_a"] += nb
+        j["body_b"] += nb
+        out["joints"] = np.concatenate([out["joints"], j])
+        nb += len(p["bodies"])
+    return out
+
+
+def _boxes(centers, hx, hy, btype, friction=0.6, density=1.0):
+    n = len(centers)
+    s = _empty()
+    b = abi.body_defs(n)
+    b["type"] = btype
+    b["position"] = np.asarray(centers, F32)
+    s["bodies"] = b
+    s["fixture_body"] = np.arange(n, dtype=np.int32)
+    sh = np.zeros(n, abi.SHAPE_DEF)
+    sh["kind"] = abi.SHAPE_BOX
+    sh["hx"] = hx
+    sh["hy"] = hy
+    s["shapes"] = sh
+    f = abi.fixture_defs(n)
+    f["friction"] = F32(friction)
+    f["density"] = F32(density if btype == abi.DYNAMIC else 0.0)
+    s["fixtures"] = f
+    return s
+
+
+def ground_box(hx=50.0, hy=10.0, y=-10.0):
+    return _boxes([(0.0, y)], hx, hy, abi.STATIC)
+
+
+def pyramid(rows=20, box=0.5, dx=1.125, dy=1.0, y0=0.75, friction=0.6, density=1.0, ground=True):
+    """Pyramid of rows*(rows+1)/2 boxes; positions accumulate in float32 like pyramid.d:59-70."""
+    centers = []
+    x = np.array([-(rows - 1) * dx / 2.0, y0], F32)
+    delta_x = np.array([dx / 2.0, dy], F32)
+    delta_y = np.array([dx, 0.0], F32)
+    for i in range(rows):
+        y = x.copy()
+        for _ in range(i, rows):
+            centers.append(y.copy())
+            y = (y + delta_y).astype(F32)
+        x = (x + delta_x).astype(F32)
+    parts = []
+    if ground:
+        parts.append(ground_box())
+    parts.append(_boxes(centers, box, box, abi.DYNAMIC, friction, density))
+    s = _concat(parts)
+    s["name"] = "pyramid%d" % rows
+    return s
+
+
+def container(width, height, thick=1.0):
+    """Four static box walls enclosing [-width/2, width/2] x [0, height]."""
+    hw = width / 2.0
+    parts = [
+        _boxes([(0.0, -thick)], hw + thick, thick, abi.STATIC),
+        _boxes([(0.0, height + thick)], hw + thick, thick, abi.STATIC),
+        _boxes([(-hw - thick, height / 2.0)], thick, height / 2.0 + 2 * thick, abi.STATIC),
+        _boxes([(hw + thick, height / 2.0)], thick, height / 2.0 + 2 * thick, abi.STATIC),
+    ]
+    return _concat(parts)
+
+
+def scatter(n, width, height, rng, spacing=1.3, jitter=0.1, y_base=1.0):
+    """n mixed circles/polygons on a jittered grid inside a width x height container."""
+    cols = max(1, int((width - 2.0) // spacing))
+    rows = (n + cols - 1) // cols
+    idx = np.arange(n)
+    gx = (idx % cols).astype(np.float64)
+    gy = (idx // cols).astype(np.float64)
+    x0 = -(cols - 1) * spacing / 2.0
+    pos = np.stack([x0 + gx * spacing, y_base + 0.65 + gy * spacing], 1)
+    pos += rng.uniform(-jitter, jitter, size=(n, 2))
+    kinds = rng.permutation(np.arange(n) % 2)  # half circles, half polygons
+    b = abi.body_defs(n)
+    b["type"] = abi.DYNAMIC
+    b["position"] = pos.astype(F32)
+    b["linear_velocity"] = rng.normal(0.0, 1.0, size=(n, 2)).astype(F32)
+    sh = np.zeros(n, abi.SHAPE_DEF)
+    circ = kinds == 0
+    sh["kind"][circ] = abi.SHAPE_CIRCLE
+    sh["radius"][circ] = rng.uniform(0.25, 0.5, size=int(circ.sum())).astype(F32)
+    poly = np.nonzero(~circ)[0]
+    sh["kind"][poly] = abi.SHAPE_POLYGON
+    for i in poly:
+        k = int(rng.integers(3, 9))
+        ang = np.sort(rng.uniform(0.0, 2.0 * math.pi, size=k))
+        r = rng.uniform(0.3, 0.6)
+        sh["count"][i] = k
+        sh["vertices"][i, :k, 0] = (r * np.cos(ang)).astype(F32)
+        sh["vertices"][i, :k, 1] = (r * np.sin(ang)).astype(F32)
+    f = abi.fixture_defs(n)
+    f["density"] = F32(1.0)
+    f["friction"] = rng.uniform(0.2, 0.8, size=n).astype(F32)
+    s = _empty()
+    s["bodies"] = b
+    s["fixture_body"] = np.arange(n, dtype=np.int32)
+    s["shapes"] = sh
+    s["fixtures"] = f
+    height = max(height, y_base + rows * spacing + 4.0)
+    out = _concat([container(width, height), s])
+    out["name"] = "scatter%d" % n
+    return out
+
+
+def scatter_world(n=16384, seed=1, width=200.0, height=400.0):
+    """Single large world: n mixed bodies in a 200 m x 400 m container."""
+    return scatter(n, width, height, np.random.default_rng(seed))
+
+
+def stacks(n, height, spacing=2.0, box=0.5):
+    cols = (n + height - 1) // height
+    centers = []
+    x0 = -(cols - 1) * spacing / 2.0
+    for i in range(n):
+        c, r = divmod(i, height)
+        centers.append((x0 + c * spacing, box + r * (2 * box)))
+    g = ground_box(hx=max(50.0, cols * spacing), hy=10.0)
+    s = _concat([g, _boxes(centers, box, box, abi.DYNAMIC, 0.6, 1.0)])
+    s["name"] = "stacks%dx%d" % (cols, height)
+    return s
+
+
+def batch(n_worlds=4096, seed=3, lo=8, hi=512):
+    """Batched workload: per-world body counts log-uniform in [lo, hi]; thirds of
+    pyramids, 40 m-container scatters and box stacks."""
+    rng = np.random.default_rng(seed)
+    counts = np.exp(rng.uniform(math.log(lo), math.log(hi), size=n_worlds)).astype(np.int64)
+    worlds = []
+    for w in range(n_worlds):
+        n = int(counts[w])
+        kind = w % 3
+        if kind == 0:
+            rows = int((math.sqrt(8 * n + 1) - 1) // 2)
+            worlds.append(pyramid(rows=max(rows, 1)))
+        elif kind == 1:
+            worlds.append(scatter(n, 40.0, 40.0, rng))
+        else:
+            worlds.append(stacks(n, int(rng.integers(1, 31))))
+    return worlds
+
+
+def hello_world():
+    """examples/hello_world/hello_world.d:31-103: ground box + one 1x1 box at y=4."""
+    g = ground_box()
+    b = _boxes([(0.0, 4.0)], 1.0, 1.0, abi.DYNAMIC, 0.3, 1.0)
+    s = _concat([g, b])
+    s["name"] = "hello_world"
+    return s
+
+
+def dynamic_body_count(scene):
+    return int((scene["bodies"]["type"] == abi.DYNAMIC).sum())

@@ -1,0 +1,264 @@
+/*
+ * dbox_gpu.h - C ABI of the GB300 b2World.Step library (libdbox_gpu.so).
+ *
+ * Drop-in boundary for the per-step hot path of dbox (a D port of Box2D 2.3.1).
+ * Every entry point is plain C: int32 status return (0 = ok, negative =
+ * DBOX_ERR_*), plain pointers and sizes, no exceptions, no torch types.
+ * Each declaration names the reference interface it replaces (paths are within
+ * the dbox project, src/dbox/...).
+ *
+ * Ownership: the library owns all device memory of a world; host buffers passed
+ * in are caller-owned and copied.  A world is not reentrant: one thread at a time.
+ *
+ * A "world" handle holds one or more independent simulation worlds stored
+ * side by side on the GPU (a batch).  The single-world calls address world 0.
+ */
+#ifndef DBOX_GPU_H
+#define DBOX_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+#define DBOX_OK 0
+#define DBOX_ERR_INVALID -1    /* bad argument (null pointer, index out of range, bad count) */
+#define DBOX_ERR_LOCKED -2     /* call not allowed while the world is stepping (b2World.IsLocked) */
+#define DBOX_ERR_CAPACITY -3   /* a device pool (contacts, pairs, islands) overflowed */
+#define DBOX_ERR_TIMEOUT -4    /* a bounded device loop hit its iteration limit */
+#define DBOX_ERR_NAN -5        /* non-finite body state after a step */
+#define DBOX_ERR_CUDA -6       /* a CUDA runtime call failed; see dbox_last_error() */
+#define DBOX_ERR_UNSUPPORTED -7 /* feature outside the implemented path (e.g. edge shapes) */
+
+/* ---------------------------------------------------------------- types */
+typedef struct { float x, y; } dbox_vec2;
+
+/* b2BodyType (dynamics/b2body.d:34-42) */
+#define DBOX_STATIC_BODY 0
+#define DBOX_KINEMATIC_BODY 1
+#define DBOX_DYNAMIC_BODY 2
+
+/* b2BodyDef (dynamics/b2body.d:51-104); dbox_body_def_default() gives the reference defaults. */
+typedef struct {
+    int32_t type;
+    dbox_vec2 position;
+    float angle;
+    dbox_vec2 linear_velocity;
+    float angular_velocity;
+    float linear_damping;
+    float angular_damping;
+    int32_t allow_sleep;
+    int32_t awake;
+    int32_t fixed_rotation;
+    int32_t bullet;
+    int32_t active;
+    float gravity_scale;
+} dbox_body_def;
+
+/* Shape kinds accepted by fixture creation. */
+#define DBOX_SHAPE_CIRCLE 0      /* b2CircleShape: m_p = center, m_radius = radius */
+#define DBOX_SHAPE_POLYGON 1     /* b2PolygonShape.Set(vertices, count): weld + gift-wrap hull */
+#define DBOX_SHAPE_BOX 2         /* b2PolygonShape.SetAsBox(hx, hy) */
+#define DBOX_SHAPE_ORIENTED_BOX 3 /* b2PolygonShape.SetAsBox(hx, hy, center, angle) */
+
+typedef struct {
+    int32_t kind;            /* DBOX_SHAPE_* */
+    int32_t count;           /* POLYGON: number of input points (3..8) */
+    dbox_vec2 vertices[8];   /* POLYGON input points */
+    dbox_vec2 center;        /* CIRCLE: center; ORIENTED_BOX: box center */
+    float radius;            /* CIRCLE radius */
+    float hx, hy;            /* BOX / ORIENTED_BOX half extents */
+    float angle;             /* ORIENTED_BOX angle */
+} dbox_shape_def;
+
+/* b2FixtureDef + b2Filter (dynamics/b2fixture.d:32-73) */
+typedef struct {
+    float friction;          /* default 0.2 */
+    float restitution;
+    float density;
+    int32_t is_sensor;
+    uint16_t category_bits;  /* default 0x0001 */
+    uint16_t mask_bits;      /* default 0xFFFF */
+    int16_t group_index;
+    int16_t pad_;
+} dbox_fixture_def;
+
+/* b2RevoluteJointDef (dynamics/joints/b2revolutejoint.d:30-110) */
+typedef struct {
+    int32_t body_a, body_b;
+    int32_t collide_connected;
+    dbox_vec2 local_anchor_a, local_anchor_b;
+    float reference_angle;
+    int32_t enable_limit;
+    float lower_angle, upper_angle;
+    int32_t enable_motor;
+    float motor_speed, max_motor_torque;
+} dbox_revolute_def;
+
+/* ------------------------------------------------------- world snapshot
+ * Flat state records, used by dbox_world_export_state / import_state
+ * (exact checkpoint/resume) and by the parity tests.  Flag words use the
+ * reference's bit values (b2Body e_* b2body.d:1118-1127, b2Contact e_*
+ * contacts/b2contact.d:242-261, b2World e_* b2world.d:922-927). */
+typedef struct {
+    int32_t body_count, fixture_count, contact_count, joint_count;
+    uint32_t world_flags;     /* e_newFixture 1, e_locked 2, e_clearForces 4 */
+    int32_t step_complete;    /* b2World.m_stepComplete */
+    float inv_dt0;            /* b2World.m_inv_dt0 */
+    int32_t reserved;
+} dbox_world_header;
+
+typedef struct {
+    uint32_t flags;          /* island 1, awake 2, autoSleep 4, bullet 8, fixedRotation 0x10, active 0x20 */
+    int32_t type;
+    float xf[4];             /* p.x, p.y, q.s, q.c */
+    float sweep[9];          /* localCenter.x/y, c0.x/y, c.x/y, a0, a, alpha0 */
+    float vel[3];            /* v.x, v.y, w */
+    float force[3];          /* force.x, force.y, torque */
+    float sleep_time;
+    float mass[4];           /* mass, invMass, I, invI */
+} dbox_body_state;
+
+typedef struct {
+    float fat_aabb[4];       /* lowerBound.x/y, upperBound.x/y of the dynamic-tree leaf */
+    int32_t moved;           /* 1 if the proxy is in the broad-phase move buffer */
+    int32_t proxy_id;        /* dynamic-tree node id of the proxy */
+} dbox_proxy_state;
+
+typedef struct {
+    float local_point[2];
+    float normal_impulse, tangent_impulse;
+    uint32_t id;             /* b2ContactID.key: indexA | indexB<<8 | typeA<<16 | typeB<<24 */
+} dbox_manifold_point;
+
+typedef struct {
+    int32_t fixture_a, fixture_b;  /* fixture creation indices, after the type-order swap */
+    uint32_t flags;                /* island 1, touching 2, enabled 4, filter 8, bulletHit 0x10, toi 0x20 */
+    int32_t toi_count;
+    float toi, friction, restitution, tangent_speed;
+    int32_t point_count, type;     /* b2Manifold.pointCount / type (circles 0, faceA 1, faceB 2) */
+    float local_normal[2], local_point[2];
+    dbox_manifold_point points[2];
+} dbox_contact_state;              /* exported oldest first = reverse of b2World.GetContactList order */
+
+typedef struct {
+    float impulse[3];
+    float motor_impulse;
+    int32_t limit_state;
+} dbox_joint_state;
+
+/* b2Profile (dynamics/b2timestep.d:37-47), milliseconds, measured with CUDA events. */
+typedef struct {
+    float step, collide, solve, solve_init, solve_velocity, solve_position, broadphase, solve_toi;
+} dbox_profile;
+
+/* Contact listener (b2ContactListener, dynamics/b2worldcallbacks.d:87-128).
+ * Events are recorded on the device in reference order and delivered on the
+ * calling thread before dbox_world_step returns. */
+#define DBOX_EVENT_BEGIN 1
+#define DBOX_EVENT_END 2
+#define DBOX_EVENT_PRESOLVE 3
+#define DBOX_EVENT_POSTSOLVE 4
+typedef struct {
+    int32_t kind;              /* DBOX_EVENT_* */
+    int32_t world;             /* world index inside the handle */
+    int32_t fixture_a, fixture_b;
+    int32_t point_count;       /* manifold points (BEGIN/PRESOLVE) or impulse count (POSTSOLVE) */
+    float normal_impulses[2];
+    float tangent_impulses[2];
+} dbox_contact_event;
+typedef void (*dbox_event_fn)(const dbox_contact_event* events, int32_t count, void* user);
+
+typedef struct dbox_world dbox_world;
+
+/* -------------------------------------------------------------- lifecycle */
+
+/* Sizing hints; zero fields take defaults. */
+typedef struct {
+    int32_t contacts_per_body;   /* contact pool per world = contacts_per_body * bodies + 64 (default 8) */
+    int32_t team;                /* 0 auto, 32 = one warp per world, 128/256/512 = one block per world */
+} dbox_world_caps;
+
+/* b2World(gravity) constructor (dynamics/b2world.d:865-895). Creates n_worlds
+ * independent worlds sharing gravity; worlds are addressed 0..n_worlds-1. */
+int32_t dbox_world_create(dbox_vec2 gravity, int32_t n_worlds, const dbox_world_caps* caps,
+                          dbox_world** out);
+/* b2World destructor (b2world.d:897-920). */
+int32_t dbox_world_destroy(dbox_world* w);
+
+/* Fill reference defaults (b2BodyDef b2body.d:51-104, b2FixtureDef b2fixture.d:49-73). */
+void dbox_body_def_default(dbox_body_def* def);
+void dbox_fixture_def_default(dbox_fixture_def* def);
+
+/* b2World.CreateBody (b2world.d:75-99). Body ids count from 0 per world, in creation order. */
+int32_t dbox_body_create(dbox_world* w, int32_t world, const dbox_body_def* def, int32_t* out_body);
+/* b2Body.CreateFixture(def) (b2body.d:116-155) with the shape of b2PolygonShape.Set/SetAsBox
+ * (collision/shapes/b2polygonshape.d:74-262) or b2CircleShape (b2circleshape.d). */
+int32_t dbox_fixture_create(dbox_world* w, int32_t world, int32_t body, const dbox_shape_def* shape,
+                            const dbox_fixture_def* def, int32_t* out_fixture);
+/* b2World.CreateJoint with a b2RevoluteJointDef (b2world.d:196-261, joints/b2revolutejoint.d). */
+int32_t dbox_joint_create_revolute(dbox_world* w, int32_t world, const dbox_revolute_def* def,
+                                   int32_t* out_joint);
+
+/* Bulk creation of a whole scene into one world: n bodies, then m fixtures
+ * (fixture_body[i] indexes the bodies created by this call), then k joints
+ * (body indices relative to this call).  Same effect as the single calls in
+ * the order bodies, fixtures, joints. */
+int32_t dbox_scene_create(dbox_world* w, int32_t world, int32_t n_bodies, const dbox_body_def* bodies,
+                          int32_t n_fixtures, const int32_t* fixture_body, const dbox_shape_def* shapes,
+                          const dbox_fixture_def* fixtures, int32_t n_joints, const dbox_revolute_def* joints);
+
+/* World flag setters (b2World.SetWarmStarting/SetContinuousPhysics/SetSubStepping/
+ * SetAllowSleeping/SetAutoClearForces, b2world.d:622-753), applied to every world of the handle. */
+int32_t dbox_world_set_flags(dbox_world* w, int32_t warm_starting, int32_t continuous,
+                             int32_t sub_stepping, int32_t allow_sleep, int32_t auto_clear_forces);
+/* b2World.SetGravity (b2world.d:711-714). */
+int32_t dbox_world_set_gravity(dbox_world* w, dbox_vec2 gravity);
+
+/* b2World.SetContactListener (b2world.d:59-62): events are delivered through fn,
+ * in reference order, at the end of each step.  fn = NULL removes the listener. */
+int32_t dbox_world_set_listener(dbox_world* w, dbox_event_fn fn, void* user);
+
+/* b2World.Step(dt, velocityIterations, positionIterations) (b2world.d:367-434),
+ * applied to every world of the handle.  Inputs and outputs stay on the device. */
+int32_t dbox_world_step(dbox_world* w, float dt, int32_t velocity_iterations, int32_t position_iterations);
+
+/* Same as dbox_world_step, with `steps` steps captured once into a CUDA graph and replayed. */
+int32_t dbox_world_step_n(dbox_world* w, float dt, int32_t velocity_iterations,
+                          int32_t position_iterations, int32_t steps);
+
+/* Body readback (b2Body.GetPosition/GetAngle/GetLinearVelocity/GetAngularVelocity,
+ * b2body.d:271-340) for every body of every world, in (world, body id) order.
+ * Any pointer may be NULL; each non-NULL array holds total_bodies entries. */
+int32_t dbox_world_get_bodies(dbox_world* w, dbox_vec2* position, float* angle,
+                              dbox_vec2* linear_velocity, float* angular_velocity, int32_t* awake);
+int32_t dbox_world_body_count(dbox_world* w, int32_t world, int32_t* out);
+int32_t dbox_world_contact_count(dbox_world* w, int32_t world, int32_t* out);
+
+/* Snapshot of one world (b2World.Dump b2world.d:796-855 replaced by an exact binary form).
+ * Arrays are sized from the header: bodies[body_count], proxies[fixture_count],
+ * contacts[contact_count], joints[joint_count].  Pass NULL arrays to read the header only. */
+int32_t dbox_world_export_state(dbox_world* w, int32_t world, dbox_world_header* header,
+                                dbox_body_state* bodies, dbox_proxy_state* proxies,
+                                dbox_contact_state* contacts, dbox_joint_state* joints);
+/* Restore a snapshot into a world whose bodies, fixtures and joints were created identically. */
+int32_t dbox_world_import_state(dbox_world* w, int32_t world, const dbox_world_header* header,
+                                const dbox_body_state* bodies, const dbox_proxy_state* proxies,
+                                const dbox_contact_state* contacts, const dbox_joint_state* joints);
+
+/* b2World.GetProfile (b2world.d:789-792): phase times of the last step, summed over worlds. */
+int32_t dbox_world_get_profile(dbox_world* w, dbox_profile* out);
+
+/* Device kernels launched by the last step (for launch accounting). */
+int32_t dbox_world_last_launches(dbox_world* w, int32_t* out);
+
+/* Text of the last error on the calling thread (never NULL). */
+const char* dbox_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DBOX_GPU_H */

@@ -1,0 +1,150 @@
+"""TEST INFRASTRUCTURE ONLY: Python loader for the CPU oracle (b2_oracle.cpp).
+
+The oracle restates dbox's b2World.Step on the CPU (see b2_oracle.h for the
+parity status).  Only tests/, __graft_entry__.smoke() and bench.py's CPU
+baseline legs use this module; the product library never does.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+from dbox_gb300 import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "liboracle.so")
+SRC = os.path.join(HERE, "b2_oracle.cpp")
+HDRS = [os.path.join(HERE, "b2_oracle.h"), os.path.join(HERE, "..", "include", "dbox_gpu.h"),
+        os.path.join(HERE, "..", "dbox_gb300", "csrc", "dbox_trig.h")]
+
+_lib = None
+
+
+def build(force=False):
+    """Compile liboracle.so: -O2 -ffp-contract=off keeps every float op singly rounded."""
+    os.makedirs(BUILD, exist_ok=True)
+    newest = max(os.path.getmtime(p) for p in [SRC] + HDRS)
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest:
+        return LIB
+    cmd = ["g++", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-std=c++17", SRC, "-o", LIB + ".tmp"]
+    subprocess.check_call(cmd)
+    os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        vp, i32, f32 = ctypes.c_void_p, ctypes.c_int, ctypes.c_float
+        L.orc_world_create.restype = vp
+        L.orc_world_create.argtypes = [f32, f32]
+        L.orc_world_destroy.argtypes = [vp]
+        L.orc_scene_create.argtypes = [vp, i32, vp, i32, vp, vp, vp, i32, vp]
+        L.orc_world_set_flags.argtypes = [vp, i32, i32, i32, i32, i32]
+        L.orc_world_step.argtypes = [vp, f32, i32, i32]
+        L.orc_world_step_n.argtypes = [vp, f32, i32, i32, i32]
+        L.orc_world_export_state.argtypes = [vp, vp, vp, vp, vp, vp]
+        L.orc_world_record_events.argtypes = [vp, i32]
+        L.orc_world_event_count.argtypes = [vp]
+        L.orc_world_get_events.argtypes = [vp, vp, i32]
+        L.orc_world_clear_events.argtypes = [vp]
+        L.orc_world_last_toi_events.argtypes = [vp]
+        L.orc_world_last_islands.argtypes = [vp]
+        L.orc_set_trig_mode.argtypes = [i32]
+        L.orc_sincos.argtypes = [f32, ctypes.POINTER(f32), ctypes.POINTER(f32)]
+        L.orc_polygon_set.argtypes = [vp, i32, vp, vp, vp]
+        L.orc_collide.argtypes = [vp, vp, vp, vp, vp]
+        _lib = L
+    return _lib
+
+
+def set_trig_mode(mode):
+    """0: host libm sinf/cosf (the reference's arithmetic); 1: the portable dbox_sincosf."""
+    lib().orc_set_trig_mode(int(mode))
+
+
+def sincos(a):
+    s, c = ctypes.c_float(), ctypes.c_float()
+    lib().orc_sincos(ctypes.c_float(a), ctypes.byref(s), ctypes.byref(c))
+    return s.value, c.value
+
+
+class OracleWorld:
+    """One b2World on the CPU, built from a scene dict (dbox_gb300.scenes)."""
+
+    def __init__(self, scene, flags=None):
+        L = lib()
+        g = scene.get("gravity", (0.0, -10.0))
+        self.h = L.orc_world_create(float(g[0]), float(g[1]))
+        b = np.ascontiguousarray(scene["bodies"])
+        fb = np.ascontiguousarray(scene["fixture_body"], dtype=np.int32)
+        sh = np.ascontiguousarray(scene["shapes"])
+        fx = np.ascontiguousarray(scene["fixtures"])
+        j = np.ascontiguousarray(scene["joints"])
+        rc = L.orc_scene_create(self.h, len(b), abi.ptr(b), len(fb), abi.ptr(fb), abi.ptr(sh), abi.ptr(fx),
+                                len(j), abi.ptr(j) if len(j) else None)
+        if rc != 0:
+            raise ValueError("oracle scene creation failed")
+        if flags is not None:
+            self.set_flags(**flags)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_world_destroy(self.h)
+            self.h = None
+
+    def set_flags(self, warm=1, continuous=1, substep=0, sleep=1, autoclear=1):
+        lib().orc_world_set_flags(self.h, warm, continuous, substep, sleep, autoclear)
+
+    def step(self, dt=1.0 / 60.0, vel_iters=8, pos_iters=3, steps=1):
+        if steps == 1:
+            lib().orc_world_step(self.h, ctypes.c_float(dt), vel_iters, pos_iters)
+        else:
+            lib().orc_world_step_n(self.h, ctypes.c_float(dt), vel_iters, pos_iters, steps)
+
+    def record_events(self, on=True):
+        lib().orc_world_record_events(self.h, 1 if on else 0)
+
+    def events(self, clear=True):
+        n = lib().orc_world_event_count(self.h)
+        out = np.zeros(n, abi.CONTACT_EVENT)
+        if n:
+            lib().orc_world_get_events(self.h, abi.ptr(out), n)
+        if clear:
+            lib().orc_world_clear_events(self.h)
+        return out
+
+    def last_toi_events(self):
+        return lib().orc_world_last_toi_events(self.h)
+
+    def last_islands(self):
+        return lib().orc_world_last_islands(self.h)
+
+    def export_state(self):
+        L = lib()
+        hdr = np.zeros(1, abi.WORLD_HEADER)
+        L.orc_world_export_state(self.h, abi.ptr(hdr), None, None, None, None)
+        h = hdr[0]
+        bodies = np.zeros(int(h["body_count"]), abi.BODY_STATE)
+        proxies = np.zeros(int(h["fixture_count"]), abi.PROXY_STATE)
+        contacts = np.zeros(int(h["contact_count"]), abi.CONTACT_STATE)
+        joints = np.zeros(int(h["joint_count"]), abi.JOINT_STATE)
+        L.orc_world_export_state(self.h, abi.ptr(hdr), abi.ptr(bodies), abi.ptr(proxies), abi.ptr(contacts),
+                                 abi.ptr(joints))
+        return {"header": hdr, "bodies": bodies, "proxies": proxies, "contacts": contacts, "joints": joints}
+
+
+def polygon_set(points):
+    """b2PolygonShape.Set on the given points: (vertices, normals, centroid) or None if degenerate."""
+    pts = np.ascontiguousarray(points, dtype=np.float32).reshape(-1, 2)
+    v = np.zeros((8, 2), np.float32)
+    nrm = np.zeros((8, 2), np.float32)
+    c = np.zeros(2, np.float32)
+    n = lib().orc_polygon_set(abi.ptr(pts), len(pts), abi.ptr(v), abi.ptr(nrm), abi.ptr(c))
+    if n == 0:
+        return None
+    return v[:n].copy(), nrm[:n].copy(), c
