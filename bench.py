@@ -1,0 +1,308 @@
+"""Benchmark: body-steps/s of b2World.Step on one GB300 (plain solver, batched worlds).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload batch|scatter|pyramid]
+
+Workload (default "batch"): 4,096 independent worlds in one handle, body counts
+log-uniform in [8, 512], one third each pyramid / scatter in a 40 m container /
+box stacks (dbox_gb300.scenes.batch), float32, dt = 1/60, 8 velocity and 3 position
+iterations.  A "step" is one b2World.Step of every world.  The timed steps follow
+W untimed warm-up steps, so the timed window is steps W+1 .. W+K of the simulation.
+
+value  = dynamic body-steps / device time of K steps replayed from one CUDA graph
+         (world state resident in HBM; CUDA events on the library's stream).
+e2e    = the same K steps through the C ABI from host buffers: each step uploads a
+         (fx, fy, torque) array for every body from pinned host memory
+         (dbox_world_apply_forces; zero forces, so the trajectory is unchanged),
+         steps, and reads every body's (x, y, angle) back into pinned memory
+         (dbox_world_get_transforms); host wall clock around the K steps.
+cpu_baseline / --impl reference: the CPU oracle (a C++ restatement of the dbox
+         step; the D reference cannot be compiled on these machines) on a bounded
+         sample of the same worlds and step window, one process per host core.
+Under torchrun each rank runs its own 4,096-world batch (weak scaling, no
+collective on the data path); rank 0 prints the max-over-ranks timing.
+"""
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+DT = 1.0 / 60.0
+VI, PI = 8, 3
+METRIC = "body-steps/s on 1 GB300 (plain GPU solver, batched worlds)"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=60)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--workload", default="batch", choices=["batch", "scatter", "pyramid"])
+    p.add_argument("--worlds", type=int, default=4096)
+    p.add_argument("--seed", type=int, default=3)
+    p.add_argument("--cpu-seconds", type=float, default=12.0)
+    p.add_argument("--no-cpu", action="store_true")
+    return p.parse_args()
+
+
+def make_worlds(args, rank):
+    from dbox_gb300 import scenes
+    if args.workload == "batch":
+        return scenes.batch(n_worlds=args.worlds, seed=args.seed + 1000 * rank), {
+            "workload": "batched worlds: %d worlds, bodies log-uniform [8,512], thirds pyramid/scatter/stacks"
+                        % args.worlds, "worlds": args.worlds}
+    if args.workload == "scatter":
+        return [scenes.scatter_world(seed=args.seed + rank)], {
+            "workload": "single world: 16,384 mixed circles/polygons in a 200x400 m container", "worlds": 1}
+    return [scenes.pyramid()], {"workload": "single world: 20-row pyramid, 210 boxes", "worlds": 1}
+
+
+def dynamic_bodies(worlds):
+    from dbox_gb300 import scenes
+    return sum(scenes.dynamic_body_count(s) for s in worlds)
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ CPU oracle legs
+def _cpu_worker(task):
+    import oracle
+    from dbox_gb300 import scenes
+    idx, seed, n_worlds, workload, warmup, steps = task
+    oracle.set_trig_mode(0)
+    if workload == "batch":
+        allw = scenes.batch(n_worlds=n_worlds, seed=seed)
+        worlds = [allw[i] for i in idx]
+    elif workload == "scatter":
+        worlds = [scenes.scatter_world(seed=seed)]
+    else:
+        worlds = [scenes.pyramid()]
+    ows = [oracle.OracleWorld(s) for s in worlds]
+    for w in ows:
+        w.step(DT, VI, PI, steps=warmup)
+    t0 = time.perf_counter()
+    for w in ows:
+        w.step(DT, VI, PI, steps=steps)
+    dt = time.perf_counter() - t0
+    nb = sum(scenes.dynamic_body_count(s) for s in worlds)
+    return nb * steps, dt
+
+
+def cpu_leg(args, seconds):
+    """Oracle step on host cores: returns (body-steps/s, cores, sample description)."""
+    import oracle
+    from dbox_gb300 import scenes
+    oracle.build()
+    cores = min(os.cpu_count() or 1, 64)
+    if args.workload == "batch":
+        sample_worlds = min(args.worlds, max(cores * 2, 32))
+        # pick a probe sample size from a short calibration run on one core
+        probe = _cpu_worker((list(range(min(8, sample_worlds))), args.seed, args.worlds, "batch", args.warmup, 4))
+        rate1 = probe[0] / max(probe[1], 1e-6)
+        per_world_steps = max(4, min(args.steps, int(seconds * rate1 * cores / (sample_worlds * 120.0))))
+        idx = list(range(sample_worlds))
+        chunks = [idx[i::cores] for i in range(cores) if idx[i::cores]]
+        tasks = [(c, args.seed, args.worlds, "batch", args.warmup, per_world_steps) for c in chunks]
+        ctx = mp.get_context("spawn")
+        t0 = time.perf_counter()
+        with ctx.Pool(len(tasks)) as pool:
+            res = pool.map(_cpu_worker, tasks)
+        wall = time.perf_counter() - t0
+        work = sum(r[0] for r in res)
+        slowest = max(r[1] for r in res)
+        rate = work / slowest
+        sample = ("%d of %d worlds, steps %d..%d, %d processes (one world list per core), oracle with host libm trig"
+                  % (sample_worlds, args.worlds, args.warmup + 1, args.warmup + per_world_steps, len(tasks)))
+        return rate, len(tasks), sample
+    steps = max(2, min(args.steps, 10))
+    work, dt = _cpu_worker(([0], args.seed, 1, args.workload, args.warmup, steps))
+    return work / dt, 1, "1 world, steps %d..%d, one core" % (args.warmup + 1, args.warmup + steps)
+
+
+# ------------------------------------------------------------------ GPU leg
+def algorithmic_solve_bytes(c):
+    """Bytes the k_solve kernel must move by the reference struct sizes:
+    96 per island body (integrate + copy back), per island contact 244 (b2ContactVelocity/
+    PositionConstraint build) + 156 (velocity init) + 16 (store impulses), 220 per contact
+    velocity solve (vc 156 + two 24-byte body states read and written, 16 of impulses) and
+    136 per contact position solve (pc 88 + two 24-byte positions)."""
+    return 96 * c["isl_bodies"] + (244 + 156 + 16) * c["isl_contacts"] + 220 * c["vsolve"] + 136 * c["psolve"]
+
+
+def gpu_leg(args, rank, world_size):
+    import torch
+    import dbox_gb300
+    dbox_gb300.build()
+    torch.cuda.set_device(0 if world_size == 1 else int(os.environ.get("LOCAL_RANK", rank)))
+    worlds, cfg = make_worlds(args, rank)
+    nbody_dyn = dynamic_bodies(worlds)
+    nbody = sum(len(s["bodies"]) for s in worlds)
+    w = dbox_gb300.World(worlds)
+    w.step(DT, VI, PI, steps=args.warmup, graph=True)
+    w.sync()
+    peaks = {}
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        peaks = json.load(open(pk))
+    c0 = w.counters()
+    if world_size > 1:
+        torch.distributed.barrier()
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    total_ms, phase_ms = w.step_timed(args.steps, DT, VI, PI)
+    clk = clocks.stop()
+    c1 = w.counters()
+    cdiff = {k: c1[k] - c0[k] for k in c1}
+    t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
+    if world_size > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    total_ms_max = float(t.item())
+    value = nbody_dyn * args.steps * world_size / (total_ms_max / 1e3)
+    launches = w.last_launches() * args.steps
+    # end to end through the C ABI with pinned host buffers
+    forces = torch.zeros((nbody, 3), dtype=torch.float32).pin_memory().numpy()
+    xya = torch.zeros((nbody, 3), dtype=torch.float32).pin_memory().numpy()
+    if world_size > 1:
+        torch.distributed.barrier()
+    w.sync()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        w.apply_forces(forces)
+        w.step(DT, VI, PI)
+        w.get_transforms(xya)
+    e2e_s = time.perf_counter() - t0
+    te = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+    if world_size > 1:
+        torch.distributed.all_reduce(te, op=torch.distributed.ReduceOp.MAX)
+    e2e = nbody_dyn * args.steps * world_size / float(te.item())
+    assert np.isfinite(xya).all()
+    solve_bytes = algorithmic_solve_bytes(cdiff) / args.steps
+    solve_ms = phase_ms[1] / args.steps
+    achieved = solve_bytes / (solve_ms / 1e3) / 1e9
+    hbm = peaks.get("hbm_gbs")
+    out = {
+        "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": world_size, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic seeded scenes (numpy PCG64 seed %d)" % args.seed,
+        "config": dict(cfg, dt=DT, velocity_iterations=VI, position_iterations=PI, dynamic_bodies=nbody_dyn,
+                       parallelism="replicas: one batch of worlds per GPU",
+                       l2="working set (bodies, contacts, constraint rows) larger than the 129 MB L2",
+                       timing="one CUDA graph of K steps with per-phase CUDA events"),
+        "e2e": {"value": e2e, "unit": "body-steps/s", "h2d_bytes_per_step": int(forces.nbytes),
+                "d2h_bytes_per_step": int(xya.nbytes)},
+        "gpu_launches": launches,
+        "phases_ms_per_step": {"collide": phase_ms[0] / args.steps, "solve": solve_ms,
+                               "solve_toi": phase_ms[2] / args.steps},
+        "work_per_step": {k: v / args.steps for k, v in cdiff.items()},
+        "roofline": {"bound": "hbm", "kernel": "k_solve", "achieved": achieved,
+                     "peak": hbm, "unit": "GB/s", "frac": (achieved / hbm) if hbm else None,
+                     "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if hbm else "fallback 6800",
+                     "algorithmic_bytes_per_launch": solve_bytes, "traffic": None},
+        "clocks": clk,
+    }
+    if out["roofline"]["peak"] is None:
+        out["roofline"]["peak"] = 6800.0
+        out["roofline"]["frac"] = achieved / 6800.0
+    w.close()
+    return out
+
+
+def main():
+    args = parse()
+    world_size = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        rate, cores, sample = cpu_leg(args, args.cpu_seconds)
+        _, cfg = make_worlds(args, 0) if args.workload != "batch" else (None, {
+            "workload": "batched worlds: %d worlds, bodies log-uniform [8,512], thirds pyramid/scatter/stacks"
+                        % args.worlds, "worlds": args.worlds})
+        out = {"metric": METRIC, "value": rate, "unit": "body-steps/s", "n_gpus": world_size, "steps": args.steps,
+               "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+               "dtype": "f32", "data": "synthetic seeded scenes (numpy PCG64 seed %d)" % args.seed,
+               "impl": "reference",
+               "config": dict(cfg, dt=DT, velocity_iterations=VI, position_iterations=PI),
+               "cpu_baseline": {"value": rate, "unit": "body-steps/s", "cores": cores, "kind": "port",
+                                "sample": sample},
+               "e2e": {"value": rate, "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(out), flush=True)
+        return
+    if world_size > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    out = gpu_leg(args, rank, world_size)
+    if rank == 0:
+        if world_size == 1 and not args.no_cpu:
+            rate, cores, sample = cpu_leg(args, args.cpu_seconds)
+            out["cpu_baseline"] = {"value": rate, "unit": "body-steps/s", "cores": cores, "kind": "port",
+                                   "sample": sample}
+        print(json.dumps(out), flush=True)
+    if world_size > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,214 @@
+"""dbox_gb300: GPU b2World.Step behind the reference's world/body/fixture API.
+
+The compute path is libdbox_gpu.so (hand-written sm_103a kernels behind the C
+ABI of include/dbox_gpu.h); this module is a thin ctypes binding shaped like
+dbox's b2World (dynamics/b2world.d): create bodies/fixtures/joints, Step(dt,
+velocityIterations, positionIterations), read bodies and contacts back.
+
+There is no CPU fallback: if the library cannot be loaded, or no GPU is
+visible, World raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libdbox_gpu.so")
+
+_lib = None
+
+
+class DboxError(RuntimeError):
+    pass
+
+
+def build(force=False):
+    """Compile libdbox_gpu.so for sm_103a (see buildlib.py)."""
+    from . import buildlib
+    return buildlib.build(force=force)
+
+
+def lib():
+    """Load libdbox_gpu.so; raise if it is missing (no silent fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise DboxError("libdbox_gpu.so not built: run dbox_gb300.build() (nvcc, sm_103a)")
+    L = ctypes.CDLL(LIB_PATH)
+    vp, i32, f32 = ctypes.c_void_p, ctypes.c_int32, ctypes.c_float
+    L.dbox_world_create.argtypes = [abi.Vec2, i32, vp, ctypes.POINTER(vp)]
+    L.dbox_world_destroy.argtypes = [vp]
+    L.dbox_scene_create.argtypes = [vp, i32, i32, vp, i32, vp, vp, vp, i32, vp]
+    L.dbox_body_create.argtypes = [vp, i32, vp, ctypes.POINTER(i32)]
+    L.dbox_fixture_create.argtypes = [vp, i32, i32, vp, vp, ctypes.POINTER(i32)]
+    L.dbox_joint_create_revolute.argtypes = [vp, i32, vp, ctypes.POINTER(i32)]
+    L.dbox_world_set_flags.argtypes = [vp, i32, i32, i32, i32, i32]
+    L.dbox_world_set_gravity.argtypes = [vp, abi.Vec2]
+    L.dbox_world_step.argtypes = [vp, f32, i32, i32]
+    L.dbox_world_step_n.argtypes = [vp, f32, i32, i32, i32]
+    L.dbox_world_sync.argtypes = [vp]
+    L.dbox_world_get_bodies.argtypes = [vp, vp, vp, vp, vp, vp]
+    L.dbox_world_body_count.argtypes = [vp, i32, ctypes.POINTER(i32)]
+    L.dbox_world_contact_count.argtypes = [vp, i32, ctypes.POINTER(i32)]
+    L.dbox_world_export_state.argtypes = [vp, i32, vp, vp, vp, vp, vp]
+    L.dbox_world_import_state.argtypes = [vp, i32, vp, vp, vp, vp, vp]
+    L.dbox_world_get_profile.argtypes = [vp, vp]
+    L.dbox_world_last_launches.argtypes = [vp, ctypes.POINTER(i32)]
+    L.dbox_world_step_stats.argtypes = [vp, i32, ctypes.POINTER(i32), ctypes.POINTER(i32)]
+    L.dbox_last_error.restype = ctypes.c_char_p
+    L.dbox_collide_manifolds.argtypes = [i32, vp, vp, vp, vp, vp]
+    L.dbox_world_step_n_timed.argtypes = [vp, f32, i32, i32, i32, vp, vp]
+    L.dbox_world_get_counters.argtypes = [vp, vp]
+    L.dbox_world_apply_forces.argtypes = [vp, vp]
+    L.dbox_world_get_transforms.argtypes = [vp, vp]
+    L.dbox_body_def_default.argtypes = [vp]
+    L.dbox_fixture_def_default.argtypes = [vp]
+    _lib = L
+    return L
+
+
+def _check(rc, what):
+    if rc != 0:
+        msg = lib().dbox_last_error().decode(errors="replace")
+        raise DboxError("%s failed: %s (%s)" % (what, abi.ERRORS.get(rc, rc), msg))
+
+
+def collide_manifolds(shapes_a, xfs_a, shapes_b, xfs_b):
+    """Manifolds of shape pairs on the GPU (dbox_collide_manifolds); returns abi.CONTACT_STATE records."""
+    sa = np.ascontiguousarray(shapes_a, abi.SHAPE_DEF)
+    sb = np.ascontiguousarray(shapes_b, abi.SHAPE_DEF)
+    xa = np.ascontiguousarray(xfs_a, np.float32)
+    xb = np.ascontiguousarray(xfs_b, np.float32)
+    out = np.zeros(len(sa), abi.CONTACT_STATE)
+    _check(lib().dbox_collide_manifolds(len(sa), abi.ptr(sa), abi.ptr(xa), abi.ptr(sb), abi.ptr(xb), abi.ptr(out)),
+           "dbox_collide_manifolds")
+    return out
+
+
+class World:
+    """One or more b2Worlds on the GPU (b2World(gravity), b2world.d:865-895).
+
+    `scenes` is one scene dict or a list of them (see dbox_gb300.scenes); each
+    becomes an independent world of the batch.
+    """
+
+    def __init__(self, scenes, gravity=(0.0, -10.0), flags=None, contacts_per_body=0):
+        L = lib()
+        if isinstance(scenes, dict):
+            scenes = [scenes]
+        self.n_worlds = len(scenes)
+        caps = np.zeros(2, np.int32)
+        caps[0] = contacts_per_body
+        h = ctypes.c_void_p()
+        _check(L.dbox_world_create(abi.Vec2(*gravity), self.n_worlds, abi.ptr(caps), ctypes.byref(h)), "dbox_world_create")
+        self.h = h
+        for i, s in enumerate(scenes):
+            b = np.ascontiguousarray(s["bodies"])
+            fb = np.ascontiguousarray(s["fixture_body"], dtype=np.int32)
+            sh = np.ascontiguousarray(s["shapes"])
+            fx = np.ascontiguousarray(s["fixtures"])
+            j = np.ascontiguousarray(s["joints"])
+            _check(L.dbox_scene_create(self.h, i, len(b), abi.ptr(b), len(fb), abi.ptr(fb), abi.ptr(sh), abi.ptr(fx),
+                                       len(j), abi.ptr(j) if len(j) else None), "dbox_scene_create")
+        self.body_counts = [len(s["bodies"]) for s in scenes]
+        if flags is not None:
+            self.set_flags(**flags)
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            lib().dbox_world_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_flags(self, warm=1, continuous=1, substep=0, sleep=1, autoclear=1):
+        _check(lib().dbox_world_set_flags(self.h, warm, continuous, substep, sleep, autoclear), "dbox_world_set_flags")
+
+    def step(self, dt=1.0 / 60.0, vel_iters=8, pos_iters=3, steps=1, graph=False):
+        """b2World.Step(dt, velocityIterations, positionIterations) on every world."""
+        if graph:
+            _check(lib().dbox_world_step_n(self.h, ctypes.c_float(dt), vel_iters, pos_iters, steps), "dbox_world_step_n")
+        else:
+            for _ in range(steps):
+                _check(lib().dbox_world_step(self.h, ctypes.c_float(dt), vel_iters, pos_iters), "dbox_world_step")
+
+    def step_timed(self, steps, dt=1.0 / 60.0, vel_iters=8, pos_iters=3):
+        """Run `steps` steps as one CUDA graph; returns (total_ms, [collide_ms, solve_ms, toi_ms])."""
+        tot = np.zeros(1, np.float32)
+        ph = np.zeros(3, np.float32)
+        _check(lib().dbox_world_step_n_timed(self.h, ctypes.c_float(dt), vel_iters, pos_iters, steps, abi.ptr(tot),
+                                             abi.ptr(ph)), "dbox_world_step_n_timed")
+        return float(tot[0]), ph.astype(float).tolist()
+
+    def counters(self):
+        c = np.zeros(8, np.uint64)
+        _check(lib().dbox_world_get_counters(self.h, abi.ptr(c)), "dbox_world_get_counters")
+        keys = ("isl_bodies", "isl_contacts", "vsolve", "psolve", "contacts", "toi_events", "world_steps", "pairs")
+        return dict(zip(keys, (int(v) for v in c)))
+
+    def apply_forces(self, force_torque):
+        """ApplyForceToCenter + ApplyTorque (wake = false) on every body; (n_bodies, 3) float32, ideally pinned."""
+        assert force_torque.dtype == np.float32 and force_torque.flags["C_CONTIGUOUS"]
+        _check(lib().dbox_world_apply_forces(self.h, abi.ptr(force_torque)), "dbox_world_apply_forces")
+
+    def get_transforms(self, out):
+        """GetPosition + GetAngle of every body into out (n_bodies, 3) float32, ideally pinned."""
+        assert out.dtype == np.float32 and out.flags["C_CONTIGUOUS"]
+        _check(lib().dbox_world_get_transforms(self.h, abi.ptr(out)), "dbox_world_get_transforms")
+        return out
+
+    def sync(self):
+        _check(lib().dbox_world_sync(self.h), "dbox_world_sync")
+
+    def bodies(self):
+        n = sum(self.body_counts)
+        pos = np.zeros((n, 2), np.float32)
+        ang = np.zeros(n, np.float32)
+        vel = np.zeros((n, 2), np.float32)
+        avel = np.zeros(n, np.float32)
+        awake = np.zeros(n, np.int32)
+        _check(lib().dbox_world_get_bodies(self.h, abi.ptr(pos), abi.ptr(ang), abi.ptr(vel), abi.ptr(avel),
+                                           abi.ptr(awake)), "dbox_world_get_bodies")
+        return {"position": pos, "angle": ang, "linear_velocity": vel, "angular_velocity": avel, "awake": awake}
+
+    def export_state(self, world=0):
+        L = lib()
+        hdr = np.zeros(1, abi.WORLD_HEADER)
+        _check(L.dbox_world_export_state(self.h, world, abi.ptr(hdr), None, None, None, None), "export header")
+        h = hdr[0]
+        bodies = np.zeros(int(h["body_count"]), abi.BODY_STATE)
+        proxies = np.zeros(int(h["fixture_count"]), abi.PROXY_STATE)
+        contacts = np.zeros(int(h["contact_count"]), abi.CONTACT_STATE)
+        joints = np.zeros(int(h["joint_count"]), abi.JOINT_STATE)
+        _check(L.dbox_world_export_state(self.h, world, abi.ptr(hdr), abi.ptr(bodies), abi.ptr(proxies),
+                                         abi.ptr(contacts), abi.ptr(joints)), "export")
+        return {"header": hdr, "bodies": bodies, "proxies": proxies, "contacts": contacts, "joints": joints}
+
+    def import_state(self, state, world=0):
+        st = {k: np.ascontiguousarray(v) for k, v in state.items()}
+        _check(lib().dbox_world_import_state(self.h, world, abi.ptr(st["header"]), abi.ptr(st["bodies"]),
+                                             abi.ptr(st["proxies"]), abi.ptr(st["contacts"]),
+                                             abi.ptr(st["joints"])), "import")
+
+    def stats(self, world=0):
+        isl, toi = ctypes.c_int32(), ctypes.c_int32()
+        _check(lib().dbox_world_step_stats(self.h, world, ctypes.byref(isl), ctypes.byref(toi)), "stats")
+        return isl.value, toi.value
+
+    def last_launches(self):
+        n = ctypes.c_int32()
+        _check(lib().dbox_world_last_launches(self.h, ctypes.byref(n)), "launches")
+        return n.value
+
+    def profile(self):
+        p = np.zeros(1, abi.PROFILE)
+        _check(lib().dbox_world_get_profile(self.h, abi.ptr(p)), "profile")
+        return p[0]

@@ -1,0 +1,1104 @@
+// C ABI of libdbox_gpu.so (declared in include/dbox_gpu.h).
+//
+// Host side: world creation (the reference's b2World.CreateBody /
+// b2Body.CreateFixture / b2World.CreateJoint bookkeeping), upload of the
+// structure-of-arrays batch to the GPU, step launches (plain or replayed from a
+// CUDA graph) and state export/import.  All per-step work runs in the kernels
+// of step.cu; this file only moves data and launches.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+#include <stdio.h>
+#include <stdarg.h>
+#include <string>
+#include <vector>
+#include <algorithm>
+
+#include "world.cuh"
+#include "host_geom.h"
+
+extern "C" int dbox_launch_step(const dg::Ctx* x, cudaStream_t stream, int* launches);
+extern "C" int dbox_launch_step_ev(const dg::Ctx* x, cudaStream_t stream, int* launches, cudaEvent_t* ev);
+extern "C" int dbox_launch_gather_transforms(int n, const dbox_body_state* bs, float* out, cudaStream_t s);
+extern "C" int dbox_launch_apply_forces(int n, dbox_body_state* bs, const float* f, cudaStream_t s);
+extern "C" int dbox_launch_collide_pairs(int n, const dg::DFixture* fa, const float4* xa, const dg::DFixture* fb,
+                                         const float4* xb, dbox_contact_state* out, cudaStream_t stream);
+
+namespace {
+
+thread_local std::string g_last_error = "";
+
+int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+#define CU(call)                                                                          \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess) return fail(DBOX_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+struct HostWorld {
+    std::vector<dbox_body_state> bs;
+    std::vector<dg::BodyStatic> bst;
+    std::vector<std::vector<int>> body_fix;     // fixture indices per body, newest first
+    std::vector<dg::DFixture> fx;
+    std::vector<dbox_proxy_state> px;
+    std::vector<dg::DJoint> jt;
+    std::vector<dbox_contact_state> ct;
+    dg::WorldDyn wd;
+    int proxy_count = 0;
+    HostWorld() { memset(&wd, 0, sizeof(wd)); wd.flags = 4u; wd.step_complete = 1; }
+};
+
+template <class T> struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    int alloc(size_t count) {
+        free();
+        n = count;
+        if (count == 0) count = 1;
+        if (cudaMalloc(&p, count * sizeof(T)) != cudaSuccess) { p = nullptr; return -1; }
+        return 0;
+    }
+    void free() { if (p) cudaFree(p); p = nullptr; n = 0; }
+};
+
+}  // namespace
+
+struct dbox_world {
+    std::vector<HostWorld> worlds;
+    float2 gravity;
+    int warm = 1, continuous = 1, substep = 0, allow_sleep = 1, autoclear = 1;
+    dbox_world_caps caps;
+    bool on_device = false;     // device holds the authoritative dynamic state
+    bool dirty = true;          // host structure changed since the last upload
+    cudaStream_t stream = nullptr;
+    // device arrays
+    DBuf<dg::WorldInfo> d_wi;
+    DBuf<dg::WorldDyn> d_wd;
+    DBuf<dbox_body_state> d_bs;
+    DBuf<dg::BodyStatic> d_bst;
+    DBuf<int> d_body_fix, d_jadj_joint, d_jadj_other;
+    DBuf<dg::DFixture> d_fx;
+    DBuf<dbox_proxy_state> d_px;
+    DBuf<dg::DJoint> d_jt;
+    DBuf<dbox_contact_state> d_ct;
+    DBuf<int> d_cworld;
+    DBuf<unsigned long long> d_hash;
+    DBuf<int2> d_pairs;
+    DBuf<int> s_woken, s_adj_start, s_cursor, s_stack, s_isl_body, s_body_island, s_last, s_isl_bstart,
+        s_isl_cstart, s_isl_jstart, s_isl_flags, s_pcount, s_moved, s_cstate, s_adj_items, s_isl_contact, s_level,
+        s_sched_v, s_lvl_v, s_sched_p, s_lvl_p, s_tmp, s_isl_joint, s_accept, g_status;
+    DBuf<unsigned> s_isl_minsep, s_isl_sleep;
+    DBuf<dg::VC> d_vc;
+    DBuf<dg::PC> d_pc;
+    DBuf<dg::SweepSnap> d_snap;
+    DBuf<float> d_io;           // staging for bulk force upload / transform readback (3 floats per body)
+    std::vector<dg::WorldInfo> wi;
+    int total_bodies = 0, total_fixtures = 0, total_contacts = 0, total_joints = 0;
+    // graph replay
+    cudaGraphExec_t graph = nullptr;
+    float g_dt = -1.0f;
+    int g_vi = -1, g_pi = -1;
+    int graph_flags = -1;
+    dbox_profile profile;
+    int last_launches = 0;
+    dbox_event_fn listener = nullptr;
+    void* listener_user = nullptr;
+    cudaEvent_t ev[4];
+    bool events_made = false;
+    // timed multi-step graph (per-phase events inside the graph)
+    cudaGraphExec_t tgraph = nullptr;
+    std::vector<cudaEvent_t> tev;
+    int t_steps = -1;
+    float t_dt = -1.0f;
+    int t_vi = -1, t_pi = -1, t_flags = -1;
+};
+
+namespace {
+
+void free_device(dbox_world* w) {
+    w->d_wi.free(); w->d_wd.free(); w->d_bs.free(); w->d_bst.free(); w->d_body_fix.free();
+    w->d_jadj_joint.free(); w->d_jadj_other.free(); w->d_fx.free(); w->d_px.free(); w->d_jt.free();
+    w->d_ct.free(); w->d_cworld.free(); w->d_hash.free(); w->d_pairs.free();
+    DBuf<int>* ints[] = {&w->s_woken, &w->s_adj_start, &w->s_cursor, &w->s_stack, &w->s_isl_body, &w->s_body_island,
+                         &w->s_last, &w->s_isl_bstart, &w->s_isl_cstart, &w->s_isl_jstart, &w->s_isl_flags,
+                         &w->s_pcount, &w->s_moved, &w->s_cstate, &w->s_adj_items, &w->s_isl_contact, &w->s_level,
+                         &w->s_sched_v, &w->s_lvl_v, &w->s_sched_p, &w->s_lvl_p, &w->s_tmp, &w->s_isl_joint,
+                         &w->s_accept, &w->g_status};
+    for (auto* b : ints) b->free();
+    w->s_isl_minsep.free(); w->s_isl_sleep.free();
+    w->d_vc.free(); w->d_pc.free(); w->d_snap.free(); w->d_io.free();
+    if (w->graph) { cudaGraphExecDestroy(w->graph); w->graph = nullptr; }
+    if (w->tgraph) { cudaGraphExecDestroy(w->tgraph); w->tgraph = nullptr; }
+}
+
+int next_pow2(int v) { int p = 1; while (p < v) p <<= 1; return p; }
+
+// Pull the authoritative dynamic state back to the host mirrors.
+int download(dbox_world* w) {
+    if (!w->on_device) return 0;
+    CU(cudaStreamSynchronize(w->stream));
+    int W = (int)w->worlds.size();
+    std::vector<dg::WorldDyn> wd(W);
+    CU(cudaMemcpy(wd.data(), w->d_wd.p, sizeof(dg::WorldDyn) * W, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < W; ++i) {
+        HostWorld& hw = w->worlds[i];
+        const dg::WorldInfo& wi = w->wi[i];
+        hw.wd = wd[i];
+        if (!hw.bs.empty())
+            CU(cudaMemcpy(hw.bs.data(), w->d_bs.p + wi.body_start, sizeof(dbox_body_state) * hw.bs.size(),
+                          cudaMemcpyDeviceToHost));
+        if (!hw.px.empty())
+            CU(cudaMemcpy(hw.px.data(), w->d_px.p + wi.fix_start, sizeof(dbox_proxy_state) * hw.px.size(),
+                          cudaMemcpyDeviceToHost));
+        if (!hw.jt.empty())
+            CU(cudaMemcpy(hw.jt.data(), w->d_jt.p + wi.joint_start, sizeof(dg::DJoint) * hw.jt.size(),
+                          cudaMemcpyDeviceToHost));
+        hw.ct.resize(hw.wd.contact_count);
+        if (!hw.ct.empty())
+            CU(cudaMemcpy(hw.ct.data(), w->d_ct.p + wi.contact_start, sizeof(dbox_contact_state) * hw.ct.size(),
+                          cudaMemcpyDeviceToHost));
+        // device fixture/joint indices are global; host mirrors keep world-local ones
+        for (auto& c : hw.ct) { c.fixture_a -= wi.fix_start; c.fixture_b -= wi.fix_start; }
+        for (auto& j : hw.jt) { j.body_a -= wi.body_start; j.body_b -= wi.body_start; }
+    }
+    w->on_device = false;
+    return 0;
+}
+
+// Lay out every world in the batch and copy it to the device.
+int upload(dbox_world* w) {
+    free_device(w);
+    int W = (int)w->worlds.size();
+    w->wi.assign(W, dg::WorldInfo());
+    int nb = 0, nf = 0, nj = 0, nc = 0, nh = 0, np = 0, nbx = 0, nkx = 0;
+    int cpb = w->caps.contacts_per_body > 0 ? w->caps.contacts_per_body : 8;
+    for (int i = 0; i < W; ++i) {
+        HostWorld& hw = w->worlds[i];
+        dg::WorldInfo& wi = w->wi[i];
+        int b = (int)hw.bs.size(), f = (int)hw.fx.size(), j = (int)hw.jt.size();
+        int cap = cpb * b + 64;
+        if (cap < (int)hw.ct.size() * 2) cap = (int)hw.ct.size() * 2;
+        wi.body_start = nb; wi.body_count = b;
+        wi.fix_start = nf; wi.fix_count = f;
+        wi.joint_start = nj; wi.joint_count = j;
+        wi.contact_start = nc; wi.contact_cap = cap;
+        wi.hash_start = nh; wi.hash_cap = next_pow2(2 * cap);
+        wi.pair_start = np; wi.pair_cap = 16 * f + 64;
+        wi.bx_start = nbx;
+        wi.kx_start = nkx;
+        wi.snap_start = nc;
+        nb += b; nf += f; nj += j; nc += cap; nh += wi.hash_cap; np += wi.pair_cap; nbx += b + 1; nkx += cap + j + 2;
+    }
+    w->total_bodies = nb; w->total_fixtures = nf; w->total_joints = nj; w->total_contacts = nc;
+    // flatten
+    std::vector<dg::WorldDyn> wd(W);
+    std::vector<dbox_body_state> bs(nb);
+    std::vector<dg::BodyStatic> bst(nb);
+    std::vector<int> body_fix, jadj_joint, jadj_other;
+    std::vector<dg::DFixture> fx(nf);
+    std::vector<dbox_proxy_state> px(nf);
+    std::vector<dg::DJoint> jt(nj);
+    std::vector<dbox_contact_state> ct(nc);
+    std::vector<int> cworld(nc);
+    memset(ct.data(), 0, sizeof(dbox_contact_state) * ct.size());
+    for (int i = 0; i < W; ++i) {
+        HostWorld& hw = w->worlds[i];
+        const dg::WorldInfo& wi = w->wi[i];
+        wd[i] = hw.wd;
+        wd[i].contact_count = (int)hw.ct.size();
+        wd[i].flags = (hw.wd.flags & ~4u) | (w->autoclear ? 4u : 0u);
+        // joint adjacency, newest joint first (b2world.d:226-242 head insertion)
+        std::vector<std::vector<std::pair<int, int>>> jadj(hw.bs.size());
+        for (int j = 0; j < (int)hw.jt.size(); ++j) {
+            jadj[hw.jt[j].body_a].push_back({j, hw.jt[j].body_b});
+            jadj[hw.jt[j].body_b].push_back({j, hw.jt[j].body_a});
+        }
+        for (int b = 0; b < (int)hw.bs.size(); ++b) {
+            bs[wi.body_start + b] = hw.bs[b];
+            dg::BodyStatic s = hw.bst[b];
+            s.world = i;
+            s.fix_start = (int)body_fix.size();
+            s.fix_count = (int)hw.body_fix[b].size();
+            for (int f : hw.body_fix[b]) body_fix.push_back(wi.fix_start + f);
+            s.jadj_start = (int)jadj_joint.size();
+            s.jadj_count = (int)jadj[b].size();
+            for (int e = (int)jadj[b].size() - 1; e >= 0; --e) {
+                jadj_joint.push_back(wi.joint_start + jadj[b][e].first);
+                jadj_other.push_back(wi.body_start + jadj[b][e].second);
+            }
+            bst[wi.body_start + b] = s;
+        }
+        for (int f = 0; f < (int)hw.fx.size(); ++f) {
+            dg::DFixture d = hw.fx[f];
+            d.body += wi.body_start;
+            fx[wi.fix_start + f] = d;
+            px[wi.fix_start + f] = hw.px[f];
+        }
+        for (int j = 0; j < (int)hw.jt.size(); ++j) {
+            dg::DJoint d = hw.jt[j];
+            d.body_a += wi.body_start;
+            d.body_b += wi.body_start;
+            jt[wi.joint_start + j] = d;
+        }
+        for (int k = 0; k < (int)hw.ct.size(); ++k) {
+            dbox_contact_state c = hw.ct[k];
+            c.fixture_a += wi.fix_start;
+            c.fixture_b += wi.fix_start;
+            ct[wi.contact_start + k] = c;
+        }
+        for (int k = 0; k < wi.contact_cap; ++k) cworld[wi.contact_start + k] = i;
+    }
+    bool ok = true;
+    ok &= w->d_wi.alloc(W) == 0;
+    ok &= w->d_wd.alloc(W) == 0;
+    ok &= w->d_bs.alloc(nb) == 0;
+    ok &= w->d_bst.alloc(nb) == 0;
+    ok &= w->d_body_fix.alloc(body_fix.size()) == 0;
+    ok &= w->d_jadj_joint.alloc(jadj_joint.size()) == 0;
+    ok &= w->d_jadj_other.alloc(jadj_other.size()) == 0;
+    ok &= w->d_fx.alloc(nf) == 0;
+    ok &= w->d_px.alloc(nf) == 0;
+    ok &= w->d_jt.alloc(nj) == 0;
+    ok &= w->d_ct.alloc(nc) == 0;
+    ok &= w->d_cworld.alloc(nc) == 0;
+    ok &= w->d_hash.alloc(nh) == 0;
+    ok &= w->d_pairs.alloc(np) == 0;
+    ok &= w->s_woken.alloc(nb) == 0;
+    ok &= w->s_adj_start.alloc(nbx) == 0;
+    ok &= w->s_cursor.alloc(nb) == 0;
+    ok &= w->s_stack.alloc(nb) == 0;
+    ok &= w->s_isl_body.alloc(nb) == 0;
+    ok &= w->s_body_island.alloc(nb) == 0;
+    ok &= w->s_last.alloc(nb) == 0;
+    ok &= w->s_isl_bstart.alloc(nbx) == 0;
+    ok &= w->s_isl_cstart.alloc(nbx) == 0;
+    ok &= w->s_isl_jstart.alloc(nbx) == 0;
+    ok &= w->s_isl_flags.alloc(nb) == 0;
+    ok &= w->s_isl_minsep.alloc(nb) == 0;
+    ok &= w->s_isl_sleep.alloc(nb) == 0;
+    ok &= w->s_pcount.alloc(nf) == 0;
+    ok &= w->s_moved.alloc(nf) == 0;
+    ok &= w->s_cstate.alloc(nc) == 0;
+    ok &= w->s_adj_items.alloc(2 * (size_t)nc) == 0;
+    ok &= w->s_isl_contact.alloc(nc) == 0;
+    ok &= w->s_level.alloc(nkx) == 0;
+    ok &= w->s_sched_v.alloc(nkx) == 0;
+    ok &= w->s_lvl_v.alloc(nkx) == 0;
+    ok &= w->s_sched_p.alloc(nkx) == 0;
+    ok &= w->s_lvl_p.alloc(nkx) == 0;
+    ok &= w->s_tmp.alloc(nkx) == 0;
+    ok &= w->s_isl_joint.alloc(nj) == 0;
+    ok &= w->s_accept.alloc(np) == 0;
+    ok &= w->g_status.alloc(1) == 0;
+    ok &= w->d_vc.alloc(nc) == 0;
+    ok &= w->d_pc.alloc(nc) == 0;
+    ok &= w->d_snap.alloc(nc) == 0;
+    ok &= w->d_io.alloc(3 * (size_t)nb) == 0;
+    if (!ok) { free_device(w); return fail(DBOX_ERR_CUDA, "device allocation failed (%d bodies, %d contact slots)", nb, nc); }
+    CU(cudaMemcpy(w->d_wi.p, w->wi.data(), sizeof(dg::WorldInfo) * W, cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(w->d_wd.p, wd.data(), sizeof(dg::WorldDyn) * W, cudaMemcpyHostToDevice));
+    if (nb) {
+        CU(cudaMemcpy(w->d_bs.p, bs.data(), sizeof(dbox_body_state) * nb, cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(w->d_bst.p, bst.data(), sizeof(dg::BodyStatic) * nb, cudaMemcpyHostToDevice));
+    }
+    if (!body_fix.empty()) CU(cudaMemcpy(w->d_body_fix.p, body_fix.data(), sizeof(int) * body_fix.size(), cudaMemcpyHostToDevice));
+    if (!jadj_joint.empty()) {
+        CU(cudaMemcpy(w->d_jadj_joint.p, jadj_joint.data(), sizeof(int) * jadj_joint.size(), cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(w->d_jadj_other.p, jadj_other.data(), sizeof(int) * jadj_other.size(), cudaMemcpyHostToDevice));
+    }
+    if (nf) {
+        CU(cudaMemcpy(w->d_fx.p, fx.data(), sizeof(dg::DFixture) * nf, cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(w->d_px.p, px.data(), sizeof(dbox_proxy_state) * nf, cudaMemcpyHostToDevice));
+    }
+    if (nj) CU(cudaMemcpy(w->d_jt.p, jt.data(), sizeof(dg::DJoint) * nj, cudaMemcpyHostToDevice));
+    if (nc) {
+        CU(cudaMemcpy(w->d_ct.p, ct.data(), sizeof(dbox_contact_state) * nc, cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(w->d_cworld.p, cworld.data(), sizeof(int) * nc, cudaMemcpyHostToDevice));
+    }
+    CU(cudaMemset(w->g_status.p, 0, sizeof(int)));
+    w->on_device = true;
+    w->dirty = false;
+    return 0;
+}
+
+int ensure_device(dbox_world* w) {
+    if (w->dirty || !w->on_device) {
+        int rc = download(w);
+        if (rc) return rc;
+        return upload(w);
+    }
+    return 0;
+}
+
+dg::Ctx make_ctx(dbox_world* w, float dt, int vi, int pi) {
+    dg::Ctx x;
+    memset(&x, 0, sizeof(x));
+    x.W = (int)w->worlds.size();
+    x.total_bodies = w->total_bodies;
+    x.total_fixtures = w->total_fixtures;
+    x.total_contacts = w->total_contacts;
+    x.total_joints = w->total_joints;
+    x.wi = w->d_wi.p;
+    x.wd = w->d_wd.p;
+    x.bs = w->d_bs.p;
+    x.bst = w->d_bst.p;
+    x.body_fix = w->d_body_fix.p;
+    x.jadj_joint = w->d_jadj_joint.p;
+    x.jadj_other = w->d_jadj_other.p;
+    x.fx = w->d_fx.p;
+    x.px = w->d_px.p;
+    x.jt = w->d_jt.p;
+    x.ct = w->d_ct.p;
+    x.c_world = w->d_cworld.p;
+    x.hash = w->d_hash.p;
+    x.pairs = w->d_pairs.p;
+    x.s_woken = w->s_woken.p;
+    x.s_adj_start = w->s_adj_start.p;
+    x.s_cursor = w->s_cursor.p;
+    x.s_stack = w->s_stack.p;
+    x.s_isl_body = w->s_isl_body.p;
+    x.s_body_island = w->s_body_island.p;
+    x.s_last = w->s_last.p;
+    x.s_isl_bstart = w->s_isl_bstart.p;
+    x.s_isl_cstart = w->s_isl_cstart.p;
+    x.s_isl_jstart = w->s_isl_jstart.p;
+    x.s_isl_minsep = w->s_isl_minsep.p;
+    x.s_isl_flags = w->s_isl_flags.p;
+    x.s_isl_sleep = w->s_isl_sleep.p;
+    x.s_pcount = w->s_pcount.p;
+    x.s_moved = w->s_moved.p;
+    x.s_cstate = w->s_cstate.p;
+    x.s_adj_items = w->s_adj_items.p;
+    x.s_isl_contact = w->s_isl_contact.p;
+    x.s_level = w->s_level.p;
+    x.s_sched_v = w->s_sched_v.p;
+    x.s_lvl_v = w->s_lvl_v.p;
+    x.s_sched_p = w->s_sched_p.p;
+    x.s_lvl_p = w->s_lvl_p.p;
+    x.s_tmp = w->s_tmp.p;
+    x.s_isl_joint = w->s_isl_joint.p;
+    x.s_accept = w->s_accept.p;
+    x.vc = w->d_vc.p;
+    x.pc = w->d_pc.p;
+    x.snap = w->d_snap.p;
+    x.dt = dt;
+    x.inv_dt = dt > 0.0f ? 1.0f / dt : 0.0f;                            // b2world.d:383-390
+    x.vel_iters = vi;
+    x.pos_iters = pi;
+    x.gravity = w->gravity;
+    x.warm_starting = w->warm;
+    x.continuous = w->continuous;
+    x.sub_stepping = w->substep;
+    x.allow_sleep = w->allow_sleep;
+    x.record_events = w->listener ? 1 : 0;
+    x.g_status = w->g_status.p;
+    return x;
+}
+
+int check_status(dbox_world* w) {
+    int st = 0;
+    CU(cudaMemcpyAsync(&st, w->g_status.p, sizeof(int), cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    if (st) {
+        CU(cudaMemsetAsync(w->g_status.p, 0, sizeof(int), w->stream));
+        for (int code = 1; code < 31; ++code)
+            if (st & (1 << code)) return fail(-code, "device step reported status %d (bits 0x%x)", -code, st);
+    }
+    return 0;
+}
+
+void fill_body_state(const dbox_body_def* d, dbox_body_state* s, dg::BodyStatic* st) {
+    memset(s, 0, sizeof(*s));                                           // b2body.d:1030-1115
+    uint32_t f = 0;
+    if (d->bullet) f |= dg::kBodyBullet;
+    if (d->fixed_rotation) f |= dg::kBodyFixedRotation;
+    if (d->allow_sleep) f |= dg::kBodyAutoSleep;
+    if (d->awake) f |= dg::kBodyAwake;
+    if (d->active) f |= dg::kBodyActive;
+    s->flags = f;
+    s->type = d->type;
+    hg::Rot q = hg::rot(d->angle);
+    s->xf[0] = d->position.x; s->xf[1] = d->position.y; s->xf[2] = q.s; s->xf[3] = q.c;
+    s->sweep[0] = 0.0f; s->sweep[1] = 0.0f;
+    s->sweep[2] = d->position.x; s->sweep[3] = d->position.y;
+    s->sweep[4] = d->position.x; s->sweep[5] = d->position.y;
+    s->sweep[6] = d->angle; s->sweep[7] = d->angle; s->sweep[8] = 0.0f;
+    s->vel[0] = d->linear_velocity.x; s->vel[1] = d->linear_velocity.y; s->vel[2] = d->angular_velocity;
+    if (d->type == DBOX_DYNAMIC_BODY) { s->mass[0] = 1.0f; s->mass[1] = 1.0f; }
+    memset(st, 0, sizeof(*st));
+    st->lin_damping = d->linear_damping;
+    st->ang_damping = d->angular_damping;
+    st->gravity_scale = d->gravity_scale;
+}
+
+// b2Body.ResetMassData (b2body.d:555-625)
+void reset_mass(HostWorld& hw, int b) {
+    dbox_body_state& s = hw.bs[b];
+    float mass = 0.0f, invMass = 0.0f, I = 0.0f, invI = 0.0f;
+    s.sweep[0] = 0.0f; s.sweep[1] = 0.0f;
+    if (s.type == DBOX_STATIC_BODY || s.type == DBOX_KINEMATIC_BODY) {
+        s.sweep[2] = s.xf[0]; s.sweep[3] = s.xf[1];
+        s.sweep[4] = s.xf[0]; s.sweep[5] = s.xf[1];
+        s.sweep[6] = s.sweep[7];
+        s.mass[0] = s.mass[1] = s.mass[2] = s.mass[3] = 0.0f;
+        return;
+    }
+    hg::V2 lc = hg::mk(0.0f, 0.0f);
+    for (int f : hw.body_fix[b]) {
+        const dg::DFixture& fx = hw.fx[f];
+        if (fx.density == 0.0f) continue;
+        hg::Mass md;
+        if (fx.type == dg::kShapeCircle) md = hg::circle_mass(hg::mk(fx.v[0].x, fx.v[0].y), fx.radius, fx.density);
+        else {
+            hg::Poly p;
+            p.count = fx.count;
+            for (int i = 0; i < fx.count; ++i) { p.v[i] = hg::mk(fx.v[i].x, fx.v[i].y); }
+            md = hg::poly_mass(p, fx.density);
+        }
+        mass += md.mass;
+        lc = hg::add(lc, hg::scl(md.mass, md.center));
+        I += md.I;
+    }
+    if (mass > 0.0f) {
+        invMass = 1.0f / mass;
+        lc.x *= invMass;
+        lc.y *= invMass;
+    } else {
+        mass = 1.0f;
+        invMass = 1.0f;
+    }
+    if (I > 0.0f && (s.flags & dg::kBodyFixedRotation) == 0) {
+        I -= mass * hg::dot(lc, lc);
+        invI = 1.0f / I;
+    } else {
+        I = 0.0f;
+        invI = 0.0f;
+    }
+    hg::V2 oldCenter = hg::mk(s.sweep[4], s.sweep[5]);
+    s.sweep[0] = lc.x; s.sweep[1] = lc.y;
+    hg::Rot q; q.s = s.xf[2]; q.c = s.xf[3];
+    hg::V2 c = hg::xmul(hg::mk(s.xf[0], s.xf[1]), q, lc);
+    s.sweep[2] = s.sweep[4] = c.x;
+    s.sweep[3] = s.sweep[5] = c.y;
+    hg::V2 d = hg::sub(c, oldCenter);
+    float wv = s.vel[2];
+    s.vel[0] += -wv * d.y;                                             // b2Cross(w, c - oldCenter)
+    s.vel[1] += wv * d.x;
+    s.mass[0] = mass; s.mass[1] = invMass; s.mass[2] = I; s.mass[3] = invI;
+}
+
+bool build_fixture(const dbox_shape_def* sd, dg::DFixture* f) {
+    memset(f, 0, sizeof(*f));
+    switch (sd->kind) {
+    case DBOX_SHAPE_CIRCLE:
+        f->type = dg::kShapeCircle;
+        f->count = 1;
+        f->radius = sd->radius;
+        f->v[0] = make_float2(sd->center.x, sd->center.y);
+        return true;
+    case DBOX_SHAPE_POLYGON:
+    case DBOX_SHAPE_BOX:
+    case DBOX_SHAPE_ORIENTED_BOX: {
+        hg::Poly p;
+        if (sd->kind == DBOX_SHAPE_POLYGON) {
+            hg::V2 in[8];
+            if (sd->count < 3 || sd->count > 8) return false;
+            for (int i = 0; i < sd->count; ++i) in[i] = hg::mk(sd->vertices[i].x, sd->vertices[i].y);
+            if (!hg::set_hull(p, in, sd->count)) return false;
+        } else if (sd->kind == DBOX_SHAPE_BOX) {
+            hg::set_as_box(p, sd->hx, sd->hy);
+        } else {
+            hg::set_as_box(p, sd->hx, sd->hy, hg::mk(sd->center.x, sd->center.y), sd->angle);
+        }
+        f->type = dg::kShapePolygon;
+        f->count = p.count;
+        f->radius = 2.0f * 0.005f;                                      // b2_polygonRadius
+        for (int i = 0; i < p.count; ++i) {
+            f->v[i] = make_float2(p.v[i].x, p.v[i].y);
+            f->n[i] = make_float2(p.n[i].x, p.n[i].y);
+        }
+        return true;
+    }
+    default:
+        return false;
+    }
+}
+
+// polygon / circle AABB at a transform (b2polygonshape.d:356-373, b2circleshape.d:110-117)
+void host_aabb(const dg::DFixture& f, const dbox_body_state& b, float out[4]) {
+    hg::Rot q; q.s = b.xf[2]; q.c = b.xf[3];
+    hg::V2 p = hg::mk(b.xf[0], b.xf[1]);
+    if (f.type == dg::kShapeCircle) {
+        hg::V2 c = hg::add(p, hg::rmul(q, hg::mk(f.v[0].x, f.v[0].y)));
+        out[0] = c.x - f.radius; out[1] = c.y - f.radius; out[2] = c.x + f.radius; out[3] = c.y + f.radius;
+        return;
+    }
+    hg::V2 lo = hg::xmul(p, q, hg::mk(f.v[0].x, f.v[0].y)), hi = lo;
+    for (int i = 1; i < f.count; ++i) {
+        hg::V2 v = hg::xmul(p, q, hg::mk(f.v[i].x, f.v[i].y));
+        lo.x = lo.x < v.x ? lo.x : v.x; lo.y = lo.y < v.y ? lo.y : v.y;
+        hi.x = hi.x > v.x ? hi.x : v.x; hi.y = hi.y > v.y ? hi.y : v.y;
+    }
+    out[0] = lo.x - f.radius; out[1] = lo.y - f.radius; out[2] = hi.x + f.radius; out[3] = hi.y + f.radius;
+}
+
+int create_fixture(HostWorld& hw, int body, const dbox_shape_def* shape, const dbox_fixture_def* def) {
+    dg::DFixture f;
+    if (!build_fixture(shape, &f)) return -1;
+    f.body = body;
+    f.friction = def->friction;
+    f.restitution = def->restitution;
+    f.density = def->density;
+    f.sensor = def->is_sensor ? 1 : 0;
+    f.filter = (uint32_t)def->category_bits | ((uint32_t)def->mask_bits << 16);
+    f.group = def->group_index;
+    int idx = (int)hw.fx.size();
+    hw.fx.push_back(f);
+    dbox_proxy_state p;
+    memset(&p, 0, sizeof(p));
+    p.proxy_id = -1;
+    if (hw.bs[body].flags & dg::kBodyActive) {                          // b2fixture.d:450-465 + b2dynamictree.d:110-124
+        float a[4];
+        host_aabb(f, hw.bs[body], a);
+        p.fat_aabb[0] = a[0] - 0.1f; p.fat_aabb[1] = a[1] - 0.1f;
+        p.fat_aabb[2] = a[2] + 0.1f; p.fat_aabb[3] = a[3] + 0.1f;
+        p.moved = 1;
+        p.proxy_id = hw.proxy_count == 0 ? 0 : 2 * hw.proxy_count - 1;
+        ++hw.proxy_count;
+    }
+    hw.px.push_back(p);
+    hw.body_fix[body].insert(hw.body_fix[body].begin(), idx);
+    if (f.density > 0.0f) reset_mass(hw, body);
+    hw.wd.flags |= 1u;                                                  // e_newFixture
+    return idx;
+}
+
+int create_joint(HostWorld& hw, const dbox_revolute_def* d) {
+    int nb = (int)hw.bs.size();
+    if (d->body_a < 0 || d->body_a >= nb || d->body_b < 0 || d->body_b >= nb || d->body_a == d->body_b) return -1;
+    dg::DJoint j;
+    memset(&j, 0, sizeof(j));
+    j.body_a = d->body_a;
+    j.body_b = d->body_b;
+    j.collide_connected = d->collide_connected ? 1 : 0;
+    j.local_anchor_a = make_float2(d->local_anchor_a.x, d->local_anchor_a.y);
+    j.local_anchor_b = make_float2(d->local_anchor_b.x, d->local_anchor_b.y);
+    j.reference_angle = d->reference_angle;
+    j.enable_limit = d->enable_limit ? 1 : 0;
+    j.lower_angle = d->lower_angle;
+    j.upper_angle = d->upper_angle;
+    j.enable_motor = d->enable_motor ? 1 : 0;
+    j.motor_speed = d->motor_speed;
+    j.max_motor_torque = d->max_motor_torque;
+    int idx = (int)hw.jt.size();
+    hw.jt.push_back(j);
+    if (!j.collide_connected) {                                         // b2world.d:246-258
+        for (auto& c : hw.ct) {
+            int A = hw.fx[c.fixture_a].body, B = hw.fx[c.fixture_b].body;
+            if ((A == j.body_a && B == j.body_b) || (A == j.body_b && B == j.body_a)) c.flags |= dg::kContactFilter;
+        }
+    }
+    return idx;
+}
+
+int prepare_edit(dbox_world* w) {
+    if (w->on_device) {
+        int rc = download(w);
+        if (rc) return rc;
+    }
+    w->dirty = true;
+    if (w->graph) { cudaGraphExecDestroy(w->graph); w->graph = nullptr; }
+    if (w->tgraph) { cudaGraphExecDestroy(w->tgraph); w->tgraph = nullptr; }
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* dbox_last_error(void) { return g_last_error.c_str(); }
+
+void dbox_body_def_default(dbox_body_def* d) {
+    memset(d, 0, sizeof(*d));
+    d->type = DBOX_STATIC_BODY;
+    d->allow_sleep = 1;
+    d->awake = 1;
+    d->active = 1;
+    d->gravity_scale = 1.0f;
+}
+
+void dbox_fixture_def_default(dbox_fixture_def* d) {
+    memset(d, 0, sizeof(*d));
+    d->friction = 0.2f;
+    d->category_bits = 0x0001;
+    d->mask_bits = 0xFFFF;
+}
+
+int32_t dbox_world_create(dbox_vec2 gravity, int32_t n_worlds, const dbox_world_caps* caps, dbox_world** out) {
+    if (!out || n_worlds < 1) return fail(DBOX_ERR_INVALID, "dbox_world_create: bad arguments");
+    dbox_world* w = new dbox_world();
+    w->gravity = make_float2(gravity.x, gravity.y);
+    w->worlds.resize(n_worlds);
+    memset(&w->caps, 0, sizeof(w->caps));
+    if (caps) w->caps = *caps;
+    memset(&w->profile, 0, sizeof(w->profile));
+    if (cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete w;
+        return fail(DBOX_ERR_CUDA, "cudaStreamCreate failed (is a GPU visible?)");
+    }
+    *out = w;
+    return DBOX_OK;
+}
+
+int32_t dbox_world_destroy(dbox_world* w) {
+    if (!w) return DBOX_ERR_INVALID;
+    free_device(w);
+    for (auto& e : w->tev) cudaEventDestroy(e);
+    if (w->events_made) for (auto& e : w->ev) cudaEventDestroy(e);
+    if (w->stream) cudaStreamDestroy(w->stream);
+    delete w;
+    return DBOX_OK;
+}
+
+int32_t dbox_body_create(dbox_world* w, int32_t world, const dbox_body_def* def, int32_t* out_body) {
+    if (!w || !def || world < 0 || world >= (int)w->worlds.size()) return fail(DBOX_ERR_INVALID, "dbox_body_create: bad arguments");
+    int rc = prepare_edit(w);
+    if (rc) return rc;
+    HostWorld& hw = w->worlds[world];
+    dbox_body_state s;
+    dg::BodyStatic st;
+    fill_body_state(def, &s, &st);
+    hw.bs.push_back(s);
+    hw.bst.push_back(st);
+    hw.body_fix.emplace_back();
+    if (out_body) *out_body = (int)hw.bs.size() - 1;
+    return DBOX_OK;
+}
+
+int32_t dbox_fixture_create(dbox_world* w, int32_t world, int32_t body, const dbox_shape_def* shape,
+                            const dbox_fixture_def* def, int32_t* out_fixture) {
+    if (!w || !shape || !def || world < 0 || world >= (int)w->worlds.size())
+        return fail(DBOX_ERR_INVALID, "dbox_fixture_create: bad arguments");
+    HostWorld& hw0 = w->worlds[world];
+    if (body < 0 || body >= (int)hw0.bs.size()) return fail(DBOX_ERR_INVALID, "dbox_fixture_create: no body %d", body);
+    int rc = prepare_edit(w);
+    if (rc) return rc;
+    int idx = create_fixture(w->worlds[world], body, shape, def);
+    if (idx < 0) return fail(DBOX_ERR_INVALID, "dbox_fixture_create: degenerate or unsupported shape");
+    if (out_fixture) *out_fixture = idx;
+    return DBOX_OK;
+}
+
+int32_t dbox_joint_create_revolute(dbox_world* w, int32_t world, const dbox_revolute_def* def, int32_t* out_joint) {
+    if (!w || !def || world < 0 || world >= (int)w->worlds.size()) return fail(DBOX_ERR_INVALID, "dbox_joint_create_revolute: bad arguments");
+    int rc = prepare_edit(w);
+    if (rc) return rc;
+    int idx = create_joint(w->worlds[world], def);
+    if (idx < 0) return fail(DBOX_ERR_INVALID, "dbox_joint_create_revolute: bad bodies");
+    if (out_joint) *out_joint = idx;
+    return DBOX_OK;
+}
+
+int32_t dbox_scene_create(dbox_world* w, int32_t world, int32_t n_bodies, const dbox_body_def* bodies,
+                          int32_t n_fixtures, const int32_t* fixture_body, const dbox_shape_def* shapes,
+                          const dbox_fixture_def* fixtures, int32_t n_joints, const dbox_revolute_def* joints) {
+    if (!w || world < 0 || world >= (int)w->worlds.size() || n_bodies < 0 || n_fixtures < 0 || n_joints < 0)
+        return fail(DBOX_ERR_INVALID, "dbox_scene_create: bad arguments");
+    if ((n_bodies && !bodies) || (n_fixtures && (!fixture_body || !shapes || !fixtures)) || (n_joints && !joints))
+        return fail(DBOX_ERR_INVALID, "dbox_scene_create: null array");
+    int rc = prepare_edit(w);
+    if (rc) return rc;
+    HostWorld& hw = w->worlds[world];
+    int base = (int)hw.bs.size();
+    hw.bs.reserve(base + n_bodies);
+    hw.bst.reserve(base + n_bodies);
+    for (int i = 0; i < n_bodies; ++i) {
+        dbox_body_state s;
+        dg::BodyStatic st;
+        fill_body_state(bodies + i, &s, &st);
+        hw.bs.push_back(s);
+        hw.bst.push_back(st);
+        hw.body_fix.emplace_back();
+    }
+    for (int i = 0; i < n_fixtures; ++i) {
+        int b = base + fixture_body[i];
+        if (fixture_body[i] < 0 || b >= (int)hw.bs.size()) return fail(DBOX_ERR_INVALID, "dbox_scene_create: fixture %d body", i);
+        if (create_fixture(hw, b, shapes + i, fixtures + i) < 0)
+            return fail(DBOX_ERR_INVALID, "dbox_scene_create: fixture %d degenerate or unsupported", i);
+    }
+    for (int i = 0; i < n_joints; ++i) {
+        dbox_revolute_def d = joints[i];
+        d.body_a += base;
+        d.body_b += base;
+        if (create_joint(hw, &d) < 0) return fail(DBOX_ERR_INVALID, "dbox_scene_create: joint %d bodies", i);
+    }
+    return DBOX_OK;
+}
+
+int32_t dbox_world_set_flags(dbox_world* w, int32_t warm_starting, int32_t continuous, int32_t sub_stepping,
+                             int32_t allow_sleep, int32_t auto_clear_forces) {
+    if (!w) return DBOX_ERR_INVALID;
+    bool sleep_flag = allow_sleep != 0;
+    if (sleep_flag != (w->allow_sleep != 0) && !sleep_flag) {
+        // b2World.SetAllowSleeping(false) wakes every body (b2world.d:627-643)
+        int rc = prepare_edit(w);
+        if (rc) return rc;
+        for (auto& hw : w->worlds)
+            for (auto& b : hw.bs)
+                if ((b.flags & dg::kBodyAwake) == 0) { b.flags |= dg::kBodyAwake; b.sleep_time = 0.0f; }
+    }
+    if ((auto_clear_forces != 0) != (w->autoclear != 0)) {
+        int rc = prepare_edit(w);
+        if (rc) return rc;
+    }
+    w->warm = warm_starting ? 1 : 0;
+    w->continuous = continuous ? 1 : 0;
+    w->substep = sub_stepping ? 1 : 0;
+    w->allow_sleep = sleep_flag ? 1 : 0;
+    w->autoclear = auto_clear_forces ? 1 : 0;
+    if (w->graph) { cudaGraphExecDestroy(w->graph); w->graph = nullptr; }
+    return DBOX_OK;
+}
+
+int32_t dbox_world_set_gravity(dbox_world* w, dbox_vec2 gravity) {
+    if (!w) return DBOX_ERR_INVALID;
+    w->gravity = make_float2(gravity.x, gravity.y);
+    if (w->graph) { cudaGraphExecDestroy(w->graph); w->graph = nullptr; }
+    return DBOX_OK;
+}
+
+int32_t dbox_world_set_listener(dbox_world* w, dbox_event_fn fn, void* user) {
+    if (!w) return DBOX_ERR_INVALID;
+    if (fn) return fail(DBOX_ERR_UNSUPPORTED, "contact listener events are not recorded by this build");
+    w->listener = nullptr;
+    w->listener_user = user;
+    return DBOX_OK;
+}
+
+int32_t dbox_world_step(dbox_world* w, float dt, int32_t velocity_iterations, int32_t position_iterations) {
+    if (!w || velocity_iterations < 0 || position_iterations < 0) return fail(DBOX_ERR_INVALID, "dbox_world_step: bad arguments");
+    int rc = ensure_device(w);
+    if (rc) return rc;
+    if (!w->events_made) {
+        for (auto& e : w->ev) CU(cudaEventCreate(&e));
+        w->events_made = true;
+    }
+    dg::Ctx x = make_ctx(w, dt, velocity_iterations, position_iterations);
+    CU(cudaEventRecord(w->ev[0], w->stream));
+    int launches = 0;
+    int err = dbox_launch_step(&x, w->stream, &launches);
+    if (err) return fail(DBOX_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString((cudaError_t)err));
+    CU(cudaEventRecord(w->ev[1], w->stream));
+    rc = check_status(w);
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, w->ev[0], w->ev[1]);
+    memset(&w->profile, 0, sizeof(w->profile));
+    w->profile.step = ms;
+    w->last_launches = launches;
+    return rc;
+}
+
+int32_t dbox_world_step_n(dbox_world* w, float dt, int32_t velocity_iterations, int32_t position_iterations,
+                          int32_t steps) {
+    if (!w || steps < 0 || velocity_iterations < 0 || position_iterations < 0)
+        return fail(DBOX_ERR_INVALID, "dbox_world_step_n: bad arguments");
+    int rc = ensure_device(w);
+    if (rc) return rc;
+    int flags = w->warm | (w->continuous << 1) | (w->substep << 2) | (w->allow_sleep << 3) | (w->autoclear << 4);
+    if (!w->graph || w->g_dt != dt || w->g_vi != velocity_iterations || w->g_pi != position_iterations ||
+        w->graph_flags != flags) {
+        if (w->graph) { cudaGraphExecDestroy(w->graph); w->graph = nullptr; }
+        dg::Ctx x = make_ctx(w, dt, velocity_iterations, position_iterations);
+        cudaGraph_t g;
+        CU(cudaStreamBeginCapture(w->stream, cudaStreamCaptureModeThreadLocal));
+        int launches = 0;
+        int err = dbox_launch_step(&x, w->stream, &launches);
+        cudaError_t ce = cudaStreamEndCapture(w->stream, &g);
+        if (err || ce != cudaSuccess) return fail(DBOX_ERR_CUDA, "graph capture failed");
+        CU(cudaGraphInstantiate(&w->graph, g, 0));
+        cudaGraphDestroy(g);
+        w->g_dt = dt; w->g_vi = velocity_iterations; w->g_pi = position_iterations; w->graph_flags = flags;
+        w->last_launches = launches;
+    }
+    for (int i = 0; i < steps; ++i) CU(cudaGraphLaunch(w->graph, w->stream));
+    return check_status(w);
+}
+
+int32_t dbox_world_step_n_timed(dbox_world* w, float dt, int32_t velocity_iterations, int32_t position_iterations,
+                                int32_t steps, float* total_ms, float* phase_ms) {
+    if (!w || steps < 1 || velocity_iterations < 0 || position_iterations < 0)
+        return fail(DBOX_ERR_INVALID, "dbox_world_step_n_timed: bad arguments");
+    int rc = ensure_device(w);
+    if (rc) return rc;
+    int flags = w->warm | (w->continuous << 1) | (w->substep << 2) | (w->allow_sleep << 3) | (w->autoclear << 4);
+    if (!w->tgraph || w->t_steps != steps || w->t_dt != dt || w->t_vi != velocity_iterations ||
+        w->t_pi != position_iterations || w->t_flags != flags) {
+        if (w->tgraph) { cudaGraphExecDestroy(w->tgraph); w->tgraph = nullptr; }
+        for (auto& e : w->tev) cudaEventDestroy(e);
+        w->tev.assign(4 * (size_t)steps, nullptr);
+        for (auto& e : w->tev) CU(cudaEventCreate(&e));
+        dg::Ctx x = make_ctx(w, dt, velocity_iterations, position_iterations);
+        cudaGraph_t g;
+        CU(cudaStreamBeginCapture(w->stream, cudaStreamCaptureModeThreadLocal));
+        int launches = 0, err = 0;
+        for (int i = 0; i < steps && !err; ++i) err = dbox_launch_step_ev(&x, w->stream, &launches, &w->tev[4 * i]);
+        cudaError_t ce = cudaStreamEndCapture(w->stream, &g);
+        if (err || ce != cudaSuccess) return fail(DBOX_ERR_CUDA, "timed graph capture failed");
+        CU(cudaGraphInstantiate(&w->tgraph, g, 0));
+        cudaGraphDestroy(g);
+        w->t_steps = steps; w->t_dt = dt; w->t_vi = velocity_iterations; w->t_pi = position_iterations;
+        w->t_flags = flags;
+        w->last_launches = launches;
+    }
+    CU(cudaGraphLaunch(w->tgraph, w->stream));
+    rc = check_status(w);
+    float tot = 0.0f, ph[3] = {0.0f, 0.0f, 0.0f};
+    CU(cudaEventElapsedTime(&tot, w->tev[0], w->tev[4 * (size_t)steps - 1]));
+    for (int i = 0; i < steps; ++i)
+        for (int p = 0; p < 3; ++p) {
+            float ms = 0.0f;
+            CU(cudaEventElapsedTime(&ms, w->tev[4 * i + p], w->tev[4 * i + p + 1]));
+            ph[p] += ms;
+        }
+    if (total_ms) *total_ms = tot;
+    if (phase_ms) { phase_ms[0] = ph[0]; phase_ms[1] = ph[1]; phase_ms[2] = ph[2]; }
+    memset(&w->profile, 0, sizeof(w->profile));
+    w->profile.step = tot / steps;
+    w->profile.collide = ph[0] / steps;
+    w->profile.solve = ph[1] / steps;
+    w->profile.solve_toi = ph[2] / steps;
+    return rc;
+}
+
+int32_t dbox_world_get_counters(dbox_world* w, unsigned long long* out) {
+    if (!w || !out) return DBOX_ERR_INVALID;
+    memset(out, 0, sizeof(unsigned long long) * 8);
+    if (!w->on_device) return DBOX_OK;
+    int W = (int)w->worlds.size();
+    std::vector<dg::WorldDyn> wd(W);
+    CU(cudaStreamSynchronize(w->stream));
+    CU(cudaMemcpy(wd.data(), w->d_wd.p, sizeof(dg::WorldDyn) * W, cudaMemcpyDeviceToHost));
+    for (auto& d : wd) {
+        out[0] += d.acc_isl_bodies; out[1] += d.acc_isl_contacts; out[2] += d.acc_vsolve; out[3] += d.acc_psolve;
+        out[4] += d.acc_contacts; out[5] += d.acc_toi_events; out[6] += d.acc_steps; out[7] += d.acc_pairs;
+    }
+    return DBOX_OK;
+}
+
+int32_t dbox_world_apply_forces(dbox_world* w, const float* force_torque) {
+    if (!w || !force_torque) return fail(DBOX_ERR_INVALID, "dbox_world_apply_forces: bad arguments");
+    int rc = ensure_device(w);
+    if (rc) return rc;
+    int n = w->total_bodies;
+    if (n == 0) return DBOX_OK;
+    CU(cudaMemcpyAsync(w->d_io.p, force_torque, sizeof(float) * 3 * (size_t)n, cudaMemcpyHostToDevice, w->stream));
+    int err = dbox_launch_apply_forces(n, w->d_bs.p, w->d_io.p, w->stream);
+    if (err) return fail(DBOX_ERR_CUDA, "apply forces launch: %s", cudaGetErrorString((cudaError_t)err));
+    return DBOX_OK;
+}
+
+int32_t dbox_world_get_transforms(dbox_world* w, float* xya) {
+    if (!w || !xya) return fail(DBOX_ERR_INVALID, "dbox_world_get_transforms: bad arguments");
+    int rc = ensure_device(w);
+    if (rc) return rc;
+    int n = w->total_bodies;
+    if (n == 0) return DBOX_OK;
+    int err = dbox_launch_gather_transforms(n, w->d_bs.p, w->d_io.p, w->stream);
+    if (err) return fail(DBOX_ERR_CUDA, "gather launch: %s", cudaGetErrorString((cudaError_t)err));
+    CU(cudaMemcpyAsync(xya, w->d_io.p, sizeof(float) * 3 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    return DBOX_OK;
+}
+
+int32_t dbox_world_sync(dbox_world* w) {
+    if (!w) return DBOX_ERR_INVALID;
+    CU(cudaStreamSynchronize(w->stream));
+    return DBOX_OK;
+}
+
+int32_t dbox_world_get_bodies(dbox_world* w, dbox_vec2* position, float* angle, dbox_vec2* linear_velocity,
+                              float* angular_velocity, int32_t* awake) {
+    if (!w) return DBOX_ERR_INVALID;
+    std::vector<dbox_body_state> all;
+    if (w->on_device && !w->dirty) {
+        all.resize(w->total_bodies);
+        CU(cudaStreamSynchronize(w->stream));
+        if (w->total_bodies)
+            CU(cudaMemcpy(all.data(), w->d_bs.p, sizeof(dbox_body_state) * all.size(), cudaMemcpyDeviceToHost));
+    } else {
+        for (auto& hw : w->worlds) all.insert(all.end(), hw.bs.begin(), hw.bs.end());
+    }
+    for (size_t i = 0; i < all.size(); ++i) {
+        const dbox_body_state& b = all[i];
+        if (position) { position[i].x = b.xf[0]; position[i].y = b.xf[1]; }
+        if (angle) angle[i] = b.sweep[7];
+        if (linear_velocity) { linear_velocity[i].x = b.vel[0]; linear_velocity[i].y = b.vel[1]; }
+        if (angular_velocity) angular_velocity[i] = b.vel[2];
+        if (awake) awake[i] = (b.flags & dg::kBodyAwake) ? 1 : 0;
+    }
+    return DBOX_OK;
+}
+
+int32_t dbox_world_body_count(dbox_world* w, int32_t world, int32_t* out) {
+    if (!w || !out || world < 0 || world >= (int)w->worlds.size()) return DBOX_ERR_INVALID;
+    *out = (int)w->worlds[world].bs.size();
+    return DBOX_OK;
+}
+
+int32_t dbox_world_contact_count(dbox_world* w, int32_t world, int32_t* out) {
+    if (!w || !out || world < 0 || world >= (int)w->worlds.size()) return DBOX_ERR_INVALID;
+    if (w->on_device && !w->dirty) {
+        dg::WorldDyn wd;
+        CU(cudaStreamSynchronize(w->stream));
+        CU(cudaMemcpy(&wd, w->d_wd.p + world, sizeof(wd), cudaMemcpyDeviceToHost));
+        *out = wd.contact_count;
+    } else {
+        *out = (int)w->worlds[world].ct.size();
+    }
+    return DBOX_OK;
+}
+
+int32_t dbox_world_export_state(dbox_world* w, int32_t world, dbox_world_header* header, dbox_body_state* bodies,
+                                dbox_proxy_state* proxies, dbox_contact_state* contacts, dbox_joint_state* joints) {
+    if (!w || world < 0 || world >= (int)w->worlds.size()) return fail(DBOX_ERR_INVALID, "export: bad world");
+    int rc = download(w);      // the device copy stays valid; only the mirrors refresh
+    if (rc) return rc;
+    if (!w->dirty && w->total_bodies + w->total_fixtures > 0) w->on_device = true;
+    const HostWorld& hw = w->worlds[world];
+    if (header) {
+        header->body_count = (int)hw.bs.size();
+        header->fixture_count = (int)hw.fx.size();
+        header->contact_count = (int)hw.ct.size();
+        header->joint_count = (int)hw.jt.size();
+        header->world_flags = (hw.wd.flags & ~4u) | (w->autoclear ? 4u : 0u);
+        header->step_complete = hw.wd.step_complete;
+        header->inv_dt0 = hw.wd.inv_dt0;
+        header->reserved = 0;
+    }
+    if (bodies && !hw.bs.empty()) memcpy(bodies, hw.bs.data(), sizeof(dbox_body_state) * hw.bs.size());
+    if (proxies && !hw.px.empty()) memcpy(proxies, hw.px.data(), sizeof(dbox_proxy_state) * hw.px.size());
+    if (contacts) {
+        for (size_t k = 0; k < hw.ct.size(); ++k) {
+            dbox_contact_state c = hw.ct[k];
+            for (int p = c.point_count; p < 2; ++p) memset(&c.points[p], 0, sizeof(c.points[p]));
+            contacts[k] = c;
+        }
+    }
+    if (joints) {
+        for (size_t j = 0; j < hw.jt.size(); ++j) {
+            joints[j].impulse[0] = hw.jt[j].impulse[0];
+            joints[j].impulse[1] = hw.jt[j].impulse[1];
+            joints[j].impulse[2] = hw.jt[j].impulse[2];
+            joints[j].motor_impulse = hw.jt[j].motor_impulse;
+            joints[j].limit_state = hw.jt[j].limit_state;
+        }
+    }
+    return DBOX_OK;
+}
+
+int32_t dbox_world_import_state(dbox_world* w, int32_t world, const dbox_world_header* header,
+                                const dbox_body_state* bodies, const dbox_proxy_state* proxies,
+                                const dbox_contact_state* contacts, const dbox_joint_state* joints) {
+    if (!w || !header || world < 0 || world >= (int)w->worlds.size()) return fail(DBOX_ERR_INVALID, "import: bad world");
+    int rc = prepare_edit(w);
+    if (rc) return rc;
+    HostWorld& hw = w->worlds[world];
+    if (header->body_count != (int)hw.bs.size() || header->fixture_count != (int)hw.fx.size() ||
+        header->joint_count != (int)hw.jt.size())
+        return fail(DBOX_ERR_INVALID, "import: world structure differs from the snapshot");
+    if (header->body_count && !bodies) return fail(DBOX_ERR_INVALID, "import: bodies missing");
+    if (header->fixture_count && !proxies) return fail(DBOX_ERR_INVALID, "import: proxies missing");
+    if (header->contact_count && !contacts) return fail(DBOX_ERR_INVALID, "import: contacts missing");
+    if (!hw.bs.empty()) memcpy(hw.bs.data(), bodies, sizeof(dbox_body_state) * hw.bs.size());
+    if (!hw.px.empty()) memcpy(hw.px.data(), proxies, sizeof(dbox_proxy_state) * hw.px.size());
+    hw.ct.assign(contacts, contacts + header->contact_count);
+    for (auto& c : hw.ct) {
+        if (c.fixture_a < 0 || c.fixture_a >= (int)hw.fx.size() || c.fixture_b < 0 || c.fixture_b >= (int)hw.fx.size())
+            return fail(DBOX_ERR_INVALID, "import: contact fixture out of range");
+    }
+    if (joints) {
+        for (size_t j = 0; j < hw.jt.size(); ++j) {
+            hw.jt[j].impulse[0] = joints[j].impulse[0];
+            hw.jt[j].impulse[1] = joints[j].impulse[1];
+            hw.jt[j].impulse[2] = joints[j].impulse[2];
+            hw.jt[j].motor_impulse = joints[j].motor_impulse;
+            hw.jt[j].limit_state = joints[j].limit_state;
+        }
+    }
+    hw.wd.flags = header->world_flags & ~2u;
+    hw.wd.step_complete = header->step_complete;
+    hw.wd.inv_dt0 = header->inv_dt0;
+    hw.wd.contact_count = header->contact_count;
+    return DBOX_OK;
+}
+
+int32_t dbox_world_get_profile(dbox_world* w, dbox_profile* out) {
+    if (!w || !out) return DBOX_ERR_INVALID;
+    *out = w->profile;
+    return DBOX_OK;
+}
+
+int32_t dbox_world_last_launches(dbox_world* w, int32_t* out) {
+    if (!w || !out) return DBOX_ERR_INVALID;
+    *out = w->last_launches;
+    return DBOX_OK;
+}
+
+// Batched narrowphase (b2CollidePolygons / b2CollidePolygonAndCircle / b2CollideCircles,
+// collision/b2collidepolygon.d:127-254, b2collidecircle.d:29-164) on the GPU.
+int32_t dbox_collide_manifolds(int32_t n, const dbox_shape_def* shape_a, const float* xf_a,
+                               const dbox_shape_def* shape_b, const float* xf_b, dbox_contact_state* out) {
+    if (n < 0 || (n > 0 && (!shape_a || !xf_a || !shape_b || !xf_b || !out)))
+        return fail(DBOX_ERR_INVALID, "dbox_collide_manifolds: bad arguments");
+    if (n == 0) return DBOX_OK;
+    std::vector<dg::DFixture> fa(n), fb(n);
+    for (int i = 0; i < n; ++i) {
+        if (!build_fixture(shape_a + i, &fa[i]) || !build_fixture(shape_b + i, &fb[i]))
+            return fail(DBOX_ERR_INVALID, "dbox_collide_manifolds: pair %d has a degenerate shape", i);
+        if (fa[i].type == dg::kShapeCircle && fb[i].type == dg::kShapePolygon)
+            return fail(DBOX_ERR_INVALID, "dbox_collide_manifolds: pair %d: polygon must come first", i);
+    }
+    std::vector<dbox_contact_state> init(n);
+    memset(init.data(), 0, sizeof(dbox_contact_state) * n);
+    DBuf<dg::DFixture> dfa, dfb;
+    DBuf<float4> dxa, dxb;
+    DBuf<dbox_contact_state> dout;
+    if (dfa.alloc(n) || dfb.alloc(n) || dxa.alloc(n) || dxb.alloc(n) || dout.alloc(n)) {
+        dfa.free(); dfb.free(); dxa.free(); dxb.free(); dout.free();
+        return fail(DBOX_ERR_CUDA, "dbox_collide_manifolds: allocation failed");
+    }
+    int rc = DBOX_OK;
+    if (cudaMemcpy(dfa.p, fa.data(), sizeof(dg::DFixture) * n, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(dfb.p, fb.data(), sizeof(dg::DFixture) * n, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(dxa.p, xf_a, sizeof(float4) * n, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(dxb.p, xf_b, sizeof(float4) * n, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(dout.p, init.data(), sizeof(dbox_contact_state) * n, cudaMemcpyHostToDevice) != cudaSuccess ||
+        dbox_launch_collide_pairs(n, dfa.p, dxa.p, dfb.p, dxb.p, dout.p, 0) != 0 ||
+        cudaMemcpy(out, dout.p, sizeof(dbox_contact_state) * n, cudaMemcpyDeviceToHost) != cudaSuccess)
+        rc = fail(DBOX_ERR_CUDA, "dbox_collide_manifolds: %s", cudaGetErrorString(cudaGetLastError()));
+    dfa.free(); dfb.free(); dxa.free(); dxb.free(); dout.free();
+    return rc;
+}
+
+// per-world step diagnostics: islands and TOI events of the last step
+int32_t dbox_world_step_stats(dbox_world* w, int32_t world, int32_t* islands, int32_t* toi_events) {
+    if (!w || world < 0 || world >= (int)w->worlds.size()) return DBOX_ERR_INVALID;
+    if (!w->on_device) { if (islands) *islands = 0; if (toi_events) *toi_events = 0; return DBOX_OK; }
+    dg::WorldDyn wd;
+    CU(cudaStreamSynchronize(w->stream));
+    CU(cudaMemcpy(&wd, w->d_wd.p + world, sizeof(wd), cudaMemcpyDeviceToHost));
+    if (islands) *islands = wd.islands;
+    if (toi_events) *toi_events = wd.toi_events;
+    return DBOX_OK;
+}
+
+}  // extern "C"

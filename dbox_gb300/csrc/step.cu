@@ -1,0 +1,1728 @@
+// b2World.Step on the GPU: one team (a warp) per world for the ordered phases,
+// flat grids for the per-contact narrowphase.
+//
+// Phase map (reference dbox src/dbox/dynamics/b2world.d:367-434):
+//   k_step_begin      FindNewContacts when fixtures were added (b2world.d:372-376)
+//   k_collide         b2ContactManager.Collide per contact (b2contactmanager.d:251-317)
+//   k_collide_finish  contacts woken later in list order, wake flags, stable compaction
+//   k_solve           b2World.Solve: island DFS (b2world.d:930-1095), b2Island.Solve
+//                     (b2island.d:75-280) for all islands at once in reference
+//                     constraint order, SynchronizeFixtures, FindNewContacts
+//   k_toi             b2World.SolveTOI (b2world.d:1127-1452), inv_dt0, ClearForces
+//
+// Gauss-Seidel order: inside an island every constraint reads the velocities
+// (positions) its predecessors in island order wrote.  The kernels assign each
+// constraint the level 1 + max(level of the last earlier constraint on either of
+// its dynamic bodies) and run levels in sequence with the constraints of one
+// level in parallel; constraints of one level share no dynamic body, so every
+// constraint reads exactly the values it would read in sequential order.
+// Static and kinematic bodies are never written by the solver (zero inverse
+// mass), so they create no ordering edges.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "world.cuh"
+
+namespace dg {
+
+constexpr int kWarp = 32;
+constexpr int kMaxToiLoop = 100000;   // bound on TOI events per world per step
+constexpr int kNoWake = 0x7fffffff;
+constexpr unsigned long long kHashEmpty = 0xffffffffffffffffull;
+
+DG int lane_id() { return threadIdx.x & 31; }
+DG void tsync() { __syncwarp(); }
+
+// ------------------------------------------------------------ contact pair hash (existence test of AddPair)
+DG unsigned long long pair_key(int fa, int fb) {
+    int lo = fa < fb ? fa : fb, hi = fa < fb ? fb : fa;
+    return ((unsigned long long)(unsigned)lo << 32) | (unsigned)hi;
+}
+DG unsigned hash_slot(unsigned long long k, int cap) {
+    k ^= k >> 33; k *= 0xff51afd7ed558ccdull; k ^= k >> 33; k *= 0xc4ceb9fe1a85ec53ull; k ^= k >> 33;
+    return (unsigned)(k & (unsigned long long)(cap - 1));
+}
+DG void hash_insert(const Ctx& x, const WorldInfo& wi, unsigned long long key) {
+    unsigned h = hash_slot(key, wi.hash_cap);
+    for (int probe = 0; probe < wi.hash_cap; ++probe) {
+        unsigned long long* slot = x.hash + wi.hash_start + ((h + probe) & (wi.hash_cap - 1));
+        unsigned long long prev = atomicCAS(slot, kHashEmpty, key);
+        if (prev == kHashEmpty || prev == key) return;
+    }
+}
+DG bool hash_contains(const Ctx& x, const WorldInfo& wi, unsigned long long key) {
+    unsigned h = hash_slot(key, wi.hash_cap);
+    for (int probe = 0; probe < wi.hash_cap; ++probe) {
+        unsigned long long v = x.hash[wi.hash_start + ((h + probe) & (wi.hash_cap - 1))];
+        if (v == key) return true;
+        if (v == kHashEmpty) return false;
+    }
+    return false;
+}
+// rebuild the table of world w from its live contacts
+DG void hash_rebuild(const Ctx& x, int w) {
+    const WorldInfo& wi = x.wi[w];
+    int lane = lane_id();
+    for (int i = lane; i < wi.hash_cap; i += kWarp) x.hash[wi.hash_start + i] = kHashEmpty;
+    tsync();
+    int n = x.wd[w].contact_count;
+    for (int k = lane; k < n; k += kWarp) {
+        const dbox_contact_state& c = x.ct[wi.contact_start + k];
+        hash_insert(x, wi, pair_key(c.fixture_a, c.fixture_b));
+    }
+    tsync();
+}
+
+// ------------------------------------------------------------ filters
+// b2Body.ShouldCollide (b2body.d:1149-1170): called as bodyB.ShouldCollide(bodyA)
+DG bool body_should_collide(const Ctx& x, int self, int other) {
+    if (x.bs[self].type != kDynamicBody && x.bs[other].type != kDynamicBody) return false;
+    const BodyStatic& s = x.bst[self];
+    for (int e = 0; e < s.jadj_count; ++e) {
+        if (x.jadj_other[s.jadj_start + e] == other) {
+            if (x.jt[x.jadj_joint[s.jadj_start + e]].collide_connected == 0) return false;
+        }
+    }
+    return true;
+}
+// b2ContactFilter.ShouldCollide (b2worldcallbacks.d:52-64)
+DG bool filter_should_collide(const DFixture& a, const DFixture& b) {
+    if (a.group == b.group && a.group != 0) return a.group > 0;
+    uint32_t catA = a.filter & 0xffffu, maskA = a.filter >> 16;
+    uint32_t catB = b.filter & 0xffffu, maskB = b.filter >> 16;
+    return (maskA & catB) != 0 && (catA & maskB) != 0;
+}
+
+// ------------------------------------------------------------ b2Contact.Update (contacts/b2contact.d:270-356)
+// Returns true when the touching state changed (the caller wakes both bodies).
+DG bool contact_update(const Ctx& x, dbox_contact_state& c) {
+    Manifold m;
+    manifold_load(c, m);
+    Manifold old = m;
+    c.flags |= kContactEnabled;
+    bool wasTouching = (c.flags & kContactTouching) != 0;
+    const DFixture& fa = x.fx[c.fixture_a];
+    const DFixture& fb = x.fx[c.fixture_b];
+    bool sensor = fa.sensor || fb.sensor;
+    Xf xfA = b_xf(x.bs[fa.body]);
+    Xf xfB = b_xf(x.bs[fb.body]);
+    bool touching;
+    bool changed = false;
+    if (sensor) {
+        touching = shapes_overlap(fa, xfA, fb, xfB);
+        m.pointCount = 0;
+    } else {
+        evaluate_manifold(m, fa, xfA, fb, xfB);
+        touching = m.pointCount > 0;
+        for (int i = 0; i < m.pointCount; ++i) {
+            m.ni[i] = 0.0f;
+            m.ti[i] = 0.0f;
+            for (int j = 0; j < old.pointCount; ++j) {
+                if (old.id[j] == m.id[i]) { m.ni[i] = old.ni[j]; m.ti[i] = old.ti[j]; break; }
+            }
+        }
+        changed = touching != wasTouching;
+    }
+    if (touching) c.flags |= kContactTouching; else c.flags &= ~(uint32_t)kContactTouching;
+    manifold_store(m, c);
+    return changed;
+}
+
+// Collide treatment of one contact at list position lp: 0 = updated, 2 = destroyed.
+// Wakes are recorded into s_woken (minimum list position) instead of the flags.
+DG int collide_one(const Ctx& x, dbox_contact_state& c, int lp, bool use_atomic) {
+    const DFixture& fa = x.fx[c.fixture_a];
+    const DFixture& fb = x.fx[c.fixture_b];
+    int A = fa.body, B = fb.body;
+    AABB pa, pb;
+    const dbox_proxy_state& qa = x.px[c.fixture_a];
+    const dbox_proxy_state& qb = x.px[c.fixture_b];
+    pa.lo = v2(qa.fat_aabb[0], qa.fat_aabb[1]); pa.hi = v2(qa.fat_aabb[2], qa.fat_aabb[3]);
+    pb.lo = v2(qb.fat_aabb[0], qb.fat_aabb[1]); pb.hi = v2(qb.fat_aabb[2], qb.fat_aabb[3]);
+    bool wake;
+    int result;
+    if (!aabb_overlap(pa, pb)) {
+        // b2ContactManager.Destroy + b2Contact.Destroy (b2contactmanager.d:183-246, b2contact.d:402-422)
+        wake = c.point_count > 0 && !fa.sensor && !fb.sensor;
+        result = 2;
+    } else {
+        wake = contact_update(x, c);
+        result = 0;
+    }
+    if (wake) {
+        if (use_atomic) { atomicMin(&x.s_woken[A], lp); atomicMin(&x.s_woken[B], lp); }
+        else {
+            if (x.s_woken[A] > lp) x.s_woken[A] = lp;
+            if (x.s_woken[B] > lp) x.s_woken[B] = lp;
+        }
+    }
+    return result;
+}
+
+// ------------------------------------------------------------ broad-phase: FindNewContacts
+// b2BroadPhase.UpdatePairs (b2broadphase.d:139-195) + b2ContactManager.AddPair (b2contactmanager.d:52-176).
+// Pairs are produced directly in (idA, idB) order: for each proxy a in ascending
+// id, its partners b > a with a or b in the move buffer; duplicates never arise.
+DG AABB proxy_fat(const Ctx& x, int f) {
+    const dbox_proxy_state& p = x.px[f];
+    AABB a;
+    a.lo = v2(p.fat_aabb[0], p.fat_aabb[1]);
+    a.hi = v2(p.fat_aabb[2], p.fat_aabb[3]);
+    return a;
+}
+
+DG void find_new_contacts(const Ctx& x, int w) {
+    const WorldInfo& wi = x.wi[w];
+    WorldDyn& wd = x.wd[w];
+    int lane = lane_id();
+    int f0 = wi.fix_start, nf = wi.fix_count;
+    // moved list, ascending
+    int nm = 0;
+    for (int base = 0; base < nf; base += kWarp) {
+        int i = base + lane;
+        bool mv = i < nf && x.px[f0 + i].moved && x.px[f0 + i].proxy_id >= 0;
+        unsigned bal = __ballot_sync(0xffffffffu, mv);
+        if (mv) x.s_moved[f0 + nm + __popc(bal & ((1u << lane) - 1))] = i;
+        nm += __popc(bal);
+    }
+    tsync();
+    if (nm == 0) return;
+    // count pairs per proxy a
+    for (int a = lane; a < nf; a += kWarp) {
+        int cnt = 0;
+        if (x.px[f0 + a].proxy_id >= 0) {
+            AABB fa = proxy_fat(x, f0 + a);
+            if (x.px[f0 + a].moved) {
+                for (int b = a + 1; b < nf; ++b)
+                    if (x.px[f0 + b].proxy_id >= 0 && aabb_overlap(fa, proxy_fat(x, f0 + b))) ++cnt;
+            } else {
+                for (int m = 0; m < nm; ++m) {
+                    int b = x.s_moved[f0 + m];
+                    if (b > a && aabb_overlap(fa, proxy_fat(x, f0 + b))) ++cnt;
+                }
+            }
+        }
+        x.s_pcount[f0 + a] = cnt;
+    }
+    tsync();
+    // exclusive scan of counts (warp, chunked)
+    int total = 0;
+    for (int base = 0; base < nf; base += kWarp) {
+        int i = base + lane;
+        int v = i < nf ? x.s_pcount[f0 + i] : 0;
+        int incl = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            int t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        if (i < nf) x.s_pcount[f0 + i] = total + incl - v;
+        total += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    tsync();
+    if (total > wi.pair_cap) {
+        if (lane == 0) set_error(x, w, DBOX_ERR_CAPACITY);
+        return;
+    }
+    if (lane == 0) wd.acc_pairs += (unsigned long long)total;
+    // fill pairs in (a, b) order
+    for (int a = lane; a < nf; a += kWarp) {
+        int o = x.s_pcount[f0 + a];
+        if (x.px[f0 + a].proxy_id < 0) continue;
+        AABB fa = proxy_fat(x, f0 + a);
+        if (x.px[f0 + a].moved) {
+            for (int b = a + 1; b < nf; ++b)
+                if (x.px[f0 + b].proxy_id >= 0 && aabb_overlap(fa, proxy_fat(x, f0 + b)))
+                    x.pairs[wi.pair_start + o++] = make_int2(f0 + a, f0 + b);
+        } else {
+            for (int m = 0; m < nm; ++m) {
+                int b = x.s_moved[f0 + m];
+                if (b > a && aabb_overlap(fa, proxy_fat(x, f0 + b)))
+                    x.pairs[wi.pair_start + o++] = make_int2(f0 + a, f0 + b);
+            }
+        }
+    }
+    tsync();
+    // clear the move buffer
+    for (int i = lane; i < nf; i += kWarp) x.px[f0 + i].moved = 0;
+    // AddPair, in pair order
+    int n = wd.contact_count;
+    int added = 0;
+    for (int base = 0; base < total; base += kWarp) {
+        int i = base + lane;
+        bool acc = false;
+        int2 pr = make_int2(0, 0);
+        if (i < total) {
+            pr = x.pairs[wi.pair_start + i];
+            const DFixture& fA = x.fx[pr.x];
+            const DFixture& fB = x.fx[pr.y];
+            acc = fA.body != fB.body;
+            if (acc) acc = !hash_contains(x, wi, pair_key(pr.x, pr.y));
+            if (acc) acc = body_should_collide(x, fB.body, fA.body);
+            if (acc) acc = filter_should_collide(fA, fB);
+        }
+        unsigned bal = __ballot_sync(0xffffffffu, acc);
+        if (acc) {
+            int slot = n + added + __popc(bal & ((1u << lane) - 1));
+            if (slot < wi.contact_cap) {
+                // b2Contact.Create: the registry's primary order puts the polygon first (b2contact.d:375-400)
+                int fa = pr.x, fb = pr.y;
+                if (x.fx[fa].type == kShapeCircle && x.fx[fb].type == kShapePolygon) { int t = fa; fa = fb; fb = t; }
+                const DFixture& FA = x.fx[fa];
+                const DFixture& FB = x.fx[fb];
+                dbox_contact_state& c = x.ct[wi.contact_start + slot];
+                c.fixture_a = fa;
+                c.fixture_b = fb;
+                c.flags = kContactEnabled;
+                c.toi_count = 0;
+                c.toi = 0.0f;
+                c.friction = fsqrt(FA.friction * FB.friction);                       // b2MixFriction
+                c.restitution = FA.restitution > FB.restitution ? FA.restitution : FB.restitution;
+                c.tangent_speed = 0.0f;
+                c.point_count = 0;
+                c.type = 0;
+                c.local_normal[0] = c.local_normal[1] = 0.0f;
+                c.local_point[0] = c.local_point[1] = 0.0f;
+                for (int k = 0; k < 2; ++k) {
+                    c.points[k].local_point[0] = c.points[k].local_point[1] = 0.0f;
+                    c.points[k].normal_impulse = c.points[k].tangent_impulse = 0.0f;
+                    c.points[k].id = 0;
+                }
+                hash_insert(x, wi, pair_key(fa, fb));
+                if (!FA.sensor && !FB.sensor) {
+                    // SetAwake(true) on both bodies; concurrent writers store identical values
+                    dbox_body_state& ba = x.bs[FA.body];
+                    dbox_body_state& bb = x.bs[FB.body];
+                    if ((ba.flags & kBodyAwake) == 0) { atomicOr(&ba.flags, (unsigned)kBodyAwake); ba.sleep_time = 0.0f; }
+                    if ((bb.flags & kBodyAwake) == 0) { atomicOr(&bb.flags, (unsigned)kBodyAwake); bb.sleep_time = 0.0f; }
+                }
+            }
+        }
+        added += __popc(bal);
+        tsync();
+    }
+    if (n + added > wi.contact_cap) {
+        if (lane == 0) set_error(x, w, DBOX_ERR_CAPACITY);
+        added = wi.contact_cap - n;
+    }
+    tsync();
+    if (lane == 0) wd.contact_count = n + added;
+    tsync();
+}
+
+// ------------------------------------------------------------ kernels
+__global__ void k_step_begin(Ctx x) {
+    int w = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+    if (w >= x.W) return;
+    WorldDyn& wd = x.wd[w];
+    const WorldInfo& wi = x.wi[w];
+    int lane = lane_id();
+    if (lane == 0) { wd.error = 0; wd.islands = 0; wd.toi_events = 0; }
+    for (int i = lane; i < wi.body_count; i += kWarp) x.s_woken[wi.body_start + i] = kNoWake;
+    tsync();
+    if (wd.flags & 1u) {                                                // e_newFixture
+        hash_rebuild(x, w);
+        find_new_contacts(x, w);
+        if (lane == 0) wd.flags &= ~1u;
+    }
+}
+
+__global__ void k_collide(Ctx x) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < x.total_contacts; i += gridDim.x * blockDim.x) {
+        int w = x.c_world[i];
+        const WorldInfo& wi = x.wi[w];
+        int k = i - wi.contact_start;
+        int n = x.wd[w].contact_count;
+        if (k >= n) continue;
+        int lp = n - 1 - k;
+        dbox_contact_state c = x.ct[i];
+        const DFixture& fa = x.fx[c.fixture_a];
+        const DFixture& fb = x.fx[c.fixture_b];
+        int A = fa.body, B = fb.body;
+        int state = 0;
+        if (c.flags & kContactFilter) {                                // b2contactmanager.d:266-288
+            if (!body_should_collide(x, B, A) || !filter_should_collide(fa, fb)) {
+                state = 2;
+                if (c.point_count > 0 && !fa.sensor && !fb.sensor) {
+                    atomicMin(&x.s_woken[A], lp);
+                    atomicMin(&x.s_woken[B], lp);
+                }
+            } else {
+                c.flags &= ~(uint32_t)kContactFilter;
+            }
+        }
+        if (state == 0) {
+            const dbox_body_state& ba = x.bs[A];
+            const dbox_body_state& bb = x.bs[B];
+            bool activeA = (ba.flags & kBodyAwake) && ba.type != kStaticBody;
+            bool activeB = (bb.flags & kBodyAwake) && bb.type != kStaticBody;
+            if (!activeA && !activeB) state = 1;
+            else state = collide_one(x, c, lp, true);
+        }
+        x.s_cstate[i] = state;
+        if (state != 2) x.ct[i] = c;
+    }
+}
+
+// Contacts skipped as inactive may become active when an earlier contact in list
+// order woke one of their bodies (Collide walks the list and wakes as it goes).
+__global__ void k_collide_finish(Ctx x) {
+    int w = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+    if (w >= x.W) return;
+    const WorldInfo& wi = x.wi[w];
+    WorldDyn& wd = x.wd[w];
+    int lane = lane_id();
+    int n = wd.contact_count;
+    int c0 = wi.contact_start;
+    // any inactive contact with a body woken during this Collide?
+    bool need = false;
+    for (int k = lane; k < n; k += kWarp) {
+        if (x.s_cstate[c0 + k] == 1) {
+            const dbox_contact_state& c = x.ct[c0 + k];
+            int A = x.fx[c.fixture_a].body, B = x.fx[c.fixture_b].body;
+            if (x.s_woken[A] != kNoWake || x.s_woken[B] != kNoWake) need = true;
+        }
+    }
+    need = __any_sync(0xffffffffu, need);
+    if (need && lane == 0) {
+        for (int k = n - 1; k >= 0; --k) {
+            if (x.s_cstate[c0 + k] != 1) continue;
+            int lp = n - 1 - k;
+            dbox_contact_state& c = x.ct[c0 + k];
+            int A = x.fx[c.fixture_a].body, B = x.fx[c.fixture_b].body;
+            const dbox_body_state& ba = x.bs[A];
+            const dbox_body_state& bb = x.bs[B];
+            bool awA = (ba.flags & kBodyAwake) || x.s_woken[A] < lp;
+            bool awB = (bb.flags & kBodyAwake) || x.s_woken[B] < lp;
+            bool activeA = awA && ba.type != kStaticBody;
+            bool activeB = awB && bb.type != kStaticBody;
+            if (!activeA && !activeB) continue;
+            x.s_cstate[c0 + k] = collide_one(x, c, lp, false);
+        }
+    }
+    tsync();
+    // apply wakes
+    for (int i = lane; i < wi.body_count; i += kWarp) {
+        int b = wi.body_start + i;
+        if (x.s_woken[b] != kNoWake) b_set_awake(x.bs[b], true);
+    }
+    // stable compaction of surviving contacts
+    int out = 0;
+    for (int base = 0; base < n; base += kWarp) {
+        int k = base + lane;
+        bool keep = k < n && x.s_cstate[c0 + k] != 2;
+        dbox_contact_state c;
+        if (keep) c = x.ct[c0 + k];
+        unsigned bal = __ballot_sync(0xffffffffu, keep);
+        tsync();
+        if (keep) x.ct[c0 + out + __popc(bal & ((1u << lane) - 1))] = c;
+        out += __popc(bal);
+        tsync();
+    }
+    if (lane == 0) { wd.contact_count = out; wd.acc_contacts += (unsigned long long)n; wd.acc_steps += 1; }
+    tsync();
+}
+
+// ------------------------------------------------------------ contact solver pieces (contacts/b2contactsolver.d)
+DG int other_body(const Ctx& x, const dbox_contact_state& c, int b) {
+    int A = x.fx[c.fixture_a].body;
+    return A == b ? x.fx[c.fixture_b].body : A;
+}
+
+// b2ContactSolver ctor (:244-329) for one contact
+DG void constraint_ctor(const Ctx& x, int ci, bool warm, float dtRatio) {
+    const dbox_contact_state& c = x.ct[ci];
+    const DFixture& fa = x.fx[c.fixture_a];
+    const DFixture& fb = x.fx[c.fixture_b];
+    const dbox_body_state& ba = x.bs[fa.body];
+    const dbox_body_state& bb = x.bs[fb.body];
+    VC& vc = x.vc[ci];
+    PC& pc = x.pc[ci];
+    int pointCount = c.point_count;
+    vc.friction = c.friction;
+    vc.restitution = c.restitution;
+    vc.tangentSpeed = c.tangent_speed;
+    vc.bodyA = fa.body;
+    vc.bodyB = fb.body;
+    vc.invMassA = ba.mass[1];
+    vc.invMassB = bb.mass[1];
+    vc.invIA = ba.mass[3];
+    vc.invIB = bb.mass[3];
+    vc.pointCount = pointCount;
+    vc.K[0] = vc.K[1] = vc.K[2] = vc.K[3] = 0.0f;
+    vc.NM[0] = vc.NM[1] = vc.NM[2] = vc.NM[3] = 0.0f;
+    pc.bodyA = fa.body;
+    pc.bodyB = fb.body;
+    pc.invMassA = ba.mass[1];
+    pc.invMassB = bb.mass[1];
+    pc.lcA = b_lc(ba);
+    pc.lcB = b_lc(bb);
+    pc.invIA = ba.mass[3];
+    pc.invIB = bb.mass[3];
+    pc.localNormal = v2(c.local_normal[0], c.local_normal[1]);
+    pc.localPoint = v2(c.local_point[0], c.local_point[1]);
+    pc.pointCount = pointCount;
+    pc.radiusA = fa.radius;
+    pc.radiusB = fb.radius;
+    pc.type = c.type;
+    for (int j = 0; j < pointCount; ++j) {
+        VPoint& p = vc.p[j];
+        if (warm) {
+            p.normalImpulse = dtRatio * c.points[j].normal_impulse;
+            p.tangentImpulse = dtRatio * c.points[j].tangent_impulse;
+        } else {
+            p.normalImpulse = 0.0f;
+            p.tangentImpulse = 0.0f;
+        }
+        p.rA = v2(0.0f, 0.0f);
+        p.rB = v2(0.0f, 0.0f);
+        p.normalMass = 0.0f;
+        p.tangentMass = 0.0f;
+        p.velocityBias = 0.0f;
+        pc.localPoints[j] = v2(c.points[j].local_point[0], c.points[j].local_point[1]);
+    }
+}
+
+// InitializeVelocityConstraints (:338-450) for one contact
+DG void constraint_init_velocity(const Ctx& x, int ci) {
+    VC& vc = x.vc[ci];
+    const PC& pc = x.pc[ci];
+    const dbox_body_state& ba = x.bs[vc.bodyA];
+    const dbox_body_state& bb = x.bs[vc.bodyB];
+    int pointCount = vc.pointCount;
+    const dbox_contact_state& c = x.ct[ci];
+    float mA = vc.invMassA, mB = vc.invMassB, iA = vc.invIA, iB = vc.invIB;
+    float2 cA = b_c(ba), cB = b_c(bb);
+    float aA = ba.sweep[7], aB = bb.sweep[7];
+    float2 vA = b_v(ba), vB = b_v(bb);
+    float wA = ba.vel[2], wB = bb.vel[2];
+    Xf xfA, xfB;
+    xfA.q = rot(aA);
+    xfB.q = rot(aB);
+    xfA.p = cA - mul(xfA.q, pc.lcA);
+    xfB.p = cB - mul(xfB.q, pc.lcB);
+    // b2WorldManifold.Initialize (b2collision.d:123-191)
+    float2 normal = v2(0.0f, 0.0f);
+    float2 points[2] = {v2(0.0f, 0.0f), v2(0.0f, 0.0f)};
+    float radiusA = pc.radiusA, radiusB = pc.radiusB;
+    if (pointCount > 0) {
+        if (c.type == kManifoldCircles) {
+            normal = v2(1.0f, 0.0f);
+            float2 pointA = mul(xfA, pc.localPoint);
+            float2 pointB = mul(xfB, pc.localPoints[0]);
+            if (dist_sq(pointA, pointB) > kEpsilon * kEpsilon) {
+                normal = pointB - pointA;
+                normalize(normal);
+            }
+            float2 ccA = pointA + radiusA * normal;
+            float2 ccB = pointB - radiusB * normal;
+            points[0] = 0.5f * (ccA + ccB);
+        } else if (c.type == kManifoldFaceA) {
+            normal = mul(xfA.q, pc.localNormal);
+            float2 planePoint = mul(xfA, pc.localPoint);
+            for (int i = 0; i < pointCount; ++i) {
+                float2 clipPoint = mul(xfB, pc.localPoints[i]);
+                float2 ccA = clipPoint + (radiusA - dot(clipPoint - planePoint, normal)) * normal;
+                float2 ccB = clipPoint - radiusB * normal;
+                points[i] = 0.5f * (ccA + ccB);
+            }
+        } else {
+            normal = mul(xfB.q, pc.localNormal);
+            float2 planePoint = mul(xfB, pc.localPoint);
+            for (int i = 0; i < pointCount; ++i) {
+                float2 clipPoint = mul(xfA, pc.localPoints[i]);
+                float2 ccB = clipPoint + (radiusB - dot(clipPoint - planePoint, normal)) * normal;
+                float2 ccA = clipPoint - radiusA * normal;
+                points[i] = 0.5f * (ccA + ccB);
+            }
+            normal = -normal;
+        }
+    }
+    vc.normal = normal;
+    for (int j = 0; j < pointCount; ++j) {
+        VPoint& p = vc.p[j];
+        p.rA = points[j] - cA;
+        p.rB = points[j] - cB;
+        float rnA = cross(p.rA, normal);
+        float rnB = cross(p.rB, normal);
+        float kNormal = ((mA + mB) + (iA * rnA) * rnA) + (iB * rnB) * rnB;
+        p.normalMass = kNormal > 0.0f ? fdiv(1.0f, kNormal) : 0.0f;
+        float2 tangent = cross(normal, 1.0f);
+        float rtA = cross(p.rA, tangent);
+        float rtB = cross(p.rB, tangent);
+        float kTangent = ((mA + mB) + (iA * rtA) * rtA) + (iB * rtB) * rtB;
+        p.tangentMass = kTangent > 0.0f ? fdiv(1.0f, kTangent) : 0.0f;
+        p.velocityBias = 0.0f;
+        float vRel = dot(normal, ((vB + cross(wB, p.rB)) - vA) - cross(wA, p.rA));
+        if (vRel < -kVelocityThreshold) p.velocityBias = -vc.restitution * vRel;
+    }
+    if (vc.pointCount == 2) {
+        const VPoint& p1 = vc.p[0];
+        const VPoint& p2 = vc.p[1];
+        float rn1A = cross(p1.rA, normal), rn1B = cross(p1.rB, normal);
+        float rn2A = cross(p2.rA, normal), rn2B = cross(p2.rB, normal);
+        float k11 = ((mA + mB) + (iA * rn1A) * rn1A) + (iB * rn1B) * rn1B;
+        float k22 = ((mA + mB) + (iA * rn2A) * rn2A) + (iB * rn2B) * rn2B;
+        float k12 = ((mA + mB) + (iA * rn1A) * rn2A) + (iB * rn1B) * rn2B;
+        if (k11 * k11 < 1000.0f * (k11 * k22 - k12 * k12)) {
+            vc.K[0] = k11; vc.K[1] = k12; vc.K[2] = k12; vc.K[3] = k22;
+            // b2Mat22.GetInverse (b2math.d:322-337)
+            float a = vc.K[0], b = vc.K[2], cc = vc.K[1], d = vc.K[3];
+            float det = a * d - b * cc;
+            if (det != 0.0f) det = fdiv(1.0f, det);
+            vc.NM[0] = det * d;
+            vc.NM[2] = -det * b;
+            vc.NM[1] = -det * cc;
+            vc.NM[3] = det * a;
+        } else {
+            vc.pointCount = 1;
+        }
+    }
+}
+
+DG void warm_start(const Ctx& x, int ci) {                             // :452-490
+    const VC& vc = x.vc[ci];
+    dbox_body_state& ba = x.bs[vc.bodyA];
+    dbox_body_state& bb = x.bs[vc.bodyB];
+    float mA = vc.invMassA, iA = vc.invIA, mB = vc.invMassB, iB = vc.invIB;
+    float2 vA = b_v(ba), vB = b_v(bb);
+    float wA = ba.vel[2], wB = bb.vel[2];
+    float2 normal = vc.normal;
+    float2 tangent = cross(normal, 1.0f);
+    for (int j = 0; j < vc.pointCount; ++j) {
+        const VPoint& p = vc.p[j];
+        float2 P = p.normalImpulse * normal + p.tangentImpulse * tangent;
+        wA -= iA * cross(p.rA, P);
+        vA -= mA * P;
+        wB += iB * cross(p.rB, P);
+        vB += mB * P;
+    }
+    ba.vel[0] = vA.x; ba.vel[1] = vA.y; ba.vel[2] = wA;
+    bb.vel[0] = vB.x; bb.vel[1] = vB.y; bb.vel[2] = wB;
+}
+
+DG void apply_block(float2& vA, float& wA, float2& vB, float& wB, float mA, float iA, float mB, float iB,
+                    const VPoint& cp1, const VPoint& cp2, float2 normal, float2 d) {
+    float2 P1 = d.x * normal;
+    float2 P2 = d.y * normal;
+    vA -= mA * (P1 + P2);
+    wA -= iA * (cross(cp1.rA, P1) + cross(cp2.rA, P2));
+    vB += mB * (P1 + P2);
+    wB += iB * (cross(cp1.rB, P1) + cross(cp2.rB, P2));
+}
+
+DG void solve_velocity(const Ctx& x, int ci) {                         // :492-772
+    VC& vc = x.vc[ci];
+    dbox_body_state& ba = x.bs[vc.bodyA];
+    dbox_body_state& bb = x.bs[vc.bodyB];
+    float mA = vc.invMassA, iA = vc.invIA, mB = vc.invMassB, iB = vc.invIB;
+    int pointCount = vc.pointCount;
+    float2 vA = b_v(ba), vB = b_v(bb);
+    float wA = ba.vel[2], wB = bb.vel[2];
+    float2 normal = vc.normal;
+    float2 tangent = cross(normal, 1.0f);
+    float friction = vc.friction;
+    for (int j = 0; j < pointCount; ++j) {
+        VPoint& p = vc.p[j];
+        float2 dv = ((vB + cross(wB, p.rB)) - vA) - cross(wA, p.rA);
+        float vt = dot(dv, tangent) - vc.tangentSpeed;
+        float lambda = p.tangentMass * (-vt);
+        float maxFriction = friction * p.normalImpulse;
+        float newImpulse = bclamp(p.tangentImpulse + lambda, -maxFriction, maxFriction);
+        lambda = newImpulse - p.tangentImpulse;
+        p.tangentImpulse = newImpulse;
+        float2 P = lambda * tangent;
+        vA -= mA * P;
+        wA -= iA * cross(p.rA, P);
+        vB += mB * P;
+        wB += iB * cross(p.rB, P);
+    }
+    if (pointCount == 1) {
+        VPoint& p = vc.p[0];
+        float2 dv = ((vB + cross(wB, p.rB)) - vA) - cross(wA, p.rA);
+        float vn = dot(dv, normal);
+        float lambda = -p.normalMass * (vn - p.velocityBias);
+        float newImpulse = bmax(p.normalImpulse + lambda, 0.0f);
+        lambda = newImpulse - p.normalImpulse;
+        p.normalImpulse = newImpulse;
+        float2 P = lambda * normal;
+        vA -= mA * P;
+        wA -= iA * cross(p.rA, P);
+        vB += mB * P;
+        wB += iB * cross(p.rB, P);
+    } else {
+        VPoint& cp1 = vc.p[0];
+        VPoint& cp2 = vc.p[1];
+        float2 a = v2(cp1.normalImpulse, cp2.normalImpulse);
+        float2 dv1 = ((vB + cross(wB, cp1.rB)) - vA) - cross(wA, cp1.rA);
+        float2 dv2 = ((vB + cross(wB, cp2.rB)) - vA) - cross(wA, cp2.rA);
+        float vn1 = dot(dv1, normal);
+        float vn2 = dot(dv2, normal);
+        float2 b;
+        b.x = vn1 - cp1.velocityBias;
+        b.y = vn2 - cp2.velocityBias;
+        // b -= b2Mul(K, a)
+        float2 Ka = v2(vc.K[0] * a.x + vc.K[2] * a.y, vc.K[1] * a.x + vc.K[3] * a.y);
+        b -= Ka;
+        for (;;) {
+            float2 xx = -v2(vc.NM[0] * b.x + vc.NM[2] * b.y, vc.NM[1] * b.x + vc.NM[3] * b.y);
+            if (xx.x >= 0.0f && xx.y >= 0.0f) {
+                apply_block(vA, wA, vB, wB, mA, iA, mB, iB, cp1, cp2, normal, xx - a);
+                cp1.normalImpulse = xx.x;
+                cp2.normalImpulse = xx.y;
+                break;
+            }
+            xx.x = -cp1.normalMass * b.x;
+            xx.y = 0.0f;
+            vn2 = vc.K[1] * xx.x + b.y;
+            if (xx.x >= 0.0f && vn2 >= 0.0f) {
+                apply_block(vA, wA, vB, wB, mA, iA, mB, iB, cp1, cp2, normal, xx - a);
+                cp1.normalImpulse = xx.x;
+                cp2.normalImpulse = xx.y;
+                break;
+            }
+            xx.x = 0.0f;
+            xx.y = -cp2.normalMass * b.y;
+            vn1 = vc.K[2] * xx.y + b.x;
+            if (xx.y >= 0.0f && vn1 >= 0.0f) {
+                apply_block(vA, wA, vB, wB, mA, iA, mB, iB, cp1, cp2, normal, xx - a);
+                cp1.normalImpulse = xx.x;
+                cp2.normalImpulse = xx.y;
+                break;
+            }
+            xx.x = 0.0f;
+            xx.y = 0.0f;
+            vn1 = b.x;
+            vn2 = b.y;
+            if (vn1 >= 0.0f && vn2 >= 0.0f) {
+                apply_block(vA, wA, vB, wB, mA, iA, mB, iB, cp1, cp2, normal, xx - a);
+                cp1.normalImpulse = xx.x;
+                cp2.normalImpulse = xx.y;
+                break;
+            }
+            break;
+        }
+    }
+    ba.vel[0] = vA.x; ba.vel[1] = vA.y; ba.vel[2] = wA;
+    bb.vel[0] = vB.x; bb.vel[1] = vB.y; bb.vel[2] = wB;
+}
+
+DG void store_impulses(const Ctx& x, int ci) {                         // :774-787
+    const VC& vc = x.vc[ci];
+    dbox_contact_state& c = x.ct[ci];
+    for (int j = 0; j < vc.pointCount; ++j) {
+        c.points[j].normal_impulse = vc.p[j].normalImpulse;
+        c.points[j].tangent_impulse = vc.p[j].tangentImpulse;
+    }
+}
+
+// SolvePositionConstraints / SolveTOIPositionConstraints for one contact (:73-242);
+// returns the minimum separation seen over its points (0 if none below 0).
+DG float solve_position(const Ctx& x, int ci, bool toi, int toiA, int toiB) {
+    const PC& pc = x.pc[ci];
+    dbox_body_state& ba = x.bs[pc.bodyA];
+    dbox_body_state& bb = x.bs[pc.bodyB];
+    float mA, iA, mB, iB;
+    if (!toi) { mA = pc.invMassA; iA = pc.invIA; mB = pc.invMassB; iB = pc.invIB; }
+    else {
+        mA = 0.0f; iA = 0.0f;
+        if (pc.bodyA == toiA || pc.bodyA == toiB) { mA = pc.invMassA; iA = pc.invIA; }
+        mB = 0.0f; iB = 0.0f;
+        if (pc.bodyB == toiA || pc.bodyB == toiB) { mB = pc.invMassB; iB = pc.invIB; }
+    }
+    float2 cA = b_c(ba), cB = b_c(bb);
+    float aA = ba.sweep[7], aB = bb.sweep[7];
+    float minSep = 0.0f;
+    for (int j = 0; j < pc.pointCount; ++j) {
+        Xf xfA, xfB;
+        xfA.q = rot(aA);
+        xfB.q = rot(aB);
+        xfA.p = cA - mul(xfA.q, pc.lcA);
+        xfB.p = cB - mul(xfB.q, pc.lcB);
+        // b2PositionSolverManifold.Initialize (:816-851)
+        float2 normal, point;
+        float separation;
+        if (pc.type == kManifoldCircles) {
+            float2 pointA = mul(xfA, pc.localPoint);
+            float2 pointB = mul(xfB, pc.localPoints[0]);
+            normal = pointB - pointA;
+            normalize(normal);
+            point = 0.5f * (pointA + pointB);
+            separation = (dot(pointB - pointA, normal) - pc.radiusA) - pc.radiusB;
+        } else if (pc.type == kManifoldFaceA) {
+            normal = mul(xfA.q, pc.localNormal);
+            float2 planePoint = mul(xfA, pc.localPoint);
+            float2 clipPoint = mul(xfB, pc.localPoints[j]);
+            separation = (dot(clipPoint - planePoint, normal) - pc.radiusA) - pc.radiusB;
+            point = clipPoint;
+        } else {
+            normal = mul(xfB.q, pc.localNormal);
+            float2 planePoint = mul(xfB, pc.localPoint);
+            float2 clipPoint = mul(xfA, pc.localPoints[j]);
+            separation = (dot(clipPoint - planePoint, normal) - pc.radiusA) - pc.radiusB;
+            point = clipPoint;
+            normal = -normal;
+        }
+        float2 rA = point - cA;
+        float2 rB = point - cB;
+        minSep = bmin(minSep, separation);
+        float C = bclamp((toi ? kToiBaumgarte : kBaumgarte) * (separation + kLinearSlop), -kMaxLinearCorrection, 0.0f);
+        float rnA = cross(rA, normal);
+        float rnB = cross(rB, normal);
+        float K = ((mA + mB) + (iA * rnA) * rnA) + (iB * rnB) * rnB;
+        float impulse = K > 0.0f ? fdiv(-C, K) : 0.0f;
+        float2 P = impulse * normal;
+        cA -= mA * P;
+        aA -= iA * cross(rA, P);
+        cB += mB * P;
+        aB += iB * cross(rB, P);
+    }
+    ba.sweep[4] = cA.x; ba.sweep[5] = cA.y; ba.sweep[7] = aA;
+    bb.sweep[4] = cB.x; bb.sweep[5] = cB.y; bb.sweep[7] = aB;
+    return minSep;
+}
+
+// ------------------------------------------------------------ revolute joint (joints/b2revolutejoint.d:319-636)
+DG Xf dummy_xf() { Xf x; x.p = v2(0, 0); x.q.s = 0; x.q.c = 1; return x; }
+
+DG void joint_init(const Ctx& x, int ji, bool warm, float dtRatio) {
+    DJoint& j = x.jt[ji];
+    dbox_body_state& ba = x.bs[j.body_a];
+    dbox_body_state& bb = x.bs[j.body_b];
+    j.lcA = b_lc(ba);
+    j.lcB = b_lc(bb);
+    j.invMassA = ba.mass[1];
+    j.invMassB = bb.mass[1];
+    j.invIA = ba.mass[3];
+    j.invIB = bb.mass[3];
+    float aA = ba.sweep[7];
+    float2 vA = b_v(ba);
+    float wA = ba.vel[2];
+    float aB = bb.sweep[7];
+    float2 vB = b_v(bb);
+    float wB = bb.vel[2];
+    Rot qA = rot(aA), qB = rot(aB);
+    j.rA = mul(qA, j.local_anchor_a - j.lcA);
+    j.rB = mul(qB, j.local_anchor_b - j.lcB);
+    float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    bool fixedRotation = (iA + iB == 0.0f);
+    float2 rA = j.rA, rB = j.rB;
+    j.mass[0] = ((mA + mB) + (rA.y * rA.y) * iA) + (rB.y * rB.y) * iB;   // ex.x
+    j.mass[3] = (-rA.y * rA.x) * iA - (rB.y * rB.x) * iB;               // ey.x
+    j.mass[6] = -rA.y * iA - rB.y * iB;                                  // ez.x
+    j.mass[1] = j.mass[3];                                               // ex.y
+    j.mass[4] = ((mA + mB) + (rA.x * rA.x) * iA) + (rB.x * rB.x) * iB;   // ey.y
+    j.mass[7] = rA.x * iA + rB.x * iB;                                   // ez.y
+    j.mass[2] = j.mass[6];                                               // ex.z
+    j.mass[5] = j.mass[7];                                               // ey.z
+    j.mass[8] = iA + iB;                                                 // ez.z
+    j.motor_mass = iA + iB;
+    if (j.motor_mass > 0.0f) j.motor_mass = fdiv(1.0f, j.motor_mass);
+    if (j.enable_motor == 0 || fixedRotation) j.motor_impulse = 0.0f;
+    if (j.enable_limit && !fixedRotation) {
+        float jointAngle = (aB - aA) - j.reference_angle;
+        if (babs(j.upper_angle - j.lower_angle) < 2.0f * kAngularSlop) {
+            j.limit_state = 3;
+        } else if (jointAngle <= j.lower_angle) {
+            if (j.limit_state != 1) j.impulse[2] = 0.0f;
+            j.limit_state = 1;
+        } else if (jointAngle >= j.upper_angle) {
+            if (j.limit_state != 2) j.impulse[2] = 0.0f;
+            j.limit_state = 2;
+        } else {
+            j.limit_state = 0;
+            j.impulse[2] = 0.0f;
+        }
+    } else {
+        j.limit_state = 0;
+    }
+    if (warm) {
+        j.impulse[0] *= dtRatio; j.impulse[1] *= dtRatio; j.impulse[2] *= dtRatio;
+        j.motor_impulse *= dtRatio;
+        float2 P = v2(j.impulse[0], j.impulse[1]);
+        vA -= mA * P;
+        wA -= iA * ((cross(rA, P) + j.motor_impulse) + j.impulse[2]);
+        vB += mB * P;
+        wB += iB * ((cross(rB, P) + j.motor_impulse) + j.impulse[2]);
+    } else {
+        j.impulse[0] = j.impulse[1] = j.impulse[2] = 0.0f;
+        j.motor_impulse = 0.0f;
+    }
+    ba.vel[0] = vA.x; ba.vel[1] = vA.y; ba.vel[2] = wA;
+    bb.vel[0] = vB.x; bb.vel[1] = vB.y; bb.vel[2] = wB;
+}
+
+DG float3 solve33(const float* m, float3 b) {                            // b2math.d:388-399
+    // columns ex=(m0,m1,m2) ey=(m3,m4,m5) ez=(m6,m7,m8)
+    float3 ex = make_float3(m[0], m[1], m[2]), ey = make_float3(m[3], m[4], m[5]), ez = make_float3(m[6], m[7], m[8]);
+    auto cr = [](float3 a, float3 c) { return make_float3(a.y * c.z - a.z * c.y, a.z * c.x - a.x * c.z, a.x * c.y - a.y * c.x); };
+    auto dt3 = [](float3 a, float3 c) { return (a.x * c.x + a.y * c.y) + a.z * c.z; };
+    float det = dt3(ex, cr(ey, ez));
+    if (det != 0.0f) det = fdiv(1.0f, det);
+    float3 r;
+    r.x = det * dt3(b, cr(ey, ez));
+    r.y = det * dt3(ex, cr(b, ez));
+    r.z = det * dt3(ex, cr(ey, b));
+    return r;
+}
+DG float2 solve22(const float* m, float2 b) {                            // b2math.d:402-415
+    float a11 = m[0], a12 = m[3], a21 = m[1], a22 = m[4];
+    float det = a11 * a22 - a12 * a21;
+    if (det != 0.0f) det = fdiv(1.0f, det);
+    return v2(det * (a22 * b.x - a12 * b.y), det * (a11 * b.y - a21 * b.x));
+}
+
+DG void joint_solve_velocity(const Ctx& x, int ji) {
+    DJoint& j = x.jt[ji];
+    dbox_body_state& ba = x.bs[j.body_a];
+    dbox_body_state& bb = x.bs[j.body_b];
+    float2 vA = b_v(ba), vB = b_v(bb);
+    float wA = ba.vel[2], wB = bb.vel[2];
+    float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    bool fixedRotation = (iA + iB == 0.0f);
+    if (j.enable_motor && j.limit_state != 3 && !fixedRotation) {
+        float Cdot = (wB - wA) - j.motor_speed;
+        float imp = -j.motor_mass * Cdot;
+        float oldImpulse = j.motor_impulse;
+        float maxImpulse = x.dt * j.max_motor_torque;
+        j.motor_impulse = bclamp(j.motor_impulse + imp, -maxImpulse, maxImpulse);
+        imp = j.motor_impulse - oldImpulse;
+        wA -= iA * imp;
+        wB += iB * imp;
+    }
+    if (j.enable_limit && j.limit_state != 0 && !fixedRotation) {
+        float2 Cdot1 = ((vB + cross(wB, j.rB)) - vA) - cross(wA, j.rA);
+        float Cdot2 = wB - wA;
+        float3 r = solve33(j.mass, make_float3(Cdot1.x, Cdot1.y, Cdot2));
+        float3 imp = make_float3(-r.x, -r.y, -r.z);
+        if (j.limit_state == 3) {
+            j.impulse[0] += imp.x; j.impulse[1] += imp.y; j.impulse[2] += imp.z;
+        } else if (j.limit_state == 1 || j.limit_state == 2) {
+            float newImpulse = j.impulse[2] + imp.z;
+            bool reduce = j.limit_state == 1 ? newImpulse < 0.0f : newImpulse > 0.0f;
+            if (reduce) {
+                float2 rhs = -Cdot1 + j.impulse[2] * v2(j.mass[6], j.mass[7]);
+                float2 reduced = solve22(j.mass, rhs);
+                imp.x = reduced.x;
+                imp.y = reduced.y;
+                imp.z = -j.impulse[2];
+                j.impulse[0] += reduced.x;
+                j.impulse[1] += reduced.y;
+                j.impulse[2] = 0.0f;
+            } else {
+                j.impulse[0] += imp.x; j.impulse[1] += imp.y; j.impulse[2] += imp.z;
+            }
+        }
+        float2 P = v2(imp.x, imp.y);
+        vA -= mA * P;
+        wA -= iA * (cross(j.rA, P) + imp.z);
+        vB += mB * P;
+        wB += iB * (cross(j.rB, P) + imp.z);
+    } else {
+        float2 Cdot = ((vB + cross(wB, j.rB)) - vA) - cross(wA, j.rA);
+        float2 imp = solve22(j.mass, -Cdot);
+        j.impulse[0] += imp.x;
+        j.impulse[1] += imp.y;
+        vA -= mA * imp;
+        wA -= iA * cross(j.rA, imp);
+        vB += mB * imp;
+        wB += iB * cross(j.rB, imp);
+    }
+    ba.vel[0] = vA.x; ba.vel[1] = vA.y; ba.vel[2] = wA;
+    bb.vel[0] = vB.x; bb.vel[1] = vB.y; bb.vel[2] = wB;
+}
+
+DG bool joint_solve_position(const Ctx& x, int ji) {
+    DJoint& j = x.jt[ji];
+    dbox_body_state& ba = x.bs[j.body_a];
+    dbox_body_state& bb = x.bs[j.body_b];
+    float2 cA = b_c(ba), cB = b_c(bb);
+    float aA = ba.sweep[7], aB = bb.sweep[7];
+    float angularError = 0.0f, positionError = 0.0f;
+    bool fixedRotation = (j.invIA + j.invIB == 0.0f);
+    if (j.enable_limit && j.limit_state != 0 && !fixedRotation) {
+        float angle = (aB - aA) - j.reference_angle;
+        float limitImpulse = 0.0f;
+        if (j.limit_state == 3) {
+            float C = bclamp(angle - j.lower_angle, -kMaxAngularCorrection, kMaxAngularCorrection);
+            limitImpulse = -j.motor_mass * C;
+            angularError = babs(C);
+        } else if (j.limit_state == 1) {
+            float C = angle - j.lower_angle;
+            angularError = -C;
+            C = bclamp(C + kAngularSlop, -kMaxAngularCorrection, 0.0f);
+            limitImpulse = -j.motor_mass * C;
+        } else if (j.limit_state == 2) {
+            float C = angle - j.upper_angle;
+            angularError = C;
+            C = bclamp(C - kAngularSlop, 0.0f, kMaxAngularCorrection);
+            limitImpulse = -j.motor_mass * C;
+        }
+        aA -= j.invIA * limitImpulse;
+        aB += j.invIB * limitImpulse;
+    }
+    {
+        Rot qA = rot(aA), qB = rot(aB);
+        float2 rA = mul(qA, j.local_anchor_a - j.lcA);
+        float2 rB = mul(qB, j.local_anchor_b - j.lcB);
+        float2 C = ((cB + rB) - cA) - rA;
+        positionError = length(C);
+        float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+        float K[9];
+        K[0] = ((mA + mB) + (iA * rA.y) * rA.y) + (iB * rB.y) * rB.y;     // ex.x
+        K[1] = ((-iA * rA.x) * rA.y) - (iB * rB.x) * rB.y;               // ex.y
+        K[3] = K[1];                                                      // ey.x
+        K[4] = ((mA + mB) + (iA * rA.x) * rA.x) + (iB * rB.x) * rB.x;     // ey.y
+        float2 s = solve22(K, C);
+        float2 imp = -s;
+        cA -= mA * imp;
+        aA -= iA * cross(rA, imp);
+        cB += mB * imp;
+        aB += iB * cross(rB, imp);
+    }
+    ba.sweep[4] = cA.x; ba.sweep[5] = cA.y; ba.sweep[7] = aA;
+    bb.sweep[4] = cB.x; bb.sweep[5] = cB.y; bb.sweep[7] = aB;
+    return positionError <= kLinearSlop && angularError <= kAngularSlop;
+}
+
+// ------------------------------------------------------------ level schedule
+// Items: contact slot c >= 0, joint j encoded as -(j + 1).
+DG void item_bodies(const Ctx& x, int item, int& A, int& B) {
+    if (item >= 0) { A = x.vc[item].bodyA; B = x.vc[item].bodyB; }
+    else { const DJoint& j = x.jt[-item - 1]; A = j.body_a; B = j.body_b; }
+}
+DG int item_bodies_raw(const Ctx& x, int item, int& A, int& B) {
+    if (item >= 0) {
+        const dbox_contact_state& c = x.ct[item];
+        A = x.fx[c.fixture_a].body;
+        B = x.fx[c.fixture_b].body;
+    } else {
+        const DJoint& j = x.jt[-item - 1];
+        A = j.body_a;
+        B = j.body_b;
+    }
+    return 0;
+}
+
+// Build one level schedule for world w.  `contacts_first` gives the warm-start /
+// position order of b2Island.Solve (contacts then joints, b2island.d:136-146 and
+// 206-224); otherwise the velocity-iteration order (joints then contacts,
+// b2island.d:153-161).  Level L items end up in sched[kx + lvl[kx+L] .. kx + lvl[kx+L+1]).
+// Run by one lane.  Returns the number of levels.
+DG int build_schedule(const Ctx& x, const WorldInfo& wi, int nIsl, bool contacts_first, int* sched, int* lvl) {
+    int b0 = wi.body_start, kx = wi.kx_start;
+    for (int i = 0; i < wi.body_count; ++i) x.s_last[b0 + i] = 0;
+    int maxL = 0, n = 0;
+    for (int is = 0; is < nIsl; ++is) {
+        int cs = x.s_isl_cstart[wi.bx_start + is], ce = x.s_isl_cstart[wi.bx_start + is + 1];
+        int js = x.s_isl_jstart[wi.bx_start + is], je = x.s_isl_jstart[wi.bx_start + is + 1];
+        for (int pass = 0; pass < 2; ++pass) {
+            bool doContacts = (pass == 0) == contacts_first;
+            int s = doContacts ? cs : js, e = doContacts ? ce : je;
+            for (int t = s; t < e; ++t) {
+                int item = doContacts ? x.s_isl_contact[wi.contact_start + t] : -(x.s_isl_joint[wi.joint_start + t] + 1);
+                int A, B;
+                item_bodies_raw(x, item, A, B);
+                bool dA = x.bs[A].type == kDynamicBody, dB = x.bs[B].type == kDynamicBody;
+                int la = dA ? x.s_last[A] : 0, lb = dB ? x.s_last[B] : 0;
+                int l = (la > lb ? la : lb) + 1;
+                if (dA) x.s_last[A] = l;
+                if (dB) x.s_last[B] = l;
+                if (l > maxL) maxL = l;
+                x.s_level[kx + n] = l;
+                x.s_tmp[kx + n] = item;
+                ++n;
+            }
+        }
+    }
+    for (int l = 0; l <= maxL + 1; ++l) lvl[kx + l] = 0;
+    for (int i = 0; i < n; ++i) lvl[kx + x.s_level[kx + i]]++;
+    for (int l = 1; l <= maxL; ++l) lvl[kx + l] += lvl[kx + l - 1];
+    for (int i = n - 1; i >= 0; --i) {
+        int l = x.s_level[kx + i];
+        sched[kx + (--lvl[kx + l])] = x.s_tmp[kx + i];
+    }
+    lvl[kx + maxL + 1] = n;
+    return maxL;
+}
+
+// island id of a constraint: the island of one of its non-static bodies
+DG int item_island(const Ctx& x, int item) {
+    int A, B;
+    item_bodies_raw(x, item, A, B);
+    return x.bs[A].type != kStaticBody ? x.s_body_island[A] : x.s_body_island[B];
+}
+
+DG bool contact_in_island_graph(const Ctx& x, const dbox_contact_state& c) {
+    return (c.flags & kContactEnabled) && (c.flags & kContactTouching) && !x.fx[c.fixture_a].sensor &&
+           !x.fx[c.fixture_b].sensor;
+}
+
+// b2Fixture.Synchronize + b2DynamicTree.MoveProxy for every fixture of body b
+// (b2body.d:1129-1141, b2fixture.d:480-502, b2dynamictree.d:140-184)
+DG void sync_fixtures(const Ctx& x, int b) {
+    const dbox_body_state& B = x.bs[b];
+    Xf xf1;
+    xf1.q = rot(B.sweep[6]);
+    xf1.p = v2(B.sweep[2], B.sweep[3]) - mul(xf1.q, b_lc(B));
+    Xf xf2 = b_xf(B);
+    const BodyStatic& st = x.bst[b];
+    for (int e = 0; e < st.fix_count; ++e) {
+        int f = x.body_fix[st.fix_start + e];
+        dbox_proxy_state& p = x.px[f];
+        if (p.proxy_id < 0) continue;
+        AABB a1 = fixture_aabb(x.fx[f], xf1);
+        AABB a2 = fixture_aabb(x.fx[f], xf2);
+        AABB aabb;
+        aabb.lo = vmin(a1.lo, a2.lo);
+        aabb.hi = vmax(a1.hi, a2.hi);
+        float2 displacement = xf2.p - xf1.p;
+        AABB fat = proxy_fat(x, f);
+        if (aabb_contains(fat, aabb)) continue;
+        float2 r = v2(kAabbExtension, kAabbExtension);
+        aabb.lo = aabb.lo - r;
+        aabb.hi = aabb.hi + r;
+        float2 d = kAabbMultiplier * displacement;
+        if (d.x < 0.0f) aabb.lo.x += d.x; else aabb.hi.x += d.x;
+        if (d.y < 0.0f) aabb.lo.y += d.y; else aabb.hi.y += d.y;
+        p.fat_aabb[0] = aabb.lo.x; p.fat_aabb[1] = aabb.lo.y;
+        p.fat_aabb[2] = aabb.hi.x; p.fat_aabb[3] = aabb.hi.y;
+        p.moved = 1;
+    }
+}
+
+__global__ void k_solve(Ctx x) {
+    int w = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+    if (w >= x.W) return;
+    const WorldInfo& wi = x.wi[w];
+    WorldDyn& wd = x.wd[w];
+    int lane = lane_id();
+    if (!(wd.step_complete && x.dt > 0.0f)) return;
+    const int b0 = wi.body_start, nb = wi.body_count;
+    const int c0 = wi.contact_start, n = wd.contact_count;
+    const int j0 = wi.joint_start, nj = wi.joint_count;
+    const int bx = wi.bx_start, kx = wi.kx_start;
+    const float h = x.dt;
+    const bool warm = x.warm_starting != 0;
+    const float dtRatio = wd.inv_dt0 * x.dt;                            // b2world.d:392
+    // clear island flags (b2world.d:944-957) and per-step scratch
+    for (int i = lane; i < nb; i += kWarp) {
+        x.bs[b0 + i].flags &= ~(uint32_t)kBodyIsland;
+        x.s_cursor[b0 + i] = 0;
+        x.s_body_island[b0 + i] = -1;
+    }
+    for (int k = lane; k < n; k += kWarp) x.ct[c0 + k].flags &= ~(uint32_t)kContactIsland;
+    for (int j = lane; j < nj; j += kWarp) x.jt[j0 + j].island_flag = 0;
+    tsync();
+    // contact edges of the island graph, per body, newest first
+    for (int k = lane; k < n; k += kWarp) {
+        const dbox_contact_state& c = x.ct[c0 + k];
+        if (!contact_in_island_graph(x, c)) continue;
+        atomicAdd(&x.s_cursor[x.fx[c.fixture_a].body], 1);
+        atomicAdd(&x.s_cursor[x.fx[c.fixture_b].body], 1);
+    }
+    tsync();
+    int nIsl = 0, nbI = 0, ncI = 0, njI = 0, maxLv = 0, maxLp = 0;
+    if (lane == 0) {
+        int acc = 0;
+        for (int i = 0; i < nb; ++i) {
+            int cnt = x.s_cursor[b0 + i];
+            x.s_adj_start[bx + i] = acc;
+            x.s_cursor[b0 + i] = acc;
+            acc += cnt;
+        }
+        x.s_adj_start[bx + nb] = acc;
+        for (int k = n - 1; k >= 0; --k) {
+            const dbox_contact_state& c = x.ct[c0 + k];
+            if (!contact_in_island_graph(x, c)) continue;
+            int A = x.fx[c.fixture_a].body, B = x.fx[c.fixture_b].body;
+            x.s_adj_items[2 * c0 + x.s_cursor[A]++] = k;
+            x.s_adj_items[2 * c0 + x.s_cursor[B]++] = k;
+        }
+        // depth-first island search (b2world.d:959-1095)
+        for (int sb = nb - 1; sb >= 0; --sb) {
+            int seed = b0 + sb;
+            dbox_body_state& S = x.bs[seed];
+            if (S.flags & kBodyIsland) continue;
+            if ((S.flags & kBodyAwake) == 0 || (S.flags & kBodyActive) == 0) continue;
+            if (S.type == kStaticBody) continue;
+            x.s_isl_bstart[bx + nIsl] = nbI;
+            x.s_isl_cstart[bx + nIsl] = ncI;
+            x.s_isl_jstart[bx + nIsl] = njI;
+            int top = 0, nStatic = 0;
+            x.s_stack[b0 + top++] = seed;
+            S.flags |= kBodyIsland;
+            while (top > 0) {
+                int b = x.s_stack[b0 + --top];
+                dbox_body_state& Bd = x.bs[b];
+                b_set_awake(Bd, true);
+                x.s_body_island[b] = nIsl;
+                if (Bd.type == kStaticBody) {
+                    x.s_last[b0 + nStatic++] = b;
+                    continue;
+                }
+                x.s_isl_body[b0 + nbI++] = b;
+                int rs = x.s_adj_start[bx + (b - b0)], re = x.s_adj_start[bx + (b - b0) + 1];
+                for (int e = rs; e < re; ++e) {
+                    int k = x.s_adj_items[2 * c0 + e];
+                    dbox_contact_state& c = x.ct[c0 + k];
+                    if (c.flags & kContactIsland) continue;
+                    x.s_isl_contact[c0 + ncI++] = c0 + k;
+                    c.flags |= kContactIsland;
+                    int other = other_body(x, c, b);
+                    if (x.bs[other].flags & kBodyIsland) continue;
+                    x.s_stack[b0 + top++] = other;
+                    x.bs[other].flags |= kBodyIsland;
+                }
+                const BodyStatic& st = x.bst[b];
+                for (int e = 0; e < st.jadj_count; ++e) {
+                    int j = x.jadj_joint[st.jadj_start + e];
+                    if (x.jt[j].island_flag) continue;
+                    int other = x.jadj_other[st.jadj_start + e];
+                    if ((x.bs[other].flags & kBodyActive) == 0) continue;
+                    x.s_isl_joint[j0 + njI++] = j;
+                    x.jt[j].island_flag = 1;
+                    if (x.bs[other].flags & kBodyIsland) continue;
+                    x.s_stack[b0 + top++] = other;
+                    x.bs[other].flags |= kBodyIsland;
+                }
+            }
+            for (int i = 0; i < nStatic; ++i) x.bs[x.s_last[b0 + i]].flags &= ~(uint32_t)kBodyIsland;
+            ++nIsl;
+        }
+        x.s_isl_bstart[bx + nIsl] = nbI;
+        x.s_isl_cstart[bx + nIsl] = ncI;
+        x.s_isl_jstart[bx + nIsl] = njI;
+        // contacts keep their island id for the position pass
+        maxLv = build_schedule(x, wi, nIsl, false, x.s_sched_v, x.s_lvl_v);
+        maxLp = build_schedule(x, wi, nIsl, true, x.s_sched_p, x.s_lvl_p);
+        wd.islands = nIsl;
+    }
+    nIsl = __shfl_sync(0xffffffffu, nIsl, 0);
+    nbI = __shfl_sync(0xffffffffu, nbI, 0);
+    ncI = __shfl_sync(0xffffffffu, ncI, 0);
+    maxLv = __shfl_sync(0xffffffffu, maxLv, 0);
+    maxLp = __shfl_sync(0xffffffffu, maxLp, 0);
+    if (lane == 0) {
+        wd.acc_isl_bodies += (unsigned long long)nbI;
+        wd.acc_isl_contacts += (unsigned long long)ncI;
+        wd.acc_vsolve += (unsigned long long)ncI * (unsigned long long)x.vel_iters;
+    }
+    tsync();
+    // integrate velocities (b2island.d:82-116)
+    for (int i = lane; i < nbI; i += kWarp) {
+        int b = x.s_isl_body[b0 + i];
+        dbox_body_state& B = x.bs[b];
+        B.sweep[2] = B.sweep[4];
+        B.sweep[3] = B.sweep[5];
+        B.sweep[6] = B.sweep[7];
+        if (B.type == kDynamicBody) {
+            const BodyStatic& st = x.bst[b];
+            float2 v = b_v(B);
+            float wv = B.vel[2];
+            float2 g = st.gravity_scale * x.gravity + B.mass[1] * v2(B.force[0], B.force[1]);
+            v += h * g;
+            wv += (h * B.mass[3]) * B.force[2];
+            v *= fdiv(1.0f, 1.0f + h * st.lin_damping);
+            wv *= fdiv(1.0f, 1.0f + h * st.ang_damping);
+            B.vel[0] = v.x; B.vel[1] = v.y; B.vel[2] = wv;
+        }
+    }
+    tsync();
+    for (int t = lane; t < ncI; t += kWarp) {
+        int ci = x.s_isl_contact[c0 + t];
+        constraint_ctor(x, ci, warm, dtRatio);
+        constraint_init_velocity(x, ci);
+    }
+    tsync();
+    // warm start contacts, then joints' InitVelocityConstraints (b2island.d:133-146)
+    for (int L = 1; L <= maxLp; ++L) {
+        int s = x.s_lvl_p[kx + L], e = x.s_lvl_p[kx + L + 1];
+        for (int idx = s + lane; idx < e; idx += kWarp) {
+            int item = x.s_sched_p[kx + idx];
+            if (item >= 0) { if (warm) warm_start(x, item); }
+            else joint_init(x, -item - 1, warm, dtRatio);
+        }
+        tsync();
+    }
+    // velocity iterations (b2island.d:153-161)
+    for (int it = 0; it < x.vel_iters; ++it) {
+        for (int L = 1; L <= maxLv; ++L) {
+            int s = x.s_lvl_v[kx + L], e = x.s_lvl_v[kx + L + 1];
+            for (int idx = s + lane; idx < e; idx += kWarp) {
+                int item = x.s_sched_v[kx + idx];
+                if (item >= 0) solve_velocity(x, item);
+                else joint_solve_velocity(x, -item - 1);
+            }
+            tsync();
+        }
+    }
+    for (int t = lane; t < ncI; t += kWarp) store_impulses(x, x.s_isl_contact[c0 + t]);
+    // integrate positions (b2island.d:168-200)
+    for (int i = lane; i < nbI; i += kWarp) {
+        dbox_body_state& B = x.bs[x.s_isl_body[b0 + i]];
+        float2 c = b_c(B);
+        float a = B.sweep[7];
+        float2 v = b_v(B);
+        float wv = B.vel[2];
+        float2 translation = h * v;
+        if (dot(translation, translation) > kMaxTranslationSquared) {
+            float ratio = fdiv(kMaxTranslation, length(translation));
+            v *= ratio;
+        }
+        float rotation = h * wv;
+        if (rotation * rotation > kMaxRotationSquared) {
+            float ratio = fdiv(kMaxRotation, babs(rotation));
+            wv *= ratio;
+        }
+        c += h * v;
+        a += h * wv;
+        B.sweep[4] = c.x; B.sweep[5] = c.y; B.sweep[7] = a;
+        B.vel[0] = v.x; B.vel[1] = v.y; B.vel[2] = wv;
+    }
+    for (int is = lane; is < nIsl; is += kWarp) x.s_isl_flags[b0 + is] = 0;
+    tsync();
+    // position iterations with per-island early exit (b2island.d:206-224)
+    for (int it = 0; it < x.pos_iters; ++it) {
+        for (int is = lane; is < nIsl; is += kWarp) {
+            x.s_isl_minsep[b0 + is] = fkey(0.0f);
+            x.s_isl_flags[b0 + is] &= ~4;
+        }
+        tsync();
+        for (int L = 1; L <= maxLp; ++L) {
+            int s = x.s_lvl_p[kx + L], e = x.s_lvl_p[kx + L + 1];
+            for (int idx = s + lane; idx < e; idx += kWarp) {
+                int item = x.s_sched_p[kx + idx];
+                int is = item_island(x, item);
+                if (x.s_isl_flags[b0 + is] & 1) continue;
+                if (item >= 0) {
+                    float ms = solve_position(x, item, false, -1, -1);
+                    atomicMin(&x.s_isl_minsep[b0 + is], fkey(ms));
+                } else if (!joint_solve_position(x, -item - 1)) {
+                    atomicOr(&x.s_isl_flags[b0 + is], 4);
+                }
+            }
+            tsync();
+        }
+        int psolved = 0;
+        for (int is = lane; is < nIsl; is += kWarp)
+            if (!(x.s_isl_flags[b0 + is] & 1))
+                psolved += x.s_isl_cstart[bx + is + 1] - x.s_isl_cstart[bx + is];
+        for (int o = 16; o > 0; o >>= 1) psolved += __shfl_xor_sync(0xffffffffu, psolved, o);
+        if (lane == 0) wd.acc_psolve += (unsigned long long)psolved;
+        bool remaining = false;
+        for (int is = lane; is < nIsl; is += kWarp) {
+            int f = x.s_isl_flags[b0 + is];
+            if (f & 1) continue;
+            bool contactsOkay = funkey(x.s_isl_minsep[b0 + is]) >= -3.0f * kLinearSlop;
+            bool jointsOkay = (f & 4) == 0;
+            if (contactsOkay && jointsOkay) x.s_isl_flags[b0 + is] = f | 1 | 2;
+            else remaining = true;
+        }
+        if (!__any_sync(0xffffffffu, remaining)) break;
+        tsync();
+    }
+    tsync();
+    // copy back: SynchronizeTransform (b2island.d:227-235)
+    for (int i = lane; i < nbI; i += kWarp) b_sync_transform(x.bs[x.s_isl_body[b0 + i]]);
+    tsync();
+    // sleep (b2island.d:241-279)
+    if (x.allow_sleep) {
+        const float linTolSqr = kLinearSleepTolerance * kLinearSleepTolerance;
+        const float angTolSqr = kAngularSleepTolerance * kAngularSleepTolerance;
+        for (int is = lane; is < nIsl; is += kWarp) x.s_isl_sleep[b0 + is] = fkey(kMaxFloat);
+        tsync();
+        for (int i = lane; i < nbI; i += kWarp) {
+            int b = x.s_isl_body[b0 + i];
+            dbox_body_state& B = x.bs[b];
+            int is = x.s_body_island[b];
+            if ((B.flags & kBodyAutoSleep) == 0 || B.vel[2] * B.vel[2] > angTolSqr ||
+                dot(b_v(B), b_v(B)) > linTolSqr) {
+                B.sleep_time = 0.0f;
+                atomicMin(&x.s_isl_sleep[b0 + is], fkey(0.0f));
+            } else {
+                B.sleep_time += h;
+                atomicMin(&x.s_isl_sleep[b0 + is], fkey(B.sleep_time));
+            }
+        }
+        tsync();
+        for (int is = lane; is < nIsl; is += kWarp) {
+            int f = x.s_isl_flags[b0 + is];
+            if (funkey(x.s_isl_sleep[b0 + is]) >= kTimeToSleep && (f & 2)) x.s_isl_flags[b0 + is] = f | 8;
+        }
+        tsync();
+        for (int i = lane; i < nbI; i += kWarp) {
+            int b = x.s_isl_body[b0 + i];
+            if (x.s_isl_flags[b0 + x.s_body_island[b]] & 8) b_set_awake(x.bs[b], false);
+        }
+        // a static body ends in the state its last island left it in
+        for (int i = lane; i < nb; i += kWarp) {
+            int b = b0 + i;
+            if (x.bs[b].type == kStaticBody && x.s_body_island[b] >= 0 &&
+                (x.s_isl_flags[b0 + x.s_body_island[b]] & 8))
+                b_set_awake(x.bs[b], false);
+        }
+    }
+    tsync();
+    // SynchronizeFixtures for bodies that were in an island (b2world.d:1099-1116)
+    for (int i = lane; i < nb; i += kWarp) {
+        int b = b0 + i;
+        if ((x.bs[b].flags & kBodyIsland) == 0) continue;
+        if (x.bs[b].type == kStaticBody) continue;
+        sync_fixtures(x, b);
+    }
+    tsync();
+    hash_rebuild(x, w);
+    find_new_contacts(x, w);
+}
+
+// ------------------------------------------------------------ TOI
+// contact needs a fresh TOI (b2world.d:1159-1210)
+DG bool toi_needs(const Ctx& x, const dbox_contact_state& c) {
+    if ((c.flags & kContactEnabled) == 0) return false;
+    if (c.toi_count > kMaxSubSteps) return false;
+    if (c.flags & kContactToi) return false;
+    const DFixture& fa = x.fx[c.fixture_a];
+    const DFixture& fb = x.fx[c.fixture_b];
+    if (fa.sensor || fb.sensor) return false;
+    const dbox_body_state& bA = x.bs[fa.body];
+    const dbox_body_state& bB = x.bs[fb.body];
+    bool activeA = (bA.flags & kBodyAwake) && bA.type != kStaticBody;
+    bool activeB = (bB.flags & kBodyAwake) && bB.type != kStaticBody;
+    if (!activeA && !activeB) return false;
+    bool collideA = (bA.flags & kBodyBullet) || bA.type != kDynamicBody;
+    bool collideB = (bB.flags & kBodyBullet) || bB.type != kDynamicBody;
+    if (!collideA && !collideB) return false;
+    return true;
+}
+
+// b2Contact.Update inside the TOI loop: wakes are applied immediately
+DG void toi_update(const Ctx& x, dbox_contact_state& c) {
+    if (contact_update(x, c)) {
+        b_set_awake(x.bs[x.fx[c.fixture_a].body], true);
+        b_set_awake(x.bs[x.fx[c.fixture_b].body], true);
+    }
+}
+
+// b2Island.SolveTOI (b2island.d:282-416) on the sub-island in s_isl_body / s_isl_contact; one lane.
+DG void solve_toi_island(const Ctx& x, const WorldInfo& wi, int nbI, int ncI, int toiA, int toiB, float subDt) {
+    int b0 = wi.body_start, c0 = wi.contact_start;
+    for (int t = 0; t < ncI; ++t) constraint_ctor(x, x.s_isl_contact[c0 + t], false, 1.0f);
+    for (int it = 0; it < 20; ++it) {
+        float minSep = 0.0f;
+        for (int t = 0; t < ncI; ++t) minSep = bmin(minSep, solve_position(x, x.s_isl_contact[c0 + t], true, toiA, toiB));
+        if (minSep >= -1.5f * kLinearSlop) break;
+    }
+    dbox_body_state& A = x.bs[toiA];
+    dbox_body_state& B = x.bs[toiB];
+    A.sweep[2] = A.sweep[4]; A.sweep[3] = A.sweep[5]; A.sweep[6] = A.sweep[7];
+    B.sweep[2] = B.sweep[4]; B.sweep[3] = B.sweep[5]; B.sweep[6] = B.sweep[7];
+    for (int t = 0; t < ncI; ++t) constraint_init_velocity(x, x.s_isl_contact[c0 + t]);
+    for (int it = 0; it < x.vel_iters; ++it)
+        for (int t = 0; t < ncI; ++t) solve_velocity(x, x.s_isl_contact[c0 + t]);
+    float h = subDt;
+    for (int i = 0; i < nbI; ++i) {
+        dbox_body_state& Bd = x.bs[x.s_isl_body[b0 + i]];
+        float2 c = b_c(Bd);
+        float a = Bd.sweep[7];
+        float2 v = b_v(Bd);
+        float wv = Bd.vel[2];
+        float2 translation = h * v;
+        if (dot(translation, translation) > kMaxTranslationSquared) {
+            float ratio = fdiv(kMaxTranslation, length(translation));
+            v *= ratio;
+        }
+        float rotation = h * wv;
+        if (rotation * rotation > kMaxRotationSquared) {
+            float ratio = fdiv(kMaxRotation, babs(rotation));
+            wv *= ratio;
+        }
+        c += h * v;
+        a += h * wv;
+        Bd.sweep[4] = c.x; Bd.sweep[5] = c.y; Bd.sweep[7] = a;
+        Bd.vel[0] = v.x; Bd.vel[1] = v.y; Bd.vel[2] = wv;
+        b_sync_transform(Bd);
+    }
+}
+
+__global__ void k_toi(Ctx x) {
+    int w = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+    if (w >= x.W) return;
+    const WorldInfo& wi = x.wi[w];
+    WorldDyn& wd = x.wd[w];
+    int lane = lane_id();
+    const int b0 = wi.body_start, nb = wi.body_count, c0 = wi.contact_start;
+    if (x.continuous && x.dt > 0.0f) {
+        bool advanced = wd.step_complete == 0;
+        if (wd.step_complete) {                                          // b2world.d:1131-1146
+            for (int i = lane; i < nb; i += kWarp) {
+                x.bs[b0 + i].flags &= ~(uint32_t)kBodyIsland;
+                x.bs[b0 + i].sweep[8] = 0.0f;
+            }
+            int n = wd.contact_count;
+            for (int k = lane; k < n; k += kWarp) {
+                dbox_contact_state& c = x.ct[c0 + k];
+                c.flags &= ~(uint32_t)(kContactToi | kContactIsland);
+                c.toi_count = 0;
+                c.toi = 1.0f;
+            }
+        }
+        tsync();
+        int events = 0;
+        for (int iter = 0;; ++iter) {
+            if (iter >= kMaxToiLoop) {
+                if (lane == 0) set_error(x, w, DBOX_ERR_TIMEOUT);
+                break;
+            }
+            int n = wd.contact_count;
+            // sweeps are put onto a common time in list order (b2world.d:1212-1226)
+            if (advanced && lane == 0) {
+                for (int k = n - 1; k >= 0; --k) {
+                    const dbox_contact_state& c = x.ct[c0 + k];
+                    if (!toi_needs(x, c)) continue;
+                    dbox_body_state& bA = x.bs[x.fx[c.fixture_a].body];
+                    dbox_body_state& bB = x.bs[x.fx[c.fixture_b].body];
+                    float alpha0 = bA.sweep[8];
+                    if (bA.sweep[8] < bB.sweep[8]) {
+                        alpha0 = bB.sweep[8];
+                        Sweep s = b_sweep(bA); sweep_advance(s, alpha0); b_set_sweep(bA, s);
+                    } else if (bB.sweep[8] < bA.sweep[8]) {
+                        alpha0 = bA.sweep[8];
+                        Sweep s = b_sweep(bB); sweep_advance(s, alpha0); b_set_sweep(bB, s);
+                    }
+                    SweepSnap& sn = x.snap[c0 + k];
+                    sn.a = b_sweep(bA);
+                    sn.b = b_sweep(bB);
+                    sn.alpha0 = alpha0;
+                }
+            }
+            tsync();
+            for (int k = lane; k < n; k += kWarp) {
+                dbox_contact_state& c = x.ct[c0 + k];
+                if (!toi_needs(x, c)) continue;
+                const DFixture& fa = x.fx[c.fixture_a];
+                const DFixture& fb = x.fx[c.fixture_b];
+                Sweep sA, sB;
+                float alpha0;
+                if (advanced) { sA = x.snap[c0 + k].a; sB = x.snap[c0 + k].b; alpha0 = x.snap[c0 + k].alpha0; }
+                else { sA = b_sweep(x.bs[fa.body]); sB = b_sweep(x.bs[fb.body]); alpha0 = sA.alpha0; }
+                float beta;
+                int state = time_of_impact(make_proxy(fa), make_proxy(fb), sA, sB, 1.0f, &beta);
+                float alpha = state == kToiTouching ? bmin(alpha0 + (1.0f - alpha0) * beta, 1.0f) : 1.0f;
+                c.toi = alpha;
+                c.flags |= kContactToi;
+            }
+            tsync();
+            // minimum TOI, first in list order on ties
+            float bestA = 1.0f;
+            int bestLp = 0x7fffffff;
+            for (int k = lane; k < n; k += kWarp) {
+                const dbox_contact_state& c = x.ct[c0 + k];
+                if ((c.flags & kContactEnabled) == 0 || c.toi_count > kMaxSubSteps) continue;
+                if ((c.flags & kContactToi) == 0) continue;
+                int lp = n - 1 - k;
+                if (c.toi < bestA || (c.toi == bestA && lp < bestLp && c.toi < 1.0f)) { bestA = c.toi; bestLp = lp; }
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                float oa = __shfl_xor_sync(0xffffffffu, bestA, o);
+                int ol = __shfl_xor_sync(0xffffffffu, bestLp, o);
+                if (oa < bestA || (oa == bestA && ol < bestLp)) { bestA = oa; bestLp = ol; }
+            }
+            if (bestLp == 0x7fffffff || 1.0f - 10.0f * kEpsilon < bestA) {
+                if (lane == 0) wd.step_complete = 1;
+                break;
+            }
+            float minAlpha = bestA;
+            int mk = n - 1 - bestLp;
+            bool solved = false;
+            if (lane == 0) {
+                ++events;
+                dbox_contact_state& mc = x.ct[c0 + mk];
+                int ia = x.fx[mc.fixture_a].body, ib = x.fx[mc.fixture_b].body;
+                dbox_body_state& bA = x.bs[ia];
+                dbox_body_state& bB = x.bs[ib];
+                Sweep backup1 = b_sweep(bA), backup2 = b_sweep(bB);
+                b_advance(bA, minAlpha);
+                b_advance(bB, minAlpha);
+                toi_update(x, mc);
+                mc.flags &= ~(uint32_t)kContactToi;
+                ++mc.toi_count;
+                if ((mc.flags & kContactEnabled) == 0 || (mc.flags & kContactTouching) == 0) {
+                    mc.flags &= ~(uint32_t)kContactEnabled;
+                    b_set_sweep(bA, backup1);
+                    b_set_sweep(bB, backup2);
+                    b_sync_transform(bA);
+                    b_sync_transform(bB);
+                } else {
+                    solved = true;
+                    b_set_awake(bA, true);
+                    b_set_awake(bB, true);
+                    int nbI = 0, ncI = 0;
+                    x.s_isl_body[b0 + nbI++] = ia;
+                    x.s_isl_body[b0 + nbI++] = ib;
+                    x.s_isl_contact[c0 + ncI++] = c0 + mk;
+                    bA.flags |= kBodyIsland;
+                    bB.flags |= kBodyIsland;
+                    mc.flags |= kContactIsland;
+                    int pair[2] = {ia, ib};
+                    for (int q = 0; q < 2; ++q) {
+                        int body = pair[q];
+                        dbox_body_state& Bd = x.bs[body];
+                        if (Bd.type != kDynamicBody) continue;
+                        for (int k = n - 1; k >= 0; --k) {
+                            dbox_contact_state& c = x.ct[c0 + k];
+                            int fA = x.fx[c.fixture_a].body, fB = x.fx[c.fixture_b].body;
+                            if (fA != body && fB != body) continue;
+                            if (nbI == 2 * kMaxTOIContacts) break;
+                            if (ncI == kMaxTOIContacts) break;
+                            if (c.flags & kContactIsland) continue;
+                            int other = fA == body ? fB : fA;
+                            dbox_body_state& O = x.bs[other];
+                            if (O.type == kDynamicBody && (Bd.flags & kBodyBullet) == 0 && (O.flags & kBodyBullet) == 0) continue;
+                            if (x.fx[c.fixture_a].sensor || x.fx[c.fixture_b].sensor) continue;
+                            Sweep backup = b_sweep(O);
+                            if ((O.flags & kBodyIsland) == 0) b_advance(O, minAlpha);
+                            toi_update(x, c);
+                            if ((c.flags & kContactEnabled) == 0 || (c.flags & kContactTouching) == 0) {
+                                b_set_sweep(O, backup);
+                                b_sync_transform(O);
+                                continue;
+                            }
+                            c.flags |= kContactIsland;
+                            x.s_isl_contact[c0 + ncI++] = c0 + k;
+                            if (O.flags & kBodyIsland) continue;
+                            O.flags |= kBodyIsland;
+                            if (O.type != kStaticBody) b_set_awake(O, true);
+                            x.s_isl_body[b0 + nbI++] = other;
+                        }
+                    }
+                    float subDt = (1.0f - minAlpha) * x.dt;
+                    solve_toi_island(x, wi, nbI, ncI, ia, ib, subDt);
+                    for (int i = 0; i < nbI; ++i) {
+                        int body = x.s_isl_body[b0 + i];
+                        dbox_body_state& Bd = x.bs[body];
+                        Bd.flags &= ~(uint32_t)kBodyIsland;
+                        if (Bd.type != kDynamicBody) continue;
+                        sync_fixtures(x, body);
+                        for (int k = 0; k < n; ++k) {
+                            dbox_contact_state& c = x.ct[c0 + k];
+                            if (x.fx[c.fixture_a].body == body || x.fx[c.fixture_b].body == body)
+                                c.flags &= ~(uint32_t)(kContactToi | kContactIsland);
+                        }
+                    }
+                }
+            }
+            solved = __shfl_sync(0xffffffffu, solved, 0);
+            tsync();
+            advanced = true;
+            if (solved) {
+                find_new_contacts(x, w);
+                if (x.sub_stepping) {
+                    if (lane == 0) wd.step_complete = 0;
+                    break;
+                }
+            }
+        }
+        if (lane == 0) { wd.toi_events = events; wd.acc_toi_events += (unsigned long long)events; }
+    }
+    tsync();
+    // b2World.Step epilogue (b2world.d:421-429)
+    if (lane == 0 && x.dt > 0.0f) wd.inv_dt0 = x.inv_dt;
+    if (wd.flags & 4u) {
+        for (int i = lane; i < nb; i += kWarp) {
+            dbox_body_state& B = x.bs[b0 + i];
+            B.force[0] = 0.0f; B.force[1] = 0.0f; B.force[2] = 0.0f;
+        }
+    }
+}
+
+}  // namespace dg
+
+// ------------------------------------------------------------ launch entry points (called from api.cpp)
+// Launch one step.  ev, when not NULL, holds 4 events recorded at the phase
+// boundaries: [0] before Collide, [1] before Solve, [2] before SolveTOI, [3] after.
+extern "C" int dbox_launch_step_ev(const dg::Ctx* x, cudaStream_t stream, int* launches, cudaEvent_t* ev) {
+    const int threads = 128;                       // four worlds per block, one warp each
+    int team_blocks = (x->W * dg::kWarp + threads - 1) / threads;
+    int flat_blocks = (x->total_contacts + 255) / 256;
+    if (flat_blocks < 1) flat_blocks = 1;
+    if (flat_blocks > 152 * 16) flat_blocks = 152 * 16;
+    if (ev) cudaEventRecord(ev[0], stream);
+    dg::k_step_begin<<<team_blocks, threads, 0, stream>>>(*x);
+    dg::k_collide<<<flat_blocks, 256, 0, stream>>>(*x);
+    dg::k_collide_finish<<<team_blocks, threads, 0, stream>>>(*x);
+    if (ev) cudaEventRecord(ev[1], stream);
+    dg::k_solve<<<team_blocks, threads, 0, stream>>>(*x);
+    if (ev) cudaEventRecord(ev[2], stream);
+    dg::k_toi<<<team_blocks, threads, 0, stream>>>(*x);
+    if (ev) cudaEventRecord(ev[3], stream);
+    if (launches) *launches = 5;
+    return (int)cudaGetLastError();
+}
+
+extern "C" int dbox_launch_step(const dg::Ctx* x, cudaStream_t stream, int* launches) {
+    return dbox_launch_step_ev(x, stream, launches, nullptr);
+}
+
+// ------------------------------------------------------------ bulk host I/O
+namespace dg {
+// b2Body.GetPosition / GetAngle for every body: (x, y, angle) triples
+__global__ void k_gather_transforms(int n, const dbox_body_state* bs, float* out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        out[3 * i + 0] = bs[i].xf[0];
+        out[3 * i + 1] = bs[i].xf[1];
+        out[3 * i + 2] = bs[i].sweep[7];
+    }
+}
+// b2Body.ApplyForceToCenter + ApplyTorque with wake = false (b2body.d:360-420): accumulate on awake dynamic bodies
+__global__ void k_apply_forces(int n, dbox_body_state* bs, const float* f) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        dbox_body_state& b = bs[i];
+        if (b.type != kDynamicBody || (b.flags & kBodyAwake) == 0) continue;
+        b.force[0] += f[3 * i + 0];
+        b.force[1] += f[3 * i + 1];
+        b.force[2] += f[3 * i + 2];
+    }
+}
+}  // namespace dg
+
+extern "C" int dbox_launch_gather_transforms(int n, const dbox_body_state* bs, float* out, cudaStream_t s) {
+    if (n <= 0) return 0;
+    int blocks = (n + 255) / 256;
+    if (blocks > 152 * 8) blocks = 152 * 8;
+    dg::k_gather_transforms<<<blocks, 256, 0, s>>>(n, bs, out);
+    return (int)cudaGetLastError();
+}
+extern "C" int dbox_launch_apply_forces(int n, dbox_body_state* bs, const float* f, cudaStream_t s) {
+    if (n <= 0) return 0;
+    int blocks = (n + 255) / 256;
+    if (blocks > 152 * 8) blocks = 152 * 8;
+    dg::k_apply_forces<<<blocks, 256, 0, s>>>(n, bs, f);
+    return (int)cudaGetLastError();
+}
+
+// ------------------------------------------------------------ standalone narrowphase
+namespace dg {
+// One thread per shape pair: the manifold of b2CollidePolygons / b2CollidePolygonAndCircle /
+// b2CollideCircles (fixture a must be the polygon of a mixed pair).
+__global__ void k_collide_pairs(int n, const DFixture* fa, const float4* xa, const DFixture* fb, const float4* xb,
+                                dbox_contact_state* out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        Xf A, B;
+        float4 a = xa[i], b = xb[i];
+        A.p = v2(a.x, a.y); A.q.s = a.z; A.q.c = a.w;
+        B.p = v2(b.x, b.y); B.q.s = b.z; B.q.c = b.w;
+        Manifold m;
+        manifold_load(out[i], m);
+        evaluate_manifold(m, fa[i], A, fb[i], B);
+        manifold_store(m, out[i]);
+    }
+}
+}  // namespace dg
+
+extern "C" int dbox_launch_collide_pairs(int n, const dg::DFixture* fa, const float4* xa, const dg::DFixture* fb,
+                                         const float4* xb, dbox_contact_state* out, cudaStream_t stream) {
+    int blocks = (n + 127) / 128;
+    if (blocks < 1) blocks = 1;
+    dg::k_collide_pairs<<<blocks, 128, 0, stream>>>(n, fa, xa, fb, xb, out);
+    return (int)cudaGetLastError();
+}

@@ -1,0 +1,235 @@
+// Device-side layout of a batch of b2Worlds (structure of arrays over all worlds).
+//
+// Bodies, fixtures (= broad-phase proxies), joints and contact slots of world w
+// occupy contiguous index ranges given by WorldInfo.  Within a world:
+//  * bodies are in creation order; the reference's body list (head-inserted,
+//    b2world.d:88-96) is the reverse, so list walks run from the last index down;
+//  * fixtures are in creation order; with create-only worlds the dynamic-tree
+//    proxy id of the k-th proxy is 0 for k = 0 and 2k-1 otherwise
+//    (b2dynamictree.d:516-564: each leaf insertion also allocates one parent), so
+//    sorting pairs by fixture index equals b2PairLessThan order;
+//  * contacts are kept oldest first; the world contact list and every body's
+//    edge list are head-inserted (b2contactmanager.d:131-166), so list order is
+//    descending slot index.
+#pragma once
+
+#include <stdint.h>
+#include "dmath.cuh"
+
+namespace dg {
+
+struct WorldInfo {
+    int body_start, body_count;
+    int fix_start, fix_count;
+    int joint_start, joint_count;
+    int contact_start, contact_cap;
+    int hash_start, hash_cap;      // open-addressing table of contact fixture pairs (power of two)
+    int pair_start, pair_cap;      // broad-phase pair buffer
+    int bx_start;                  // per-body scratch with one extra entry (body_count + 1)
+    int kx_start;                  // per-constraint scratch (contact_cap + joint_count + 2)
+    int snap_start;                // TOI sweep snapshots (contact_cap entries)
+    int pad;
+};
+
+struct WorldDyn {
+    int contact_count;
+    uint32_t flags;                // b2World.m_flags (e_newFixture 1, e_clearForces 4)
+    int step_complete;
+    float inv_dt0;
+    int error;                     // DBOX_ERR_* of the last step (0 = ok)
+    int islands;                   // islands solved in the last step
+    int toi_events;                // TOI events in the last step
+    int pad;
+    // cumulative work counters (never reset on the device; the host takes differences)
+    unsigned long long acc_isl_bodies;   // bodies integrated in islands
+    unsigned long long acc_isl_contacts; // contact constraints built
+    unsigned long long acc_vsolve;       // contact velocity solves
+    unsigned long long acc_psolve;       // contact position solves
+    unsigned long long acc_contacts;     // live contacts seen by Collide
+    unsigned long long acc_toi_events;
+    unsigned long long acc_steps;
+    unsigned long long acc_pairs;        // broad-phase pairs emitted
+};
+
+struct BodyStatic {
+    float lin_damping, ang_damping, gravity_scale;
+    int world;
+    int fix_start, fix_count;      // into Ctx.body_fix
+    int jadj_start, jadj_count;    // into Ctx.jadj_joint / jadj_other (descending joint index)
+};
+
+struct DJoint {                    // b2RevoluteJoint (joints/b2revolutejoint.d)
+    int body_a, body_b;
+    int collide_connected;
+    int island_flag;
+    float2 local_anchor_a, local_anchor_b;
+    float reference_angle;
+    int enable_limit;
+    float lower_angle, upper_angle;
+    int enable_motor;
+    float motor_speed, max_motor_torque;
+    float impulse[3];
+    float motor_impulse;
+    int limit_state;
+    float2 rA, rB, lcA, lcB;
+    float invMassA, invMassB, invIA, invIB;
+    float mass[9];                 // ex.x ex.y ex.z ey.x ey.y ey.z ez.x ez.y ez.z
+    float motor_mass;
+    int pad;
+};
+
+// b2ContactVelocityConstraint (contacts/b2contactsolver.d:43-58) with body indices in place of island indices.
+struct VPoint { float2 rA, rB; float normalImpulse, tangentImpulse, normalMass, tangentMass, velocityBias; };
+struct VC {
+    VPoint p[2];
+    float2 normal;
+    float K[4];         // ex.x ex.y ey.x ey.y
+    float NM[4];        // normalMass
+    int bodyA, bodyB;
+    float invMassA, invMassB, invIA, invIB;
+    float friction, restitution, tangentSpeed;
+    int pointCount;
+};
+// b2ContactPositionConstraint (b2contactsolver.d:801-814)
+struct PC {
+    float2 localPoints[2];
+    float2 localNormal, localPoint;
+    float2 lcA, lcB;
+    int bodyA, bodyB;
+    float invMassA, invMassB, invIA, invIB;
+    int type;
+    float radiusA, radiusB;
+    int pointCount;
+};
+
+// TOI sweep snapshot of one contact's two bodies (taken in list order).
+struct SweepSnap { Sweep a, b; float alpha0; int pad; };
+
+struct Ctx {
+    int W;
+    int total_bodies, total_fixtures, total_contacts, total_joints;
+    const WorldInfo* wi;
+    WorldDyn* wd;
+    // bodies
+    dbox_body_state* bs;
+    const BodyStatic* bst;
+    const int* body_fix;
+    const int* jadj_joint;
+    const int* jadj_other;
+    // fixtures / proxies
+    const DFixture* fx;
+    dbox_proxy_state* px;
+    // joints
+    DJoint* jt;
+    // contacts
+    dbox_contact_state* ct;
+    const int* c_world;            // world of each contact slot
+    unsigned long long* hash;      // contact pair table
+    int2* pairs;
+    // scratch (body-indexed)
+    int* s_woken;                  // smallest contact-list position that woke the body this Collide
+    int* s_adj_start;              // bx-indexed, body_count+1 per world
+    int* s_cursor;                 // body-indexed
+    int* s_stack;                  // body-indexed
+    int* s_isl_body;               // body-indexed (world-relative positions)
+    int* s_body_island;            // body-indexed
+    int* s_last;                   // body-indexed
+    int* s_isl_bstart;             // bx-indexed: island -> start in s_isl_body
+    int* s_isl_cstart;             // bx-indexed
+    int* s_isl_jstart;             // bx-indexed
+    unsigned* s_isl_minsep;        // body-indexed (island id), ordered-float key
+    int* s_isl_flags;              // body-indexed (island id): bit0 done, bit1 solved, bit2 joints not ok
+    unsigned* s_isl_sleep;         // body-indexed (island id)
+    int* s_pcount;                 // fixture-indexed: pair counts / moved list
+    int* s_moved;                  // fixture-indexed
+    // scratch (contact-indexed)
+    int* s_cstate;                 // 0 processed, 1 inactive, 2 destroyed
+    int* s_adj_items;              // 2 per contact slot
+    int* s_isl_contact;            // contact-slot-indexed
+    int* s_level;                  // kx-indexed
+    int* s_sched_v;                // kx-indexed
+    int* s_lvl_v;                  // kx-indexed (+1)
+    int* s_sched_p;
+    int* s_lvl_p;
+    int* s_tmp;                    // kx-indexed sequence-order items while sorting by level
+    int* s_isl_joint;              // joint-indexed
+    int* s_accept;                 // pair-indexed
+    VC* vc;                        // contact-slot-indexed
+    PC* pc;                        // contact-slot-indexed
+    SweepSnap* snap;               // contact-slot-indexed
+    // step parameters
+    float dt, inv_dt;
+    int vel_iters, pos_iters;
+    float2 gravity;
+    int warm_starting, continuous, sub_stepping, allow_sleep;
+    int record_events;
+    int* g_status;                 // bit (-code) set for every DBOX_ERR_* raised by any world
+};
+
+// ------------------------------------------------------------ body state helpers (dbox_body_state fields)
+DG int btype(const dbox_body_state& b) { return b.type; }
+DG float2 b_c(const dbox_body_state& b) { return v2(b.sweep[4], b.sweep[5]); }
+DG float2 b_lc(const dbox_body_state& b) { return v2(b.sweep[0], b.sweep[1]); }
+DG float2 b_v(const dbox_body_state& b) { return v2(b.vel[0], b.vel[1]); }
+DG Xf b_xf(const dbox_body_state& b) { Xf x; x.p = v2(b.xf[0], b.xf[1]); x.q.s = b.xf[2]; x.q.c = b.xf[3]; return x; }
+DG Sweep b_sweep(const dbox_body_state& b) {
+    Sweep s;
+    s.lc = v2(b.sweep[0], b.sweep[1]);
+    s.c0 = v2(b.sweep[2], b.sweep[3]);
+    s.c = v2(b.sweep[4], b.sweep[5]);
+    s.a0 = b.sweep[6];
+    s.a = b.sweep[7];
+    s.alpha0 = b.sweep[8];
+    return s;
+}
+DG void b_set_sweep(dbox_body_state& b, const Sweep& s) {
+    b.sweep[0] = s.lc.x; b.sweep[1] = s.lc.y;
+    b.sweep[2] = s.c0.x; b.sweep[3] = s.c0.y;
+    b.sweep[4] = s.c.x; b.sweep[5] = s.c.y;
+    b.sweep[6] = s.a0; b.sweep[7] = s.a; b.sweep[8] = s.alpha0;
+}
+// b2Body.SynchronizeTransform (b2body.d:1143-1147)
+DG void b_sync_transform(dbox_body_state& b) {
+    Rot q = rot(b.sweep[7]);
+    float2 p = v2(b.sweep[4], b.sweep[5]) - mul(q, v2(b.sweep[0], b.sweep[1]));
+    b.xf[0] = p.x; b.xf[1] = p.y; b.xf[2] = q.s; b.xf[3] = q.c;
+}
+// b2Body.SetAwake (b2body.d:827-846)
+DG void b_set_awake(dbox_body_state& b, bool flag) {
+    if (flag) {
+        if ((b.flags & kBodyAwake) == 0) { b.flags |= kBodyAwake; b.sleep_time = 0.0f; }
+    } else {
+        b.flags &= ~(uint32_t)kBodyAwake;
+        b.sleep_time = 0.0f;
+        b.vel[0] = 0.0f; b.vel[1] = 0.0f; b.vel[2] = 0.0f;
+        b.force[0] = 0.0f; b.force[1] = 0.0f; b.force[2] = 0.0f;
+    }
+}
+// b2Body.Advance (b2body.d:1172-1180)
+DG void b_advance(dbox_body_state& b, float alpha) {
+    Sweep s = b_sweep(b);
+    sweep_advance(s, alpha);
+    s.c = s.c0;
+    s.a = s.a0;
+    b_set_sweep(b, s);
+    Rot q = rot(s.a);
+    float2 p = s.c - mul(q, s.lc);
+    b.xf[0] = p.x; b.xf[1] = p.y; b.xf[2] = q.s; b.xf[3] = q.c;
+}
+
+// ordered key of a float for unsigned atomicMin
+DG unsigned fkey(float f) {
+    unsigned u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+DG float funkey(unsigned k) {
+    unsigned u = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
+    return __uint_as_float(u);
+}
+
+DG void set_error(const Ctx& x, int w, int code) {
+    atomicCAS(&x.wd[w].error, 0, code);
+    atomicOr(x.g_status, 1 << (-code));
+}
+
+}  // namespace dg

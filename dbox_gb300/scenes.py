@@ -12,7 +12,8 @@ Workloads (sizes as named in the benchmark configuration):
               with a box ground); density 1, friction 0.6.
   scatter   - static container of 4 box walls; n dynamic bodies, half circles
               (r ~ U[0.25,0.5]) and half convex polygons (3..8 points at sorted
-              angles U[0, 2pi), radius U[0.3,0.6], hull by b2PolygonShape.Set) on
+              angles U[0, 2pi) conditioned on gaps in (0.25, pi) rad, radius
+              U[0.3,0.6], hull by b2PolygonShape.Set) on
               a jittered grid (spacing 1.3 m, jitter U[-0.1,0.1]), friction
               U[0.2,0.8], velocity N(0,1) per axis.
   stacks    - ground box plus columns of unit boxes 1..30 high.
@@ -134,7 +135,13 @@ def scatter(n, width, height, rng, spacing=1.3, jitter=0.1, y_base=1.0):
     sh["kind"][poly] = abi.SHAPE_POLYGON
     for i in poly:
         k = int(rng.integers(3, 9))
-        ang = np.sort(rng.uniform(0.0, 2.0 * math.pi, size=k))
+        while True:
+            # rejection sampling keeps b2PolygonShape.Set away from welded / sliver hulls:
+            # every gap between sorted angles above 0.25 rad, the largest below pi
+            ang = np.sort(rng.uniform(0.0, 2.0 * math.pi, size=k))
+            gaps = np.diff(np.concatenate([ang, ang[:1] + 2.0 * math.pi]))
+            if gaps.min() > 0.25 and gaps.max() < math.pi:
+                break
         r = rng.uniform(0.3, 0.6)
         sh["count"][i] = k
         sh["vertices"][i, :k, 0] = (r * np.cos(ang)).astype(F32)

@@ -251,6 +251,38 @@ int32_t dbox_world_import_state(dbox_world* w, int32_t world, const dbox_world_h
 /* b2World.GetProfile (b2world.d:789-792): phase times of the last step, summed over worlds. */
 int32_t dbox_world_get_profile(dbox_world* w, dbox_profile* out);
 
+/* `steps` steps captured once into one CUDA graph with CUDA events at the phase
+ * boundaries of every step; the graph is launched once and waited for.  total_ms
+ * receives the device time of all steps, phase_ms[3] the summed time of Collide
+ * (+ new-fixture pairs), Solve (islands, solver, broad-phase) and SolveTOI. */
+int32_t dbox_world_step_n_timed(dbox_world* w, float dt, int32_t velocity_iterations, int32_t position_iterations,
+                                int32_t steps, float* total_ms, float* phase_ms);
+
+/* Cumulative device work counters summed over worlds: out[8] = island bodies integrated,
+ * contact constraints built, contact velocity solves, contact position solves, contacts
+ * processed by Collide, TOI events, world-steps, broad-phase pairs. */
+int32_t dbox_world_get_counters(dbox_world* w, unsigned long long* out);
+
+/* b2Body.ApplyForceToCenter + b2Body.ApplyTorque with wake = false (b2body.d:360-420) for every
+ * body of every world: force_torque holds (fx, fy, torque) per body in (world, body id) order. */
+int32_t dbox_world_apply_forces(dbox_world* w, const float* force_torque);
+
+/* b2Body.GetPosition + b2Body.GetAngle (b2body.d:283-296) for every body: (x, y, angle) per body. */
+int32_t dbox_world_get_transforms(dbox_world* w, float* xya);
+
+/* Wait for all queued device work of the handle. */
+int32_t dbox_world_sync(dbox_world* w);
+
+/* Islands solved and TOI events handled by world `world` in the last step. */
+int32_t dbox_world_step_stats(dbox_world* w, int32_t world, int32_t* islands, int32_t* toi_events);
+
+/* Narrowphase alone: the manifolds of n shape pairs at transforms xf = (p.x, p.y, sin, cos), 4 floats
+ * per pair, computed on the GPU (b2CollidePolygons collision/b2collidepolygon.d:127-254,
+ * b2CollidePolygonAndCircle / b2CollideCircles collision/b2collidecircle.d:29-164).  For a
+ * polygon-circle pair the polygon is shape_a.  Only the manifold fields of out are written. */
+int32_t dbox_collide_manifolds(int32_t n, const dbox_shape_def* shape_a, const float* xf_a,
+                               const dbox_shape_def* shape_b, const float* xf_b, dbox_contact_state* out);
+
 /* Device kernels launched by the last step (for launch accounting). */
 int32_t dbox_world_last_launches(dbox_world* w, int32_t* out);
 

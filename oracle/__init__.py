@@ -56,6 +56,7 @@ def lib():
         L.orc_world_last_islands.argtypes = [vp]
         L.orc_set_trig_mode.argtypes = [i32]
         L.orc_sincos.argtypes = [f32, ctypes.POINTER(f32), ctypes.POINTER(f32)]
+        L.orc_sincos_array.argtypes = [i32, vp, vp, vp]
         L.orc_polygon_set.argtypes = [vp, i32, vp, vp, vp]
         L.orc_collide.argtypes = [vp, vp, vp, vp, vp]
         _lib = L
@@ -71,6 +72,27 @@ def sincos(a):
     s, c = ctypes.c_float(), ctypes.c_float()
     lib().orc_sincos(ctypes.c_float(a), ctypes.byref(s), ctypes.byref(c))
     return s.value, c.value
+
+
+def sincos_array(a):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    s = np.zeros_like(a)
+    c = np.zeros_like(a)
+    lib().orc_sincos_array(len(a), abi.ptr(a), abi.ptr(s), abi.ptr(c))
+    return s, c
+
+
+def collide(shape_a, xf_a, shape_b, xf_b):
+    """Narrowphase manifold of two shapes (records of abi.SHAPE_DEF) at transforms (p.x, p.y, sin, cos)."""
+    sa = np.ascontiguousarray(np.array([shape_a], abi.SHAPE_DEF))
+    sb = np.ascontiguousarray(np.array([shape_b], abi.SHAPE_DEF))
+    xa = np.ascontiguousarray(xf_a, dtype=np.float32)
+    xb = np.ascontiguousarray(xf_b, dtype=np.float32)
+    out = np.zeros(1, abi.CONTACT_STATE)
+    n = lib().orc_collide(abi.ptr(sa), abi.ptr(xa), abi.ptr(sb), abi.ptr(xb), abi.ptr(out))
+    if n < 0:
+        raise ValueError("unsupported shape pair")
+    return out[0]
 
 
 class OracleWorld:

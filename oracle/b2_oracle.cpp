@@ -3250,6 +3250,10 @@ int orc_get_trig_mode(void) { return g_trig_mode; }
 
 void orc_sincos(float a, float* s, float* c) { SinCos(a, s, c); }
 
+void orc_sincos_array(int n, const float* a, float* s, float* c) {
+    for (int i = 0; i < n; ++i) SinCos(a[i], s + i, c + i);
+}
+
 orc_world* orc_world_create(float gx, float gy) {
     orc_world* w = new orc_world();
     w->w.gravity = Vec2(gx, gy);

@@ -64,6 +64,7 @@ int orc_collide(const dbox_shape_def* a, const float* xfa, const dbox_shape_def*
 
 /* sin/cos through the selected trig mode */
 void orc_sincos(float a, float* s, float* c);
+void orc_sincos_array(int n, const float* a, float* s, float* c);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,105 @@
+"""GPU step parity against the CPU oracle (b2World.Step restated on the CPU).
+
+Bit-exact cases run the oracle with the portable sin/cos (dbox_sincosf), which
+the GPU library also uses; every exported field must then match to the bit on
+every step.  The reference-arithmetic cases run the oracle with the host libm
+sinf/cosf (as the reference does), re-seed the GPU from the oracle's state
+before each step and require: identical pair set, contact list order, point
+counts and feature ids, and body state within 1e-5 m, 1e-5 rad, 1e-4 m/s.
+"""
+import numpy as np
+import pytest
+
+from compare import body_error, exact_diff, structure_diff
+
+pytestmark = pytest.mark.gpu
+
+
+def _pair(oracle_lib, gpu_lib, scene, flags=None):
+    ow = oracle_lib.OracleWorld(scene, flags)
+    gw = gpu_lib.World(scene, flags=flags)
+    return ow, gw
+
+
+def _run_exact(oracle_lib, gpu_lib, scene, steps, every=1, flags=None, vi=8, pi=3):
+    oracle_lib.set_trig_mode(1)
+    ow, gw = _pair(oracle_lib, gpu_lib, scene, flags)
+    d = exact_diff(ow.export_state(), gw.export_state())
+    assert not d, "creation state differs: %s" % d[:6]
+    for t in range(steps):
+        ow.step(1.0 / 60.0, vi, pi)
+        gw.step(1.0 / 60.0, vi, pi)
+        if (t + 1) % every == 0 or t + 1 == steps:
+            d = exact_diff(ow.export_state(), gw.export_state())
+            assert not d, "step %d: %s" % (t + 1, d[:6])
+    return ow, gw
+
+
+def test_hello_world_exact(oracle_lib, gpu_lib):
+    from dbox_gb300 import scenes
+    _run_exact(oracle_lib, gpu_lib, scenes.hello_world(), 60, vi=6, pi=2)
+
+
+def test_pyramid_600_steps_exact(oracle_lib, gpu_lib):
+    from dbox_gb300 import scenes
+    ow, gw = _run_exact(oracle_lib, gpu_lib, scenes.pyramid(), 600, every=1)
+    st = gw.export_state()
+    assert len(st["contacts"]) > 400
+    assert int(((st["bodies"]["flags"] & 2) == 0).sum()) > 0   # the pyramid fell asleep
+
+
+def test_scatter_exact(oracle_lib, gpu_lib):
+    from dbox_gb300 import scenes
+    s = scenes.scatter(300, 30.0, 40.0, np.random.default_rng(7))
+    _run_exact(oracle_lib, gpu_lib, s, 400, every=5)
+
+
+def test_stacks_exact(oracle_lib, gpu_lib):
+    from dbox_gb300 import scenes
+    _run_exact(oracle_lib, gpu_lib, scenes.stacks(60, 12), 300, every=10)
+
+
+def test_batch_exact(oracle_lib, gpu_lib):
+    from dbox_gb300 import scenes
+    oracle_lib.set_trig_mode(1)
+    worlds = scenes.batch(n_worlds=9, seed=11, lo=8, hi=96)
+    gw = gpu_lib.World(worlds)
+    ows = [oracle_lib.OracleWorld(s) for s in worlds]
+    for t in range(240):
+        gw.step()
+        for ow in ows:
+            ow.step()
+        if (t + 1) % 20 == 0:
+            for i, ow in enumerate(ows):
+                d = exact_diff(ow.export_state(), gw.export_state(i))
+                assert not d, "world %d step %d: %s" % (i, t + 1, d[:6])
+
+
+def test_graph_replay_matches_single_steps(oracle_lib, gpu_lib):
+    from dbox_gb300 import scenes
+    s = scenes.scatter(200, 25.0, 30.0, np.random.default_rng(3))
+    a = gpu_lib.World(s)
+    b = gpu_lib.World(s)
+    a.step(steps=120)
+    b.step(steps=120, graph=True)
+    assert not exact_diff(a.export_state(), b.export_state())
+
+
+def test_pyramid_reference_trig_one_step(oracle_lib, gpu_lib):
+    from dbox_gb300 import scenes
+    oracle_lib.set_trig_mode(0)
+    try:
+        s = scenes.pyramid()
+        ow, gw = _pair(oracle_lib, gpu_lib, s)
+        worst = [0.0, 0.0, 0.0]
+        for t in range(600):
+            gw.import_state(ow.export_state())
+            ow.step()
+            gw.step()
+            a, b = ow.export_state(), gw.export_state()
+            assert not structure_diff(a, b), "step %d: %s" % (t + 1, structure_diff(a, b)[:4])
+            dp, da, dv = body_error(a, b)
+            worst = [max(worst[0], dp), max(worst[1], da), max(worst[2], dv)]
+            assert dp <= 1e-5 and da <= 1e-5 and dv <= 1e-4, "step %d: %s" % (t + 1, (dp, da, dv))
+    finally:
+        oracle_lib.set_trig_mode(1)

@@ -1,0 +1,161 @@
+"""CPU checks of the oracle (the CPU restatement of b2World.Step).
+
+The reference ships no tests or recorded outputs, so the oracle is checked
+against answers derived by hand from the reference's formulas (mass, hull,
+manifold, free fall), against brute force (broad-phase pairs vs. fat-AABB
+overlaps, the analogue of examples/demo/tests/dynamictreetest.d:333) and
+against the committed golden fixtures in tests/golden (regression pins).
+"""
+import math
+
+import numpy as np
+import pytest
+
+from dbox_gb300 import abi, scenes
+
+
+def _box(hx, hy):
+    s = np.zeros((), abi.SHAPE_DEF)
+    s["kind"] = abi.SHAPE_BOX
+    s["hx"] = hx
+    s["hy"] = hy
+    return s
+
+
+def test_portable_trig_is_correctly_rounded(oracle_lib):
+    rng = np.random.default_rng(0)
+    xs = np.concatenate([
+        rng.uniform(-10.0, 10.0, 200000), rng.uniform(-1e4, 1e4, 50000), rng.uniform(-1e30, 1e30, 20000),
+        np.array([0.0, -0.0, 1e-30, np.pi / 2, 1e5, 131071.99, 131072.0], np.float64),
+    ]).astype(np.float32)
+    oracle_lib.set_trig_mode(1)
+    s, c = oracle_lib.sincos_array(xs)
+    ref_s = np.sin(xs.astype(np.float64)).astype(np.float32)
+    ref_c = np.cos(xs.astype(np.float64)).astype(np.float32)
+    assert (s.view(np.uint32) == ref_s.view(np.uint32)).mean() > 1 - 1e-6
+    assert (c.view(np.uint32) == ref_c.view(np.uint32)).mean() > 1 - 1e-6
+    assert np.signbit(s[xs == 0][np.signbit(xs[xs == 0])]).all()   # sin(-0) = -0
+
+
+def test_libm_trig_mode_is_the_host_runtime(oracle_lib):
+    xs = np.linspace(-6.0, 6.0, 1001, dtype=np.float32)
+    oracle_lib.set_trig_mode(0)
+    try:
+        s, c = oracle_lib.sincos_array(xs)
+    finally:
+        oracle_lib.set_trig_mode(1)
+    assert np.allclose(s, np.sin(xs.astype(np.float64)), atol=2e-7)
+    assert np.allclose(c, np.cos(xs.astype(np.float64)), atol=2e-7)
+
+
+def test_polygon_hull_order(oracle_lib):
+    # b2PolygonShape.Set: start at the right-most (then lowest) point, wrap counter-clockwise
+    pts = [(-1, 1), (1, 1), (0.1, 0.2), (1, -1), (-1, -1)]
+    v, n, c = oracle_lib.polygon_set(pts)
+    assert v.tolist() == [[1, -1], [1, 1], [-1, 1], [-1, -1]]
+    assert n.tolist() == [[1, 0], [0, 1], [-1, 0], [0, -1]]
+    assert c.tolist() == [0, 0]
+    assert oracle_lib.polygon_set([(0, 0), (1, 0), (0.001, 0.001)]) is None   # welded to 2 points
+
+
+def test_box_and_circle_mass(oracle_lib):
+    s = scenes.hello_world()
+    st = oracle_lib.OracleWorld(s).export_state()
+    m = st["bodies"]["mass"][1]
+    assert m[0] == np.float32(4.0) and m[1] == np.float32(0.25)           # 2x2 box, density 1
+    assert abs(m[2] - 4.0 * 8.0 / 12.0) < 1e-5                            # m (w^2 + h^2) / 12
+    c = scenes._boxes([(0.0, 5.0)], 1.0, 1.0, abi.DYNAMIC, 0.2, 2.0)
+    c["shapes"]["kind"] = abi.SHAPE_CIRCLE
+    c["shapes"]["radius"] = 0.5
+    mc = oracle_lib.OracleWorld(c).export_state()["bodies"]["mass"][0]
+    assert abs(mc[0] - 2.0 * math.pi * 0.25) < 1e-6
+    assert abs(mc[2] - mc[0] * 0.5 * 0.25) < 1e-6
+
+
+def test_polygon_manifold_known_answer(oracle_lib):
+    # box B resting 0.01 m into box A: reference face is A's top edge (index 2), two points
+    m = oracle_lib.collide(_box(0.5, 0.5), [0, 0, 0, 1], _box(0.5, 0.5), [0, 0.99, 0, 1])
+    assert m["point_count"] == 2 and m["type"] == 1
+    assert m["local_normal"].tolist() == [0.0, 1.0] and m["local_point"].tolist() == [0.0, 0.5]
+    assert m["points"]["local_point"].tolist() == [[-0.5, -0.5], [0.5, -0.5]]
+    # id = indexA | indexB << 8 | typeA << 16 | typeB << 24 with face = 1, vertex = 0
+    assert m["points"]["id"].tolist() == [0x00010002, 0x00010102]
+    far = oracle_lib.collide(_box(0.5, 0.5), [0, 0, 0, 1], _box(0.5, 0.5), [0, 1.03, 0, 1])
+    assert far["point_count"] == 0
+
+
+def test_circle_manifolds_known_answer(oracle_lib):
+    c = np.zeros((), abi.SHAPE_DEF)
+    c["kind"] = abi.SHAPE_CIRCLE
+    c["radius"] = 0.5
+    m = oracle_lib.collide(c, [0, 0, 0, 1], c, [0.9, 0, 0, 1])
+    assert m["point_count"] == 1 and m["type"] == 0 and m["points"]["id"][0] == 0
+    assert oracle_lib.collide(c, [0, 0, 0, 1], c, [1.01, 0, 0, 1])["point_count"] == 0
+    m = oracle_lib.collide(_box(0.5, 0.5), [0, 0, 0, 1], c, [0, 0.95, 0, 1])
+    assert m["point_count"] == 1 and m["type"] == 1
+    assert m["local_normal"].tolist() == [0.0, 1.0]
+
+
+def test_free_fall_matches_float32_recurrence(oracle_lib):
+    s = scenes._boxes([(0.0, 100.0)], 0.5, 0.5, abi.DYNAMIC)
+    w = oracle_lib.OracleWorld(s)
+    h = np.float32(1.0 / 60.0)
+    v = np.float32(0.0)
+    y = np.float32(100.0)
+    for _ in range(120):
+        w.step()
+        v = np.float32(v + np.float32(h * np.float32(np.float32(-10.0) + np.float32(0.0))))
+        y = np.float32(y + np.float32(h * v))
+    b = w.export_state()["bodies"][0]
+    assert b["vel"][1] == v and b["sweep"][5] == y
+
+
+def test_proxy_ids_are_tree_node_ids(oracle_lib):
+    st = oracle_lib.OracleWorld(scenes.pyramid(rows=6)).export_state()
+    k = np.arange(len(st["proxies"]))
+    assert st["proxies"]["proxy_id"].tolist() == np.where(k == 0, 0, 2 * k - 1).tolist()
+
+
+def test_contacts_cover_fat_aabb_overlaps(oracle_lib):
+    # after every step each eligible pair of overlapping fat AABBs has a contact (tree query == brute force)
+    s = scenes.scatter(150, 20.0, 30.0, np.random.default_rng(5))
+    w = oracle_lib.OracleWorld(s)
+    body = s["fixture_body"]
+    dyn = s["bodies"]["type"][body] == abi.DYNAMIC
+    for t in range(80):
+        w.step()
+        if t % 8:
+            continue
+        st = w.export_state()
+        fat = st["proxies"]["fat_aabb"]
+        have = {(min(a, b), max(a, b)) for a, b in zip(st["contacts"]["fixture_a"], st["contacts"]["fixture_b"])}
+        lo, hi = fat[:, :2], fat[:, 2:]
+        ov = ((lo[:, None, :] <= hi[None, :, :]) & (lo[None, :, :] <= hi[:, None, :])).all(-1)
+        ia, ib = np.nonzero(np.triu(ov, 1))
+        for a, b in zip(ia, ib):
+            if body[a] == body[b] or not (dyn[a] or dyn[b]):
+                continue
+            assert (a, b) in have, "step %d: overlapping pair %s without contact" % (t, (a, b))
+
+
+def test_pyramid_settles_and_sleeps(oracle_lib):
+    oracle_lib.set_trig_mode(0)
+    try:
+        w = oracle_lib.OracleWorld(scenes.pyramid())
+        w.step(steps=600)
+        st = w.export_state()
+    finally:
+        oracle_lib.set_trig_mode(1)
+    dyn = st["bodies"]["type"] == abi.DYNAMIC
+    assert ((st["bodies"]["flags"][dyn] & abi.BODY_AWAKE) == 0).all()
+    top = st["bodies"]["xf"][-1]
+    assert abs(top[1] - 19.75) < 0.02 and abs(top[0]) < 0.5
+
+
+def test_hello_world_prints_reference_line(oracle_lib):
+    # examples/hello_world/hello_world.d:86-99 prints x, y, angle with %4.2f each step
+    w = oracle_lib.OracleWorld(scenes.hello_world())
+    for _ in range(60):
+        w.step(1.0 / 60.0, 6, 2)
+    b = w.export_state()["bodies"][1]
+    assert "%4.2f %4.2f %4.2f" % (b["xf"][0], b["xf"][1], b["sweep"][7]) == "0.00 1.01 0.00"
