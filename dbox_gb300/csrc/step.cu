@@ -1646,15 +1646,15 @@ extern "C" int dbox_launch_step_ev(const dg::Ctx* x, cudaStream_t stream, int* l
     int flat_blocks = (x->total_contacts + 255) / 256;
     if (flat_blocks < 1) flat_blocks = 1;
     if (flat_blocks > 152 * 16) flat_blocks = 152 * 16;
-    if (ev) cudaEventRecord(ev[0], stream);
+    if (ev) cudaEventRecordWithFlags(ev[0], stream, cudaEventRecordExternal);
     dg::k_step_begin<<<team_blocks, threads, 0, stream>>>(*x);
     dg::k_collide<<<flat_blocks, 256, 0, stream>>>(*x);
     dg::k_collide_finish<<<team_blocks, threads, 0, stream>>>(*x);
-    if (ev) cudaEventRecord(ev[1], stream);
+    if (ev) cudaEventRecordWithFlags(ev[1], stream, cudaEventRecordExternal);
     dg::k_solve<<<team_blocks, threads, 0, stream>>>(*x);
-    if (ev) cudaEventRecord(ev[2], stream);
+    if (ev) cudaEventRecordWithFlags(ev[2], stream, cudaEventRecordExternal);
     dg::k_toi<<<team_blocks, threads, 0, stream>>>(*x);
-    if (ev) cudaEventRecord(ev[3], stream);
+    if (ev) cudaEventRecordWithFlags(ev[3], stream, cudaEventRecordExternal);
     if (launches) *launches = 5;
     return (int)cudaGetLastError();
 }
