@@ -61,6 +61,7 @@ def lib():
     L.dbox_world_step_stats.argtypes = [vp, i32, ctypes.POINTER(i32), ctypes.POINTER(i32)]
     L.dbox_last_error.restype = ctypes.c_char_p
     L.dbox_collide_manifolds.argtypes = [i32, vp, vp, vp, vp, vp]
+    L.dbox_collide_manifolds_noalloc.argtypes = [i32, vp, vp, vp, vp, vp]
     L.dbox_world_step_n_timed.argtypes = [vp, f32, i32, i32, i32, vp, vp]
     L.dbox_world_get_counters.argtypes = [vp, vp]
     L.dbox_world_apply_forces.argtypes = [vp, vp]
@@ -86,6 +87,19 @@ def collide_manifolds(shapes_a, xfs_a, shapes_b, xfs_b):
     out = np.zeros(len(sa), abi.CONTACT_STATE)
     _check(lib().dbox_collide_manifolds(len(sa), abi.ptr(sa), abi.ptr(xa), abi.ptr(sb), abi.ptr(xb), abi.ptr(out)),
            "dbox_collide_manifolds")
+    return out
+
+
+def collide_manifolds_noalloc(shapes_a, xfs_a, shapes_b, xfs_b):
+    """dbox_collide_manifolds_noalloc: same as collide_manifolds, using the library's static
+    device array instead of allocating (at most 4096 pairs per call)."""
+    sa = np.ascontiguousarray(shapes_a, abi.SHAPE_DEF)
+    sb = np.ascontiguousarray(shapes_b, abi.SHAPE_DEF)
+    xa = np.ascontiguousarray(xfs_a, np.float32)
+    xb = np.ascontiguousarray(xfs_b, np.float32)
+    out = np.zeros(len(sa), abi.CONTACT_STATE)
+    _check(lib().dbox_collide_manifolds_noalloc(len(sa), abi.ptr(sa), abi.ptr(xa), abi.ptr(sb), abi.ptr(xb),
+                                                abi.ptr(out)), "dbox_collide_manifolds_noalloc")
     return out
 
 

@@ -13,6 +13,7 @@
 #include <string>
 #include <vector>
 #include <algorithm>
+#include <mutex>
 
 #include "world.cuh"
 #include "host_geom.h"
@@ -1087,6 +1088,88 @@ int32_t dbox_collide_manifolds(int32_t n, const dbox_shape_def* shape_a, const f
         rc = fail(DBOX_ERR_CUDA, "dbox_collide_manifolds: %s", cudaGetErrorString(cudaGetLastError()));
     dfa.free(); dfb.free(); dxa.free(); dxb.free(); dout.free();
     return rc;
+}
+
+// ---------------------------------------------------------------- allocation-free narrowphase
+// For callers that must not allocate device memory: code running where a
+// cudaMalloc would stall or be refused (inside a real-time frame loop that has
+// a no-allocation rule, under a memory budget enforced by another allocator,
+// or in a process whose device memory is owned by a host engine).  The device
+// memory this entry point needs lives in one file-scope array that every GPU
+// which loads the library holds until the process exits; calls allocate nothing.
+namespace {
+
+constexpr int kNoAllocMaxPairs = 4096;   // pairs per call
+constexpr int kNoAllocChunk = 32;        // pairs converted per host staging chunk (stack)
+
+struct NoAllocScratch {
+    dg::DFixture fa[kNoAllocMaxPairs];
+    dg::DFixture fb[kNoAllocMaxPairs];
+    float4 xa[kNoAllocMaxPairs];
+    float4 xb[kNoAllocMaxPairs];
+    dbox_contact_state out[kNoAllocMaxPairs];
+};
+
+// 4096 * (2*176 + 2*16 + 96) bytes = 1,966,080 bytes of device memory per GPU.
+static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
+
+std::mutex g_noalloc_mutex;
+NoAllocScratch* g_noalloc_ptr[64] = {nullptr};   // device address of the array, per device ordinal
+
+// Set-up, once per device, with that device current: the host-side name of the
+// array is only a stand-in, so its device address is fetched here.
+int noalloc_scratch(NoAllocScratch** out) {
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess || dev < 0 || dev >= 64)
+        return fail(DBOX_ERR_CUDA, "dbox_collide_manifolds_noalloc: no current device (%s)", cudaGetErrorString(e));
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            return fail(DBOX_ERR_CUDA, "dbox_collide_manifolds_noalloc: cudaGetSymbolAddress failed (%s)",
+                        cudaGetErrorString(e));
+        g_noalloc_ptr[dev] = (NoAllocScratch*)p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return DBOX_OK;
+}
+
+}  // namespace
+
+extern "C" int32_t dbox_collide_manifolds_noalloc(int32_t n, const dbox_shape_def* shape_a, const float* xf_a,
+                                                  const dbox_shape_def* shape_b, const float* xf_b,
+                                                  dbox_contact_state* out) {
+    if (n < 0 || (n > 0 && (!shape_a || !xf_a || !shape_b || !xf_b || !out)))
+        return fail(DBOX_ERR_INVALID, "dbox_collide_manifolds_noalloc: bad arguments");
+    if (n > kNoAllocMaxPairs)
+        return fail(DBOX_ERR_CAPACITY, "dbox_collide_manifolds_noalloc: %d pairs requested, at most %d per call",
+                    n, kNoAllocMaxPairs);
+    if (n == 0) return DBOX_OK;
+    NoAllocScratch* d = nullptr;
+    int rc = noalloc_scratch(&d);
+    if (rc) return rc;
+    dg::DFixture ca[kNoAllocChunk], cb[kNoAllocChunk];
+    for (int base = 0; base < n; base += kNoAllocChunk) {
+        int m = n - base < kNoAllocChunk ? n - base : kNoAllocChunk;
+        for (int i = 0; i < m; ++i) {
+            if (!build_fixture(shape_a + base + i, &ca[i]) || !build_fixture(shape_b + base + i, &cb[i]))
+                return fail(DBOX_ERR_INVALID, "dbox_collide_manifolds_noalloc: pair %d has a degenerate shape", base + i);
+            if (ca[i].type == dg::kShapeCircle && cb[i].type == dg::kShapePolygon)
+                return fail(DBOX_ERR_INVALID, "dbox_collide_manifolds_noalloc: pair %d: polygon must come first", base + i);
+        }
+        CU(cudaMemcpy(d->fa + base, ca, sizeof(dg::DFixture) * m, cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(d->fb + base, cb, sizeof(dg::DFixture) * m, cudaMemcpyHostToDevice));
+    }
+    CU(cudaMemcpy(d->xa, xf_a, sizeof(float4) * n, cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(d->xb, xf_b, sizeof(float4) * n, cudaMemcpyHostToDevice));
+    // the array keeps the previous call's manifolds: start from zero as dbox_collide_manifolds does
+    CU(cudaMemset(d->out, 0, sizeof(dbox_contact_state) * n));
+    int err = dbox_launch_collide_pairs(n, d->fa, d->xa, d->fb, d->xb, d->out, 0);
+    if (err) return fail(DBOX_ERR_CUDA, "dbox_collide_manifolds_noalloc: launch: %s", cudaGetErrorString((cudaError_t)err));
+    CU(cudaMemcpy(out, d->out, sizeof(dbox_contact_state) * n, cudaMemcpyDeviceToHost));
+    return DBOX_OK;
 }
 
 // per-world step diagnostics: islands and TOI events of the last step

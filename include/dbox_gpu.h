@@ -283,6 +283,19 @@ int32_t dbox_world_step_stats(dbox_world* w, int32_t world, int32_t* islands, in
 int32_t dbox_collide_manifolds(int32_t n, const dbox_shape_def* shape_a, const float* xf_a,
                                const dbox_shape_def* shape_b, const float* xf_b, dbox_contact_state* out);
 
+/* Same result as dbox_collide_manifolds, without allocating anything.  No counterpart in
+ * the reference (dbox allocates nothing on a GPU).  For callers that must not call
+ * cudaMalloc: code in a frame loop with a no-allocation rule, or a process whose device
+ * memory belongs to another allocator.  The device memory used lives in one file-scope
+ * array of the library (4096 pairs, 1,966,080 bytes), held by every GPU that loads the
+ * library until the process exits.  At most 4096 pairs per call (DBOX_ERR_CAPACITY
+ * beyond that).  The first call on each device looks up the array's device address,
+ * so make that first call before any stream capture.  All calls share the array:
+ * calls that overlap on the GPU (several host threads, or several processes sharing a
+ * context) race and must be serialised by the caller.  Synchronous on the default stream. */
+int32_t dbox_collide_manifolds_noalloc(int32_t n, const dbox_shape_def* shape_a, const float* xf_a,
+                                       const dbox_shape_def* shape_b, const float* xf_b, dbox_contact_state* out);
+
 /* Device kernels launched by the last step (for launch accounting). */
 int32_t dbox_world_last_launches(dbox_world* w, int32_t* out);
 
