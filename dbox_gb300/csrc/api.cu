@@ -102,6 +102,9 @@ struct dbox_world {
     DBuf<dg::PC> d_pc;
     DBuf<dg::SweepSnap> d_snap;
     DBuf<float> d_io;           // staging for bulk force upload / transform readback (3 floats per body)
+    DBuf<int2> s_cbody;
+    DBuf<unsigned char> s_cq, s_cvis, s_bfl;
+    DBuf<float> s_sbody;
     std::vector<dg::WorldInfo> wi;
     int total_bodies = 0, total_fixtures = 0, total_contacts = 0, total_joints = 0;
     // graph replay
@@ -137,6 +140,7 @@ void free_device(dbox_world* w) {
     for (auto* b : ints) b->free();
     w->s_isl_minsep.free(); w->s_isl_sleep.free();
     w->d_vc.free(); w->d_pc.free(); w->d_snap.free(); w->d_io.free();
+    w->s_cbody.free(); w->s_cq.free(); w->s_cvis.free(); w->s_bfl.free(); w->s_sbody.free();
     if (w->graph) { cudaGraphExecDestroy(w->graph); w->graph = nullptr; }
     if (w->tgraph) { cudaGraphExecDestroy(w->tgraph); w->tgraph = nullptr; }
 }
@@ -304,6 +308,11 @@ int upload(dbox_world* w) {
     ok &= w->d_pc.alloc(nc) == 0;
     ok &= w->d_snap.alloc(nc) == 0;
     ok &= w->d_io.alloc(3 * (size_t)nb) == 0;
+    ok &= w->s_cbody.alloc(nc) == 0;
+    ok &= w->s_cq.alloc(nc) == 0;
+    ok &= w->s_cvis.alloc(nc) == 0;
+    ok &= w->s_bfl.alloc(nb) == 0;
+    ok &= w->s_sbody.alloc(6 * (size_t)nb) == 0;
     if (!ok) { free_device(w); return fail(DBOX_ERR_CUDA, "device allocation failed (%d bodies, %d contact slots)", nb, nc); }
     CU(cudaMemcpy(w->d_wi.p, w->wi.data(), sizeof(dg::WorldInfo) * W, cudaMemcpyHostToDevice));
     CU(cudaMemcpy(w->d_wd.p, wd.data(), sizeof(dg::WorldDyn) * W, cudaMemcpyHostToDevice));
@@ -391,6 +400,11 @@ dg::Ctx make_ctx(dbox_world* w, float dt, int vi, int pi) {
     x.vc = w->d_vc.p;
     x.pc = w->d_pc.p;
     x.snap = w->d_snap.p;
+    x.s_cbody = w->s_cbody.p;
+    x.s_cq = w->s_cq.p;
+    x.s_cvis = w->s_cvis.p;
+    x.s_bfl = w->s_bfl.p;
+    x.s_sbody = w->s_sbody.p;
     x.dt = dt;
     x.inv_dt = dt > 0.0f ? 1.0f / dt : 0.0f;                            // b2world.d:383-390
     x.vel_iters = vi;

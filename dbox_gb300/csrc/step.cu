@@ -26,7 +26,6 @@
 namespace dg {
 
 constexpr int kWarp = 32;
-constexpr int kMaxToiLoop = 100000;   // bound on TOI events per world per step
 constexpr int kNoWake = 0x7fffffff;
 constexpr unsigned long long kHashEmpty = 0xffffffffffffffffull;
 
@@ -288,6 +287,8 @@ DG void find_new_contacts(const Ctx& x, int w) {
                     c.points[k].id = 0;
                 }
                 hash_insert(x, wi, pair_key(fa, fb));
+                x.s_cbody[wi.contact_start + slot] = make_int2(FA.body - wi.body_start, FB.body - wi.body_start);
+                x.s_cq[wi.contact_start + slot] = (unsigned char)((FA.sensor || FB.sensor) ? 2 : 0);
                 if (!FA.sensor && !FB.sensor) {
                     // SetAwake(true) on both bodies; concurrent writers store identical values
                     dbox_body_state& ba = x.bs[FA.body];
@@ -422,27 +423,44 @@ __global__ void k_collide_finish(Ctx x) {
     tsync();
 }
 
-// ------------------------------------------------------------ contact solver pieces (contacts/b2contactsolver.d)
-DG int other_body(const Ctx& x, const dbox_contact_state& c, int b) {
-    int A = x.fx[c.fixture_a].body;
-    return A == b ? x.fx[c.fixture_b].body : A;
+// ------------------------------------------------------------ solver body state
+// b2Position / b2Velocity of the island solver (dynamics/b2timestep.d:61-72) for every
+// body of a world, by world-local body index: vx vy w cx cy a.  Shared memory when the
+// world fits, else a global scratch row.
+struct SB {
+    float* p;
+    DG float2 v(int i) const { return v2(p[6 * i], p[6 * i + 1]); }
+    DG float w(int i) const { return p[6 * i + 2]; }
+    DG float2 c(int i) const { return v2(p[6 * i + 3], p[6 * i + 4]); }
+    DG float a(int i) const { return p[6 * i + 5]; }
+    DG void set_v(int i, float2 v, float w) { p[6 * i] = v.x; p[6 * i + 1] = v.y; p[6 * i + 2] = w; }
+    DG void set_c(int i, float2 c, float a) { p[6 * i + 3] = c.x; p[6 * i + 4] = c.y; p[6 * i + 5] = a; }
+};
+
+DG void sb_load(SB sb, int i, const dbox_body_state& b) {
+    sb.set_v(i, b_v(b), b.vel[2]);
+    sb.set_c(i, b_c(b), b.sweep[7]);
 }
 
-// b2ContactSolver ctor (:244-329) for one contact
-DG void constraint_ctor(const Ctx& x, int ci, bool warm, float dtRatio) {
+// flags of the compact per-body byte (s_bfl)
+enum { kBfAwake = 1, kBfActive = 2, kBfStatic = 4, kBfDynamic = 8, kBfVisited = 16, kBfMark = 32 };
+
+// ------------------------------------------------------------ contact solver pieces (contacts/b2contactsolver.d)
+// b2ContactSolver ctor (:244-329) for one contact; body indices are world-local.
+DG void constraint_ctor(const Ctx& x, int ci, int b0, bool warm, float dtRatio) {
     const dbox_contact_state& c = x.ct[ci];
     const DFixture& fa = x.fx[c.fixture_a];
     const DFixture& fb = x.fx[c.fixture_b];
     const dbox_body_state& ba = x.bs[fa.body];
     const dbox_body_state& bb = x.bs[fb.body];
-    VC& vc = x.vc[ci];
-    PC& pc = x.pc[ci];
+    VC vc;
+    PC pc;
     int pointCount = c.point_count;
     vc.friction = c.friction;
     vc.restitution = c.restitution;
     vc.tangentSpeed = c.tangent_speed;
-    vc.bodyA = fa.body;
-    vc.bodyB = fb.body;
+    vc.bodyA = fa.body - b0;
+    vc.bodyB = fb.body - b0;
     vc.invMassA = ba.mass[1];
     vc.invMassB = bb.mass[1];
     vc.invIA = ba.mass[3];
@@ -450,8 +468,9 @@ DG void constraint_ctor(const Ctx& x, int ci, bool warm, float dtRatio) {
     vc.pointCount = pointCount;
     vc.K[0] = vc.K[1] = vc.K[2] = vc.K[3] = 0.0f;
     vc.NM[0] = vc.NM[1] = vc.NM[2] = vc.NM[3] = 0.0f;
-    pc.bodyA = fa.body;
-    pc.bodyB = fb.body;
+    vc.normal = v2(0.0f, 0.0f);
+    pc.bodyA = vc.bodyA;
+    pc.bodyB = vc.bodyB;
     pc.invMassA = ba.mass[1];
     pc.invMassB = bb.mass[1];
     pc.lcA = b_lc(ba);
@@ -464,37 +483,35 @@ DG void constraint_ctor(const Ctx& x, int ci, bool warm, float dtRatio) {
     pc.radiusA = fa.radius;
     pc.radiusB = fb.radius;
     pc.type = c.type;
-    for (int j = 0; j < pointCount; ++j) {
+    for (int j = 0; j < 2; ++j) {
         VPoint& p = vc.p[j];
-        if (warm) {
+        p.normalImpulse = 0.0f;
+        p.tangentImpulse = 0.0f;
+        if (j < pointCount && warm) {
             p.normalImpulse = dtRatio * c.points[j].normal_impulse;
             p.tangentImpulse = dtRatio * c.points[j].tangent_impulse;
-        } else {
-            p.normalImpulse = 0.0f;
-            p.tangentImpulse = 0.0f;
         }
         p.rA = v2(0.0f, 0.0f);
         p.rB = v2(0.0f, 0.0f);
         p.normalMass = 0.0f;
         p.tangentMass = 0.0f;
         p.velocityBias = 0.0f;
-        pc.localPoints[j] = v2(c.points[j].local_point[0], c.points[j].local_point[1]);
+        pc.localPoints[j] = j < pointCount ? v2(c.points[j].local_point[0], c.points[j].local_point[1]) : v2(0.0f, 0.0f);
     }
+    x.vc[ci] = vc;
+    x.pc[ci] = pc;
 }
 
 // InitializeVelocityConstraints (:338-450) for one contact
-DG void constraint_init_velocity(const Ctx& x, int ci) {
-    VC& vc = x.vc[ci];
+DG void constraint_init_velocity(const Ctx& x, int ci, SB sb) {
+    VC vc = x.vc[ci];
     const PC& pc = x.pc[ci];
-    const dbox_body_state& ba = x.bs[vc.bodyA];
-    const dbox_body_state& bb = x.bs[vc.bodyB];
     int pointCount = vc.pointCount;
-    const dbox_contact_state& c = x.ct[ci];
     float mA = vc.invMassA, mB = vc.invMassB, iA = vc.invIA, iB = vc.invIB;
-    float2 cA = b_c(ba), cB = b_c(bb);
-    float aA = ba.sweep[7], aB = bb.sweep[7];
-    float2 vA = b_v(ba), vB = b_v(bb);
-    float wA = ba.vel[2], wB = bb.vel[2];
+    float2 cA = sb.c(vc.bodyA), cB = sb.c(vc.bodyB);
+    float aA = sb.a(vc.bodyA), aB = sb.a(vc.bodyB);
+    float2 vA = sb.v(vc.bodyA), vB = sb.v(vc.bodyB);
+    float wA = sb.w(vc.bodyA), wB = sb.w(vc.bodyB);
     Xf xfA, xfB;
     xfA.q = rot(aA);
     xfB.q = rot(aB);
@@ -505,7 +522,7 @@ DG void constraint_init_velocity(const Ctx& x, int ci) {
     float2 points[2] = {v2(0.0f, 0.0f), v2(0.0f, 0.0f)};
     float radiusA = pc.radiusA, radiusB = pc.radiusB;
     if (pointCount > 0) {
-        if (c.type == kManifoldCircles) {
+        if (pc.type == kManifoldCircles) {
             normal = v2(1.0f, 0.0f);
             float2 pointA = mul(xfA, pc.localPoint);
             float2 pointB = mul(xfB, pc.localPoints[0]);
@@ -516,7 +533,7 @@ DG void constraint_init_velocity(const Ctx& x, int ci) {
             float2 ccA = pointA + radiusA * normal;
             float2 ccB = pointB - radiusB * normal;
             points[0] = 0.5f * (ccA + ccB);
-        } else if (c.type == kManifoldFaceA) {
+        } else if (pc.type == kManifoldFaceA) {
             normal = mul(xfA.q, pc.localNormal);
             float2 planePoint = mul(xfA, pc.localPoint);
             for (int i = 0; i < pointCount; ++i) {
@@ -577,15 +594,14 @@ DG void constraint_init_velocity(const Ctx& x, int ci) {
             vc.pointCount = 1;
         }
     }
+    x.vc[ci] = vc;
 }
 
-DG void warm_start(const Ctx& x, int ci) {                             // :452-490
-    const VC& vc = x.vc[ci];
-    dbox_body_state& ba = x.bs[vc.bodyA];
-    dbox_body_state& bb = x.bs[vc.bodyB];
+DG void warm_start(const Ctx& x, int ci, SB sb) {                      // :452-490
+    const VC vc = x.vc[ci];
     float mA = vc.invMassA, iA = vc.invIA, mB = vc.invMassB, iB = vc.invIB;
-    float2 vA = b_v(ba), vB = b_v(bb);
-    float wA = ba.vel[2], wB = bb.vel[2];
+    float2 vA = sb.v(vc.bodyA), vB = sb.v(vc.bodyB);
+    float wA = sb.w(vc.bodyA), wB = sb.w(vc.bodyB);
     float2 normal = vc.normal;
     float2 tangent = cross(normal, 1.0f);
     for (int j = 0; j < vc.pointCount; ++j) {
@@ -596,8 +612,8 @@ DG void warm_start(const Ctx& x, int ci) {                             // :452-4
         wB += iB * cross(p.rB, P);
         vB += mB * P;
     }
-    ba.vel[0] = vA.x; ba.vel[1] = vA.y; ba.vel[2] = wA;
-    bb.vel[0] = vB.x; bb.vel[1] = vB.y; bb.vel[2] = wB;
+    sb.set_v(vc.bodyA, vA, wA);
+    sb.set_v(vc.bodyB, vB, wB);
 }
 
 DG void apply_block(float2& vA, float& wA, float2& vB, float& wB, float mA, float iA, float mB, float iB,
@@ -610,14 +626,12 @@ DG void apply_block(float2& vA, float& wA, float2& vB, float& wB, float mA, floa
     wB += iB * (cross(cp1.rB, P1) + cross(cp2.rB, P2));
 }
 
-DG void solve_velocity(const Ctx& x, int ci) {                         // :492-772
-    VC& vc = x.vc[ci];
-    dbox_body_state& ba = x.bs[vc.bodyA];
-    dbox_body_state& bb = x.bs[vc.bodyB];
+DG void solve_velocity(const Ctx& x, int ci, SB sb) {                  // :492-772
+    VC vc = x.vc[ci];
     float mA = vc.invMassA, iA = vc.invIA, mB = vc.invMassB, iB = vc.invIB;
     int pointCount = vc.pointCount;
-    float2 vA = b_v(ba), vB = b_v(bb);
-    float wA = ba.vel[2], wB = bb.vel[2];
+    float2 vA = sb.v(vc.bodyA), vB = sb.v(vc.bodyB);
+    float wA = sb.w(vc.bodyA), wB = sb.w(vc.bodyB);
     float2 normal = vc.normal;
     float2 tangent = cross(normal, 1.0f);
     float friction = vc.friction;
@@ -660,7 +674,6 @@ DG void solve_velocity(const Ctx& x, int ci) {                         // :492-7
         float2 b;
         b.x = vn1 - cp1.velocityBias;
         b.y = vn2 - cp2.velocityBias;
-        // b -= b2Mul(K, a)
         float2 Ka = v2(vc.K[0] * a.x + vc.K[2] * a.y, vc.K[1] * a.x + vc.K[3] * a.y);
         b -= Ka;
         for (;;) {
@@ -702,8 +715,13 @@ DG void solve_velocity(const Ctx& x, int ci) {                         // :492-7
             break;
         }
     }
-    ba.vel[0] = vA.x; ba.vel[1] = vA.y; ba.vel[2] = wA;
-    bb.vel[0] = vB.x; bb.vel[1] = vB.y; bb.vel[2] = wB;
+    sb.set_v(vc.bodyA, vA, wA);
+    sb.set_v(vc.bodyB, vB, wB);
+    VC& out = x.vc[ci];
+    out.p[0].normalImpulse = vc.p[0].normalImpulse;
+    out.p[0].tangentImpulse = vc.p[0].tangentImpulse;
+    out.p[1].normalImpulse = vc.p[1].normalImpulse;
+    out.p[1].tangentImpulse = vc.p[1].tangentImpulse;
 }
 
 DG void store_impulses(const Ctx& x, int ci) {                         // :774-787
@@ -717,10 +735,8 @@ DG void store_impulses(const Ctx& x, int ci) {                         // :774-7
 
 // SolvePositionConstraints / SolveTOIPositionConstraints for one contact (:73-242);
 // returns the minimum separation seen over its points (0 if none below 0).
-DG float solve_position(const Ctx& x, int ci, bool toi, int toiA, int toiB) {
-    const PC& pc = x.pc[ci];
-    dbox_body_state& ba = x.bs[pc.bodyA];
-    dbox_body_state& bb = x.bs[pc.bodyB];
+DG float solve_position(const Ctx& x, int ci, SB sb, bool toi, int toiA, int toiB) {
+    const PC pc = x.pc[ci];
     float mA, iA, mB, iB;
     if (!toi) { mA = pc.invMassA; iA = pc.invIA; mB = pc.invMassB; iB = pc.invIB; }
     else {
@@ -729,8 +745,8 @@ DG float solve_position(const Ctx& x, int ci, bool toi, int toiA, int toiB) {
         mB = 0.0f; iB = 0.0f;
         if (pc.bodyB == toiA || pc.bodyB == toiB) { mB = pc.invMassB; iB = pc.invIB; }
     }
-    float2 cA = b_c(ba), cB = b_c(bb);
-    float aA = ba.sweep[7], aB = bb.sweep[7];
+    float2 cA = sb.c(pc.bodyA), cB = sb.c(pc.bodyB);
+    float aA = sb.a(pc.bodyA), aB = sb.a(pc.bodyB);
     float minSep = 0.0f;
     for (int j = 0; j < pc.pointCount; ++j) {
         Xf xfA, xfB;
@@ -776,30 +792,29 @@ DG float solve_position(const Ctx& x, int ci, bool toi, int toiA, int toiB) {
         cB += mB * P;
         aB += iB * cross(rB, P);
     }
-    ba.sweep[4] = cA.x; ba.sweep[5] = cA.y; ba.sweep[7] = aA;
-    bb.sweep[4] = cB.x; bb.sweep[5] = cB.y; bb.sweep[7] = aB;
+    sb.set_c(pc.bodyA, cA, aA);
+    sb.set_c(pc.bodyB, cB, aB);
     return minSep;
 }
 
 // ------------------------------------------------------------ revolute joint (joints/b2revolutejoint.d:319-636)
-DG Xf dummy_xf() { Xf x; x.p = v2(0, 0); x.q.s = 0; x.q.c = 1; return x; }
-
-DG void joint_init(const Ctx& x, int ji, bool warm, float dtRatio) {
+DG void joint_init(const Ctx& x, int ji, int b0, SB sb, bool warm, float dtRatio) {
     DJoint& j = x.jt[ji];
-    dbox_body_state& ba = x.bs[j.body_a];
-    dbox_body_state& bb = x.bs[j.body_b];
+    const dbox_body_state& ba = x.bs[j.body_a];
+    const dbox_body_state& bb = x.bs[j.body_b];
+    int la = j.body_a - b0, lb = j.body_b - b0;
     j.lcA = b_lc(ba);
     j.lcB = b_lc(bb);
     j.invMassA = ba.mass[1];
     j.invMassB = bb.mass[1];
     j.invIA = ba.mass[3];
     j.invIB = bb.mass[3];
-    float aA = ba.sweep[7];
-    float2 vA = b_v(ba);
-    float wA = ba.vel[2];
-    float aB = bb.sweep[7];
-    float2 vB = b_v(bb);
-    float wB = bb.vel[2];
+    float aA = sb.a(la);
+    float2 vA = sb.v(la);
+    float wA = sb.w(la);
+    float aB = sb.a(lb);
+    float2 vB = sb.v(lb);
+    float wB = sb.w(lb);
     Rot qA = rot(aA), qB = rot(aB);
     j.rA = mul(qA, j.local_anchor_a - j.lcA);
     j.rB = mul(qB, j.local_anchor_b - j.lcB);
@@ -847,12 +862,11 @@ DG void joint_init(const Ctx& x, int ji, bool warm, float dtRatio) {
         j.impulse[0] = j.impulse[1] = j.impulse[2] = 0.0f;
         j.motor_impulse = 0.0f;
     }
-    ba.vel[0] = vA.x; ba.vel[1] = vA.y; ba.vel[2] = wA;
-    bb.vel[0] = vB.x; bb.vel[1] = vB.y; bb.vel[2] = wB;
+    sb.set_v(la, vA, wA);
+    sb.set_v(lb, vB, wB);
 }
 
 DG float3 solve33(const float* m, float3 b) {                            // b2math.d:388-399
-    // columns ex=(m0,m1,m2) ey=(m3,m4,m5) ez=(m6,m7,m8)
     float3 ex = make_float3(m[0], m[1], m[2]), ey = make_float3(m[3], m[4], m[5]), ez = make_float3(m[6], m[7], m[8]);
     auto cr = [](float3 a, float3 c) { return make_float3(a.y * c.z - a.z * c.y, a.z * c.x - a.x * c.z, a.x * c.y - a.y * c.x); };
     auto dt3 = [](float3 a, float3 c) { return (a.x * c.x + a.y * c.y) + a.z * c.z; };
@@ -871,12 +885,11 @@ DG float2 solve22(const float* m, float2 b) {                            // b2ma
     return v2(det * (a22 * b.x - a12 * b.y), det * (a11 * b.y - a21 * b.x));
 }
 
-DG void joint_solve_velocity(const Ctx& x, int ji) {
+DG void joint_solve_velocity(const Ctx& x, int ji, int b0, SB sb) {
     DJoint& j = x.jt[ji];
-    dbox_body_state& ba = x.bs[j.body_a];
-    dbox_body_state& bb = x.bs[j.body_b];
-    float2 vA = b_v(ba), vB = b_v(bb);
-    float wA = ba.vel[2], wB = bb.vel[2];
+    int la = j.body_a - b0, lb = j.body_b - b0;
+    float2 vA = sb.v(la), vB = sb.v(lb);
+    float wA = sb.w(la), wB = sb.w(lb);
     float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
     bool fixedRotation = (iA + iB == 0.0f);
     if (j.enable_motor && j.limit_state != 3 && !fixedRotation) {
@@ -927,16 +940,15 @@ DG void joint_solve_velocity(const Ctx& x, int ji) {
         vB += mB * imp;
         wB += iB * cross(j.rB, imp);
     }
-    ba.vel[0] = vA.x; ba.vel[1] = vA.y; ba.vel[2] = wA;
-    bb.vel[0] = vB.x; bb.vel[1] = vB.y; bb.vel[2] = wB;
+    sb.set_v(la, vA, wA);
+    sb.set_v(lb, vB, wB);
 }
 
-DG bool joint_solve_position(const Ctx& x, int ji) {
+DG bool joint_solve_position(const Ctx& x, int ji, int b0, SB sb) {
     DJoint& j = x.jt[ji];
-    dbox_body_state& ba = x.bs[j.body_a];
-    dbox_body_state& bb = x.bs[j.body_b];
-    float2 cA = b_c(ba), cB = b_c(bb);
-    float aA = ba.sweep[7], aB = bb.sweep[7];
+    int la = j.body_a - b0, lb = j.body_b - b0;
+    float2 cA = sb.c(la), cB = sb.c(lb);
+    float aA = sb.a(la), aB = sb.a(lb);
     float angularError = 0.0f, positionError = 0.0f;
     bool fixedRotation = (j.invIA + j.invIB == 0.0f);
     if (j.enable_limit && j.limit_state != 0 && !fixedRotation) {
@@ -979,28 +991,16 @@ DG bool joint_solve_position(const Ctx& x, int ji) {
         cB += mB * imp;
         aB += iB * cross(rB, imp);
     }
-    ba.sweep[4] = cA.x; ba.sweep[5] = cA.y; ba.sweep[7] = aA;
-    bb.sweep[4] = cB.x; bb.sweep[5] = cB.y; bb.sweep[7] = aB;
+    sb.set_c(la, cA, aA);
+    sb.set_c(lb, cB, aB);
     return positionError <= kLinearSlop && angularError <= kAngularSlop;
 }
 
 // ------------------------------------------------------------ level schedule
-// Items: contact slot c >= 0, joint j encoded as -(j + 1).
-DG void item_bodies(const Ctx& x, int item, int& A, int& B) {
-    if (item >= 0) { A = x.vc[item].bodyA; B = x.vc[item].bodyB; }
-    else { const DJoint& j = x.jt[-item - 1]; A = j.body_a; B = j.body_b; }
-}
-DG int item_bodies_raw(const Ctx& x, int item, int& A, int& B) {
-    if (item >= 0) {
-        const dbox_contact_state& c = x.ct[item];
-        A = x.fx[c.fixture_a].body;
-        B = x.fx[c.fixture_b].body;
-    } else {
-        const DJoint& j = x.jt[-item - 1];
-        A = j.body_a;
-        B = j.body_b;
-    }
-    return 0;
+// Items: contact slot c >= 0, joint j encoded as -(j + 1).  Bodies are world-local.
+DG void item_bodies(const Ctx& x, int item, int b0, int& A, int& B) {
+    if (item >= 0) { int2 cb = x.s_cbody[item]; A = cb.x; B = cb.y; }
+    else { const DJoint& j = x.jt[-item - 1]; A = j.body_a - b0; B = j.body_b - b0; }
 }
 
 // Build one level schedule for world w.  `contacts_first` gives the warm-start /
@@ -1009,8 +1009,10 @@ DG int item_bodies_raw(const Ctx& x, int item, int& A, int& B) {
 // b2island.d:153-161).  Level L items end up in sched[kx + lvl[kx+L] .. kx + lvl[kx+L+1]).
 // Run by one lane.  Returns the number of levels.
 DG int build_schedule(const Ctx& x, const WorldInfo& wi, int nIsl, bool contacts_first, int* sched, int* lvl) {
-    int b0 = wi.body_start, kx = wi.kx_start;
-    for (int i = 0; i < wi.body_count; ++i) x.s_last[b0 + i] = 0;
+    const int b0 = wi.body_start, kx = wi.kx_start;
+    const unsigned char* bfl = x.s_bfl + b0;
+    int* last = x.s_last + b0;
+    for (int i = 0; i < wi.body_count; ++i) last[i] = 0;
     int maxL = 0, n = 0;
     for (int is = 0; is < nIsl; ++is) {
         int cs = x.s_isl_cstart[wi.bx_start + is], ce = x.s_isl_cstart[wi.bx_start + is + 1];
@@ -1021,12 +1023,12 @@ DG int build_schedule(const Ctx& x, const WorldInfo& wi, int nIsl, bool contacts
             for (int t = s; t < e; ++t) {
                 int item = doContacts ? x.s_isl_contact[wi.contact_start + t] : -(x.s_isl_joint[wi.joint_start + t] + 1);
                 int A, B;
-                item_bodies_raw(x, item, A, B);
-                bool dA = x.bs[A].type == kDynamicBody, dB = x.bs[B].type == kDynamicBody;
-                int la = dA ? x.s_last[A] : 0, lb = dB ? x.s_last[B] : 0;
+                item_bodies(x, item, b0, A, B);
+                bool dA = (bfl[A] & kBfDynamic) != 0, dB = (bfl[B] & kBfDynamic) != 0;
+                int la = dA ? last[A] : 0, lb = dB ? last[B] : 0;
                 int l = (la > lb ? la : lb) + 1;
-                if (dA) x.s_last[A] = l;
-                if (dB) x.s_last[B] = l;
+                if (dA) last[A] = l;
+                if (dB) last[B] = l;
                 if (l > maxL) maxL = l;
                 x.s_level[kx + n] = l;
                 x.s_tmp[kx + n] = item;
@@ -1046,15 +1048,10 @@ DG int build_schedule(const Ctx& x, const WorldInfo& wi, int nIsl, bool contacts
 }
 
 // island id of a constraint: the island of one of its non-static bodies
-DG int item_island(const Ctx& x, int item) {
+DG int item_island(const Ctx& x, int item, int b0) {
     int A, B;
-    item_bodies_raw(x, item, A, B);
-    return x.bs[A].type != kStaticBody ? x.s_body_island[A] : x.s_body_island[B];
-}
-
-DG bool contact_in_island_graph(const Ctx& x, const dbox_contact_state& c) {
-    return (c.flags & kContactEnabled) && (c.flags & kContactTouching) && !x.fx[c.fixture_a].sensor &&
-           !x.fx[c.fixture_b].sensor;
+    item_bodies(x, item, b0, A, B);
+    return (x.s_bfl[b0 + A] & kBfStatic) ? x.s_body_island[b0 + B] : x.s_body_island[b0 + A];
 }
 
 // b2Fixture.Synchronize + b2DynamicTree.MoveProxy for every fixture of body b
@@ -1090,7 +1087,32 @@ DG void sync_fixtures(const Ctx& x, int b) {
     }
 }
 
-__global__ void k_solve(Ctx x) {
+// per-contact compact data for the sequential walks: world-local bodies, and
+// s_cq bit0 = enabled & touching & no sensor (island graph edge), bit1 = a sensor fixture
+DG void contact_compact(const Ctx& x, int ci, int b0) {
+    const dbox_contact_state& c = x.ct[ci];
+    const DFixture& fa = x.fx[c.fixture_a];
+    const DFixture& fb = x.fx[c.fixture_b];
+    x.s_cbody[ci] = make_int2(fa.body - b0, fb.body - b0);
+    int sensor = (fa.sensor || fb.sensor) ? 1 : 0;
+    int edge = ((c.flags & kContactEnabled) && (c.flags & kContactTouching) && !sensor) ? 1 : 0;
+    x.s_cq[ci] = (unsigned char)(edge | (sensor << 1));
+}
+
+DG unsigned char body_flag_byte(const dbox_body_state& b) {
+    unsigned char f = 0;
+    if (b.flags & kBodyAwake) f |= kBfAwake;
+    if (b.flags & kBodyActive) f |= kBfActive;
+    if (b.type == kStaticBody) f |= kBfStatic;
+    if (b.type == kDynamicBody) f |= kBfDynamic;
+    return f;
+}
+
+constexpr int kSolveWarps = 4;          // worlds per block in k_solve
+constexpr int kSmemBodies = 320;        // worlds up to this many bodies keep solver state in shared memory
+
+__global__ void __launch_bounds__(kSolveWarps * 32) k_solve(Ctx x) {
+    extern __shared__ float smem_sb[];
     int w = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
     if (w >= x.W) return;
     const WorldInfo& wi = x.wi[w];
@@ -1104,95 +1126,121 @@ __global__ void k_solve(Ctx x) {
     const float h = x.dt;
     const bool warm = x.warm_starting != 0;
     const float dtRatio = wd.inv_dt0 * x.dt;                            // b2world.d:392
-    // clear island flags (b2world.d:944-957) and per-step scratch
+    SB sb;
+    sb.p = nb <= kSmemBodies ? smem_sb + (threadIdx.x >> 5) * (kSmemBodies * 6) : x.s_sbody + 6 * (size_t)b0;
+    unsigned char* bfl = x.s_bfl + b0;
+    // compact per-body / per-contact data; island flags cleared (b2world.d:944-957)
     for (int i = lane; i < nb; i += kWarp) {
-        x.bs[b0 + i].flags &= ~(uint32_t)kBodyIsland;
+        dbox_body_state& B = x.bs[b0 + i];
+        B.flags &= ~(uint32_t)kBodyIsland;
+        bfl[i] = body_flag_byte(B);
         x.s_cursor[b0 + i] = 0;
         x.s_body_island[b0 + i] = -1;
+        sb_load(sb, i, B);
     }
-    for (int k = lane; k < n; k += kWarp) x.ct[c0 + k].flags &= ~(uint32_t)kContactIsland;
+    for (int k = lane; k < n; k += kWarp) {
+        x.ct[c0 + k].flags &= ~(uint32_t)kContactIsland;
+        contact_compact(x, c0 + k, b0);
+        x.s_cvis[c0 + k] = 0;
+    }
     for (int j = lane; j < nj; j += kWarp) x.jt[j0 + j].island_flag = 0;
     tsync();
-    // contact edges of the island graph, per body, newest first
+    // contact edges of the island graph per body, newest first
     for (int k = lane; k < n; k += kWarp) {
-        const dbox_contact_state& c = x.ct[c0 + k];
-        if (!contact_in_island_graph(x, c)) continue;
-        atomicAdd(&x.s_cursor[x.fx[c.fixture_a].body], 1);
-        atomicAdd(&x.s_cursor[x.fx[c.fixture_b].body], 1);
+        if (x.s_cq[c0 + k] & 1) {
+            int2 cb = x.s_cbody[c0 + k];
+            atomicAdd(&x.s_cursor[b0 + cb.x], 1);
+            atomicAdd(&x.s_cursor[b0 + cb.y], 1);
+        }
+    }
+    tsync();
+    {
+        int total = 0;
+        for (int base = 0; base < nb; base += kWarp) {
+            int i = base + lane;
+            int v = i < nb ? x.s_cursor[b0 + i] : 0;
+            int incl = v;
+            for (int o = 1; o < 32; o <<= 1) {
+                int t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
+            }
+            if (i < nb) { x.s_adj_start[bx + i] = total + incl - v; x.s_cursor[b0 + i] = total + incl - v; }
+            total += __shfl_sync(0xffffffffu, incl, 31);
+        }
+        if (lane == 0) x.s_adj_start[bx + nb] = total;
     }
     tsync();
     int nIsl = 0, nbI = 0, ncI = 0, njI = 0, maxLv = 0, maxLp = 0;
     if (lane == 0) {
-        int acc = 0;
-        for (int i = 0; i < nb; ++i) {
-            int cnt = x.s_cursor[b0 + i];
-            x.s_adj_start[bx + i] = acc;
-            x.s_cursor[b0 + i] = acc;
-            acc += cnt;
-        }
-        x.s_adj_start[bx + nb] = acc;
+        int* cursor = x.s_cursor + b0;
+        int* items = x.s_adj_items + 2 * (size_t)c0;
+        const int2* cbody = x.s_cbody + c0;
+        const unsigned char* cq = x.s_cq + c0;
+        unsigned char* cvis = x.s_cvis + c0;
         for (int k = n - 1; k >= 0; --k) {
-            const dbox_contact_state& c = x.ct[c0 + k];
-            if (!contact_in_island_graph(x, c)) continue;
-            int A = x.fx[c.fixture_a].body, B = x.fx[c.fixture_b].body;
-            x.s_adj_items[2 * c0 + x.s_cursor[A]++] = k;
-            x.s_adj_items[2 * c0 + x.s_cursor[B]++] = k;
+            if (!(cq[k] & 1)) continue;
+            int2 cb = cbody[k];
+            items[cursor[cb.x]++] = k;
+            items[cursor[cb.y]++] = k;
         }
+        const int* adj = x.s_adj_start + bx;
+        int* stack = x.s_stack + b0;
+        int* statics = x.s_last + b0;
+        int* isl_body = x.s_isl_body + b0;
+        int* isl_contact = x.s_isl_contact + c0;
+        int* body_island = x.s_body_island + b0;
         // depth-first island search (b2world.d:959-1095)
-        for (int sb = nb - 1; sb >= 0; --sb) {
-            int seed = b0 + sb;
-            dbox_body_state& S = x.bs[seed];
-            if (S.flags & kBodyIsland) continue;
-            if ((S.flags & kBodyAwake) == 0 || (S.flags & kBodyActive) == 0) continue;
-            if (S.type == kStaticBody) continue;
+        for (int seed = nb - 1; seed >= 0; --seed) {
+            unsigned char fs = bfl[seed];
+            if (fs & kBfVisited) continue;
+            if ((fs & kBfAwake) == 0 || (fs & kBfActive) == 0) continue;
+            if (fs & kBfStatic) continue;
             x.s_isl_bstart[bx + nIsl] = nbI;
             x.s_isl_cstart[bx + nIsl] = ncI;
             x.s_isl_jstart[bx + nIsl] = njI;
             int top = 0, nStatic = 0;
-            x.s_stack[b0 + top++] = seed;
-            S.flags |= kBodyIsland;
+            stack[top++] = seed;
+            bfl[seed] = fs | kBfVisited;
             while (top > 0) {
-                int b = x.s_stack[b0 + --top];
-                dbox_body_state& Bd = x.bs[b];
-                b_set_awake(Bd, true);
-                x.s_body_island[b] = nIsl;
-                if (Bd.type == kStaticBody) {
-                    x.s_last[b0 + nStatic++] = b;
+                int b = stack[--top];
+                body_island[b] = nIsl;
+                if (bfl[b] & kBfStatic) {
+                    statics[nStatic++] = b;
                     continue;
                 }
-                x.s_isl_body[b0 + nbI++] = b;
-                int rs = x.s_adj_start[bx + (b - b0)], re = x.s_adj_start[bx + (b - b0) + 1];
-                for (int e = rs; e < re; ++e) {
-                    int k = x.s_adj_items[2 * c0 + e];
-                    dbox_contact_state& c = x.ct[c0 + k];
-                    if (c.flags & kContactIsland) continue;
-                    x.s_isl_contact[c0 + ncI++] = c0 + k;
-                    c.flags |= kContactIsland;
-                    int other = other_body(x, c, b);
-                    if (x.bs[other].flags & kBodyIsland) continue;
-                    x.s_stack[b0 + top++] = other;
-                    x.bs[other].flags |= kBodyIsland;
+                isl_body[nbI++] = b;
+                for (int e = adj[b], ee = adj[b + 1]; e < ee; ++e) {
+                    int k = items[e];
+                    if (cvis[k]) continue;
+                    isl_contact[ncI++] = c0 + k;
+                    cvis[k] = 1;
+                    int2 cb = cbody[k];
+                    int other = cb.x == b ? cb.y : cb.x;
+                    unsigned char fo = bfl[other];
+                    if (fo & kBfVisited) continue;
+                    stack[top++] = other;
+                    bfl[other] = fo | kBfVisited;
                 }
-                const BodyStatic& st = x.bst[b];
+                const BodyStatic& st = x.bst[b0 + b];
                 for (int e = 0; e < st.jadj_count; ++e) {
                     int j = x.jadj_joint[st.jadj_start + e];
                     if (x.jt[j].island_flag) continue;
-                    int other = x.jadj_other[st.jadj_start + e];
-                    if ((x.bs[other].flags & kBodyActive) == 0) continue;
+                    int other = x.jadj_other[st.jadj_start + e] - b0;
+                    unsigned char fo = bfl[other];
+                    if ((fo & kBfActive) == 0) continue;
                     x.s_isl_joint[j0 + njI++] = j;
                     x.jt[j].island_flag = 1;
-                    if (x.bs[other].flags & kBodyIsland) continue;
-                    x.s_stack[b0 + top++] = other;
-                    x.bs[other].flags |= kBodyIsland;
+                    if (fo & kBfVisited) continue;
+                    stack[top++] = other;
+                    bfl[other] = fo | kBfVisited;
                 }
             }
-            for (int i = 0; i < nStatic; ++i) x.bs[x.s_last[b0 + i]].flags &= ~(uint32_t)kBodyIsland;
+            for (int i = 0; i < nStatic; ++i) bfl[statics[i]] &= ~kBfVisited;
             ++nIsl;
         }
         x.s_isl_bstart[bx + nIsl] = nbI;
         x.s_isl_cstart[bx + nIsl] = ncI;
         x.s_isl_jstart[bx + nIsl] = njI;
-        // contacts keep their island id for the position pass
         maxLv = build_schedule(x, wi, nIsl, false, x.s_sched_v, x.s_lvl_v);
         maxLp = build_schedule(x, wi, nIsl, true, x.s_sched_p, x.s_lvl_p);
         wd.islands = nIsl;
@@ -1208,30 +1256,38 @@ __global__ void k_solve(Ctx x) {
         wd.acc_vsolve += (unsigned long long)ncI * (unsigned long long)x.vel_iters;
     }
     tsync();
+    // island flags and SetAwake(true) of the search (b2world.d:985-1004), applied after it
+    for (int i = lane; i < nb; i += kWarp) {
+        dbox_body_state& B = x.bs[b0 + i];
+        if ((bfl[i] & kBfVisited) && !(bfl[i] & kBfStatic)) B.flags |= kBodyIsland;
+        if (x.s_body_island[b0 + i] >= 0) b_set_awake(B, true);
+    }
+    for (int k = lane; k < n; k += kWarp)
+        if (x.s_cvis[c0 + k]) x.ct[c0 + k].flags |= kContactIsland;
     // integrate velocities (b2island.d:82-116)
-    for (int i = lane; i < nbI; i += kWarp) {
-        int b = x.s_isl_body[b0 + i];
-        dbox_body_state& B = x.bs[b];
+    for (int t = lane; t < nbI; t += kWarp) {
+        int i = x.s_isl_body[b0 + t];
+        dbox_body_state& B = x.bs[b0 + i];
         B.sweep[2] = B.sweep[4];
         B.sweep[3] = B.sweep[5];
         B.sweep[6] = B.sweep[7];
         if (B.type == kDynamicBody) {
-            const BodyStatic& st = x.bst[b];
-            float2 v = b_v(B);
-            float wv = B.vel[2];
+            const BodyStatic& st = x.bst[b0 + i];
+            float2 v = sb.v(i);
+            float wv = sb.w(i);
             float2 g = st.gravity_scale * x.gravity + B.mass[1] * v2(B.force[0], B.force[1]);
             v += h * g;
             wv += (h * B.mass[3]) * B.force[2];
             v *= fdiv(1.0f, 1.0f + h * st.lin_damping);
             wv *= fdiv(1.0f, 1.0f + h * st.ang_damping);
-            B.vel[0] = v.x; B.vel[1] = v.y; B.vel[2] = wv;
+            sb.set_v(i, v, wv);
         }
     }
     tsync();
     for (int t = lane; t < ncI; t += kWarp) {
         int ci = x.s_isl_contact[c0 + t];
-        constraint_ctor(x, ci, warm, dtRatio);
-        constraint_init_velocity(x, ci);
+        constraint_ctor(x, ci, b0, warm, dtRatio);
+        constraint_init_velocity(x, ci, sb);
     }
     tsync();
     // warm start contacts, then joints' InitVelocityConstraints (b2island.d:133-146)
@@ -1239,8 +1295,8 @@ __global__ void k_solve(Ctx x) {
         int s = x.s_lvl_p[kx + L], e = x.s_lvl_p[kx + L + 1];
         for (int idx = s + lane; idx < e; idx += kWarp) {
             int item = x.s_sched_p[kx + idx];
-            if (item >= 0) { if (warm) warm_start(x, item); }
-            else joint_init(x, -item - 1, warm, dtRatio);
+            if (item >= 0) { if (warm) warm_start(x, item, sb); }
+            else joint_init(x, -item - 1, b0, sb, warm, dtRatio);
         }
         tsync();
     }
@@ -1250,20 +1306,20 @@ __global__ void k_solve(Ctx x) {
             int s = x.s_lvl_v[kx + L], e = x.s_lvl_v[kx + L + 1];
             for (int idx = s + lane; idx < e; idx += kWarp) {
                 int item = x.s_sched_v[kx + idx];
-                if (item >= 0) solve_velocity(x, item);
-                else joint_solve_velocity(x, -item - 1);
+                if (item >= 0) solve_velocity(x, item, sb);
+                else joint_solve_velocity(x, -item - 1, b0, sb);
             }
             tsync();
         }
     }
     for (int t = lane; t < ncI; t += kWarp) store_impulses(x, x.s_isl_contact[c0 + t]);
     // integrate positions (b2island.d:168-200)
-    for (int i = lane; i < nbI; i += kWarp) {
-        dbox_body_state& B = x.bs[x.s_isl_body[b0 + i]];
-        float2 c = b_c(B);
-        float a = B.sweep[7];
-        float2 v = b_v(B);
-        float wv = B.vel[2];
+    for (int t = lane; t < nbI; t += kWarp) {
+        int i = x.s_isl_body[b0 + t];
+        float2 c = sb.c(i);
+        float a = sb.a(i);
+        float2 v = sb.v(i);
+        float wv = sb.w(i);
         float2 translation = h * v;
         if (dot(translation, translation) > kMaxTranslationSquared) {
             float ratio = fdiv(kMaxTranslation, length(translation));
@@ -1276,8 +1332,8 @@ __global__ void k_solve(Ctx x) {
         }
         c += h * v;
         a += h * wv;
-        B.sweep[4] = c.x; B.sweep[5] = c.y; B.sweep[7] = a;
-        B.vel[0] = v.x; B.vel[1] = v.y; B.vel[2] = wv;
+        sb.set_c(i, c, a);
+        sb.set_v(i, v, wv);
     }
     for (int is = lane; is < nIsl; is += kWarp) x.s_isl_flags[b0 + is] = 0;
     tsync();
@@ -1292,12 +1348,12 @@ __global__ void k_solve(Ctx x) {
             int s = x.s_lvl_p[kx + L], e = x.s_lvl_p[kx + L + 1];
             for (int idx = s + lane; idx < e; idx += kWarp) {
                 int item = x.s_sched_p[kx + idx];
-                int is = item_island(x, item);
+                int is = item_island(x, item, b0);
                 if (x.s_isl_flags[b0 + is] & 1) continue;
                 if (item >= 0) {
-                    float ms = solve_position(x, item, false, -1, -1);
+                    float ms = solve_position(x, item, sb, false, -1, -1);
                     atomicMin(&x.s_isl_minsep[b0 + is], fkey(ms));
-                } else if (!joint_solve_position(x, -item - 1)) {
+                } else if (!joint_solve_position(x, -item - 1, b0, sb)) {
                     atomicOr(&x.s_isl_flags[b0 + is], 4);
                 }
             }
@@ -1322,8 +1378,15 @@ __global__ void k_solve(Ctx x) {
         tsync();
     }
     tsync();
-    // copy back: SynchronizeTransform (b2island.d:227-235)
-    for (int i = lane; i < nbI; i += kWarp) b_sync_transform(x.bs[x.s_isl_body[b0 + i]]);
+    // copy back + SynchronizeTransform (b2island.d:227-235)
+    for (int t = lane; t < nbI; t += kWarp) {
+        int i = x.s_isl_body[b0 + t];
+        dbox_body_state& B = x.bs[b0 + i];
+        float2 c = sb.c(i), v = sb.v(i);
+        B.sweep[4] = c.x; B.sweep[5] = c.y; B.sweep[7] = sb.a(i);
+        B.vel[0] = v.x; B.vel[1] = v.y; B.vel[2] = sb.w(i);
+        b_sync_transform(B);
+    }
     tsync();
     // sleep (b2island.d:241-279)
     if (x.allow_sleep) {
@@ -1331,10 +1394,10 @@ __global__ void k_solve(Ctx x) {
         const float angTolSqr = kAngularSleepTolerance * kAngularSleepTolerance;
         for (int is = lane; is < nIsl; is += kWarp) x.s_isl_sleep[b0 + is] = fkey(kMaxFloat);
         tsync();
-        for (int i = lane; i < nbI; i += kWarp) {
-            int b = x.s_isl_body[b0 + i];
-            dbox_body_state& B = x.bs[b];
-            int is = x.s_body_island[b];
+        for (int t = lane; t < nbI; t += kWarp) {
+            int i = x.s_isl_body[b0 + t];
+            dbox_body_state& B = x.bs[b0 + i];
+            int is = x.s_body_island[b0 + i];
             if ((B.flags & kBodyAutoSleep) == 0 || B.vel[2] * B.vel[2] > angTolSqr ||
                 dot(b_v(B), b_v(B)) > linTolSqr) {
                 B.sleep_time = 0.0f;
@@ -1350,16 +1413,15 @@ __global__ void k_solve(Ctx x) {
             if (funkey(x.s_isl_sleep[b0 + is]) >= kTimeToSleep && (f & 2)) x.s_isl_flags[b0 + is] = f | 8;
         }
         tsync();
-        for (int i = lane; i < nbI; i += kWarp) {
-            int b = x.s_isl_body[b0 + i];
-            if (x.s_isl_flags[b0 + x.s_body_island[b]] & 8) b_set_awake(x.bs[b], false);
+        for (int t = lane; t < nbI; t += kWarp) {
+            int i = x.s_isl_body[b0 + t];
+            if (x.s_isl_flags[b0 + x.s_body_island[b0 + i]] & 8) b_set_awake(x.bs[b0 + i], false);
         }
         // a static body ends in the state its last island left it in
         for (int i = lane; i < nb; i += kWarp) {
-            int b = b0 + i;
-            if (x.bs[b].type == kStaticBody && x.s_body_island[b] >= 0 &&
-                (x.s_isl_flags[b0 + x.s_body_island[b]] & 8))
-                b_set_awake(x.bs[b], false);
+            if ((bfl[i] & kBfStatic) && x.s_body_island[b0 + i] >= 0 &&
+                (x.s_isl_flags[b0 + x.s_body_island[b0 + i]] & 8))
+                b_set_awake(x.bs[b0 + i], false);
         }
     }
     tsync();
@@ -1376,16 +1438,16 @@ __global__ void k_solve(Ctx x) {
 }
 
 // ------------------------------------------------------------ TOI
-// contact needs a fresh TOI (b2world.d:1159-1210)
-DG bool toi_needs(const Ctx& x, const dbox_contact_state& c) {
+// contact needs a fresh TOI (b2world.d:1159-1210); bodies from the compact arrays
+DG bool toi_needs(const Ctx& x, int ci, int b0) {
+    const dbox_contact_state& c = x.ct[ci];
     if ((c.flags & kContactEnabled) == 0) return false;
     if (c.toi_count > kMaxSubSteps) return false;
     if (c.flags & kContactToi) return false;
-    const DFixture& fa = x.fx[c.fixture_a];
-    const DFixture& fb = x.fx[c.fixture_b];
-    if (fa.sensor || fb.sensor) return false;
-    const dbox_body_state& bA = x.bs[fa.body];
-    const dbox_body_state& bB = x.bs[fb.body];
+    if (x.s_cq[ci] & 2) return false;
+    int2 cb = x.s_cbody[ci];
+    const dbox_body_state& bA = x.bs[b0 + cb.x];
+    const dbox_body_state& bB = x.bs[b0 + cb.y];
     bool activeA = (bA.flags & kBodyAwake) && bA.type != kStaticBody;
     bool activeB = (bB.flags & kBodyAwake) && bB.type != kStaticBody;
     if (!activeA && !activeB) return false;
@@ -1403,29 +1465,38 @@ DG void toi_update(const Ctx& x, dbox_contact_state& c) {
     }
 }
 
-// b2Island.SolveTOI (b2island.d:282-416) on the sub-island in s_isl_body / s_isl_contact; one lane.
-DG void solve_toi_island(const Ctx& x, const WorldInfo& wi, int nbI, int ncI, int toiA, int toiB, float subDt) {
-    int b0 = wi.body_start, c0 = wi.contact_start;
-    for (int t = 0; t < ncI; ++t) constraint_ctor(x, x.s_isl_contact[c0 + t], false, 1.0f);
+// b2Island.SolveTOI (b2island.d:282-416) on the sub-island in s_isl_body (world-local)
+// and s_isl_contact; one lane.  sb holds the island bodies' state for the solve.
+DG void solve_toi_island(const Ctx& x, const WorldInfo& wi, SB sb, int nbI, int ncI, int toiA, int toiB,
+                         float subDt) {
+    const int b0 = wi.body_start, c0 = wi.contact_start;
+    for (int i = 0; i < nbI; ++i) {
+        int b = x.s_isl_body[b0 + i];
+        sb_load(sb, b, x.bs[b0 + b]);
+    }
+    for (int t = 0; t < ncI; ++t) constraint_ctor(x, x.s_isl_contact[c0 + t], b0, false, 1.0f);
     for (int it = 0; it < 20; ++it) {
         float minSep = 0.0f;
-        for (int t = 0; t < ncI; ++t) minSep = bmin(minSep, solve_position(x, x.s_isl_contact[c0 + t], true, toiA, toiB));
+        for (int t = 0; t < ncI; ++t)
+            minSep = bmin(minSep, solve_position(x, x.s_isl_contact[c0 + t], sb, true, toiA, toiB));
         if (minSep >= -1.5f * kLinearSlop) break;
     }
-    dbox_body_state& A = x.bs[toiA];
-    dbox_body_state& B = x.bs[toiB];
-    A.sweep[2] = A.sweep[4]; A.sweep[3] = A.sweep[5]; A.sweep[6] = A.sweep[7];
-    B.sweep[2] = B.sweep[4]; B.sweep[3] = B.sweep[5]; B.sweep[6] = B.sweep[7];
-    for (int t = 0; t < ncI; ++t) constraint_init_velocity(x, x.s_isl_contact[c0 + t]);
+    dbox_body_state& A = x.bs[b0 + toiA];
+    dbox_body_state& B = x.bs[b0 + toiB];
+    float2 cA = sb.c(toiA), cB = sb.c(toiB);
+    A.sweep[2] = cA.x; A.sweep[3] = cA.y; A.sweep[6] = sb.a(toiA);
+    B.sweep[2] = cB.x; B.sweep[3] = cB.y; B.sweep[6] = sb.a(toiB);
+    for (int t = 0; t < ncI; ++t) constraint_init_velocity(x, x.s_isl_contact[c0 + t], sb);
     for (int it = 0; it < x.vel_iters; ++it)
-        for (int t = 0; t < ncI; ++t) solve_velocity(x, x.s_isl_contact[c0 + t]);
+        for (int t = 0; t < ncI; ++t) solve_velocity(x, x.s_isl_contact[c0 + t], sb);
     float h = subDt;
     for (int i = 0; i < nbI; ++i) {
-        dbox_body_state& Bd = x.bs[x.s_isl_body[b0 + i]];
-        float2 c = b_c(Bd);
-        float a = Bd.sweep[7];
-        float2 v = b_v(Bd);
-        float wv = Bd.vel[2];
+        int b = x.s_isl_body[b0 + i];
+        dbox_body_state& Bd = x.bs[b0 + b];
+        float2 c = sb.c(b);
+        float a = sb.a(b);
+        float2 v = sb.v(b);
+        float wv = sb.w(b);
         float2 translation = h * v;
         if (dot(translation, translation) > kMaxTranslationSquared) {
             float ratio = fdiv(kMaxTranslation, length(translation));
@@ -1453,6 +1524,12 @@ __global__ void k_toi(Ctx x) {
     const int b0 = wi.body_start, nb = wi.body_count, c0 = wi.contact_start;
     if (x.continuous && x.dt > 0.0f) {
         bool advanced = wd.step_complete == 0;
+        SB sb;
+        sb.p = x.s_sbody + 6 * (size_t)b0;
+        {
+            int n = wd.contact_count;
+            for (int k = lane; k < n; k += kWarp) contact_compact(x, c0 + k, b0);
+        }
         if (wd.step_complete) {                                          // b2world.d:1131-1146
             for (int i = lane; i < nb; i += kWarp) {
                 x.bs[b0 + i].flags &= ~(uint32_t)kBodyIsland;
@@ -1466,39 +1543,50 @@ __global__ void k_toi(Ctx x) {
                 c.toi = 1.0f;
             }
         }
+        for (int i = lane; i < nb; i += kWarp) x.s_bfl[b0 + i] = 0;
         tsync();
         int events = 0;
+        const int max_events = 9 * wi.contact_cap + 16;   // each contact takes at most 9 events
         for (int iter = 0;; ++iter) {
-            if (iter >= kMaxToiLoop) {
+            if (iter >= max_events) {
                 if (lane == 0) set_error(x, w, DBOX_ERR_TIMEOUT);
                 break;
             }
             int n = wd.contact_count;
             // sweeps are put onto a common time in list order (b2world.d:1212-1226)
-            if (advanced && lane == 0) {
-                for (int k = n - 1; k >= 0; --k) {
-                    const dbox_contact_state& c = x.ct[c0 + k];
-                    if (!toi_needs(x, c)) continue;
-                    dbox_body_state& bA = x.bs[x.fx[c.fixture_a].body];
-                    dbox_body_state& bB = x.bs[x.fx[c.fixture_b].body];
-                    float alpha0 = bA.sweep[8];
-                    if (bA.sweep[8] < bB.sweep[8]) {
-                        alpha0 = bB.sweep[8];
-                        Sweep s = b_sweep(bA); sweep_advance(s, alpha0); b_set_sweep(bA, s);
-                    } else if (bB.sweep[8] < bA.sweep[8]) {
-                        alpha0 = bA.sweep[8];
-                        Sweep s = b_sweep(bB); sweep_advance(s, alpha0); b_set_sweep(bB, s);
+            if (advanced) {
+                for (int base = n - 1; base >= 0; base -= kWarp) {
+                    int k = base - lane;
+                    bool need = k >= 0 && toi_needs(x, c0 + k, b0);
+                    unsigned bal = __ballot_sync(0xffffffffu, need);
+                    if (lane == 0) {
+                        while (bal) {
+                            int l = __ffs(bal) - 1;
+                            bal &= bal - 1;
+                            int kk = base - l;
+                            int2 cb = x.s_cbody[c0 + kk];
+                            dbox_body_state& bA = x.bs[b0 + cb.x];
+                            dbox_body_state& bB = x.bs[b0 + cb.y];
+                            float alpha0 = bA.sweep[8];
+                            if (bA.sweep[8] < bB.sweep[8]) {
+                                alpha0 = bB.sweep[8];
+                                Sweep s = b_sweep(bA); sweep_advance(s, alpha0); b_set_sweep(bA, s);
+                            } else if (bB.sweep[8] < bA.sweep[8]) {
+                                alpha0 = bA.sweep[8];
+                                Sweep s = b_sweep(bB); sweep_advance(s, alpha0); b_set_sweep(bB, s);
+                            }
+                            SweepSnap& sn = x.snap[c0 + kk];
+                            sn.a = b_sweep(bA);
+                            sn.b = b_sweep(bB);
+                            sn.alpha0 = alpha0;
+                        }
                     }
-                    SweepSnap& sn = x.snap[c0 + k];
-                    sn.a = b_sweep(bA);
-                    sn.b = b_sweep(bB);
-                    sn.alpha0 = alpha0;
+                    tsync();
                 }
             }
-            tsync();
             for (int k = lane; k < n; k += kWarp) {
+                if (!toi_needs(x, c0 + k, b0)) continue;
                 dbox_contact_state& c = x.ct[c0 + k];
-                if (!toi_needs(x, c)) continue;
                 const DFixture& fa = x.fx[c.fixture_a];
                 const DFixture& fb = x.fx[c.fixture_b];
                 Sweep sA, sB;
@@ -1531,15 +1619,15 @@ __global__ void k_toi(Ctx x) {
                 if (lane == 0) wd.step_complete = 1;
                 break;
             }
-            float minAlpha = bestA;
-            int mk = n - 1 - bestLp;
-            bool solved = false;
+            const float minAlpha = bestA;
+            const int mk = n - 1 - bestLp;
+            const int2 mcb = x.s_cbody[c0 + mk];
+            int solved = 0, nbI = 0, ncI = 0;
             if (lane == 0) {
                 ++events;
                 dbox_contact_state& mc = x.ct[c0 + mk];
-                int ia = x.fx[mc.fixture_a].body, ib = x.fx[mc.fixture_b].body;
-                dbox_body_state& bA = x.bs[ia];
-                dbox_body_state& bB = x.bs[ib];
+                dbox_body_state& bA = x.bs[b0 + mcb.x];
+                dbox_body_state& bB = x.bs[b0 + mcb.y];
                 Sweep backup1 = b_sweep(bA), backup2 = b_sweep(bB);
                 b_advance(bA, minAlpha);
                 b_advance(bB, minAlpha);
@@ -1553,73 +1641,95 @@ __global__ void k_toi(Ctx x) {
                     b_sync_transform(bA);
                     b_sync_transform(bB);
                 } else {
-                    solved = true;
+                    solved = 1;
                     b_set_awake(bA, true);
                     b_set_awake(bB, true);
-                    int nbI = 0, ncI = 0;
-                    x.s_isl_body[b0 + nbI++] = ia;
-                    x.s_isl_body[b0 + nbI++] = ib;
+                    x.s_isl_body[b0 + nbI++] = mcb.x;
+                    x.s_isl_body[b0 + nbI++] = mcb.y;
                     x.s_isl_contact[c0 + ncI++] = c0 + mk;
                     bA.flags |= kBodyIsland;
                     bB.flags |= kBodyIsland;
                     mc.flags |= kContactIsland;
-                    int pair[2] = {ia, ib};
-                    for (int q = 0; q < 2; ++q) {
-                        int body = pair[q];
-                        dbox_body_state& Bd = x.bs[body];
-                        if (Bd.type != kDynamicBody) continue;
-                        for (int k = n - 1; k >= 0; --k) {
-                            dbox_contact_state& c = x.ct[c0 + k];
-                            int fA = x.fx[c.fixture_a].body, fB = x.fx[c.fixture_b].body;
-                            if (fA != body && fB != body) continue;
-                            if (nbI == 2 * kMaxTOIContacts) break;
-                            if (ncI == kMaxTOIContacts) break;
-                            if (c.flags & kContactIsland) continue;
-                            int other = fA == body ? fB : fA;
-                            dbox_body_state& O = x.bs[other];
-                            if (O.type == kDynamicBody && (Bd.flags & kBodyBullet) == 0 && (O.flags & kBodyBullet) == 0) continue;
-                            if (x.fx[c.fixture_a].sensor || x.fx[c.fixture_b].sensor) continue;
-                            Sweep backup = b_sweep(O);
-                            if ((O.flags & kBodyIsland) == 0) b_advance(O, minAlpha);
-                            toi_update(x, c);
-                            if ((c.flags & kContactEnabled) == 0 || (c.flags & kContactTouching) == 0) {
-                                b_set_sweep(O, backup);
-                                b_sync_transform(O);
-                                continue;
-                            }
-                            c.flags |= kContactIsland;
-                            x.s_isl_contact[c0 + ncI++] = c0 + k;
-                            if (O.flags & kBodyIsland) continue;
-                            O.flags |= kBodyIsland;
-                            if (O.type != kStaticBody) b_set_awake(O, true);
-                            x.s_isl_body[b0 + nbI++] = other;
-                        }
-                    }
-                    float subDt = (1.0f - minAlpha) * x.dt;
-                    solve_toi_island(x, wi, nbI, ncI, ia, ib, subDt);
-                    for (int i = 0; i < nbI; ++i) {
-                        int body = x.s_isl_body[b0 + i];
-                        dbox_body_state& Bd = x.bs[body];
-                        Bd.flags &= ~(uint32_t)kBodyIsland;
-                        if (Bd.type != kDynamicBody) continue;
-                        sync_fixtures(x, body);
-                        for (int k = 0; k < n; ++k) {
-                            dbox_contact_state& c = x.ct[c0 + k];
-                            if (x.fx[c.fixture_a].body == body || x.fx[c.fixture_b].body == body)
-                                c.flags &= ~(uint32_t)(kContactToi | kContactIsland);
-                        }
-                    }
                 }
             }
             solved = __shfl_sync(0xffffffffu, solved, 0);
-            tsync();
-            advanced = true;
+            nbI = __shfl_sync(0xffffffffu, nbI, 0);
+            ncI = __shfl_sync(0xffffffffu, ncI, 0);
             if (solved) {
-                find_new_contacts(x, w);
-                if (x.sub_stepping) {
-                    if (lane == 0) wd.step_complete = 0;
-                    break;
+                // contacts of each dynamic event body, in its edge-list order (b2world.d:1306-1411)
+                for (int q = 0; q < 2; ++q) {
+                    const int body = q == 0 ? mcb.x : mcb.y;
+                    if (x.bs[b0 + body].type != kDynamicBody) continue;
+                    bool stop = false;
+                    for (int base = n - 1; base >= 0 && !stop; base -= kWarp) {
+                        int k = base - lane;
+                        bool hit = false;
+                        if (k >= 0) { int2 cb = x.s_cbody[c0 + k]; hit = cb.x == body || cb.y == body; }
+                        unsigned bal = __ballot_sync(0xffffffffu, hit);
+                        if (lane == 0) {
+                            dbox_body_state& Bd = x.bs[b0 + body];
+                            while (bal) {
+                                int l = __ffs(bal) - 1;
+                                bal &= bal - 1;
+                                int kk = base - l;
+                                if (nbI == 2 * kMaxTOIContacts || ncI == kMaxTOIContacts) { stop = true; break; }
+                                dbox_contact_state& c = x.ct[c0 + kk];
+                                if (c.flags & kContactIsland) continue;
+                                int2 cb = x.s_cbody[c0 + kk];
+                                int other = cb.x == body ? cb.y : cb.x;
+                                dbox_body_state& O = x.bs[b0 + other];
+                                if (O.type == kDynamicBody && (Bd.flags & kBodyBullet) == 0 && (O.flags & kBodyBullet) == 0) continue;
+                                if (x.s_cq[c0 + kk] & 2) continue;
+                                Sweep backup = b_sweep(O);
+                                if ((O.flags & kBodyIsland) == 0) b_advance(O, minAlpha);
+                                toi_update(x, c);
+                                if ((c.flags & kContactEnabled) == 0 || (c.flags & kContactTouching) == 0) {
+                                    b_set_sweep(O, backup);
+                                    b_sync_transform(O);
+                                    continue;
+                                }
+                                c.flags |= kContactIsland;
+                                x.s_isl_contact[c0 + ncI++] = c0 + kk;
+                                if (O.flags & kBodyIsland) continue;
+                                O.flags |= kBodyIsland;
+                                if (O.type != kStaticBody) b_set_awake(O, true);
+                                x.s_isl_body[b0 + nbI++] = other;
+                            }
+                        }
+                        stop = __shfl_sync(0xffffffffu, stop, 0);
+                    }
+                    nbI = __shfl_sync(0xffffffffu, nbI, 0);
+                    ncI = __shfl_sync(0xffffffffu, ncI, 0);
                 }
+                if (lane == 0) {
+                    float subDt = (1.0f - minAlpha) * x.dt;
+                    solve_toi_island(x, wi, sb, nbI, ncI, mcb.x, mcb.y, subDt);
+                    for (int i = 0; i < nbI; ++i) {
+                        int body = x.s_isl_body[b0 + i];
+                        dbox_body_state& Bd = x.bs[b0 + body];
+                        Bd.flags &= ~(uint32_t)kBodyIsland;
+                        if (Bd.type != kDynamicBody) continue;
+                        x.s_bfl[b0 + body] = kBfMark;
+                        sync_fixtures(x, b0 + body);
+                    }
+                }
+                tsync();
+                // invalidate the TOIs of every contact on a displaced dynamic body
+                for (int k = lane; k < n; k += kWarp) {
+                    int2 cb = x.s_cbody[c0 + k];
+                    if ((x.s_bfl[b0 + cb.x] | x.s_bfl[b0 + cb.y]) & kBfMark)
+                        x.ct[c0 + k].flags &= ~(uint32_t)(kContactToi | kContactIsland);
+                }
+                tsync();
+                if (lane == 0)
+                    for (int i = 0; i < nbI; ++i) x.s_bfl[b0 + x.s_isl_body[b0 + i]] = 0;
+                tsync();
+                find_new_contacts(x, w);
+            }
+            advanced = true;
+            if (solved && x.sub_stepping) {
+                if (lane == 0) wd.step_complete = 0;
+                break;
             }
         }
         if (lane == 0) { wd.toi_events = events; wd.acc_toi_events += (unsigned long long)events; }
@@ -1651,7 +1761,7 @@ extern "C" int dbox_launch_step_ev(const dg::Ctx* x, cudaStream_t stream, int* l
     dg::k_collide<<<flat_blocks, 256, 0, stream>>>(*x);
     dg::k_collide_finish<<<team_blocks, threads, 0, stream>>>(*x);
     if (ev) cudaEventRecordWithFlags(ev[1], stream, cudaEventRecordExternal);
-    dg::k_solve<<<team_blocks, threads, 0, stream>>>(*x);
+    dg::k_solve<<<team_blocks, threads, dg::kSolveWarps * dg::kSmemBodies * 6 * sizeof(float), stream>>>(*x);
     if (ev) cudaEventRecordWithFlags(ev[2], stream, cudaEventRecordExternal);
     dg::k_toi<<<team_blocks, threads, 0, stream>>>(*x);
     if (ev) cudaEventRecordWithFlags(ev[3], stream, cudaEventRecordExternal);

@@ -157,6 +157,11 @@ struct Ctx {
     VC* vc;                        // contact-slot-indexed
     PC* pc;                        // contact-slot-indexed
     SweepSnap* snap;               // contact-slot-indexed
+    int2* s_cbody;                 // contact-slot-indexed: world-local bodies of the contact
+    unsigned char* s_cq;           // contact-slot-indexed: bit0 island-graph edge, bit1 sensor
+    unsigned char* s_cvis;         // contact-slot-indexed: visited by the island search
+    unsigned char* s_bfl;          // body-indexed: awake/active/static/dynamic/visited/mark bits
+    float* s_sbody;                // 6 per body: solver velocity and position (global fallback)
     // step parameters
     float dt, inv_dt;
     int vel_iters, pos_iters;
