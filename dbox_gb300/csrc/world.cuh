@@ -80,7 +80,7 @@ struct DJoint {                    // b2RevoluteJoint (joints/b2revolutejoint.d)
 
 // b2ContactVelocityConstraint (contacts/b2contactsolver.d:43-58) with body indices in place of island indices.
 struct VPoint { float2 rA, rB; float normalImpulse, tangentImpulse, normalMass, tangentMass, velocityBias; };
-struct VC {
+struct __align__(16) VC {
     VPoint p[2];
     float2 normal;
     float K[4];         // ex.x ex.y ey.x ey.y
@@ -91,7 +91,7 @@ struct VC {
     int pointCount;
 };
 // b2ContactPositionConstraint (b2contactsolver.d:801-814)
-struct PC {
+struct __align__(16) PC {
     float2 localPoints[2];
     float2 localNormal, localPoint;
     float2 lcA, lcB;

@@ -22,19 +22,34 @@ def _box(hx, hy):
     return s
 
 
-def test_portable_trig_is_correctly_rounded(oracle_lib):
+def _ulp_error(got, x, fn):
+    exact = fn(x.astype(np.float64))
+    r = exact.astype(np.float32)
+    _, e = np.frexp(r.astype(np.float64))
+    ulp = np.ldexp(1.0, e - 24)
+    return np.abs(got.astype(np.float64) - exact) / ulp
+
+
+def test_portable_trig_accuracy(oracle_lib):
+    # dbox_sincosf: binary32 + FMA below |x| = 1024 (error < 0.75 ulp), binary64 above (correctly rounded)
     rng = np.random.default_rng(0)
-    xs = np.concatenate([
-        rng.uniform(-10.0, 10.0, 200000), rng.uniform(-1e4, 1e4, 50000), rng.uniform(-1e30, 1e30, 20000),
-        np.array([0.0, -0.0, 1e-30, np.pi / 2, 1e5, 131071.99, 131072.0], np.float64),
-    ]).astype(np.float32)
+    small = np.concatenate([rng.uniform(-10.0, 10.0, 300000), rng.uniform(-1024.0, 1024.0, 100000),
+                            np.array([1e-30, 1e-8, np.pi / 4, np.pi / 2, 1024.0], np.float64)]).astype(np.float32)
     oracle_lib.set_trig_mode(1)
-    s, c = oracle_lib.sincos_array(xs)
-    ref_s = np.sin(xs.astype(np.float64)).astype(np.float32)
-    ref_c = np.cos(xs.astype(np.float64)).astype(np.float32)
-    assert (s.view(np.uint32) == ref_s.view(np.uint32)).mean() > 1 - 1e-6
-    assert (c.view(np.uint32) == ref_c.view(np.uint32)).mean() > 1 - 1e-6
-    assert np.signbit(s[xs == 0][np.signbit(xs[xs == 0])]).all()   # sin(-0) = -0
+    s, c = oracle_lib.sincos_array(small)
+    assert _ulp_error(s, small, np.sin).max() < 0.75
+    assert _ulp_error(c, small, np.cos).max() < 0.75
+    cr = (s == np.sin(small.astype(np.float64)).astype(np.float32)).mean()
+    assert cr > 0.98          # glibc 2.39 sinf: 0.987 on the same kind of sample
+    big = np.concatenate([rng.uniform(-1e5, 1e5, 50000), rng.uniform(-1e30, 1e30, 20000),
+                          np.array([1024.0001, 131071.99, 131072.0], np.float64)]).astype(np.float32)
+    big = big[np.abs(big) > 1024.0]
+    s, c = oracle_lib.sincos_array(big)
+    assert (s == np.sin(big.astype(np.float64)).astype(np.float32)).mean() > 1 - 1e-5
+    assert (c == np.cos(big.astype(np.float64)).astype(np.float32)).mean() > 1 - 1e-5
+    z = np.array([0.0, -0.0], np.float32)
+    s, c = oracle_lib.sincos_array(z)
+    assert np.signbit(s).tolist() == [False, True] and c.tolist() == [1.0, 1.0]
 
 
 def test_libm_trig_mode_is_the_host_runtime(oracle_lib):
