@@ -64,6 +64,8 @@ def lib():
     L.dbox_collide_manifolds_noalloc.argtypes = [i32, vp, vp, vp, vp, vp]
     L.dbox_world_step_n_timed.argtypes = [vp, f32, i32, i32, i32, vp, vp]
     L.dbox_world_get_counters.argtypes = [vp, vp]
+    L.dbox_world_set_phase_profile.argtypes = [vp, i32]
+    L.dbox_world_get_phase_profile.argtypes = [vp, vp]
     L.dbox_world_apply_forces.argtypes = [vp, vp]
     L.dbox_world_get_transforms.argtypes = [vp, vp]
     L.dbox_body_def_default.argtypes = [vp]
@@ -167,6 +169,15 @@ class World:
         _check(lib().dbox_world_get_counters(self.h, abi.ptr(c)), "dbox_world_get_counters")
         keys = ("isl_bodies", "isl_contacts", "vsolve", "psolve", "contacts", "toi_events", "world_steps", "pairs")
         return dict(zip(keys, (int(v) for v in c)))
+
+    def set_phase_profile(self, on=True):
+        _check(lib().dbox_world_set_phase_profile(self.h, 1 if on else 0), "set_phase_profile")
+
+    def phase_profile(self):
+        """(n_worlds, 16) uint64: clock64 stamps of the solve phases, then levels, contacts, bodies."""
+        out = np.zeros((self.n_worlds, 16), np.uint64)
+        _check(lib().dbox_world_get_phase_profile(self.h, abi.ptr(out)), "get_phase_profile")
+        return out
 
     def apply_forces(self, force_torque):
         """ApplyForceToCenter + ApplyTorque (wake = false) on every body; (n_bodies, 3) float32, ideally pinned."""

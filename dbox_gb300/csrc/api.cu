@@ -19,6 +19,7 @@
 #include "host_geom.h"
 
 extern "C" int dbox_launch_step(const dg::Ctx* x, cudaStream_t stream, int* launches);
+extern "C" const void* dbox_solve_kernel();
 extern "C" int dbox_launch_step_ev(const dg::Ctx* x, cudaStream_t stream, int* launches, cudaEvent_t* ev);
 extern "C" int dbox_launch_gather_transforms(int n, const dbox_body_state* bs, float* out, cudaStream_t s);
 extern "C" int dbox_launch_apply_forces(int n, dbox_body_state* bs, const float* f, cudaStream_t s);
@@ -98,13 +99,17 @@ struct dbox_world {
         s_isl_cstart, s_isl_jstart, s_isl_flags, s_pcount, s_moved, s_cstate, s_adj_items, s_isl_contact, s_level,
         s_sched_v, s_lvl_v, s_sched_p, s_lvl_p, s_tmp, s_isl_joint, s_accept, g_status;
     DBuf<unsigned> s_isl_minsep, s_isl_sleep;
-    DBuf<dg::VC> d_vc;
-    DBuf<dg::PC> d_pc;
+    DBuf<dg::VRow> d_vr, d_tvr;
+    DBuf<dg::PRow> d_pr, d_tpr;
+    DBuf<int> s_vpos, d_solve_world, d_solve_smem;
+    int solve_blocks = 0, solve_smem_floats = 0;
     DBuf<dg::SweepSnap> d_snap;
     DBuf<float> d_io;           // staging for bulk force upload / transform readback (3 floats per body)
     DBuf<int2> s_cbody;
     DBuf<unsigned char> s_cq, s_cvis, s_bfl;
     DBuf<float> s_sbody;
+    DBuf<unsigned long long> d_prof;
+    int profiling = 0;
     std::vector<dg::WorldInfo> wi;
     int total_bodies = 0, total_fixtures = 0, total_contacts = 0, total_joints = 0;
     // graph replay
@@ -139,13 +144,73 @@ void free_device(dbox_world* w) {
                          &w->s_accept, &w->g_status};
     for (auto* b : ints) b->free();
     w->s_isl_minsep.free(); w->s_isl_sleep.free();
-    w->d_vc.free(); w->d_pc.free(); w->d_snap.free(); w->d_io.free();
-    w->s_cbody.free(); w->s_cq.free(); w->s_cvis.free(); w->s_bfl.free(); w->s_sbody.free();
+    w->d_vr.free(); w->d_tvr.free(); w->d_pr.free(); w->d_tpr.free(); w->d_snap.free(); w->d_io.free();
+    w->s_vpos.free(); w->d_solve_world.free(); w->d_solve_smem.free();
+    w->s_cbody.free(); w->s_cq.free(); w->s_cvis.free(); w->s_bfl.free(); w->s_sbody.free(); w->d_prof.free();
     if (w->graph) { cudaGraphExecDestroy(w->graph); w->graph = nullptr; }
     if (w->tgraph) { cudaGraphExecDestroy(w->tgraph); w->tgraph = nullptr; }
 }
 
 int next_pow2(int v) { int p = 1; while (p < v) p <<= 1; return p; }
+
+// Warp slots of the solve kernel (four per block).  Each world's solver body rows
+// (24 bytes a body) go to shared memory when they fit the block's budget; worlds are
+// placed largest first (first fit over the open blocks), so the biggest worlds sit in
+// the lowest blocks and start first, and small worlds fill the remaining room.
+int pack_solve_slots(dbox_world* w) {
+    const int W = (int)w->wi.size();
+    int max_nb = 0;
+    for (const auto& wi : w->wi) max_nb = std::max(max_nb, wi.body_count);
+    // budget in bodies per block: room for the largest world, at least 1024, and at most
+    // 1536 when there are enough worlds to fill the GPU (three blocks per SM stay resident);
+    // the front of the block holds each warp's constraint-row staging slots
+    const int stage_floats = dg::kSolveWarps * dg::kStageFloats;
+    const int hard_cap = (227 * 1024 - 1024 - 4 * stage_floats) / 24;
+    int budget = std::max(1024, max_nb);
+    budget = std::min(budget, W >= 3 * 152 ? 1536 : hard_cap);
+    std::vector<int> order(W);
+    for (int i = 0; i < W; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return w->wi[a].body_count > w->wi[b].body_count; });
+    std::vector<int> used, count, slot_world, slot_off;
+    size_t first_open = 0;
+    for (int wid : order) {
+        int nbw = w->wi[wid].body_count;
+        bool in_smem = nbw <= budget;
+        int need = in_smem ? nbw : 0;
+        int chosen = -1;
+        for (size_t b = first_open, tries = 0; b < used.size() && tries < 64; ++b, ++tries)
+            if (count[b] < dg::kSolveWarps && used[b] + need <= budget) { chosen = (int)b; break; }
+        if (chosen < 0) {
+            chosen = (int)used.size();
+            used.push_back(0);
+            count.push_back(0);
+            slot_world.resize(used.size() * dg::kSolveWarps, -1);
+            slot_off.resize(used.size() * dg::kSolveWarps, -1);
+        }
+        int slot = chosen * dg::kSolveWarps + count[chosen]++;
+        slot_world[slot] = wid;
+        slot_off[slot] = in_smem ? stage_floats + 6 * used[chosen] : -1;
+        used[chosen] += need;
+        while (first_open < used.size() && count[first_open] == dg::kSolveWarps) ++first_open;
+    }
+    if (used.empty()) {                     // no worlds: one idle block
+        used.push_back(0);
+        slot_world.assign(dg::kSolveWarps, -1);
+        slot_off.assign(dg::kSolveWarps, -1);
+    }
+    int max_used = 0;
+    for (int u : used) max_used = std::max(max_used, u);
+    w->solve_blocks = (int)used.size();
+    w->solve_smem_floats = stage_floats + 6 * std::max(max_used, 1);
+    if (w->d_solve_world.alloc(slot_world.size()) || w->d_solve_smem.alloc(slot_off.size()))
+        return fail(DBOX_ERR_CUDA, "device allocation failed (solve slots)");
+    CU(cudaMemcpy(w->d_solve_world.p, slot_world.data(), sizeof(int) * slot_world.size(), cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(w->d_solve_smem.p, slot_off.data(), sizeof(int) * slot_off.size(), cudaMemcpyHostToDevice));
+    CU(cudaFuncSetAttribute(dbox_solve_kernel(), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)(sizeof(float) * w->solve_smem_floats)));
+    return DBOX_OK;
+}
 
 // Pull the authoritative dynamic state back to the host mirrors.
 int download(dbox_world* w) {
@@ -304,8 +369,11 @@ int upload(dbox_world* w) {
     ok &= w->s_isl_joint.alloc(nj) == 0;
     ok &= w->s_accept.alloc(np) == 0;
     ok &= w->g_status.alloc(1) == 0;
-    ok &= w->d_vc.alloc(nc) == 0;
-    ok &= w->d_pc.alloc(nc) == 0;
+    ok &= w->d_vr.alloc(nkx) == 0;
+    ok &= w->d_pr.alloc(nkx) == 0;
+    ok &= w->d_tvr.alloc((size_t)dg::kMaxTOIContacts * W) == 0;
+    ok &= w->d_tpr.alloc((size_t)dg::kMaxTOIContacts * W) == 0;
+    ok &= w->s_vpos.alloc(nc) == 0;
     ok &= w->d_snap.alloc(nc) == 0;
     ok &= w->d_io.alloc(3 * (size_t)nb) == 0;
     ok &= w->s_cbody.alloc(nc) == 0;
@@ -313,7 +381,9 @@ int upload(dbox_world* w) {
     ok &= w->s_cvis.alloc(nc) == 0;
     ok &= w->s_bfl.alloc(nb) == 0;
     ok &= w->s_sbody.alloc(6 * (size_t)nb) == 0;
+    ok &= w->d_prof.alloc(16 * (size_t)W) == 0;
     if (!ok) { free_device(w); return fail(DBOX_ERR_CUDA, "device allocation failed (%d bodies, %d contact slots)", nb, nc); }
+    if (pack_solve_slots(w) != DBOX_OK) { free_device(w); return DBOX_ERR_CUDA; }
     CU(cudaMemcpy(w->d_wi.p, w->wi.data(), sizeof(dg::WorldInfo) * W, cudaMemcpyHostToDevice));
     CU(cudaMemcpy(w->d_wd.p, wd.data(), sizeof(dg::WorldDyn) * W, cudaMemcpyHostToDevice));
     if (nb) {
@@ -397,8 +467,15 @@ dg::Ctx make_ctx(dbox_world* w, float dt, int vi, int pi) {
     x.s_tmp = w->s_tmp.p;
     x.s_isl_joint = w->s_isl_joint.p;
     x.s_accept = w->s_accept.p;
-    x.vc = w->d_vc.p;
-    x.pc = w->d_pc.p;
+    x.vr = w->d_vr.p;
+    x.pr = w->d_pr.p;
+    x.tvr = w->d_tvr.p;
+    x.tpr = w->d_tpr.p;
+    x.s_vpos = w->s_vpos.p;
+    x.solve_world = w->d_solve_world.p;
+    x.solve_smem = w->d_solve_smem.p;
+    x.solve_blocks = w->solve_blocks;
+    x.solve_smem_floats = w->solve_smem_floats;
     x.snap = w->d_snap.p;
     x.s_cbody = w->s_cbody.p;
     x.s_cq = w->s_cq.p;
@@ -416,6 +493,7 @@ dg::Ctx make_ctx(dbox_world* w, float dt, int vi, int pi) {
     x.allow_sleep = w->allow_sleep;
     x.record_events = w->listener ? 1 : 0;
     x.g_status = w->g_status.p;
+    x.prof = w->profiling ? w->d_prof.p : nullptr;
     return x;
 }
 
@@ -931,6 +1009,22 @@ int32_t dbox_world_get_transforms(dbox_world* w, float* xya) {
     if (err) return fail(DBOX_ERR_CUDA, "gather launch: %s", cudaGetErrorString((cudaError_t)err));
     CU(cudaMemcpyAsync(xya, w->d_io.p, sizeof(float) * 3 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
     CU(cudaStreamSynchronize(w->stream));
+    return DBOX_OK;
+}
+
+int32_t dbox_world_set_phase_profile(dbox_world* w, int32_t enable) {
+    if (!w) return DBOX_ERR_INVALID;
+    w->profiling = enable ? 1 : 0;
+    if (w->graph) { cudaGraphExecDestroy(w->graph); w->graph = nullptr; }
+    if (w->tgraph) { cudaGraphExecDestroy(w->tgraph); w->tgraph = nullptr; }
+    return DBOX_OK;
+}
+
+int32_t dbox_world_get_phase_profile(dbox_world* w, unsigned long long* out) {
+    if (!w || !out) return DBOX_ERR_INVALID;
+    if (!w->on_device || !w->d_prof.p) return DBOX_ERR_INVALID;
+    CU(cudaStreamSynchronize(w->stream));
+    CU(cudaMemcpy(out, w->d_prof.p, sizeof(unsigned long long) * 16 * w->worlds.size(), cudaMemcpyDeviceToHost));
     return DBOX_OK;
 }
 

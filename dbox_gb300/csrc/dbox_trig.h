@@ -209,13 +209,12 @@ DBOX_TRIG_HD void sincos_f32(float x, float* s_out, float* c_out) {
     float lo = (1.0f - hi) - w;                      // exact: |w| <= 0.31
     float cos_lo = ((lo - 0.5f * ez) - rh * rl) + (z * z) * pc;
     float cr = hi + cos_lo;
-    float s, c;
-    switch (((int)k) & 3) {
-    case 0: s = sr; c = cr; break;
-    case 1: s = cr; c = -sr; break;
-    case 2: s = -sr; c = -cr; break;
-    default: s = -cr; c = sr; break;
-    }
+    // quadrant q: (sin, cos) = (sr, cr), (cr, -sr), (-sr, -cr), (-cr, sr) for q = 0..3
+    int q = ((int)k) & 3;
+    float s = (q & 1) ? cr : sr;
+    float c = (q & 1) ? sr : cr;
+    if (q & 2) s = -s;
+    if ((q + 1) & 2) c = -c;
     *s_out = s;
     *c_out = c;
 }
@@ -224,6 +223,24 @@ DBOX_TRIG_HD void sincos_f32(float x, float* s_out, float* c_out) {
 
 // sin and cos of a binary32 angle (b2Rot.Set): identical bits on the host and the device.
 DBOX_TRIG_HD void dbox_sincosf(float x, float* s_out, float* c_out) {
+#ifdef __CUDA_ARCH__
+    // device: the binary32 path runs for every input and the rare cases are patched after
+    // it, so the lanes of a warp stay on one path (same results as the branches below)
+    float s, c;
+    dbox_trig::sincos_f32(x, &s, &c);
+    float ax = fabsf(x);
+    if (!(ax <= 1024.0f)) {
+        if (ax == ax && ax != __int_as_float(0x7f800000)) {
+            dbox_trig::sincos_f64(x, &s, &c);
+        } else {
+            s = x - x;
+            c = s;
+        }
+    }
+    if (x == 0.0f) { s = x; c = 1.0f; }
+    *s_out = s;
+    *c_out = c;
+#else
     union { float f; uint32_t u; } cv; cv.f = x;
     if ((cv.u & 0x7f800000u) == 0x7f800000u) {  // inf or nan
         float n = x - x;
@@ -234,4 +251,5 @@ DBOX_TRIG_HD void dbox_sincosf(float x, float* s_out, float* c_out) {
     float ax = x < 0.0f ? -x : x;
     if (ax <= 1024.0f) dbox_trig::sincos_f32(x, s_out, c_out);
     else dbox_trig::sincos_f64(x, s_out, c_out);
+#endif
 }

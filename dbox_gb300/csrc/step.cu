@@ -30,6 +30,10 @@ constexpr int kNoWake = 0x7fffffff;
 constexpr unsigned long long kHashEmpty = 0xffffffffffffffffull;
 
 DG int lane_id() { return threadIdx.x & 31; }
+// phase stamp for the optional per-world profile (slot 0..15), lane 0 only
+DG void stamp(const Ctx& x, int w, int slot) {
+    if (x.prof && (threadIdx.x & 31) == 0) x.prof[16 * (size_t)w + slot] = clock64();
+}
 DG void tsync() { __syncwarp(); }
 
 // ------------------------------------------------------------ contact pair hash (existence test of AddPair)
@@ -447,14 +451,12 @@ enum { kBfAwake = 1, kBfActive = 2, kBfStatic = 4, kBfDynamic = 8, kBfVisited = 
 
 // ------------------------------------------------------------ contact solver pieces (contacts/b2contactsolver.d)
 // b2ContactSolver ctor (:244-329) for one contact; body indices are world-local.
-DG void constraint_ctor(const Ctx& x, int ci, int b0, bool warm, float dtRatio) {
+DG void constraint_ctor(const Ctx& x, int ci, int b0, bool warm, float dtRatio, VC& vc, PC& pc) {
     const dbox_contact_state& c = x.ct[ci];
     const DFixture& fa = x.fx[c.fixture_a];
     const DFixture& fb = x.fx[c.fixture_b];
     const dbox_body_state& ba = x.bs[fa.body];
     const dbox_body_state& bb = x.bs[fb.body];
-    VC vc;
-    PC pc;
     int pointCount = c.point_count;
     vc.friction = c.friction;
     vc.restitution = c.restitution;
@@ -499,14 +501,10 @@ DG void constraint_ctor(const Ctx& x, int ci, int b0, bool warm, float dtRatio) 
         p.velocityBias = 0.0f;
         pc.localPoints[j] = j < pointCount ? v2(c.points[j].local_point[0], c.points[j].local_point[1]) : v2(0.0f, 0.0f);
     }
-    x.vc[ci] = vc;
-    x.pc[ci] = pc;
 }
 
 // InitializeVelocityConstraints (:338-450) for one contact
-DG void constraint_init_velocity(const Ctx& x, int ci, SB sb) {
-    VC vc = x.vc[ci];
-    const PC& pc = x.pc[ci];
+DG void constraint_init_velocity(VC& vc, const PC& pc, SB sb) {
     int pointCount = vc.pointCount;
     float mA = vc.invMassA, mB = vc.invMassB, iA = vc.invIA, iB = vc.invIB;
     float2 cA = sb.c(vc.bodyA), cB = sb.c(vc.bodyB);
@@ -603,11 +601,9 @@ DG void constraint_init_velocity(const Ctx& x, int ci, SB sb) {
             vc.pointCount = 1;
         }
     }
-    x.vc[ci] = vc;
 }
 
-DG void warm_start(const Ctx& x, int ci, SB sb) {                      // :452-490
-    const VC vc = x.vc[ci];
+DG void warm_start(const VC& vc, SB sb) {                              // :452-490
     float mA = vc.invMassA, iA = vc.invIA, mB = vc.invMassB, iB = vc.invIB;
     float2 vA = sb.v(vc.bodyA), vB = sb.v(vc.bodyB);
     float wA = sb.w(vc.bodyA), wB = sb.w(vc.bodyB);
@@ -637,8 +633,7 @@ DG void apply_block(float2& vA, float& wA, float2& vB, float& wB, float mA, floa
     wB += iB * (cross(cp1.rB, P1) + cross(cp2.rB, P2));
 }
 
-DG void solve_velocity(const Ctx& x, int ci, SB sb) {                  // :492-772
-    VC vc = x.vc[ci];
+DG void solve_velocity(VC& vc, SB sb) {                                // :492-772
     float mA = vc.invMassA, iA = vc.invIA, mB = vc.invMassB, iB = vc.invIB;
     int pointCount = vc.pointCount;
     float2 vA = sb.v(vc.bodyA), vB = sb.v(vc.bodyB);
@@ -689,69 +684,105 @@ DG void solve_velocity(const Ctx& x, int ci, SB sb) {                  // :492-7
         b.y = vn2 - cp2.velocityBias;
         float2 Ka = v2(vc.K[0] * a.x + vc.K[2] * a.y, vc.K[1] * a.x + vc.K[3] * a.y);
         b -= Ka;
-        for (;;) {
-            float2 xx = -v2(vc.NM[0] * b.x + vc.NM[2] * b.y, vc.NM[1] * b.x + vc.NM[3] * b.y);
-            if (xx.x >= 0.0f && xx.y >= 0.0f) {
-                apply_block(vA, wA, vB, wB, mA, iA, mB, iB, cp1, cp2, normal, xx - a);
-                cp1.normalImpulse = xx.x;
-                cp2.normalImpulse = xx.y;
-                break;
-            }
-            xx.x = -cp1.normalMass * b.x;
-            xx.y = 0.0f;
-            vn2 = vc.K[1] * xx.x + b.y;
-            if (xx.x >= 0.0f && vn2 >= 0.0f) {
-                apply_block(vA, wA, vB, wB, mA, iA, mB, iB, cp1, cp2, normal, xx - a);
-                cp1.normalImpulse = xx.x;
-                cp2.normalImpulse = xx.y;
-                break;
-            }
-            xx.x = 0.0f;
-            xx.y = -cp2.normalMass * b.y;
-            vn1 = vc.K[2] * xx.y + b.x;
-            if (xx.y >= 0.0f && vn1 >= 0.0f) {
-                apply_block(vA, wA, vB, wB, mA, iA, mB, iB, cp1, cp2, normal, xx - a);
-                cp1.normalImpulse = xx.x;
-                cp2.normalImpulse = xx.y;
-                break;
-            }
-            xx.x = 0.0f;
-            xx.y = 0.0f;
-            vn1 = b.x;
-            vn2 = b.y;
-            if (vn1 >= 0.0f && vn2 >= 0.0f) {
-                apply_block(vA, wA, vB, wB, mA, iA, mB, iB, cp1, cp2, normal, xx - a);
-                cp1.normalImpulse = xx.x;
-                cp2.normalImpulse = xx.y;
-                break;
-            }
-            break;
+        // The four cases of the 2x2 LCP (b2contactsolver.d:620-760) are evaluated side by side
+        // and the first one that holds is applied, exactly as the sequential case chain does;
+        // evaluating them all keeps the lanes of a level on one path.
+        float2 x1 = -v2(vc.NM[0] * b.x + vc.NM[2] * b.y, vc.NM[1] * b.x + vc.NM[3] * b.y);
+        bool c1 = x1.x >= 0.0f && x1.y >= 0.0f;
+        float x2 = -cp1.normalMass * b.x;
+        bool c2 = x2 >= 0.0f && vc.K[1] * x2 + b.y >= 0.0f;
+        float x3 = -cp2.normalMass * b.y;
+        bool c3 = x3 >= 0.0f && vc.K[2] * x3 + b.x >= 0.0f;
+        bool c4 = b.x >= 0.0f && b.y >= 0.0f;
+        float2 xx = c1 ? x1 : (c2 ? v2(x2, 0.0f) : (c3 ? v2(0.0f, x3) : v2(0.0f, 0.0f)));
+        if (c1 || c2 || c3 || c4) {
+            apply_block(vA, wA, vB, wB, mA, iA, mB, iB, cp1, cp2, normal, xx - a);
+            cp1.normalImpulse = xx.x;
+            cp2.normalImpulse = xx.y;
         }
     }
     sb.set_v(vc.bodyA, vA, wA);
     sb.set_v(vc.bodyB, vB, wB);
-    VC& out = x.vc[ci];
-    out.p[0].normalImpulse = vc.p[0].normalImpulse;
-    out.p[0].tangentImpulse = vc.p[0].tangentImpulse;
-    out.p[1].normalImpulse = vc.p[1].normalImpulse;
-    out.p[1].tangentImpulse = vc.p[1].tangentImpulse;
 }
 
-DG void store_impulses(const Ctx& x, int ci) {                         // :774-787
-    const VC& vc = x.vc[ci];
-    dbox_contact_state& c = x.ct[ci];
-#pragma unroll
-    for (int j = 0; j < 2; ++j) {
-        if (j >= vc.pointCount) break;
-        c.points[j].normal_impulse = vc.p[j].normalImpulse;
-        c.points[j].tangent_impulse = vc.p[j].tangentImpulse;
+DG void store_impulses(const Ctx& x, const VRow& r) {                 // :774-787
+    dbox_contact_state& c = x.ct[r.ids.w];
+    c.points[0].normal_impulse = r.imp.x;
+    c.points[0].tangent_impulse = r.imp.y;
+    if (r.ids.z > 1) {
+        c.points[1].normal_impulse = r.imp.z;
+        c.points[1].tangent_impulse = r.imp.w;
     }
+}
+
+// ------------------------------------------------------------ constraint rows
+DG VRow pack_v(const VC& vc, int item) {
+    VRow r;
+    r.r0 = make_float4(vc.p[0].rA.x, vc.p[0].rA.y, vc.p[0].rB.x, vc.p[0].rB.y);
+    r.r1 = make_float4(vc.p[1].rA.x, vc.p[1].rA.y, vc.p[1].rB.x, vc.p[1].rB.y);
+    r.imp = make_float4(vc.p[0].normalImpulse, vc.p[0].tangentImpulse, vc.p[1].normalImpulse, vc.p[1].tangentImpulse);
+    r.mass = make_float4(vc.p[0].normalMass, vc.p[0].tangentMass, vc.p[1].normalMass, vc.p[1].tangentMass);
+    r.nb = make_float4(vc.normal.x, vc.normal.y, vc.p[0].velocityBias, vc.p[1].velocityBias);
+    r.K = make_float4(vc.K[0], vc.K[1], vc.K[3], vc.friction);
+    r.NM = make_float4(vc.NM[0], vc.NM[1], vc.NM[3], vc.tangentSpeed);
+    r.inv = make_float4(vc.invMassA, vc.invIA, vc.invMassB, vc.invIB);
+    r.ids = make_int4(vc.bodyA, vc.bodyB, vc.pointCount, item);
+    return r;
+}
+DG VRow load_v(const VRow* p) {
+    VRow r;
+    r.r0 = p->r0; r.r1 = p->r1; r.imp = p->imp; r.mass = p->mass; r.nb = p->nb;
+    r.K = p->K; r.NM = p->NM; r.inv = p->inv; r.ids = p->ids;
+    return r;
+}
+DG VC unpack_v(const VRow& r) {
+    VC vc;
+    vc.p[0].rA = v2(r.r0.x, r.r0.y); vc.p[0].rB = v2(r.r0.z, r.r0.w);
+    vc.p[1].rA = v2(r.r1.x, r.r1.y); vc.p[1].rB = v2(r.r1.z, r.r1.w);
+    vc.p[0].normalImpulse = r.imp.x; vc.p[0].tangentImpulse = r.imp.y;
+    vc.p[1].normalImpulse = r.imp.z; vc.p[1].tangentImpulse = r.imp.w;
+    vc.p[0].normalMass = r.mass.x; vc.p[0].tangentMass = r.mass.y;
+    vc.p[1].normalMass = r.mass.z; vc.p[1].tangentMass = r.mass.w;
+    vc.normal = v2(r.nb.x, r.nb.y);
+    vc.p[0].velocityBias = r.nb.z; vc.p[1].velocityBias = r.nb.w;
+    vc.K[0] = r.K.x; vc.K[1] = r.K.y; vc.K[2] = r.K.y; vc.K[3] = r.K.z;
+    vc.friction = r.K.w;
+    vc.NM[0] = r.NM.x; vc.NM[1] = r.NM.y; vc.NM[2] = r.NM.y; vc.NM[3] = r.NM.z;
+    vc.tangentSpeed = r.NM.w;
+    vc.restitution = 0.0f;                       // only read while the row is built
+    vc.invMassA = r.inv.x; vc.invIA = r.inv.y; vc.invMassB = r.inv.z; vc.invIB = r.inv.w;
+    vc.bodyA = r.ids.x; vc.bodyB = r.ids.y; vc.pointCount = r.ids.z;
+    return vc;
+}
+DG PRow pack_p(const PC& pc, int island) {
+    PRow r;
+    r.lp = make_float4(pc.localPoints[0].x, pc.localPoints[0].y, pc.localPoints[1].x, pc.localPoints[1].y);
+    r.ln = make_float4(pc.localNormal.x, pc.localNormal.y, pc.localPoint.x, pc.localPoint.y);
+    r.lc = make_float4(pc.lcA.x, pc.lcA.y, pc.lcB.x, pc.lcB.y);
+    r.inv = make_float4(pc.invMassA, pc.invIA, pc.invMassB, pc.invIB);
+    r.rad = make_float4(pc.radiusA, pc.radiusB, 0.0f, 0.0f);
+    r.ids = make_int4(pc.bodyA, pc.bodyB, pc.type | (pc.pointCount << 4), island);
+    return r;
+}
+DG PRow load_p(const PRow* p) {
+    PRow r;
+    r.lp = p->lp; r.ln = p->ln; r.lc = p->lc; r.inv = p->inv; r.rad = p->rad; r.ids = p->ids;
+    return r;
+}
+DG PC unpack_p(const PRow& r) {
+    PC pc;
+    pc.localPoints[0] = v2(r.lp.x, r.lp.y); pc.localPoints[1] = v2(r.lp.z, r.lp.w);
+    pc.localNormal = v2(r.ln.x, r.ln.y); pc.localPoint = v2(r.ln.z, r.ln.w);
+    pc.lcA = v2(r.lc.x, r.lc.y); pc.lcB = v2(r.lc.z, r.lc.w);
+    pc.invMassA = r.inv.x; pc.invIA = r.inv.y; pc.invMassB = r.inv.z; pc.invIB = r.inv.w;
+    pc.radiusA = r.rad.x; pc.radiusB = r.rad.y;
+    pc.bodyA = r.ids.x; pc.bodyB = r.ids.y; pc.type = r.ids.z & 15; pc.pointCount = r.ids.z >> 4;
+    return pc;
 }
 
 // SolvePositionConstraints / SolveTOIPositionConstraints for one contact (:73-242);
 // returns the minimum separation seen over its points (0 if none below 0).
-DG float solve_position(const Ctx& x, int ci, SB sb, bool toi, int toiA, int toiB) {
-    const PC pc = x.pc[ci];
+DG float solve_position(const PC& pc, SB sb, bool toi, int toiA, int toiB) {
     float mA, iA, mB, iB;
     if (!toi) { mA = pc.invMassA; iA = pc.invIA; mB = pc.invMassB; iB = pc.invIB; }
     else {
@@ -781,19 +812,17 @@ DG float solve_position(const Ctx& x, int ci, SB sb, bool toi, int toiA, int toi
             normalize(normal);
             point = 0.5f * (pointA + pointB);
             separation = (dot(pointB - pointA, normal) - pc.radiusA) - pc.radiusB;
-        } else if (pc.type == kManifoldFaceA) {
-            normal = mul(xfA.q, pc.localNormal);
-            float2 planePoint = mul(xfA, pc.localPoint);
-            float2 clipPoint = mul(xfB, pc.localPoints[j]);
-            separation = (dot(clipPoint - planePoint, normal) - pc.radiusA) - pc.radiusB;
-            point = clipPoint;
         } else {
-            normal = mul(xfB.q, pc.localNormal);
-            float2 planePoint = mul(xfB, pc.localPoint);
-            float2 clipPoint = mul(xfA, pc.localPoints[j]);
+            // e_faceA and e_faceB share one path: the reference face's transform is picked
+            // first, and the normal is flipped for e_faceB
+            bool faceA = pc.type == kManifoldFaceA;
+            Xf xfN = faceA ? xfA : xfB, xfC = faceA ? xfB : xfA;
+            normal = mul(xfN.q, pc.localNormal);
+            float2 planePoint = mul(xfN, pc.localPoint);
+            float2 clipPoint = mul(xfC, pc.localPoints[j]);
             separation = (dot(clipPoint - planePoint, normal) - pc.radiusA) - pc.radiusB;
             point = clipPoint;
-            normal = -normal;
+            if (!faceA) normal = -normal;
         }
         float2 rA = point - cA;
         float2 rB = point - cB;
@@ -1125,13 +1154,107 @@ DG unsigned char body_flag_byte(const dbox_body_state& b) {
     return f;
 }
 
-constexpr int kSolveWarps = 4;          // worlds per block in k_solve
-constexpr int kSmemBodies = 320;        // worlds up to this many bodies keep solver state in shared memory
+// Level offsets of a schedule (lvl[0 .. last]) held in registers: lane k of q0 / q1 / q2
+// has lvl[32 * (blk + j) + k].  The level being solved and the levels read ahead of it
+// are at most one block apart, so each offset is one shuffle away, and the block after
+// next is loaded 32 levels before it is needed.
+struct LevelQ {
+    const int* lvl;
+    int last, blk, q0, q1, q2;
+    DG int ld(int i) const { return i <= last ? lvl[i] : 0; }
+    DG void init(const int* l, int last_) {
+        lvl = l; last = last_; blk = 0;
+        int lane = lane_id();
+        q0 = ld(lane); q1 = ld(32 + lane); q2 = ld(64 + lane);
+    }
+    DG void step_to(int L) {
+        while ((L >> 5) > blk) { ++blk; q0 = q1; q1 = q2; q2 = ld(32 * (blk + 2) + lane_id()); }
+    }
+    DG int get(int i) const {
+        int a = __shfl_sync(0xffffffffu, q0, i & 31), b = __shfl_sync(0xffffffffu, q1, i & 31);
+        return (i >> 5) == blk ? a : b;
+    }
+};
 
-__global__ void __launch_bounds__(kSolveWarps * 32, 4) k_solve(Ctx x) {
+template <class F>
+DG void run_levels(const int* lvl, int maxL, F&& f) {
+    LevelQ q;
+    q.init(lvl, maxL + 1);
+    const int lane = lane_id();
+    for (int L = 1; L <= maxL; ++L) {
+        q.step_to(L);
+        int s = q.get(L), e = q.get(L + 1);
+        for (int idx = s + lane; idx < e; idx += kWarp) f(idx);
+        tsync();
+    }
+}
+
+DG VRow load_row(const VRow* p) { return load_v(p); }
+DG PRow load_row(const PRow* p) { return load_p(p); }
+
+// 16-byte asynchronous global -> shared copies (L2 only), committed as one group per level
+DG void cp_async16(void* smem_dst, const void* gsrc) {
+    unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" :: "r"(d), "l"(gsrc) : "memory");
+}
+DG void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+DG void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+DG void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+template <class RowT>
+DG void stage_row(RowT* dst, const RowT* src) {
+    static_assert(sizeof(RowT) % 16 == 0, "rows are whole 16-byte chunks");
+    const float4* s = reinterpret_cast<const float4*>(src);
+    float4* d = reinterpret_cast<float4*>(dst);
+#pragma unroll
+    for (int k = 0; k < (int)(sizeof(RowT) / 16); ++k) cp_async16(d + k, s + k);
+}
+
+// One sweep over levels 1..maxL of a schedule whose rows are stored in schedule order:
+// f(row, idx) for every position of a level, levels in order, positions of a level spread
+// over the lanes.  Each lane's row of the next level is copied into shared memory (stage:
+// this warp's two slots of 32 rows) while the current level is solved, and the level
+// offsets are read one level ahead, so neither load sits on the dependent chain between
+// levels.  A row of a later level is never written by an earlier one; a lane's staged
+// row is only read by that lane.
+template <class RowT, class F>
+DG void sweep_levels(const int* lvl, int maxL, const RowT* rows, RowT* stage, F&& f) {
+    if (maxL < 1) return;
+    const int lane = lane_id();
+    LevelQ q;
+    q.init(lvl, maxL + 1);
+    int s = q.get(1), e = q.get(2);
+    int e2 = maxL >= 2 ? q.get(3) : e;                   // end of level 2 (it starts at e)
+    bool hc = s + lane < e;
+    int slot = 0;
+    if (hc) stage_row(stage + lane, rows + s + lane);
+    cp_async_commit();
+    for (int L = 1; L <= maxL; ++L) {
+        bool hn = L < maxL && e + lane < e2;
+        if (hn) stage_row(stage + (slot ^ 1) * kWarp + lane, rows + e + lane);
+        cp_async_commit();
+        q.step_to(L);
+        int e3 = L + 3 <= maxL + 1 ? q.get(L + 3) : e2;  // end of level L + 2
+        cp_async_wait_prev();
+        if (hc) {
+            f(stage[slot * kWarp + lane], s + lane);
+            for (int idx = s + lane + kWarp; idx < e; idx += kWarp) f(load_row(rows + idx), idx);
+        }
+        tsync();
+        slot ^= 1;
+        hc = hn;
+        s = e;
+        e = e2;
+        e2 = e3;
+    }
+    cp_async_wait_all();
+}
+
+
+__global__ void __launch_bounds__(kSolveWarps * 32, 3) k_solve(Ctx x) {
     extern __shared__ float smem_sb[];
-    int w = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
-    if (w >= x.W) return;
+    const int slot = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+    const int w = x.solve_world[slot];
+    if (w < 0) return;
     const WorldInfo& wi = x.wi[w];
     WorldDyn& wd = x.wd[w];
     int lane = lane_id();
@@ -1143,8 +1266,14 @@ __global__ void __launch_bounds__(kSolveWarps * 32, 4) k_solve(Ctx x) {
     const float h = x.dt;
     const bool warm = x.warm_starting != 0;
     const float dtRatio = wd.inv_dt0 * x.dt;                            // b2world.d:392
+    stamp(x, w, 0);
     SB sb;
-    sb.p = nb <= kSmemBodies ? smem_sb + (threadIdx.x >> 5) * (kSmemBodies * 6) : x.s_sbody + 6 * (size_t)b0;
+    const int soff = x.solve_smem[slot];
+    sb.p = soff >= 0 ? smem_sb + soff : x.s_sbody + 6 * (size_t)b0;
+    // this warp's row staging slots (two levels of 32 rows) at the front of the block's shared memory
+    float* stage_f = smem_sb + (threadIdx.x >> 5) * kStageFloats;
+    VRow* vstage = reinterpret_cast<VRow*>(stage_f);
+    PRow* pstage = reinterpret_cast<PRow*>(stage_f);
     unsigned char* bfl = x.s_bfl + b0;
     // compact per-body / per-contact data; island flags cleared (b2world.d:944-957)
     for (int i = lane; i < nb; i += kWarp) {
@@ -1187,6 +1316,7 @@ __global__ void __launch_bounds__(kSolveWarps * 32, 4) k_solve(Ctx x) {
         if (lane == 0) x.s_adj_start[bx + nb] = total;
     }
     tsync();
+    stamp(x, w, 1);
     int nIsl = 0, nbI = 0, ncI = 0, njI = 0, maxLv = 0, maxLp = 0;
     if (lane == 0) {
         int* cursor = x.s_cursor + b0;
@@ -1258,10 +1388,13 @@ __global__ void __launch_bounds__(kSolveWarps * 32, 4) k_solve(Ctx x) {
         x.s_isl_bstart[bx + nIsl] = nbI;
         x.s_isl_cstart[bx + nIsl] = ncI;
         x.s_isl_jstart[bx + nIsl] = njI;
+        stamp(x, w, 2);
         maxLv = build_schedule(x, wi, nIsl, false, x.s_sched_v, x.s_lvl_v);
         maxLp = build_schedule(x, wi, nIsl, true, x.s_sched_p, x.s_lvl_p);
         wd.islands = nIsl;
+        if (x.prof) { x.prof[16 * (size_t)w + 12] = maxLv; x.prof[16 * (size_t)w + 13] = n; x.prof[16 * (size_t)w + 14] = nb; }
     }
+    stamp(x, w, 3);
     nIsl = __shfl_sync(0xffffffffu, nIsl, 0);
     nbI = __shfl_sync(0xffffffffu, nbI, 0);
     ncI = __shfl_sync(0xffffffffu, ncI, 0);
@@ -1301,35 +1434,67 @@ __global__ void __launch_bounds__(kSolveWarps * 32, 4) k_solve(Ctx x) {
         }
     }
     tsync();
-    for (int t = lane; t < ncI; t += kWarp) {
-        int ci = x.s_isl_contact[c0 + t];
-        constraint_ctor(x, ci, b0, warm, dtRatio);
-        constraint_init_velocity(x, ci, sb);
+    // constraint rows in schedule order: b2ContactSolver ctor + InitializeVelocityConstraints
+    // (b2contactsolver.d:244-450); joint positions carry only the joint index
+    const int nItems = ncI + njI;
+    VRow* vrow = x.vr + kx;
+    PRow* prow = x.pr + kx;
+    for (int idx = lane; idx < nItems; idx += kWarp) {
+        int item = x.s_sched_v[kx + idx];
+        if (item >= 0) {
+            VC vc;
+            PC pc;
+            constraint_ctor(x, item, b0, warm, dtRatio, vc, pc);
+            constraint_init_velocity(vc, pc, sb);
+            vrow[idx] = pack_v(vc, item);
+            if (njI) x.s_vpos[item] = idx;
+        } else {
+            vrow[idx].ids = make_int4(0, 0, 0, item);
+        }
+        int pitem = x.s_sched_p[kx + idx];
+        int is = item_island(x, pitem, b0);
+        if (pitem >= 0) {
+            VC vc;
+            PC pc;
+            constraint_ctor(x, pitem, b0, warm, dtRatio, vc, pc);
+            prow[idx] = pack_p(pc, is);
+        } else {
+            prow[idx].ids = make_int4(0, 0, pitem, is);
+        }
     }
     tsync();
+    stamp(x, w, 4);
     // warm start contacts, then joints' InitVelocityConstraints (b2island.d:133-146)
-    for (int L = 1; L <= maxLp; ++L) {
-        int s = x.s_lvl_p[kx + L], e = x.s_lvl_p[kx + L + 1];
-        for (int idx = s + lane; idx < e; idx += kWarp) {
+    if (njI == 0) {
+        // without joints the position-order and velocity-order schedules coincide
+        if (warm)
+            sweep_levels(x.s_lvl_v + kx, maxLv, vrow, vstage, [&](const VRow& r, int) { warm_start(unpack_v(r), sb); });
+    } else {
+        run_levels(x.s_lvl_p + kx, maxLp, [&](int idx) {
             int item = x.s_sched_p[kx + idx];
-            if (item >= 0) { if (warm) warm_start(x, item, sb); }
+            if (item >= 0) { if (warm) warm_start(unpack_v(load_v(vrow + x.s_vpos[item])), sb); }
             else joint_init(x, -item - 1, b0, sb, warm, dtRatio);
-        }
-        tsync();
+        });
     }
+    stamp(x, w, 5);
     // velocity iterations (b2island.d:153-161)
     for (int it = 0; it < x.vel_iters; ++it) {
-        for (int L = 1; L <= maxLv; ++L) {
-            int s = x.s_lvl_v[kx + L], e = x.s_lvl_v[kx + L + 1];
-            for (int idx = s + lane; idx < e; idx += kWarp) {
-                int item = x.s_sched_v[kx + idx];
-                if (item >= 0) solve_velocity(x, item, sb);
-                else joint_solve_velocity(x, -item - 1, b0, sb);
+        sweep_levels(x.s_lvl_v + kx, maxLv, vrow, vstage, [&](const VRow& r, int idx) {
+            if (r.ids.w >= 0) {
+                VC vc = unpack_v(r);
+                solve_velocity(vc, sb);
+                vrow[idx].imp = make_float4(vc.p[0].normalImpulse, vc.p[0].tangentImpulse, vc.p[1].normalImpulse,
+                                            vc.p[1].tangentImpulse);
+            } else {
+                joint_solve_velocity(x, -r.ids.w - 1, b0, sb);
             }
-            tsync();
-        }
+        });
     }
-    for (int t = lane; t < ncI; t += kWarp) store_impulses(x, x.s_isl_contact[c0 + t]);
+    stamp(x, w, 6);
+    for (int idx = lane; idx < nItems; idx += kWarp) {
+        VRow r = load_v(vrow + idx);
+        if (r.ids.w >= 0) store_impulses(x, r);
+    }
     // integrate positions (b2island.d:168-200)
     for (int t = lane; t < nbI; t += kWarp) {
         int i = x.s_isl_body[b0 + t];
@@ -1354,6 +1519,7 @@ __global__ void __launch_bounds__(kSolveWarps * 32, 4) k_solve(Ctx x) {
     }
     for (int is = lane; is < nIsl; is += kWarp) x.s_isl_flags[b0 + is] = 0;
     tsync();
+    stamp(x, w, 7);
     // position iterations with per-island early exit (b2island.d:206-224)
     for (int it = 0; it < x.pos_iters; ++it) {
         for (int is = lane; is < nIsl; is += kWarp) {
@@ -1361,21 +1527,16 @@ __global__ void __launch_bounds__(kSolveWarps * 32, 4) k_solve(Ctx x) {
             x.s_isl_flags[b0 + is] &= ~4;
         }
         tsync();
-        for (int L = 1; L <= maxLp; ++L) {
-            int s = x.s_lvl_p[kx + L], e = x.s_lvl_p[kx + L + 1];
-            for (int idx = s + lane; idx < e; idx += kWarp) {
-                int item = x.s_sched_p[kx + idx];
-                int is = item_island(x, item, b0);
-                if (x.s_isl_flags[b0 + is] & 1) continue;
-                if (item >= 0) {
-                    float ms = solve_position(x, item, sb, false, -1, -1);
-                    atomicMin(&x.s_isl_minsep[b0 + is], fkey(ms));
-                } else if (!joint_solve_position(x, -item - 1, b0, sb)) {
-                    atomicOr(&x.s_isl_flags[b0 + is], 4);
-                }
+        sweep_levels(x.s_lvl_p + kx, maxLp, prow, pstage, [&](const PRow& r, int) {
+            int is = r.ids.w;
+            if (x.s_isl_flags[b0 + is] & 1) return;
+            if (r.ids.z >= 0) {
+                float ms = solve_position(unpack_p(r), sb, false, -1, -1);
+                atomicMin(&x.s_isl_minsep[b0 + is], fkey(ms));
+            } else if (!joint_solve_position(x, -r.ids.z - 1, b0, sb)) {
+                atomicOr(&x.s_isl_flags[b0 + is], 4);
             }
-            tsync();
-        }
+        });
         int psolved = 0;
         for (int is = lane; is < nIsl; is += kWarp)
             if (!(x.s_isl_flags[b0 + is] & 1))
@@ -1395,6 +1556,7 @@ __global__ void __launch_bounds__(kSolveWarps * 32, 4) k_solve(Ctx x) {
         tsync();
     }
     tsync();
+    stamp(x, w, 8);
     // copy back + SynchronizeTransform (b2island.d:227-235)
     for (int t = lane; t < nbI; t += kWarp) {
         int i = x.s_isl_body[b0 + t];
@@ -1442,6 +1604,7 @@ __global__ void __launch_bounds__(kSolveWarps * 32, 4) k_solve(Ctx x) {
         }
     }
     tsync();
+    stamp(x, w, 9);
     // SynchronizeFixtures for bodies that were in an island (b2world.d:1099-1116)
     for (int i = lane; i < nb; i += kWarp) {
         int b = b0 + i;
@@ -1450,8 +1613,10 @@ __global__ void __launch_bounds__(kSolveWarps * 32, 4) k_solve(Ctx x) {
         sync_fixtures(x, b);
     }
     tsync();
+    stamp(x, w, 10);
     hash_rebuild(x, w);
     find_new_contacts(x, w);
+    stamp(x, w, 11);
 }
 
 // ------------------------------------------------------------ TOI
@@ -1484,18 +1649,25 @@ DG void toi_update(const Ctx& x, dbox_contact_state& c) {
 
 // b2Island.SolveTOI (b2island.d:282-416) on the sub-island in s_isl_body (world-local)
 // and s_isl_contact; one lane.  sb holds the island bodies' state for the solve.
-DG void solve_toi_island(const Ctx& x, const WorldInfo& wi, SB sb, int nbI, int ncI, int toiA, int toiB,
+DG void solve_toi_island(const Ctx& x, int w, const WorldInfo& wi, SB sb, int nbI, int ncI, int toiA, int toiB,
                          float subDt) {
     const int b0 = wi.body_start, c0 = wi.contact_start;
+    VRow* tv = x.tvr + (size_t)kMaxTOIContacts * w;
+    PRow* tp = x.tpr + (size_t)kMaxTOIContacts * w;
     for (int i = 0; i < nbI; ++i) {
         int b = x.s_isl_body[b0 + i];
         sb_load(sb, b, x.bs[b0 + b]);
     }
-    for (int t = 0; t < ncI; ++t) constraint_ctor(x, x.s_isl_contact[c0 + t], b0, false, 1.0f);
+    for (int t = 0; t < ncI; ++t) {
+        VC vc;
+        PC pc;
+        constraint_ctor(x, x.s_isl_contact[c0 + t], b0, false, 1.0f, vc, pc);
+        tp[t] = pack_p(pc, 0);
+    }
     for (int it = 0; it < 20; ++it) {
         float minSep = 0.0f;
         for (int t = 0; t < ncI; ++t)
-            minSep = bmin(minSep, solve_position(x, x.s_isl_contact[c0 + t], sb, true, toiA, toiB));
+            minSep = bmin(minSep, solve_position(unpack_p(load_p(tp + t)), sb, true, toiA, toiB));
         if (minSep >= -1.5f * kLinearSlop) break;
     }
     dbox_body_state& A = x.bs[b0 + toiA];
@@ -1503,9 +1675,21 @@ DG void solve_toi_island(const Ctx& x, const WorldInfo& wi, SB sb, int nbI, int 
     float2 cA = sb.c(toiA), cB = sb.c(toiB);
     A.sweep[2] = cA.x; A.sweep[3] = cA.y; A.sweep[6] = sb.a(toiA);
     B.sweep[2] = cB.x; B.sweep[3] = cB.y; B.sweep[6] = sb.a(toiB);
-    for (int t = 0; t < ncI; ++t) constraint_init_velocity(x, x.s_isl_contact[c0 + t], sb);
+    for (int t = 0; t < ncI; ++t) {
+        int ci = x.s_isl_contact[c0 + t];
+        VC vc;
+        PC pc;
+        constraint_ctor(x, ci, b0, false, 1.0f, vc, pc);
+        constraint_init_velocity(vc, pc, sb);
+        tv[t] = pack_v(vc, ci);
+    }
     for (int it = 0; it < x.vel_iters; ++it)
-        for (int t = 0; t < ncI; ++t) solve_velocity(x, x.s_isl_contact[c0 + t], sb);
+        for (int t = 0; t < ncI; ++t) {
+            VC vc = unpack_v(load_v(tv + t));
+            solve_velocity(vc, sb);
+            tv[t].imp = make_float4(vc.p[0].normalImpulse, vc.p[0].tangentImpulse, vc.p[1].normalImpulse,
+                                    vc.p[1].tangentImpulse);
+        }
     float h = subDt;
     for (int i = 0; i < nbI; ++i) {
         int b = x.s_isl_body[b0 + i];
@@ -1720,7 +1904,7 @@ __global__ void k_toi(Ctx x) {
                 }
                 if (lane == 0) {
                     float subDt = (1.0f - minAlpha) * x.dt;
-                    solve_toi_island(x, wi, sb, nbI, ncI, mcb.x, mcb.y, subDt);
+                    solve_toi_island(x, w, wi, sb, nbI, ncI, mcb.x, mcb.y, subDt);
                     for (int i = 0; i < nbI; ++i) {
                         int body = x.s_isl_body[b0 + i];
                         dbox_body_state& Bd = x.bs[b0 + body];
@@ -1770,6 +1954,7 @@ __global__ void k_toi(Ctx x) {
 extern "C" int dbox_launch_step_ev(const dg::Ctx* x, cudaStream_t stream, int* launches, cudaEvent_t* ev) {
     const int threads = 128;                       // four worlds per block, one warp each
     int team_blocks = (x->W * dg::kWarp + threads - 1) / threads;
+    if (x->solve_blocks < 1) return (int)cudaErrorInvalidValue;
     int flat_blocks = (x->total_contacts + 255) / 256;
     if (flat_blocks < 1) flat_blocks = 1;
     if (flat_blocks > 152 * 16) flat_blocks = 152 * 16;
@@ -1778,13 +1963,15 @@ extern "C" int dbox_launch_step_ev(const dg::Ctx* x, cudaStream_t stream, int* l
     dg::k_collide<<<flat_blocks, 256, 0, stream>>>(*x);
     dg::k_collide_finish<<<team_blocks, threads, 0, stream>>>(*x);
     if (ev) cudaEventRecordWithFlags(ev[1], stream, cudaEventRecordExternal);
-    dg::k_solve<<<team_blocks, threads, dg::kSolveWarps * dg::kSmemBodies * 6 * sizeof(float), stream>>>(*x);
+    dg::k_solve<<<x->solve_blocks, dg::kSolveWarps * dg::kWarp, x->solve_smem_floats * sizeof(float), stream>>>(*x);
     if (ev) cudaEventRecordWithFlags(ev[2], stream, cudaEventRecordExternal);
     dg::k_toi<<<team_blocks, threads, 0, stream>>>(*x);
     if (ev) cudaEventRecordWithFlags(ev[3], stream, cudaEventRecordExternal);
     if (launches) *launches = 5;
     return (int)cudaGetLastError();
 }
+
+extern "C" const void* dbox_solve_kernel() { return reinterpret_cast<const void*>(&dg::k_solve); }
 
 extern "C" int dbox_launch_step(const dg::Ctx* x, cudaStream_t stream, int* launches) {
     return dbox_launch_step_ev(x, stream, launches, nullptr);

@@ -102,8 +102,34 @@ struct __align__(16) PC {
     int pointCount;
 };
 
+// Stored forms of the two constraints, read with 16-byte vector loads.  The solver
+// works on VC / PC in registers; these rows hold the same values (the normal mass
+// matrices are symmetric, K.ex.y == K.ey.x, so three entries each are kept).
+struct __align__(16) VRow {
+    float4 r0;          // rA.x rA.y rB.x rB.y of point 0
+    float4 r1;          // the same for point 1
+    float4 imp;         // normalImpulse0 tangentImpulse0 normalImpulse1 tangentImpulse1
+    float4 mass;        // normalMass0 tangentMass0 normalMass1 tangentMass1
+    float4 nb;          // normal.x normal.y velocityBias0 velocityBias1
+    float4 K;           // K.ex.x K.ex.y K.ey.y friction
+    float4 NM;          // normalMass.ex.x .ex.y .ey.y tangentSpeed
+    float4 inv;         // invMassA invIA invMassB invIB
+    int4 ids;           // bodyA bodyB pointCount item (contact slot, or -1 - joint)
+};
+struct __align__(16) PRow {
+    float4 lp;          // localPoints[0] localPoints[1]
+    float4 ln;          // localNormal localPoint
+    float4 lc;          // localCenterA localCenterB
+    float4 inv;         // invMassA invIA invMassB invIB
+    float4 rad;         // radiusA radiusB (z, w unused)
+    int4 ids;           // bodyA bodyB meta island; meta = type | pointCount << 4, or -1 - joint
+};
+
 // TOI sweep snapshot of one contact's two bodies (taken in list order).
 struct SweepSnap { Sweep a, b; float alpha0; int pad; };
+
+constexpr int kSolveWarps = 4;          // warp slots (worlds) per block of the solve kernel
+constexpr int kStageFloats = 2 * 32 * 36; // per warp: two levels of 32 staged 144-byte rows
 
 struct Ctx {
     int W;
@@ -154,8 +180,15 @@ struct Ctx {
     int* s_tmp;                    // kx-indexed sequence-order items while sorting by level
     int* s_isl_joint;              // joint-indexed
     int* s_accept;                 // pair-indexed
-    VC* vc;                        // contact-slot-indexed
-    PC* pc;                        // contact-slot-indexed
+    VRow* vr;                      // kx-indexed: velocity rows in velocity-schedule order
+    PRow* pr;                      // kx-indexed: position rows in position-schedule order
+    VRow* tvr;                     // 32 per world: rows of the current TOI island
+    PRow* tpr;                     // 32 per world
+    int* s_vpos;                   // contact-slot-indexed: velocity-schedule position (worlds with joints)
+    const int* solve_world;        // per warp slot of the solve kernel: world index or -1
+    const int* solve_smem;         // per warp slot: float offset of its body rows in shared memory, or -1
+    int solve_blocks;              // blocks of the solve kernel (four warp slots each)
+    int solve_smem_floats;         // dynamic shared memory of one solve block, in floats
     SweepSnap* snap;               // contact-slot-indexed
     int2* s_cbody;                 // contact-slot-indexed: world-local bodies of the contact
     unsigned char* s_cq;           // contact-slot-indexed: bit0 island-graph edge, bit1 sensor
@@ -169,6 +202,7 @@ struct Ctx {
     int warm_starting, continuous, sub_stepping, allow_sleep;
     int record_events;
     int* g_status;                 // bit (-code) set for every DBOX_ERR_* raised by any world
+    unsigned long long* prof;      // optional: 16 clock64 phase stamps per world (NULL = off)
 };
 
 // ------------------------------------------------------------ body state helpers (dbox_body_state fields)

@@ -270,6 +270,12 @@ int32_t dbox_world_apply_forces(dbox_world* w, const float* force_torque);
 /* b2Body.GetPosition + b2Body.GetAngle (b2body.d:283-296) for every body: (x, y, angle) per body. */
 int32_t dbox_world_get_transforms(dbox_world* w, float* xya);
 
+/* Per-world device clock stamps at the phase boundaries of the solve kernel (diagnostics):
+ * enable before stepping; out receives 16 uint64 per world (stamps 0..11, then the number of
+ * velocity levels, contacts and bodies of the world in slots 12..14). */
+int32_t dbox_world_set_phase_profile(dbox_world* w, int32_t enable);
+int32_t dbox_world_get_phase_profile(dbox_world* w, unsigned long long* out);
+
 /* Wait for all queued device work of the handle. */
 int32_t dbox_world_sync(dbox_world* w);
 
