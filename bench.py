@@ -10,7 +10,8 @@ W untimed warm-up steps, so the timed window is steps W+1 .. W+K of the simulati
 
 value  = dynamic body-steps / device time of K steps replayed from one CUDA graph
          (world state resident in HBM; CUDA events on the library's stream).
-e2e    = the same K steps through the C ABI from host buffers: each step uploads a
+e2e    = the same K steps (on a twin handle built from the same scenes and warmed up
+         the same way) through the C ABI from host buffers: each step uploads a
          (fx, fy, torque) array for every body from pinned host memory
          (dbox_world_apply_forces; zero forces, so the trajectory is unchanged),
          steps, and reads every body's (x, y, angle) back into pinned memory
@@ -181,7 +182,8 @@ def cpu_leg(args, seconds):
 
 # ------------------------------------------------------------------ GPU leg
 def algorithmic_solve_bytes(c):
-    """Bytes the k_solve kernel must move by the reference struct sizes:
+    """Bytes the solve part of the fused solve + SolveTOI kernel must move, by the reference
+    struct sizes (the SolveTOI part is not counted, so the figure is a lower bound):
     96 per island body (integrate + copy back), per island contact 244 (b2ContactVelocity/
     PositionConstraint build) + 156 (velocity init) + 16 (store impulses), 220 per contact
     velocity solve (vc 156 + two 24-byte body states read and written, 16 of impulses) and
@@ -198,8 +200,13 @@ def gpu_leg(args, rank, world_size):
     nbody_dyn = dynamic_bodies(worlds)
     nbody = sum(len(s["bodies"]) for s in worlds)
     w = dbox_gb300.World(worlds)
+    # twin handle for the end-to-end leg: the same scenes and warm-up, so it replays exactly
+    # the steps the device-timed leg measures
+    we = dbox_gb300.World(worlds)
     w.step(DT, VI, PI, steps=args.warmup, graph=True)
+    we.step(DT, VI, PI, steps=args.warmup, graph=True)
     w.sync()
+    we.sync()
     peaks = {}
     pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(pk):
@@ -224,12 +231,12 @@ def gpu_leg(args, rank, world_size):
     xya = torch.zeros((nbody, 3), dtype=torch.float32).pin_memory().numpy()
     if world_size > 1:
         torch.distributed.barrier()
-    w.sync()
+    we.sync()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        w.apply_forces(forces)
-        w.step(DT, VI, PI)
-        w.get_transforms(xya)
+        we.apply_forces(forces)
+        we.step(DT, VI, PI)
+        we.get_transforms(xya)
     e2e_s = time.perf_counter() - t0
     te = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
     if world_size > 1:
@@ -237,7 +244,7 @@ def gpu_leg(args, rank, world_size):
     e2e = nbody_dyn * args.steps * world_size / float(te.item())
     assert np.isfinite(xya).all()
     solve_bytes = algorithmic_solve_bytes(cdiff) / args.steps
-    solve_ms = phase_ms[1] / args.steps
+    solve_ms = phase_ms[1] / args.steps          # the fused solve + SolveTOI kernel
     achieved = solve_bytes / (solve_ms / 1e3) / 1e9
     hbm = peaks.get("hbm_gbs")
     out = {
@@ -252,10 +259,9 @@ def gpu_leg(args, rank, world_size):
         "e2e": {"value": e2e, "unit": "body-steps/s", "h2d_bytes_per_step": int(forces.nbytes),
                 "d2h_bytes_per_step": int(xya.nbytes)},
         "gpu_launches": launches,
-        "phases_ms_per_step": {"collide": phase_ms[0] / args.steps, "solve": solve_ms,
-                               "solve_toi": phase_ms[2] / args.steps},
+        "phases_ms_per_step": {"collide": phase_ms[0] / args.steps, "solve_and_toi": solve_ms},
         "work_per_step": {k: v / args.steps for k, v in cdiff.items()},
-        "roofline": {"bound": "hbm", "kernel": "k_solve", "achieved": achieved,
+        "roofline": {"bound": "hbm", "kernel": "k_solve_toi", "achieved": achieved,
                      "peak": hbm, "unit": "GB/s", "frac": (achieved / hbm) if hbm else None,
                      "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if hbm else "fallback 6800",
                      "algorithmic_bytes_per_launch": solve_bytes, "traffic": None},

@@ -174,8 +174,8 @@ class World:
         _check(lib().dbox_world_set_phase_profile(self.h, 1 if on else 0), "set_phase_profile")
 
     def phase_profile(self):
-        """(n_worlds, 16) uint64: clock64 stamps of the solve phases, then levels, contacts, bodies."""
-        out = np.zeros((self.n_worlds, 16), np.uint64)
+        """(n_worlds, 32) uint64 per-world clock figures of the last step (layout in dbox_gpu.h)."""
+        out = np.zeros((self.n_worlds, 32), np.uint64)
         _check(lib().dbox_world_get_phase_profile(self.h, abi.ptr(out)), "get_phase_profile")
         return out
 

@@ -96,7 +96,7 @@ struct dbox_world {
     DBuf<unsigned long long> d_hash;
     DBuf<int2> d_pairs;
     DBuf<int> s_woken, s_adj_start, s_cursor, s_stack, s_isl_body, s_body_island, s_last, s_isl_bstart,
-        s_isl_cstart, s_isl_jstart, s_isl_flags, s_pcount, s_moved, s_cstate, s_adj_items, s_isl_contact, s_level,
+        s_isl_cstart, s_isl_jstart, s_isl_flags, s_pcount, s_moved, s_cstate, s_isl_contact, s_level, s_lcur, s_tcand,
         s_sched_v, s_lvl_v, s_sched_p, s_lvl_p, s_tmp, s_isl_joint, s_accept, g_status;
     DBuf<unsigned> s_isl_minsep, s_isl_sleep;
     DBuf<dg::VRow> d_vr, d_tvr;
@@ -105,7 +105,7 @@ struct dbox_world {
     int solve_blocks = 0, solve_smem_floats = 0;
     DBuf<dg::SweepSnap> d_snap;
     DBuf<float> d_io;           // staging for bulk force upload / transform readback (3 floats per body)
-    DBuf<int2> s_cbody;
+    DBuf<int2> s_cbody, s_adj_items, s_isl_pair;
     DBuf<unsigned char> s_cq, s_cvis, s_bfl;
     DBuf<float> s_sbody;
     DBuf<unsigned long long> d_prof;
@@ -139,14 +139,14 @@ void free_device(dbox_world* w) {
     w->d_ct.free(); w->d_cworld.free(); w->d_hash.free(); w->d_pairs.free();
     DBuf<int>* ints[] = {&w->s_woken, &w->s_adj_start, &w->s_cursor, &w->s_stack, &w->s_isl_body, &w->s_body_island,
                          &w->s_last, &w->s_isl_bstart, &w->s_isl_cstart, &w->s_isl_jstart, &w->s_isl_flags,
-                         &w->s_pcount, &w->s_moved, &w->s_cstate, &w->s_adj_items, &w->s_isl_contact, &w->s_level,
+                         &w->s_pcount, &w->s_moved, &w->s_cstate, &w->s_isl_contact, &w->s_level, &w->s_lcur, &w->s_tcand,
                          &w->s_sched_v, &w->s_lvl_v, &w->s_sched_p, &w->s_lvl_p, &w->s_tmp, &w->s_isl_joint,
                          &w->s_accept, &w->g_status};
     for (auto* b : ints) b->free();
     w->s_isl_minsep.free(); w->s_isl_sleep.free();
     w->d_vr.free(); w->d_tvr.free(); w->d_pr.free(); w->d_tpr.free(); w->d_snap.free(); w->d_io.free();
     w->s_vpos.free(); w->d_solve_world.free(); w->d_solve_smem.free();
-    w->s_cbody.free(); w->s_cq.free(); w->s_cvis.free(); w->s_bfl.free(); w->s_sbody.free(); w->d_prof.free();
+    w->s_cbody.free(); w->s_adj_items.free(); w->s_isl_pair.free(); w->s_cq.free(); w->s_cvis.free(); w->s_bfl.free(); w->s_sbody.free(); w->d_prof.free();
     if (w->graph) { cudaGraphExecDestroy(w->graph); w->graph = nullptr; }
     if (w->tgraph) { cudaGraphExecDestroy(w->tgraph); w->tgraph = nullptr; }
 }
@@ -173,26 +173,31 @@ int pack_solve_slots(dbox_world* w) {
     std::stable_sort(order.begin(), order.end(),
                      [&](int a, int b) { return w->wi[a].body_count > w->wi[b].body_count; });
     std::vector<int> used, count, slot_world, slot_off;
-    size_t first_open = 0;
+    std::vector<int> open;                  // blocks with a free slot, in creation order
     for (int wid : order) {
         int nbw = w->wi[wid].body_count;
         bool in_smem = nbw <= budget;
         int need = in_smem ? nbw : 0;
         int chosen = -1;
-        for (size_t b = first_open, tries = 0; b < used.size() && tries < 64; ++b, ++tries)
-            if (count[b] < dg::kSolveWarps && used[b] + need <= budget) { chosen = (int)b; break; }
+        size_t keep = 0;
+        for (size_t t = 0; t < open.size(); ++t) {
+            int b = open[t];
+            if (chosen < 0 && used[b] + need <= budget) chosen = b;
+            if (count[b] + (b == chosen) < dg::kSolveWarps) open[keep++] = b;   // still has a free slot
+        }
+        open.resize(keep);
         if (chosen < 0) {
             chosen = (int)used.size();
             used.push_back(0);
             count.push_back(0);
             slot_world.resize(used.size() * dg::kSolveWarps, -1);
             slot_off.resize(used.size() * dg::kSolveWarps, -1);
+            if (dg::kSolveWarps > 1) open.push_back(chosen);
         }
         int slot = chosen * dg::kSolveWarps + count[chosen]++;
         slot_world[slot] = wid;
         slot_off[slot] = in_smem ? stage_floats + 6 * used[chosen] : -1;
         used[chosen] += need;
-        while (first_open < used.size() && count[first_open] == dg::kSolveWarps) ++first_open;
     }
     if (used.empty()) {                     // no worlds: one idle block
         used.push_back(0);
@@ -359,6 +364,9 @@ int upload(dbox_world* w) {
     ok &= w->s_moved.alloc(nf) == 0;
     ok &= w->s_cstate.alloc(nc) == 0;
     ok &= w->s_adj_items.alloc(2 * (size_t)nc) == 0;
+    ok &= w->s_isl_pair.alloc(nc) == 0;
+    ok &= w->s_lcur.alloc(nkx) == 0;
+    ok &= w->s_tcand.alloc(nc) == 0;
     ok &= w->s_isl_contact.alloc(nc) == 0;
     ok &= w->s_level.alloc(nkx) == 0;
     ok &= w->s_sched_v.alloc(nkx) == 0;
@@ -381,7 +389,7 @@ int upload(dbox_world* w) {
     ok &= w->s_cvis.alloc(nc) == 0;
     ok &= w->s_bfl.alloc(nb) == 0;
     ok &= w->s_sbody.alloc(6 * (size_t)nb) == 0;
-    ok &= w->d_prof.alloc(16 * (size_t)W) == 0;
+    ok &= w->d_prof.alloc((size_t)dg::kProfSlots * W) == 0;
     if (!ok) { free_device(w); return fail(DBOX_ERR_CUDA, "device allocation failed (%d bodies, %d contact slots)", nb, nc); }
     if (pack_solve_slots(w) != DBOX_OK) { free_device(w); return DBOX_ERR_CUDA; }
     CU(cudaMemcpy(w->d_wi.p, w->wi.data(), sizeof(dg::WorldInfo) * W, cudaMemcpyHostToDevice));
@@ -458,6 +466,9 @@ dg::Ctx make_ctx(dbox_world* w, float dt, int vi, int pi) {
     x.s_moved = w->s_moved.p;
     x.s_cstate = w->s_cstate.p;
     x.s_adj_items = w->s_adj_items.p;
+    x.s_isl_pair = w->s_isl_pair.p;
+    x.s_lcur = w->s_lcur.p;
+    x.s_tcand = w->s_tcand.p;
     x.s_isl_contact = w->s_isl_contact.p;
     x.s_level = w->s_level.p;
     x.s_sched_v = w->s_sched_v.p;
@@ -1024,7 +1035,7 @@ int32_t dbox_world_get_phase_profile(dbox_world* w, unsigned long long* out) {
     if (!w || !out) return DBOX_ERR_INVALID;
     if (!w->on_device || !w->d_prof.p) return DBOX_ERR_INVALID;
     CU(cudaStreamSynchronize(w->stream));
-    CU(cudaMemcpy(out, w->d_prof.p, sizeof(unsigned long long) * 16 * w->worlds.size(), cudaMemcpyDeviceToHost));
+    CU(cudaMemcpy(out, w->d_prof.p, sizeof(unsigned long long) * dg::kProfSlots * w->worlds.size(), cudaMemcpyDeviceToHost));
     return DBOX_OK;
 }
 

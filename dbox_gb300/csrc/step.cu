@@ -32,7 +32,7 @@ constexpr unsigned long long kHashEmpty = 0xffffffffffffffffull;
 DG int lane_id() { return threadIdx.x & 31; }
 // phase stamp for the optional per-world profile (slot 0..15), lane 0 only
 DG void stamp(const Ctx& x, int w, int slot) {
-    if (x.prof && (threadIdx.x & 31) == 0) x.prof[16 * (size_t)w + slot] = clock64();
+    if (x.prof && (threadIdx.x & 31) == 0) x.prof[kProfSlots * (size_t)w + slot] = clock64();
 }
 DG void tsync() { __syncwarp(); }
 
@@ -1049,47 +1049,78 @@ DG void item_bodies(const Ctx& x, int item, int b0, int& A, int& B) {
     else { const DJoint& j = x.jt[-item - 1]; A = j.body_a - b0; B = j.body_b - b0; }
 }
 
-// Build one level schedule for world w.  `contacts_first` gives the warm-start /
-// position order of b2Island.Solve (contacts then joints, b2island.d:136-146 and
-// 206-224); otherwise the velocity-iteration order (joints then contacts,
-// b2island.d:153-161).  Level L items end up in sched[kx + lvl[kx+L] .. kx + lvl[kx+L+1]).
-// Run by one lane.  Returns the number of levels.
-DG int build_schedule(const Ctx& x, const WorldInfo& wi, int nIsl, bool contacts_first, int* sched, int* lvl) {
-    const int b0 = wi.body_start, kx = wi.kx_start;
-    const unsigned char* bfl = x.s_bfl + b0;
-    int* last = x.s_last + b0;
-    for (int i = 0; i < wi.body_count; ++i) last[i] = 0;
+// Build one level schedule for world w (all lanes).  `contacts_first` gives the warm-start /
+// position order of b2Island.Solve (contacts then joints, b2island.d:136-146 and 206-224);
+// otherwise the velocity-iteration order (joints then contacts, b2island.d:153-161).
+// Lane 0 walks the island sequence once and gives each constraint the level 1 + the last
+// level of its dynamic bodies; the warp then buckets the constraints by level.  Level L
+// items end up in sched[kx + lvl[kx+L] .. kx + lvl[kx+L+1]) (in any order inside a level:
+// they share no dynamic body).  Returns the number of levels.
+DG int build_schedule(const Ctx& x, const WorldInfo& wi, int nIsl, bool contacts_first, const unsigned char* vbf,
+                      int* last, int* sched, int* lvl) {
+    const int b0 = wi.body_start, kx = wi.kx_start, c0 = wi.contact_start;
+    const int lane = lane_id();
+    for (int i = lane; i < wi.body_count; i += kWarp) last[i] = 0;
+    tsync();
     int maxL = 0, n = 0;
-    for (int is = 0; is < nIsl; ++is) {
-        int cs = x.s_isl_cstart[wi.bx_start + is], ce = x.s_isl_cstart[wi.bx_start + is + 1];
-        int js = x.s_isl_jstart[wi.bx_start + is], je = x.s_isl_jstart[wi.bx_start + is + 1];
-        for (int pass = 0; pass < 2; ++pass) {
-            bool doContacts = (pass == 0) == contacts_first;
-            int s = doContacts ? cs : js, e = doContacts ? ce : je;
-            for (int t = s; t < e; ++t) {
-                int item = doContacts ? x.s_isl_contact[wi.contact_start + t] : -(x.s_isl_joint[wi.joint_start + t] + 1);
-                int A, B;
-                item_bodies(x, item, b0, A, B);
-                bool dA = (bfl[A] & kBfDynamic) != 0, dB = (bfl[B] & kBfDynamic) != 0;
-                int la = dA ? last[A] : 0, lb = dB ? last[B] : 0;
-                int l = (la > lb ? la : lb) + 1;
-                if (dA) last[A] = l;
-                if (dB) last[B] = l;
-                if (l > maxL) maxL = l;
-                x.s_level[kx + n] = l;
-                x.s_tmp[kx + n] = item;
-                ++n;
+    if (lane == 0) {
+        for (int is = 0; is < nIsl; ++is) {
+            int cs = x.s_isl_cstart[wi.bx_start + is], ce = x.s_isl_cstart[wi.bx_start + is + 1];
+            int js = x.s_isl_jstart[wi.bx_start + is], je = x.s_isl_jstart[wi.bx_start + is + 1];
+            for (int pass = 0; pass < 2; ++pass) {
+                bool doContacts = (pass == 0) == contacts_first;
+                int s = doContacts ? cs : js, e = doContacts ? ce : je;
+                for (int t = s; t < e; ++t) {
+                    int item, A, B;
+                    if (doContacts) {
+                        item = x.s_isl_contact[c0 + t];
+                        int2 pr = x.s_isl_pair[c0 + t];
+                        A = pr.x;
+                        B = pr.y;
+                    } else {
+                        item = -(x.s_isl_joint[wi.joint_start + t] + 1);
+                        item_bodies(x, item, b0, A, B);
+                    }
+                    bool dA = (vbf[A] & kBfDynamic) != 0, dB = (vbf[B] & kBfDynamic) != 0;
+                    int la = dA ? last[A] : 0, lb = dB ? last[B] : 0;
+                    int l = (la > lb ? la : lb) + 1;
+                    if (dA) last[A] = l;
+                    if (dB) last[B] = l;
+                    if (l > maxL) maxL = l;
+                    x.s_level[kx + n] = l;
+                    x.s_tmp[kx + n] = item;
+                    ++n;
+                }
             }
         }
     }
-    for (int l = 0; l <= maxL + 1; ++l) lvl[kx + l] = 0;
-    for (int i = 0; i < n; ++i) lvl[kx + x.s_level[kx + i]]++;
-    for (int l = 1; l <= maxL; ++l) lvl[kx + l] += lvl[kx + l - 1];
-    for (int i = n - 1; i >= 0; --i) {
-        int l = x.s_level[kx + i];
-        sched[kx + (--lvl[kx + l])] = x.s_tmp[kx + i];
+    maxL = __shfl_sync(0xffffffffu, maxL, 0);
+    n = __shfl_sync(0xffffffffu, n, 0);
+    for (int l = lane; l <= maxL + 1; l += kWarp) lvl[kx + l] = 0;
+    tsync();
+    for (int i = lane; i < n; i += kWarp) atomicAdd(&lvl[kx + x.s_level[kx + i]], 1);
+    tsync();
+    int total = 0;
+    for (int base = 0; base <= maxL + 1; base += kWarp) {
+        int l = base + lane;
+        int v = l <= maxL + 1 ? lvl[kx + l] : 0;
+        int incl = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            int t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        if (l <= maxL + 1) {
+            lvl[kx + l] = total + incl - v;
+            x.s_lcur[kx + l] = total + incl - v;
+        }
+        total += __shfl_sync(0xffffffffu, incl, 31);
     }
-    lvl[kx + maxL + 1] = n;
+    tsync();
+    for (int i = lane; i < n; i += kWarp) {
+        int pos = atomicAdd(&x.s_lcur[kx + x.s_level[kx + i]], 1);
+        sched[kx + pos] = x.s_tmp[kx + i];
+    }
+    tsync();
     return maxL;
 }
 
@@ -1250,11 +1281,10 @@ DG void sweep_levels(const int* lvl, int maxL, const RowT* rows, RowT* stage, F&
 }
 
 
-__global__ void __launch_bounds__(kSolveWarps * 32, 3) k_solve(Ctx x) {
-    extern __shared__ float smem_sb[];
-    const int slot = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
-    const int w = x.solve_world[slot];
-    if (w < 0) return;
+// b2World.Solve (b2world.d:930-1124) for world w: islands, contact solver, sleep,
+// SynchronizeFixtures, FindNewContacts.  sbp: the world's solver body rows; stage_f: this
+// warp's staging area in shared memory.
+DG void solve_world(const Ctx& x, int w, float* sbp, float* stage_f) {
     const WorldInfo& wi = x.wi[w];
     WorldDyn& wd = x.wd[w];
     int lane = lane_id();
@@ -1268,10 +1298,7 @@ __global__ void __launch_bounds__(kSolveWarps * 32, 3) k_solve(Ctx x) {
     const float dtRatio = wd.inv_dt0 * x.dt;                            // b2world.d:392
     stamp(x, w, 0);
     SB sb;
-    const int soff = x.solve_smem[slot];
-    sb.p = soff >= 0 ? smem_sb + soff : x.s_sbody + 6 * (size_t)b0;
-    // this warp's row staging slots (two levels of 32 rows) at the front of the block's shared memory
-    float* stage_f = smem_sb + (threadIdx.x >> 5) * kStageFloats;
+    sb.p = sbp;
     VRow* vstage = reinterpret_cast<VRow*>(stage_f);
     PRow* pstage = reinterpret_cast<PRow*>(stage_f);
     unsigned char* bfl = x.s_bfl + b0;
@@ -1284,19 +1311,32 @@ __global__ void __launch_bounds__(kSolveWarps * 32, 3) k_solve(Ctx x) {
         x.s_body_island[b0 + i] = -1;
         sb_load(sb, i, B);
     }
+    // scratch of the island search: this warp's staging area when the world fits, else
+    // global rows: edge counts / adjacency starts, the DFS stack (later the per-body last
+    // level of the schedule), body flag bytes and contact visit marks
+    const int nbA = (nb + 4) & ~3;
+    const bool gsm = 4 * (nb + 1) + 4 * nb + nbA + ((n + 3) & ~3) <= (int)(kStageFloats * sizeof(float));
+    int* adj = gsm ? reinterpret_cast<int*>(stage_f) : x.s_adj_start + bx;
+    int* stack = gsm ? adj + nb + 1 : x.s_stack + b0;
+    unsigned char* vbf = gsm ? reinterpret_cast<unsigned char*>(stack + nb) : bfl;
+    unsigned char* cvis = gsm ? vbf + nbA : x.s_cvis + c0;
+    for (int i = lane; i < nb; i += kWarp) {
+        adj[i] = 0;
+        if (gsm) vbf[i] = bfl[i];
+    }
     for (int k = lane; k < n; k += kWarp) {
         x.ct[c0 + k].flags &= ~(uint32_t)kContactIsland;
         contact_compact(x, c0 + k, b0);
-        x.s_cvis[c0 + k] = 0;
+        cvis[k] = 0;
     }
     for (int j = lane; j < nj; j += kWarp) x.jt[j0 + j].island_flag = 0;
     tsync();
-    // contact edges of the island graph per body, newest first
+    // contact edges of the island graph per body (b2world.d:1026-1062 walks them newest first)
     for (int k = lane; k < n; k += kWarp) {
         if (x.s_cq[c0 + k] & 1) {
             int2 cb = x.s_cbody[c0 + k];
-            atomicAdd(&x.s_cursor[b0 + cb.x], 1);
-            atomicAdd(&x.s_cursor[b0 + cb.y], 1);
+            atomicAdd(&adj[cb.x], 1);
+            atomicAdd(&adj[cb.y], 1);
         }
     }
     tsync();
@@ -1304,41 +1344,56 @@ __global__ void __launch_bounds__(kSolveWarps * 32, 3) k_solve(Ctx x) {
         int total = 0;
         for (int base = 0; base < nb; base += kWarp) {
             int i = base + lane;
-            int v = i < nb ? x.s_cursor[b0 + i] : 0;
+            int v = i < nb ? adj[i] : 0;
             int incl = v;
             for (int o = 1; o < 32; o <<= 1) {
                 int t = __shfl_up_sync(0xffffffffu, incl, o);
                 if (lane >= o) incl += t;
             }
-            if (i < nb) { x.s_adj_start[bx + i] = total + incl - v; x.s_cursor[b0 + i] = total + incl - v; }
+            if (i < nb) { adj[i] = total + incl - v; stack[i] = total + incl - v; }
             total += __shfl_sync(0xffffffffu, incl, 31);
         }
-        if (lane == 0) x.s_adj_start[bx + nb] = total;
+        if (lane == 0) adj[nb] = total;
     }
     tsync();
+    // adjacency lists, newest contact first: 32 contacts at a time, lane 0 the newest; an
+    // edge's place is its body's running count plus the newer edges of that body in the batch
+    int2* items = x.s_adj_items + 2 * (size_t)c0;
+    for (int top = n - 1; top >= 0; top -= kWarp) {
+        int k = top - lane;
+        bool edge = k >= 0 && (x.s_cq[c0 + k] & 1);
+        int2 cb = edge ? x.s_cbody[c0 + k] : make_int2(-1, -1);
+        int rA = 0, rB = 0;
+#pragma unroll 8
+        for (int j = 0; j < kWarp; ++j) {
+            int oa = __shfl_sync(0xffffffffu, cb.x, j), ob = __shfl_sync(0xffffffffu, cb.y, j);
+            if (j < lane && oa >= 0) {
+                rA += (oa == cb.x) + (ob == cb.x);
+                rB += (oa == cb.y) + (ob == cb.y);
+            }
+        }
+        int pA = 0, pB = 0;
+        if (edge) { pA = stack[cb.x] + rA; pB = stack[cb.y] + rB; }
+        tsync();
+        if (edge) {
+            items[pA] = make_int2(k, cb.y);
+            items[pB] = make_int2(k, cb.x);
+            atomicAdd(&stack[cb.x], 1);
+            atomicAdd(&stack[cb.y], 1);
+        }
+        tsync();
+    }
     stamp(x, w, 1);
     int nIsl = 0, nbI = 0, ncI = 0, njI = 0, maxLv = 0, maxLp = 0;
     if (lane == 0) {
-        int* cursor = x.s_cursor + b0;
-        int* items = x.s_adj_items + 2 * (size_t)c0;
-        const int2* cbody = x.s_cbody + c0;
-        const unsigned char* cq = x.s_cq + c0;
-        unsigned char* cvis = x.s_cvis + c0;
-        for (int k = n - 1; k >= 0; --k) {
-            if (!(cq[k] & 1)) continue;
-            int2 cb = cbody[k];
-            items[cursor[cb.x]++] = k;
-            items[cursor[cb.y]++] = k;
-        }
-        const int* adj = x.s_adj_start + bx;
-        int* stack = x.s_stack + b0;
         int* statics = x.s_last + b0;
         int* isl_body = x.s_isl_body + b0;
         int* isl_contact = x.s_isl_contact + c0;
+        int2* isl_pair = x.s_isl_pair + c0;
         int* body_island = x.s_body_island + b0;
         // depth-first island search (b2world.d:959-1095)
         for (int seed = nb - 1; seed >= 0; --seed) {
-            unsigned char fs = bfl[seed];
+            unsigned char fs = vbf[seed];
             if (fs & kBfVisited) continue;
             if ((fs & kBfAwake) == 0 || (fs & kBfActive) == 0) continue;
             if (fs & kBfStatic) continue;
@@ -1347,59 +1402,74 @@ __global__ void __launch_bounds__(kSolveWarps * 32, 3) k_solve(Ctx x) {
             x.s_isl_jstart[bx + nIsl] = njI;
             int top = 0, nStatic = 0;
             stack[top++] = seed;
-            bfl[seed] = fs | kBfVisited;
+            vbf[seed] = fs | kBfVisited;
             while (top > 0) {
                 int b = stack[--top];
                 body_island[b] = nIsl;
-                if (bfl[b] & kBfStatic) {
+                unsigned char fb = vbf[b];
+                if (fb & kBfStatic) {
                     statics[nStatic++] = b;
                     continue;
                 }
                 isl_body[nbI++] = b;
                 for (int e = adj[b], ee = adj[b + 1]; e < ee; ++e) {
-                    int k = items[e];
-                    if (cvis[k]) continue;
-                    isl_contact[ncI++] = c0 + k;
-                    cvis[k] = 1;
-                    int2 cb = cbody[k];
-                    int other = cb.x == b ? cb.y : cb.x;
-                    unsigned char fo = bfl[other];
+                    int2 it = items[e];
+                    if (cvis[it.x]) continue;
+                    isl_contact[ncI] = c0 + it.x;
+                    isl_pair[ncI] = make_int2(b, it.y);
+                    ++ncI;
+                    cvis[it.x] = 1;
+                    unsigned char fo = vbf[it.y];
                     if (fo & kBfVisited) continue;
-                    stack[top++] = other;
-                    bfl[other] = fo | kBfVisited;
+                    stack[top++] = it.y;
+                    vbf[it.y] = fo | kBfVisited;
                 }
                 const BodyStatic& st = x.bst[b0 + b];
                 for (int e = 0; e < st.jadj_count; ++e) {
                     int j = x.jadj_joint[st.jadj_start + e];
                     if (x.jt[j].island_flag) continue;
                     int other = x.jadj_other[st.jadj_start + e] - b0;
-                    unsigned char fo = bfl[other];
+                    unsigned char fo = vbf[other];
                     if ((fo & kBfActive) == 0) continue;
                     x.s_isl_joint[j0 + njI++] = j;
                     x.jt[j].island_flag = 1;
                     if (fo & kBfVisited) continue;
                     stack[top++] = other;
-                    bfl[other] = fo | kBfVisited;
+                    vbf[other] = fo | kBfVisited;
                 }
             }
-            for (int i = 0; i < nStatic; ++i) bfl[statics[i]] &= ~kBfVisited;
+            for (int i = 0; i < nStatic; ++i) vbf[statics[i]] &= ~kBfVisited;
             ++nIsl;
         }
         x.s_isl_bstart[bx + nIsl] = nbI;
         x.s_isl_cstart[bx + nIsl] = ncI;
         x.s_isl_jstart[bx + nIsl] = njI;
-        stamp(x, w, 2);
-        maxLv = build_schedule(x, wi, nIsl, false, x.s_sched_v, x.s_lvl_v);
-        maxLp = build_schedule(x, wi, nIsl, true, x.s_sched_p, x.s_lvl_p);
         wd.islands = nIsl;
-        if (x.prof) { x.prof[16 * (size_t)w + 12] = maxLv; x.prof[16 * (size_t)w + 13] = n; x.prof[16 * (size_t)w + 14] = nb; }
     }
-    stamp(x, w, 3);
     nIsl = __shfl_sync(0xffffffffu, nIsl, 0);
     nbI = __shfl_sync(0xffffffffu, nbI, 0);
     ncI = __shfl_sync(0xffffffffu, ncI, 0);
-    maxLv = __shfl_sync(0xffffffffu, maxLv, 0);
-    maxLp = __shfl_sync(0xffffffffu, maxLp, 0);
+    njI = __shfl_sync(0xffffffffu, njI, 0);
+    tsync();
+    stamp(x, w, 2);
+    if (gsm)
+        for (int i = lane; i < nb; i += kWarp) bfl[i] = vbf[i];
+    for (int k = lane; k < n; k += kWarp)
+        if (cvis[k]) x.ct[c0 + k].flags |= kContactIsland;
+    // level schedules; without joints in the islands the two orders coincide and one
+    // schedule serves both
+    int* last = gsm ? stack : x.s_last + b0;
+    maxLv = build_schedule(x, wi, nIsl, false, vbf, last, x.s_sched_v, x.s_lvl_v);
+    int* sched_p = x.s_sched_v;
+    int* lvl_p = x.s_lvl_v;
+    maxLp = maxLv;
+    if (njI) {
+        sched_p = x.s_sched_p;
+        lvl_p = x.s_lvl_p;
+        maxLp = build_schedule(x, wi, nIsl, true, vbf, last, sched_p, lvl_p);
+    }
+    if (x.prof && lane == 0) { x.prof[kProfSlots * (size_t)w + 12] = maxLv; x.prof[kProfSlots * (size_t)w + 13] = n; x.prof[kProfSlots * (size_t)w + 14] = nb; }
+    stamp(x, w, 3);
     if (lane == 0) {
         wd.acc_isl_bodies += (unsigned long long)nbI;
         wd.acc_isl_contacts += (unsigned long long)ncI;
@@ -1412,8 +1482,6 @@ __global__ void __launch_bounds__(kSolveWarps * 32, 3) k_solve(Ctx x) {
         if ((bfl[i] & kBfVisited) && !(bfl[i] & kBfStatic)) B.flags |= kBodyIsland;
         if (x.s_body_island[b0 + i] >= 0) b_set_awake(B, true);
     }
-    for (int k = lane; k < n; k += kWarp)
-        if (x.s_cvis[c0 + k]) x.ct[c0 + k].flags |= kContactIsland;
     // integrate velocities (b2island.d:82-116)
     for (int t = lane; t < nbI; t += kWarp) {
         int i = x.s_isl_body[b0 + t];
@@ -1451,7 +1519,7 @@ __global__ void __launch_bounds__(kSolveWarps * 32, 3) k_solve(Ctx x) {
         } else {
             vrow[idx].ids = make_int4(0, 0, 0, item);
         }
-        int pitem = x.s_sched_p[kx + idx];
+        int pitem = sched_p[kx + idx];
         int is = item_island(x, pitem, b0);
         if (pitem >= 0) {
             VC vc;
@@ -1470,8 +1538,8 @@ __global__ void __launch_bounds__(kSolveWarps * 32, 3) k_solve(Ctx x) {
         if (warm)
             sweep_levels(x.s_lvl_v + kx, maxLv, vrow, vstage, [&](const VRow& r, int) { warm_start(unpack_v(r), sb); });
     } else {
-        run_levels(x.s_lvl_p + kx, maxLp, [&](int idx) {
-            int item = x.s_sched_p[kx + idx];
+        run_levels(lvl_p + kx, maxLp, [&](int idx) {
+            int item = sched_p[kx + idx];
             if (item >= 0) { if (warm) warm_start(unpack_v(load_v(vrow + x.s_vpos[item])), sb); }
             else joint_init(x, -item - 1, b0, sb, warm, dtRatio);
         });
@@ -1527,7 +1595,7 @@ __global__ void __launch_bounds__(kSolveWarps * 32, 3) k_solve(Ctx x) {
             x.s_isl_flags[b0 + is] &= ~4;
         }
         tsync();
-        sweep_levels(x.s_lvl_p + kx, maxLp, prow, pstage, [&](const PRow& r, int) {
+        sweep_levels(lvl_p + kx, maxLp, prow, pstage, [&](const PRow& r, int) {
             int is = r.ids.w;
             if (x.s_isl_flags[b0 + is] & 1) return;
             if (r.ids.z >= 0) {
@@ -1639,6 +1707,32 @@ DG bool toi_needs(const Ctx& x, int ci, int b0) {
     return true;
 }
 
+// contact that can ever need a TOI this step: no sensor, and a static, kinematic or bullet
+// body on one side (b2world.d:1172-1188; body types and bullet flags do not change inside a step)
+DG bool toi_candidate(const Ctx& x, int ci, int b0) {
+    if (x.s_cq[ci] & 2) return false;
+    int2 cb = x.s_cbody[ci];
+    const dbox_body_state& bA = x.bs[b0 + cb.x];
+    const dbox_body_state& bB = x.bs[b0 + cb.y];
+    bool collideA = (bA.flags & kBodyBullet) || bA.type != kDynamicBody;
+    bool collideB = (bB.flags & kBodyBullet) || bB.type != kDynamicBody;
+    return collideA || collideB;
+}
+
+// append the candidates among contact slots [k0, k1) (world-local) to list[cnt ..] in
+// ascending order; returns the new count (all lanes)
+DG int toi_collect(const Ctx& x, int c0, int b0, int k0, int k1, int* list, int cnt) {
+    const int lane = lane_id();
+    for (int base = k0; base < k1; base += kWarp) {
+        int k = base + lane;
+        bool cand = k < k1 && toi_candidate(x, c0 + k, b0);
+        unsigned bal = __ballot_sync(0xffffffffu, cand);
+        if (cand) list[cnt + __popc(bal & ((1u << lane) - 1u))] = k;
+        cnt += __popc(bal);
+    }
+    return cnt;
+}
+
 // b2Contact.Update inside the TOI loop: wakes are applied immediately
 DG void toi_update(const Ctx& x, dbox_contact_state& c) {
     if (contact_update(x, c)) {
@@ -1716,17 +1810,22 @@ DG void solve_toi_island(const Ctx& x, int w, const WorldInfo& wi, SB sb, int nb
     }
 }
 
-__global__ void k_toi(Ctx x) {
-    int w = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
-    if (w >= x.W) return;
+// b2World.SolveTOI (b2world.d:1127-1452) for world w, then the end of b2World.Step
+DG void toi_world(const Ctx& x, int w, float* sbp) {
     const WorldInfo& wi = x.wi[w];
     WorldDyn& wd = x.wd[w];
     int lane = lane_id();
     const int b0 = wi.body_start, nb = wi.body_count, c0 = wi.contact_start;
+    // optional profile: slot 16 total cycles, 17 events, 18.. cycles per part of the event loop
+    long long tlast = clock64(), t_start = tlast;
+    long long tacc[7] = {0, 0, 0, 0, 0, 0, 0};
+    auto mark = [&](int part) {
+        if (x.prof) { long long t = clock64(); tacc[part] += t - tlast; tlast = t; }
+    };
     if (x.continuous && x.dt > 0.0f) {
         bool advanced = wd.step_complete == 0;
         SB sb;
-        sb.p = x.s_sbody + 6 * (size_t)b0;
+        sb.p = sbp;
         {
             int n = wd.contact_count;
             for (int k = lane; k < n; k += kWarp) contact_compact(x, c0 + k, b0);
@@ -1746,6 +1845,11 @@ __global__ void k_toi(Ctx x) {
         }
         for (int i = lane; i < nb; i += kWarp) x.s_bfl[b0 + i] = 0;
         tsync();
+        // TOI candidates in list order (ascending slot): only these can get a TOI, join a TOI
+        // island as a neighbour or carry the TOI / island flags that an event clears
+        int* cand = x.s_tcand + c0;
+        int ncand = toi_collect(x, c0, b0, 0, wd.contact_count, cand, 0);
+        tsync();
         int events = 0;
         const int max_events = 9 * wi.contact_cap + 16;   // each contact takes at most 9 events
         for (int iter = 0;; ++iter) {
@@ -1756,15 +1860,15 @@ __global__ void k_toi(Ctx x) {
             int n = wd.contact_count;
             // sweeps are put onto a common time in list order (b2world.d:1212-1226)
             if (advanced) {
-                for (int base = n - 1; base >= 0; base -= kWarp) {
-                    int k = base - lane;
-                    bool need = k >= 0 && toi_needs(x, c0 + k, b0);
+                for (int base = ncand - 1; base >= 0; base -= kWarp) {
+                    int t = base - lane;
+                    bool need = t >= 0 && toi_needs(x, c0 + cand[t], b0);
                     unsigned bal = __ballot_sync(0xffffffffu, need);
                     if (lane == 0) {
                         while (bal) {
                             int l = __ffs(bal) - 1;
                             bal &= bal - 1;
-                            int kk = base - l;
+                            int kk = cand[base - l];
                             int2 cb = x.s_cbody[c0 + kk];
                             dbox_body_state& bA = x.bs[b0 + cb.x];
                             dbox_body_state& bB = x.bs[b0 + cb.y];
@@ -1785,7 +1889,9 @@ __global__ void k_toi(Ctx x) {
                     tsync();
                 }
             }
-            for (int k = lane; k < n; k += kWarp) {
+            mark(0);
+            for (int t = lane; t < ncand; t += kWarp) {
+                int k = cand[t];
                 if (!toi_needs(x, c0 + k, b0)) continue;
                 dbox_contact_state& c = x.ct[c0 + k];
                 const DFixture& fa = x.fx[c.fixture_a];
@@ -1801,10 +1907,12 @@ __global__ void k_toi(Ctx x) {
                 c.flags |= kContactToi;
             }
             tsync();
+            mark(1);
             // minimum TOI, first in list order on ties
             float bestA = 1.0f;
             int bestLp = 0x7fffffff;
-            for (int k = lane; k < n; k += kWarp) {
+            for (int t = lane; t < ncand; t += kWarp) {
+                int k = cand[t];
                 const dbox_contact_state& c = x.ct[c0 + k];
                 if ((c.flags & kContactEnabled) == 0 || c.toi_count > kMaxSubSteps) continue;
                 if ((c.flags & kContactToi) == 0) continue;
@@ -1816,6 +1924,7 @@ __global__ void k_toi(Ctx x) {
                 int ol = __shfl_xor_sync(0xffffffffu, bestLp, o);
                 if (oa < bestA || (oa == bestA && ol < bestLp)) { bestA = oa; bestLp = ol; }
             }
+            mark(2);
             if (bestLp == 0x7fffffff || 1.0f - 10.0f * kEpsilon < bestA) {
                 if (lane == 0) wd.step_complete = 1;
                 break;
@@ -1856,23 +1965,25 @@ __global__ void k_toi(Ctx x) {
             solved = __shfl_sync(0xffffffffu, solved, 0);
             nbI = __shfl_sync(0xffffffffu, nbI, 0);
             ncI = __shfl_sync(0xffffffffu, ncI, 0);
+            mark(3);
             if (solved) {
                 // contacts of each dynamic event body, in its edge-list order (b2world.d:1306-1411)
                 for (int q = 0; q < 2; ++q) {
                     const int body = q == 0 ? mcb.x : mcb.y;
                     if (x.bs[b0 + body].type != kDynamicBody) continue;
                     bool stop = false;
-                    for (int base = n - 1; base >= 0 && !stop; base -= kWarp) {
-                        int k = base - lane;
+                    // every contact that can join (b2world.d:1330-1346) is a candidate
+                    for (int base = ncand - 1; base >= 0 && !stop; base -= kWarp) {
+                        int t = base - lane;
                         bool hit = false;
-                        if (k >= 0) { int2 cb = x.s_cbody[c0 + k]; hit = cb.x == body || cb.y == body; }
+                        if (t >= 0) { int2 cb = x.s_cbody[c0 + cand[t]]; hit = cb.x == body || cb.y == body; }
                         unsigned bal = __ballot_sync(0xffffffffu, hit);
                         if (lane == 0) {
                             dbox_body_state& Bd = x.bs[b0 + body];
                             while (bal) {
                                 int l = __ffs(bal) - 1;
                                 bal &= bal - 1;
-                                int kk = base - l;
+                                int kk = cand[base - l];
                                 if (nbI == 2 * kMaxTOIContacts || ncI == kMaxTOIContacts) { stop = true; break; }
                                 dbox_contact_state& c = x.ct[c0 + kk];
                                 if (c.flags & kContactIsland) continue;
@@ -1902,9 +2013,11 @@ __global__ void k_toi(Ctx x) {
                     nbI = __shfl_sync(0xffffffffu, nbI, 0);
                     ncI = __shfl_sync(0xffffffffu, ncI, 0);
                 }
+                mark(4);
                 if (lane == 0) {
                     float subDt = (1.0f - minAlpha) * x.dt;
                     solve_toi_island(x, w, wi, sb, nbI, ncI, mcb.x, mcb.y, subDt);
+                    mark(5);
                     for (int i = 0; i < nbI; ++i) {
                         int body = x.s_isl_body[b0 + i];
                         dbox_body_state& Bd = x.bs[b0 + body];
@@ -1915,8 +2028,10 @@ __global__ void k_toi(Ctx x) {
                     }
                 }
                 tsync();
-                // invalidate the TOIs of every contact on a displaced dynamic body
-                for (int k = lane; k < n; k += kWarp) {
+                // invalidate the TOIs of every contact on a displaced dynamic body (only
+                // candidates carry the two flags)
+                for (int t = lane; t < ncand; t += kWarp) {
+                    int k = cand[t];
                     int2 cb = x.s_cbody[c0 + k];
                     if ((x.s_bfl[b0 + cb.x] | x.s_bfl[b0 + cb.y]) & kBfMark)
                         x.ct[c0 + k].flags &= ~(uint32_t)(kContactToi | kContactIsland);
@@ -1926,6 +2041,9 @@ __global__ void k_toi(Ctx x) {
                     for (int i = 0; i < nbI; ++i) x.s_bfl[b0 + x.s_isl_body[b0 + i]] = 0;
                 tsync();
                 find_new_contacts(x, w);
+                ncand = toi_collect(x, c0, b0, n, wd.contact_count, cand, ncand);
+                tsync();
+                mark(6);
             }
             advanced = true;
             if (solved && x.sub_stepping) {
@@ -1936,6 +2054,13 @@ __global__ void k_toi(Ctx x) {
         if (lane == 0) { wd.toi_events = events; wd.acc_toi_events += (unsigned long long)events; }
     }
     tsync();
+    if (x.prof && lane == 0) {
+        unsigned long long* pr = x.prof + kProfSlots * (size_t)w;
+        pr[16] = clock64() - t_start;
+        pr[17] = wd.toi_events;
+#pragma unroll
+        for (int i = 0; i < 7; ++i) pr[18 + i] = tacc[i];
+    }
     // b2World.Step epilogue (b2world.d:421-429)
     if (lane == 0 && x.dt > 0.0f) wd.inv_dt0 = x.inv_dt;
     if (wd.flags & 4u) {
@@ -1946,11 +2071,37 @@ __global__ void k_toi(Ctx x) {
     }
 }
 
+// The solve phase and the TOI phase of one step, one warp per world: each world goes
+// from its island solve straight to its TOI events, so a world that is slow in one phase
+// overlaps with worlds that are slow in the other.  Warp slots and their shared memory
+// (row staging, solver body rows) come from the host's packing of worlds into blocks.
+__global__ void __launch_bounds__(kSolveWarps * 32, 3) k_solve_toi(Ctx x) {
+    extern __shared__ float smem_sb[];
+    const int slot = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+    const int w = x.solve_world[slot];
+    if (w < 0) return;
+    const int soff = x.solve_smem[slot];
+    float* sbp = soff >= 0 ? smem_sb + soff : x.s_sbody + 6 * (size_t)x.wi[w].body_start;
+    float* stage_f = smem_sb + (threadIdx.x >> 5) * kStageFloats;
+    unsigned long long g0 = 0;
+    if (x.prof) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(g0));
+    solve_world(x, w, sbp, stage_f);
+    tsync();
+    toi_world(x, w, sbp);
+    if (x.prof && lane_id() == 0) {
+        unsigned long long g1;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(g1));
+        x.prof[kProfSlots * (size_t)w + 25] = g0;
+        x.prof[kProfSlots * (size_t)w + 26] = g1;
+        x.prof[kProfSlots * (size_t)w + 27] = slot;
+    }
+}
+
 }  // namespace dg
 
 // ------------------------------------------------------------ launch entry points (called from api.cpp)
 // Launch one step.  ev, when not NULL, holds 4 events recorded at the phase
-// boundaries: [0] before Collide, [1] before Solve, [2] before SolveTOI, [3] after.
+// boundaries: [0] before Collide, [1] before Solve, [2] and [3] after Solve + SolveTOI (one kernel).
 extern "C" int dbox_launch_step_ev(const dg::Ctx* x, cudaStream_t stream, int* launches, cudaEvent_t* ev) {
     const int threads = 128;                       // four worlds per block, one warp each
     int team_blocks = (x->W * dg::kWarp + threads - 1) / threads;
@@ -1963,15 +2114,14 @@ extern "C" int dbox_launch_step_ev(const dg::Ctx* x, cudaStream_t stream, int* l
     dg::k_collide<<<flat_blocks, 256, 0, stream>>>(*x);
     dg::k_collide_finish<<<team_blocks, threads, 0, stream>>>(*x);
     if (ev) cudaEventRecordWithFlags(ev[1], stream, cudaEventRecordExternal);
-    dg::k_solve<<<x->solve_blocks, dg::kSolveWarps * dg::kWarp, x->solve_smem_floats * sizeof(float), stream>>>(*x);
+    dg::k_solve_toi<<<x->solve_blocks, dg::kSolveWarps * dg::kWarp, x->solve_smem_floats * sizeof(float), stream>>>(*x);
     if (ev) cudaEventRecordWithFlags(ev[2], stream, cudaEventRecordExternal);
-    dg::k_toi<<<team_blocks, threads, 0, stream>>>(*x);
     if (ev) cudaEventRecordWithFlags(ev[3], stream, cudaEventRecordExternal);
-    if (launches) *launches = 5;
+    if (launches) *launches = 4;
     return (int)cudaGetLastError();
 }
 
-extern "C" const void* dbox_solve_kernel() { return reinterpret_cast<const void*>(&dg::k_solve); }
+extern "C" const void* dbox_solve_kernel() { return reinterpret_cast<const void*>(&dg::k_solve_toi); }
 
 extern "C" int dbox_launch_step(const dg::Ctx* x, cudaStream_t stream, int* launches) {
     return dbox_launch_step_ev(x, stream, launches, nullptr);

@@ -128,6 +128,7 @@ struct __align__(16) PRow {
 // TOI sweep snapshot of one contact's two bodies (taken in list order).
 struct SweepSnap { Sweep a, b; float alpha0; int pad; };
 
+constexpr int kProfSlots = 32;         // per-world slots of the optional phase profile
 constexpr int kSolveWarps = 4;          // warp slots (worlds) per block of the solve kernel
 constexpr int kStageFloats = 2 * 32 * 36; // per warp: two levels of 32 staged 144-byte rows
 
@@ -170,7 +171,9 @@ struct Ctx {
     int* s_moved;                  // fixture-indexed
     // scratch (contact-indexed)
     int* s_cstate;                 // 0 processed, 1 inactive, 2 destroyed
-    int* s_adj_items;              // 2 per contact slot
+    int2* s_adj_items;             // 2 per contact slot: (contact, other body) edges by body
+    int2* s_isl_pair;              // contact-slot-indexed: bodies of the island contact sequence
+    int* s_tcand;                  // contact-slot-indexed: TOI candidate contacts of the world
     int* s_isl_contact;            // contact-slot-indexed
     int* s_level;                  // kx-indexed
     int* s_sched_v;                // kx-indexed
@@ -178,6 +181,7 @@ struct Ctx {
     int* s_sched_p;
     int* s_lvl_p;
     int* s_tmp;                    // kx-indexed sequence-order items while sorting by level
+    int* s_lcur;                   // kx-indexed level cursors while bucketing by level
     int* s_isl_joint;              // joint-indexed
     int* s_accept;                 // pair-indexed
     VRow* vr;                      // kx-indexed: velocity rows in velocity-schedule order
@@ -202,7 +206,7 @@ struct Ctx {
     int warm_starting, continuous, sub_stepping, allow_sleep;
     int record_events;
     int* g_status;                 // bit (-code) set for every DBOX_ERR_* raised by any world
-    unsigned long long* prof;      // optional: 16 clock64 phase stamps per world (NULL = off)
+    unsigned long long* prof;      // optional: kProfSlots clock64 figures per world (NULL = off)
 };
 
 // ------------------------------------------------------------ body state helpers (dbox_body_state fields)

@@ -270,9 +270,13 @@ int32_t dbox_world_apply_forces(dbox_world* w, const float* force_torque);
 /* b2Body.GetPosition + b2Body.GetAngle (b2body.d:283-296) for every body: (x, y, angle) per body. */
 int32_t dbox_world_get_transforms(dbox_world* w, float* xya);
 
-/* Per-world device clock stamps at the phase boundaries of the solve kernel (diagnostics):
- * enable before stepping; out receives 16 uint64 per world (stamps 0..11, then the number of
- * velocity levels, contacts and bodies of the world in slots 12..14). */
+/* Per-world device clock figures of the last step (diagnostics): enable before stepping;
+ * out receives 32 uint64 per world: slots 0..11 clock stamps at the phase boundaries of the
+ * solve kernel, 12..14 the world's velocity levels, contacts and bodies, 16 the cycles of the
+ * SolveTOI kernel, 17 its TOI events, 18..24 its cycles per part of the event loop (sweep
+ * advance, TOI, minimum, event contact, neighbours, sub-step solve, fixture sync and pairs),
+ * 25..26 the global timer (ns) when the world's warp started and ended the solve + SolveTOI
+ * kernel, 27 its warp slot. */
 int32_t dbox_world_set_phase_profile(dbox_world* w, int32_t enable);
 int32_t dbox_world_get_phase_profile(dbox_world* w, unsigned long long* out);
 
