@@ -153,8 +153,8 @@ void free_device(dbox_world* w) {
 
 int next_pow2(int v) { int p = 1; while (p < v) p <<= 1; return p; }
 
-// Warp slots of the solve kernel (four per block).  Each world's solver body rows
-// (24 bytes a body) go to shared memory when they fit the block's budget; worlds are
+// Warp slots of the solve kernel (four per block).  Each world's solver body rows and
+// island words (32 bytes a body) go to shared memory when they fit the block's budget; worlds are
 // placed largest first (first fit over the open blocks), so the biggest worlds sit in
 // the lowest blocks and start first, and small worlds fill the remaining room.
 int pack_solve_slots(dbox_world* w) {
@@ -164,8 +164,8 @@ int pack_solve_slots(dbox_world* w) {
     // budget in bodies per block: room for the largest world, at least 1024, and at most
     // 1536 when there are enough worlds to fill the GPU (three blocks per SM stay resident);
     // the front of the block holds each warp's constraint-row staging slots
-    const int stage_floats = dg::kSolveWarps * dg::kStageFloats;
-    const int hard_cap = (227 * 1024 - 1024 - 4 * stage_floats) / 24;
+    const int stage_floats = dg::kSolveWarps * dg::kWarpSmemFloats;
+    const int hard_cap = (227 * 1024 - 1024 - 4 * stage_floats) / 32;
     int budget = std::max(1024, max_nb);
     budget = std::min(budget, W >= 3 * 152 ? 1536 : hard_cap);
     std::vector<int> order(W);
@@ -196,7 +196,7 @@ int pack_solve_slots(dbox_world* w) {
         }
         int slot = chosen * dg::kSolveWarps + count[chosen]++;
         slot_world[slot] = wid;
-        slot_off[slot] = in_smem ? stage_floats + 6 * used[chosen] : -1;
+        slot_off[slot] = in_smem ? stage_floats + 8 * used[chosen] : -1;
         used[chosen] += need;
     }
     if (used.empty()) {                     // no worlds: one idle block
@@ -207,7 +207,7 @@ int pack_solve_slots(dbox_world* w) {
     int max_used = 0;
     for (int u : used) max_used = std::max(max_used, u);
     w->solve_blocks = (int)used.size();
-    w->solve_smem_floats = stage_floats + 6 * std::max(max_used, 1);
+    w->solve_smem_floats = stage_floats + 8 * std::max(max_used, 1);
     if (w->d_solve_world.alloc(slot_world.size()) || w->d_solve_smem.alloc(slot_off.size()))
         return fail(DBOX_ERR_CUDA, "device allocation failed (solve slots)");
     CU(cudaMemcpy(w->d_solve_world.p, slot_world.data(), sizeof(int) * slot_world.size(), cudaMemcpyHostToDevice));

@@ -1215,7 +1215,9 @@ DG void run_levels(const int* lvl, int maxL, F&& f) {
     for (int L = 1; L <= maxL; ++L) {
         q.step_to(L);
         int s = q.get(L), e = q.get(L + 1);
-        for (int idx = s + lane; idx < e; idx += kWarp) f(idx);
+        if (s + lane < e) f(s + lane);
+        if (e - s > kWarp)
+            for (int idx = s + lane + kWarp; idx < e; idx += kWarp) f(idx);
         tsync();
     }
 }
@@ -1223,68 +1225,122 @@ DG void run_levels(const int* lvl, int maxL, F&& f) {
 DG VRow load_row(const VRow* p) { return load_v(p); }
 DG PRow load_row(const PRow* p) { return load_p(p); }
 
-// 16-byte asynchronous global -> shared copies (L2 only), committed as one group per level
-DG void cp_async16(void* smem_dst, const void* gsrc) {
-    unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" :: "r"(d), "l"(gsrc) : "memory");
+// ---- bulk staging of constraint rows (one-dimensional TMA copies completed on mbarriers)
+DG unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+DG void mbar_init(unsigned long long* bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(bar)) : "memory");
 }
-DG void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-DG void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
-DG void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
-template <class RowT>
-DG void stage_row(RowT* dst, const RowT* src) {
-    static_assert(sizeof(RowT) % 16 == 0, "rows are whole 16-byte chunks");
-    const float4* s = reinterpret_cast<const float4*>(src);
-    float4* d = reinterpret_cast<float4*>(dst);
-#pragma unroll
-    for (int k = 0; k < (int)(sizeof(RowT) / 16); ++k) cp_async16(d + k, s + k);
+DG void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+DG void fence_async_shared() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+DG void fence_async_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
+// arm `bar` for `bytes` and copy them global -> shared; completes the barrier's phase
+DG void bulk_copy(unsigned long long* bar, void* dst, const void* src, unsigned bytes) {
+    unsigned b = smem_u32(bar);
+    unsigned long long state;
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 %0, [%1], %2;" : "=l"(state) : "r"(b), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 :: "r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(b) : "memory");
+    (void)state;
 }
+constexpr int kMbarSpinLimit = 1 << 20;
+// wait for the phase of `bar` with the given parity; false when the spin limit ran out
+DG bool mbar_wait(unsigned long long* bar, unsigned parity) {
+    unsigned b = smem_u32(bar);
+    for (int i = 0; i < kMbarSpinLimit; ++i) {
+        unsigned done;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}" : "=r"(done) : "r"(b), "r"(parity) : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// Row staging of one warp: a ring of two halves in shared memory, each one block of
+// consecutive schedule positions (32 velocity rows or 48 position rows, 4608 bytes), with
+// one mbarrier per half.  `par` holds the phase bit each half waits for next.
+struct RowRing {
+    float* base;                   // 9216 bytes of rows
+    unsigned long long* bar;       // two mbarriers
+    unsigned par;
+    bool ok;
+};
 
 // One sweep over levels 1..maxL of a schedule whose rows are stored in schedule order:
 // f(row, idx) for every position of a level, levels in order, positions of a level spread
-// over the lanes.  Each lane's row of the next level is copied into shared memory (stage:
-// this warp's two slots of 32 rows) while the current level is solved, and the level
-// offsets are read one level ahead, so neither load sits on the dependent chain between
-// levels.  A row of a later level is never written by an earlier one; a lane's staged
-// row is only read by that lane.
+// over the lanes.  Rows arrive by blocks: block m+1 is copied by one bulk copy as soon as
+// the levels reach block m, so a level reads its rows from shared memory and the copies
+// stay off the dependent chain between levels; rows of a level wider than the two
+// resident blocks are read from global memory.  A row of a later position is never
+// written by an earlier level, and the rows' global writes of the previous sweep are
+// ordered before the copies by the proxy fence at the start.
 template <class RowT, class F>
-DG void sweep_levels(const int* lvl, int maxL, const RowT* rows, RowT* stage, F&& f) {
+DG void sweep_levels(const int* lvl, int maxL, int nItems, const RowT* rows, RowRing& ring, F&& f) {
     if (maxL < 1) return;
+    constexpr int B = (int)(4608 / sizeof(RowT));
+    static_assert(4608 % sizeof(RowT) == 0 && sizeof(RowT) % 16 == 0, "rows tile a half of the ring");
     const int lane = lane_id();
-    LevelQ q;
-    q.init(lvl, maxL + 1);
-    int s = q.get(1), e = q.get(2);
-    int e2 = maxL >= 2 ? q.get(3) : e;                   // end of level 2 (it starts at e)
-    bool hc = s + lane < e;
-    int slot = 0;
-    if (hc) stage_row(stage + lane, rows + s + lane);
-    cp_async_commit();
+    RowT* slots = reinterpret_cast<RowT*>(ring.base);
+    const int nblk = (nItems + B - 1) / B;
+    int issued = -1, waited = -1;
+    auto wait_next = [&]() {
+        ++waited;
+        const int h = waited & 1;
+        ring.ok &= mbar_wait(&ring.bar[h], (ring.par >> h) & 1u);
+        ring.par ^= 1u << h;
+    };
+    auto issue_upto = [&](int want) {
+        want = want < nblk - 1 ? want : nblk - 1;
+        while (issued < want) {
+            const int m = issued + 1;
+            while (waited < m - 2) wait_next();          // the half's previous block has landed
+            if (lane == 0) {
+                fence_async_shared();
+                int cnt = nItems - m * B;
+                cnt = cnt < B ? cnt : B;
+                bulk_copy(&ring.bar[m & 1], slots + (m & 1) * B, rows + (size_t)m * B, (unsigned)(cnt * sizeof(RowT)));
+            }
+            issued = m;
+        }
+    };
+    fence_async_global();                                // this lane's row writes before the copies
+    tsync();
+    issue_upto(1);
+    // level offsets two levels ahead in registers (plain loads; their latency hides behind a level)
+    auto off = [&](int i) { return i <= maxL + 1 ? lvl[i] : nItems; };
+    int s = off(1), e = off(2), e2 = off(3);
     for (int L = 1; L <= maxL; ++L) {
-        bool hn = L < maxL && e + lane < e2;
-        if (hn) stage_row(stage + (slot ^ 1) * kWarp + lane, rows + e + lane);
-        cp_async_commit();
-        q.step_to(L);
-        int e3 = L + 3 <= maxL + 1 ? q.get(L + 3) : e2;  // end of level L + 2
-        cp_async_wait_prev();
-        if (hc) {
-            f(stage[slot * kWarp + lane], s + lane);
-            for (int idx = s + lane + kWarp; idx < e; idx += kWarp) f(load_row(rows + idx), idx);
+        const int e3 = off(L + 3);
+        const int mlo = s / B;
+        issue_upto(mlo + 1);
+        const int mhi = (e - 1) / B;
+        const int mneed = mhi < mlo + 1 ? mhi : mlo + 1;
+        while (waited < mneed) wait_next();
+        // one position per lane; a level wider than the warp takes the rest in a uniform branch
+        // (a loop whose trip count differs between lanes costs hundreds of cycles per level)
+        if (s + lane < e) {
+            const int idx = s + lane, m = idx / B;
+            f(slots[(m & 1) * B + (idx - m * B)], idx);
+        }
+        if (e - s > kWarp) {
+            for (int idx = s + lane + kWarp; idx < e; idx += kWarp) {
+                const int m = idx / B;
+                if (m <= mlo + 1) f(slots[(m & 1) * B + (idx - m * B)], idx);
+                else f(load_row(rows + idx), idx);
+            }
         }
         tsync();
-        slot ^= 1;
-        hc = hn;
         s = e;
         e = e2;
         e2 = e3;
     }
-    cp_async_wait_all();
+    while (waited < issued) wait_next();
 }
 
 
 // b2World.Solve (b2world.d:930-1124) for world w: islands, contact solver, sleep,
 // SynchronizeFixtures, FindNewContacts.  sbp: the world's solver body rows; stage_f: this
 // warp's staging area in shared memory.
-DG void solve_world(const Ctx& x, int w, float* sbp, float* stage_f) {
+DG void solve_world(const Ctx& x, int w, float* sbp, bool sb_smem, float* stage_f) {
     const WorldInfo& wi = x.wi[w];
     WorldDyn& wd = x.wd[w];
     int lane = lane_id();
@@ -1299,8 +1355,20 @@ DG void solve_world(const Ctx& x, int w, float* sbp, float* stage_f) {
     stamp(x, w, 0);
     SB sb;
     sb.p = sbp;
-    VRow* vstage = reinterpret_cast<VRow*>(stage_f);
-    PRow* pstage = reinterpret_cast<PRow*>(stage_f);
+    // per-island flags and minimum separations of the position iterations: after the
+    // world's body rows in shared memory when those are there, else global rows
+    int* iflags = sb_smem ? reinterpret_cast<int*>(sbp + 6 * nb) : x.s_isl_flags + b0;
+    unsigned* iminsep = sb_smem ? reinterpret_cast<unsigned*>(sbp + 7 * nb) : x.s_isl_minsep + b0;
+    RowRing ring;
+    ring.base = stage_f;
+    ring.bar = reinterpret_cast<unsigned long long*>(stage_f + kStageFloats);
+    ring.par = 0;
+    ring.ok = true;
+    if (lane == 0) {
+        mbar_init(&ring.bar[0]);
+        mbar_init(&ring.bar[1]);
+        fence_mbar_init();
+    }
     unsigned char* bfl = x.s_bfl + b0;
     // compact per-body / per-contact data; island flags cleared (b2world.d:944-957)
     for (int i = lane; i < nb; i += kWarp) {
@@ -1424,6 +1492,7 @@ DG void solve_world(const Ctx& x, int w, float* sbp, float* stage_f) {
                     stack[top++] = it.y;
                     vbf[it.y] = fo | kBfVisited;
                 }
+                if (nj == 0) continue;
                 const BodyStatic& st = x.bst[b0 + b];
                 for (int e = 0; e < st.jadj_count; ++e) {
                     int j = x.jadj_joint[st.jadj_start + e];
@@ -1515,7 +1584,13 @@ DG void solve_world(const Ctx& x, int w, float* sbp, float* stage_f) {
             constraint_ctor(x, item, b0, warm, dtRatio, vc, pc);
             constraint_init_velocity(vc, pc, sb);
             vrow[idx] = pack_v(vc, item);
-            if (njI) x.s_vpos[item] = idx;
+            if (njI) {
+                x.s_vpos[item] = idx;
+            } else {
+                // one schedule serves both orders: the position row of this place is this contact's
+                prow[idx] = pack_p(pc, x.s_body_island[b0 + ((bfl[vc.bodyA] & kBfStatic) ? vc.bodyB : vc.bodyA)]);
+                continue;
+            }
         } else {
             vrow[idx].ids = make_int4(0, 0, 0, item);
         }
@@ -1536,7 +1611,7 @@ DG void solve_world(const Ctx& x, int w, float* sbp, float* stage_f) {
     if (njI == 0) {
         // without joints the position-order and velocity-order schedules coincide
         if (warm)
-            sweep_levels(x.s_lvl_v + kx, maxLv, vrow, vstage, [&](const VRow& r, int) { warm_start(unpack_v(r), sb); });
+            sweep_levels(x.s_lvl_v + kx, maxLv, nItems, vrow, ring, [&](const VRow& r, int) { warm_start(unpack_v(r), sb); });
     } else {
         run_levels(lvl_p + kx, maxLp, [&](int idx) {
             int item = sched_p[kx + idx];
@@ -1547,7 +1622,7 @@ DG void solve_world(const Ctx& x, int w, float* sbp, float* stage_f) {
     stamp(x, w, 5);
     // velocity iterations (b2island.d:153-161)
     for (int it = 0; it < x.vel_iters; ++it) {
-        sweep_levels(x.s_lvl_v + kx, maxLv, vrow, vstage, [&](const VRow& r, int idx) {
+        sweep_levels(x.s_lvl_v + kx, maxLv, nItems, vrow, ring, [&](const VRow& r, int idx) {
             if (r.ids.w >= 0) {
                 VC vc = unpack_v(r);
                 solve_velocity(vc, sb);
@@ -1585,45 +1660,46 @@ DG void solve_world(const Ctx& x, int w, float* sbp, float* stage_f) {
         sb.set_c(i, c, a);
         sb.set_v(i, v, wv);
     }
-    for (int is = lane; is < nIsl; is += kWarp) x.s_isl_flags[b0 + is] = 0;
+    for (int is = lane; is < nIsl; is += kWarp) iflags[is] = 0;
     tsync();
     stamp(x, w, 7);
     // position iterations with per-island early exit (b2island.d:206-224)
     for (int it = 0; it < x.pos_iters; ++it) {
         for (int is = lane; is < nIsl; is += kWarp) {
-            x.s_isl_minsep[b0 + is] = fkey(0.0f);
-            x.s_isl_flags[b0 + is] &= ~4;
+            iminsep[is] = fkey(0.0f);
+            iflags[is] &= ~4;
         }
         tsync();
-        sweep_levels(lvl_p + kx, maxLp, prow, pstage, [&](const PRow& r, int) {
+        sweep_levels(lvl_p + kx, maxLp, nItems, prow, ring, [&](const PRow& r, int) {
             int is = r.ids.w;
-            if (x.s_isl_flags[b0 + is] & 1) return;
+            if (iflags[is] & 1) return;
             if (r.ids.z >= 0) {
                 float ms = solve_position(unpack_p(r), sb, false, -1, -1);
-                atomicMin(&x.s_isl_minsep[b0 + is], fkey(ms));
+                atomicMin(&iminsep[is], fkey(ms));
             } else if (!joint_solve_position(x, -r.ids.z - 1, b0, sb)) {
-                atomicOr(&x.s_isl_flags[b0 + is], 4);
+                atomicOr(&iflags[is], 4);
             }
         });
         int psolved = 0;
         for (int is = lane; is < nIsl; is += kWarp)
-            if (!(x.s_isl_flags[b0 + is] & 1))
+            if (!(iflags[is] & 1))
                 psolved += x.s_isl_cstart[bx + is + 1] - x.s_isl_cstart[bx + is];
         for (int o = 16; o > 0; o >>= 1) psolved += __shfl_xor_sync(0xffffffffu, psolved, o);
         if (lane == 0) wd.acc_psolve += (unsigned long long)psolved;
         bool remaining = false;
         for (int is = lane; is < nIsl; is += kWarp) {
-            int f = x.s_isl_flags[b0 + is];
+            int f = iflags[is];
             if (f & 1) continue;
-            bool contactsOkay = funkey(x.s_isl_minsep[b0 + is]) >= -3.0f * kLinearSlop;
+            bool contactsOkay = funkey(iminsep[is]) >= -3.0f * kLinearSlop;
             bool jointsOkay = (f & 4) == 0;
-            if (contactsOkay && jointsOkay) x.s_isl_flags[b0 + is] = f | 1 | 2;
+            if (contactsOkay && jointsOkay) iflags[is] = f | 1 | 2;
             else remaining = true;
         }
         if (!__any_sync(0xffffffffu, remaining)) break;
         tsync();
     }
     tsync();
+    if (!__all_sync(0xffffffffu, ring.ok) && lane == 0) set_error(x, w, DBOX_ERR_TIMEOUT);
     stamp(x, w, 8);
     // copy back + SynchronizeTransform (b2island.d:227-235)
     for (int t = lane; t < nbI; t += kWarp) {
@@ -1656,18 +1732,18 @@ DG void solve_world(const Ctx& x, int w, float* sbp, float* stage_f) {
         }
         tsync();
         for (int is = lane; is < nIsl; is += kWarp) {
-            int f = x.s_isl_flags[b0 + is];
-            if (funkey(x.s_isl_sleep[b0 + is]) >= kTimeToSleep && (f & 2)) x.s_isl_flags[b0 + is] = f | 8;
+            int f = iflags[is];
+            if (funkey(x.s_isl_sleep[b0 + is]) >= kTimeToSleep && (f & 2)) iflags[is] = f | 8;
         }
         tsync();
         for (int t = lane; t < nbI; t += kWarp) {
             int i = x.s_isl_body[b0 + t];
-            if (x.s_isl_flags[b0 + x.s_body_island[b0 + i]] & 8) b_set_awake(x.bs[b0 + i], false);
+            if (iflags[x.s_body_island[b0 + i]] & 8) b_set_awake(x.bs[b0 + i], false);
         }
         // a static body ends in the state its last island left it in
         for (int i = lane; i < nb; i += kWarp) {
             if ((bfl[i] & kBfStatic) && x.s_body_island[b0 + i] >= 0 &&
-                (x.s_isl_flags[b0 + x.s_body_island[b0 + i]] & 8))
+                (iflags[x.s_body_island[b0 + i]] & 8))
                 b_set_awake(x.bs[b0 + i], false);
         }
     }
@@ -2082,10 +2158,10 @@ __global__ void __launch_bounds__(kSolveWarps * 32, 3) k_solve_toi(Ctx x) {
     if (w < 0) return;
     const int soff = x.solve_smem[slot];
     float* sbp = soff >= 0 ? smem_sb + soff : x.s_sbody + 6 * (size_t)x.wi[w].body_start;
-    float* stage_f = smem_sb + (threadIdx.x >> 5) * kStageFloats;
+    float* stage_f = smem_sb + (threadIdx.x >> 5) * kWarpSmemFloats;
     unsigned long long g0 = 0;
     if (x.prof) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(g0));
-    solve_world(x, w, sbp, stage_f);
+    solve_world(x, w, sbp, soff >= 0, stage_f);
     tsync();
     toi_world(x, w, sbp);
     if (x.prof && lane_id() == 0) {

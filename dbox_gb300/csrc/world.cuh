@@ -130,7 +130,8 @@ struct SweepSnap { Sweep a, b; float alpha0; int pad; };
 
 constexpr int kProfSlots = 32;         // per-world slots of the optional phase profile
 constexpr int kSolveWarps = 4;          // warp slots (worlds) per block of the solve kernel
-constexpr int kStageFloats = 2 * 32 * 36; // per warp: two levels of 32 staged 144-byte rows
+constexpr int kStageFloats = 2 * 32 * 36; // per warp: row ring of two 4608-byte halves
+constexpr int kWarpSmemFloats = kStageFloats + 4;   // + the ring's two mbarriers
 
 struct Ctx {
     int W;
