@@ -70,6 +70,23 @@ def lib():
     L.dbox_world_get_transforms.argtypes = [vp, vp]
     L.dbox_body_def_default.argtypes = [vp]
     L.dbox_fixture_def_default.argtypes = [vp]
+    u64 = ctypes.c_uint64
+    L.dbox_mlp_create.argtypes = [ctypes.POINTER(vp)]
+    L.dbox_mlp_destroy.argtypes = [vp]
+    L.dbox_mlp_init.argtypes = [vp, u64]
+    L.dbox_mlp_set_params.argtypes = [vp, vp, vp]
+    L.dbox_mlp_get_params.argtypes = [vp, vp, vp]
+    L.dbox_mlp_fit_normalization.argtypes = [vp, i32, vp, vp]
+    L.dbox_mlp_gradient.argtypes = [vp, i32, vp, vp, vp, vp]
+    L.dbox_mlp_train.argtypes = [vp, i32, vp, vp, i32, i32, f32, u64, vp]
+    L.dbox_mlp_train_world.argtypes = [vp, vp, i32, i32, f32, u64, vp]
+    L.dbox_mlp_forward.argtypes = [vp, i32, vp, vp]
+    L.dbox_world_set_warmstart.argtypes = [vp, i32, vp, i32]
+    L.dbox_world_sample_count.argtypes = [vp, ctypes.POINTER(i32)]
+    L.dbox_world_get_samples.argtypes = [vp, i32, i32, vp]
+    L.dbox_world_clear_samples.argtypes = [vp]
+    L.dbox_world_set_measure.argtypes = [vp, i32]
+    L.dbox_world_get_quality.argtypes = [vp, vp]
     _lib = L
     return L
 
@@ -103,6 +120,79 @@ def collide_manifolds_noalloc(shapes_a, xfs_a, shapes_b, xfs_b):
     _check(lib().dbox_collide_manifolds_noalloc(len(sa), abi.ptr(sa), abi.ptr(xa), abi.ptr(sb), abi.ptr(xb),
                                                 abi.ptr(out)), "dbox_collide_manifolds_noalloc")
     return out
+
+
+MLP_PARAMS, MLP_NORM, MLP_SAMPLE, MLP_FEAT = 21768, 72, 36, 32
+
+
+class Mlp:
+    """The learned warm-start network (dbox_mlp_*): 32 -> 128 -> 128 -> 4, GELU, BF16 on the
+    tensor cores with FP32 accumulation.  Parameters are one flat FP32 vector (layout in
+    dbox_gpu.h); norm holds feature mean/std (32 + 32) and target mean/std (4 + 4)."""
+
+    def __init__(self, seed=None):
+        h = ctypes.c_void_p()
+        _check(lib().dbox_mlp_create(ctypes.byref(h)), "dbox_mlp_create")
+        self.h = h
+        if seed is not None:
+            _check(lib().dbox_mlp_init(self.h, ctypes.c_uint64(seed)), "dbox_mlp_init")
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            lib().dbox_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_params(self, params=None, norm=None):
+        p = None if params is None else np.ascontiguousarray(params, np.float32)
+        q = None if norm is None else np.ascontiguousarray(norm, np.float32)
+        _check(lib().dbox_mlp_set_params(self.h, abi.ptr(p) if p is not None else None,
+                                         abi.ptr(q) if q is not None else None), "dbox_mlp_set_params")
+
+    def params(self):
+        p = np.zeros(MLP_PARAMS, np.float32)
+        q = np.zeros(MLP_NORM, np.float32)
+        _check(lib().dbox_mlp_get_params(self.h, abi.ptr(p), abi.ptr(q)), "dbox_mlp_get_params")
+        return p, q
+
+    def fit_normalization(self, feats, targets):
+        f = np.ascontiguousarray(feats, np.float32)
+        t = np.ascontiguousarray(targets, np.float32)
+        _check(lib().dbox_mlp_fit_normalization(self.h, len(f), abi.ptr(f), abi.ptr(t)), "fit_normalization")
+
+    def gradient(self, feats, targets):
+        f = np.ascontiguousarray(feats, np.float32)
+        t = np.ascontiguousarray(targets, np.float32)
+        g = np.zeros(MLP_PARAMS, np.float32)
+        loss = np.zeros(1, np.float32)
+        _check(lib().dbox_mlp_gradient(self.h, len(f), abi.ptr(f), abi.ptr(t), abi.ptr(g), abi.ptr(loss)),
+               "dbox_mlp_gradient")
+        return g, float(loss[0])
+
+    def train(self, feats, targets, epochs=1, batch=65536, lr=1e-3, seed=0):
+        f = np.ascontiguousarray(feats, np.float32)
+        t = np.ascontiguousarray(targets, np.float32)
+        losses = np.zeros(epochs, np.float32)
+        _check(lib().dbox_mlp_train(self.h, len(f), abi.ptr(f), abi.ptr(t), epochs, batch, ctypes.c_float(lr),
+                                    ctypes.c_uint64(seed), abi.ptr(losses)), "dbox_mlp_train")
+        return losses
+
+    def train_world(self, world, epochs=1, batch=65536, lr=1e-3, seed=0):
+        losses = np.zeros(epochs, np.float32)
+        _check(lib().dbox_mlp_train_world(self.h, world.h, epochs, batch, ctypes.c_float(lr), ctypes.c_uint64(seed),
+                                          abi.ptr(losses)), "dbox_mlp_train_world")
+        return losses
+
+    def forward(self, feats):
+        f = np.ascontiguousarray(feats, np.float32)
+        out = np.zeros((len(f), 4), np.float32)
+        _check(lib().dbox_mlp_forward(self.h, len(f), abi.ptr(f), abi.ptr(out)), "dbox_mlp_forward")
+        return out
 
 
 class World:
@@ -169,6 +259,37 @@ class World:
         _check(lib().dbox_world_get_counters(self.h, abi.ptr(c)), "dbox_world_get_counters")
         keys = ("isl_bodies", "isl_contacts", "vsolve", "psolve", "contacts", "toi_events", "world_steps", "pairs")
         return dict(zip(keys, (int(v) for v in c)))
+
+    def set_warmstart(self, mode, model=None, sample_capacity=0):
+        """0 plain (the reference step), 1 plain + log training samples, 2 learned start with model."""
+        self._model = model                     # the library keeps a pointer: hold a reference
+        _check(lib().dbox_world_set_warmstart(self.h, mode, model.h if model is not None else None, sample_capacity),
+               "dbox_world_set_warmstart")
+
+    def sample_count(self):
+        n = ctypes.c_int32()
+        _check(lib().dbox_world_sample_count(self.h, ctypes.byref(n)), "dbox_world_sample_count")
+        return n.value
+
+    def samples(self, offset=0, n=None):
+        """(features (n, 32), targets (n, 4)) of the logged samples."""
+        if n is None:
+            n = self.sample_count() - offset
+        rows = np.zeros((n, MLP_SAMPLE), np.float32)
+        _check(lib().dbox_world_get_samples(self.h, offset, n, abi.ptr(rows)), "dbox_world_get_samples")
+        return rows[:, :MLP_FEAT].copy(), rows[:, MLP_FEAT:].copy()
+
+    def clear_samples(self):
+        _check(lib().dbox_world_clear_samples(self.h), "dbox_world_clear_samples")
+
+    def set_measure(self, on=True):
+        _check(lib().dbox_world_set_measure(self.h, 1 if on else 0), "dbox_world_set_measure")
+
+    def quality(self):
+        """(n_worlds, 4): sum of |dlambda|^2, max |dlambda|, points, min separation of the last step."""
+        out = np.zeros((self.n_worlds, 4), np.float32)
+        _check(lib().dbox_world_get_quality(self.h, abi.ptr(out)), "dbox_world_get_quality")
+        return out
 
     def set_phase_profile(self, on=True):
         _check(lib().dbox_world_set_phase_profile(self.h, 1 if on else 0), "set_phase_profile")

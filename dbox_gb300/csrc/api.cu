@@ -20,6 +20,7 @@
 
 extern "C" int dbox_launch_step(const dg::Ctx* x, cudaStream_t stream, int* launches);
 extern "C" const void* dbox_solve_kernel();
+const dg::MlpDev* dbox_mlp_device_view(const dbox_mlp* m, dg::MlpDev* out);
 extern "C" int dbox_launch_step_ev(const dg::Ctx* x, cudaStream_t stream, int* launches, cudaEvent_t* ev);
 extern "C" int dbox_launch_gather_transforms(int n, const dbox_body_state* bs, float* out, cudaStream_t s);
 extern "C" int dbox_launch_apply_forces(int n, dbox_body_state* bs, const float* f, cudaStream_t s);
@@ -39,6 +40,13 @@ int fail(int code, const char* fmt, ...) {
     g_last_error = buf;
     return code;
 }
+
+}  // namespace
+
+// error text for the other translation units of the library (not part of the public header)
+extern "C" int dbox_set_error(int code, const char* msg) { return fail(code, "%s", msg); }
+
+namespace {
 
 #define CU(call)                                                                          \
     do {                                                                                  \
@@ -110,6 +118,14 @@ struct dbox_world {
     DBuf<float> s_sbody;
     DBuf<unsigned long long> d_prof;
     int profiling = 0;
+    // learned warm start and solver-quality measurement
+    int ws_mode = 0;
+    dbox_mlp* mlp = nullptr;
+    int sample_cap = 0;
+    DBuf<float> d_samples, s_feat, s_vsave;
+    DBuf<unsigned> d_sample_count;
+    DBuf<int> s_slog, s_pend;
+    int measure = 0;
     std::vector<dg::WorldInfo> wi;
     int total_bodies = 0, total_fixtures = 0, total_contacts = 0, total_joints = 0;
     // graph replay
@@ -146,12 +162,31 @@ void free_device(dbox_world* w) {
     w->s_isl_minsep.free(); w->s_isl_sleep.free();
     w->d_vr.free(); w->d_tvr.free(); w->d_pr.free(); w->d_tpr.free(); w->d_snap.free(); w->d_io.free();
     w->s_vpos.free(); w->d_solve_world.free(); w->d_solve_smem.free();
+    w->s_feat.free(); w->s_vsave.free(); w->s_slog.free(); w->s_pend.free();
     w->s_cbody.free(); w->s_adj_items.free(); w->s_isl_pair.free(); w->s_cq.free(); w->s_cvis.free(); w->s_bfl.free(); w->s_sbody.free(); w->d_prof.free();
     if (w->graph) { cudaGraphExecDestroy(w->graph); w->graph = nullptr; }
     if (w->tgraph) { cudaGraphExecDestroy(w->tgraph); w->tgraph = nullptr; }
 }
 
 int next_pow2(int v) { int p = 1; while (p < v) p <<= 1; return p; }
+
+// scratch of the learned warm start (features and pending lists per contact slot, sample
+// slots per velocity row) and of the measure mode (saved velocities per body), only while
+// those modes are on
+int alloc_mode_scratch(dbox_world* w) {
+    if (w->wi.empty()) return DBOX_OK;
+    size_t nc = (size_t)w->total_contacts, nb = (size_t)w->total_bodies, nkx = 0;
+    for (const auto& wi : w->wi) nkx = std::max(nkx, (size_t)wi.kx_start + wi.contact_cap + wi.joint_count + 2);
+    bool ok = true;
+    if (w->ws_mode) {
+        if (!w->s_slog.p) ok &= w->s_slog.alloc(nkx) == 0;
+        if (!w->s_feat.p) ok &= w->s_feat.alloc((size_t)dg::kFeat * nc) == 0;
+        if (!w->s_pend.p) ok &= w->s_pend.alloc(nc) == 0;
+    }
+    if (w->measure && !w->s_vsave.p) ok &= w->s_vsave.alloc(3 * nb) == 0;
+    if (!ok) return fail(DBOX_ERR_CUDA, "device allocation failed (warm-start / measure scratch)");
+    return DBOX_OK;
+}
 
 // Warp slots of the solve kernel (four per block).  Each world's solver body rows and
 // island words (32 bytes a body) go to shared memory when they fit the block's budget; worlds are
@@ -392,6 +427,7 @@ int upload(dbox_world* w) {
     ok &= w->d_prof.alloc((size_t)dg::kProfSlots * W) == 0;
     if (!ok) { free_device(w); return fail(DBOX_ERR_CUDA, "device allocation failed (%d bodies, %d contact slots)", nb, nc); }
     if (pack_solve_slots(w) != DBOX_OK) { free_device(w); return DBOX_ERR_CUDA; }
+    if (alloc_mode_scratch(w) != DBOX_OK) { free_device(w); return DBOX_ERR_CUDA; }
     CU(cudaMemcpy(w->d_wi.p, w->wi.data(), sizeof(dg::WorldInfo) * W, cudaMemcpyHostToDevice));
     CU(cudaMemcpy(w->d_wd.p, wd.data(), sizeof(dg::WorldDyn) * W, cudaMemcpyHostToDevice));
     if (nb) {
@@ -505,6 +541,16 @@ dg::Ctx make_ctx(dbox_world* w, float dt, int vi, int pi) {
     x.record_events = w->listener ? 1 : 0;
     x.g_status = w->g_status.p;
     x.prof = w->profiling ? w->d_prof.p : nullptr;
+    x.ws_mode = w->ws_mode;
+    if (w->ws_mode == 2 && w->mlp) dbox_mlp_device_view(w->mlp, &x.mlp);
+    x.samples = w->d_samples.p;
+    x.sample_count = w->d_sample_count.p;
+    x.sample_cap = w->sample_cap;
+    x.s_slog = w->s_slog.p;
+    x.s_feat = w->s_feat.p;
+    x.s_pend = w->s_pend.p;
+    x.measure = w->measure;
+    x.s_vsave = w->s_vsave.p;
     return x;
 }
 
@@ -1020,6 +1066,94 @@ int32_t dbox_world_get_transforms(dbox_world* w, float* xya) {
     if (err) return fail(DBOX_ERR_CUDA, "gather launch: %s", cudaGetErrorString((cudaError_t)err));
     CU(cudaMemcpyAsync(xya, w->d_io.p, sizeof(float) * 3 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
     CU(cudaStreamSynchronize(w->stream));
+    return DBOX_OK;
+}
+
+int32_t dbox_world_set_warmstart(dbox_world* w, int32_t mode, dbox_mlp* model, int32_t sample_capacity) {
+    if (!w || mode < 0 || mode > 2) return fail(DBOX_ERR_INVALID, "dbox_world_set_warmstart: bad mode");
+    if (mode == 2 && !model) return fail(DBOX_ERR_INVALID, "dbox_world_set_warmstart: learned mode needs a model");
+    if (mode == 1 && sample_capacity <= 0) return fail(DBOX_ERR_INVALID, "dbox_world_set_warmstart: sample capacity must be > 0");
+    w->ws_mode = mode;
+    w->mlp = mode == 2 ? model : nullptr;
+    if (mode == 1 && sample_capacity != w->sample_cap) {
+        w->d_samples.free();
+        w->d_sample_count.free();
+        if (w->d_samples.alloc((size_t)dg::kSampleFloats * sample_capacity) || w->d_sample_count.alloc(1))
+            return fail(DBOX_ERR_CUDA, "device allocation failed (%d samples)", sample_capacity);
+        w->sample_cap = sample_capacity;
+        CU(cudaMemset(w->d_sample_count.p, 0, sizeof(unsigned)));
+    }
+    if (w->on_device) {
+        int rc = alloc_mode_scratch(w);
+        if (rc) return rc;
+    }
+    if (w->graph) { cudaGraphExecDestroy(w->graph); w->graph = nullptr; }
+    if (w->tgraph) { cudaGraphExecDestroy(w->tgraph); w->tgraph = nullptr; }
+    return DBOX_OK;
+}
+
+int32_t dbox_world_sample_count(dbox_world* w, int32_t* count) {
+    if (!w || !count) return fail(DBOX_ERR_INVALID, "dbox_world_sample_count: null argument");
+    unsigned c = 0;
+    if (w->d_sample_count.p) {
+        CU(cudaStreamSynchronize(w->stream));
+        CU(cudaMemcpy(&c, w->d_sample_count.p, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    }
+    *count = (int32_t)std::min<unsigned>(c, (unsigned)w->sample_cap);
+    return DBOX_OK;
+}
+
+int32_t dbox_world_get_samples(dbox_world* w, int32_t offset, int32_t n, float* rows) {
+    if (!w || !rows || offset < 0 || n < 0 || offset + n > w->sample_cap)
+        return fail(DBOX_ERR_INVALID, "dbox_world_get_samples: bad range");
+    if (n == 0) return DBOX_OK;
+    CU(cudaStreamSynchronize(w->stream));
+    CU(cudaMemcpy(rows, w->d_samples.p + (size_t)dg::kSampleFloats * offset, sizeof(float) * dg::kSampleFloats * n,
+                  cudaMemcpyDeviceToHost));
+    return DBOX_OK;
+}
+
+int32_t dbox_world_clear_samples(dbox_world* w) {
+    if (!w) return DBOX_ERR_INVALID;
+    if (w->d_sample_count.p) CU(cudaMemsetAsync(w->d_sample_count.p, 0, sizeof(unsigned), w->stream));
+    return DBOX_OK;
+}
+
+int32_t dbox_mlp_train_world(dbox_mlp* m, dbox_world* w, int32_t epochs, int32_t batch, float lr, uint64_t seed,
+                             float* epoch_loss) {
+    if (!m || !w) return fail(DBOX_ERR_INVALID, "dbox_mlp_train_world: null argument");
+    int32_t n = 0;
+    int rc = dbox_world_sample_count(w, &n);
+    if (rc) return rc;
+    if (n <= 0) return fail(DBOX_ERR_INVALID, "dbox_mlp_train_world: the world holds no samples");
+    return dbox_mlp_train_device(m, n, w->d_samples.p, epochs, batch, lr, seed, epoch_loss);
+}
+
+int32_t dbox_world_set_measure(dbox_world* w, int32_t enable) {
+    if (!w) return DBOX_ERR_INVALID;
+    w->measure = enable ? 1 : 0;
+    if (w->on_device) {
+        int rc = alloc_mode_scratch(w);
+        if (rc) return rc;
+    }
+    if (w->graph) { cudaGraphExecDestroy(w->graph); w->graph = nullptr; }
+    if (w->tgraph) { cudaGraphExecDestroy(w->tgraph); w->tgraph = nullptr; }
+    return DBOX_OK;
+}
+
+int32_t dbox_world_get_quality(dbox_world* w, float* out) {
+    if (!w || !out) return fail(DBOX_ERR_INVALID, "dbox_world_get_quality: null argument");
+    if (!w->on_device) return fail(DBOX_ERR_INVALID, "dbox_world_get_quality: no step taken");
+    size_t W = w->worlds.size();
+    std::vector<dg::WorldDyn> wd(W);
+    CU(cudaStreamSynchronize(w->stream));
+    CU(cudaMemcpy(wd.data(), w->d_wd.p, sizeof(dg::WorldDyn) * W, cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < W; ++i) {
+        out[4 * i] = wd[i].q_sumsq;
+        out[4 * i + 1] = wd[i].q_max;
+        out[4 * i + 2] = (float)wd[i].q_points;
+        out[4 * i + 3] = wd[i].q_minsep;
+    }
     return DBOX_OK;
 }
 

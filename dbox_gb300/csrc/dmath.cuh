@@ -48,7 +48,10 @@ enum { kShapeCircle = 0, kShapePolygon = 2 };
 enum { kBodyIsland = 0x1, kBodyAwake = 0x2, kBodyAutoSleep = 0x4, kBodyBullet = 0x8, kBodyFixedRotation = 0x10,
        kBodyActive = 0x20 };
 enum { kContactIsland = 0x1, kContactTouching = 0x2, kContactEnabled = 0x4, kContactFilter = 0x8,
-       kContactBulletHit = 0x10, kContactToi = 0x20 };
+       kContactBulletHit = 0x10, kContactToi = 0x20,
+       // learned warm start only (never set in the plain method): manifold point 0 / 1 had no
+       // feature-id match in the last update, so its impulse started from zero
+       kContactNew0 = 0x40, kContactNew1 = 0x80 };
 enum { kManifoldCircles = 0, kManifoldFaceA = 1, kManifoldFaceB = 2 };
 
 // ------------------------------------------------------------ vector algebra (common/b2math.d)

@@ -117,13 +117,17 @@ DG bool contact_update(const Ctx& x, dbox_contact_state& c) {
     } else {
         evaluate_manifold(m, fa, xfA, fb, xfB);
         touching = m.pointCount > 0;
+        unsigned fresh = 0;
         for (int i = 0; i < m.pointCount; ++i) {
             m.ni[i] = 0.0f;
             m.ti[i] = 0.0f;
+            bool matched = false;
             for (int j = 0; j < old.pointCount; ++j) {
-                if (old.id[j] == m.id[i]) { m.ni[i] = old.ni[j]; m.ti[i] = old.ti[j]; break; }
+                if (old.id[j] == m.id[i]) { m.ni[i] = old.ni[j]; m.ti[i] = old.ti[j]; matched = true; break; }
             }
+            if (!matched) fresh |= i == 0 ? (unsigned)kContactNew0 : (unsigned)kContactNew1;
         }
+        if (x.ws_mode) c.flags = (c.flags & ~(uint32_t)(kContactNew0 | kContactNew1)) | fresh;
         changed = touching != wasTouching;
     }
     if (touching) c.flags |= kContactTouching; else c.flags &= ~(uint32_t)kContactTouching;
@@ -504,7 +508,7 @@ DG void constraint_ctor(const Ctx& x, int ci, int b0, bool warm, float dtRatio, 
 }
 
 // InitializeVelocityConstraints (:338-450) for one contact
-DG void constraint_init_velocity(VC& vc, const PC& pc, SB sb) {
+DG void constraint_init_velocity(VC& vc, const PC& pc, SB sb, float* sep = nullptr) {
     int pointCount = vc.pointCount;
     float mA = vc.invMassA, mB = vc.invMassB, iA = vc.invIA, iB = vc.invIB;
     float2 cA = sb.c(vc.bodyA), cB = sb.c(vc.bodyB);
@@ -532,6 +536,7 @@ DG void constraint_init_velocity(VC& vc, const PC& pc, SB sb) {
             float2 ccA = pointA + radiusA * normal;
             float2 ccB = pointB - radiusB * normal;
             points[0] = 0.5f * (ccA + ccB);
+            if (sep) sep[0] = dot(ccB - ccA, normal);
         } else if (pc.type == kManifoldFaceA) {
             normal = mul(xfA.q, pc.localNormal);
             float2 planePoint = mul(xfA, pc.localPoint);
@@ -542,6 +547,7 @@ DG void constraint_init_velocity(VC& vc, const PC& pc, SB sb) {
                     float2 ccA = clipPoint + (radiusA - dot(clipPoint - planePoint, normal)) * normal;
                     float2 ccB = clipPoint - radiusB * normal;
                     points[i] = 0.5f * (ccA + ccB);
+                    if (sep) sep[i] = dot(ccB - ccA, normal);
                 }
             }
         } else {
@@ -554,6 +560,7 @@ DG void constraint_init_velocity(VC& vc, const PC& pc, SB sb) {
                     float2 ccB = clipPoint + (radiusB - dot(clipPoint - planePoint, normal)) * normal;
                     float2 ccA = clipPoint - radiusA * normal;
                     points[i] = 0.5f * (ccA + ccB);
+                    if (sep) sep[i] = dot(ccA - ccB, normal);
                 }
             }
             normal = -normal;
@@ -705,11 +712,52 @@ DG void solve_velocity(VC& vc, SB sb) {                                // :492-7
     sb.set_v(vc.bodyB, vB, wB);
 }
 
+// ---- learned warm start: the 32 input features of a contact (after
+// InitializeVelocityConstraints, before the warm start), in this order: normal (2); per point
+// (0 then 1, zeros when absent): rA (2), rB (2), relative normal and tangent velocity, normal
+// mass, tangent mass, velocity bias; inverse masses and inertias (4); friction, restitution,
+// point count, separation of each point (2), gravity along the normal times dt, wA, wB.
+DG void contact_features(const VC& vc, const float sep[2], int pointCount, SB sb, float2 gravity, float h, float* f) {
+    float2 n = vc.normal, t = cross(n, 1.0f);
+    float2 vA = sb.v(vc.bodyA), vB = sb.v(vc.bodyB);
+    float wA = sb.w(vc.bodyA), wB = sb.w(vc.bodyB);
+    f[0] = n.x;
+    f[1] = n.y;
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        float* q = f + 2 + 9 * j;
+        const VPoint& p = vc.p[j];
+        bool on = j < pointCount;
+        float2 dv = ((vB + cross(wB, p.rB)) - vA) - cross(wA, p.rA);
+        q[0] = on ? p.rA.x : 0.0f;
+        q[1] = on ? p.rA.y : 0.0f;
+        q[2] = on ? p.rB.x : 0.0f;
+        q[3] = on ? p.rB.y : 0.0f;
+        q[4] = on ? dot(dv, n) : 0.0f;
+        q[5] = on ? dot(dv, t) : 0.0f;
+        q[6] = on ? p.normalMass : 0.0f;
+        q[7] = on ? p.tangentMass : 0.0f;
+        q[8] = on ? p.velocityBias : 0.0f;
+    }
+    f[20] = vc.invMassA;
+    f[21] = vc.invIA;
+    f[22] = vc.invMassB;
+    f[23] = vc.invIB;
+    f[24] = vc.friction;
+    f[25] = vc.restitution;
+    f[26] = (float)pointCount;
+    f[27] = pointCount > 0 ? sep[0] : 0.0f;
+    f[28] = pointCount > 1 ? sep[1] : 0.0f;
+    f[29] = dot(gravity, n) * h;
+    f[30] = wA;
+    f[31] = wB;
+}
+
 DG void store_impulses(const Ctx& x, const VRow& r) {                 // :774-787
     dbox_contact_state& c = x.ct[r.ids.w];
     c.points[0].normal_impulse = r.imp.x;
     c.points[0].tangent_impulse = r.imp.y;
-    if (r.ids.z > 1) {
+    if ((r.ids.z & 0xff) > 1) {
         c.points[1].normal_impulse = r.imp.z;
         c.points[1].tangent_impulse = r.imp.w;
     }
@@ -751,7 +799,7 @@ DG VC unpack_v(const VRow& r) {
     vc.tangentSpeed = r.NM.w;
     vc.restitution = 0.0f;                       // only read while the row is built
     vc.invMassA = r.inv.x; vc.invIA = r.inv.y; vc.invMassB = r.inv.z; vc.invIB = r.inv.w;
-    vc.bodyA = r.ids.x; vc.bodyB = r.ids.y; vc.pointCount = r.ids.z;
+    vc.bodyA = r.ids.x; vc.bodyB = r.ids.y; vc.pointCount = r.ids.z & 0xff;
     return vc;
 }
 DG PRow pack_p(const PC& pc, int island) {
@@ -1185,6 +1233,85 @@ DG unsigned char body_flag_byte(const dbox_body_state& b) {
     return f;
 }
 
+// Learned start, first velocity iteration (b2contactsolver.d:492-772 run twice): the contact
+// is solved from its predicted start and from the zero start of its new points (the
+// prediction's warm-start impulse taken back out of the two bodies), each on a private copy
+// of the two bodies' velocities; the start whose first correction |dlambda| is smaller
+// wins (the prediction on ties) and its velocities and impulses are kept.
+__device__ __noinline__ void solve_velocity_learned(const VRow& r, SB sb, float4* imp) {
+    VC vp = unpack_v(r);
+    const int ids = r.ids.z;
+    VC vz = vp;
+    float2 vA = sb.v(vp.bodyA), vB = sb.v(vp.bodyB);
+    float wA = sb.w(vp.bodyA), wB = sb.w(vp.bodyB);
+    float2 vA0 = vA, vB0 = vB;
+    float wA0 = wA, wB0 = wB;
+    float2 n = vp.normal, t = cross(n, 1.0f);
+    for (int j = 0; j < 2; ++j) {
+        if (!(ids & (0x200 << j)) || j >= vp.pointCount) continue;
+        float2 P = vp.p[j].normalImpulse * n + vp.p[j].tangentImpulse * t;
+        vA0 += vp.invMassA * P;
+        wA0 += vp.invIA * cross(vp.p[j].rA, P);
+        vB0 -= vp.invMassB * P;
+        wB0 -= vp.invIB * cross(vp.p[j].rB, P);
+        vz.p[j].normalImpulse = 0.0f;
+        vz.p[j].tangentImpulse = 0.0f;
+    }
+    float la[12] = {vA.x, vA.y, wA, 0.0f, 0.0f, 0.0f, vB.x, vB.y, wB, 0.0f, 0.0f, 0.0f};
+    float lz[12] = {vA0.x, vA0.y, wA0, 0.0f, 0.0f, 0.0f, vB0.x, vB0.y, wB0, 0.0f, 0.0f, 0.0f};
+    SB sa, sz;
+    sa.p = la;
+    sz.p = lz;
+    VC pa = vp, pz = vz;
+    pa.bodyA = 0; pa.bodyB = 1;
+    pz.bodyA = 0; pz.bodyB = 1;
+    solve_velocity(pa, sa);
+    solve_velocity(pz, sz);
+    float ra = 0.0f, rz = 0.0f;
+    for (int j = 0; j < vp.pointCount; ++j) {
+        float dn = pa.p[j].normalImpulse - vp.p[j].normalImpulse, dt = pa.p[j].tangentImpulse - vp.p[j].tangentImpulse;
+        ra += dn * dn + dt * dt;
+        dn = pz.p[j].normalImpulse - vz.p[j].normalImpulse;
+        dt = pz.p[j].tangentImpulse - vz.p[j].tangentImpulse;
+        rz += dn * dn + dt * dt;
+    }
+    const bool zero = rz < ra;
+    const float* st = zero ? lz : la;
+    const VC& ch = zero ? pz : pa;
+    sb.set_v(vp.bodyA, v2(st[0], st[1]), st[2]);
+    sb.set_v(vp.bodyB, v2(st[6], st[7]), st[8]);
+    *imp = make_float4(ch.p[0].normalImpulse, ch.p[0].tangentImpulse, ch.p[1].normalImpulse, ch.p[1].tangentImpulse);
+}
+
+// deepest separation over the points of a contact at the current positions
+// (b2PositionSolverManifold, b2contactsolver.d:816-851); 0 when none is below 0
+DG float position_min_separation(const PC& pc, SB sb) {
+    float2 cA = sb.c(pc.bodyA), cB = sb.c(pc.bodyB);
+    Xf xfA, xfB;
+    xfA.q = rot(sb.a(pc.bodyA));
+    xfB.q = rot(sb.a(pc.bodyB));
+    xfA.p = cA - mul(xfA.q, pc.lcA);
+    xfB.p = cB - mul(xfB.q, pc.lcB);
+    float minSep = 0.0f;
+    for (int j = 0; j < pc.pointCount; ++j) {
+        float separation;
+        if (pc.type == kManifoldCircles) {
+            float2 pointA = mul(xfA, pc.localPoint), pointB = mul(xfB, pc.localPoints[0]);
+            float2 normal = pointB - pointA;
+            normalize(normal);
+            separation = (dot(pointB - pointA, normal) - pc.radiusA) - pc.radiusB;
+        } else {
+            bool faceA = pc.type == kManifoldFaceA;
+            Xf xfN = faceA ? xfA : xfB, xfC = faceA ? xfB : xfA;
+            float2 normal = mul(xfN.q, pc.localNormal);
+            float2 planePoint = mul(xfN, pc.localPoint), clipPoint = mul(xfC, pc.localPoints[j]);
+            separation = (dot(clipPoint - planePoint, normal) - pc.radiusA) - pc.radiusB;
+        }
+        minSep = bmin(minSep, separation);
+    }
+    return minSep;
+}
+
 // Level offsets of a schedule (lvl[0 .. last]) held in registers: lane k of q0 / q1 / q2
 // has lvl[32 * (blk + j) + k].  The level being solved and the levels read ahead of it
 // are at most one block apart, so each offset is one shuffle away, and the block after
@@ -1236,11 +1363,10 @@ DG void fence_async_global() { asm volatile("fence.proxy.async.global;" ::: "mem
 // arm `bar` for `bytes` and copy them global -> shared; completes the barrier's phase
 DG void bulk_copy(unsigned long long* bar, void* dst, const void* src, unsigned bytes) {
     unsigned b = smem_u32(bar);
-    unsigned long long state;
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 %0, [%1], %2;" : "=l"(state) : "r"(b), "r"(bytes) : "memory");
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}"
+                 :: "r"(b), "r"(bytes) : "memory");
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
                  :: "r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(b) : "memory");
-    (void)state;
 }
 constexpr int kMbarSpinLimit = 1 << 20;
 // wait for the phase of `bar` with the given parity; false when the spin limit ran out
@@ -1353,6 +1479,7 @@ DG void solve_world(const Ctx& x, int w, float* sbp, bool sb_smem, float* stage_
     const bool warm = x.warm_starting != 0;
     const float dtRatio = wd.inv_dt0 * x.dt;                            // b2world.d:392
     stamp(x, w, 0);
+    if (x.measure && lane == 0) { wd.q_sumsq = 0.0f; wd.q_max = 0.0f; wd.q_points = 0; wd.q_minsep = 0.0f; }
     SB sb;
     sb.p = sbp;
     // per-island flags and minimum separations of the position iterations: after the
@@ -1576,34 +1703,123 @@ DG void solve_world(const Ctx& x, int w, float* sbp, bool sb_smem, float* stage_
     const int nItems = ncI + njI;
     VRow* vrow = x.vr + kx;
     PRow* prow = x.pr + kx;
-    for (int idx = lane; idx < nItems; idx += kWarp) {
-        int item = x.s_sched_v[kx + idx];
-        if (item >= 0) {
-            VC vc;
-            PC pc;
-            constraint_ctor(x, item, b0, warm, dtRatio, vc, pc);
-            constraint_init_velocity(vc, pc, sb);
-            vrow[idx] = pack_v(vc, item);
-            if (njI) {
-                x.s_vpos[item] = idx;
+    int npend = 0;                                   // learned start: contacts waiting for a prediction
+    for (int base = 0; base < nItems; base += kWarp) {
+        const int idx = base + lane;
+        bool pend = false;
+        if (idx < nItems) {
+            int item = x.s_sched_v[kx + idx];
+            bool pdone = false;
+            if (item >= 0) {
+                VC vc;
+                PC pc;
+                constraint_ctor(x, item, b0, warm, dtRatio, vc, pc);
+                float sep[2] = {0.0f, 0.0f};
+                constraint_init_velocity(vc, pc, sb, sep);
+                VRow vr = pack_v(vc, item);
+                if (x.ws_mode) {
+                    // points whose impulse started from zero (no feature-id match in Collide)
+                    unsigned fr = x.ct[item].flags & (kContactNew0 | kContactNew1);
+                    if (pc.pointCount < 2) fr &= ~(unsigned)kContactNew1;
+                    if (x.ws_mode == 1) x.s_slog[kx + idx] = -1;
+                    if (fr) {
+                        vr.ids.z |= (fr & kContactNew0 ? 0x200 : 0) | (fr & kContactNew1 ? 0x400 : 0);
+                        float* f = x.ws_mode == 1 ? nullptr : x.s_feat + (size_t)kFeat * item;
+                        if (x.ws_mode == 1) {
+                            unsigned slot = atomicAdd(x.sample_count, 1u);
+                            if ((int)slot < x.sample_cap) {
+                                f = x.samples + (size_t)kSampleFloats * slot;
+                                x.s_slog[kx + idx] = (int)slot;
+                            }
+                        }
+                        if (f) {
+                            float fv[kFeat];
+                            contact_features(vc, sep, pc.pointCount, sb, x.gravity, h, fv);
+#pragma unroll
+                            for (int q = 0; q < kFeat; ++q) f[q] = fv[q];
+                        }
+                        pend = x.ws_mode == 2;
+                    }
+                }
+                vrow[idx] = vr;
+                if (njI) {
+                    x.s_vpos[item] = idx;
+                } else {
+                    // one schedule serves both orders: the position row of this place is this contact's
+                    prow[idx] = pack_p(pc, x.s_body_island[b0 + ((bfl[vc.bodyA] & kBfStatic) ? vc.bodyB : vc.bodyA)]);
+                    pdone = true;
+                }
             } else {
-                // one schedule serves both orders: the position row of this place is this contact's
-                prow[idx] = pack_p(pc, x.s_body_island[b0 + ((bfl[vc.bodyA] & kBfStatic) ? vc.bodyB : vc.bodyA)]);
-                continue;
+                vrow[idx].ids = make_int4(0, 0, 0, item);
+                if (x.ws_mode == 1) x.s_slog[kx + idx] = -1;
             }
-        } else {
-            vrow[idx].ids = make_int4(0, 0, 0, item);
+            if (!pdone) {
+                int pitem = sched_p[kx + idx];
+                int is = item_island(x, pitem, b0);
+                if (pitem >= 0) {
+                    VC vc;
+                    PC pc;
+                    constraint_ctor(x, pitem, b0, warm, dtRatio, vc, pc);
+                    prow[idx] = pack_p(pc, is);
+                } else {
+                    prow[idx].ids = make_int4(0, 0, pitem, is);
+                }
+            }
         }
-        int pitem = sched_p[kx + idx];
-        int is = item_island(x, pitem, b0);
-        if (pitem >= 0) {
-            VC vc;
-            PC pc;
-            constraint_ctor(x, pitem, b0, warm, dtRatio, vc, pc);
-            prow[idx] = pack_p(pc, is);
-        } else {
-            prow[idx].ids = make_int4(0, 0, pitem, is);
+        if (x.ws_mode == 2) {
+            unsigned bal = __ballot_sync(0xffffffffu, pend);
+            if (pend) x.s_pend[c0 + npend + __popc(bal & ((1u << lane) - 1u))] = idx;
+            npend += __popc(bal);
         }
+    }
+    tsync();
+    // learned start: predicted impulses for the new points, 16 contacts per tensor-core pass,
+    // in this warp's staging area (free until the sweeps)
+    for (int p0 = 0; p0 < npend; p0 += 16) {
+        __nv_bfloat16* X = reinterpret_cast<__nv_bfloat16*>(stage_f);
+        __nv_bfloat16* H1 = X + 16 * kFeat;
+        __nv_bfloat16* H2 = H1 + 16 * kHid;
+        for (int e = lane; e < 16 * kFeat; e += kWarp) {
+            int r = e / kFeat, q = e % kFeat;
+            float v = 0.0f;
+            if (p0 + r < npend) {
+                int item = vrow[x.s_pend[c0 + p0 + r]].ids.w;
+                v = (x.s_feat[(size_t)kFeat * item + q] - x.mlp.fmean[q]) / x.mlp.fstd[q];
+            }
+            X[e] = __float2bfloat16_rn(v);
+        }
+        tsync();
+        float y[4];
+        mlp_infer16(x.mlp, X, H1, H2, y, lane);
+        tsync();
+        const int g = lane >> 2, t = lane & 3;
+        if (t < 2) {
+#pragma unroll
+            for (int hrow = 0; hrow < 2; ++hrow) {
+                const int r = g + 8 * hrow;
+                if (p0 + r >= npend) continue;
+                const int idx = x.s_pend[c0 + p0 + r];
+                VRow* vr = vrow + idx;
+                const int ids = vr->ids.z;
+                const int j = t;                              // lane t predicts point t
+                if (!(ids & (0x200 << j)) || j >= (ids & 0xff)) continue;
+                const int c = 2 * t;
+                float ln = y[2 * hrow] * x.mlp.tstd[c] + x.mlp.tmean[c];
+                float lt = y[2 * hrow + 1] * x.mlp.tstd[c + 1] + x.mlp.tmean[c + 1];
+                ln = ln > 0.0f ? ln : 0.0f;                   // a start the solver itself could reach
+                float mf = vr->K.w * ln;
+                lt = lt < -mf ? -mf : (lt > mf ? mf : lt);
+                if (j == 0) { vr->imp.x = ln; vr->imp.y = lt; }
+                else { vr->imp.z = ln; vr->imp.w = lt; }
+            }
+        }
+        if (t == 0) {
+            for (int hrow = 0; hrow < 2; ++hrow) {
+                const int r = g + 8 * hrow;
+                if (p0 + r < npend) atomicOr(&vrow[x.s_pend[c0 + p0 + r]].ids.z, 0x100);
+            }
+        }
+        tsync();
     }
     tsync();
     stamp(x, w, 4);
@@ -1624,6 +1840,12 @@ DG void solve_world(const Ctx& x, int w, float* sbp, bool sb_smem, float* stage_
     for (int it = 0; it < x.vel_iters; ++it) {
         sweep_levels(x.s_lvl_v + kx, maxLv, nItems, vrow, ring, [&](const VRow& r, int idx) {
             if (r.ids.w >= 0) {
+                if (it == 0 && (r.ids.z & 0x100)) {
+                    float4 im;
+                    solve_velocity_learned(r, sb, &im);
+                    vrow[idx].imp = im;
+                    return;
+                }
                 VC vc = unpack_v(r);
                 solve_velocity(vc, sb);
                 vrow[idx].imp = make_float4(vc.p[0].normalImpulse, vc.p[0].tangentImpulse, vc.p[1].normalImpulse,
@@ -1634,9 +1856,57 @@ DG void solve_world(const Ctx& x, int w, float* sbp, bool sb_smem, float* stage_
         });
     }
     stamp(x, w, 6);
+    if (x.measure) {
+        // one extra velocity sweep that changes nothing: the bodies' velocities are kept
+        // aside and put back, impulses are not written, joints are left out
+        for (int t = lane; t < nbI; t += kWarp) {
+            int i = x.s_isl_body[b0 + t];
+            float2 v = sb.v(i);
+            x.s_vsave[3 * (size_t)(b0 + i)] = v.x;
+            x.s_vsave[3 * (size_t)(b0 + i) + 1] = v.y;
+            x.s_vsave[3 * (size_t)(b0 + i) + 2] = sb.w(i);
+        }
+        tsync();
+        float ssq = 0.0f, smax = 0.0f;
+        int npts = 0;
+        sweep_levels(x.s_lvl_v + kx, maxLv, nItems, vrow, ring, [&](const VRow& r, int) {
+            if (r.ids.w < 0) return;
+            VC vc = unpack_v(r);
+            VC before = vc;
+            solve_velocity(vc, sb);
+            for (int j = 0; j < vc.pointCount; ++j) {
+                float dn = vc.p[j].normalImpulse - before.p[j].normalImpulse;
+                float dt = vc.p[j].tangentImpulse - before.p[j].tangentImpulse;
+                float d2 = dn * dn + dt * dt;
+                ssq += d2;
+                smax = bmax(smax, sqrtf(d2));
+                ++npts;
+            }
+        });
+        for (int o = 16; o > 0; o >>= 1) {
+            ssq += __shfl_xor_sync(0xffffffffu, ssq, o);
+            smax = bmax(smax, __shfl_xor_sync(0xffffffffu, smax, o));
+            npts += __shfl_xor_sync(0xffffffffu, npts, o);
+        }
+        if (lane == 0) { wd.q_sumsq = ssq; wd.q_max = smax; wd.q_points = npts; }
+        tsync();
+        for (int t = lane; t < nbI; t += kWarp) {
+            int i = x.s_isl_body[b0 + t];
+            const float* sv = x.s_vsave + 3 * (size_t)(b0 + i);
+            sb.set_v(i, v2(sv[0], sv[1]), sv[2]);
+        }
+        tsync();
+    }
     for (int idx = lane; idx < nItems; idx += kWarp) {
         VRow r = load_v(vrow + idx);
         if (r.ids.w >= 0) store_impulses(x, r);
+        if (x.ws_mode == 1) {
+            int slot = x.s_slog[kx + idx];
+            if (slot >= 0) {
+                float* tg = x.samples + (size_t)kSampleFloats * slot + kFeat;
+                tg[0] = r.imp.x; tg[1] = r.imp.y; tg[2] = r.imp.z; tg[3] = r.imp.w;
+            }
+        }
     }
     // integrate positions (b2island.d:168-200)
     for (int t = lane; t < nbI; t += kWarp) {
@@ -1700,6 +1970,15 @@ DG void solve_world(const Ctx& x, int w, float* sbp, bool sb_smem, float* stage_
     }
     tsync();
     if (!__all_sync(0xffffffffu, ring.ok) && lane == 0) set_error(x, w, DBOX_ERR_TIMEOUT);
+    if (x.measure) {
+        float ms = 0.0f;
+        for (int idx = lane; idx < nItems; idx += kWarp) {
+            PRow r = load_p(prow + idx);
+            if (r.ids.z >= 0) ms = bmin(ms, position_min_separation(unpack_p(r), sb));
+        }
+        for (int o = 16; o > 0; o >>= 1) ms = bmin(ms, __shfl_xor_sync(0xffffffffu, ms, o));
+        if (lane == 0) wd.q_minsep = ms;
+    }
     stamp(x, w, 8);
     // copy back + SynchronizeTransform (b2island.d:227-235)
     for (int t = lane; t < nbI; t += kWarp) {

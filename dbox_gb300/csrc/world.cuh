@@ -12,6 +12,7 @@
 //    edge list are head-inserted (b2contactmanager.d:131-166), so list order is
 //    descending slot index.
 #pragma once
+#include "mlp.cuh"
 
 #include <stdint.h>
 #include "dmath.cuh"
@@ -49,6 +50,13 @@ struct WorldDyn {
     unsigned long long acc_toi_events;
     unsigned long long acc_steps;
     unsigned long long acc_pairs;        // broad-phase pairs emitted
+    // solver quality of the last step (measure mode): one extra non-mutating velocity sweep
+    // after the last iteration gives |lambda_next - lambda| per contact point (normal and
+    // tangent together); the position manifold after the step gives the deepest separation
+    float q_sumsq;                 // sum over points of |dlambda|^2
+    float q_max;                   // max over points of |dlambda|
+    int q_points;                  // points measured
+    float q_minsep;                // minimum separation over points after the step (<= 0)
 };
 
 struct BodyStatic {
@@ -207,6 +215,17 @@ struct Ctx {
     int warm_starting, continuous, sub_stepping, allow_sleep;
     int record_events;
     int* g_status;                 // bit (-code) set for every DBOX_ERR_* raised by any world
+    // learned warm start: 0 plain (Box2D), 1 plain + log training samples, 2 learned start
+    int ws_mode;
+    MlpDev mlp;                    // ws_mode 2: the network
+    float* samples;                // ws_mode 1: kSampleFloats per sample (32 features, 4 targets)
+    unsigned* sample_count;        // ws_mode 1: samples written so far (may exceed sample_cap)
+    int sample_cap;
+    int* s_slog;                   // kx-indexed: sample slot of the velocity row, or -1
+    float* s_feat;                 // contact-slot-indexed: 32 features per pending learned contact
+    int* s_pend;                   // contact-slot-indexed: velocity-schedule positions awaiting a prediction
+    int measure;                   // 1: fill the q_* fields of WorldDyn each step
+    float* s_vsave;                // body-indexed, 3 floats: velocities kept across the measuring sweep
     unsigned long long* prof;      // optional: kProfSlots clock64 figures per world (NULL = off)
 };
 

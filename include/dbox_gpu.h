@@ -306,6 +306,52 @@ int32_t dbox_collide_manifolds(int32_t n, const dbox_shape_def* shape_a, const f
 int32_t dbox_collide_manifolds_noalloc(int32_t n, const dbox_shape_def* shape_a, const float* xf_a,
                                        const dbox_shape_def* shape_b, const float* xf_b, dbox_contact_state* out);
 
+/* ---- Learned warm start (new in this library; dbox has no counterpart) ----
+ * A 32 -> 128 -> 128 -> 4 GELU network (BF16 weights and activations, FP32 accumulation, run
+ * on the tensor cores) predicts the normal and tangent impulses of manifold points that
+ * b2Contact.Update (contacts/b2contact.d:306-324) starts from zero because no feature id
+ * matched.  The plain method (mode 0) is the reference step, bit for bit.  Parameters are
+ * one flat FP32 vector of DBOX_MLP_PARAMS floats: w1[32][128], w2[128][128], w3[128][8]
+ * (columns 4..7 unused), b1[128], b2[128], b3[8]; normalisation is DBOX_MLP_NORM floats:
+ * feature mean[32], std[32], target mean[4], std[4].  Samples are DBOX_MLP_SAMPLE floats:
+ * 32 features (normal; per point rA, rB, relative normal / tangent velocity, normal mass,
+ * tangent mass, velocity bias; inverse masses and inertias; friction, restitution, point
+ * count, separations, gravity along the normal times dt, wA, wB) then the 4 impulses the
+ * plain solver converged to in that step. */
+#define DBOX_MLP_PARAMS 21768
+#define DBOX_MLP_NORM 72
+#define DBOX_MLP_SAMPLE 36
+typedef struct dbox_mlp dbox_mlp;
+int32_t dbox_mlp_create(dbox_mlp** out);
+int32_t dbox_mlp_destroy(dbox_mlp* m);
+int32_t dbox_mlp_init(dbox_mlp* m, uint64_t seed);                       /* uniform fan-in init, zero biases */
+int32_t dbox_mlp_set_params(dbox_mlp* m, const float* params, const float* norm);   /* either may be NULL */
+int32_t dbox_mlp_get_params(dbox_mlp* m, float* params, float* norm);
+int32_t dbox_mlp_fit_normalization(dbox_mlp* m, int32_t n, const float* feats, const float* targets);
+/* loss = mean over samples and outputs of (MLP(x) - t)^2 in normalised units; grad = its gradient */
+int32_t dbox_mlp_gradient(dbox_mlp* m, int32_t n, const float* feats, const float* targets, float* grad, float* loss);
+/* Adam (beta 0.9 / 0.999, eps 1e-8) over shuffled batches; epoch_loss[epochs] (may be NULL) */
+int32_t dbox_mlp_train(dbox_mlp* m, int32_t n, const float* feats, const float* targets, int32_t epochs,
+                       int32_t batch, float lr, uint64_t seed, float* epoch_loss);
+int32_t dbox_mlp_train_device(dbox_mlp* m, int32_t n, const float* device_rows, int32_t epochs, int32_t batch,
+                              float lr, uint64_t seed, float* epoch_loss);
+int32_t dbox_mlp_train_world(dbox_mlp* m, dbox_world* w, int32_t epochs, int32_t batch, float lr, uint64_t seed,
+                             float* epoch_loss);                          /* on the world's logged samples */
+int32_t dbox_mlp_forward(dbox_mlp* m, int32_t n, const float* feats, float* out);   /* out: n x 4 impulses */
+/* mode 0 plain; 1 plain + log up to sample_capacity samples on the device; 2 learned start
+ * with `model` (kept by the caller while the mode is on).  In mode 2 the first velocity
+ * iteration keeps, per contact, the start (predicted or zero) whose first correction is
+ * smaller.  Modes 1 and 2 set contact flags 0x40 / 0x80 (point 0 / 1 new this step). */
+int32_t dbox_world_set_warmstart(dbox_world* w, int32_t mode, dbox_mlp* model, int32_t sample_capacity);
+int32_t dbox_world_sample_count(dbox_world* w, int32_t* count);
+int32_t dbox_world_get_samples(dbox_world* w, int32_t offset, int32_t n, float* rows);  /* n x 36 */
+int32_t dbox_world_clear_samples(dbox_world* w);
+/* Solver quality of each step while enabled: out[4 per world] = sum over contact points of
+ * |lambda_next - lambda|^2 from one extra non-mutating velocity sweep after the last
+ * iteration, its maximum, the number of points, and the minimum separation after the step. */
+int32_t dbox_world_set_measure(dbox_world* w, int32_t enable);
+int32_t dbox_world_get_quality(dbox_world* w, float* out);
+
 /* Device kernels launched by the last step (for launch accounting). */
 int32_t dbox_world_last_launches(dbox_world* w, int32_t* out);
 
