@@ -54,6 +54,9 @@ def parse():
     p.add_argument("--seed", type=int, default=3)
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-learned", action="store_true", help="skip the learned warm-start comparison")
+    p.add_argument("--learned-worlds", type=int, default=1024)
+    p.add_argument("--learned-log-steps", type=int, default=2000)
     return p.parse_args()
 
 
@@ -247,6 +250,12 @@ def gpu_leg(args, rank, world_size):
     solve_ms = phase_ms[1] / args.steps          # the fused solve + SolveTOI kernel
     achieved = solve_bytes / (solve_ms / 1e3) / 1e9
     hbm = peaks.get("hbm_gbs")
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "k_solve_toi_batch4096.md")
+    if args.workload == "batch" and args.worlds == 4096 and os.path.exists(prof):
+        for line in open(prof):
+            if line.startswith("traffic_bytes_per_launch:"):
+                traffic = int(line.split(":")[1])
     out = {
         "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": world_size, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms_max / args.steps, "higher_is_better": True,
@@ -264,7 +273,9 @@ def gpu_leg(args, rank, world_size):
         "roofline": {"bound": "hbm", "kernel": "k_solve_toi", "achieved": achieved,
                      "peak": hbm, "unit": "GB/s", "frac": (achieved / hbm) if hbm else None,
                      "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if hbm else "fallback 6800",
-                     "algorithmic_bytes_per_launch": solve_bytes, "traffic": None},
+                     "algorithmic_bytes_per_launch": solve_bytes, "traffic": traffic,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch of this "
+                                       "workload (profiles/k_solve_toi_batch4096.md)" if traffic else None},
         "clocks": clk,
     }
     if out["roofline"]["peak"] is None:
@@ -272,6 +283,68 @@ def gpu_leg(args, rank, world_size):
         out["roofline"]["frac"] = achieved / 6800.0
     w.close()
     return out
+
+
+def learned_leg(args):
+    """Learned warm start vs the plain solver (the project's learned-start configuration):
+    1,024 scatter worlds of 256 bodies in 40 m containers.  The plain solver logs up to 10M
+    new-contact samples over its first steps; the MLP (32-128-128-4, BF16 tensor cores) is
+    trained with Adam (lr 1e-3, batch 65,536, 20 epochs); then new-seed worlds run plain with
+    8 and 5 velocity iterations and learned with 5 and 4, each from the same warmed-up state:
+    velocity residual (one extra non-mutating sweep per step), deepest penetration and
+    body-steps/s (CUDA graph of the timed steps, measurement off)."""
+    import dbox_gb300
+    from dbox_gb300 import scenes
+    rng = np.random.default_rng(args.seed + 77)
+    train_worlds = [scenes.scatter(256, 40.0, 40.0, rng) for _ in range(args.learned_worlds)]
+    eval_worlds = [scenes.scatter(256, 40.0, 40.0, rng) for _ in range(args.learned_worlds)]
+    nd = sum(scenes.dynamic_body_count(s) for s in eval_worlds)
+    log = dbox_gb300.World(train_worlds)
+    log.set_warmstart(1, None, 10_000_000)
+    t0 = time.perf_counter()
+    log.step(DT, VI, PI, steps=args.learned_log_steps, graph=True)
+    log.sync()
+    t_log = time.perf_counter() - t0
+    n = log.sample_count()
+    f, tg = log.samples(0, min(n, 1_000_000))
+    model = dbox_gb300.Mlp(seed=args.seed)
+    model.fit_normalization(f, tg)
+    t0 = time.perf_counter()
+    losses = model.train_world(log, epochs=20, batch=65536, lr=1e-3, seed=args.seed)
+    t_train = time.perf_counter() - t0
+    log.close()
+    res = {}
+    for label, mode, vi in (("plain_8", 0, 8), ("plain_5", 0, 5), ("learned_5", 2, 5), ("learned_4", 2, 4)):
+        w = dbox_gb300.World(eval_worlds)
+        w.step(DT, VI, PI, steps=100, graph=True)
+        w.set_warmstart(mode, model if mode == 2 else None, 0)
+        w.set_measure(True)
+        rms, mx, pen = [], [], []
+        for _ in range(30):
+            w.step(DT, vi, PI)
+            q = w.quality()
+            rms.append(float(np.sqrt(q[:, 0].sum() / max(q[:, 2].sum(), 1.0))))
+            mx.append(float(q[:, 1].max()))
+            pen.append(float(-q[:, 3].min()))
+        w.set_measure(False)
+        w.step(DT, vi, PI, steps=3, graph=True)
+        tot_ms, _ = w.step_timed(30, DT, vi, PI)
+        res[label] = {"velocity_iterations": vi, "residual_rms": float(np.mean(rms)),
+                      "residual_max": float(np.mean(mx)), "penetration_max_m": float(np.max(pen)),
+                      "body_steps_per_s": nd * 30 / (tot_ms / 1e3)}
+        w.close()
+    p8, l5 = res["plain_8"], res["learned_5"]
+    return {
+        "config": "%d scatter worlds x 256 bodies (40 m containers), dt 1/60, %d position iterations; "
+                  "samples from %d plain steps, evaluation on new-seed worlds after 100 steps, 30 steps"
+                  % (args.learned_worlds, PI, args.learned_log_steps),
+        "samples": n, "log_seconds": t_log, "train_seconds": t_train,
+        "loss_first_epoch": float(losses[0]), "loss_last_epoch": float(losses[-1]),
+        "runs": res,
+        "speedup_learned_5_vs_plain_8": l5["body_steps_per_s"] / p8["body_steps_per_s"],
+        "learned_5_reaches_plain_8_residual": bool(l5["residual_rms"] <= p8["residual_rms"] and
+                                                   l5["residual_max"] <= p8["residual_max"]),
+    }
 
 
 def main():
@@ -300,6 +373,8 @@ def main():
         torch.distributed.init_process_group("nccl")
     out = gpu_leg(args, rank, world_size)
     if rank == 0:
+        if world_size == 1 and not args.no_learned:
+            out["learned_warmstart"] = learned_leg(args)
         if world_size == 1 and not args.no_cpu:
             rate, cores, sample = cpu_leg(args, args.cpu_seconds)
             out["cpu_baseline"] = {"value": rate, "unit": "body-steps/s", "cores": cores, "kind": "port",

@@ -1,0 +1,92 @@
+"""Learned warm start on the GPU: the plumbing leaves the reference step untouched, the
+plain solver logs usable samples, and a network trained on them gives a smaller velocity
+residual than the zero start at the same iteration count."""
+import numpy as np
+import pytest
+
+from dbox_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def _scatter(n_worlds, bodies, seed):
+    rng = np.random.default_rng(seed)
+    return [scenes.scatter(bodies, 40.0, 40.0, rng) for _ in range(n_worlds)]
+
+
+def test_zero_network_is_the_plain_step(gpu_lib):
+    # a network that predicts 0 for every new point: learned mode must give the plain step bit for bit
+    worlds = _scatter(12, 150, 21)
+    m = gpu_lib.Mlp()
+    norm = np.concatenate([np.zeros(32), np.ones(32), np.zeros(4), np.ones(4)]).astype(np.float32)
+    m.set_params(np.zeros(gpu_lib.MLP_PARAMS, np.float32), norm)
+    plain, learned = gpu_lib.World(worlds), gpu_lib.World(worlds)
+    learned.set_warmstart(2, m)
+    for _ in range(60):
+        plain.step()
+        learned.step()
+    for i in range(len(worlds)):
+        a, b = plain.export_state(i), learned.export_state(i)
+        assert a["bodies"].tobytes() == b["bodies"].tobytes()
+        ca, cb = a["contacts"].copy(), b["contacts"].copy()
+        cb["flags"] &= ~np.uint32(0xC0)                 # the learned mode's new-point marks
+        assert ca.tobytes() == cb.tobytes()
+        assert (a["contacts"]["flags"] & 0xC0).sum() == 0
+
+
+def test_plain_solver_logs_samples(gpu_lib):
+    w = gpu_lib.World(_scatter(32, 128, 22))
+    w.set_warmstart(1, None, 200000)
+    w.step(steps=100, graph=True)
+    n = w.sample_count()
+    assert n > 1000
+    f, t = w.samples()
+    assert np.isfinite(f).all() and np.isfinite(t).all()
+    assert set(np.unique(f[:, 26])) <= {1.0, 2.0}            # point count
+    assert (t[:, [0, 2]] >= 0).all()                         # converged normal impulses are clamped at 0
+    assert (t[f[:, 26] == 1.0][:, 2:] == 0).all()            # one-point contacts have no second point
+
+
+def test_quality_measure_orders_iteration_counts(gpu_lib):
+    res = {}
+    for vi in (3, 8):
+        w = gpu_lib.World(_scatter(16, 128, 23))
+        w.step(steps=80, graph=True)
+        w.set_measure(True)
+        acc = []
+        for _ in range(10):
+            w.step(vel_iters=vi)
+            q = w.quality()
+            acc.append(np.sqrt(q[:, 0].sum() / max(q[:, 2].sum(), 1)))
+        res[vi] = np.mean(acc)
+    assert res[8] < res[3]
+
+
+def test_trained_start_lowers_the_residual(gpu_lib):
+    worlds = _scatter(96, 200, 24)
+    log = gpu_lib.World(worlds)
+    log.set_warmstart(1, None, 1_000_000)
+    log.step(steps=250, graph=True)
+    f, t = log.samples(0, min(log.sample_count(), 300000))
+    m = gpu_lib.Mlp(seed=3)
+    m.fit_normalization(f, t)
+    losses = m.train_world(log, epochs=20, batch=16384, lr=1e-3, seed=4)
+    assert losses[-1] < 0.8 * losses[0]
+
+    def measure(mode, model):
+        w = gpu_lib.World(worlds)
+        w.step(steps=250, graph=True)
+        w.set_warmstart(mode, model, 0)
+        w.set_measure(True)
+        mx, rms = [], []
+        for _ in range(30):
+            w.step(vel_iters=5)
+            q = w.quality()
+            mx.append(q[:, 1].max())
+            rms.append(np.sqrt(q[:, 0].sum() / max(q[:, 2].sum(), 1)))
+        return np.mean(mx), np.mean(rms)
+
+    plain_max, plain_rms = measure(0, None)
+    learned_max, learned_rms = measure(2, m)
+    assert learned_max < plain_max
+    assert learned_rms <= 1.02 * plain_rms
