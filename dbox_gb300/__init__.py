@@ -86,6 +86,7 @@ def lib():
     L.dbox_world_get_samples.argtypes = [vp, i32, i32, vp]
     L.dbox_world_clear_samples.argtypes = [vp]
     L.dbox_world_set_measure.argtypes = [vp, i32]
+    L.dbox_world_set_listener.argtypes = [vp, vp, vp]
     L.dbox_world_get_quality.argtypes = [vp, vp]
     _lib = L
     return L
@@ -281,6 +282,24 @@ class World:
 
     def clear_samples(self):
         _check(lib().dbox_world_clear_samples(self.h), "dbox_world_clear_samples")
+
+    _EVENT_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p)
+
+    def set_listener(self, fn):
+        """b2World.SetContactListener: fn(events) is called after each step with the step's
+        events (abi.CONTACT_EVENT records, in reference order, world by world); None removes it."""
+        if fn is None:
+            self._listener = None
+            _check(lib().dbox_world_set_listener(self.h, None, None), "dbox_world_set_listener")
+            return
+
+        def tramp(ptr, count, user):
+            buf = (ctypes.c_char * (count * abi.CONTACT_EVENT.itemsize)).from_address(ptr)
+            fn(np.frombuffer(bytes(buf), abi.CONTACT_EVENT).copy())
+
+        self._listener = World._EVENT_FN(tramp)
+        _check(lib().dbox_world_set_listener(self.h, ctypes.cast(self._listener, ctypes.c_void_p), None),
+               "dbox_world_set_listener")
 
     def set_measure(self, on=True):
         _check(lib().dbox_world_set_measure(self.h, 1 if on else 0), "dbox_world_set_measure")

@@ -70,6 +70,7 @@ CONTACT_EVENT = np.dtype([
     ("point_count", "<i4"), ("normal_impulses", "<f4", 2), ("tangent_impulses", "<f4", 2),
 ])
 assert CONTACT_EVENT.itemsize == 36
+EVENT_BEGIN, EVENT_END, EVENT_PRESOLVE, EVENT_POSTSOLVE = 1, 2, 3, 4   # DBOX_EVENT_*
 
 PROFILE = np.dtype([(n, "<f4") for n in (
     "step", "collide", "solve", "solve_init", "solve_velocity", "solve_position", "broadphase", "solve_toi")])

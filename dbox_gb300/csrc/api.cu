@@ -126,6 +126,10 @@ struct dbox_world {
     DBuf<unsigned> d_sample_count;
     DBuf<int> s_slog, s_pend;
     int measure = 0;
+    // contact listener
+    DBuf<dbox_contact_event> d_events;
+    DBuf<unsigned char> s_cevt;
+    std::vector<dbox_contact_event> h_events;
     std::vector<dg::WorldInfo> wi;
     int total_bodies = 0, total_fixtures = 0, total_contacts = 0, total_joints = 0;
     // graph replay
@@ -163,6 +167,7 @@ void free_device(dbox_world* w) {
     w->d_vr.free(); w->d_tvr.free(); w->d_pr.free(); w->d_tpr.free(); w->d_snap.free(); w->d_io.free();
     w->s_vpos.free(); w->d_solve_world.free(); w->d_solve_smem.free();
     w->s_feat.free(); w->s_vsave.free(); w->s_slog.free(); w->s_pend.free();
+    w->d_events.free(); w->s_cevt.free();
     w->s_cbody.free(); w->s_adj_items.free(); w->s_isl_pair.free(); w->s_cq.free(); w->s_cvis.free(); w->s_bfl.free(); w->s_sbody.free(); w->d_prof.free();
     if (w->graph) { cudaGraphExecDestroy(w->graph); w->graph = nullptr; }
     if (w->tgraph) { cudaGraphExecDestroy(w->tgraph); w->tgraph = nullptr; }
@@ -184,6 +189,10 @@ int alloc_mode_scratch(dbox_world* w) {
         if (!w->s_pend.p) ok &= w->s_pend.alloc(nc) == 0;
     }
     if (w->measure && !w->s_vsave.p) ok &= w->s_vsave.alloc(3 * nb) == 0;
+    if (w->listener) {
+        if (!w->s_cevt.p) ok &= w->s_cevt.alloc(nc) == 0;
+        if (!w->d_events.p) ok &= w->d_events.alloc(4 * nc + 64 * w->wi.size()) == 0;
+    }
     if (!ok) return fail(DBOX_ERR_CUDA, "device allocation failed (warm-start / measure scratch)");
     return DBOX_OK;
 }
@@ -551,6 +560,8 @@ dg::Ctx make_ctx(dbox_world* w, float dt, int vi, int pi) {
     x.s_pend = w->s_pend.p;
     x.measure = w->measure;
     x.s_vsave = w->s_vsave.p;
+    x.events = w->d_events.p;
+    x.s_cevt = w->s_cevt.p;
     return x;
 }
 
@@ -928,9 +939,35 @@ int32_t dbox_world_set_gravity(dbox_world* w, dbox_vec2 gravity) {
 
 int32_t dbox_world_set_listener(dbox_world* w, dbox_event_fn fn, void* user) {
     if (!w) return DBOX_ERR_INVALID;
-    if (fn) return fail(DBOX_ERR_UNSUPPORTED, "contact listener events are not recorded by this build");
-    w->listener = nullptr;
+    w->listener = fn;
     w->listener_user = user;
+    if (fn && w->on_device) {
+        int rc = alloc_mode_scratch(w);
+        if (rc) return rc;
+    }
+    if (w->graph) { cudaGraphExecDestroy(w->graph); w->graph = nullptr; }
+    if (w->tgraph) { cudaGraphExecDestroy(w->tgraph); w->tgraph = nullptr; }
+    return DBOX_OK;
+}
+
+// the events of the last step, world by world, handed to the listener on this thread
+static int deliver_events(dbox_world* w) {
+    if (!w->listener || !w->d_events.p) return DBOX_OK;
+    size_t W = w->worlds.size();
+    std::vector<dg::WorldDyn> wd(W);
+    CU(cudaStreamSynchronize(w->stream));
+    CU(cudaMemcpy(wd.data(), w->d_wd.p, sizeof(dg::WorldDyn) * W, cudaMemcpyDeviceToHost));
+    w->h_events.clear();
+    for (size_t i = 0; i < W; ++i) {
+        const dg::WorldInfo& wi = w->wi[i];
+        int cnt = std::min(wd[i].ev_count, 4 * wi.contact_cap + 64);
+        if (cnt <= 0) continue;
+        size_t at = w->h_events.size();
+        w->h_events.resize(at + cnt);
+        CU(cudaMemcpy(&w->h_events[at], w->d_events.p + 4 * (size_t)wi.contact_start + 64 * i,
+                      sizeof(dbox_contact_event) * cnt, cudaMemcpyDeviceToHost));
+    }
+    if (!w->h_events.empty()) w->listener(w->h_events.data(), (int32_t)w->h_events.size(), w->listener_user);
     return DBOX_OK;
 }
 
@@ -954,6 +991,7 @@ int32_t dbox_world_step(dbox_world* w, float dt, int32_t velocity_iterations, in
     memset(&w->profile, 0, sizeof(w->profile));
     w->profile.step = ms;
     w->last_launches = launches;
+    if (!rc) rc = deliver_events(w);
     return rc;
 }
 
@@ -963,6 +1001,10 @@ int32_t dbox_world_step_n(dbox_world* w, float dt, int32_t velocity_iterations, 
         return fail(DBOX_ERR_INVALID, "dbox_world_step_n: bad arguments");
     int rc = ensure_device(w);
     if (rc) return rc;
+    if (w->listener) {                      // events are delivered after every step
+        for (int i = 0; i < steps && !rc; ++i) rc = dbox_world_step(w, dt, velocity_iterations, position_iterations);
+        return rc;
+    }
     int flags = w->warm | (w->continuous << 1) | (w->substep << 2) | (w->allow_sleep << 3) | (w->autoclear << 4);
     if (!w->graph || w->g_dt != dt || w->g_vi != velocity_iterations || w->g_pi != position_iterations ||
         w->graph_flags != flags) {

@@ -98,7 +98,7 @@ DG bool filter_should_collide(const DFixture& a, const DFixture& b) {
 
 // ------------------------------------------------------------ b2Contact.Update (contacts/b2contact.d:270-356)
 // Returns true when the touching state changed (the caller wakes both bodies).
-DG bool contact_update(const Ctx& x, dbox_contact_state& c) {
+DG bool contact_update(const Ctx& x, dbox_contact_state& c, unsigned* evt = nullptr) {
     Manifold m;
     manifold_load(c, m);
     Manifold old = m;
@@ -132,12 +132,40 @@ DG bool contact_update(const Ctx& x, dbox_contact_state& c) {
     }
     if (touching) c.flags |= kContactTouching; else c.flags &= ~(uint32_t)kContactTouching;
     manifold_store(m, c);
+    // listener calls of b2Contact.Update (b2contact.d:340-355): BeginContact, EndContact, PreSolve
+    if (evt) *evt = (!wasTouching && touching ? 1u : 0u) | (wasTouching && !touching ? 2u : 0u) | (!sensor && touching ? 4u : 0u);
     return changed;
+}
+
+// ------------------------------------------------------------ contact-listener events
+DG dbox_contact_event* world_events(const Ctx& x, const WorldInfo& wi, int w) {
+    return x.events + 4 * (size_t)wi.contact_start + 64 * (size_t)w;
+}
+DG int world_event_cap(const WorldInfo& wi) { return 4 * wi.contact_cap + 64; }
+DG void put_event(const Ctx& x, const WorldInfo& wi, int w, int slot, int kind, const dbox_contact_state& c,
+                  int count, const float* ni, const float* ti) {
+    if (slot >= world_event_cap(wi)) { set_error(x, w, DBOX_ERR_CAPACITY); return; }
+    dbox_contact_event& e = world_events(x, wi, w)[slot];
+    e.kind = kind;
+    e.world = w;
+    e.fixture_a = c.fixture_a - wi.fix_start;
+    e.fixture_b = c.fixture_b - wi.fix_start;
+    e.point_count = count;
+    e.normal_impulses[0] = ni ? ni[0] : 0.0f;
+    e.normal_impulses[1] = ni && count > 1 ? ni[1] : 0.0f;
+    e.tangent_impulses[0] = ti ? ti[0] : 0.0f;
+    e.tangent_impulses[1] = ti && count > 1 ? ti[1] : 0.0f;
+}
+// one lane appends the listener events of b2Contact.Update in their order
+DG void put_update_events(const Ctx& x, const WorldInfo& wi, int w, WorldDyn& wd, unsigned evt, const dbox_contact_state& c) {
+    if (evt & 1u) put_event(x, wi, w, wd.ev_count++, DBOX_EVENT_BEGIN, c, c.point_count, nullptr, nullptr);
+    if (evt & 2u) put_event(x, wi, w, wd.ev_count++, DBOX_EVENT_END, c, c.point_count, nullptr, nullptr);
+    if (evt & 4u) put_event(x, wi, w, wd.ev_count++, DBOX_EVENT_PRESOLVE, c, c.point_count, nullptr, nullptr);
 }
 
 // Collide treatment of one contact at list position lp: 0 = updated, 2 = destroyed.
 // Wakes are recorded into s_woken (minimum list position) instead of the flags.
-DG int collide_one(const Ctx& x, dbox_contact_state& c, int lp, bool use_atomic) {
+DG int collide_one(const Ctx& x, dbox_contact_state& c, int lp, bool use_atomic, unsigned* evt) {
     const DFixture& fa = x.fx[c.fixture_a];
     const DFixture& fb = x.fx[c.fixture_b];
     int A = fa.body, B = fb.body;
@@ -152,8 +180,9 @@ DG int collide_one(const Ctx& x, dbox_contact_state& c, int lp, bool use_atomic)
         // b2ContactManager.Destroy + b2Contact.Destroy (b2contactmanager.d:183-246, b2contact.d:402-422)
         wake = c.point_count > 0 && !fa.sensor && !fb.sensor;
         result = 2;
+        *evt = (c.flags & kContactTouching) ? 2u : 0u;                 // EndContact on Destroy
     } else {
-        wake = contact_update(x, c);
+        wake = contact_update(x, c, evt);
         result = 0;
     }
     if (wake) {
@@ -325,7 +354,7 @@ __global__ void k_step_begin(Ctx x) {
     WorldDyn& wd = x.wd[w];
     const WorldInfo& wi = x.wi[w];
     int lane = lane_id();
-    if (lane == 0) { wd.error = 0; wd.islands = 0; wd.toi_events = 0; }
+    if (lane == 0) { wd.error = 0; wd.islands = 0; wd.toi_events = 0; wd.ev_count = 0; }
     for (int i = lane; i < wi.body_count; i += kWarp) x.s_woken[wi.body_start + i] = kNoWake;
     tsync();
     if (wd.flags & 1u) {                                                // e_newFixture
@@ -348,9 +377,11 @@ __global__ void k_collide(Ctx x) {
         const DFixture& fb = x.fx[c.fixture_b];
         int A = fa.body, B = fb.body;
         int state = 0;
+        unsigned evt = 0;
         if (c.flags & kContactFilter) {                                // b2contactmanager.d:266-288
             if (!body_should_collide(x, B, A) || !filter_should_collide(fa, fb)) {
                 state = 2;
+                evt = (c.flags & kContactTouching) ? 2u : 0u;
                 if (c.point_count > 0 && !fa.sensor && !fb.sensor) {
                     atomicMin(&x.s_woken[A], lp);
                     atomicMin(&x.s_woken[B], lp);
@@ -365,9 +396,10 @@ __global__ void k_collide(Ctx x) {
             bool activeA = (ba.flags & kBodyAwake) && ba.type != kStaticBody;
             bool activeB = (bb.flags & kBodyAwake) && bb.type != kStaticBody;
             if (!activeA && !activeB) state = 1;
-            else state = collide_one(x, c, lp, true);
+            else state = collide_one(x, c, lp, true, &evt);
         }
         x.s_cstate[i] = state;
+        if (x.record_events) x.s_cevt[i] = (unsigned char)evt;
         if (state != 2) x.ct[i] = c;
     }
 }
@@ -405,10 +437,36 @@ __global__ void k_collide_finish(Ctx x) {
             bool activeA = awA && ba.type != kStaticBody;
             bool activeB = awB && bb.type != kStaticBody;
             if (!activeA && !activeB) continue;
-            x.s_cstate[c0 + k] = collide_one(x, c, lp, false);
+            unsigned evt = 0;
+            x.s_cstate[c0 + k] = collide_one(x, c, lp, false, &evt);
+            if (x.record_events) x.s_cevt[c0 + k] = (unsigned char)evt;
         }
     }
     tsync();
+    // listener events of this Collide, in list order (newest contact first)
+    if (x.record_events) {
+        int base = 0;
+        for (int top = n - 1; top >= 0; top -= kWarp) {
+            int k = top - lane;
+            unsigned evt = k >= 0 ? x.s_cevt[c0 + k] : 0u;
+            int cnt = __popc(evt);
+            int incl = cnt;
+            for (int o = 1; o < 32; o <<= 1) {
+                int t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
+            }
+            if (cnt) {
+                const dbox_contact_state& c = x.ct[c0 + k];
+                int slot = base + incl - cnt;
+                if (evt & 1u) put_event(x, wi, w, slot++, DBOX_EVENT_BEGIN, c, c.point_count, nullptr, nullptr);
+                if (evt & 2u) put_event(x, wi, w, slot++, DBOX_EVENT_END, c, c.point_count, nullptr, nullptr);
+                if (evt & 4u) put_event(x, wi, w, slot++, DBOX_EVENT_PRESOLVE, c, c.point_count, nullptr, nullptr);
+            }
+            base += __shfl_sync(0xffffffffu, incl, 31);
+        }
+        if (lane == 0) wd.ev_count = base;
+        tsync();
+    }
     // apply wakes
     for (int i = lane; i < wi.body_count; i += kWarp) {
         int b = wi.body_start + i;
@@ -1742,9 +1800,8 @@ DG void solve_world(const Ctx& x, int w, float* sbp, bool sb_smem, float* stage_
                     }
                 }
                 vrow[idx] = vr;
-                if (njI) {
-                    x.s_vpos[item] = idx;
-                } else {
+                if (njI || x.record_events) x.s_vpos[item] = idx;
+                if (!njI) {
                     // one schedule serves both orders: the position row of this place is this contact's
                     prow[idx] = pack_p(pc, x.s_body_island[b0 + ((bfl[vc.bodyA] & kBfStatic) ? vc.bodyB : vc.bodyA)]);
                     pdone = true;
@@ -1979,6 +2036,19 @@ DG void solve_world(const Ctx& x, int w, float* sbp, bool sb_smem, float* stage_
         for (int o = 16; o > 0; o >>= 1) ms = bmin(ms, __shfl_xor_sync(0xffffffffu, ms, o));
         if (lane == 0) wd.q_minsep = ms;
     }
+    if (x.record_events) {
+        // b2Island.Report (b2island.d:419-438): PostSolve per island contact in island order
+        const int e0 = wd.ev_count;
+        for (int t = lane; t < ncI; t += kWarp) {
+            int item = x.s_isl_contact[c0 + t];
+            VRow r = load_v(vrow + x.s_vpos[item]);
+            float ni[2] = {r.imp.x, r.imp.z}, ti[2] = {r.imp.y, r.imp.w};
+            put_event(x, wi, w, e0 + t, DBOX_EVENT_POSTSOLVE, x.ct[item], r.ids.z & 0xff, ni, ti);
+        }
+        tsync();
+        if (lane == 0) wd.ev_count = e0 + ncI;
+        tsync();
+    }
     stamp(x, w, 8);
     // copy back + SynchronizeTransform (b2island.d:227-235)
     for (int t = lane; t < nbI; t += kWarp) {
@@ -2089,8 +2159,8 @@ DG int toi_collect(const Ctx& x, int c0, int b0, int k0, int k1, int* list, int 
 }
 
 // b2Contact.Update inside the TOI loop: wakes are applied immediately
-DG void toi_update(const Ctx& x, dbox_contact_state& c) {
-    if (contact_update(x, c)) {
+DG void toi_update(const Ctx& x, dbox_contact_state& c, unsigned* evt = nullptr) {
+    if (contact_update(x, c, evt)) {
         b_set_awake(x.bs[x.fx[c.fixture_a].body], true);
         b_set_awake(x.bs[x.fx[c.fixture_b].body], true);
     }
@@ -2162,6 +2232,15 @@ DG void solve_toi_island(const Ctx& x, int w, const WorldInfo& wi, SB sb, int nb
         Bd.sweep[4] = c.x; Bd.sweep[5] = c.y; Bd.sweep[7] = a;
         Bd.vel[0] = v.x; Bd.vel[1] = v.y; Bd.vel[2] = wv;
         b_sync_transform(Bd);
+    }
+    if (x.record_events) {
+        // b2Island.Report at the end of b2Island.SolveTOI (b2island.d:411-416)
+        WorldDyn& wd = x.wd[w];
+        for (int q = 0; q < ncI; ++q) {
+            VRow r = load_v(tv + q);
+            float ni[2] = {r.imp.x, r.imp.z}, ti[2] = {r.imp.y, r.imp.w};
+            put_event(x, wi, w, wd.ev_count++, DBOX_EVENT_POSTSOLVE, x.ct[x.s_isl_contact[c0 + q]], r.ids.z & 0xff, ni, ti);
+        }
     }
 }
 
@@ -2296,7 +2375,9 @@ DG void toi_world(const Ctx& x, int w, float* sbp) {
                 Sweep backup1 = b_sweep(bA), backup2 = b_sweep(bB);
                 b_advance(bA, minAlpha);
                 b_advance(bB, minAlpha);
-                toi_update(x, mc);
+                unsigned evt = 0;
+                toi_update(x, mc, &evt);
+                if (x.record_events) put_update_events(x, wi, w, wd, evt, mc);
                 mc.flags &= ~(uint32_t)kContactToi;
                 ++mc.toi_count;
                 if ((mc.flags & kContactEnabled) == 0 || (mc.flags & kContactTouching) == 0) {
@@ -2349,7 +2430,9 @@ DG void toi_world(const Ctx& x, int w, float* sbp) {
                                 if (x.s_cq[c0 + kk] & 2) continue;
                                 Sweep backup = b_sweep(O);
                                 if ((O.flags & kBodyIsland) == 0) b_advance(O, minAlpha);
-                                toi_update(x, c);
+                                unsigned evt = 0;
+                                toi_update(x, c, &evt);
+                                if (x.record_events) put_update_events(x, wi, w, wd, evt, c);
                                 if ((c.flags & kContactEnabled) == 0 || (c.flags & kContactTouching) == 0) {
                                     b_set_sweep(O, backup);
                                     b_sync_transform(O);

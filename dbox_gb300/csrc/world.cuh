@@ -57,6 +57,8 @@ struct WorldDyn {
     float q_max;                   // max over points of |dlambda|
     int q_points;                  // points measured
     float q_minsep;                // minimum separation over points after the step (<= 0)
+    int ev_count;                  // contact-listener events recorded in the last step
+    int ev_pad;
 };
 
 struct BodyStatic {
@@ -214,6 +216,8 @@ struct Ctx {
     float2 gravity;
     int warm_starting, continuous, sub_stepping, allow_sleep;
     int record_events;
+    dbox_contact_event* events;    // per world: 4 * contact_start + 64 * world, 4 * contact_cap + 64 records
+    unsigned char* s_cevt;         // contact-slot-indexed: listener events of this Collide (1 begin, 2 end, 4 presolve)
     int* g_status;                 // bit (-code) set for every DBOX_ERR_* raised by any world
     // learned warm start: 0 plain (Box2D), 1 plain + log training samples, 2 learned start
     int ws_mode;

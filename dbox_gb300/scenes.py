@@ -178,6 +178,40 @@ def stacks(n, height, spacing=2.0, box=0.5):
     return s
 
 
+def chains(n_chains=4, links=32, hx=0.125, hy=0.025, x0=-12.0, spacing=6.0, y=12.0, pile=True):
+    """Revolute-joint chains (b2RevoluteJointDef, joints/b2revolutejoint.d:30-110): each chain
+    is `links` boxes of half-extents hx x hy laid out horizontally from a static post and
+    joined end to end; odd chains limit their joints to +-0.5 rad, every third chain drives
+    its first joint with a motor.  Optional box stacks on the ground below."""
+    parts = [ground_box()]
+    if pile:
+        parts.append(stacks(4 * n_chains, 4, spacing=spacing / 2.0))
+    for c in range(n_chains):
+        x = x0 + c * spacing
+        post = _boxes([(x, y)], 0.1, 0.1, abi.STATIC)
+        chain = _boxes([(x + hx + 2 * hx * i, y) for i in range(links)], hx, hy, abi.DYNAMIC, 0.4, 20.0)
+        part = _concat([post, chain])
+        j = np.zeros(links, abi.REVOLUTE_DEF)
+        for i in range(links):
+            j[i]["body_a"] = i               # the post for i = 0, else link i-1
+            j[i]["body_b"] = i + 1
+            j[i]["local_anchor_a"] = (0.0, 0.0) if i == 0 else (hx, 0.0)
+            j[i]["local_anchor_b"] = (-hx, 0.0)
+            if c % 2 == 1:
+                j[i]["enable_limit"] = 1
+                j[i]["lower_angle"] = -0.5
+                j[i]["upper_angle"] = 0.5
+        if c % 3 == 0:
+            j[0]["enable_motor"] = 1
+            j[0]["motor_speed"] = 1.0
+            j[0]["max_motor_torque"] = 50.0
+        part["joints"] = j
+        parts.append(part)
+    out = _concat(parts)
+    out["name"] = "chains"
+    return out
+
+
 def batch(n_worlds=4096, seed=3, lo=8, hi=512):
     """Batched workload: per-world body counts log-uniform in [lo, hi]; thirds of
     pyramids, 40 m-container scatters and box stacks."""

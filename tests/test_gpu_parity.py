@@ -59,6 +59,16 @@ def test_stacks_exact(oracle_lib, gpu_lib):
     _run_exact(oracle_lib, gpu_lib, scenes.stacks(60, 12), 300, every=10)
 
 
+def test_revolute_chains_exact(oracle_lib, gpu_lib):
+    # revolute joints (b2revolutejoint.d:319-636): plain, limited and motor-driven chains
+    # falling onto box stacks, joints in the islands with contacts
+    from dbox_gb300 import scenes
+    ow, gw = _run_exact(oracle_lib, gpu_lib, scenes.chains(n_chains=4, links=16), 300, every=5)
+    st = gw.export_state()
+    assert len(st["joints"]) == 64
+    assert np.abs(st["joints"]["impulse"]).max() > 0
+
+
 def test_batch_exact(oracle_lib, gpu_lib):
     from dbox_gb300 import scenes
     oracle_lib.set_trig_mode(1)
