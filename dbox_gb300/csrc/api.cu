@@ -128,6 +128,9 @@ struct dbox_world {
     int measure = 0;
     // contact listener
     DBuf<dbox_contact_event> d_events;
+    DBuf<unsigned> s_sapk0, s_sapk1;
+    DBuf<int> s_sapi0, s_sapi1;
+    DBuf<float4> s_sapbox;
     DBuf<unsigned char> s_cevt;
     std::vector<dbox_contact_event> h_events;
     std::vector<dg::WorldInfo> wi;
@@ -168,6 +171,7 @@ void free_device(dbox_world* w) {
     w->s_vpos.free(); w->d_solve_world.free(); w->d_solve_smem.free();
     w->s_feat.free(); w->s_vsave.free(); w->s_slog.free(); w->s_pend.free();
     w->d_events.free(); w->s_cevt.free();
+    w->s_sapk0.free(); w->s_sapk1.free(); w->s_sapi0.free(); w->s_sapi1.free(); w->s_sapbox.free();
     w->s_cbody.free(); w->s_adj_items.free(); w->s_isl_pair.free(); w->s_cq.free(); w->s_cvis.free(); w->s_bfl.free(); w->s_sbody.free(); w->d_prof.free();
     if (w->graph) { cudaGraphExecDestroy(w->graph); w->graph = nullptr; }
     if (w->tgraph) { cudaGraphExecDestroy(w->tgraph); w->tgraph = nullptr; }
@@ -406,6 +410,9 @@ int upload(dbox_world* w) {
     ok &= w->s_isl_sleep.alloc(nb) == 0;
     ok &= w->s_pcount.alloc(nf) == 0;
     ok &= w->s_moved.alloc(nf) == 0;
+    ok &= w->s_sapk0.alloc(nf) == 0 && w->s_sapk1.alloc(nf) == 0;
+    ok &= w->s_sapi0.alloc(nf) == 0 && w->s_sapi1.alloc(nf) == 0;
+    ok &= w->s_sapbox.alloc(nf) == 0;
     ok &= w->s_cstate.alloc(nc) == 0;
     ok &= w->s_adj_items.alloc(2 * (size_t)nc) == 0;
     ok &= w->s_isl_pair.alloc(nc) == 0;
@@ -561,6 +568,11 @@ dg::Ctx make_ctx(dbox_world* w, float dt, int vi, int pi) {
     x.measure = w->measure;
     x.s_vsave = w->s_vsave.p;
     x.events = w->d_events.p;
+    x.s_sapk[0] = w->s_sapk0.p;
+    x.s_sapk[1] = w->s_sapk1.p;
+    x.s_sapi[0] = w->s_sapi0.p;
+    x.s_sapi[1] = w->s_sapi1.p;
+    x.s_sapbox = w->s_sapbox.p;
     x.s_cevt = w->s_cevt.p;
     return x;
 }

@@ -207,6 +207,185 @@ DG AABB proxy_fat(const Ctx& x, int f) {
     return a;
 }
 
+// ---- sweep-and-prune candidates for worlds with many proxies.  UpdatePairs wants every
+// pair (a < b) of overlapping fat AABBs with a or b moved (b2broadphase.d:139-195); for a
+// world of thousands of proxies testing all pairs on one warp is quadratic, so the proxies
+// are radix-sorted by the lower bound of their fat AABB along the axis with the larger
+// spread, and a proxy's candidates are the sorted range whose lower bounds lie in
+// [lo - largest extent, hi].  Partners are then ordered by id, which gives the same pair
+// list as the all-pairs search.
+constexpr int kSapMinProxies = 1024;
+
+DG unsigned sort_key(float f) {                   // order-preserving float -> unsigned
+    unsigned u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+struct Sap {
+    const unsigned* key;   // sorted keys of the ordinary proxies
+    const float4* box;     // their fat AABBs, then those of the wide proxies
+    const int* idx;        // their world-local proxy index | moved << 31
+    int n;                 // ordinary proxies
+    const int* wide;       // wide proxies (extent over 4x the mean, e.g. container walls): index | moved << 31
+    int nwide;
+    int axis;              // 0 x, 1 y
+    float ext;             // largest extent of an ordinary proxy along the axis
+};
+
+// Sort the world's valid proxies (one warp; stable LSD radix sort, 4 passes of 8 bits).
+DG Sap sap_build(const Ctx& x, int w, int* hist) {
+    const WorldInfo& wi = x.wi[w];
+    const int lane = lane_id();
+    const int f0 = wi.fix_start, nf = wi.fix_count;
+    // axis with the larger spread of centres; mean extent along each axis
+    float mn[2] = {3.4e38f, 3.4e38f}, mx[2] = {-3.4e38f, -3.4e38f}, sum[2] = {0.0f, 0.0f};
+    int cnt = 0;
+    for (int i = lane; i < nf; i += kWarp) {
+        const dbox_proxy_state& p = x.px[f0 + i];
+        if (p.proxy_id < 0) continue;
+        ++cnt;
+        for (int a = 0; a < 2; ++a) {
+            float c = 0.5f * (p.fat_aabb[a] + p.fat_aabb[2 + a]);
+            mn[a] = bmin(mn[a], c);
+            mx[a] = bmax(mx[a], c);
+            sum[a] += p.fat_aabb[2 + a] - p.fat_aabb[a];
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+        for (int a = 0; a < 2; ++a) {
+            mn[a] = bmin(mn[a], __shfl_xor_sync(0xffffffffu, mn[a], o));
+            mx[a] = bmax(mx[a], __shfl_xor_sync(0xffffffffu, mx[a], o));
+            sum[a] += __shfl_xor_sync(0xffffffffu, sum[a], o);
+        }
+    }
+    Sap s;
+    s.axis = (mx[1] - mn[1]) > (mx[0] - mn[0]) ? 1 : 0;
+    const float cut = 4.0f * sum[s.axis] / (float)(cnt > 0 ? cnt : 1);
+    auto is_wide = [&](const dbox_proxy_state& p) { return p.fat_aabb[2 + s.axis] - p.fat_aabb[s.axis] > cut; };
+    float ext = 0.0f;
+    for (int i = lane; i < nf; i += kWarp) {
+        const dbox_proxy_state& p = x.px[f0 + i];
+        if (p.proxy_id >= 0 && !is_wide(p)) ext = bmax(ext, p.fat_aabb[2 + s.axis] - p.fat_aabb[s.axis]);
+    }
+    for (int o = 16; o > 0; o >>= 1) ext = bmax(ext, __shfl_xor_sync(0xffffffffu, ext, o));
+    s.ext = ext;
+    unsigned* k0 = x.s_sapk[0] + f0;
+    unsigned* k1 = x.s_sapk[1] + f0;
+    int* i0 = x.s_sapi[0] + f0;
+    int* i1 = x.s_sapi[1] + f0;
+    int nv = 0;
+    for (int base = 0; base < nf; base += kWarp) {   // ordinary proxies, in id order
+        int i = base + lane;
+        bool v = i < nf && x.px[f0 + i].proxy_id >= 0 && !is_wide(x.px[f0 + i]);
+        unsigned bal = __ballot_sync(0xffffffffu, v);
+        if (v) {
+            int r = nv + __popc(bal & ((1u << lane) - 1u));
+            k0[r] = sort_key(x.px[f0 + i].fat_aabb[s.axis]);
+            i0[r] = i;
+        }
+        nv += __popc(bal);
+    }
+    tsync();
+    for (int pass = 0; pass < 4; ++pass) {
+        const int shift = 8 * pass;
+        const unsigned* kin = pass & 1 ? k1 : k0;
+        const int* iin = pass & 1 ? i1 : i0;
+        unsigned* kout = pass & 1 ? k0 : k1;
+        int* iout = pass & 1 ? i0 : i1;
+        for (int b = lane; b < 256; b += kWarp) hist[b] = 0;
+        tsync();
+        for (int i = lane; i < nv; i += kWarp) atomicAdd(&hist[(kin[i] >> shift) & 255u], 1);
+        tsync();
+        int run = 0;                                  // exclusive scan of the 256 bins
+        for (int base = 0; base < 256; base += kWarp) {
+            int v = hist[base + lane];
+            int incl = v;
+            for (int o = 1; o < 32; o <<= 1) {
+                int t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
+            }
+            hist[base + lane] = run + incl - v;
+            run += __shfl_sync(0xffffffffu, incl, 31);
+        }
+        tsync();
+        for (int base = 0; base < nv; base += kWarp) {    // stable scatter, 32 keys at a time
+            int i = base + lane;
+            unsigned k = i < nv ? kin[i] : 0u;
+            int d = i < nv ? (int)((k >> shift) & 255u) : 256 + lane;
+            unsigned peers = __match_any_sync(0xffffffffu, d);
+            if (i < nv) {
+                int pos = hist[d] + __popc(peers & ((1u << lane) - 1u));
+                kout[pos] = k;
+                iout[pos] = iin[i];
+            }
+            tsync();
+            if (i < nv && (peers & ((1u << lane) - 1u)) == 0) hist[d] += __popc(peers);
+            tsync();
+        }
+    }
+    // boxes in sorted order and the moved flag in the index
+    for (int r = lane; r < nv; r += kWarp) {
+        int i = i0[r];
+        const dbox_proxy_state& p = x.px[f0 + i];
+        x.s_sapbox[f0 + r] = make_float4(p.fat_aabb[0], p.fat_aabb[1], p.fat_aabb[2], p.fat_aabb[3]);
+        if (p.moved) i0[r] = i | (int)0x80000000;
+    }
+    // the wide proxies after them (boxes) and in the free ping-pong index buffer
+    int nw = 0;
+    for (int base = 0; base < nf; base += kWarp) {
+        int i = base + lane;
+        bool v = i < nf && x.px[f0 + i].proxy_id >= 0 && is_wide(x.px[f0 + i]);
+        unsigned bal = __ballot_sync(0xffffffffu, v);
+        if (v) {
+            int r = nw + __popc(bal & ((1u << lane) - 1u));
+            const dbox_proxy_state& p = x.px[f0 + i];
+            x.s_sapbox[f0 + nv + r] = make_float4(p.fat_aabb[0], p.fat_aabb[1], p.fat_aabb[2], p.fat_aabb[3]);
+            i1[r] = p.moved ? (i | (int)0x80000000) : i;
+        }
+        nw += __popc(bal);
+    }
+    tsync();
+    s.key = k0;
+    s.box = x.s_sapbox + f0;
+    s.idx = i0;
+    s.n = nv;
+    s.wide = i1;
+    s.nwide = nw;
+    return s;
+}
+
+// fn(b) for every partner b > a of proxy a (overlapping fat AABBs, a or b moved), by sorted rank
+template <class F>
+DG void sap_partners(const Sap& s, const AABB& fa, int a, bool amoved, F&& fn) {
+    float lo = s.axis ? fa.lo.y : fa.lo.x, hi = s.axis ? fa.hi.y : fa.hi.x;
+    float qlo = lo - s.ext;
+    qlo -= 1e-3f * (1.0f + babs(qlo));               // round the bound outwards
+    unsigned klo = sort_key(qlo), khi = sort_key(hi);
+    int l = 0, r = s.n;                               // first key >= klo
+    while (l < r) { int m = (l + r) >> 1; if (s.key[m] < klo) l = m + 1; else r = m; }
+    for (int q = l; q < s.n && s.key[q] <= khi; ++q) {
+        int bi = s.idx[q];
+        int b = bi & 0x7fffffff;
+        if (b <= a || (!amoved && bi >= 0)) continue;
+        float4 bb = s.box[q];
+        AABB fb;
+        fb.lo = v2(bb.x, bb.y);
+        fb.hi = v2(bb.z, bb.w);
+        if (aabb_overlap(fa, fb)) fn(b);
+    }
+    for (int q = 0; q < s.nwide; ++q) {
+        int bi = s.wide[q];
+        int b = bi & 0x7fffffff;
+        if (b <= a || (!amoved && bi >= 0)) continue;
+        float4 bb = s.box[s.n + q];
+        AABB fb;
+        fb.lo = v2(bb.x, bb.y);
+        fb.hi = v2(bb.z, bb.w);
+        if (aabb_overlap(fa, fb)) fn(b);
+    }
+}
+
 DG void find_new_contacts(const Ctx& x, int w) {
     const WorldInfo& wi = x.wi[w];
     WorldDyn& wd = x.wd[w];
@@ -223,10 +402,17 @@ DG void find_new_contacts(const Ctx& x, int w) {
     }
     tsync();
     if (nm == 0) return;
+    __shared__ int sap_hist[kSolveWarps][256];
+    const bool use_sap = nf >= kSapMinProxies;
+    Sap sap;
+    if (use_sap) sap = sap_build(x, w, sap_hist[(threadIdx.x >> 5) % kSolveWarps]);
     // count pairs per proxy a
     for (int a = lane; a < nf; a += kWarp) {
         int cnt = 0;
-        if (x.px[f0 + a].proxy_id >= 0) {
+        if (use_sap) {
+            if (x.px[f0 + a].proxy_id >= 0)
+                sap_partners(sap, proxy_fat(x, f0 + a), a, x.px[f0 + a].moved != 0, [&](int) { ++cnt; });
+        } else if (x.px[f0 + a].proxy_id >= 0) {
             AABB fa = proxy_fat(x, f0 + a);
             if (x.px[f0 + a].moved) {
                 for (int b = a + 1; b < nf; ++b)
@@ -265,7 +451,17 @@ DG void find_new_contacts(const Ctx& x, int w) {
         int o = x.s_pcount[f0 + a];
         if (x.px[f0 + a].proxy_id < 0) continue;
         AABB fa = proxy_fat(x, f0 + a);
-        if (x.px[f0 + a].moved) {
+        if (use_sap) {
+            int2* seg = x.pairs + wi.pair_start + o;
+            int cnt = 0;
+            sap_partners(sap, fa, a, x.px[f0 + a].moved != 0, [&](int b) { seg[cnt++] = make_int2(f0 + a, f0 + b); });
+            for (int i = 1; i < cnt; ++i) {           // partners by id (insertion sort)
+                int2 v = seg[i];
+                int j = i - 1;
+                while (j >= 0 && seg[j].y > v.y) { seg[j + 1] = seg[j]; --j; }
+                seg[j + 1] = v;
+            }
+        } else if (x.px[f0 + a].moved) {
             for (int b = a + 1; b < nf; ++b)
                 if (x.px[f0 + b].proxy_id >= 0 && aabb_overlap(fa, proxy_fat(x, f0 + b)))
                     x.pairs[wi.pair_start + o++] = make_int2(f0 + a, f0 + b);

@@ -180,6 +180,9 @@ struct Ctx {
     unsigned* s_isl_sleep;         // body-indexed (island id)
     int* s_pcount;                 // fixture-indexed: pair counts / moved list
     int* s_moved;                  // fixture-indexed
+    unsigned* s_sapk[2];           // fixture-indexed: sweep-and-prune keys (radix-sort ping-pong)
+    int* s_sapi[2];                // fixture-indexed: proxy of each sorted key (top bit: moved)
+    float4* s_sapbox;              // fixture-indexed: fat AABBs in sorted order
     // scratch (contact-indexed)
     int* s_cstate;                 // 0 processed, 1 inactive, 2 destroyed
     int2* s_adj_items;             // 2 per contact slot: (contact, other body) edges by body

@@ -54,6 +54,13 @@ def test_scatter_exact(oracle_lib, gpu_lib):
     _run_exact(oracle_lib, gpu_lib, s, 400, every=5)
 
 
+def test_large_scatter_exact(oracle_lib, gpu_lib):
+    # more than 1,024 proxies: the broad-phase takes the sweep-and-prune path
+    from dbox_gb300 import scenes
+    s = scenes.scatter(1500, 60.0, 60.0, np.random.default_rng(9))
+    _run_exact(oracle_lib, gpu_lib, s, 120, every=10)
+
+
 def test_stacks_exact(oracle_lib, gpu_lib):
     from dbox_gb300 import scenes
     _run_exact(oracle_lib, gpu_lib, scenes.stacks(60, 12), 300, every=10)
