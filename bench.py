@@ -55,6 +55,7 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-learned", action="store_true", help="skip the learned warm-start comparison")
+    p.add_argument("--no-autotune", action="store_true", help="keep the default world-to-block mapping")
     p.add_argument("--learned-worlds", type=int, default=1024)
     p.add_argument("--learned-log-steps", type=int, default=2000)
     return p.parse_args()
@@ -202,10 +203,21 @@ def gpu_leg(args, rank, world_size):
     worlds, cfg = make_worlds(args, rank)
     nbody_dyn = dynamic_bodies(worlds)
     nbody = sum(len(s["bodies"]) for s in worlds)
+    # the autotuner picks the world-to-block mapping on a throwaway handle of the same worlds
+    # (it advances the worlds it times); the measured handles then use that mapping
+    mapping = None
+    if not args.no_autotune:
+        wt = dbox_gb300.World(worlds)
+        wt.step(DT, VI, PI, steps=args.warmup, graph=True)
+        mapping = wt.autotune(steps=3, dt=DT, vel_iters=VI, pos_iters=PI)
+        wt.close()
     w = dbox_gb300.World(worlds)
     # twin handle for the end-to-end leg: the same scenes and warm-up, so it replays exactly
     # the steps the device-timed leg measures
     we = dbox_gb300.World(worlds)
+    if mapping:
+        w.set_mapping(*mapping)
+        we.set_mapping(*mapping)
     w.step(DT, VI, PI, steps=args.warmup, graph=True)
     we.step(DT, VI, PI, steps=args.warmup, graph=True)
     w.sync()
@@ -263,6 +275,8 @@ def gpu_leg(args, rank, world_size):
         "data": "synthetic seeded scenes (numpy PCG64 seed %d)" % args.seed,
         "config": dict(cfg, dt=DT, velocity_iterations=VI, position_iterations=PI, dynamic_bodies=nbody_dyn,
                        parallelism="replicas: one batch of worlds per GPU",
+                       mapping=({"warps_per_block": mapping[0], "body_budget": mapping[1], "chosen_by": "autotuner"}
+                                if mapping else "default"),
                        l2="working set (bodies, contacts, constraint rows) larger than the 129 MB L2",
                        timing="one CUDA graph of K steps with per-phase CUDA events"),
         "e2e": {"value": e2e, "unit": "body-steps/s", "h2d_bytes_per_step": int(forces.nbytes),

@@ -111,6 +111,8 @@ struct dbox_world {
     DBuf<dg::PRow> d_pr, d_tpr;
     DBuf<int> s_vpos, d_solve_world, d_solve_smem;
     int solve_blocks = 0, solve_smem_floats = 0;
+    int solve_wpb = dg::kSolveWarps;    // warp slots (worlds) per block of the solve kernel
+    int solve_budget = 0;               // body budget per block (0: chosen from the worlds)
     DBuf<dg::SweepSnap> d_snap;
     DBuf<float> d_io;           // staging for bulk force upload / transform readback (3 floats per body)
     DBuf<int2> s_cbody, s_adj_items, s_isl_pair;
@@ -212,10 +214,12 @@ int pack_solve_slots(dbox_world* w) {
     // budget in bodies per block: room for the largest world, at least 1024, and at most
     // 1536 when there are enough worlds to fill the GPU (three blocks per SM stay resident);
     // the front of the block holds each warp's constraint-row staging slots
-    const int stage_floats = dg::kSolveWarps * dg::kWarpSmemFloats;
-    const int hard_cap = (227 * 1024 - 1024 - 4 * stage_floats) / 32;
+    const int wpb = w->solve_wpb;
+    const int stage_floats = wpb * dg::kWarpSmemFloats;
+    const int hard_cap = (227 * 1024 - 1024 - 4096 - 4 * stage_floats) / 32;
     int budget = std::max(1024, max_nb);
     budget = std::min(budget, W >= 3 * 152 ? 1536 : hard_cap);
+    if (w->solve_budget > 0) budget = std::min(w->solve_budget, hard_cap);
     std::vector<int> order(W);
     for (int i = 0; i < W; ++i) order[i] = i;
     std::stable_sort(order.begin(), order.end(),
@@ -231,26 +235,26 @@ int pack_solve_slots(dbox_world* w) {
         for (size_t t = 0; t < open.size(); ++t) {
             int b = open[t];
             if (chosen < 0 && used[b] + need <= budget) chosen = b;
-            if (count[b] + (b == chosen) < dg::kSolveWarps) open[keep++] = b;   // still has a free slot
+            if (count[b] + (b == chosen) < wpb) open[keep++] = b;   // still has a free slot
         }
         open.resize(keep);
         if (chosen < 0) {
             chosen = (int)used.size();
             used.push_back(0);
             count.push_back(0);
-            slot_world.resize(used.size() * dg::kSolveWarps, -1);
-            slot_off.resize(used.size() * dg::kSolveWarps, -1);
-            if (dg::kSolveWarps > 1) open.push_back(chosen);
+            slot_world.resize(used.size() * wpb, -1);
+            slot_off.resize(used.size() * wpb, -1);
+            if (wpb > 1) open.push_back(chosen);
         }
-        int slot = chosen * dg::kSolveWarps + count[chosen]++;
+        int slot = chosen * wpb + count[chosen]++;
         slot_world[slot] = wid;
         slot_off[slot] = in_smem ? stage_floats + 8 * used[chosen] : -1;
         used[chosen] += need;
     }
     if (used.empty()) {                     // no worlds: one idle block
         used.push_back(0);
-        slot_world.assign(dg::kSolveWarps, -1);
-        slot_off.assign(dg::kSolveWarps, -1);
+        slot_world.assign(wpb, -1);
+        slot_off.assign(wpb, -1);
     }
     int max_used = 0;
     for (int u : used) max_used = std::max(max_used, u);
@@ -538,6 +542,7 @@ dg::Ctx make_ctx(dbox_world* w, float dt, int vi, int pi) {
     x.solve_world = w->d_solve_world.p;
     x.solve_smem = w->d_solve_smem.p;
     x.solve_blocks = w->solve_blocks;
+    x.solve_wpb = w->solve_wpb;
     x.solve_smem_floats = w->solve_smem_floats;
     x.snap = w->d_snap.p;
     x.s_cbody = w->s_cbody.p;
@@ -1209,6 +1214,55 @@ int32_t dbox_world_get_quality(dbox_world* w, float* out) {
         out[4 * i + 3] = wd[i].q_minsep;
     }
     return DBOX_OK;
+}
+
+int32_t dbox_world_set_mapping(dbox_world* w, int32_t warps_per_block, int32_t body_budget) {
+    if (!w || !(warps_per_block == 1 || warps_per_block == 2 || warps_per_block == dg::kSolveWarps) || body_budget < 0)
+        return fail(DBOX_ERR_INVALID, "dbox_world_set_mapping: warps per block must be 1, 2 or %d", dg::kSolveWarps);
+    w->solve_wpb = warps_per_block;
+    w->solve_budget = body_budget;
+    if (w->on_device) {
+        int rc = pack_solve_slots(w);
+        if (rc) return rc;
+    }
+    if (w->graph) { cudaGraphExecDestroy(w->graph); w->graph = nullptr; }
+    if (w->tgraph) { cudaGraphExecDestroy(w->tgraph); w->tgraph = nullptr; }
+    return DBOX_OK;
+}
+
+int32_t dbox_world_autotune(dbox_world* w, float dt, int32_t velocity_iterations, int32_t position_iterations,
+                            int32_t steps, int32_t* choice) {
+    if (!w || steps < 1) return fail(DBOX_ERR_INVALID, "dbox_world_autotune: bad arguments");
+    int rc = ensure_device(w);
+    if (rc) return rc;
+    // candidate mappings of worlds onto the solve kernel: warp slots per block x body budget
+    const int cand[][2] = {{dg::kSolveWarps, 0}, {2, 0}, {1, 0}, {dg::kSolveWarps, 2048}, {2, 2048}};
+    const int ncand = (int)(sizeof(cand) / sizeof(cand[0]));
+    cudaEvent_t e0, e1;
+    CU(cudaEventCreate(&e0));
+    CU(cudaEventCreate(&e1));
+    float best = 3.4e38f;
+    int bi = 0;
+    for (int round = 0; round < 2 && !rc; ++round) {            // two rounds: the state drifts between trials
+        for (int c = 0; c < ncand && !rc; ++c) {
+            rc = dbox_world_set_mapping(w, cand[c][0], cand[c][1]);
+            if (!rc) rc = dbox_world_step_n(w, dt, velocity_iterations, position_iterations, 1);   // builds the graph
+            if (rc) break;
+            CU(cudaEventRecord(e0, w->stream));
+            rc = dbox_world_step_n(w, dt, velocity_iterations, position_iterations, steps);
+            CU(cudaEventRecord(e1, w->stream));
+            CU(cudaEventSynchronize(e1));
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (round == 1 && ms < best) { best = ms; bi = c; }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    rc = dbox_world_set_mapping(w, cand[bi][0], cand[bi][1]);
+    if (choice) { choice[0] = cand[bi][0]; choice[1] = cand[bi][1]; }
+    return rc;
 }
 
 int32_t dbox_world_set_phase_profile(dbox_world* w, int32_t enable) {

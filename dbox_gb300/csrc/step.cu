@@ -2711,7 +2711,7 @@ DG void toi_world(const Ctx& x, int w, float* sbp) {
 // (row staging, solver body rows) come from the host's packing of worlds into blocks.
 __global__ void __launch_bounds__(kSolveWarps * 32, 3) k_solve_toi(Ctx x) {
     extern __shared__ float smem_sb[];
-    const int slot = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+    const int slot = blockIdx.x * x.solve_wpb + (threadIdx.x >> 5);
     const int w = x.solve_world[slot];
     if (w < 0) return;
     const int soff = x.solve_smem[slot];
@@ -2748,7 +2748,7 @@ extern "C" int dbox_launch_step_ev(const dg::Ctx* x, cudaStream_t stream, int* l
     dg::k_collide<<<flat_blocks, 256, 0, stream>>>(*x);
     dg::k_collide_finish<<<team_blocks, threads, 0, stream>>>(*x);
     if (ev) cudaEventRecordWithFlags(ev[1], stream, cudaEventRecordExternal);
-    dg::k_solve_toi<<<x->solve_blocks, dg::kSolveWarps * dg::kWarp, x->solve_smem_floats * sizeof(float), stream>>>(*x);
+    dg::k_solve_toi<<<x->solve_blocks, x->solve_wpb * dg::kWarp, x->solve_smem_floats * sizeof(float), stream>>>(*x);
     if (ev) cudaEventRecordWithFlags(ev[2], stream, cudaEventRecordExternal);
     if (ev) cudaEventRecordWithFlags(ev[3], stream, cudaEventRecordExternal);
     if (launches) *launches = 4;

@@ -139,7 +139,7 @@ struct __align__(16) PRow {
 struct SweepSnap { Sweep a, b; float alpha0; int pad; };
 
 constexpr int kProfSlots = 32;         // per-world slots of the optional phase profile
-constexpr int kSolveWarps = 4;          // warp slots (worlds) per block of the solve kernel
+constexpr int kSolveWarps = 4;          // most warp slots (worlds) per block of the solve kernel
 constexpr int kStageFloats = 2 * 32 * 36; // per warp: row ring of two 4608-byte halves
 constexpr int kWarpSmemFloats = kStageFloats + 4;   // + the ring's two mbarriers
 
@@ -205,7 +205,8 @@ struct Ctx {
     int* s_vpos;                   // contact-slot-indexed: velocity-schedule position (worlds with joints)
     const int* solve_world;        // per warp slot of the solve kernel: world index or -1
     const int* solve_smem;         // per warp slot: float offset of its body rows in shared memory, or -1
-    int solve_blocks;              // blocks of the solve kernel (four warp slots each)
+    int solve_blocks;              // blocks of the solve kernel
+    int solve_wpb;                 // warp slots per block (1, 2 or kSolveWarps)
     int solve_smem_floats;         // dynamic shared memory of one solve block, in floats
     SweepSnap* snap;               // contact-slot-indexed
     int2* s_cbody;                 // contact-slot-indexed: world-local bodies of the contact

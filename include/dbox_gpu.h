@@ -352,6 +352,15 @@ int32_t dbox_world_clear_samples(dbox_world* w);
 int32_t dbox_world_set_measure(dbox_world* w, int32_t enable);
 int32_t dbox_world_get_quality(dbox_world* w, float* out);
 
+/* Mapping of the worlds onto the solve kernel (new; no counterpart in dbox): warp slots
+ * (worlds) per block, 1, 2 or 4, and the per-block budget of solver body rows in shared
+ * memory, in bodies (0 = chosen from the worlds).  Results do not depend on it. */
+int32_t dbox_world_set_mapping(dbox_world* w, int32_t warps_per_block, int32_t body_budget);
+/* Autotuner: times `steps` steps (the simulation advances) under each candidate mapping,
+ * twice, and keeps the fastest; choice[2] receives (warps per block, body budget). */
+int32_t dbox_world_autotune(dbox_world* w, float dt, int32_t velocity_iterations, int32_t position_iterations,
+                            int32_t steps, int32_t* choice);
+
 /* Device kernels launched by the last step (for launch accounting). */
 int32_t dbox_world_last_launches(dbox_world* w, int32_t* out);
 

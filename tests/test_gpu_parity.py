@@ -92,6 +92,33 @@ def test_batch_exact(oracle_lib, gpu_lib):
                 assert not d, "world %d step %d: %s" % (i, t + 1, d[:6])
 
 
+def test_mappings_and_autotune_keep_results(oracle_lib, gpu_lib):
+    # the world-to-block mapping (warps per block, shared-memory budget) and the autotuner's
+    # choice among mappings change where worlds run, never what they compute
+    from dbox_gb300 import scenes
+    oracle_lib.set_trig_mode(1)
+    worlds = scenes.batch(n_worlds=9, seed=12, lo=8, hi=200)
+    gw = gpu_lib.World(worlds)
+    ows = [oracle_lib.OracleWorld(s) for s in worlds]
+    steps = 0
+    for wpb, budget in ((1, 0), (2, 2048), (4, 0)):
+        gw.set_mapping(wpb, budget)
+        for _ in range(30):
+            gw.step()
+        steps += 30
+    choice = gw.autotune(steps=2)
+    assert choice[0] in (1, 2, 4)
+    steps += 10 * 3
+    for _ in range(30):
+        gw.step()
+    steps += 30
+    for ow in ows:
+        ow.step(steps=steps)
+    for i, ow in enumerate(ows):
+        d = exact_diff(ow.export_state(), gw.export_state(i))
+        assert not d, "world %d: %s" % (i, d[:6])
+
+
 def test_graph_replay_matches_single_steps(oracle_lib, gpu_lib):
     from dbox_gb300 import scenes
     s = scenes.scatter(200, 25.0, 30.0, np.random.default_rng(3))
