@@ -275,7 +275,8 @@ def gpu_leg(args, rank, world_size):
         "data": "synthetic seeded scenes (numpy PCG64 seed %d)" % args.seed,
         "config": dict(cfg, dt=DT, velocity_iterations=VI, position_iterations=PI, dynamic_bodies=nbody_dyn,
                        parallelism="replicas: one batch of worlds per GPU",
-                       mapping=({"warps_per_block": mapping[0], "body_budget": mapping[1], "chosen_by": "autotuner"}
+                       mapping=({"warps_per_block": mapping[0], "body_budget": mapping[1],
+                                 "isolated_largest_worlds": mapping[2], "chosen_by": "autotuner"}
                                 if mapping else "default"),
                        l2="working set (bodies, contacts, constraint rows) larger than the 129 MB L2",
                        timing="one CUDA graph of K steps with per-phase CUDA events"),

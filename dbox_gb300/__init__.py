@@ -88,6 +88,7 @@ def lib():
     L.dbox_world_set_measure.argtypes = [vp, i32]
     L.dbox_world_set_listener.argtypes = [vp, vp, vp]
     L.dbox_world_set_mapping.argtypes = [vp, i32, i32]
+    L.dbox_world_set_mapping_isolated.argtypes = [vp, i32, i32, i32]
     L.dbox_world_autotune.argtypes = [vp, f32, i32, i32, i32, vp]
     L.dbox_world_get_quality.argtypes = [vp, vp]
     _lib = L
@@ -303,16 +304,18 @@ class World:
         _check(lib().dbox_world_set_listener(self.h, ctypes.cast(self._listener, ctypes.c_void_p), None),
                "dbox_world_set_listener")
 
-    def set_mapping(self, warps_per_block=4, body_budget=0):
-        _check(lib().dbox_world_set_mapping(self.h, warps_per_block, body_budget), "dbox_world_set_mapping")
+    def set_mapping(self, warps_per_block=4, body_budget=0, isolate=0):
+        _check(lib().dbox_world_set_mapping_isolated(self.h, warps_per_block, body_budget, isolate),
+               "dbox_world_set_mapping")
 
     def autotune(self, steps=3, dt=1.0 / 60.0, vel_iters=8, pos_iters=3):
         """Time the candidate world-to-block mappings on the live worlds and keep the fastest;
-        returns (warps per block, body budget).  The worlds advance by 10 * (steps + 1) steps."""
-        out = np.zeros(2, np.int32)
+        returns (warps per block, body budget, isolated largest worlds).  The worlds advance by
+        14 * (steps + 1) steps."""
+        out = np.zeros(3, np.int32)
         _check(lib().dbox_world_autotune(self.h, ctypes.c_float(dt), vel_iters, pos_iters, steps, abi.ptr(out)),
                "dbox_world_autotune")
-        return int(out[0]), int(out[1])
+        return int(out[0]), int(out[1]), int(out[2])
 
     def set_measure(self, on=True):
         _check(lib().dbox_world_set_measure(self.h, 1 if on else 0), "dbox_world_set_measure")

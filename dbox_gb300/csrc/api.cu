@@ -113,6 +113,7 @@ struct dbox_world {
     int solve_blocks = 0, solve_smem_floats = 0;
     int solve_wpb = dg::kSolveWarps;    // warp slots (worlds) per block of the solve kernel
     int solve_budget = 0;               // body budget per block (0: chosen from the worlds)
+    int solve_isolate = 0;              // this many largest worlds get a block of their own
     DBuf<dg::SweepSnap> d_snap;
     DBuf<float> d_io;           // staging for bulk force upload / transform readback (3 floats per body)
     DBuf<int2> s_cbody, s_adj_items, s_isl_pair;
@@ -226,7 +227,20 @@ int pack_solve_slots(dbox_world* w) {
                      [&](int a, int b) { return w->wi[a].body_count > w->wi[b].body_count; });
     std::vector<int> used, count, slot_world, slot_off;
     std::vector<int> open;                  // blocks with a free slot, in creation order
+    int placed = 0;
     for (int wid : order) {
+        if (placed++ < w->solve_isolate) {   // a block of its own: no other warp competes on that block
+            int nbw = w->wi[wid].body_count;
+            bool in_smem = nbw <= budget;
+            int b = (int)used.size();
+            used.push_back(in_smem ? nbw : 0);
+            count.push_back(wpb);
+            slot_world.resize(used.size() * wpb, -1);
+            slot_off.resize(used.size() * wpb, -1);
+            slot_world[b * wpb] = wid;
+            slot_off[b * wpb] = in_smem ? stage_floats : -1;
+            continue;
+        }
         int nbw = w->wi[wid].body_count;
         bool in_smem = nbw <= budget;
         int need = in_smem ? nbw : 0;
@@ -1217,10 +1231,16 @@ int32_t dbox_world_get_quality(dbox_world* w, float* out) {
 }
 
 int32_t dbox_world_set_mapping(dbox_world* w, int32_t warps_per_block, int32_t body_budget) {
-    if (!w || !(warps_per_block == 1 || warps_per_block == 2 || warps_per_block == dg::kSolveWarps) || body_budget < 0)
+    return dbox_world_set_mapping_isolated(w, warps_per_block, body_budget, 0);
+}
+
+int32_t dbox_world_set_mapping_isolated(dbox_world* w, int32_t warps_per_block, int32_t body_budget, int32_t isolate) {
+    if (!w || !(warps_per_block == 1 || warps_per_block == 2 || warps_per_block == dg::kSolveWarps) || body_budget < 0 ||
+        isolate < 0)
         return fail(DBOX_ERR_INVALID, "dbox_world_set_mapping: warps per block must be 1, 2 or %d", dg::kSolveWarps);
     w->solve_wpb = warps_per_block;
     w->solve_budget = body_budget;
+    w->solve_isolate = isolate;
     if (w->on_device) {
         int rc = pack_solve_slots(w);
         if (rc) return rc;
@@ -1236,7 +1256,8 @@ int32_t dbox_world_autotune(dbox_world* w, float dt, int32_t velocity_iterations
     int rc = ensure_device(w);
     if (rc) return rc;
     // candidate mappings of worlds onto the solve kernel: warp slots per block x body budget
-    const int cand[][2] = {{dg::kSolveWarps, 0}, {2, 0}, {1, 0}, {dg::kSolveWarps, 2048}, {2, 2048}};
+    const int cand[][3] = {{dg::kSolveWarps, 0, 0}, {2, 0, 0}, {1, 0, 0}, {dg::kSolveWarps, 2048, 0}, {2, 2048, 0},
+                           {dg::kSolveWarps, 2048, 152}, {dg::kSolveWarps, 2048, 304}};
     const int ncand = (int)(sizeof(cand) / sizeof(cand[0]));
     cudaEvent_t e0, e1;
     CU(cudaEventCreate(&e0));
@@ -1245,7 +1266,7 @@ int32_t dbox_world_autotune(dbox_world* w, float dt, int32_t velocity_iterations
     int bi = 0;
     for (int round = 0; round < 2 && !rc; ++round) {            // two rounds: the state drifts between trials
         for (int c = 0; c < ncand && !rc; ++c) {
-            rc = dbox_world_set_mapping(w, cand[c][0], cand[c][1]);
+            rc = dbox_world_set_mapping_isolated(w, cand[c][0], cand[c][1], cand[c][2]);
             if (!rc) rc = dbox_world_step_n(w, dt, velocity_iterations, position_iterations, 1);   // builds the graph
             if (rc) break;
             CU(cudaEventRecord(e0, w->stream));
@@ -1260,8 +1281,8 @@ int32_t dbox_world_autotune(dbox_world* w, float dt, int32_t velocity_iterations
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (rc) return rc;
-    rc = dbox_world_set_mapping(w, cand[bi][0], cand[bi][1]);
-    if (choice) { choice[0] = cand[bi][0]; choice[1] = cand[bi][1]; }
+    rc = dbox_world_set_mapping_isolated(w, cand[bi][0], cand[bi][1], cand[bi][2]);
+    if (choice) { choice[0] = cand[bi][0]; choice[1] = cand[bi][1]; choice[2] = cand[bi][2]; }
     return rc;
 }
 

@@ -356,8 +356,10 @@ int32_t dbox_world_get_quality(dbox_world* w, float* out);
  * (worlds) per block, 1, 2 or 4, and the per-block budget of solver body rows in shared
  * memory, in bodies (0 = chosen from the worlds).  Results do not depend on it. */
 int32_t dbox_world_set_mapping(dbox_world* w, int32_t warps_per_block, int32_t body_budget);
+/* The same, with the `isolate` largest worlds each given a block of its own. */
+int32_t dbox_world_set_mapping_isolated(dbox_world* w, int32_t warps_per_block, int32_t body_budget, int32_t isolate);
 /* Autotuner: times `steps` steps (the simulation advances) under each candidate mapping,
- * twice, and keeps the fastest; choice[2] receives (warps per block, body budget). */
+ * twice, and keeps the fastest; choice[3] receives (warps per block, body budget, isolated). */
 int32_t dbox_world_autotune(dbox_world* w, float dt, int32_t velocity_iterations, int32_t position_iterations,
                             int32_t steps, int32_t* choice);
 

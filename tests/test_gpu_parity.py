@@ -101,14 +101,14 @@ def test_mappings_and_autotune_keep_results(oracle_lib, gpu_lib):
     gw = gpu_lib.World(worlds)
     ows = [oracle_lib.OracleWorld(s) for s in worlds]
     steps = 0
-    for wpb, budget in ((1, 0), (2, 2048), (4, 0)):
-        gw.set_mapping(wpb, budget)
+    for wpb, budget, iso in ((1, 0, 0), (2, 2048, 0), (4, 0, 3)):
+        gw.set_mapping(wpb, budget, iso)
         for _ in range(30):
             gw.step()
         steps += 30
     choice = gw.autotune(steps=2)
     assert choice[0] in (1, 2, 4)
-    steps += 10 * 3
+    steps += 14 * 3
     for _ in range(30):
         gw.step()
     steps += 30
