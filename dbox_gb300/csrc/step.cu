@@ -207,69 +207,77 @@ DG AABB proxy_fat(const Ctx& x, int f) {
     return a;
 }
 
-// ---- sweep-and-prune candidates for worlds with many proxies.  UpdatePairs wants every
-// pair (a < b) of overlapping fat AABBs with a or b moved (b2broadphase.d:139-195); for a
-// world of thousands of proxies testing all pairs on one warp is quadratic, so the proxies
-// are radix-sorted by the lower bound of their fat AABB along the axis with the larger
-// spread, and a proxy's candidates are the sorted range whose lower bounds lie in
-// [lo - largest extent, hi].  Partners are then ordered by id, which gives the same pair
-// list as the all-pairs search.
+// ---- grid candidates for worlds with many proxies.  UpdatePairs wants every pair (a < b)
+// of overlapping fat AABBs with a or b moved (b2broadphase.d:139-195); for a world of
+// thousands of proxies testing all pairs on one warp is quadratic.  Instead the ordinary
+// proxies are radix-sorted by the grid cell of their lower corner (cells as large as the
+// largest ordinary extent, row-major ids), so a proxy's candidates lie in the cells of the
+// rows cy-1 .. cy of its corners, columns cx-1 .. cx: one key range per row.  Proxies much
+// wider than the mean (e.g. container walls) are tested against everything.  Partners are
+// then ordered by id, which gives the same pair list as the all-pairs search.
 constexpr int kSapMinProxies = 1024;
 
-DG unsigned sort_key(float f) {                   // order-preserving float -> unsigned
-    unsigned u = __float_as_uint(f);
-    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
-}
-
 struct Sap {
-    const unsigned* key;   // sorted keys of the ordinary proxies
+    const unsigned* key;   // sorted cell ids of the ordinary proxies
     const float4* box;     // their fat AABBs, then those of the wide proxies
     const int* idx;        // their world-local proxy index | moved << 31
     int n;                 // ordinary proxies
-    const int* wide;       // wide proxies (extent over 4x the mean, e.g. container walls): index | moved << 31
+    const int* wide;       // wide proxies (extent over 4x the mean): index | moved << 31
     int nwide;
-    int axis;              // 0 x, 1 y
-    float ext;             // largest extent of an ordinary proxy along the axis
+    float ox, oy, inv;     // grid origin and 1 / cell size
+    int ncx, ncy;          // cells per row, rows
 };
 
-// Sort the world's valid proxies (one warp; stable LSD radix sort, 4 passes of 8 bits).
+DG int sap_cell(float v, float o, float inv, int n) {
+    int c = (int)floorf((v - o) * inv);
+    return c < 0 ? 0 : (c >= n ? n - 1 : c);
+}
+
+// Sort the world's ordinary proxies by cell (one warp; stable LSD radix sort, 8 bits a pass).
 DG Sap sap_build(const Ctx& x, int w, int* hist) {
     const WorldInfo& wi = x.wi[w];
     const int lane = lane_id();
     const int f0 = wi.fix_start, nf = wi.fix_count;
-    // axis with the larger spread of centres; mean extent along each axis
-    float mn[2] = {3.4e38f, 3.4e38f}, mx[2] = {-3.4e38f, -3.4e38f}, sum[2] = {0.0f, 0.0f};
+    float lo[2] = {3.4e38f, 3.4e38f}, hi[2] = {-3.4e38f, -3.4e38f}, sum = 0.0f;
     int cnt = 0;
     for (int i = lane; i < nf; i += kWarp) {
         const dbox_proxy_state& p = x.px[f0 + i];
         if (p.proxy_id < 0) continue;
         ++cnt;
-        for (int a = 0; a < 2; ++a) {
-            float c = 0.5f * (p.fat_aabb[a] + p.fat_aabb[2 + a]);
-            mn[a] = bmin(mn[a], c);
-            mx[a] = bmax(mx[a], c);
-            sum[a] += p.fat_aabb[2 + a] - p.fat_aabb[a];
-        }
+        sum += bmax(p.fat_aabb[2] - p.fat_aabb[0], p.fat_aabb[3] - p.fat_aabb[1]);
     }
     for (int o = 16; o > 0; o >>= 1) {
         cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-        for (int a = 0; a < 2; ++a) {
-            mn[a] = bmin(mn[a], __shfl_xor_sync(0xffffffffu, mn[a], o));
-            mx[a] = bmax(mx[a], __shfl_xor_sync(0xffffffffu, mx[a], o));
-            sum[a] += __shfl_xor_sync(0xffffffffu, sum[a], o);
-        }
+        sum += __shfl_xor_sync(0xffffffffu, sum, o);
     }
-    Sap s;
-    s.axis = (mx[1] - mn[1]) > (mx[0] - mn[0]) ? 1 : 0;
-    const float cut = 4.0f * sum[s.axis] / (float)(cnt > 0 ? cnt : 1);
-    auto is_wide = [&](const dbox_proxy_state& p) { return p.fat_aabb[2 + s.axis] - p.fat_aabb[s.axis] > cut; };
+    const float cut = 4.0f * sum / (float)(cnt > 0 ? cnt : 1);
+    auto is_wide = [&](const dbox_proxy_state& p) {
+        return bmax(p.fat_aabb[2] - p.fat_aabb[0], p.fat_aabb[3] - p.fat_aabb[1]) > cut;
+    };
     float ext = 0.0f;
     for (int i = lane; i < nf; i += kWarp) {
         const dbox_proxy_state& p = x.px[f0 + i];
-        if (p.proxy_id >= 0 && !is_wide(p)) ext = bmax(ext, p.fat_aabb[2 + s.axis] - p.fat_aabb[s.axis]);
+        if (p.proxy_id < 0 || is_wide(p)) continue;
+        ext = bmax(ext, bmax(p.fat_aabb[2] - p.fat_aabb[0], p.fat_aabb[3] - p.fat_aabb[1]));
+        for (int a = 0; a < 2; ++a) { lo[a] = bmin(lo[a], p.fat_aabb[a]); hi[a] = bmax(hi[a], p.fat_aabb[a]); }
     }
-    for (int o = 16; o > 0; o >>= 1) ext = bmax(ext, __shfl_xor_sync(0xffffffffu, ext, o));
-    s.ext = ext;
+    for (int o = 16; o > 0; o >>= 1) {
+        ext = bmax(ext, __shfl_xor_sync(0xffffffffu, ext, o));
+        for (int a = 0; a < 2; ++a) {
+            lo[a] = bmin(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
+            hi[a] = bmax(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
+        }
+    }
+    Sap s;
+    float cellsz = ext > 1e-6f ? ext * 1.001f : 1.0f;
+    // keep the grid at most 4096 x 4096 cells (larger cells only widen the candidate ranges)
+    float span = bmax(hi[0] - lo[0], hi[1] - lo[1]);
+    if (span / cellsz > 4000.0f) cellsz = span / 4000.0f;
+    s.ox = lo[0];
+    s.oy = lo[1];
+    s.inv = 1.0f / cellsz;
+    s.ncx = (int)((hi[0] - lo[0]) * s.inv) + 2;
+    s.ncy = (int)((hi[1] - lo[1]) * s.inv) + 2;
     unsigned* k0 = x.s_sapk[0] + f0;
     unsigned* k1 = x.s_sapk[1] + f0;
     int* i0 = x.s_sapi[0] + f0;
@@ -281,13 +289,15 @@ DG Sap sap_build(const Ctx& x, int w, int* hist) {
         unsigned bal = __ballot_sync(0xffffffffu, v);
         if (v) {
             int r = nv + __popc(bal & ((1u << lane) - 1u));
-            k0[r] = sort_key(x.px[f0 + i].fat_aabb[s.axis]);
+            const dbox_proxy_state& p = x.px[f0 + i];
+            int cx = sap_cell(p.fat_aabb[0], s.ox, s.inv, s.ncx), cy = sap_cell(p.fat_aabb[1], s.oy, s.inv, s.ncy);
+            k0[r] = (unsigned)(cy * s.ncx + cx);
             i0[r] = i;
         }
         nv += __popc(bal);
     }
     tsync();
-    for (int pass = 0; pass < 4; ++pass) {
+    for (int pass = 0; pass < 3; ++pass) {           // cell ids < 2^24
         const int shift = 8 * pass;
         const unsigned* kin = pass & 1 ? k1 : k0;
         const int* iin = pass & 1 ? i1 : i0;
@@ -297,7 +307,7 @@ DG Sap sap_build(const Ctx& x, int w, int* hist) {
         tsync();
         for (int i = lane; i < nv; i += kWarp) atomicAdd(&hist[(kin[i] >> shift) & 255u], 1);
         tsync();
-        int run = 0;                                  // exclusive scan of the 256 bins
+        int run = 0;
         for (int base = 0; base < 256; base += kWarp) {
             int v = hist[base + lane];
             int incl = v;
@@ -324,16 +334,15 @@ DG Sap sap_build(const Ctx& x, int w, int* hist) {
             tsync();
         }
     }
-    // boxes in sorted order and the moved flag in the index
+    // three passes: the sorted data is in the second buffer
     for (int r = lane; r < nv; r += kWarp) {
-        int i = i0[r];
+        int i = i1[r];
         const dbox_proxy_state& p = x.px[f0 + i];
         x.s_sapbox[f0 + r] = make_float4(p.fat_aabb[0], p.fat_aabb[1], p.fat_aabb[2], p.fat_aabb[3]);
-        if (p.moved) i0[r] = i | (int)0x80000000;
+        if (p.moved) i1[r] = i | (int)0x80000000;
     }
-    // the wide proxies after them (boxes) and in the free ping-pong index buffer
     int nw = 0;
-    for (int base = 0; base < nf; base += kWarp) {
+    for (int base = 0; base < nf; base += kWarp) {   // wide proxies after them, indices in the free buffer
         int i = base + lane;
         bool v = i < nf && x.px[f0 + i].proxy_id >= 0 && is_wide(x.px[f0 + i]);
         unsigned bal = __ballot_sync(0xffffffffu, v);
@@ -341,49 +350,41 @@ DG Sap sap_build(const Ctx& x, int w, int* hist) {
             int r = nw + __popc(bal & ((1u << lane) - 1u));
             const dbox_proxy_state& p = x.px[f0 + i];
             x.s_sapbox[f0 + nv + r] = make_float4(p.fat_aabb[0], p.fat_aabb[1], p.fat_aabb[2], p.fat_aabb[3]);
-            i1[r] = p.moved ? (i | (int)0x80000000) : i;
+            i0[r] = p.moved ? (i | (int)0x80000000) : i;
         }
         nw += __popc(bal);
     }
     tsync();
-    s.key = k0;
+    s.key = k1;
     s.box = x.s_sapbox + f0;
-    s.idx = i0;
+    s.idx = i1;
     s.n = nv;
-    s.wide = i1;
+    s.wide = i0;
     s.nwide = nw;
     return s;
 }
 
-// fn(b) for every partner b > a of proxy a (overlapping fat AABBs, a or b moved), by sorted rank
+// fn(b) for every partner b > a of proxy a (overlapping fat AABBs, a or b moved)
 template <class F>
 DG void sap_partners(const Sap& s, const AABB& fa, int a, bool amoved, F&& fn) {
-    float lo = s.axis ? fa.lo.y : fa.lo.x, hi = s.axis ? fa.hi.y : fa.hi.x;
-    float qlo = lo - s.ext;
-    qlo -= 1e-3f * (1.0f + babs(qlo));               // round the bound outwards
-    unsigned klo = sort_key(qlo), khi = sort_key(hi);
-    int l = 0, r = s.n;                               // first key >= klo
-    while (l < r) { int m = (l + r) >> 1; if (s.key[m] < klo) l = m + 1; else r = m; }
-    for (int q = l; q < s.n && s.key[q] <= khi; ++q) {
-        int bi = s.idx[q];
+    auto test = [&](int bi, const float4& bb) {
         int b = bi & 0x7fffffff;
-        if (b <= a || (!amoved && bi >= 0)) continue;
-        float4 bb = s.box[q];
+        if (b <= a || (!amoved && bi >= 0)) return;
         AABB fb;
         fb.lo = v2(bb.x, bb.y);
         fb.hi = v2(bb.z, bb.w);
         if (aabb_overlap(fa, fb)) fn(b);
+    };
+    const int cx0 = sap_cell(fa.lo.x, s.ox, s.inv, s.ncx), cy0 = sap_cell(fa.lo.y, s.oy, s.inv, s.ncy);
+    const int cx1 = sap_cell(fa.hi.x, s.ox, s.inv, s.ncx), cy1 = sap_cell(fa.hi.y, s.oy, s.inv, s.ncy);
+    const int xa = cx0 > 0 ? cx0 - 1 : 0;
+    for (int cy = cy0 > 0 ? cy0 - 1 : 0; cy <= cy1; ++cy) {
+        const unsigned klo = (unsigned)(cy * s.ncx + xa), khi = (unsigned)(cy * s.ncx + cx1);
+        int l = 0, r = s.n;                           // first key >= klo
+        while (l < r) { int m = (l + r) >> 1; if (s.key[m] < klo) l = m + 1; else r = m; }
+        for (int q = l; q < s.n && s.key[q] <= khi; ++q) test(s.idx[q], s.box[q]);
     }
-    for (int q = 0; q < s.nwide; ++q) {
-        int bi = s.wide[q];
-        int b = bi & 0x7fffffff;
-        if (b <= a || (!amoved && bi >= 0)) continue;
-        float4 bb = s.box[s.n + q];
-        AABB fb;
-        fb.lo = v2(bb.x, bb.y);
-        fb.hi = v2(bb.z, bb.w);
-        if (aabb_overlap(fa, fb)) fn(b);
-    }
+    for (int q = 0; q < s.nwide; ++q) test(s.wide[q], s.box[s.n + q]);
 }
 
 DG void find_new_contacts(const Ctx& x, int w) {
