@@ -4,11 +4,13 @@
 // Phase map (reference dbox src/dbox/dynamics/b2world.d:367-434):
 //   k_step_begin      FindNewContacts when fixtures were added (b2world.d:372-376)
 //   k_collide         b2ContactManager.Collide per contact (b2contactmanager.d:251-317)
-//   k_collide_finish  contacts woken later in list order, wake flags, stable compaction
-//   k_solve           b2World.Solve: island DFS (b2world.d:930-1095), b2Island.Solve
-//                     (b2island.d:75-280) for all islands at once in reference
-//                     constraint order, SynchronizeFixtures, FindNewContacts
-//   k_toi             b2World.SolveTOI (b2world.d:1127-1452), inv_dt0, ClearForces
+//   k_collide_finish  contacts woken later in list order, wake flags, listener events,
+//                     stable compaction
+//   k_solve_toi       per world: b2World.Solve (solve_world: island search
+//                     b2world.d:930-1095, b2Island.Solve b2island.d:75-280 for all islands
+//                     at once in reference constraint order, SynchronizeFixtures,
+//                     FindNewContacts), then b2World.SolveTOI (toi_world:
+//                     b2world.d:1127-1452), inv_dt0 and ClearForces
 //
 // Gauss-Seidel order: inside an island every constraint reads the velocities
 // (positions) its predecessors in island order wrote.  The kernels assign each
@@ -30,7 +32,7 @@ constexpr int kNoWake = 0x7fffffff;
 constexpr unsigned long long kHashEmpty = 0xffffffffffffffffull;
 
 DG int lane_id() { return threadIdx.x & 31; }
-// phase stamp for the optional per-world profile (slot 0..15), lane 0 only
+// phase stamp for the optional per-world profile (slots 0..11), lane 0 only
 DG void stamp(const Ctx& x, int w, int slot) {
     if (x.prof && (threadIdx.x & 31) == 0) x.prof[kProfSlots * (size_t)w + slot] = clock64();
 }
