@@ -1691,23 +1691,30 @@ DG void sweep_levels(const int* lvl, int maxL, int nItems, const RowT* rows, Row
     // level offsets two levels ahead in registers (plain loads; their latency hides behind a level)
     auto off = [&](int i) { return i <= maxL + 1 ? lvl[i] : nItems; };
     int s = off(1), e = off(2), e2 = off(3);
+    // fast path: the rows of the level are already waited for and the next block is issued;
+    // the bookkeeping runs only when a level crosses a block boundary
+    int t_wait = 0, t_issue = 0;
     for (int L = 1; L <= maxL; ++L) {
         const int e3 = off(L + 3);
-        const int mlo = s / B;
-        issue_upto(mlo + 1);
-        const int mhi = (e - 1) / B;
-        const int mneed = mhi < mlo + 1 ? mhi : mlo + 1;
-        while (waited < mneed) wait_next();
+        if (e > t_wait || s >= t_issue) {
+            const int mlo = s / B;
+            issue_upto(mlo + 1);
+            const int mhi = (e - 1) / B;
+            const int mneed = mhi < mlo + 1 ? mhi : mlo + 1;
+            while (waited < mneed) wait_next();
+            t_wait = (waited + 1) * B;
+            t_issue = issued < nblk - 1 ? issued * B : 0x7fffffff;
+        }
         // one position per lane; a level wider than the warp takes the rest in a uniform branch
         // (a loop whose trip count differs between lanes costs hundreds of cycles per level)
         if (s + lane < e) {
-            const int idx = s + lane, m = idx / B;
-            f(slots[(m & 1) * B + (idx - m * B)], idx);
+            const int idx = s + lane;
+            f(slots[idx % (2 * B)], idx);
         }
         if (e - s > kWarp) {
+            const int mlo = s / B;
             for (int idx = s + lane + kWarp; idx < e; idx += kWarp) {
-                const int m = idx / B;
-                if (m <= mlo + 1) f(slots[(m & 1) * B + (idx - m * B)], idx);
+                if (idx / B <= mlo + 1) f(slots[idx % (2 * B)], idx);
                 else f(load_row(rows + idx), idx);
             }
         }
