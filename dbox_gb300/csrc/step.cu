@@ -969,6 +969,70 @@ DG void solve_velocity(VC& vc, SB sb) {                                // :492-7
     sb.set_v(vc.bodyB, vB, wB);
 }
 
+// solve_velocity for a contact with two points, with no branch inside: both friction points,
+// then the block solver's four cases side by side; when no case holds, the velocities and
+// impulses keep their values through selects instead of a skipped branch.  The same
+// operations in the same order as solve_velocity, so the same bits; a branch costs tens of
+// cycles on the dependent chain between levels, a select a few.
+DG void solve_velocity_two(VC& vc, SB sb) {
+    float mA = vc.invMassA, iA = vc.invIA, mB = vc.invMassB, iB = vc.invIB;
+    float2 vA = sb.v(vc.bodyA), vB = sb.v(vc.bodyB);
+    float wA = sb.w(vc.bodyA), wB = sb.w(vc.bodyB);
+    float2 normal = vc.normal;
+    float2 tangent = cross(normal, 1.0f);
+    float friction = vc.friction;
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        VPoint& p = vc.p[j];
+        float2 dv = ((vB + cross(wB, p.rB)) - vA) - cross(wA, p.rA);
+        float vt = dot(dv, tangent) - vc.tangentSpeed;
+        float lambda = p.tangentMass * (-vt);
+        float maxFriction = friction * p.normalImpulse;
+        float newImpulse = bclamp(p.tangentImpulse + lambda, -maxFriction, maxFriction);
+        lambda = newImpulse - p.tangentImpulse;
+        p.tangentImpulse = newImpulse;
+        float2 P = lambda * tangent;
+        vA -= mA * P;
+        wA -= iA * cross(p.rA, P);
+        vB += mB * P;
+        wB += iB * cross(p.rB, P);
+    }
+    VPoint& cp1 = vc.p[0];
+    VPoint& cp2 = vc.p[1];
+    float2 a = v2(cp1.normalImpulse, cp2.normalImpulse);
+    float2 dv1 = ((vB + cross(wB, cp1.rB)) - vA) - cross(wA, cp1.rA);
+    float2 dv2 = ((vB + cross(wB, cp2.rB)) - vA) - cross(wA, cp2.rA);
+    float vn1 = dot(dv1, normal);
+    float vn2 = dot(dv2, normal);
+    float2 b;
+    b.x = vn1 - cp1.velocityBias;
+    b.y = vn2 - cp2.velocityBias;
+    float2 Ka = v2(vc.K[0] * a.x + vc.K[2] * a.y, vc.K[1] * a.x + vc.K[3] * a.y);
+    b -= Ka;
+    float2 x1 = -v2(vc.NM[0] * b.x + vc.NM[2] * b.y, vc.NM[1] * b.x + vc.NM[3] * b.y);
+    bool c1 = x1.x >= 0.0f && x1.y >= 0.0f;
+    float x2 = -cp1.normalMass * b.x;
+    bool c2 = x2 >= 0.0f && vc.K[1] * x2 + b.y >= 0.0f;
+    float x3 = -cp2.normalMass * b.y;
+    bool c3 = x3 >= 0.0f && vc.K[2] * x3 + b.x >= 0.0f;
+    bool c4 = b.x >= 0.0f && b.y >= 0.0f;
+    float2 xx = c1 ? x1 : (c2 ? v2(x2, 0.0f) : (c3 ? v2(0.0f, x3) : v2(0.0f, 0.0f)));
+    const bool any = c1 || c2 || c3 || c4;
+    float2 vA2 = vA, vB2 = vB;
+    float wA2 = wA, wB2 = wB;
+    apply_block(vA2, wA2, vB2, wB2, mA, iA, mB, iB, cp1, cp2, normal, xx - a);
+    vA.x = any ? vA2.x : vA.x;
+    vA.y = any ? vA2.y : vA.y;
+    wA = any ? wA2 : wA;
+    vB.x = any ? vB2.x : vB.x;
+    vB.y = any ? vB2.y : vB.y;
+    wB = any ? wB2 : wB;
+    cp1.normalImpulse = any ? xx.x : a.x;
+    cp2.normalImpulse = any ? xx.y : a.y;
+    sb.set_v(vc.bodyA, vA, wA);
+    sb.set_v(vc.bodyB, vB, wB);
+}
+
 // ---- learned warm start: the 32 input features of a contact (after
 // InitializeVelocityConstraints, before the warm start), in this order: normal (2); per point
 // (0 then 1, zeros when absent): rA (2), rB (2), relative normal and tangent velocity, normal
@@ -1146,6 +1210,70 @@ DG float solve_position(const PC& pc, SB sb, bool toi, int toiA, int toiB) {
     sb.set_c(pc.bodyA, cA, aA);
     sb.set_c(pc.bodyB, cB, aB);
     return minSep;
+}
+
+// sin and cos on the binary32 path of dbox_sincosf alone (|x| <= 1024; zero handled the same way)
+DG Rot rot_near(float x) {
+    Rot q;
+    dbox_trig::sincos_f32(x, &q.s, &q.c);
+    if (x == 0.0f) { q.s = x; q.c = 1.0f; }
+    return q;
+}
+
+// solve_position (non-TOI) for a polygon contact (e_faceA / e_faceB) with two points, with
+// the rotations on the binary32 path only: one range test for the row replaces a rare-case
+// branch inside each of its four rotations.  Returns false, with the bodies untouched, when
+// an angle was outside |a| <= 1024 (or not finite); the caller then runs solve_position,
+// which gives the row's true result.  Otherwise the same operations in the same order as
+// solve_position, so the same bits.
+DG bool solve_position_two(const PC& pc, SB sb, float& minSepOut) {
+    const float mA = pc.invMassA, iA = pc.invIA, mB = pc.invMassB, iB = pc.invIB;
+    float2 cA = sb.c(pc.bodyA), cB = sb.c(pc.bodyB);
+    float aA = sb.a(pc.bodyA), aB = sb.a(pc.bodyB);
+    const bool faceA = pc.type == kManifoldFaceA;
+    float minSep = 0.0f;
+    bool near = true;
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        near = near && fabsf(aA) <= 1024.0f && fabsf(aB) <= 1024.0f;
+        Xf xfA, xfB;
+        xfA.q = rot_near(aA);
+        xfB.q = rot_near(aB);
+        xfA.p = cA - mul(xfA.q, pc.lcA);
+        xfB.p = cB - mul(xfB.q, pc.lcB);
+        Xf xfN = faceA ? xfA : xfB, xfC = faceA ? xfB : xfA;
+        float2 normal = mul(xfN.q, pc.localNormal);
+        float2 planePoint = mul(xfN, pc.localPoint);
+        float2 clipPoint = mul(xfC, pc.localPoints[j]);
+        float separation = (dot(clipPoint - planePoint, normal) - pc.radiusA) - pc.radiusB;
+        float2 point = clipPoint;
+        if (!faceA) normal = -normal;
+        float2 rA = point - cA;
+        float2 rB = point - cB;
+        minSep = bmin(minSep, separation);
+        float C = bclamp(kBaumgarte * (separation + kLinearSlop), -kMaxLinearCorrection, 0.0f);
+        float rnA = cross(rA, normal);
+        float rnB = cross(rB, normal);
+        float K = ((mA + mB) + (iA * rnA) * rnA) + (iB * rnB) * rnB;
+        float impulse = K > 0.0f ? fdiv(-C, K) : 0.0f;
+        float2 P = impulse * normal;
+        cA -= mA * P;
+        aA -= iA * cross(rA, P);
+        cB += mB * P;
+        aB += iB * cross(rB, P);
+    }
+    if (!near) return false;
+    sb.set_c(pc.bodyA, cA, aA);
+    sb.set_c(pc.bodyB, cB, aB);
+    minSepOut = minSep;
+    return true;
+}
+
+// one position row of SolvePositionConstraints: the two-point polygon path when it applies
+DG float solve_position_row(const PC& pc, SB sb) {
+    float ms;
+    if (pc.pointCount == 2 && pc.type != kManifoldCircles && solve_position_two(pc, sb, ms)) return ms;
+    return solve_position(pc, sb, false, -1, -1);
 }
 
 // ------------------------------------------------------------ revolute joint (joints/b2revolutejoint.d:319-636)
@@ -2100,7 +2228,19 @@ DG void solve_world(const Ctx& x, int w, float* sbp, bool sb_smem, float* stage_
     }
     stamp(x, w, 5);
     // velocity iterations (b2island.d:153-161)
+    auto contact_velocity = [&](const VRow& r, int idx) {
+        VC vc = unpack_v(r);
+        if (vc.pointCount == 2) solve_velocity_two(vc, sb);
+        else solve_velocity(vc, sb);
+        vrow[idx].imp = make_float4(vc.p[0].normalImpulse, vc.p[0].tangentImpulse, vc.p[1].normalImpulse,
+                                    vc.p[1].tangentImpulse);
+    };
     for (int it = 0; it < x.vel_iters; ++it) {
+        if (njI == 0 && !(it == 0 && x.ws_mode == 2)) {
+            // contacts only, no learned first iteration: the row needs no kind test
+            sweep_levels(x.s_lvl_v + kx, maxLv, nItems, vrow, ring, contact_velocity);
+            continue;
+        }
         sweep_levels(x.s_lvl_v + kx, maxLv, nItems, vrow, ring, [&](const VRow& r, int idx) {
             if (r.ids.w >= 0) {
                 if (it == 0 && (r.ids.z & 0x100)) {
@@ -2109,10 +2249,7 @@ DG void solve_world(const Ctx& x, int w, float* sbp, bool sb_smem, float* stage_
                     vrow[idx].imp = im;
                     return;
                 }
-                VC vc = unpack_v(r);
-                solve_velocity(vc, sb);
-                vrow[idx].imp = make_float4(vc.p[0].normalImpulse, vc.p[0].tangentImpulse, vc.p[1].normalImpulse,
-                                            vc.p[1].tangentImpulse);
+                contact_velocity(r, idx);
             } else {
                 joint_solve_velocity(x, -r.ids.w - 1, b0, sb);
             }
@@ -2207,7 +2344,7 @@ DG void solve_world(const Ctx& x, int w, float* sbp, bool sb_smem, float* stage_
             int is = r.ids.w;
             if (iflags[is] & 1) return;
             if (r.ids.z >= 0) {
-                float ms = solve_position(unpack_p(r), sb, false, -1, -1);
+                float ms = solve_position_row(unpack_p(r), sb);
                 atomicMin(&iminsep[is], fkey(ms));
             } else if (!joint_solve_position(x, -r.ids.z - 1, b0, sb)) {
                 atomicOr(&iflags[is], 4);
