@@ -219,6 +219,12 @@ DBOX_TRIG_HD void sincos_f32(float x, float* s_out, float* c_out) {
     *c_out = c;
 }
 
+#ifdef __CUDACC__
+// the binary64 path as one out-of-line device function: it runs for |x| > 1024 only, and a
+// copy inlined at every rotation would fill the instruction cache with code that never runs
+static __device__ __noinline__ void sincos_f64_cold(float x, float* s_out, float* c_out) { sincos_f64(x, s_out, c_out); }
+#endif
+
 }  // namespace dbox_trig
 
 // sin and cos of a binary32 angle (b2Rot.Set): identical bits on the host and the device.
@@ -231,7 +237,7 @@ DBOX_TRIG_HD void dbox_sincosf(float x, float* s_out, float* c_out) {
     float ax = fabsf(x);
     if (!(ax <= 1024.0f)) {
         if (ax == ax && ax != __int_as_float(0x7f800000)) {
-            dbox_trig::sincos_f64(x, &s, &c);
+            dbox_trig::sincos_f64_cold(x, &s, &c);
         } else {
             s = x - x;
             c = s;

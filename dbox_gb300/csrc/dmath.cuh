@@ -557,7 +557,10 @@ struct Simplex {
 };
 
 // b2Distance (b2distance.d:185-350); returns distance, witness points via out params.
-DG float gjk_distance(SimplexCache& cache, const Proxy& pA, const Xf& xA, const Proxy& pB, const Xf& xB,
+// Out of line (like the separation-function members and time_of_impact below): each is
+// large and called from several places, and inlined copies crowd the instruction cache of
+// the fused solve kernel, whose warps run different phases side by side.
+static __device__ __noinline__ float gjk_distance(SimplexCache& cache, const Proxy& pA, const Xf& xA, const Proxy& pB, const Xf& xB,
                       bool useRadii, float2* outA, float2* outB) {
     Simplex simplex;
     simplex.read_cache(cache, pA, xA, pB, xB);
@@ -627,7 +630,7 @@ struct SepFn {
     Sweep sA, sB;
     int type;
     float2 localPoint, axis;
-    DG void init(const SimplexCache& cache, const Proxy& a, const Sweep& sa, const Proxy& b, const Sweep& sb, float t1) {
+    __device__ __noinline__ void init(const SimplexCache& cache, const Proxy& a, const Sweep& sa, const Proxy& b, const Sweep& sb, float t1) {
         pA = a; pB = b;                                                 // b2timeofimpact.d:323-407
         int count = cache.count;
         sA = sa; sB = sb;
@@ -664,7 +667,7 @@ struct SepFn {
             if (s < 0.0f) axis = -axis;
         }
     }
-    DG float find_min(int* ia, int* ib, float t) const {                // b2timeofimpact.d:410-474
+    __device__ __noinline__ float find_min(int* ia, int* ib, float t) const {                // b2timeofimpact.d:410-474
         Xf xfA, xfB;
         sweep_xf(sA, &xfA, t);
         sweep_xf(sB, &xfB, t);
@@ -694,7 +697,7 @@ struct SepFn {
             return dot(pointA - pointB, normal);
         }
     }
-    DG float evaluate(int ia, int ib, float t) const {                  // b2timeofimpact.d:477-519
+    __device__ __noinline__ float evaluate(int ia, int ib, float t) const {                  // b2timeofimpact.d:477-519
         Xf xfA, xfB;
         sweep_xf(sA, &xfA, t);
         sweep_xf(sB, &xfB, t);
@@ -717,7 +720,7 @@ struct SepFn {
 };
 
 // b2TimeOfImpact (b2timeofimpact.d:67-302) with tMax = 1.  Returns the state; *t receives output.t.
-DG int time_of_impact(const Proxy& pA, const Proxy& pB, Sweep sweepA, Sweep sweepB, float tMax, float* tOut) {
+static __device__ __noinline__ int time_of_impact(const Proxy& pA, const Proxy& pB, Sweep sweepA, Sweep sweepB, float tMax, float* tOut) {
     int state = kToiUnknown;
     float tres = tMax;
     sweep_normalize(sweepA);

@@ -389,7 +389,7 @@ DG void sap_partners(const Sap& s, const AABB& fa, int a, bool amoved, F&& fn) {
     for (int q = 0; q < s.nwide; ++q) test(s.wide[q], s.box[s.n + q]);
 }
 
-DG void find_new_contacts(const Ctx& x, int w) {
+__device__ __noinline__ void find_new_contacts(const Ctx& x, int w) {
     const WorldInfo& wi = x.wi[w];
     WorldDyn& wd = x.wd[w];
     int lane = lane_id();
@@ -547,7 +547,7 @@ DG void find_new_contacts(const Ctx& x, int w) {
 }
 
 // ------------------------------------------------------------ kernels
-__global__ void k_step_begin(Ctx x) {
+__global__ void k_step_begin(const __grid_constant__ Ctx x) {
     int w = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
     if (w >= x.W) return;
     WorldDyn& wd = x.wd[w];
@@ -897,11 +897,17 @@ DG void apply_block(float2& vA, float& wA, float2& vB, float& wB, float mA, floa
     wB += iB * (cross(cp1.rB, P1) + cross(cp2.rB, P2));
 }
 
-DG void solve_velocity(VC& vc, SB sb) {                                // :492-772
+// The velocities of the contact's two bodies in registers: loaded before a row picks its
+// path, so the loads are in flight while the row's kind is tested.
+struct BodyVel { float2 vA, vB; float wA, wB; };
+DG BodyVel load_vel(SB sb, int a, int b) { BodyVel q; q.vA = sb.v(a); q.wA = sb.w(a); q.vB = sb.v(b); q.wB = sb.w(b); return q; }
+DG void store_vel(SB sb, int a, int b, const BodyVel& q) { sb.set_v(a, q.vA, q.wA); sb.set_v(b, q.vB, q.wB); }
+
+DG void solve_velocity(VC& vc, BodyVel& q) {                           // :492-772
     float mA = vc.invMassA, iA = vc.invIA, mB = vc.invMassB, iB = vc.invIB;
     int pointCount = vc.pointCount;
-    float2 vA = sb.v(vc.bodyA), vB = sb.v(vc.bodyB);
-    float wA = sb.w(vc.bodyA), wB = sb.w(vc.bodyB);
+    float2 vA = q.vA, vB = q.vB;
+    float wA = q.wA, wB = q.wB;
     float2 normal = vc.normal;
     float2 tangent = cross(normal, 1.0f);
     float friction = vc.friction;
@@ -965,8 +971,12 @@ DG void solve_velocity(VC& vc, SB sb) {                                // :492-7
             cp2.normalImpulse = xx.y;
         }
     }
-    sb.set_v(vc.bodyA, vA, wA);
-    sb.set_v(vc.bodyB, vB, wB);
+    q.vA = vA; q.wA = wA; q.vB = vB; q.wB = wB;
+}
+DG void solve_velocity(VC& vc, SB sb) {
+    BodyVel q = load_vel(sb, vc.bodyA, vc.bodyB);
+    solve_velocity(vc, q);
+    store_vel(sb, vc.bodyA, vc.bodyB, q);
 }
 
 // solve_velocity for a contact with two points, with no branch inside: both friction points,
@@ -974,10 +984,10 @@ DG void solve_velocity(VC& vc, SB sb) {                                // :492-7
 // impulses keep their values through selects instead of a skipped branch.  The same
 // operations in the same order as solve_velocity, so the same bits; a branch costs tens of
 // cycles on the dependent chain between levels, a select a few.
-DG void solve_velocity_two(VC& vc, SB sb) {
+DG void solve_velocity_two(VC& vc, BodyVel& q) {
     float mA = vc.invMassA, iA = vc.invIA, mB = vc.invMassB, iB = vc.invIB;
-    float2 vA = sb.v(vc.bodyA), vB = sb.v(vc.bodyB);
-    float wA = sb.w(vc.bodyA), wB = sb.w(vc.bodyB);
+    float2 vA = q.vA, vB = q.vB;
+    float wA = q.wA, wB = q.wB;
     float2 normal = vc.normal;
     float2 tangent = cross(normal, 1.0f);
     float friction = vc.friction;
@@ -1029,8 +1039,7 @@ DG void solve_velocity_two(VC& vc, SB sb) {
     wB = any ? wB2 : wB;
     cp1.normalImpulse = any ? xx.x : a.x;
     cp2.normalImpulse = any ? xx.y : a.y;
-    sb.set_v(vc.bodyA, vA, wA);
-    sb.set_v(vc.bodyB, vB, wB);
+    q.vA = vA; q.wA = wA; q.vB = vB; q.wB = wB;
 }
 
 // ---- learned warm start: the 32 input features of a contact (after
@@ -1226,10 +1235,10 @@ DG Rot rot_near(float x) {
 // an angle was outside |a| <= 1024 (or not finite); the caller then runs solve_position,
 // which gives the row's true result.  Otherwise the same operations in the same order as
 // solve_position, so the same bits.
-DG bool solve_position_two(const PC& pc, SB sb, float& minSepOut) {
+DG bool solve_position_two(const PC& pc, float2& cA_io, float& aA_io, float2& cB_io, float& aB_io, float& minSepOut) {
     const float mA = pc.invMassA, iA = pc.invIA, mB = pc.invMassB, iB = pc.invIB;
-    float2 cA = sb.c(pc.bodyA), cB = sb.c(pc.bodyB);
-    float aA = sb.a(pc.bodyA), aB = sb.a(pc.bodyB);
+    float2 cA = cA_io, cB = cB_io;
+    float aA = aA_io, aB = aB_io;
     const bool faceA = pc.type == kManifoldFaceA;
     float minSep = 0.0f;
     bool near = true;
@@ -1262,17 +1271,22 @@ DG bool solve_position_two(const PC& pc, SB sb, float& minSepOut) {
         cB += mB * P;
         aB += iB * cross(rB, P);
     }
-    if (!near) return false;
-    sb.set_c(pc.bodyA, cA, aA);
-    sb.set_c(pc.bodyB, cB, aB);
+    cA_io = cA; aA_io = aA; cB_io = cB; aB_io = aB;
     minSepOut = minSep;
-    return true;
+    return near;
 }
 
 // one position row of SolvePositionConstraints: the two-point polygon path when it applies
+// (the bodies' positions are loaded before the row's kind is tested)
 DG float solve_position_row(const PC& pc, SB sb) {
+    float2 cA = sb.c(pc.bodyA), cB = sb.c(pc.bodyB);
+    float aA = sb.a(pc.bodyA), aB = sb.a(pc.bodyB);
     float ms;
-    if (pc.pointCount == 2 && pc.type != kManifoldCircles && solve_position_two(pc, sb, ms)) return ms;
+    if (pc.pointCount == 2 && pc.type != kManifoldCircles && solve_position_two(pc, cA, aA, cB, aB, ms)) {
+        sb.set_c(pc.bodyA, cA, aA);
+        sb.set_c(pc.bodyB, cB, aB);
+        return ms;
+    }
     return solve_position(pc, sb, false, -1, -1);
 }
 
@@ -1779,16 +1793,20 @@ struct RowRing {
 // One sweep over levels 1..maxL of a schedule whose rows are stored in schedule order:
 // f(row, idx) for every position of a level, levels in order, positions of a level spread
 // over the lanes.  Rows arrive by blocks: block m+1 is copied by one bulk copy as soon as
-// the levels reach block m, so a level reads its rows from shared memory and the copies
-// stay off the dependent chain between levels; rows of a level wider than the two
-// resident blocks are read from global memory.  A row of a later position is never
-// written by an earlier level, and the rows' global writes of the previous sweep are
-// ordered before the copies by the proxy fence at the start.
+// the sweep reaches block m, so a level reads its rows from shared memory and the copies
+// stay off the dependent chain between levels.  A level wider than the warp runs as chunks
+// of 32 positions with a warp sync between them (positions of a level are independent, so
+// any split keeps the result); a chunk spans at most two consecutive blocks, which are
+// both resident.  A row of a later position is never written by an earlier level, and the
+// rows' global writes of the previous sweep are ordered before the copies by the proxy
+// fence at the start.  f has one call site, which keeps the loop small in the instruction
+// cache.
 template <class RowT, class F>
 DG void sweep_levels(const int* lvl, int maxL, int nItems, const RowT* rows, RowRing& ring, F&& f) {
     if (maxL < 1) return;
     constexpr int B = (int)(4608 / sizeof(RowT));
     static_assert(4608 % sizeof(RowT) == 0 && sizeof(RowT) % 16 == 0, "rows tile a half of the ring");
+    static_assert(B >= kWarp, "a chunk spans at most two blocks");
     const int lane = lane_id();
     RowT* slots = reinterpret_cast<RowT*>(ring.base);
     const int nblk = (nItems + B - 1) / B;
@@ -1816,40 +1834,33 @@ DG void sweep_levels(const int* lvl, int maxL, int nItems, const RowT* rows, Row
     fence_async_global();                                // this lane's row writes before the copies
     tsync();
     issue_upto(1);
-    // level offsets two levels ahead in registers (plain loads; their latency hides behind a level)
+    // level ends two levels ahead in registers (plain loads; their latency hides behind a level)
     auto off = [&](int i) { return i <= maxL + 1 ? lvl[i] : nItems; };
     int s = off(1), e = off(2), e2 = off(3);
-    // fast path: the rows of the level are already waited for and the next block is issued;
-    // the bookkeeping runs only when a level crosses a block boundary
+    // the bookkeeping runs only when a chunk reaches a block that is not yet waited for or
+    // passes the point where the next block is issued
     int t_wait = 0, t_issue = 0;
-    for (int L = 1; L <= maxL; ++L) {
+    for (int L = 1; L <= maxL;) {
         const int e3 = off(L + 3);
-        if (e > t_wait || s >= t_issue) {
+        const int ce = e - s > kWarp ? s + kWarp : e;    // end of this chunk of the level
+        if (ce > t_wait || s >= t_issue) {
             const int mlo = s / B;
             issue_upto(mlo + 1);
-            const int mhi = (e - 1) / B;
-            const int mneed = mhi < mlo + 1 ? mhi : mlo + 1;
+            const int mneed = (ce - 1) / B;
             while (waited < mneed) wait_next();
             t_wait = (waited + 1) * B;
             t_issue = issued < nblk - 1 ? issued * B : 0x7fffffff;
         }
-        // one position per lane; a level wider than the warp takes the rest in a uniform branch
-        // (a loop whose trip count differs between lanes costs hundreds of cycles per level)
-        if (s + lane < e) {
+        if (s + lane < ce) {
             const int idx = s + lane;
             f(slots[idx % (2 * B)], idx);
         }
-        if (e - s > kWarp) {
-            const int mlo = s / B;
-            for (int idx = s + lane + kWarp; idx < e; idx += kWarp) {
-                if (idx / B <= mlo + 1) f(slots[idx % (2 * B)], idx);
-                else f(load_row(rows + idx), idx);
-            }
-        }
         tsync();
-        s = e;
-        e = e2;
-        e2 = e3;
+        const bool next_level = ce == e;
+        s = ce;
+        L += next_level;
+        e = next_level ? e2 : e;
+        e2 = next_level ? e3 : e2;
     }
     while (waited < issued) wait_next();
 }
@@ -2230,8 +2241,10 @@ DG void solve_world(const Ctx& x, int w, float* sbp, bool sb_smem, float* stage_
     // velocity iterations (b2island.d:153-161)
     auto contact_velocity = [&](const VRow& r, int idx) {
         VC vc = unpack_v(r);
-        if (vc.pointCount == 2) solve_velocity_two(vc, sb);
-        else solve_velocity(vc, sb);
+        BodyVel q = load_vel(sb, vc.bodyA, vc.bodyB);
+        if (vc.pointCount == 2) solve_velocity_two(vc, q);
+        else solve_velocity(vc, q);
+        store_vel(sb, vc.bodyA, vc.bodyB, q);
         vrow[idx].imp = make_float4(vc.p[0].normalImpulse, vc.p[0].tangentImpulse, vc.p[1].normalImpulse,
                                     vc.p[1].tangentImpulse);
     };
@@ -2501,8 +2514,9 @@ DG int toi_collect(const Ctx& x, int c0, int b0, int k0, int k1, int* list, int 
     return cnt;
 }
 
-// b2Contact.Update inside the TOI loop: wakes are applied immediately
-DG void toi_update(const Ctx& x, dbox_contact_state& c, unsigned* evt = nullptr) {
+// b2Contact.Update inside the TOI loop: wakes are applied immediately (out of line: TOI events
+// are rare, and the narrowphase inlined here would double the kernel's collision code)
+__device__ __noinline__ void toi_update(const Ctx& x, dbox_contact_state& c, unsigned* evt = nullptr) {
     if (contact_update(x, c, evt)) {
         b_set_awake(x.bs[x.fx[c.fixture_a].body], true);
         b_set_awake(x.bs[x.fx[c.fixture_b].body], true);
@@ -2511,7 +2525,7 @@ DG void toi_update(const Ctx& x, dbox_contact_state& c, unsigned* evt = nullptr)
 
 // b2Island.SolveTOI (b2island.d:282-416) on the sub-island in s_isl_body (world-local)
 // and s_isl_contact; one lane.  sb holds the island bodies' state for the solve.
-DG void solve_toi_island(const Ctx& x, int w, const WorldInfo& wi, SB sb, int nbI, int ncI, int toiA, int toiB,
+__device__ __noinline__ void solve_toi_island(const Ctx& x, int w, const WorldInfo& wi, SB sb, int nbI, int ncI, int toiA, int toiB,
                          float subDt) {
     const int b0 = wi.body_start, c0 = wi.contact_start;
     VRow* tv = x.tvr + (size_t)kMaxTOIContacts * w;
@@ -2856,7 +2870,7 @@ DG void toi_world(const Ctx& x, int w, float* sbp) {
 // from its island solve straight to its TOI events, so a world that is slow in one phase
 // overlaps with worlds that are slow in the other.  Warp slots and their shared memory
 // (row staging, solver body rows) come from the host's packing of worlds into blocks.
-__global__ void __launch_bounds__(kSolveWarps * 32, 3) k_solve_toi(Ctx x) {
+__global__ void __launch_bounds__(kSolveWarps * 32, 3) k_solve_toi(const __grid_constant__ Ctx x) {
     extern __shared__ float smem_sb[];
     const int slot = blockIdx.x * x.solve_wpb + (threadIdx.x >> 5);
     const int w = x.solve_world[slot];
@@ -2875,6 +2889,11 @@ __global__ void __launch_bounds__(kSolveWarps * 32, 3) k_solve_toi(Ctx x) {
         x.prof[kProfSlots * (size_t)w + 25] = g0;
         x.prof[kProfSlots * (size_t)w + 26] = g1;
         x.prof[kProfSlots * (size_t)w + 27] = slot;
+        unsigned smid, warpid;
+        asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+        asm volatile("mov.u32 %0, %%warpid;" : "=r"(warpid));
+        x.prof[kProfSlots * (size_t)w + 28] = smid;
+        x.prof[kProfSlots * (size_t)w + 29] = warpid;
     }
 }
 

@@ -276,7 +276,7 @@ int32_t dbox_world_get_transforms(dbox_world* w, float* xya);
  * SolveTOI kernel, 17 its TOI events, 18..24 its cycles per part of the event loop (sweep
  * advance, TOI, minimum, event contact, neighbours, sub-step solve, fixture sync and pairs),
  * 25..26 the global timer (ns) when the world's warp started and ended the solve + SolveTOI
- * kernel, 27 its warp slot. */
+ * kernel, 27 its warp slot, 28..29 the SM and the warp's slot on the SM (%smid, %warpid). */
 int32_t dbox_world_set_phase_profile(dbox_world* w, int32_t enable);
 int32_t dbox_world_get_phase_profile(dbox_world* w, unsigned long long* out);
 
