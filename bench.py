@@ -210,14 +210,16 @@ def gpu_leg(args, rank, world_size):
         wt = dbox_gb300.World(worlds)
         wt.step(DT, VI, PI, steps=args.warmup, graph=True)
         mapping = wt.autotune(steps=3, dt=DT, vel_iters=VI, pos_iters=PI)
+        costs = wt.world_costs()
         wt.close()
     w = dbox_gb300.World(worlds)
     # twin handle for the end-to-end leg: the same scenes and warm-up, so it replays exactly
     # the steps the device-timed leg measures
     we = dbox_gb300.World(worlds)
     if mapping:
-        w.set_mapping(*mapping)
-        we.set_mapping(*mapping)
+        for h in (w, we):
+            h.set_world_costs(costs)
+            h.apply_mapping(mapping)
     w.step(DT, VI, PI, steps=args.warmup, graph=True)
     we.step(DT, VI, PI, steps=args.warmup, graph=True)
     w.sync()
@@ -275,8 +277,10 @@ def gpu_leg(args, rank, world_size):
         "data": "synthetic seeded scenes (numpy PCG64 seed %d)" % args.seed,
         "config": dict(cfg, dt=DT, velocity_iterations=VI, position_iterations=PI, dynamic_bodies=nbody_dyn,
                        parallelism="replicas: one batch of worlds per GPU",
-                       mapping=({"warps_per_block": mapping[0], "body_budget": mapping[1],
-                                 "isolated_largest_worlds": mapping[2], "chosen_by": "autotuner"}
+                       mapping=(({"queue": 1, "heavy_worlds_one_per_subpartition": mapping[4],
+                                  "exclusive": mapping[5], "chosen_by": "autotuner"} if mapping[3] else
+                                 {"warps_per_block": mapping[0], "body_budget": mapping[1],
+                                  "isolated_largest_worlds": mapping[2], "chosen_by": "autotuner"})
                                 if mapping else "default"),
                        l2="working set (bodies, contacts, constraint rows) larger than the 129 MB L2",
                        timing="one CUDA graph of K steps with per-phase CUDA events"),

@@ -90,6 +90,9 @@ def lib():
     L.dbox_world_set_mapping.argtypes = [vp, i32, i32]
     L.dbox_world_set_mapping_isolated.argtypes = [vp, i32, i32, i32]
     L.dbox_world_autotune.argtypes = [vp, f32, i32, i32, i32, vp]
+    L.dbox_world_set_mapping_queue.argtypes = [vp, i32, i32, i32]
+    L.dbox_world_set_world_costs.argtypes = [vp, vp]
+    L.dbox_world_get_world_costs.argtypes = [vp, vp]
     L.dbox_world_get_quality.argtypes = [vp, vp]
     _lib = L
     return L
@@ -308,14 +311,47 @@ class World:
         _check(lib().dbox_world_set_mapping_isolated(self.h, warps_per_block, body_budget, isolate),
                "dbox_world_set_mapping")
 
+    def set_mapping_queue(self, heavy=0, exclusive=False, blocks_per_sm=0):
+        """Queue mapping: a resident wave of warps takes worlds costliest first; the `heavy`
+        costliest go one per SM sub-partition (alone there with `exclusive`); blocks_per_sm
+        limits the resident four-warp blocks per SM (0: as many as fit)."""
+        _check(lib().dbox_world_set_mapping_queue(self.h, heavy, 1 if exclusive else 0, blocks_per_sm),
+               "dbox_world_set_mapping_queue")
+
+    def set_world_costs(self, cost=None):
+        """Per-world cost estimates for the queue order (None: body counts)."""
+        if cost is None:
+            _check(lib().dbox_world_set_world_costs(self.h, None), "dbox_world_set_world_costs")
+            return
+        c = np.ascontiguousarray(cost, np.float32)
+        assert c.shape == (self.n_worlds,)
+        _check(lib().dbox_world_set_world_costs(self.h, abi.ptr(c)), "dbox_world_set_world_costs")
+
+    def world_costs(self):
+        out = np.zeros(self.n_worlds, np.float32)
+        _check(lib().dbox_world_get_world_costs(self.h, abi.ptr(out)), "dbox_world_get_world_costs")
+        return out
+
+    def apply_mapping(self, choice):
+        """Apply a mapping returned by autotune()."""
+        if choice[3]:
+            self.set_mapping_queue(choice[4], bool(choice[5]))
+        else:
+            self.set_mapping(choice[0], choice[1], choice[2])
+
+    @staticmethod
+    def autotune_steps(steps):
+        """Steps the worlds advance during autotune(steps)."""
+        return 1 + 20 * (steps + 1)
+
     def autotune(self, steps=3, dt=1.0 / 60.0, vel_iters=8, pos_iters=3):
-        """Time the candidate world-to-block mappings on the live worlds and keep the fastest;
-        returns (warps per block, body budget, isolated largest worlds).  The worlds advance by
-        14 * (steps + 1) steps."""
-        out = np.zeros(3, np.int32)
+        """Time the candidate mappings of worlds onto the solve kernel on the live worlds and
+        keep the fastest; returns (warps per block, body budget, isolated largest worlds, queue,
+        heavy, exclusive).  The worlds advance by autotune_steps(steps) steps."""
+        out = np.zeros(6, np.int32)
         _check(lib().dbox_world_autotune(self.h, ctypes.c_float(dt), vel_iters, pos_iters, steps, abi.ptr(out)),
                "dbox_world_autotune")
-        return int(out[0]), int(out[1]), int(out[2])
+        return tuple(int(v) for v in out)
 
     def set_measure(self, on=True):
         _check(lib().dbox_world_set_measure(self.h, 1 if on else 0), "dbox_world_set_measure")

@@ -88,6 +88,7 @@ struct dbox_world {
     int warm = 1, continuous = 1, substep = 0, allow_sleep = 1, autoclear = 1;
     dbox_world_caps caps;
     bool on_device = false;     // device holds the authoritative dynamic state
+    bool mirrors_fresh = false; // host mirrors equal the device state (no device work since the last download)
     bool dirty = true;          // host structure changed since the last upload
     cudaStream_t stream = nullptr;
     // device arrays
@@ -114,6 +115,15 @@ struct dbox_world {
     int solve_wpb = dg::kSolveWarps;    // warp slots (worlds) per block of the solve kernel
     int solve_budget = 0;               // body budget per block (0: chosen from the worlds)
     int solve_isolate = 0;              // this many largest worlds get a block of their own
+    // world-queue mapping: a resident wave of warps takes worlds costliest first
+    int solve_queue_mode = 0;           // 1: queue mapping, 0: packing into blocks
+    int solve_heavy = 0;                // costliest worlds spread one per SM sub-partition
+    int solve_exclusive = 0;            // their sub-partitions take no other world meanwhile
+    int solve_bps = 0;                  // resident blocks per SM of the queue mapping (0: as many as fit)
+    int solve_cap = 0;
+    int nsm = 0;
+    DBuf<int> d_solve_order, d_solve_queue;
+    std::vector<float> world_cost;      // per world, for the queue order (empty: body counts)
     DBuf<dg::SweepSnap> d_snap;
     DBuf<float> d_io;           // staging for bulk force upload / transform readback (3 floats per body)
     DBuf<int2> s_cbody, s_adj_items, s_isl_pair;
@@ -172,6 +182,7 @@ void free_device(dbox_world* w) {
     w->s_isl_minsep.free(); w->s_isl_sleep.free();
     w->d_vr.free(); w->d_tvr.free(); w->d_pr.free(); w->d_tpr.free(); w->d_snap.free(); w->d_io.free();
     w->s_vpos.free(); w->d_solve_world.free(); w->d_solve_smem.free();
+    w->d_solve_order.free(); w->d_solve_queue.free();
     w->s_feat.free(); w->s_vsave.free(); w->s_slog.free(); w->s_pend.free();
     w->d_events.free(); w->s_cevt.free();
     w->s_sapk0.free(); w->s_sapk1.free(); w->s_sapi0.free(); w->s_sapi1.free(); w->s_sapbox.free();
@@ -204,11 +215,53 @@ int alloc_mode_scratch(dbox_world* w) {
     return DBOX_OK;
 }
 
+// World-queue mapping: one resident wave of four-warp blocks (as many as fit on every SM);
+// each warp owns a fixed region of shared memory (row staging + solver body rows for up to
+// solve_cap bodies) and takes worlds from the queue, costliest first (measured costs when
+// the autotuner has them, else body counts).
+int pack_solve_queue(dbox_world* w) {
+    const int W = (int)w->wi.size();
+    if (w->nsm <= 0) {
+        int dev = 0;
+        CU(cudaGetDevice(&dev));
+        CU(cudaDeviceGetAttribute(&w->nsm, cudaDevAttrMultiProcessorCount, dev));
+    }
+    int max_nb = 1;
+    for (const auto& wi : w->wi) max_nb = std::max(max_nb, wi.body_count);
+    // two blocks per SM: 113 KB of shared memory per block, 4 KB of it static
+    const int per_warp_bytes = (113 * 1024 - 4096) / dg::kSolveWarps;
+    const int cap_max = (per_warp_bytes - (int)sizeof(float) * dg::kWarpSmemFloats) / 32;
+    w->solve_cap = std::min(max_nb, cap_max);
+    w->solve_wpb = dg::kSolveWarps;
+    w->solve_smem_floats = dg::kSolveWarps * (dg::kWarpSmemFloats + 8 * w->solve_cap);
+    CU(cudaFuncSetAttribute(dbox_solve_kernel(), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)(sizeof(float) * w->solve_smem_floats)));
+    int occ = 0;
+    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, dbox_solve_kernel(), dg::kSolveWarps * 32,
+                                                     sizeof(float) * w->solve_smem_floats));
+    if (occ < 1) return fail(DBOX_ERR_CUDA, "solve kernel does not fit on an SM");
+    if (w->solve_bps > 0) occ = std::min(occ, w->solve_bps);
+    w->solve_blocks = std::max(1, std::min(w->nsm * occ, (W + dg::kSolveWarps - 1) / dg::kSolveWarps));
+    std::vector<int> order(W);
+    for (int i = 0; i < W; ++i) order[i] = i;
+    const bool measured = (int)w->world_cost.size() == W;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        if (measured) return w->world_cost[a] > w->world_cost[b];
+        return w->wi[a].body_count > w->wi[b].body_count;
+    });
+    if (w->d_solve_order.alloc(std::max(W, 1)) || w->d_solve_queue.alloc(2 + 4 * (size_t)w->nsm))
+        return fail(DBOX_ERR_CUDA, "device allocation failed (solve queue)");
+    if (W) CU(cudaMemcpy(w->d_solve_order.p, order.data(), sizeof(int) * W, cudaMemcpyHostToDevice));
+    CU(cudaMemset(w->d_solve_queue.p, 0, sizeof(int) * (2 + 4 * (size_t)w->nsm)));
+    return DBOX_OK;
+}
+
 // Warp slots of the solve kernel (four per block).  Each world's solver body rows and
 // island words (32 bytes a body) go to shared memory when they fit the block's budget; worlds are
 // placed largest first (first fit over the open blocks), so the biggest worlds sit in
 // the lowest blocks and start first, and small worlds fill the remaining room.
 int pack_solve_slots(dbox_world* w) {
+    if (w->solve_queue_mode) return pack_solve_queue(w);
     const int W = (int)w->wi.size();
     int max_nb = 0;
     for (const auto& wi : w->wi) max_nb = std::max(max_nb, wi.body_count);
@@ -312,6 +365,7 @@ int download(dbox_world* w) {
         for (auto& j : hw.jt) { j.body_a -= wi.body_start; j.body_b -= wi.body_start; }
     }
     w->on_device = false;
+    w->mirrors_fresh = true;
     return 0;
 }
 
@@ -489,6 +543,7 @@ int upload(dbox_world* w) {
 }
 
 int ensure_device(dbox_world* w) {
+    w->mirrors_fresh = false;              // device work follows
     if (w->dirty || !w->on_device) {
         int rc = download(w);
         if (rc) return rc;
@@ -558,6 +613,12 @@ dg::Ctx make_ctx(dbox_world* w, float dt, int vi, int pi) {
     x.solve_blocks = w->solve_blocks;
     x.solve_wpb = w->solve_wpb;
     x.solve_smem_floats = w->solve_smem_floats;
+    x.solve_order = w->d_solve_order.p;
+    x.solve_queue = w->solve_queue_mode ? w->d_solve_queue.p : nullptr;
+    x.solve_heavy = std::min(w->solve_heavy, (int)w->worlds.size());
+    x.solve_exclusive = w->solve_exclusive;
+    x.solve_cap = w->solve_cap;
+    x.solve_nsm = w->nsm;
     x.snap = w->d_snap.p;
     x.s_cbody = w->s_cbody.p;
     x.s_cq = w->s_cq.p;
@@ -1238,6 +1299,7 @@ int32_t dbox_world_set_mapping_isolated(dbox_world* w, int32_t warps_per_block, 
     if (!w || !(warps_per_block == 1 || warps_per_block == 2 || warps_per_block == dg::kSolveWarps) || body_budget < 0 ||
         isolate < 0)
         return fail(DBOX_ERR_INVALID, "dbox_world_set_mapping: warps per block must be 1, 2 or %d", dg::kSolveWarps);
+    w->solve_queue_mode = 0;
     w->solve_wpb = warps_per_block;
     w->solve_budget = body_budget;
     w->solve_isolate = isolate;
@@ -1250,15 +1312,77 @@ int32_t dbox_world_set_mapping_isolated(dbox_world* w, int32_t warps_per_block, 
     return DBOX_OK;
 }
 
+int32_t dbox_world_set_mapping_queue(dbox_world* w, int32_t heavy, int32_t exclusive, int32_t blocks_per_sm) {
+    if (!w || heavy < 0 || blocks_per_sm < 0)
+        return fail(DBOX_ERR_INVALID, "dbox_world_set_mapping_queue: bad arguments");
+    w->solve_queue_mode = 1;
+    w->solve_heavy = heavy;
+    w->solve_exclusive = exclusive ? 1 : 0;
+    w->solve_bps = blocks_per_sm;
+    if (w->on_device) {
+        int rc = pack_solve_slots(w);
+        if (rc) return rc;
+    }
+    if (w->graph) { cudaGraphExecDestroy(w->graph); w->graph = nullptr; }
+    if (w->tgraph) { cudaGraphExecDestroy(w->tgraph); w->tgraph = nullptr; }
+    return DBOX_OK;
+}
+
+int32_t dbox_world_set_world_costs(dbox_world* w, const float* cost) {
+    if (!w) return DBOX_ERR_INVALID;
+    if (cost) w->world_cost.assign(cost, cost + w->worlds.size());
+    else w->world_cost.clear();
+    if (w->on_device && w->solve_queue_mode) {
+        int rc = pack_solve_slots(w);
+        if (rc) return rc;
+    }
+    return DBOX_OK;
+}
+
+int32_t dbox_world_get_world_costs(dbox_world* w, float* out) {
+    if (!w || !out) return DBOX_ERR_INVALID;
+    for (size_t i = 0; i < w->worlds.size(); ++i)
+        out[i] = i < w->world_cost.size() ? w->world_cost[i] : (float)w->worlds[i].bs.size();
+    return DBOX_OK;
+}
+
 int32_t dbox_world_autotune(dbox_world* w, float dt, int32_t velocity_iterations, int32_t position_iterations,
                             int32_t steps, int32_t* choice) {
     if (!w || steps < 1) return fail(DBOX_ERR_INVALID, "dbox_world_autotune: bad arguments");
     int rc = ensure_device(w);
     if (rc) return rc;
-    // candidate mappings of worlds onto the solve kernel: warp slots per block x body budget
-    const int cand[][3] = {{dg::kSolveWarps, 0, 0}, {2, 0, 0}, {1, 0, 0}, {dg::kSolveWarps, 2048, 0}, {2, 2048, 0},
-                           {dg::kSolveWarps, 2048, 152}, {dg::kSolveWarps, 2048, 304}};
+    if (w->nsm <= 0) {
+        int dev = 0;
+        CU(cudaGetDevice(&dev));
+        CU(cudaDeviceGetAttribute(&w->nsm, cudaDevAttrMultiProcessorCount, dev));
+    }
+    // per-world costs for the queue order: the warp time of each world in one profiled step
+    {
+        const int was = w->profiling;
+        rc = dbox_world_set_phase_profile(w, 1);
+        if (!rc) rc = dbox_world_step_n(w, dt, velocity_iterations, position_iterations, 1);
+        std::vector<unsigned long long> prof((size_t)dg::kProfSlots * w->worlds.size());
+        if (!rc) rc = dbox_world_get_phase_profile(w, prof.data());
+        int rc2 = dbox_world_set_phase_profile(w, was);
+        if (rc) return rc;
+        if (rc2) return rc2;
+        std::vector<float> cost(w->worlds.size());
+        for (size_t i = 0; i < cost.size(); ++i) {
+            unsigned long long g0 = prof[dg::kProfSlots * i + 25], g1 = prof[dg::kProfSlots * i + 26];
+            cost[i] = g1 > g0 ? (float)(g1 - g0) : 0.0f;
+        }
+        w->world_cost = cost;
+    }
+    // candidates: {queue, warps per block or heavy worlds, body budget or exclusive, isolated}
+    const int S = w->nsm;
+    const int cand[][4] = {{0, dg::kSolveWarps, 0, 0}, {0, 2, 0, 0}, {0, 1, 0, 0}, {0, dg::kSolveWarps, 2048, 0},
+                           {0, 2, 2048, 0}, {0, dg::kSolveWarps, 2048, 152}, {0, dg::kSolveWarps, 2048, 304},
+                           {1, 0, 0, 0}, {1, S, 0, 0}, {1, S / 2, 1, 0}};
     const int ncand = (int)(sizeof(cand) / sizeof(cand[0]));
+    auto apply = [&](int c) {
+        if (cand[c][0]) return dbox_world_set_mapping_queue(w, cand[c][1], cand[c][2], 0);
+        return dbox_world_set_mapping_isolated(w, cand[c][1], cand[c][2], cand[c][3]);
+    };
     cudaEvent_t e0, e1;
     CU(cudaEventCreate(&e0));
     CU(cudaEventCreate(&e1));
@@ -1266,7 +1390,7 @@ int32_t dbox_world_autotune(dbox_world* w, float dt, int32_t velocity_iterations
     int bi = 0;
     for (int round = 0; round < 2 && !rc; ++round) {            // two rounds: the state drifts between trials
         for (int c = 0; c < ncand && !rc; ++c) {
-            rc = dbox_world_set_mapping_isolated(w, cand[c][0], cand[c][1], cand[c][2]);
+            rc = apply(c);
             if (!rc) rc = dbox_world_step_n(w, dt, velocity_iterations, position_iterations, 1);   // builds the graph
             if (rc) break;
             CU(cudaEventRecord(e0, w->stream));
@@ -1281,8 +1405,11 @@ int32_t dbox_world_autotune(dbox_world* w, float dt, int32_t velocity_iterations
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (rc) return rc;
-    rc = dbox_world_set_mapping_isolated(w, cand[bi][0], cand[bi][1], cand[bi][2]);
-    if (choice) { choice[0] = cand[bi][0]; choice[1] = cand[bi][1]; choice[2] = cand[bi][2]; }
+    rc = apply(bi);
+    if (choice) {
+        if (cand[bi][0]) { choice[0] = 0; choice[1] = 0; choice[2] = 0; choice[3] = 1; choice[4] = cand[bi][1]; choice[5] = cand[bi][2]; }
+        else { choice[0] = cand[bi][1]; choice[1] = cand[bi][2]; choice[2] = cand[bi][3]; choice[3] = 0; choice[4] = 0; choice[5] = 0; }
+    }
     return rc;
 }
 
@@ -1353,9 +1480,11 @@ int32_t dbox_world_contact_count(dbox_world* w, int32_t world, int32_t* out) {
 int32_t dbox_world_export_state(dbox_world* w, int32_t world, dbox_world_header* header, dbox_body_state* bodies,
                                 dbox_proxy_state* proxies, dbox_contact_state* contacts, dbox_joint_state* joints) {
     if (!w || world < 0 || world >= (int)w->worlds.size()) return fail(DBOX_ERR_INVALID, "export: bad world");
-    int rc = download(w);      // the device copy stays valid; only the mirrors refresh
-    if (rc) return rc;
-    if (!w->dirty && w->total_bodies + w->total_fixtures > 0) w->on_device = true;
+    if (w->on_device && !w->mirrors_fresh) {
+        int rc = download(w);  // the device copy stays valid; only the mirrors refresh
+        if (rc) return rc;
+        if (!w->dirty && w->total_bodies + w->total_fixtures > 0) w->on_device = true;
+    }
     const HostWorld& hw = w->worlds[world];
     if (header) {
         header->body_count = (int)hw.bs.size();

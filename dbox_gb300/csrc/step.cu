@@ -1868,8 +1868,9 @@ DG void sweep_levels(const int* lvl, int maxL, int nItems, const RowT* rows, Row
 
 // b2World.Solve (b2world.d:930-1124) for world w: islands, contact solver, sleep,
 // SynchronizeFixtures, FindNewContacts.  sbp: the world's solver body rows; stage_f: this
-// warp's staging area in shared memory.
-DG void solve_world(const Ctx& x, int w, float* sbp, bool sb_smem, float* stage_f) {
+// warp's staging area in shared memory; ring: the warp's row ring in that area, whose
+// barriers are initialised once per launch and carry their phases from world to world.
+DG void solve_world(const Ctx& x, int w, float* sbp, bool sb_smem, float* stage_f, RowRing& ring) {
     const WorldInfo& wi = x.wi[w];
     WorldDyn& wd = x.wd[w];
     int lane = lane_id();
@@ -1889,16 +1890,7 @@ DG void solve_world(const Ctx& x, int w, float* sbp, bool sb_smem, float* stage_
     // world's body rows in shared memory when those are there, else global rows
     int* iflags = sb_smem ? reinterpret_cast<int*>(sbp + 6 * nb) : x.s_isl_flags + b0;
     unsigned* iminsep = sb_smem ? reinterpret_cast<unsigned*>(sbp + 7 * nb) : x.s_isl_minsep + b0;
-    RowRing ring;
-    ring.base = stage_f;
-    ring.bar = reinterpret_cast<unsigned long long*>(stage_f + kStageFloats);
-    ring.par = 0;
     ring.ok = true;
-    if (lane == 0) {
-        mbar_init(&ring.bar[0]);
-        mbar_init(&ring.bar[1]);
-        fence_mbar_init();
-    }
     unsigned char* bfl = x.s_bfl + b0;
     // compact per-body / per-contact data; island flags cleared (b2world.d:944-957)
     for (int i = lane; i < nb; i += kWarp) {
@@ -2868,32 +2860,104 @@ DG void toi_world(const Ctx& x, int w, float* sbp) {
 
 // The solve phase and the TOI phase of one step, one warp per world: each world goes
 // from its island solve straight to its TOI events, so a world that is slow in one phase
-// overlaps with worlds that are slow in the other.  Warp slots and their shared memory
-// (row staging, solver body rows) come from the host's packing of worlds into blocks.
+// overlaps with worlds that are slow in the other.  Worlds reach warps in one of two ways:
+// the host's packing of worlds into blocks (solve_world / solve_smem per warp slot), or a
+// queue: one resident wave of warps takes worlds costliest first, with the heavy worlds
+// spread one per SM sub-partition so that two long dependent chains do not share an issue
+// slot.  Each warp's shared memory holds its row staging and, when the world fits, the
+// world's solver body rows.
+constexpr int kQueueWaitLimit = 1 << 16;      // bounded wait of the exclusive queue mode (x 2 us)
+
+DG int ld_acquire_int(const int* p) { return *reinterpret_cast<const volatile int*>(p); }
+
 __global__ void __launch_bounds__(kSolveWarps * 32, 3) k_solve_toi(const __grid_constant__ Ctx x) {
     extern __shared__ float smem_sb[];
-    const int slot = blockIdx.x * x.solve_wpb + (threadIdx.x >> 5);
-    const int w = x.solve_world[slot];
-    if (w < 0) return;
-    const int soff = x.solve_smem[slot];
-    float* sbp = soff >= 0 ? smem_sb + soff : x.s_sbody + 6 * (size_t)x.wi[w].body_start;
-    float* stage_f = smem_sb + (threadIdx.x >> 5) * kWarpSmemFloats;
-    unsigned long long g0 = 0;
-    if (x.prof) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(g0));
-    solve_world(x, w, sbp, soff >= 0, stage_f);
+    const int warp = threadIdx.x >> 5, lane = lane_id();
+    const int slot = blockIdx.x * x.solve_wpb + warp;
+    const bool queued = x.solve_queue != nullptr;
+    float* stage_f;
+    float* own = nullptr;
+    if (queued) {
+        stage_f = smem_sb + warp * (kWarpSmemFloats + 8 * x.solve_cap);
+        own = stage_f + kWarpSmemFloats;
+    } else {
+        stage_f = smem_sb + warp * kWarpSmemFloats;
+    }
+    // the warp's row ring: its two barriers are initialised once, before the first world
+    RowRing ring;
+    ring.base = stage_f;
+    ring.bar = reinterpret_cast<unsigned long long*>(stage_f + kStageFloats);
+    ring.par = 0;
+    ring.ok = true;
+    if (lane == 0) {
+        mbar_init(&ring.bar[0]);
+        mbar_init(&ring.bar[1]);
+        fence_mbar_init();
+    }
     tsync();
-    toi_world(x, w, sbp);
-    if (x.prof && lane_id() == 0) {
-        unsigned long long g1;
-        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(g1));
-        x.prof[kProfSlots * (size_t)w + 25] = g0;
-        x.prof[kProfSlots * (size_t)w + 26] = g1;
-        x.prof[kProfSlots * (size_t)w + 27] = slot;
+    int sub = -1;                                      // this warp's SM sub-partition (queue mode)
+    if (queued && lane == 0) {
         unsigned smid, warpid;
         asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
         asm volatile("mov.u32 %0, %%warpid;" : "=r"(warpid));
-        x.prof[kProfSlots * (size_t)w + 28] = smid;
-        x.prof[kProfSlots * (size_t)w + 29] = warpid;
+        if ((int)smid < x.solve_nsm) sub = 4 * (int)smid + (int)(warpid & 3u);
+    }
+    for (int round = 0;; ++round) {
+        int w = -1, heavy = 0;
+        if (!queued) {
+            if (round > 0) break;
+            w = x.solve_world[slot];
+        } else {
+            if (lane == 0) {
+                int* q = x.solve_queue;
+                const int H = x.solve_heavy, nl = x.W - H;
+                if (H > 0 && sub >= 0 && ld_acquire_int(&q[0]) < H && atomicCAS(&q[2 + sub], 0, 1) == 0) {
+                    const int i = atomicAdd(&q[0], 1);
+                    if (i < H) { w = x.solve_order[i]; heavy = 1; }
+                    else atomicExch(&q[2 + sub], 0);
+                }
+                if (w < 0) {
+                    if (x.solve_exclusive && sub >= 0)
+                        for (int k = 0; k < kQueueWaitLimit && ld_acquire_int(&q[2 + sub]) != 0 &&
+                                        ld_acquire_int(&q[1]) < nl; ++k)
+                            __nanosleep(2000);
+                    const int i = atomicAdd(&q[1], 1);
+                    if (i < nl) w = x.solve_order[H + i];
+                }
+            }
+            w = __shfl_sync(0xffffffffu, w, 0);
+            heavy = __shfl_sync(0xffffffffu, heavy, 0);
+        }
+        if (w < 0) break;
+        float* sbp;
+        bool in_smem;
+        if (queued) {
+            in_smem = x.wi[w].body_count <= x.solve_cap;
+            sbp = in_smem ? own : x.s_sbody + 6 * (size_t)x.wi[w].body_start;
+        } else {
+            const int soff = x.solve_smem[slot];
+            in_smem = soff >= 0;
+            sbp = in_smem ? smem_sb + soff : x.s_sbody + 6 * (size_t)x.wi[w].body_start;
+        }
+        unsigned long long g0 = 0;
+        if (x.prof) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(g0));
+        solve_world(x, w, sbp, in_smem, stage_f, ring);
+        tsync();
+        toi_world(x, w, sbp);
+        tsync();
+        if (heavy && lane == 0) atomicExch(&x.solve_queue[2 + sub], 0);
+        if (x.prof && lane == 0) {
+            unsigned long long g1;
+            asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(g1));
+            x.prof[kProfSlots * (size_t)w + 25] = g0;
+            x.prof[kProfSlots * (size_t)w + 26] = g1;
+            x.prof[kProfSlots * (size_t)w + 27] = slot;
+            unsigned smid, warpid;
+            asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+            asm volatile("mov.u32 %0, %%warpid;" : "=r"(warpid));
+            x.prof[kProfSlots * (size_t)w + 28] = smid;
+            x.prof[kProfSlots * (size_t)w + 29] = warpid;
+        }
     }
 }
 
@@ -2914,6 +2978,7 @@ extern "C" int dbox_launch_step_ev(const dg::Ctx* x, cudaStream_t stream, int* l
     dg::k_collide<<<flat_blocks, 256, 0, stream>>>(*x);
     dg::k_collide_finish<<<team_blocks, threads, 0, stream>>>(*x);
     if (ev) cudaEventRecordWithFlags(ev[1], stream, cudaEventRecordExternal);
+    if (x->solve_queue) cudaMemsetAsync(x->solve_queue, 0, sizeof(int) * (2 + 4 * (size_t)x->solve_nsm), stream);
     dg::k_solve_toi<<<x->solve_blocks, x->solve_wpb * dg::kWarp, x->solve_smem_floats * sizeof(float), stream>>>(*x);
     if (ev) cudaEventRecordWithFlags(ev[2], stream, cudaEventRecordExternal);
     if (ev) cudaEventRecordWithFlags(ev[3], stream, cudaEventRecordExternal);

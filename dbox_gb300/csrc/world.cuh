@@ -208,6 +208,15 @@ struct Ctx {
     int solve_blocks;              // blocks of the solve kernel
     int solve_wpb;                 // warp slots per block (1, 2 or kSolveWarps)
     int solve_smem_floats;         // dynamic shared memory of one solve block, in floats
+    // world-queue mapping (solve_queue != nullptr): one resident wave of warps takes worlds
+    // from solve_order (costliest first); the first solve_heavy entries go one per SM
+    // sub-partition at a time
+    const int* solve_order;        // W world indices, costliest first
+    int* solve_queue;              // [0] next heavy entry, [1] next light entry, [2 + 4*sm + sub] heavy flags
+    int solve_heavy;               // number of heavy entries at the front of solve_order
+    int solve_exclusive;           // a warp whose sub-partition runs a heavy world takes no light world meanwhile
+    int solve_cap;                 // bodies per warp region of shared memory (larger worlds use global rows)
+    int solve_nsm;                 // SMs of the device
     SweepSnap* snap;               // contact-slot-indexed
     int2* s_cbody;                 // contact-slot-indexed: world-local bodies of the contact
     unsigned char* s_cq;           // contact-slot-indexed: bit0 island-graph edge, bit1 sensor

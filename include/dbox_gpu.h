@@ -358,8 +358,23 @@ int32_t dbox_world_get_quality(dbox_world* w, float* out);
 int32_t dbox_world_set_mapping(dbox_world* w, int32_t warps_per_block, int32_t body_budget);
 /* The same, with the `isolate` largest worlds each given a block of its own. */
 int32_t dbox_world_set_mapping_isolated(dbox_world* w, int32_t warps_per_block, int32_t body_budget, int32_t isolate);
-/* Autotuner: times `steps` steps (the simulation advances) under each candidate mapping,
- * twice, and keeps the fastest; choice[3] receives (warps per block, body budget, isolated). */
+/* World-queue mapping: one resident wave of warps takes worlds from a queue, costliest first
+ * (the costs given by dbox_world_set_world_costs, else body counts); the `heavy` costliest
+ * worlds go one per SM sub-partition at a time, and with `exclusive` a warp whose
+ * sub-partition runs a heavy world waits (bounded) before it takes another world;
+ * blocks_per_sm limits the resident four-warp blocks per SM (0: as many as fit).  Worlds
+ * of up to about 580 bodies keep their solver rows in shared memory.  Results do not depend
+ * on the mapping. */
+int32_t dbox_world_set_mapping_queue(dbox_world* w, int32_t heavy, int32_t exclusive, int32_t blocks_per_sm);
+/* Per-world cost estimates (n_worlds floats; NULL clears them) for the queue order. */
+int32_t dbox_world_set_world_costs(dbox_world* w, const float* cost);
+/* The per-world costs in use (measured by the autotuner, or given; else body counts). */
+int32_t dbox_world_get_world_costs(dbox_world* w, float* out);
+/* Autotuner: measures each world's warp time in one profiled step (kept as the queue
+ * costs), then times `steps` steps (the simulation advances) under each candidate mapping,
+ * twice, and keeps the fastest; choice[6] receives (warps per block, body budget, isolated,
+ * queue, heavy, exclusive): the first three for a block packing (queue = 0), the last two
+ * for a queue mapping (queue = 1). */
 int32_t dbox_world_autotune(dbox_world* w, float dt, int32_t velocity_iterations, int32_t position_iterations,
                             int32_t steps, int32_t* choice);
 

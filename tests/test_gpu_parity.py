@@ -93,8 +93,8 @@ def test_batch_exact(oracle_lib, gpu_lib):
 
 
 def test_mappings_and_autotune_keep_results(oracle_lib, gpu_lib):
-    # the world-to-block mapping (warps per block, shared-memory budget) and the autotuner's
-    # choice among mappings change where worlds run, never what they compute
+    # the world-to-block mapping (warps per block, shared-memory budget, or the world queue)
+    # and the autotuner's choice among mappings change where worlds run, never what they compute
     from dbox_gb300 import scenes
     oracle_lib.set_trig_mode(1)
     worlds = scenes.batch(n_worlds=9, seed=12, lo=8, hi=200)
@@ -106,14 +106,45 @@ def test_mappings_and_autotune_keep_results(oracle_lib, gpu_lib):
         for _ in range(30):
             gw.step()
         steps += 30
+    # queue mappings: plain, heavy worlds spread over sub-partitions, exclusive; graph and single steps
+    for heavy, excl in ((0, False), (4, False), (3, True)):
+        gw.set_mapping_queue(heavy, excl)
+        gw.step(steps=10, graph=True)
+        for _ in range(10):
+            gw.step()
+        steps += 20
+    gw.set_world_costs(np.arange(len(worlds), dtype=np.float32))
+    gw.step(steps=10, graph=True)
+    steps += 10
     choice = gw.autotune(steps=2)
-    assert choice[0] in (1, 2, 4)
-    steps += 14 * 3
+    assert choice[3] in (0, 1) and (choice[3] == 1 or choice[0] in (1, 2, 4))
+    steps += gw.autotune_steps(2)
     for _ in range(30):
         gw.step()
     steps += 30
     for ow in ows:
         ow.step(steps=steps)
+    for i, ow in enumerate(ows):
+        d = exact_diff(ow.export_state(), gw.export_state(i))
+        assert not d, "world %d: %s" % (i, d[:6])
+
+
+def test_queue_mapping_with_more_worlds_than_warps_exact(oracle_lib, gpu_lib):
+    # more worlds than the resident warps of the queue mapping, so warps take several worlds
+    # one after another in a step (and carry their row ring from world to world)
+    from dbox_gb300 import scenes
+    oracle_lib.set_trig_mode(1)
+    worlds = scenes.batch(n_worlds=2000, seed=14, lo=8, hi=40)
+    gw = gpu_lib.World(worlds)
+    ows = [oracle_lib.OracleWorld(s) for s in worlds]
+    gw.set_mapping_queue(64, False)
+    gw.step(steps=12, graph=True)
+    for _ in range(4):
+        gw.step()
+    gw.set_mapping_queue(32, True)
+    gw.step(steps=4, graph=True)
+    for ow in ows:
+        ow.step(steps=20)
     for i, ow in enumerate(ows):
         d = exact_diff(ow.export_state(), gw.export_state(i))
         assert not d, "world %d: %s" % (i, d[:6])
