@@ -56,6 +56,8 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-learned", action="store_true", help="skip the learned warm-start comparison")
     p.add_argument("--no-autotune", action="store_true", help="keep the default world-to-block mapping")
+    p.add_argument("--mapping", default="auto", choices=["auto", "default", "queue"],
+                   help="auto: the autotuner's choice; default: default block packing; queue: world queue")
     p.add_argument("--learned-worlds", type=int, default=1024)
     p.add_argument("--learned-log-steps", type=int, default=2000)
     return p.parse_args()
@@ -206,7 +208,10 @@ def gpu_leg(args, rank, world_size):
     # the autotuner picks the world-to-block mapping on a throwaway handle of the same worlds
     # (it advances the worlds it times); the measured handles then use that mapping
     mapping = None
-    if not args.no_autotune:
+    if args.mapping == "queue":
+        mapping = (0, 0, 0, 1, 0, 0)
+        costs = None
+    elif not args.no_autotune and args.mapping == "auto":
         wt = dbox_gb300.World(worlds)
         wt.step(DT, VI, PI, steps=args.warmup, graph=True)
         mapping = wt.autotune(steps=3, dt=DT, vel_iters=VI, pos_iters=PI)
@@ -218,7 +223,8 @@ def gpu_leg(args, rank, world_size):
     we = dbox_gb300.World(worlds)
     if mapping:
         for h in (w, we):
-            h.set_world_costs(costs)
+            if costs is not None:
+                h.set_world_costs(costs)
             h.apply_mapping(mapping)
     w.step(DT, VI, PI, steps=args.warmup, graph=True)
     we.step(DT, VI, PI, steps=args.warmup, graph=True)
@@ -277,11 +283,7 @@ def gpu_leg(args, rank, world_size):
         "data": "synthetic seeded scenes (numpy PCG64 seed %d)" % args.seed,
         "config": dict(cfg, dt=DT, velocity_iterations=VI, position_iterations=PI, dynamic_bodies=nbody_dyn,
                        parallelism="replicas: one batch of worlds per GPU",
-                       mapping=(({"queue": 1, "heavy_worlds_one_per_subpartition": mapping[4],
-                                  "exclusive": mapping[5], "chosen_by": "autotuner"} if mapping[3] else
-                                 {"warps_per_block": mapping[0], "body_budget": mapping[1],
-                                  "isolated_largest_worlds": mapping[2], "chosen_by": "autotuner"})
-                                if mapping else "default"),
+                       mapping=mapping_report(mapping, args.mapping),
                        l2="working set (bodies, contacts, constraint rows) larger than the 129 MB L2",
                        timing="one CUDA graph of K steps with per-phase CUDA events"),
         "e2e": {"value": e2e, "unit": "body-steps/s", "h2d_bytes_per_step": int(forces.nbytes),
@@ -364,6 +366,17 @@ def learned_leg(args):
         "learned_5_reaches_plain_8_residual": bool(l5["residual_rms"] <= p8["residual_rms"] and
                                                    l5["residual_max"] <= p8["residual_max"]),
     }
+
+
+def mapping_report(mapping, how):
+    """The world-to-warp mapping of the measured handles, for the JSON line."""
+    if not mapping:
+        return "default"
+    by = "autotuner" if how == "auto" else "--mapping " + how
+    if mapping[3]:
+        return {"queue": 1, "heavy_worlds_one_per_subpartition": mapping[4], "exclusive": mapping[5], "chosen_by": by}
+    return {"warps_per_block": mapping[0], "body_budget": mapping[1], "isolated_largest_worlds": mapping[2],
+            "chosen_by": by}
 
 
 def main():
