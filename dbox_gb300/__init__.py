@@ -46,6 +46,7 @@ def lib():
     L.dbox_body_create.argtypes = [vp, i32, vp, ctypes.POINTER(i32)]
     L.dbox_fixture_create.argtypes = [vp, i32, i32, vp, vp, ctypes.POINTER(i32)]
     L.dbox_joint_create_revolute.argtypes = [vp, i32, vp, ctypes.POINTER(i32)]
+    L.dbox_joint_create_distance.argtypes = [vp, i32, vp, ctypes.POINTER(i32)]
     L.dbox_world_set_flags.argtypes = [vp, i32, i32, i32, i32, i32]
     L.dbox_world_set_gravity.argtypes = [vp, abi.Vec2]
     L.dbox_world_step.argtypes = [vp, f32, i32, i32]
@@ -227,9 +228,18 @@ class World:
             j = np.ascontiguousarray(s["joints"])
             _check(L.dbox_scene_create(self.h, i, len(b), abi.ptr(b), len(fb), abi.ptr(fb), abi.ptr(sh), abi.ptr(fx),
                                        len(j), abi.ptr(j) if len(j) else None), "dbox_scene_create")
+            for d in s.get("distance_joints", ()):           # created after the revolute joints
+                self.create_distance_joint(i, d)
         self.body_counts = [len(s["bodies"]) for s in scenes]
         if flags is not None:
             self.set_flags(**flags)
+
+    def create_distance_joint(self, world, d):
+        """b2World.CreateJoint with a b2DistanceJointDef (a DISTANCE_DEF record); returns the joint index."""
+        dd = np.ascontiguousarray(np.array([d], abi.DISTANCE_DEF))
+        out = ctypes.c_int32()
+        _check(lib().dbox_joint_create_distance(self.h, world, abi.ptr(dd), ctypes.byref(out)), "dbox_joint_create_distance")
+        return out.value
 
     def close(self):
         if getattr(self, "h", None) is not None and self.h.value:

@@ -35,6 +35,12 @@ REVOLUTE_DEF = np.dtype([
     ("enable_motor", "<i4"), ("motor_speed", "<f4"), ("max_motor_torque", "<f4"),
 ])
 assert REVOLUTE_DEF.itemsize == 56
+DISTANCE_DEF = np.dtype([
+    ("body_a", "<i4"), ("body_b", "<i4"), ("collide_connected", "<i4"),
+    ("local_anchor_a", "<f4", 2), ("local_anchor_b", "<f4", 2),
+    ("length", "<f4"), ("frequency_hz", "<f4"), ("damping_ratio", "<f4"),
+])
+assert DISTANCE_DEF.itemsize == 40
 
 WORLD_HEADER = np.dtype([
     ("body_count", "<i4"), ("fixture_count", "<i4"), ("contact_count", "<i4"), ("joint_count", "<i4"),

@@ -835,6 +835,20 @@ int create_fixture(HostWorld& hw, int body, const dbox_shape_def* shape, const d
     return idx;
 }
 
+// append a joint (joint lists are rebuilt newest first from creation order at upload) and
+// flag the contacts between its bodies when they may not collide (b2world.d:246-258)
+int link_joint(HostWorld& hw, const dg::DJoint& j) {
+    int idx = (int)hw.jt.size();
+    hw.jt.push_back(j);
+    if (!j.collide_connected) {
+        for (auto& c : hw.ct) {
+            int A = hw.fx[c.fixture_a].body, B = hw.fx[c.fixture_b].body;
+            if ((A == j.body_a && B == j.body_b) || (A == j.body_b && B == j.body_a)) c.flags |= dg::kContactFilter;
+        }
+    }
+    return idx;
+}
+
 int create_joint(HostWorld& hw, const dbox_revolute_def* d) {
     int nb = (int)hw.bs.size();
     if (d->body_a < 0 || d->body_a >= nb || d->body_b < 0 || d->body_b >= nb || d->body_a == d->body_b) return -1;
@@ -852,15 +866,26 @@ int create_joint(HostWorld& hw, const dbox_revolute_def* d) {
     j.enable_motor = d->enable_motor ? 1 : 0;
     j.motor_speed = d->motor_speed;
     j.max_motor_torque = d->max_motor_torque;
-    int idx = (int)hw.jt.size();
-    hw.jt.push_back(j);
-    if (!j.collide_connected) {                                         // b2world.d:246-258
-        for (auto& c : hw.ct) {
-            int A = hw.fx[c.fixture_a].body, B = hw.fx[c.fixture_b].body;
-            if ((A == j.body_a && B == j.body_b) || (A == j.body_b && B == j.body_a)) c.flags |= dg::kContactFilter;
-        }
-    }
-    return idx;
+    j.type = dg::kRevoluteJoint;
+    return link_joint(hw, j);
+}
+
+// b2World.CreateJoint with a b2DistanceJointDef (b2world.d:196-261, b2distancejoint.d:122-133)
+int create_distance_joint(HostWorld& hw, const dbox_distance_def* d) {
+    int nb = (int)hw.bs.size();
+    if (d->body_a < 0 || d->body_a >= nb || d->body_b < 0 || d->body_b >= nb || d->body_a == d->body_b) return -1;
+    dg::DJoint j;
+    memset(&j, 0, sizeof(j));
+    j.type = dg::kDistanceJoint;
+    j.body_a = d->body_a;
+    j.body_b = d->body_b;
+    j.collide_connected = d->collide_connected ? 1 : 0;
+    j.local_anchor_a = make_float2(d->local_anchor_a.x, d->local_anchor_a.y);
+    j.local_anchor_b = make_float2(d->local_anchor_b.x, d->local_anchor_b.y);
+    j.length = d->length;
+    j.frequency_hz = d->frequency_hz;
+    j.damping_ratio = d->damping_ratio;
+    return link_joint(hw, j);
 }
 
 int prepare_edit(dbox_world* w) {
@@ -957,6 +982,16 @@ int32_t dbox_joint_create_revolute(dbox_world* w, int32_t world, const dbox_revo
     if (rc) return rc;
     int idx = create_joint(w->worlds[world], def);
     if (idx < 0) return fail(DBOX_ERR_INVALID, "dbox_joint_create_revolute: bad bodies");
+    if (out_joint) *out_joint = idx;
+    return DBOX_OK;
+}
+
+int32_t dbox_joint_create_distance(dbox_world* w, int32_t world, const dbox_distance_def* def, int32_t* out_joint) {
+    if (!w || !def || world < 0 || world >= (int)w->worlds.size()) return fail(DBOX_ERR_INVALID, "dbox_joint_create_distance: bad arguments");
+    int rc = prepare_edit(w);
+    if (rc) return rc;
+    int idx = create_distance_joint(w->worlds[world], def);
+    if (idx < 0) return fail(DBOX_ERR_INVALID, "dbox_joint_create_distance: bad bodies");
     if (out_joint) *out_joint = idx;
     return DBOX_OK;
 }

@@ -1290,8 +1290,105 @@ DG float solve_position_row(const PC& pc, SB sb) {
     return solve_position(pc, sb, false, -1, -1);
 }
 
+// ------------------------------------------------------------ distance joint (joints/b2distancejoint.d:211-372)
+__device__ __noinline__ void distance_init(const Ctx& x, int ji, int b0, SB sb, bool warm, float dtRatio) {
+    DJoint& j = x.jt[ji];
+    const dbox_body_state& ba = x.bs[j.body_a];
+    const dbox_body_state& bb = x.bs[j.body_b];
+    int la = j.body_a - b0, lb = j.body_b - b0;
+    j.lcA = b_lc(ba);
+    j.lcB = b_lc(bb);
+    j.invMassA = ba.mass[1];
+    j.invMassB = bb.mass[1];
+    j.invIA = ba.mass[3];
+    j.invIB = bb.mass[3];
+    float2 cA = sb.c(la), cB = sb.c(lb);
+    float aA = sb.a(la), aB = sb.a(lb);
+    float2 vA = sb.v(la), vB = sb.v(lb);
+    float wA = sb.w(la), wB = sb.w(lb);
+    Rot qA = rot(aA), qB = rot(aB);
+    j.rA = mul(qA, j.local_anchor_a - j.lcA);
+    j.rB = mul(qB, j.local_anchor_b - j.lcB);
+    float2 u = ((cB + j.rB) - cA) - j.rA;
+    float len = length(u);                                              // singularity: u = 0 below linearSlop
+    if (len > kLinearSlop) u *= fdiv(1.0f, len);
+    else u = v2(0.0f, 0.0f);
+    j.u = u;
+    float crAu = cross(j.rA, u), crBu = cross(j.rB, u);
+    float invMass = ((j.invMassA + (j.invIA * crAu) * crAu) + j.invMassB) + (j.invIB * crBu) * crBu;
+    float mass = invMass != 0.0f ? fdiv(1.0f, invMass) : 0.0f;
+    if (j.frequency_hz > 0.0f) {
+        float C = len - j.length;
+        float omega = (2.0f * kPi) * j.frequency_hz;
+        float d = ((2.0f * mass) * j.damping_ratio) * omega;
+        float k = (mass * omega) * omega;
+        float h = x.dt;
+        float gamma = h * (d + h * k);
+        gamma = gamma != 0.0f ? fdiv(1.0f, gamma) : 0.0f;
+        j.gamma = gamma;
+        j.bias = ((C * h) * k) * gamma;
+        invMass += gamma;
+        mass = invMass != 0.0f ? fdiv(1.0f, invMass) : 0.0f;
+    } else {
+        j.gamma = 0.0f;
+        j.bias = 0.0f;
+    }
+    j.mass[0] = mass;
+    if (warm) {
+        j.impulse[0] *= dtRatio;
+        float2 P = j.impulse[0] * u;
+        vA -= j.invMassA * P;
+        wA -= j.invIA * cross(j.rA, P);
+        vB += j.invMassB * P;
+        wB += j.invIB * cross(j.rB, P);
+    } else {
+        j.impulse[0] = 0.0f;
+    }
+    sb.set_v(la, vA, wA);
+    sb.set_v(lb, vB, wB);
+}
+
+DG void distance_solve_velocity(DJoint& j, int la, int lb, SB sb) {
+    float2 vA = sb.v(la), vB = sb.v(lb);
+    float wA = sb.w(la), wB = sb.w(lb);
+    float2 vpA = vA + cross(wA, j.rA);
+    float2 vpB = vB + cross(wB, j.rB);
+    float Cdot = dot(j.u, vpB - vpA);
+    float impulse = -j.mass[0] * ((Cdot + j.bias) + j.gamma * j.impulse[0]);
+    j.impulse[0] += impulse;
+    float2 P = impulse * j.u;
+    vA -= j.invMassA * P;
+    wA -= j.invIA * cross(j.rA, P);
+    vB += j.invMassB * P;
+    wB += j.invIB * cross(j.rB, P);
+    sb.set_v(la, vA, wA);
+    sb.set_v(lb, vB, wB);
+}
+
+__device__ __noinline__ bool distance_solve_position(const DJoint& j, int la, int lb, SB sb) {
+    if (j.frequency_hz > 0.0f) return true;                            // soft: no position correction
+    float2 cA = sb.c(la), cB = sb.c(lb);
+    float aA = sb.a(la), aB = sb.a(lb);
+    Rot qA = rot(aA), qB = rot(aB);
+    float2 rA = mul(qA, j.local_anchor_a - j.lcA);
+    float2 rB = mul(qB, j.local_anchor_b - j.lcB);
+    float2 u = ((cB + rB) - cA) - rA;
+    float len = normalize(u);
+    float C = bclamp(len - j.length, -kMaxLinearCorrection, kMaxLinearCorrection);
+    float impulse = -j.mass[0] * C;
+    float2 P = impulse * u;
+    cA -= j.invMassA * P;
+    aA -= j.invIA * cross(rA, P);
+    cB += j.invMassB * P;
+    aB += j.invIB * cross(rB, P);
+    sb.set_c(la, cA, aA);
+    sb.set_c(lb, cB, aB);
+    return babs(C) < kLinearSlop;
+}
+
 // ------------------------------------------------------------ revolute joint (joints/b2revolutejoint.d:319-636)
 DG void joint_init(const Ctx& x, int ji, int b0, SB sb, bool warm, float dtRatio) {
+    if (x.jt[ji].type == kDistanceJoint) { distance_init(x, ji, b0, sb, warm, dtRatio); return; }
     DJoint& j = x.jt[ji];
     const dbox_body_state& ba = x.bs[j.body_a];
     const dbox_body_state& bb = x.bs[j.body_b];
@@ -1381,6 +1478,7 @@ DG float2 solve22(const float* m, float2 b) {                            // b2ma
 DG void joint_solve_velocity(const Ctx& x, int ji, int b0, SB sb) {
     DJoint& j = x.jt[ji];
     int la = j.body_a - b0, lb = j.body_b - b0;
+    if (j.type == kDistanceJoint) { distance_solve_velocity(j, la, lb, sb); return; }
     float2 vA = sb.v(la), vB = sb.v(lb);
     float wA = sb.w(la), wB = sb.w(lb);
     float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
@@ -1440,6 +1538,7 @@ DG void joint_solve_velocity(const Ctx& x, int ji, int b0, SB sb) {
 DG bool joint_solve_position(const Ctx& x, int ji, int b0, SB sb) {
     DJoint& j = x.jt[ji];
     int la = j.body_a - b0, lb = j.body_b - b0;
+    if (j.type == kDistanceJoint) return distance_solve_position(j, la, lb, sb);
     float2 cA = sb.c(la), cB = sb.c(lb);
     float aA = sb.a(la), aB = sb.a(lb);
     float angularError = 0.0f, positionError = 0.0f;

@@ -68,7 +68,8 @@ struct BodyStatic {
     int jadj_start, jadj_count;    // into Ctx.jadj_joint / jadj_other (descending joint index)
 };
 
-struct DJoint {                    // b2RevoluteJoint (joints/b2revolutejoint.d)
+enum { kRevoluteJoint = 0, kDistanceJoint = 1 };
+struct DJoint {                    // b2RevoluteJoint / b2DistanceJoint (joints/b2revolutejoint.d, b2distancejoint.d)
     int body_a, body_b;
     int collide_connected;
     int island_flag;
@@ -83,9 +84,11 @@ struct DJoint {                    // b2RevoluteJoint (joints/b2revolutejoint.d)
     int limit_state;
     float2 rA, rB, lcA, lcB;
     float invMassA, invMassB, invIA, invIB;
-    float mass[9];                 // ex.x ex.y ex.z ey.x ey.y ey.z ez.x ez.y ez.z
+    float mass[9];                 // ex.x ex.y ex.z ey.x ey.y ey.z ez.x ez.y ez.z; distance: mass[0]
     float motor_mass;
-    int pad;
+    int type;                      // kRevoluteJoint or kDistanceJoint; a distance joint keeps its impulse in impulse[0]
+    float length, frequency_hz, damping_ratio, gamma, bias;   // distance joint
+    float2 u;                      // distance joint: unit vector from anchor A to anchor B
 };
 
 // b2ContactVelocityConstraint (contacts/b2contactsolver.d:43-58) with body indices in place of island indices.

@@ -34,7 +34,8 @@ def _empty():
     return {
         "bodies": abi.body_defs(0), "fixture_body": np.zeros(0, np.int32),
         "shapes": np.zeros(0, abi.SHAPE_DEF), "fixtures": abi.fixture_defs(0),
-        "joints": np.zeros(0, abi.REVOLUTE_DEF), "gravity": (0.0, -10.0), "name": "",
+        "joints": np.zeros(0, abi.REVOLUTE_DEF), "distance_joints": np.zeros(0, abi.DISTANCE_DEF),
+        "gravity": (0.0, -10.0), "name": "",
     }
 
 
@@ -51,6 +52,10 @@ def _concat(parts):
         j["body_a"] += nb
         j["body_b"] += nb
         out["joints"] = np.concatenate([out["joints"], j])
+        d = p.get("distance_joints", np.zeros(0, abi.DISTANCE_DEF)).copy()
+        d["body_a"] += nb
+        d["body_b"] += nb
+        out["distance_joints"] = np.concatenate([out["distance_joints"], d])
         nb += len(p["bodies"])
     return out
 
@@ -209,6 +214,49 @@ def chains(n_chains=4, links=32, hx=0.125, hy=0.025, x0=-12.0, spacing=6.0, y=12
         parts.append(part)
     out = _concat(parts)
     out["name"] = "chains"
+    return out
+
+
+def ropes(n_ropes=4, links=20, box=0.1, gap=0.3, x0=-9.0, spacing=6.0, y=14.0, pile=True, revolute=True):
+    """Distance-joint ropes (b2DistanceJointDef, joints/b2distancejoint.d:33-93): each rope is
+    `links` small boxes hanging in a horizontal line from a static post, consecutive boxes
+    joined by a distance joint of length `gap` between their centres (the first from the
+    post); even ropes are rigid, odd ropes soft (4 Hz, damping ratio 0.5), and the last
+    link of every third rope is tied back to the post by a long soft joint.  With `revolute`,
+    a revolute chain hangs beside them (the revolute joints are created first), and box
+    stacks stand on the ground below when `pile` is set."""
+    parts = [ground_box()]
+    if pile:
+        parts.append(stacks(4 * n_ropes, 3, spacing=spacing / 2.0))
+    if revolute:
+        c = chains(n_chains=1, links=12, x0=x0 + n_ropes * spacing, y=y, pile=False)
+        parts.append({k: c[k] for k in ("bodies", "fixture_body", "shapes", "fixtures", "joints")})
+    for r in range(n_ropes):
+        x = x0 + r * spacing
+        post = _boxes([(x, y)], 0.1, 0.1, abi.STATIC)
+        rope = _boxes([(x + gap * (i + 1), y) for i in range(links)], box, box, abi.DYNAMIC, 0.4, 5.0)
+        part = _concat([post, rope])
+        soft = r % 2 == 1
+        tie = r % 3 == 0
+        d = np.zeros(links + (1 if tie else 0), abi.DISTANCE_DEF)
+        for i in range(links):
+            d[i]["body_a"] = i               # the post for i = 0, else link i-1
+            d[i]["body_b"] = i + 1
+            d[i]["length"] = gap
+            if soft:
+                d[i]["frequency_hz"] = 4.0
+                d[i]["damping_ratio"] = 0.5
+        if tie:
+            d[links]["body_a"] = 0
+            d[links]["body_b"] = links
+            d[links]["local_anchor_b"] = (box, 0.0)
+            d[links]["length"] = gap * links * 0.7
+            d[links]["frequency_hz"] = 1.5
+            d[links]["damping_ratio"] = 0.2
+        part["distance_joints"] = d
+        parts.append(part)
+    out = _concat(parts)
+    out["name"] = "ropes"
     return out
 
 

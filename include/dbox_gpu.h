@@ -97,6 +97,16 @@ typedef struct {
     float motor_speed, max_motor_torque;
 } dbox_revolute_def;
 
+/* b2DistanceJointDef (dynamics/joints/b2distancejoint.d:33-93) */
+typedef struct {
+    int32_t body_a, body_b;
+    int32_t collide_connected;
+    dbox_vec2 local_anchor_a, local_anchor_b;
+    float length;          /* natural length between the anchors */
+    float frequency_hz;    /* mass-spring-damper frequency; 0 = rigid */
+    float damping_ratio;
+} dbox_distance_def;
+
 /* ------------------------------------------------------- world snapshot
  * Flat state records, used by dbox_world_export_state / import_state
  * (exact checkpoint/resume) and by the parity tests.  Flag words use the
@@ -200,6 +210,11 @@ int32_t dbox_fixture_create(dbox_world* w, int32_t world, int32_t body, const db
                             const dbox_fixture_def* def, int32_t* out_fixture);
 /* b2World.CreateJoint with a b2RevoluteJointDef (b2world.d:196-261, joints/b2revolutejoint.d). */
 int32_t dbox_joint_create_revolute(dbox_world* w, int32_t world, const dbox_revolute_def* def,
+                                   int32_t* out_joint);
+/* b2World.CreateJoint with a b2DistanceJointDef (b2world.d:196-261, joints/b2distancejoint.d).
+ * Joint indices count all joint kinds in creation order; the snapshot's impulse[0] holds the
+ * distance joint's impulse. */
+int32_t dbox_joint_create_distance(dbox_world* w, int32_t world, const dbox_distance_def* def,
                                    int32_t* out_joint);
 
 /* Bulk creation of a whole scene into one world: n bodies, then m fixtures

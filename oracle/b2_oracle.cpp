@@ -1702,7 +1702,10 @@ struct Velocity { Vec2 v; f32 w = 0; };
 struct TimeStep { f32 dt = 0, inv_dt = 0, dtRatio = 0; int velocityIterations = 0, positionIterations = 0; bool warmStarting = false; };
 struct SolverData { TimeStep step; Position* positions = nullptr; Velocity* velocities = nullptr; };
 
-struct Joint {                                                          // joints/b2joint.d, b2revolutejoint.d
+enum { kRevoluteJoint = 0, kDistanceJoint = 1 };
+
+struct Joint {                                                          // joints/b2joint.d, b2revolutejoint.d, b2distancejoint.d
+    int type = kRevoluteJoint;
     Joint* prev = nullptr;
     Joint* next = nullptr;
     JointEdge edgeA, edgeB;
@@ -1725,8 +1728,127 @@ struct Joint {                                                          // joint
     Mat33 massM;
     f32 motorMass = 0;
     int limitState = kInactiveLimit;
+    // distance (the impulse is impulse.x)
+    f32 length = 0, frequencyHz = 0, dampingRatio = 0, gamma = 0, bias = 0, distMass = 0;
+    Vec2 u;
 
-    void InitVelocityConstraints(const SolverData& data) {              // b2revolutejoint.d:319-439
+    void InitVelocityConstraints(const SolverData& data) {
+        if (type == kDistanceJoint) DistanceInit(data); else RevoluteInit(data);
+    }
+    void SolveVelocityConstraints(const SolverData& data) {
+        if (type == kDistanceJoint) DistanceSolveVelocity(data); else RevoluteSolveVelocity(data);
+    }
+    bool SolvePositionConstraints(const SolverData& data) {
+        return type == kDistanceJoint ? DistanceSolvePosition(data) : RevoluteSolvePosition(data);
+    }
+
+    void DistanceInit(const SolverData& data) {                         // b2distancejoint.d:211-306
+        indexA = bodyA->islandIndex;
+        indexB = bodyB->islandIndex;
+        localCenterA = bodyA->sweep.localCenter;
+        localCenterB = bodyB->sweep.localCenter;
+        invMassA = bodyA->invMass;
+        invMassB = bodyB->invMass;
+        invIA = bodyA->invI;
+        invIB = bodyB->invI;
+        Vec2 cA = data.positions[indexA].c;
+        f32 aA = data.positions[indexA].a;
+        Vec2 vA = data.velocities[indexA].v;
+        f32 wA = data.velocities[indexA].w;
+        Vec2 cB = data.positions[indexB].c;
+        f32 aB = data.positions[indexB].a;
+        Vec2 vB = data.velocities[indexB].v;
+        f32 wB = data.velocities[indexB].w;
+        Rot qA(aA), qB(aB);
+        rA = Mul(qA, localAnchorA - localCenterA);
+        rB = Mul(qB, localAnchorB - localCenterB);
+        u = ((cB + rB) - cA) - rA;
+        f32 len = u.Length();                                           // singularity: u = 0 below linearSlop
+        if (len > kLinearSlop) u *= 1.0f / len;
+        else u.Set(0.0f, 0.0f);
+        f32 crAu = Cross(rA, u);
+        f32 crBu = Cross(rB, u);
+        f32 invMass = ((invMassA + (invIA * crAu) * crAu) + invMassB) + (invIB * crBu) * crBu;
+        distMass = invMass != 0.0f ? 1.0f / invMass : 0.0f;
+        if (frequencyHz > 0.0f) {
+            f32 C = len - length;
+            f32 omega = (2.0f * kPi) * frequencyHz;
+            f32 d = ((2.0f * distMass) * dampingRatio) * omega;
+            f32 k = (distMass * omega) * omega;
+            f32 h = data.step.dt;
+            gamma = h * (d + h * k);
+            gamma = gamma != 0.0f ? 1.0f / gamma : 0.0f;
+            bias = ((C * h) * k) * gamma;
+            invMass += gamma;
+            distMass = invMass != 0.0f ? 1.0f / invMass : 0.0f;
+        } else {
+            gamma = 0.0f;
+            bias = 0.0f;
+        }
+        if (data.step.warmStarting) {
+            impulse.x *= data.step.dtRatio;
+            Vec2 P = impulse.x * u;
+            vA -= invMassA * P;
+            wA -= invIA * Cross(rA, P);
+            vB += invMassB * P;
+            wB += invIB * Cross(rB, P);
+        } else {
+            impulse.x = 0.0f;
+        }
+        data.velocities[indexA].v = vA;
+        data.velocities[indexA].w = wA;
+        data.velocities[indexB].v = vB;
+        data.velocities[indexB].w = wB;
+    }
+
+    void DistanceSolveVelocity(const SolverData& data) {                // b2distancejoint.d:308-333
+        Vec2 vA = data.velocities[indexA].v;
+        f32 wA = data.velocities[indexA].w;
+        Vec2 vB = data.velocities[indexB].v;
+        f32 wB = data.velocities[indexB].w;
+        Vec2 vpA = vA + Cross(wA, rA);
+        Vec2 vpB = vB + Cross(wB, rB);
+        f32 Cdot = Dot(u, vpB - vpA);
+        f32 imp = -distMass * ((Cdot + bias) + gamma * impulse.x);
+        impulse.x += imp;
+        Vec2 P = imp * u;
+        vA -= invMassA * P;
+        wA -= invIA * Cross(rA, P);
+        vB += invMassB * P;
+        wB += invIB * Cross(rB, P);
+        data.velocities[indexA].v = vA;
+        data.velocities[indexA].w = wA;
+        data.velocities[indexB].v = vB;
+        data.velocities[indexB].w = wB;
+    }
+
+    bool DistanceSolvePosition(const SolverData& data) {                // b2distancejoint.d:335-372
+        if (frequencyHz > 0.0f) return true;                            // soft: no position correction
+        Vec2 cA = data.positions[indexA].c;
+        f32 aA = data.positions[indexA].a;
+        Vec2 cB = data.positions[indexB].c;
+        f32 aB = data.positions[indexB].a;
+        Rot qA(aA), qB(aB);
+        Vec2 rA_ = Mul(qA, localAnchorA - localCenterA);
+        Vec2 rB_ = Mul(qB, localAnchorB - localCenterB);
+        Vec2 d = ((cB + rB_) - cA) - rA_;
+        f32 len = d.Normalize();
+        f32 C = len - length;
+        C = Clamp(C, -kMaxLinearCorrection, kMaxLinearCorrection);
+        f32 imp = -distMass * C;
+        Vec2 P = imp * d;
+        cA -= invMassA * P;
+        aA -= invIA * Cross(rA_, P);
+        cB += invMassB * P;
+        aB += invIB * Cross(rB_, P);
+        data.positions[indexA].c = cA;
+        data.positions[indexA].a = aA;
+        data.positions[indexB].c = cB;
+        data.positions[indexB].a = aB;
+        return Abs(C) < kLinearSlop;
+    }
+
+    void RevoluteInit(const SolverData& data) {                         // b2revolutejoint.d:319-439
         indexA = bodyA->islandIndex;
         indexB = bodyB->islandIndex;
         localCenterA = bodyA->sweep.localCenter;
@@ -1794,7 +1916,7 @@ struct Joint {                                                          // joint
         data.velocities[indexB].w = wB;
     }
 
-    void SolveVelocityConstraints(const SolverData& data) {             // b2revolutejoint.d:441-549
+    void RevoluteSolveVelocity(const SolverData& data) {                // b2revolutejoint.d:441-549
         Vec2 vA = data.velocities[indexA].v;
         f32 wA = data.velocities[indexA].w;
         Vec2 vB = data.velocities[indexB].v;
@@ -1869,7 +1991,7 @@ struct Joint {                                                          // joint
         data.velocities[indexB].w = wB;
     }
 
-    bool SolvePositionConstraints(const SolverData& data) {             // b2revolutejoint.d:551-636
+    bool RevoluteSolvePosition(const SolverData& data) {                // b2revolutejoint.d:551-636
         Vec2 cA = data.positions[indexA].c;
         f32 aA = data.positions[indexA].a;
         Vec2 cB = data.positions[indexB].c;
@@ -2866,6 +2988,24 @@ struct World {                                                          // dynam
         return f;
     }
 
+    Joint* CreateDistance(const dbox_distance_def* def) {               // b2world.d:196-261, b2distancejoint.d:122-133
+        Joint* j = new Joint();
+        j->type = kDistanceJoint;
+        j->bodyA = bodiesByIndex[def->body_a];
+        j->bodyB = bodiesByIndex[def->body_b];
+        j->collideConnected = def->collide_connected != 0;
+        j->islandFlag = false;
+        j->localAnchorA = Vec2(def->local_anchor_a.x, def->local_anchor_a.y);
+        j->localAnchorB = Vec2(def->local_anchor_b.x, def->local_anchor_b.y);
+        j->length = def->length;
+        j->frequencyHz = def->frequency_hz;
+        j->dampingRatio = def->damping_ratio;
+        j->impulse.SetZero();
+        j->gamma = 0.0f;
+        j->bias = 0.0f;
+        return LinkJoint(j);
+    }
+
     Joint* CreateRevolute(const dbox_revolute_def* def) {               // b2world.d:196-261
         Joint* j = new Joint();
         j->bodyA = bodiesByIndex[def->body_a];
@@ -2884,6 +3024,12 @@ struct World {                                                          // dynam
         j->enableLimit = def->enable_limit != 0;
         j->enableMotor = def->enable_motor != 0;
         j->limitState = kInactiveLimit;
+        return LinkJoint(j);
+    }
+
+    // the joint into the world's list and both bodies' edge lists, and the contact filter
+    // flag when the bodies may not collide (b2world.d:206-258)
+    Joint* LinkJoint(Joint* j) {
         j->prev = nullptr;
         j->next = jointList;
         if (jointList) jointList->prev = j;
@@ -2901,7 +3047,7 @@ struct World {                                                          // dynam
         j->edgeB.next = j->bodyB->jointList;
         if (j->bodyB->jointList) j->bodyB->jointList->prev = &j->edgeB;
         j->bodyB->jointList = &j->edgeB;
-        if (def->collide_connected == 0) {
+        if (!j->collideConnected) {
             for (ContactEdge* edge = j->bodyB->contactList; edge; edge = edge->next) {
                 if (edge->other == j->bodyA) edge->contact->flags |= kContactFilter;
             }
@@ -3275,6 +3421,12 @@ int orc_joint_create_revolute(orc_world* w, const dbox_revolute_def* def) {
     int n = (int)w->w.bodiesByIndex.size();
     if (def->body_a < 0 || def->body_a >= n || def->body_b < 0 || def->body_b >= n || def->body_a == def->body_b) return -1;
     return w->w.CreateRevolute(def)->index;
+}
+
+int orc_joint_create_distance(orc_world* w, const dbox_distance_def* def) {
+    int n = (int)w->w.bodiesByIndex.size();
+    if (def->body_a < 0 || def->body_a >= n || def->body_b < 0 || def->body_b >= n || def->body_a == def->body_b) return -1;
+    return w->w.CreateDistance(def)->index;
 }
 
 int orc_scene_create(orc_world* w, int n_bodies, const dbox_body_def* bodies, int n_fixtures,

@@ -178,3 +178,22 @@ def test_pyramid_reference_trig_one_step(oracle_lib, gpu_lib):
             assert dp <= 1e-5 and da <= 1e-5 and dv <= 1e-4, "step %d: %s" % (t + 1, (dp, da, dv))
     finally:
         oracle_lib.set_trig_mode(1)
+
+
+def test_distance_joint_ropes_exact(oracle_lib, gpu_lib):
+    # distance joints (rigid, soft, a long soft tie) beside a revolute chain and box stacks:
+    # bit-exact against the oracle, in one world and in a batch with other worlds
+    from dbox_gb300 import scenes
+    oracle_lib.set_trig_mode(1)
+    worlds = [scenes.ropes(), scenes.ropes(n_ropes=3, links=8, revolute=False),
+              scenes.pyramid(rows=6), scenes.chains(n_chains=2, links=10)]
+    gw = gpu_lib.World(worlds)
+    ows = [oracle_lib.OracleWorld(s) for s in worlds]
+    for t in range(150):
+        gw.step()
+        for ow in ows:
+            ow.step()
+        if t % 30 == 29:
+            for i, ow in enumerate(ows):
+                d = exact_diff(ow.export_state(), gw.export_state(i))
+                assert not d, "world %d step %d: %s" % (i, t + 1, d[:6])

@@ -174,3 +174,25 @@ def test_hello_world_prints_reference_line(oracle_lib):
         w.step(1.0 / 60.0, 6, 2)
     b = w.export_state()["bodies"][1]
     assert "%4.2f %4.2f %4.2f" % (b["xf"][0], b["xf"][1], b["sweep"][7]) == "0.00 1.01 0.00"
+
+
+def test_distance_joint_ropes_hold_their_length(oracle_lib):
+    # b2DistanceJoint (joints/b2distancejoint.d): rigid ropes keep each link at the joint
+    # length from its neighbour; soft ropes (4 Hz) stretch under their weight but stay bounded;
+    # the joint impulses carry over between steps (warm start)
+    from dbox_gb300 import scenes
+    oracle_lib.set_trig_mode(1)
+    s = scenes.ropes(n_ropes=2, links=10, pile=False, revolute=False)
+    ow = oracle_lib.OracleWorld(s)
+    ow.step(steps=240)
+    st = ow.export_state()
+    xy = st["bodies"]["xf"][:, :2].astype(np.float64)
+    gap = 0.3
+    for r, rigid in ((0, True), (1, False)):
+        post = 1 + r * 11                      # ground, then per rope: post + 10 links
+        d = np.linalg.norm(np.diff(xy[post:post + 11], axis=0), axis=1)
+        if rigid:
+            assert np.abs(d - gap).max() < 0.01, d
+        else:
+            assert d.max() < 4.0 * gap and d.min() > 0.5 * gap, d
+    assert (st["joints"]["impulse"][:, 0] != 0).all()
