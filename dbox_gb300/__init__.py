@@ -47,6 +47,8 @@ def lib():
     L.dbox_fixture_create.argtypes = [vp, i32, i32, vp, vp, ctypes.POINTER(i32)]
     L.dbox_joint_create_revolute.argtypes = [vp, i32, vp, ctypes.POINTER(i32)]
     L.dbox_joint_create_distance.argtypes = [vp, i32, vp, ctypes.POINTER(i32)]
+    L.dbox_joint_create_rope.argtypes = [vp, i32, vp, ctypes.POINTER(i32)]
+    L.dbox_joint_create_weld.argtypes = [vp, i32, vp, ctypes.POINTER(i32)]
     L.dbox_world_set_flags.argtypes = [vp, i32, i32, i32, i32, i32]
     L.dbox_world_set_gravity.argtypes = [vp, abi.Vec2]
     L.dbox_world_step.argtypes = [vp, f32, i32, i32]
@@ -228,17 +230,29 @@ class World:
             j = np.ascontiguousarray(s["joints"])
             _check(L.dbox_scene_create(self.h, i, len(b), abi.ptr(b), len(fb), abi.ptr(fb), abi.ptr(sh), abi.ptr(fx),
                                        len(j), abi.ptr(j) if len(j) else None), "dbox_scene_create")
-            for d in s.get("distance_joints", ()):           # created after the revolute joints
-                self.create_distance_joint(i, d)
+            # joint kinds after the revolute joints, in this order (the oracle's order too)
+            for d in s.get("distance_joints", ()):
+                self.create_joint(i, "distance", d)
+            for d in s.get("rope_joints", ()):
+                self.create_joint(i, "rope", d)
+            for d in s.get("weld_joints", ()):
+                self.create_joint(i, "weld", d)
         self.body_counts = [len(s["bodies"]) for s in scenes]
         if flags is not None:
             self.set_flags(**flags)
 
-    def create_distance_joint(self, world, d):
-        """b2World.CreateJoint with a b2DistanceJointDef (a DISTANCE_DEF record); returns the joint index."""
-        dd = np.ascontiguousarray(np.array([d], abi.DISTANCE_DEF))
+    _JOINT_KINDS = {"distance": ("DISTANCE_DEF", "dbox_joint_create_distance"),
+                    "rope": ("ROPE_DEF", "dbox_joint_create_rope"),
+                    "weld": ("WELD_DEF", "dbox_joint_create_weld")}
+
+    def create_joint(self, world, kind, d):
+        """b2World.CreateJoint with a b2DistanceJointDef / b2RopeJointDef / b2WeldJointDef
+        (kind "distance", "rope" or "weld"; d a DISTANCE_DEF / ROPE_DEF / WELD_DEF record);
+        returns the joint index."""
+        dtype, fn = World._JOINT_KINDS[kind]
+        dd = np.ascontiguousarray(np.array([d], getattr(abi, dtype)))
         out = ctypes.c_int32()
-        _check(lib().dbox_joint_create_distance(self.h, world, abi.ptr(dd), ctypes.byref(out)), "dbox_joint_create_distance")
+        _check(getattr(lib(), fn)(self.h, world, abi.ptr(dd), ctypes.byref(out)), fn)
         return out.value
 
     def close(self):

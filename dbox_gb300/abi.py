@@ -41,6 +41,17 @@ DISTANCE_DEF = np.dtype([
     ("length", "<f4"), ("frequency_hz", "<f4"), ("damping_ratio", "<f4"),
 ])
 assert DISTANCE_DEF.itemsize == 40
+ROPE_DEF = np.dtype([
+    ("body_a", "<i4"), ("body_b", "<i4"), ("collide_connected", "<i4"),
+    ("local_anchor_a", "<f4", 2), ("local_anchor_b", "<f4", 2), ("max_length", "<f4"),
+])
+assert ROPE_DEF.itemsize == 32
+WELD_DEF = np.dtype([
+    ("body_a", "<i4"), ("body_b", "<i4"), ("collide_connected", "<i4"),
+    ("local_anchor_a", "<f4", 2), ("local_anchor_b", "<f4", 2),
+    ("reference_angle", "<f4"), ("frequency_hz", "<f4"), ("damping_ratio", "<f4"),
+])
+assert WELD_DEF.itemsize == 40
 
 WORLD_HEADER = np.dtype([
     ("body_count", "<i4"), ("fixture_count", "<i4"), ("contact_count", "<i4"), ("joint_count", "<i4"),

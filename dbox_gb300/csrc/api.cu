@@ -986,6 +986,60 @@ int32_t dbox_joint_create_revolute(dbox_world* w, int32_t world, const dbox_revo
     return DBOX_OK;
 }
 
+// b2World.CreateJoint with a b2RopeJointDef (b2ropejoint.d:140-153)
+int create_rope_joint(HostWorld& hw, const dbox_rope_def* d) {
+    int nb = (int)hw.bs.size();
+    if (d->body_a < 0 || d->body_a >= nb || d->body_b < 0 || d->body_b >= nb || d->body_a == d->body_b) return -1;
+    dg::DJoint j;
+    memset(&j, 0, sizeof(j));
+    j.type = dg::kRopeJoint;
+    j.body_a = d->body_a;
+    j.body_b = d->body_b;
+    j.collide_connected = d->collide_connected ? 1 : 0;
+    j.local_anchor_a = make_float2(d->local_anchor_a.x, d->local_anchor_a.y);
+    j.local_anchor_b = make_float2(d->local_anchor_b.x, d->local_anchor_b.y);
+    j.length = d->max_length;
+    return link_joint(hw, j);
+}
+
+// b2World.CreateJoint with a b2WeldJointDef (b2weldjoint.d:107-119)
+int create_weld_joint(HostWorld& hw, const dbox_weld_def* d) {
+    int nb = (int)hw.bs.size();
+    if (d->body_a < 0 || d->body_a >= nb || d->body_b < 0 || d->body_b >= nb || d->body_a == d->body_b) return -1;
+    dg::DJoint j;
+    memset(&j, 0, sizeof(j));
+    j.type = dg::kWeldJoint;
+    j.body_a = d->body_a;
+    j.body_b = d->body_b;
+    j.collide_connected = d->collide_connected ? 1 : 0;
+    j.local_anchor_a = make_float2(d->local_anchor_a.x, d->local_anchor_a.y);
+    j.local_anchor_b = make_float2(d->local_anchor_b.x, d->local_anchor_b.y);
+    j.reference_angle = d->reference_angle;
+    j.frequency_hz = d->frequency_hz;
+    j.damping_ratio = d->damping_ratio;
+    return link_joint(hw, j);
+}
+
+int32_t dbox_joint_create_rope(dbox_world* w, int32_t world, const dbox_rope_def* def, int32_t* out_joint) {
+    if (!w || !def || world < 0 || world >= (int)w->worlds.size()) return fail(DBOX_ERR_INVALID, "dbox_joint_create_rope: bad arguments");
+    int rc = prepare_edit(w);
+    if (rc) return rc;
+    int idx = create_rope_joint(w->worlds[world], def);
+    if (idx < 0) return fail(DBOX_ERR_INVALID, "dbox_joint_create_rope: bad bodies");
+    if (out_joint) *out_joint = idx;
+    return DBOX_OK;
+}
+
+int32_t dbox_joint_create_weld(dbox_world* w, int32_t world, const dbox_weld_def* def, int32_t* out_joint) {
+    if (!w || !def || world < 0 || world >= (int)w->worlds.size()) return fail(DBOX_ERR_INVALID, "dbox_joint_create_weld: bad arguments");
+    int rc = prepare_edit(w);
+    if (rc) return rc;
+    int idx = create_weld_joint(w->worlds[world], def);
+    if (idx < 0) return fail(DBOX_ERR_INVALID, "dbox_joint_create_weld: bad bodies");
+    if (out_joint) *out_joint = idx;
+    return DBOX_OK;
+}
+
 int32_t dbox_joint_create_distance(dbox_world* w, int32_t world, const dbox_distance_def* def, int32_t* out_joint) {
     if (!w || !def || world < 0 || world >= (int)w->worlds.size()) return fail(DBOX_ERR_INVALID, "dbox_joint_create_distance: bad arguments");
     int rc = prepare_edit(w);

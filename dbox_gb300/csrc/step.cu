@@ -1290,6 +1290,25 @@ DG float solve_position_row(const PC& pc, SB sb) {
     return solve_position(pc, sb, false, -1, -1);
 }
 
+DG float3 solve33(const float* m, float3 b) {                            // b2math.d:388-399
+    float3 ex = make_float3(m[0], m[1], m[2]), ey = make_float3(m[3], m[4], m[5]), ez = make_float3(m[6], m[7], m[8]);
+    auto cr = [](float3 a, float3 c) { return make_float3(a.y * c.z - a.z * c.y, a.z * c.x - a.x * c.z, a.x * c.y - a.y * c.x); };
+    auto dt3 = [](float3 a, float3 c) { return (a.x * c.x + a.y * c.y) + a.z * c.z; };
+    float det = dt3(ex, cr(ey, ez));
+    if (det != 0.0f) det = fdiv(1.0f, det);
+    float3 r;
+    r.x = det * dt3(b, cr(ey, ez));
+    r.y = det * dt3(ex, cr(b, ez));
+    r.z = det * dt3(ex, cr(ey, b));
+    return r;
+}
+DG float2 solve22(const float* m, float2 b) {                            // b2math.d:402-415
+    float a11 = m[0], a12 = m[3], a21 = m[1], a22 = m[4];
+    float det = a11 * a22 - a12 * a21;
+    if (det != 0.0f) det = fdiv(1.0f, det);
+    return v2(det * (a22 * b.x - a12 * b.y), det * (a11 * b.y - a21 * b.x));
+}
+
 // ------------------------------------------------------------ distance joint (joints/b2distancejoint.d:211-372)
 __device__ __noinline__ void distance_init(const Ctx& x, int ji, int b0, SB sb, bool warm, float dtRatio) {
     DJoint& j = x.jt[ji];
@@ -1386,9 +1405,290 @@ __device__ __noinline__ bool distance_solve_position(const DJoint& j, int la, in
     return babs(C) < kLinearSlop;
 }
 
+// ------------------------------------------------------------ rope joint (joints/b2ropejoint.d:165-317)
+__device__ __noinline__ void rope_init(const Ctx& x, int ji, int b0, SB sb, bool warm, float dtRatio) {
+    DJoint& j = x.jt[ji];
+    const dbox_body_state& ba = x.bs[j.body_a];
+    const dbox_body_state& bb = x.bs[j.body_b];
+    int la = j.body_a - b0, lb = j.body_b - b0;
+    j.lcA = b_lc(ba);
+    j.lcB = b_lc(bb);
+    j.invMassA = ba.mass[1];
+    j.invMassB = bb.mass[1];
+    j.invIA = ba.mass[3];
+    j.invIB = bb.mass[3];
+    float2 cA = sb.c(la), cB = sb.c(lb);
+    float aA = sb.a(la), aB = sb.a(lb);
+    float2 vA = sb.v(la), vB = sb.v(lb);
+    float wA = sb.w(la), wB = sb.w(lb);
+    Rot qA = rot(aA), qB = rot(aB);
+    j.rA = mul(qA, j.local_anchor_a - j.lcA);
+    j.rB = mul(qB, j.local_anchor_b - j.lcB);
+    float2 u = ((cB + j.rB) - cA) - j.rA;
+    j.cur_length = length(u);
+    float C = j.cur_length - j.length;
+    j.limit_state = C > 0.0f ? 2 : 0;                                  // at upper limit / inactive
+    if (j.cur_length > kLinearSlop) {
+        u *= fdiv(1.0f, j.cur_length);
+    } else {
+        j.u = v2(0.0f, 0.0f);
+        j.mass[0] = 0.0f;
+        j.impulse[0] = 0.0f;
+        return;
+    }
+    j.u = u;
+    float crA = cross(j.rA, u), crB = cross(j.rB, u);
+    float invMass = ((j.invMassA + (j.invIA * crA) * crA) + j.invMassB) + (j.invIB * crB) * crB;
+    j.mass[0] = invMass != 0.0f ? fdiv(1.0f, invMass) : 0.0f;
+    if (warm) {
+        j.impulse[0] *= dtRatio;
+        float2 P = j.impulse[0] * u;
+        vA -= j.invMassA * P;
+        wA -= j.invIA * cross(j.rA, P);
+        vB += j.invMassB * P;
+        wB += j.invIB * cross(j.rB, P);
+    } else {
+        j.impulse[0] = 0.0f;
+    }
+    sb.set_v(la, vA, wA);
+    sb.set_v(lb, vB, wB);
+}
+
+DG void rope_solve_velocity(const Ctx& x, DJoint& j, int la, int lb, SB sb) {
+    float2 vA = sb.v(la), vB = sb.v(lb);
+    float wA = sb.w(la), wB = sb.w(lb);
+    float2 vpA = vA + cross(wA, j.rA);
+    float2 vpB = vB + cross(wB, j.rB);
+    float C = j.cur_length - j.length;
+    float Cdot = dot(j.u, vpB - vpA);
+    if (C < 0.0f) Cdot += x.inv_dt * C;                                 // predictive constraint
+    float impulse = -j.mass[0] * Cdot;
+    float oldImpulse = j.impulse[0];
+    j.impulse[0] = bmin(0.0f, j.impulse[0] + impulse);
+    impulse = j.impulse[0] - oldImpulse;
+    float2 P = impulse * j.u;
+    vA -= j.invMassA * P;
+    wA -= j.invIA * cross(j.rA, P);
+    vB += j.invMassB * P;
+    wB += j.invIB * cross(j.rB, P);
+    sb.set_v(la, vA, wA);
+    sb.set_v(lb, vB, wB);
+}
+
+__device__ __noinline__ bool rope_solve_position(const DJoint& j, int la, int lb, SB sb) {
+    float2 cA = sb.c(la), cB = sb.c(lb);
+    float aA = sb.a(la), aB = sb.a(lb);
+    Rot qA = rot(aA), qB = rot(aB);
+    float2 rA = mul(qA, j.local_anchor_a - j.lcA);
+    float2 rB = mul(qB, j.local_anchor_b - j.lcB);
+    float2 u = ((cB + rB) - cA) - rA;
+    float len = normalize(u);
+    float C = bclamp(len - j.length, 0.0f, kMaxLinearCorrection);
+    float impulse = -j.mass[0] * C;
+    float2 P = impulse * u;
+    cA -= j.invMassA * P;
+    aA -= j.invIA * cross(rA, P);
+    cB += j.invMassB * P;
+    aB += j.invIB * cross(rB, P);
+    sb.set_c(la, cA, aA);
+    sb.set_c(lb, cB, aB);
+    return len - j.length < kLinearSlop;
+}
+
+// ------------------------------------------------------------ weld joint (joints/b2weldjoint.d:196-444)
+// b2Mat33 in the joint's mass[9] layout: ex.x ex.y ex.z ey.x ey.y ey.z ez.x ez.y ez.z
+DG void weld_k(float* K, float mA, float mB, float iA, float iB, float2 ra, float2 rb) {
+    K[0] = ((mA + mB) + (ra.y * ra.y) * iA) + (rb.y * rb.y) * iB;       // ex.x
+    K[3] = ((-ra.y) * ra.x) * iA - (rb.y * rb.x) * iB;                  // ey.x
+    K[6] = (-ra.y) * iA - rb.y * iB;                                    // ez.x
+    K[1] = K[3];                                                        // ex.y
+    K[4] = ((mA + mB) + (ra.x * ra.x) * iA) + (rb.x * rb.x) * iB;       // ey.y
+    K[7] = ra.x * iA + rb.x * iB;                                       // ez.y
+    K[2] = K[6];                                                        // ex.z
+    K[5] = K[7];                                                        // ey.z
+    K[8] = iA + iB;                                                     // ez.z
+}
+DG void inverse22(const float* K, float* M) {                             // b2math.d:419-440
+    float a = K[0], b = K[3], c = K[1], d = K[4];
+    float det = a * d - b * c;
+    if (det != 0.0f) det = fdiv(1.0f, det);
+    M[0] = det * d;
+    M[3] = -det * b;
+    M[2] = 0.0f;
+    M[1] = -det * c;
+    M[4] = det * a;
+    M[5] = 0.0f;
+    M[6] = 0.0f;
+    M[7] = 0.0f;
+    M[8] = 0.0f;
+}
+DG void sym_inverse33(const float* K, float* M) {                        // b2math.d:442-465
+    float3 ex = make_float3(K[0], K[1], K[2]), ey = make_float3(K[3], K[4], K[5]), ez = make_float3(K[6], K[7], K[8]);
+    float3 c = make_float3(ey.y * ez.z - ey.z * ez.y, ey.z * ez.x - ey.x * ez.z, ey.x * ez.y - ey.y * ez.x);
+    float det = (ex.x * c.x + ex.y * c.y) + ex.z * c.z;
+    if (det != 0.0f) det = fdiv(1.0f, det);
+    float a11 = ex.x, a12 = ey.x, a13 = ez.x;
+    float a22 = ey.y, a23 = ez.y;
+    float a33 = ez.z;
+    M[0] = det * (a22 * a33 - a23 * a23);
+    M[1] = det * (a13 * a23 - a12 * a33);
+    M[2] = det * (a12 * a23 - a13 * a22);
+    M[3] = M[1];
+    M[4] = det * (a11 * a33 - a13 * a13);
+    M[5] = det * (a13 * a12 - a11 * a23);
+    M[6] = M[2];
+    M[7] = M[5];
+    M[8] = det * (a11 * a22 - a12 * a12);
+}
+
+__device__ __noinline__ void weld_init(const Ctx& x, int ji, int b0, SB sb, bool warm, float dtRatio) {
+    DJoint& j = x.jt[ji];
+    const dbox_body_state& ba = x.bs[j.body_a];
+    const dbox_body_state& bb = x.bs[j.body_b];
+    int la = j.body_a - b0, lb = j.body_b - b0;
+    j.lcA = b_lc(ba);
+    j.lcB = b_lc(bb);
+    j.invMassA = ba.mass[1];
+    j.invMassB = bb.mass[1];
+    j.invIA = ba.mass[3];
+    j.invIB = bb.mass[3];
+    float aA = sb.a(la), aB = sb.a(lb);
+    float2 vA = sb.v(la), vB = sb.v(lb);
+    float wA = sb.w(la), wB = sb.w(lb);
+    Rot qA = rot(aA), qB = rot(aB);
+    j.rA = mul(qA, j.local_anchor_a - j.lcA);
+    j.rB = mul(qB, j.local_anchor_b - j.lcB);
+    const float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    float K[9];
+    weld_k(K, mA, mB, iA, iB, j.rA, j.rB);
+    if (j.frequency_hz > 0.0f) {
+        inverse22(K, j.mass);
+        float invM = iA + iB;
+        float m = invM > 0.0f ? fdiv(1.0f, invM) : 0.0f;
+        float C = (aB - aA) - j.reference_angle;
+        float omega = (2.0f * kPi) * j.frequency_hz;
+        float d = ((2.0f * m) * j.damping_ratio) * omega;
+        float k = (m * omega) * omega;
+        float h = x.dt;
+        float gamma = h * (d + h * k);
+        gamma = gamma != 0.0f ? fdiv(1.0f, gamma) : 0.0f;
+        j.gamma = gamma;
+        j.bias = ((C * h) * k) * gamma;
+        invM += gamma;
+        j.mass[8] = invM != 0.0f ? fdiv(1.0f, invM) : 0.0f;
+    } else if (K[8] == 0.0f) {
+        inverse22(K, j.mass);
+        j.gamma = 0.0f;
+        j.bias = 0.0f;
+    } else {
+        sym_inverse33(K, j.mass);
+        j.gamma = 0.0f;
+        j.bias = 0.0f;
+    }
+    if (warm) {
+        j.impulse[0] *= dtRatio; j.impulse[1] *= dtRatio; j.impulse[2] *= dtRatio;
+        float2 P = v2(j.impulse[0], j.impulse[1]);
+        vA -= mA * P;
+        wA -= iA * (cross(j.rA, P) + j.impulse[2]);
+        vB += mB * P;
+        wB += iB * (cross(j.rB, P) + j.impulse[2]);
+    } else {
+        j.impulse[0] = 0.0f; j.impulse[1] = 0.0f; j.impulse[2] = 0.0f;
+    }
+    sb.set_v(la, vA, wA);
+    sb.set_v(lb, vB, wB);
+}
+
+__device__ __noinline__ void weld_solve_velocity(DJoint& j, int la, int lb, SB sb) {
+    float2 vA = sb.v(la), vB = sb.v(lb);
+    float wA = sb.w(la), wB = sb.w(lb);
+    const float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    const float* M = j.mass;
+    if (j.frequency_hz > 0.0f) {
+        float Cdot2 = wB - wA;
+        float impulse2 = -M[8] * ((Cdot2 + j.bias) + j.gamma * j.impulse[2]);
+        j.impulse[2] += impulse2;
+        wA -= iA * impulse2;
+        wB += iB * impulse2;
+        float2 Cdot1 = ((vB + cross(wB, j.rB)) - vA) - cross(wA, j.rA);
+        float2 impulse1 = -v2(M[0] * Cdot1.x + M[3] * Cdot1.y, M[1] * Cdot1.x + M[4] * Cdot1.y);
+        j.impulse[0] += impulse1.x;
+        j.impulse[1] += impulse1.y;
+        float2 P = impulse1;
+        vA -= mA * P;
+        wA -= iA * cross(j.rA, P);
+        vB += mB * P;
+        wB += iB * cross(j.rB, P);
+    } else {
+        float2 Cdot1 = ((vB + cross(wB, j.rB)) - vA) - cross(wA, j.rA);
+        float Cdot2 = wB - wA;
+        float3 imp = make_float3(-((Cdot1.x * M[0] + Cdot1.y * M[3]) + Cdot2 * M[6]),
+                                 -((Cdot1.x * M[1] + Cdot1.y * M[4]) + Cdot2 * M[7]),
+                                 -((Cdot1.x * M[2] + Cdot1.y * M[5]) + Cdot2 * M[8]));
+        j.impulse[0] += imp.x;
+        j.impulse[1] += imp.y;
+        j.impulse[2] += imp.z;
+        float2 P = v2(imp.x, imp.y);
+        vA -= mA * P;
+        wA -= iA * (cross(j.rA, P) + imp.z);
+        vB += mB * P;
+        wB += iB * (cross(j.rB, P) + imp.z);
+    }
+    sb.set_v(la, vA, wA);
+    sb.set_v(lb, vB, wB);
+}
+
+__device__ __noinline__ bool weld_solve_position(const DJoint& j, int la, int lb, SB sb) {
+    float2 cA = sb.c(la), cB = sb.c(lb);
+    float aA = sb.a(la), aB = sb.a(lb);
+    Rot qA = rot(aA), qB = rot(aB);
+    const float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    float2 rA = mul(qA, j.local_anchor_a - j.lcA);
+    float2 rB = mul(qB, j.local_anchor_b - j.lcB);
+    float positionError, angularError;
+    float K[9];
+    weld_k(K, mA, mB, iA, iB, rA, rB);
+    if (j.frequency_hz > 0.0f) {
+        float2 C1 = ((cB + rB) - cA) - rA;
+        positionError = length(C1);
+        angularError = 0.0f;
+        float2 P = -solve22(K, C1);
+        cA -= mA * P;
+        aA -= iA * cross(rA, P);
+        cB += mB * P;
+        aB += iB * cross(rB, P);
+    } else {
+        float2 C1 = ((cB + rB) - cA) - rA;
+        float C2 = (aB - aA) - j.reference_angle;
+        positionError = length(C1);
+        angularError = babs(C2);
+        float3 imp;
+        if (K[8] > 0.0f) {
+            float3 r = solve33(K, make_float3(C1.x, C1.y, C2));
+            imp = make_float3(-r.x, -r.y, -r.z);
+        } else {
+            float2 r = solve22(K, C1);
+            imp = make_float3(-r.x, -r.y, 0.0f);
+        }
+        float2 P = v2(imp.x, imp.y);
+        cA -= mA * P;
+        aA -= iA * (cross(rA, P) + imp.z);
+        cB += mB * P;
+        aB += iB * (cross(rB, P) + imp.z);
+    }
+    sb.set_c(la, cA, aA);
+    sb.set_c(lb, cB, aB);
+    return positionError <= kLinearSlop && angularError <= kAngularSlop;
+}
+
 // ------------------------------------------------------------ revolute joint (joints/b2revolutejoint.d:319-636)
 DG void joint_init(const Ctx& x, int ji, int b0, SB sb, bool warm, float dtRatio) {
-    if (x.jt[ji].type == kDistanceJoint) { distance_init(x, ji, b0, sb, warm, dtRatio); return; }
+    switch (x.jt[ji].type) {
+    case kDistanceJoint: distance_init(x, ji, b0, sb, warm, dtRatio); return;
+    case kRopeJoint: rope_init(x, ji, b0, sb, warm, dtRatio); return;
+    case kWeldJoint: weld_init(x, ji, b0, sb, warm, dtRatio); return;
+    default: break;
+    }
     DJoint& j = x.jt[ji];
     const dbox_body_state& ba = x.bs[j.body_a];
     const dbox_body_state& bb = x.bs[j.body_b];
@@ -1456,29 +1756,12 @@ DG void joint_init(const Ctx& x, int ji, int b0, SB sb, bool warm, float dtRatio
     sb.set_v(lb, vB, wB);
 }
 
-DG float3 solve33(const float* m, float3 b) {                            // b2math.d:388-399
-    float3 ex = make_float3(m[0], m[1], m[2]), ey = make_float3(m[3], m[4], m[5]), ez = make_float3(m[6], m[7], m[8]);
-    auto cr = [](float3 a, float3 c) { return make_float3(a.y * c.z - a.z * c.y, a.z * c.x - a.x * c.z, a.x * c.y - a.y * c.x); };
-    auto dt3 = [](float3 a, float3 c) { return (a.x * c.x + a.y * c.y) + a.z * c.z; };
-    float det = dt3(ex, cr(ey, ez));
-    if (det != 0.0f) det = fdiv(1.0f, det);
-    float3 r;
-    r.x = det * dt3(b, cr(ey, ez));
-    r.y = det * dt3(ex, cr(b, ez));
-    r.z = det * dt3(ex, cr(ey, b));
-    return r;
-}
-DG float2 solve22(const float* m, float2 b) {                            // b2math.d:402-415
-    float a11 = m[0], a12 = m[3], a21 = m[1], a22 = m[4];
-    float det = a11 * a22 - a12 * a21;
-    if (det != 0.0f) det = fdiv(1.0f, det);
-    return v2(det * (a22 * b.x - a12 * b.y), det * (a11 * b.y - a21 * b.x));
-}
-
 DG void joint_solve_velocity(const Ctx& x, int ji, int b0, SB sb) {
     DJoint& j = x.jt[ji];
     int la = j.body_a - b0, lb = j.body_b - b0;
     if (j.type == kDistanceJoint) { distance_solve_velocity(j, la, lb, sb); return; }
+    if (j.type == kRopeJoint) { rope_solve_velocity(x, j, la, lb, sb); return; }
+    if (j.type == kWeldJoint) { weld_solve_velocity(j, la, lb, sb); return; }
     float2 vA = sb.v(la), vB = sb.v(lb);
     float wA = sb.w(la), wB = sb.w(lb);
     float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
@@ -1539,6 +1822,8 @@ DG bool joint_solve_position(const Ctx& x, int ji, int b0, SB sb) {
     DJoint& j = x.jt[ji];
     int la = j.body_a - b0, lb = j.body_b - b0;
     if (j.type == kDistanceJoint) return distance_solve_position(j, la, lb, sb);
+    if (j.type == kRopeJoint) return rope_solve_position(j, la, lb, sb);
+    if (j.type == kWeldJoint) return weld_solve_position(j, la, lb, sb);
     float2 cA = sb.c(la), cB = sb.c(lb);
     float aA = sb.a(la), aB = sb.a(lb);
     float angularError = 0.0f, positionError = 0.0f;

@@ -68,8 +68,10 @@ struct BodyStatic {
     int jadj_start, jadj_count;    // into Ctx.jadj_joint / jadj_other (descending joint index)
 };
 
-enum { kRevoluteJoint = 0, kDistanceJoint = 1 };
-struct DJoint {                    // b2RevoluteJoint / b2DistanceJoint (joints/b2revolutejoint.d, b2distancejoint.d)
+enum { kRevoluteJoint = 0, kDistanceJoint = 1, kRopeJoint = 2, kWeldJoint = 3 };
+// b2RevoluteJoint / b2DistanceJoint / b2RopeJoint / b2WeldJoint (joints/b2revolutejoint.d,
+// b2distancejoint.d, b2ropejoint.d, b2weldjoint.d)
+struct DJoint {
     int body_a, body_b;
     int collide_connected;
     int island_flag;
@@ -86,9 +88,11 @@ struct DJoint {                    // b2RevoluteJoint / b2DistanceJoint (joints/
     float invMassA, invMassB, invIA, invIB;
     float mass[9];                 // ex.x ex.y ex.z ey.x ey.y ey.z ez.x ez.y ez.z; distance: mass[0]
     float motor_mass;
-    int type;                      // kRevoluteJoint or kDistanceJoint; a distance joint keeps its impulse in impulse[0]
-    float length, frequency_hz, damping_ratio, gamma, bias;   // distance joint
-    float2 u;                      // distance joint: unit vector from anchor A to anchor B
+    int type;                      // k*Joint; distance and rope joints keep their impulse in impulse[0]
+    float length, frequency_hz, damping_ratio, gamma, bias;   // distance (length), rope (maximum length), weld
+    float2 u;                      // distance / rope: unit vector from anchor A to anchor B
+    float cur_length;              // rope: anchor distance at InitVelocityConstraints
+    int pad2;
 };
 
 // b2ContactVelocityConstraint (contacts/b2contactsolver.d:43-58) with body indices in place of island indices.

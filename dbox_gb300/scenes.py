@@ -35,6 +35,7 @@ def _empty():
         "bodies": abi.body_defs(0), "fixture_body": np.zeros(0, np.int32),
         "shapes": np.zeros(0, abi.SHAPE_DEF), "fixtures": abi.fixture_defs(0),
         "joints": np.zeros(0, abi.REVOLUTE_DEF), "distance_joints": np.zeros(0, abi.DISTANCE_DEF),
+        "rope_joints": np.zeros(0, abi.ROPE_DEF), "weld_joints": np.zeros(0, abi.WELD_DEF),
         "gravity": (0.0, -10.0), "name": "",
     }
 
@@ -52,10 +53,12 @@ def _concat(parts):
         j["body_a"] += nb
         j["body_b"] += nb
         out["joints"] = np.concatenate([out["joints"], j])
-        d = p.get("distance_joints", np.zeros(0, abi.DISTANCE_DEF)).copy()
-        d["body_a"] += nb
-        d["body_b"] += nb
-        out["distance_joints"] = np.concatenate([out["distance_joints"], d])
+        for key, dtype in (("distance_joints", abi.DISTANCE_DEF), ("rope_joints", abi.ROPE_DEF),
+                           ("weld_joints", abi.WELD_DEF)):
+            d = p.get(key, np.zeros(0, dtype)).copy()
+            d["body_a"] += nb
+            d["body_b"] += nb
+            out[key] = np.concatenate([out[key], d])
         nb += len(p["bodies"])
     return out
 
@@ -257,6 +260,53 @@ def ropes(n_ropes=4, links=20, box=0.1, gap=0.3, x0=-9.0, spacing=6.0, y=14.0, p
         parts.append(part)
     out = _concat(parts)
     out["name"] = "ropes"
+    return out
+
+
+def welded(n_beams=3, links=8, hx=0.3, hy=0.08, x0=-8.0, spacing=6.0, y=10.0, pile=True):
+    """Weld and rope joints (b2WeldJointDef joints/b2weldjoint.d:30-86, b2RopeJointDef
+    joints/b2ropejoint.d:30-52): each beam is `links` boxes welded end to end and to a
+    static post (rigid welds on even beams, angularly soft welds, 3 Hz, on odd beams); a
+    rope of maximum length 1.5 m ties the free end of each beam to a box hanging below it,
+    and a second, taut rope ties that box to a point on the ground below it.  Box stacks stand below when `pile` is set."""
+    parts = [ground_box()]
+    if pile:
+        parts.append(stacks(3 * n_beams, 3, spacing=spacing / 2.0))
+    for b in range(n_beams):
+        x = x0 + b * spacing
+        post = _boxes([(x, y)], 0.2, 0.2, abi.STATIC)
+        beam = _boxes([(x + 0.2 + hx + 2 * hx * i, y) for i in range(links)], hx, hy, abi.DYNAMIC, 0.5, 2.0)
+        weight = _boxes([(x + 0.2 + 2 * hx * links, y - 1.2)], 0.25, 0.25, abi.DYNAMIC, 0.5, 1.0)
+        part = _concat([post, beam, weight])
+        soft = b % 2 == 1
+        wj = np.zeros(links, abi.WELD_DEF)
+        for i in range(links):
+            wj[i]["body_a"] = i                      # the post for i = 0, else beam link i-1
+            wj[i]["body_b"] = i + 1
+            wj[i]["local_anchor_a"] = (0.2, 0.0) if i == 0 else (hx, 0.0)
+            wj[i]["local_anchor_b"] = (-hx, 0.0)
+            if soft:
+                wj[i]["frequency_hz"] = 3.0
+                wj[i]["damping_ratio"] = 0.4
+        rj = np.zeros(1, abi.ROPE_DEF)
+        rj[0]["body_a"] = links                      # the last beam link
+        rj[0]["body_b"] = links + 1                  # the weight
+        rj[0]["local_anchor_a"] = (hx, 0.0)
+        rj[0]["max_length"] = 1.5
+        part["weld_joints"] = wj
+        part["rope_joints"] = rj
+        parts.append(part)
+    out = _concat(parts)
+    # ropes from each weight to the ground body (body 0)
+    weights = np.nonzero(np.isclose(out["bodies"]["position"][:, 1], y - 1.2))[0]
+    extra = np.zeros(len(weights), abi.ROPE_DEF)
+    for k, wi in enumerate(weights):
+        extra[k]["body_a"] = 0
+        extra[k]["body_b"] = wi
+        extra[k]["local_anchor_a"] = (float(out["bodies"]["position"][wi, 0]), 10.0)
+        extra[k]["max_length"] = (y - 1.2) - 0.8        # taut: pulls the weight 0.8 m down
+    out["rope_joints"] = np.concatenate([out["rope_joints"], extra])
+    out["name"] = "welded"
     return out
 
 

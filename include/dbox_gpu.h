@@ -107,6 +107,24 @@ typedef struct {
     float damping_ratio;
 } dbox_distance_def;
 
+/* b2RopeJointDef (dynamics/joints/b2ropejoint.d:30-52) */
+typedef struct {
+    int32_t body_a, body_b;
+    int32_t collide_connected;
+    dbox_vec2 local_anchor_a, local_anchor_b;
+    float max_length;
+} dbox_rope_def;
+
+/* b2WeldJointDef (dynamics/joints/b2weldjoint.d:30-86) */
+typedef struct {
+    int32_t body_a, body_b;
+    int32_t collide_connected;
+    dbox_vec2 local_anchor_a, local_anchor_b;
+    float reference_angle;
+    float frequency_hz;    /* angular softness; 0 = rigid */
+    float damping_ratio;
+} dbox_weld_def;
+
 /* ------------------------------------------------------- world snapshot
  * Flat state records, used by dbox_world_export_state / import_state
  * (exact checkpoint/resume) and by the parity tests.  Flag words use the
@@ -216,6 +234,10 @@ int32_t dbox_joint_create_revolute(dbox_world* w, int32_t world, const dbox_revo
  * distance joint's impulse. */
 int32_t dbox_joint_create_distance(dbox_world* w, int32_t world, const dbox_distance_def* def,
                                    int32_t* out_joint);
+/* b2World.CreateJoint with a b2RopeJointDef (joints/b2ropejoint.d); snapshot: impulse[0], limit_state. */
+int32_t dbox_joint_create_rope(dbox_world* w, int32_t world, const dbox_rope_def* def, int32_t* out_joint);
+/* b2World.CreateJoint with a b2WeldJointDef (joints/b2weldjoint.d); snapshot: impulse[0..2]. */
+int32_t dbox_joint_create_weld(dbox_world* w, int32_t world, const dbox_weld_def* def, int32_t* out_joint);
 
 /* Bulk creation of a whole scene into one world: n bodies, then m fixtures
  * (fixture_body[i] indexes the bodies created by this call), then k joints

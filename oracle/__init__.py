@@ -45,6 +45,8 @@ def lib():
         L.orc_world_destroy.argtypes = [vp]
         L.orc_scene_create.argtypes = [vp, i32, vp, i32, vp, vp, vp, i32, vp]
         L.orc_joint_create_distance.argtypes = [vp, vp]
+        L.orc_joint_create_rope.argtypes = [vp, vp]
+        L.orc_joint_create_weld.argtypes = [vp, vp]
         L.orc_world_set_flags.argtypes = [vp, i32, i32, i32, i32, i32]
         L.orc_world_step.argtypes = [vp, f32, i32, i32]
         L.orc_world_step_n.argtypes = [vp, f32, i32, i32, i32]
@@ -112,10 +114,14 @@ class OracleWorld:
                                 len(j), abi.ptr(j) if len(j) else None)
         if rc != 0:
             raise ValueError("oracle scene creation failed")
-        for d in scene.get("distance_joints", ()):             # created after the revolute joints
-            dd = np.ascontiguousarray(np.array([d], abi.DISTANCE_DEF))
-            if L.orc_joint_create_distance(self.h, abi.ptr(dd)) < 0:
-                raise ValueError("oracle distance joint creation failed")
+        # joint kinds after the revolute joints, in this order (the same as the library's)
+        for key, dtype, fn in (("distance_joints", abi.DISTANCE_DEF, L.orc_joint_create_distance),
+                               ("rope_joints", abi.ROPE_DEF, L.orc_joint_create_rope),
+                               ("weld_joints", abi.WELD_DEF, L.orc_joint_create_weld)):
+            for d in scene.get(key, ()):
+                dd = np.ascontiguousarray(np.array([d], dtype))
+                if fn(self.h, abi.ptr(dd)) < 0:
+                    raise ValueError("oracle %s creation failed" % key)
         if flags is not None:
             self.set_flags(**flags)
 

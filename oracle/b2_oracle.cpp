@@ -149,6 +149,36 @@ struct Mat33 {                                                          // b2mat
         x.z = det * Dot(ex, Cross(ey, b));
         return x;
     }
+    void GetInverse22(Mat33* M) const {                                 // b2math.d:419-440
+        f32 a = ex.x, b = ey.x, c = ex.y, d = ey.y;
+        f32 det = a * d - b * c;
+        if (det != 0.0f) det = 1.0f / det;
+        M->ex.x = det * d;
+        M->ey.x = -det * b;
+        M->ex.z = 0.0f;
+        M->ex.y = -det * c;
+        M->ey.y = det * a;
+        M->ey.z = 0.0f;
+        M->ez.x = 0.0f;
+        M->ez.y = 0.0f;
+        M->ez.z = 0.0f;
+    }
+    void GetSymInverse33(Mat33* M) const {                              // b2math.d:442-465
+        f32 det = Dot(ex, Cross(ey, ez));
+        if (det != 0.0f) det = 1.0f / det;
+        f32 a11 = ex.x, a12 = ey.x, a13 = ez.x;
+        f32 a22 = ey.y, a23 = ez.y;
+        f32 a33 = ez.z;
+        M->ex.x = det * (a22 * a33 - a23 * a23);
+        M->ex.y = det * (a13 * a23 - a12 * a33);
+        M->ex.z = det * (a12 * a23 - a13 * a22);
+        M->ey.x = M->ex.y;
+        M->ey.y = det * (a11 * a33 - a13 * a13);
+        M->ey.z = det * (a13 * a12 - a11 * a23);
+        M->ez.x = M->ex.z;
+        M->ez.y = M->ey.z;
+        M->ez.z = det * (a11 * a22 - a12 * a12);
+    }
     Vec2 Solve22(Vec2 b) const {
         f32 a11 = ex.x, a12 = ey.x, a21 = ex.y, a22 = ey.y;
         f32 det = a11 * a22 - a12 * a21;
@@ -159,6 +189,13 @@ struct Mat33 {                                                          // b2mat
         return x;
     }
 };
+static inline Vec3 Mul(const Mat33& A, Vec3 v) {                        // b2math.d:679-682
+    return Vec3((v.x * A.ex.x + v.y * A.ey.x) + v.z * A.ez.x, (v.x * A.ex.y + v.y * A.ey.y) + v.z * A.ez.y,
+                (v.x * A.ex.z + v.y * A.ey.z) + v.z * A.ez.z);
+}
+static inline Vec2 Mul22(const Mat33& A, Vec2 v) {                      // b2math.d:685-688
+    return Vec2(A.ex.x * v.x + A.ey.x * v.y, A.ex.y * v.x + A.ey.y * v.y);
+}
 
 static inline void SinCos(f32 angle, f32* s, f32* c) {
     if (g_trig_mode == 0) {
@@ -1702,7 +1739,7 @@ struct Velocity { Vec2 v; f32 w = 0; };
 struct TimeStep { f32 dt = 0, inv_dt = 0, dtRatio = 0; int velocityIterations = 0, positionIterations = 0; bool warmStarting = false; };
 struct SolverData { TimeStep step; Position* positions = nullptr; Velocity* velocities = nullptr; };
 
-enum { kRevoluteJoint = 0, kDistanceJoint = 1 };
+enum { kRevoluteJoint = 0, kDistanceJoint = 1, kRopeJoint = 2, kWeldJoint = 3 };
 
 struct Joint {                                                          // joints/b2joint.d, b2revolutejoint.d, b2distancejoint.d
     int type = kRevoluteJoint;
@@ -1728,18 +1765,293 @@ struct Joint {                                                          // joint
     Mat33 massM;
     f32 motorMass = 0;
     int limitState = kInactiveLimit;
-    // distance (the impulse is impulse.x)
+    // distance and rope (the impulse is impulse.x; the rope's maximum length is `length`,
+    // its state limitState); weld (referenceAngle, frequency, damping, gamma, bias; its
+    // mass matrix is massM)
     f32 length = 0, frequencyHz = 0, dampingRatio = 0, gamma = 0, bias = 0, distMass = 0;
+    f32 curLength = 0;
     Vec2 u;
 
     void InitVelocityConstraints(const SolverData& data) {
-        if (type == kDistanceJoint) DistanceInit(data); else RevoluteInit(data);
+        switch (type) {
+        case kDistanceJoint: DistanceInit(data); break;
+        case kRopeJoint: RopeInit(data); break;
+        case kWeldJoint: WeldInit(data); break;
+        default: RevoluteInit(data);
+        }
     }
     void SolveVelocityConstraints(const SolverData& data) {
-        if (type == kDistanceJoint) DistanceSolveVelocity(data); else RevoluteSolveVelocity(data);
+        switch (type) {
+        case kDistanceJoint: DistanceSolveVelocity(data); break;
+        case kRopeJoint: RopeSolveVelocity(data); break;
+        case kWeldJoint: WeldSolveVelocity(data); break;
+        default: RevoluteSolveVelocity(data);
+        }
     }
     bool SolvePositionConstraints(const SolverData& data) {
-        return type == kDistanceJoint ? DistanceSolvePosition(data) : RevoluteSolvePosition(data);
+        switch (type) {
+        case kDistanceJoint: return DistanceSolvePosition(data);
+        case kRopeJoint: return RopeSolvePosition(data);
+        case kWeldJoint: return WeldSolvePosition(data);
+        default: return RevoluteSolvePosition(data);
+        }
+    }
+
+    void LoadBodies() {
+        indexA = bodyA->islandIndex;
+        indexB = bodyB->islandIndex;
+        localCenterA = bodyA->sweep.localCenter;
+        localCenterB = bodyB->sweep.localCenter;
+        invMassA = bodyA->invMass;
+        invMassB = bodyB->invMass;
+        invIA = bodyA->invI;
+        invIB = bodyB->invI;
+    }
+
+    void RopeInit(const SolverData& data) {                             // b2ropejoint.d:165-245
+        LoadBodies();
+        Vec2 cA = data.positions[indexA].c;
+        f32 aA = data.positions[indexA].a;
+        Vec2 vA = data.velocities[indexA].v;
+        f32 wA = data.velocities[indexA].w;
+        Vec2 cB = data.positions[indexB].c;
+        f32 aB = data.positions[indexB].a;
+        Vec2 vB = data.velocities[indexB].v;
+        f32 wB = data.velocities[indexB].w;
+        Rot qA(aA), qB(aB);
+        rA = Mul(qA, localAnchorA - localCenterA);
+        rB = Mul(qB, localAnchorB - localCenterB);
+        u = ((cB + rB) - cA) - rA;
+        curLength = u.Length();
+        f32 C = curLength - length;
+        limitState = C > 0.0f ? kAtUpperLimit : kInactiveLimit;
+        if (curLength > kLinearSlop) {
+            u *= 1.0f / curLength;
+        } else {
+            u.SetZero();
+            distMass = 0.0f;
+            impulse.x = 0.0f;
+            return;
+        }
+        f32 crA = Cross(rA, u);
+        f32 crB = Cross(rB, u);
+        f32 invMass = ((invMassA + (invIA * crA) * crA) + invMassB) + (invIB * crB) * crB;
+        distMass = invMass != 0.0f ? 1.0f / invMass : 0.0f;
+        if (data.step.warmStarting) {
+            impulse.x *= data.step.dtRatio;
+            Vec2 P = impulse.x * u;
+            vA -= invMassA * P;
+            wA -= invIA * Cross(rA, P);
+            vB += invMassB * P;
+            wB += invIB * Cross(rB, P);
+        } else {
+            impulse.x = 0.0f;
+        }
+        data.velocities[indexA].v = vA;
+        data.velocities[indexA].w = wA;
+        data.velocities[indexB].v = vB;
+        data.velocities[indexB].w = wB;
+    }
+
+    void RopeSolveVelocity(const SolverData& data) {                    // b2ropejoint.d:247-281
+        Vec2 vA = data.velocities[indexA].v;
+        f32 wA = data.velocities[indexA].w;
+        Vec2 vB = data.velocities[indexB].v;
+        f32 wB = data.velocities[indexB].w;
+        Vec2 vpA = vA + Cross(wA, rA);
+        Vec2 vpB = vB + Cross(wB, rB);
+        f32 C = curLength - length;
+        f32 Cdot = Dot(u, vpB - vpA);
+        if (C < 0.0f) Cdot += data.step.inv_dt * C;                      // predictive constraint
+        f32 imp = -distMass * Cdot;
+        f32 oldImpulse = impulse.x;
+        impulse.x = Min(0.0f, impulse.x + imp);
+        imp = impulse.x - oldImpulse;
+        Vec2 P = imp * u;
+        vA -= invMassA * P;
+        wA -= invIA * Cross(rA, P);
+        vB += invMassB * P;
+        wB += invIB * Cross(rB, P);
+        data.velocities[indexA].v = vA;
+        data.velocities[indexA].w = wA;
+        data.velocities[indexB].v = vB;
+        data.velocities[indexB].w = wB;
+    }
+
+    bool RopeSolvePosition(const SolverData& data) {                    // b2ropejoint.d:283-317
+        Vec2 cA = data.positions[indexA].c;
+        f32 aA = data.positions[indexA].a;
+        Vec2 cB = data.positions[indexB].c;
+        f32 aB = data.positions[indexB].a;
+        Rot qA(aA), qB(aB);
+        Vec2 rA_ = Mul(qA, localAnchorA - localCenterA);
+        Vec2 rB_ = Mul(qB, localAnchorB - localCenterB);
+        Vec2 d = ((cB + rB_) - cA) - rA_;
+        f32 len = d.Normalize();
+        f32 C = Clamp(len - length, 0.0f, kMaxLinearCorrection);
+        f32 imp = -distMass * C;
+        Vec2 P = imp * d;
+        cA -= invMassA * P;
+        aA -= invIA * Cross(rA_, P);
+        cB += invMassB * P;
+        aB += invIB * Cross(rB_, P);
+        data.positions[indexA].c = cA;
+        data.positions[indexA].a = aA;
+        data.positions[indexB].c = cB;
+        data.positions[indexB].a = aB;
+        return len - length < kLinearSlop;
+    }
+
+    // the weld joint's K (b2weldjoint.d:229-238 and 387-396)
+    static Mat33 WeldK(f32 mA, f32 mB, f32 iA, f32 iB, Vec2 ra, Vec2 rb) {
+        Mat33 K;
+        K.ex.x = ((mA + mB) + (ra.y * ra.y) * iA) + (rb.y * rb.y) * iB;
+        K.ey.x = ((-ra.y) * ra.x) * iA - (rb.y * rb.x) * iB;
+        K.ez.x = (-ra.y) * iA - rb.y * iB;
+        K.ex.y = K.ey.x;
+        K.ey.y = ((mA + mB) + (ra.x * ra.x) * iA) + (rb.x * rb.x) * iB;
+        K.ez.y = ra.x * iA + rb.x * iB;
+        K.ex.z = K.ez.x;
+        K.ey.z = K.ez.y;
+        K.ez.z = iA + iB;
+        return K;
+    }
+
+    void WeldInit(const SolverData& data) {                             // b2weldjoint.d:196-306
+        LoadBodies();
+        f32 aA = data.positions[indexA].a;
+        Vec2 vA = data.velocities[indexA].v;
+        f32 wA = data.velocities[indexA].w;
+        f32 aB = data.positions[indexB].a;
+        Vec2 vB = data.velocities[indexB].v;
+        f32 wB = data.velocities[indexB].w;
+        Rot qA(aA), qB(aB);
+        rA = Mul(qA, localAnchorA - localCenterA);
+        rB = Mul(qB, localAnchorB - localCenterB);
+        f32 mA = invMassA, mB = invMassB, iA = invIA, iB = invIB;
+        Mat33 K = WeldK(mA, mB, iA, iB, rA, rB);
+        if (frequencyHz > 0.0f) {
+            K.GetInverse22(&massM);
+            f32 invM = iA + iB;
+            f32 m = invM > 0.0f ? 1.0f / invM : 0.0f;
+            f32 C = (aB - aA) - referenceAngle;
+            f32 omega = (2.0f * kPi) * frequencyHz;
+            f32 d = ((2.0f * m) * dampingRatio) * omega;
+            f32 k = (m * omega) * omega;
+            f32 h = data.step.dt;
+            gamma = h * (d + h * k);
+            gamma = gamma != 0.0f ? 1.0f / gamma : 0.0f;
+            bias = ((C * h) * k) * gamma;
+            invM += gamma;
+            massM.ez.z = invM != 0.0f ? 1.0f / invM : 0.0f;
+        } else if (K.ez.z == 0.0f) {
+            K.GetInverse22(&massM);
+            gamma = 0.0f;
+            bias = 0.0f;
+        } else {
+            K.GetSymInverse33(&massM);
+            gamma = 0.0f;
+            bias = 0.0f;
+        }
+        if (data.step.warmStarting) {
+            impulse *= data.step.dtRatio;
+            Vec2 P(impulse.x, impulse.y);
+            vA -= mA * P;
+            wA -= iA * (Cross(rA, P) + impulse.z);
+            vB += mB * P;
+            wB += iB * (Cross(rB, P) + impulse.z);
+        } else {
+            impulse.SetZero();
+        }
+        data.velocities[indexA].v = vA;
+        data.velocities[indexA].w = wA;
+        data.velocities[indexB].v = vB;
+        data.velocities[indexB].w = wB;
+    }
+
+    void WeldSolveVelocity(const SolverData& data) {                    // b2weldjoint.d:308-364
+        Vec2 vA = data.velocities[indexA].v;
+        f32 wA = data.velocities[indexA].w;
+        Vec2 vB = data.velocities[indexB].v;
+        f32 wB = data.velocities[indexB].w;
+        f32 mA = invMassA, mB = invMassB, iA = invIA, iB = invIB;
+        if (frequencyHz > 0.0f) {
+            f32 Cdot2 = wB - wA;
+            f32 impulse2 = -massM.ez.z * ((Cdot2 + bias) + gamma * impulse.z);
+            impulse.z += impulse2;
+            wA -= iA * impulse2;
+            wB += iB * impulse2;
+            Vec2 Cdot1 = ((vB + Cross(wB, rB)) - vA) - Cross(wA, rA);
+            Vec2 impulse1 = -Mul22(massM, Cdot1);
+            impulse.x += impulse1.x;
+            impulse.y += impulse1.y;
+            Vec2 P = impulse1;
+            vA -= mA * P;
+            wA -= iA * Cross(rA, P);
+            vB += mB * P;
+            wB += iB * Cross(rB, P);
+        } else {
+            Vec2 Cdot1 = ((vB + Cross(wB, rB)) - vA) - Cross(wA, rA);
+            f32 Cdot2 = wB - wA;
+            Vec3 Cdot(Cdot1.x, Cdot1.y, Cdot2);
+            Vec3 imp = -Mul(massM, Cdot);
+            impulse += imp;
+            Vec2 P(imp.x, imp.y);
+            vA -= mA * P;
+            wA -= iA * (Cross(rA, P) + imp.z);
+            vB += mB * P;
+            wB += iB * (Cross(rB, P) + imp.z);
+        }
+        data.velocities[indexA].v = vA;
+        data.velocities[indexA].w = wA;
+        data.velocities[indexB].v = vB;
+        data.velocities[indexB].w = wB;
+    }
+
+    bool WeldSolvePosition(const SolverData& data) {                    // b2weldjoint.d:366-444
+        Vec2 cA = data.positions[indexA].c;
+        f32 aA = data.positions[indexA].a;
+        Vec2 cB = data.positions[indexB].c;
+        f32 aB = data.positions[indexB].a;
+        Rot qA(aA), qB(aB);
+        f32 mA = invMassA, mB = invMassB, iA = invIA, iB = invIB;
+        Vec2 rA_ = Mul(qA, localAnchorA - localCenterA);
+        Vec2 rB_ = Mul(qB, localAnchorB - localCenterB);
+        f32 positionError = 0.0f, angularError = 0.0f;
+        Mat33 K = WeldK(mA, mB, iA, iB, rA_, rB_);
+        if (frequencyHz > 0.0f) {
+            Vec2 C1 = ((cB + rB_) - cA) - rA_;
+            positionError = C1.Length();
+            angularError = 0.0f;
+            Vec2 P = -K.Solve22(C1);
+            cA -= mA * P;
+            aA -= iA * Cross(rA_, P);
+            cB += mB * P;
+            aB += iB * Cross(rB_, P);
+        } else {
+            Vec2 C1 = ((cB + rB_) - cA) - rA_;
+            f32 C2 = (aB - aA) - referenceAngle;
+            positionError = C1.Length();
+            angularError = Abs(C2);
+            Vec3 C(C1.x, C1.y, C2);
+            Vec3 imp;
+            if (K.ez.z > 0.0f) {
+                imp = -K.Solve33(C);
+            } else {
+                Vec2 imp2 = -K.Solve22(C1);
+                imp = Vec3(imp2.x, imp2.y, 0.0f);
+            }
+            Vec2 P(imp.x, imp.y);
+            cA -= mA * P;
+            aA -= iA * (Cross(rA_, P) + imp.z);
+            cB += mB * P;
+            aB += iB * (Cross(rB_, P) + imp.z);
+        }
+        data.positions[indexA].c = cA;
+        data.positions[indexA].a = aA;
+        data.positions[indexB].c = cB;
+        data.positions[indexB].a = aB;
+        return positionError <= kLinearSlop && angularError <= kAngularSlop;
     }
 
     void DistanceInit(const SolverData& data) {                         // b2distancejoint.d:211-306
@@ -3006,6 +3318,37 @@ struct World {                                                          // dynam
         return LinkJoint(j);
     }
 
+    Joint* CreateRope(const dbox_rope_def* def) {                       // b2ropejoint.d:140-153
+        Joint* j = new Joint();
+        j->type = kRopeJoint;
+        j->bodyA = bodiesByIndex[def->body_a];
+        j->bodyB = bodiesByIndex[def->body_b];
+        j->collideConnected = def->collide_connected != 0;
+        j->localAnchorA = Vec2(def->local_anchor_a.x, def->local_anchor_a.y);
+        j->localAnchorB = Vec2(def->local_anchor_b.x, def->local_anchor_b.y);
+        j->length = def->max_length;
+        j->distMass = 0.0f;
+        j->impulse.SetZero();
+        j->limitState = kInactiveLimit;
+        j->curLength = 0.0f;
+        return LinkJoint(j);
+    }
+
+    Joint* CreateWeld(const dbox_weld_def* def) {                       // b2weldjoint.d:107-119
+        Joint* j = new Joint();
+        j->type = kWeldJoint;
+        j->bodyA = bodiesByIndex[def->body_a];
+        j->bodyB = bodiesByIndex[def->body_b];
+        j->collideConnected = def->collide_connected != 0;
+        j->localAnchorA = Vec2(def->local_anchor_a.x, def->local_anchor_a.y);
+        j->localAnchorB = Vec2(def->local_anchor_b.x, def->local_anchor_b.y);
+        j->referenceAngle = def->reference_angle;
+        j->frequencyHz = def->frequency_hz;
+        j->dampingRatio = def->damping_ratio;
+        j->impulse.SetZero();
+        return LinkJoint(j);
+    }
+
     Joint* CreateRevolute(const dbox_revolute_def* def) {               // b2world.d:196-261
         Joint* j = new Joint();
         j->bodyA = bodiesByIndex[def->body_a];
@@ -3427,6 +3770,18 @@ int orc_joint_create_distance(orc_world* w, const dbox_distance_def* def) {
     int n = (int)w->w.bodiesByIndex.size();
     if (def->body_a < 0 || def->body_a >= n || def->body_b < 0 || def->body_b >= n || def->body_a == def->body_b) return -1;
     return w->w.CreateDistance(def)->index;
+}
+
+int orc_joint_create_rope(orc_world* w, const dbox_rope_def* def) {
+    int n = (int)w->w.bodiesByIndex.size();
+    if (def->body_a < 0 || def->body_a >= n || def->body_b < 0 || def->body_b >= n || def->body_a == def->body_b) return -1;
+    return w->w.CreateRope(def)->index;
+}
+
+int orc_joint_create_weld(orc_world* w, const dbox_weld_def* def) {
+    int n = (int)w->w.bodiesByIndex.size();
+    if (def->body_a < 0 || def->body_a >= n || def->body_b < 0 || def->body_b >= n || def->body_a == def->body_b) return -1;
+    return w->w.CreateWeld(def)->index;
 }
 
 int orc_scene_create(orc_world* w, int n_bodies, const dbox_body_def* bodies, int n_fixtures,

@@ -197,3 +197,21 @@ def test_distance_joint_ropes_exact(oracle_lib, gpu_lib):
             for i, ow in enumerate(ows):
                 d = exact_diff(ow.export_state(), gw.export_state(i))
                 assert not d, "world %d step %d: %s" % (i, t + 1, d[:6])
+
+
+def test_weld_and_rope_joints_exact(oracle_lib, gpu_lib):
+    # rigid and soft weld beams, ropes at and below their maximum length, beside stacks and
+    # the other joint kinds: bit-exact against the oracle
+    from dbox_gb300 import scenes
+    oracle_lib.set_trig_mode(1)
+    worlds = [scenes.welded(), scenes.welded(n_beams=2, links=5, pile=False), scenes.ropes(n_ropes=2, links=6)]
+    gw = gpu_lib.World(worlds)
+    ows = [oracle_lib.OracleWorld(s) for s in worlds]
+    for t in range(150):
+        gw.step()
+        for ow in ows:
+            ow.step()
+        if t % 30 == 29:
+            for i, ow in enumerate(ows):
+                d = exact_diff(ow.export_state(), gw.export_state(i))
+                assert not d, "world %d step %d: %s" % (i, t + 1, d[:6])

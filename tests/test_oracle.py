@@ -196,3 +196,35 @@ def test_distance_joint_ropes_hold_their_length(oracle_lib):
         else:
             assert d.max() < 4.0 * gap and d.min() > 0.5 * gap, d
     assert (st["joints"]["impulse"][:, 0] != 0).all()
+
+
+def test_weld_beams_and_ropes(oracle_lib):
+    # b2WeldJoint keeps rigid beams straight and near their welds' reference angle; b2RopeJoint
+    # never lets its anchors get further apart than the maximum length (plus the solver slop)
+    from dbox_gb300 import scenes
+    oracle_lib.set_trig_mode(1)
+    s = scenes.welded(n_beams=2, links=6, pile=False)
+    ow = oracle_lib.OracleWorld(s)
+    ow.step(steps=240)
+    st = ow.export_state()
+    b = st["bodies"]
+    ang = b["sweep"][:, 7]
+    # beam 0 (rigid welds): bodies 2..7 (ground 0, post 1); the welds hold each link close to
+    # its neighbour's angle (a long weld chain sags a little under 8/3 iterations) and the
+    # beam stays up
+    assert np.abs(np.diff(ang[1:8])).max() < 0.2, ang[1:8]
+    assert b["xf"][7, 1] > b["xf"][2, 1] - 2.0
+    # rope constraints: distance between anchors within max length + 2 linear slops
+    xy = b["xf"][:, :2].astype(np.float64)
+    c, sn = b["xf"][:, 3].astype(np.float64), b["xf"][:, 2].astype(np.float64)
+
+    def world_point(i, p):
+        return xy[i] + np.array([c[i] * p[0] - sn[i] * p[1], sn[i] * p[0] + c[i] * p[1]])
+
+    for r in s["rope_joints"]:
+        d = np.linalg.norm(world_point(r["body_b"], r["local_anchor_b"]) - world_point(r["body_a"], r["local_anchor_a"]))
+        assert d <= r["max_length"] + 0.02, (d, r["max_length"])
+    n_rev, n_dist, n_rope = len(s["joints"]), len(s["distance_joints"]), len(s["rope_joints"])
+    imp = st["joints"]["impulse"]
+    assert (imp[n_rev + n_dist:n_rev + n_dist + n_rope, 0] <= 0).all()          # ropes only pull
+    assert (st["joints"]["limit_state"][n_rev + n_dist:n_rev + n_dist + n_rope] == 2).any()
