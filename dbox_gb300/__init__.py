@@ -49,6 +49,9 @@ def lib():
     L.dbox_joint_create_distance.argtypes = [vp, i32, vp, ctypes.POINTER(i32)]
     L.dbox_joint_create_rope.argtypes = [vp, i32, vp, ctypes.POINTER(i32)]
     L.dbox_joint_create_weld.argtypes = [vp, i32, vp, ctypes.POINTER(i32)]
+    L.dbox_joint_create_friction.argtypes = [vp, i32, vp, ctypes.POINTER(i32)]
+    L.dbox_joint_create_motor.argtypes = [vp, i32, vp, ctypes.POINTER(i32)]
+    L.dbox_joint_create_wheel.argtypes = [vp, i32, vp, ctypes.POINTER(i32)]
     L.dbox_world_set_flags.argtypes = [vp, i32, i32, i32, i32, i32]
     L.dbox_world_set_gravity.argtypes = [vp, abi.Vec2]
     L.dbox_world_step.argtypes = [vp, f32, i32, i32]
@@ -212,10 +215,16 @@ class World:
     becomes an independent world of the batch.
     """
 
-    def __init__(self, scenes, gravity=(0.0, -10.0), flags=None, contacts_per_body=0):
+    def __init__(self, scenes, gravity=None, flags=None, contacts_per_body=0):
         L = lib()
         if isinstance(scenes, dict):
             scenes = [scenes]
+        if gravity is None:
+            # one gravity per handle (b2World's): the scenes' own, which must agree
+            gs = {tuple(float(v) for v in sc.get("gravity", (0.0, -10.0))) for sc in scenes} or {(0.0, -10.0)}
+            if len(gs) != 1:
+                raise ValueError("scenes with different gravity need separate World handles")
+            gravity = gs.pop()
         self.n_worlds = len(scenes)
         caps = np.zeros(2, np.int32)
         caps[0] = contacts_per_body
@@ -235,20 +244,25 @@ class World:
                 self.create_joint(i, "distance", d)
             for d in s.get("rope_joints", ()):
                 self.create_joint(i, "rope", d)
-            for d in s.get("weld_joints", ()):
-                self.create_joint(i, "weld", d)
+            for kind in ("weld", "friction", "motor", "wheel"):
+                for d in s.get(kind + "_joints", ()):
+                    self.create_joint(i, kind, d)
         self.body_counts = [len(s["bodies"]) for s in scenes]
         if flags is not None:
             self.set_flags(**flags)
 
     _JOINT_KINDS = {"distance": ("DISTANCE_DEF", "dbox_joint_create_distance"),
                     "rope": ("ROPE_DEF", "dbox_joint_create_rope"),
-                    "weld": ("WELD_DEF", "dbox_joint_create_weld")}
+                    "weld": ("WELD_DEF", "dbox_joint_create_weld"),
+                    "friction": ("FRICTION_DEF", "dbox_joint_create_friction"),
+                    "motor": ("MOTOR_DEF", "dbox_joint_create_motor"),
+                    "wheel": ("WHEEL_DEF", "dbox_joint_create_wheel")}
 
     def create_joint(self, world, kind, d):
-        """b2World.CreateJoint with a b2DistanceJointDef / b2RopeJointDef / b2WeldJointDef
-        (kind "distance", "rope" or "weld"; d a DISTANCE_DEF / ROPE_DEF / WELD_DEF record);
-        returns the joint index."""
+        """b2World.CreateJoint with a b2DistanceJointDef / b2RopeJointDef / b2WeldJointDef /
+        b2FrictionJointDef / b2MotorJointDef / b2WheelJointDef (kind "distance", "rope",
+        "weld", "friction", "motor" or "wheel"; d the matching *_DEF record); returns the
+        joint index."""
         dtype, fn = World._JOINT_KINDS[kind]
         dd = np.ascontiguousarray(np.array([d], getattr(abi, dtype)))
         out = ctypes.c_int32()

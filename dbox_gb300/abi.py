@@ -52,6 +52,24 @@ WELD_DEF = np.dtype([
     ("reference_angle", "<f4"), ("frequency_hz", "<f4"), ("damping_ratio", "<f4"),
 ])
 assert WELD_DEF.itemsize == 40
+FRICTION_DEF = np.dtype([
+    ("body_a", "<i4"), ("body_b", "<i4"), ("collide_connected", "<i4"),
+    ("local_anchor_a", "<f4", 2), ("local_anchor_b", "<f4", 2), ("max_force", "<f4"), ("max_torque", "<f4"),
+])
+assert FRICTION_DEF.itemsize == 36
+MOTOR_DEF = np.dtype([
+    ("body_a", "<i4"), ("body_b", "<i4"), ("collide_connected", "<i4"),
+    ("linear_offset", "<f4", 2), ("angular_offset", "<f4"), ("max_force", "<f4"), ("max_torque", "<f4"),
+    ("correction_factor", "<f4"),
+])
+assert MOTOR_DEF.itemsize == 36
+WHEEL_DEF = np.dtype([
+    ("body_a", "<i4"), ("body_b", "<i4"), ("collide_connected", "<i4"),
+    ("local_anchor_a", "<f4", 2), ("local_anchor_b", "<f4", 2), ("local_axis_a", "<f4", 2),
+    ("enable_motor", "<i4"), ("max_motor_torque", "<f4"), ("motor_speed", "<f4"),
+    ("frequency_hz", "<f4"), ("damping_ratio", "<f4"),
+])
+assert WHEEL_DEF.itemsize == 56
 
 WORLD_HEADER = np.dtype([
     ("body_count", "<i4"), ("fixture_count", "<i4"), ("contact_count", "<i4"), ("joint_count", "<i4"),

@@ -1020,6 +1020,92 @@ int create_weld_joint(HostWorld& hw, const dbox_weld_def* d) {
     return link_joint(hw, j);
 }
 
+// b2World.CreateJoint with a b2FrictionJointDef / b2MotorJointDef (b2frictionjoint.d:85-96, b2motorjoint.d:92-106)
+int create_friction_joint(HostWorld& hw, const dbox_friction_def* d) {
+    int nb = (int)hw.bs.size();
+    if (d->body_a < 0 || d->body_a >= nb || d->body_b < 0 || d->body_b >= nb || d->body_a == d->body_b) return -1;
+    dg::DJoint j;
+    memset(&j, 0, sizeof(j));
+    j.type = dg::kFrictionJoint;
+    j.body_a = d->body_a;
+    j.body_b = d->body_b;
+    j.collide_connected = d->collide_connected ? 1 : 0;
+    j.local_anchor_a = make_float2(d->local_anchor_a.x, d->local_anchor_a.y);
+    j.local_anchor_b = make_float2(d->local_anchor_b.x, d->local_anchor_b.y);
+    j.max_force = d->max_force;
+    j.max_torque = d->max_torque;
+    return link_joint(hw, j);
+}
+
+int create_motor_joint(HostWorld& hw, const dbox_motor_def* d) {
+    int nb = (int)hw.bs.size();
+    if (d->body_a < 0 || d->body_a >= nb || d->body_b < 0 || d->body_b >= nb || d->body_a == d->body_b) return -1;
+    dg::DJoint j;
+    memset(&j, 0, sizeof(j));
+    j.type = dg::kMotorJoint;
+    j.body_a = d->body_a;
+    j.body_b = d->body_b;
+    j.collide_connected = d->collide_connected ? 1 : 0;
+    j.linear_offset = make_float2(d->linear_offset.x, d->linear_offset.y);
+    j.angular_offset = d->angular_offset;
+    j.max_force = d->max_force;
+    j.max_torque = d->max_torque;
+    j.correction_factor = d->correction_factor;
+    return link_joint(hw, j);
+}
+
+// b2World.CreateJoint with a b2WheelJointDef (b2wheeljoint.d:110-139)
+int create_wheel_joint(HostWorld& hw, const dbox_wheel_def* d) {
+    int nb = (int)hw.bs.size();
+    if (d->body_a < 0 || d->body_a >= nb || d->body_b < 0 || d->body_b >= nb || d->body_a == d->body_b) return -1;
+    dg::DJoint j;
+    memset(&j, 0, sizeof(j));
+    j.type = dg::kWheelJoint;
+    j.body_a = d->body_a;
+    j.body_b = d->body_b;
+    j.collide_connected = d->collide_connected ? 1 : 0;
+    j.local_anchor_a = make_float2(d->local_anchor_a.x, d->local_anchor_a.y);
+    j.local_anchor_b = make_float2(d->local_anchor_b.x, d->local_anchor_b.y);
+    j.local_axis_x = make_float2(d->local_axis_a.x, d->local_axis_a.y);
+    j.local_axis_y = make_float2(-1.0f * d->local_axis_a.y, 1.0f * d->local_axis_a.x);   // b2Cross(1, x)
+    j.enable_motor = d->enable_motor ? 1 : 0;
+    j.max_motor_torque = d->max_motor_torque;
+    j.motor_speed = d->motor_speed;
+    j.frequency_hz = d->frequency_hz;
+    j.damping_ratio = d->damping_ratio;
+    return link_joint(hw, j);
+}
+
+int32_t dbox_joint_create_wheel(dbox_world* w, int32_t world, const dbox_wheel_def* def, int32_t* out_joint) {
+    if (!w || !def || world < 0 || world >= (int)w->worlds.size()) return fail(DBOX_ERR_INVALID, "dbox_joint_create_wheel: bad arguments");
+    int rc = prepare_edit(w);
+    if (rc) return rc;
+    int idx = create_wheel_joint(w->worlds[world], def);
+    if (idx < 0) return fail(DBOX_ERR_INVALID, "dbox_joint_create_wheel: bad bodies");
+    if (out_joint) *out_joint = idx;
+    return DBOX_OK;
+}
+
+int32_t dbox_joint_create_friction(dbox_world* w, int32_t world, const dbox_friction_def* def, int32_t* out_joint) {
+    if (!w || !def || world < 0 || world >= (int)w->worlds.size()) return fail(DBOX_ERR_INVALID, "dbox_joint_create_friction: bad arguments");
+    int rc = prepare_edit(w);
+    if (rc) return rc;
+    int idx = create_friction_joint(w->worlds[world], def);
+    if (idx < 0) return fail(DBOX_ERR_INVALID, "dbox_joint_create_friction: bad bodies");
+    if (out_joint) *out_joint = idx;
+    return DBOX_OK;
+}
+
+int32_t dbox_joint_create_motor(dbox_world* w, int32_t world, const dbox_motor_def* def, int32_t* out_joint) {
+    if (!w || !def || world < 0 || world >= (int)w->worlds.size()) return fail(DBOX_ERR_INVALID, "dbox_joint_create_motor: bad arguments");
+    int rc = prepare_edit(w);
+    if (rc) return rc;
+    int idx = create_motor_joint(w->worlds[world], def);
+    if (idx < 0) return fail(DBOX_ERR_INVALID, "dbox_joint_create_motor: bad bodies");
+    if (out_joint) *out_joint = idx;
+    return DBOX_OK;
+}
+
 int32_t dbox_joint_create_rope(dbox_world* w, int32_t world, const dbox_rope_def* def, int32_t* out_joint) {
     if (!w || !def || world < 0 || world >= (int)w->worlds.size()) return fail(DBOX_ERR_INVALID, "dbox_joint_create_rope: bad arguments");
     int rc = prepare_edit(w);

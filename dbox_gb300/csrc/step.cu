@@ -1681,12 +1681,261 @@ __device__ __noinline__ bool weld_solve_position(const DJoint& j, int la, int lb
     return positionError <= kLinearSlop && angularError <= kAngularSlop;
 }
 
+// ------------------------------------------------------------ friction and motor joints
+// b2FrictionJoint (joints/b2frictionjoint.d:178-315), b2MotorJoint (joints/b2motorjoint.d:223-366):
+// a 2x2 linear and a 1x1 angular block with force / torque caps; the motor's anchors are the
+// bodies' origins and it drives towards its offset with a correction factor
+__device__ __noinline__ void friction_motor_init(const Ctx& x, int ji, int b0, SB sb, bool warm, float dtRatio) {
+    DJoint& j = x.jt[ji];
+    const dbox_body_state& ba = x.bs[j.body_a];
+    const dbox_body_state& bb = x.bs[j.body_b];
+    int la = j.body_a - b0, lb = j.body_b - b0;
+    j.lcA = b_lc(ba);
+    j.lcB = b_lc(bb);
+    j.invMassA = ba.mass[1];
+    j.invMassB = bb.mass[1];
+    j.invIA = ba.mass[3];
+    j.invIB = bb.mass[3];
+    float2 cA = sb.c(la), cB = sb.c(lb);
+    float aA = sb.a(la), aB = sb.a(lb);
+    float2 vA = sb.v(la), vB = sb.v(lb);
+    float wA = sb.w(la), wB = sb.w(lb);
+    Rot qA = rot(aA), qB = rot(aB);
+    const bool motor = j.type == kMotorJoint;
+    if (motor) {
+        j.rA = mul(qA, -j.lcA);
+        j.rB = mul(qB, -j.lcB);
+    } else {
+        j.rA = mul(qA, j.local_anchor_a - j.lcA);
+        j.rB = mul(qB, j.local_anchor_b - j.lcB);
+    }
+    const float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    const float2 rA = j.rA, rB = j.rB;
+    float k11 = ((mA + mB) + (iA * rA.y) * rA.y) + (iB * rB.y) * rB.y;
+    float k21 = ((-iA) * rA.x) * rA.y - (iB * rB.x) * rB.y;
+    float k22 = ((mA + mB) + (iA * rA.x) * rA.x) + (iB * rB.x) * rB.x;
+    float det = k11 * k22 - k21 * k21;                                  // b2Mat22.GetInverse (b2math.d:322-337)
+    if (det != 0.0f) det = fdiv(1.0f, det);
+    j.mass[0] = det * k22;
+    j.mass[3] = -det * k21;
+    j.mass[1] = -det * k21;
+    j.mass[4] = det * k11;
+    float am = iA + iB;
+    if (am > 0.0f) am = fdiv(1.0f, am);
+    j.angular_mass = am;
+    if (motor) {
+        j.linear_error = (((cB + rB) - cA) - rA) - mul(qA, j.linear_offset);
+        j.angular_error = (aB - aA) - j.angular_offset;
+    }
+    if (warm) {
+        j.impulse[0] *= dtRatio; j.impulse[1] *= dtRatio; j.impulse[2] *= dtRatio;
+        float2 P = v2(j.impulse[0], j.impulse[1]);
+        vA -= mA * P;
+        wA -= iA * (cross(rA, P) + j.impulse[2]);
+        vB += mB * P;
+        wB += iB * (cross(rB, P) + j.impulse[2]);
+    } else {
+        j.impulse[0] = 0.0f; j.impulse[1] = 0.0f; j.impulse[2] = 0.0f;
+    }
+    sb.set_v(la, vA, wA);
+    sb.set_v(lb, vB, wB);
+}
+
+__device__ __noinline__ void friction_motor_solve_velocity(const Ctx& x, DJoint& j, int la, int lb, SB sb) {
+    float2 vA = sb.v(la), vB = sb.v(lb);
+    float wA = sb.w(la), wB = sb.w(lb);
+    const float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    const float h = x.dt, inv_h = x.inv_dt;
+    const bool motor = j.type == kMotorJoint;
+    {
+        float Cdot = wB - wA;
+        if (motor) Cdot = Cdot + (inv_h * j.correction_factor) * j.angular_error;
+        float impulse = -j.angular_mass * Cdot;
+        float oldImpulse = j.impulse[2];
+        float maxImpulse = h * j.max_torque;
+        j.impulse[2] = bclamp(j.impulse[2] + impulse, -maxImpulse, maxImpulse);
+        impulse = j.impulse[2] - oldImpulse;
+        wA -= iA * impulse;
+        wB += iB * impulse;
+    }
+    {
+        float2 Cdot = ((vB + cross(wB, j.rB)) - vA) - cross(wA, j.rA);
+        if (motor) Cdot = Cdot + (inv_h * j.correction_factor) * j.linear_error;
+        float2 impulse = -v2(j.mass[0] * Cdot.x + j.mass[3] * Cdot.y, j.mass[1] * Cdot.x + j.mass[4] * Cdot.y);
+        float2 oldImpulse = v2(j.impulse[0], j.impulse[1]);
+        float2 li = v2(j.impulse[0] + impulse.x, j.impulse[1] + impulse.y);
+        float maxImpulse = h * j.max_force;
+        if (li.x * li.x + li.y * li.y > maxImpulse * maxImpulse) {
+            normalize(li);
+            li *= maxImpulse;
+        }
+        j.impulse[0] = li.x;
+        j.impulse[1] = li.y;
+        impulse = li - oldImpulse;
+        vA -= mA * impulse;
+        wA -= iA * cross(j.rA, impulse);
+        vB += mB * impulse;
+        wB += iB * cross(j.rB, impulse);
+    }
+    sb.set_v(la, vA, wA);
+    sb.set_v(lb, vB, wB);
+}
+
+// ------------------------------------------------------------ wheel joint (joints/b2wheeljoint.d:302-553)
+__device__ __noinline__ void wheel_init(const Ctx& x, int ji, int b0, SB sb, bool warm, float dtRatio) {
+    DJoint& j = x.jt[ji];
+    const dbox_body_state& ba = x.bs[j.body_a];
+    const dbox_body_state& bb = x.bs[j.body_b];
+    int la = j.body_a - b0, lb = j.body_b - b0;
+    j.lcA = b_lc(ba);
+    j.lcB = b_lc(bb);
+    j.invMassA = ba.mass[1];
+    j.invMassB = bb.mass[1];
+    j.invIA = ba.mass[3];
+    j.invIB = bb.mass[3];
+    const float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    float2 cA = sb.c(la), cB = sb.c(lb);
+    float aA = sb.a(la), aB = sb.a(lb);
+    float2 vA = sb.v(la), vB = sb.v(lb);
+    float wA = sb.w(la), wB = sb.w(lb);
+    Rot qA = rot(aA), qB = rot(aB);
+    float2 rA = mul(qA, j.local_anchor_a - j.lcA);
+    float2 rB = mul(qB, j.local_anchor_b - j.lcB);
+    float2 d = ((cB + rB) - cA) - rA;
+    j.ay = mul(qA, j.local_axis_y);                                     // point to line
+    j.sAy = cross(d + rA, j.ay);
+    j.sBy = cross(rB, j.ay);
+    float m = ((mA + mB) + (iA * j.sAy) * j.sAy) + (iB * j.sBy) * j.sBy;
+    if (m > 0.0f) m = fdiv(1.0f, m);
+    j.mass[0] = m;
+    j.spring_mass = 0.0f;                                               // spring
+    j.bias = 0.0f;
+    j.gamma = 0.0f;
+    if (j.frequency_hz > 0.0f) {
+        j.ax = mul(qA, j.local_axis_x);
+        j.sAx = cross(d + rA, j.ax);
+        j.sBx = cross(rB, j.ax);
+        float invMass = ((mA + mB) + (iA * j.sAx) * j.sAx) + (iB * j.sBx) * j.sBx;
+        if (invMass > 0.0f) {
+            float sm = fdiv(1.0f, invMass);
+            float C = dot(d, j.ax);
+            float omega = (2.0f * kPi) * j.frequency_hz;
+            float d2 = ((2.0f * sm) * j.damping_ratio) * omega;
+            float k = (sm * omega) * omega;
+            float h = x.dt;
+            float gamma = h * (d2 + h * k);
+            if (gamma > 0.0f) gamma = fdiv(1.0f, gamma);
+            j.gamma = gamma;
+            j.bias = ((C * h) * k) * gamma;
+            sm = invMass + gamma;
+            if (sm > 0.0f) sm = fdiv(1.0f, sm);
+            j.spring_mass = sm;
+        }
+    } else {
+        j.impulse[1] = 0.0f;
+    }
+    if (j.enable_motor) {                                               // rotational motor
+        float mm = iA + iB;
+        if (mm > 0.0f) mm = fdiv(1.0f, mm);
+        j.motor_mass = mm;
+    } else {
+        j.motor_mass = 0.0f;
+        j.motor_impulse = 0.0f;
+    }
+    if (warm) {
+        j.impulse[0] *= dtRatio;
+        j.impulse[1] *= dtRatio;
+        j.motor_impulse *= dtRatio;
+        float2 P = j.impulse[0] * j.ay + j.impulse[1] * j.ax;
+        float LA = (j.impulse[0] * j.sAy + j.impulse[1] * j.sAx) + j.motor_impulse;
+        float LB = (j.impulse[0] * j.sBy + j.impulse[1] * j.sBx) + j.motor_impulse;
+        vA -= mA * P;
+        wA -= iA * LA;
+        vB += mB * P;
+        wB += iB * LB;
+    } else {
+        j.impulse[0] = 0.0f;
+        j.impulse[1] = 0.0f;
+        j.motor_impulse = 0.0f;
+    }
+    sb.set_v(la, vA, wA);
+    sb.set_v(lb, vB, wB);
+}
+
+__device__ __noinline__ void wheel_solve_velocity(const Ctx& x, DJoint& j, int la, int lb, SB sb) {
+    const float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    float2 vA = sb.v(la), vB = sb.v(lb);
+    float wA = sb.w(la), wB = sb.w(lb);
+    {                                                                   // spring
+        float Cdot = (dot(j.ax, vB - vA) + j.sBx * wB) - j.sAx * wA;
+        float impulse = -j.spring_mass * ((Cdot + j.bias) + j.gamma * j.impulse[1]);
+        j.impulse[1] += impulse;
+        float2 P = impulse * j.ax;
+        float LA = impulse * j.sAx, LB = impulse * j.sBx;
+        vA -= mA * P;
+        wA -= iA * LA;
+        vB += mB * P;
+        wB += iB * LB;
+    }
+    {                                                                   // rotational motor
+        float Cdot = (wB - wA) - j.motor_speed;
+        float impulse = -j.motor_mass * Cdot;
+        float oldImpulse = j.motor_impulse;
+        float maxImpulse = x.dt * j.max_motor_torque;
+        j.motor_impulse = bclamp(j.motor_impulse + impulse, -maxImpulse, maxImpulse);
+        impulse = j.motor_impulse - oldImpulse;
+        wA -= iA * impulse;
+        wB += iB * impulse;
+    }
+    {                                                                   // point to line
+        float Cdot = (dot(j.ay, vB - vA) + j.sBy * wB) - j.sAy * wA;
+        float impulse = -j.mass[0] * Cdot;
+        j.impulse[0] += impulse;
+        float2 P = impulse * j.ay;
+        float LA = impulse * j.sAy, LB = impulse * j.sBy;
+        vA -= mA * P;
+        wA -= iA * LA;
+        vB += mB * P;
+        wB += iB * LB;
+    }
+    sb.set_v(la, vA, wA);
+    sb.set_v(lb, vB, wB);
+}
+
+__device__ __noinline__ bool wheel_solve_position(const DJoint& j, int la, int lb, SB sb) {
+    float2 cA = sb.c(la), cB = sb.c(lb);
+    float aA = sb.a(la), aB = sb.a(lb);
+    Rot qA = rot(aA), qB = rot(aB);
+    float2 rA = mul(qA, j.local_anchor_a - j.lcA);
+    float2 rB = mul(qB, j.local_anchor_b - j.lcB);
+    float2 d = ((cB - cA) + rB) - rA;
+    float2 ay = mul(qA, j.local_axis_y);
+    float sAy = cross(d + rA, ay);
+    float sBy = cross(rB, ay);
+    float C = dot(d, ay);
+    // the effective mass uses the velocity pass's sAy / sBy, as the reference does
+    float k = ((j.invMassA + j.invMassB) + (j.invIA * j.sAy) * j.sAy) + (j.invIB * j.sBy) * j.sBy;
+    float impulse = k != 0.0f ? fdiv(-C, k) : 0.0f;
+    float2 P = impulse * ay;
+    float LA = impulse * sAy, LB = impulse * sBy;
+    cA -= j.invMassA * P;
+    aA -= j.invIA * LA;
+    cB += j.invMassB * P;
+    aB += j.invIB * LB;
+    sb.set_c(la, cA, aA);
+    sb.set_c(lb, cB, aB);
+    return babs(C) <= kLinearSlop;
+}
+
 // ------------------------------------------------------------ revolute joint (joints/b2revolutejoint.d:319-636)
 DG void joint_init(const Ctx& x, int ji, int b0, SB sb, bool warm, float dtRatio) {
     switch (x.jt[ji].type) {
     case kDistanceJoint: distance_init(x, ji, b0, sb, warm, dtRatio); return;
     case kRopeJoint: rope_init(x, ji, b0, sb, warm, dtRatio); return;
     case kWeldJoint: weld_init(x, ji, b0, sb, warm, dtRatio); return;
+    case kFrictionJoint:
+    case kMotorJoint: friction_motor_init(x, ji, b0, sb, warm, dtRatio); return;
+    case kWheelJoint: wheel_init(x, ji, b0, sb, warm, dtRatio); return;
     default: break;
     }
     DJoint& j = x.jt[ji];
@@ -1762,6 +2011,8 @@ DG void joint_solve_velocity(const Ctx& x, int ji, int b0, SB sb) {
     if (j.type == kDistanceJoint) { distance_solve_velocity(j, la, lb, sb); return; }
     if (j.type == kRopeJoint) { rope_solve_velocity(x, j, la, lb, sb); return; }
     if (j.type == kWeldJoint) { weld_solve_velocity(j, la, lb, sb); return; }
+    if (j.type == kFrictionJoint || j.type == kMotorJoint) { friction_motor_solve_velocity(x, j, la, lb, sb); return; }
+    if (j.type == kWheelJoint) { wheel_solve_velocity(x, j, la, lb, sb); return; }
     float2 vA = sb.v(la), vB = sb.v(lb);
     float wA = sb.w(la), wB = sb.w(lb);
     float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
@@ -1824,6 +2075,8 @@ DG bool joint_solve_position(const Ctx& x, int ji, int b0, SB sb) {
     if (j.type == kDistanceJoint) return distance_solve_position(j, la, lb, sb);
     if (j.type == kRopeJoint) return rope_solve_position(j, la, lb, sb);
     if (j.type == kWeldJoint) return weld_solve_position(j, la, lb, sb);
+    if (j.type == kFrictionJoint || j.type == kMotorJoint) return true;   // no position correction
+    if (j.type == kWheelJoint) return wheel_solve_position(j, la, lb, sb);
     float2 cA = sb.c(la), cB = sb.c(lb);
     float aA = sb.a(la), aB = sb.a(lb);
     float angularError = 0.0f, positionError = 0.0f;

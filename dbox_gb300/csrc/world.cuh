@@ -68,9 +68,11 @@ struct BodyStatic {
     int jadj_start, jadj_count;    // into Ctx.jadj_joint / jadj_other (descending joint index)
 };
 
-enum { kRevoluteJoint = 0, kDistanceJoint = 1, kRopeJoint = 2, kWeldJoint = 3 };
-// b2RevoluteJoint / b2DistanceJoint / b2RopeJoint / b2WeldJoint (joints/b2revolutejoint.d,
-// b2distancejoint.d, b2ropejoint.d, b2weldjoint.d)
+enum { kRevoluteJoint = 0, kDistanceJoint = 1, kRopeJoint = 2, kWeldJoint = 3, kFrictionJoint = 4, kMotorJoint = 5,
+       kWheelJoint = 6 };
+// b2RevoluteJoint / b2DistanceJoint / b2RopeJoint / b2WeldJoint / b2FrictionJoint / b2MotorJoint /
+// b2WheelJoint (joints/b2revolutejoint.d, b2distancejoint.d, b2ropejoint.d, b2weldjoint.d,
+// b2frictionjoint.d, b2motorjoint.d, b2wheeljoint.d)
 struct DJoint {
     int body_a, body_b;
     int collide_connected;
@@ -92,7 +94,14 @@ struct DJoint {
     float length, frequency_hz, damping_ratio, gamma, bias;   // distance (length), rope (maximum length), weld
     float2 u;                      // distance / rope: unit vector from anchor A to anchor B
     float cur_length;              // rope: anchor distance at InitVelocityConstraints
-    int pad2;
+    // friction / motor: linear impulse in impulse[0..1], angular in impulse[2]; the linear
+    // mass (a b2Mat22) in mass[0] ex.x, mass[1] ex.y, mass[3] ey.x, mass[4] ey.y
+    float max_force, max_torque, correction_factor, angular_offset, angular_error, angular_mass;
+    float2 linear_offset, linear_error;
+    // wheel: point-to-line impulse impulse[0] and mass mass[0], spring impulse impulse[1]
+    float2 local_axis_x, local_axis_y, ax, ay;
+    float sAx, sBx, sAy, sBy, spring_mass;
+    int pad3;
 };
 
 // b2ContactVelocityConstraint (contacts/b2contactsolver.d:43-58) with body indices in place of island indices.

@@ -36,6 +36,8 @@ def _empty():
         "shapes": np.zeros(0, abi.SHAPE_DEF), "fixtures": abi.fixture_defs(0),
         "joints": np.zeros(0, abi.REVOLUTE_DEF), "distance_joints": np.zeros(0, abi.DISTANCE_DEF),
         "rope_joints": np.zeros(0, abi.ROPE_DEF), "weld_joints": np.zeros(0, abi.WELD_DEF),
+        "friction_joints": np.zeros(0, abi.FRICTION_DEF), "motor_joints": np.zeros(0, abi.MOTOR_DEF),
+        "wheel_joints": np.zeros(0, abi.WHEEL_DEF),
         "gravity": (0.0, -10.0), "name": "",
     }
 
@@ -54,7 +56,8 @@ def _concat(parts):
         j["body_b"] += nb
         out["joints"] = np.concatenate([out["joints"], j])
         for key, dtype in (("distance_joints", abi.DISTANCE_DEF), ("rope_joints", abi.ROPE_DEF),
-                           ("weld_joints", abi.WELD_DEF)):
+                           ("weld_joints", abi.WELD_DEF), ("friction_joints", abi.FRICTION_DEF),
+                           ("motor_joints", abi.MOTOR_DEF), ("wheel_joints", abi.WHEEL_DEF)):
             d = p.get(key, np.zeros(0, dtype)).copy()
             d["body_a"] += nb
             d["body_b"] += nb
@@ -307,6 +310,85 @@ def welded(n_beams=3, links=8, hx=0.3, hy=0.08, x0=-8.0, spacing=6.0, y=10.0, pi
         extra[k]["max_length"] = (y - 1.2) - 0.8        # taut: pulls the weight 0.8 m down
     out["rope_joints"] = np.concatenate([out["rope_joints"], extra])
     out["name"] = "welded"
+    return out
+
+
+def top_down(n=12, seed=5, width=16.0):
+    """Zero-gravity table top (the reference testbed's top-down use of b2FrictionJoint,
+    joints/b2frictionjoint.d:30-73, and b2MotorJoint, joints/b2motorjoint.d:30-80): boxes and
+    circles with a friction joint each to a static table body (max force ~ mass, max torque ~
+    mass), pushed by their initial velocities; two platforms are driven by motor joints
+    towards offsets from the table (one rotated, one translated) and push the others."""
+    rng = np.random.default_rng(seed)
+    table = _boxes([(0.0, 0.0)], 0.5, 0.5, abi.STATIC)
+    walls = container(width, width, thick=0.5)
+    walls["bodies"]["position"][:, 1] -= width / 2.0
+    items = []
+    for i in range(n):
+        x, y = rng.uniform(-width / 2 + 1.5, width / 2 - 1.5, 2)
+        items.append(_boxes([(x, y)], 0.4, 0.3, abi.DYNAMIC, 0.3, 1.0))
+    platforms = _boxes([(-3.0, -4.0), (3.0, 4.0)], 1.2, 0.2, abi.DYNAMIC, 0.3, 2.0)
+    out = _concat([table, walls] + items + [platforms])
+    out["gravity"] = (0.0, 0.0)
+    nb = len(out["bodies"])
+    dyn = np.nonzero(out["bodies"]["type"] == abi.DYNAMIC)[0]
+    out["bodies"]["linear_velocity"][dyn] = rng.normal(0.0, 3.0, (len(dyn), 2))
+    out["bodies"]["angular_velocity"][dyn] = rng.normal(0.0, 2.0, len(dyn))
+    fj = np.zeros(len(dyn) - 2, abi.FRICTION_DEF)
+    for k, b in enumerate(dyn[:-2]):
+        fj[k]["body_a"] = 0                      # the table
+        fj[k]["body_b"] = b
+        fj[k]["collide_connected"] = 1
+        fj[k]["max_force"] = 0.12 * 10.0 * 0.48   # mu * g * mass of a 0.8 x 0.6 box, density 1
+        fj[k]["max_torque"] = 0.12 * 10.0 * 0.48 * 0.3
+    mj = np.zeros(2, abi.MOTOR_DEF)
+    for k, b in enumerate(dyn[-2:]):
+        mj[k]["body_a"] = 0
+        mj[k]["body_b"] = b
+        mj[k]["collide_connected"] = 1
+        mj[k]["linear_offset"] = (-2.0, 1.0) if k == 0 else (4.0, -3.0)
+        mj[k]["angular_offset"] = 1.2 if k == 0 else 0.0
+        mj[k]["max_force"] = 40.0
+        mj[k]["max_torque"] = 20.0
+        mj[k]["correction_factor"] = 0.3
+    out["friction_joints"] = fj
+    out["motor_joints"] = mj
+    out["name"] = "top_down"
+    assert nb == len(out["bodies"])
+    return out
+
+
+def cars(n_cars=3, x0=-20.0, spacing=8.0, bumps=12, seed=7):
+    """Wheel joints (b2WheelJointDef, joints/b2wheeljoint.d:30-99): cars with a box chassis
+    and two circle wheels on spring suspensions (4 Hz, damping ratio 0.7, vertical axis), the
+    rear wheel driven by a motor (max torque 20, speed -10 rad/s; every other car without a
+    motor), driving over small box bumps on the ground."""
+    rng = np.random.default_rng(seed)
+    parts = [ground_box(hx=80.0)]
+    parts.append(_boxes([(float(x), 0.1) for x in rng.uniform(-15.0, 35.0, bumps)], 0.4, 0.1, abi.STATIC, 0.8))
+    for c in range(n_cars):
+        x = x0 + c * spacing
+        chassis = _boxes([(x, 1.0)], 1.5, 0.25, abi.DYNAMIC, 0.6, 1.0)
+        wheels = _boxes([(x - 1.0, 0.4), (x + 1.0, 0.4)], 0.4, 0.4, abi.DYNAMIC, 0.9, 1.0)
+        wheels["shapes"]["kind"] = abi.SHAPE_CIRCLE
+        wheels["shapes"]["radius"] = 0.4
+        part = _concat([chassis, wheels])
+        wj = np.zeros(2, abi.WHEEL_DEF)
+        for k in range(2):
+            wj[k]["body_a"] = 0
+            wj[k]["body_b"] = 1 + k
+            wj[k]["local_anchor_a"] = (-1.0 if k == 0 else 1.0, -0.6)
+            wj[k]["local_axis_a"] = (0.0, 1.0)
+            wj[k]["frequency_hz"] = 4.0
+            wj[k]["damping_ratio"] = 0.7
+        if c % 2 == 0:
+            wj[0]["enable_motor"] = 1
+            wj[0]["max_motor_torque"] = 20.0
+            wj[0]["motor_speed"] = -10.0
+        part["wheel_joints"] = wj
+        parts.append(part)
+    out = _concat(parts)
+    out["name"] = "cars"
     return out
 
 

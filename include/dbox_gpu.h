@@ -125,6 +125,35 @@ typedef struct {
     float damping_ratio;
 } dbox_weld_def;
 
+/* b2FrictionJointDef (dynamics/joints/b2frictionjoint.d:30-73) */
+typedef struct {
+    int32_t body_a, body_b;
+    int32_t collide_connected;
+    dbox_vec2 local_anchor_a, local_anchor_b;
+    float max_force, max_torque;
+} dbox_friction_def;
+
+/* b2MotorJointDef (dynamics/joints/b2motorjoint.d:30-80) */
+typedef struct {
+    int32_t body_a, body_b;
+    int32_t collide_connected;
+    dbox_vec2 linear_offset;     /* position of body B minus the position of body A, in A's frame */
+    float angular_offset;        /* angle of body B minus the angle of body A */
+    float max_force, max_torque;
+    float correction_factor;     /* position correction factor in [0, 1] */
+} dbox_motor_def;
+
+/* b2WheelJointDef (dynamics/joints/b2wheeljoint.d:30-99) */
+typedef struct {
+    int32_t body_a, body_b;
+    int32_t collide_connected;
+    dbox_vec2 local_anchor_a, local_anchor_b;
+    dbox_vec2 local_axis_a;      /* translation axis in body A (unit length) */
+    int32_t enable_motor;
+    float max_motor_torque, motor_speed;
+    float frequency_hz, damping_ratio;   /* suspension spring */
+} dbox_wheel_def;
+
 /* ------------------------------------------------------- world snapshot
  * Flat state records, used by dbox_world_export_state / import_state
  * (exact checkpoint/resume) and by the parity tests.  Flag words use the
@@ -238,6 +267,13 @@ int32_t dbox_joint_create_distance(dbox_world* w, int32_t world, const dbox_dist
 int32_t dbox_joint_create_rope(dbox_world* w, int32_t world, const dbox_rope_def* def, int32_t* out_joint);
 /* b2World.CreateJoint with a b2WeldJointDef (joints/b2weldjoint.d); snapshot: impulse[0..2]. */
 int32_t dbox_joint_create_weld(dbox_world* w, int32_t world, const dbox_weld_def* def, int32_t* out_joint);
+/* b2World.CreateJoint with a b2FrictionJointDef / b2MotorJointDef (joints/b2frictionjoint.d,
+ * b2motorjoint.d); snapshot: impulse[0..1] the linear impulse, impulse[2] the angular one. */
+int32_t dbox_joint_create_friction(dbox_world* w, int32_t world, const dbox_friction_def* def, int32_t* out_joint);
+int32_t dbox_joint_create_motor(dbox_world* w, int32_t world, const dbox_motor_def* def, int32_t* out_joint);
+/* b2World.CreateJoint with a b2WheelJointDef (joints/b2wheeljoint.d); snapshot: impulse[0] the
+ * point-to-line impulse, impulse[1] the spring impulse, motor_impulse. */
+int32_t dbox_joint_create_wheel(dbox_world* w, int32_t world, const dbox_wheel_def* def, int32_t* out_joint);
 
 /* Bulk creation of a whole scene into one world: n bodies, then m fixtures
  * (fixture_body[i] indexes the bodies created by this call), then k joints

@@ -47,6 +47,9 @@ def lib():
         L.orc_joint_create_distance.argtypes = [vp, vp]
         L.orc_joint_create_rope.argtypes = [vp, vp]
         L.orc_joint_create_weld.argtypes = [vp, vp]
+        L.orc_joint_create_friction.argtypes = [vp, vp]
+        L.orc_joint_create_motor.argtypes = [vp, vp]
+        L.orc_joint_create_wheel.argtypes = [vp, vp]
         L.orc_world_set_flags.argtypes = [vp, i32, i32, i32, i32, i32]
         L.orc_world_step.argtypes = [vp, f32, i32, i32]
         L.orc_world_step_n.argtypes = [vp, f32, i32, i32, i32]
@@ -117,7 +120,10 @@ class OracleWorld:
         # joint kinds after the revolute joints, in this order (the same as the library's)
         for key, dtype, fn in (("distance_joints", abi.DISTANCE_DEF, L.orc_joint_create_distance),
                                ("rope_joints", abi.ROPE_DEF, L.orc_joint_create_rope),
-                               ("weld_joints", abi.WELD_DEF, L.orc_joint_create_weld)):
+                               ("weld_joints", abi.WELD_DEF, L.orc_joint_create_weld),
+                               ("friction_joints", abi.FRICTION_DEF, L.orc_joint_create_friction),
+                               ("motor_joints", abi.MOTOR_DEF, L.orc_joint_create_motor),
+                               ("wheel_joints", abi.WHEEL_DEF, L.orc_joint_create_wheel)):
             for d in scene.get(key, ()):
                 dd = np.ascontiguousarray(np.array([d], dtype))
                 if fn(self.h, abi.ptr(dd)) < 0:

@@ -1739,7 +1739,8 @@ struct Velocity { Vec2 v; f32 w = 0; };
 struct TimeStep { f32 dt = 0, inv_dt = 0, dtRatio = 0; int velocityIterations = 0, positionIterations = 0; bool warmStarting = false; };
 struct SolverData { TimeStep step; Position* positions = nullptr; Velocity* velocities = nullptr; };
 
-enum { kRevoluteJoint = 0, kDistanceJoint = 1, kRopeJoint = 2, kWeldJoint = 3 };
+enum { kRevoluteJoint = 0, kDistanceJoint = 1, kRopeJoint = 2, kWeldJoint = 3, kFrictionJoint = 4, kMotorJoint = 5,
+       kWheelJoint = 6 };
 
 struct Joint {                                                          // joints/b2joint.d, b2revolutejoint.d, b2distancejoint.d
     int type = kRevoluteJoint;
@@ -1771,12 +1772,22 @@ struct Joint {                                                          // joint
     f32 length = 0, frequencyHz = 0, dampingRatio = 0, gamma = 0, bias = 0, distMass = 0;
     f32 curLength = 0;
     Vec2 u;
+    // friction and motor (linear impulse impulse.x/.y, angular impulse impulse.z)
+    f32 maxForce = 0, maxTorque = 0, correctionFactor = 0, angularOffset = 0, angularError = 0, angularMass = 0;
+    Vec2 linearOffset, linearError;
+    Mat22 linearMass;
+    // wheel (point-to-line impulse impulse.x, spring impulse impulse.y, motorImpulse)
+    Vec2 localXAxisA, localYAxisA, ax, ay;
+    f32 sAx = 0, sBx = 0, sAy = 0, sBy = 0, wheelMass = 0, springMass = 0;
 
     void InitVelocityConstraints(const SolverData& data) {
         switch (type) {
         case kDistanceJoint: DistanceInit(data); break;
         case kRopeJoint: RopeInit(data); break;
         case kWeldJoint: WeldInit(data); break;
+        case kFrictionJoint:
+        case kMotorJoint: FrictionMotorInit(data); break;
+        case kWheelJoint: WheelInit(data); break;
         default: RevoluteInit(data);
         }
     }
@@ -1785,6 +1796,9 @@ struct Joint {                                                          // joint
         case kDistanceJoint: DistanceSolveVelocity(data); break;
         case kRopeJoint: RopeSolveVelocity(data); break;
         case kWeldJoint: WeldSolveVelocity(data); break;
+        case kFrictionJoint:
+        case kMotorJoint: FrictionMotorSolveVelocity(data); break;
+        case kWheelJoint: WheelSolveVelocity(data); break;
         default: RevoluteSolveVelocity(data);
         }
     }
@@ -1793,6 +1807,9 @@ struct Joint {                                                          // joint
         case kDistanceJoint: return DistanceSolvePosition(data);
         case kRopeJoint: return RopeSolvePosition(data);
         case kWeldJoint: return WeldSolvePosition(data);
+        case kFrictionJoint:
+        case kMotorJoint: return true;                                 // no position correction
+        case kWheelJoint: return WheelSolvePosition(data);
         default: return RevoluteSolvePosition(data);
         }
     }
@@ -1900,6 +1917,247 @@ struct Joint {                                                          // joint
         data.positions[indexB].c = cB;
         data.positions[indexB].a = aB;
         return len - length < kLinearSlop;
+    }
+
+    // b2FrictionJoint (b2frictionjoint.d:178-315) and b2MotorJoint (b2motorjoint.d:223-366): the
+    // same 2x2 linear and 1x1 angular blocks with force / torque caps; the motor's anchors are
+    // the bodies' origins and it drives towards an offset with a correction factor
+    void FrictionMotorInit(const SolverData& data) {
+        LoadBodies();
+        Vec2 cA = data.positions[indexA].c;
+        f32 aA = data.positions[indexA].a;
+        Vec2 vA = data.velocities[indexA].v;
+        f32 wA = data.velocities[indexA].w;
+        Vec2 cB = data.positions[indexB].c;
+        f32 aB = data.positions[indexB].a;
+        Vec2 vB = data.velocities[indexB].v;
+        f32 wB = data.velocities[indexB].w;
+        Rot qA(aA), qB(aB);
+        if (type == kMotorJoint) {
+            rA = Mul(qA, -localCenterA);
+            rB = Mul(qB, -localCenterB);
+        } else {
+            rA = Mul(qA, localAnchorA - localCenterA);
+            rB = Mul(qB, localAnchorB - localCenterB);
+        }
+        f32 mA = invMassA, mB = invMassB, iA = invIA, iB = invIB;
+        Mat22 K;
+        K.ex.x = ((mA + mB) + (iA * rA.y) * rA.y) + (iB * rB.y) * rB.y;
+        K.ex.y = ((-iA) * rA.x) * rA.y - (iB * rB.x) * rB.y;
+        K.ey.x = K.ex.y;
+        K.ey.y = ((mA + mB) + (iA * rA.x) * rA.x) + (iB * rB.x) * rB.x;
+        linearMass = K.GetInverse();
+        angularMass = iA + iB;
+        if (angularMass > 0.0f) angularMass = 1.0f / angularMass;
+        if (type == kMotorJoint) {
+            linearError = ((((cB + rB) - cA) - rA) - Mul(qA, linearOffset));
+            angularError = (aB - aA) - angularOffset;
+        }
+        if (data.step.warmStarting) {
+            impulse.x *= data.step.dtRatio;
+            impulse.y *= data.step.dtRatio;
+            impulse.z *= data.step.dtRatio;
+            Vec2 P(impulse.x, impulse.y);
+            vA -= mA * P;
+            wA -= iA * (Cross(rA, P) + impulse.z);
+            vB += mB * P;
+            wB += iB * (Cross(rB, P) + impulse.z);
+        } else {
+            impulse.SetZero();
+        }
+        data.velocities[indexA].v = vA;
+        data.velocities[indexA].w = wA;
+        data.velocities[indexB].v = vB;
+        data.velocities[indexB].w = wB;
+    }
+
+    void FrictionMotorSolveVelocity(const SolverData& data) {
+        Vec2 vA = data.velocities[indexA].v;
+        f32 wA = data.velocities[indexA].w;
+        Vec2 vB = data.velocities[indexB].v;
+        f32 wB = data.velocities[indexB].w;
+        f32 mA = invMassA, mB = invMassB, iA = invIA, iB = invIB;
+        f32 h = data.step.dt, inv_h = data.step.inv_dt;
+        {
+            f32 Cdot = wB - wA;
+            if (type == kMotorJoint) Cdot = Cdot + (inv_h * correctionFactor) * angularError;
+            f32 imp = -angularMass * Cdot;
+            f32 oldImpulse = impulse.z;
+            f32 maxImpulse = h * maxTorque;
+            impulse.z = Clamp(impulse.z + imp, -maxImpulse, maxImpulse);
+            imp = impulse.z - oldImpulse;
+            wA -= iA * imp;
+            wB += iB * imp;
+        }
+        {
+            Vec2 Cdot = ((vB + Cross(wB, rB)) - vA) - Cross(wA, rA);
+            if (type == kMotorJoint) Cdot = Cdot + (inv_h * correctionFactor) * linearError;
+            Vec2 imp = -Mul(linearMass, Cdot);
+            Vec2 oldImpulse(impulse.x, impulse.y);
+            Vec2 li(impulse.x + imp.x, impulse.y + imp.y);
+            f32 maxImpulse = h * maxForce;
+            if (li.LengthSquared() > maxImpulse * maxImpulse) {
+                li.Normalize();
+                li *= maxImpulse;
+            }
+            impulse.x = li.x;
+            impulse.y = li.y;
+            imp = li - oldImpulse;
+            vA -= mA * imp;
+            wA -= iA * Cross(rA, imp);
+            vB += mB * imp;
+            wB += iB * Cross(rB, imp);
+        }
+        data.velocities[indexA].v = vA;
+        data.velocities[indexA].w = wA;
+        data.velocities[indexB].v = vB;
+        data.velocities[indexB].w = wB;
+    }
+
+    void WheelInit(const SolverData& data) {                            // b2wheeljoint.d:302-443
+        LoadBodies();
+        f32 mA = invMassA, mB = invMassB, iA = invIA, iB = invIB;
+        Vec2 cA = data.positions[indexA].c;
+        f32 aA = data.positions[indexA].a;
+        Vec2 vA = data.velocities[indexA].v;
+        f32 wA = data.velocities[indexA].w;
+        Vec2 cB = data.positions[indexB].c;
+        f32 aB = data.positions[indexB].a;
+        Vec2 vB = data.velocities[indexB].v;
+        f32 wB = data.velocities[indexB].w;
+        Rot qA(aA), qB(aB);
+        Vec2 rA_ = Mul(qA, localAnchorA - localCenterA);
+        Vec2 rB_ = Mul(qB, localAnchorB - localCenterB);
+        Vec2 d = ((cB + rB_) - cA) - rA_;
+        ay = Mul(qA, localYAxisA);                                      // point to line
+        sAy = Cross(d + rA_, ay);
+        sBy = Cross(rB_, ay);
+        wheelMass = ((mA + mB) + (iA * sAy) * sAy) + (iB * sBy) * sBy;
+        if (wheelMass > 0.0f) wheelMass = 1.0f / wheelMass;
+        springMass = 0.0f;                                              // spring
+        bias = 0.0f;
+        gamma = 0.0f;
+        if (frequencyHz > 0.0f) {
+            ax = Mul(qA, localXAxisA);
+            sAx = Cross(d + rA_, ax);
+            sBx = Cross(rB_, ax);
+            f32 invMass = ((mA + mB) + (iA * sAx) * sAx) + (iB * sBx) * sBx;
+            if (invMass > 0.0f) {
+                springMass = 1.0f / invMass;
+                f32 C = Dot(d, ax);
+                f32 omega = (2.0f * kPi) * frequencyHz;
+                f32 d2 = ((2.0f * springMass) * dampingRatio) * omega;
+                f32 k = (springMass * omega) * omega;
+                f32 h = data.step.dt;
+                gamma = h * (d2 + h * k);
+                if (gamma > 0.0f) gamma = 1.0f / gamma;
+                bias = ((C * h) * k) * gamma;
+                springMass = invMass + gamma;
+                if (springMass > 0.0f) springMass = 1.0f / springMass;
+            }
+        } else {
+            impulse.y = 0.0f;
+        }
+        if (enableMotor) {                                              // rotational motor
+            motorMass = iA + iB;
+            if (motorMass > 0.0f) motorMass = 1.0f / motorMass;
+        } else {
+            motorMass = 0.0f;
+            motorImpulse = 0.0f;
+        }
+        if (data.step.warmStarting) {
+            impulse.x *= data.step.dtRatio;
+            impulse.y *= data.step.dtRatio;
+            motorImpulse *= data.step.dtRatio;
+            Vec2 P = impulse.x * ay + impulse.y * ax;
+            f32 LA = (impulse.x * sAy + impulse.y * sAx) + motorImpulse;
+            f32 LB = (impulse.x * sBy + impulse.y * sBx) + motorImpulse;
+            vA -= invMassA * P;
+            wA -= invIA * LA;
+            vB += invMassB * P;
+            wB += invIB * LB;
+        } else {
+            impulse.x = 0.0f;
+            impulse.y = 0.0f;
+            motorImpulse = 0.0f;
+        }
+        data.velocities[indexA].v = vA;
+        data.velocities[indexA].w = wA;
+        data.velocities[indexB].v = vB;
+        data.velocities[indexB].w = wB;
+    }
+
+    void WheelSolveVelocity(const SolverData& data) {                   // b2wheeljoint.d:445-507
+        f32 mA = invMassA, mB = invMassB, iA = invIA, iB = invIB;
+        Vec2 vA = data.velocities[indexA].v;
+        f32 wA = data.velocities[indexA].w;
+        Vec2 vB = data.velocities[indexB].v;
+        f32 wB = data.velocities[indexB].w;
+        {                                                               // spring
+            f32 Cdot = (Dot(ax, vB - vA) + sBx * wB) - sAx * wA;
+            f32 imp = -springMass * ((Cdot + bias) + gamma * impulse.y);
+            impulse.y += imp;
+            Vec2 P = imp * ax;
+            f32 LA = imp * sAx, LB = imp * sBx;
+            vA -= mA * P;
+            wA -= iA * LA;
+            vB += mB * P;
+            wB += iB * LB;
+        }
+        {                                                               // rotational motor
+            f32 Cdot = (wB - wA) - motorSpeed;
+            f32 imp = -motorMass * Cdot;
+            f32 oldImpulse = motorImpulse;
+            f32 maxImpulse = data.step.dt * maxMotorTorque;
+            motorImpulse = Clamp(motorImpulse + imp, -maxImpulse, maxImpulse);
+            imp = motorImpulse - oldImpulse;
+            wA -= iA * imp;
+            wB += iB * imp;
+        }
+        {                                                               // point to line
+            f32 Cdot = (Dot(ay, vB - vA) + sBy * wB) - sAy * wA;
+            f32 imp = -wheelMass * Cdot;
+            impulse.x += imp;
+            Vec2 P = imp * ay;
+            f32 LA = imp * sAy, LB = imp * sBy;
+            vA -= mA * P;
+            wA -= iA * LA;
+            vB += mB * P;
+            wB += iB * LB;
+        }
+        data.velocities[indexA].v = vA;
+        data.velocities[indexA].w = wA;
+        data.velocities[indexB].v = vB;
+        data.velocities[indexB].w = wB;
+    }
+
+    bool WheelSolvePosition(const SolverData& data) {                   // b2wheeljoint.d:509-553
+        Vec2 cA = data.positions[indexA].c;
+        f32 aA = data.positions[indexA].a;
+        Vec2 cB = data.positions[indexB].c;
+        f32 aB = data.positions[indexB].a;
+        Rot qA(aA), qB(aB);
+        Vec2 rA_ = Mul(qA, localAnchorA - localCenterA);
+        Vec2 rB_ = Mul(qB, localAnchorB - localCenterB);
+        Vec2 d = ((cB - cA) + rB_) - rA_;
+        Vec2 ay_ = Mul(qA, localYAxisA);
+        f32 sAy_ = Cross(d + rA_, ay_);
+        f32 sBy_ = Cross(rB_, ay_);
+        f32 C = Dot(d, ay_);
+        // the effective mass uses the velocity pass's sAy / sBy, as the reference does
+        f32 k = ((invMassA + invMassB) + (invIA * sAy) * sAy) + (invIB * sBy) * sBy;
+        f32 imp = k != 0.0f ? -C / k : 0.0f;
+        Vec2 P = imp * ay_;
+        f32 LA = imp * sAy_, LB = imp * sBy_;
+        cA -= invMassA * P;
+        aA -= invIA * LA;
+        cB += invMassB * P;
+        aB += invIB * LB;
+        data.positions[indexA].c = cA;
+        data.positions[indexA].a = aA;
+        data.positions[indexB].c = cB;
+        data.positions[indexB].a = aB;
+        return Abs(C) <= kLinearSlop;
     }
 
     // the weld joint's K (b2weldjoint.d:229-238 and 387-396)
@@ -3349,6 +3607,62 @@ struct World {                                                          // dynam
         return LinkJoint(j);
     }
 
+    Joint* CreateFriction(const dbox_friction_def* def) {               // b2frictionjoint.d:85-96
+        Joint* j = new Joint();
+        j->type = kFrictionJoint;
+        j->bodyA = bodiesByIndex[def->body_a];
+        j->bodyB = bodiesByIndex[def->body_b];
+        j->collideConnected = def->collide_connected != 0;
+        j->localAnchorA = Vec2(def->local_anchor_a.x, def->local_anchor_a.y);
+        j->localAnchorB = Vec2(def->local_anchor_b.x, def->local_anchor_b.y);
+        j->impulse.SetZero();
+        j->maxForce = def->max_force;
+        j->maxTorque = def->max_torque;
+        return LinkJoint(j);
+    }
+
+    Joint* CreateMotor(const dbox_motor_def* def) {                     // b2motorjoint.d:92-106
+        Joint* j = new Joint();
+        j->type = kMotorJoint;
+        j->bodyA = bodiesByIndex[def->body_a];
+        j->bodyB = bodiesByIndex[def->body_b];
+        j->collideConnected = def->collide_connected != 0;
+        j->linearOffset = Vec2(def->linear_offset.x, def->linear_offset.y);
+        j->angularOffset = def->angular_offset;
+        j->impulse.SetZero();
+        j->maxForce = def->max_force;
+        j->maxTorque = def->max_torque;
+        j->correctionFactor = def->correction_factor;
+        return LinkJoint(j);
+    }
+
+    Joint* CreateWheel(const dbox_wheel_def* def) {                     // b2wheeljoint.d:110-139
+        Joint* j = new Joint();
+        j->type = kWheelJoint;
+        j->bodyA = bodiesByIndex[def->body_a];
+        j->bodyB = bodiesByIndex[def->body_b];
+        j->collideConnected = def->collide_connected != 0;
+        j->localAnchorA = Vec2(def->local_anchor_a.x, def->local_anchor_a.y);
+        j->localAnchorB = Vec2(def->local_anchor_b.x, def->local_anchor_b.y);
+        j->localXAxisA = Vec2(def->local_axis_a.x, def->local_axis_a.y);
+        j->localYAxisA = Cross(1.0f, j->localXAxisA);
+        j->wheelMass = 0.0f;
+        j->impulse.SetZero();
+        j->motorMass = 0.0f;
+        j->motorImpulse = 0.0f;
+        j->springMass = 0.0f;
+        j->maxMotorTorque = def->max_motor_torque;
+        j->motorSpeed = def->motor_speed;
+        j->enableMotor = def->enable_motor != 0;
+        j->frequencyHz = def->frequency_hz;
+        j->dampingRatio = def->damping_ratio;
+        j->bias = 0.0f;
+        j->gamma = 0.0f;
+        j->ax.SetZero();
+        j->ay.SetZero();
+        return LinkJoint(j);
+    }
+
     Joint* CreateRevolute(const dbox_revolute_def* def) {               // b2world.d:196-261
         Joint* j = new Joint();
         j->bodyA = bodiesByIndex[def->body_a];
@@ -3782,6 +4096,24 @@ int orc_joint_create_weld(orc_world* w, const dbox_weld_def* def) {
     int n = (int)w->w.bodiesByIndex.size();
     if (def->body_a < 0 || def->body_a >= n || def->body_b < 0 || def->body_b >= n || def->body_a == def->body_b) return -1;
     return w->w.CreateWeld(def)->index;
+}
+
+int orc_joint_create_friction(orc_world* w, const dbox_friction_def* def) {
+    int n = (int)w->w.bodiesByIndex.size();
+    if (def->body_a < 0 || def->body_a >= n || def->body_b < 0 || def->body_b >= n || def->body_a == def->body_b) return -1;
+    return w->w.CreateFriction(def)->index;
+}
+
+int orc_joint_create_motor(orc_world* w, const dbox_motor_def* def) {
+    int n = (int)w->w.bodiesByIndex.size();
+    if (def->body_a < 0 || def->body_a >= n || def->body_b < 0 || def->body_b >= n || def->body_a == def->body_b) return -1;
+    return w->w.CreateMotor(def)->index;
+}
+
+int orc_joint_create_wheel(orc_world* w, const dbox_wheel_def* def) {
+    int n = (int)w->w.bodiesByIndex.size();
+    if (def->body_a < 0 || def->body_a >= n || def->body_b < 0 || def->body_b >= n || def->body_a == def->body_b) return -1;
+    return w->w.CreateWheel(def)->index;
 }
 
 int orc_scene_create(orc_world* w, int n_bodies, const dbox_body_def* bodies, int n_fixtures,

@@ -38,6 +38,9 @@ int orc_joint_create_revolute(orc_world* w, const dbox_revolute_def* def);
 int orc_joint_create_distance(orc_world* w, const dbox_distance_def* def);
 int orc_joint_create_rope(orc_world* w, const dbox_rope_def* def);
 int orc_joint_create_weld(orc_world* w, const dbox_weld_def* def);
+int orc_joint_create_friction(orc_world* w, const dbox_friction_def* def);
+int orc_joint_create_motor(orc_world* w, const dbox_motor_def* def);
+int orc_joint_create_wheel(orc_world* w, const dbox_wheel_def* def);
 int orc_scene_create(orc_world* w, int n_bodies, const dbox_body_def* bodies, int n_fixtures,
                      const int* fixture_body, const dbox_shape_def* shapes, const dbox_fixture_def* fixtures,
                      int n_joints, const dbox_revolute_def* joints);

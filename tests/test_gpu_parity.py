@@ -215,3 +215,41 @@ def test_weld_and_rope_joints_exact(oracle_lib, gpu_lib):
             for i, ow in enumerate(ows):
                 d = exact_diff(ow.export_state(), gw.export_state(i))
                 assert not d, "world %d step %d: %s" % (i, t + 1, d[:6])
+
+
+def test_friction_and_motor_joints_exact(oracle_lib, gpu_lib):
+    # zero-gravity top-down worlds with friction joints to a table body and two motor-driven
+    # platforms: bit-exact against the oracle
+    from dbox_gb300 import scenes
+    oracle_lib.set_trig_mode(1)
+    # zero gravity: one handle for the top-down worlds (a handle has one gravity, as a b2World)
+    worlds = [scenes.top_down(), scenes.top_down(n=20, seed=9)]
+    gw = gpu_lib.World(worlds)
+    ows = [oracle_lib.OracleWorld(s) for s in worlds]
+    for t in range(150):
+        gw.step()
+        for ow in ows:
+            ow.step()
+        if t % 30 == 29:
+            for i, ow in enumerate(ows):
+                d = exact_diff(ow.export_state(), gw.export_state(i))
+                assert not d, "world %d step %d: %s" % (i, t + 1, d[:6])
+
+
+def test_wheel_joint_cars_exact(oracle_lib, gpu_lib):
+    # sprung, motor-driven wheels over bumps (circle wheels against boxes), batched with
+    # the other joint kinds: bit-exact against the oracle
+    from dbox_gb300 import scenes
+    oracle_lib.set_trig_mode(1)
+    worlds = [scenes.cars(), scenes.cars(n_cars=2, seed=11), scenes.welded(n_beams=1, links=4, pile=False),
+              scenes.ropes(n_ropes=1, links=5)]
+    gw = gpu_lib.World(worlds)
+    ows = [oracle_lib.OracleWorld(s) for s in worlds]
+    for t in range(180):
+        gw.step()
+        for ow in ows:
+            ow.step()
+        if t % 30 == 29:
+            for i, ow in enumerate(ows):
+                d = exact_diff(ow.export_state(), gw.export_state(i))
+                assert not d, "world %d step %d: %s" % (i, t + 1, d[:6])

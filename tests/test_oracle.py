@@ -228,3 +228,43 @@ def test_weld_beams_and_ropes(oracle_lib):
     imp = st["joints"]["impulse"]
     assert (imp[n_rev + n_dist:n_rev + n_dist + n_rope, 0] <= 0).all()          # ropes only pull
     assert (st["joints"]["limit_state"][n_rev + n_dist:n_rev + n_dist + n_rope] == 2).any()
+
+
+def test_friction_and_motor_joints_top_down(oracle_lib):
+    # b2FrictionJoint brakes the top-down bodies (no gravity); b2MotorJoint drives its
+    # platform to the offset (position and angle) from the table body
+    from dbox_gb300 import scenes
+    oracle_lib.set_trig_mode(1)
+    s = scenes.top_down()
+    ow = oracle_lib.OracleWorld(s)
+    ow.step(steps=240)
+    b = ow.export_state()["bodies"]
+    v0 = np.abs(s["bodies"]["linear_velocity"]).sum()
+    assert np.abs(b["vel"][:, :2]).sum() < 0.2 * v0
+    m = s["motor_joints"][0]
+    p = b["xf"][m["body_b"], :2]
+    assert np.abs(p - m["linear_offset"]).max() < 0.05, p
+    assert abs(b["sweep"][m["body_b"], 7] - m["angular_offset"]) < 0.02
+
+
+def test_wheel_joint_cars_drive(oracle_lib):
+    # b2WheelJoint: the motor-driven cars drive forward over the bumps on sprung wheels that
+    # stay under the chassis (point-to-line constraint) and stay on their axles
+    from dbox_gb300 import scenes
+    oracle_lib.set_trig_mode(1)
+    s = scenes.cars()
+    ow = oracle_lib.OracleWorld(s)
+    ow.step(steps=300)
+    st = ow.export_state()
+    b = st["bodies"]
+    n = len(s["bodies"])
+    for c in range(3):
+        chassis, rear, front = n - 9 + 3 * c, n - 8 + 3 * c, n - 7 + 3 * c
+        if c % 2 == 0:
+            assert b["xf"][chassis, 0] - s["bodies"]["position"][chassis, 0] > 5.0
+        # each wheel's centre stays on the chassis' suspension line (body-frame x within 1 cm)
+        cx, cy, sn, cs = b["xf"][chassis]
+        for wheel, ax in ((rear, -1.0), (front, 1.0)):
+            dx, dy = b["xf"][wheel, 0] - cx, b["xf"][wheel, 1] - cy
+            assert abs(cs * dx + sn * dy - ax) < 0.01
+    assert st["joints"]["motor_impulse"][0] != 0
