@@ -52,6 +52,10 @@ def lib():
     L.dbox_joint_create_friction.argtypes = [vp, i32, vp, ctypes.POINTER(i32)]
     L.dbox_joint_create_motor.argtypes = [vp, i32, vp, ctypes.POINTER(i32)]
     L.dbox_joint_create_wheel.argtypes = [vp, i32, vp, ctypes.POINTER(i32)]
+    L.dbox_joint_create_prismatic.argtypes = [vp, i32, vp, ctypes.POINTER(i32)]
+    L.dbox_joint_create_pulley.argtypes = [vp, i32, vp, ctypes.POINTER(i32)]
+    L.dbox_joint_create_mouse.argtypes = [vp, i32, vp, ctypes.POINTER(i32)]
+    L.dbox_joint_set_mouse_target.argtypes = [vp, i32, i32, abi.Vec2]
     L.dbox_world_set_flags.argtypes = [vp, i32, i32, i32, i32, i32]
     L.dbox_world_set_gravity.argtypes = [vp, abi.Vec2]
     L.dbox_world_step.argtypes = [vp, f32, i32, i32]
@@ -244,7 +248,7 @@ class World:
                 self.create_joint(i, "distance", d)
             for d in s.get("rope_joints", ()):
                 self.create_joint(i, "rope", d)
-            for kind in ("weld", "friction", "motor", "wheel"):
+            for kind in ("weld", "friction", "motor", "wheel", "prismatic", "pulley", "mouse"):
                 for d in s.get(kind + "_joints", ()):
                     self.create_joint(i, kind, d)
         self.body_counts = [len(s["bodies"]) for s in scenes]
@@ -256,18 +260,26 @@ class World:
                     "weld": ("WELD_DEF", "dbox_joint_create_weld"),
                     "friction": ("FRICTION_DEF", "dbox_joint_create_friction"),
                     "motor": ("MOTOR_DEF", "dbox_joint_create_motor"),
-                    "wheel": ("WHEEL_DEF", "dbox_joint_create_wheel")}
+                    "wheel": ("WHEEL_DEF", "dbox_joint_create_wheel"),
+                    "prismatic": ("PRISMATIC_DEF", "dbox_joint_create_prismatic"),
+                    "pulley": ("PULLEY_DEF", "dbox_joint_create_pulley"),
+                    "mouse": ("MOUSE_DEF", "dbox_joint_create_mouse")}
 
     def create_joint(self, world, kind, d):
         """b2World.CreateJoint with a b2DistanceJointDef / b2RopeJointDef / b2WeldJointDef /
-        b2FrictionJointDef / b2MotorJointDef / b2WheelJointDef (kind "distance", "rope",
-        "weld", "friction", "motor" or "wheel"; d the matching *_DEF record); returns the
-        joint index."""
+        b2FrictionJointDef / b2MotorJointDef / b2WheelJointDef / b2PrismaticJointDef /
+        b2PulleyJointDef / b2MouseJointDef (kind "distance", "rope", "weld", "friction",
+        "motor", "wheel", "prismatic", "pulley" or "mouse"; d the matching *_DEF record);
+        returns the joint index."""
         dtype, fn = World._JOINT_KINDS[kind]
         dd = np.ascontiguousarray(np.array([d], getattr(abi, dtype)))
         out = ctypes.c_int32()
         _check(getattr(lib(), fn)(self.h, world, abi.ptr(dd), ctypes.byref(out)), fn)
         return out.value
+
+    def set_mouse_target(self, world, joint, target):
+        """b2MouseJoint.SetTarget: wakes the dragged body and moves the target."""
+        _check(lib().dbox_joint_set_mouse_target(self.h, world, joint, abi.Vec2(*target)), "dbox_joint_set_mouse_target")
 
     def close(self):
         if getattr(self, "h", None) is not None and self.h.value:

@@ -70,6 +70,25 @@ WHEEL_DEF = np.dtype([
     ("frequency_hz", "<f4"), ("damping_ratio", "<f4"),
 ])
 assert WHEEL_DEF.itemsize == 56
+PRISMATIC_DEF = np.dtype([
+    ("body_a", "<i4"), ("body_b", "<i4"), ("collide_connected", "<i4"),
+    ("local_anchor_a", "<f4", 2), ("local_anchor_b", "<f4", 2), ("local_axis_a", "<f4", 2),
+    ("reference_angle", "<f4"), ("enable_limit", "<i4"), ("lower_translation", "<f4"), ("upper_translation", "<f4"),
+    ("enable_motor", "<i4"), ("max_motor_force", "<f4"), ("motor_speed", "<f4"),
+])
+assert PRISMATIC_DEF.itemsize == 64
+PULLEY_DEF = np.dtype([
+    ("body_a", "<i4"), ("body_b", "<i4"), ("collide_connected", "<i4"),
+    ("ground_anchor_a", "<f4", 2), ("ground_anchor_b", "<f4", 2),
+    ("local_anchor_a", "<f4", 2), ("local_anchor_b", "<f4", 2),
+    ("length_a", "<f4"), ("length_b", "<f4"), ("ratio", "<f4"),
+])
+assert PULLEY_DEF.itemsize == 56
+MOUSE_DEF = np.dtype([
+    ("body_a", "<i4"), ("body_b", "<i4"), ("collide_connected", "<i4"),
+    ("target", "<f4", 2), ("max_force", "<f4"), ("frequency_hz", "<f4"), ("damping_ratio", "<f4"),
+])
+assert MOUSE_DEF.itemsize == 32
 
 WORLD_HEADER = np.dtype([
     ("body_count", "<i4"), ("fixture_count", "<i4"), ("contact_count", "<i4"), ("joint_count", "<i4"),

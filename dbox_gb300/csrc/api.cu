@@ -6,6 +6,7 @@
 // CUDA graph) and state export/import.  All per-step work runs in the kernels
 // of step.cu; this file only moves data and launches.
 #include <cuda_runtime.h>
+#include <cfloat>
 #include <stdint.h>
 #include <string.h>
 #include <stdio.h>
@@ -1074,6 +1075,121 @@ int create_wheel_joint(HostWorld& hw, const dbox_wheel_def* d) {
     j.frequency_hz = d->frequency_hz;
     j.damping_ratio = d->damping_ratio;
     return link_joint(hw, j);
+}
+
+// b2World.CreateJoint with a b2PrismaticJointDef (b2prismaticjoint.d:163-187): the axis is
+// normalised as b2Vec2.Normalize does (b2math.d:160-175)
+int create_prismatic_joint(HostWorld& hw, const dbox_prismatic_def* d) {
+    int nb = (int)hw.bs.size();
+    if (d->body_a < 0 || d->body_a >= nb || d->body_b < 0 || d->body_b >= nb || d->body_a == d->body_b) return -1;
+    dg::DJoint j;
+    memset(&j, 0, sizeof(j));
+    j.type = dg::kPrismaticJoint;
+    j.body_a = d->body_a;
+    j.body_b = d->body_b;
+    j.collide_connected = d->collide_connected ? 1 : 0;
+    j.local_anchor_a = make_float2(d->local_anchor_a.x, d->local_anchor_a.y);
+    j.local_anchor_b = make_float2(d->local_anchor_b.x, d->local_anchor_b.y);
+    float ax = d->local_axis_a.x, ay = d->local_axis_a.y;
+    float len = sqrtf(ax * ax + ay * ay);
+    if (!(len < FLT_EPSILON)) {
+        float inv = 1.0f / len;
+        ax *= inv;
+        ay *= inv;
+    }
+    j.local_axis_x = make_float2(ax, ay);
+    j.local_axis_y = make_float2(-1.0f * ay, 1.0f * ax);                 // b2Cross(1, x)
+    j.reference_angle = d->reference_angle;
+    j.enable_limit = d->enable_limit ? 1 : 0;
+    j.lower_translation = d->lower_translation;
+    j.upper_translation = d->upper_translation;
+    j.enable_motor = d->enable_motor ? 1 : 0;
+    j.max_motor_force = d->max_motor_force;
+    j.motor_speed = d->motor_speed;
+    return link_joint(hw, j);
+}
+
+// b2World.CreateJoint with a b2PulleyJointDef (b2pulleyjoint.d:116-131)
+int create_pulley_joint(HostWorld& hw, const dbox_pulley_def* d) {
+    int nb = (int)hw.bs.size();
+    if (d->body_a < 0 || d->body_a >= nb || d->body_b < 0 || d->body_b >= nb || d->body_a == d->body_b) return -1;
+    dg::DJoint j;
+    memset(&j, 0, sizeof(j));
+    j.type = dg::kPulleyJoint;
+    j.body_a = d->body_a;
+    j.body_b = d->body_b;
+    j.collide_connected = d->collide_connected ? 1 : 0;
+    j.ground_a = make_float2(d->ground_anchor_a.x, d->ground_anchor_a.y);
+    j.ground_b = make_float2(d->ground_anchor_b.x, d->ground_anchor_b.y);
+    j.local_anchor_a = make_float2(d->local_anchor_a.x, d->local_anchor_a.y);
+    j.local_anchor_b = make_float2(d->local_anchor_b.x, d->local_anchor_b.y);
+    j.ratio = d->ratio;
+    j.constant = d->length_a + d->ratio * d->length_b;
+    return link_joint(hw, j);
+}
+
+// b2World.CreateJoint with a b2MouseJointDef (b2mousejoint.d:112-129): the local anchor is the
+// target in body B's frame now (b2MulT(xf, v), b2math.d:743-751)
+int create_mouse_joint(HostWorld& hw, const dbox_mouse_def* d) {
+    int nb = (int)hw.bs.size();
+    if (d->body_a < 0 || d->body_a >= nb || d->body_b < 0 || d->body_b >= nb || d->body_a == d->body_b) return -1;
+    dg::DJoint j;
+    memset(&j, 0, sizeof(j));
+    j.type = dg::kMouseJoint;
+    j.body_a = d->body_a;
+    j.body_b = d->body_b;
+    j.collide_connected = d->collide_connected ? 1 : 0;
+    j.target = make_float2(d->target.x, d->target.y);
+    const float* xf = hw.bs[d->body_b].xf;
+    float px = d->target.x - xf[0], py = d->target.y - xf[1];
+    j.local_anchor_b = make_float2(xf[3] * px + xf[2] * py, -xf[2] * px + xf[3] * py);
+    j.max_force = d->max_force;
+    j.frequency_hz = d->frequency_hz;
+    j.damping_ratio = d->damping_ratio;
+    return link_joint(hw, j);
+}
+
+int32_t dbox_joint_create_pulley(dbox_world* w, int32_t world, const dbox_pulley_def* def, int32_t* out_joint) {
+    if (!w || !def || world < 0 || world >= (int)w->worlds.size()) return fail(DBOX_ERR_INVALID, "dbox_joint_create_pulley: bad arguments");
+    int rc = prepare_edit(w);
+    if (rc) return rc;
+    int idx = create_pulley_joint(w->worlds[world], def);
+    if (idx < 0) return fail(DBOX_ERR_INVALID, "dbox_joint_create_pulley: bad bodies");
+    if (out_joint) *out_joint = idx;
+    return DBOX_OK;
+}
+
+int32_t dbox_joint_create_mouse(dbox_world* w, int32_t world, const dbox_mouse_def* def, int32_t* out_joint) {
+    if (!w || !def || world < 0 || world >= (int)w->worlds.size()) return fail(DBOX_ERR_INVALID, "dbox_joint_create_mouse: bad arguments");
+    int rc = prepare_edit(w);
+    if (rc) return rc;
+    int idx = create_mouse_joint(w->worlds[world], def);
+    if (idx < 0) return fail(DBOX_ERR_INVALID, "dbox_joint_create_mouse: bad bodies");
+    if (out_joint) *out_joint = idx;
+    return DBOX_OK;
+}
+
+int32_t dbox_joint_set_mouse_target(dbox_world* w, int32_t world, int32_t joint, dbox_vec2 target) {
+    if (!w || world < 0 || world >= (int)w->worlds.size()) return fail(DBOX_ERR_INVALID, "dbox_joint_set_mouse_target: bad world");
+    int rc = prepare_edit(w);
+    if (rc) return rc;
+    HostWorld& hw = w->worlds[world];
+    if (joint < 0 || joint >= (int)hw.jt.size() || hw.jt[joint].type != dg::kMouseJoint)
+        return fail(DBOX_ERR_INVALID, "dbox_joint_set_mouse_target: not a mouse joint");
+    dbox_body_state& b = hw.bs[hw.jt[joint].body_b];
+    if ((b.flags & dg::kBodyAwake) == 0) { b.flags |= dg::kBodyAwake; b.sleep_time = 0.0f; }   // SetAwake(true)
+    hw.jt[joint].target = make_float2(target.x, target.y);
+    return DBOX_OK;
+}
+
+int32_t dbox_joint_create_prismatic(dbox_world* w, int32_t world, const dbox_prismatic_def* def, int32_t* out_joint) {
+    if (!w || !def || world < 0 || world >= (int)w->worlds.size()) return fail(DBOX_ERR_INVALID, "dbox_joint_create_prismatic: bad arguments");
+    int rc = prepare_edit(w);
+    if (rc) return rc;
+    int idx = create_prismatic_joint(w->worlds[world], def);
+    if (idx < 0) return fail(DBOX_ERR_INVALID, "dbox_joint_create_prismatic: bad bodies");
+    if (out_joint) *out_joint = idx;
+    return DBOX_OK;
 }
 
 int32_t dbox_joint_create_wheel(dbox_world* w, int32_t world, const dbox_wheel_def* def, int32_t* out_joint) {

@@ -1927,6 +1927,364 @@ __device__ __noinline__ bool wheel_solve_position(const DJoint& j, int la, int l
     return babs(C) <= kLinearSlop;
 }
 
+// ------------------------------------------------------------ prismatic joint (joints/b2prismaticjoint.d:391-757)
+__device__ __noinline__ void prismatic_init(const Ctx& x, int ji, int b0, SB sb, bool warm, float dtRatio) {
+    DJoint& j = x.jt[ji];
+    const dbox_body_state& ba = x.bs[j.body_a];
+    const dbox_body_state& bb = x.bs[j.body_b];
+    int la = j.body_a - b0, lb = j.body_b - b0;
+    j.lcA = b_lc(ba);
+    j.lcB = b_lc(bb);
+    j.invMassA = ba.mass[1];
+    j.invMassB = bb.mass[1];
+    j.invIA = ba.mass[3];
+    j.invIB = bb.mass[3];
+    float2 cA = sb.c(la), cB = sb.c(lb);
+    float aA = sb.a(la), aB = sb.a(lb);
+    float2 vA = sb.v(la), vB = sb.v(lb);
+    float wA = sb.w(la), wB = sb.w(lb);
+    Rot qA = rot(aA), qB = rot(aB);
+    float2 rA = mul(qA, j.local_anchor_a - j.lcA);
+    float2 rB = mul(qB, j.local_anchor_b - j.lcB);
+    float2 d = ((cB - cA) + rB) - rA;
+    const float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    j.axis = mul(qA, j.local_axis_x);                                   // motor
+    j.a1 = cross(d + rA, j.axis);
+    j.a2 = cross(rB, j.axis);
+    float mm = ((mA + mB) + (iA * j.a1) * j.a1) + (iB * j.a2) * j.a2;
+    if (mm > 0.0f) mm = fdiv(1.0f, mm);
+    j.motor_mass = mm;
+    j.perp = mul(qA, j.local_axis_y);                                   // prismatic constraint
+    j.s1 = cross(d + rA, j.perp);
+    j.s2 = cross(rB, j.perp);
+    float k11 = ((mA + mB) + (iA * j.s1) * j.s1) + (iB * j.s2) * j.s2;
+    float k12 = iA * j.s1 + iB * j.s2;
+    float k13 = (iA * j.s1) * j.a1 + (iB * j.s2) * j.a2;
+    float k22 = iA + iB;
+    if (k22 == 0.0f) k22 = 1.0f;
+    float k23 = iA * j.a1 + iB * j.a2;
+    float k33 = ((mA + mB) + (iA * j.a1) * j.a1) + (iB * j.a2) * j.a2;
+    j.mass[0] = k11; j.mass[1] = k12; j.mass[2] = k13;
+    j.mass[3] = k12; j.mass[4] = k22; j.mass[5] = k23;
+    j.mass[6] = k13; j.mass[7] = k23; j.mass[8] = k33;
+    if (j.enable_limit) {
+        float jointTranslation = dot(j.axis, d);
+        if (babs(j.upper_translation - j.lower_translation) < 2.0f * kLinearSlop) {
+            j.limit_state = 3;
+        } else if (jointTranslation <= j.lower_translation) {
+            if (j.limit_state != 1) { j.limit_state = 1; j.impulse[2] = 0.0f; }
+        } else if (jointTranslation >= j.upper_translation) {
+            if (j.limit_state != 2) { j.limit_state = 2; j.impulse[2] = 0.0f; }
+        } else {
+            j.limit_state = 0;
+            j.impulse[2] = 0.0f;
+        }
+    } else {
+        j.limit_state = 0;
+        j.impulse[2] = 0.0f;
+    }
+    if (!j.enable_motor) j.motor_impulse = 0.0f;
+    if (warm) {
+        j.impulse[0] *= dtRatio; j.impulse[1] *= dtRatio; j.impulse[2] *= dtRatio;
+        j.motor_impulse *= dtRatio;
+        float2 P = j.impulse[0] * j.perp + (j.motor_impulse + j.impulse[2]) * j.axis;
+        float LA = (j.impulse[0] * j.s1 + j.impulse[1]) + (j.motor_impulse + j.impulse[2]) * j.a1;
+        float LB = (j.impulse[0] * j.s2 + j.impulse[1]) + (j.motor_impulse + j.impulse[2]) * j.a2;
+        vA -= mA * P;
+        wA -= iA * LA;
+        vB += mB * P;
+        wB += iB * LB;
+    } else {
+        j.impulse[0] = 0.0f; j.impulse[1] = 0.0f; j.impulse[2] = 0.0f;
+        j.motor_impulse = 0.0f;
+    }
+    sb.set_v(la, vA, wA);
+    sb.set_v(lb, vB, wB);
+}
+
+__device__ __noinline__ void prismatic_solve_velocity(const Ctx& x, DJoint& j, int la, int lb, SB sb) {
+    float2 vA = sb.v(la), vB = sb.v(lb);
+    float wA = sb.w(la), wB = sb.w(lb);
+    const float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    if (j.enable_motor && j.limit_state != 3) {
+        float Cdot = (dot(j.axis, vB - vA) + j.a2 * wB) - j.a1 * wA;
+        float impulse = j.motor_mass * (j.motor_speed - Cdot);
+        float oldImpulse = j.motor_impulse;
+        float maxImpulse = x.dt * j.max_motor_force;
+        j.motor_impulse = bclamp(j.motor_impulse + impulse, -maxImpulse, maxImpulse);
+        impulse = j.motor_impulse - oldImpulse;
+        float2 P = impulse * j.axis;
+        float LA = impulse * j.a1, LB = impulse * j.a2;
+        vA -= mA * P;
+        wA -= iA * LA;
+        vB += mB * P;
+        wB += iB * LB;
+    }
+    float2 Cdot1;
+    Cdot1.x = (dot(j.perp, vB - vA) + j.s2 * wB) - j.s1 * wA;
+    Cdot1.y = wB - wA;
+    if (j.enable_limit && j.limit_state != 0) {
+        float Cdot2 = (dot(j.axis, vB - vA) + j.a2 * wB) - j.a1 * wA;
+        float3 f1 = make_float3(j.impulse[0], j.impulse[1], j.impulse[2]);
+        float3 df = solve33(j.mass, make_float3(-Cdot1.x, -Cdot1.y, -Cdot2));
+        float3 imp = make_float3(f1.x + df.x, f1.y + df.y, f1.z + df.z);
+        if (j.limit_state == 1) imp.z = bmax(imp.z, 0.0f);
+        else if (j.limit_state == 2) imp.z = bmin(imp.z, 0.0f);
+        float2 b = -Cdot1 - (imp.z - f1.z) * v2(j.mass[6], j.mass[7]);
+        float2 f2r = solve22(j.mass, b) + v2(f1.x, f1.y);
+        imp.x = f2r.x;
+        imp.y = f2r.y;
+        j.impulse[0] = imp.x; j.impulse[1] = imp.y; j.impulse[2] = imp.z;
+        float3 d3 = make_float3(imp.x - f1.x, imp.y - f1.y, imp.z - f1.z);
+        float2 P = d3.x * j.perp + d3.z * j.axis;
+        float LA = (d3.x * j.s1 + d3.y) + d3.z * j.a1;
+        float LB = (d3.x * j.s2 + d3.y) + d3.z * j.a2;
+        vA -= mA * P;
+        wA -= iA * LA;
+        vB += mB * P;
+        wB += iB * LB;
+    } else {
+        float2 df = solve22(j.mass, -Cdot1);
+        j.impulse[0] += df.x;
+        j.impulse[1] += df.y;
+        float2 P = df.x * j.perp;
+        float LA = df.x * j.s1 + df.y;
+        float LB = df.x * j.s2 + df.y;
+        vA -= mA * P;
+        wA -= iA * LA;
+        vB += mB * P;
+        wB += iB * LB;
+    }
+    sb.set_v(la, vA, wA);
+    sb.set_v(lb, vB, wB);
+}
+
+__device__ __noinline__ bool prismatic_solve_position(const DJoint& j, int la, int lb, SB sb) {
+    float2 cA = sb.c(la), cB = sb.c(lb);
+    float aA = sb.a(la), aB = sb.a(lb);
+    Rot qA = rot(aA), qB = rot(aB);
+    const float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    float2 rA = mul(qA, j.local_anchor_a - j.lcA);
+    float2 rB = mul(qB, j.local_anchor_b - j.lcB);
+    float2 d = ((cB + rB) - cA) - rA;
+    float2 axis = mul(qA, j.local_axis_x);
+    float a1 = cross(d + rA, axis);
+    float a2 = cross(rB, axis);
+    float2 perp = mul(qA, j.local_axis_y);
+    float s1 = cross(d + rA, perp);
+    float s2 = cross(rB, perp);
+    float2 C1 = v2(dot(perp, d), (aB - aA) - j.reference_angle);
+    float linearError = babs(C1.x);
+    float angularError = babs(C1.y);
+    bool active = false;
+    float C2 = 0.0f;
+    if (j.enable_limit) {
+        float translation = dot(axis, d);
+        if (babs(j.upper_translation - j.lower_translation) < 2.0f * kLinearSlop) {
+            C2 = bclamp(translation, -kMaxLinearCorrection, kMaxLinearCorrection);
+            linearError = bmax(linearError, babs(translation));
+            active = true;
+        } else if (translation <= j.lower_translation) {
+            C2 = bclamp((translation - j.lower_translation) + kLinearSlop, -kMaxLinearCorrection, 0.0f);
+            linearError = bmax(linearError, j.lower_translation - translation);
+            active = true;
+        } else if (translation >= j.upper_translation) {
+            C2 = bclamp((translation - j.upper_translation) - kLinearSlop, 0.0f, kMaxLinearCorrection);
+            linearError = bmax(linearError, translation - j.upper_translation);
+            active = true;
+        }
+    }
+    float3 imp;
+    float k11 = ((mA + mB) + (iA * s1) * s1) + (iB * s2) * s2;
+    float k12 = iA * s1 + iB * s2;
+    float k22 = iA + iB;
+    if (k22 == 0.0f) k22 = 1.0f;
+    if (active) {
+        float k13 = (iA * s1) * a1 + (iB * s2) * a2;
+        float k23 = iA * a1 + iB * a2;
+        float k33 = ((mA + mB) + (iA * a1) * a1) + (iB * a2) * a2;
+        float K[9] = {k11, k12, k13, k12, k22, k23, k13, k23, k33};
+        imp = solve33(K, make_float3(-C1.x, -C1.y, -C2));
+    } else {
+        float K[9] = {k11, k12, 0.0f, k12, k22, 0.0f, 0.0f, 0.0f, 0.0f};
+        float2 i1 = solve22(K, -C1);
+        imp = make_float3(i1.x, i1.y, 0.0f);
+    }
+    float2 P = imp.x * perp + imp.z * axis;
+    float LA = (imp.x * s1 + imp.y) + imp.z * a1;
+    float LB = (imp.x * s2 + imp.y) + imp.z * a2;
+    cA -= mA * P;
+    aA -= iA * LA;
+    cB += mB * P;
+    aB += iB * LB;
+    sb.set_c(la, cA, aA);
+    sb.set_c(lb, cB, aB);
+    return linearError <= kLinearSlop && angularError <= kAngularSlop;
+}
+
+// ------------------------------------------------------------ pulley joint (joints/b2pulleyjoint.d:181-350)
+__device__ __noinline__ void pulley_init(const Ctx& x, int ji, int b0, SB sb, bool warm, float dtRatio) {
+    DJoint& j = x.jt[ji];
+    const dbox_body_state& ba = x.bs[j.body_a];
+    const dbox_body_state& bb = x.bs[j.body_b];
+    int la = j.body_a - b0, lb = j.body_b - b0;
+    j.lcA = b_lc(ba);
+    j.lcB = b_lc(bb);
+    j.invMassA = ba.mass[1];
+    j.invMassB = bb.mass[1];
+    j.invIA = ba.mass[3];
+    j.invIB = bb.mass[3];
+    float2 cA = sb.c(la), cB = sb.c(lb);
+    float aA = sb.a(la), aB = sb.a(lb);
+    float2 vA = sb.v(la), vB = sb.v(lb);
+    float wA = sb.w(la), wB = sb.w(lb);
+    Rot qA = rot(aA), qB = rot(aB);
+    j.rA = mul(qA, j.local_anchor_a - j.lcA);
+    j.rB = mul(qB, j.local_anchor_b - j.lcB);
+    float2 uA = (cA + j.rA) - j.ground_a;
+    float2 uB = (cB + j.rB) - j.ground_b;
+    float lengthA = length(uA), lengthB = length(uB);
+    if (lengthA > 10.0f * kLinearSlop) uA *= fdiv(1.0f, lengthA); else uA = v2(0.0f, 0.0f);
+    if (lengthB > 10.0f * kLinearSlop) uB *= fdiv(1.0f, lengthB); else uB = v2(0.0f, 0.0f);
+    j.uA = uA;
+    j.uB = uB;
+    float ruA = cross(j.rA, uA), ruB = cross(j.rB, uB);
+    float mA = j.invMassA + (j.invIA * ruA) * ruA;
+    float mB = j.invMassB + (j.invIB * ruB) * ruB;
+    float mass = mA + (j.ratio * j.ratio) * mB;
+    if (mass > 0.0f) mass = fdiv(1.0f, mass);
+    j.mass[0] = mass;
+    if (warm) {
+        j.impulse[0] *= dtRatio;
+        float2 PA = (-j.impulse[0]) * uA;
+        float2 PB = ((-j.ratio) * j.impulse[0]) * uB;
+        vA += j.invMassA * PA;
+        wA += j.invIA * cross(j.rA, PA);
+        vB += j.invMassB * PB;
+        wB += j.invIB * cross(j.rB, PB);
+    } else {
+        j.impulse[0] = 0.0f;
+    }
+    sb.set_v(la, vA, wA);
+    sb.set_v(lb, vB, wB);
+}
+
+__device__ __noinline__ void pulley_solve_velocity(DJoint& j, int la, int lb, SB sb) {
+    float2 vA = sb.v(la), vB = sb.v(lb);
+    float wA = sb.w(la), wB = sb.w(lb);
+    float2 vpA = vA + cross(wA, j.rA);
+    float2 vpB = vB + cross(wB, j.rB);
+    float Cdot = (-dot(j.uA, vpA)) - j.ratio * dot(j.uB, vpB);
+    float impulse = -j.mass[0] * Cdot;
+    j.impulse[0] += impulse;
+    float2 PA = (-impulse) * j.uA;
+    float2 PB = ((-j.ratio) * impulse) * j.uB;
+    vA += j.invMassA * PA;
+    wA += j.invIA * cross(j.rA, PA);
+    vB += j.invMassB * PB;
+    wB += j.invIB * cross(j.rB, PB);
+    sb.set_v(la, vA, wA);
+    sb.set_v(lb, vB, wB);
+}
+
+__device__ __noinline__ bool pulley_solve_position(const DJoint& j, int la, int lb, SB sb) {
+    float2 cA = sb.c(la), cB = sb.c(lb);
+    float aA = sb.a(la), aB = sb.a(lb);
+    Rot qA = rot(aA), qB = rot(aB);
+    float2 rA = mul(qA, j.local_anchor_a - j.lcA);
+    float2 rB = mul(qB, j.local_anchor_b - j.lcB);
+    float2 uA = (cA + rA) - j.ground_a;
+    float2 uB = (cB + rB) - j.ground_b;
+    float lengthA = length(uA), lengthB = length(uB);
+    if (lengthA > 10.0f * kLinearSlop) uA *= fdiv(1.0f, lengthA); else uA = v2(0.0f, 0.0f);
+    if (lengthB > 10.0f * kLinearSlop) uB *= fdiv(1.0f, lengthB); else uB = v2(0.0f, 0.0f);
+    float ruA = cross(rA, uA), ruB = cross(rB, uB);
+    float mA = j.invMassA + (j.invIA * ruA) * ruA;
+    float mB = j.invMassB + (j.invIB * ruB) * ruB;
+    float mass = mA + (j.ratio * j.ratio) * mB;
+    if (mass > 0.0f) mass = fdiv(1.0f, mass);
+    float C = (j.constant - lengthA) - j.ratio * lengthB;
+    float linearError = babs(C);
+    float impulse = -mass * C;
+    float2 PA = (-impulse) * uA;
+    float2 PB = ((-j.ratio) * impulse) * uB;
+    cA += j.invMassA * PA;
+    aA += j.invIA * cross(rA, PA);
+    cB += j.invMassB * PB;
+    aB += j.invIB * cross(rB, PB);
+    sb.set_c(la, cA, aA);
+    sb.set_c(lb, cB, aB);
+    return linearError < kLinearSlop;
+}
+
+// ------------------------------------------------------------ mouse joint (joints/b2mousejoint.d:132-226), body B only
+__device__ __noinline__ void mouse_init(const Ctx& x, int ji, int b0, SB sb, bool warm, float dtRatio) {
+    DJoint& j = x.jt[ji];
+    const dbox_body_state& bb = x.bs[j.body_b];
+    int lb = j.body_b - b0;
+    j.lcB = b_lc(bb);
+    j.invMassB = bb.mass[1];
+    j.invIB = bb.mass[3];
+    float2 cB = sb.c(lb);
+    float aB = sb.a(lb);
+    float2 vB = sb.v(lb);
+    float wB = sb.w(lb);
+    Rot qB = rot(aB);
+    float mass = bb.mass[0];
+    float omega = (2.0f * kPi) * j.frequency_hz;
+    float d = ((2.0f * mass) * j.damping_ratio) * omega;
+    float k = mass * (omega * omega);
+    float h = x.dt;
+    float gamma = h * (d + h * k);
+    if (gamma != 0.0f) gamma = fdiv(1.0f, gamma);
+    j.gamma = gamma;
+    j.beta = (h * k) * gamma;
+    j.rB = mul(qB, j.local_anchor_b - j.lcB);
+    float k11 = (j.invMassB + (j.invIB * j.rB.y) * j.rB.y) + gamma;
+    float k21 = ((-j.invIB) * j.rB.x) * j.rB.y;
+    float k22 = (j.invMassB + (j.invIB * j.rB.x) * j.rB.x) + gamma;
+    float det = k11 * k22 - k21 * k21;                                  // b2Mat22.GetInverse
+    if (det != 0.0f) det = fdiv(1.0f, det);
+    j.mass[0] = det * k22;
+    j.mass[3] = -det * k21;
+    j.mass[1] = -det * k21;
+    j.mass[4] = det * k11;
+    float2 C = (cB + j.rB) - j.target;
+    C *= j.beta;
+    j.mouse_c = C;
+    wB *= 0.98f;                                                        // the reference's extra damping
+    if (warm) {
+        j.impulse[0] *= dtRatio;
+        j.impulse[1] *= dtRatio;
+        float2 I = v2(j.impulse[0], j.impulse[1]);
+        vB += j.invMassB * I;
+        wB += j.invIB * cross(j.rB, I);
+    } else {
+        j.impulse[0] = 0.0f;
+        j.impulse[1] = 0.0f;
+    }
+    sb.set_v(lb, vB, wB);
+}
+
+__device__ __noinline__ void mouse_solve_velocity(const Ctx& x, DJoint& j, int lb, SB sb) {
+    float2 vB = sb.v(lb);
+    float wB = sb.w(lb);
+    float2 Cdot = vB + cross(wB, j.rB);
+    float2 I = v2(j.impulse[0], j.impulse[1]);
+    float2 rhs = -((Cdot + j.mouse_c) + j.gamma * I);
+    float2 impulse = v2(j.mass[0] * rhs.x + j.mass[3] * rhs.y, j.mass[1] * rhs.x + j.mass[4] * rhs.y);
+    float2 oldImpulse = I;
+    I += impulse;
+    float maxImpulse = x.dt * j.max_force;
+    if (I.x * I.x + I.y * I.y > maxImpulse * maxImpulse) I *= fdiv(maxImpulse, length(I));
+    j.impulse[0] = I.x;
+    j.impulse[1] = I.y;
+    impulse = I - oldImpulse;
+    vB += j.invMassB * impulse;
+    wB += j.invIB * cross(j.rB, impulse);
+    sb.set_v(lb, vB, wB);
+}
+
 // ------------------------------------------------------------ revolute joint (joints/b2revolutejoint.d:319-636)
 DG void joint_init(const Ctx& x, int ji, int b0, SB sb, bool warm, float dtRatio) {
     switch (x.jt[ji].type) {
@@ -1936,6 +2294,9 @@ DG void joint_init(const Ctx& x, int ji, int b0, SB sb, bool warm, float dtRatio
     case kFrictionJoint:
     case kMotorJoint: friction_motor_init(x, ji, b0, sb, warm, dtRatio); return;
     case kWheelJoint: wheel_init(x, ji, b0, sb, warm, dtRatio); return;
+    case kPrismaticJoint: prismatic_init(x, ji, b0, sb, warm, dtRatio); return;
+    case kPulleyJoint: pulley_init(x, ji, b0, sb, warm, dtRatio); return;
+    case kMouseJoint: mouse_init(x, ji, b0, sb, warm, dtRatio); return;
     default: break;
     }
     DJoint& j = x.jt[ji];
@@ -2013,6 +2374,9 @@ DG void joint_solve_velocity(const Ctx& x, int ji, int b0, SB sb) {
     if (j.type == kWeldJoint) { weld_solve_velocity(j, la, lb, sb); return; }
     if (j.type == kFrictionJoint || j.type == kMotorJoint) { friction_motor_solve_velocity(x, j, la, lb, sb); return; }
     if (j.type == kWheelJoint) { wheel_solve_velocity(x, j, la, lb, sb); return; }
+    if (j.type == kPrismaticJoint) { prismatic_solve_velocity(x, j, la, lb, sb); return; }
+    if (j.type == kPulleyJoint) { pulley_solve_velocity(j, la, lb, sb); return; }
+    if (j.type == kMouseJoint) { mouse_solve_velocity(x, j, lb, sb); return; }
     float2 vA = sb.v(la), vB = sb.v(lb);
     float wA = sb.w(la), wB = sb.w(lb);
     float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
@@ -2077,6 +2441,9 @@ DG bool joint_solve_position(const Ctx& x, int ji, int b0, SB sb) {
     if (j.type == kWeldJoint) return weld_solve_position(j, la, lb, sb);
     if (j.type == kFrictionJoint || j.type == kMotorJoint) return true;   // no position correction
     if (j.type == kWheelJoint) return wheel_solve_position(j, la, lb, sb);
+    if (j.type == kPrismaticJoint) return prismatic_solve_position(j, la, lb, sb);
+    if (j.type == kPulleyJoint) return pulley_solve_position(j, la, lb, sb);
+    if (j.type == kMouseJoint) return true;
     float2 cA = sb.c(la), cB = sb.c(lb);
     float aA = sb.a(la), aB = sb.a(lb);
     float angularError = 0.0f, positionError = 0.0f;

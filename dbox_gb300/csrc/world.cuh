@@ -69,10 +69,11 @@ struct BodyStatic {
 };
 
 enum { kRevoluteJoint = 0, kDistanceJoint = 1, kRopeJoint = 2, kWeldJoint = 3, kFrictionJoint = 4, kMotorJoint = 5,
-       kWheelJoint = 6 };
+       kWheelJoint = 6, kPrismaticJoint = 7, kPulleyJoint = 8, kMouseJoint = 9 };
 // b2RevoluteJoint / b2DistanceJoint / b2RopeJoint / b2WeldJoint / b2FrictionJoint / b2MotorJoint /
-// b2WheelJoint (joints/b2revolutejoint.d, b2distancejoint.d, b2ropejoint.d, b2weldjoint.d,
-// b2frictionjoint.d, b2motorjoint.d, b2wheeljoint.d)
+// b2WheelJoint / b2PrismaticJoint / b2PulleyJoint / b2MouseJoint (joints/b2revolutejoint.d,
+// b2distancejoint.d, b2ropejoint.d, b2weldjoint.d, b2frictionjoint.d, b2motorjoint.d,
+// b2wheeljoint.d, b2prismaticjoint.d, b2pulleyjoint.d, b2mousejoint.d)
 struct DJoint {
     int body_a, body_b;
     int collide_connected;
@@ -101,7 +102,15 @@ struct DJoint {
     // wheel: point-to-line impulse impulse[0] and mass mass[0], spring impulse impulse[1]
     float2 local_axis_x, local_axis_y, ax, ay;
     float sAx, sBx, sAy, sBy, spring_mass;
-    int pad3;
+    // prismatic: axes in local_axis_x / local_axis_y, impulse[0..2] (perpendicular, angular,
+    // limit), K in mass[9], motor as the revolute's fields with max_motor_force
+    float lower_translation, upper_translation, max_motor_force;
+    float s1, s2, a1, a2;
+    float2 axis, perp;
+    // pulley: impulse[0], mass[0]; mouse: impulse[0..1], mass matrix as friction's
+    float2 ground_a, ground_b, uA, uB, target, mouse_c;
+    float ratio, constant, beta;
+    int pad4;
 };
 
 // b2ContactVelocityConstraint (contacts/b2contactsolver.d:43-58) with body indices in place of island indices.

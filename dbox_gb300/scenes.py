@@ -37,7 +37,8 @@ def _empty():
         "joints": np.zeros(0, abi.REVOLUTE_DEF), "distance_joints": np.zeros(0, abi.DISTANCE_DEF),
         "rope_joints": np.zeros(0, abi.ROPE_DEF), "weld_joints": np.zeros(0, abi.WELD_DEF),
         "friction_joints": np.zeros(0, abi.FRICTION_DEF), "motor_joints": np.zeros(0, abi.MOTOR_DEF),
-        "wheel_joints": np.zeros(0, abi.WHEEL_DEF),
+        "wheel_joints": np.zeros(0, abi.WHEEL_DEF), "prismatic_joints": np.zeros(0, abi.PRISMATIC_DEF),
+        "pulley_joints": np.zeros(0, abi.PULLEY_DEF), "mouse_joints": np.zeros(0, abi.MOUSE_DEF),
         "gravity": (0.0, -10.0), "name": "",
     }
 
@@ -57,7 +58,9 @@ def _concat(parts):
         out["joints"] = np.concatenate([out["joints"], j])
         for key, dtype in (("distance_joints", abi.DISTANCE_DEF), ("rope_joints", abi.ROPE_DEF),
                            ("weld_joints", abi.WELD_DEF), ("friction_joints", abi.FRICTION_DEF),
-                           ("motor_joints", abi.MOTOR_DEF), ("wheel_joints", abi.WHEEL_DEF)):
+                           ("motor_joints", abi.MOTOR_DEF), ("wheel_joints", abi.WHEEL_DEF),
+                           ("prismatic_joints", abi.PRISMATIC_DEF), ("pulley_joints", abi.PULLEY_DEF),
+                           ("mouse_joints", abi.MOUSE_DEF)):
             d = p.get(key, np.zeros(0, dtype)).copy()
             d["body_a"] += nb
             d["body_b"] += nb
@@ -389,6 +392,87 @@ def cars(n_cars=3, x0=-20.0, spacing=8.0, bumps=12, seed=7):
         parts.append(part)
     out = _concat(parts)
     out["name"] = "cars"
+    return out
+
+
+def sliders(n=4, x0=-12.0, spacing=7.0, boxes=5):
+    """Prismatic joints (b2PrismaticJointDef, joints/b2prismaticjoint.d:30-158): platforms on
+    axes to the ground body, each loaded with a small stack of boxes.  Platform k: vertical
+    axis with a motor (k even: lifting at 1 m/s, max force 400) and translation limits
+    [-0.5, 3]; odd platforms slide on a tilted axis (30 degrees) with limits [-2, 2] and no
+    motor; the last platform has equal limits (locked) and a reference angle of 0.1 rad."""
+    parts = [ground_box()]
+    for k in range(n):
+        x = x0 + k * spacing
+        plat = _boxes([(x, 2.0)], 1.5, 0.2, abi.DYNAMIC, 0.6, 2.0)
+        load = _boxes([(x, 2.7 + 0.5 * i) for i in range(boxes)], 0.25, 0.25, abi.DYNAMIC, 0.6, 1.0)
+        parts.append(_concat([plat, load]))
+    out = _concat(parts)
+    pj = np.zeros(n, abi.PRISMATIC_DEF)
+    for k in range(n):
+        body = 1 + k * (boxes + 1)
+        x = x0 + k * spacing
+        pj[k]["body_a"] = 0
+        pj[k]["body_b"] = body
+        pj[k]["local_anchor_a"] = (x, 12.0)                       # (x, 2) in the world
+        if k % 2 == 0:
+            pj[k]["local_axis_a"] = (0.0, 2.0)                    # normalised on creation
+            pj[k]["enable_motor"] = 1
+            pj[k]["motor_speed"] = 1.0
+            pj[k]["max_motor_force"] = 400.0
+            pj[k]["enable_limit"] = 1
+            pj[k]["lower_translation"] = -0.5
+            pj[k]["upper_translation"] = 3.0
+        else:
+            pj[k]["local_axis_a"] = (0.8660254, 0.5)
+            pj[k]["enable_limit"] = 1
+            pj[k]["lower_translation"] = -2.0
+            pj[k]["upper_translation"] = 2.0
+        if k == n - 1:
+            pj[k]["enable_motor"] = 0
+            pj[k]["lower_translation"] = 0.5
+            pj[k]["upper_translation"] = 0.5
+            pj[k]["reference_angle"] = 0.1
+    out["prismatic_joints"] = pj
+    out["name"] = "sliders"
+    return out
+
+
+def pulleys(n=3, x0=-10.0, spacing=8.0):
+    """Pulley and mouse joints (b2PulleyJointDef joints/b2pulleyjoint.d:30-97, b2MouseJointDef
+    joints/b2mousejoint.d:28-58): pairs of boxes hanging from two ground anchors 10 m up, one
+    side heavier (ratio 1, 1.5 and 2 for the three pulleys), so the heavy side sinks onto the
+    ground; a mouse joint drags a box on the ground towards a target above it (max force 200,
+    5 Hz, damping 0.7)."""
+    parts = [ground_box()]
+    for k in range(n):
+        x = x0 + k * spacing
+        parts.append(_boxes([(x - 1.5, 5.0)], 0.5, 0.5, abi.DYNAMIC, 0.6, 1.0))
+        parts.append(_boxes([(x + 1.5, 5.0)], 0.5, 0.5, abi.DYNAMIC, 0.6, 1.5 + 0.5 * k))
+    parts.append(_boxes([(x0 + n * spacing, 0.5)], 0.4, 0.4, abi.DYNAMIC, 0.6, 1.0))
+    out = _concat(parts)
+    pj = np.zeros(n, abi.PULLEY_DEF)
+    for k in range(n):
+        x = x0 + k * spacing
+        pj[k]["body_a"] = 1 + 2 * k
+        pj[k]["body_b"] = 2 + 2 * k
+        pj[k]["ground_anchor_a"] = (x - 1.5, 10.0)
+        pj[k]["ground_anchor_b"] = (x + 1.5, 10.0)
+        pj[k]["local_anchor_a"] = (0.0, 0.5)
+        pj[k]["local_anchor_b"] = (0.0, 0.5)
+        pj[k]["length_a"] = 4.5
+        pj[k]["length_b"] = 4.5
+        pj[k]["ratio"] = 1.0 + 0.5 * k
+    mj = np.zeros(1, abi.MOUSE_DEF)
+    mj[0]["body_a"] = 0
+    mj[0]["body_b"] = 1 + 2 * n
+    mj[0]["target"] = (x0 + n * spacing + 0.2, 0.7)
+    mj[0]["max_force"] = 200.0
+    mj[0]["frequency_hz"] = 5.0
+    mj[0]["damping_ratio"] = 0.7
+    out["pulley_joints"] = pj
+    out["mouse_joints"] = mj
+    out["name"] = "pulleys"
     return out
 
 

@@ -154,6 +154,38 @@ typedef struct {
     float frequency_hz, damping_ratio;   /* suspension spring */
 } dbox_wheel_def;
 
+/* b2PrismaticJointDef (dynamics/joints/b2prismaticjoint.d:30-158) */
+typedef struct {
+    int32_t body_a, body_b;
+    int32_t collide_connected;
+    dbox_vec2 local_anchor_a, local_anchor_b;
+    dbox_vec2 local_axis_a;      /* translation axis in body A (normalised on creation) */
+    float reference_angle;
+    int32_t enable_limit;
+    float lower_translation, upper_translation;
+    int32_t enable_motor;
+    float max_motor_force, motor_speed;
+} dbox_prismatic_def;
+
+/* b2PulleyJointDef (dynamics/joints/b2pulleyjoint.d:30-97) */
+typedef struct {
+    int32_t body_a, body_b;
+    int32_t collide_connected;
+    dbox_vec2 ground_anchor_a, ground_anchor_b;   /* world points the two sides hang from */
+    dbox_vec2 local_anchor_a, local_anchor_b;
+    float length_a, length_b;                     /* reference lengths of the two sides */
+    float ratio;                                  /* lengthA + ratio * lengthB stays constant */
+} dbox_pulley_def;
+
+/* b2MouseJointDef (dynamics/joints/b2mousejoint.d:28-58): drags body_b's point under
+ * `target` towards the target; body_a only anchors the joint (usually the ground). */
+typedef struct {
+    int32_t body_a, body_b;
+    int32_t collide_connected;
+    dbox_vec2 target;
+    float max_force, frequency_hz, damping_ratio;
+} dbox_mouse_def;
+
 /* ------------------------------------------------------- world snapshot
  * Flat state records, used by dbox_world_export_state / import_state
  * (exact checkpoint/resume) and by the parity tests.  Flag words use the
@@ -274,6 +306,16 @@ int32_t dbox_joint_create_motor(dbox_world* w, int32_t world, const dbox_motor_d
 /* b2World.CreateJoint with a b2WheelJointDef (joints/b2wheeljoint.d); snapshot: impulse[0] the
  * point-to-line impulse, impulse[1] the spring impulse, motor_impulse. */
 int32_t dbox_joint_create_wheel(dbox_world* w, int32_t world, const dbox_wheel_def* def, int32_t* out_joint);
+/* b2World.CreateJoint with a b2PrismaticJointDef (joints/b2prismaticjoint.d); snapshot:
+ * impulse[0..2] (perpendicular, angular, limit), motor_impulse, limit_state. */
+int32_t dbox_joint_create_prismatic(dbox_world* w, int32_t world, const dbox_prismatic_def* def, int32_t* out_joint);
+/* b2World.CreateJoint with a b2PulleyJointDef / b2MouseJointDef (joints/b2pulleyjoint.d,
+ * b2mousejoint.d); snapshot: impulse[0] (pulley), impulse[0..1] (mouse).  The mouse joint's
+ * local anchor is the target in body B's frame at creation. */
+int32_t dbox_joint_create_pulley(dbox_world* w, int32_t world, const dbox_pulley_def* def, int32_t* out_joint);
+int32_t dbox_joint_create_mouse(dbox_world* w, int32_t world, const dbox_mouse_def* def, int32_t* out_joint);
+/* b2MouseJoint.SetTarget (b2mousejoint.d:83-91): wakes body B and moves the target. */
+int32_t dbox_joint_set_mouse_target(dbox_world* w, int32_t world, int32_t joint, dbox_vec2 target);
 
 /* Bulk creation of a whole scene into one world: n bodies, then m fixtures
  * (fixture_body[i] indexes the bodies created by this call), then k joints

@@ -50,6 +50,10 @@ def lib():
         L.orc_joint_create_friction.argtypes = [vp, vp]
         L.orc_joint_create_motor.argtypes = [vp, vp]
         L.orc_joint_create_wheel.argtypes = [vp, vp]
+        L.orc_joint_create_prismatic.argtypes = [vp, vp]
+        L.orc_joint_create_pulley.argtypes = [vp, vp]
+        L.orc_joint_create_mouse.argtypes = [vp, vp]
+        L.orc_joint_set_mouse_target.argtypes = [vp, i32, f32, f32]
         L.orc_world_set_flags.argtypes = [vp, i32, i32, i32, i32, i32]
         L.orc_world_step.argtypes = [vp, f32, i32, i32]
         L.orc_world_step_n.argtypes = [vp, f32, i32, i32, i32]
@@ -123,7 +127,10 @@ class OracleWorld:
                                ("weld_joints", abi.WELD_DEF, L.orc_joint_create_weld),
                                ("friction_joints", abi.FRICTION_DEF, L.orc_joint_create_friction),
                                ("motor_joints", abi.MOTOR_DEF, L.orc_joint_create_motor),
-                               ("wheel_joints", abi.WHEEL_DEF, L.orc_joint_create_wheel)):
+                               ("wheel_joints", abi.WHEEL_DEF, L.orc_joint_create_wheel),
+                               ("prismatic_joints", abi.PRISMATIC_DEF, L.orc_joint_create_prismatic),
+                               ("pulley_joints", abi.PULLEY_DEF, L.orc_joint_create_pulley),
+                               ("mouse_joints", abi.MOUSE_DEF, L.orc_joint_create_mouse)):
             for d in scene.get(key, ()):
                 dd = np.ascontiguousarray(np.array([d], dtype))
                 if fn(self.h, abi.ptr(dd)) < 0:
@@ -162,6 +169,11 @@ class OracleWorld:
 
     def last_islands(self):
         return lib().orc_world_last_islands(self.h)
+
+    def set_mouse_target(self, joint, target):
+        """b2MouseJoint.SetTarget (b2mousejoint.d:83-91)."""
+        if lib().orc_joint_set_mouse_target(self.h, joint, float(target[0]), float(target[1])) != 0:
+            raise ValueError("not a mouse joint")
 
     def export_state(self):
         L = lib()

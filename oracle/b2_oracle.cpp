@@ -1740,7 +1740,7 @@ struct TimeStep { f32 dt = 0, inv_dt = 0, dtRatio = 0; int velocityIterations = 
 struct SolverData { TimeStep step; Position* positions = nullptr; Velocity* velocities = nullptr; };
 
 enum { kRevoluteJoint = 0, kDistanceJoint = 1, kRopeJoint = 2, kWeldJoint = 3, kFrictionJoint = 4, kMotorJoint = 5,
-       kWheelJoint = 6 };
+       kWheelJoint = 6, kPrismaticJoint = 7, kPulleyJoint = 8, kMouseJoint = 9 };
 
 struct Joint {                                                          // joints/b2joint.d, b2revolutejoint.d, b2distancejoint.d
     int type = kRevoluteJoint;
@@ -1779,6 +1779,13 @@ struct Joint {                                                          // joint
     // wheel (point-to-line impulse impulse.x, spring impulse impulse.y, motorImpulse)
     Vec2 localXAxisA, localYAxisA, ax, ay;
     f32 sAx = 0, sBx = 0, sAy = 0, sBy = 0, wheelMass = 0, springMass = 0;
+    // prismatic (impulse: perpendicular, angular, limit; K in massM)
+    f32 lowerTranslation = 0, upperTranslation = 0, maxMotorForce = 0;
+    Vec2 axis, perp;
+    f32 s1 = 0, s2 = 0, a1 = 0, a2 = 0;
+    // pulley (impulse.x) and mouse (impulse.x/.y; mass matrix in linearMass)
+    Vec2 groundAnchorA, groundAnchorB, uA, uB, targetA, mouseC;
+    f32 ratio = 0, constant = 0, beta = 0;
 
     void InitVelocityConstraints(const SolverData& data) {
         switch (type) {
@@ -1788,6 +1795,9 @@ struct Joint {                                                          // joint
         case kFrictionJoint:
         case kMotorJoint: FrictionMotorInit(data); break;
         case kWheelJoint: WheelInit(data); break;
+        case kPrismaticJoint: PrismaticInit(data); break;
+        case kPulleyJoint: PulleyInit(data); break;
+        case kMouseJoint: MouseInit(data); break;
         default: RevoluteInit(data);
         }
     }
@@ -1799,6 +1809,9 @@ struct Joint {                                                          // joint
         case kFrictionJoint:
         case kMotorJoint: FrictionMotorSolveVelocity(data); break;
         case kWheelJoint: WheelSolveVelocity(data); break;
+        case kPrismaticJoint: PrismaticSolveVelocity(data); break;
+        case kPulleyJoint: PulleySolveVelocity(data); break;
+        case kMouseJoint: MouseSolveVelocity(data); break;
         default: RevoluteSolveVelocity(data);
         }
     }
@@ -1810,6 +1823,9 @@ struct Joint {                                                          // joint
         case kFrictionJoint:
         case kMotorJoint: return true;                                 // no position correction
         case kWheelJoint: return WheelSolvePosition(data);
+        case kPrismaticJoint: return PrismaticSolvePosition(data);
+        case kPulleyJoint: return PulleySolvePosition(data);
+        case kMouseJoint: return true;
         default: return RevoluteSolvePosition(data);
         }
     }
@@ -2158,6 +2174,372 @@ struct Joint {                                                          // joint
         data.positions[indexB].c = cB;
         data.positions[indexB].a = aB;
         return Abs(C) <= kLinearSlop;
+    }
+
+    void PrismaticInit(const SolverData& data) {                        // b2prismaticjoint.d:391-533
+        LoadBodies();
+        Vec2 cA = data.positions[indexA].c;
+        f32 aA = data.positions[indexA].a;
+        Vec2 vA = data.velocities[indexA].v;
+        f32 wA = data.velocities[indexA].w;
+        Vec2 cB = data.positions[indexB].c;
+        f32 aB = data.positions[indexB].a;
+        Vec2 vB = data.velocities[indexB].v;
+        f32 wB = data.velocities[indexB].w;
+        Rot qA(aA), qB(aB);
+        Vec2 rA_ = Mul(qA, localAnchorA - localCenterA);
+        Vec2 rB_ = Mul(qB, localAnchorB - localCenterB);
+        Vec2 d = ((cB - cA) + rB_) - rA_;
+        f32 mA = invMassA, mB = invMassB, iA = invIA, iB = invIB;
+        axis = Mul(qA, localXAxisA);                                    // motor Jacobian and effective mass
+        a1 = Cross(d + rA_, axis);
+        a2 = Cross(rB_, axis);
+        motorMass = ((mA + mB) + (iA * a1) * a1) + (iB * a2) * a2;
+        if (motorMass > 0.0f) motorMass = 1.0f / motorMass;
+        perp = Mul(qA, localYAxisA);                                    // prismatic constraint
+        s1 = Cross(d + rA_, perp);
+        s2 = Cross(rB_, perp);
+        f32 k11 = ((mA + mB) + (iA * s1) * s1) + (iB * s2) * s2;
+        f32 k12 = iA * s1 + iB * s2;
+        f32 k13 = (iA * s1) * a1 + (iB * s2) * a2;
+        f32 k22 = iA + iB;
+        if (k22 == 0.0f) k22 = 1.0f;                                    // fixed rotation
+        f32 k23 = iA * a1 + iB * a2;
+        f32 k33 = ((mA + mB) + (iA * a1) * a1) + (iB * a2) * a2;
+        massM.ex = Vec3(k11, k12, k13);
+        massM.ey = Vec3(k12, k22, k23);
+        massM.ez = Vec3(k13, k23, k33);
+        if (enableLimit) {                                              // limit state
+            f32 jointTranslation = Dot(axis, d);
+            if (Abs(upperTranslation - lowerTranslation) < 2.0f * kLinearSlop) {
+                limitState = kEqualLimits;
+            } else if (jointTranslation <= lowerTranslation) {
+                if (limitState != kAtLowerLimit) { limitState = kAtLowerLimit; impulse.z = 0.0f; }
+            } else if (jointTranslation >= upperTranslation) {
+                if (limitState != kAtUpperLimit) { limitState = kAtUpperLimit; impulse.z = 0.0f; }
+            } else {
+                limitState = kInactiveLimit;
+                impulse.z = 0.0f;
+            }
+        } else {
+            limitState = kInactiveLimit;
+            impulse.z = 0.0f;
+        }
+        if (!enableMotor) motorImpulse = 0.0f;
+        if (data.step.warmStarting) {
+            impulse *= data.step.dtRatio;
+            motorImpulse *= data.step.dtRatio;
+            Vec2 P = impulse.x * perp + (motorImpulse + impulse.z) * axis;
+            f32 LA = (impulse.x * s1 + impulse.y) + (motorImpulse + impulse.z) * a1;
+            f32 LB = (impulse.x * s2 + impulse.y) + (motorImpulse + impulse.z) * a2;
+            vA -= mA * P;
+            wA -= iA * LA;
+            vB += mB * P;
+            wB += iB * LB;
+        } else {
+            impulse.SetZero();
+            motorImpulse = 0.0f;
+        }
+        data.velocities[indexA].v = vA;
+        data.velocities[indexA].w = wA;
+        data.velocities[indexB].v = vB;
+        data.velocities[indexB].w = wB;
+    }
+
+    void PrismaticSolveVelocity(const SolverData& data) {               // b2prismaticjoint.d:535-630
+        Vec2 vA = data.velocities[indexA].v;
+        f32 wA = data.velocities[indexA].w;
+        Vec2 vB = data.velocities[indexB].v;
+        f32 wB = data.velocities[indexB].w;
+        f32 mA = invMassA, mB = invMassB, iA = invIA, iB = invIB;
+        if (enableMotor && limitState != kEqualLimits) {                // motor
+            f32 Cdot = (Dot(axis, vB - vA) + a2 * wB) - a1 * wA;
+            f32 imp = motorMass * (motorSpeed - Cdot);
+            f32 oldImpulse = motorImpulse;
+            f32 maxImpulse = data.step.dt * maxMotorForce;
+            motorImpulse = Clamp(motorImpulse + imp, -maxImpulse, maxImpulse);
+            imp = motorImpulse - oldImpulse;
+            Vec2 P = imp * axis;
+            f32 LA = imp * a1, LB = imp * a2;
+            vA -= mA * P;
+            wA -= iA * LA;
+            vB += mB * P;
+            wB += iB * LB;
+        }
+        Vec2 Cdot1;
+        Cdot1.x = (Dot(perp, vB - vA) + s2 * wB) - s1 * wA;
+        Cdot1.y = wB - wA;
+        if (enableLimit && limitState != kInactiveLimit) {              // prismatic and limit together
+            f32 Cdot2 = (Dot(axis, vB - vA) + a2 * wB) - a1 * wA;
+            Vec3 Cdot(Cdot1.x, Cdot1.y, Cdot2);
+            Vec3 f1 = impulse;
+            Vec3 df = massM.Solve33(-Cdot);
+            impulse += df;
+            if (limitState == kAtLowerLimit) impulse.z = Max(impulse.z, 0.0f);
+            else if (limitState == kAtUpperLimit) impulse.z = Min(impulse.z, 0.0f);
+            // f2(1:2) = invK(1:2,1:2) * (-Cdot(1:2) - K(1:2,3) * (f2(3) - f1(3))) + f1(1:2)
+            Vec2 b = -Cdot1 - (impulse.z - f1.z) * Vec2(massM.ez.x, massM.ez.y);
+            Vec2 f2r = massM.Solve22(b) + Vec2(f1.x, f1.y);
+            impulse.x = f2r.x;
+            impulse.y = f2r.y;
+            df = Vec3(impulse.x - f1.x, impulse.y - f1.y, impulse.z - f1.z);
+            Vec2 P = df.x * perp + df.z * axis;
+            f32 LA = (df.x * s1 + df.y) + df.z * a1;
+            f32 LB = (df.x * s2 + df.y) + df.z * a2;
+            vA -= mA * P;
+            wA -= iA * LA;
+            vB += mB * P;
+            wB += iB * LB;
+        } else {                                                        // prismatic only
+            Vec2 df = massM.Solve22(-Cdot1);
+            impulse.x += df.x;
+            impulse.y += df.y;
+            Vec2 P = df.x * perp;
+            f32 LA = df.x * s1 + df.y;
+            f32 LB = df.x * s2 + df.y;
+            vA -= mA * P;
+            wA -= iA * LA;
+            vB += mB * P;
+            wB += iB * LB;
+        }
+        data.velocities[indexA].v = vA;
+        data.velocities[indexA].w = wA;
+        data.velocities[indexB].v = vB;
+        data.velocities[indexB].w = wB;
+    }
+
+    bool PrismaticSolvePosition(const SolverData& data) {               // b2prismaticjoint.d:632-757
+        Vec2 cA = data.positions[indexA].c;
+        f32 aA = data.positions[indexA].a;
+        Vec2 cB = data.positions[indexB].c;
+        f32 aB = data.positions[indexB].a;
+        Rot qA(aA), qB(aB);
+        f32 mA = invMassA, mB = invMassB, iA = invIA, iB = invIB;
+        Vec2 rA_ = Mul(qA, localAnchorA - localCenterA);
+        Vec2 rB_ = Mul(qB, localAnchorB - localCenterB);
+        Vec2 d = ((cB + rB_) - cA) - rA_;
+        Vec2 axis_ = Mul(qA, localXAxisA);
+        f32 a1_ = Cross(d + rA_, axis_);
+        f32 a2_ = Cross(rB_, axis_);
+        Vec2 perp_ = Mul(qA, localYAxisA);
+        f32 s1_ = Cross(d + rA_, perp_);
+        f32 s2_ = Cross(rB_, perp_);
+        Vec3 imp;
+        Vec2 C1;
+        C1.x = Dot(perp_, d);
+        C1.y = (aB - aA) - referenceAngle;
+        f32 linearError = Abs(C1.x);
+        f32 angularError = Abs(C1.y);
+        bool active = false;
+        f32 C2 = 0.0f;
+        if (enableLimit) {
+            f32 translation = Dot(axis_, d);
+            if (Abs(upperTranslation - lowerTranslation) < 2.0f * kLinearSlop) {
+                C2 = Clamp(translation, -kMaxLinearCorrection, kMaxLinearCorrection);
+                linearError = Max(linearError, Abs(translation));
+                active = true;
+            } else if (translation <= lowerTranslation) {
+                C2 = Clamp((translation - lowerTranslation) + kLinearSlop, -kMaxLinearCorrection, 0.0f);
+                linearError = Max(linearError, lowerTranslation - translation);
+                active = true;
+            } else if (translation >= upperTranslation) {
+                C2 = Clamp((translation - upperTranslation) - kLinearSlop, 0.0f, kMaxLinearCorrection);
+                linearError = Max(linearError, translation - upperTranslation);
+                active = true;
+            }
+        }
+        if (active) {
+            f32 k11 = ((mA + mB) + (iA * s1_) * s1_) + (iB * s2_) * s2_;
+            f32 k12 = iA * s1_ + iB * s2_;
+            f32 k13 = (iA * s1_) * a1_ + (iB * s2_) * a2_;
+            f32 k22 = iA + iB;
+            if (k22 == 0.0f) k22 = 1.0f;
+            f32 k23 = iA * a1_ + iB * a2_;
+            f32 k33 = ((mA + mB) + (iA * a1_) * a1_) + (iB * a2_) * a2_;
+            Mat33 K;
+            K.ex = Vec3(k11, k12, k13);
+            K.ey = Vec3(k12, k22, k23);
+            K.ez = Vec3(k13, k23, k33);
+            imp = K.Solve33(-Vec3(C1.x, C1.y, C2));
+        } else {
+            f32 k11 = ((mA + mB) + (iA * s1_) * s1_) + (iB * s2_) * s2_;
+            f32 k12 = iA * s1_ + iB * s2_;
+            f32 k22 = iA + iB;
+            if (k22 == 0.0f) k22 = 1.0f;
+            Mat33 K;
+            K.ex = Vec3(k11, k12, 0.0f);
+            K.ey = Vec3(k12, k22, 0.0f);
+            Vec2 impulse1 = K.Solve22(-C1);                             // b2Mat22.Solve: the same 2x2 solve
+            imp = Vec3(impulse1.x, impulse1.y, 0.0f);
+        }
+        Vec2 P = imp.x * perp_ + imp.z * axis_;
+        f32 LA = (imp.x * s1_ + imp.y) + imp.z * a1_;
+        f32 LB = (imp.x * s2_ + imp.y) + imp.z * a2_;
+        cA -= mA * P;
+        aA -= iA * LA;
+        cB += mB * P;
+        aB += iB * LB;
+        data.positions[indexA].c = cA;
+        data.positions[indexA].a = aA;
+        data.positions[indexB].c = cB;
+        data.positions[indexB].a = aB;
+        return linearError <= kLinearSlop && angularError <= kAngularSlop;
+    }
+
+    void PulleyInit(const SolverData& data) {                           // b2pulleyjoint.d:181-262
+        LoadBodies();
+        Vec2 cA = data.positions[indexA].c;
+        f32 aA = data.positions[indexA].a;
+        Vec2 vA = data.velocities[indexA].v;
+        f32 wA = data.velocities[indexA].w;
+        Vec2 cB = data.positions[indexB].c;
+        f32 aB = data.positions[indexB].a;
+        Vec2 vB = data.velocities[indexB].v;
+        f32 wB = data.velocities[indexB].w;
+        Rot qA(aA), qB(aB);
+        rA = Mul(qA, localAnchorA - localCenterA);
+        rB = Mul(qB, localAnchorB - localCenterB);
+        uA = (cA + rA) - groundAnchorA;                                 // the pulley axes
+        uB = (cB + rB) - groundAnchorB;
+        f32 lengthA = uA.Length(), lengthB = uB.Length();
+        if (lengthA > 10.0f * kLinearSlop) uA *= 1.0f / lengthA; else uA.SetZero();
+        if (lengthB > 10.0f * kLinearSlop) uB *= 1.0f / lengthB; else uB.SetZero();
+        f32 ruA = Cross(rA, uA), ruB = Cross(rB, uB);
+        f32 mA = invMassA + (invIA * ruA) * ruA;
+        f32 mB = invMassB + (invIB * ruB) * ruB;
+        distMass = mA + (ratio * ratio) * mB;
+        if (distMass > 0.0f) distMass = 1.0f / distMass;
+        if (data.step.warmStarting) {
+            impulse.x *= data.step.dtRatio;
+            Vec2 PA = (-impulse.x) * uA;
+            Vec2 PB = ((-ratio) * impulse.x) * uB;
+            vA += invMassA * PA;
+            wA += invIA * Cross(rA, PA);
+            vB += invMassB * PB;
+            wB += invIB * Cross(rB, PB);
+        } else {
+            impulse.x = 0.0f;
+        }
+        data.velocities[indexA].v = vA;
+        data.velocities[indexA].w = wA;
+        data.velocities[indexB].v = vB;
+        data.velocities[indexB].w = wB;
+    }
+
+    void PulleySolveVelocity(const SolverData& data) {                  // b2pulleyjoint.d:264-289
+        Vec2 vA = data.velocities[indexA].v;
+        f32 wA = data.velocities[indexA].w;
+        Vec2 vB = data.velocities[indexB].v;
+        f32 wB = data.velocities[indexB].w;
+        Vec2 vpA = vA + Cross(wA, rA);
+        Vec2 vpB = vB + Cross(wB, rB);
+        f32 Cdot = (-Dot(uA, vpA)) - ratio * Dot(uB, vpB);
+        f32 imp = -distMass * Cdot;
+        impulse.x += imp;
+        Vec2 PA = (-imp) * uA;
+        Vec2 PB = ((-ratio) * imp) * uB;
+        vA += invMassA * PA;
+        wA += invIA * Cross(rA, PA);
+        vB += invMassB * PB;
+        wB += invIB * Cross(rB, PB);
+        data.velocities[indexA].v = vA;
+        data.velocities[indexA].w = wA;
+        data.velocities[indexB].v = vB;
+        data.velocities[indexB].w = wB;
+    }
+
+    bool PulleySolvePosition(const SolverData& data) {                  // b2pulleyjoint.d:291-350
+        Vec2 cA = data.positions[indexA].c;
+        f32 aA = data.positions[indexA].a;
+        Vec2 cB = data.positions[indexB].c;
+        f32 aB = data.positions[indexB].a;
+        Rot qA(aA), qB(aB);
+        Vec2 rA_ = Mul(qA, localAnchorA - localCenterA);
+        Vec2 rB_ = Mul(qB, localAnchorB - localCenterB);
+        Vec2 uA_ = (cA + rA_) - groundAnchorA;
+        Vec2 uB_ = (cB + rB_) - groundAnchorB;
+        f32 lengthA = uA_.Length(), lengthB = uB_.Length();
+        if (lengthA > 10.0f * kLinearSlop) uA_ *= 1.0f / lengthA; else uA_.SetZero();
+        if (lengthB > 10.0f * kLinearSlop) uB_ *= 1.0f / lengthB; else uB_.SetZero();
+        f32 ruA = Cross(rA_, uA_), ruB = Cross(rB_, uB_);
+        f32 mA = invMassA + (invIA * ruA) * ruA;
+        f32 mB = invMassB + (invIB * ruB) * ruB;
+        f32 mass = mA + (ratio * ratio) * mB;
+        if (mass > 0.0f) mass = 1.0f / mass;
+        f32 C = (constant - lengthA) - ratio * lengthB;
+        f32 linearError = Abs(C);
+        f32 imp = -mass * C;
+        Vec2 PA = (-imp) * uA_;
+        Vec2 PB = ((-ratio) * imp) * uB_;
+        cA += invMassA * PA;
+        aA += invIA * Cross(rA_, PA);
+        cB += invMassB * PB;
+        aB += invIB * Cross(rB_, PB);
+        data.positions[indexA].c = cA;
+        data.positions[indexA].a = aA;
+        data.positions[indexB].c = cB;
+        data.positions[indexB].a = aB;
+        return linearError < kLinearSlop;
+    }
+
+    void MouseInit(const SolverData& data) {                            // b2mousejoint.d:132-192 (body B only)
+        indexB = bodyB->islandIndex;
+        localCenterB = bodyB->sweep.localCenter;
+        invMassB = bodyB->invMass;
+        invIB = bodyB->invI;
+        Vec2 cB = data.positions[indexB].c;
+        f32 aB = data.positions[indexB].a;
+        Vec2 vB = data.velocities[indexB].v;
+        f32 wB = data.velocities[indexB].w;
+        Rot qB(aB);
+        f32 mass = bodyB->mass;
+        f32 omega = (2.0f * kPi) * frequencyHz;                         // frequency
+        f32 d = ((2.0f * mass) * dampingRatio) * omega;                 // damping coefficient
+        f32 k = mass * (omega * omega);                                 // spring stiffness
+        f32 h = data.step.dt;
+        gamma = h * (d + h * k);
+        if (gamma != 0.0f) gamma = 1.0f / gamma;
+        beta = (h * k) * gamma;
+        rB = Mul(qB, localAnchorB - localCenterB);
+        Mat22 K;
+        K.ex.x = (invMassB + (invIB * rB.y) * rB.y) + gamma;
+        K.ex.y = ((-invIB) * rB.x) * rB.y;
+        K.ey.x = K.ex.y;
+        K.ey.y = (invMassB + (invIB * rB.x) * rB.x) + gamma;
+        linearMass = K.GetInverse();
+        mouseC = (cB + rB) - targetA;
+        mouseC *= beta;
+        wB *= 0.98f;                                                    // cheat with some damping
+        if (data.step.warmStarting) {
+            impulse.x *= data.step.dtRatio;
+            impulse.y *= data.step.dtRatio;
+            Vec2 I(impulse.x, impulse.y);
+            vB += invMassB * I;
+            wB += invIB * Cross(rB, I);
+        } else {
+            impulse.SetZero();
+        }
+        data.velocities[indexB].v = vB;
+        data.velocities[indexB].w = wB;
+    }
+
+    void MouseSolveVelocity(const SolverData& data) {                   // b2mousejoint.d:194-220
+        Vec2 vB = data.velocities[indexB].v;
+        f32 wB = data.velocities[indexB].w;
+        Vec2 Cdot = vB + Cross(wB, rB);
+        Vec2 I(impulse.x, impulse.y);
+        Vec2 imp = Mul(linearMass, -((Cdot + mouseC) + gamma * I));
+        Vec2 oldImpulse = I;
+        I += imp;
+        f32 maxImpulse = data.step.dt * maxForce;
+        if (I.LengthSquared() > maxImpulse * maxImpulse) I *= maxImpulse / I.Length();
+        impulse.x = I.x;
+        impulse.y = I.y;
+        imp = I - oldImpulse;
+        vB += invMassB * imp;
+        wB += invIB * Cross(rB, imp);
+        data.velocities[indexB].v = vB;
+        data.velocities[indexB].w = wB;
     }
 
     // the weld joint's K (b2weldjoint.d:229-238 and 387-396)
@@ -3663,6 +4045,66 @@ struct World {                                                          // dynam
         return LinkJoint(j);
     }
 
+    Joint* CreatePrismatic(const dbox_prismatic_def* def) {             // b2prismaticjoint.d:163-187
+        Joint* j = new Joint();
+        j->type = kPrismaticJoint;
+        j->bodyA = bodiesByIndex[def->body_a];
+        j->bodyB = bodiesByIndex[def->body_b];
+        j->collideConnected = def->collide_connected != 0;
+        j->localAnchorA = Vec2(def->local_anchor_a.x, def->local_anchor_a.y);
+        j->localAnchorB = Vec2(def->local_anchor_b.x, def->local_anchor_b.y);
+        j->localXAxisA = Vec2(def->local_axis_a.x, def->local_axis_a.y);
+        j->localXAxisA.Normalize();
+        j->localYAxisA = Cross(1.0f, j->localXAxisA);
+        j->referenceAngle = def->reference_angle;
+        j->impulse.SetZero();
+        j->motorMass = 0.0f;
+        j->motorImpulse = 0.0f;
+        j->lowerTranslation = def->lower_translation;
+        j->upperTranslation = def->upper_translation;
+        j->maxMotorForce = def->max_motor_force;
+        j->motorSpeed = def->motor_speed;
+        j->enableLimit = def->enable_limit != 0;
+        j->enableMotor = def->enable_motor != 0;
+        j->limitState = kInactiveLimit;
+        j->axis.SetZero();
+        j->perp.SetZero();
+        return LinkJoint(j);
+    }
+
+    Joint* CreatePulley(const dbox_pulley_def* def) {                   // b2pulleyjoint.d:116-131
+        Joint* j = new Joint();
+        j->type = kPulleyJoint;
+        j->bodyA = bodiesByIndex[def->body_a];
+        j->bodyB = bodiesByIndex[def->body_b];
+        j->collideConnected = def->collide_connected != 0;
+        j->groundAnchorA = Vec2(def->ground_anchor_a.x, def->ground_anchor_a.y);
+        j->groundAnchorB = Vec2(def->ground_anchor_b.x, def->ground_anchor_b.y);
+        j->localAnchorA = Vec2(def->local_anchor_a.x, def->local_anchor_a.y);
+        j->localAnchorB = Vec2(def->local_anchor_b.x, def->local_anchor_b.y);
+        j->ratio = def->ratio;
+        j->constant = def->length_a + def->ratio * def->length_b;
+        j->impulse.SetZero();
+        return LinkJoint(j);
+    }
+
+    Joint* CreateMouse(const dbox_mouse_def* def) {                     // b2mousejoint.d:112-129
+        Joint* j = new Joint();
+        j->type = kMouseJoint;
+        j->bodyA = bodiesByIndex[def->body_a];
+        j->bodyB = bodiesByIndex[def->body_b];
+        j->collideConnected = def->collide_connected != 0;
+        j->targetA = Vec2(def->target.x, def->target.y);
+        j->localAnchorB = MulT(j->bodyB->xf, j->targetA);
+        j->maxForce = def->max_force;
+        j->impulse.SetZero();
+        j->frequencyHz = def->frequency_hz;
+        j->dampingRatio = def->damping_ratio;
+        j->beta = 0.0f;
+        j->gamma = 0.0f;
+        return LinkJoint(j);
+    }
+
     Joint* CreateRevolute(const dbox_revolute_def* def) {               // b2world.d:196-261
         Joint* j = new Joint();
         j->bodyA = bodiesByIndex[def->body_a];
@@ -4114,6 +4556,33 @@ int orc_joint_create_wheel(orc_world* w, const dbox_wheel_def* def) {
     int n = (int)w->w.bodiesByIndex.size();
     if (def->body_a < 0 || def->body_a >= n || def->body_b < 0 || def->body_b >= n || def->body_a == def->body_b) return -1;
     return w->w.CreateWheel(def)->index;
+}
+
+int orc_joint_create_prismatic(orc_world* w, const dbox_prismatic_def* def) {
+    int n = (int)w->w.bodiesByIndex.size();
+    if (def->body_a < 0 || def->body_a >= n || def->body_b < 0 || def->body_b >= n || def->body_a == def->body_b) return -1;
+    return w->w.CreatePrismatic(def)->index;
+}
+
+int orc_joint_create_pulley(orc_world* w, const dbox_pulley_def* def) {
+    int n = (int)w->w.bodiesByIndex.size();
+    if (def->body_a < 0 || def->body_a >= n || def->body_b < 0 || def->body_b >= n || def->body_a == def->body_b) return -1;
+    return w->w.CreatePulley(def)->index;
+}
+
+int orc_joint_create_mouse(orc_world* w, const dbox_mouse_def* def) {
+    int n = (int)w->w.bodiesByIndex.size();
+    if (def->body_a < 0 || def->body_a >= n || def->body_b < 0 || def->body_b >= n || def->body_a == def->body_b) return -1;
+    return w->w.CreateMouse(def)->index;
+}
+
+int orc_joint_set_mouse_target(orc_world* w, int joint, float x, float y) {   // b2mousejoint.d:83-91
+    if (joint < 0 || joint >= (int)w->w.jointsByIndex.size()) return -1;
+    Joint* j = w->w.jointsByIndex[joint];
+    if (j->type != kMouseJoint) return -1;
+    if (!j->bodyB->IsAwake()) j->bodyB->SetAwake(true);
+    j->targetA = Vec2(x, y);
+    return 0;
 }
 
 int orc_scene_create(orc_world* w, int n_bodies, const dbox_body_def* bodies, int n_fixtures,

@@ -41,6 +41,10 @@ int orc_joint_create_weld(orc_world* w, const dbox_weld_def* def);
 int orc_joint_create_friction(orc_world* w, const dbox_friction_def* def);
 int orc_joint_create_motor(orc_world* w, const dbox_motor_def* def);
 int orc_joint_create_wheel(orc_world* w, const dbox_wheel_def* def);
+int orc_joint_create_prismatic(orc_world* w, const dbox_prismatic_def* def);
+int orc_joint_create_pulley(orc_world* w, const dbox_pulley_def* def);
+int orc_joint_create_mouse(orc_world* w, const dbox_mouse_def* def);
+int orc_joint_set_mouse_target(orc_world* w, int joint, float x, float y);
 int orc_scene_create(orc_world* w, int n_bodies, const dbox_body_def* bodies, int n_fixtures,
                      const int* fixture_body, const dbox_shape_def* shapes, const dbox_fixture_def* fixtures,
                      int n_joints, const dbox_revolute_def* joints);

@@ -253,3 +253,46 @@ def test_wheel_joint_cars_exact(oracle_lib, gpu_lib):
             for i, ow in enumerate(ows):
                 d = exact_diff(ow.export_state(), gw.export_state(i))
                 assert not d, "world %d step %d: %s" % (i, t + 1, d[:6])
+
+
+def test_prismatic_joints_exact(oracle_lib, gpu_lib):
+    # prismatic platforms with motors, limits (lower, upper, equal) and a reference angle,
+    # batched with wheels and welds: bit-exact against the oracle
+    from dbox_gb300 import scenes
+    oracle_lib.set_trig_mode(1)
+    worlds = [scenes.sliders(), scenes.sliders(n=3, boxes=3), scenes.cars(n_cars=1),
+              scenes.welded(n_beams=1, links=3, pile=False)]
+    gw = gpu_lib.World(worlds)
+    ows = [oracle_lib.OracleWorld(s) for s in worlds]
+    for t in range(180):
+        gw.step()
+        for ow in ows:
+            ow.step()
+        if t % 30 == 29:
+            for i, ow in enumerate(ows):
+                d = exact_diff(ow.export_state(), gw.export_state(i))
+                assert not d, "world %d step %d: %s" % (i, t + 1, d[:6])
+
+
+def test_pulley_and_mouse_joints_exact(oracle_lib, gpu_lib):
+    # pulleys of three ratios and a mouse joint whose target moves twice (SetTarget wakes the
+    # body), batched with prismatic sliders: bit-exact against the oracle
+    from dbox_gb300 import scenes
+    oracle_lib.set_trig_mode(1)
+    worlds = [scenes.pulleys(), scenes.pulleys(n=2, x0=-4.0), scenes.sliders(n=2, boxes=2)]
+    gw = gpu_lib.World(worlds)
+    ows = [oracle_lib.OracleWorld(s) for s in worlds]
+    targets = {60: (6.0, 4.0), 120: (-2.0, 1.5)}
+    for t in range(180):
+        if t in targets:
+            for i in (0, 1):
+                mj = len(worlds[i]["pulley_joints"])          # the mouse joint comes after the pulleys
+                gw.set_mouse_target(i, mj, targets[t])
+                ows[i].set_mouse_target(mj, targets[t])
+        gw.step()
+        for ow in ows:
+            ow.step()
+        if t % 30 == 29:
+            for i, ow in enumerate(ows):
+                d = exact_diff(ow.export_state(), gw.export_state(i))
+                assert not d, "world %d step %d: %s" % (i, t + 1, d[:6])

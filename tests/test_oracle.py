@@ -268,3 +268,39 @@ def test_wheel_joint_cars_drive(oracle_lib):
             dx, dy = b["xf"][wheel, 0] - cx, b["xf"][wheel, 1] - cy
             assert abs(cs * dx + sn * dy - ax) < 0.01
     assert st["joints"]["motor_impulse"][0] != 0
+
+
+def test_prismatic_sliders(oracle_lib):
+    # b2PrismaticJoint: motor-lifted platforms stop at their upper limit, the tilted slider
+    # rests at its lower limit, the locked one holds its reference angle
+    from dbox_gb300 import scenes
+    oracle_lib.set_trig_mode(1)
+    s = scenes.sliders()
+    ow = oracle_lib.OracleWorld(s)
+    ow.step(steps=240)
+    st = ow.export_state()
+    b, jt = st["bodies"], st["joints"]
+    assert abs(b["xf"][1, 1] - 5.0) < 0.02 and jt["limit_state"][0] == 2 and jt["motor_impulse"][0] > 0
+    assert jt["limit_state"][1] == 1
+    assert abs(b["sweep"][1 + 3 * 6, 7] - 0.1) < 0.01 and jt["limit_state"][3] == 3
+
+
+def test_pulley_and_mouse_joints(oracle_lib):
+    # b2PulleyJoint keeps lengthA + ratio * lengthB at its constant (within the position
+    # tolerance) while the heavier side sinks; b2MouseJoint drags its body to a moved target
+    from dbox_gb300 import scenes
+    oracle_lib.set_trig_mode(1)
+    s = scenes.pulleys(n=2)
+    ow = oracle_lib.OracleWorld(s)
+    ow.step(steps=150)
+    ow.set_mouse_target(2, (4.0, 3.0))
+    ow.step(steps=150)
+    b = ow.export_state()["bodies"]
+    for p in s["pulley_joints"]:
+        ya, yb = b["xf"][p["body_a"], 1] + 0.5, b["xf"][p["body_b"], 1] + 0.5
+        la = np.hypot(b["xf"][p["body_a"], 0] - p["ground_anchor_a"][0], 10.0 - ya)
+        lb = np.hypot(b["xf"][p["body_b"], 0] - p["ground_anchor_b"][0], 10.0 - yb)
+        assert abs(la + p["ratio"] * lb - (p["length_a"] + p["ratio"] * p["length_b"])) < 0.05
+    assert b["xf"][2, 1] < b["xf"][1, 1]                      # the heavier side went down
+    m = s["mouse_joints"][0]["body_b"]
+    assert np.hypot(b["xf"][m, 0] - 4.0, b["xf"][m, 1] - 3.0) < 0.6      # centre; the anchor is 0.28 m off it
