@@ -130,7 +130,7 @@ PROFILE = np.dtype([(n, "<f4") for n in (
     "step", "collide", "solve", "solve_init", "solve_velocity", "solve_position", "broadphase", "solve_toi")])
 
 STATIC, KINEMATIC, DYNAMIC = 0, 1, 2
-SHAPE_CIRCLE, SHAPE_POLYGON, SHAPE_BOX, SHAPE_ORIENTED_BOX = 0, 1, 2, 3
+SHAPE_CIRCLE, SHAPE_POLYGON, SHAPE_BOX, SHAPE_ORIENTED_BOX, SHAPE_EDGE = 0, 1, 2, 3, 4
 
 # b2Body / b2Contact flag bits (dynamics/b2body.d:1118-1127, contacts/b2contact.d:242-261)
 BODY_ISLAND, BODY_AWAKE, BODY_AUTOSLEEP, BODY_BULLET, BODY_FIXED_ROTATION, BODY_ACTIVE = 1, 2, 4, 8, 0x10, 0x20

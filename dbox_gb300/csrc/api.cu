@@ -712,7 +712,11 @@ void reset_mass(HostWorld& hw, int b) {
         if (fx.density == 0.0f) continue;
         hg::Mass md;
         if (fx.type == dg::kShapeCircle) md = hg::circle_mass(hg::mk(fx.v[0].x, fx.v[0].y), fx.radius, fx.density);
-        else {
+        else if (fx.type == dg::kShapeEdge) {                           // b2EdgeShape.ComputeMass: no mass
+            md.mass = 0.0f;
+            md.center = hg::scl(0.5f, hg::add(hg::mk(fx.v[0].x, fx.v[0].y), hg::mk(fx.v[1].x, fx.v[1].y)));
+            md.I = 0.0f;
+        } else {
             hg::Poly p;
             p.count = fx.count;
             for (int i = 0; i < fx.count; ++i) { p.v[i] = hg::mk(fx.v[i].x, fx.v[i].y); }
@@ -780,8 +784,19 @@ bool build_fixture(const dbox_shape_def* sd, dg::DFixture* f) {
             f->v[i] = make_float2(p.v[i].x, p.v[i].y);
             f->n[i] = make_float2(p.n[i].x, p.n[i].y);
         }
+        f->centroid = make_float2(p.centroid.x, p.centroid.y);
         return true;
     }
+    case DBOX_SHAPE_EDGE:                                               // b2EdgeShape.Set + ghost vertices (b2edgeshape.d)
+        f->type = dg::kShapeEdge;
+        f->count = 2;
+        f->radius = 2.0f * 0.005f;                                      // b2_polygonRadius
+        f->v[0] = make_float2(sd->vertices[0].x, sd->vertices[0].y);
+        f->v[1] = make_float2(sd->vertices[1].x, sd->vertices[1].y);
+        f->edge_flags = sd->count & 3;
+        f->v[2] = (sd->count & 1) ? make_float2(sd->vertices[2].x, sd->vertices[2].y) : make_float2(0.0f, 0.0f);
+        f->v[3] = (sd->count & 2) ? make_float2(sd->vertices[3].x, sd->vertices[3].y) : make_float2(0.0f, 0.0f);
+        return true;
     default:
         return false;
     }

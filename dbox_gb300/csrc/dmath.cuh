@@ -44,7 +44,7 @@ constexpr float kLinearSleepTolerance = 0.01f;
 constexpr float kAngularSleepTolerance = (2.0f / 180.0f * kPi);
 
 enum { kStaticBody = 0, kKinematicBody = 1, kDynamicBody = 2 };
-enum { kShapeCircle = 0, kShapePolygon = 2 };
+enum { kShapeCircle = 0, kShapeEdge = 1, kShapePolygon = 2 };
 enum { kBodyIsland = 0x1, kBodyAwake = 0x2, kBodyAutoSleep = 0x4, kBodyBullet = 0x8, kBodyFixedRotation = 0x10,
        kBodyActive = 0x20 };
 enum { kContactIsland = 0x1, kContactTouching = 0x2, kContactEnabled = 0x4, kContactFilter = 0x8,
@@ -129,19 +129,23 @@ DG void sweep_normalize(Sweep& s) {
 }
 
 // ------------------------------------------------------------ shapes
-// Device fixture record: shape + material + filter.  For a circle, v[0] is m_p.
+// Device fixture record: shape + material + filter.  For a circle, v[0] is m_p; for an edge,
+// v[0], v[1] are m_vertex1, m_vertex2 (count 2) and v[2], v[3] the ghost vertices m_vertex0,
+// m_vertex3 when edge_flags has bit 0 (hasVertex0) / bit 1 (hasVertex3).
 struct DFixture {
     int body;          // global body index
-    int type;          // kShapeCircle / kShapePolygon
-    int count;         // polygon vertex count (1 for a circle)
+    int type;          // kShapeCircle / kShapeEdge / kShapePolygon
+    int count;         // polygon vertex count (1 for a circle, 2 for an edge)
     float radius;
     float friction, restitution, density;
     int sensor;
     uint32_t filter;   // categoryBits | maskBits << 16
     int group;         // groupIndex
-    int pad0, pad1;
+    float2 centroid;   // polygon centroid (b2polygonshape.d:561-565)
     float2 v[8];
     float2 n[8];
+    int edge_flags;
+    int pad0;
 };
 
 struct AABB { float2 lo, hi; };
@@ -426,11 +430,234 @@ DG void collide_polygon_circle(Manifold& m, const DFixture& polygonA, const Xf& 
     }
 }
 
-// Shape-pair dispatch of b2PolygonContact / b2PolygonAndCircleContact / b2CircleContact
-// (contacts/b2polygoncontact.d:56-61 and siblings).  Fixture A is the "primary" type.
+// b2CollideEdgeAndCircle (collision/b2collideedge.d:31-155): the circle against the edge's
+// regions A and B (vertices, unless an adjacent edge owns the region) and AB (the face)
+static __device__ __noinline__ void collide_edge_circle(Manifold& m, const DFixture& edgeA, const Xf& xfA,
+                                                 const DFixture& circleB, const Xf& xfB) {
+    m.pointCount = 0;
+    float2 Q = mulT(xfA, mul(xfB, circleB.v[0]));                     // circle in the edge's frame
+    float2 A = edgeA.v[0], B = edgeA.v[1];
+    float2 e = B - A;
+    float u = dot(e, B - Q);                                            // barycentric coordinates
+    float v = dot(e, Q - A);
+    float radius = edgeA.radius + circleB.radius;
+    if (v <= 0.0f) {                                                    // region A
+        float2 d = Q - A;
+        if (dot(d, d) > radius * radius) return;
+        if (edgeA.edge_flags & 1) {
+            float2 A1 = edgeA.v[2], B1 = A;
+            float2 e1 = B1 - A1;
+            if (dot(e1, B1 - Q) > 0.0f) return;                         // region AB of the previous edge
+        }
+        m.pointCount = 1;
+        m.type = kManifoldCircles;
+        m.localNormal = v2(0.0f, 0.0f);
+        m.localPoint = A;
+        m.lp[0] = circleB.v[0];
+        m.id[0] = make_id(0u, 0u, kFeatureVertex, kFeatureVertex);
+        return;
+    }
+    if (u <= 0.0f) {                                                    // region B
+        float2 d = Q - B;
+        if (dot(d, d) > radius * radius) return;
+        if (edgeA.edge_flags & 2) {
+            float2 B2 = edgeA.v[3], A2 = B;
+            float2 e2 = B2 - A2;
+            if (dot(e2, Q - A2) > 0.0f) return;                         // region AB of the next edge
+        }
+        m.pointCount = 1;
+        m.type = kManifoldCircles;
+        m.localNormal = v2(0.0f, 0.0f);
+        m.localPoint = B;
+        m.lp[0] = circleB.v[0];
+        m.id[0] = make_id(1u, 0u, kFeatureVertex, kFeatureVertex);
+        return;
+    }
+    float den = dot(e, e);                                              // region AB
+    float2 P = fdiv(1.0f, den) * (u * A + v * B);
+    float2 d = Q - P;
+    if (dot(d, d) > radius * radius) return;
+    float2 n = v2(-e.y, e.x);
+    if (dot(n, Q - A) < 0.0f) n = v2(-n.x, -n.y);
+    normalize(n);
+    m.pointCount = 1;
+    m.type = kManifoldFaceA;
+    m.localNormal = n;
+    m.localPoint = A;
+    m.lp[0] = circleB.v[0];
+    m.id[0] = make_id(0u, 0u, kFeatureFace, kFeatureVertex);
+}
+
+// b2EPCollider (collision/b2collideedge.d:157-717): an edge against a polygon, the edge's
+// ghost vertices limiting the admissible normals
+static __device__ __noinline__ void collide_edge_polygon(Manifold& m, const DFixture& edgeA, const Xf& xfA,
+                                                  const DFixture& polygonB, const Xf& xfB) {
+    enum { kUnknown = 0, kEdgeA = 1, kEdgeB = 2 };
+    Xf xf = mulT(xfA, xfB);
+    float2 centroidB = mul(xf, polygonB.centroid);
+    float2 v0 = edgeA.v[2], v1 = edgeA.v[0], v2_ = edgeA.v[1], v3 = edgeA.v[3];
+    const bool hasVertex0 = (edgeA.edge_flags & 1) != 0, hasVertex3 = (edgeA.edge_flags & 2) != 0;
+    float2 edge1 = v2_ - v1;
+    normalize(edge1);
+    float2 normal0 = v2(0.0f, 0.0f), normal1 = v2(edge1.y, -edge1.x), normal2 = v2(0.0f, 0.0f);
+    float offset1 = dot(normal1, centroidB - v1);
+    float offset0 = 0.0f, offset2 = 0.0f;
+    bool convex1 = false, convex2 = false;
+    if (hasVertex0) {                                                   // a preceding edge
+        float2 edge0 = v1 - v0;
+        normalize(edge0);
+        normal0 = v2(edge0.y, -edge0.x);
+        convex1 = cross(edge0, edge1) >= 0.0f;
+        offset0 = dot(normal0, centroidB - v0);
+    }
+    if (hasVertex3) {                                                   // a following edge
+        float2 edge2 = v3 - v2_;
+        normalize(edge2);
+        normal2 = v2(edge2.y, -edge2.x);
+        convex2 = cross(edge1, edge2) > 0.0f;
+        offset2 = dot(normal2, centroidB - v2_);
+    }
+    // front or back collision; the collision normal and its limits
+    bool front;
+    float2 normal, lowerLimit, upperLimit;
+    auto set = [&](bool f, float2 nf, float2 lf, float2 uf, float2 nb, float2 lb, float2 ub) {
+        front = f;
+        if (front) { normal = nf; lowerLimit = lf; upperLimit = uf; }
+        else { normal = nb; lowerLimit = lb; upperLimit = ub; }
+    };
+    if (hasVertex0 && hasVertex3) {
+        if (convex1 && convex2)
+            set(offset0 >= 0.0f || offset1 >= 0.0f || offset2 >= 0.0f, normal1, normal0, normal2, -normal1, -normal1, -normal1);
+        else if (convex1)
+            set(offset0 >= 0.0f || (offset1 >= 0.0f && offset2 >= 0.0f), normal1, normal0, normal1, -normal1, -normal2, -normal1);
+        else if (convex2)
+            set(offset2 >= 0.0f || (offset0 >= 0.0f && offset1 >= 0.0f), normal1, normal1, normal2, -normal1, -normal1, -normal0);
+        else
+            set(offset0 >= 0.0f && offset1 >= 0.0f && offset2 >= 0.0f, normal1, normal1, normal1, -normal1, -normal2, -normal0);
+    } else if (hasVertex0) {
+        if (convex1) set(offset0 >= 0.0f || offset1 >= 0.0f, normal1, normal0, -normal1, -normal1, normal1, -normal1);
+        else set(offset0 >= 0.0f && offset1 >= 0.0f, normal1, normal1, -normal1, -normal1, normal1, -normal0);
+    } else if (hasVertex3) {
+        if (convex2) set(offset1 >= 0.0f || offset2 >= 0.0f, normal1, -normal1, normal2, -normal1, -normal1, normal1);
+        else set(offset1 >= 0.0f && offset2 >= 0.0f, normal1, -normal1, normal1, -normal1, -normal2, normal1);
+    } else {
+        set(offset1 >= 0.0f, normal1, -normal1, -normal1, -normal1, normal1, normal1);
+    }
+    float2 pv[8], pn[8];                                                // polygon B in frame A
+    const int pcount = polygonB.count;
+    for (int i = 0; i < pcount; ++i) {
+        pv[i] = mul(xf, polygonB.v[i]);
+        pn[i] = mul(xf.q, polygonB.n[i]);
+    }
+    const float radius = 2.0f * (2.0f * kLinearSlop);                   // 2 * b2_polygonRadius
+    m.pointCount = 0;
+    // edge separation (b2collideedge.d:636-653)
+    int edgeType = kEdgeA, edgeIndex = front ? 0 : 1;
+    float edgeSeparation = kMaxFloat;
+    for (int i = 0; i < pcount; ++i) {
+        float s = dot(normal, pv[i] - v1);
+        if (s < edgeSeparation) edgeSeparation = s;
+    }
+    if (edgeSeparation > radius) return;
+    // polygon separation (b2collideedge.d:655-700)
+    int polyType = kUnknown, polyIndex = -1;
+    float polySeparation = -kMaxFloat;
+    {
+        float2 perp = v2(-normal.y, normal.x);
+        for (int i = 0; i < pcount; ++i) {
+            float2 n = -pn[i];
+            float s1 = dot(n, pv[i] - v1);
+            float s2 = dot(n, pv[i] - v2_);
+            float s = bmin(s1, s2);
+            if (s > radius) { polyType = kEdgeB; polyIndex = i; polySeparation = s; break; }   // no collision
+            if (dot(n, perp) >= 0.0f) {                                 // adjacency
+                if (dot(n - upperLimit, normal) < -kAngularSlop) continue;
+            } else {
+                if (dot(n - lowerLimit, normal) < -kAngularSlop) continue;
+            }
+            if (s > polySeparation) { polyType = kEdgeB; polyIndex = i; polySeparation = s; }
+        }
+    }
+    if (polyType != kUnknown && polySeparation > radius) return;
+    const float k_relativeTol = 0.98f, k_absoluteTol = 0.001f;         // hysteresis
+    int primaryType, primaryIndex;
+    if (polyType == kUnknown) { primaryType = edgeType; primaryIndex = edgeIndex; }
+    else if (polySeparation > k_relativeTol * edgeSeparation + k_absoluteTol) { primaryType = polyType; primaryIndex = polyIndex; }
+    else { primaryType = edgeType; primaryIndex = edgeIndex; }
+    ClipVertex ie[2];
+    int rf_i1, rf_i2;
+    float2 rf_v1, rf_v2, rf_normal;
+    if (primaryType == kEdgeA) {
+        m.type = kManifoldFaceA;
+        int bestIndex = 0;                                              // the most anti-parallel polygon normal
+        float bestValue = dot(normal, pn[0]);
+        for (int i = 1; i < pcount; ++i) {
+            float value = dot(normal, pn[i]);
+            if (value < bestValue) { bestValue = value; bestIndex = i; }
+        }
+        int i1 = bestIndex;
+        int i2 = i1 + 1 < pcount ? i1 + 1 : 0;
+        ie[0].v = pv[i1];
+        ie[0].id = make_id(0u, (uint32_t)i1, kFeatureFace, kFeatureVertex);
+        ie[1].v = pv[i2];
+        ie[1].id = make_id(0u, (uint32_t)i2, kFeatureFace, kFeatureVertex);
+        if (front) { rf_i1 = 0; rf_i2 = 1; rf_v1 = v1; rf_v2 = v2_; rf_normal = normal1; }
+        else { rf_i1 = 1; rf_i2 = 0; rf_v1 = v2_; rf_v2 = v1; rf_normal = -normal1; }
+    } else {
+        m.type = kManifoldFaceB;
+        ie[0].v = v1;
+        ie[0].id = make_id(0u, (uint32_t)primaryIndex, kFeatureVertex, kFeatureFace);
+        ie[1].v = v2_;
+        ie[1].id = make_id(0u, (uint32_t)primaryIndex, kFeatureVertex, kFeatureFace);
+        rf_i1 = primaryIndex;
+        rf_i2 = rf_i1 + 1 < pcount ? rf_i1 + 1 : 0;
+        rf_v1 = pv[rf_i1];
+        rf_v2 = pv[rf_i2];
+        rf_normal = pn[rf_i1];
+    }
+    float2 sideNormal1 = v2(rf_normal.y, -rf_normal.x);
+    float2 sideNormal2 = -sideNormal1;
+    float sideOffset1 = dot(sideNormal1, rf_v1);
+    float sideOffset2 = dot(sideNormal2, rf_v2);
+    ClipVertex clipPoints1[2], clipPoints2[2];                          // clip against the side edges
+    int np = clip_segment(clipPoints1, ie, sideNormal1, sideOffset1, rf_i1);
+    if (np < 2) return;
+    np = clip_segment(clipPoints2, clipPoints1, sideNormal2, sideOffset2, rf_i2);
+    if (np < 2) return;
+    if (primaryType == kEdgeA) {
+        m.localNormal = rf_normal;
+        m.localPoint = rf_v1;
+    } else {
+        m.localNormal = polygonB.n[rf_i1];
+        m.localPoint = polygonB.v[rf_i1];
+    }
+    int pointCount = 0;
+    for (int i = 0; i < 2; ++i) {
+        float separation = dot(rf_normal, clipPoints2[i].v - rf_v1);
+        if (separation <= radius) {
+            if (primaryType == kEdgeA) {
+                m.lp[pointCount] = mulT(xf, clipPoints2[i].v);
+                m.id[pointCount] = clipPoints2[i].id;
+            } else {
+                uint32_t id = clipPoints2[i].id;
+                uint32_t ia = id & 0xffu, ib = (id >> 8) & 0xffu, ta = (id >> 16) & 0xffu, tb = (id >> 24) & 0xffu;
+                m.lp[pointCount] = clipPoints2[i].v;
+                m.id[pointCount] = make_id(ib, ia, tb, ta);
+            }
+            ++pointCount;
+        }
+    }
+    m.pointCount = pointCount;
+}
+
+// Shape-pair dispatch of b2PolygonContact / b2PolygonAndCircleContact / b2CircleContact /
+// b2EdgeAndCircleContact / b2EdgeAndPolygonContact (contacts/b2polygoncontact.d:56-61 and
+// siblings).  Fixture A is the "primary" type.
 DG void evaluate_manifold(Manifold& m, const DFixture& fa, const Xf& xfA, const DFixture& fb, const Xf& xfB) {
     if (fa.type == kShapePolygon && fb.type == kShapePolygon) collide_polygons(m, fa, xfA, fb, xfB);
     else if (fa.type == kShapePolygon) collide_polygon_circle(m, fa, xfA, fb, xfB);
+    else if (fa.type == kShapeEdge && fb.type == kShapeCircle) collide_edge_circle(m, fa, xfA, fb, xfB);
+    else if (fa.type == kShapeEdge) collide_edge_polygon(m, fa, xfA, fb, xfB);
     else collide_circles(m, fa, xfA, fb, xfB);
 }
 

@@ -491,6 +491,7 @@ __device__ __noinline__ void find_new_contacts(const Ctx& x, int w) {
             const DFixture& fA = x.fx[pr.x];
             const DFixture& fB = x.fx[pr.y];
             acc = fA.body != fB.body;
+            if (acc) acc = !(fA.type == kShapeEdge && fB.type == kShapeEdge);   // no edge-edge contact type
             if (acc) acc = !hash_contains(x, wi, pair_key(pr.x, pr.y));
             if (acc) acc = body_should_collide(x, fB.body, fA.body);
             if (acc) acc = filter_should_collide(fA, fB);
@@ -499,9 +500,11 @@ __device__ __noinline__ void find_new_contacts(const Ctx& x, int w) {
         if (acc) {
             int slot = n + added + __popc(bal & ((1u << lane) - 1));
             if (slot < wi.contact_cap) {
-                // b2Contact.Create: the registry's primary order puts the polygon first (b2contact.d:375-400)
+                // b2Contact.Create: the registry's primary order puts the polygon before a circle and
+                // an edge before a circle or a polygon (b2contact.d:358-400)
                 int fa = pr.x, fb = pr.y;
-                if (x.fx[fa].type == kShapeCircle && x.fx[fb].type == kShapePolygon) { int t = fa; fa = fb; fb = t; }
+                const int ta = x.fx[fa].type, tb = x.fx[fb].type;
+                if ((ta == kShapeCircle && tb == kShapePolygon) || (ta != kShapeEdge && tb == kShapeEdge)) { int t = fa; fa = fb; fb = t; }
                 const DFixture& FA = x.fx[fa];
                 const DFixture& FB = x.fx[fb];
                 dbox_contact_state& c = x.ct[wi.contact_start + slot];

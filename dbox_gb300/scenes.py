@@ -476,6 +476,82 @@ def pulleys(n=3, x0=-10.0, spacing=8.0):
     return out
 
 
+def _edges(points, ghosts=True, body_type=abi.STATIC, friction=0.6):
+    """One body at the origin with an edge fixture per segment of the polyline `points`
+    (b2EdgeShape, shapes/b2edgeshape.d); with `ghosts` each segment knows its neighbours
+    (hasVertex0 / hasVertex3), as a chain's child edges do."""
+    pts = np.asarray(points, F32)
+    n = len(pts) - 1
+    s = _empty()
+    b = abi.body_defs(1)
+    b["type"] = body_type
+    s["bodies"] = b
+    s["fixture_body"] = np.zeros(n, np.int32)
+    sh = np.zeros(n, abi.SHAPE_DEF)
+    sh["kind"] = abi.SHAPE_EDGE
+    for i in range(n):
+        sh["vertices"][i, 0] = pts[i]
+        sh["vertices"][i, 1] = pts[i + 1]
+        flags = 0
+        if ghosts and i > 0:
+            sh["vertices"][i, 2] = pts[i - 1]
+            flags |= 1
+        if ghosts and i + 1 < n:
+            sh["vertices"][i, 3] = pts[i + 2]
+            flags |= 2
+        sh["count"][i] = flags
+    s["shapes"] = sh
+    fx = abi.fixture_defs(n)
+    fx["friction"] = friction
+    fx["density"] = 0.0
+    s["fixtures"] = fx
+    return s
+
+
+def edge_ground(n=40, seed=13, pyramid_rows=6):
+    """Edge shapes (b2EdgeShape, b2CollideEdgeAndCircle / b2EPCollider, collision/b2collideedge.d):
+    a terrain of connected edges with ghost vertices (smooth collision across the joints),
+    loose edges without neighbours, circles and convex polygons dropped onto it, a small box
+    pyramid standing on a flat edge (the reference's pyramid demo uses an edge ground), and a
+    dynamic body carrying an edge fixture next to its box (edges never touch edges)."""
+    rng = np.random.default_rng(seed)
+    xs = np.linspace(-30.0, 30.0, 25)
+    ys = np.where(np.abs(xs) < 8.0, 0.0, 0.15 * (np.abs(xs) - 8.0) + 0.4 * np.sin(xs))
+    parts = [_edges(np.stack([xs, ys], 1))]
+    parts.append(_edges([(-12.0, 6.0), (-4.0, 4.0)], ghosts=False))                 # a loose ramp
+    parts.append(_edges([(4.0, 4.0), (12.0, 6.0)], ghosts=False))
+    if pyramid_rows:
+        pyr = pyramid(rows=pyramid_rows, ground=False)
+        pyr["bodies"]["position"][:, 1] -= 0.25                         # resting on y = 0
+        parts.append(pyr)
+    k = n // 2
+    circ = _boxes([(float(x), 10.0 + float(y)) for x, y in zip(rng.uniform(-25.0, 25.0, k), rng.uniform(0.0, 8.0, k))],
+                  0.3, 0.3, abi.DYNAMIC, 0.5, 1.0)
+    circ["shapes"]["kind"] = abi.SHAPE_CIRCLE
+    circ["shapes"]["radius"] = rng.uniform(0.2, 0.5, k).astype(F32)
+    parts.append(circ)
+    polys = _boxes([(float(x), 12.0 + float(y)) for x, y in zip(rng.uniform(-25.0, 25.0, n - k), rng.uniform(0.0, 8.0, n - k))],
+                   0.3, 0.3, abi.DYNAMIC, 0.5, 1.0)
+    polys["shapes"]["kind"] = abi.SHAPE_POLYGON
+    for i in range(n - k):
+        m = int(rng.integers(3, 9))
+        ang = np.sort(rng.uniform(0.0, 2.0 * np.pi, m))
+        r = rng.uniform(0.3, 0.6)
+        polys["shapes"]["count"][i] = m
+        polys["shapes"]["vertices"][i, :m, 0] = r * np.cos(ang)
+        polys["shapes"]["vertices"][i, :m, 1] = r * np.sin(ang)
+    parts.append(polys)
+    carrier = _boxes([(20.0, 3.0)], 0.5, 0.25, abi.DYNAMIC, 0.5, 1.0)   # box + an edge fixture below it
+    e = _edges([(-0.6, -0.4), (0.6, -0.4)], ghosts=False)
+    carrier["fixture_body"] = np.concatenate([carrier["fixture_body"], np.zeros(1, np.int32)])
+    carrier["shapes"] = np.concatenate([carrier["shapes"], e["shapes"]])
+    carrier["fixtures"] = np.concatenate([carrier["fixtures"], e["fixtures"]])
+    parts.append(carrier)
+    out = _concat(parts)
+    out["name"] = "edge_ground"
+    return out
+
+
 def batch(n_worlds=4096, seed=3, lo=8, hi=512):
     """Batched workload: per-world body counts log-uniform in [lo, hi]; thirds of
     pyramids, 40 m-container scatters and box stacks."""

@@ -62,6 +62,9 @@ typedef struct {
 #define DBOX_SHAPE_POLYGON 1     /* b2PolygonShape.Set(vertices, count): weld + gift-wrap hull */
 #define DBOX_SHAPE_BOX 2         /* b2PolygonShape.SetAsBox(hx, hy) */
 #define DBOX_SHAPE_ORIENTED_BOX 3 /* b2PolygonShape.SetAsBox(hx, hy, center, angle) */
+#define DBOX_SHAPE_EDGE 4        /* b2EdgeShape: vertices[0..1] = vertex1, vertex2; count bit 0 =
+                                    hasVertex0 with vertices[2] = vertex0, bit 1 = hasVertex3 with
+                                    vertices[3] = vertex3 (the neighbours for smooth collision) */
 
 typedef struct {
     int32_t kind;            /* DBOX_SHAPE_* */

@@ -282,6 +282,9 @@ struct Shape {
     Vec2 vertices[kMaxPolygonVertices];
     Vec2 normals[kMaxPolygonVertices];
     int count = 0;
+    // edge (b2edgeshape.d): vertices[0..1] = m_vertex1, m_vertex2 (count 2); ghost vertices
+    Vec2 vertex0, vertex3;
+    bool hasVertex0 = false, hasVertex3 = false;
 };
 
 struct MassData { f32 mass = 0; Vec2 center; f32 I = 0; };
@@ -439,6 +442,12 @@ static void ShapeComputeAABB(const Shape& s, AABB* aabb, const Transform& xf) {
 }
 
 static void ShapeComputeMass(const Shape& s, MassData* md, f32 density) {
+    if (s.type == kEdge) {                                              // b2edgeshape.d: no mass
+        md->mass = 0.0f;
+        md->center = 0.5f * (s.vertices[0] + s.vertices[1]);
+        md->I = 0.0f;
+        return;
+    }
     if (s.type == kCircle) {                                            // b2circleshape.d:120-127
         md->mass = ((density * kPi) * s.radius) * s.radius;
         md->center = s.p;
@@ -775,6 +784,295 @@ static void CollidePolygonAndCircle(Manifold* manifold, const Shape& polygonA, c
         manifold->points[0].localPoint = circleB.p;
         manifold->points[0].id.key = 0;
     }
+}
+
+// b2CollideEdgeAndCircle (b2collideedge.d:31-155): the circle against the edge's regions A, B
+// (vertices, unless an adjacent edge owns the region) and AB (the face)
+static void CollideEdgeAndCircle(Manifold* manifold, const Shape& edgeA, const Transform& xfA,
+                                 const Shape& circleB, const Transform& xfB) {
+    manifold->pointCount = 0;
+    Vec2 Q = MulT(xfA, Mul(xfB, circleB.p));                            // circle in the edge's frame
+    Vec2 A = edgeA.vertices[0], B = edgeA.vertices[1];
+    Vec2 e = B - A;
+    f32 u = Dot(e, B - Q);                                              // barycentric coordinates
+    f32 v = Dot(e, Q - A);
+    f32 radius = edgeA.radius + circleB.radius;
+    ContactID id;
+    id.key = 0;
+    id.cf.indexB = 0;
+    id.cf.typeB = kFeatureVertex;
+    if (v <= 0.0f) {                                                    // region A
+        Vec2 P = A;
+        Vec2 d = Q - P;
+        f32 dd = Dot(d, d);
+        if (dd > radius * radius) return;
+        if (edgeA.hasVertex0) {
+            Vec2 A1 = edgeA.vertex0;
+            Vec2 B1 = A;
+            Vec2 e1 = B1 - A1;
+            f32 u1 = Dot(e1, B1 - Q);
+            if (u1 > 0.0f) return;                                      // region AB of the previous edge
+        }
+        id.cf.indexA = 0;
+        id.cf.typeA = kFeatureVertex;
+        manifold->pointCount = 1;
+        manifold->type = kManifoldCircles;
+        manifold->localNormal.SetZero();
+        manifold->localPoint = P;
+        manifold->points[0].id = id;
+        manifold->points[0].localPoint = circleB.p;
+        return;
+    }
+    if (u <= 0.0f) {                                                    // region B
+        Vec2 P = B;
+        Vec2 d = Q - P;
+        f32 dd = Dot(d, d);
+        if (dd > radius * radius) return;
+        if (edgeA.hasVertex3) {
+            Vec2 B2 = edgeA.vertex3;
+            Vec2 A2 = B;
+            Vec2 e2 = B2 - A2;
+            f32 v2 = Dot(e2, Q - A2);
+            if (v2 > 0.0f) return;                                      // region AB of the next edge
+        }
+        id.cf.indexA = 1;
+        id.cf.typeA = kFeatureVertex;
+        manifold->pointCount = 1;
+        manifold->type = kManifoldCircles;
+        manifold->localNormal.SetZero();
+        manifold->localPoint = P;
+        manifold->points[0].id = id;
+        manifold->points[0].localPoint = circleB.p;
+        return;
+    }
+    f32 den = Dot(e, e);                                                // region AB
+    Vec2 P = (1.0f / den) * (u * A + v * B);
+    Vec2 d = Q - P;
+    f32 dd = Dot(d, d);
+    if (dd > radius * radius) return;
+    Vec2 n(-e.y, e.x);
+    if (Dot(n, Q - A) < 0.0f) n.Set(-n.x, -n.y);
+    n.Normalize();
+    id.cf.indexA = 0;
+    id.cf.typeA = kFeatureFace;
+    manifold->pointCount = 1;
+    manifold->type = kManifoldFaceA;
+    manifold->localNormal = n;
+    manifold->localPoint = A;
+    manifold->points[0].id = id;
+    manifold->points[0].localPoint = circleB.p;
+}
+
+// b2EPCollider (b2collideedge.d:157-717): an edge against a polygon with the edge's
+// adjacency (ghost vertices) limiting the admissible normals
+struct EPCollider {
+    enum { kUnknown = 0, kEdgeA, kEdgeB };
+    struct Axis { int type = kUnknown; int index = 0; f32 separation = 0; };
+    struct ReferenceFace { int i1 = 0, i2 = 0; Vec2 v1, v2, normal, sideNormal1, sideNormal2; f32 sideOffset1 = 0, sideOffset2 = 0; };
+    Vec2 pv[kMaxPolygonVertices], pn[kMaxPolygonVertices];            // polygon B in frame A
+    int pcount = 0;
+    Transform xf;
+    Vec2 centroidB, v0, v1, v2, v3, normal0, normal1, normal2, normal, lowerLimit, upperLimit;
+    f32 radius = 0;
+    bool front = false;
+
+    Axis ComputeEdgeSeparation() const {                                // b2collideedge.d:636-653
+        Axis axis;
+        axis.type = kEdgeA;
+        axis.index = front ? 0 : 1;
+        axis.separation = kMaxFloat;
+        for (int i = 0; i < pcount; ++i) {
+            f32 s = Dot(normal, pv[i] - v1);
+            if (s < axis.separation) axis.separation = s;
+        }
+        return axis;
+    }
+
+    Axis ComputePolygonSeparation() const {                             // b2collideedge.d:655-700
+        Axis axis;
+        axis.type = kUnknown;
+        axis.index = -1;
+        axis.separation = -kMaxFloat;
+        Vec2 perp(-normal.y, normal.x);
+        for (int i = 0; i < pcount; ++i) {
+            Vec2 n = -pn[i];
+            f32 s1 = Dot(n, pv[i] - v1);
+            f32 s2 = Dot(n, pv[i] - v2);
+            f32 s = Min(s1, s2);
+            if (s > radius) {                                           // no collision
+                axis.type = kEdgeB;
+                axis.index = i;
+                axis.separation = s;
+                return axis;
+            }
+            if (Dot(n, perp) >= 0.0f) {                                 // adjacency
+                if (Dot(n - upperLimit, normal) < -kAngularSlop) continue;
+            } else {
+                if (Dot(n - lowerLimit, normal) < -kAngularSlop) continue;
+            }
+            if (s > axis.separation) {
+                axis.type = kEdgeB;
+                axis.index = i;
+                axis.separation = s;
+            }
+        }
+        return axis;
+    }
+
+    void Collide(Manifold* manifold, const Shape& edgeA, const Transform& xfA, const Shape& polygonB,
+                 const Transform& xfB) {                                // b2collideedge.d:193-634
+        xf = MulT(xfA, xfB);
+        centroidB = Mul(xf, polygonB.centroid);
+        v0 = edgeA.vertex0;
+        v1 = edgeA.vertices[0];
+        v2 = edgeA.vertices[1];
+        v3 = edgeA.vertex3;
+        bool hasVertex0 = edgeA.hasVertex0, hasVertex3 = edgeA.hasVertex3;
+        Vec2 edge1 = v2 - v1;
+        edge1.Normalize();
+        normal1.Set(edge1.y, -edge1.x);
+        f32 offset1 = Dot(normal1, centroidB - v1);
+        f32 offset0 = 0.0f, offset2 = 0.0f;
+        bool convex1 = false, convex2 = false;
+        if (hasVertex0) {                                               // a preceding edge
+            Vec2 edge0 = v1 - v0;
+            edge0.Normalize();
+            normal0.Set(edge0.y, -edge0.x);
+            convex1 = Cross(edge0, edge1) >= 0.0f;
+            offset0 = Dot(normal0, centroidB - v0);
+        }
+        if (hasVertex3) {                                               // a following edge
+            Vec2 edge2 = v3 - v2;
+            edge2.Normalize();
+            normal2.Set(edge2.y, -edge2.x);
+            convex2 = Cross(edge1, edge2) > 0.0f;
+            offset2 = Dot(normal2, centroidB - v2);
+        }
+        // front or back collision; the collision normal's limits
+        auto set = [&](bool f, Vec2 nf, Vec2 lf, Vec2 uf, Vec2 nb, Vec2 lb, Vec2 ub) {
+            front = f;
+            if (front) { normal = nf; lowerLimit = lf; upperLimit = uf; }
+            else { normal = nb; lowerLimit = lb; upperLimit = ub; }
+        };
+        if (hasVertex0 && hasVertex3) {
+            if (convex1 && convex2)
+                set(offset0 >= 0.0f || offset1 >= 0.0f || offset2 >= 0.0f, normal1, normal0, normal2, -normal1, -normal1, -normal1);
+            else if (convex1)
+                set(offset0 >= 0.0f || (offset1 >= 0.0f && offset2 >= 0.0f), normal1, normal0, normal1, -normal1, -normal2, -normal1);
+            else if (convex2)
+                set(offset2 >= 0.0f || (offset0 >= 0.0f && offset1 >= 0.0f), normal1, normal1, normal2, -normal1, -normal1, -normal0);
+            else
+                set(offset0 >= 0.0f && offset1 >= 0.0f && offset2 >= 0.0f, normal1, normal1, normal1, -normal1, -normal2, -normal0);
+        } else if (hasVertex0) {
+            if (convex1) set(offset0 >= 0.0f || offset1 >= 0.0f, normal1, normal0, -normal1, -normal1, normal1, -normal1);
+            else set(offset0 >= 0.0f && offset1 >= 0.0f, normal1, normal1, -normal1, -normal1, normal1, -normal0);
+        } else if (hasVertex3) {
+            if (convex2) set(offset1 >= 0.0f || offset2 >= 0.0f, normal1, -normal1, normal2, -normal1, -normal1, normal1);
+            else set(offset1 >= 0.0f && offset2 >= 0.0f, normal1, -normal1, normal1, -normal1, -normal2, normal1);
+        } else {
+            set(offset1 >= 0.0f, normal1, -normal1, -normal1, -normal1, normal1, normal1);
+        }
+        pcount = polygonB.count;                                        // polygon B in frame A
+        for (int i = 0; i < polygonB.count; ++i) {
+            pv[i] = Mul(xf, polygonB.vertices[i]);
+            pn[i] = Mul(xf.q, polygonB.normals[i]);
+        }
+        radius = 2.0f * kPolygonRadius;
+        manifold->pointCount = 0;
+        Axis edgeAxis = ComputeEdgeSeparation();
+        if (edgeAxis.type == kUnknown) return;                          // no valid normal
+        if (edgeAxis.separation > radius) return;
+        Axis polygonAxis = ComputePolygonSeparation();
+        if (polygonAxis.type != kUnknown && polygonAxis.separation > radius) return;
+        const f32 k_relativeTol = 0.98f, k_absoluteTol = 0.001f;          // hysteresis
+        Axis primaryAxis;
+        if (polygonAxis.type == kUnknown) primaryAxis = edgeAxis;
+        else if (polygonAxis.separation > k_relativeTol * edgeAxis.separation + k_absoluteTol) primaryAxis = polygonAxis;
+        else primaryAxis = edgeAxis;
+        ClipVertex ie[2];
+        ReferenceFace rf;
+        if (primaryAxis.type == kEdgeA) {
+            manifold->type = kManifoldFaceA;
+            int bestIndex = 0;                                          // the most anti-parallel polygon normal
+            f32 bestValue = Dot(normal, pn[0]);
+            for (int i = 1; i < pcount; ++i) {
+                f32 value = Dot(normal, pn[i]);
+                if (value < bestValue) { bestValue = value; bestIndex = i; }
+            }
+            int i1 = bestIndex;
+            int i2 = i1 + 1 < pcount ? i1 + 1 : 0;
+            ie[0].v = pv[i1];
+            ie[0].id.cf.indexA = 0;
+            ie[0].id.cf.indexB = (uint8_t)i1;
+            ie[0].id.cf.typeA = kFeatureFace;
+            ie[0].id.cf.typeB = kFeatureVertex;
+            ie[1].v = pv[i2];
+            ie[1].id.cf.indexA = 0;
+            ie[1].id.cf.indexB = (uint8_t)i2;
+            ie[1].id.cf.typeA = kFeatureFace;
+            ie[1].id.cf.typeB = kFeatureVertex;
+            if (front) { rf.i1 = 0; rf.i2 = 1; rf.v1 = v1; rf.v2 = v2; rf.normal = normal1; }
+            else { rf.i1 = 1; rf.i2 = 0; rf.v1 = v2; rf.v2 = v1; rf.normal = -normal1; }
+        } else {
+            manifold->type = kManifoldFaceB;
+            ie[0].v = v1;
+            ie[0].id.cf.indexA = 0;
+            ie[0].id.cf.indexB = (uint8_t)primaryAxis.index;
+            ie[0].id.cf.typeA = kFeatureVertex;
+            ie[0].id.cf.typeB = kFeatureFace;
+            ie[1].v = v2;
+            ie[1].id.cf.indexA = 0;
+            ie[1].id.cf.indexB = (uint8_t)primaryAxis.index;
+            ie[1].id.cf.typeA = kFeatureVertex;
+            ie[1].id.cf.typeB = kFeatureFace;
+            rf.i1 = primaryAxis.index;
+            rf.i2 = rf.i1 + 1 < pcount ? rf.i1 + 1 : 0;
+            rf.v1 = pv[rf.i1];
+            rf.v2 = pv[rf.i2];
+            rf.normal = pn[rf.i1];
+        }
+        rf.sideNormal1.Set(rf.normal.y, -rf.normal.x);
+        rf.sideNormal2 = -rf.sideNormal1;
+        rf.sideOffset1 = Dot(rf.sideNormal1, rf.v1);
+        rf.sideOffset2 = Dot(rf.sideNormal2, rf.v2);
+        ClipVertex clipPoints1[2], clipPoints2[2];                      // clip against the side edges
+        int np = ClipSegmentToLine(clipPoints1, ie, rf.sideNormal1, rf.sideOffset1, rf.i1);
+        if (np < kMaxManifoldPoints) return;
+        np = ClipSegmentToLine(clipPoints2, clipPoints1, rf.sideNormal2, rf.sideOffset2, rf.i2);
+        if (np < kMaxManifoldPoints) return;
+        if (primaryAxis.type == kEdgeA) {
+            manifold->localNormal = rf.normal;
+            manifold->localPoint = rf.v1;
+        } else {
+            manifold->localNormal = polygonB.normals[rf.i1];
+            manifold->localPoint = polygonB.vertices[rf.i1];
+        }
+        int pointCount = 0;
+        for (int i = 0; i < kMaxManifoldPoints; ++i) {
+            f32 separation = Dot(rf.normal, clipPoints2[i].v - rf.v1);
+            if (separation <= radius) {
+                ManifoldPoint* cp = manifold->points + pointCount;
+                if (primaryAxis.type == kEdgeA) {
+                    cp->localPoint = MulT(xf, clipPoints2[i].v);
+                    cp->id = clipPoints2[i].id;
+                } else {
+                    cp->localPoint = clipPoints2[i].v;
+                    cp->id.cf.typeA = clipPoints2[i].id.cf.typeB;
+                    cp->id.cf.typeB = clipPoints2[i].id.cf.typeA;
+                    cp->id.cf.indexA = clipPoints2[i].id.cf.indexB;
+                    cp->id.cf.indexB = clipPoints2[i].id.cf.indexA;
+                }
+                ++pointCount;
+            }
+        }
+        manifold->pointCount = pointCount;
+    }
+};
+
+static void CollideEdgeAndPolygon(Manifold* manifold, const Shape& edgeA, const Transform& xfA,
+                                  const Shape& polygonB, const Transform& xfB) {
+    EPCollider collider;
+    collider.Collide(manifold, edgeA, xfA, polygonB, xfB);
 }
 
 // ------------------------------------------------------------ distance (GJK)
@@ -1656,6 +1954,8 @@ struct Contact {
         const Shape& b = fixtureB->shape;
         if (a.type == kPolygon && b.type == kPolygon) CollidePolygons(m, a, xfA, b, xfB);
         else if (a.type == kPolygon && b.type == kCircle) CollidePolygonAndCircle(m, a, xfA, b, xfB);
+        else if (a.type == kEdge && b.type == kCircle) CollideEdgeAndCircle(m, a, xfA, b, xfB);
+        else if (a.type == kEdge && b.type == kPolygon) CollideEdgeAndPolygon(m, a, xfA, b, xfB);
         else CollideCircles(m, a, xfA, b, xfB);
     }
     void Update(Listener* listener);
@@ -3739,12 +4039,15 @@ void ContactManager::AddPair(void* proxyUserDataA, void* proxyUserDataB) {
     }
     if (bodyB->ShouldCollide(bodyA) == false) return;
     if (FilterShouldCollide(fixtureA, fixtureB) == false) return;
-    // Contact.Create: registry primary order is (circle,circle), (polygon,circle), (polygon,polygon)
+    // Contact.Create: the registry's primary order is (circle, circle), (polygon, circle),
+    // (polygon, polygon), (edge, circle), (edge, polygon); edges do not collide with edges
     int type1 = fixtureA->shape.type;
     int type2 = fixtureB->shape.type;
-    if (!((type1 == kCircle || type1 == kPolygon) && (type2 == kCircle || type2 == kPolygon))) return;
+    if (!((type1 == kCircle || type1 == kPolygon || type1 == kEdge) && (type2 == kCircle || type2 == kPolygon || type2 == kEdge)))
+        return;
+    if (type1 == kEdge && type2 == kEdge) return;
     Contact* c = new Contact();
-    if (type1 == kCircle && type2 == kPolygon) {
+    if ((type1 == kCircle && type2 == kPolygon) || (type1 != kEdge && type2 == kEdge)) {
         c->fixtureA = fixtureB; c->indexA = indexB;
         c->fixtureB = fixtureA; c->indexB = indexA;
     } else {
@@ -4476,6 +4779,17 @@ static bool BuildShape(const dbox_shape_def* sd, Shape* s) {
         s->type = kPolygon;
         s->radius = kPolygonRadius;
         PolygonSetAsBox(s, sd->hx, sd->hy, Vec2(sd->center.x, sd->center.y), sd->angle);
+        return true;
+    case DBOX_SHAPE_EDGE:                                               // b2EdgeShape.Set + ghost vertices
+        s->type = kEdge;
+        s->radius = kPolygonRadius;
+        s->count = 2;
+        s->vertices[0] = Vec2(sd->vertices[0].x, sd->vertices[0].y);
+        s->vertices[1] = Vec2(sd->vertices[1].x, sd->vertices[1].y);
+        s->hasVertex0 = (sd->count & 1) != 0;
+        s->hasVertex3 = (sd->count & 2) != 0;
+        s->vertex0 = s->hasVertex0 ? Vec2(sd->vertices[2].x, sd->vertices[2].y) : Vec2(0.0f, 0.0f);
+        s->vertex3 = s->hasVertex3 ? Vec2(sd->vertices[3].x, sd->vertices[3].y) : Vec2(0.0f, 0.0f);
         return true;
     default:
         return false;

@@ -296,3 +296,22 @@ def test_pulley_and_mouse_joints_exact(oracle_lib, gpu_lib):
             for i, ow in enumerate(ows):
                 d = exact_diff(ow.export_state(), gw.export_state(i))
                 assert not d, "world %d step %d: %s" % (i, t + 1, d[:6])
+
+
+def test_edge_shapes_exact(oracle_lib, gpu_lib):
+    # edge terrain with ghost vertices, loose edges, circles and polygons, a pyramid on an
+    # edge ground, an edge on a dynamic body: bit-exact against the oracle (contact list,
+    # manifolds with feature ids, bodies)
+    from dbox_gb300 import scenes
+    oracle_lib.set_trig_mode(1)
+    worlds = [scenes.edge_ground(), scenes.edge_ground(n=24, seed=21, pyramid_rows=4)]
+    gw = gpu_lib.World(worlds)
+    ows = [oracle_lib.OracleWorld(s) for s in worlds]
+    for t in range(240):
+        gw.step()
+        for ow in ows:
+            ow.step()
+        if t % 30 == 29:
+            for i, ow in enumerate(ows):
+                d = exact_diff(ow.export_state(), gw.export_state(i))
+                assert not d, "world %d step %d: %s" % (i, t + 1, d[:6])

@@ -304,3 +304,25 @@ def test_pulley_and_mouse_joints(oracle_lib):
     assert b["xf"][2, 1] < b["xf"][1, 1]                      # the heavier side went down
     m = s["mouse_joints"][0]["body_b"]
     assert np.hypot(b["xf"][m, 0] - 4.0, b["xf"][m, 1] - 3.0) < 0.6      # centre; the anchor is 0.28 m off it
+
+
+def test_edge_shapes_collide(oracle_lib):
+    # b2EdgeShape with b2CollideEdgeAndCircle / b2EPCollider: bodies come to rest on the edge
+    # terrain, contacts pair an edge (fixture A) with circles and polygons (face-A and face-B
+    # manifolds both occur), edges never touch edges, and the pyramid on the flat edge stands
+    from dbox_gb300 import scenes
+    oracle_lib.set_trig_mode(1)
+    s = scenes.edge_ground()
+    ow = oracle_lib.OracleWorld(s)
+    ow.step(steps=300)
+    st = ow.export_state()
+    b, c = st["bodies"], st["contacts"]
+    kind = s["shapes"]["kind"]
+    ka, kb = kind[c["fixture_a"]], kind[c["fixture_b"]]
+    assert ((ka == 4) & (kb != 4)).any() and not ((kb == 4) & (ka != 4)).any() and not ((ka == 4) & (kb == 4)).any()
+    edge_c = c[(ka == 4) & (c["point_count"] > 0)]
+    assert set(np.unique(edge_c["type"])) >= {1, 2}
+    dyn = b["type"] == 2
+    assert np.isfinite(b["xf"]).all() and b["xf"][dyn, 1].min() > -0.05
+    pyr = slice(1 + 1 + 1, 1 + 1 + 1 + 21)                    # ground, two ramps, then the 6-row pyramid
+    assert np.abs(b["sweep"][pyr, 7]).max() < 0.05             # still standing
