@@ -45,6 +45,7 @@ def lib():
     L.dbox_scene_create.argtypes = [vp, i32, i32, vp, i32, vp, vp, vp, i32, vp]
     L.dbox_body_create.argtypes = [vp, i32, vp, ctypes.POINTER(i32)]
     L.dbox_fixture_create.argtypes = [vp, i32, i32, vp, vp, ctypes.POINTER(i32)]
+    L.dbox_fixture_create_chain.argtypes = [vp, i32, i32, vp, i32, i32, vp, vp, vp, ctypes.POINTER(i32)]
     L.dbox_joint_create_revolute.argtypes = [vp, i32, vp, ctypes.POINTER(i32)]
     L.dbox_joint_create_distance.argtypes = [vp, i32, vp, ctypes.POINTER(i32)]
     L.dbox_joint_create_rope.argtypes = [vp, i32, vp, ctypes.POINTER(i32)]
@@ -243,6 +244,10 @@ class World:
             j = np.ascontiguousarray(s["joints"])
             _check(L.dbox_scene_create(self.h, i, len(b), abi.ptr(b), len(fb), abi.ptr(fb), abi.ptr(sh), abi.ptr(fx),
                                        len(j), abi.ptr(j) if len(j) else None), "dbox_scene_create")
+            for c in s.get("chains", ()):
+                fd = abi.fixture_defs(1)[0]
+                fd["friction"] = c.get("friction", 0.2)
+                self.create_chain(i, c["body"], c["vertices"], c["loop"], c.get("prev"), c.get("next"), fd)
             # joint kinds after the revolute joints, in this order (the oracle's order too)
             for d in s.get("distance_joints", ()):
                 self.create_joint(i, "distance", d)
@@ -275,6 +280,21 @@ class World:
         dd = np.ascontiguousarray(np.array([d], getattr(abi, dtype)))
         out = ctypes.c_int32()
         _check(getattr(lib(), fn)(self.h, world, abi.ptr(dd), ctypes.byref(out)), fn)
+        return out.value
+
+    def create_chain(self, world, body, vertices, loop=False, prev=None, next=None, fixture=None):
+        """b2Body.CreateFixture with a b2ChainShape (CreateChain / CreateLoop, SetPrevVertex /
+        SetNextVertex), created as its child edges; returns the first child's fixture index."""
+        v = np.ascontiguousarray(vertices, np.float32)
+        pv = np.ascontiguousarray(prev, np.float32) if prev is not None else None
+        nv = np.ascontiguousarray(next, np.float32) if next is not None else None
+        fd = fixture if fixture is not None else abi.fixture_defs(1)[0]
+        fd = np.ascontiguousarray(np.array([fd], abi.FIXTURE_DEF))
+        out = ctypes.c_int32()
+        _check(lib().dbox_fixture_create_chain(self.h, world, body, abi.ptr(v), len(v), 1 if loop else 0,
+                                               abi.ptr(pv) if pv is not None else None,
+                                               abi.ptr(nv) if nv is not None else None, abi.ptr(fd), ctypes.byref(out)),
+               "dbox_fixture_create_chain")
         return out.value
 
     def set_mouse_target(self, world, joint, target):

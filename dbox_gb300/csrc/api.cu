@@ -992,6 +992,60 @@ int32_t dbox_fixture_create(dbox_world* w, int32_t world, int32_t body, const db
     return DBOX_OK;
 }
 
+// the child edges of a b2ChainShape (b2chainshape.d: CreateChain / CreateLoop, GetChildEdge)
+// as edge shape records, in child order
+static std::vector<dbox_shape_def> chain_children(const dbox_vec2* vertices, int count, bool loop, const dbox_vec2* prev,
+                                                  const dbox_vec2* next) {
+    std::vector<dbox_vec2> v(vertices, vertices + count);
+    bool hasPrev = prev != nullptr, hasNext = next != nullptr;
+    dbox_vec2 pv = prev ? *prev : dbox_vec2{0.0f, 0.0f}, nv = next ? *next : dbox_vec2{0.0f, 0.0f};
+    if (loop) {
+        v.push_back(vertices[0]);
+        pv = v[v.size() - 2];
+        nv = v[1];
+        hasPrev = hasNext = true;
+    }
+    const int m = (int)v.size();
+    std::vector<dbox_shape_def> out;
+    for (int i = 0; i + 1 < m; ++i) {
+        dbox_shape_def e;
+        memset(&e, 0, sizeof(e));
+        e.kind = DBOX_SHAPE_EDGE;
+        e.vertices[0] = v[i];
+        e.vertices[1] = v[i + 1];
+        int flags = 0;
+        if (i > 0) { e.vertices[2] = v[i - 1]; flags |= 1; }
+        else if (hasPrev) { e.vertices[2] = pv; flags |= 1; }
+        if (i < m - 2) { e.vertices[3] = v[i + 2]; flags |= 2; }
+        else if (hasNext) { e.vertices[3] = nv; flags |= 2; }
+        e.count = flags;
+        out.push_back(e);
+    }
+    return out;
+}
+
+int32_t dbox_fixture_create_chain(dbox_world* w, int32_t world, int32_t body, const dbox_vec2* vertices, int32_t count,
+                                  int32_t loop, const dbox_vec2* prev_vertex, const dbox_vec2* next_vertex,
+                                  const dbox_fixture_def* def, int32_t* out_first) {
+    if (!w || !vertices || !def || world < 0 || world >= (int)w->worlds.size() || count < (loop ? 3 : 2))
+        return fail(DBOX_ERR_INVALID, "dbox_fixture_create_chain: bad arguments");
+    HostWorld& hw0 = w->worlds[world];
+    if (body < 0 || body >= (int)hw0.bs.size()) return fail(DBOX_ERR_INVALID, "dbox_fixture_create_chain: no body %d", body);
+    int rc = prepare_edit(w);
+    if (rc) return rc;
+    dbox_fixture_def d = *def;
+    d.density = 0.0f;
+    int first = -1;
+    for (const dbox_shape_def& e : chain_children(vertices, count, loop != 0, loop ? nullptr : prev_vertex,
+                                                  loop ? nullptr : next_vertex)) {
+        int idx = create_fixture(w->worlds[world], body, &e, &d);
+        if (idx < 0) return fail(DBOX_ERR_INVALID, "dbox_fixture_create_chain: bad child edge");
+        if (first < 0) first = idx;
+    }
+    if (out_first) *out_first = first;
+    return DBOX_OK;
+}
+
 int32_t dbox_joint_create_revolute(dbox_world* w, int32_t world, const dbox_revolute_def* def, int32_t* out_joint) {
     if (!w || !def || world < 0 || world >= (int)w->worlds.size()) return fail(DBOX_ERR_INVALID, "dbox_joint_create_revolute: bad arguments");
     int rc = prepare_edit(w);

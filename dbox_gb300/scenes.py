@@ -39,7 +39,7 @@ def _empty():
         "friction_joints": np.zeros(0, abi.FRICTION_DEF), "motor_joints": np.zeros(0, abi.MOTOR_DEF),
         "wheel_joints": np.zeros(0, abi.WHEEL_DEF), "prismatic_joints": np.zeros(0, abi.PRISMATIC_DEF),
         "pulley_joints": np.zeros(0, abi.PULLEY_DEF), "mouse_joints": np.zeros(0, abi.MOUSE_DEF),
-        "gravity": (0.0, -10.0), "name": "",
+        "chains": [], "gravity": (0.0, -10.0), "name": "",
     }
 
 
@@ -65,6 +65,7 @@ def _concat(parts):
             d["body_a"] += nb
             d["body_b"] += nb
             out[key] = np.concatenate([out[key], d])
+        out["chains"] = out["chains"] + [dict(c, body=c["body"] + nb) for c in p.get("chains", ())]
         nb += len(p["bodies"])
     return out
 
@@ -549,6 +550,59 @@ def edge_ground(n=40, seed=13, pyramid_rows=6):
     parts.append(carrier)
     out = _concat(parts)
     out["name"] = "edge_ground"
+    return out
+
+
+def chain_ground(n=40, seed=17):
+    """Chain shapes (b2ChainShape, collision/shapes/b2chainshape.d, created as their child
+    edges): a closed loop (CreateLoop) forming an irregular bowl, an open chain (CreateChain)
+    with SetPrevVertex / SetNextVertex ghosts across a valley, a second open chain without
+    ghosts, and circles and convex polygons dropped into them; a dynamic box carries a
+    small loop chain (no mass of its own).  Chains are created after the scene's fixtures,
+    in list order."""
+    rng = np.random.default_rng(seed)
+    ground = abi.body_defs(2)
+    ground["type"] = abi.STATIC
+    ground["position"][1] = (0.0, 0.5)
+    base = _empty()
+    base["bodies"] = ground
+    ang = np.linspace(np.pi * 1.05, np.pi * 1.95, 18)
+    bowl = np.concatenate([np.stack([14.0 * np.cos(ang), 10.0 + 8.0 * np.sin(ang) + 0.3 * np.sin(5 * ang)], 1),
+                           [(12.0, 14.0), (-12.0, 14.0)]])
+    xs = np.linspace(-34.0, -16.0, 12)
+    valley = np.stack([xs, 4.0 + 0.05 * (xs + 25.0) ** 2 - 3.0], 1)
+    base["chains"] = [
+        dict(body=0, vertices=bowl.astype(F32), loop=True, prev=None, next=None, friction=0.6),
+        dict(body=0, vertices=valley.astype(F32), loop=False, prev=(-36.0, 9.0), next=(-14.0, 9.0), friction=0.4),
+        dict(body=1, vertices=np.array([(16.0, 0.0), (22.0, 1.5), (30.0, 1.0)], F32), loop=False, prev=None,
+             next=None, friction=0.6),
+    ]
+    parts = [base]
+    k = n // 2
+    circ = _boxes([(float(x), 9.0 + float(y)) for x, y in zip(rng.uniform(-10.0, 10.0, k), rng.uniform(0.0, 4.0, k))],
+                  0.3, 0.3, abi.DYNAMIC, 0.5, 1.0)
+    circ["shapes"]["kind"] = abi.SHAPE_CIRCLE
+    circ["shapes"]["radius"] = rng.uniform(0.2, 0.5, k).astype(F32)
+    parts.append(circ)
+    m = n - k
+    polys = _boxes([(float(x), 12.0 + float(y)) for x, y in zip(
+        np.concatenate([rng.uniform(-9.0, 9.0, m - 6), rng.uniform(-30.0, -20.0, 3), rng.uniform(18.0, 28.0, 3)]),
+        rng.uniform(0.0, 4.0, m))], 0.3, 0.3, abi.DYNAMIC, 0.5, 1.0)
+    polys["shapes"]["kind"] = abi.SHAPE_POLYGON
+    for i in range(m):
+        c = int(rng.integers(3, 9))
+        a = np.sort(rng.uniform(0.0, 2.0 * np.pi, c))
+        r = rng.uniform(0.3, 0.6)
+        polys["shapes"]["count"][i] = c
+        polys["shapes"]["vertices"][i, :c, 0] = r * np.cos(a)
+        polys["shapes"]["vertices"][i, :c, 1] = r * np.sin(a)
+    parts.append(polys)
+    carrier = _boxes([(0.0, 20.0)], 0.5, 0.5, abi.DYNAMIC, 0.5, 1.0)
+    carrier["chains"] = [dict(body=0, vertices=np.array([(-0.8, -0.8), (0.8, -0.8), (0.8, 0.8), (-0.8, 0.8)], F32),
+                              loop=True, prev=None, next=None, friction=0.5)]
+    parts.append(carrier)
+    out = _concat(parts)
+    out["name"] = "chain_ground"
     return out
 
 

@@ -290,6 +290,17 @@ int32_t dbox_body_create(dbox_world* w, int32_t world, const dbox_body_def* def,
  * (collision/shapes/b2polygonshape.d:74-262) or b2CircleShape (b2circleshape.d). */
 int32_t dbox_fixture_create(dbox_world* w, int32_t world, int32_t body, const dbox_shape_def* shape,
                             const dbox_fixture_def* def, int32_t* out_fixture);
+/* b2Body.CreateFixture with a b2ChainShape (collision/shapes/b2chainshape.d): CreateChain(vertices,
+ * count) or, with loop != 0, CreateLoop; prev / next (may be NULL) are SetPrevVertex /
+ * SetNextVertex.  The chain is created as its child edges (b2ChainShape.GetChildEdge), one
+ * fixture index per child in child order, each with the chain's neighbour vertices as ghost
+ * vertices: the same proxies (ids in child order), pairs, contacts (a chain child first, no
+ * chain-edge or chain-chain contacts) and manifolds as the reference's chain.  A chain has no
+ * mass; its child edges are created with density 0.  out_first receives the first child's
+ * fixture index. */
+int32_t dbox_fixture_create_chain(dbox_world* w, int32_t world, int32_t body, const dbox_vec2* vertices, int32_t count,
+                                  int32_t loop, const dbox_vec2* prev_vertex, const dbox_vec2* next_vertex,
+                                  const dbox_fixture_def* def, int32_t* out_first);
 /* b2World.CreateJoint with a b2RevoluteJointDef (b2world.d:196-261, joints/b2revolutejoint.d). */
 int32_t dbox_joint_create_revolute(dbox_world* w, int32_t world, const dbox_revolute_def* def,
                                    int32_t* out_joint);

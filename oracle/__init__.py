@@ -45,6 +45,7 @@ def lib():
         L.orc_world_destroy.argtypes = [vp]
         L.orc_scene_create.argtypes = [vp, i32, vp, i32, vp, vp, vp, i32, vp]
         L.orc_joint_create_distance.argtypes = [vp, vp]
+        L.orc_fixture_create_chain.argtypes = [vp, i32, vp, i32, i32, vp, vp, vp]
         L.orc_joint_create_rope.argtypes = [vp, vp]
         L.orc_joint_create_weld.argtypes = [vp, vp]
         L.orc_joint_create_friction.argtypes = [vp, vp]
@@ -121,6 +122,10 @@ class OracleWorld:
                                 len(j), abi.ptr(j) if len(j) else None)
         if rc != 0:
             raise ValueError("oracle scene creation failed")
+        for c in scene.get("chains", ()):
+            fd = abi.fixture_defs(1)[0]
+            fd["friction"] = c.get("friction", 0.2)
+            self.create_chain(c["body"], c["vertices"], c["loop"], c.get("prev"), c.get("next"), fd)
         # joint kinds after the revolute joints, in this order (the same as the library's)
         for key, dtype, fn in (("distance_joints", abi.DISTANCE_DEF, L.orc_joint_create_distance),
                                ("rope_joints", abi.ROPE_DEF, L.orc_joint_create_rope),
@@ -169,6 +174,21 @@ class OracleWorld:
 
     def last_islands(self):
         return lib().orc_world_last_islands(self.h)
+
+    def create_chain(self, body, vertices, loop=False, prev=None, next=None, fixture=None):
+        """b2Body.CreateFixture with a b2ChainShape, created as its child edges; returns the
+        first child's fixture index."""
+        v = np.ascontiguousarray(vertices, np.float32)
+        pv = np.ascontiguousarray(prev, np.float32) if prev is not None else None
+        nv = np.ascontiguousarray(next, np.float32) if next is not None else None
+        fd = fixture if fixture is not None else abi.fixture_defs(1)[0]
+        fd = np.ascontiguousarray(np.array([fd], abi.FIXTURE_DEF))
+        r = lib().orc_fixture_create_chain(self.h, body, abi.ptr(v), len(v), 1 if loop else 0,
+                                           abi.ptr(pv) if pv is not None else None,
+                                           abi.ptr(nv) if nv is not None else None, abi.ptr(fd))
+        if r < 0:
+            raise ValueError("oracle chain creation failed")
+        return r
 
     def set_mouse_target(self, joint, target):
         """b2MouseJoint.SetTarget (b2mousejoint.d:83-91)."""

@@ -4830,6 +4830,45 @@ int orc_fixture_create(orc_world* w, int body, const dbox_shape_def* shape, cons
     return w->w.CreateFixture(w->w.bodiesByIndex[body], s, def)->index;
 }
 
+// b2Body.CreateFixture with a b2ChainShape (b2chainshape.d: CreateChain / CreateLoop,
+// SetPrevVertex / SetNextVertex) as its child edges (GetChildEdge), in child order
+int orc_fixture_create_chain(orc_world* w, int body, const dbox_vec2* vertices, int count, int loop,
+                             const dbox_vec2* prev, const dbox_vec2* next, const dbox_fixture_def* def) {
+    if (body < 0 || body >= (int)w->w.bodiesByIndex.size() || count < (loop ? 3 : 2)) return -1;
+    std::vector<Vec2> v;
+    for (int i = 0; i < count; ++i) v.push_back(Vec2(vertices[i].x, vertices[i].y));
+    bool hasPrev = !loop && prev, hasNext = !loop && next;
+    Vec2 pv = hasPrev ? Vec2(prev->x, prev->y) : Vec2(0.0f, 0.0f);
+    Vec2 nv = hasNext ? Vec2(next->x, next->y) : Vec2(0.0f, 0.0f);
+    if (loop) {
+        v.push_back(v[0]);
+        pv = v[v.size() - 2];
+        nv = v[1];
+        hasPrev = hasNext = true;
+    }
+    dbox_fixture_def d = *def;
+    d.density = 0.0f;                                                   // a chain has no mass
+    int first = -1;
+    const int m = (int)v.size();
+    for (int i = 0; i + 1 < m; ++i) {
+        Shape s;
+        s.type = kEdge;
+        s.radius = kPolygonRadius;
+        s.count = 2;
+        s.vertices[0] = v[i];
+        s.vertices[1] = v[i + 1];
+        if (i > 0) { s.vertex0 = v[i - 1]; s.hasVertex0 = true; }
+        else { s.vertex0 = pv; s.hasVertex0 = hasPrev; }
+        if (i < m - 2) { s.vertex3 = v[i + 2]; s.hasVertex3 = true; }
+        else { s.vertex3 = nv; s.hasVertex3 = hasNext; }
+        if (!s.hasVertex0) s.vertex0.SetZero();
+        if (!s.hasVertex3) s.vertex3.SetZero();
+        int idx = w->w.CreateFixture(w->w.bodiesByIndex[body], s, &d)->index;
+        if (first < 0) first = idx;
+    }
+    return first;
+}
+
 int orc_joint_create_revolute(orc_world* w, const dbox_revolute_def* def) {
     int n = (int)w->w.bodiesByIndex.size();
     if (def->body_a < 0 || def->body_a >= n || def->body_b < 0 || def->body_b >= n || def->body_a == def->body_b) return -1;

@@ -35,6 +35,8 @@ void orc_world_destroy(orc_world* w);
 int orc_body_create(orc_world* w, const dbox_body_def* def);
 int orc_fixture_create(orc_world* w, int body, const dbox_shape_def* shape, const dbox_fixture_def* def);
 int orc_joint_create_revolute(orc_world* w, const dbox_revolute_def* def);
+int orc_fixture_create_chain(orc_world* w, int body, const dbox_vec2* vertices, int count, int loop,
+                             const dbox_vec2* prev, const dbox_vec2* next, const dbox_fixture_def* def);
 int orc_joint_create_distance(orc_world* w, const dbox_distance_def* def);
 int orc_joint_create_rope(orc_world* w, const dbox_rope_def* def);
 int orc_joint_create_weld(orc_world* w, const dbox_weld_def* def);

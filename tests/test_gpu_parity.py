@@ -315,3 +315,22 @@ def test_edge_shapes_exact(oracle_lib, gpu_lib):
             for i, ow in enumerate(ows):
                 d = exact_diff(ow.export_state(), gw.export_state(i))
                 assert not d, "world %d step %d: %s" % (i, t + 1, d[:6])
+
+
+def test_chain_shapes_exact(oracle_lib, gpu_lib):
+    # chain shapes (a loop bowl, open chains with and without prev/next ghosts, a loop on a
+    # dynamic body) created as their child edges after the scene's fixtures: bit-exact
+    # against the oracle
+    from dbox_gb300 import scenes
+    oracle_lib.set_trig_mode(1)
+    worlds = [scenes.chain_ground(), scenes.chain_ground(n=24, seed=29)]
+    gw = gpu_lib.World(worlds)
+    ows = [oracle_lib.OracleWorld(s) for s in worlds]
+    for t in range(240):
+        gw.step()
+        for ow in ows:
+            ow.step()
+        if t % 30 == 29:
+            for i, ow in enumerate(ows):
+                d = exact_diff(ow.export_state(), gw.export_state(i))
+                assert not d, "world %d step %d: %s" % (i, t + 1, d[:6])

@@ -326,3 +326,27 @@ def test_edge_shapes_collide(oracle_lib):
     assert np.isfinite(b["xf"]).all() and b["xf"][dyn, 1].min() > -0.05
     pyr = slice(1 + 1 + 1, 1 + 1 + 1 + 21)                    # ground, two ramps, then the 6-row pyramid
     assert np.abs(b["sweep"][pyr, 7]).max() < 0.05             # still standing
+
+
+def test_chain_shapes_collide(oracle_lib):
+    # b2ChainShape as its child edges (GetChildEdge ghosts; CreateLoop closes the bowl):
+    # bodies dropped into the loop bowl stay in it, the valley chain and the open chain carry
+    # their bodies, every chain contact has the chain child as fixture A, and the carrier's
+    # loop chain adds no mass
+    from dbox_gb300 import scenes
+    oracle_lib.set_trig_mode(1)
+    s = scenes.chain_ground()
+    n_fix = len(s["fixtures"])
+    ow = oracle_lib.OracleWorld(s)
+    ow.step(steps=300)
+    st = ow.export_state()
+    b, c = st["bodies"], st["contacts"]
+    children = 20 + 11 + 2 + 4                                 # loop of 20 vertices, chains of 12 and 3, loop of 4
+    assert c["fixture_a"].max() < n_fix + children
+    chain_c = c[(c["fixture_a"] >= n_fix) | (c["fixture_b"] >= n_fix)]
+    assert len(chain_c) and (chain_c["fixture_a"] >= n_fix).all()
+    assert not ((c["fixture_a"] >= n_fix) & (c["fixture_b"] >= n_fix)).any()
+    dyn = b["type"] == 2
+    assert np.isfinite(b["xf"]).all()
+    assert b["xf"][dyn, 1].min() > 0.5                         # nothing fell through a chain (lowest at y = 1)
+    assert (chain_c["point_count"] > 0).sum() > 10
