@@ -57,6 +57,10 @@ def lib():
     L.dbox_joint_create_pulley.argtypes = [vp, i32, vp, ctypes.POINTER(i32)]
     L.dbox_joint_create_mouse.argtypes = [vp, i32, vp, ctypes.POINTER(i32)]
     L.dbox_joint_set_mouse_target.argtypes = [vp, i32, i32, abi.Vec2]
+    L.dbox_world_query_aabb.argtypes = [vp, i32, vp, vp, i32, vp, vp]
+    L.dbox_world_raycast.argtypes = [vp, i32, vp, vp, vp, i32, i32, vp, vp]
+    L.dbox_world_query_aabb_device.argtypes = [vp, i32, vp, vp, i32, vp, vp]
+    L.dbox_world_raycast_device.argtypes = [vp, i32, vp, vp, vp, i32, i32, vp, vp]
     L.dbox_world_set_flags.argtypes = [vp, i32, i32, i32, i32, i32]
     L.dbox_world_set_gravity.argtypes = [vp, abi.Vec2]
     L.dbox_world_step.argtypes = [vp, f32, i32, i32]
@@ -296,6 +300,44 @@ class World:
                                                abi.ptr(nv) if nv is not None else None, abi.ptr(fd), ctypes.byref(out)),
                "dbox_fixture_create_chain")
         return out.value
+
+    def query_aabb(self, worlds, boxes, capacity=64):
+        """b2World.QueryAABB for a batch: boxes (n, 4) = lower x, y, upper x, y, one per entry of
+        `worlds`.  Returns (counts (n,), fixtures (n, capacity)): every fixture whose fat AABB
+        overlaps, in fixture order; counts may exceed capacity (the rest is dropped)."""
+        wv = np.ascontiguousarray(np.broadcast_to(np.asarray(worlds, np.int32), (len(boxes),)))
+        bv = np.ascontiguousarray(boxes, np.float32).reshape(-1, 4)
+        counts = np.zeros(len(bv), np.int32)
+        out = np.full((len(bv), capacity), -1, np.int32)
+        _check(lib().dbox_world_query_aabb(self.h, len(bv), abi.ptr(wv), abi.ptr(bv), capacity, abi.ptr(counts),
+                                           abi.ptr(out)), "dbox_world_query_aabb")
+        return counts, out
+
+    def raycast(self, worlds, p1, p2, mode="closest", capacity=None):
+        """b2World.RayCast for a batch of rays p1 -> p2 (n, 2).  mode "closest": the hit with the
+        smallest fraction (capacity 1); "all": every hit in fixture order.  Returns (counts,
+        hits (n, capacity) of abi.RAY_HIT)."""
+        m = abi.RAY_CLOSEST if mode == "closest" else abi.RAY_ALL
+        cap = capacity if capacity is not None else (1 if m == abi.RAY_CLOSEST else 32)
+        a = np.ascontiguousarray(p1, np.float32).reshape(-1, 2)
+        b = np.ascontiguousarray(p2, np.float32).reshape(-1, 2)
+        wv = np.ascontiguousarray(np.broadcast_to(np.asarray(worlds, np.int32), (len(a),)))
+        counts = np.zeros(len(a), np.int32)
+        hits = np.zeros((len(a), cap), abi.RAY_HIT)
+        hits["fixture"] = -1
+        _check(lib().dbox_world_raycast(self.h, len(a), abi.ptr(wv), abi.ptr(a), abi.ptr(b), m, cap, abi.ptr(counts),
+                                        abi.ptr(hits)), "dbox_world_raycast")
+        return counts, hits
+
+    def query_aabb_device(self, n, worlds_ptr, boxes_ptr, capacity, counts_ptr, out_ptr):
+        """dbox_world_query_aabb_device on device addresses (ints), enqueued without a wait."""
+        _check(lib().dbox_world_query_aabb_device(self.h, n, worlds_ptr, boxes_ptr, capacity, counts_ptr, out_ptr),
+               "dbox_world_query_aabb_device")
+
+    def raycast_device(self, n, worlds_ptr, p1_ptr, p2_ptr, mode, capacity, counts_ptr, hits_ptr):
+        """dbox_world_raycast_device on device addresses (ints), enqueued without a wait."""
+        _check(lib().dbox_world_raycast_device(self.h, n, worlds_ptr, p1_ptr, p2_ptr, mode, capacity, counts_ptr,
+                                               hits_ptr), "dbox_world_raycast_device")
 
     def set_mouse_target(self, world, joint, target):
         """b2MouseJoint.SetTarget: wakes the dragged body and moves the target."""

@@ -102,6 +102,9 @@ BODY_STATE = np.dtype([
 ])
 assert BODY_STATE.itemsize == 104
 
+RAY_HIT = np.dtype([("fixture", "<i4"), ("fraction", "<f4"), ("point", "<f4", 2), ("normal", "<f4", 2)])
+RAY_CLOSEST = 0
+RAY_ALL = 1
 PROXY_STATE = np.dtype([("fat_aabb", "<f4", 4), ("moved", "<i4"), ("proxy_id", "<i4")])
 assert PROXY_STATE.itemsize == 24
 

@@ -14,7 +14,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libdbox_gpu.so")
-SOURCES = [os.path.join(CSRC, "step.cu"), os.path.join(CSRC, "api.cu"), os.path.join(CSRC, "mlp.cu")]
+SOURCES = [os.path.join(CSRC, "step.cu"), os.path.join(CSRC, "api.cu"), os.path.join(CSRC, "mlp.cu"),
+           os.path.join(CSRC, "query.cu")]
 HEADERS = [os.path.join(CSRC, n) for n in os.listdir(CSRC) if n.endswith((".h", ".cuh"))] + [
     os.path.join(HERE, "..", "include", "dbox_gpu.h")]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"

@@ -25,6 +25,32 @@ const dg::MlpDev* dbox_mlp_device_view(const dbox_mlp* m, dg::MlpDev* out);
 extern "C" int dbox_launch_step_ev(const dg::Ctx* x, cudaStream_t stream, int* launches, cudaEvent_t* ev);
 extern "C" int dbox_launch_gather_transforms(int n, const dbox_body_state* bs, float* out, cudaStream_t s);
 extern "C" int dbox_launch_apply_forces(int n, dbox_body_state* bs, const float* f, cudaStream_t s);
+struct dbox_query_buffers {
+    int W;
+    const dg::WorldInfo* wi;
+    const dg::DFixture* fx;
+    const dbox_proxy_state* px;
+    const dbox_body_state* bs;
+    float4* box;
+    int* idx;
+    float4* bucket;
+    float4* group;
+    int* live;
+    unsigned* key0;
+    unsigned* key1;
+    int* sidx0;
+    int* sidx1;
+    unsigned* bitmap;
+    int bm_words;
+    int query_blocks;
+};
+extern "C" int dbox_launch_query_build(const dbox_query_buffers* b, cudaStream_t s);
+extern "C" int dbox_launch_query_aabb(const dbox_query_buffers* b, int n, const int* world, const dbox_aabb* boxes,
+                                      int cap, int* counts, int* out, cudaStream_t s);
+extern "C" int dbox_launch_raycast(const dbox_query_buffers* b, int n, const int* world, const dbox_vec2* p1,
+                                   const dbox_vec2* p2, int mode, int cap, int* counts, dbox_ray_hit* out,
+                                   cudaStream_t s);
+extern "C" int dbox_query_warps_per_block();
 extern "C" int dbox_launch_collide_pairs(int n, const dg::DFixture* fa, const float4* xa, const dg::DFixture* fb,
                                          const float4* xb, dbox_contact_state* out, cudaStream_t stream);
 
@@ -166,6 +192,14 @@ struct dbox_world {
     int t_steps = -1;
     float t_dt = -1.0f;
     int t_vi = -1, t_pi = -1, t_flags = -1;
+    // world queries: the device index of the broad-phase's fat AABBs
+    unsigned long long gen = 0;         // bumped before any device work that may move proxies
+    unsigned long long q_gen = ~0ull;   // gen the index was built at
+    DBuf<float4> q_box, q_bucket, q_group;
+    DBuf<int> q_idx, q_live, q_sidx0, q_sidx1;
+    DBuf<unsigned> q_key0, q_key1, q_bitmap;
+    int q_bm_words = 0, q_blocks = 0;
+    DBuf<unsigned char> q_in, q_out;    // staging of the host-buffer query calls
 };
 
 namespace {
@@ -183,6 +217,11 @@ void free_device(dbox_world* w) {
     w->s_isl_minsep.free(); w->s_isl_sleep.free();
     w->d_vr.free(); w->d_tvr.free(); w->d_pr.free(); w->d_tpr.free(); w->d_snap.free(); w->d_io.free();
     w->s_vpos.free(); w->d_solve_world.free(); w->d_solve_smem.free();
+    w->q_box.free(); w->q_bucket.free(); w->q_group.free(); w->q_idx.free(); w->q_live.free(); w->q_sidx0.free();
+    w->q_sidx1.free(); w->q_key0.free(); w->q_key1.free(); w->q_bitmap.free(); w->q_in.free(); w->q_out.free();
+    w->q_bm_words = 0;
+    w->q_blocks = 0;
+    w->q_gen = ~0ull;
     w->d_solve_order.free(); w->d_solve_queue.free();
     w->s_feat.free(); w->s_vsave.free(); w->s_slog.free(); w->s_pend.free();
     w->d_events.free(); w->s_cevt.free();
@@ -545,6 +584,7 @@ int upload(dbox_world* w) {
 
 int ensure_device(dbox_world* w) {
     w->mirrors_fresh = false;              // device work follows
+    ++w->gen;                              // and may move proxies: the query index goes stale
     if (w->dirty || !w->on_device) {
         int rc = download(w);
         if (rc) return rc;
@@ -1910,6 +1950,144 @@ int32_t dbox_world_import_state(dbox_world* w, int32_t world, const dbox_world_h
     hw.wd.step_complete = header->step_complete;
     hw.wd.inv_dt0 = header->inv_dt0;
     hw.wd.contact_count = header->contact_count;
+    return DBOX_OK;
+}
+
+// ---------------------------------------------------------------- world queries
+// The device index of the fat AABBs (query.cu), rebuilt when device work ran since the last build.
+static int query_prepare(dbox_world* w, dbox_query_buffers* b) {
+    if (w->dirty || !w->on_device) {
+        int rc = ensure_device(w);
+        if (rc) return rc;
+    }
+    const int W = (int)w->worlds.size();
+    const int nf = w->total_fixtures;
+    int maxnf = 0;
+    for (auto& hw : w->worlds) maxnf = std::max(maxnf, (int)hw.fx.size());
+    const int words = std::max(1, (maxnf + 31) / 32);
+    if (w->nsm <= 0) {
+        int dev = 0;
+        CU(cudaGetDevice(&dev));
+        CU(cudaDeviceGetAttribute(&w->nsm, cudaDevAttrMultiProcessorCount, dev));
+    }
+    const int blocks = std::max(1, w->nsm * 8);
+    if (w->q_box.n != (size_t)nf || w->q_live.n != (size_t)W) {
+        if (w->q_box.alloc(nf) || w->q_idx.alloc(nf) || w->q_sidx0.alloc(nf) || w->q_sidx1.alloc(nf) ||
+            w->q_key0.alloc(nf) || w->q_key1.alloc(nf) || w->q_bucket.alloc((size_t)nf / 32 + W + 2) ||
+            w->q_group.alloc((size_t)nf / 1024 + W + 2) || w->q_live.alloc(W))
+            return fail(DBOX_ERR_CUDA, "query index: out of device memory");
+        w->q_gen = ~0ull;
+    }
+    if (w->q_bm_words < words || w->q_blocks != blocks) {
+        const size_t n = (size_t)blocks * dbox_query_warps_per_block() * words;
+        if (w->q_bitmap.alloc(n)) return fail(DBOX_ERR_CUDA, "query bitmaps: out of device memory");
+        CU(cudaMemsetAsync(w->q_bitmap.p, 0, n * sizeof(unsigned), w->stream));
+        w->q_bm_words = words;
+        w->q_blocks = blocks;
+    }
+    b->W = W;
+    b->wi = w->d_wi.p;
+    b->fx = w->d_fx.p;
+    b->px = w->d_px.p;
+    b->bs = w->d_bs.p;
+    b->box = w->q_box.p;
+    b->idx = w->q_idx.p;
+    b->bucket = w->q_bucket.p;
+    b->group = w->q_group.p;
+    b->live = w->q_live.p;
+    b->key0 = w->q_key0.p;
+    b->key1 = w->q_key1.p;
+    b->sidx0 = w->q_sidx0.p;
+    b->sidx1 = w->q_sidx1.p;
+    b->bitmap = w->q_bitmap.p;
+    b->bm_words = w->q_bm_words;
+    b->query_blocks = w->q_blocks;
+    if (w->q_gen != w->gen) {
+        int err = dbox_launch_query_build(b, w->stream);
+        if (err) return fail(DBOX_ERR_CUDA, "query index build: %s", cudaGetErrorString((cudaError_t)err));
+        w->q_gen = w->gen;
+    }
+    return DBOX_OK;
+}
+
+int32_t dbox_world_query_aabb_device(dbox_world* w, int32_t n, const int32_t* world, const dbox_aabb* boxes,
+                                     int32_t capacity, int32_t* counts, int32_t* fixtures) {
+    if (!w || n < 0 || capacity < 0 || (n > 0 && (!world || !boxes || !counts || (capacity > 0 && !fixtures))))
+        return fail(DBOX_ERR_INVALID, "dbox_world_query_aabb: bad arguments");
+    dbox_query_buffers b;
+    int rc = query_prepare(w, &b);
+    if (rc) return rc;
+    int err = dbox_launch_query_aabb(&b, n, world, boxes, capacity, counts, fixtures, w->stream);
+    if (err) return fail(DBOX_ERR_CUDA, "query launch: %s", cudaGetErrorString((cudaError_t)err));
+    return DBOX_OK;
+}
+
+int32_t dbox_world_raycast_device(dbox_world* w, int32_t n, const int32_t* world, const dbox_vec2* p1,
+                                  const dbox_vec2* p2, int32_t mode, int32_t capacity, int32_t* counts,
+                                  dbox_ray_hit* hits) {
+    if (!w || n < 0 || (mode != DBOX_RAY_CLOSEST && mode != DBOX_RAY_ALL) || capacity < 0 ||
+        (mode == DBOX_RAY_CLOSEST && capacity < 1) || (n > 0 && (!world || !p1 || !p2 || !counts || (capacity > 0 && !hits))))
+        return fail(DBOX_ERR_INVALID, "dbox_world_raycast: bad arguments");
+    dbox_query_buffers b;
+    int rc = query_prepare(w, &b);
+    if (rc) return rc;
+    int err = dbox_launch_raycast(&b, n, world, p1, p2, mode, capacity, counts, hits, w->stream);
+    if (err) return fail(DBOX_ERR_CUDA, "ray cast launch: %s", cudaGetErrorString((cudaError_t)err));
+    return DBOX_OK;
+}
+
+// host-buffer forms: inputs packed into one upload, outputs read back in one copy each
+static int query_stage(dbox_world* w, size_t in_bytes, size_t out_bytes) {
+    if (w->q_in.n < in_bytes && w->q_in.alloc(in_bytes)) return fail(DBOX_ERR_CUDA, "query staging: out of device memory");
+    if (w->q_out.n < out_bytes && w->q_out.alloc(out_bytes)) return fail(DBOX_ERR_CUDA, "query staging: out of device memory");
+    return DBOX_OK;
+}
+
+static size_t align16(size_t v) { return (v + 15) & ~(size_t)15; }
+
+int32_t dbox_world_query_aabb(dbox_world* w, int32_t n, const int32_t* world, const dbox_aabb* boxes,
+                              int32_t capacity, int32_t* counts, int32_t* fixtures) {
+    if (!w || n < 0 || capacity < 0 || (n > 0 && (!world || !boxes || !counts || (capacity > 0 && !fixtures))))
+        return fail(DBOX_ERR_INVALID, "dbox_world_query_aabb: bad arguments");
+    if (n == 0) return DBOX_OK;
+    const size_t sw = align16(sizeof(int32_t) * n), sb = sizeof(dbox_aabb) * (size_t)n;
+    const size_t sc = align16(sizeof(int32_t) * n), so = sizeof(int32_t) * (size_t)n * capacity;
+    int rc = query_stage(w, sw + sb, sc + so);
+    if (rc) return rc;
+    unsigned char* in = w->q_in.p;
+    unsigned char* out = w->q_out.p;
+    CU(cudaMemcpyAsync(in, world, sizeof(int32_t) * n, cudaMemcpyHostToDevice, w->stream));
+    CU(cudaMemcpyAsync(in + sw, boxes, sb, cudaMemcpyHostToDevice, w->stream));
+    rc = dbox_world_query_aabb_device(w, n, (const int32_t*)in, (const dbox_aabb*)(in + sw), capacity, (int32_t*)out,
+                                      (int32_t*)(out + sc));
+    if (rc) return rc;
+    CU(cudaMemcpyAsync(counts, out, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, w->stream));
+    if (so) CU(cudaMemcpyAsync(fixtures, out + sc, so, cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
+    return DBOX_OK;
+}
+
+int32_t dbox_world_raycast(dbox_world* w, int32_t n, const int32_t* world, const dbox_vec2* p1, const dbox_vec2* p2,
+                           int32_t mode, int32_t capacity, int32_t* counts, dbox_ray_hit* hits) {
+    if (!w || n < 0 || (mode != DBOX_RAY_CLOSEST && mode != DBOX_RAY_ALL) || capacity < 0 ||
+        (mode == DBOX_RAY_CLOSEST && capacity < 1) || (n > 0 && (!world || !p1 || !p2 || !counts || (capacity > 0 && !hits))))
+        return fail(DBOX_ERR_INVALID, "dbox_world_raycast: bad arguments");
+    if (n == 0) return DBOX_OK;
+    const size_t sw = align16(sizeof(int32_t) * n), sp = align16(sizeof(dbox_vec2) * (size_t)n);
+    const size_t sc = align16(sizeof(int32_t) * n), so = sizeof(dbox_ray_hit) * (size_t)n * capacity;
+    int rc = query_stage(w, sw + 2 * sp, sc + so);
+    if (rc) return rc;
+    unsigned char* in = w->q_in.p;
+    unsigned char* out = w->q_out.p;
+    CU(cudaMemcpyAsync(in, world, sizeof(int32_t) * n, cudaMemcpyHostToDevice, w->stream));
+    CU(cudaMemcpyAsync(in + sw, p1, sizeof(dbox_vec2) * (size_t)n, cudaMemcpyHostToDevice, w->stream));
+    CU(cudaMemcpyAsync(in + sw + sp, p2, sizeof(dbox_vec2) * (size_t)n, cudaMemcpyHostToDevice, w->stream));
+    rc = dbox_world_raycast_device(w, n, (const int32_t*)in, (const dbox_vec2*)(in + sw), (const dbox_vec2*)(in + sw + sp),
+                                   mode, capacity, (int32_t*)out, (dbox_ray_hit*)(out + sc));
+    if (rc) return rc;
+    CU(cudaMemcpyAsync(counts, out, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, w->stream));
+    if (so) CU(cudaMemcpyAsync(hits, out + sc, so, cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaStreamSynchronize(w->stream));
     return DBOX_OK;
 }
 

@@ -34,6 +34,12 @@ extern "C" {
 
 /* ---------------------------------------------------------------- types */
 typedef struct { float x, y; } dbox_vec2;
+/* b2AABB (collision/b2collision.d:300-345) */
+typedef struct { dbox_vec2 lower, upper; } dbox_aabb;
+/* One ray hit: the fixture, b2RayCastOutput.fraction, the point (1 - fraction) p1 + fraction p2
+ * and b2RayCastOutput.normal, as b2WorldRayCastWrapper hands them to ReportFixture
+ * (dynamics/b2world.d:1605-1629). */
+typedef struct { int32_t fixture; float fraction; dbox_vec2 point, normal; } dbox_ray_hit;
 
 /* b2BodyType (dynamics/b2body.d:34-42) */
 #define DBOX_STATIC_BODY 0
@@ -414,6 +420,35 @@ int32_t dbox_world_sync(dbox_world* w);
 
 /* Islands solved and TOI events handled by world `world` in the last step. */
 int32_t dbox_world_step_stats(dbox_world* w, int32_t world, int32_t* islands, int32_t* toi_events);
+
+/* ---- World queries, batched (b2World.QueryAABB b2world.d:563-569, b2World.RayCast
+ * b2world.d:577-587, over b2DynamicTree.Query / RayCast b2dynamictree.d:203-331).
+ * Each query names its world.  The broad-phase's fat AABBs are indexed on the device by a
+ * Morton-ordered 32-ary bounding-volume hierarchy, rebuilt on the first query after any
+ * step or edit.  The reference reports fixtures in the order of its tree walk and lets the
+ * callback stop or clip the walk; here the results are the callback-independent forms:
+ *   QueryAABB: every fixture whose fat AABB overlaps the box (b2TestOverlap), in
+ *              fixture order (a callback that returns true for each);
+ *   RayCast DBOX_RAY_ALL: every fixture the ray hits (b2Fixture.RayCast with maxFraction 1,
+ *              the callback returning 1), in fixture order;
+ *   RayCast DBOX_RAY_CLOSEST: the hit with the smallest fraction, the lower fixture index on
+ *              a tie (the closest-hit callback that returns the fraction).
+ * counts[q] receives the number of results of query q (it may exceed capacity; results
+ * beyond capacity are dropped; -1: the query names no world, or p1 == p2 for a ray, where
+ * the reference asserts); results of query q start at q * capacity, and entries past
+ * min(count, capacity) are unspecified. */
+#define DBOX_RAY_CLOSEST 0
+#define DBOX_RAY_ALL 1
+int32_t dbox_world_query_aabb(dbox_world* w, int32_t n, const int32_t* world, const dbox_aabb* boxes,
+                              int32_t capacity, int32_t* counts, int32_t* fixtures);
+int32_t dbox_world_raycast(dbox_world* w, int32_t n, const int32_t* world, const dbox_vec2* p1, const dbox_vec2* p2,
+                           int32_t mode, int32_t capacity, int32_t* counts, dbox_ray_hit* hits);
+/* The same with every array in device memory: enqueued on the handle's stream, no wait. */
+int32_t dbox_world_query_aabb_device(dbox_world* w, int32_t n, const int32_t* world, const dbox_aabb* boxes,
+                                     int32_t capacity, int32_t* counts, int32_t* fixtures);
+int32_t dbox_world_raycast_device(dbox_world* w, int32_t n, const int32_t* world, const dbox_vec2* p1,
+                                  const dbox_vec2* p2, int32_t mode, int32_t capacity, int32_t* counts,
+                                  dbox_ray_hit* hits);
 
 /* Narrowphase alone: the manifolds of n shape pairs at transforms xf = (p.x, p.y, sin, cos), 4 floats
  * per pair, computed on the GPU (b2CollidePolygons collision/b2collidepolygon.d:127-254,

@@ -46,6 +46,8 @@ def lib():
         L.orc_scene_create.argtypes = [vp, i32, vp, i32, vp, vp, vp, i32, vp]
         L.orc_joint_create_distance.argtypes = [vp, vp]
         L.orc_fixture_create_chain.argtypes = [vp, i32, vp, i32, i32, vp, vp, vp]
+        L.orc_query_aabb.argtypes = [vp, f32, f32, f32, f32, vp, i32]
+        L.orc_raycast.argtypes = [vp, f32, f32, f32, f32, i32, vp, i32]
         L.orc_joint_create_rope.argtypes = [vp, vp]
         L.orc_joint_create_weld.argtypes = [vp, vp]
         L.orc_joint_create_friction.argtypes = [vp, vp]
@@ -189,6 +191,25 @@ class OracleWorld:
         if r < 0:
             raise ValueError("oracle chain creation failed")
         return r
+
+    def query_aabb(self, box, capacity=4096):
+        """b2World.QueryAABB through the oracle's dynamic tree: the fixtures whose fat AABB
+        overlaps box = (lower x, y, upper x, y), sorted by fixture index."""
+        out = np.zeros(capacity, np.int32)
+        n = lib().orc_query_aabb(self.h, *[float(v) for v in box], abi.ptr(out), capacity)
+        return out[:min(n, capacity)].copy()
+
+    def raycast(self, p1, p2, mode="closest", capacity=4096):
+        """b2World.RayCast through the oracle's dynamic tree.  mode "closest": the smallest
+        fraction over all hits (lower fixture index on a tie); "all": every hit in fixture
+        order; "clip": the reference's clipping closest-hit callback as it runs.  Returns an
+        array of abi.RAY_HIT (None for p1 == p2)."""
+        m = {"closest": 0, "all": 1, "clip": 2}[mode]
+        out = np.zeros(capacity, abi.RAY_HIT)
+        n = lib().orc_raycast(self.h, float(p1[0]), float(p1[1]), float(p2[0]), float(p2[1]), m, abi.ptr(out), capacity)
+        if n < 0:
+            return None
+        return out[:min(n, capacity)].copy()
 
     def set_mouse_target(self, joint, target):
         """b2MouseJoint.SetTarget (b2mousejoint.d:83-91)."""

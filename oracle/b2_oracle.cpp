@@ -1660,6 +1660,48 @@ struct DynamicTree {
             }
         }
     }
+    // b2dynamictree.d:246-331: callback->RayCastCallback(p1, p2, maxFraction, proxyId) returns
+    // 0 to stop, a positive value to clip the ray to it, a negative one to go on unchanged
+    template <class CB> void RayCast(CB* callback, Vec2 p1, Vec2 p2, f32 inputMaxFraction) const {
+        Vec2 r = p2 - p1;
+        r.Normalize();
+        Vec2 v = Cross(1.0f, r);
+        Vec2 abs_v(Abs(v.x), Abs(v.y));
+        f32 maxFraction = inputMaxFraction;
+        AABB segmentAABB;
+        {
+            Vec2 t = p1 + maxFraction * (p2 - p1);
+            segmentAABB.lowerBound = Min(p1, t);
+            segmentAABB.upperBound = Max(p1, t);
+        }
+        std::vector<int> stack;
+        stack.reserve(256);
+        stack.push_back(root);
+        while (!stack.empty()) {
+            int nodeId = stack.back();
+            stack.pop_back();
+            if (nodeId == kNullNode) continue;
+            const TreeNode* node = &nodes[nodeId];
+            if (!TestOverlap(node->aabb, segmentAABB)) continue;
+            Vec2 c = 0.5f * (node->aabb.lowerBound + node->aabb.upperBound);
+            Vec2 h = 0.5f * (node->aabb.upperBound - node->aabb.lowerBound);
+            f32 separation = Abs(Dot(v, p1 - c)) - Dot(abs_v, h);
+            if (separation > 0.0f) continue;
+            if (node->IsLeaf()) {
+                f32 value = callback->RayCastCallback(p1, p2, maxFraction, nodeId);
+                if (value == 0.0f) return;
+                if (value > 0.0f) {
+                    maxFraction = value;
+                    Vec2 t = p1 + maxFraction * (p2 - p1);
+                    segmentAABB.lowerBound = Min(p1, t);
+                    segmentAABB.upperBound = Max(p1, t);
+                }
+            } else {
+                stack.push_back(node->child1);
+                stack.push_back(node->child2);
+            }
+        }
+    }
     void InsertLeaf(int leaf) {                                         // b2dynamictree.d:566-708
         if (root == kNullNode) {
             root = leaf;
@@ -4802,7 +4844,165 @@ using namespace orc;
 
 struct orc_world { World w; };
 
+// ------------------------------------------------------------ world queries
+// Shape ray casts (b2RayCastInput p1, p2, maxFraction -> fraction, normal).
+static bool RayCastCircle(const Shape& s, const Transform& xf, Vec2 p1, Vec2 p2, f32 maxFraction, f32* fraction,
+                          Vec2* normal) {                               // b2circleshape.d:72-104
+    Vec2 position = xf.p + Mul(xf.q, s.p);
+    Vec2 d = p1 - position;
+    f32 b = Dot(d, d) - s.radius * s.radius;
+    Vec2 r = p2 - p1;
+    f32 c = Dot(d, r);
+    f32 rr = Dot(r, r);
+    f32 sigma = c * c - rr * b;
+    if (sigma < 0.0f || rr < kEpsilon) return false;
+    f32 a = -(c + sqrtf(sigma));
+    if (0.0f <= a && a <= maxFraction * rr) {
+        a /= rr;
+        *fraction = a;
+        *normal = d + a * r;
+        normal->Normalize();
+        return true;
+    }
+    return false;
+}
+
+static bool RayCastPolygon(const Shape& s, const Transform& xf, Vec2 rp1, Vec2 rp2, f32 maxFraction, f32* fraction,
+                           Vec2* normal) {                              // b2polygonshape.d:283-351
+    Vec2 p1 = MulT(xf.q, rp1 - xf.p);
+    Vec2 p2 = MulT(xf.q, rp2 - xf.p);
+    Vec2 d = p2 - p1;
+    f32 lower = 0.0f, upper = maxFraction;
+    int index = -1;
+    for (int i = 0; i < s.count; ++i) {
+        f32 numerator = Dot(s.normals[i], s.vertices[i] - p1);
+        f32 denominator = Dot(s.normals[i], d);
+        if (denominator == 0.0f) {
+            if (numerator < 0.0f) return false;
+        } else if (denominator < 0.0f && numerator < lower * denominator) {
+            lower = numerator / denominator;                            // the segment enters this half-space
+            index = i;
+        } else if (denominator > 0.0f && numerator < upper * denominator) {
+            upper = numerator / denominator;                            // the segment leaves it
+        }
+        if (upper < lower) return false;
+    }
+    if (index >= 0) {
+        *fraction = lower;
+        *normal = Mul(xf.q, s.normals[index]);
+        return true;
+    }
+    return false;
+}
+
+static bool RayCastEdge(const Shape& s, const Transform& xf, Vec2 rp1, Vec2 rp2, f32 maxFraction, f32* fraction,
+                        Vec2* normal) {                                 // b2edgeshape.d:96-157
+    Vec2 p1 = MulT(xf.q, rp1 - xf.p);
+    Vec2 p2 = MulT(xf.q, rp2 - xf.p);
+    Vec2 d = p2 - p1;
+    Vec2 v1 = s.vertices[0], v2 = s.vertices[1];
+    Vec2 e = v2 - v1;
+    Vec2 n(e.y, -e.x);
+    n.Normalize();
+    f32 numerator = Dot(n, v1 - p1);
+    f32 denominator = Dot(n, d);
+    if (denominator == 0.0f) return false;
+    f32 t = numerator / denominator;
+    if (t < 0.0f || maxFraction < t) return false;
+    Vec2 q = p1 + t * d;
+    Vec2 r = v2 - v1;
+    f32 rr = Dot(r, r);
+    if (rr == 0.0f) return false;
+    f32 sv = Dot(q - v1, r) / rr;
+    if (sv < 0.0f || 1.0f < sv) return false;
+    *fraction = t;
+    Vec2 wn = Mul(xf.q, n);
+    *normal = numerator > 0.0f ? Vec2(-wn.x, -wn.y) : wn;
+    return true;
+}
+
+static bool RayCastFixture(const Fixture* f, Vec2 p1, Vec2 p2, f32 maxFraction, f32* fraction, Vec2* normal) {
+    const Transform& xf = f->body->xf;                                  // b2fixture.d:217-220
+    if (f->shape.type == kCircle) return RayCastCircle(f->shape, xf, p1, p2, maxFraction, fraction, normal);
+    if (f->shape.type == kEdge) return RayCastEdge(f->shape, xf, p1, p2, maxFraction, fraction, normal);
+    return RayCastPolygon(f->shape, xf, p1, p2, maxFraction, fraction, normal);
+}
+
+// b2World.QueryAABB (b2world.d:563-569) through b2WorldQueryWrapper (b2world.d:1592-1603) with a
+// callback that keeps every fixture reported
+struct QueryCollect {
+    const DynamicTree* tree;
+    std::vector<int> found;
+    bool QueryCallback(int proxyId) {
+        found.push_back(((const FixtureProxy*)tree->nodes[proxyId].userData)->fixture->index);
+        return true;
+    }
+};
+
+// b2World.RayCast (b2world.d:577-587) through b2WorldRayCastWrapper (b2world.d:1605-1629);
+// clip = true is the closest-hit callback (returns the fraction), false keeps every hit (returns 1)
+struct RayCollect {
+    const DynamicTree* tree;
+    bool clip;
+    std::vector<dbox_ray_hit> hits;
+    f32 RayCastCallback(Vec2 p1, Vec2 p2, f32 maxFraction, int proxyId) {
+        const Fixture* f = ((const FixtureProxy*)tree->nodes[proxyId].userData)->fixture;
+        f32 fraction;
+        Vec2 normal;
+        if (!RayCastFixture(f, p1, p2, maxFraction, &fraction, &normal)) return maxFraction;
+        Vec2 point = (1.0f - fraction) * p1 + fraction * p2;
+        dbox_ray_hit h;
+        h.fixture = f->index;
+        h.fraction = fraction;
+        h.point.x = point.x;
+        h.point.y = point.y;
+        h.normal.x = normal.x;
+        h.normal.y = normal.y;
+        if (clip) {
+            hits.assign(1, h);
+            return fraction;
+        }
+        hits.push_back(h);
+        return 1.0f;
+    }
+};
+
 extern "C" {
+
+// every fixture whose fat AABB overlaps [lower, upper], in fixture order; returns the count
+int orc_query_aabb(orc_world* w, float lx, float ly, float ux, float uy, int* out, int cap) {
+    QueryCollect cb;
+    cb.tree = &w->w.contactManager.broadPhase.tree;
+    AABB a;
+    a.lowerBound = Vec2(lx, ly);
+    a.upperBound = Vec2(ux, uy);
+    cb.tree->Query(&cb, a);
+    std::sort(cb.found.begin(), cb.found.end());
+    for (int i = 0; i < (int)cb.found.size() && i < cap; ++i) out[i] = cb.found[i];
+    return (int)cb.found.size();
+}
+
+// mode 0: the closest hit (the smallest fraction, the lower fixture index on a tie), from all
+// hits; mode 1: every hit, in fixture order; mode 2: the reference's clipping closest-hit
+// callback as it runs (the last hit it reports).  Returns the count; -1 for p1 == p2.
+int orc_raycast(orc_world* w, float x1, float y1, float x2, float y2, int mode, dbox_ray_hit* out, int cap) {
+    Vec2 p1(x1, y1), p2(x2, y2);
+    if ((p2 - p1).LengthSquared() <= 0.0f) return -1;
+    RayCollect cb;
+    cb.tree = &w->w.contactManager.broadPhase.tree;
+    cb.clip = mode == 2;
+    cb.tree->RayCast(&cb, p1, p2, 1.0f);
+    std::vector<dbox_ray_hit>& h = cb.hits;
+    std::sort(h.begin(), h.end(), [](const dbox_ray_hit& a, const dbox_ray_hit& b) { return a.fixture < b.fixture; });
+    if (mode == 0 && !h.empty()) {
+        size_t best = 0;
+        for (size_t i = 1; i < h.size(); ++i)
+            if (h[i].fraction < h[best].fraction) best = i;             // in fixture order: ties keep the lower index
+        h.assign(1, h[best]);
+    }
+    for (int i = 0; i < (int)h.size() && i < cap; ++i) out[i] = h[i];
+    return (int)h.size();
+}
 
 void orc_set_trig_mode(int mode) { g_trig_mode = mode; }
 int orc_get_trig_mode(void) { return g_trig_mode; }

@@ -35,6 +35,8 @@ void orc_world_destroy(orc_world* w);
 int orc_body_create(orc_world* w, const dbox_body_def* def);
 int orc_fixture_create(orc_world* w, int body, const dbox_shape_def* shape, const dbox_fixture_def* def);
 int orc_joint_create_revolute(orc_world* w, const dbox_revolute_def* def);
+int orc_query_aabb(orc_world* w, float lx, float ly, float ux, float uy, int* out, int cap);
+int orc_raycast(orc_world* w, float x1, float y1, float x2, float y2, int mode, dbox_ray_hit* out, int cap);
 int orc_fixture_create_chain(orc_world* w, int body, const dbox_vec2* vertices, int count, int loop,
                              const dbox_vec2* prev, const dbox_vec2* next, const dbox_fixture_def* def);
 int orc_joint_create_distance(orc_world* w, const dbox_distance_def* def);
