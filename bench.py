@@ -58,6 +58,8 @@ def parse():
     p.add_argument("--no-autotune", action="store_true", help="keep the default world-to-block mapping")
     p.add_argument("--mapping", default="auto", choices=["auto", "default", "queue"],
                    help="auto: the autotuner's choice; default: default block packing; queue: world queue")
+    p.add_argument("--queries", type=int, default=1 << 20, help="rays / boxes per world-query batch")
+    p.add_argument("--no-queries", action="store_true", help="skip the world-query measurement")
     p.add_argument("--learned-worlds", type=int, default=1024)
     p.add_argument("--learned-log-steps", type=int, default=2000)
     return p.parse_args()
@@ -302,8 +304,114 @@ def gpu_leg(args, rank, world_size):
     if out["roofline"]["peak"] is None:
         out["roofline"]["peak"] = 6800.0
         out["roofline"]["frac"] = achieved / 6800.0
+    if world_size == 1 and not args.no_queries:
+        out["world_queries"] = queries_leg(args, w, worlds, out["roofline"]["peak"])
     w.close()
     return out
+
+
+def _query_inputs(rng, n, worlds, xy):
+    """n seeded queries over the worlds: a random world, a random body of it; the ray starts
+    within 2 m of the body and runs 8 m in a random direction; the box is 2 m x 2 m around it."""
+    nb = np.array([len(s["bodies"]) for s in worlds])
+    starts = np.concatenate([[0], np.cumsum(nb)[:-1]])
+    wid = rng.integers(0, len(worlds), n).astype(np.int32)
+    b = starts[wid] + (rng.random(n) * nb[wid]).astype(np.int64)
+    ang = rng.uniform(0.0, 2.0 * np.pi, n)
+    p1 = (xy[b] + rng.uniform(-2.0, 2.0, (n, 2))).astype(np.float32)
+    p2 = (p1 + 8.0 * np.stack([np.cos(ang), np.sin(ang)], 1)).astype(np.float32)
+    boxes = np.concatenate([xy[b] - 1.0, xy[b] + 1.0], 1).astype(np.float32)
+    return wid, p1, p2, boxes
+
+
+def queries_leg(args, w, worlds, hbm_peak):
+    """b2World.RayCast (closest hit, all hits) and b2World.QueryAABB as batches of queries over
+    the measured handle's worlds after its timed steps.  Device-resident batches are timed
+    with CUDA events on the handle's stream, L2 flushed before each timed batch; the index
+    build (once per step) is timed on the first batch after one more step; e2e is the host
+    API with host arrays; the CPU figure is the oracle's b2DynamicTree walk on a sample."""
+    import torch
+    import oracle
+    n = args.queries
+    nbody = sum(len(s["bodies"]) for s in worlds)
+    xya = np.zeros((nbody, 3), np.float32)
+    w.get_transforms(xya)
+    rng = np.random.default_rng(args.seed + 101)
+    wid, p1, p2, boxes = _query_inputs(rng, n, worlds, xya[:, :2])
+    dev = torch.device("cuda")
+    t_w, t_p1, t_p2, t_box = (torch.from_numpy(a).to(dev) for a in (wid, p1, p2, boxes))
+    cap_all, cap_box = 16, 32
+    t_cnt = torch.zeros(n, dtype=torch.int32, device=dev)
+    t_hits = torch.zeros((n, cap_all, 6), dtype=torch.float32, device=dev)        # dbox_ray_hit, 24 bytes
+    t_fx = torch.zeros((n, cap_box), dtype=torch.int32, device=dev)
+    stream = torch.cuda.ExternalStream(w.stream())
+    flush = torch.empty(64 << 20, dtype=torch.float32, device=dev)              # 256 MB, twice the L2
+
+    def run(kind):
+        if kind == "query_aabb":
+            w.query_aabb_device(n, t_w.data_ptr(), t_box.data_ptr(), cap_box, t_cnt.data_ptr(), t_fx.data_ptr())
+        else:
+            mode, cap = (0, 1) if kind == "raycast_closest" else (1, cap_all)
+            w.raycast_device(n, t_w.data_ptr(), t_p1.data_ptr(), t_p2.data_ptr(), mode, cap, t_cnt.data_ptr(),
+                             t_hits.data_ptr())
+
+    def timed(kind, reps):
+        ts = []
+        for _ in range(reps):
+            with torch.cuda.stream(stream):
+                flush.fill_(1.0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            run(kind)
+            e1.record(stream)
+            stream.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return float(np.median(ts))
+
+    res = {"queries_per_batch": n,
+           "workload": "the bench's worlds after its timed steps; per query a random world and body, a ray from "
+                       "within 2 m of the body running 8 m in a random direction, a 2 m x 2 m box around the body"}
+    for kind in ("raycast_closest", "raycast_all", "query_aabb"):
+        for _ in range(3):
+            run(kind)
+        ms = timed(kind, 5)
+        cnt = t_cnt.cpu().numpy()
+        in_bytes = 4 + (16 if kind == "query_aabb" else 16)
+        out_bytes = 4 + (4 * np.minimum(cnt, cap_box).mean() if kind == "query_aabb" else
+                         24 * np.minimum(cnt, 1 if kind == "raycast_closest" else cap_all).mean())
+        gbs = n * (in_bytes + out_bytes) / (ms / 1e3) / 1e9
+        res[kind] = {"value": n / (ms / 1e3), "unit": "queries/s", "ms_per_batch": ms,
+                     "mean_results": float(cnt.mean()), "io_gbs": gbs, "io_frac_of_hbm": gbs / hbm_peak}
+    w.step(DT, VI, PI)                                                           # the index goes stale
+    res["raycast_closest"]["ms_first_batch_after_step"] = timed("raycast_closest", 1)
+    res["index_build_ms"] = res["raycast_closest"]["ms_first_batch_after_step"] - res["raycast_closest"]["ms_per_batch"]
+    # end to end: host arrays in, host arrays out, through the C ABI
+    w.raycast(wid[:1024], p1[:1024], p2[:1024], "closest", 1)
+    t0 = time.perf_counter()
+    w.raycast(wid, p1, p2, "closest", 1)
+    e2e_s = time.perf_counter() - t0
+    res["raycast_closest"]["e2e"] = {"value": n / e2e_s, "unit": "queries/s", "h2d_bytes": int(n * 20),
+                                     "d2h_bytes": int(n * 28)}
+    # CPU: the oracle's tree walk (b2DynamicTree.RayCast + b2World.RayCast's wrapper), one core
+    if not args.no_cpu:
+        sample = list(range(min(len(worlds), 32)))
+        oracle.set_trig_mode(0)
+        ows = [oracle.OracleWorld(worlds[i]) for i in sample]
+        for ow in ows:
+            ow.step(DT, VI, PI, steps=args.warmup + args.steps)
+        per = 2048
+        cpu_t = 0.0
+        for ow, i in zip(ows, sample):
+            xy = ow.export_state()["bodies"]["xf"][:, :2].astype(np.float32)
+            _, a, b, _ = _query_inputs(np.random.default_rng(args.seed + i), per, [worlds[i]], xy)
+            t0 = time.perf_counter()
+            ow.raycast_many(a, b, "closest", 1)
+            cpu_t += time.perf_counter() - t0
+        res["raycast_closest"]["cpu_baseline"] = {
+            "value": per * len(sample) / cpu_t, "unit": "queries/s", "cores": 1, "kind": "port",
+            "sample": "%d rays in each of the first %d worlds, oracle stepped %d steps, one core"
+                      % (per, len(sample), args.warmup + args.steps)}
+    return res
 
 
 def learned_leg(args):

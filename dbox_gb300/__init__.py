@@ -58,6 +58,7 @@ def lib():
     L.dbox_joint_create_mouse.argtypes = [vp, i32, vp, ctypes.POINTER(i32)]
     L.dbox_joint_set_mouse_target.argtypes = [vp, i32, i32, abi.Vec2]
     L.dbox_world_query_aabb.argtypes = [vp, i32, vp, vp, i32, vp, vp]
+    L.dbox_world_get_stream.argtypes = [vp, ctypes.POINTER(vp)]
     L.dbox_world_raycast.argtypes = [vp, i32, vp, vp, vp, i32, i32, vp, vp]
     L.dbox_world_query_aabb_device.argtypes = [vp, i32, vp, vp, i32, vp, vp]
     L.dbox_world_raycast_device.argtypes = [vp, i32, vp, vp, vp, i32, i32, vp, vp]
@@ -328,6 +329,12 @@ class World:
         _check(lib().dbox_world_raycast(self.h, len(a), abi.ptr(wv), abi.ptr(a), abi.ptr(b), m, cap, abi.ptr(counts),
                                         abi.ptr(hits)), "dbox_world_raycast")
         return counts, hits
+
+    def stream(self):
+        """The cudaStream_t (as an int) the handle's device work runs on."""
+        s = ctypes.c_void_p()
+        _check(lib().dbox_world_get_stream(self.h, ctypes.byref(s)), "dbox_world_get_stream")
+        return s.value or 0
 
     def query_aabb_device(self, n, worlds_ptr, boxes_ptr, capacity, counts_ptr, out_ptr):
         """dbox_world_query_aabb_device on device addresses (ints), enqueued without a wait."""

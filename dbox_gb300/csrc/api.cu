@@ -2091,6 +2091,12 @@ int32_t dbox_world_raycast(dbox_world* w, int32_t n, const int32_t* world, const
     return DBOX_OK;
 }
 
+int32_t dbox_world_get_stream(dbox_world* w, void** out) {
+    if (!w || !out) return fail(DBOX_ERR_INVALID, "dbox_world_get_stream: bad arguments");
+    *out = (void*)w->stream;
+    return DBOX_OK;
+}
+
 int32_t dbox_world_get_profile(dbox_world* w, dbox_profile* out) {
     if (!w || !out) return DBOX_ERR_INVALID;
     *out = w->profile;

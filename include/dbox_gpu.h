@@ -415,6 +415,10 @@ int32_t dbox_world_get_transforms(dbox_world* w, float* xya);
 int32_t dbox_world_set_phase_profile(dbox_world* w, int32_t enable);
 int32_t dbox_world_get_phase_profile(dbox_world* w, unsigned long long* out);
 
+/* The CUDA stream (a cudaStream_t) all device work of the handle is enqueued on, for callers
+ * that order their own work or events after it.  No counterpart in the reference. */
+int32_t dbox_world_get_stream(dbox_world* w, void** out);
+
 /* Wait for all queued device work of the handle. */
 int32_t dbox_world_sync(dbox_world* w);
 

@@ -48,6 +48,8 @@ def lib():
         L.orc_fixture_create_chain.argtypes = [vp, i32, vp, i32, i32, vp, vp, vp]
         L.orc_query_aabb.argtypes = [vp, f32, f32, f32, f32, vp, i32]
         L.orc_raycast.argtypes = [vp, f32, f32, f32, f32, i32, vp, i32]
+        L.orc_raycast_many.argtypes = [vp, i32, vp, vp, i32, vp, vp, i32]
+        L.orc_query_aabb_many.argtypes = [vp, i32, vp, vp, vp, i32]
         L.orc_joint_create_rope.argtypes = [vp, vp]
         L.orc_joint_create_weld.argtypes = [vp, vp]
         L.orc_joint_create_friction.argtypes = [vp, vp]
@@ -210,6 +212,24 @@ class OracleWorld:
         if n < 0:
             return None
         return out[:min(n, capacity)].copy()
+
+    def raycast_many(self, p1, p2, mode="closest", capacity=1):
+        """orc_raycast over arrays of rays in one C loop: (counts, hits (n, capacity))."""
+        a = np.ascontiguousarray(p1, np.float32).reshape(-1, 2)
+        b = np.ascontiguousarray(p2, np.float32).reshape(-1, 2)
+        counts = np.zeros(len(a), np.int32)
+        hits = np.zeros((len(a), capacity), abi.RAY_HIT)
+        lib().orc_raycast_many(self.h, len(a), abi.ptr(a), abi.ptr(b), {"closest": 0, "all": 1}[mode],
+                               abi.ptr(counts), abi.ptr(hits), capacity)
+        return counts, hits
+
+    def query_aabb_many(self, boxes, capacity=64):
+        """orc_query_aabb over an array of boxes in one C loop: (counts, fixtures (n, capacity))."""
+        bx = np.ascontiguousarray(boxes, np.float32).reshape(-1, 4)
+        counts = np.zeros(len(bx), np.int32)
+        out = np.zeros((len(bx), capacity), np.int32)
+        lib().orc_query_aabb_many(self.h, len(bx), abi.ptr(bx), abi.ptr(counts), abi.ptr(out), capacity)
+        return counts, out
 
     def set_mouse_target(self, joint, target):
         """b2MouseJoint.SetTarget (b2mousejoint.d:83-91)."""

@@ -5004,6 +5004,20 @@ int orc_raycast(orc_world* w, float x1, float y1, float x2, float y2, int mode, 
     return (int)h.size();
 }
 
+// n rays through orc_raycast (mode 0 or 1), counts[n], hits[n * cap]
+void orc_raycast_many(orc_world* w, int n, const float* p1, const float* p2, int mode, int* counts, dbox_ray_hit* hits,
+                      int cap) {
+    for (int i = 0; i < n; ++i)
+        counts[i] = orc_raycast(w, p1[2 * i], p1[2 * i + 1], p2[2 * i], p2[2 * i + 1], mode, hits + (size_t)i * cap, cap);
+}
+
+// n boxes (lower x, y, upper x, y) through orc_query_aabb, counts[n], out[n * cap]
+void orc_query_aabb_many(orc_world* w, int n, const float* boxes, int* counts, int* out, int cap) {
+    for (int i = 0; i < n; ++i)
+        counts[i] = orc_query_aabb(w, boxes[4 * i], boxes[4 * i + 1], boxes[4 * i + 2], boxes[4 * i + 3],
+                                   out + (size_t)i * cap, cap);
+}
+
 void orc_set_trig_mode(int mode) { g_trig_mode = mode; }
 int orc_get_trig_mode(void) { return g_trig_mode; }
 

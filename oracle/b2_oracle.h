@@ -36,6 +36,9 @@ int orc_body_create(orc_world* w, const dbox_body_def* def);
 int orc_fixture_create(orc_world* w, int body, const dbox_shape_def* shape, const dbox_fixture_def* def);
 int orc_joint_create_revolute(orc_world* w, const dbox_revolute_def* def);
 int orc_query_aabb(orc_world* w, float lx, float ly, float ux, float uy, int* out, int cap);
+void orc_raycast_many(orc_world* w, int n, const float* p1, const float* p2, int mode, int* counts, dbox_ray_hit* hits,
+                      int cap);
+void orc_query_aabb_many(orc_world* w, int n, const float* boxes, int* counts, int* out, int cap);
 int orc_raycast(orc_world* w, float x1, float y1, float x2, float y2, int mode, dbox_ray_hit* out, int cap);
 int orc_fixture_create_chain(orc_world* w, int body, const dbox_vec2* vertices, int count, int loop,
                              const dbox_vec2* prev, const dbox_vec2* next, const dbox_fixture_def* def);
