@@ -59,6 +59,7 @@ def lib():
     L.dbox_joint_set_mouse_target.argtypes = [vp, i32, i32, abi.Vec2]
     L.dbox_world_query_aabb.argtypes = [vp, i32, vp, vp, i32, vp, vp]
     L.dbox_world_get_stream.argtypes = [vp, ctypes.POINTER(vp)]
+    L.dbox_world_dump.argtypes = [vp, i32, ctypes.c_char_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]
     L.dbox_world_raycast.argtypes = [vp, i32, vp, vp, vp, i32, i32, vp, vp]
     L.dbox_world_query_aabb_device.argtypes = [vp, i32, vp, vp, i32, vp, vp]
     L.dbox_world_raycast_device.argtypes = [vp, i32, vp, vp, vp, i32, i32, vp, vp]
@@ -265,7 +266,8 @@ class World:
         if flags is not None:
             self.set_flags(**flags)
 
-    _JOINT_KINDS = {"distance": ("DISTANCE_DEF", "dbox_joint_create_distance"),
+    _JOINT_KINDS = {"revolute": ("REVOLUTE_DEF", "dbox_joint_create_revolute"),
+                    "distance": ("DISTANCE_DEF", "dbox_joint_create_distance"),
                     "rope": ("ROPE_DEF", "dbox_joint_create_rope"),
                     "weld": ("WELD_DEF", "dbox_joint_create_weld"),
                     "friction": ("FRICTION_DEF", "dbox_joint_create_friction"),
@@ -285,6 +287,22 @@ class World:
         dd = np.ascontiguousarray(np.array([d], getattr(abi, dtype)))
         out = ctypes.c_int32()
         _check(getattr(lib(), fn)(self.h, world, abi.ptr(dd), ctypes.byref(out)), fn)
+        return out.value
+
+    def create_body(self, world, body_def):
+        """b2World.CreateBody with a BODY_DEF record; returns the body index."""
+        dd = np.ascontiguousarray(np.array([body_def], abi.BODY_DEF))
+        out = ctypes.c_int32()
+        _check(lib().dbox_body_create(self.h, world, abi.ptr(dd), ctypes.byref(out)), "dbox_body_create")
+        return out.value
+
+    def create_fixture(self, world, body, shape_def, fixture_def):
+        """b2Body.CreateFixture with SHAPE_DEF and FIXTURE_DEF records; returns the fixture index."""
+        sd = np.ascontiguousarray(np.array([shape_def], abi.SHAPE_DEF))
+        fd = np.ascontiguousarray(np.array([fixture_def], abi.FIXTURE_DEF))
+        out = ctypes.c_int32()
+        _check(lib().dbox_fixture_create(self.h, world, body, abi.ptr(sd), abi.ptr(fd), ctypes.byref(out)),
+               "dbox_fixture_create")
         return out.value
 
     def create_chain(self, world, body, vertices, loop=False, prev=None, next=None, fixture=None):
@@ -329,6 +347,14 @@ class World:
         _check(lib().dbox_world_raycast(self.h, len(a), abi.ptr(wv), abi.ptr(a), abi.ptr(b), m, cap, abi.ptr(counts),
                                         abi.ptr(hits)), "dbox_world_raycast")
         return counts, hits
+
+    def dump(self, world=0):
+        """b2World.Dump's text for one world of the handle."""
+        n = ctypes.c_int64()
+        _check(lib().dbox_world_dump(self.h, world, None, 0, ctypes.byref(n)), "dbox_world_dump")
+        buf = ctypes.create_string_buffer(n.value + 1)
+        _check(lib().dbox_world_dump(self.h, world, buf, n.value + 1, ctypes.byref(n)), "dbox_world_dump")
+        return buf.value.decode()
 
     def stream(self):
         """The cudaStream_t (as an int) the handle's device work runs on."""

@@ -81,7 +81,19 @@ namespace {
         if (e_ != cudaSuccess) return fail(DBOX_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
     } while (0)
 
+// A b2ChainShape as created (b2chainshape.d:45-110): its vertex list (a loop repeats the first
+// vertex), ghost vertices and the definition's density; its child edges are the fixtures
+// [first, first + vertices - 1).
+struct ChainRec {
+    std::vector<dbox_vec2> v;
+    dbox_vec2 prev, next;
+    int has_prev, has_next;
+    float density;
+    int first;
+};
+
 struct HostWorld {
+    std::vector<ChainRec> chains;
     std::vector<dbox_body_state> bs;
     std::vector<dg::BodyStatic> bst;
     std::vector<std::vector<int>> body_fix;     // fixture indices per body, newest first
@@ -1034,17 +1046,28 @@ int32_t dbox_fixture_create(dbox_world* w, int32_t world, int32_t body, const db
 
 // the child edges of a b2ChainShape (b2chainshape.d: CreateChain / CreateLoop, GetChildEdge)
 // as edge shape records, in child order
-static std::vector<dbox_shape_def> chain_children(const dbox_vec2* vertices, int count, bool loop, const dbox_vec2* prev,
-                                                  const dbox_vec2* next) {
-    std::vector<dbox_vec2> v(vertices, vertices + count);
-    bool hasPrev = prev != nullptr, hasNext = next != nullptr;
-    dbox_vec2 pv = prev ? *prev : dbox_vec2{0.0f, 0.0f}, nv = next ? *next : dbox_vec2{0.0f, 0.0f};
+static ChainRec make_chain(const dbox_vec2* vertices, int count, bool loop, const dbox_vec2* prev, const dbox_vec2* next) {
+    ChainRec c;
+    c.v.assign(vertices, vertices + count);
+    c.has_prev = prev != nullptr;
+    c.has_next = next != nullptr;
+    c.prev = prev ? *prev : dbox_vec2{0.0f, 0.0f};
+    c.next = next ? *next : dbox_vec2{0.0f, 0.0f};
     if (loop) {
-        v.push_back(vertices[0]);
-        pv = v[v.size() - 2];
-        nv = v[1];
-        hasPrev = hasNext = true;
+        c.v.push_back(vertices[0]);
+        c.prev = c.v[c.v.size() - 2];
+        c.next = c.v[1];
+        c.has_prev = c.has_next = 1;
     }
+    c.density = 0.0f;
+    c.first = -1;
+    return c;
+}
+
+static std::vector<dbox_shape_def> chain_children(const ChainRec& c) {
+    const std::vector<dbox_vec2>& v = c.v;
+    const bool hasPrev = c.has_prev != 0, hasNext = c.has_next != 0;
+    const dbox_vec2 pv = c.prev, nv = c.next;
     const int m = (int)v.size();
     std::vector<dbox_shape_def> out;
     for (int i = 0; i + 1 < m; ++i) {
@@ -1076,12 +1099,15 @@ int32_t dbox_fixture_create_chain(dbox_world* w, int32_t world, int32_t body, co
     dbox_fixture_def d = *def;
     d.density = 0.0f;
     int first = -1;
-    for (const dbox_shape_def& e : chain_children(vertices, count, loop != 0, loop ? nullptr : prev_vertex,
-                                                  loop ? nullptr : next_vertex)) {
+    ChainRec c = make_chain(vertices, count, loop != 0, loop ? nullptr : prev_vertex, loop ? nullptr : next_vertex);
+    for (const dbox_shape_def& e : chain_children(c)) {
         int idx = create_fixture(w->worlds[world], body, &e, &d);
         if (idx < 0) return fail(DBOX_ERR_INVALID, "dbox_fixture_create_chain: bad child edge");
         if (first < 0) first = idx;
     }
+    c.density = def->density;
+    c.first = first;
+    w->worlds[world].chains.push_back(c);
     if (out_first) *out_first = first;
     return DBOX_OK;
 }
@@ -1233,6 +1259,8 @@ int create_pulley_joint(HostWorld& hw, const dbox_pulley_def* d) {
     j.local_anchor_a = make_float2(d->local_anchor_a.x, d->local_anchor_a.y);
     j.local_anchor_b = make_float2(d->local_anchor_b.x, d->local_anchor_b.y);
     j.ratio = d->ratio;
+    j.length_a = d->length_a;
+    j.length_b = d->length_b;
     j.constant = d->length_a + d->ratio * d->length_b;
     return link_joint(hw, j);
 }
@@ -2088,6 +2116,232 @@ int32_t dbox_world_raycast(dbox_world* w, int32_t n, const int32_t* world, const
     CU(cudaMemcpyAsync(counts, out, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, w->stream));
     if (so) CU(cudaMemcpyAsync(hits, out + sc, so, cudaMemcpyDeviceToHost, w->stream));
     CU(cudaStreamSynchronize(w->stream));
+    return DBOX_OK;
+}
+
+// ---------------------------------------------------------------- b2World.Dump
+// The text b2World.Dump logs (b2world.d:796-855, b2body.d:992-1022, b2fixture.d:280-358, the
+// joints' Dump): statements that rebuild the world, floats as %.15e with an 'f' suffix.  The
+// reference walks its body, fixture and joint lists, newest first: bodies[i] is body
+// count - 1 - i, joints[k] joint count - 1 - k, and a body's fixtures come newest first.
+namespace {
+struct Dumper {
+    std::string s;
+    void put(const char* fmt, ...) __attribute__((format(printf, 2, 3))) {
+        char tmp[512];
+        va_list ap;
+        va_start(ap, fmt);
+        int n = vsnprintf(tmp, sizeof(tmp), fmt, ap);
+        va_end(ap);
+        s.append(tmp, n < (int)sizeof(tmp) ? n : (int)sizeof(tmp) - 1);
+    }
+    void vec(const char* in, const char* what, float x, float y) {
+        put("%s%s.Set(%.15ef, %.15ef);\n", in, what, (double)x, (double)y);
+    }
+    void vec(const char* in, const char* what, float2 v) { vec(in, what, v.x, v.y); }
+    void num(const char* in, const char* what, float v) { put("%s%s = %.15ef;\n", in, what, (double)v); }
+    void flag(const char* in, const char* what, int v) { put("%s%s = bool(%d);\n", in, what, v); }
+
+    void fixture(const HostWorld& hw, int fi, int body_index, const ChainRec* chain) {
+        const dg::DFixture& f = hw.fx[fi];
+        const char* in = "    ";
+        put("    b2FixtureDef fd;\n");
+        num(in, "fd.friction", f.friction);
+        num(in, "fd.restitution", f.restitution);
+        num(in, "fd.density", chain ? chain->density : f.density);
+        put("    fd.isSensor = bool(%d);\n", f.sensor ? 1 : 0);
+        put("    fd.filter.categoryBits = uint16(%d);\n", (int)(f.filter & 0xffffu));
+        put("    fd.filter.maskBits = uint16(%d);\n", (int)(f.filter >> 16));
+        put("    fd.filter.groupIndex = int16(%d);\n", f.group);
+        if (chain) {
+            const int n = (int)chain->v.size();
+            put("    b2ChainShape shape;\n");
+            put("    b2Vec2 vs[%d];\n", n);
+            for (int i = 0; i < n; ++i) put("    vs[%d].Set(%.15ef, %.15ef);\n", i, (double)chain->v[i].x, (double)chain->v[i].y);
+            put("    shape.CreateChain(vs, %d);\n", n);
+            vec(in, "shape.m_prevVertex", chain->prev.x, chain->prev.y);
+            vec(in, "shape.m_nextVertex", chain->next.x, chain->next.y);
+            flag(in, "shape.m_hasPrevVertex", chain->has_prev ? 1 : 0);
+            flag(in, "shape.m_hasNextVertex", chain->has_next ? 1 : 0);
+        } else if (f.type == dg::kShapeCircle) {
+            put("    b2CircleShape shape;\n");
+            num(in, "shape.m_radius", f.radius);
+            vec(in, "shape.m_p", f.v[0]);
+        } else if (f.type == dg::kShapeEdge) {
+            put("    b2EdgeShape shape;\n");
+            num(in, "shape.m_radius", f.radius);
+            vec(in, "shape.m_vertex0", f.v[2]);
+            vec(in, "shape.m_vertex1", f.v[0]);
+            vec(in, "shape.m_vertex2", f.v[1]);
+            vec(in, "shape.m_vertex3", f.v[3]);
+            flag(in, "shape.m_hasVertex0", f.edge_flags & 1);
+            flag(in, "shape.m_hasVertex3", (f.edge_flags >> 1) & 1);
+        } else {
+            put("    b2PolygonShape shape;\n");
+            put("    b2Vec2 vs[%d];\n", 8);                             // b2_maxPolygonVertices
+            for (int i = 0; i < f.count; ++i) put("    vs[%d].Set(%.15ef, %.15ef);\n", i, (double)f.v[i].x, (double)f.v[i].y);
+            put("    shape.Set(vs, %d);\n", f.count);
+        }
+        put("\n");
+        put("    fd.shape = &shape;\n");
+        put("\n");
+        put("    bodies[%d].CreateFixture(&fd);\n", body_index);
+    }
+
+    void joint(const dg::DJoint& j, int index_a, int index_b, int index) {
+        static const char* names[] = {"b2RevoluteJointDef", "b2DistanceJointDef", "b2RopeJointDef", "b2WeldJointDef",
+                                      "b2FrictionJointDef", "b2MotorJointDef", "b2WheelJointDef", "b2PrismaticJointDef",
+                                      "b2PulleyJointDef"};
+        if (j.type == dg::kMouseJoint) {                                 // b2mousejoint.d:180-183
+            put("Mouse joint dumping is not supported.\n");
+            return;
+        }
+        const char* in = "  ";
+        put("  %s jd;\n", names[j.type]);
+        put("  jd.bodyA = bodies[%d];\n", index_a);
+        put("  jd.bodyB = bodies[%d];\n", index_b);
+        flag(in, "jd.collideConnected", j.collide_connected ? 1 : 0);
+        const bool anchors = j.type != dg::kMotorJoint && j.type != dg::kPulleyJoint;
+        if (j.type == dg::kPulleyJoint) {
+            vec(in, "jd.groundAnchorA", j.ground_a);
+            vec(in, "jd.groundAnchorB", j.ground_b);
+        }
+        if (anchors || j.type == dg::kPulleyJoint) {
+            vec(in, "jd.localAnchorA", j.local_anchor_a);
+            vec(in, "jd.localAnchorB", j.local_anchor_b);
+        }
+        switch (j.type) {
+        case dg::kRevoluteJoint:                                        // b2revolutejoint.d:293-312
+            num(in, "jd.referenceAngle", j.reference_angle);
+            flag(in, "jd.enableLimit", j.enable_limit ? 1 : 0);
+            num(in, "jd.lowerAngle", j.lower_angle);
+            num(in, "jd.upperAngle", j.upper_angle);
+            flag(in, "jd.enableMotor", j.enable_motor ? 1 : 0);
+            num(in, "jd.motorSpeed", j.motor_speed);
+            num(in, "jd.maxMotorTorque", j.max_motor_torque);
+            break;
+        case dg::kDistanceJoint:                                        // b2distancejoint.d:189-203
+            num(in, "jd.length", j.length);
+            num(in, "jd.frequencyHz", j.frequency_hz);
+            num(in, "jd.dampingRatio", j.damping_ratio);
+            break;
+        case dg::kRopeJoint:                                            // b2ropejoint.d:145-157
+            num(in, "jd.maxLength", j.length);
+            break;
+        case dg::kWeldJoint:                                            // b2weldjoint.d:174-188
+            num(in, "jd.referenceAngle", j.reference_angle);
+            num(in, "jd.frequencyHz", j.frequency_hz);
+            num(in, "jd.dampingRatio", j.damping_ratio);
+            break;
+        case dg::kFrictionJoint:                                        // b2frictionjoint.d:157-170
+            num(in, "jd.maxForce", j.max_force);
+            num(in, "jd.maxTorque", j.max_torque);
+            break;
+        case dg::kMotorJoint:                                           // b2motorjoint.d:201-215
+            vec(in, "jd.linearOffset", j.linear_offset);
+            num(in, "jd.angularOffset", j.angular_offset);
+            num(in, "jd.maxForce", j.max_force);
+            num(in, "jd.maxTorque", j.max_torque);
+            num(in, "jd.correctionFactor", j.correction_factor);
+            break;
+        case dg::kWheelJoint:                                           // b2wheeljoint.d:277-294
+            vec(in, "jd.localAxisA", j.local_axis_x);
+            flag(in, "jd.enableMotor", j.enable_motor ? 1 : 0);
+            num(in, "jd.motorSpeed", j.motor_speed);
+            num(in, "jd.maxMotorTorque", j.max_motor_torque);
+            num(in, "jd.frequencyHz", j.frequency_hz);
+            num(in, "jd.dampingRatio", j.damping_ratio);
+            break;
+        case dg::kPrismaticJoint:                                       // b2prismaticjoint.d:364-383
+            vec(in, "jd.localAxisA", j.local_axis_x);
+            num(in, "jd.referenceAngle", j.reference_angle);
+            flag(in, "jd.enableLimit", j.enable_limit ? 1 : 0);
+            num(in, "jd.lowerTranslation", j.lower_translation);
+            num(in, "jd.upperTranslation", j.upper_translation);
+            flag(in, "jd.enableMotor", j.enable_motor ? 1 : 0);
+            num(in, "jd.motorSpeed", j.motor_speed);
+            num(in, "jd.maxMotorForce", j.max_motor_force);
+            break;
+        case dg::kPulleyJoint:                                          // b2pulleyjoint.d:207-223
+            num(in, "jd.lengthA", j.length_a);
+            num(in, "jd.lengthB", j.length_b);
+            num(in, "jd.ratio", j.ratio);
+            break;
+        }
+        put("  joints[%d] = m_world.CreateJoint(&jd);\n", index);
+    }
+
+    void world(const HostWorld& hw, float2 g) {
+        const int nb = (int)hw.bs.size(), nj = (int)hw.jt.size();
+        put("b2Vec2 g(%.15ef, %.15ef);\n", (double)g.x, (double)g.y);
+        put("m_world.SetGravity(g);\n");
+        put("b2Body** bodies = cast(b2Body**)b2Alloc(%d * (b2Body*).sizeof);\n", nb);
+        put("b2Joint joints = cast(b2Joint)b2Alloc(%d * (b2Joint).sizeof);\n", nj);
+        for (int i = 0; i < nb; ++i) {
+            const int b = nb - 1 - i;
+            const dbox_body_state& s = hw.bs[b];
+            const dg::BodyStatic& st = hw.bst[b];
+            const char* in = "  ";
+            put("{\n");
+            put("  b2BodyDef bd;\n");
+            put("  bd.type = b2BodyType(%d);\n", s.type);
+            vec(in, "bd.position", s.xf[0], s.xf[1]);
+            num(in, "bd.angle", s.sweep[7]);
+            vec(in, "bd.linearVelocity", s.vel[0], s.vel[1]);
+            num(in, "bd.angularVelocity", s.vel[2]);
+            num(in, "bd.linearDamping", st.lin_damping);
+            num(in, "bd.angularDamping", st.ang_damping);
+            flag(in, "bd.allowSleep", (int)(s.flags & 0x4u));
+            flag(in, "bd.awake", (int)(s.flags & 0x2u));
+            flag(in, "bd.fixedRotation", (int)(s.flags & 0x10u));
+            flag(in, "bd.bullet", (int)(s.flags & 0x8u));
+            flag(in, "bd.active", (int)(s.flags & 0x20u));
+            num(in, "bd.gravityScale", st.gravity_scale);
+            put("  bodies[%d] = m_world.CreateBody(&bd);\n", i);
+            put("\n");
+            const ChainRec* last = nullptr;
+            for (int fi : hw.body_fix[b]) {
+                const ChainRec* chain = nullptr;
+                for (const ChainRec& c : hw.chains)
+                    if (fi >= c.first && fi < c.first + (int)c.v.size() - 1) chain = &c;
+                if (chain && chain == last) continue;                   // one fixture per chain
+                last = chain;
+                put("  {\n");
+                fixture(hw, fi, i, chain);
+                put("  }\n");
+            }
+            put("}\n");
+        }
+        for (int k = 0; k < nj; ++k) {                                  // no gear joints: one pass
+            const dg::DJoint& j = hw.jt[nj - 1 - k];
+            put("{\n");
+            joint(j, nb - 1 - j.body_a, nb - 1 - j.body_b, k);
+            put("}\n");
+        }
+        put("b2Free(joints);\n");
+        put("b2Free(bodies);\n");
+        put("joints = null;\n");
+        put("bodies = null;\n");
+    }
+};
+}  // namespace
+
+int32_t dbox_world_dump(dbox_world* w, int32_t world, char* buf, int64_t capacity, int64_t* out_length) {
+    if (!w || world < 0 || world >= (int)w->worlds.size() || capacity < 0 || (capacity > 0 && !buf))
+        return fail(DBOX_ERR_INVALID, "dbox_world_dump: bad arguments");
+    if (w->on_device && !w->mirrors_fresh) {
+        int rc = download(w);
+        if (rc) return rc;
+        if (!w->dirty && w->total_bodies + w->total_fixtures > 0) w->on_device = true;
+    }
+    Dumper d;
+    d.world(w->worlds[world], w->gravity);
+    if (capacity > 0) {
+        const size_t n = d.s.size() < (size_t)capacity - 1 ? d.s.size() : (size_t)capacity - 1;
+        memcpy(buf, d.s.data(), n);
+        buf[n] = 0;
+    }
+    if (out_length) *out_length = (int64_t)d.s.size();
     return DBOX_OK;
 }
 

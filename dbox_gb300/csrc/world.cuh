@@ -110,6 +110,7 @@ struct DJoint {
     // pulley: impulse[0], mass[0]; mouse: impulse[0..1], mass matrix as friction's
     float2 ground_a, ground_b, uA, uB, target, mouse_c;
     float ratio, constant, beta;
+    float length_a, length_b;      // pulley: the definition's lengths (kept for the dump)
     int pad4;
 };
 

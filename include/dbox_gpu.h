@@ -415,6 +415,14 @@ int32_t dbox_world_get_transforms(dbox_world* w, float* xya);
 int32_t dbox_world_set_phase_profile(dbox_world* w, int32_t enable);
 int32_t dbox_world_get_phase_profile(dbox_world* w, unsigned long long* out);
 
+/* b2World.Dump (b2world.d:796-855 with b2Body.Dump b2body.d:992-1022, b2Fixture.Dump
+ * b2fixture.d:280-358 and the joints' Dump): the text the reference logs, statements that
+ * rebuild world `world` with its current positions, angles and velocities (contacts and
+ * warm-start impulses are not part of it).  A chain is dumped as its b2ChainShape, a mouse
+ * joint as the reference's "not supported" line.  The text is written to buf when capacity
+ * > 0 (NUL-terminated, cut at capacity - 1 bytes); out_length receives its full length. */
+int32_t dbox_world_dump(dbox_world* w, int32_t world, char* buf, int64_t capacity, int64_t* out_length);
+
 /* The CUDA stream (a cudaStream_t) all device work of the handle is enqueued on, for callers
  * that order their own work or events after it.  No counterpart in the reference. */
 int32_t dbox_world_get_stream(dbox_world* w, void** out);

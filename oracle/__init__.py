@@ -48,6 +48,10 @@ def lib():
         L.orc_fixture_create_chain.argtypes = [vp, i32, vp, i32, i32, vp, vp, vp]
         L.orc_query_aabb.argtypes = [vp, f32, f32, f32, f32, vp, i32]
         L.orc_raycast.argtypes = [vp, f32, f32, f32, f32, i32, vp, i32]
+        L.orc_world_dump.argtypes = [vp, ctypes.c_char_p, i32]
+        L.orc_body_create.argtypes = [vp, vp]
+        L.orc_fixture_create.argtypes = [vp, i32, vp, vp]
+        L.orc_joint_create_revolute.argtypes = [vp, vp]
         L.orc_raycast_many.argtypes = [vp, i32, vp, vp, i32, vp, vp, i32]
         L.orc_query_aabb_many.argtypes = [vp, i32, vp, vp, vp, i32]
         L.orc_joint_create_rope.argtypes = [vp, vp]
@@ -212,6 +216,36 @@ class OracleWorld:
         if n < 0:
             return None
         return out[:min(n, capacity)].copy()
+
+    _JOINTS = {"revolute": "REVOLUTE_DEF", "distance": "DISTANCE_DEF", "rope": "ROPE_DEF", "weld": "WELD_DEF",
+               "friction": "FRICTION_DEF", "motor": "MOTOR_DEF", "wheel": "WHEEL_DEF", "prismatic": "PRISMATIC_DEF",
+               "pulley": "PULLEY_DEF", "mouse": "MOUSE_DEF"}
+
+    def create_body(self, body_def):
+        dd = np.ascontiguousarray(np.array([body_def], abi.BODY_DEF))
+        return lib().orc_body_create(self.h, abi.ptr(dd))
+
+    def create_fixture(self, body, shape_def, fixture_def):
+        sd = np.ascontiguousarray(np.array([shape_def], abi.SHAPE_DEF))
+        fd = np.ascontiguousarray(np.array([fixture_def], abi.FIXTURE_DEF))
+        r = lib().orc_fixture_create(self.h, body, abi.ptr(sd), abi.ptr(fd))
+        if r < 0:
+            raise ValueError("oracle fixture creation failed")
+        return r
+
+    def create_joint(self, kind, d):
+        dd = np.ascontiguousarray(np.array([d], getattr(abi, self._JOINTS[kind])))
+        r = getattr(lib(), "orc_joint_create_" + kind)(self.h, abi.ptr(dd))
+        if r < 0:
+            raise ValueError("oracle %s joint creation failed" % kind)
+        return r
+
+    def dump(self):
+        """b2World.Dump's text."""
+        n = lib().orc_world_dump(self.h, None, 0)
+        buf = ctypes.create_string_buffer(n + 1)
+        lib().orc_world_dump(self.h, buf, n + 1)
+        return buf.value.decode()
 
     def raycast_many(self, p1, p2, mode="closest", capacity=1):
         """orc_raycast over arrays of rays in one C loop: (counts, hits (n, capacity))."""

@@ -18,6 +18,8 @@
 #include <string.h>
 #include <stdlib.h>
 #include <algorithm>
+#include <cstdarg>
+#include <string>
 #include <vector>
 
 namespace orc {
@@ -1906,6 +1908,7 @@ struct Fixture {                                                        // dynam
     Filter filter;
     bool isSensor = false;
     int index = 0;   // creation order (for export)
+    int chain = -1;  // the b2ChainShape this child edge belongs to (World::chains), or -1
 };
 
 enum { kStaticBody = 0, kKinematicBody = 1, kDynamicBody = 2 };
@@ -2127,7 +2130,8 @@ struct Joint {                                                          // joint
     f32 s1 = 0, s2 = 0, a1 = 0, a2 = 0;
     // pulley (impulse.x) and mouse (impulse.x/.y; mass matrix in linearMass)
     Vec2 groundAnchorA, groundAnchorB, uA, uB, targetA, mouseC;
-    f32 ratio = 0, constant = 0, beta = 0;
+    f32 ratio = 0, constant = 0, beta = 0, lengthA = 0, lengthB = 0;
+    int dumpIndex = 0;           // b2Joint.m_index: the joint's place in the world list, set by Dump
 
     void InitVelocityConstraints(const SolverData& data) {
         switch (type) {
@@ -4185,8 +4189,19 @@ void ContactManager::Collide() {                                        // b2con
 
 
 // ------------------------------------------------------------ world
+// A b2ChainShape as created (b2chainshape.d:45-110): its vertex list (a loop repeats the first
+// vertex), ghost vertices and the fixture data; its child edges are fixtures [first, first + count - 1).
+struct ChainRec {
+    std::vector<Vec2> vertices;
+    Vec2 prevVertex, nextVertex;
+    bool hasPrevVertex = false, hasNextVertex = false;
+    f32 density = 0;
+    int first = -1;
+};
+
 struct World {                                                          // dynamics/b2world.d
     enum { kNewFixture = 0x0001, kLocked = 0x0002, kClearForces = 0x0004 };
+    std::vector<ChainRec> chains;
     Body* bodyList = nullptr;
     Joint* jointList = nullptr;
     int bodyCount = 0, jointCount = 0;
@@ -4428,6 +4443,8 @@ struct World {                                                          // dynam
         j->localAnchorA = Vec2(def->local_anchor_a.x, def->local_anchor_a.y);
         j->localAnchorB = Vec2(def->local_anchor_b.x, def->local_anchor_b.y);
         j->ratio = def->ratio;
+        j->lengthA = def->length_a;
+        j->lengthB = def->length_b;
         j->constant = def->length_a + def->ratio * def->length_b;
         j->impulse.SetZero();
         return LinkJoint(j);
@@ -4844,6 +4861,218 @@ using namespace orc;
 
 struct orc_world { World w; };
 
+// ------------------------------------------------------------ b2World.Dump
+// The text b2World.Dump logs (b2world.d:796-855, b2body.d:992-1022, b2fixture.d:280-358 and the
+// joints' Dump): D statements that rebuild the world, every float as %.15e with an 'f' suffix.
+struct DumpText {
+    std::string s;
+    void put(const char* fmt, ...) __attribute__((format(printf, 2, 3))) {
+        char tmp[512];
+        va_list ap;
+        va_start(ap, fmt);
+        int n = vsnprintf(tmp, sizeof(tmp), fmt, ap);
+        va_end(ap);
+        s.append(tmp, n < (int)sizeof(tmp) ? n : (int)sizeof(tmp) - 1);
+    }
+    void vec(const char* indent, const char* what, Vec2 v) { put("%s%s.Set(%.15ef, %.15ef);\n", indent, what, (double)v.x, (double)v.y); }
+    void num(const char* indent, const char* what, f32 v) { put("%s%s = %.15ef;\n", indent, what, (double)v); }
+    void flag(const char* indent, const char* what, int v) { put("%s%s = bool(%d);\n", indent, what, v); }
+};
+
+static void DumpFixture(DumpText& t, const World& w, const Fixture* f, int bodyIndex) {   // b2fixture.d:280-358
+    const char* in = "    ";
+    const bool chain = f->chain >= 0;
+    t.put("    b2FixtureDef fd;\n");
+    t.num(in, "fd.friction", f->friction);
+    t.num(in, "fd.restitution", f->restitution);
+    t.num(in, "fd.density", chain ? w.chains[f->chain].density : f->density);
+    t.put("    fd.isSensor = bool(%d);\n", f->isSensor ? 1 : 0);
+    t.put("    fd.filter.categoryBits = uint16(%d);\n", (int)f->filter.categoryBits);
+    t.put("    fd.filter.maskBits = uint16(%d);\n", (int)f->filter.maskBits);
+    t.put("    fd.filter.groupIndex = int16(%d);\n", (int)f->filter.groupIndex);
+    const Shape& s = f->shape;
+    if (chain) {
+        const ChainRec& c = w.chains[f->chain];
+        const int n = (int)c.vertices.size();
+        t.put("    b2ChainShape shape;\n");
+        t.put("    b2Vec2 vs[%d];\n", n);
+        for (int i = 0; i < n; ++i)
+            t.put("    vs[%d].Set(%.15ef, %.15ef);\n", i, (double)c.vertices[i].x, (double)c.vertices[i].y);
+        t.put("    shape.CreateChain(vs, %d);\n", n);
+        t.vec(in, "shape.m_prevVertex", c.prevVertex);
+        t.vec(in, "shape.m_nextVertex", c.nextVertex);
+        t.flag(in, "shape.m_hasPrevVertex", c.hasPrevVertex ? 1 : 0);
+        t.flag(in, "shape.m_hasNextVertex", c.hasNextVertex ? 1 : 0);
+    } else if (s.type == kCircle) {
+        t.put("    b2CircleShape shape;\n");
+        t.num(in, "shape.m_radius", s.radius);
+        t.vec(in, "shape.m_p", s.p);
+    } else if (s.type == kEdge) {
+        t.put("    b2EdgeShape shape;\n");
+        t.num(in, "shape.m_radius", s.radius);
+        t.vec(in, "shape.m_vertex0", s.vertex0);
+        t.vec(in, "shape.m_vertex1", s.vertices[0]);
+        t.vec(in, "shape.m_vertex2", s.vertices[1]);
+        t.vec(in, "shape.m_vertex3", s.vertex3);
+        t.flag(in, "shape.m_hasVertex0", s.hasVertex0 ? 1 : 0);
+        t.flag(in, "shape.m_hasVertex3", s.hasVertex3 ? 1 : 0);
+    } else {
+        t.put("    b2PolygonShape shape;\n");
+        t.put("    b2Vec2 vs[%d];\n", kMaxPolygonVertices);
+        for (int i = 0; i < s.count; ++i)
+            t.put("    vs[%d].Set(%.15ef, %.15ef);\n", i, (double)s.vertices[i].x, (double)s.vertices[i].y);
+        t.put("    shape.Set(vs, %d);\n", s.count);
+    }
+    t.put("\n");
+    t.put("    fd.shape = &shape;\n");
+    t.put("\n");
+    t.put("    bodies[%d].CreateFixture(&fd);\n", bodyIndex);
+}
+
+static void DumpJoint(DumpText& t, const Joint* j) {                    // the joints' Dump
+    static const char* names[] = {"b2RevoluteJointDef", "b2DistanceJointDef", "b2RopeJointDef", "b2WeldJointDef",
+                                  "b2FrictionJointDef", "b2MotorJointDef", "b2WheelJointDef", "b2PrismaticJointDef",
+                                  "b2PulleyJointDef"};
+    if (j->type == kMouseJoint) {                                       // b2mousejoint.d:180-183
+        t.put("Mouse joint dumping is not supported.\n");
+        return;
+    }
+    const char* in = "  ";
+    t.put("  %s jd;\n", names[j->type]);
+    t.put("  jd.bodyA = bodies[%d];\n", j->bodyA->islandIndex);
+    t.put("  jd.bodyB = bodies[%d];\n", j->bodyB->islandIndex);
+    t.flag(in, "jd.collideConnected", j->collideConnected ? 1 : 0);
+    switch (j->type) {
+    case kRevoluteJoint:                                                // b2revolutejoint.d:293-312
+        t.vec(in, "jd.localAnchorA", j->localAnchorA);
+        t.vec(in, "jd.localAnchorB", j->localAnchorB);
+        t.num(in, "jd.referenceAngle", j->referenceAngle);
+        t.flag(in, "jd.enableLimit", j->enableLimit ? 1 : 0);
+        t.num(in, "jd.lowerAngle", j->lowerAngle);
+        t.num(in, "jd.upperAngle", j->upperAngle);
+        t.flag(in, "jd.enableMotor", j->enableMotor ? 1 : 0);
+        t.num(in, "jd.motorSpeed", j->motorSpeed);
+        t.num(in, "jd.maxMotorTorque", j->maxMotorTorque);
+        break;
+    case kDistanceJoint:                                                // b2distancejoint.d:189-203
+        t.vec(in, "jd.localAnchorA", j->localAnchorA);
+        t.vec(in, "jd.localAnchorB", j->localAnchorB);
+        t.num(in, "jd.length", j->length);
+        t.num(in, "jd.frequencyHz", j->frequencyHz);
+        t.num(in, "jd.dampingRatio", j->dampingRatio);
+        break;
+    case kRopeJoint:                                                    // b2ropejoint.d:145-157
+        t.vec(in, "jd.localAnchorA", j->localAnchorA);
+        t.vec(in, "jd.localAnchorB", j->localAnchorB);
+        t.num(in, "jd.maxLength", j->length);
+        break;
+    case kWeldJoint:                                                    // b2weldjoint.d:174-188
+        t.vec(in, "jd.localAnchorA", j->localAnchorA);
+        t.vec(in, "jd.localAnchorB", j->localAnchorB);
+        t.num(in, "jd.referenceAngle", j->referenceAngle);
+        t.num(in, "jd.frequencyHz", j->frequencyHz);
+        t.num(in, "jd.dampingRatio", j->dampingRatio);
+        break;
+    case kFrictionJoint:                                                // b2frictionjoint.d:157-170
+        t.vec(in, "jd.localAnchorA", j->localAnchorA);
+        t.vec(in, "jd.localAnchorB", j->localAnchorB);
+        t.num(in, "jd.maxForce", j->maxForce);
+        t.num(in, "jd.maxTorque", j->maxTorque);
+        break;
+    case kMotorJoint:                                                   // b2motorjoint.d:201-215
+        t.vec(in, "jd.linearOffset", j->linearOffset);
+        t.num(in, "jd.angularOffset", j->angularOffset);
+        t.num(in, "jd.maxForce", j->maxForce);
+        t.num(in, "jd.maxTorque", j->maxTorque);
+        t.num(in, "jd.correctionFactor", j->correctionFactor);
+        break;
+    case kWheelJoint:                                                   // b2wheeljoint.d:277-294
+        t.vec(in, "jd.localAnchorA", j->localAnchorA);
+        t.vec(in, "jd.localAnchorB", j->localAnchorB);
+        t.vec(in, "jd.localAxisA", j->localXAxisA);
+        t.flag(in, "jd.enableMotor", j->enableMotor ? 1 : 0);
+        t.num(in, "jd.motorSpeed", j->motorSpeed);
+        t.num(in, "jd.maxMotorTorque", j->maxMotorTorque);
+        t.num(in, "jd.frequencyHz", j->frequencyHz);
+        t.num(in, "jd.dampingRatio", j->dampingRatio);
+        break;
+    case kPrismaticJoint:                                               // b2prismaticjoint.d:364-383
+        t.vec(in, "jd.localAnchorA", j->localAnchorA);
+        t.vec(in, "jd.localAnchorB", j->localAnchorB);
+        t.vec(in, "jd.localAxisA", j->localXAxisA);
+        t.num(in, "jd.referenceAngle", j->referenceAngle);
+        t.flag(in, "jd.enableLimit", j->enableLimit ? 1 : 0);
+        t.num(in, "jd.lowerTranslation", j->lowerTranslation);
+        t.num(in, "jd.upperTranslation", j->upperTranslation);
+        t.flag(in, "jd.enableMotor", j->enableMotor ? 1 : 0);
+        t.num(in, "jd.motorSpeed", j->motorSpeed);
+        t.num(in, "jd.maxMotorForce", j->maxMotorForce);
+        break;
+    case kPulleyJoint:                                                  // b2pulleyjoint.d:207-223
+        t.vec(in, "jd.groundAnchorA", j->groundAnchorA);
+        t.vec(in, "jd.groundAnchorB", j->groundAnchorB);
+        t.vec(in, "jd.localAnchorA", j->localAnchorA);
+        t.vec(in, "jd.localAnchorB", j->localAnchorB);
+        t.num(in, "jd.lengthA", j->lengthA);
+        t.num(in, "jd.lengthB", j->lengthB);
+        t.num(in, "jd.ratio", j->ratio);
+        break;
+    }
+    t.put("  joints[%d] = m_world.CreateJoint(&jd);\n", j->dumpIndex);
+}
+
+static std::string DumpWorld(World& w) {                                // b2world.d:796-855
+    DumpText t;
+    if (w.flags & World::kLocked) return t.s;
+    t.put("b2Vec2 g(%.15ef, %.15ef);\n", (double)w.gravity.x, (double)w.gravity.y);
+    t.put("m_world.SetGravity(g);\n");
+    t.put("b2Body** bodies = cast(b2Body**)b2Alloc(%d * (b2Body*).sizeof);\n", w.bodyCount);
+    t.put("b2Joint joints = cast(b2Joint)b2Alloc(%d * (b2Joint).sizeof);\n", w.jointCount);
+    int i = 0;
+    for (Body* b = w.bodyList; b; b = b->next, ++i) {                   // b2body.d:992-1022
+        b->islandIndex = i;
+        const char* in = "  ";
+        t.put("{\n");
+        t.put("  b2BodyDef bd;\n");
+        t.put("  bd.type = b2BodyType(%d);\n", b->type);
+        t.vec(in, "bd.position", b->xf.p);
+        t.num(in, "bd.angle", b->sweep.a);
+        t.vec(in, "bd.linearVelocity", b->linearVelocity);
+        t.num(in, "bd.angularVelocity", b->angularVelocity);
+        t.num(in, "bd.linearDamping", b->linearDamping);
+        t.num(in, "bd.angularDamping", b->angularDamping);
+        t.flag(in, "bd.allowSleep", b->flags & kBodyAutoSleep);
+        t.flag(in, "bd.awake", b->flags & kBodyAwake);
+        t.flag(in, "bd.fixedRotation", b->flags & kBodyFixedRotation);
+        t.flag(in, "bd.bullet", b->flags & kBodyBullet);
+        t.flag(in, "bd.active", b->flags & kBodyActive);
+        t.num(in, "bd.gravityScale", b->gravityScale);
+        t.put("  bodies[%d] = m_world.CreateBody(&bd);\n", i);
+        t.put("\n");
+        int lastChain = -1;
+        for (Fixture* f = b->fixtureList; f; f = f->next) {
+            if (f->chain >= 0 && f->chain == lastChain) continue;       // one fixture per chain
+            lastChain = f->chain;
+            t.put("  {\n");
+            DumpFixture(t, w, f, i);
+            t.put("  }\n");
+        }
+        t.put("}\n");
+    }
+    i = 0;
+    for (Joint* j = w.jointList; j; j = j->next) j->dumpIndex = i++;    // b2Joint.m_index
+    for (Joint* j = w.jointList; j; j = j->next) {                      // no gear joints: one pass
+        t.put("{\n");
+        DumpJoint(t, j);
+        t.put("}\n");
+    }
+    t.put("b2Free(joints);\n");
+    t.put("b2Free(bodies);\n");
+    t.put("joints = null;\n");
+    t.put("bodies = null;\n");
+    return t.s;
+}
+
 // ------------------------------------------------------------ world queries
 // Shape ray casts (b2RayCastInput p1, p2, maxFraction -> fraction, normal).
 static bool RayCastCircle(const Shape& s, const Transform& xf, Vec2 p1, Vec2 p2, f32 maxFraction, f32* fraction,
@@ -5018,6 +5247,17 @@ void orc_query_aabb_many(orc_world* w, int n, const float* boxes, int* counts, i
                                    out + (size_t)i * cap, cap);
 }
 
+// b2World.Dump into buf (NUL-terminated when it fits); returns the text's length
+int orc_world_dump(orc_world* w, char* buf, int cap) {
+    std::string s = DumpWorld(w->w);
+    if (buf && cap > 0) {
+        size_t n = s.size() < (size_t)cap - 1 ? s.size() : (size_t)cap - 1;
+        memcpy(buf, s.data(), n);
+        buf[n] = 0;
+    }
+    return (int)s.size();
+}
+
 void orc_set_trig_mode(int mode) { g_trig_mode = mode; }
 int orc_get_trig_mode(void) { return g_trig_mode; }
 
@@ -5064,6 +5304,14 @@ int orc_fixture_create_chain(orc_world* w, int body, const dbox_vec2* vertices, 
     d.density = 0.0f;                                                   // a chain has no mass
     int first = -1;
     const int m = (int)v.size();
+    ChainRec rec;
+    rec.vertices = v;
+    rec.prevVertex = pv;
+    rec.nextVertex = nv;
+    rec.hasPrevVertex = hasPrev;
+    rec.hasNextVertex = hasNext;
+    rec.density = def->density;
+    const int chain_id = (int)w->w.chains.size();
     for (int i = 0; i + 1 < m; ++i) {
         Shape s;
         s.type = kEdge;
@@ -5077,9 +5325,12 @@ int orc_fixture_create_chain(orc_world* w, int body, const dbox_vec2* vertices, 
         else { s.vertex3 = nv; s.hasVertex3 = hasNext; }
         if (!s.hasVertex0) s.vertex0.SetZero();
         if (!s.hasVertex3) s.vertex3.SetZero();
-        int idx = w->w.CreateFixture(w->w.bodiesByIndex[body], s, &d)->index;
-        if (first < 0) first = idx;
+        Fixture* f = w->w.CreateFixture(w->w.bodiesByIndex[body], s, &d);
+        f->chain = chain_id;
+        if (first < 0) first = f->index;
     }
+    rec.first = first;
+    w->w.chains.push_back(rec);
     return first;
 }
 
