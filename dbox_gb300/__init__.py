@@ -59,6 +59,8 @@ def lib():
     L.dbox_joint_set_mouse_target.argtypes = [vp, i32, i32, abi.Vec2]
     L.dbox_world_query_aabb.argtypes = [vp, i32, vp, vp, i32, vp, vp]
     L.dbox_world_get_stream.argtypes = [vp, ctypes.POINTER(vp)]
+    for fn in ("dbox_body_destroy", "dbox_fixture_destroy", "dbox_joint_destroy"):
+        getattr(L, fn).argtypes = [vp, i32, i32]
     L.dbox_world_dump.argtypes = [vp, i32, ctypes.c_char_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]
     L.dbox_world_raycast.argtypes = [vp, i32, vp, vp, vp, i32, i32, vp, vp]
     L.dbox_world_query_aabb_device.argtypes = [vp, i32, vp, vp, i32, vp, vp]
@@ -304,6 +306,18 @@ class World:
         _check(lib().dbox_fixture_create(self.h, world, body, abi.ptr(sd), abi.ptr(fd), ctypes.byref(out)),
                "dbox_fixture_create")
         return out.value
+
+    def destroy_body(self, world, body):
+        """b2World.DestroyBody: its joints, contacts (EndContact to the listener) and fixtures."""
+        _check(lib().dbox_body_destroy(self.h, world, body), "dbox_body_destroy")
+
+    def destroy_fixture(self, world, fixture):
+        """b2Body.DestroyFixture (a chain child destroys its chain)."""
+        _check(lib().dbox_fixture_destroy(self.h, world, fixture), "dbox_fixture_destroy")
+
+    def destroy_joint(self, world, joint):
+        """b2World.DestroyJoint."""
+        _check(lib().dbox_joint_destroy(self.h, world, joint), "dbox_joint_destroy")
 
     def create_chain(self, world, body, vertices, loop=False, prev=None, next=None, fixture=None):
         """b2Body.CreateFixture with a b2ChainShape (CreateChain / CreateLoop, SetPrevVertex /

@@ -90,10 +90,43 @@ struct ChainRec {
     int has_prev, has_next;
     float density;
     int first;
+    int dead;
+};
+
+// b2DynamicTree node allocation as far as proxy ids depend on it (b2dynamictree.d:110-134,
+// 516-564): freed nodes are reused last in, first out, before never-used ones.  A new proxy
+// takes a leaf and then, unless the tree was empty, an internal parent; destroying a proxy
+// frees its parent (unless it was the root) and then the leaf.  So the stack always holds
+// (leaf, parent) pairs, with one lone leaf on top while the tree is empty: a parent's id is
+// never handed out as a proxy id, and its place in the stack is all that is kept (-1).  Moving
+// a proxy frees and at once retakes its parent, which changes nothing here.
+struct ProxyIds {
+    std::vector<int> free_nodes;
+    int fresh = 0;      // lowest node id never used
+    int live = 0;       // proxies in the tree
+    int take() {
+        if (free_nodes.empty()) return fresh++;
+        int id = free_nodes.back();
+        free_nodes.pop_back();
+        return id;
+    }
+    int create() {
+        int id = take();
+        if (live > 0) take();                                           // the new leaf's parent
+        ++live;
+        return id;
+    }
+    void destroy(int id) {
+        if (live > 1) free_nodes.push_back(-1);                         // RemoveLeaf frees the parent first
+        free_nodes.push_back(id);
+        --live;
+    }
 };
 
 struct HostWorld {
     std::vector<ChainRec> chains;
+    ProxyIds ids;
+    std::vector<char> body_dead;   // destroyed bodies (kept as all-zero records so indices stay put)
     std::vector<dbox_body_state> bs;
     std::vector<dg::BodyStatic> bst;
     std::vector<std::vector<int>> body_fix;     // fixture indices per body, newest first
@@ -102,7 +135,6 @@ struct HostWorld {
     std::vector<dg::DJoint> jt;
     std::vector<dbox_contact_state> ct;
     dg::WorldDyn wd;
-    int proxy_count = 0;
     HostWorld() { memset(&wd, 0, sizeof(wd)); wd.flags = 4u; wd.step_complete = 1; }
 };
 
@@ -466,6 +498,7 @@ int upload(dbox_world* w) {
         // joint adjacency, newest joint first (b2world.d:226-242 head insertion)
         std::vector<std::vector<std::pair<int, int>>> jadj(hw.bs.size());
         for (int j = 0; j < (int)hw.jt.size(); ++j) {
+            if (hw.jt[j].type < 0) continue;                            // destroyed
             jadj[hw.jt[j].body_a].push_back({j, hw.jt[j].body_b});
             jadj[hw.jt[j].body_b].push_back({j, hw.jt[j].body_a});
         }
@@ -747,6 +780,8 @@ void fill_body_state(const dbox_body_def* d, dbox_body_state* s, dg::BodyStatic*
 }
 
 // b2Body.ResetMassData (b2body.d:555-625)
+bool body_gone(const HostWorld& hw, int b) { return b < (int)hw.body_dead.size() && hw.body_dead[b]; }
+
 void reset_mass(HostWorld& hw, int b) {
     dbox_body_state& s = hw.bs[b];
     float mass = 0.0f, invMass = 0.0f, I = 0.0f, invI = 0.0f;
@@ -893,8 +928,7 @@ int create_fixture(HostWorld& hw, int body, const dbox_shape_def* shape, const d
         p.fat_aabb[0] = a[0] - 0.1f; p.fat_aabb[1] = a[1] - 0.1f;
         p.fat_aabb[2] = a[2] + 0.1f; p.fat_aabb[3] = a[3] + 0.1f;
         p.moved = 1;
-        p.proxy_id = hw.proxy_count == 0 ? 0 : 2 * hw.proxy_count - 1;
-        ++hw.proxy_count;
+        p.proxy_id = hw.ids.create();
     }
     hw.px.push_back(p);
     hw.body_fix[body].insert(hw.body_fix[body].begin(), idx);
@@ -919,7 +953,8 @@ int link_joint(HostWorld& hw, const dg::DJoint& j) {
 
 int create_joint(HostWorld& hw, const dbox_revolute_def* d) {
     int nb = (int)hw.bs.size();
-    if (d->body_a < 0 || d->body_a >= nb || d->body_b < 0 || d->body_b >= nb || d->body_a == d->body_b) return -1;
+    if (d->body_a < 0 || d->body_a >= nb || d->body_b < 0 || d->body_b >= nb || d->body_a == d->body_b ||
+        body_gone(hw, d->body_a) || body_gone(hw, d->body_b)) return -1;
     dg::DJoint j;
     memset(&j, 0, sizeof(j));
     j.body_a = d->body_a;
@@ -941,7 +976,8 @@ int create_joint(HostWorld& hw, const dbox_revolute_def* d) {
 // b2World.CreateJoint with a b2DistanceJointDef (b2world.d:196-261, b2distancejoint.d:122-133)
 int create_distance_joint(HostWorld& hw, const dbox_distance_def* d) {
     int nb = (int)hw.bs.size();
-    if (d->body_a < 0 || d->body_a >= nb || d->body_b < 0 || d->body_b >= nb || d->body_a == d->body_b) return -1;
+    if (d->body_a < 0 || d->body_a >= nb || d->body_b < 0 || d->body_b >= nb || d->body_a == d->body_b ||
+        body_gone(hw, d->body_a) || body_gone(hw, d->body_b)) return -1;
     dg::DJoint j;
     memset(&j, 0, sizeof(j));
     j.type = dg::kDistanceJoint;
@@ -1035,7 +1071,7 @@ int32_t dbox_fixture_create(dbox_world* w, int32_t world, int32_t body, const db
     if (!w || !shape || !def || world < 0 || world >= (int)w->worlds.size())
         return fail(DBOX_ERR_INVALID, "dbox_fixture_create: bad arguments");
     HostWorld& hw0 = w->worlds[world];
-    if (body < 0 || body >= (int)hw0.bs.size()) return fail(DBOX_ERR_INVALID, "dbox_fixture_create: no body %d", body);
+    if (body < 0 || body >= (int)hw0.bs.size() || body_gone(hw0, body)) return fail(DBOX_ERR_INVALID, "dbox_fixture_create: no body %d", body);
     int rc = prepare_edit(w);
     if (rc) return rc;
     int idx = create_fixture(w->worlds[world], body, shape, def);
@@ -1061,6 +1097,7 @@ static ChainRec make_chain(const dbox_vec2* vertices, int count, bool loop, cons
     }
     c.density = 0.0f;
     c.first = -1;
+    c.dead = 0;
     return c;
 }
 
@@ -1093,7 +1130,7 @@ int32_t dbox_fixture_create_chain(dbox_world* w, int32_t world, int32_t body, co
     if (!w || !vertices || !def || world < 0 || world >= (int)w->worlds.size() || count < (loop ? 3 : 2))
         return fail(DBOX_ERR_INVALID, "dbox_fixture_create_chain: bad arguments");
     HostWorld& hw0 = w->worlds[world];
-    if (body < 0 || body >= (int)hw0.bs.size()) return fail(DBOX_ERR_INVALID, "dbox_fixture_create_chain: no body %d", body);
+    if (body < 0 || body >= (int)hw0.bs.size() || body_gone(hw0, body)) return fail(DBOX_ERR_INVALID, "dbox_fixture_create_chain: no body %d", body);
     int rc = prepare_edit(w);
     if (rc) return rc;
     dbox_fixture_def d = *def;
@@ -1112,6 +1149,165 @@ int32_t dbox_fixture_create_chain(dbox_world* w, int32_t world, int32_t body, co
     return DBOX_OK;
 }
 
+// ---------------------------------------------------------------- destruction
+// b2World.DestroyBody / DestroyJoint and b2Body.DestroyFixture on the host mirrors, between
+// steps.  Destroyed bodies, fixtures and joints keep their indices as all-zero records (a
+// fixture without a proxy, a joint of type -1); the contact list loses the destroyed
+// contacts and keeps its order.  A body's contact list is its contacts newest first (the
+// host list is oldest first), its joint list its joints newest first.
+namespace {
+
+void wake(dbox_body_state& s) {                                         // b2Body.SetAwake(true), b2body.d:827-846
+    if ((s.flags & dg::kBodyAwake) == 0) {
+        s.flags |= dg::kBodyAwake;
+        s.sleep_time = 0.0f;
+    }
+}
+
+// b2ContactManager.Destroy (b2contactmanager.d:183-246) with b2Contact.Destroy (b2contact.d:402-422)
+void destroy_contact(HostWorld& hw, int ci, int world, std::vector<dbox_contact_event>& ev) {
+    const dbox_contact_state c = hw.ct[ci];
+    const dg::DFixture& fa = hw.fx[c.fixture_a];
+    const dg::DFixture& fb = hw.fx[c.fixture_b];
+    if (c.flags & dg::kContactTouching) {
+        dbox_contact_event e;
+        memset(&e, 0, sizeof(e));
+        e.kind = DBOX_EVENT_END;
+        e.world = world;
+        e.fixture_a = c.fixture_a;
+        e.fixture_b = c.fixture_b;
+        e.point_count = c.point_count;
+        ev.push_back(e);
+    }
+    if (c.point_count > 0 && !fa.sensor && !fb.sensor) {
+        wake(hw.bs[fa.body]);
+        wake(hw.bs[fb.body]);
+    }
+    hw.ct.erase(hw.ct.begin() + ci);
+}
+
+void destroy_joint(HostWorld& hw, int j) {                              // b2world.d:265-360
+    dg::DJoint& d = hw.jt[j];
+    const bool collide = d.collide_connected != 0;
+    const int A = d.body_a, B = d.body_b;
+    wake(hw.bs[A]);
+    wake(hw.bs[B]);
+    memset(&d, 0, sizeof(d));
+    d.type = -1;
+    d.body_a = A;
+    d.body_b = B;
+    if (!collide) {
+        for (auto& c : hw.ct) {
+            int a = hw.fx[c.fixture_a].body, b = hw.fx[c.fixture_b].body;
+            if ((a == A && b == B) || (a == B && b == A)) c.flags |= dg::kContactFilter;
+        }
+    }
+}
+
+// the fixtures that are one reference fixture: a chain's child edges (child order), else fi
+std::vector<int> fixture_group(const HostWorld& hw, int fi) {
+    for (const ChainRec& c : hw.chains)
+        if (!c.dead && fi >= c.first && fi < c.first + (int)c.v.size() - 1) {
+            std::vector<int> g;
+            for (int i = c.first; i < c.first + (int)c.v.size() - 1; ++i) g.push_back(i);
+            return g;
+        }
+    return std::vector<int>(1, fi);
+}
+
+// b2Fixture.DestroyProxies (b2fixture.d:467-478) of a group, in child order
+void free_proxies(HostWorld& hw, const std::vector<int>& g) {
+    for (int fi : g) {
+        dbox_proxy_state& p = hw.px[fi];
+        if (p.proxy_id >= 0) hw.ids.destroy(p.proxy_id);
+        memset(&p, 0, sizeof(p));
+        p.proxy_id = -1;
+    }
+}
+
+bool in_group(const std::vector<int>& g, int fi) { return std::find(g.begin(), g.end(), fi) != g.end(); }
+
+void destroy_fixture(HostWorld& hw, int fi, int world, std::vector<dbox_contact_event>& ev) {   // b2body.d:179-247
+    const int b = hw.fx[fi].body;
+    const std::vector<int> g = fixture_group(hw, fi);
+    std::vector<int>& list = hw.body_fix[b];
+    list.erase(std::remove_if(list.begin(), list.end(), [&](int f) { return in_group(g, f); }), list.end());
+    for (int ci = (int)hw.ct.size() - 1; ci >= 0; --ci) {
+        const dbox_contact_state& c = hw.ct[ci];
+        if (in_group(g, c.fixture_a) || in_group(g, c.fixture_b)) destroy_contact(hw, ci, world, ev);
+    }
+    if (hw.bs[b].flags & dg::kBodyActive) free_proxies(hw, g);
+    for (ChainRec& c : hw.chains)
+        if (c.first == g[0] && g.size() > 1) c.dead = 1;                // the chain is gone
+    reset_mass(hw, b);
+}
+
+void destroy_body(HostWorld& hw, int b, int world, std::vector<dbox_contact_event>& ev) {      // b2world.d:105-193
+    for (int j = (int)hw.jt.size() - 1; j >= 0; --j)
+        if (hw.jt[j].type >= 0 && (hw.jt[j].body_a == b || hw.jt[j].body_b == b)) destroy_joint(hw, j);
+    for (int ci = (int)hw.ct.size() - 1; ci >= 0; --ci) {
+        const dbox_contact_state& c = hw.ct[ci];
+        if (hw.fx[c.fixture_a].body == b || hw.fx[c.fixture_b].body == b) destroy_contact(hw, ci, world, ev);
+    }
+    std::vector<int> list = hw.body_fix[b];
+    for (size_t k = 0; k < list.size();) {
+        const std::vector<int> g = fixture_group(hw, list[k]);
+        while (k < list.size() && in_group(g, list[k])) ++k;            // a chain is one fixture
+        free_proxies(hw, g);
+        for (ChainRec& c : hw.chains)
+            if (c.first == g[0] && g.size() > 1) c.dead = 1;
+    }
+    hw.body_fix[b].clear();
+    memset(&hw.bs[b], 0, sizeof(hw.bs[b]));
+    if ((int)hw.body_dead.size() < (int)hw.bs.size()) hw.body_dead.resize(hw.bs.size(), 0);
+    hw.body_dead[b] = 1;
+}
+
+int deliver_host_events(dbox_world* w, const std::vector<dbox_contact_event>& ev) {
+    if (w->listener && !ev.empty()) w->listener(ev.data(), (int32_t)ev.size(), w->listener_user);
+    return DBOX_OK;
+}
+
+}  // namespace
+
+int32_t dbox_body_destroy(dbox_world* w, int32_t world, int32_t body) {
+    if (!w || world < 0 || world >= (int)w->worlds.size()) return fail(DBOX_ERR_INVALID, "dbox_body_destroy: bad world");
+    HostWorld& hw0 = w->worlds[world];
+    if (body < 0 || body >= (int)hw0.bs.size() || body_gone(hw0, body))
+        return fail(DBOX_ERR_INVALID, "dbox_body_destroy: no body %d", body);
+    int rc = prepare_edit(w);
+    if (rc) return rc;
+    std::vector<dbox_contact_event> ev;
+    destroy_body(w->worlds[world], body, world, ev);
+    return deliver_host_events(w, ev);
+}
+
+int32_t dbox_fixture_destroy(dbox_world* w, int32_t world, int32_t fixture) {
+    if (!w || world < 0 || world >= (int)w->worlds.size()) return fail(DBOX_ERR_INVALID, "dbox_fixture_destroy: bad world");
+    HostWorld& hw0 = w->worlds[world];
+    if (fixture < 0 || fixture >= (int)hw0.fx.size() || body_gone(hw0, hw0.fx[fixture].body))
+        return fail(DBOX_ERR_INVALID, "dbox_fixture_destroy: no fixture %d", fixture);
+    const std::vector<int>& list = hw0.body_fix[hw0.fx[fixture].body];
+    if (std::find(list.begin(), list.end(), fixture) == list.end())
+        return fail(DBOX_ERR_INVALID, "dbox_fixture_destroy: fixture %d was destroyed", fixture);
+    int rc = prepare_edit(w);
+    if (rc) return rc;
+    std::vector<dbox_contact_event> ev;
+    destroy_fixture(w->worlds[world], fixture, world, ev);
+    return deliver_host_events(w, ev);
+}
+
+int32_t dbox_joint_destroy(dbox_world* w, int32_t world, int32_t joint) {
+    if (!w || world < 0 || world >= (int)w->worlds.size()) return fail(DBOX_ERR_INVALID, "dbox_joint_destroy: bad world");
+    HostWorld& hw0 = w->worlds[world];
+    if (joint < 0 || joint >= (int)hw0.jt.size() || hw0.jt[joint].type < 0)
+        return fail(DBOX_ERR_INVALID, "dbox_joint_destroy: no joint %d", joint);
+    int rc = prepare_edit(w);
+    if (rc) return rc;
+    destroy_joint(w->worlds[world], joint);
+    return DBOX_OK;
+}
+
 int32_t dbox_joint_create_revolute(dbox_world* w, int32_t world, const dbox_revolute_def* def, int32_t* out_joint) {
     if (!w || !def || world < 0 || world >= (int)w->worlds.size()) return fail(DBOX_ERR_INVALID, "dbox_joint_create_revolute: bad arguments");
     int rc = prepare_edit(w);
@@ -1125,7 +1321,8 @@ int32_t dbox_joint_create_revolute(dbox_world* w, int32_t world, const dbox_revo
 // b2World.CreateJoint with a b2RopeJointDef (b2ropejoint.d:140-153)
 int create_rope_joint(HostWorld& hw, const dbox_rope_def* d) {
     int nb = (int)hw.bs.size();
-    if (d->body_a < 0 || d->body_a >= nb || d->body_b < 0 || d->body_b >= nb || d->body_a == d->body_b) return -1;
+    if (d->body_a < 0 || d->body_a >= nb || d->body_b < 0 || d->body_b >= nb || d->body_a == d->body_b ||
+        body_gone(hw, d->body_a) || body_gone(hw, d->body_b)) return -1;
     dg::DJoint j;
     memset(&j, 0, sizeof(j));
     j.type = dg::kRopeJoint;
@@ -1141,7 +1338,8 @@ int create_rope_joint(HostWorld& hw, const dbox_rope_def* d) {
 // b2World.CreateJoint with a b2WeldJointDef (b2weldjoint.d:107-119)
 int create_weld_joint(HostWorld& hw, const dbox_weld_def* d) {
     int nb = (int)hw.bs.size();
-    if (d->body_a < 0 || d->body_a >= nb || d->body_b < 0 || d->body_b >= nb || d->body_a == d->body_b) return -1;
+    if (d->body_a < 0 || d->body_a >= nb || d->body_b < 0 || d->body_b >= nb || d->body_a == d->body_b ||
+        body_gone(hw, d->body_a) || body_gone(hw, d->body_b)) return -1;
     dg::DJoint j;
     memset(&j, 0, sizeof(j));
     j.type = dg::kWeldJoint;
@@ -1159,7 +1357,8 @@ int create_weld_joint(HostWorld& hw, const dbox_weld_def* d) {
 // b2World.CreateJoint with a b2FrictionJointDef / b2MotorJointDef (b2frictionjoint.d:85-96, b2motorjoint.d:92-106)
 int create_friction_joint(HostWorld& hw, const dbox_friction_def* d) {
     int nb = (int)hw.bs.size();
-    if (d->body_a < 0 || d->body_a >= nb || d->body_b < 0 || d->body_b >= nb || d->body_a == d->body_b) return -1;
+    if (d->body_a < 0 || d->body_a >= nb || d->body_b < 0 || d->body_b >= nb || d->body_a == d->body_b ||
+        body_gone(hw, d->body_a) || body_gone(hw, d->body_b)) return -1;
     dg::DJoint j;
     memset(&j, 0, sizeof(j));
     j.type = dg::kFrictionJoint;
@@ -1175,7 +1374,8 @@ int create_friction_joint(HostWorld& hw, const dbox_friction_def* d) {
 
 int create_motor_joint(HostWorld& hw, const dbox_motor_def* d) {
     int nb = (int)hw.bs.size();
-    if (d->body_a < 0 || d->body_a >= nb || d->body_b < 0 || d->body_b >= nb || d->body_a == d->body_b) return -1;
+    if (d->body_a < 0 || d->body_a >= nb || d->body_b < 0 || d->body_b >= nb || d->body_a == d->body_b ||
+        body_gone(hw, d->body_a) || body_gone(hw, d->body_b)) return -1;
     dg::DJoint j;
     memset(&j, 0, sizeof(j));
     j.type = dg::kMotorJoint;
@@ -1193,7 +1393,8 @@ int create_motor_joint(HostWorld& hw, const dbox_motor_def* d) {
 // b2World.CreateJoint with a b2WheelJointDef (b2wheeljoint.d:110-139)
 int create_wheel_joint(HostWorld& hw, const dbox_wheel_def* d) {
     int nb = (int)hw.bs.size();
-    if (d->body_a < 0 || d->body_a >= nb || d->body_b < 0 || d->body_b >= nb || d->body_a == d->body_b) return -1;
+    if (d->body_a < 0 || d->body_a >= nb || d->body_b < 0 || d->body_b >= nb || d->body_a == d->body_b ||
+        body_gone(hw, d->body_a) || body_gone(hw, d->body_b)) return -1;
     dg::DJoint j;
     memset(&j, 0, sizeof(j));
     j.type = dg::kWheelJoint;
@@ -1216,7 +1417,8 @@ int create_wheel_joint(HostWorld& hw, const dbox_wheel_def* d) {
 // normalised as b2Vec2.Normalize does (b2math.d:160-175)
 int create_prismatic_joint(HostWorld& hw, const dbox_prismatic_def* d) {
     int nb = (int)hw.bs.size();
-    if (d->body_a < 0 || d->body_a >= nb || d->body_b < 0 || d->body_b >= nb || d->body_a == d->body_b) return -1;
+    if (d->body_a < 0 || d->body_a >= nb || d->body_b < 0 || d->body_b >= nb || d->body_a == d->body_b ||
+        body_gone(hw, d->body_a) || body_gone(hw, d->body_b)) return -1;
     dg::DJoint j;
     memset(&j, 0, sizeof(j));
     j.type = dg::kPrismaticJoint;
@@ -1247,7 +1449,8 @@ int create_prismatic_joint(HostWorld& hw, const dbox_prismatic_def* d) {
 // b2World.CreateJoint with a b2PulleyJointDef (b2pulleyjoint.d:116-131)
 int create_pulley_joint(HostWorld& hw, const dbox_pulley_def* d) {
     int nb = (int)hw.bs.size();
-    if (d->body_a < 0 || d->body_a >= nb || d->body_b < 0 || d->body_b >= nb || d->body_a == d->body_b) return -1;
+    if (d->body_a < 0 || d->body_a >= nb || d->body_b < 0 || d->body_b >= nb || d->body_a == d->body_b ||
+        body_gone(hw, d->body_a) || body_gone(hw, d->body_b)) return -1;
     dg::DJoint j;
     memset(&j, 0, sizeof(j));
     j.type = dg::kPulleyJoint;
@@ -1269,7 +1472,8 @@ int create_pulley_joint(HostWorld& hw, const dbox_pulley_def* d) {
 // target in body B's frame now (b2MulT(xf, v), b2math.d:743-751)
 int create_mouse_joint(HostWorld& hw, const dbox_mouse_def* d) {
     int nb = (int)hw.bs.size();
-    if (d->body_a < 0 || d->body_a >= nb || d->body_b < 0 || d->body_b >= nb || d->body_a == d->body_b) return -1;
+    if (d->body_a < 0 || d->body_a >= nb || d->body_b < 0 || d->body_b >= nb || d->body_a == d->body_b ||
+        body_gone(hw, d->body_a) || body_gone(hw, d->body_b)) return -1;
     dg::DJoint j;
     memset(&j, 0, sizeof(j));
     j.type = dg::kMouseJoint;
@@ -2272,13 +2476,22 @@ struct Dumper {
     }
 
     void world(const HostWorld& hw, float2 g) {
-        const int nb = (int)hw.bs.size(), nj = (int)hw.jt.size();
+        // the world lists, newest first, without destroyed bodies and joints
+        std::vector<int> bodies, joints, list_index(hw.bs.size(), -1);
+        for (int b = (int)hw.bs.size() - 1; b >= 0; --b)
+            if (!body_gone(hw, b)) {
+                list_index[b] = (int)bodies.size();
+                bodies.push_back(b);
+            }
+        for (int j = (int)hw.jt.size() - 1; j >= 0; --j)
+            if (hw.jt[j].type >= 0) joints.push_back(j);
+        const int nb = (int)bodies.size(), nj = (int)joints.size();
         put("b2Vec2 g(%.15ef, %.15ef);\n", (double)g.x, (double)g.y);
         put("m_world.SetGravity(g);\n");
         put("b2Body** bodies = cast(b2Body**)b2Alloc(%d * (b2Body*).sizeof);\n", nb);
         put("b2Joint joints = cast(b2Joint)b2Alloc(%d * (b2Joint).sizeof);\n", nj);
         for (int i = 0; i < nb; ++i) {
-            const int b = nb - 1 - i;
+            const int b = bodies[i];
             const dbox_body_state& s = hw.bs[b];
             const dg::BodyStatic& st = hw.bst[b];
             const char* in = "  ";
@@ -2303,7 +2516,7 @@ struct Dumper {
             for (int fi : hw.body_fix[b]) {
                 const ChainRec* chain = nullptr;
                 for (const ChainRec& c : hw.chains)
-                    if (fi >= c.first && fi < c.first + (int)c.v.size() - 1) chain = &c;
+                    if (!c.dead && fi >= c.first && fi < c.first + (int)c.v.size() - 1) chain = &c;
                 if (chain && chain == last) continue;                   // one fixture per chain
                 last = chain;
                 put("  {\n");
@@ -2313,9 +2526,9 @@ struct Dumper {
             put("}\n");
         }
         for (int k = 0; k < nj; ++k) {                                  // no gear joints: one pass
-            const dg::DJoint& j = hw.jt[nj - 1 - k];
+            const dg::DJoint& j = hw.jt[joints[k]];
             put("{\n");
-            joint(j, nb - 1 - j.body_a, nb - 1 - j.body_b, k);
+            joint(j, list_index[j.body_a], list_index[j.body_b], k);
             put("}\n");
         }
         put("b2Free(joints);\n");

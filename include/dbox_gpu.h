@@ -307,6 +307,19 @@ int32_t dbox_fixture_create(dbox_world* w, int32_t world, int32_t body, const db
 int32_t dbox_fixture_create_chain(dbox_world* w, int32_t world, int32_t body, const dbox_vec2* vertices, int32_t count,
                                   int32_t loop, const dbox_vec2* prev_vertex, const dbox_vec2* next_vertex,
                                   const dbox_fixture_def* def, int32_t* out_first);
+/* b2World.DestroyBody (dynamics/b2world.d:105-193): its joints (newest first), its contacts
+ * (EndContact to the listener for touching ones, waking both bodies of contacts with points),
+ * then its fixtures' broad-phase proxies.  b2Body.DestroyFixture (dynamics/b2body.d:179-247):
+ * the fixture's contacts, its proxies, then the body's mass (a chain child destroys its whole
+ * chain, as the reference's chain fixture).  b2World.DestroyJoint (dynamics/b2world.d:265-360):
+ * wakes both bodies and flags their contacts for filtering unless collideConnected.  Between
+ * steps only.  Indices of other bodies, fixtures and joints do not change; a destroyed one
+ * exports as an all-zero record (a proxy of id -1).  New proxies take the ids the reference's
+ * tree hands out: freed leaves last in, first out, then never-used node ids. */
+int32_t dbox_body_destroy(dbox_world* w, int32_t world, int32_t body);
+int32_t dbox_fixture_destroy(dbox_world* w, int32_t world, int32_t fixture);
+int32_t dbox_joint_destroy(dbox_world* w, int32_t world, int32_t joint);
+
 /* b2World.CreateJoint with a b2RevoluteJointDef (b2world.d:196-261, joints/b2revolutejoint.d). */
 int32_t dbox_joint_create_revolute(dbox_world* w, int32_t world, const dbox_revolute_def* def,
                                    int32_t* out_joint);

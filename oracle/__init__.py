@@ -50,6 +50,8 @@ def lib():
         L.orc_raycast.argtypes = [vp, f32, f32, f32, f32, i32, vp, i32]
         L.orc_world_dump.argtypes = [vp, ctypes.c_char_p, i32]
         L.orc_body_create.argtypes = [vp, vp]
+        for fn in ("orc_body_destroy", "orc_fixture_destroy", "orc_joint_destroy"):
+            getattr(L, fn).argtypes = [vp, i32]
         L.orc_fixture_create.argtypes = [vp, i32, vp, vp]
         L.orc_joint_create_revolute.argtypes = [vp, vp]
         L.orc_raycast_many.argtypes = [vp, i32, vp, vp, i32, vp, vp, i32]
@@ -232,6 +234,18 @@ class OracleWorld:
         if r < 0:
             raise ValueError("oracle fixture creation failed")
         return r
+
+    def destroy_body(self, body):
+        if lib().orc_body_destroy(self.h, body) < 0:
+            raise ValueError("oracle: no body %d" % body)
+
+    def destroy_fixture(self, fixture):
+        if lib().orc_fixture_destroy(self.h, fixture) < 0:
+            raise ValueError("oracle: no fixture %d" % fixture)
+
+    def destroy_joint(self, joint):
+        if lib().orc_joint_destroy(self.h, joint) < 0:
+            raise ValueError("oracle: no joint %d" % joint)
 
     def create_joint(self, kind, d):
         dd = np.ascontiguousarray(np.array([d], getattr(abi, self._JOINTS[kind])))

@@ -1629,6 +1629,10 @@ struct DynamicTree {
         InsertLeaf(proxyId);
         return proxyId;
     }
+    void DestroyProxy(int proxyId) {                                    // b2dynamictree.d:127-134
+        RemoveLeaf(proxyId);
+        FreeNode(proxyId);
+    }
     bool MoveProxy(int proxyId, const AABB& aabb, Vec2 displacement) {  // b2dynamictree.d:140-184
         if (nodes[proxyId].aabb.Contains(aabb)) return false;
         RemoveLeaf(proxyId);
@@ -4001,6 +4005,12 @@ struct BroadPhase {                                                     // colli
         if (buffer) BufferMove(proxyId);
     }
     void BufferMove(int proxyId) { moveBuffer.push_back(proxyId); }
+    void DestroyProxy(int proxyId) {                                    // b2broadphase.d: DestroyProxy, UnBufferMove
+        for (int& id : moveBuffer)
+            if (id == proxyId) id = -1;
+        --proxyCount;
+        tree.DestroyProxy(proxyId);
+    }
     bool TestOverlapProxies(int a, int b) const { return TestOverlap(tree.nodes[a].aabb, tree.nodes[b].aabb); }
     bool QueryCallback(int proxyId) {                                   // b2broadphase.d:271-294
         if (proxyId == queryProxyId) return true;
@@ -4516,6 +4526,111 @@ struct World {                                                          // dynam
         j->index = (int)jointsByIndex.size();
         jointsByIndex.push_back(j);
         return j;
+    }
+
+    void DestroyJoint(Joint* j) {                                        // b2world.d:265-360
+        const bool collideConnected = j->collideConnected;
+        if (j->prev) j->prev->next = j->next;
+        if (j->next) j->next->prev = j->prev;
+        if (j == jointList) jointList = j->next;
+        Body* bodyA = j->bodyA;
+        Body* bodyB = j->bodyB;
+        bodyA->SetAwake(true);
+        bodyB->SetAwake(true);
+        if (j->edgeA.prev) j->edgeA.prev->next = j->edgeA.next;
+        if (j->edgeA.next) j->edgeA.next->prev = j->edgeA.prev;
+        if (&j->edgeA == bodyA->jointList) bodyA->jointList = j->edgeA.next;
+        if (j->edgeB.prev) j->edgeB.prev->next = j->edgeB.next;
+        if (j->edgeB.next) j->edgeB.next->prev = j->edgeB.prev;
+        if (&j->edgeB == bodyB->jointList) bodyB->jointList = j->edgeB.next;
+        jointsByIndex[j->index] = nullptr;
+        delete j;
+        --jointCount;
+        if (!collideConnected) {
+            for (ContactEdge* edge = bodyB->contactList; edge; edge = edge->next)
+                if (edge->other == bodyA) edge->contact->flags |= kContactFilter;
+        }
+    }
+
+    // The fixtures that are one reference fixture: a chain's child edges, else the fixture.
+    std::vector<Fixture*> FixtureGroup(Fixture* f) {
+        std::vector<Fixture*> g;
+        if (f->chain < 0) {
+            g.push_back(f);
+            return g;
+        }
+        const ChainRec& c = chains[f->chain];
+        for (int i = 0; i + 1 < (int)c.vertices.size(); ++i) g.push_back(fixturesByIndex[c.first + i]);
+        return g;
+    }
+
+    // b2Fixture.DestroyProxies (b2fixture.d:467-478) for a group, in child order, then free it.
+    void FreeFixtureGroup(const std::vector<Fixture*>& g, bool proxies) {
+        for (Fixture* f : g) {
+            if (proxies && f->proxyCount > 0) {
+                contactManager.broadPhase.DestroyProxy(f->proxy.proxyId);
+                f->proxy.proxyId = -1;
+                f->proxyCount = 0;
+            }
+        }
+        for (Fixture* f : g) {
+            fixturesByIndex[f->index] = nullptr;
+            delete f;
+        }
+    }
+
+    void DestroyFixture(Fixture* fixture) {                              // b2body.d:179-247
+        Body* b = fixture->body;
+        std::vector<Fixture*> g = FixtureGroup(fixture);
+        auto inGroup = [&](const Fixture* f) { return std::find(g.begin(), g.end(), f) != g.end(); };
+        Fixture** node = &b->fixtureList;                               // unlink from the body's list
+        while (*node) {
+            if (inGroup(*node)) *node = (*node)->next;
+            else node = &(*node)->next;
+        }
+        ContactEdge* edge = b->contactList;
+        while (edge) {
+            Contact* c = edge->contact;
+            edge = edge->next;
+            if (inGroup(c->fixtureA) || inGroup(c->fixtureB)) contactManager.Destroy(c);
+        }
+        FreeFixtureGroup(g, (b->flags & kBodyActive) != 0);
+        --b->fixtureCount;
+        b->ResetMassData();
+    }
+
+    void DestroyBody(Body* b) {                                         // b2world.d:105-193
+        JointEdge* je = b->jointList;
+        while (je) {
+            JointEdge* je0 = je;
+            je = je->next;
+            DestroyJoint(je0->joint);
+            b->jointList = je;
+        }
+        b->jointList = nullptr;
+        ContactEdge* ce = b->contactList;
+        while (ce) {
+            ContactEdge* ce0 = ce;
+            ce = ce->next;
+            contactManager.Destroy(ce0->contact);
+        }
+        b->contactList = nullptr;
+        Fixture* f = b->fixtureList;
+        while (f) {
+            std::vector<Fixture*> g = FixtureGroup(f);
+            while (f && std::find(g.begin(), g.end(), f) != g.end()) f = f->next;   // a chain is one fixture
+            FreeFixtureGroup(g, true);
+            b->fixtureList = f;
+            --b->fixtureCount;
+        }
+        b->fixtureList = nullptr;
+        b->fixtureCount = 0;
+        if (b->prev) b->prev->next = b->next;
+        if (b->next) b->next->prev = b->prev;
+        if (b == bodyList) bodyList = b->next;
+        --bodyCount;
+        bodiesByIndex[b->index] = nullptr;
+        delete b;
     }
 
     void Step(f32 dt, int velocityIterations, int positionIterations) { // b2world.d:367-434
@@ -5281,6 +5396,7 @@ int orc_fixture_create(orc_world* w, int body, const dbox_shape_def* shape, cons
     if (body < 0 || body >= (int)w->w.bodiesByIndex.size()) return -1;
     Shape s;
     if (!BuildShape(shape, &s)) return -1;
+    if (!w->w.bodiesByIndex[body]) return -1;
     return w->w.CreateFixture(w->w.bodiesByIndex[body], s, def)->index;
 }
 
@@ -5288,7 +5404,8 @@ int orc_fixture_create(orc_world* w, int body, const dbox_shape_def* shape, cons
 // SetPrevVertex / SetNextVertex) as its child edges (GetChildEdge), in child order
 int orc_fixture_create_chain(orc_world* w, int body, const dbox_vec2* vertices, int count, int loop,
                              const dbox_vec2* prev, const dbox_vec2* next, const dbox_fixture_def* def) {
-    if (body < 0 || body >= (int)w->w.bodiesByIndex.size() || count < (loop ? 3 : 2)) return -1;
+    if (body < 0 || body >= (int)w->w.bodiesByIndex.size() || !w->w.bodiesByIndex[body] || count < (loop ? 3 : 2))
+        return -1;
     std::vector<Vec2> v;
     for (int i = 0; i < count; ++i) v.push_back(Vec2(vertices[i].x, vertices[i].y));
     bool hasPrev = !loop && prev, hasNext = !loop && next;
@@ -5336,68 +5453,97 @@ int orc_fixture_create_chain(orc_world* w, int body, const dbox_vec2* vertices, 
 
 int orc_joint_create_revolute(orc_world* w, const dbox_revolute_def* def) {
     int n = (int)w->w.bodiesByIndex.size();
-    if (def->body_a < 0 || def->body_a >= n || def->body_b < 0 || def->body_b >= n || def->body_a == def->body_b) return -1;
+    if (def->body_a < 0 || def->body_a >= n || def->body_b < 0 || def->body_b >= n || def->body_a == def->body_b ||
+        !w->w.bodiesByIndex[def->body_a] || !w->w.bodiesByIndex[def->body_b]) return -1;
     return w->w.CreateRevolute(def)->index;
 }
 
 int orc_joint_create_distance(orc_world* w, const dbox_distance_def* def) {
     int n = (int)w->w.bodiesByIndex.size();
-    if (def->body_a < 0 || def->body_a >= n || def->body_b < 0 || def->body_b >= n || def->body_a == def->body_b) return -1;
+    if (def->body_a < 0 || def->body_a >= n || def->body_b < 0 || def->body_b >= n || def->body_a == def->body_b ||
+        !w->w.bodiesByIndex[def->body_a] || !w->w.bodiesByIndex[def->body_b]) return -1;
     return w->w.CreateDistance(def)->index;
 }
 
 int orc_joint_create_rope(orc_world* w, const dbox_rope_def* def) {
     int n = (int)w->w.bodiesByIndex.size();
-    if (def->body_a < 0 || def->body_a >= n || def->body_b < 0 || def->body_b >= n || def->body_a == def->body_b) return -1;
+    if (def->body_a < 0 || def->body_a >= n || def->body_b < 0 || def->body_b >= n || def->body_a == def->body_b ||
+        !w->w.bodiesByIndex[def->body_a] || !w->w.bodiesByIndex[def->body_b]) return -1;
     return w->w.CreateRope(def)->index;
 }
 
 int orc_joint_create_weld(orc_world* w, const dbox_weld_def* def) {
     int n = (int)w->w.bodiesByIndex.size();
-    if (def->body_a < 0 || def->body_a >= n || def->body_b < 0 || def->body_b >= n || def->body_a == def->body_b) return -1;
+    if (def->body_a < 0 || def->body_a >= n || def->body_b < 0 || def->body_b >= n || def->body_a == def->body_b ||
+        !w->w.bodiesByIndex[def->body_a] || !w->w.bodiesByIndex[def->body_b]) return -1;
     return w->w.CreateWeld(def)->index;
 }
 
 int orc_joint_create_friction(orc_world* w, const dbox_friction_def* def) {
     int n = (int)w->w.bodiesByIndex.size();
-    if (def->body_a < 0 || def->body_a >= n || def->body_b < 0 || def->body_b >= n || def->body_a == def->body_b) return -1;
+    if (def->body_a < 0 || def->body_a >= n || def->body_b < 0 || def->body_b >= n || def->body_a == def->body_b ||
+        !w->w.bodiesByIndex[def->body_a] || !w->w.bodiesByIndex[def->body_b]) return -1;
     return w->w.CreateFriction(def)->index;
 }
 
 int orc_joint_create_motor(orc_world* w, const dbox_motor_def* def) {
     int n = (int)w->w.bodiesByIndex.size();
-    if (def->body_a < 0 || def->body_a >= n || def->body_b < 0 || def->body_b >= n || def->body_a == def->body_b) return -1;
+    if (def->body_a < 0 || def->body_a >= n || def->body_b < 0 || def->body_b >= n || def->body_a == def->body_b ||
+        !w->w.bodiesByIndex[def->body_a] || !w->w.bodiesByIndex[def->body_b]) return -1;
     return w->w.CreateMotor(def)->index;
 }
 
 int orc_joint_create_wheel(orc_world* w, const dbox_wheel_def* def) {
     int n = (int)w->w.bodiesByIndex.size();
-    if (def->body_a < 0 || def->body_a >= n || def->body_b < 0 || def->body_b >= n || def->body_a == def->body_b) return -1;
+    if (def->body_a < 0 || def->body_a >= n || def->body_b < 0 || def->body_b >= n || def->body_a == def->body_b ||
+        !w->w.bodiesByIndex[def->body_a] || !w->w.bodiesByIndex[def->body_b]) return -1;
     return w->w.CreateWheel(def)->index;
 }
 
 int orc_joint_create_prismatic(orc_world* w, const dbox_prismatic_def* def) {
     int n = (int)w->w.bodiesByIndex.size();
-    if (def->body_a < 0 || def->body_a >= n || def->body_b < 0 || def->body_b >= n || def->body_a == def->body_b) return -1;
+    if (def->body_a < 0 || def->body_a >= n || def->body_b < 0 || def->body_b >= n || def->body_a == def->body_b ||
+        !w->w.bodiesByIndex[def->body_a] || !w->w.bodiesByIndex[def->body_b]) return -1;
     return w->w.CreatePrismatic(def)->index;
 }
 
 int orc_joint_create_pulley(orc_world* w, const dbox_pulley_def* def) {
     int n = (int)w->w.bodiesByIndex.size();
-    if (def->body_a < 0 || def->body_a >= n || def->body_b < 0 || def->body_b >= n || def->body_a == def->body_b) return -1;
+    if (def->body_a < 0 || def->body_a >= n || def->body_b < 0 || def->body_b >= n || def->body_a == def->body_b ||
+        !w->w.bodiesByIndex[def->body_a] || !w->w.bodiesByIndex[def->body_b]) return -1;
     return w->w.CreatePulley(def)->index;
 }
 
 int orc_joint_create_mouse(orc_world* w, const dbox_mouse_def* def) {
     int n = (int)w->w.bodiesByIndex.size();
-    if (def->body_a < 0 || def->body_a >= n || def->body_b < 0 || def->body_b >= n || def->body_a == def->body_b) return -1;
+    if (def->body_a < 0 || def->body_a >= n || def->body_b < 0 || def->body_b >= n || def->body_a == def->body_b ||
+        !w->w.bodiesByIndex[def->body_a] || !w->w.bodiesByIndex[def->body_b]) return -1;
     return w->w.CreateMouse(def)->index;
+}
+
+// b2World.DestroyBody / DestroyJoint, b2Body.DestroyFixture (a chain child destroys its chain)
+int orc_body_destroy(orc_world* w, int body) {
+    if (body < 0 || body >= (int)w->w.bodiesByIndex.size() || !w->w.bodiesByIndex[body]) return -1;
+    w->w.DestroyBody(w->w.bodiesByIndex[body]);
+    return 0;
+}
+
+int orc_fixture_destroy(orc_world* w, int fixture) {
+    if (fixture < 0 || fixture >= (int)w->w.fixturesByIndex.size() || !w->w.fixturesByIndex[fixture]) return -1;
+    w->w.DestroyFixture(w->w.fixturesByIndex[fixture]);
+    return 0;
+}
+
+int orc_joint_destroy(orc_world* w, int joint) {
+    if (joint < 0 || joint >= (int)w->w.jointsByIndex.size() || !w->w.jointsByIndex[joint]) return -1;
+    w->w.DestroyJoint(w->w.jointsByIndex[joint]);
+    return 0;
 }
 
 int orc_joint_set_mouse_target(orc_world* w, int joint, float x, float y) {   // b2mousejoint.d:83-91
     if (joint < 0 || joint >= (int)w->w.jointsByIndex.size()) return -1;
     Joint* j = w->w.jointsByIndex[joint];
-    if (j->type != kMouseJoint) return -1;
+    if (!j || j->type != kMouseJoint) return -1;
     if (!j->bodyB->IsAwake()) j->bodyB->SetAwake(true);
     j->targetA = Vec2(x, y);
     return 0;
@@ -5439,7 +5585,10 @@ void orc_world_step_n(orc_world* w, float dt, int vel_iters, int pos_iters, int 
     for (int i = 0; i < steps; ++i) w->w.Step(dt, vel_iters, pos_iters);
 }
 
-void orc_world_record_events(orc_world* w, int enable) { w->w.recording = enable != 0; }
+void orc_world_record_events(orc_world* w, int enable) {               // the listener for steps and destruction
+    w->w.recording = enable != 0;
+    w->w.contactManager.listener = w->w.recording ? &w->w.recorder : nullptr;
+}
 int orc_world_event_count(orc_world* w) { return (int)w->w.recorder.events.size(); }
 int orc_world_get_events(orc_world* w, dbox_contact_event* out, int cap) {
     int n = (int)w->w.recorder.events.size();
@@ -5472,6 +5621,10 @@ int orc_world_export_state(orc_world* w, dbox_world_header* header, dbox_body_st
         for (size_t i = 0; i < W.bodiesByIndex.size(); ++i) {
             const Body* b = W.bodiesByIndex[i];
             dbox_body_state* o = bodies + i;
+            if (!b) {                                                   // destroyed: an all-zero record
+                memset(o, 0, sizeof(*o));
+                continue;
+            }
             o->flags = b->flags;
             o->type = b->type;
             o->xf[0] = b->xf.p.x; o->xf[1] = b->xf.p.y; o->xf[2] = b->xf.q.s; o->xf[3] = b->xf.q.c;
@@ -5491,7 +5644,7 @@ int orc_world_export_state(orc_world* w, dbox_world_header* header, dbox_body_st
         for (size_t i = 0; i < W.fixturesByIndex.size(); ++i) {
             const Fixture* f = W.fixturesByIndex[i];
             dbox_proxy_state* o = proxies + i;
-            int id = f->proxy.proxyId;
+            int id = f ? f->proxy.proxyId : -1;                         // destroyed: no proxy
             o->proxy_id = id;
             if (id >= 0) {
                 const AABB& a = W.contactManager.broadPhase.tree.nodes[id].aabb;
@@ -5534,6 +5687,10 @@ int orc_world_export_state(orc_world* w, dbox_world_header* header, dbox_body_st
     if (joints) {
         for (size_t i = 0; i < W.jointsByIndex.size(); ++i) {
             const Joint* j = W.jointsByIndex[i];
+            if (!j) {                                                   // destroyed: an all-zero record
+                memset(joints + i, 0, sizeof(joints[i]));
+                continue;
+            }
             joints[i].impulse[0] = j->impulse.x;
             joints[i].impulse[1] = j->impulse.y;
             joints[i].impulse[2] = j->impulse.z;

@@ -36,6 +36,9 @@ int orc_body_create(orc_world* w, const dbox_body_def* def);
 int orc_fixture_create(orc_world* w, int body, const dbox_shape_def* shape, const dbox_fixture_def* def);
 int orc_joint_create_revolute(orc_world* w, const dbox_revolute_def* def);
 int orc_world_dump(orc_world* w, char* buf, int cap);
+int orc_body_destroy(orc_world* w, int body);
+int orc_fixture_destroy(orc_world* w, int fixture);
+int orc_joint_destroy(orc_world* w, int joint);
 int orc_query_aabb(orc_world* w, float lx, float ly, float ux, float uy, int* out, int cap);
 void orc_raycast_many(orc_world* w, int n, const float* p1, const float* p2, int mode, int* counts, dbox_ray_hit* hits,
                       int cap);
