@@ -215,6 +215,7 @@ struct dbox_world {
     DBuf<unsigned> s_sapk0, s_sapk1;
     DBuf<int> s_sapi0, s_sapi1;
     DBuf<float4> s_sapbox;
+    DBuf<int> d_porder;         // per world: fixtures in proxy-id order
     DBuf<unsigned char> s_cevt;
     std::vector<dbox_contact_event> h_events;
     std::vector<dg::WorldInfo> wi;
@@ -269,7 +270,7 @@ void free_device(dbox_world* w) {
     w->d_solve_order.free(); w->d_solve_queue.free();
     w->s_feat.free(); w->s_vsave.free(); w->s_slog.free(); w->s_pend.free();
     w->d_events.free(); w->s_cevt.free();
-    w->s_sapk0.free(); w->s_sapk1.free(); w->s_sapi0.free(); w->s_sapi1.free(); w->s_sapbox.free();
+    w->s_sapk0.free(); w->s_sapk1.free(); w->s_sapi0.free(); w->s_sapi1.free(); w->s_sapbox.free(); w->d_porder.free();
     w->s_cbody.free(); w->s_adj_items.free(); w->s_isl_pair.free(); w->s_cq.free(); w->s_cvis.free(); w->s_bfl.free(); w->s_sbody.free(); w->d_prof.free();
     if (w->graph) { cudaGraphExecDestroy(w->graph); w->graph = nullptr; }
     if (w->tgraph) { cudaGraphExecDestroy(w->tgraph); w->tgraph = nullptr; }
@@ -460,6 +461,7 @@ int upload(dbox_world* w) {
     w->wi.assign(W, dg::WorldInfo());
     int nb = 0, nf = 0, nj = 0, nc = 0, nh = 0, np = 0, nbx = 0, nkx = 0;
     int cpb = w->caps.contacts_per_body > 0 ? w->caps.contacts_per_body : 8;
+    std::vector<int> porder;
     for (int i = 0; i < W; ++i) {
         HostWorld& hw = w->worlds[i];
         dg::WorldInfo& wi = w->wi[i];
@@ -475,6 +477,22 @@ int upload(dbox_world* w) {
         wi.bx_start = nbx;
         wi.kx_start = nkx;
         wi.snap_start = nc;
+        // broad-phase walk order: fixtures by proxy id (no-proxy fixtures last); the plain
+        // fixture order while the ids rise with the fixture index (always, without destruction)
+        wi.proxy_order = 0;
+        for (int i = 0, last = -1; i < f; ++i) {
+            const int id = hw.px[i].proxy_id;
+            if (id < 0) continue;
+            if (id < last) wi.proxy_order = 1;
+            last = id;
+        }
+        porder.resize(nf + f);
+        for (int i = 0; i < f; ++i) porder[nf + i] = i;
+        if (wi.proxy_order)
+            std::stable_sort(porder.begin() + nf, porder.end(), [&](int a, int c) {
+                const unsigned ia = (unsigned)hw.px[a].proxy_id, ic = (unsigned)hw.px[c].proxy_id;   // -1 sorts last
+                return ia < ic;
+            });
         nb += b; nf += f; nj += j; nc += cap; nh += wi.hash_cap; np += wi.pair_cap; nbx += b + 1; nkx += cap + j + 2;
     }
     w->total_bodies = nb; w->total_fixtures = nf; w->total_joints = nj; w->total_contacts = nc;
@@ -570,6 +588,7 @@ int upload(dbox_world* w) {
     ok &= w->s_sapk0.alloc(nf) == 0 && w->s_sapk1.alloc(nf) == 0;
     ok &= w->s_sapi0.alloc(nf) == 0 && w->s_sapi1.alloc(nf) == 0;
     ok &= w->s_sapbox.alloc(nf) == 0;
+    ok &= w->d_porder.alloc(nf) == 0;
     ok &= w->s_cstate.alloc(nc) == 0;
     ok &= w->s_adj_items.alloc(2 * (size_t)nc) == 0;
     ok &= w->s_isl_pair.alloc(nc) == 0;
@@ -615,6 +634,7 @@ int upload(dbox_world* w) {
     if (nf) {
         CU(cudaMemcpy(w->d_fx.p, fx.data(), sizeof(dg::DFixture) * nf, cudaMemcpyHostToDevice));
         CU(cudaMemcpy(w->d_px.p, px.data(), sizeof(dbox_proxy_state) * nf, cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(w->d_porder.p, porder.data(), sizeof(int) * nf, cudaMemcpyHostToDevice));
     }
     if (nj) CU(cudaMemcpy(w->d_jt.p, jt.data(), sizeof(dg::DJoint) * nj, cudaMemcpyHostToDevice));
     if (nc) {
@@ -739,6 +759,7 @@ dg::Ctx make_ctx(dbox_world* w, float dt, int vi, int pi) {
     x.s_sapi[0] = w->s_sapi0.p;
     x.s_sapi[1] = w->s_sapi1.p;
     x.s_sapbox = w->s_sapbox.p;
+    x.proxy_order = w->d_porder.p;
     x.s_cevt = w->s_cevt.p;
     return x;
 }

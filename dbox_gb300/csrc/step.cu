@@ -240,10 +240,12 @@ DG Sap sap_build(const Ctx& x, int w, int* hist) {
     const WorldInfo& wi = x.wi[w];
     const int lane = lane_id();
     const int f0 = wi.fix_start, nf = wi.fix_count;
+    const int* ord = wi.proxy_order ? x.proxy_order + f0 : nullptr;   // ranks in proxy-id order
+    auto PX = [ord](int r) { return ord ? ord[r] : r; };
     float lo[2] = {3.4e38f, 3.4e38f}, hi[2] = {-3.4e38f, -3.4e38f}, sum = 0.0f;
     int cnt = 0;
     for (int i = lane; i < nf; i += kWarp) {
-        const dbox_proxy_state& p = x.px[f0 + i];
+        const dbox_proxy_state& p = x.px[f0 + PX(i)];
         if (p.proxy_id < 0) continue;
         ++cnt;
         sum += bmax(p.fat_aabb[2] - p.fat_aabb[0], p.fat_aabb[3] - p.fat_aabb[1]);
@@ -258,7 +260,7 @@ DG Sap sap_build(const Ctx& x, int w, int* hist) {
     };
     float ext = 0.0f;
     for (int i = lane; i < nf; i += kWarp) {
-        const dbox_proxy_state& p = x.px[f0 + i];
+        const dbox_proxy_state& p = x.px[f0 + PX(i)];
         if (p.proxy_id < 0 || is_wide(p)) continue;
         ext = bmax(ext, bmax(p.fat_aabb[2] - p.fat_aabb[0], p.fat_aabb[3] - p.fat_aabb[1]));
         for (int a = 0; a < 2; ++a) { lo[a] = bmin(lo[a], p.fat_aabb[a]); hi[a] = bmax(hi[a], p.fat_aabb[a]); }
@@ -287,11 +289,11 @@ DG Sap sap_build(const Ctx& x, int w, int* hist) {
     int nv = 0;
     for (int base = 0; base < nf; base += kWarp) {   // ordinary proxies, in id order
         int i = base + lane;
-        bool v = i < nf && x.px[f0 + i].proxy_id >= 0 && !is_wide(x.px[f0 + i]);
+        bool v = i < nf && x.px[f0 + PX(i)].proxy_id >= 0 && !is_wide(x.px[f0 + PX(i)]);
         unsigned bal = __ballot_sync(0xffffffffu, v);
         if (v) {
             int r = nv + __popc(bal & ((1u << lane) - 1u));
-            const dbox_proxy_state& p = x.px[f0 + i];
+            const dbox_proxy_state& p = x.px[f0 + PX(i)];
             int cx = sap_cell(p.fat_aabb[0], s.ox, s.inv, s.ncx), cy = sap_cell(p.fat_aabb[1], s.oy, s.inv, s.ncy);
             k0[r] = (unsigned)(cy * s.ncx + cx);
             i0[r] = i;
@@ -339,18 +341,18 @@ DG Sap sap_build(const Ctx& x, int w, int* hist) {
     // three passes: the sorted data is in the second buffer
     for (int r = lane; r < nv; r += kWarp) {
         int i = i1[r];
-        const dbox_proxy_state& p = x.px[f0 + i];
+        const dbox_proxy_state& p = x.px[f0 + PX(i)];
         x.s_sapbox[f0 + r] = make_float4(p.fat_aabb[0], p.fat_aabb[1], p.fat_aabb[2], p.fat_aabb[3]);
         if (p.moved) i1[r] = i | (int)0x80000000;
     }
     int nw = 0;
     for (int base = 0; base < nf; base += kWarp) {   // wide proxies after them, indices in the free buffer
         int i = base + lane;
-        bool v = i < nf && x.px[f0 + i].proxy_id >= 0 && is_wide(x.px[f0 + i]);
+        bool v = i < nf && x.px[f0 + PX(i)].proxy_id >= 0 && is_wide(x.px[f0 + PX(i)]);
         unsigned bal = __ballot_sync(0xffffffffu, v);
         if (v) {
             int r = nw + __popc(bal & ((1u << lane) - 1u));
-            const dbox_proxy_state& p = x.px[f0 + i];
+            const dbox_proxy_state& p = x.px[f0 + PX(i)];
             x.s_sapbox[f0 + nv + r] = make_float4(p.fat_aabb[0], p.fat_aabb[1], p.fat_aabb[2], p.fat_aabb[3]);
             i0[r] = p.moved ? (i | (int)0x80000000) : i;
         }
@@ -394,11 +396,15 @@ __device__ __noinline__ void find_new_contacts(const Ctx& x, int w) {
     WorldDyn& wd = x.wd[w];
     int lane = lane_id();
     int f0 = wi.fix_start, nf = wi.fix_count;
-    // moved list, ascending
+    // proxies are walked by rank, in ascending proxy id (b2PairLessThan, b2broadphase.d:166):
+    // the rank is the fixture index unless destruction let a newer fixture reuse a lower id
+    const int* ord = wi.proxy_order ? x.proxy_order + f0 : nullptr;
+    auto PX = [ord](int r) { return ord ? ord[r] : r; };
+    // moved list, ascending rank
     int nm = 0;
     for (int base = 0; base < nf; base += kWarp) {
         int i = base + lane;
-        bool mv = i < nf && x.px[f0 + i].moved && x.px[f0 + i].proxy_id >= 0;
+        bool mv = i < nf && x.px[f0 + PX(i)].moved && x.px[f0 + PX(i)].proxy_id >= 0;
         unsigned bal = __ballot_sync(0xffffffffu, mv);
         if (mv) x.s_moved[f0 + nm + __popc(bal & ((1u << lane) - 1))] = i;
         nm += __popc(bal);
@@ -413,17 +419,17 @@ __device__ __noinline__ void find_new_contacts(const Ctx& x, int w) {
     for (int a = lane; a < nf; a += kWarp) {
         int cnt = 0;
         if (use_sap) {
-            if (x.px[f0 + a].proxy_id >= 0)
-                sap_partners(sap, proxy_fat(x, f0 + a), a, x.px[f0 + a].moved != 0, [&](int) { ++cnt; });
-        } else if (x.px[f0 + a].proxy_id >= 0) {
-            AABB fa = proxy_fat(x, f0 + a);
-            if (x.px[f0 + a].moved) {
+            if (x.px[f0 + PX(a)].proxy_id >= 0)
+                sap_partners(sap, proxy_fat(x, f0 + PX(a)), a, x.px[f0 + PX(a)].moved != 0, [&](int) { ++cnt; });
+        } else if (x.px[f0 + PX(a)].proxy_id >= 0) {
+            AABB fa = proxy_fat(x, f0 + PX(a));
+            if (x.px[f0 + PX(a)].moved) {
                 for (int b = a + 1; b < nf; ++b)
-                    if (x.px[f0 + b].proxy_id >= 0 && aabb_overlap(fa, proxy_fat(x, f0 + b))) ++cnt;
+                    if (x.px[f0 + PX(b)].proxy_id >= 0 && aabb_overlap(fa, proxy_fat(x, f0 + PX(b)))) ++cnt;
             } else {
                 for (int m = 0; m < nm; ++m) {
                     int b = x.s_moved[f0 + m];
-                    if (b > a && aabb_overlap(fa, proxy_fat(x, f0 + b))) ++cnt;
+                    if (b > a && aabb_overlap(fa, proxy_fat(x, f0 + PX(b)))) ++cnt;
                 }
             }
         }
@@ -452,33 +458,34 @@ __device__ __noinline__ void find_new_contacts(const Ctx& x, int w) {
     // fill pairs in (a, b) order
     for (int a = lane; a < nf; a += kWarp) {
         int o = x.s_pcount[f0 + a];
-        if (x.px[f0 + a].proxy_id < 0) continue;
-        AABB fa = proxy_fat(x, f0 + a);
+        if (x.px[f0 + PX(a)].proxy_id < 0) continue;
+        AABB fa = proxy_fat(x, f0 + PX(a));
         if (use_sap) {
             int2* seg = x.pairs + wi.pair_start + o;
             int cnt = 0;
-            sap_partners(sap, fa, a, x.px[f0 + a].moved != 0, [&](int b) { seg[cnt++] = make_int2(f0 + a, f0 + b); });
-            for (int i = 1; i < cnt; ++i) {           // partners by id (insertion sort)
+            sap_partners(sap, fa, a, x.px[f0 + PX(a)].moved != 0, [&](int b) { seg[cnt++] = make_int2(a, b); });
+            for (int i = 1; i < cnt; ++i) {           // partners by id (insertion sort of ranks)
                 int2 v = seg[i];
                 int j = i - 1;
                 while (j >= 0 && seg[j].y > v.y) { seg[j + 1] = seg[j]; --j; }
                 seg[j + 1] = v;
             }
-        } else if (x.px[f0 + a].moved) {
+            for (int i = 0; i < cnt; ++i) seg[i] = make_int2(f0 + PX(seg[i].x), f0 + PX(seg[i].y));
+        } else if (x.px[f0 + PX(a)].moved) {
             for (int b = a + 1; b < nf; ++b)
-                if (x.px[f0 + b].proxy_id >= 0 && aabb_overlap(fa, proxy_fat(x, f0 + b)))
-                    x.pairs[wi.pair_start + o++] = make_int2(f0 + a, f0 + b);
+                if (x.px[f0 + PX(b)].proxy_id >= 0 && aabb_overlap(fa, proxy_fat(x, f0 + PX(b))))
+                    x.pairs[wi.pair_start + o++] = make_int2(f0 + PX(a), f0 + PX(b));
         } else {
             for (int m = 0; m < nm; ++m) {
                 int b = x.s_moved[f0 + m];
-                if (b > a && aabb_overlap(fa, proxy_fat(x, f0 + b)))
-                    x.pairs[wi.pair_start + o++] = make_int2(f0 + a, f0 + b);
+                if (b > a && aabb_overlap(fa, proxy_fat(x, f0 + PX(b))))
+                    x.pairs[wi.pair_start + o++] = make_int2(f0 + PX(a), f0 + PX(b));
             }
         }
     }
     tsync();
     // clear the move buffer
-    for (int i = lane; i < nf; i += kWarp) x.px[f0 + i].moved = 0;
+    for (int i = lane; i < nf; i += kWarp) x.px[f0 + PX(i)].moved = 0;
     // AddPair, in pair order
     int n = wd.contact_count;
     int added = 0;

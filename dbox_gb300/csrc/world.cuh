@@ -29,7 +29,7 @@ struct WorldInfo {
     int bx_start;                  // per-body scratch with one extra entry (body_count + 1)
     int kx_start;                  // per-constraint scratch (contact_cap + joint_count + 2)
     int snap_start;                // TOI sweep snapshots (contact_cap entries)
-    int pad;
+    int proxy_order;               // 1: fixtures out of proxy-id order, walk them by Ctx.proxy_order
 };
 
 struct WorldDyn {
@@ -209,6 +209,7 @@ struct Ctx {
     unsigned* s_sapk[2];           // fixture-indexed: sweep-and-prune keys (radix-sort ping-pong)
     int* s_sapi[2];                // fixture-indexed: proxy of each sorted key (top bit: moved)
     float4* s_sapbox;              // fixture-indexed: fat AABBs in sorted order
+    const int* proxy_order;        // fixture-indexed: world-local fixture of each proxy-id rank
     // scratch (contact-indexed)
     int* s_cstate;                 // 0 processed, 1 inactive, 2 destroyed
     int2* s_adj_items;             // 2 per contact slot: (contact, other body) edges by body

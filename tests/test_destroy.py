@@ -144,8 +144,10 @@ def test_destroy_exact(oracle_lib, gpu_lib):
     nb = len(s["bodies"])
     nf = len(s["fixtures"])
     chain_child = nf + 5                                # a child of the first chain shape
-    for kind, idx in (("body", 4), ("body", 37), ("fixture", 10), ("joint", 3), ("fixture", chain_child),
-                      ("body", nb - 1)):
+    # the low ids freed last come back first: the new fixtures below get ids under those of
+    # older fixtures, so the broad-phase must walk proxies by id, not by fixture index
+    for kind, idx in (("body", nb - 1), ("fixture", chain_child), ("joint", 3), ("fixture", 10), ("body", 37),
+                      ("body", 4)):
         getattr(ow, "destroy_" + kind)(idx)
         getattr(gw, "destroy_" + kind)(0, idx)
         ref = ow.events()
@@ -161,12 +163,15 @@ def test_destroy_exact(oracle_lib, gpu_lib):
         ow.events()
         _compare(ow, gw, "step %d" % (30 * (t + 1)))
     for k in range(5):                                  # new proxies take the freed ids
-        b, sd, fd = _box(-3.0 + 1.5 * k, 14.0)
+        b, sd, fd = _box(-3.0 + 1.2 * k, 10.0 + 0.1 * k)
         ob = ow.create_body(b)
         gb = gw.create_body(0, b)
         assert ob == gb
         assert ow.create_fixture(ob, sd, fd) == gw.create_fixture(0, gb, sd, fd)
     _compare(ow, gw, "after creating")
+    ids = gw.export_state(0)["proxies"]["proxy_id"]
+    live = ids[ids >= 0]
+    assert (np.diff(live) < 0).any()                    # proxy ids no longer rise with the index
     gw.step(steps=90)
     ow.step(steps=90)
     _compare(ow, gw, "end")
