@@ -57,6 +57,7 @@ def lib():
     L.dbox_joint_create_pulley.argtypes = [vp, i32, vp, ctypes.POINTER(i32)]
     L.dbox_joint_create_mouse.argtypes = [vp, i32, vp, ctypes.POINTER(i32)]
     L.dbox_joint_set_mouse_target.argtypes = [vp, i32, i32, abi.Vec2]
+    L.dbox_joint_create_gear.argtypes = [vp, i32, vp, ctypes.POINTER(i32)]
     L.dbox_world_query_aabb.argtypes = [vp, i32, vp, vp, i32, vp, vp]
     L.dbox_world_get_stream.argtypes = [vp, ctypes.POINTER(vp)]
     for fn in ("dbox_body_destroy", "dbox_fixture_destroy", "dbox_joint_destroy"):
@@ -261,7 +262,7 @@ class World:
                 self.create_joint(i, "distance", d)
             for d in s.get("rope_joints", ()):
                 self.create_joint(i, "rope", d)
-            for kind in ("weld", "friction", "motor", "wheel", "prismatic", "pulley", "mouse"):
+            for kind in ("weld", "friction", "motor", "wheel", "prismatic", "pulley", "mouse", "gear"):
                 for d in s.get(kind + "_joints", ()):
                     self.create_joint(i, kind, d)
         self.body_counts = [len(s["bodies"]) for s in scenes]
@@ -277,7 +278,8 @@ class World:
                     "wheel": ("WHEEL_DEF", "dbox_joint_create_wheel"),
                     "prismatic": ("PRISMATIC_DEF", "dbox_joint_create_prismatic"),
                     "pulley": ("PULLEY_DEF", "dbox_joint_create_pulley"),
-                    "mouse": ("MOUSE_DEF", "dbox_joint_create_mouse")}
+                    "mouse": ("MOUSE_DEF", "dbox_joint_create_mouse"),
+                    "gear": ("GEAR_DEF", "dbox_joint_create_gear")}
 
     def create_joint(self, world, kind, d):
         """b2World.CreateJoint with a b2DistanceJointDef / b2RopeJointDef / b2WeldJointDef /

@@ -90,6 +90,12 @@ MOUSE_DEF = np.dtype([
 ])
 assert MOUSE_DEF.itemsize == 32
 
+GEAR_DEF = np.dtype([
+    ("body_a", "<i4"), ("body_b", "<i4"), ("collide_connected", "<i4"),
+    ("joint1", "<i4"), ("joint2", "<i4"), ("ratio", "<f4"),
+])
+assert GEAR_DEF.itemsize == 24
+
 WORLD_HEADER = np.dtype([
     ("body_count", "<i4"), ("fixture_count", "<i4"), ("contact_count", "<i4"), ("joint_count", "<i4"),
     ("world_flags", "<u4"), ("step_complete", "<i4"), ("inv_dt0", "<f4"), ("reserved", "<i4"),

@@ -447,7 +447,14 @@ int download(dbox_world* w) {
                           cudaMemcpyDeviceToHost));
         // device fixture/joint indices are global; host mirrors keep world-local ones
         for (auto& c : hw.ct) { c.fixture_a -= wi.fix_start; c.fixture_b -= wi.fix_start; }
-        for (auto& j : hw.jt) { j.body_a -= wi.body_start; j.body_b -= wi.body_start; }
+        for (auto& j : hw.jt) {
+            j.body_a -= wi.body_start;
+            j.body_b -= wi.body_start;
+            if (j.type == dg::kGearJoint) {
+                j.body_c -= wi.body_start;
+                j.body_d -= wi.body_start;
+            }
+        }
     }
     w->on_device = false;
     w->mirrors_fresh = true;
@@ -545,6 +552,10 @@ int upload(dbox_world* w) {
             dg::DJoint d = hw.jt[j];
             d.body_a += wi.body_start;
             d.body_b += wi.body_start;
+            if (d.type == dg::kGearJoint) {
+                d.body_c += wi.body_start;
+                d.body_d += wi.body_start;
+            }
             jt[wi.joint_start + j] = d;
         }
         for (int k = 0; k < (int)hw.ct.size(); ++k) {
@@ -1323,6 +1334,9 @@ int32_t dbox_joint_destroy(dbox_world* w, int32_t world, int32_t joint) {
     HostWorld& hw0 = w->worlds[world];
     if (joint < 0 || joint >= (int)hw0.jt.size() || hw0.jt[joint].type < 0)
         return fail(DBOX_ERR_INVALID, "dbox_joint_destroy: no joint %d", joint);
+    for (const dg::DJoint& g : hw0.jt)
+        if (g.type == dg::kGearJoint && (g.joint1 == joint || g.joint2 == joint))
+            return fail(DBOX_ERR_INVALID, "dbox_joint_destroy: joint %d is used by a gear joint", joint);
     int rc = prepare_edit(w);
     if (rc) return rc;
     destroy_joint(w->worlds[world], joint);
@@ -1517,6 +1531,77 @@ int32_t dbox_joint_create_pulley(dbox_world* w, int32_t world, const dbox_pulley
     if (rc) return rc;
     int idx = create_pulley_joint(w->worlds[world], def);
     if (idx < 0) return fail(DBOX_ERR_INVALID, "dbox_joint_create_pulley: bad bodies");
+    if (out_joint) *out_joint = idx;
+    return DBOX_OK;
+}
+
+// b2World.CreateJoint with a b2GearJointDef (b2gearjoint.d:83-168, b2world.d:196-261): the
+// gear's own bodies are joint1's and joint2's B bodies; the definition's bodies only choose
+// which contacts are flagged for filtering
+int create_gear_joint(HostWorld& hw, const dbox_gear_def* d) {
+    const int nb = (int)hw.bs.size(), nj = (int)hw.jt.size();
+    if (d->body_a < 0 || d->body_a >= nb || d->body_b < 0 || d->body_b >= nb || d->body_a == d->body_b ||
+        body_gone(hw, d->body_a) || body_gone(hw, d->body_b)) return -1;
+    for (int k : {d->joint1, d->joint2})
+        if (k < 0 || k >= nj || (hw.jt[k].type != dg::kRevoluteJoint && hw.jt[k].type != dg::kPrismaticJoint)) return -1;
+    const dg::DJoint& j1 = hw.jt[d->joint1];
+    const dg::DJoint& j2 = hw.jt[d->joint2];
+    dg::DJoint j;
+    memset(&j, 0, sizeof(j));
+    j.type = dg::kGearJoint;
+    j.collide_connected = d->collide_connected ? 1 : 0;
+    j.joint1 = d->joint1;
+    j.joint2 = d->joint2;
+    j.type_a = j1.type;
+    j.type_b = j2.type;
+    // coordinate of a joint: its angle, or the slide along its axis (b2gearjoint.d:107-161)
+    auto coordinate = [&](const dg::DJoint& jn, int body_other, int body_base, float2 anchor_base, float2 anchor_other,
+                          float2 axis) {
+        const dbox_body_state& o = hw.bs[body_other];
+        const dbox_body_state& b = hw.bs[body_base];
+        if (jn.type == dg::kRevoluteJoint) return (o.sweep[7] - b.sweep[7]) - jn.reference_angle;
+        hg::Rot qo, qb;
+        qo.s = o.xf[2]; qo.c = o.xf[3];
+        qb.s = b.xf[2]; qb.c = b.xf[3];
+        const hg::V2 m = hg::rmul(qo, hg::mk(anchor_other.x, anchor_other.y));
+        const hg::V2 dp = hg::sub(hg::mk(o.xf[0], o.xf[1]), hg::mk(b.xf[0], b.xf[1]));
+        const hg::V2 t = hg::add(m, dp);
+        const hg::V2 p = hg::mk(qb.c * t.x + qb.s * t.y, -qb.s * t.x + qb.c * t.y);   // b2MulT(q, v)
+        return hg::dot(hg::sub(p, hg::mk(anchor_base.x, anchor_base.y)), hg::mk(axis.x, axis.y));
+    };
+    j.body_c = j1.body_a;
+    j.body_a = j1.body_b;
+    j.local_anchor_c = j1.local_anchor_a;
+    j.local_anchor_a = j1.local_anchor_b;
+    j.reference_angle_a = j1.reference_angle;
+    j.local_axis_c = j1.type == dg::kRevoluteJoint ? make_float2(0.0f, 0.0f) : j1.local_axis_x;
+    const float coordinateA = coordinate(j1, j.body_a, j.body_c, j.local_anchor_c, j.local_anchor_a, j.local_axis_c);
+    j.body_d = j2.body_a;
+    j.body_b = j2.body_b;
+    j.local_anchor_d = j2.local_anchor_a;
+    j.local_anchor_b = j2.local_anchor_b;
+    j.reference_angle_b = j2.reference_angle;
+    j.local_axis_d = j2.type == dg::kRevoluteJoint ? make_float2(0.0f, 0.0f) : j2.local_axis_x;
+    const float coordinateB = coordinate(j2, j.body_b, j.body_d, j.local_anchor_d, j.local_anchor_b, j.local_axis_d);
+    j.ratio = d->ratio;
+    j.constant = coordinateA + j.ratio * coordinateB;
+    const int idx = (int)hw.jt.size();
+    hw.jt.push_back(j);
+    if (!j.collide_connected) {
+        for (auto& c : hw.ct) {
+            int A = hw.fx[c.fixture_a].body, B = hw.fx[c.fixture_b].body;
+            if ((A == d->body_a && B == d->body_b) || (A == d->body_b && B == d->body_a)) c.flags |= dg::kContactFilter;
+        }
+    }
+    return idx;
+}
+
+int32_t dbox_joint_create_gear(dbox_world* w, int32_t world, const dbox_gear_def* def, int32_t* out_joint) {
+    if (!w || !def || world < 0 || world >= (int)w->worlds.size()) return fail(DBOX_ERR_INVALID, "dbox_joint_create_gear: bad arguments");
+    int rc = prepare_edit(w);
+    if (rc) return rc;
+    int idx = create_gear_joint(w->worlds[world], def);
+    if (idx < 0) return fail(DBOX_ERR_INVALID, "dbox_joint_create_gear: bad bodies or joints");
     if (out_joint) *out_joint = idx;
     return DBOX_OK;
 }
@@ -2413,10 +2498,10 @@ struct Dumper {
         put("    bodies[%d].CreateFixture(&fd);\n", body_index);
     }
 
-    void joint(const dg::DJoint& j, int index_a, int index_b, int index) {
+    void joint(const dg::DJoint& j, int index_a, int index_b, int index, const std::vector<int>& list_pos) {
         static const char* names[] = {"b2RevoluteJointDef", "b2DistanceJointDef", "b2RopeJointDef", "b2WeldJointDef",
                                       "b2FrictionJointDef", "b2MotorJointDef", "b2WheelJointDef", "b2PrismaticJointDef",
-                                      "b2PulleyJointDef"};
+                                      "b2PulleyJointDef", "", "b2GearJointDef"};
         if (j.type == dg::kMouseJoint) {                                 // b2mousejoint.d:180-183
             put("Mouse joint dumping is not supported.\n");
             return;
@@ -2426,7 +2511,7 @@ struct Dumper {
         put("  jd.bodyA = bodies[%d];\n", index_a);
         put("  jd.bodyB = bodies[%d];\n", index_b);
         flag(in, "jd.collideConnected", j.collide_connected ? 1 : 0);
-        const bool anchors = j.type != dg::kMotorJoint && j.type != dg::kPulleyJoint;
+        const bool anchors = j.type != dg::kMotorJoint && j.type != dg::kPulleyJoint && j.type != dg::kGearJoint;
         if (j.type == dg::kPulleyJoint) {
             vec(in, "jd.groundAnchorA", j.ground_a);
             vec(in, "jd.groundAnchorB", j.ground_b);
@@ -2436,6 +2521,11 @@ struct Dumper {
             vec(in, "jd.localAnchorB", j.local_anchor_b);
         }
         switch (j.type) {
+        case dg::kGearJoint:                                            // b2gearjoint.d:222-238
+            put("  jd.joint1 = joints[%d];\n", list_pos[j.joint1]);
+            put("  jd.joint2 = joints[%d];\n", list_pos[j.joint2]);
+            num(in, "jd.ratio", j.ratio);
+            break;
         case dg::kRevoluteJoint:                                        // b2revolutejoint.d:293-312
             num(in, "jd.referenceAngle", j.reference_angle);
             flag(in, "jd.enableLimit", j.enable_limit ? 1 : 0);
@@ -2546,12 +2636,16 @@ struct Dumper {
             }
             put("}\n");
         }
-        for (int k = 0; k < nj; ++k) {                                  // no gear joints: one pass
-            const dg::DJoint& j = hw.jt[joints[k]];
-            put("{\n");
-            joint(j, list_index[j.body_a], list_index[j.body_b], k);
-            put("}\n");
-        }
+        std::vector<int> list_pos(hw.jt.size(), -1);                   // b2Joint.m_index
+        for (int k = 0; k < nj; ++k) list_pos[joints[k]] = k;
+        for (int pass = 0; pass < 2; ++pass)                            // gear joints last
+            for (int k = 0; k < nj; ++k) {
+                const dg::DJoint& j = hw.jt[joints[k]];
+                if ((j.type == dg::kGearJoint) != (pass == 1)) continue;
+                put("{\n");
+                joint(j, list_index[j.body_a], list_index[j.body_b], k, list_pos);
+                put("}\n");
+            }
         put("b2Free(joints);\n");
         put("b2Free(bodies);\n");
         put("joints = null;\n");

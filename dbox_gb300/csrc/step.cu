@@ -2227,6 +2227,165 @@ __device__ __noinline__ bool pulley_solve_position(const DJoint& j, int la, int 
     return linearError < kLinearSlop;
 }
 
+// ------------------------------------------------------------ gear joint (joints/b2gearjoint.d:245-500)
+// Four bodies: A (joint1's B), B (joint2's B), C (joint1's A), D (joint2's A); the level
+// schedule gives the gear a level above the last constraint of each dynamic one.  Velocities
+// and positions are written back A, B, C, D, as the reference does (C and D may coincide).
+__device__ __noinline__ void gear_init(const Ctx& x, int ji, int b0, SB sb, bool warm) {
+    DJoint& j = x.jt[ji];
+    const dbox_body_state& bA = x.bs[j.body_a];
+    const dbox_body_state& bB = x.bs[j.body_b];
+    const dbox_body_state& bC = x.bs[j.body_c];
+    const dbox_body_state& bD = x.bs[j.body_d];
+    const int la = j.body_a - b0, lb = j.body_b - b0, lc = j.body_c - b0, ld = j.body_d - b0;
+    j.lcA = b_lc(bA);
+    j.lcB = b_lc(bB);
+    j.lcC = b_lc(bC);
+    j.lcD = b_lc(bD);
+    j.invMassA = bA.mass[1];
+    j.invMassB = bB.mass[1];
+    j.invMassC = bC.mass[1];
+    j.invMassD = bD.mass[1];
+    j.invIA = bA.mass[3];
+    j.invIB = bB.mass[3];
+    j.invIC = bC.mass[3];
+    j.invID = bD.mass[3];
+    const float aA = sb.a(la), aB = sb.a(lb), aC = sb.a(lc), aD = sb.a(ld);
+    float2 vA = sb.v(la), vB = sb.v(lb), vC = sb.v(lc), vD = sb.v(ld);
+    float wA = sb.w(la), wB = sb.w(lb), wC = sb.w(lc), wD = sb.w(ld);
+    const Rot qA = rot(aA), qB = rot(aB), qC = rot(aC), qD = rot(aD);
+    float mass = 0.0f;
+    if (j.type_a == kRevoluteJoint) {
+        j.jv_ac = v2(0.0f, 0.0f);
+        j.jw_a = 1.0f;
+        j.jw_c = 1.0f;
+        mass += j.invIA + j.invIC;
+    } else {
+        const float2 u = mul(qC, j.local_axis_c);
+        const float2 rC = mul(qC, j.local_anchor_c - j.lcC);
+        const float2 rA = mul(qA, j.local_anchor_a - j.lcA);
+        j.jv_ac = u;
+        j.jw_c = cross(rC, u);
+        j.jw_a = cross(rA, u);
+        mass += ((j.invMassC + j.invMassA) + (j.invIC * j.jw_c) * j.jw_c) + (j.invIA * j.jw_a) * j.jw_a;
+    }
+    if (j.type_b == kRevoluteJoint) {
+        j.jv_bd = v2(0.0f, 0.0f);
+        j.jw_b = j.ratio;
+        j.jw_d = j.ratio;
+        mass += (j.ratio * j.ratio) * (j.invIB + j.invID);
+    } else {
+        const float2 u = mul(qD, j.local_axis_d);
+        const float2 rD = mul(qD, j.local_anchor_d - j.lcD);
+        const float2 rB = mul(qB, j.local_anchor_b - j.lcB);
+        j.jv_bd = j.ratio * u;
+        j.jw_d = j.ratio * cross(rD, u);
+        j.jw_b = j.ratio * cross(rB, u);
+        mass += (((j.ratio * j.ratio) * (j.invMassD + j.invMassB)) + (j.invID * j.jw_d) * j.jw_d) + (j.invIB * j.jw_b) * j.jw_b;
+    }
+    j.mass[0] = mass > 0.0f ? fdiv(1.0f, mass) : 0.0f;
+    if (warm) {                                                         // no dtRatio scaling here
+        const float P = j.impulse[0];
+        vA += (j.invMassA * P) * j.jv_ac;
+        wA += (j.invIA * P) * j.jw_a;
+        vB += (j.invMassB * P) * j.jv_bd;
+        wB += (j.invIB * P) * j.jw_b;
+        vC -= (j.invMassC * P) * j.jv_ac;
+        wC -= (j.invIC * P) * j.jw_c;
+        vD -= (j.invMassD * P) * j.jv_bd;
+        wD -= (j.invID * P) * j.jw_d;
+    } else {
+        j.impulse[0] = 0.0f;
+    }
+    sb.set_v(la, vA, wA);
+    sb.set_v(lb, vB, wB);
+    sb.set_v(lc, vC, wC);
+    sb.set_v(ld, vD, wD);
+}
+
+__device__ __noinline__ void gear_solve_velocity(DJoint& j, int b0, SB sb) {
+    const int la = j.body_a - b0, lb = j.body_b - b0, lc = j.body_c - b0, ld = j.body_d - b0;
+    float2 vA = sb.v(la), vB = sb.v(lb), vC = sb.v(lc), vD = sb.v(ld);
+    float wA = sb.w(la), wB = sb.w(lb), wC = sb.w(lc), wD = sb.w(ld);
+    float Cdot = dot(j.jv_ac, vA - vC) + dot(j.jv_bd, vB - vD);
+    Cdot += ((j.jw_a * wA) - (j.jw_c * wC)) + ((j.jw_b * wB) - (j.jw_d * wD));
+    const float impulse = (-j.mass[0]) * Cdot;
+    j.impulse[0] += impulse;
+    vA += (j.invMassA * impulse) * j.jv_ac;
+    wA += (j.invIA * impulse) * j.jw_a;
+    vB += (j.invMassB * impulse) * j.jv_bd;
+    wB += (j.invIB * impulse) * j.jw_b;
+    vC -= (j.invMassC * impulse) * j.jv_ac;
+    wC -= (j.invIC * impulse) * j.jw_c;
+    vD -= (j.invMassD * impulse) * j.jv_bd;
+    wD -= (j.invID * impulse) * j.jw_d;
+    sb.set_v(la, vA, wA);
+    sb.set_v(lb, vB, wB);
+    sb.set_v(lc, vC, wC);
+    sb.set_v(ld, vD, wD);
+}
+
+__device__ __noinline__ bool gear_solve_position(const DJoint& j, int b0, SB sb) {
+    const int la = j.body_a - b0, lb = j.body_b - b0, lc = j.body_c - b0, ld = j.body_d - b0;
+    float2 cA = sb.c(la), cB = sb.c(lb), cC = sb.c(lc), cD = sb.c(ld);
+    float aA = sb.a(la), aB = sb.a(lb), aC = sb.a(lc), aD = sb.a(ld);
+    const Rot qA = rot(aA), qB = rot(aB), qC = rot(aC), qD = rot(aD);
+    float coordinateA = 0.0f, coordinateB = 0.0f;
+    float2 JvAC = v2(0.0f, 0.0f), JvBD = v2(0.0f, 0.0f);
+    float JwA = 0.0f, JwB = 0.0f, JwC = 0.0f, JwD = 0.0f;
+    float mass = 0.0f;
+    if (j.type_a == kRevoluteJoint) {
+        JwA = 1.0f;
+        JwC = 1.0f;
+        mass += j.invIA + j.invIC;
+        coordinateA = (aA - aC) - j.reference_angle_a;
+    } else {
+        const float2 u = mul(qC, j.local_axis_c);
+        const float2 rC = mul(qC, j.local_anchor_c - j.lcC);
+        const float2 rA = mul(qA, j.local_anchor_a - j.lcA);
+        JvAC = u;
+        JwC = cross(rC, u);
+        JwA = cross(rA, u);
+        mass += ((j.invMassC + j.invMassA) + (j.invIC * JwC) * JwC) + (j.invIA * JwA) * JwA;
+        const float2 pC = j.local_anchor_c - j.lcC;
+        const float2 pA = mulT(qC, rA + (cA - cC));
+        coordinateA = dot(pA - pC, j.local_axis_c);
+    }
+    if (j.type_b == kRevoluteJoint) {
+        JwB = j.ratio;
+        JwD = j.ratio;
+        mass += (j.ratio * j.ratio) * (j.invIB + j.invID);
+        coordinateB = (aB - aD) - j.reference_angle_b;
+    } else {
+        const float2 u = mul(qD, j.local_axis_d);
+        const float2 rD = mul(qD, j.local_anchor_d - j.lcD);
+        const float2 rB = mul(qB, j.local_anchor_b - j.lcB);
+        JvBD = j.ratio * u;
+        JwD = j.ratio * cross(rD, u);
+        JwB = j.ratio * cross(rB, u);
+        mass += (((j.ratio * j.ratio) * (j.invMassD + j.invMassB)) + (j.invID * JwD) * JwD) + (j.invIB * JwB) * JwB;
+        const float2 pD = j.local_anchor_d - j.lcD;
+        const float2 pB = mulT(qD, rB + (cB - cD));
+        coordinateB = dot(pB - pD, j.local_axis_d);
+    }
+    const float C = (coordinateA + j.ratio * coordinateB) - j.constant;
+    float impulse = 0.0f;
+    if (mass > 0.0f) impulse = fdiv(-C, mass);
+    cA += (j.invMassA * impulse) * JvAC;
+    aA += (j.invIA * impulse) * JwA;
+    cB += (j.invMassB * impulse) * JvBD;
+    aB += (j.invIB * impulse) * JwB;
+    cC -= (j.invMassC * impulse) * JvAC;
+    aC -= (j.invIC * impulse) * JwC;
+    cD -= (j.invMassD * impulse) * JvBD;
+    aD -= (j.invID * impulse) * JwD;
+    sb.set_c(la, cA, aA);
+    sb.set_c(lb, cB, aB);
+    sb.set_c(lc, cC, aC);
+    sb.set_c(ld, cD, aD);
+    return true;                                                        // linearError stays 0
+}
+
 // ------------------------------------------------------------ mouse joint (joints/b2mousejoint.d:132-226), body B only
 __device__ __noinline__ void mouse_init(const Ctx& x, int ji, int b0, SB sb, bool warm, float dtRatio) {
     DJoint& j = x.jt[ji];
@@ -2307,6 +2466,7 @@ DG void joint_init(const Ctx& x, int ji, int b0, SB sb, bool warm, float dtRatio
     case kPrismaticJoint: prismatic_init(x, ji, b0, sb, warm, dtRatio); return;
     case kPulleyJoint: pulley_init(x, ji, b0, sb, warm, dtRatio); return;
     case kMouseJoint: mouse_init(x, ji, b0, sb, warm, dtRatio); return;
+    case kGearJoint: gear_init(x, ji, b0, sb, warm); return;
     default: break;
     }
     DJoint& j = x.jt[ji];
@@ -2387,6 +2547,7 @@ DG void joint_solve_velocity(const Ctx& x, int ji, int b0, SB sb) {
     if (j.type == kPrismaticJoint) { prismatic_solve_velocity(x, j, la, lb, sb); return; }
     if (j.type == kPulleyJoint) { pulley_solve_velocity(j, la, lb, sb); return; }
     if (j.type == kMouseJoint) { mouse_solve_velocity(x, j, lb, sb); return; }
+    if (j.type == kGearJoint) { gear_solve_velocity(j, b0, sb); return; }
     float2 vA = sb.v(la), vB = sb.v(lb);
     float wA = sb.w(la), wB = sb.w(lb);
     float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
@@ -2454,6 +2615,7 @@ DG bool joint_solve_position(const Ctx& x, int ji, int b0, SB sb) {
     if (j.type == kPrismaticJoint) return prismatic_solve_position(j, la, lb, sb);
     if (j.type == kPulleyJoint) return pulley_solve_position(j, la, lb, sb);
     if (j.type == kMouseJoint) return true;
+    if (j.type == kGearJoint) return gear_solve_position(j, b0, sb);
     float2 cA = sb.c(la), cB = sb.c(lb);
     float aA = sb.a(la), aB = sb.a(lb);
     float angularError = 0.0f, positionError = 0.0f;
@@ -2532,7 +2694,7 @@ DG int build_schedule(const Ctx& x, const WorldInfo& wi, int nIsl, bool contacts
                 bool doContacts = (pass == 0) == contacts_first;
                 int s = doContacts ? cs : js, e = doContacts ? ce : je;
                 for (int t = s; t < e; ++t) {
-                    int item, A, B;
+                    int item, A, B, C = -1, D = -1;
                     if (doContacts) {
                         item = x.s_isl_contact[c0 + t];
                         int2 pr = x.s_isl_pair[c0 + t];
@@ -2541,12 +2703,23 @@ DG int build_schedule(const Ctx& x, const WorldInfo& wi, int nIsl, bool contacts
                     } else {
                         item = -(x.s_isl_joint[wi.joint_start + t] + 1);
                         item_bodies(x, item, b0, A, B);
+                        const DJoint& jj = x.jt[-item - 1];
+                        if (jj.type == kGearJoint) {                    // a gear also moves C and D
+                            C = jj.body_c - b0;
+                            D = jj.body_d - b0;
+                        }
                     }
                     bool dA = (vbf[A] & kBfDynamic) != 0, dB = (vbf[B] & kBfDynamic) != 0;
                     int la = dA ? last[A] : 0, lb = dB ? last[B] : 0;
-                    int l = (la > lb ? la : lb) + 1;
+                    int l = (la > lb ? la : lb);
+                    const bool dC = C >= 0 && (vbf[C] & kBfDynamic) != 0, dD = D >= 0 && (vbf[D] & kBfDynamic) != 0;
+                    if (dC && last[C] > l) l = last[C];
+                    if (dD && last[D] > l) l = last[D];
+                    l += 1;
                     if (dA) last[A] = l;
                     if (dB) last[B] = l;
+                    if (dC) last[C] = l;
+                    if (dD) last[D] = l;
                     if (l > maxL) maxL = l;
                     x.s_level[kx + n] = l;
                     x.s_tmp[kx + n] = item;

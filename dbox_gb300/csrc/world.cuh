@@ -69,7 +69,7 @@ struct BodyStatic {
 };
 
 enum { kRevoluteJoint = 0, kDistanceJoint = 1, kRopeJoint = 2, kWeldJoint = 3, kFrictionJoint = 4, kMotorJoint = 5,
-       kWheelJoint = 6, kPrismaticJoint = 7, kPulleyJoint = 8, kMouseJoint = 9 };
+       kWheelJoint = 6, kPrismaticJoint = 7, kPulleyJoint = 8, kMouseJoint = 9, kGearJoint = 10 };
 // b2RevoluteJoint / b2DistanceJoint / b2RopeJoint / b2WeldJoint / b2FrictionJoint / b2MotorJoint /
 // b2WheelJoint / b2PrismaticJoint / b2PulleyJoint / b2MouseJoint (joints/b2revolutejoint.d,
 // b2distancejoint.d, b2ropejoint.d, b2weldjoint.d, b2frictionjoint.d, b2motorjoint.d,
@@ -112,6 +112,11 @@ struct DJoint {
     float ratio, constant, beta;
     float length_a, length_b;      // pulley: the definition's lengths (kept for the dump)
     int pad4;
+    // gear (joints/b2gearjoint.d): joint1 joins body_c (its A) to body_a (its B), joint2 body_d
+    // to body_b; ratio / constant as the pulley's, the impulse in impulse[0], the mass in mass[0]
+    int joint1, joint2, type_a, type_b, body_c, body_d;
+    float2 local_anchor_c, local_anchor_d, local_axis_c, local_axis_d, lcC, lcD, jv_ac, jv_bd;
+    float reference_angle_a, reference_angle_b, jw_a, jw_b, jw_c, jw_d, invMassC, invMassD, invIC, invID;
 };
 
 // b2ContactVelocityConstraint (contacts/b2contactsolver.d:43-58) with body indices in place of island indices.

@@ -20,10 +20,11 @@ _NUM = r"[-+0-9.eEinfa]+f?"
 _BODY_TYPES = {"b2_staticBody": 0, "b2_kinematicBody": 1, "b2_dynamicBody": 2}
 _JOINT_KINDS = {"Revolute": "revolute", "Distance": "distance", "Rope": "rope", "Weld": "weld",
                 "Friction": "friction", "Motor": "motor", "Wheel": "wheel", "Prismatic": "prismatic",
-                "Pulley": "pulley"}
+                "Pulley": "pulley", "Gear": "gear"}
 _JOINT_DEFS = {"revolute": abi.REVOLUTE_DEF, "distance": abi.DISTANCE_DEF, "rope": abi.ROPE_DEF,
                "weld": abi.WELD_DEF, "friction": abi.FRICTION_DEF, "motor": abi.MOTOR_DEF,
-               "wheel": abi.WHEEL_DEF, "prismatic": abi.PRISMATIC_DEF, "pulley": abi.PULLEY_DEF}
+               "wheel": abi.WHEEL_DEF, "prismatic": abi.PRISMATIC_DEF, "pulley": abi.PULLEY_DEF,
+               "gear": abi.GEAR_DEF}
 _JOINT_FIELDS = {"maxLength": "max_length", "localAxisA": "local_axis_a"}
 
 
@@ -50,7 +51,7 @@ def _value(text):
 
 def parse(text):
     """Parse dump text into {"gravity": (x, y), "bodies": BODY_DEF array, "fixtures": [ops],
-    "joints": [(kind, record)]} where each fixture op is ("fixture", body, SHAPE_DEF record,
+    "joints": [(kind, record, dump index)]} where each fixture op is ("fixture", body, SHAPE_DEF record,
     FIXTURE_DEF record) or ("chain", body, vertices, prev or None, next or None,
     FIXTURE_DEF record), in the text's order."""
     gravity = (0.0, -10.0)
@@ -125,6 +126,10 @@ def parse(text):
             kind = _JOINT_KINDS.get(m.group(1))
             jd = (kind, np.zeros(1, _JOINT_DEFS[kind])[0]) if kind else None
             continue
+        m = re.fullmatch(r"jd\.joint([12])=joints\[(\d+)\];", line)
+        if m and jd is not None:
+            jd[1]["joint" + m.group(1)] = int(m.group(2))
+            continue
         m = re.fullmatch(r"jd\.body([AB])=bodies\[(\d+)\];", line)
         if m and jd is not None:
             jd[1]["body_" + m.group(1).lower()] = int(m.group(2))
@@ -139,7 +144,7 @@ def parse(text):
             continue
         m = re.fullmatch(r"joints\[(\d+)\]=m_world\.CreateJoint\(&jd\);", line)
         if m and jd is not None:
-            joints.append(jd)
+            joints.append((jd[0], jd[1], int(m.group(1))))
             jd = None
     out = abi.body_defs(len(bodies))
     for i, b in enumerate(bodies):
@@ -185,9 +190,13 @@ def replay(parsed, target, world=None):
         else:
             _, b, vs, prev, nxt, loop, fd = op
             target.create_chain(*args, base[b], vs, loop, prev, nxt, fd)
-    for kind, d in parsed["joints"]:
+    made = {}                                           # dump index -> joint created
+    for kind, d, k in parsed["joints"]:
         d = d.copy()
         d["body_a"] = base[d["body_a"]]
         d["body_b"] = base[d["body_b"]]
-        target.create_joint(*args, kind, d)
+        if kind == "gear":
+            d["joint1"] = made[int(d["joint1"])]
+            d["joint2"] = made[int(d["joint2"])]
+        made[k] = target.create_joint(*args, kind, d)
     return base

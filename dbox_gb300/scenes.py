@@ -39,15 +39,36 @@ def _empty():
         "friction_joints": np.zeros(0, abi.FRICTION_DEF), "motor_joints": np.zeros(0, abi.MOTOR_DEF),
         "wheel_joints": np.zeros(0, abi.WHEEL_DEF), "prismatic_joints": np.zeros(0, abi.PRISMATIC_DEF),
         "pulley_joints": np.zeros(0, abi.PULLEY_DEF), "mouse_joints": np.zeros(0, abi.MOUSE_DEF),
+        "gear_joints": np.zeros(0, abi.GEAR_DEF),
         "chains": [], "gravity": (0.0, -10.0), "name": "",
     }
 
 
+# joint kinds in creation order: a scene's joints are created kind by kind in this order, so a
+# joint's index is the count of the earlier kinds plus its place in its own kind
+JOINT_KINDS = ("joints", "distance_joints", "rope_joints", "weld_joints", "friction_joints", "motor_joints",
+               "wheel_joints", "prismatic_joints", "pulley_joints", "mouse_joints", "gear_joints")
+
+
 def _concat(parts):
-    """Concatenate scene parts; fixture_body / joint body indices are offset per part."""
+    """Concatenate scene parts; fixture_body / joint body indices are offset per part, and a
+    gear joint's joint indices are moved to the joints' places in the concatenated order."""
     out = _empty()
     nb = 0
-    for p in parts:
+    counts = [[len(p.get(k, ())) for k in JOINT_KINDS] for p in parts]
+    totals = [sum(c[i] for c in counts) for i in range(len(JOINT_KINDS))]
+    for pi, p in enumerate(parts):
+        g = p.get("gear_joints", np.zeros(0, abi.GEAR_DEF)).copy()
+        g["body_a"] += nb
+        g["body_b"] += nb
+        for f in ("joint1", "joint2"):
+            for r in range(len(g)):
+                idx, k = int(g[r][f]), 0
+                while idx >= counts[pi][k]:
+                    idx -= counts[pi][k]
+                    k += 1
+                g[r][f] = sum(totals[:k]) + sum(c[k] for c in counts[:pi]) + idx
+        out["gear_joints"] = np.concatenate([out["gear_joints"], g])
         out["bodies"] = np.concatenate([out["bodies"], p["bodies"]])
         out["fixture_body"] = np.concatenate([out["fixture_body"], p["fixture_body"] + nb]).astype(np.int32)
         out["shapes"] = np.concatenate([out["shapes"], p["shapes"]])
@@ -474,6 +495,58 @@ def pulleys(n=3, x0=-10.0, spacing=8.0):
     out["pulley_joints"] = pj
     out["mouse_joints"] = mj
     out["name"] = "pulleys"
+    return out
+
+
+def _circles(centers, radius, btype=abi.DYNAMIC, density=1.0, friction=0.6):
+    s = _boxes(centers, radius, radius, btype, friction, density)
+    s["shapes"]["kind"] = abi.SHAPE_CIRCLE
+    s["shapes"]["radius"] = radius
+    return s
+
+
+def gears(boxes=12, seed=9):
+    """Gear joints (b2GearJointDef, joints/b2gearjoint.d:30-168) over revolute and prismatic
+    joints: two wheels on ground pivots geared by their radii (1 and 2, the small one driven
+    by a motor); a motor-driven wheel geared to a plate sliding on a prismatic axis (a rack);
+    a swinging arm on a ground pivot carrying
+    two wheels geared to each other through pivots on the arm (the gear's C and D bodies are
+    the dynamic arm); boxes dropped onto the machinery."""
+    rng = np.random.default_rng(seed)
+    parts = [ground_box()]
+    parts.append(_circles([(-10.0, 8.0)], 1.0))                   # 1: small wheel
+    parts.append(_circles([(-7.0, 8.0)], 2.0))                    # 2: large wheel
+    parts.append(_circles([(2.0, 7.0)], 1.0))                     # 3: rack wheel
+    parts.append(_boxes([(2.0, 5.5)], 3.0, 0.25, abi.DYNAMIC, 0.6, 1.0))   # 4: sliding plate
+    parts.append(_boxes([(12.0, 9.0)], 3.0, 0.2, abi.DYNAMIC, 0.6, 1.0))   # 5: arm
+    parts.append(_circles([(10.0, 9.0)], 0.8))                    # 6: arm wheel 1
+    parts.append(_circles([(14.0, 9.0)], 0.6))                    # 7: arm wheel 2
+    xs = rng.uniform(-12.0, 14.0, boxes)
+    parts.append(_boxes([(float(x), 14.0 + 0.8 * i) for i, x in enumerate(xs)], 0.3, 0.3, abi.DYNAMIC, 0.6, 1.0))
+    out = _concat(parts)
+    ground_y = -10.0
+    rj = np.zeros(6, abi.REVOLUTE_DEF)
+    for k, (b, x, y) in enumerate([(1, -10.0, 8.0), (2, -7.0, 8.0), (3, 2.0, 7.0), (5, 12.0, 9.0)]):
+        rj[k]["body_a"], rj[k]["body_b"] = 0, b
+        rj[k]["local_anchor_a"] = (x, y - ground_y)
+    rj[0]["enable_motor"], rj[0]["motor_speed"], rj[0]["max_motor_torque"] = 1, 2.0, 500.0
+    rj[2]["enable_motor"], rj[2]["motor_speed"], rj[2]["max_motor_torque"] = 1, -1.0, 300.0
+    for k, (b, dx) in enumerate([(6, -2.0), (7, 2.0)]):          # wheels pinned to the arm
+        rj[4 + k]["body_a"], rj[4 + k]["body_b"] = 5, b
+        rj[4 + k]["local_anchor_a"] = (dx, 0.0)
+    out["joints"] = rj
+    pj = np.zeros(1, abi.PRISMATIC_DEF)
+    pj[0]["body_a"], pj[0]["body_b"] = 0, 4
+    pj[0]["local_anchor_a"] = (2.0, 5.5 - ground_y)
+    pj[0]["local_axis_a"] = (1.0, 0.0)
+    pj[0]["enable_limit"], pj[0]["lower_translation"], pj[0]["upper_translation"] = 1, -4.0, 4.0
+    out["prismatic_joints"] = pj
+    gj = np.zeros(3, abi.GEAR_DEF)
+    gj[0]["body_a"], gj[0]["body_b"], gj[0]["joint1"], gj[0]["joint2"], gj[0]["ratio"] = 1, 2, 0, 1, 2.0   # r2 / r1
+    gj[1]["body_a"], gj[1]["body_b"], gj[1]["joint1"], gj[1]["joint2"], gj[1]["ratio"] = 3, 4, 2, 6, -1.0
+    gj[2]["body_a"], gj[2]["body_b"], gj[2]["joint1"], gj[2]["joint2"], gj[2]["ratio"] = 6, 7, 4, 5, 0.6 / 0.8
+    out["gear_joints"] = gj
+    out["name"] = "gears"
     return out
 
 

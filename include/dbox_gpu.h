@@ -195,6 +195,17 @@ typedef struct {
     float max_force, frequency_hz, damping_ratio;
 } dbox_mouse_def;
 
+/* b2GearJointDef (dynamics/joints/b2gearjoint.d:30-48): couples joint1 and joint2, each a
+ * revolute or prismatic joint; the gear acts on joint1's body B, joint2's body B and, through
+ * them, on the joints' A bodies.  body_a / body_b are the definition's bodies, which the
+ * reference uses only to flag their contacts for filtering (b2world.d:236-254). */
+typedef struct {
+    int32_t body_a, body_b;
+    int32_t collide_connected;
+    int32_t joint1, joint2;
+    float ratio;
+} dbox_gear_def;
+
 /* ------------------------------------------------------- world snapshot
  * Flat state records, used by dbox_world_export_state / import_state
  * (exact checkpoint/resume) and by the parity tests.  Flag words use the
@@ -317,6 +328,10 @@ int32_t dbox_fixture_create_chain(dbox_world* w, int32_t world, int32_t body, co
  * exports as an all-zero record (a proxy of id -1).  New proxies take the ids the reference's
  * tree hands out: freed leaves last in, first out, then never-used node ids. */
 int32_t dbox_body_destroy(dbox_world* w, int32_t world, int32_t body);
+/* b2World.CreateJoint with a b2GearJointDef (joints/b2gearjoint.d:83-168): joint1 and joint2
+ * are live revolute or prismatic joints of the same world; a joint a gear uses cannot be
+ * destroyed before the gear (DBOX_ERR_INVALID). */
+int32_t dbox_joint_create_gear(dbox_world* w, int32_t world, const dbox_gear_def* def, int32_t* out_joint);
 int32_t dbox_fixture_destroy(dbox_world* w, int32_t world, int32_t fixture);
 int32_t dbox_joint_destroy(dbox_world* w, int32_t world, int32_t joint);
 

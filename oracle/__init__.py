@@ -64,6 +64,7 @@ def lib():
         L.orc_joint_create_prismatic.argtypes = [vp, vp]
         L.orc_joint_create_pulley.argtypes = [vp, vp]
         L.orc_joint_create_mouse.argtypes = [vp, vp]
+        L.orc_joint_create_gear.argtypes = [vp, vp]
         L.orc_joint_set_mouse_target.argtypes = [vp, i32, f32, f32]
         L.orc_world_set_flags.argtypes = [vp, i32, i32, i32, i32, i32]
         L.orc_world_step.argtypes = [vp, f32, i32, i32]
@@ -145,7 +146,8 @@ class OracleWorld:
                                ("wheel_joints", abi.WHEEL_DEF, L.orc_joint_create_wheel),
                                ("prismatic_joints", abi.PRISMATIC_DEF, L.orc_joint_create_prismatic),
                                ("pulley_joints", abi.PULLEY_DEF, L.orc_joint_create_pulley),
-                               ("mouse_joints", abi.MOUSE_DEF, L.orc_joint_create_mouse)):
+                               ("mouse_joints", abi.MOUSE_DEF, L.orc_joint_create_mouse),
+                               ("gear_joints", abi.GEAR_DEF, L.orc_joint_create_gear)):
             for d in scene.get(key, ()):
                 dd = np.ascontiguousarray(np.array([d], dtype))
                 if fn(self.h, abi.ptr(dd)) < 0:
@@ -221,7 +223,7 @@ class OracleWorld:
 
     _JOINTS = {"revolute": "REVOLUTE_DEF", "distance": "DISTANCE_DEF", "rope": "ROPE_DEF", "weld": "WELD_DEF",
                "friction": "FRICTION_DEF", "motor": "MOTOR_DEF", "wheel": "WHEEL_DEF", "prismatic": "PRISMATIC_DEF",
-               "pulley": "PULLEY_DEF", "mouse": "MOUSE_DEF"}
+               "pulley": "PULLEY_DEF", "mouse": "MOUSE_DEF", "gear": "GEAR_DEF"}
 
     def create_body(self, body_def):
         dd = np.ascontiguousarray(np.array([body_def], abi.BODY_DEF))

@@ -2089,7 +2089,7 @@ struct TimeStep { f32 dt = 0, inv_dt = 0, dtRatio = 0; int velocityIterations = 
 struct SolverData { TimeStep step; Position* positions = nullptr; Velocity* velocities = nullptr; };
 
 enum { kRevoluteJoint = 0, kDistanceJoint = 1, kRopeJoint = 2, kWeldJoint = 3, kFrictionJoint = 4, kMotorJoint = 5,
-       kWheelJoint = 6, kPrismaticJoint = 7, kPulleyJoint = 8, kMouseJoint = 9 };
+       kWheelJoint = 6, kPrismaticJoint = 7, kPulleyJoint = 8, kMouseJoint = 9, kGearJoint = 10 };
 
 struct Joint {                                                          // joints/b2joint.d, b2revolutejoint.d, b2distancejoint.d
     int type = kRevoluteJoint;
@@ -2136,6 +2136,17 @@ struct Joint {                                                          // joint
     Vec2 groundAnchorA, groundAnchorB, uA, uB, targetA, mouseC;
     f32 ratio = 0, constant = 0, beta = 0, lengthA = 0, lengthB = 0;
     int dumpIndex = 0;           // b2Joint.m_index: the joint's place in the world list, set by Dump
+    // gear (b2gearjoint.d): joint1 joins bodyC (its A) to bodyA (its B), joint2 bodyD to bodyB;
+    // the impulse is impulse.x, the ratio and constant the pulley's fields
+    Joint* joint1 = nullptr;
+    Joint* joint2 = nullptr;
+    int typeA = 0, typeB = 0;
+    Body* bodyC = nullptr;
+    Body* bodyD = nullptr;
+    int indexC = 0, indexD = 0;
+    Vec2 localAnchorC, localAnchorD, localAxisC, localAxisD, lcC, lcD, JvAC, JvBD;
+    f32 referenceAngleA = 0, referenceAngleB = 0, JwA = 0, JwB = 0, JwC = 0, JwD = 0, mC = 0, mD = 0, iC = 0, iD = 0;
+    f32 gearMass = 0;
 
     void InitVelocityConstraints(const SolverData& data) {
         switch (type) {
@@ -2148,6 +2159,7 @@ struct Joint {                                                          // joint
         case kPrismaticJoint: PrismaticInit(data); break;
         case kPulleyJoint: PulleyInit(data); break;
         case kMouseJoint: MouseInit(data); break;
+        case kGearJoint: GearInit(data); break;
         default: RevoluteInit(data);
         }
     }
@@ -2162,6 +2174,7 @@ struct Joint {                                                          // joint
         case kPrismaticJoint: PrismaticSolveVelocity(data); break;
         case kPulleyJoint: PulleySolveVelocity(data); break;
         case kMouseJoint: MouseSolveVelocity(data); break;
+        case kGearJoint: GearSolveVelocity(data); break;
         default: RevoluteSolveVelocity(data);
         }
     }
@@ -2176,6 +2189,7 @@ struct Joint {                                                          // joint
         case kPrismaticJoint: return PrismaticSolvePosition(data);
         case kPulleyJoint: return PulleySolvePosition(data);
         case kMouseJoint: return true;
+        case kGearJoint: return GearSolvePosition(data);
         default: return RevoluteSolvePosition(data);
         }
     }
@@ -2189,6 +2203,170 @@ struct Joint {                                                          // joint
         invMassB = bodyB->invMass;
         invIA = bodyA->invI;
         invIB = bodyB->invI;
+    }
+
+    void GearInit(const SolverData& data) {                             // b2gearjoint.d:245-350
+        LoadBodies();
+        indexC = bodyC->islandIndex;
+        indexD = bodyD->islandIndex;
+        lcC = bodyC->sweep.localCenter;
+        lcD = bodyD->sweep.localCenter;
+        mC = bodyC->invMass;
+        mD = bodyD->invMass;
+        iC = bodyC->invI;
+        iD = bodyD->invI;
+        f32 aA = data.positions[indexA].a, aB = data.positions[indexB].a;
+        f32 aC = data.positions[indexC].a, aD = data.positions[indexD].a;
+        Vec2 vA = data.velocities[indexA].v, vB = data.velocities[indexB].v;
+        Vec2 vC = data.velocities[indexC].v, vD = data.velocities[indexD].v;
+        f32 wA = data.velocities[indexA].w, wB = data.velocities[indexB].w;
+        f32 wC = data.velocities[indexC].w, wD = data.velocities[indexD].w;
+        Rot qA(aA), qB(aB), qC(aC), qD(aD);
+        gearMass = 0.0f;
+        if (typeA == kRevoluteJoint) {
+            JvAC.SetZero();
+            JwA = 1.0f;
+            JwC = 1.0f;
+            gearMass += invIA + iC;
+        } else {
+            Vec2 u = Mul(qC, localAxisC);
+            Vec2 rC = Mul(qC, localAnchorC - lcC);
+            Vec2 rA2 = Mul(qA, localAnchorA - localCenterA);
+            JvAC = u;
+            JwC = Cross(rC, u);
+            JwA = Cross(rA2, u);
+            gearMass += mC + invMassA + iC * JwC * JwC + invIA * JwA * JwA;
+        }
+        if (typeB == kRevoluteJoint) {
+            JvBD.SetZero();
+            JwB = ratio;
+            JwD = ratio;
+            gearMass += ratio * ratio * (invIB + iD);
+        } else {
+            Vec2 u = Mul(qD, localAxisD);
+            Vec2 rD = Mul(qD, localAnchorD - lcD);
+            Vec2 rB2 = Mul(qB, localAnchorB - localCenterB);
+            JvBD = ratio * u;
+            JwD = ratio * Cross(rD, u);
+            JwB = ratio * Cross(rB2, u);
+            gearMass += ratio * ratio * (mD + invMassB) + iD * JwD * JwD + invIB * JwB * JwB;
+        }
+        gearMass = gearMass > 0.0f ? 1.0f / gearMass : 0.0f;
+        if (data.step.warmStarting) {
+            vA += (invMassA * impulse.x) * JvAC;
+            wA += invIA * impulse.x * JwA;
+            vB += (invMassB * impulse.x) * JvBD;
+            wB += invIB * impulse.x * JwB;
+            vC -= (mC * impulse.x) * JvAC;
+            wC -= iC * impulse.x * JwC;
+            vD -= (mD * impulse.x) * JvBD;
+            wD -= iD * impulse.x * JwD;
+        } else {
+            impulse.x = 0.0f;
+        }
+        data.velocities[indexA].v = vA;
+        data.velocities[indexA].w = wA;
+        data.velocities[indexB].v = vB;
+        data.velocities[indexB].w = wB;
+        data.velocities[indexC].v = vC;
+        data.velocities[indexC].w = wC;
+        data.velocities[indexD].v = vD;
+        data.velocities[indexD].w = wD;
+    }
+
+    void GearSolveVelocity(const SolverData& data) {                    // b2gearjoint.d:352-386
+        Vec2 vA = data.velocities[indexA].v, vB = data.velocities[indexB].v;
+        Vec2 vC = data.velocities[indexC].v, vD = data.velocities[indexD].v;
+        f32 wA = data.velocities[indexA].w, wB = data.velocities[indexB].w;
+        f32 wC = data.velocities[indexC].w, wD = data.velocities[indexD].w;
+        f32 Cdot = Dot(JvAC, vA - vC) + Dot(JvBD, vB - vD);
+        Cdot += (JwA * wA - JwC * wC) + (JwB * wB - JwD * wD);
+        f32 imp = -gearMass * Cdot;
+        impulse.x += imp;
+        vA += (invMassA * imp) * JvAC;
+        wA += invIA * imp * JwA;
+        vB += (invMassB * imp) * JvBD;
+        wB += invIB * imp * JwB;
+        vC -= (mC * imp) * JvAC;
+        wC -= iC * imp * JwC;
+        vD -= (mD * imp) * JvBD;
+        wD -= iD * imp * JwD;
+        data.velocities[indexA].v = vA;
+        data.velocities[indexA].w = wA;
+        data.velocities[indexB].v = vB;
+        data.velocities[indexB].w = wB;
+        data.velocities[indexC].v = vC;
+        data.velocities[indexC].w = wC;
+        data.velocities[indexD].v = vD;
+        data.velocities[indexD].w = wD;
+    }
+
+    bool GearSolvePosition(const SolverData& data) {                    // b2gearjoint.d:388-500
+        Vec2 cA = data.positions[indexA].c, cB = data.positions[indexB].c;
+        Vec2 cC = data.positions[indexC].c, cD = data.positions[indexD].c;
+        f32 aA = data.positions[indexA].a, aB = data.positions[indexB].a;
+        f32 aC = data.positions[indexC].a, aD = data.positions[indexD].a;
+        Rot qA(aA), qB(aB), qC(aC), qD(aD);
+        f32 coordinateA = 0, coordinateB = 0;
+        Vec2 jvAC, jvBD;
+        f32 jwA = 0, jwB = 0, jwC = 0, jwD = 0;
+        f32 mass = 0.0f;
+        if (typeA == kRevoluteJoint) {
+            jvAC.SetZero();
+            jwA = 1.0f;
+            jwC = 1.0f;
+            mass += invIA + iC;
+            coordinateA = aA - aC - referenceAngleA;
+        } else {
+            Vec2 u = Mul(qC, localAxisC);
+            Vec2 rC = Mul(qC, localAnchorC - lcC);
+            Vec2 rA2 = Mul(qA, localAnchorA - localCenterA);
+            jvAC = u;
+            jwC = Cross(rC, u);
+            jwA = Cross(rA2, u);
+            mass += mC + invMassA + iC * jwC * jwC + invIA * jwA * jwA;
+            Vec2 pC = localAnchorC - lcC;
+            Vec2 pA = MulT(qC, rA2 + (cA - cC));
+            coordinateA = Dot(pA - pC, localAxisC);
+        }
+        if (typeB == kRevoluteJoint) {
+            jvBD.SetZero();
+            jwB = ratio;
+            jwD = ratio;
+            mass += ratio * ratio * (invIB + iD);
+            coordinateB = aB - aD - referenceAngleB;
+        } else {
+            Vec2 u = Mul(qD, localAxisD);
+            Vec2 rD = Mul(qD, localAnchorD - lcD);
+            Vec2 rB2 = Mul(qB, localAnchorB - localCenterB);
+            jvBD = ratio * u;
+            jwD = ratio * Cross(rD, u);
+            jwB = ratio * Cross(rB2, u);
+            mass += ratio * ratio * (mD + invMassB) + iD * jwD * jwD + invIB * jwB * jwB;
+            Vec2 pD = localAnchorD - lcD;
+            Vec2 pB = MulT(qD, rB2 + (cB - cD));
+            coordinateB = Dot(pB - pD, localAxisD);
+        }
+        f32 C = (coordinateA + ratio * coordinateB) - constant;
+        f32 imp = 0.0f;
+        if (mass > 0.0f) imp = -C / mass;
+        cA += invMassA * imp * jvAC;
+        aA += invIA * imp * jwA;
+        cB += invMassB * imp * jvBD;
+        aB += invIB * imp * jwB;
+        cC -= mC * imp * jvAC;
+        aC -= iC * imp * jwC;
+        cD -= mD * imp * jvBD;
+        aD -= iD * imp * jwD;
+        data.positions[indexA].c = cA;
+        data.positions[indexA].a = aA;
+        data.positions[indexB].c = cB;
+        data.positions[indexB].a = aB;
+        data.positions[indexC].c = cC;
+        data.positions[indexC].a = aC;
+        data.positions[indexD].c = cD;
+        data.positions[indexD].a = aD;
+        return true;                                                    // linearError stays 0
     }
 
     void RopeInit(const SolverData& data) {                             // b2ropejoint.d:165-245
@@ -4500,7 +4678,11 @@ struct World {                                                          // dynam
 
     // the joint into the world's list and both bodies' edge lists, and the contact filter
     // flag when the bodies may not collide (b2world.d:206-258)
-    Joint* LinkJoint(Joint* j) {
+    // b2World.CreateJoint (b2world.d:196-261); flagA / flagB are the definition's bodies whose
+    // contacts get flagged (the joint's own bodies unless a gear joint overrode them)
+    Joint* LinkJoint(Joint* j, Body* flagA = nullptr, Body* flagB = nullptr) {
+        if (!flagA) flagA = j->bodyA;
+        if (!flagB) flagB = j->bodyB;
         j->prev = nullptr;
         j->next = jointList;
         if (jointList) jointList->prev = j;
@@ -4519,13 +4701,60 @@ struct World {                                                          // dynam
         if (j->bodyB->jointList) j->bodyB->jointList->prev = &j->edgeB;
         j->bodyB->jointList = &j->edgeB;
         if (!j->collideConnected) {
-            for (ContactEdge* edge = j->bodyB->contactList; edge; edge = edge->next) {
-                if (edge->other == j->bodyA) edge->contact->flags |= kContactFilter;
+            for (ContactEdge* edge = flagB->contactList; edge; edge = edge->next) {
+                if (edge->other == flagA) edge->contact->flags |= kContactFilter;
             }
         }
         j->index = (int)jointsByIndex.size();
         jointsByIndex.push_back(j);
         return j;
+    }
+
+    Joint* CreateGear(const dbox_gear_def* def) {                       // b2gearjoint.d:83-168
+        Joint* j = new Joint();
+        j->type = kGearJoint;
+        j->joint1 = jointsByIndex[def->joint1];
+        j->joint2 = jointsByIndex[def->joint2];
+        j->typeA = j->joint1->type;
+        j->typeB = j->joint2->type;
+        j->collideConnected = def->collide_connected != 0;
+        f32 coordinateA = 0, coordinateB = 0;
+        j->bodyC = j->joint1->bodyA;
+        j->bodyA = j->joint1->bodyB;
+        Transform xfA = j->bodyA->xf, xfC = j->bodyC->xf;
+        f32 aA = j->bodyA->sweep.a, aC = j->bodyC->sweep.a;
+        j->localAnchorC = j->joint1->localAnchorA;
+        j->localAnchorA = j->joint1->localAnchorB;
+        j->referenceAngleA = j->joint1->referenceAngle;
+        if (j->typeA == kRevoluteJoint) {
+            j->localAxisC.SetZero();
+            coordinateA = aA - aC - j->referenceAngleA;
+        } else {
+            j->localAxisC = j->joint1->localXAxisA;
+            Vec2 pC = j->localAnchorC;
+            Vec2 pA = MulT(xfC.q, Mul(xfA.q, j->localAnchorA) + (xfA.p - xfC.p));
+            coordinateA = Dot(pA - pC, j->localAxisC);
+        }
+        j->bodyD = j->joint2->bodyA;
+        j->bodyB = j->joint2->bodyB;
+        Transform xfB = j->bodyB->xf, xfD = j->bodyD->xf;
+        f32 aB = j->bodyB->sweep.a, aD = j->bodyD->sweep.a;
+        j->localAnchorD = j->joint2->localAnchorA;
+        j->localAnchorB = j->joint2->localAnchorB;
+        j->referenceAngleB = j->joint2->referenceAngle;
+        if (j->typeB == kRevoluteJoint) {
+            j->localAxisD.SetZero();
+            coordinateB = aB - aD - j->referenceAngleB;
+        } else {
+            j->localAxisD = j->joint2->localXAxisA;
+            Vec2 pD = j->localAnchorD;
+            Vec2 pB = MulT(xfD.q, Mul(xfB.q, j->localAnchorB) + (xfB.p - xfD.p));
+            coordinateB = Dot(pB - pD, j->localAxisD);
+        }
+        j->ratio = def->ratio;
+        j->constant = coordinateA + j->ratio * coordinateB;
+        j->impulse.SetZero();
+        return LinkJoint(j, bodiesByIndex[def->body_a], bodiesByIndex[def->body_b]);
     }
 
     void DestroyJoint(Joint* j) {                                        // b2world.d:265-360
@@ -5047,7 +5276,7 @@ static void DumpFixture(DumpText& t, const World& w, const Fixture* f, int bodyI
 static void DumpJoint(DumpText& t, const Joint* j) {                    // the joints' Dump
     static const char* names[] = {"b2RevoluteJointDef", "b2DistanceJointDef", "b2RopeJointDef", "b2WeldJointDef",
                                   "b2FrictionJointDef", "b2MotorJointDef", "b2WheelJointDef", "b2PrismaticJointDef",
-                                  "b2PulleyJointDef"};
+                                  "b2PulleyJointDef", "", "b2GearJointDef"};
     if (j->type == kMouseJoint) {                                       // b2mousejoint.d:180-183
         t.put("Mouse joint dumping is not supported.\n");
         return;
@@ -5058,6 +5287,11 @@ static void DumpJoint(DumpText& t, const Joint* j) {                    // the j
     t.put("  jd.bodyB = bodies[%d];\n", j->bodyB->islandIndex);
     t.flag(in, "jd.collideConnected", j->collideConnected ? 1 : 0);
     switch (j->type) {
+    case kGearJoint:                                                    // b2gearjoint.d:222-238
+        t.put("  jd.joint1 = joints[%d];\n", j->joint1->dumpIndex);
+        t.put("  jd.joint2 = joints[%d];\n", j->joint2->dumpIndex);
+        t.num(in, "jd.ratio", j->ratio);
+        break;
     case kRevoluteJoint:                                                // b2revolutejoint.d:293-312
         t.vec(in, "jd.localAnchorA", j->localAnchorA);
         t.vec(in, "jd.localAnchorB", j->localAnchorB);
@@ -5176,11 +5410,13 @@ static std::string DumpWorld(World& w) {                                // b2wor
     }
     i = 0;
     for (Joint* j = w.jointList; j; j = j->next) j->dumpIndex = i++;    // b2Joint.m_index
-    for (Joint* j = w.jointList; j; j = j->next) {                      // no gear joints: one pass
-        t.put("{\n");
-        DumpJoint(t, j);
-        t.put("}\n");
-    }
+    for (int pass = 0; pass < 2; ++pass)                                // gear joints last
+        for (Joint* j = w.jointList; j; j = j->next) {
+            if ((j->type == kGearJoint) != (pass == 1)) continue;
+            t.put("{\n");
+            DumpJoint(t, j);
+            t.put("}\n");
+        }
     t.put("b2Free(joints);\n");
     t.put("b2Free(bodies);\n");
     t.put("joints = null;\n");
@@ -5514,6 +5750,19 @@ int orc_joint_create_pulley(orc_world* w, const dbox_pulley_def* def) {
     return w->w.CreatePulley(def)->index;
 }
 
+// a gear needs two live revolute or prismatic joints and live definition bodies
+int orc_joint_create_gear(orc_world* w, const dbox_gear_def* def) {
+    int n = (int)w->w.bodiesByIndex.size(), nj = (int)w->w.jointsByIndex.size();
+    if (def->body_a < 0 || def->body_a >= n || def->body_b < 0 || def->body_b >= n || def->body_a == def->body_b ||
+        !w->w.bodiesByIndex[def->body_a] || !w->w.bodiesByIndex[def->body_b]) return -1;
+    for (int k : {def->joint1, def->joint2}) {
+        if (k < 0 || k >= nj || !w->w.jointsByIndex[k]) return -1;
+        int t = w->w.jointsByIndex[k]->type;
+        if (t != kRevoluteJoint && t != kPrismaticJoint) return -1;
+    }
+    return w->w.CreateGear(def)->index;
+}
+
 int orc_joint_create_mouse(orc_world* w, const dbox_mouse_def* def) {
     int n = (int)w->w.bodiesByIndex.size();
     if (def->body_a < 0 || def->body_a >= n || def->body_b < 0 || def->body_b >= n || def->body_a == def->body_b ||
@@ -5536,6 +5785,9 @@ int orc_fixture_destroy(orc_world* w, int fixture) {
 
 int orc_joint_destroy(orc_world* w, int joint) {
     if (joint < 0 || joint >= (int)w->w.jointsByIndex.size() || !w->w.jointsByIndex[joint]) return -1;
+    for (Joint* g : w->w.jointsByIndex)                                 // a gear still uses it
+        if (g && g->type == kGearJoint && (g->joint1 == w->w.jointsByIndex[joint] || g->joint2 == w->w.jointsByIndex[joint]))
+            return -1;
     w->w.DestroyJoint(w->w.jointsByIndex[joint]);
     return 0;
 }

@@ -36,6 +36,7 @@ int orc_body_create(orc_world* w, const dbox_body_def* def);
 int orc_fixture_create(orc_world* w, int body, const dbox_shape_def* shape, const dbox_fixture_def* def);
 int orc_joint_create_revolute(orc_world* w, const dbox_revolute_def* def);
 int orc_world_dump(orc_world* w, char* buf, int cap);
+int orc_joint_create_gear(orc_world* w, const dbox_gear_def* def);
 int orc_body_destroy(orc_world* w, int body);
 int orc_fixture_destroy(orc_world* w, int fixture);
 int orc_joint_destroy(orc_world* w, int joint);

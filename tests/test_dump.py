@@ -109,7 +109,7 @@ def _drop_velocity(text):
 
 
 @pytest.mark.parametrize("name", ["ropes", "welded", "cars", "sliders", "pulleys", "top_down", "edge_ground",
-                                  "chain_ground"])
+                                  "chain_ground", "gears"])
 def test_dump_replay_round_trip(oracle_lib, name):
     # dump -> parse -> replay reverses the list orders; twice restores them.  Replaying a dump
     # of a replayed world gives the same text again, except the linear velocity of bodies whose
@@ -140,7 +140,7 @@ def test_dump_replay_round_trip(oracle_lib, name):
     p3 = dump.parse(texts[2])
     for f in ("position", "angle", "angular_velocity", "type", "awake"):
         assert np.array_equal(p1["bodies"][f], p3["bodies"][f]), f
-    assert [(k, d.tobytes()) for k, d in p1["joints"]] == [(k, d.tobytes()) for k, d in p3["joints"]]
+    assert [(k, d.tobytes(), i) for k, d, i in p1["joints"]] == [(k, d.tobytes(), i) for k, d, i in p3["joints"]]
 
 
 def test_mouse_joint_dump_line(oracle_lib):
@@ -197,7 +197,7 @@ def test_dump_exact(oracle_lib, gpu_lib):
     # the library's dump of each world of a handle is the oracle's text, byte for byte, after
     # 60 steps (positions, angles, velocities, awake flags as the step left them)
     oracle_lib.set_trig_mode(1)
-    groups = [[scenes.ropes(), scenes.welded(), scenes.cars(), scenes.sliders(), scenes.pulleys()],
+    groups = [[scenes.ropes(), scenes.welded(), scenes.cars(), scenes.sliders(), scenes.pulleys(), scenes.gears()],
               [scenes.top_down()], [scenes.edge_ground(), scenes.chain_ground(), dumpshell_scene()]]
     for worlds in groups:
         gw = gpu_lib.World(worlds)

@@ -334,3 +334,22 @@ def test_chain_shapes_exact(oracle_lib, gpu_lib):
             for i, ow in enumerate(ows):
                 d = exact_diff(ow.export_state(), gw.export_state(i))
                 assert not d, "world %d step %d: %s" % (i, t + 1, d[:6])
+
+
+def test_gear_joints_exact(oracle_lib, gpu_lib):
+    # gear joints over revolute / revolute, revolute / prismatic, and two wheels on a swinging
+    # arm (the gear's C and D bodies dynamic, so its schedule level depends on four bodies),
+    # with boxes falling onto the machinery: bit-exact against the oracle
+    from dbox_gb300 import scenes
+    oracle_lib.set_trig_mode(1)
+    worlds = [scenes.gears(), scenes.gears(boxes=20, seed=4)]
+    gw = gpu_lib.World(worlds)
+    ows = [oracle_lib.OracleWorld(s) for s in worlds]
+    for t in range(240):
+        gw.step()
+        for ow in ows:
+            ow.step()
+        if t % 30 == 29:
+            for i, ow in enumerate(ows):
+                d = exact_diff(ow.export_state(), gw.export_state(i))
+                assert not d, "world %d step %d: %s" % (i, t + 1, d[:6])

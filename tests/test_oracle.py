@@ -350,3 +350,25 @@ def test_chain_shapes_collide(oracle_lib):
     assert np.isfinite(b["xf"]).all()
     assert b["xf"][dyn, 1].min() > 0.5                         # nothing fell through a chain (lowest at y = 1)
     assert (chain_c["point_count"] > 0).sum() > 10
+
+
+def test_gear_joints_hold_their_ratio(oracle_lib):
+    # b2GearJoint keeps coordinate1 + ratio * coordinate2 at its initial value: the wheel of
+    # radius 2 turns at half the speed of the radius-1 wheel, in the other sense; the rack
+    # wheel moves its plate by its radius per radian; the wheels on the swinging arm keep
+    # their ratio relative to it
+    from dbox_gb300 import scenes
+    oracle_lib.set_trig_mode(1)
+    s = scenes.gears()
+    ow = oracle_lib.OracleWorld(s)
+    st0 = ow.export_state()["bodies"]
+    ow.step(steps=120)
+    st = ow.export_state()["bodies"]
+    a = lambda i: float(st["sweep"][i, 7] - st0["sweep"][i, 7])
+    assert abs(a(1)) > 1.0                                      # the motor turned the small wheel
+    assert abs(a(1) + 2.0 * a(2)) < 0.02
+    dx = float(st["xf"][4, 0] - st0["xf"][4, 0])
+    assert abs(dx) > 0.5 and abs(a(3) - dx) < 0.02
+    rel = lambda i: a(i) - a(5)
+    assert abs(rel(6) + 0.75 * rel(7)) < 0.02
+    assert np.isfinite(st["xf"]).all()
