@@ -123,6 +123,10 @@ struct ProxyIds {
     }
 };
 
+// worlds with at least this many fixtures generate their end-of-Solve pairs on a block of
+// 1024 threads instead of their solve warp
+constexpr int kPairBlockFixtures = 4096;
+
 struct HostWorld {
     std::vector<ChainRec> chains;
     ProxyIds ids;
@@ -216,6 +220,9 @@ struct dbox_world {
     DBuf<int> s_sapi0, s_sapi1;
     DBuf<float4> s_sapbox;
     DBuf<int> d_porder;         // per world: fixtures in proxy-id order
+    DBuf<int> s_sapcell;        // per world: the broad-phase grid's cell tables
+    DBuf<int> d_big;            // worlds whose end-of-Solve pairs a block generates
+    int n_big = 0;
     DBuf<unsigned char> s_cevt;
     std::vector<dbox_contact_event> h_events;
     std::vector<dg::WorldInfo> wi;
@@ -270,7 +277,7 @@ void free_device(dbox_world* w) {
     w->d_solve_order.free(); w->d_solve_queue.free();
     w->s_feat.free(); w->s_vsave.free(); w->s_slog.free(); w->s_pend.free();
     w->d_events.free(); w->s_cevt.free();
-    w->s_sapk0.free(); w->s_sapk1.free(); w->s_sapi0.free(); w->s_sapi1.free(); w->s_sapbox.free(); w->d_porder.free();
+    w->s_sapk0.free(); w->s_sapk1.free(); w->s_sapi0.free(); w->s_sapi1.free(); w->s_sapbox.free(); w->d_porder.free(); w->s_sapcell.free(); w->d_big.free(); w->n_big = 0;
     w->s_cbody.free(); w->s_adj_items.free(); w->s_isl_pair.free(); w->s_cq.free(); w->s_cvis.free(); w->s_bfl.free(); w->s_sbody.free(); w->d_prof.free();
     if (w->graph) { cudaGraphExecDestroy(w->graph); w->graph = nullptr; }
     if (w->tgraph) { cudaGraphExecDestroy(w->tgraph); w->tgraph = nullptr; }
@@ -468,7 +475,7 @@ int upload(dbox_world* w) {
     w->wi.assign(W, dg::WorldInfo());
     int nb = 0, nf = 0, nj = 0, nc = 0, nh = 0, np = 0, nbx = 0, nkx = 0;
     int cpb = w->caps.contacts_per_body > 0 ? w->caps.contacts_per_body : 8;
-    std::vector<int> porder;
+    std::vector<int> porder, big;
     for (int i = 0; i < W; ++i) {
         HostWorld& hw = w->worlds[i];
         dg::WorldInfo& wi = w->wi[i];
@@ -486,6 +493,8 @@ int upload(dbox_world* w) {
         wi.snap_start = nc;
         // broad-phase walk order: fixtures by proxy id (no-proxy fixtures last); the plain
         // fixture order while the ids rise with the fixture index (always, without destruction)
+        wi.pair_block = f >= kPairBlockFixtures ? 1 : 0;
+        if (wi.pair_block) big.push_back(i);
         wi.proxy_order = 0;
         for (int i = 0, last = -1; i < f; ++i) {
             const int id = hw.px[i].proxy_id;
@@ -600,6 +609,9 @@ int upload(dbox_world* w) {
     ok &= w->s_sapi0.alloc(nf) == 0 && w->s_sapi1.alloc(nf) == 0;
     ok &= w->s_sapbox.alloc(nf) == 0;
     ok &= w->d_porder.alloc(nf) == 0;
+    ok &= w->s_sapcell.alloc(8 * (size_t)nf + 130 * (size_t)W) == 0;
+    ok &= w->d_big.alloc(big.size()) == 0;
+    w->n_big = (int)big.size();
     ok &= w->s_cstate.alloc(nc) == 0;
     ok &= w->s_adj_items.alloc(2 * (size_t)nc) == 0;
     ok &= w->s_isl_pair.alloc(nc) == 0;
@@ -646,6 +658,7 @@ int upload(dbox_world* w) {
         CU(cudaMemcpy(w->d_fx.p, fx.data(), sizeof(dg::DFixture) * nf, cudaMemcpyHostToDevice));
         CU(cudaMemcpy(w->d_px.p, px.data(), sizeof(dbox_proxy_state) * nf, cudaMemcpyHostToDevice));
         CU(cudaMemcpy(w->d_porder.p, porder.data(), sizeof(int) * nf, cudaMemcpyHostToDevice));
+        if (!big.empty()) CU(cudaMemcpy(w->d_big.p, big.data(), sizeof(int) * big.size(), cudaMemcpyHostToDevice));
     }
     if (nj) CU(cudaMemcpy(w->d_jt.p, jt.data(), sizeof(dg::DJoint) * nj, cudaMemcpyHostToDevice));
     if (nc) {
@@ -771,6 +784,9 @@ dg::Ctx make_ctx(dbox_world* w, float dt, int vi, int pi) {
     x.s_sapi[1] = w->s_sapi1.p;
     x.s_sapbox = w->s_sapbox.p;
     x.proxy_order = w->d_porder.p;
+    x.s_sapcell = w->s_sapcell.p;
+    x.big_worlds = w->d_big.p;
+    x.n_big = w->n_big;
     x.s_cevt = w->s_cevt.p;
     return x;
 }

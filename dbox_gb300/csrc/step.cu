@@ -226,6 +226,7 @@ struct Sap {
     int n;                 // ordinary proxies
     const int* wide;       // wide proxies (extent over 4x the mean): index | moved << 31
     int nwide;
+    const int* cstart;     // per cell (and one past the last): the first sorted proxy in it or after it
     float ox, oy, inv;     // grid origin and 1 / cell size
     int ncx, ncy;          // cells per row, rows
 };
@@ -274,14 +275,25 @@ DG Sap sap_build(const Ctx& x, int w, int* hist) {
     }
     Sap s;
     float cellsz = ext > 1e-6f ? ext * 1.001f : 1.0f;
-    // keep the grid at most 4096 x 4096 cells (larger cells only widen the candidate ranges)
+    // at most 4 cells per proxy (+ 64), so the cell table fits its scratch (larger cells only
+    // widen the candidate ranges)
     float span = bmax(hi[0] - lo[0], hi[1] - lo[1]);
     if (span / cellsz > 4000.0f) cellsz = span / 4000.0f;
     s.ox = lo[0];
     s.oy = lo[1];
-    s.inv = 1.0f / cellsz;
-    s.ncx = (int)((hi[0] - lo[0]) * s.inv) + 2;
-    s.ncy = (int)((hi[1] - lo[1]) * s.inv) + 2;
+    const float cap = 4.0f * (float)nf + 64.0f;
+    for (int it = 0;; ++it) {
+        s.inv = 1.0f / cellsz;
+        s.ncx = (int)((hi[0] - lo[0]) * s.inv) + 2;
+        s.ncy = (int)((hi[1] - lo[1]) * s.inv) + 2;
+        if ((float)s.ncx * (float)s.ncy <= cap) break;
+        cellsz = it < 32 ? cellsz * 1.05f * sqrtf((float)s.ncx * (float)s.ncy / cap) : 4.0f * span + 1.0f;
+    }
+    if (!(s.ncx >= 1 && s.ncy >= 1 && s.ncx <= 65536 && s.ncy <= 65536)) {   // non-finite bounds: one cell
+        s.ncx = 1;
+        s.ncy = 1;
+        s.inv = 0.0f;
+    }
     unsigned* k0 = x.s_sapk[0] + f0;
     unsigned* k1 = x.s_sapk[1] + f0;
     int* i0 = x.s_sapi[0] + f0;
@@ -358,7 +370,28 @@ DG Sap sap_build(const Ctx& x, int w, int* hist) {
         }
         nw += __popc(bal);
     }
+    // cell table: cstart[c] = the first sorted index whose cell is >= c (cstart[ncell] = nv)
+    const int ncell = s.ncx * s.ncy;
+    int* cstart = x.s_sapcell + 8 * f0 + 130 * w;
+    for (int c = lane; c <= ncell; c += kWarp) cstart[c] = nv;
     tsync();
+    for (int r = lane; r < nv; r += kWarp)
+        if (r == 0 || k1[r] != k1[r - 1]) cstart[k1[r]] = r;
+    tsync();
+    int carry = nv;                                  // suffix minimum, 32 cells at a time from the end
+    for (int base = (ncell / kWarp) * kWarp; base >= 0; base -= kWarp) {
+        const int c = base + lane;
+        int v = c <= ncell ? cstart[c] : nv;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_down_sync(0xffffffffu, v, o);
+            if (lane + o < 32 && t < v) v = t;
+        }
+        if (carry < v) v = carry;
+        if (c <= ncell) cstart[c] = v;
+        carry = __shfl_sync(0xffffffffu, v, 0);
+    }
+    tsync();
+    s.cstart = cstart;
     s.key = k1;
     s.box = x.s_sapbox + f0;
     s.idx = i1;
@@ -383,23 +416,25 @@ DG void sap_partners(const Sap& s, const AABB& fa, int a, bool amoved, F&& fn) {
     const int cx1 = sap_cell(fa.hi.x, s.ox, s.inv, s.ncx), cy1 = sap_cell(fa.hi.y, s.oy, s.inv, s.ncy);
     const int xa = cx0 > 0 ? cx0 - 1 : 0;
     for (int cy = cy0 > 0 ? cy0 - 1 : 0; cy <= cy1; ++cy) {
-        const unsigned klo = (unsigned)(cy * s.ncx + xa), khi = (unsigned)(cy * s.ncx + cx1);
-        int l = 0, r = s.n;                           // first key >= klo
-        while (l < r) { int m = (l + r) >> 1; if (s.key[m] < klo) l = m + 1; else r = m; }
-        for (int q = l; q < s.n && s.key[q] <= khi; ++q) test(s.idx[q], s.box[q]);
+        const int klo = cy * s.ncx + xa, khi = cy * s.ncx + cx1;
+        const int qe = s.cstart[khi + 1];
+        for (int q = s.cstart[klo]; q < qe; ++q) test(s.idx[q], s.box[q]);
     }
     for (int q = 0; q < s.nwide; ++q) test(s.wide[q], s.box[s.n + q]);
 }
 
-__device__ __noinline__ void find_new_contacts(const Ctx& x, int w) {
+// The pairs of UpdatePairs in (idA, idB) order into x.pairs (one warp); returns their count, or
+// -1 when they overflow the world's pair buffer.  The move buffer is cleared.
+template <bool kPerm>
+__device__ __noinline__ int gen_pairs_warp_t(const Ctx& x, int w) {
     const WorldInfo& wi = x.wi[w];
     WorldDyn& wd = x.wd[w];
     int lane = lane_id();
     int f0 = wi.fix_start, nf = wi.fix_count;
     // proxies are walked by rank, in ascending proxy id (b2PairLessThan, b2broadphase.d:166):
     // the rank is the fixture index unless destruction let a newer fixture reuse a lower id
-    const int* ord = wi.proxy_order ? x.proxy_order + f0 : nullptr;
-    auto PX = [ord](int r) { return ord ? ord[r] : r; };
+    const int* ord = x.proxy_order + f0;
+    auto PX = [ord](int r) { return kPerm ? ord[r] : r; };          // the plain order needs no lookup
     // moved list, ascending rank
     int nm = 0;
     for (int base = 0; base < nf; base += kWarp) {
@@ -410,7 +445,7 @@ __device__ __noinline__ void find_new_contacts(const Ctx& x, int w) {
         nm += __popc(bal);
     }
     tsync();
-    if (nm == 0) return;
+    if (nm == 0) return 0;
     __shared__ int sap_hist[kSolveWarps][256];
     const bool use_sap = nf >= kSapMinProxies;
     Sap sap;
@@ -452,7 +487,7 @@ __device__ __noinline__ void find_new_contacts(const Ctx& x, int w) {
     tsync();
     if (total > wi.pair_cap) {
         if (lane == 0) set_error(x, w, DBOX_ERR_CAPACITY);
-        return;
+        return -1;
     }
     if (lane == 0) wd.acc_pairs += (unsigned long long)total;
     // fill pairs in (a, b) order
@@ -486,7 +521,19 @@ __device__ __noinline__ void find_new_contacts(const Ctx& x, int w) {
     tsync();
     // clear the move buffer
     for (int i = lane; i < nf; i += kWarp) x.px[f0 + PX(i)].moved = 0;
-    // AddPair, in pair order
+    return total;
+}
+
+__device__ __forceinline__ int gen_pairs_warp(const Ctx& x, int w) {
+    return x.wi[w].proxy_order ? gen_pairs_warp_t<true>(x, w) : gen_pairs_warp_t<false>(x, w);
+}
+
+// b2ContactManager.AddPair (b2contactmanager.d:52-176) for the world's `total` pairs in x.pairs,
+// in pair order (one warp)
+__device__ __noinline__ void add_pairs(const Ctx& x, int w, int total) {
+    const WorldInfo& wi = x.wi[w];
+    WorldDyn& wd = x.wd[w];
+    const int lane = lane_id();
     int n = wd.contact_count;
     int added = 0;
     for (int base = 0; base < total; base += kWarp) {
@@ -554,6 +601,236 @@ __device__ __noinline__ void find_new_contacts(const Ctx& x, int w) {
     tsync();
     if (lane == 0) wd.contact_count = n + added;
     tsync();
+}
+
+// b2ContactManager.FindNewContacts (b2contactmanager.d:320-323) on one warp
+__device__ __noinline__ void find_new_contacts(const Ctx& x, int w) {
+    const int total = gen_pairs_warp(x, w);
+    if (total > 0) add_pairs(x, w, total);
+}
+
+// ------------------------------------------------------------ end-of-Solve pairs of a large world, one block
+// The pairs gen_pairs_warp makes, in the same order, with a block's 1024 threads sharing the
+// work: the ordinary proxies go into the same kind of grid (cell = lower corner, cells at
+// least as large as any ordinary proxy) by a counting sort whose order inside a cell does not
+// matter (each proxy's partners are sorted by rank), the wide ones into a list every proxy
+// tests; partner counts, a block scan, then the fill.
+constexpr int kPairThreads = 1024;
+
+template <class T, class Op>
+DG T block_reduce(T v, Op op, T* sh) {
+    const int lane = lane_id(), warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) v = op(v, __shfl_xor_sync(0xffffffffu, v, o));
+    __syncthreads();
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    v = sh[0];
+    for (int k = 1; k < nwarps; ++k) v = op(v, sh[k]);
+    return v;
+}
+
+// exclusive scan of a[0..n) in place; returns the total
+DG int block_exclusive_scan(int* a, int n, int* sh) {
+    const int lane = lane_id(), warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    int carry = 0;
+    for (int base = 0; base < n; base += blockDim.x) {
+        const int i = base + (int)threadIdx.x;
+        const int v = i < n ? a[i] : 0;
+        int incl = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        __syncthreads();
+        if (lane == 31) sh[warp] = incl;
+        __syncthreads();
+        if (warp == 0) {
+            int sv = lane < nwarps ? sh[lane] : 0;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, sv, o);
+                if (lane >= o) sv += t;
+            }
+            if (lane < nwarps) sh[lane] = sv;
+        }
+        __syncthreads();
+        const int before = warp > 0 ? sh[warp - 1] : 0;
+        if (i < n) a[i] = carry + before + incl - v;
+        carry += sh[nwarps - 1];
+    }
+    __syncthreads();
+    return carry;
+}
+
+DG void sync_fixtures(const Ctx& x, int b);
+__global__ void __launch_bounds__(kPairThreads) k_pairs_block(const __grid_constant__ Ctx x) {
+    __shared__ float shf[32];
+    __shared__ int shi[32];
+    __shared__ int n_wide;
+    const int w = x.big_worlds[blockIdx.x];
+    const WorldInfo& wi = x.wi[w];
+    WorldDyn& wd = x.wd[w];
+    const int tid = threadIdx.x, nt = blockDim.x;
+    if (!(wd.step_complete && x.dt > 0.0f) || wd.error != 0) {        // solve_world did not reach its broad-phase
+        if (tid == 0) wd.pair_total = 0;
+        return;
+    }
+    // SynchronizeFixtures of the island bodies (b2world.d:1099-1116), the solve warp's last step
+    for (int i = tid; i < wi.body_count; i += nt) {
+        const int b = wi.body_start + i;
+        if ((x.bs[b].flags & kBodyIsland) == 0 || x.bs[b].type == kStaticBody) continue;
+        sync_fixtures(x, b);
+    }
+    __syncthreads();
+    const int f0 = wi.fix_start, nf = wi.fix_count;
+    const int* ord = wi.proxy_order ? x.proxy_order + f0 : nullptr;
+    auto PX = [ord](int r) { return ord ? ord[r] : r; };
+    auto extent = [](const dbox_proxy_state& p) { return bmax(p.fat_aabb[2] - p.fat_aabb[0], p.fat_aabb[3] - p.fat_aabb[1]); };
+    auto isum = [](int a, int b) { return a + b; };
+    auto fsum = [](float a, float b) { return a + b; };
+    auto fmn = [](float a, float b) { return bmin(a, b); };
+    auto fmx = [](float a, float b) { return bmax(a, b); };
+    // live proxies, moved ones, mean extent (the wide cut of sap_build)
+    int cnt = 0, nm = 0;
+    float sum = 0.0f;
+    for (int r = tid; r < nf; r += nt) {
+        const dbox_proxy_state& p = x.px[f0 + PX(r)];
+        if (p.proxy_id < 0) continue;
+        ++cnt;
+        sum += extent(p);
+        if (p.moved) ++nm;
+    }
+    cnt = block_reduce(cnt, isum, shi);
+    nm = block_reduce(nm, isum, shi);
+    sum = block_reduce(sum, fsum, shf);
+    if (nm == 0) {
+        if (tid == 0) wd.pair_total = 0;
+        return;
+    }
+    const float cut = 4.0f * sum / (float)(cnt > 0 ? cnt : 1);
+    float ext = 0.0f, lo0 = 3.4e38f, lo1 = 3.4e38f, hi0 = -3.4e38f, hi1 = -3.4e38f;
+    int nv = 0;
+    for (int r = tid; r < nf; r += nt) {
+        const dbox_proxy_state& p = x.px[f0 + PX(r)];
+        if (p.proxy_id < 0 || extent(p) > cut) continue;
+        ++nv;
+        ext = bmax(ext, extent(p));
+        lo0 = bmin(lo0, p.fat_aabb[0]);
+        lo1 = bmin(lo1, p.fat_aabb[1]);
+        hi0 = bmax(hi0, p.fat_aabb[0]);
+        hi1 = bmax(hi1, p.fat_aabb[1]);
+    }
+    nv = block_reduce(nv, isum, shi);
+    ext = block_reduce(ext, fmx, shf);
+    lo0 = block_reduce(lo0, fmn, shf);
+    lo1 = block_reduce(lo1, fmn, shf);
+    hi0 = block_reduce(hi0, fmx, shf);
+    hi1 = block_reduce(hi1, fmx, shf);
+    // the grid (as sap_build sizes it)
+    Sap s;
+    float cellsz = ext > 1e-6f ? ext * 1.001f : 1.0f;
+    const float span = bmax(hi0 - lo0, hi1 - lo1);
+    if (span / cellsz > 4000.0f) cellsz = span / 4000.0f;
+    s.ox = lo0;
+    s.oy = lo1;
+    const float capc = 4.0f * (float)nf + 64.0f;
+    for (int it = 0;; ++it) {
+        s.inv = 1.0f / cellsz;
+        s.ncx = (int)((hi0 - lo0) * s.inv) + 2;
+        s.ncy = (int)((hi1 - lo1) * s.inv) + 2;
+        if ((float)s.ncx * (float)s.ncy <= capc) break;
+        cellsz = it < 32 ? cellsz * 1.05f * sqrtf((float)s.ncx * (float)s.ncy / capc) : 4.0f * span + 1.0f;
+    }
+    if (!(s.ncx >= 1 && s.ncy >= 1 && s.ncx <= 65536 && s.ncy <= 65536)) {
+        s.ncx = 1;
+        s.ncy = 1;
+        s.inv = 0.0f;
+    }
+    const int ncell = s.ncx * s.ncy;
+    int* cstart = x.s_sapcell + 8 * f0 + 130 * w;                        // ncell + 1 entries
+    int* cursor = cstart + 4 * nf + 65;                                  // ncell entries
+    int* sidx = x.s_sapi[1] + f0;                                        // ordinary proxies by cell
+    int* wide = x.s_sapi[0] + f0;                                        // wide proxies
+    float4* box = x.s_sapbox + f0;                                       // their boxes, the wide ones after nv
+    for (int c = tid; c <= ncell; c += nt) cstart[c] = 0;
+    if (tid == 0) n_wide = 0;
+    __syncthreads();
+    for (int r = tid; r < nf; r += nt) {                                 // counts per cell; the wide list
+        const dbox_proxy_state& p = x.px[f0 + PX(r)];
+        if (p.proxy_id < 0) continue;
+        if (extent(p) > cut) {
+            const int k = atomicAdd(&n_wide, 1);
+            wide[k] = p.moved ? (r | (int)0x80000000) : r;
+            box[nv + k] = make_float4(p.fat_aabb[0], p.fat_aabb[1], p.fat_aabb[2], p.fat_aabb[3]);
+        } else {
+            const int cx = sap_cell(p.fat_aabb[0], s.ox, s.inv, s.ncx), cy = sap_cell(p.fat_aabb[1], s.oy, s.inv, s.ncy);
+            atomicAdd(&cstart[cy * s.ncx + cx], 1);
+        }
+    }
+    __syncthreads();
+    block_exclusive_scan(cstart, ncell + 1, shi);
+    for (int c = tid; c < ncell; c += nt) cursor[c] = cstart[c];
+    __syncthreads();
+    for (int r = tid; r < nf; r += nt) {                                 // counting-sort scatter
+        const dbox_proxy_state& p = x.px[f0 + PX(r)];
+        if (p.proxy_id < 0 || extent(p) > cut) continue;
+        const int cx = sap_cell(p.fat_aabb[0], s.ox, s.inv, s.ncx), cy = sap_cell(p.fat_aabb[1], s.oy, s.inv, s.ncy);
+        const int slot = atomicAdd(&cursor[cy * s.ncx + cx], 1);
+        sidx[slot] = p.moved ? (r | (int)0x80000000) : r;
+        box[slot] = make_float4(p.fat_aabb[0], p.fat_aabb[1], p.fat_aabb[2], p.fat_aabb[3]);
+    }
+    __syncthreads();
+    s.key = nullptr;
+    s.box = box;
+    s.idx = sidx;
+    s.n = nv;
+    s.wide = wide;
+    s.nwide = n_wide;
+    s.cstart = cstart;
+    for (int a = tid; a < nf; a += nt) {                                 // partners per proxy
+        int c = 0;
+        const dbox_proxy_state& p = x.px[f0 + PX(a)];
+        if (p.proxy_id >= 0)
+            sap_partners(s, proxy_fat(x, f0 + PX(a)), a, p.moved != 0, [&](int) { ++c; });
+        x.s_pcount[f0 + a] = c;
+    }
+    __syncthreads();
+    const int total = block_exclusive_scan(x.s_pcount + f0, nf, shi);
+    if (total > wi.pair_cap) {
+        if (tid == 0) { set_error(x, w, DBOX_ERR_CAPACITY); wd.pair_total = 0; }
+        return;
+    }
+    for (int a = tid; a < nf; a += nt) {                                 // the pairs, partners by rank
+        const dbox_proxy_state& p = x.px[f0 + PX(a)];
+        if (p.proxy_id < 0) continue;
+        int2* seg = x.pairs + wi.pair_start + x.s_pcount[f0 + a];
+        int c = 0;
+        sap_partners(s, proxy_fat(x, f0 + PX(a)), a, p.moved != 0, [&](int b) { seg[c++] = make_int2(a, b); });
+        for (int i = 1; i < c; ++i) {
+            int2 v = seg[i];
+            int j = i - 1;
+            while (j >= 0 && seg[j].y > v.y) { seg[j + 1] = seg[j]; --j; }
+            seg[j + 1] = v;
+        }
+        for (int i = 0; i < c; ++i) seg[i] = make_int2(f0 + PX(seg[i].x), f0 + PX(seg[i].y));
+    }
+    __syncthreads();
+    for (int i = tid; i < nf; i += nt) x.px[f0 + i].moved = 0;          // the move buffer is consumed
+    if (tid == 0) {
+        wd.acc_pairs += (unsigned long long)total;
+        wd.pair_total = total;
+    }
+}
+
+// AddPair for the block's pairs, then the world's SolveTOI (one warp per large world)
+DG void toi_world(const Ctx& x, int w, float* sbp);
+__global__ void k_finish_big(const __grid_constant__ Ctx x) {
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+    if (i >= x.n_big) return;
+    const int w = x.big_worlds[i];
+    const int total = x.wd[w].pair_total;
+    if (total > 0) add_pairs(x, w, total);
+    tsync();
+    toi_world(x, w, x.s_sbody + 6 * (size_t)x.wi[w].body_start);
 }
 
 // ------------------------------------------------------------ kernels
@@ -3633,17 +3910,19 @@ DG void solve_world(const Ctx& x, int w, float* sbp, bool sb_smem, float* stage_
     }
     tsync();
     stamp(x, w, 9);
-    // SynchronizeFixtures for bodies that were in an island (b2world.d:1099-1116)
-    for (int i = lane; i < nb; i += kWarp) {
-        int b = b0 + i;
-        if ((x.bs[b].flags & kBodyIsland) == 0) continue;
-        if (x.bs[b].type == kStaticBody) continue;
-        sync_fixtures(x, b);
-    }
+    // SynchronizeFixtures for bodies that were in an island (b2world.d:1099-1116); a large
+    // world's block does it in k_pairs_block
+    if (!wi.pair_block)
+        for (int i = lane; i < nb; i += kWarp) {
+            int b = b0 + i;
+            if ((x.bs[b].flags & kBodyIsland) == 0) continue;
+            if (x.bs[b].type == kStaticBody) continue;
+            sync_fixtures(x, b);
+        }
     tsync();
     stamp(x, w, 10);
     hash_rebuild(x, w);
-    find_new_contacts(x, w);
+    if (!wi.pair_block) find_new_contacts(x, w);                         // else k_pairs_block + k_finish_big
     stamp(x, w, 11);
 }
 
@@ -4130,7 +4409,7 @@ __global__ void __launch_bounds__(kSolveWarps * 32, 3) k_solve_toi(const __grid_
         if (x.prof) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(g0));
         solve_world(x, w, sbp, in_smem, stage_f, ring);
         tsync();
-        toi_world(x, w, sbp);
+        if (!x.wi[w].pair_block) toi_world(x, w, sbp);                   // large worlds: k_finish_big
         tsync();
         if (heavy && lane == 0) atomicExch(&x.solve_queue[2 + sub], 0);
         if (x.prof && lane == 0) {
@@ -4167,9 +4446,13 @@ extern "C" int dbox_launch_step_ev(const dg::Ctx* x, cudaStream_t stream, int* l
     if (ev) cudaEventRecordWithFlags(ev[1], stream, cudaEventRecordExternal);
     if (x->solve_queue) cudaMemsetAsync(x->solve_queue, 0, sizeof(int) * (2 + 4 * (size_t)x->solve_nsm), stream);
     dg::k_solve_toi<<<x->solve_blocks, x->solve_wpb * dg::kWarp, x->solve_smem_floats * sizeof(float), stream>>>(*x);
+    if (x->n_big > 0) {                             // large worlds: their pairs on a block each, then AddPair + TOI
+        dg::k_pairs_block<<<x->n_big, dg::kPairThreads, 0, stream>>>(*x);
+        dg::k_finish_big<<<(x->n_big * dg::kWarp + threads - 1) / threads, threads, 0, stream>>>(*x);
+    }
     if (ev) cudaEventRecordWithFlags(ev[2], stream, cudaEventRecordExternal);
     if (ev) cudaEventRecordWithFlags(ev[3], stream, cudaEventRecordExternal);
-    if (launches) *launches = 4;
+    if (launches) *launches = x->n_big > 0 ? 6 : 4;
     return (int)cudaGetLastError();
 }
 

@@ -30,6 +30,8 @@ struct WorldInfo {
     int kx_start;                  // per-constraint scratch (contact_cap + joint_count + 2)
     int snap_start;                // TOI sweep snapshots (contact_cap entries)
     int proxy_order;               // 1: fixtures out of proxy-id order, walk them by Ctx.proxy_order
+    int pair_block;                // 1: the end-of-Solve pairs come from a block of its own (large world)
+    int pad2;
 };
 
 struct WorldDyn {
@@ -40,7 +42,7 @@ struct WorldDyn {
     int error;                     // DBOX_ERR_* of the last step (0 = ok)
     int islands;                   // islands solved in the last step
     int toi_events;                // TOI events in the last step
-    int pad;
+    int pair_total;                // pairs the block pass left for AddPair (large worlds)
     // cumulative work counters (never reset on the device; the host takes differences)
     unsigned long long acc_isl_bodies;   // bodies integrated in islands
     unsigned long long acc_isl_contacts; // contact constraints built
@@ -214,6 +216,9 @@ struct Ctx {
     unsigned* s_sapk[2];           // fixture-indexed: sweep-and-prune keys (radix-sort ping-pong)
     int* s_sapi[2];                // fixture-indexed: proxy of each sorted key (top bit: moved)
     float4* s_sapbox;              // fixture-indexed: fat AABBs in sorted order
+    int* s_sapcell;                // per world 8 * fixtures + 130 from 8 * fix_start + 130 * world: cell tables
+    const int* big_worlds;         // the worlds whose end-of-Solve pairs a block generates
+    int n_big;
     const int* proxy_order;        // fixture-indexed: world-local fixture of each proxy-id rank
     // scratch (contact-indexed)
     int* s_cstate;                 // 0 processed, 1 inactive, 2 destroyed

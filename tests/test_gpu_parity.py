@@ -353,3 +353,26 @@ def test_gear_joints_exact(oracle_lib, gpu_lib):
             for i, ow in enumerate(ows):
                 d = exact_diff(ow.export_state(), gw.export_state(i))
                 assert not d, "world %d step %d: %s" % (i, t + 1, d[:6])
+
+
+def test_large_world_block_pairs_exact(oracle_lib, gpu_lib):
+    # a world of 4,500 bodies (at least 4,096 fixtures) generates its end-of-Solve pairs on a
+    # block of its own and finishes AddPair + SolveTOI in a separate warp; a small world in the
+    # same handle keeps the one-warp path: both bit-exact against the oracle
+    from dbox_gb300 import scenes
+    oracle_lib.set_trig_mode(1)
+    rng = np.random.default_rng(12)
+    big = scenes._concat([scenes.container(90.0, 90.0), scenes.scatter(4500, 88.0, 88.0, rng)])
+    worlds = [big, scenes.pyramid(rows=10)]
+    assert len(big["fixtures"]) >= 4096
+    gw = gpu_lib.World(worlds)
+    ows = [oracle_lib.OracleWorld(s) for s in worlds]
+    for t in range(90):
+        gw.step()
+        for ow in ows:
+            ow.step()
+        if t % 30 == 29:
+            for i, ow in enumerate(ows):
+                d = exact_diff(ow.export_state(), gw.export_state(i))
+                assert not d, "world %d step %d: %s" % (i, t + 1, d[:6])
+    assert gw.export_state(0)["header"][0]["contact_count"] > 1000
