@@ -2964,13 +2964,15 @@ DG int build_schedule(const Ctx& x, const WorldInfo& wi, int nIsl, bool contacts
     tsync();
     int maxL = 0, n = 0;
     if (lane == 0) {
-        for (int is = 0; is < nIsl; ++is) {
-            int cs = x.s_isl_cstart[wi.bx_start + is], ce = x.s_isl_cstart[wi.bx_start + is + 1];
-            int js = x.s_isl_jstart[wi.bx_start + is], je = x.s_isl_jstart[wi.bx_start + is + 1];
+        // islands share no dynamic body, so the levels are the same whether each island's
+        // constraints are walked island by island or all contacts (in island order) are walked
+        // before all joints (or after, for the velocity order): no per-island loop is needed
+        {
+            const int ncT = x.s_isl_cstart[wi.bx_start + nIsl], njT = x.s_isl_jstart[wi.bx_start + nIsl];
             for (int pass = 0; pass < 2; ++pass) {
                 bool doContacts = (pass == 0) == contacts_first;
-                int s = doContacts ? cs : js, e = doContacts ? ce : je;
-                for (int t = s; t < e; ++t) {
+                int e = doContacts ? ncT : njT;
+                for (int t = 0; t < e; ++t) {
                     int item, A, B, C = -1, D = -1;
                     if (doContacts) {
                         item = x.s_isl_contact[c0 + t];
