@@ -680,6 +680,13 @@ __global__ void __launch_bounds__(kPairThreads) k_pairs_block(const __grid_const
         if ((x.bs[b].flags & kBodyIsland) == 0 || x.bs[b].type == kStaticBody) continue;
         sync_fixtures(x, b);
     }
+    // the contact pair table, rebuilt from the live contacts (hash_rebuild)
+    for (int i = tid; i < wi.hash_cap; i += nt) x.hash[wi.hash_start + i] = kHashEmpty;
+    __syncthreads();
+    for (int k = tid; k < wd.contact_count; k += nt) {
+        const dbox_contact_state& c = x.ct[wi.contact_start + k];
+        hash_insert(x, wi, pair_key(c.fixture_a, c.fixture_b));
+    }
     __syncthreads();
     const int f0 = wi.fix_start, nf = wi.fix_count;
     const int* ord = wi.proxy_order ? x.proxy_order + f0 : nullptr;
@@ -3441,18 +3448,18 @@ DG void solve_world(const Ctx& x, int w, float* sbp, bool sb_smem, float* stage_
     }
     stamp(x, w, 1);
     int nIsl = 0, nbI = 0, ncI = 0, njI = 0, maxLv = 0, maxLp = 0;
-    if (lane == 0) {
+    {
         int* statics = x.s_last + b0;
         int* isl_body = x.s_isl_body + b0;
         int* isl_contact = x.s_isl_contact + c0;
         int2* isl_pair = x.s_isl_pair + c0;
         int* body_island = x.s_body_island + b0;
-        // depth-first island search (b2world.d:959-1095)
-        for (int seed = nb - 1; seed >= 0; --seed) {
+        // depth-first island search (b2world.d:959-1095), seeds in list order (descending index)
+        auto dfs_seed = [&](int seed) {
             unsigned char fs = vbf[seed];
-            if (fs & kBfVisited) continue;
-            if ((fs & kBfAwake) == 0 || (fs & kBfActive) == 0) continue;
-            if (fs & kBfStatic) continue;
+            if (fs & kBfVisited) return;
+            if ((fs & kBfAwake) == 0 || (fs & kBfActive) == 0) return;
+            if (fs & kBfStatic) return;
             x.s_isl_bstart[bx + nIsl] = nbI;
             x.s_isl_cstart[bx + nIsl] = ncI;
             x.s_isl_jstart[bx + nIsl] = njI;
@@ -3497,11 +3504,47 @@ DG void solve_world(const Ctx& x, int w, float* sbp, bool sb_smem, float* stage_
             }
             for (int i = 0; i < nStatic; ++i) vbf[statics[i]] &= ~kBfVisited;
             ++nIsl;
+        };
+        // 32 seeds at a time: a seed with no island contact and no joint is an island of its
+        // own that no other search reaches, so when every seed that starts an island in the
+        // chunk is such a body the lanes write those islands at once; otherwise lane 0 walks
+        // the chunk seed by seed
+        for (int base = nb - 1; base >= 0; base -= kWarp) {
+            const int sd = base - lane;
+            const unsigned char fs = sd >= 0 ? vbf[sd] : (unsigned char)kBfVisited;
+            const bool elig = sd >= 0 && !(fs & kBfVisited) && (fs & kBfAwake) && (fs & kBfActive) && !(fs & kBfStatic);
+            const bool lone = elig && adj[sd] == adj[sd + 1] && (nj == 0 || x.bst[b0 + sd].jadj_count == 0);
+            const unsigned em = __ballot_sync(0xffffffffu, elig), lm = __ballot_sync(0xffffffffu, lone);
+            if (em == lm) {
+                if (lone) {
+                    const int k = __popc(lm & ((1u << lane) - 1u));
+                    x.s_isl_bstart[bx + nIsl + k] = nbI + k;
+                    x.s_isl_cstart[bx + nIsl + k] = ncI;
+                    x.s_isl_jstart[bx + nIsl + k] = njI;
+                    body_island[sd] = nIsl + k;
+                    isl_body[nbI + k] = sd;
+                    vbf[sd] = fs | kBfVisited;
+                }
+                nIsl += __popc(lm);
+                nbI += __popc(lm);
+                tsync();
+                continue;
+            }
+            tsync();
+            if (lane == 0)
+                for (int seed = base; seed > base - kWarp && seed >= 0; --seed) dfs_seed(seed);
+            nIsl = __shfl_sync(0xffffffffu, nIsl, 0);
+            nbI = __shfl_sync(0xffffffffu, nbI, 0);
+            ncI = __shfl_sync(0xffffffffu, ncI, 0);
+            njI = __shfl_sync(0xffffffffu, njI, 0);
+            tsync();
         }
-        x.s_isl_bstart[bx + nIsl] = nbI;
-        x.s_isl_cstart[bx + nIsl] = ncI;
-        x.s_isl_jstart[bx + nIsl] = njI;
-        wd.islands = nIsl;
+        if (lane == 0) {
+            x.s_isl_bstart[bx + nIsl] = nbI;
+            x.s_isl_cstart[bx + nIsl] = ncI;
+            x.s_isl_jstart[bx + nIsl] = njI;
+            wd.islands = nIsl;
+        }
     }
     nIsl = __shfl_sync(0xffffffffu, nIsl, 0);
     nbI = __shfl_sync(0xffffffffu, nbI, 0);
@@ -3923,8 +3966,10 @@ DG void solve_world(const Ctx& x, int w, float* sbp, bool sb_smem, float* stage_
         }
     tsync();
     stamp(x, w, 10);
-    hash_rebuild(x, w);
-    if (!wi.pair_block) find_new_contacts(x, w);                         // else k_pairs_block + k_finish_big
+    if (!wi.pair_block) {                                               // else k_pairs_block + k_finish_big
+        hash_rebuild(x, w);
+        find_new_contacts(x, w);
+    }
     stamp(x, w, 11);
 }
 
