@@ -25,25 +25,6 @@ const dg::MlpDev* dbox_mlp_device_view(const dbox_mlp* m, dg::MlpDev* out);
 extern "C" int dbox_launch_step_ev(const dg::Ctx* x, cudaStream_t stream, int* launches, cudaEvent_t* ev);
 extern "C" int dbox_launch_gather_transforms(int n, const dbox_body_state* bs, float* out, cudaStream_t s);
 extern "C" int dbox_launch_apply_forces(int n, dbox_body_state* bs, const float* f, cudaStream_t s);
-struct dbox_query_buffers {
-    int W;
-    const dg::WorldInfo* wi;
-    const dg::DFixture* fx;
-    const dbox_proxy_state* px;
-    const dbox_body_state* bs;
-    float4* box;
-    int* idx;
-    float4* bucket;
-    float4* group;
-    int* live;
-    unsigned* key0;
-    unsigned* key1;
-    int* sidx0;
-    int* sidx1;
-    unsigned* bitmap;
-    int bm_words;
-    int query_blocks;
-};
 extern "C" int dbox_launch_query_build(const dbox_query_buffers* b, cudaStream_t s);
 extern "C" int dbox_launch_query_aabb(const dbox_query_buffers* b, int n, const int* world, const dbox_aabb* boxes,
                                       int cap, int* counts, int* out, cudaStream_t s);

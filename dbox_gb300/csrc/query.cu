@@ -471,25 +471,6 @@ __global__ void k_raycast(QIndex q, int nq, const int* qworld, const dbox_vec2* 
 }  // namespace
 }  // namespace dg
 
-struct dbox_query_buffers {
-    int W;
-    const dg::WorldInfo* wi;
-    const dg::DFixture* fx;
-    const dbox_proxy_state* px;
-    const dbox_body_state* bs;
-    float4* box;
-    int* idx;
-    float4* bucket;
-    float4* group;
-    int* live;
-    unsigned* key0;
-    unsigned* key1;
-    int* sidx0;
-    int* sidx1;
-    unsigned* bitmap;
-    int bm_words;
-    int query_blocks;
-};
 
 static dg::QIndex qindex(const dbox_query_buffers* b) {
     dg::QIndex q;

@@ -350,3 +350,25 @@ DG void set_error(const Ctx& x, int w, int code) {
 }
 
 }  // namespace dg
+
+// Device arrays of the world-query index (query.cu), filled by the host (api.cu).
+struct dbox_query_buffers {
+    int W;
+    const dg::WorldInfo* wi;
+    const dg::DFixture* fx;
+    const dbox_proxy_state* px;
+    const dbox_body_state* bs;
+    float4* box;
+    int* idx;
+    float4* bucket;
+    float4* group;
+    int* live;
+    unsigned* key0;
+    unsigned* key1;
+    int* sidx0;
+    int* sidx1;
+    unsigned* bitmap;
+    int bm_words;
+    int query_blocks;
+};
+
