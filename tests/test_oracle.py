@@ -372,3 +372,33 @@ def test_gear_joints_hold_their_ratio(oracle_lib):
     rel = lambda i: a(i) - a(5)
     assert abs(rel(6) + 0.75 * rel(7)) < 0.02
     assert np.isfinite(st["xf"]).all()
+
+
+def test_concat_moves_gear_joint_indices():
+    # a gear joint names its joints by creation index (all revolute joints, then distance, ...,
+    # prismatic, ...); merging scenes moves those indices to the joints' new places
+    from dbox_gb300 import scenes
+    a, b = scenes.gears(), scenes.gears(seed=3)
+    m = scenes._concat([a, b])
+    na_rev, nb_rev = len(a["joints"]), len(b["joints"])
+    nrev = na_rev + nb_rev
+    kinds = scenes.JOINT_KINDS
+
+    def kind_of(scene, idx):
+        for k in kinds:
+            n = len(scene.get(k, ()))
+            if idx < n:
+                return k, idx
+            idx -= n
+        raise IndexError(idx)
+
+    for part, off_rev, off_pri, gears in ((a, 0, 0, m["gear_joints"][:len(a["gear_joints"])]),
+                                          (b, na_rev, len(a["prismatic_joints"]), m["gear_joints"][len(a["gear_joints"]):])):
+        for g_old, g_new in zip(part["gear_joints"], gears):
+            for f in ("joint1", "joint2"):
+                k, i = kind_of(part, int(g_old[f]))
+                want = off_rev + i if k == "joints" else nrev + len(m["distance_joints"]) + len(m["rope_joints"]) + \
+                    len(m["weld_joints"]) + len(m["friction_joints"]) + len(m["motor_joints"]) + \
+                    len(m["wheel_joints"]) + off_pri + i
+                assert int(g_new[f]) == want, (f, k, i)
+    assert m["gear_joints"][len(a["gear_joints"]):]["body_a"].min() >= len(a["bodies"])
