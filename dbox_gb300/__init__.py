@@ -60,6 +60,7 @@ def lib():
     L.dbox_joint_create_gear.argtypes = [vp, i32, vp, ctypes.POINTER(i32)]
     L.dbox_world_query_aabb.argtypes = [vp, i32, vp, vp, i32, vp, vp]
     L.dbox_world_get_stream.argtypes = [vp, ctypes.POINTER(vp)]
+    L.dbox_world_get_counts.argtypes = [vp, i32, ctypes.POINTER(i32), ctypes.POINTER(i32), ctypes.POINTER(i32)]
     for fn in ("dbox_body_destroy", "dbox_fixture_destroy", "dbox_joint_destroy"):
         getattr(L, fn).argtypes = [vp, i32, i32]
     L.dbox_world_dump.argtypes = [vp, i32, ctypes.c_char_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]
@@ -308,6 +309,13 @@ class World:
         _check(lib().dbox_fixture_create(self.h, world, body, abi.ptr(sd), abi.ptr(fd), ctypes.byref(out)),
                "dbox_fixture_create")
         return out.value
+
+    def counts(self, world=0):
+        """b2World.GetBodyCount / GetJointCount / GetContactCount: (bodies, joints, contacts) alive."""
+        b, j, c = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        _check(lib().dbox_world_get_counts(self.h, world, ctypes.byref(b), ctypes.byref(j), ctypes.byref(c)),
+               "dbox_world_get_counts")
+        return b.value, j.value, c.value
 
     def destroy_body(self, world, body):
         """b2World.DestroyBody: its joints, contacts (EndContact to the listener) and fixtures."""

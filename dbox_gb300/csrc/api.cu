@@ -2212,6 +2212,23 @@ int32_t dbox_world_contact_count(dbox_world* w, int32_t world, int32_t* out) {
     return DBOX_OK;
 }
 
+int32_t dbox_world_get_counts(dbox_world* w, int32_t world, int32_t* bodies, int32_t* joints, int32_t* contacts) {
+    if (!w || world < 0 || world >= (int)w->worlds.size()) return fail(DBOX_ERR_INVALID, "dbox_world_get_counts: bad world");
+    const HostWorld& hw = w->worlds[world];
+    if (bodies) {
+        int n = 0;
+        for (int b = 0; b < (int)hw.bs.size(); ++b) n += body_gone(hw, b) ? 0 : 1;
+        *bodies = n;
+    }
+    if (joints) {
+        int n = 0;
+        for (const dg::DJoint& j : hw.jt) n += j.type >= 0 ? 1 : 0;
+        *joints = n;
+    }
+    if (contacts) return dbox_world_contact_count(w, world, contacts);
+    return DBOX_OK;
+}
+
 int32_t dbox_world_export_state(dbox_world* w, int32_t world, dbox_world_header* header, dbox_body_state* bodies,
                                 dbox_proxy_state* proxies, dbox_contact_state* contacts, dbox_joint_state* joints) {
     if (!w || world < 0 || world >= (int)w->worlds.size()) return fail(DBOX_ERR_INVALID, "export: bad world");

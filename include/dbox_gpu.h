@@ -397,8 +397,13 @@ int32_t dbox_world_step_n(dbox_world* w, float dt, int32_t velocity_iterations,
  * Any pointer may be NULL; each non-NULL array holds total_bodies entries. */
 int32_t dbox_world_get_bodies(dbox_world* w, dbox_vec2* position, float* angle,
                               dbox_vec2* linear_velocity, float* angular_velocity, int32_t* awake);
+/* Body slots of world `world` (body ids run 0 .. count - 1; destroyed bodies keep their slot). */
 int32_t dbox_world_body_count(dbox_world* w, int32_t world, int32_t* out);
+/* b2World.GetContactCount (b2world.d:695-699). */
 int32_t dbox_world_contact_count(dbox_world* w, int32_t world, int32_t* out);
+/* b2World.GetBodyCount / GetJointCount / GetContactCount (b2world.d:683-699): live bodies and
+ * joints (destroyed ones not counted) and contacts of world `world`; any pointer may be NULL. */
+int32_t dbox_world_get_counts(dbox_world* w, int32_t world, int32_t* bodies, int32_t* joints, int32_t* contacts);
 
 /* Snapshot of one world (b2World.Dump b2world.d:796-855 replaced by an exact binary form).
  * Arrays are sized from the header: bodies[body_count], proxies[fixture_count],

@@ -5,7 +5,7 @@ including the EndContact events the destruction reports and the ids new proxies 
 import numpy as np
 import pytest
 
-from dbox_gb300 import abi, scenes
+from dbox_gb300 import abi, dump, scenes
 from compare import exact_diff
 
 
@@ -120,7 +120,10 @@ def test_destroy_behaviour(oracle_lib):
 def _compare(ow, gw, tag):
     d = exact_diff(ow.export_state(), gw.export_state(0))
     assert not d, (tag, d[:6])
-    assert ow.dump() == gw.dump(0), tag
+    text = ow.dump()
+    assert text == gw.dump(0), tag
+    p = dump.parse(text)                                # b2World.GetBodyCount / GetJointCount / GetContactCount
+    assert gw.counts(0) == (len(p["bodies"]), len(p["joints"]), int(ow.export_state()["header"][0]["contact_count"])), tag
 
 
 @pytest.mark.gpu
