@@ -478,6 +478,10 @@ int32_t dbox_world_step_stats(dbox_world* w, int32_t world, int32_t* islands, in
  *              the callback returning 1), in fixture order;
  *   RayCast DBOX_RAY_CLOSEST: the hit with the smallest fraction, the lower fixture index on
  *              a tie (the closest-hit callback that returns the fraction).
+ * The testbed's other callbacks (examples/demo/tests/raycast.d) map onto these: the "any hit"
+ * callback (returns 0 at its first hit) is DBOX_RAY_ALL with capacity 1, which gives the hit
+ * of the lowest fixture index and the number of hits; the "multiple hits" callback (up to N
+ * hits, returning 1) is DBOX_RAY_ALL with capacity N, the first N in fixture order.
  * counts[q] receives the number of results of query q (it may exceed capacity; results
  * beyond capacity are dropped; -1: the query names no world, or p1 == p2 for a ray, where
  * the reference asserts); results of query q start at q * capacity, and entries past
