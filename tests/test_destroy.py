@@ -178,3 +178,30 @@ def test_destroy_exact(oracle_lib, gpu_lib):
     gw.step(steps=90)
     ow.step(steps=90)
     _compare(ow, gw, "end")
+
+
+def test_chain_proxy_ids_follow_the_free_list(oracle_lib):
+    # a chain's child proxies are created and destroyed as the reference's one chain fixture:
+    # created in child order, freed in child order (b2Fixture.CreateProxies / DestroyProxies),
+    # so a new chain on freed ids gets them back last freed first
+    oracle_lib.set_trig_mode(1)
+    ow = oracle_lib.OracleWorld(scenes.ground_box())
+    model = ProxyIdModel()
+    model.create()
+    b = abi.body_defs(1)[0]
+    b["type"] = abi.STATIC
+    body = ow.create_body(b)
+    verts = np.array([(-5.0, 1.0), (-2.0, 2.0), (1.0, 1.5), (4.0, 2.5), (6.0, 1.0)], np.float32)
+    first = ow.create_chain(body, verts, loop=True)
+    ids = [model.create() for _ in range(len(verts))]
+    got = ow.export_state()["proxies"]["proxy_id"][first:first + len(verts)]
+    assert list(got) == ids
+    ow.step(steps=3)
+    ow.destroy_fixture(first + 2)                       # a child destroys its whole chain
+    for i in ids:
+        model.destroy(i)
+    st = ow.export_state()["proxies"]["proxy_id"]
+    assert (st[first:first + len(verts)] == -1).all()
+    second = ow.create_chain(body, verts[:4], loop=False)
+    want = [model.create() for _ in range(3)]
+    assert list(ow.export_state()["proxies"]["proxy_id"][second:second + 3]) == want

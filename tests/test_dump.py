@@ -263,3 +263,57 @@ def dump_bodies_only(text):
     """The body and fixture statements of a dump (joint blocks left out)."""
     i = text.find("JointDef jd;")
     return text if i < 0 else text[:text.rfind("{\n", 0, i)]
+
+
+def test_parse_hand_edited_loop_and_circle(oracle_lib):
+    # testbed-style statements the reference's Dump never writes but scenes carry:
+    # CreateLoop, `true` flags, a bare b2BodyType member, an `auto shape = new ...` circle
+    text = """
+    b2Vec2 g = b2Vec2(0.000000000000000e+00f, -1.000000000000000e+01f);
+    m_world.SetGravity(g);
+    {
+        b2BodyDef bd;
+        bodies[0] = m_world.CreateBody(&bd);
+        {
+            b2FixtureDef fd;
+            fd.friction = 6.000000238418579e-01f;
+            b2ChainShape shape;
+            b2Vec2 vs[4];
+            vs[0].Set(-5.0f, 0.0f);
+            vs[1].Set(5.0f, 0.0f);
+            vs[2].Set(5.0f, 10.0f);
+            vs[3].Set(-5.0f, 10.0f);
+            shape.CreateLoop(vs, 4);
+            fd.shape = &shape;
+            bodies[0].CreateFixture(&fd);
+        }
+    }
+    {
+        b2BodyDef bd;
+        bd.type = b2BodyType.b2_dynamicBody;
+        bd.position.Set(0.0f, 5.0f);
+        bd.bullet = true;
+        bodies[1] = m_world.CreateBody(&bd);
+        {
+            b2FixtureDef fd;
+            fd.density = 2.0f;
+            auto shape = new b2CircleShape();
+            shape.m_radius = 5.000000000000000e-01f;
+            fd.shape = shape;
+            bodies[1].CreateFixture(&fd);
+        }
+    }
+    """
+    p = dump.parse(text)
+    assert len(p["bodies"]) == 2 and p["bodies"]["type"][1] == abi.DYNAMIC and p["bodies"]["bullet"][1] == 1
+    assert p["fixtures"][0][0] == "chain" and p["fixtures"][0][5] is True
+    assert p["fixtures"][1][0] == "fixture" and p["fixtures"][1][2]["kind"] == abi.SHAPE_CIRCLE
+    oracle_lib.set_trig_mode(1)
+    ow = _empty_oracle(oracle_lib, p["gravity"])
+    dump.replay(p, ow)
+    ow.step(steps=120)
+    st = ow.export_state()
+    assert len(st["proxies"]) == 4 + 1                  # a loop of 4 vertices has 4 child edges
+    assert 0.0 < st["bodies"]["xf"][1, 1] < 1.0         # the ball rests on the loop's floor
+    t = ow.dump()
+    assert "shape.CreateChain(vs, 5);" in t and "shape.m_hasPrevVertex = bool(1);" in t
