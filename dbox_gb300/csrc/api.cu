@@ -1304,6 +1304,14 @@ int32_t dbox_body_destroy(dbox_world* w, int32_t world, int32_t body) {
     HostWorld& hw0 = w->worlds[world];
     if (body < 0 || body >= (int)hw0.bs.size() || body_gone(hw0, body))
         return fail(DBOX_ERR_INVALID, "dbox_body_destroy: no body %d", body);
+    for (const dg::DJoint& g : hw0.jt) {                                 // its joints would leave a gear dangling
+        if (g.type != dg::kGearJoint) continue;
+        for (int k : {g.joint1, g.joint2}) {
+            const dg::DJoint& j = hw0.jt[k];
+            if (j.body_a == body || j.body_b == body)
+                return fail(DBOX_ERR_INVALID, "dbox_body_destroy: body %d carries a joint of a gear joint", body);
+        }
+    }
     int rc = prepare_edit(w);
     if (rc) return rc;
     std::vector<dbox_contact_event> ev;

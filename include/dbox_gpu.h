@@ -326,7 +326,9 @@ int32_t dbox_fixture_create_chain(dbox_world* w, int32_t world, int32_t body, co
  * wakes both bodies and flags their contacts for filtering unless collideConnected.  Between
  * steps only.  Indices of other bodies, fixtures and joints do not change; a destroyed one
  * exports as an all-zero record (a proxy of id -1).  New proxies take the ids the reference's
- * tree hands out: freed leaves last in, first out, then never-used node ids. */
+ * tree hands out: freed leaves last in, first out, then never-used node ids.  A body or joint
+ * that a gear joint depends on (its two joints and their bodies) cannot be destroyed before
+ * the gear (DBOX_ERR_INVALID; the reference leaves that undefined). */
 int32_t dbox_body_destroy(dbox_world* w, int32_t world, int32_t body);
 /* b2World.CreateJoint with a b2GearJointDef (joints/b2gearjoint.d:83-168): joint1 and joint2
  * are live revolute or prismatic joints of the same world; a joint a gear uses cannot be

@@ -5773,6 +5773,11 @@ int orc_joint_create_mouse(orc_world* w, const dbox_mouse_def* def) {
 // b2World.DestroyBody / DestroyJoint, b2Body.DestroyFixture (a chain child destroys its chain)
 int orc_body_destroy(orc_world* w, int body) {
     if (body < 0 || body >= (int)w->w.bodiesByIndex.size() || !w->w.bodiesByIndex[body]) return -1;
+    const Body* b = w->w.bodiesByIndex[body];
+    for (Joint* g : w->w.jointsByIndex)                                 // a gear would keep a destroyed joint
+        if (g && g->type == kGearJoint)
+            for (const Joint* j : {g->joint1, g->joint2})
+                if (j->bodyA == b || j->bodyB == b) return -1;
     w->w.DestroyBody(w->w.bodiesByIndex[body]);
     return 0;
 }

@@ -205,3 +205,23 @@ def test_chain_proxy_ids_follow_the_free_list(oracle_lib):
     second = ow.create_chain(body, verts[:4], loop=False)
     want = [model.create() for _ in range(3)]
     assert list(ow.export_state()["proxies"]["proxy_id"][second:second + 3]) == want
+
+
+def test_gear_dependencies_block_destruction(oracle_lib):
+    # the reference leaves a gear dangling when one of its joints (or a body carrying one) is
+    # destroyed first; here that is refused until the gear is gone
+    oracle_lib.set_trig_mode(1)
+    s = scenes.gears()
+    ow = oracle_lib.OracleWorld(s)
+    ow.step(steps=10)
+    nrev, npri = len(s["joints"]), len(s["prismatic_joints"])
+    gear0 = nrev + npri                                 # gear joints are created last
+    with pytest.raises(ValueError):
+        ow.destroy_joint(0)                             # joint1 of the first gear
+    with pytest.raises(ValueError):
+        ow.destroy_body(1)                              # carries that joint
+    ow.destroy_joint(gear0)
+    ow.destroy_joint(0)
+    ow.destroy_body(1)
+    ow.step(steps=10)
+    assert np.isfinite(ow.export_state()["bodies"]["xf"]).all()
