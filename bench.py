@@ -17,8 +17,9 @@ e2e    = the same K steps (on a twin handle built from the same scenes and warme
          steps, and reads every body's (x, y, angle) back into pinned memory
          (dbox_world_get_transforms); host wall clock around the K steps.
 cpu_baseline / --impl reference: the CPU oracle (a C++ restatement of the dbox
-         step; the D reference cannot be compiled on these machines) on a bounded
-         sample of the same worlds and step window, one process per host core.
+         step; the D reference cannot be compiled on these machines) on every world
+         of the workload and the same step window, worlds spread largest first over
+         all host cores, wall clock of the whole pool.
 Under torchrun each rank runs its own 4,096-world batch (weak scaling, no
 collective on the data path); rank 0 prints the max-over-ranks timing.
 """
@@ -52,7 +53,6 @@ def parse():
     p.add_argument("--workload", default="batch", choices=["batch", "scatter", "pyramid"])
     p.add_argument("--worlds", type=int, default=4096)
     p.add_argument("--seed", type=int, default=3)
-    p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-learned", action="store_true", help="skip the learned warm-start comparison")
     p.add_argument("--no-autotune", action="store_true", help="keep the default world-to-block mapping")
@@ -67,12 +67,13 @@ def parse():
 
 def make_worlds(args, rank):
     from dbox_gb300 import scenes
+    from dbox_gb300.dist import rank_seed
     if args.workload == "batch":
-        return scenes.batch(n_worlds=args.worlds, seed=args.seed + 1000 * rank), {
+        return scenes.batch(n_worlds=args.worlds, seed=rank_seed(args.seed, rank)), {
             "workload": "batched worlds: %d worlds, bodies log-uniform [8,512], thirds pyramid/scatter/stacks"
                         % args.worlds, "worlds": args.worlds}
     if args.workload == "scatter":
-        return [scenes.scatter_world(seed=args.seed + rank)], {
+        return [scenes.scatter_world(seed=rank_seed(args.seed, rank))], {
             "workload": "single world: 16,384 mixed circles/polygons in a 200x400 m container", "worlds": 1}
     return [scenes.pyramid()], {"workload": "single world: 20-row pyramid, 210 boxes", "worlds": 1}
 
@@ -134,58 +135,95 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------ CPU oracle legs
-def _cpu_worker(task):
+def _cpu_worker(scenes_list, warmup, steps, barrier, out):
+    """One host core: build the oracle worlds of its share, step them through the warm-up,
+    wait for every core at the barrier, then time steps warmup+1 .. warmup+steps."""
     import oracle
     from dbox_gb300 import scenes
-    idx, seed, n_worlds, workload, warmup, steps = task
     oracle.set_trig_mode(0)
-    if workload == "batch":
-        allw = scenes.batch(n_worlds=n_worlds, seed=seed)
-        worlds = [allw[i] for i in idx]
-    elif workload == "scatter":
-        worlds = [scenes.scatter_world(seed=seed)]
-    else:
-        worlds = [scenes.pyramid()]
-    ows = [oracle.OracleWorld(s) for s in worlds]
+    ows = [oracle.OracleWorld(s) for s in scenes_list]
     for w in ows:
         w.step(DT, VI, PI, steps=warmup)
-    t0 = time.perf_counter()
+    barrier.wait()
+    t0 = time.monotonic()
     for w in ows:
         w.step(DT, VI, PI, steps=steps)
-    dt = time.perf_counter() - t0
-    nb = sum(scenes.dynamic_body_count(s) for s in worlds)
-    return nb * steps, dt
+    t1 = time.monotonic()
+    out.put((t0, t1, sum(scenes.dynamic_body_count(s) for s in scenes_list) * steps))
 
 
-def cpu_leg(args, seconds):
-    """Oracle step on host cores: returns (body-steps/s, cores, sample description)."""
+def _cpu_cost_worker(task):
+    """Calibration (untimed): per world, the time of steps warmup+1 and warmup+2 on one core."""
+    import oracle
+    scenes_list, warmup = task
+    oracle.set_trig_mode(0)
+    out = []
+    for s in scenes_list:
+        w = oracle.OracleWorld(s)
+        w.step(DT, VI, PI, steps=warmup)
+        t0 = time.perf_counter()
+        w.step(DT, VI, PI, steps=2)
+        out.append(time.perf_counter() - t0)
+    return out
+
+
+def lpt_shares(costs, bins):
+    """Longest-processing-time assignment: items by cost, largest first, each to the least
+    loaded bin; returns the item indices of each non-empty bin."""
+    order = sorted(range(len(costs)), key=lambda i: (-costs[i], i))
+    load = [0.0] * bins
+    out = [[] for _ in range(bins)]
+    for i in order:
+        k = min(range(bins), key=lambda b: (load[b], b))
+        out[k].append(i)
+        load[k] += costs[i]
+    return [o for o in out if o]
+
+
+def cpu_leg(args, worlds=None):
+    """The oracle step (dbox's float32 step restated in C++, host libm trig) on the host cores,
+    on every world of the workload and the same step window as the GPU leg: worlds spread over
+    all cores largest first (one world list per core), each core warms its worlds up, a barrier,
+    then the wall clock of the whole pool's timed steps.  Returns (body-steps/s, cores, sample)."""
     import oracle
     from dbox_gb300 import scenes
     oracle.build()
-    cores = min(os.cpu_count() or 1, 64)
-    if args.workload == "batch":
-        sample_worlds = min(args.worlds, max(cores * 2, 32))
-        # pick a probe sample size from a short calibration run on one core
-        probe = _cpu_worker((list(range(min(8, sample_worlds))), args.seed, args.worlds, "batch", args.warmup, 4))
-        rate1 = probe[0] / max(probe[1], 1e-6)
-        per_world_steps = max(4, min(args.steps, int(seconds * rate1 * cores / (sample_worlds * 120.0))))
-        idx = list(range(sample_worlds))
-        chunks = [idx[i::cores] for i in range(cores) if idx[i::cores]]
-        tasks = [(c, args.seed, args.worlds, "batch", args.warmup, per_world_steps) for c in chunks]
-        ctx = mp.get_context("spawn")
-        t0 = time.perf_counter()
-        with ctx.Pool(len(tasks)) as pool:
-            res = pool.map(_cpu_worker, tasks)
-        wall = time.perf_counter() - t0
-        work = sum(r[0] for r in res)
-        slowest = max(r[1] for r in res)
-        rate = work / slowest
-        sample = ("%d of %d worlds, steps %d..%d, %d processes (one world list per core), oracle with host libm trig"
-                  % (sample_worlds, args.worlds, args.warmup + 1, args.warmup + per_world_steps, len(tasks)))
-        return rate, len(tasks), sample
-    steps = max(2, min(args.steps, 10))
-    work, dt = _cpu_worker(([0], args.seed, 1, args.workload, args.warmup, steps))
-    return work / dt, 1, "1 world, steps %d..%d, one core" % (args.warmup + 1, args.warmup + steps)
+    if worlds is None:
+        worlds, _ = make_worlds(args, 0)
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+    ctx = mp.get_context("spawn")
+    # per-world cost from an untimed calibration pass over all worlds (the cost per body differs
+    # between pyramids, stacks and scatter worlds), then a largest-first assignment
+    nb = min(cores, len(worlds))
+    chunks = [list(range(i, len(worlds), 4 * nb)) for i in range(4 * nb)]
+    chunks = [c for c in chunks if c]
+    with ctx.Pool(nb) as pool:
+        timed = pool.map(_cpu_cost_worker, [([worlds[i] for i in c], args.warmup) for c in chunks])
+    costs = [0.0] * len(worlds)
+    for c, t in zip(chunks, timed):
+        for i, v in zip(c, t):
+            costs[i] = v
+    shares = lpt_shares(costs, nb)
+    barrier = ctx.Barrier(len(shares))
+    out = ctx.Queue()
+    procs = [ctx.Process(target=_cpu_worker, args=([worlds[i] for i in sh], args.warmup, args.steps, barrier, out))
+             for sh in shares]
+    for p in procs:
+        p.start()
+    res = [out.get() for _ in procs]
+    for p in procs:
+        p.join()
+        if p.exitcode != 0:
+            raise RuntimeError("CPU oracle worker failed (exit code %s)" % p.exitcode)
+    wall = max(r[1] for r in res) - min(r[0] for r in res)
+    work = sum(r[2] for r in res)
+    busy = [r[1] - r[0] for r in res]
+    sample = ("%d of %d worlds, steps %d..%d, %d processes (worlds spread costliest first over the cores, "
+              "costs from an untimed calibration pass), "
+              "wall clock of the pool; per-process busy %.2f-%.2f s; oracle with host libm trig"
+              % (len(worlds), len(worlds), args.warmup + 1, args.warmup + args.steps, len(shares), min(busy),
+                 max(busy)))
+    return work / wall, len(shares), sample
 
 
 # ------------------------------------------------------------------ GPU leg
@@ -199,9 +237,30 @@ def algorithmic_solve_bytes(c):
     return 96 * c["isl_bodies"] + (244 + 156 + 16) * c["isl_contacts"] + 220 * c["vsolve"] + 136 * c["psolve"]
 
 
+def solver_chain(w):
+    """Cycles per Gauss-Seidel level of the deepest world, from one profiled step (clock64
+    stamps at the solve kernel's phase boundaries): the velocity sweeps' cycles over (levels x
+    velocity iterations), the position sweeps' over (levels x position iterations, the most
+    that can run before the early exit)."""
+    w.set_phase_profile(True)
+    w.step(DT, VI, PI)
+    p = w.phase_profile().astype(np.int64)
+    w.set_phase_profile(False)
+    span = p[:, 11] - p[:, 0]
+    k = int(np.argmax(span))
+    lv = int(p[k, 12])
+    if lv <= 0:
+        return None
+    return {"world": k, "bodies": int(p[k, 14]), "contacts": int(p[k, 13]), "levels": lv,
+            "solve_cycles": int(span[k]),
+            "velocity_cycles_per_level": float(p[k, 6] - p[k, 5]) / (lv * VI),
+            "position_cycles_per_level": float(p[k, 8] - p[k, 7]) / (lv * PI)}
+
+
 def gpu_leg(args, rank, world_size):
     import torch
     import dbox_gb300
+    from dbox_gb300.dist import max_over_ranks
     dbox_gb300.build()
     torch.cuda.set_device(0 if world_size == 1 else int(os.environ.get("LOCAL_RANK", rank)))
     worlds, cfg = make_worlds(args, rank)
@@ -245,10 +304,7 @@ def gpu_leg(args, rank, world_size):
     clk = clocks.stop()
     c1 = w.counters()
     cdiff = {k: c1[k] - c0[k] for k in c1}
-    t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
-    if world_size > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    total_ms_max = float(t.item())
+    total_ms_max = max_over_ranks(total_ms, "cuda")
     value = nbody_dyn * args.steps * world_size / (total_ms_max / 1e3)
     launches = w.last_launches() * args.steps
     # end to end through the C ABI with pinned host buffers
@@ -263,21 +319,13 @@ def gpu_leg(args, rank, world_size):
         we.step(DT, VI, PI)
         we.get_transforms(xya)
     e2e_s = time.perf_counter() - t0
-    te = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
-    if world_size > 1:
-        torch.distributed.all_reduce(te, op=torch.distributed.ReduceOp.MAX)
-    e2e = nbody_dyn * args.steps * world_size / float(te.item())
+    e2e = nbody_dyn * args.steps * world_size / max_over_ranks(e2e_s, "cuda")
     assert np.isfinite(xya).all()
     solve_bytes = algorithmic_solve_bytes(cdiff) / args.steps
     solve_ms = phase_ms[1] / args.steps          # the fused solve + SolveTOI kernel
     achieved = solve_bytes / (solve_ms / 1e3) / 1e9
     hbm = peaks.get("hbm_gbs")
-    traffic = None
-    prof = os.path.join(ROOT, "profiles", "k_solve_toi_batch4096.md")
-    if args.workload == "batch" and args.worlds == 4096 and os.path.exists(prof):
-        for line in open(prof):
-            if line.startswith("traffic_bytes_per_launch:"):
-                traffic = int(line.split(":")[1])
+    chain = solver_chain(w)
     out = {
         "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": world_size, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms_max / args.steps, "higher_is_better": True,
@@ -293,12 +341,20 @@ def gpu_leg(args, rank, world_size):
         "gpu_launches": launches,
         "phases_ms_per_step": {"collide": phase_ms[0] / args.steps, "solve_and_toi": solve_ms},
         "work_per_step": {k: v / args.steps for k, v in cdiff.items()},
-        "roofline": {"bound": "hbm", "kernel": "k_solve_toi", "achieved": achieved,
+        # The fused solve + SolveTOI kernel is bound by the dependent Gauss-Seidel chain of the
+        # deepest worlds (levels in sequence, each level a few hundred cycles of dependent
+        # arithmetic), not by HBM: the bandwidth fraction below is what that chain leaves.
+        "roofline": {"bound": "latency", "kernel": "k_solve_toi", "achieved": achieved,
                      "peak": hbm, "unit": "GB/s", "frac": (achieved / hbm) if hbm else None,
                      "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if hbm else "fallback 6800",
-                     "algorithmic_bytes_per_launch": solve_bytes, "traffic": traffic,
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch of this "
-                                       "workload (profiles/k_solve_toi_batch4096.md)" if traffic else None},
+                     "algorithmic_bytes_per_launch": solve_bytes,
+                     "algorithmic_bytes_cover": "the island solve only (bodies, constraint build, velocity and "
+                                                "position solves, impulse store); SolveTOI and Collide not counted",
+                     "solve_share_of_step": solve_ms / (total_ms_max / args.steps),
+                     "traffic": None,
+                     "traffic_note": "DRAM bytes come from a separate ncu capture of this kernel, not from the "
+                                     "timed run",
+                     "critical_chain": chain},
         "clocks": clk,
     }
     if out["roofline"]["peak"] is None:
@@ -307,7 +363,7 @@ def gpu_leg(args, rank, world_size):
     if world_size == 1 and not args.no_queries:
         out["world_queries"] = queries_leg(args, w, worlds, out["roofline"]["peak"])
     w.close()
-    return out
+    return out, worlds
 
 
 def _query_inputs(rng, n, worlds, xy):
@@ -494,15 +550,14 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        rate, cores, sample = cpu_leg(args, args.cpu_seconds)
-        _, cfg = make_worlds(args, 0) if args.workload != "batch" else (None, {
-            "workload": "batched worlds: %d worlds, bodies log-uniform [8,512], thirds pyramid/scatter/stacks"
-                        % args.worlds, "worlds": args.worlds})
+        worlds, cfg = make_worlds(args, 0)
+        rate, cores, sample = cpu_leg(args, worlds)
         out = {"metric": METRIC, "value": rate, "unit": "body-steps/s", "n_gpus": world_size, "steps": args.steps,
                "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                "dtype": "f32", "data": "synthetic seeded scenes (numpy PCG64 seed %d)" % args.seed,
                "impl": "reference",
-               "config": dict(cfg, dt=DT, velocity_iterations=VI, position_iterations=PI),
+               "config": dict(cfg, dt=DT, velocity_iterations=VI, position_iterations=PI,
+                              dynamic_bodies=dynamic_bodies(worlds)),
                "cpu_baseline": {"value": rate, "unit": "body-steps/s", "cores": cores, "kind": "port",
                                 "sample": sample},
                "e2e": {"value": rate, "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -511,12 +566,12 @@ def main():
     if world_size > 1:
         import torch
         torch.distributed.init_process_group("nccl")
-    out = gpu_leg(args, rank, world_size)
+    out, worlds = gpu_leg(args, rank, world_size)
     if rank == 0:
         if world_size == 1 and not args.no_learned:
             out["learned_warmstart"] = learned_leg(args)
         if world_size == 1 and not args.no_cpu:
-            rate, cores, sample = cpu_leg(args, args.cpu_seconds)
+            rate, cores, sample = cpu_leg(args, worlds)
             out["cpu_baseline"] = {"value": rate, "unit": "body-steps/s", "cores": cores, "kind": "port",
                                    "sample": sample}
         print(json.dumps(out), flush=True)

@@ -1304,8 +1304,12 @@ int32_t dbox_body_destroy(dbox_world* w, int32_t world, int32_t body) {
     HostWorld& hw0 = w->worlds[world];
     if (body < 0 || body >= (int)hw0.bs.size() || body_gone(hw0, body))
         return fail(DBOX_ERR_INVALID, "dbox_body_destroy: no body %d", body);
-    for (const dg::DJoint& g : hw0.jt) {                                 // its joints would leave a gear dangling
-        if (g.type != dg::kGearJoint) continue;
+    // b2World.DestroyBody destroys the body's joints newest first (b2world.d:115-131), so a
+    // gear whose edge bodies (joint1's and joint2's B bodies) include this one goes before its
+    // joints; only a body that carries a gear's joint but none of its edges would leave the
+    // gear holding a destroyed joint
+    for (const dg::DJoint& g : hw0.jt) {
+        if (g.type != dg::kGearJoint || g.body_a == body || g.body_b == body) continue;
         for (int k : {g.joint1, g.joint2}) {
             const dg::DJoint& j = hw0.jt[k];
             if (j.body_a == body || j.body_b == body)

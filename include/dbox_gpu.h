@@ -326,9 +326,11 @@ int32_t dbox_fixture_create_chain(dbox_world* w, int32_t world, int32_t body, co
  * wakes both bodies and flags their contacts for filtering unless collideConnected.  Between
  * steps only.  Indices of other bodies, fixtures and joints do not change; a destroyed one
  * exports as an all-zero record (a proxy of id -1).  New proxies take the ids the reference's
- * tree hands out: freed leaves last in, first out, then never-used node ids.  A body or joint
- * that a gear joint depends on (its two joints and their bodies) cannot be destroyed before
- * the gear (DBOX_ERR_INVALID; the reference leaves that undefined). */
+ * tree hands out: freed leaves last in, first out, then never-used node ids.  Destroying one
+ * of a gear joint's own bodies (its joint1's or joint2's body B) destroys the gear first, as the
+ * reference's newest-first joint walk does.  A joint a gear uses, or a body that carries such a
+ * joint but is neither of the gear's own bodies, cannot be destroyed before the gear
+ * (DBOX_ERR_INVALID): the reference would leave the gear holding a destroyed joint. */
 int32_t dbox_body_destroy(dbox_world* w, int32_t world, int32_t body);
 /* b2World.CreateJoint with a b2GearJointDef (joints/b2gearjoint.d:83-168): joint1 and joint2
  * are live revolute or prismatic joints of the same world; a joint a gear uses cannot be
@@ -479,7 +481,12 @@ int32_t dbox_world_step_stats(dbox_world* w, int32_t world, int32_t* islands, in
  *   RayCast DBOX_RAY_ALL: every fixture the ray hits (b2Fixture.RayCast with maxFraction 1,
  *              the callback returning 1), in fixture order;
  *   RayCast DBOX_RAY_CLOSEST: the hit with the smallest fraction, the lower fixture index on
- *              a tie (the closest-hit callback that returns the fraction).
+ *              a tie (the closest-hit callback that returns the fraction).  The tie rule
+ *              departs from the reference on purpose: there the clipping callback keeps the
+ *              last of several equal-fraction hits in tree-walk order (b2PolygonShape.RayCast
+ *              accepts lower == maxFraction), which depends on the tree's shape; this library
+ *              keeps the proxy ids and fat AABBs exact but not the tree, so it breaks ties by
+ *              fixture index (rays along a shared edge of touching boxes can differ).
  * The testbed's other callbacks (examples/demo/tests/raycast.d) map onto these: the "any hit"
  * callback (returns 0 at its first hit) is DBOX_RAY_ALL with capacity 1, which gives the hit
  * of the lowest fixture index and the number of hits; the "multiple hits" callback (up to N

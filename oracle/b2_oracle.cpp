@@ -5774,8 +5774,10 @@ int orc_joint_create_mouse(orc_world* w, const dbox_mouse_def* def) {
 int orc_body_destroy(orc_world* w, int body) {
     if (body < 0 || body >= (int)w->w.bodiesByIndex.size() || !w->w.bodiesByIndex[body]) return -1;
     const Body* b = w->w.bodiesByIndex[body];
-    for (Joint* g : w->w.jointsByIndex)                                 // a gear would keep a destroyed joint
-        if (g && g->type == kGearJoint)
+    // joints go newest first (b2world.d:115-131): a gear on this body goes before its joints;
+    // a body carrying a gear's joint but neither of the gear's bodies would leave it dangling
+    for (Joint* g : w->w.jointsByIndex)
+        if (g && g->type == kGearJoint && g->bodyA != b && g->bodyB != b)
             for (const Joint* j : {g->joint1, g->joint2})
                 if (j->bodyA == b || j->bodyB == b) return -1;
     w->w.DestroyBody(w->w.bodiesByIndex[body]);

@@ -2,7 +2,7 @@
 b2World.Dump-style text (examples/demo/tests/dumpshell.d, a dumped scene of Box2D issue 304),
 read as text through dbox_gb300.dump.parse and stored as plain numbers.
 
-Run from the repository root:  python tests/golden/make_dumpshell_scene.py [path/to/dumpshell.d]
+Run from the repository root:  python tests/golden/make_dumpshell_scene.py <dbox checkout>/examples/demo/tests/dumpshell.d
 """
 import json
 import os
@@ -15,7 +15,9 @@ from dbox_gb300 import dump  # noqa: E402
 
 
 def main():
-    src = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/examples/demo/tests/dumpshell.d"
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_dumpshell_scene.py <dbox checkout>/examples/demo/tests/dumpshell.d")
+    src = sys.argv[1]
     p = dump.parse(open(src).read())
     out = {"source": "examples/demo/tests/dumpshell.d (dbox)", "gravity": list(p["gravity"]),
            "bodies": [{k: (v.tolist() if hasattr(v, "tolist") else v) for k, v in zip(b.dtype.names, b.tolist())}

@@ -208,20 +208,48 @@ def test_chain_proxy_ids_follow_the_free_list(oracle_lib):
 
 
 def test_gear_dependencies_block_destruction(oracle_lib):
-    # the reference leaves a gear dangling when one of its joints (or a body carrying one) is
-    # destroyed first; here that is refused until the gear is gone
+    # the reference leaves a gear dangling when one of its joints, or a body that carries one
+    # of its joints but is neither of the gear's own bodies (joint1's and joint2's B bodies),
+    # is destroyed first; here that is refused until the gear is gone.  Destroying one of the
+    # gear's own bodies is well defined (its joints go newest first, the gear before them).
     oracle_lib.set_trig_mode(1)
     s = scenes.gears()
     ow = oracle_lib.OracleWorld(s)
     ow.step(steps=10)
     nrev, npri = len(s["joints"]), len(s["prismatic_joints"])
-    gear0 = nrev + npri                                 # gear joints are created last
+    gear0, gear2 = nrev + npri, nrev + npri + 2         # gear joints are created last
     with pytest.raises(ValueError):
         ow.destroy_joint(0)                             # joint1 of the first gear
     with pytest.raises(ValueError):
-        ow.destroy_body(1)                              # carries that joint
-    ow.destroy_joint(gear0)
-    ow.destroy_joint(0)
-    ow.destroy_body(1)
+        ow.destroy_body(0)                              # the ground: the A body of gear 0's joints
+    with pytest.raises(ValueError):
+        ow.destroy_body(5)                              # the arm: the A body of gear 2's joints
+    ow.destroy_body(1)                                  # gear 0's body A: the gear goes first
+    assert not np.frombuffer(ow.export_state()["joints"][gear0].tobytes(), np.uint8).any()
+    ow.destroy_joint(gear2)
+    ow.destroy_body(5)
     ow.step(steps=10)
     assert np.isfinite(ow.export_state()["bodies"]["xf"]).all()
+
+
+@pytest.mark.gpu
+def test_gear_body_destruction_exact(oracle_lib, gpu_lib):
+    # destroying a gear's own body takes the gear with it, in the library as in the oracle;
+    # a body that would leave a gear dangling is refused by both
+    oracle_lib.set_trig_mode(1)
+    s = scenes.gears()
+    ow = oracle_lib.OracleWorld(s)
+    gw = gpu_lib.World([s])
+    ow.step(steps=20)
+    gw.step(steps=20)
+    with pytest.raises(gpu_lib.DboxError):
+        gw.destroy_body(0, 0)
+    with pytest.raises(ValueError):
+        ow.destroy_body(0)
+    for body in (1, 7):                                 # gear 0's body A, gear 2's body B
+        ow.destroy_body(body)
+        gw.destroy_body(0, body)
+        _compare(ow, gw, "after destroying body %d" % body)
+    gw.step(steps=40)
+    ow.step(steps=40)
+    _compare(ow, gw, "40 steps later")
