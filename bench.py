@@ -1,6 +1,6 @@
 """Benchmark: body-steps/s of b2World.Step on one GB300 (plain solver, batched worlds).
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload batch|scatter|pyramid]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload batch|scatter|pyramid|stress]
 
 Workload (default "batch"): 4,096 independent worlds in one handle, body counts
 log-uniform in [8, 512], one third each pyramid / scatter in a 40 m container /
@@ -50,7 +50,7 @@ def parse():
     p.add_argument("--steps", type=int, default=60)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--workload", default="batch", choices=["batch", "scatter", "pyramid"])
+    p.add_argument("--workload", default="batch", choices=["batch", "scatter", "pyramid", "stress"])
     p.add_argument("--worlds", type=int, default=4096)
     p.add_argument("--seed", type=int, default=3)
     p.add_argument("--no-cpu", action="store_true")
@@ -75,6 +75,10 @@ def make_worlds(args, rank):
     if args.workload == "scatter":
         return [scenes.scatter_world(seed=rank_seed(args.seed, rank))], {
             "workload": "single world: 16,384 mixed circles/polygons in a 200x400 m container", "worlds": 1}
+    if args.workload == "stress":
+        return [scenes.stress(seed=rank_seed(args.seed, rank))], {
+            "workload": "single world: 64 container piles x 2,048 mixed circles/polygons + 256 revolute chains "
+                        "x 32 links", "worlds": 1}
     return [scenes.pyramid()], {"workload": "single world: 20-row pyramid, 210 boxes", "worlds": 1}
 
 
@@ -153,16 +157,17 @@ def _cpu_worker(scenes_list, warmup, steps, barrier, out):
 
 
 def _cpu_cost_worker(task):
-    """Calibration (untimed): per world, the time of steps warmup+1 and warmup+2 on one core."""
+    """Calibration (untimed): per world, the time of the timed window (steps warmup+1 ..
+    warmup+steps) on one core."""
     import oracle
-    scenes_list, warmup = task
+    scenes_list, warmup, steps = task
     oracle.set_trig_mode(0)
     out = []
     for s in scenes_list:
         w = oracle.OracleWorld(s)
         w.step(DT, VI, PI, steps=warmup)
         t0 = time.perf_counter()
-        w.step(DT, VI, PI, steps=2)
+        w.step(DT, VI, PI, steps=steps)
         out.append(time.perf_counter() - t0)
     return out
 
@@ -198,7 +203,7 @@ def cpu_leg(args, worlds=None):
     chunks = [list(range(i, len(worlds), 4 * nb)) for i in range(4 * nb)]
     chunks = [c for c in chunks if c]
     with ctx.Pool(nb) as pool:
-        timed = pool.map(_cpu_cost_worker, [([worlds[i] for i in c], args.warmup) for c in chunks])
+        timed = pool.map(_cpu_cost_worker, [([worlds[i] for i in c], args.warmup, args.steps) for c in chunks])
     costs = [0.0] * len(worlds)
     for c, t in zip(chunks, timed):
         for i, v in zip(c, t):
@@ -518,7 +523,33 @@ def learned_leg(args):
                       "residual_max": float(np.mean(mx)), "penetration_max_m": float(np.max(pen)),
                       "body_steps_per_s": nd * 30 / (tot_ms / 1e3)}
         w.close()
+    # upper bound of any learned start: new points start from the impulses a 50-iteration solve
+    # of the same step converged to (a perfect prediction), persistent points keep Box2D's
+    # warm start; each step a twin handle copies the state, takes the 50-iteration step first
+    for label, vi in (("perfect_5", 5), ("perfect_4", 4)):
+        w = dbox_gb300.World(eval_worlds)
+        src = dbox_gb300.World(eval_worlds)
+        w.step(DT, VI, PI, steps=100, graph=True)
+        src.step(DT, VI, PI)
+        w.set_warmstart(3)
+        w.set_start_source(src)
+        w.set_measure(True)
+        rms, mx, pen = [], [], []
+        for _ in range(30):
+            src.copy_state_from(w)
+            src.step(DT, 50, PI)
+            w.step(DT, vi, PI)
+            q = w.quality()
+            rms.append(float(np.sqrt(q[:, 0].sum() / max(q[:, 2].sum(), 1.0))))
+            mx.append(float(q[:, 1].max()))
+            pen.append(float(-q[:, 3].min()))
+        res[label] = {"velocity_iterations": vi, "residual_rms": float(np.mean(rms)),
+                      "residual_max": float(np.mean(mx)), "penetration_max_m": float(np.max(pen)),
+                      "start": "new points from the converged impulses of a 50-iteration solve of the same step"}
+        w.close()
+        src.close()
     p8, l5 = res["plain_8"], res["learned_5"]
+    u5 = res["perfect_5"]
     return {
         "config": "%d scatter worlds x 256 bodies (40 m containers), dt 1/60, %d position iterations; "
                   "samples from %d plain steps, evaluation on new-seed worlds after 100 steps, 30 steps"
@@ -529,6 +560,8 @@ def learned_leg(args):
         "speedup_learned_5_vs_plain_8": l5["body_steps_per_s"] / p8["body_steps_per_s"],
         "learned_5_reaches_plain_8_residual": bool(l5["residual_rms"] <= p8["residual_rms"] and
                                                    l5["residual_max"] <= p8["residual_max"]),
+        "perfect_start_5_reaches_plain_8_residual": bool(u5["residual_rms"] <= p8["residual_rms"] and
+                                                         u5["residual_max"] <= p8["residual_max"]),
     }
 
 

@@ -22,7 +22,11 @@ _lib = None
 
 
 class DboxError(RuntimeError):
-    pass
+    """A failed C-ABI call; `code` is its DBOX_ERR_* status."""
+
+    def __init__(self, msg, code=None):
+        super().__init__(msg)
+        self.code = code
 
 
 def build(force=False):
@@ -103,11 +107,18 @@ def lib():
     L.dbox_mlp_train_world.argtypes = [vp, vp, i32, i32, f32, u64, vp]
     L.dbox_mlp_forward.argtypes = [vp, i32, vp, vp]
     L.dbox_world_set_warmstart.argtypes = [vp, i32, vp, i32]
+    L.dbox_world_set_start_source.argtypes = [vp, vp]
+    L.dbox_world_copy_state.argtypes = [vp, vp]
     L.dbox_world_sample_count.argtypes = [vp, ctypes.POINTER(i32)]
     L.dbox_world_get_samples.argtypes = [vp, i32, i32, vp]
     L.dbox_world_clear_samples.argtypes = [vp]
     L.dbox_world_set_measure.argtypes = [vp, i32]
+    L.dbox_world_set_wait_limit.argtypes = [vp, i32]
     L.dbox_world_set_listener.argtypes = [vp, vp, vp]
+    L.dbox_world_set_presolve.argtypes = [vp, vp, vp]
+    L.dbox_fixture_set_filter.argtypes = [vp, i32, i32, ctypes.c_uint16, ctypes.c_uint16, ctypes.c_int16]
+    L.dbox_fixture_set_filter_class.argtypes = [vp, i32, i32, i32]
+    L.dbox_world_set_contact_filter.argtypes = [vp, i32, vp, i32]
     L.dbox_world_set_mapping.argtypes = [vp, i32, i32]
     L.dbox_world_set_mapping_isolated.argtypes = [vp, i32, i32, i32]
     L.dbox_world_autotune.argtypes = [vp, f32, i32, i32, i32, vp]
@@ -122,7 +133,7 @@ def lib():
 def _check(rc, what):
     if rc != 0:
         msg = lib().dbox_last_error().decode(errors="replace")
-        raise DboxError("%s failed: %s (%s)" % (what, abi.ERRORS.get(rc, rc), msg))
+        raise DboxError("%s failed: %s (%s)" % (what, abi.ERRORS.get(rc, rc), msg), rc)
 
 
 def collide_manifolds(shapes_a, xfs_a, shapes_b, xfs_b):
@@ -437,10 +448,20 @@ class World:
         return dict(zip(keys, (int(v) for v in c)))
 
     def set_warmstart(self, mode, model=None, sample_capacity=0):
-        """0 plain (the reference step), 1 plain + log training samples, 2 learned start with model."""
+        """0 plain (the reference step), 1 plain + log training samples, 2 learned start with model,
+        3 given start (see set_start_source)."""
         self._model = model                     # the library keeps a pointer: hold a reference
         _check(lib().dbox_world_set_warmstart(self.h, mode, model.h if model is not None else None, sample_capacity),
                "dbox_world_set_warmstart")
+
+    def set_start_source(self, src):
+        """Warm-start mode 3: new points start from src's impulses at the same contact slot."""
+        self._start_src = src
+        _check(lib().dbox_world_set_start_source(self.h, src.h), "dbox_world_set_start_source")
+
+    def copy_state_from(self, src):
+        """Exact device-to-device copy of src's simulation state (same worlds, same layout)."""
+        _check(lib().dbox_world_copy_state(self.h, src.h), "dbox_world_copy_state")
 
     def sample_count(self):
         n = ctypes.c_int32()
@@ -475,6 +496,43 @@ class World:
         self._listener = World._EVENT_FN(tramp)
         _check(lib().dbox_world_set_listener(self.h, ctypes.cast(self._listener, ctypes.c_void_p), None),
                "dbox_world_set_listener")
+
+    def set_filter(self, world, fixture, category_bits=0x0001, mask_bits=0xFFFF, group_index=0):
+        """b2Fixture.SetFilterData (and Refilter)."""
+        _check(lib().dbox_fixture_set_filter(self.h, world, fixture, category_bits, mask_bits, group_index),
+               "dbox_fixture_set_filter")
+
+    def set_filter_class(self, world, fixture, cls):
+        """The fixture's class for a table contact filter (and Refilter)."""
+        _check(lib().dbox_fixture_set_filter_class(self.h, world, fixture, cls), "dbox_fixture_set_filter_class")
+
+    def set_contact_filter(self, world, table=None, with_default=True):
+        """b2World.SetContactFilter with a class table: table (64,) uint64, bit b of row a lets
+        classes a and b collide; None restores the default filter."""
+        t = None if table is None else np.ascontiguousarray(table, np.uint64)
+        _check(lib().dbox_world_set_contact_filter(self.h, world, abi.ptr(t) if t is not None else None,
+                                                   1 if with_default else 0), "dbox_world_set_contact_filter")
+
+    _PRESOLVE_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p)
+
+    def set_presolve(self, fn):
+        """b2ContactListener.PreSolve through the step's PreSolve window: fn(records) is called
+        inside each step, after Collide, with the step's PreSolve calls (abi.PRESOLVE_CONTACT,
+        world by world in reference order); it may change "enabled", "friction", "restitution"
+        and "tangent_speed" in place.  None removes it."""
+        if fn is None:
+            self._presolve = None
+            _check(lib().dbox_world_set_presolve(self.h, None, None), "dbox_world_set_presolve")
+            return
+
+        def tramp(ptr, count, user):
+            buf = (ctypes.c_char * (count * abi.PRESOLVE_CONTACT.itemsize)).from_address(ptr)
+            recs = np.frombuffer(buf, abi.PRESOLVE_CONTACT)        # a view: edits go straight back
+            fn(recs)
+
+        self._presolve = World._PRESOLVE_FN(tramp)
+        _check(lib().dbox_world_set_presolve(self.h, ctypes.cast(self._presolve, ctypes.c_void_p), None),
+               "dbox_world_set_presolve")
 
     def set_mapping(self, warps_per_block=4, body_budget=0, isolate=0):
         _check(lib().dbox_world_set_mapping_isolated(self.h, warps_per_block, body_budget, isolate),
@@ -521,6 +579,10 @@ class World:
         _check(lib().dbox_world_autotune(self.h, ctypes.c_float(dt), vel_iters, pos_iters, steps, abi.ptr(out)),
                "dbox_world_autotune")
         return tuple(int(v) for v in out)
+
+    def set_wait_limit(self, polls=1 << 20):
+        """Polls a bounded device wait may take before the step reports DBOX_ERR_TIMEOUT."""
+        _check(lib().dbox_world_set_wait_limit(self.h, polls), "dbox_world_set_wait_limit")
 
     def set_measure(self, on=True):
         _check(lib().dbox_world_set_measure(self.h, 1 if on else 0), "dbox_world_set_measure")

@@ -135,6 +135,12 @@ CONTACT_EVENT = np.dtype([
 assert CONTACT_EVENT.itemsize == 36
 EVENT_BEGIN, EVENT_END, EVENT_PRESOLVE, EVENT_POSTSOLVE = 1, 2, 3, 4   # DBOX_EVENT_*
 
+PRESOLVE_CONTACT = np.dtype([
+    ("world", "<i4"), ("enabled", "<i4"), ("friction", "<f4"), ("restitution", "<f4"), ("tangent_speed", "<f4"),
+    ("contact", CONTACT_STATE),
+])
+assert PRESOLVE_CONTACT.itemsize == 116
+
 PROFILE = np.dtype([(n, "<f4") for n in (
     "step", "collide", "solve", "solve_init", "solve_velocity", "solve_position", "broadphase", "solve_toi")])
 
@@ -148,6 +154,7 @@ CONTACT_ISLAND, CONTACT_TOUCHING, CONTACT_ENABLED, CONTACT_FILTER, CONTACT_BULLE
 
 ERRORS = {0: "ok", -1: "invalid", -2: "locked", -3: "capacity", -4: "timeout", -5: "nan", -6: "cuda",
           -7: "unsupported"}
+ERR_INVALID, ERR_LOCKED, ERR_CAPACITY, ERR_TIMEOUT, ERR_NAN, ERR_CUDA, ERR_UNSUPPORTED = -1, -2, -3, -4, -5, -6, -7
 
 
 def body_defs(n):

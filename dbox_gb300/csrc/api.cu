@@ -12,6 +12,7 @@
 #include <stdio.h>
 #include <stdarg.h>
 #include <string>
+#include <unordered_map>
 #include <vector>
 #include <algorithm>
 #include <mutex>
@@ -23,6 +24,8 @@ extern "C" int dbox_launch_step(const dg::Ctx* x, cudaStream_t stream, int* laun
 extern "C" const void* dbox_solve_kernel();
 const dg::MlpDev* dbox_mlp_device_view(const dbox_mlp* m, dg::MlpDev* out);
 extern "C" int dbox_launch_step_ev(const dg::Ctx* x, cudaStream_t stream, int* launches, cudaEvent_t* ev);
+extern "C" int dbox_launch_collide(const dg::Ctx* x, cudaStream_t stream);
+extern "C" int dbox_launch_solve(const dg::Ctx* x, cudaStream_t stream, int* launches);
 extern "C" int dbox_launch_gather_transforms(int n, const dbox_body_state* bs, float* out, cudaStream_t s);
 extern "C" int dbox_launch_apply_forces(int n, dbox_body_state* bs, const float* f, cudaStream_t s);
 extern "C" int dbox_launch_query_build(const dbox_query_buffers* b, cudaStream_t s);
@@ -195,6 +198,7 @@ struct dbox_world {
     DBuf<unsigned> d_sample_count;
     DBuf<int> s_slog, s_pend;
     int measure = 0;
+    int wait_polls = 1 << 20;   // budget of one mbarrier wait in the solve kernel (polls)
     // contact listener
     DBuf<dbox_contact_event> d_events;
     DBuf<unsigned> s_sapk0, s_sapk1;
@@ -217,6 +221,16 @@ struct dbox_world {
     int last_launches = 0;
     dbox_event_fn listener = nullptr;
     void* listener_user = nullptr;
+    // table contact filters (b2World.SetContactFilter): per world a mode and 64 class rows
+    std::vector<int> fmode;
+    std::vector<unsigned long long> ftab;
+    DBuf<int> d_fmode;
+    DBuf<unsigned long long> d_ftab;
+    bool filter_dirty = false;
+    dbox_world* start_src = nullptr;         // warm-start mode 3: the handle whose contacts give the start
+    dbox_presolve_fn presolve = nullptr;     // PreSolve window between Collide and Solve
+    void* presolve_user = nullptr;
+    std::vector<dbox_presolve_contact> h_presolve;
     cudaEvent_t ev[4];
     bool events_made = false;
     // timed multi-step graph (per-phase events inside the graph)
@@ -258,6 +272,8 @@ void free_device(dbox_world* w) {
     w->d_solve_order.free(); w->d_solve_queue.free();
     w->s_feat.free(); w->s_vsave.free(); w->s_slog.free(); w->s_pend.free();
     w->d_events.free(); w->s_cevt.free();
+    w->d_fmode.free(); w->d_ftab.free();
+    w->filter_dirty = true;
     w->s_sapk0.free(); w->s_sapk1.free(); w->s_sapi0.free(); w->s_sapi1.free(); w->s_sapbox.free(); w->d_porder.free(); w->s_sapcell.free(); w->d_big.free(); w->n_big = 0;
     w->s_cbody.free(); w->s_adj_items.free(); w->s_isl_pair.free(); w->s_cq.free(); w->s_cvis.free(); w->s_bfl.free(); w->s_sbody.free(); w->d_prof.free();
     if (w->graph) { cudaGraphExecDestroy(w->graph); w->graph = nullptr; }
@@ -280,7 +296,7 @@ int alloc_mode_scratch(dbox_world* w) {
         if (!w->s_pend.p) ok &= w->s_pend.alloc(nc) == 0;
     }
     if (w->measure && !w->s_vsave.p) ok &= w->s_vsave.alloc(3 * nb) == 0;
-    if (w->listener) {
+    if (w->listener || w->presolve) {
         if (!w->s_cevt.p) ok &= w->s_cevt.alloc(nc) == 0;
         if (!w->d_events.p) ok &= w->d_events.alloc(4 * nc + 64 * w->wi.size()) == 0;
     }
@@ -652,15 +668,34 @@ int upload(dbox_world* w) {
     return 0;
 }
 
+// the table contact filters on the device (nothing while every world keeps the default rule)
+int sync_filter(dbox_world* w) {
+    if (!w->filter_dirty) return 0;
+    bool any = false;
+    for (int m : w->fmode) any |= m != 0;
+    if (!any) {
+        w->d_fmode.free();
+        w->d_ftab.free();
+    } else {
+        if (!w->d_fmode.p && w->d_fmode.alloc(w->fmode.size())) return fail(DBOX_ERR_CUDA, "filter allocation failed");
+        if (!w->d_ftab.p && w->d_ftab.alloc(w->ftab.size())) return fail(DBOX_ERR_CUDA, "filter allocation failed");
+        CU(cudaMemcpy(w->d_fmode.p, w->fmode.data(), sizeof(int) * w->fmode.size(), cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(w->d_ftab.p, w->ftab.data(), sizeof(unsigned long long) * w->ftab.size(), cudaMemcpyHostToDevice));
+    }
+    w->filter_dirty = false;
+    return 0;
+}
+
 int ensure_device(dbox_world* w) {
     w->mirrors_fresh = false;              // device work follows
     ++w->gen;                              // and may move proxies: the query index goes stale
     if (w->dirty || !w->on_device) {
         int rc = download(w);
         if (rc) return rc;
-        return upload(w);
+        rc = upload(w);
+        if (rc) return rc;
     }
-    return 0;
+    return sync_filter(w);
 }
 
 dg::Ctx make_ctx(dbox_world* w, float dt, int vi, int pi) {
@@ -745,18 +780,22 @@ dg::Ctx make_ctx(dbox_world* w, float dt, int vi, int pi) {
     x.continuous = w->continuous;
     x.sub_stepping = w->substep;
     x.allow_sleep = w->allow_sleep;
-    x.record_events = w->listener ? 1 : 0;
+    x.record_events = (w->listener || w->presolve) ? 1 : 0;
     x.g_status = w->g_status.p;
     x.prof = w->profiling ? w->d_prof.p : nullptr;
     x.ws_mode = w->ws_mode;
     if (w->ws_mode == 2 && w->mlp) dbox_mlp_device_view(w->mlp, &x.mlp);
     x.samples = w->d_samples.p;
+    x.start_ct = (w->ws_mode == 3 && w->start_src) ? w->start_src->d_ct.p : nullptr;
     x.sample_count = w->d_sample_count.p;
     x.sample_cap = w->sample_cap;
     x.s_slog = w->s_slog.p;
     x.s_feat = w->s_feat.p;
     x.s_pend = w->s_pend.p;
     x.measure = w->measure;
+    x.wait_polls = w->wait_polls;
+    x.fmode = w->d_fmode.p;
+    x.ftab = w->d_ftab.p;
     x.s_vsave = w->s_vsave.p;
     x.events = w->d_events.p;
     x.s_sapk[0] = w->s_sapk0.p;
@@ -1789,6 +1828,158 @@ int32_t dbox_world_set_listener(dbox_world* w, dbox_event_fn fn, void* user) {
     return DBOX_OK;
 }
 
+// b2Fixture.Refilter (b2fixture.d:140-180): flag the fixture's contacts for filtering and touch
+// its proxies so that new pairs may be created
+static void refilter(HostWorld& hw, int f) {
+    for (auto& c : hw.ct)
+        if (c.fixture_a == f || c.fixture_b == f) c.flags |= dg::kContactFilter;
+    for (int g : fixture_group(hw, f))
+        if (hw.px[g].proxy_id >= 0) hw.px[g].moved = 1;
+}
+
+static int edit_fixture(dbox_world* w, int32_t world, int32_t fixture, const char* what) {
+    if (!w || world < 0 || world >= (int)w->worlds.size()) return fail(DBOX_ERR_INVALID, "%s: bad world", what);
+    HostWorld& hw = w->worlds[world];
+    if (fixture < 0 || fixture >= (int)hw.fx.size() || body_gone(hw, hw.fx[fixture].body))
+        return fail(DBOX_ERR_INVALID, "%s: no fixture %d", what, fixture);
+    const std::vector<int>& list = hw.body_fix[hw.fx[fixture].body];
+    if (std::find(list.begin(), list.end(), fixture) == list.end())
+        return fail(DBOX_ERR_INVALID, "%s: fixture %d was destroyed", what, fixture);
+    return prepare_edit(w);
+}
+
+int32_t dbox_fixture_set_filter(dbox_world* w, int32_t world, int32_t fixture, uint16_t category_bits,
+                                uint16_t mask_bits, int16_t group_index) {
+    int rc = edit_fixture(w, world, fixture, "dbox_fixture_set_filter");
+    if (rc) return rc;
+    HostWorld& hw = w->worlds[world];
+    for (int g : fixture_group(hw, fixture)) {                         // a chain's children share it
+        hw.fx[g].filter = (uint32_t)category_bits | ((uint32_t)mask_bits << 16);
+        hw.fx[g].group = group_index;
+    }
+    refilter(hw, fixture);
+    return DBOX_OK;
+}
+
+int32_t dbox_fixture_set_filter_class(dbox_world* w, int32_t world, int32_t fixture, int32_t filter_class) {
+    if (filter_class < 0 || filter_class > 63) return fail(DBOX_ERR_INVALID, "dbox_fixture_set_filter_class: class %d", filter_class);
+    int rc = edit_fixture(w, world, fixture, "dbox_fixture_set_filter_class");
+    if (rc) return rc;
+    HostWorld& hw = w->worlds[world];
+    for (int g : fixture_group(hw, fixture)) hw.fx[g].fclass = filter_class;
+    refilter(hw, fixture);
+    return DBOX_OK;
+}
+
+int32_t dbox_world_set_contact_filter(dbox_world* w, int32_t world, const uint64_t* table, int32_t with_default) {
+    if (!w || world < 0 || world >= (int)w->worlds.size()) return fail(DBOX_ERR_INVALID, "dbox_world_set_contact_filter: bad world");
+    if (table) {
+        for (int a = 0; a < 64; ++a)
+            for (int b = 0; b < 64; ++b)
+                if (((table[a] >> b) & 1u) != ((table[b] >> a) & 1u))
+                    return fail(DBOX_ERR_INVALID, "dbox_world_set_contact_filter: table not symmetric at (%d, %d)", a, b);
+    }
+    w->fmode.resize(w->worlds.size(), 0);
+    w->ftab.resize(64 * w->worlds.size(), 0);
+    w->fmode[world] = table ? (with_default ? 1 : 2) : 0;
+    for (int a = 0; a < 64; ++a) w->ftab[64 * (size_t)world + a] = table ? table[a] : 0;
+    w->filter_dirty = true;
+    if (w->graph) { cudaGraphExecDestroy(w->graph); w->graph = nullptr; }
+    if (w->tgraph) { cudaGraphExecDestroy(w->tgraph); w->tgraph = nullptr; }
+    return DBOX_OK;
+}
+
+int32_t dbox_world_set_presolve(dbox_world* w, dbox_presolve_fn fn, void* user) {
+    if (!w) return DBOX_ERR_INVALID;
+    w->presolve = fn;
+    w->presolve_user = user;
+    if (fn && w->on_device) {
+        int rc = alloc_mode_scratch(w);
+        if (rc) return rc;
+    }
+    if (w->graph) { cudaGraphExecDestroy(w->graph); w->graph = nullptr; }
+    if (w->tgraph) { cudaGraphExecDestroy(w->tgraph); w->tgraph = nullptr; }
+    return DBOX_OK;
+}
+
+// The PreSolve window, after Collide and before Solve: the PRESOLVE events Collide recorded
+// (per world, in contact-list order) name their contacts by fixture pair; the callback gets
+// one record per call and may edit it; edited contacts are written back before the solve.
+static int presolve_window(dbox_world* w) {
+    const size_t W = w->worlds.size();
+    std::vector<dg::WorldDyn> wd(W);
+    CU(cudaStreamSynchronize(w->stream));
+    CU(cudaMemcpy(wd.data(), w->d_wd.p, sizeof(dg::WorldDyn) * W, cudaMemcpyDeviceToHost));
+    w->h_presolve.clear();
+    std::vector<std::pair<size_t, size_t>> spans(W, {0, 0});         // records of each world
+    std::vector<std::vector<dbox_contact_state>> cts(W);
+    std::vector<std::vector<int>> where(W);                           // record -> contact slot
+    std::vector<dbox_contact_event> ev;
+    for (size_t i = 0; i < W; ++i) {
+        const dg::WorldInfo& wi = w->wi[i];
+        const int cnt = std::min(wd[i].ev_count, 4 * wi.contact_cap + 64);
+        spans[i].first = w->h_presolve.size();
+        if (cnt <= 0) { spans[i].second = spans[i].first; continue; }
+        ev.resize(cnt);
+        CU(cudaMemcpy(ev.data(), w->d_events.p + 4 * (size_t)wi.contact_start + 64 * i, sizeof(dbox_contact_event) * cnt,
+                      cudaMemcpyDeviceToHost));
+        bool any = false;
+        for (const auto& e : ev) any |= e.kind == DBOX_EVENT_PRESOLVE;
+        if (!any) { spans[i].second = spans[i].first; continue; }
+        const int nct = wd[i].contact_count;
+        cts[i].resize(nct);
+        if (nct > 0)
+            CU(cudaMemcpy(cts[i].data(), w->d_ct.p + wi.contact_start, sizeof(dbox_contact_state) * nct,
+                          cudaMemcpyDeviceToHost));
+        std::unordered_map<unsigned long long, int> slot;             // a fixture pair has one contact
+        slot.reserve(2 * (size_t)nct);
+        for (int k = 0; k < nct; ++k)
+            slot[((unsigned long long)(unsigned)cts[i][k].fixture_a << 32) | (unsigned)cts[i][k].fixture_b] = k;
+        for (const auto& e : ev) {
+            if (e.kind != DBOX_EVENT_PRESOLVE) continue;
+            const unsigned fa = (unsigned)(e.fixture_a + wi.fix_start), fb = (unsigned)(e.fixture_b + wi.fix_start);
+            auto it = slot.find(((unsigned long long)fa << 32) | fb);
+            if (it == slot.end()) return fail(DBOX_ERR_CUDA, "PreSolve window: no contact for fixtures %d, %d", e.fixture_a, e.fixture_b);
+            const dbox_contact_state& c = cts[i][it->second];
+            dbox_presolve_contact r;
+            memset(&r, 0, sizeof(r));
+            r.world = (int32_t)i;
+            r.enabled = 1;
+            r.friction = c.friction;
+            r.restitution = c.restitution;
+            r.tangent_speed = c.tangent_speed;
+            r.contact = c;
+            r.contact.fixture_a = e.fixture_a;
+            r.contact.fixture_b = e.fixture_b;
+            r.contact.flags &= ~(uint32_t)(dg::kContactUserOff | dg::kContactNew0 | dg::kContactNew1);
+            w->h_presolve.push_back(r);
+            where[i].push_back(it->second);
+        }
+        spans[i].second = w->h_presolve.size();
+    }
+    if (w->h_presolve.empty()) return DBOX_OK;
+    w->presolve(w->h_presolve.data(), (int32_t)w->h_presolve.size(), w->presolve_user);
+    for (size_t i = 0; i < W; ++i) {
+        bool dirty = false;
+        for (size_t r = spans[i].first; r < spans[i].second; ++r) {
+            const dbox_presolve_contact& p = w->h_presolve[r];
+            dbox_contact_state& c = cts[i][where[i][r - spans[i].first]];
+            if (!p.enabled) { c.flags &= ~(uint32_t)dg::kContactEnabled; c.flags |= dg::kContactUserOff; dirty = true; }
+            if (memcmp(&p.friction, &c.friction, 4) || memcmp(&p.restitution, &c.restitution, 4) ||
+                memcmp(&p.tangent_speed, &c.tangent_speed, 4)) {
+                c.friction = p.friction;
+                c.restitution = p.restitution;
+                c.tangent_speed = p.tangent_speed;
+                dirty = true;
+            }
+        }
+        if (dirty)
+            CU(cudaMemcpyAsync(w->d_ct.p + w->wi[i].contact_start, cts[i].data(), sizeof(dbox_contact_state) * cts[i].size(),
+                               cudaMemcpyHostToDevice, w->stream));
+    }
+    return DBOX_OK;
+}
+
 // the events of the last step, world by world, handed to the listener on this thread
 static int deliver_events(dbox_world* w) {
     if (!w->listener || !w->d_events.p) return DBOX_OK;
@@ -1821,7 +2012,17 @@ int32_t dbox_world_step(dbox_world* w, float dt, int32_t velocity_iterations, in
     dg::Ctx x = make_ctx(w, dt, velocity_iterations, position_iterations);
     CU(cudaEventRecord(w->ev[0], w->stream));
     int launches = 0;
-    int err = dbox_launch_step(&x, w->stream, &launches);
+    int err;
+    if (w->presolve) {                      // Collide, the host's PreSolve window, then Solve
+        err = dbox_launch_collide(&x, w->stream);
+        if (!err) {
+            rc = presolve_window(w);
+            if (rc) return rc;
+            err = dbox_launch_solve(&x, w->stream, &launches);
+        }
+    } else {
+        err = dbox_launch_step(&x, w->stream, &launches);
+    }
     if (err) return fail(DBOX_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString((cudaError_t)err));
     CU(cudaEventRecord(w->ev[1], w->stream));
     rc = check_status(w);
@@ -1840,7 +2041,7 @@ int32_t dbox_world_step_n(dbox_world* w, float dt, int32_t velocity_iterations, 
         return fail(DBOX_ERR_INVALID, "dbox_world_step_n: bad arguments");
     int rc = ensure_device(w);
     if (rc) return rc;
-    if (w->listener) {                      // events are delivered after every step
+    if (w->listener || w->presolve) {       // events are delivered / PreSolve is called in every step
         for (int i = 0; i < steps && !rc; ++i) rc = dbox_world_step(w, dt, velocity_iterations, position_iterations);
         return rc;
     }
@@ -1868,6 +2069,7 @@ int32_t dbox_world_step_n_timed(dbox_world* w, float dt, int32_t velocity_iterat
                                 int32_t steps, float* total_ms, float* phase_ms) {
     if (!w || steps < 1 || velocity_iterations < 0 || position_iterations < 0)
         return fail(DBOX_ERR_INVALID, "dbox_world_step_n_timed: bad arguments");
+    if (w->presolve) return fail(DBOX_ERR_UNSUPPORTED, "dbox_world_step_n_timed: a PreSolve window needs dbox_world_step");
     int rc = ensure_device(w);
     if (rc) return rc;
     int flags = w->warm | (w->continuous << 1) | (w->substep << 2) | (w->allow_sleep << 3) | (w->autoclear << 4);
@@ -1951,11 +2153,12 @@ int32_t dbox_world_get_transforms(dbox_world* w, float* xya) {
 }
 
 int32_t dbox_world_set_warmstart(dbox_world* w, int32_t mode, dbox_mlp* model, int32_t sample_capacity) {
-    if (!w || mode < 0 || mode > 2) return fail(DBOX_ERR_INVALID, "dbox_world_set_warmstart: bad mode");
+    if (!w || mode < 0 || mode > 3) return fail(DBOX_ERR_INVALID, "dbox_world_set_warmstart: bad mode");
     if (mode == 2 && !model) return fail(DBOX_ERR_INVALID, "dbox_world_set_warmstart: learned mode needs a model");
     if (mode == 1 && sample_capacity <= 0) return fail(DBOX_ERR_INVALID, "dbox_world_set_warmstart: sample capacity must be > 0");
     w->ws_mode = mode;
     w->mlp = mode == 2 ? model : nullptr;
+    if (mode != 3) w->start_src = nullptr;
     if (mode == 1 && sample_capacity != w->sample_cap) {
         w->d_samples.free();
         w->d_sample_count.free();
@@ -1970,6 +2173,47 @@ int32_t dbox_world_set_warmstart(dbox_world* w, int32_t mode, dbox_mlp* model, i
     }
     if (w->graph) { cudaGraphExecDestroy(w->graph); w->graph = nullptr; }
     if (w->tgraph) { cudaGraphExecDestroy(w->tgraph); w->tgraph = nullptr; }
+    return DBOX_OK;
+}
+
+// the two handles hold the same worlds laid out the same way on the device
+static bool same_layout(const dbox_world* a, const dbox_world* b) {
+    if (a->wi.size() != b->wi.size() || !a->on_device || !b->on_device || a->dirty || b->dirty) return false;
+    return a->wi.empty() || memcmp(a->wi.data(), b->wi.data(), sizeof(dg::WorldInfo) * a->wi.size()) == 0;
+}
+
+int32_t dbox_world_set_start_source(dbox_world* w, dbox_world* src) {
+    if (!w || !src || w == src || w->ws_mode != 3) return fail(DBOX_ERR_INVALID, "dbox_world_set_start_source: bad arguments");
+    int rc = ensure_device(w);
+    if (!rc) rc = ensure_device(src);
+    if (rc) return rc;
+    if (!same_layout(w, src)) return fail(DBOX_ERR_INVALID, "dbox_world_set_start_source: the handles' worlds differ");
+    w->start_src = src;
+    if (w->graph) { cudaGraphExecDestroy(w->graph); w->graph = nullptr; }
+    if (w->tgraph) { cudaGraphExecDestroy(w->tgraph); w->tgraph = nullptr; }
+    return DBOX_OK;
+}
+
+int32_t dbox_world_copy_state(dbox_world* dst, dbox_world* src) {
+    if (!dst || !src || dst == src) return fail(DBOX_ERR_INVALID, "dbox_world_copy_state: bad arguments");
+    int rc = ensure_device(dst);
+    if (!rc) rc = ensure_device(src);
+    if (rc) return rc;
+    if (!same_layout(dst, src)) return fail(DBOX_ERR_INVALID, "dbox_world_copy_state: the handles' worlds differ");
+    CU(cudaStreamSynchronize(src->stream));
+    CU(cudaStreamSynchronize(dst->stream));
+    auto cp = [&](void* d, const void* s, size_t bytes) -> cudaError_t {
+        return bytes ? cudaMemcpyAsync(d, s, bytes, cudaMemcpyDeviceToDevice, dst->stream) : cudaSuccess;
+    };
+    CU(cp(dst->d_wd.p, src->d_wd.p, sizeof(dg::WorldDyn) * src->wi.size()));
+    CU(cp(dst->d_bs.p, src->d_bs.p, sizeof(dbox_body_state) * src->d_bs.n));
+    CU(cp(dst->d_px.p, src->d_px.p, sizeof(dbox_proxy_state) * src->d_px.n));
+    CU(cp(dst->d_jt.p, src->d_jt.p, sizeof(dg::DJoint) * src->d_jt.n));
+    CU(cp(dst->d_ct.p, src->d_ct.p, sizeof(dbox_contact_state) * src->d_ct.n));
+    CU(cp(dst->d_hash.p, src->d_hash.p, sizeof(unsigned long long) * src->d_hash.n));
+    CU(cudaStreamSynchronize(dst->stream));
+    dst->mirrors_fresh = false;
+    ++dst->gen;
     return DBOX_OK;
 }
 
@@ -2008,6 +2252,14 @@ int32_t dbox_mlp_train_world(dbox_mlp* m, dbox_world* w, int32_t epochs, int32_t
     if (rc) return rc;
     if (n <= 0) return fail(DBOX_ERR_INVALID, "dbox_mlp_train_world: the world holds no samples");
     return dbox_mlp_train_device(m, n, w->d_samples.p, epochs, batch, lr, seed, epoch_loss);
+}
+
+int32_t dbox_world_set_wait_limit(dbox_world* w, int32_t polls) {
+    if (!w || polls < 0) return fail(DBOX_ERR_INVALID, "dbox_world_set_wait_limit: bad arguments");
+    w->wait_polls = polls < (1 << 20) ? polls : (1 << 20);
+    if (w->graph) { cudaGraphExecDestroy(w->graph); w->graph = nullptr; }
+    if (w->tgraph) { cudaGraphExecDestroy(w->tgraph); w->tgraph = nullptr; }
+    return DBOX_OK;
 }
 
 int32_t dbox_world_set_measure(dbox_world* w, int32_t enable) {

@@ -51,7 +51,10 @@ enum { kContactIsland = 0x1, kContactTouching = 0x2, kContactEnabled = 0x4, kCon
        kContactBulletHit = 0x10, kContactToi = 0x20,
        // learned warm start only (never set in the plain method): manifold point 0 / 1 had no
        // feature-id match in the last update, so its impulse started from zero
-       kContactNew0 = 0x40, kContactNew1 = 0x80 };
+       kContactNew0 = 0x40, kContactNew1 = 0x80,
+       // set by the host's PreSolve window when the callback disabled the contact; the sub-step
+       // updates of SolveTOI keep it disabled, the next Collide clears it
+       kContactUserOff = 0x100 };
 enum { kManifoldCircles = 0, kManifoldFaceA = 1, kManifoldFaceB = 2 };
 
 // ------------------------------------------------------------ vector algebra (common/b2math.d)
@@ -145,7 +148,7 @@ struct DFixture {
     float2 v[8];
     float2 n[8];
     int edge_flags;
-    int pad0;
+    int fclass;        // filter class 0..63 of a table contact filter (dbox_world_set_contact_filter)
 };
 
 struct AABB { float2 lo, hi; };

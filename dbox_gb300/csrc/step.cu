@@ -90,21 +90,35 @@ DG bool body_should_collide(const Ctx& x, int self, int other) {
     }
     return true;
 }
-// b2ContactFilter.ShouldCollide (b2worldcallbacks.d:52-64)
-DG bool filter_should_collide(const DFixture& a, const DFixture& b) {
-    if (a.group == b.group && a.group != 0) return a.group > 0;
-    uint32_t catA = a.filter & 0xffffu, maskA = a.filter >> 16;
-    uint32_t catB = b.filter & 0xffffu, maskB = b.filter >> 16;
-    return (maskA & catB) != 0 && (catA & maskB) != 0;
+// b2ContactFilter.ShouldCollide (b2worldcallbacks.d:52-64), or the world's table filter
+// (b2World.SetContactFilter with a class table: bit b of row a lets classes a and b collide),
+// alone or together with the default rule
+DG bool filter_should_collide(const Ctx& x, int w, const DFixture& a, const DFixture& b) {
+    bool def;
+    if (a.group == b.group && a.group != 0) {
+        def = a.group > 0;
+    } else {
+        uint32_t catA = a.filter & 0xffffu, maskA = a.filter >> 16;
+        uint32_t catB = b.filter & 0xffffu, maskB = b.filter >> 16;
+        def = (maskA & catB) != 0 && (catA & maskB) != 0;
+    }
+    const int mode = x.fmode ? x.fmode[w] : 0;
+    if (mode == 0) return def;
+    const bool tab = (x.ftab[64 * (size_t)w + (a.fclass & 63)] >> (b.fclass & 63)) & 1ull;
+    return mode == 1 ? (tab && def) : tab;
 }
 
 // ------------------------------------------------------------ b2Contact.Update (contacts/b2contact.d:270-356)
 // Returns true when the touching state changed (the caller wakes both bodies).
-DG bool contact_update(const Ctx& x, dbox_contact_state& c, unsigned* evt = nullptr) {
+// `toi`: a sub-step update of SolveTOI, where a contact the host's PreSolve window disabled in
+// this step stays disabled (the window's decision stands in for PreSolve's there).
+DG bool contact_update(const Ctx& x, dbox_contact_state& c, unsigned* evt = nullptr, bool toi = false) {
     Manifold m;
     manifold_load(c, m);
     Manifold old = m;
+    const bool userOff = toi && (c.flags & kContactUserOff) != 0;
     c.flags |= kContactEnabled;
+    if (!toi) c.flags &= ~(uint32_t)kContactUserOff;
     bool wasTouching = (c.flags & kContactTouching) != 0;
     const DFixture& fa = x.fx[c.fixture_a];
     const DFixture& fb = x.fx[c.fixture_b];
@@ -133,6 +147,7 @@ DG bool contact_update(const Ctx& x, dbox_contact_state& c, unsigned* evt = null
         changed = touching != wasTouching;
     }
     if (touching) c.flags |= kContactTouching; else c.flags &= ~(uint32_t)kContactTouching;
+    if (userOff && !sensor && touching) c.flags &= ~(uint32_t)kContactEnabled;
     manifold_store(m, c);
     // listener calls of b2Contact.Update (b2contact.d:340-355): BeginContact, EndContact, PreSolve
     if (evt) *evt = (!wasTouching && touching ? 1u : 0u) | (wasTouching && !touching ? 2u : 0u) | (!sensor && touching ? 4u : 0u);
@@ -548,7 +563,7 @@ __device__ __noinline__ void add_pairs(const Ctx& x, int w, int total) {
             if (acc) acc = !(fA.type == kShapeEdge && fB.type == kShapeEdge);   // no edge-edge contact type
             if (acc) acc = !hash_contains(x, wi, pair_key(pr.x, pr.y));
             if (acc) acc = body_should_collide(x, fB.body, fA.body);
-            if (acc) acc = filter_should_collide(fA, fB);
+            if (acc) acc = filter_should_collide(x, w, fA, fB);
         }
         unsigned bal = __ballot_sync(0xffffffffu, acc);
         if (acc) {
@@ -872,7 +887,7 @@ __global__ void k_collide(Ctx x) {
         int state = 0;
         unsigned evt = 0;
         if (c.flags & kContactFilter) {                                // b2contactmanager.d:266-288
-            if (!body_should_collide(x, B, A) || !filter_should_collide(fa, fb)) {
+            if (!body_should_collide(x, B, A) || !filter_should_collide(x, w, fa, fb)) {
                 state = 2;
                 evt = (c.flags & kContactTouching) ? 2u : 0u;
                 if (c.point_count > 0 && !fa.sensor && !fb.sensor) {
@@ -3241,14 +3256,18 @@ DG void bulk_copy(unsigned long long* bar, void* dst, const void* src, unsigned 
                  :: "r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(b) : "memory");
 }
 constexpr int kMbarSpinLimit = 1 << 20;
-// wait for the phase of `bar` with the given parity; false when the spin limit ran out
-DG bool mbar_wait(unsigned long long* bar, unsigned parity) {
+// Wait for the phase of `bar` with the given parity.  `budget` polls is what the wait may take
+// (Ctx.wait_polls, kMbarSpinLimit unless a caller lowers it): past it the wait is reported
+// (false) but keeps polling, up to kMbarSpinLimit polls in all, so that the copy has landed
+// before its rows are read and no copy is still in flight when the block exits.  Only a copy
+// that never completes within kMbarSpinLimit polls leaves stale (in-bounds) rows behind.
+DG bool mbar_wait(unsigned long long* bar, unsigned parity, int budget) {
     unsigned b = smem_u32(bar);
     for (int i = 0; i < kMbarSpinLimit; ++i) {
         unsigned done;
         asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
                      "selp.u32 %0, 1, 0, p;\n\t}" : "=r"(done) : "r"(b), "r"(parity) : "memory");
-        if (done) return true;
+        if (done) return i < budget;
     }
     return false;
 }
@@ -3260,7 +3279,8 @@ struct RowRing {
     float* base;                   // 9216 bytes of rows
     unsigned long long* bar;       // two mbarriers
     unsigned par;
-    bool ok;
+    bool ok;                       // no wait went past its budget
+    int budget;                    // polls a wait may take (Ctx.wait_polls)
 };
 
 // One sweep over levels 1..maxL of a schedule whose rows are stored in schedule order:
@@ -3287,7 +3307,7 @@ DG void sweep_levels(const int* lvl, int maxL, int nItems, const RowT* rows, Row
     auto wait_next = [&]() {
         ++waited;
         const int h = waited & 1;
-        ring.ok &= mbar_wait(&ring.bar[h], (ring.par >> h) & 1u);
+        ring.ok &= mbar_wait(&ring.bar[h], (ring.par >> h) & 1u, ring.budget);
         ring.par ^= 1u << h;
     };
     auto issue_upto = [&](int want) {
@@ -3643,6 +3663,20 @@ DG void solve_world(const Ctx& x, int w, float* sbp, bool sb_smem, float* stage_
                             for (int q = 0; q < kFeat; ++q) f[q] = fv[q];
                         }
                         pend = x.ws_mode == 2;
+                        if (x.ws_mode == 3 && x.start_ct) {
+                            // given start: the impulses another handle's step from the same state
+                            // ended with at this contact slot (clamped as a prediction is)
+                            const dbox_contact_state& g = x.start_ct[item];
+                            for (int j = 0; j < pc.pointCount; ++j) {
+                                if (!(fr & (j == 0 ? kContactNew0 : kContactNew1))) continue;
+                                float ln = g.points[j].normal_impulse, lt = g.points[j].tangent_impulse;
+                                ln = ln > 0.0f ? ln : 0.0f;
+                                const float mf = vr.K.w * ln;
+                                lt = lt < -mf ? -mf : (lt > mf ? mf : lt);
+                                if (j == 0) { vr.imp.x = ln; vr.imp.y = lt; }
+                                else { vr.imp.z = ln; vr.imp.w = lt; }
+                            }
+                        }
                     }
                 }
                 vrow[idx] = vr;
@@ -3908,6 +3942,7 @@ DG void solve_world(const Ctx& x, int w, float* sbp, bool sb_smem, float* stage_
     }
     stamp(x, w, 8);
     // copy back + SynchronizeTransform (b2island.d:227-235)
+    bool nonfinite = false;
     for (int t = lane; t < nbI; t += kWarp) {
         int i = x.s_isl_body[b0 + t];
         dbox_body_state& B = x.bs[b0 + i];
@@ -3915,7 +3950,12 @@ DG void solve_world(const Ctx& x, int w, float* sbp, bool sb_smem, float* stage_
         B.sweep[4] = c.x; B.sweep[5] = c.y; B.sweep[7] = sb.a(i);
         B.vel[0] = v.x; B.vel[1] = v.y; B.vel[2] = sb.w(i);
         b_sync_transform(B);
+        nonfinite |= !(isfinite(c.x) && isfinite(c.y) && isfinite(B.sweep[7]) && isfinite(v.x) && isfinite(v.y) &&
+                       isfinite(B.vel[2]));
     }
+    // the reference has no such check (b2Body asserts IsValid on its setters only); a world
+    // whose bodies left the finite range is reported as DBOX_ERR_NAN after the step
+    if (__any_sync(0xffffffffu, nonfinite) && lane == 0) set_error(x, w, DBOX_ERR_NAN);
     tsync();
     // sleep (b2island.d:241-279)
     if (x.allow_sleep) {
@@ -4022,7 +4062,7 @@ DG int toi_collect(const Ctx& x, int c0, int b0, int k0, int k1, int* list, int 
 // b2Contact.Update inside the TOI loop: wakes are applied immediately (out of line: TOI events
 // are rare, and the narrowphase inlined here would double the kernel's collision code)
 __device__ __noinline__ void toi_update(const Ctx& x, dbox_contact_state& c, unsigned* evt = nullptr) {
-    if (contact_update(x, c, evt)) {
+    if (contact_update(x, c, evt, true)) {
         b_set_awake(x.bs[x.fx[c.fixture_a].body], true);
         b_set_awake(x.bs[x.fx[c.fixture_b].body], true);
     }
@@ -4402,6 +4442,7 @@ __global__ void __launch_bounds__(kSolveWarps * 32, 3) k_solve_toi(const __grid_
     ring.bar = reinterpret_cast<unsigned long long*>(stage_f + kStageFloats);
     ring.par = 0;
     ring.ok = true;
+    ring.budget = x.wait_polls;
     if (lane == 0) {
         mbar_init(&ring.bar[0]);
         mbar_init(&ring.bar[1]);
@@ -4479,6 +4520,33 @@ __global__ void __launch_bounds__(kSolveWarps * 32, 3) k_solve_toi(const __grid_
 // ------------------------------------------------------------ launch entry points (called from api.cpp)
 // Launch one step.  ev, when not NULL, holds 4 events recorded at the phase
 // boundaries: [0] before Collide, [1] before Solve, [2] and [3] after Solve + SolveTOI (one kernel).
+// part 1 of a step: FindNewContacts for new fixtures, then Collide (3 launches)
+extern "C" int dbox_launch_collide(const dg::Ctx* x, cudaStream_t stream) {
+    const int threads = 128;                       // four worlds per block, one warp each
+    int team_blocks = (x->W * dg::kWarp + threads - 1) / threads;
+    int flat_blocks = (x->total_contacts + 255) / 256;
+    if (flat_blocks < 1) flat_blocks = 1;
+    if (flat_blocks > 152 * 16) flat_blocks = 152 * 16;
+    dg::k_step_begin<<<team_blocks, threads, 0, stream>>>(*x);
+    dg::k_collide<<<flat_blocks, 256, 0, stream>>>(*x);
+    dg::k_collide_finish<<<team_blocks, threads, 0, stream>>>(*x);
+    return (int)cudaGetLastError();
+}
+
+// part 2 of a step: Solve and SolveTOI (1 launch, 3 with a large world); *launches = all of the step's
+extern "C" int dbox_launch_solve(const dg::Ctx* x, cudaStream_t stream, int* launches) {
+    const int threads = 128;
+    if (x->solve_blocks < 1) return (int)cudaErrorInvalidValue;
+    if (x->solve_queue) cudaMemsetAsync(x->solve_queue, 0, sizeof(int) * (2 + 4 * (size_t)x->solve_nsm), stream);
+    dg::k_solve_toi<<<x->solve_blocks, x->solve_wpb * dg::kWarp, x->solve_smem_floats * sizeof(float), stream>>>(*x);
+    if (x->n_big > 0) {                             // large worlds: their pairs on a block each, then AddPair + TOI
+        dg::k_pairs_block<<<x->n_big, dg::kPairThreads, 0, stream>>>(*x);
+        dg::k_finish_big<<<(x->n_big * dg::kWarp + threads - 1) / threads, threads, 0, stream>>>(*x);
+    }
+    if (launches) *launches = x->n_big > 0 ? 6 : 4;
+    return (int)cudaGetLastError();
+}
+
 extern "C" int dbox_launch_step_ev(const dg::Ctx* x, cudaStream_t stream, int* launches, cudaEvent_t* ev) {
     const int threads = 128;                       // four worlds per block, one warp each
     int team_blocks = (x->W * dg::kWarp + threads - 1) / threads;

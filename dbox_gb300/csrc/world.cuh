@@ -272,6 +272,7 @@ struct Ctx {
     // learned warm start: 0 plain (Box2D), 1 plain + log training samples, 2 learned start
     int ws_mode;
     MlpDev mlp;                    // ws_mode 2: the network
+    const dbox_contact_state* start_ct;  // ws_mode 3: contacts (same slots) whose impulses start the new points
     float* samples;                // ws_mode 1: kSampleFloats per sample (32 features, 4 targets)
     unsigned* sample_count;        // ws_mode 1: samples written so far (may exceed sample_cap)
     int sample_cap;
@@ -279,6 +280,9 @@ struct Ctx {
     float* s_feat;                 // contact-slot-indexed: 32 features per pending learned contact
     int* s_pend;                   // contact-slot-indexed: velocity-schedule positions awaiting a prediction
     int measure;                   // 1: fill the q_* fields of WorldDyn each step
+    int wait_polls;                // polls an mbarrier wait may take before it counts as DBOX_ERR_TIMEOUT
+    const int* fmode;              // per world: 0 the default contact filter, 1 table and default, 2 table only
+    const unsigned long long* ftab;  // per world 64 rows: class a collides with class b when bit b of row a is set
     float* s_vsave;                // body-indexed, 3 floats: velocities kept across the measuring sweep
     unsigned long long* prof;      // optional: kProfSlots clock64 figures per world (NULL = off)
 };

@@ -679,6 +679,129 @@ def chain_ground(n=40, seed=17):
     return out
 
 
+def features(seed=23):
+    """The less common parts of a step in one world: sensor fixtures (a static sensor region
+    and a sensor beside a solid fixture on one dynamic body: b2Contact.Update's sensor branch,
+    contacts/b2contact.d:283-296); a bullet circle fired into a box stack and a fast non-bullet
+    box flying at a thin static wall (b2World.SolveTOI with bullets and static bodies,
+    b2world.d:1172-1188); a kinematic platform sliding and turning through boxes; collision
+    filtering (b2ContactFilter.ShouldCollide, b2worldcallbacks.d:52-64): a negative group that
+    overlaps itself, a positive group, and category / mask pairs that skip each other; a bouncy
+    ball (restitution), damped bodies, a body with gravity scale 0.5 and a fixed-rotation box."""
+    rng = np.random.default_rng(seed)
+    parts = [ground_box(hx=60.0)]                                          # 0: ground
+    parts.append(_boxes([(30.0, 4.0)], 0.1, 4.0, abi.STATIC))              # 1: thin wall
+    sensor = _boxes([(-20.0, 3.0)], 3.0, 3.0, abi.STATIC)                  # 2: sensor region
+    sensor["fixtures"]["is_sensor"] = 1
+    parts.append(sensor)
+    stack = _boxes([(18.0, 0.5 + k) for k in range(6)], 0.5, 0.5, abi.DYNAMIC, 0.5, 1.0)   # 3..8
+    parts.append(stack)
+    bullet = _circles([(-5.0, 2.5)], 0.1, abi.DYNAMIC, 4.0, 0.3)           # 9: bullet
+    bullet["bodies"]["bullet"] = 1
+    bullet["bodies"]["linear_velocity"] = (150.0, 0.0)
+    parts.append(bullet)
+    fast = _boxes([(0.0, 5.0)], 0.15, 0.15, abi.DYNAMIC, 0.4, 1.0)         # 10: fast, not a bullet
+    fast["bodies"]["linear_velocity"] = (120.0, 4.0)
+    fast["bodies"]["angular_velocity"] = 3.0
+    parts.append(fast)
+    plat = _boxes([(-32.0, 1.2)], 3.0, 0.25, abi.KINEMATIC)                # 11: kinematic platform
+    plat["bodies"]["linear_velocity"] = (1.5, 0.0)
+    plat["bodies"]["angular_velocity"] = 0.15
+    parts.append(plat)
+    riders = _boxes([(-33.5 + 1.1 * k, 2.2) for k in range(4)], 0.4, 0.4, abi.DYNAMIC, 0.6, 1.0)   # 12..15
+    parts.append(riders)
+    # falling through the sensor region: circles and boxes
+    xs = rng.uniform(-22.5, -17.5, 8)
+    fall = _concat([_circles([(float(x), 8.0 + 1.2 * k)], 0.3) for k, x in enumerate(xs[:4])] +
+                   [_boxes([(float(x), 13.0 + 1.2 * k)], 0.3, 0.3, abi.DYNAMIC) for k, x in enumerate(xs[4:])])
+    parts.append(fall)                                                      # 16..23
+    # two-fixture body: a solid box and a sensor circle around it
+    two = _boxes([(-14.0, 6.0)], 0.5, 0.5, abi.DYNAMIC, 0.6, 1.0)          # 24
+    sc = np.zeros(1, abi.SHAPE_DEF)
+    sc["kind"] = abi.SHAPE_CIRCLE
+    sc["radius"] = 1.5
+    sf = abi.fixture_defs(1)
+    sf["is_sensor"] = 1
+    sf["density"] = 0.0
+    two["shapes"] = np.concatenate([two["shapes"], sc])
+    two["fixtures"] = np.concatenate([two["fixtures"], sf])
+    two["fixture_body"] = np.array([0, 0], np.int32)
+    parts.append(two)
+    # filtering: a negative group stacked into itself (its members never collide with each other)
+    neg = _boxes([(-8.0, 1.0), (-7.7, 1.5), (-8.2, 2.0), (-7.9, 2.6)], 0.5, 0.5, abi.DYNAMIC)   # 25..28
+    neg["fixtures"]["group_index"] = -3
+    parts.append(neg)
+    pos = _boxes([(-3.0, 0.5), (-3.0, 1.5), (-3.0, 2.5)], 0.5, 0.5, abi.DYNAMIC)               # 29..31
+    pos["fixtures"]["group_index"] = 2
+    pos["fixtures"]["category_bits"] = 0x0002
+    pos["fixtures"]["mask_bits"] = 0x0001                                  # ground only, but the group wins
+    parts.append(pos)
+    cat_a = _boxes([(4.0, 0.5), (4.2, 1.5)], 0.5, 0.5, abi.DYNAMIC)       # 32..33: category 4
+    cat_a["fixtures"]["category_bits"] = 0x0004
+    cat_a["fixtures"]["mask_bits"] = 0xFFFF & ~0x0008
+    parts.append(cat_a)
+    cat_b = _boxes([(4.1, 2.6), (4.3, 3.7)], 0.5, 0.5, abi.DYNAMIC)       # 34..35: category 8, skips 4
+    cat_b["fixtures"]["category_bits"] = 0x0008
+    cat_b["fixtures"]["mask_bits"] = 0xFFFF & ~0x0004
+    parts.append(cat_b)
+    ball = _circles([(10.0, 6.0)], 0.4)                                     # 36: restitution 0.8
+    ball["fixtures"]["restitution"] = 0.8
+    parts.append(ball)
+    damped = _boxes([(12.0, 3.0), (13.5, 3.0)], 0.4, 0.4, abi.DYNAMIC)    # 37..38
+    damped["bodies"]["linear_damping"] = 0.5
+    damped["bodies"]["angular_damping"] = 0.8
+    damped["bodies"]["angular_velocity"] = (4.0, -4.0)
+    parts.append(damped)
+    light = _boxes([(15.0, 6.0)], 0.4, 0.4, abi.DYNAMIC)                    # 39: gravity scale 0.5
+    light["bodies"]["gravity_scale"] = 0.5
+    parts.append(light)
+    fixed = _boxes([(7.0, 4.0)], 0.6, 0.3, abi.DYNAMIC)                     # 40: fixed rotation
+    fixed["bodies"]["fixed_rotation"] = 1
+    fixed["bodies"]["angular_velocity"] = 2.0
+    parts.append(fixed)
+    out = _concat(parts)
+    out["name"] = "features"
+    return out
+
+
+def _hanging_chain(x, y, links, hx=0.125, hy=0.025):
+    """A static post at (x, y) and `links` boxes of half-extents hx x hy hanging straight down
+    from it, joined end to end by revolute joints (link density 20, friction 0.4)."""
+    post = _boxes([(x, y)], 0.1, 0.1, abi.STATIC)
+    chain = _boxes([(x, y - hx - 2 * hx * i) for i in range(links)], hy, hx, abi.DYNAMIC, 0.4, 20.0)
+    part = _concat([post, chain])
+    j = np.zeros(links, abi.REVOLUTE_DEF)
+    for i in range(links):
+        j[i]["body_a"] = i                   # the post for i = 0, else link i-1
+        j[i]["body_b"] = i + 1
+        j[i]["local_anchor_a"] = (0.0, 0.0) if i == 0 else (0.0, -hx)
+        j[i]["local_anchor_b"] = (0.0, hx)
+    part["joints"] = j
+    return part
+
+
+def stress(piles=64, per_pile=2048, chains_per_pile=4, links=32, width=40.0, seed=5, gap=4.0):
+    """Large-island stress world: `piles` separate containers (width x tall enough for the grid)
+    side by side, each filled with `per_pile` mixed circles / polygons drawn as in scatter (they
+    fall into one pile, one large island per container), and `chains_per_pile` revolute-joint
+    chains of `links` 0.25 x 0.05 m box links hanging from static posts over each container into
+    its pile.  The default sizes are 64 piles x 2,048 bodies and 256 chains x 32 links."""
+    rng = np.random.default_rng(seed)
+    parts = []
+    for k in range(piles):
+        pile = scatter(per_pile, width, 0.0, rng)
+        height = float(pile["bodies"]["position"][:, 1].max()) + 2.0
+        dx = k * (width + 2.0 + gap)
+        pile["bodies"]["position"][:, 0] += F32(dx)
+        parts.append(pile)
+        for c in range(chains_per_pile):
+            x = dx - width / 2.0 + width * (c + 1) / (chains_per_pile + 1)
+            parts.append(_hanging_chain(x, height + 2.0 * 0.125 * links + 1.0, links))
+    out = _concat(parts)
+    out["name"] = "stress%dx%d" % (piles, per_pile)
+    return out
+
+
 def batch(n_worlds=4096, seed=3, lo=8, hi=512):
     """Batched workload: per-world body counts log-uniform in [lo, hi]; thirds of
     pyramids, 40 m-container scatters and box stacks."""

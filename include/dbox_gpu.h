@@ -388,6 +388,56 @@ int32_t dbox_world_set_gravity(dbox_world* w, dbox_vec2 gravity);
  * in reference order, at the end of each step.  fn = NULL removes the listener. */
 int32_t dbox_world_set_listener(dbox_world* w, dbox_event_fn fn, void* user);
 
+/* b2Fixture.SetFilterData (dynamics/b2fixture.d:132-137): new category, mask and group bits, then
+ * b2Fixture.Refilter (:140-180): the fixture's contacts are flagged so that the next Collide
+ * checks b2ContactFilter.ShouldCollide again (and destroys those that fail), and its proxies go
+ * into the move buffer so that the next FindNewContacts may create new pairs.  Between steps. */
+int32_t dbox_fixture_set_filter(dbox_world* w, int32_t world, int32_t fixture, uint16_t category_bits,
+                                uint16_t mask_bits, int16_t group_index);
+/* b2World.SetContactFilter (dynamics/b2world.d:52-55) with a user b2ContactFilter
+ * (b2worldcallbacks.d:47-64) given as data, since ShouldCollide is called on the device (in
+ * AddPair, b2contactmanager.d:52-176, and in Collide for flagged contacts, :266-288): every
+ * fixture has a filter class 0..63 (0 unless set), and fixtures of classes a and b may collide
+ * when bit b of table[a] is set (table: 64 rows, symmetric, else DBOX_ERR_INVALID).  With
+ * with_default != 0 the reference's default rule (groups, categories and masks) must pass too, as
+ * in a subclass that calls the base class first; with 0 the table alone decides.  table = NULL
+ * restores the default filter.  As in the reference, existing contacts are checked again only
+ * once flagged (dbox_fixture_set_filter / _class, or joint creation and destruction).
+ * dbox_fixture_set_filter_class sets a fixture's class (a chain's children together) and
+ * refilters it as dbox_fixture_set_filter does. */
+int32_t dbox_world_set_contact_filter(dbox_world* w, int32_t world, const uint64_t* table, int32_t with_default);
+int32_t dbox_fixture_set_filter_class(dbox_world* w, int32_t world, int32_t fixture, int32_t filter_class);
+
+/* One b2ContactListener.PreSolve call (dynamics/b2worldcallbacks.d:101-115), made by
+ * b2Contact.Update (contacts/b2contact.d:354) for a touching, non-sensor contact during the
+ * step's Collide.  `contact` is the contact after its update (fixtures as world-local indices,
+ * flags, the new manifold with its warm-start impulses); the old manifold is not passed.  The
+ * callback may change the four edit fields, as b2Contact.SetEnabled / SetFriction /
+ * SetRestitution / SetTangentSpeed (contacts/b2contact.d:105-190) would: `enabled` 0 disables
+ * the contact for this step, the other three persist until changed again. */
+typedef struct {
+    int32_t world;
+    int32_t enabled;               /* in: 1; out: 0 = SetEnabled(false) */
+    float friction;                /* in: the contact's friction; out: SetFriction */
+    float restitution;             /* in / out: SetRestitution */
+    float tangent_speed;           /* in / out: SetTangentSpeed */
+    dbox_contact_state contact;    /* read only */
+} dbox_presolve_contact;
+typedef void (*dbox_presolve_fn)(dbox_presolve_contact* contacts, int32_t count, void* user);
+
+/* b2World.SetContactListener with a PreSolve callback (b2world.d:59-62): while fn is set,
+ * every step stops after Collide, hands fn the step's PreSolve calls of all worlds (world by
+ * world, each in the reference's order: the contact list walked newest first), applies the
+ * edits fn made, then runs the solve.  The edits take effect exactly as in the reference, since
+ * a PreSolve edit only touches its own contact and nothing later in Collide reads it.  One
+ * difference: b2World.SolveTOI also calls b2Contact.Update (and PreSolve) on the contacts of
+ * its sub-steps; there the library keeps the window's decision (a contact disabled in the
+ * window stays disabled through the step's sub-steps) and reports those calls only as
+ * recorded PRESOLVE events to the listener of dbox_world_set_listener.  fn = NULL removes it.
+ * The window costs one device synchronisation and a download of the affected worlds'
+ * contacts per step. */
+int32_t dbox_world_set_presolve(dbox_world* w, dbox_presolve_fn fn, void* user);
+
 /* b2World.Step(dt, velocityIterations, positionIterations) (b2world.d:367-434),
  * applied to every world of the handle.  Inputs and outputs stay on the device. */
 int32_t dbox_world_step(dbox_world* w, float dt, int32_t velocity_iterations, int32_t position_iterations);
@@ -561,10 +611,22 @@ int32_t dbox_mlp_train_world(dbox_mlp* m, dbox_world* w, int32_t epochs, int32_t
                              float* epoch_loss);                          /* on the world's logged samples */
 int32_t dbox_mlp_forward(dbox_mlp* m, int32_t n, const float* feats, float* out);   /* out: n x 4 impulses */
 /* mode 0 plain; 1 plain + log up to sample_capacity samples on the device; 2 learned start
- * with `model` (kept by the caller while the mode is on).  In mode 2 the first velocity
- * iteration keeps, per contact, the start (predicted or zero) whose first correction is
- * smaller.  Modes 1 and 2 set contact flags 0x40 / 0x80 (point 0 / 1 new this step). */
+ * with `model` (kept by the caller while the mode is on); 3 given start: new points start from
+ * the impulses of the same contact slot in the handle named by dbox_world_set_start_source
+ * (for measuring what a perfect prediction would give: that handle steps the same state with
+ * more iterations first).  In mode 2 the first velocity iteration keeps, per contact, the
+ * start (predicted or zero) whose first correction is smaller.  Modes 1 to 3 set contact flags
+ * 0x40 / 0x80 (point 0 / 1 new this step). */
 int32_t dbox_world_set_warmstart(dbox_world* w, int32_t mode, dbox_mlp* model, int32_t sample_capacity);
+/* Mode 3's source: a handle of the same worlds, laid out the same way (created from the same
+ * scenes and sizing hints, no edits since); read during each step of w.  No counterpart in
+ * the reference. */
+int32_t dbox_world_set_start_source(dbox_world* w, dbox_world* src);
+/* Exact copy of the simulation state of src into dst, device to device (bodies, proxies,
+ * contacts with their warm-start impulses, joints, the pair table): the checkpoint of
+ * dbox_world_export_state / import_state without a host round trip, for handles of the same
+ * worlds laid out the same way.  No counterpart in the reference. */
+int32_t dbox_world_copy_state(dbox_world* dst, dbox_world* src);
 int32_t dbox_world_sample_count(dbox_world* w, int32_t* count);
 int32_t dbox_world_get_samples(dbox_world* w, int32_t offset, int32_t n, float* rows);  /* n x 36 */
 int32_t dbox_world_clear_samples(dbox_world* w);
@@ -599,6 +661,13 @@ int32_t dbox_world_get_world_costs(dbox_world* w, float* out);
  * for a queue mapping (queue = 1). */
 int32_t dbox_world_autotune(dbox_world* w, float dt, int32_t velocity_iterations, int32_t position_iterations,
                             int32_t steps, int32_t* choice);
+
+/* Budget of one bounded device wait (no counterpart in the reference): the solve kernel waits
+ * on an mbarrier for each block of constraint rows it copies into shared memory; a wait that
+ * takes more than `polls` polls (default and maximum 2^20) makes the step return
+ * DBOX_ERR_TIMEOUT.  The wait itself goes on until the copy has landed (up to 2^20 polls), so the
+ * step's results are unaffected; a lower budget lets a caller check its handling of the error. */
+int32_t dbox_world_set_wait_limit(dbox_world* w, int32_t polls);
 
 /* Device kernels launched by the last step (for launch accounting). */
 int32_t dbox_world_last_launches(dbox_world* w, int32_t* out);

@@ -74,6 +74,10 @@ def lib():
         L.orc_world_event_count.argtypes = [vp]
         L.orc_world_get_events.argtypes = [vp, vp, i32]
         L.orc_world_clear_events.argtypes = [vp]
+        L.orc_world_set_presolve.argtypes = [vp, vp, vp]
+        L.orc_fixture_set_filter.argtypes = [vp, i32, i32, i32, i32]
+        L.orc_fixture_set_filter_class.argtypes = [vp, i32, i32]
+        L.orc_world_set_contact_filter.argtypes = [vp, vp, i32]
         L.orc_world_last_toi_events.argtypes = [vp]
         L.orc_world_last_islands.argtypes = [vp]
         L.orc_set_trig_mode.argtypes = [i32]
@@ -180,6 +184,38 @@ class OracleWorld:
         if clear:
             lib().orc_world_clear_events(self.h)
         return out
+
+    def set_filter(self, fixture, category_bits=0x0001, mask_bits=0xFFFF, group_index=0):
+        """b2Fixture.SetFilterData (and Refilter)."""
+        if lib().orc_fixture_set_filter(self.h, fixture, category_bits, mask_bits, group_index) < 0:
+            raise ValueError("oracle: no fixture %d" % fixture)
+
+    def set_filter_class(self, fixture, cls):
+        if lib().orc_fixture_set_filter_class(self.h, fixture, cls) < 0:
+            raise ValueError("oracle: no fixture %d" % fixture)
+
+    def set_contact_filter(self, table=None, with_default=True):
+        """b2World.SetContactFilter with a user filter over a class table (None: the default)."""
+        t = None if table is None else np.ascontiguousarray(table, np.uint64)
+        lib().orc_world_set_contact_filter(self.h, abi.ptr(t) if t is not None else None, 1 if with_default else 0)
+
+    _PRESOLVE_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p)
+
+    def set_presolve(self, fn):
+        """A user b2ContactListener.PreSolve: fn(records) with one abi.PRESOLVE_CONTACT record per
+        call, made inside Collide and SolveTOI as the reference makes it; in-place edits of
+        "enabled", "friction", "restitution" and "tangent_speed" are applied to the contact."""
+        if fn is None:
+            self._presolve = None
+            lib().orc_world_set_presolve(self.h, None, None)
+            return
+
+        def tramp(ptr, count, user):
+            buf = (ctypes.c_char * (count * abi.PRESOLVE_CONTACT.itemsize)).from_address(ptr)
+            fn(np.frombuffer(buf, abi.PRESOLVE_CONTACT))
+
+        self._presolve = OracleWorld._PRESOLVE_FN(tramp)
+        lib().orc_world_set_presolve(self.h, ctypes.cast(self._presolve, ctypes.c_void_p), None)
 
     def last_toi_events(self):
         return lib().orc_world_last_toi_events(self.h)

@@ -1913,6 +1913,7 @@ struct Fixture {                                                        // dynam
     bool isSensor = false;
     int index = 0;   // creation order (for export)
     int chain = -1;  // the b2ChainShape this child edge belongs to (World::chains), or -1
+    int fclass = 0;  // user data a table contact filter reads (stands in for b2Fixture.m_userData)
 };
 
 enum { kStaticBody = 0, kKinematicBody = 1, kDynamicBody = 2 };
@@ -2013,7 +2014,12 @@ struct Contact {
 // Recording listener: stands in for a user b2ContactListener (b2worldcallbacks.d:87-128).
 struct Listener {
     std::vector<dbox_contact_event> events;
+    bool record = false;                 // keep the events
+    dbox_presolve_fn presolve = nullptr; // a user's PreSolve, called with one record per call
+    void* presolve_user = nullptr;
+    bool inToi = false;                  // calls made by SolveTOI's sub-step updates
     void Push(int kind, const Contact* c, int pointCount, const f32* ni, const f32* ti) {
+        if (!record) return;
         dbox_contact_event e;
         memset(&e, 0, sizeof(e));
         e.kind = kind;
@@ -2028,9 +2034,54 @@ struct Listener {
     }
     void BeginContact(Contact* c) { Push(DBOX_EVENT_BEGIN, c, c->manifold.pointCount, nullptr, nullptr); }
     void EndContact(Contact* c) { Push(DBOX_EVENT_END, c, c->manifold.pointCount, nullptr, nullptr); }
-    void PreSolve(Contact* c, const Manifold*) { Push(DBOX_EVENT_PRESOLVE, c, c->manifold.pointCount, nullptr, nullptr); }
+    void PreSolve(Contact* c, const Manifold*);
     void PostSolve(Contact* c, int count, const f32* ni, const f32* ti) { Push(DBOX_EVENT_POSTSOLVE, c, count, ni, ti); }
 };
+
+void FillContactState(const Contact* c, dbox_contact_state* o) {
+    memset(o, 0, sizeof(*o));
+    o->fixture_a = c->fixtureA->index;
+    o->fixture_b = c->fixtureB->index;
+    o->flags = c->flags;
+    o->toi_count = c->toiCount;
+    o->toi = c->toi;
+    o->friction = c->friction;
+    o->restitution = c->restitution;
+    o->tangent_speed = c->tangentSpeed;
+    o->point_count = c->manifold.pointCount;
+    o->type = c->manifold.type;
+    o->local_normal[0] = c->manifold.localNormal.x; o->local_normal[1] = c->manifold.localNormal.y;
+    o->local_point[0] = c->manifold.localPoint.x; o->local_point[1] = c->manifold.localPoint.y;
+    for (int k = 0; k < c->manifold.pointCount; ++k) {
+        const ManifoldPoint& mp = c->manifold.points[k];
+        o->points[k].local_point[0] = mp.localPoint.x;
+        o->points[k].local_point[1] = mp.localPoint.y;
+        o->points[k].normal_impulse = mp.normalImpulse;
+        o->points[k].tangent_impulse = mp.tangentImpulse;
+        o->points[k].id = mp.id.key;
+    }
+}
+
+
+// b2ContactListener.PreSolve (b2worldcallbacks.d:101-115): the user's callback may call
+// SetEnabled / SetFriction / SetRestitution / SetTangentSpeed (contacts/b2contact.d:105-190)
+void Listener::PreSolve(Contact* c, const Manifold*) {
+    Push(DBOX_EVENT_PRESOLVE, c, c->manifold.pointCount, nullptr, nullptr);
+    if (!presolve) return;
+    dbox_presolve_contact r;
+    memset(&r, 0, sizeof(r));
+    r.world = inToi ? -1 : 0;            // test aid: -1 marks a call from SolveTOI
+    r.enabled = c->IsEnabled() ? 1 : 0;
+    r.friction = c->friction;
+    r.restitution = c->restitution;
+    r.tangent_speed = c->tangentSpeed;
+    FillContactState(c, &r.contact);
+    presolve(&r, 1, presolve_user);
+    c->SetEnabled(r.enabled != 0);
+    c->friction = r.friction;
+    c->restitution = r.restitution;
+    c->tangentSpeed = r.tangent_speed;
+}
 
 // b2contact.d:32-42
 static inline f32 MixFriction(f32 f1, f32 f2) { return sqrtf(f1 * f2); }
@@ -4201,11 +4252,32 @@ struct BroadPhase {                                                     // colli
     void UpdatePairs(ContactManager* cm);                               // b2broadphase.d:139-195
 };
 
+static bool FilterShouldCollide(const Fixture* fixtureA, const Fixture* fixtureB);
+
+// b2ContactFilter (b2worldcallbacks.d:47-64): the default rule, which a user subclass overrides
+struct ContactFilter {
+    virtual ~ContactFilter() {}
+    virtual bool ShouldCollide(Fixture* a, Fixture* b) { return FilterShouldCollide(a, b); }
+};
+
+// A user's b2ContactFilter: fixtures of classes a and b collide when bit b of row a is set,
+// optionally together with the default rule (a subclass calling the base class first)
+struct TableFilter : ContactFilter {
+    uint64_t table[64] = {};
+    bool withDefault = true;
+    bool ShouldCollide(Fixture* a, Fixture* b) override {
+        const bool t = ((table[a->fclass & 63] >> (b->fclass & 63)) & 1u) != 0;
+        return withDefault ? (ContactFilter::ShouldCollide(a, b) && t) : t;
+    }
+};
+
 struct ContactManager {                                                 // dynamics/b2contactmanager.d
     BroadPhase broadPhase;
     Contact* contactList = nullptr;
     int contactCount = 0;
     Listener* listener = nullptr;
+    ContactFilter defaultFilter;                                        // b2_defaultFilter
+    ContactFilter* filter = &defaultFilter;                              // b2World.SetContactFilter
 
     void AddPair(void* proxyUserDataA, void* proxyUserDataB);
     void FindNewContacts() { broadPhase.UpdatePairs(this); }
@@ -4272,7 +4344,7 @@ void ContactManager::AddPair(void* proxyUserDataA, void* proxyUserDataB) {
         }
     }
     if (bodyB->ShouldCollide(bodyA) == false) return;
-    if (FilterShouldCollide(fixtureA, fixtureB) == false) return;
+    if (filter->ShouldCollide(fixtureA, fixtureB) == false) return;
     // Contact.Create: the registry's primary order is (circle, circle), (polygon, circle),
     // (polygon, polygon), (edge, circle), (edge, polygon); edges do not collide with edges
     int type1 = fixtureA->shape.type;
@@ -4356,7 +4428,7 @@ void ContactManager::Collide() {                                        // b2con
             if (bodyB->ShouldCollide(bodyA) == false) {
                 Contact* cNuke = c; c = cNuke->next; Destroy(cNuke); continue;
             }
-            if (FilterShouldCollide(fixtureA, fixtureB) == false) {
+            if (filter->ShouldCollide(fixtureA, fixtureB) == false) {
                 Contact* cNuke = c; c = cNuke->next; Destroy(cNuke); continue;
             }
             c->flags &= ~kContactFilter;
@@ -4782,6 +4854,23 @@ struct World {                                                          // dynam
     }
 
     // The fixtures that are one reference fixture: a chain's child edges, else the fixture.
+    TableFilter tableFilter;
+
+    // b2Fixture.Refilter (b2fixture.d:140-180): flag the fixture's contacts for filtering and
+    // touch its proxies (a chain's children, as the chain fixture's proxies)
+    void Refilter(Fixture* f) {
+        for (ContactEdge* e = f->body->contactList; e; e = e->next) {
+            Contact* c = e->contact;
+            if (c->fixtureA == f || c->fixtureB == f) c->flags |= kContactFilter;
+        }
+        for (Fixture* g : FixtureGroup(f)) {
+            if (g != f)
+                for (ContactEdge* e = g->body->contactList; e; e = e->next)
+                    if (e->contact->fixtureA == g || e->contact->fixtureB == g) e->contact->flags |= kContactFilter;
+            if (g->proxy.proxyId >= 0) contactManager.broadPhase.BufferMove(g->proxy.proxyId);
+        }
+    }
+
     std::vector<Fixture*> FixtureGroup(Fixture* f) {
         std::vector<Fixture*> g;
         if (f->chain < 0) {
@@ -4863,7 +4952,8 @@ struct World {                                                          // dynam
     }
 
     void Step(f32 dt, int velocityIterations, int positionIterations) { // b2world.d:367-434
-        contactManager.listener = recording ? &recorder : nullptr;
+        recorder.record = recording;
+        contactManager.listener = (recording || recorder.presolve) ? &recorder : nullptr;
         lastToiEvents = 0;
         lastIslands = 0;
         if (flags & kNewFixture) {
@@ -4880,7 +4970,11 @@ struct World {                                                          // dynam
         step.warmStarting = warmStarting;
         contactManager.Collide();
         if (stepComplete && step.dt > 0.0f) Solve(step);
-        if (continuousPhysics && step.dt > 0.0f) SolveTOI(step);
+        if (continuousPhysics && step.dt > 0.0f) {
+            recorder.inToi = true;
+            SolveTOI(step);
+            recorder.inToi = false;
+        }
         if (step.dt > 0.0f) inv_dt0 = step.inv_dt;
         if (flags & kClearForces) {
             for (Body* b = bodyList; b; b = b->next) { b->force.SetZero(); b->torque = 0.0f; }
@@ -5844,9 +5938,46 @@ void orc_world_step_n(orc_world* w, float dt, int vel_iters, int pos_iters, int 
     for (int i = 0; i < steps; ++i) w->w.Step(dt, vel_iters, pos_iters);
 }
 
+int orc_fixture_set_filter(orc_world* w, int fixture, int category, int mask, int group) {   // b2fixture.d:132-137
+    if (fixture < 0 || fixture >= (int)w->w.fixturesByIndex.size() || !w->w.fixturesByIndex[fixture]) return -1;
+    Fixture* f = w->w.fixturesByIndex[fixture];
+    for (Fixture* g : w->w.FixtureGroup(f)) {
+        g->filter.categoryBits = (uint16_t)category;
+        g->filter.maskBits = (uint16_t)mask;
+        g->filter.groupIndex = (int16_t)group;
+    }
+    w->w.Refilter(f);
+    return 0;
+}
+
+int orc_fixture_set_filter_class(orc_world* w, int fixture, int cls) {
+    if (fixture < 0 || fixture >= (int)w->w.fixturesByIndex.size() || !w->w.fixturesByIndex[fixture]) return -1;
+    Fixture* f = w->w.fixturesByIndex[fixture];
+    for (Fixture* g : w->w.FixtureGroup(f)) g->fclass = cls;
+    w->w.Refilter(f);
+    return 0;
+}
+
+void orc_world_set_contact_filter(orc_world* w, const uint64_t* table, int with_default) {   // b2world.d:52-55
+    if (!table) {
+        w->w.contactManager.filter = &w->w.contactManager.defaultFilter;
+        return;
+    }
+    memcpy(w->w.tableFilter.table, table, sizeof(w->w.tableFilter.table));
+    w->w.tableFilter.withDefault = with_default != 0;
+    w->w.contactManager.filter = &w->w.tableFilter;
+}
+
+void orc_world_set_presolve(orc_world* w, dbox_presolve_fn fn, void* user) {
+    w->w.recorder.presolve = fn;
+    w->w.recorder.presolve_user = user;
+    w->w.contactManager.listener = (w->w.recording || fn) ? &w->w.recorder : nullptr;
+}
+
 void orc_world_record_events(orc_world* w, int enable) {               // the listener for steps and destruction
     w->w.recording = enable != 0;
-    w->w.contactManager.listener = w->w.recording ? &w->w.recorder : nullptr;
+    w->w.recorder.record = w->w.recording;
+    w->w.contactManager.listener = (w->w.recording || w->w.recorder.presolve) ? &w->w.recorder : nullptr;
 }
 int orc_world_event_count(orc_world* w) { return (int)w->w.recorder.events.size(); }
 int orc_world_get_events(orc_world* w, dbox_contact_event* out, int cap) {
@@ -5916,33 +6047,8 @@ int orc_world_export_state(orc_world* w, dbox_world_header* header, dbox_body_st
             }
         }
     }
-    if (contacts) {
-        for (size_t i = 0; i < cs.size(); ++i) {
-            const Contact* c = cs[i];
-            dbox_contact_state* o = contacts + i;
-            memset(o, 0, sizeof(*o));
-            o->fixture_a = c->fixtureA->index;
-            o->fixture_b = c->fixtureB->index;
-            o->flags = c->flags;
-            o->toi_count = c->toiCount;
-            o->toi = c->toi;
-            o->friction = c->friction;
-            o->restitution = c->restitution;
-            o->tangent_speed = c->tangentSpeed;
-            o->point_count = c->manifold.pointCount;
-            o->type = c->manifold.type;
-            o->local_normal[0] = c->manifold.localNormal.x; o->local_normal[1] = c->manifold.localNormal.y;
-            o->local_point[0] = c->manifold.localPoint.x; o->local_point[1] = c->manifold.localPoint.y;
-            for (int k = 0; k < c->manifold.pointCount; ++k) {
-                const ManifoldPoint& mp = c->manifold.points[k];
-                o->points[k].local_point[0] = mp.localPoint.x;
-                o->points[k].local_point[1] = mp.localPoint.y;
-                o->points[k].normal_impulse = mp.normalImpulse;
-                o->points[k].tangent_impulse = mp.tangentImpulse;
-                o->points[k].id = mp.id.key;
-            }
-        }
-    }
+    if (contacts)
+        for (size_t i = 0; i < cs.size(); ++i) FillContactState(cs[i], contacts + i);
     if (joints) {
         for (size_t i = 0; i < W.jointsByIndex.size(); ++i) {
             const Joint* j = W.jointsByIndex[i];

@@ -69,6 +69,16 @@ void orc_world_record_events(orc_world* w, int enable);
 int orc_world_event_count(orc_world* w);
 int orc_world_get_events(orc_world* w, dbox_contact_event* out, int cap);
 void orc_world_clear_events(orc_world* w);
+/* a user PreSolve (b2ContactListener.PreSolve) called with one record per call, inside Collide
+ * and SolveTOI as the reference calls it; its edits are applied to the contact.  The record's
+ * world is 0 for a call from Collide and -1 for one from SolveTOI's sub-step updates. */
+void orc_world_set_presolve(orc_world* w, dbox_presolve_fn fn, void* user);
+/* b2Fixture.SetFilterData + Refilter; a user b2ContactFilter over a class table (the
+ * fixture's class stands in for the user data such a filter reads), optionally with the
+ * default rule; table NULL restores b2_defaultFilter */
+int orc_fixture_set_filter(orc_world* w, int fixture, int category, int mask, int group);
+int orc_fixture_set_filter_class(orc_world* w, int fixture, int cls);
+void orc_world_set_contact_filter(orc_world* w, const uint64_t* table, int with_default);
 
 int orc_world_export_state(orc_world* w, dbox_world_header* header, dbox_body_state* bodies,
                            dbox_proxy_state* proxies, dbox_contact_state* contacts, dbox_joint_state* joints);

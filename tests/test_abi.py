@@ -79,3 +79,4 @@ def test_invalid_arguments_rejected_without_device(gpu_lib):
     assert L.dbox_world_create(abi.Vec2(0.0, -10.0), 0, None, ctypes.byref(out)) == -1
     assert L.dbox_world_destroy(None) == -1
     assert L.dbox_world_step(None, ctypes.c_float(0.016), 8, 3) == -1
+    assert L.dbox_world_set_wait_limit(None, 0) == -1

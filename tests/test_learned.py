@@ -90,3 +90,50 @@ def test_trained_start_lowers_the_residual(gpu_lib):
     learned_max, learned_rms = measure(2, m)
     assert learned_max < plain_max
     assert learned_rms <= 1.02 * plain_rms
+
+
+def test_copy_state_is_an_exact_checkpoint(oracle_lib, gpu_lib):
+    # dbox_world_copy_state: a twin handle continues exactly where the source stood
+    from compare import exact_diff
+    oracle_lib.set_trig_mode(1)
+    worlds = _scatter(6, 120, 25) + [scenes.pyramid(rows=9), scenes.chains(n_chains=2, links=8)]
+    a = gpu_lib.World(worlds)
+    b = gpu_lib.World(worlds)
+    b.step()                                            # both on the device, b one step apart
+    a.step(steps=40, graph=True)
+    b.copy_state_from(a)
+    a.step(steps=25)
+    b.step(steps=25, graph=True)
+    ows = [oracle_lib.OracleWorld(s) for s in worlds]
+    for i, ow in enumerate(ows):
+        ow.step(steps=65)
+        assert not exact_diff(ow.export_state(), b.export_state(i)), i
+        assert not exact_diff(a.export_state(i), b.export_state(i)), i
+
+
+def test_given_start_slots_line_up(gpu_lib):
+    # warm-start mode 3 reads the start of each new point from the source handle's contact at
+    # the same slot.  With no velocity iterations on the source, its impulses at those slots
+    # after its step are the reference's zero start, so the given-start step is the plain one
+    from compare import exact_diff
+    worlds = _scatter(32, 160, 26)
+    plain = gpu_lib.World(worlds)
+    given = gpu_lib.World(worlds)
+    src = gpu_lib.World(worlds)
+    for h in (plain, given, src):
+        h.step(steps=60, graph=True)
+    given.set_warmstart(3)
+    given.set_start_source(src)
+    for _ in range(10):
+        src.copy_state_from(given)
+        src.step(vel_iters=0)
+        given.step(vel_iters=0)
+        plain.step(vel_iters=0)
+    for i in range(len(worlds)):
+        assert not exact_diff(plain.export_state(i), given.export_state(i)), i
+    # with iterations on the source the given start changes the step (new points start elsewhere)
+    src.copy_state_from(given)
+    src.step(vel_iters=8)
+    given.step(vel_iters=4)
+    plain.step(vel_iters=4)
+    assert any(exact_diff(plain.export_state(i), given.export_state(i)) for i in range(len(worlds)))
