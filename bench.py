@@ -555,6 +555,9 @@ def learned_leg(args):
                   "samples from %d plain steps, evaluation on new-seed worlds after 100 steps, 30 steps"
                   % (args.learned_worlds, PI, args.learned_log_steps),
         "samples": n, "log_seconds": t_log, "train_seconds": t_train,
+        # forward 2 (32*128 + 128*128 + 128*4) FLOP per sample, training about 3x that
+        "train_tflops": 3 * 41984 * n * 20 / t_train / 1e12,
+        "train_kernel": "k_mlp_train: tcgen05.mma (bf16 in shared memory, f32 accumulators in tensor memory)",
         "loss_first_epoch": float(losses[0]), "loss_last_epoch": float(losses[-1]),
         "runs": res,
         "speedup_learned_5_vs_plain_8": l5["body_steps_per_s"] / p8["body_steps_per_s"],
@@ -602,7 +605,12 @@ def main():
     out, worlds = gpu_leg(args, rank, world_size)
     if rank == 0:
         if world_size == 1 and not args.no_learned:
-            out["learned_warmstart"] = learned_leg(args)
+            out["learned_warmstart"] = lw = learned_leg(args)
+            pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+            bf = json.load(open(pk)).get("bf16_tflops") if os.path.exists(pk) else None
+            lw["train_tflops_peak"] = bf or 1900.0
+            lw["train_tflops_peak_source"] = "measured (MEASURED_PEAKS.json bf16_tflops)" if bf else "fallback 1900"
+            lw["train_tflops_frac"] = lw["train_tflops"] / lw["train_tflops_peak"]
         if world_size == 1 and not args.no_cpu:
             rate, cores, sample = cpu_leg(args, worlds)
             out["cpu_baseline"] = {"value": rate, "unit": "body-steps/s", "cores": cores, "kind": "port",

@@ -12,6 +12,7 @@
 #include <vector>
 #include <algorithm>
 #include "mlp.cuh"
+#include "tc.cuh"
 #include "../../include/dbox_gpu.h"
 
 static_assert(dg::kNParams == DBOX_MLP_PARAMS && dg::kSampleFloats == DBOX_MLP_SAMPLE, "header sizes");
@@ -20,221 +21,319 @@ extern "C" int dbox_set_error(int code, const char* msg);
 
 namespace dg {
 
-constexpr int kTrainWarps = 4;
-// per warp: X 16x32, pre1/h1/pre2/h2/d2/d1 16x128 each, dY 16x16 (bf16)
-constexpr int kTileX = 16 * kFeat, kTileH = 16 * kHid, kTileY = 16 * 16;
-constexpr int kWarpTrainElems = kTileX + 6 * kTileH + kTileY;
+// ---------------------------------------------------------------- training on tcgen05
+// One CTA (8 warps) per SM takes 128-sample tiles in turn.  Per tile, one thread issues the
+// tensor-core MMAs of the forward and backward passes (accumulators in tensor memory,
+// operands in shared memory), the warps run the epilogues (bias, GELU, loss, GELU
+// derivative) between them, and the weight and bias gradients stay in tensor memory across
+// all of the CTA's tiles; they leave the SM once, at the end.  Warp w and w + 4 read tensor
+// memory lanes 32 (w % 4) .. +31, i.e. the tile's samples (or, for the gradients, hidden
+// units) 32 (w % 4) .. +31, and split the columns between them.
+//
+//   forward   Z1 = X W1, H1 = gelu(Z1 + b1)            X: 128 x 32 (padded to 64), W1: 32 x 128
+//             Z2 = H1 W2, H2 = gelu(Z2 + b2)           W2: 128 x 128
+//             Y = H2 W3 + b3, dY = 2 (Y - T) / (4 n)   W3: 128 x 4 (padded to 16)
+//   backward  dW3 += H2^T dY, db3 += colsum dY
+//             dZ2 = (dY W3^T) * gelu'(P2),  dW2 += H1^T dZ2,  db2 += colsum dZ2
+//             dZ1 = (dZ2 W2^T) * gelu'(P1), dW1 += X^T dZ1,   db1 += colsum dZ1
+// The transposed operands are the same shared-memory tiles read MN-major (see tc.cuh); column
+// sums are MMAs against a tile of ones.
+constexpr int kTcThreads = 256;
+constexpr uint32_t kOffW1 = 0;          // W1^T [128 hidden][64] (features 32..63 zero)      16 KB
+constexpr uint32_t kOffW2 = 16384;      // W2^T [128 out][128 in]                             32 KB
+constexpr uint32_t kOffW3 = 49152;      // W3^T [16 out][128 hidden] (rows 4..15 zero)         4 KB
+constexpr uint32_t kOffOnes = 53248;    // [16][128] ones                                      4 KB
+constexpr uint32_t kOffX = 57344;       // X [128 samples][64] (features 32..63 zero)         16 KB
+constexpr uint32_t kOffH1 = 73728;      // H1 [128][128], then dZ1                            32 KB
+constexpr uint32_t kOffH2 = 106496;     // H2 [128][128], then dZ2                            32 KB
+constexpr uint32_t kOffDY = 139264;     // dY [128][64] (columns 4..63 zero)                  16 KB
+constexpr uint32_t kOffP1 = 155648;     // P1 = Z1 + b1 (bf16, 272-byte rows)                 34 KB
+constexpr uint32_t kOffP2 = 190464;     // P2 = Z2 + b2                                       34 KB
+constexpr uint32_t kPRow = 272;
+constexpr uint32_t kTcSmemBytes = 225280 + 1024;   // + slack to align the base to 1024 bytes
+// tensor-memory columns
+constexpr uint32_t kTZ = 0, kTdW2 = 128, kTdW3 = 256, kTdW1 = 320, kTY = 384, kTdb2 = 400, kTdb1 = 416;
+constexpr uint32_t kTCols = 512;
 
-__device__ __forceinline__ float bf(const __nv_bfloat16* s, int i) { return __bfloat162float(s[i]); }
-
-// A fragment of the transpose of a row-major [K rows x M cols] tile: A[m][k] = s[k][m]
-__device__ __forceinline__ void load_a_trans(uint32_t a[4], const __nv_bfloat16* s, int ld, int m0, int k0, int lane) {
-    const int g = lane >> 2, t = lane & 3;
-    auto e = [&](int m, int k) { return s[(k0 + k) * ld + m0 + m]; };
-    a[0] = pack_raw(e(g, 2 * t), e(g, 2 * t + 1));
-    a[1] = pack_raw(e(g + 8, 2 * t), e(g + 8, 2 * t + 1));
-    a[2] = pack_raw(e(g, 2 * t + 8), e(g, 2 * t + 9));
-    a[3] = pack_raw(e(g + 8, 2 * t + 8), e(g + 8, 2 * t + 9));
+__device__ __forceinline__ void gelu_both(float x, float& h, float& g) {
+    const float k0 = 0.7978845608028654f, k1 = 0.044715f;
+    float t = tanhf(k0 * (x + k1 * x * x * x));
+    h = 0.5f * x * (1.0f + t);
+    g = 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * k0 * (1.0f + 3.0f * k1 * x * x);
 }
-// B fragment of a row-major [K x N] tile: B[k][n] = s[k][n]
-__device__ __forceinline__ void load_b_rowmajor(uint32_t b[2], const __nv_bfloat16* s, int ld, int k0, int n0, int lane) {
-    const int g = lane >> 2, t = lane & 3;
-    b[0] = pack_raw(s[(k0 + 2 * t) * ld + n0 + g], s[(k0 + 2 * t + 1) * ld + n0 + g]);
-    b[1] = pack_raw(s[(k0 + 2 * t + 8) * ld + n0 + g], s[(k0 + 2 * t + 9) * ld + n0 + g]);
+// 16 bf16 values into row `row`, columns c0 .. c0 + 15 of a swizzled tile of 128 rows
+__device__ __forceinline__ void put16(uint8_t* tile, int row, int c0, const float* v) {
+    uint4 a, b;
+    a.x = pack_bf16x2(v[0], v[1]); a.y = pack_bf16x2(v[2], v[3]); a.z = pack_bf16x2(v[4], v[5]); a.w = pack_bf16x2(v[6], v[7]);
+    b.x = pack_bf16x2(v[8], v[9]); b.y = pack_bf16x2(v[10], v[11]); b.z = pack_bf16x2(v[12], v[13]); b.w = pack_bf16x2(v[14], v[15]);
+    *reinterpret_cast<uint4*>(tile + tc::sw128_offset(row, c0, 128)) = a;
+    *reinterpret_cast<uint4*>(tile + tc::sw128_offset(row, c0 + 8, 128)) = b;
 }
-
-// column sums of a C fragment over its 16 rows, added into g[col0 + 2t .. +1] by the lanes of row group 0
-__device__ __forceinline__ void add_colsum(float* g, int col0, const float c[4], int lane) {
-    float s0 = c[0] + c[2], s1 = c[1] + c[3];
+__device__ __forceinline__ void put16_rows(uint8_t* buf, int row, int c0, const float* v) {
+    uint4 a, b;
+    a.x = pack_bf16x2(v[0], v[1]); a.y = pack_bf16x2(v[2], v[3]); a.z = pack_bf16x2(v[4], v[5]); a.w = pack_bf16x2(v[6], v[7]);
+    b.x = pack_bf16x2(v[8], v[9]); b.y = pack_bf16x2(v[10], v[11]); b.z = pack_bf16x2(v[12], v[13]); b.w = pack_bf16x2(v[14], v[15]);
+    uint4* p = reinterpret_cast<uint4*>(buf + row * kPRow + c0 * 2);
+    p[0] = a;
+    p[1] = b;
+}
+__device__ __forceinline__ void get16_rows(const uint8_t* buf, int row, int c0, float* v) {
+    const __nv_bfloat16* p = reinterpret_cast<const __nv_bfloat16*>(buf + row * kPRow + c0 * 2);
 #pragma unroll
-    for (int o = 4; o < 32; o <<= 1) {
-        s0 += __shfl_xor_sync(0xffffffffu, s0, o);
-        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
-    }
-    if ((lane >> 2) == 0) {
-        atomicAdd(g + col0 + 2 * (lane & 3), s0);
-        atomicAdd(g + col0 + 2 * (lane & 3) + 1, s1);
-    }
+    for (int j = 0; j < 16; ++j) v[j] = __bfloat162float(p[j]);
 }
 
 // Forward + backward of MSE(MLP(x), t) / (n * 4) over the samples idx[0 .. n) of `rows`
 // (kSampleFloats per sample: features, then targets), normalised with the model's
 // statistics; gradients added into grad (kNParams), the sum of squared errors into *loss.
-__global__ void __launch_bounds__(kTrainWarps * 32) k_mlp_train(MlpDev m, float* grad, const float* rows,
-                                                                const int* idx, int n, float* loss) {
-    extern __shared__ __nv_bfloat16 sm_mlp[];
-    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int tile = blockIdx.x * kTrainWarps + wib;
-    const int r0 = tile * 16;
-    if (r0 >= n) return;
-    __nv_bfloat16* X = sm_mlp + wib * kWarpTrainElems;
-    __nv_bfloat16* P1 = X + kTileX;
-    __nv_bfloat16* H1 = P1 + kTileH;
-    __nv_bfloat16* P2 = H1 + kTileH;
-    __nv_bfloat16* H2 = P2 + kTileH;
-    __nv_bfloat16* D2 = H2 + kTileH;
-    __nv_bfloat16* D1 = D2 + kTileH;
-    __nv_bfloat16* DY = D1 + kTileH;
-    const int g = lane >> 2, t = lane & 3;
+// *status gets 1 if a wait for the tensor core ran past its bound.
+__global__ void __launch_bounds__(kTcThreads, 1) k_mlp_train(MlpDev m, float* grad, const float* rows, const int* idx,
+                                                             int n, float* loss, int* status) {
+    extern __shared__ uint8_t tc_smem_raw[];
+    uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(tc_smem_raw) + 1023) & ~uintptr_t(1023));
+    __shared__ uint64_t bar;
+    __shared__ uint32_t tbase;
+    __shared__ float s_db3[4], s_loss;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int quad = warp & 3, half = warp >> 2;
+    const int row = quad * 32 + lane;                    // sample (or hidden unit) of this thread's lane
+    const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
+    const int ntiles = (n + 127) / 128;
+    uint8_t* W1 = sm + kOffW1;
+    uint8_t* W2 = sm + kOffW2;
+    uint8_t* W3 = sm + kOffW3;
+    uint8_t* ONES = sm + kOffOnes;
+    uint8_t* X = sm + kOffX;
+    uint8_t* H1 = sm + kOffH1;
+    uint8_t* H2 = sm + kOffH2;
+    uint8_t* DY = sm + kOffDY;
+    uint8_t* P1 = sm + kOffP1;
+    uint8_t* P2 = sm + kOffP2;
     const float* b1 = m.p + kW1 + kW2 + kW3;
     const float* b2 = b1 + kHid;
     const float* b3 = b2 + kHid;
+    // weights and constant tiles (the zero padding of X and dY stays zero for every tile)
+    const __nv_bfloat16 zero = __float2bfloat16_rn(0.0f), one = __float2bfloat16_rn(1.0f);
+    for (int i = tid; i < 128 * 64; i += kTcThreads) {
+        const int r = i >> 6, c = i & 63;
+        *reinterpret_cast<__nv_bfloat16*>(W1 + tc::sw128_offset(r, c, 128)) = c < kFeat ? m.wt1[r * kFeat + c] : zero;
+        *reinterpret_cast<__nv_bfloat16*>(X + tc::sw128_offset(r, c, 128)) = zero;
+        *reinterpret_cast<__nv_bfloat16*>(DY + tc::sw128_offset(r, c, 128)) = zero;
+    }
+    for (int i = tid; i < 128 * 128; i += kTcThreads) {
+        const int r = i >> 7, c = i & 127;
+        *reinterpret_cast<__nv_bfloat16*>(W2 + tc::sw128_offset(r, c, 128)) = m.wt2[r * kHid + c];
+    }
+    for (int i = tid; i < 16 * 128; i += kTcThreads) {
+        const int r = i >> 7, c = i & 127;
+        *reinterpret_cast<__nv_bfloat16*>(W3 + tc::sw128_offset(r, c, 16)) = r < kOutPad ? m.wt3[r * kHid + c] : zero;
+        *reinterpret_cast<__nv_bfloat16*>(ONES + tc::sw128_offset(r, c, 16)) = one;
+    }
+    if (tid == 0) {
+        tc::mbar_init(&bar);
+        s_loss = 0.0f;
+        s_db3[0] = s_db3[1] = s_db3[2] = s_db3[3] = 0.0f;
+    }
+    if (warp == 0) tc::tmem_alloc(&tbase, kTCols);
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t T = tbase;
+    const uint32_t aX = tc::smem_addr(X), aH1 = tc::smem_addr(H1), aH2 = tc::smem_addr(H2), aDY = tc::smem_addr(DY);
+    const uint32_t aW1 = tc::smem_addr(W1), aW2 = tc::smem_addr(W2), aW3 = tc::smem_addr(W3), aON = tc::smem_addr(ONES);
+    constexpr uint32_t kKK128 = tc::idesc_bf16(128, 128, 0, 0), kKK16 = tc::idesc_bf16(128, 16, 0, 0);
+    constexpr uint32_t kKM128 = tc::idesc_bf16(128, 128, 0, 1), kMM128 = tc::idesc_bf16(128, 128, 1, 1);
+    constexpr uint32_t kMM64 = tc::idesc_bf16(128, 64, 1, 1), kMK16 = tc::idesc_bf16(128, 16, 1, 0);
+    uint32_t phase = 0;
+    bool ok = true;
+    auto wait_mma = [&]() {
+        ok &= tc::mbar_wait(&bar, phase, 1 << 24);
+        phase ^= 1u;
+        tc::fence_after_sync();
+    };
+    // shared-memory writes and tensor-memory reads of the epilogue done before the next MMAs
+    auto sync_for_mma = [&]() {
+        tc::fence_async_smem();
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+    };
+    const float inv = 1.0f / (4.0f * (float)n);
+    const int cbeg = half * 64;
+    float lsum = 0.0f, db3[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    bool first = true;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int r0 = tile * 128;
+        const bool valid = r0 + row < n;
+        const float* sample = valid ? rows + (size_t)idx[r0 + row] * kSampleFloats : nullptr;
+        {   // inputs: half 0 writes features 0..15 of its row, half 1 features 16..31
+            float v[16];
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const int f = half * 16 + j;
+                v[j] = valid ? (sample[f] - m.fmean[f]) / m.fstd[f] : 0.0f;
+            }
+            put16(X, row, half * 16, v);
+        }
+        sync_for_mma();
+        if (tid == 0) {                                   // Z1 = X W1 (K = 32)
+            for (int ks = 0; ks < 2; ++ks) tc::mma(T + kTZ, tc::desc_k(aX, ks, 16384), tc::desc_k(aW1, ks, 16384), kKK128, ks > 0);
+            tc::commit(&bar);
+        }
+        wait_mma();
+        for (int c0 = cbeg; c0 < cbeg + 64; c0 += 16) {  // H1 = gelu(Z1 + b1), P1
+            float z[16], h[16];
+            tc::ld16(T + lane_off + kTZ + c0, z);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                z[j] += b1[c0 + j];
+                h[j] = gelu_f(z[j]);
+            }
+            put16(H1, row, c0, h);
+            put16_rows(P1, row, c0, z);
+        }
+        sync_for_mma();
+        if (tid == 0) {                                   // Z2 = H1 W2
+            for (int ks = 0; ks < 8; ++ks) tc::mma(T + kTZ, tc::desc_k(aH1, ks, 16384), tc::desc_k(aW2, ks, 16384), kKK128, ks > 0);
+            tc::commit(&bar);
+        }
+        wait_mma();
+        for (int c0 = cbeg; c0 < cbeg + 64; c0 += 16) {  // H2 = gelu(Z2 + b2), P2
+            float z[16], h[16];
+            tc::ld16(T + lane_off + kTZ + c0, z);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                z[j] += b2[c0 + j];
+                h[j] = gelu_f(z[j]);
+            }
+            put16(H2, row, c0, h);
+            put16_rows(P2, row, c0, z);
+        }
+        sync_for_mma();
+        if (tid == 0) {                                   // Y = H2 W3 (N = 16)
+            for (int ks = 0; ks < 8; ++ks) tc::mma(T + kTY, tc::desc_k(aH2, ks, 16384), tc::desc_k(aW3, ks, 2048), kKK16, ks > 0);
+            tc::commit(&bar);
+        }
+        wait_mma();
+        if (half == 0) {                                  // loss and dY = 2 (Y + b3 - T) / (4 n)
+            float y[16];
+            tc::ld16(T + lane_off + kTY, y);
+            float d[4];
+#pragma unroll
+            for (int o = 0; o < kOut; ++o) {
+                d[o] = 0.0f;
+                if (valid) {
+                    const float tv = (sample[kFeat + o] - m.tmean[o]) / m.tstd[o];
+                    const float diff = y[o] + b3[o] - tv;
+                    lsum += diff * diff;
+                    d[o] = 2.0f * diff * inv;
+                }
+            }
+            uint2 q;
+            q.x = pack_bf16x2(d[0], d[1]);
+            q.y = pack_bf16x2(d[2], d[3]);
+            *reinterpret_cast<uint2*>(DY + tc::sw128_offset(row, 0, 128)) = q;
+#pragma unroll
+            for (int o = 0; o < kOut; ++o) db3[o] += d[o];
+        }
+        sync_for_mma();
+        if (tid == 0) {
+            // dW3 += H2^T dY (M = hidden, N = 64, K = samples); dH2 = dY W3^T (K = 16)
+            for (int ks = 0; ks < 8; ++ks)
+                tc::mma(T + kTdW3, tc::desc_mn(aH2, ks, 16384), tc::desc_mn(aDY, ks, 16384), kMM64, !first || ks > 0);
+            tc::mma(T + kTZ, tc::desc_k(aDY, 0, 16384), tc::desc_mn(aW3, 0, 2048), kKM128, false);
+            tc::commit(&bar);
+        }
+        wait_mma();
+        for (int c0 = cbeg; c0 < cbeg + 64; c0 += 16) {  // dZ2 = dH2 * gelu'(P2), over H2
+            float z[16], p[16];
+            tc::ld16(T + lane_off + kTZ + c0, z);
+            get16_rows(P2, row, c0, p);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) z[j] *= gelu_grad(p[j]);
+            put16(H2, row, c0, z);
+        }
+        sync_for_mma();
+        if (tid == 0) {
+            // dW2 += H1^T dZ2, db2 += dZ2^T 1, dH1 = dZ2 W2^T
+            for (int ks = 0; ks < 8; ++ks) {
+                tc::mma(T + kTdW2, tc::desc_mn(aH1, ks, 16384), tc::desc_mn(aH2, ks, 16384), kMM128, !first || ks > 0);
+                tc::mma(T + kTdb2, tc::desc_mn(aH2, ks, 16384), tc::desc_k(aON, ks, 2048), kMK16, !first || ks > 0);
+            }
+            for (int ks = 0; ks < 8; ++ks) tc::mma(T + kTZ, tc::desc_k(aH2, ks, 16384), tc::desc_mn(aW2, ks, 16384), kKM128, ks > 0);
+            tc::commit(&bar);
+        }
+        wait_mma();
+        for (int c0 = cbeg; c0 < cbeg + 64; c0 += 16) {  // dZ1 = dH1 * gelu'(P1), over H1
+            float z[16], p[16];
+            tc::ld16(T + lane_off + kTZ + c0, z);
+            get16_rows(P1, row, c0, p);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) z[j] *= gelu_grad(p[j]);
+            put16(H1, row, c0, z);
+        }
+        sync_for_mma();
+        if (tid == 0) {
+            // dW1^T += dZ1^T X (M = hidden, N = 64 features), db1 += dZ1^T 1
+            for (int ks = 0; ks < 8; ++ks) {
+                tc::mma(T + kTdW1, tc::desc_mn(aH1, ks, 16384), tc::desc_mn(aX, ks, 16384), kMM64, !first || ks > 0);
+                tc::mma(T + kTdb1, tc::desc_mn(aH1, ks, 16384), tc::desc_k(aON, ks, 2048), kMK16, !first || ks > 0);
+            }
+            tc::commit(&bar);
+        }
+        wait_mma();
+        first = false;
+        __syncthreads();                                  // the next tile rewrites X and the activations
+    }
+    // loss and db3: warp sums, then the block's
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+#pragma unroll
+        for (int q = 0; q < kOut; ++q) db3[q] += __shfl_xor_sync(0xffffffffu, db3[q], o);
+    }
+    if (lane == 0 && half == 0) {
+        atomicAdd(&s_loss, lsum);
+#pragma unroll
+        for (int q = 0; q < kOut; ++q) atomicAdd(&s_db3[q], db3[q]);
+    }
+    // the CTA's gradients: this thread's lane is hidden unit `row`
     float* gw1 = grad;
     float* gw2 = gw1 + kW1;
     float* gw3 = gw2 + kW2;
     float* gb1 = gw3 + kW3;
     float* gb2 = gb1 + kHid;
     float* gb3 = gb2 + kHid;
-    const float inv = 1.0f / (4.0f * (float)n);
-    // inputs
-    for (int e = lane; e < 16 * kFeat; e += 32) {
-        int r = e / kFeat, f = e % kFeat;
-        float v = 0.0f;
-        if (r0 + r < n) v = (rows[(size_t)idx[r0 + r] * kSampleFloats + f] - m.fmean[f]) / m.fstd[f];
-        X[e] = __float2bfloat16_rn(v);
-    }
-    __syncwarp();
-    uint32_t a[4], b[2];
-    // layer 1
-    for (int nb = 0; nb < kHid / 8; ++nb) {
-        float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-        for (int kb = 0; kb < kFeat / 16; ++kb) {
-            load_a_rowmajor(a, X, kFeat, kb * 16, lane);
-            load_b_trans(b, m.wt1, kFeat, kb * 16, nb * 8, lane);
-            mma_bf16(c, a, b);
-        }
-        int col = nb * 8 + 2 * t;
-        float p00 = c[0] + b1[col], p01 = c[1] + b1[col + 1], p10 = c[2] + b1[col], p11 = c[3] + b1[col + 1];
-        *reinterpret_cast<uint32_t*>(P1 + g * kHid + col) = pack_bf16x2(p00, p01);
-        *reinterpret_cast<uint32_t*>(P1 + (g + 8) * kHid + col) = pack_bf16x2(p10, p11);
-        *reinterpret_cast<uint32_t*>(H1 + g * kHid + col) = pack_bf16x2(gelu_f(p00), gelu_f(p01));
-        *reinterpret_cast<uint32_t*>(H1 + (g + 8) * kHid + col) = pack_bf16x2(gelu_f(p10), gelu_f(p11));
-    }
-    __syncwarp();
-    // layer 2
-    for (int nb = 0; nb < kHid / 8; ++nb) {
-        float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-        for (int kb = 0; kb < kHid / 16; ++kb) {
-            load_a_rowmajor(a, H1, kHid, kb * 16, lane);
-            load_b_trans(b, m.wt2, kHid, kb * 16, nb * 8, lane);
-            mma_bf16(c, a, b);
-        }
-        int col = nb * 8 + 2 * t;
-        float p00 = c[0] + b2[col], p01 = c[1] + b2[col + 1], p10 = c[2] + b2[col], p11 = c[3] + b2[col + 1];
-        *reinterpret_cast<uint32_t*>(P2 + g * kHid + col) = pack_bf16x2(p00, p01);
-        *reinterpret_cast<uint32_t*>(P2 + (g + 8) * kHid + col) = pack_bf16x2(p10, p11);
-        *reinterpret_cast<uint32_t*>(H2 + g * kHid + col) = pack_bf16x2(gelu_f(p00), gelu_f(p01));
-        *reinterpret_cast<uint32_t*>(H2 + (g + 8) * kHid + col) = pack_bf16x2(gelu_f(p10), gelu_f(p11));
-    }
-    __syncwarp();
-    // layer 3 and the loss gradient dY = 2 (y - t) / (4 n)
-    {
-        float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-        for (int kb = 0; kb < kHid / 16; ++kb) {
-            load_a_rowmajor(a, H2, kHid, kb * 16, lane);
-            load_b_trans(b, m.wt3, kHid, kb * 16, 0, lane);
-            mma_bf16(c, a, b);
-        }
-        float d[4], lsum = 0.0f;
+    for (int c0 = cbeg; c0 < cbeg + 64; c0 += 16) {      // dW2[in = row][out]
+        float v[16];
+        tc::ld16(T + lane_off + kTdW2 + c0, v);
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            int row = g + (q >> 1) * 8, col = 2 * t + (q & 1);
-            float y = c[q] + b3[col];
-            float dv = 0.0f;
-            if (col < kOut && r0 + row < n) {
-                float tv = (rows[(size_t)idx[r0 + row] * kSampleFloats + kFeat + col] - m.tmean[col]) / m.tstd[col];
-                float diff = y - tv;
-                lsum += diff * diff;
-                dv = 2.0f * diff * inv;
-            }
-            d[q] = dv;
+        for (int j = 0; j < 16; ++j) atomicAdd(gw2 + row * kHid + c0 + j, v[j]);
+    }
+    if (half == 0) {
+        float v[16];
+        tc::ld16(T + lane_off + kTdW3, v);                // dW3[hidden = row][0..3]
+#pragma unroll
+        for (int j = 0; j < kOut; ++j) atomicAdd(gw3 + row * kOutPad + j, v[j]);
+        for (int c0 = 0; c0 < kFeat; c0 += 16) {          // dW1[feature][hidden = row]
+            tc::ld16(T + lane_off + kTdW1 + c0, v);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) atomicAdd(gw1 + (c0 + j) * kHid + row, v[j]);
         }
-        for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
-        if (lane == 0) atomicAdd(loss, lsum);
-        for (int e = lane; e < kTileY; e += 32) DY[e] = __float2bfloat16_rn(0.0f);
-        __syncwarp();
-        DY[g * 16 + 2 * t] = __float2bfloat16_rn(d[0]);
-        DY[g * 16 + 2 * t + 1] = __float2bfloat16_rn(d[1]);
-        DY[(g + 8) * 16 + 2 * t] = __float2bfloat16_rn(d[2]);
-        DY[(g + 8) * 16 + 2 * t + 1] = __float2bfloat16_rn(d[3]);
-        add_colsum(gb3, 0, d, lane);
+        tc::ld16(T + lane_off + kTdb2, v);
+        atomicAdd(gb2 + row, v[0]);
+    } else {
+        float v[16];
+        tc::ld16(T + lane_off + kTdb1, v);
+        atomicAdd(gb1 + row, v[0]);
     }
-    __syncwarp();
-    // dW3 = H2^T dY  (128 x 8)
-    for (int mb = 0; mb < kHid / 16; ++mb) {
-        float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-        load_a_trans(a, H2, kHid, mb * 16, 0, lane);
-        load_b_rowmajor(b, DY, 16, 0, 0, lane);
-        mma_bf16(c, a, b);
-        int row = mb * 16 + g, col = 2 * t;
-        atomicAdd(gw3 + row * kOutPad + col, c[0]);
-        atomicAdd(gw3 + row * kOutPad + col + 1, c[1]);
-        atomicAdd(gw3 + (row + 8) * kOutPad + col, c[2]);
-        atomicAdd(gw3 + (row + 8) * kOutPad + col + 1, c[3]);
-    }
-    // dH2 = (dY W3^T) * gelu'(P2)   (K = 8 outputs, padded to 16 with zeros)
-    for (int nb = 0; nb < kHid / 8; ++nb) {
-        float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-        load_a_rowmajor(a, DY, 16, 0, lane);
-        load_b_trans(b, m.wb3, kOutPad, 0, nb * 8, lane);
-        b[1] = 0u;                                   // k = 8..15 are padding
-        mma_bf16(c, a, b);
-        int col = nb * 8 + 2 * t;
-        c[0] *= gelu_grad(bf(P2, g * kHid + col));
-        c[1] *= gelu_grad(bf(P2, g * kHid + col + 1));
-        c[2] *= gelu_grad(bf(P2, (g + 8) * kHid + col));
-        c[3] *= gelu_grad(bf(P2, (g + 8) * kHid + col + 1));
-        *reinterpret_cast<uint32_t*>(D2 + g * kHid + col) = pack_bf16x2(c[0], c[1]);
-        *reinterpret_cast<uint32_t*>(D2 + (g + 8) * kHid + col) = pack_bf16x2(c[2], c[3]);
-        add_colsum(gb2, nb * 8, c, lane);
-    }
-    __syncwarp();
-    // dW2 = H1^T dH2  (128 x 128)
-    for (int mb = 0; mb < kHid / 16; ++mb) {
-        load_a_trans(a, H1, kHid, mb * 16, 0, lane);
-        for (int nb = 0; nb < kHid / 8; ++nb) {
-            float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-            load_b_rowmajor(b, D2, kHid, 0, nb * 8, lane);
-            mma_bf16(c, a, b);
-            int row = mb * 16 + g, col = nb * 8 + 2 * t;
-            atomicAdd(gw2 + row * kHid + col, c[0]);
-            atomicAdd(gw2 + row * kHid + col + 1, c[1]);
-            atomicAdd(gw2 + (row + 8) * kHid + col, c[2]);
-            atomicAdd(gw2 + (row + 8) * kHid + col + 1, c[3]);
-        }
-    }
-    // dH1 = (dH2 W2^T) * gelu'(P1)
-    for (int nb = 0; nb < kHid / 8; ++nb) {
-        float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-        for (int kb = 0; kb < kHid / 16; ++kb) {
-            load_a_rowmajor(a, D2, kHid, kb * 16, lane);
-            load_b_trans(b, m.wb2, kHid, kb * 16, nb * 8, lane);
-            mma_bf16(c, a, b);
-        }
-        int col = nb * 8 + 2 * t;
-        c[0] *= gelu_grad(bf(P1, g * kHid + col));
-        c[1] *= gelu_grad(bf(P1, g * kHid + col + 1));
-        c[2] *= gelu_grad(bf(P1, (g + 8) * kHid + col));
-        c[3] *= gelu_grad(bf(P1, (g + 8) * kHid + col + 1));
-        *reinterpret_cast<uint32_t*>(D1 + g * kHid + col) = pack_bf16x2(c[0], c[1]);
-        *reinterpret_cast<uint32_t*>(D1 + (g + 8) * kHid + col) = pack_bf16x2(c[2], c[3]);
-        add_colsum(gb1, nb * 8, c, lane);
-    }
-    __syncwarp();
-    // dW1 = X^T dH1  (32 x 128)
-    for (int mb = 0; mb < kFeat / 16; ++mb) {
-        load_a_trans(a, X, kFeat, mb * 16, 0, lane);
-        for (int nb = 0; nb < kHid / 8; ++nb) {
-            float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-            load_b_rowmajor(b, D1, kHid, 0, nb * 8, lane);
-            mma_bf16(c, a, b);
-            int row = mb * 16 + g, col = nb * 8 + 2 * t;
-            atomicAdd(gw1 + row * kHid + col, c[0]);
-            atomicAdd(gw1 + row * kHid + col + 1, c[1]);
-            atomicAdd(gw1 + (row + 8) * kHid + col, c[2]);
-            atomicAdd(gw1 + (row + 8) * kHid + col + 1, c[3]);
-        }
-    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (tid < kOut) atomicAdd(gb3 + tid, s_db3[tid]);
+    if (tid == 0) atomicAdd(loss, s_loss);
+    if (!ok && lane == 0) atomicExch(status, 1);
+    if (warp == 0) tc::tmem_free(T, kTCols);
 }
 
 // BF16 copies of the FP32 parameters: transposed (forward) and row-major (backward)
@@ -318,6 +417,8 @@ struct dbox_mlp {
     float* norm = nullptr;        // fmean 32, fstd 32, tmean 4, tstd 4
     __nv_bfloat16* wbuf = nullptr;  // wt1 wt2 wt3 wb1 wb2 wb3
     float* loss = nullptr;
+    int* status = nullptr;        // set by k_mlp_train when a tensor-core wait ran past its bound
+    int nsm = 1;
     int step = 0;
 };
 
@@ -357,15 +458,26 @@ int refresh(dbox_mlp* m) {
     return cuerr(cudaGetLastError(), "k_mlp_refresh");
 }
 
-size_t train_smem() { return sizeof(__nv_bfloat16) * dg::kTrainWarps * dg::kWarpTrainElems; }
-
-// gradient of one batch (rows idx[0..n)) added into m->grad; loss sum into m->loss
+// gradient of one batch (rows idx[0..n)) added into m->grad; loss sum into m->loss: one CTA per
+// SM at most, each taking 128-sample tiles in turn
 int run_batch(dbox_mlp* m, const float* rows, const int* idx, int n) {
     if (n <= 0) return DBOX_OK;
-    int tiles = (n + 15) / 16;
-    int blocks = (tiles + dg::kTrainWarps - 1) / dg::kTrainWarps;
-    dg::k_mlp_train<<<blocks, dg::kTrainWarps * 32, train_smem()>>>(mlp_dev(m), m->grad, rows, idx, n, m->loss);
+    const int tiles = (n + 127) / 128;
+    const int blocks = tiles < m->nsm ? tiles : m->nsm;
+    dg::k_mlp_train<<<blocks, dg::kTcThreads, dg::kTcSmemBytes>>>(mlp_dev(m), m->grad, rows, idx, n, m->loss, m->status);
     return cuerr(cudaGetLastError(), "k_mlp_train");
+}
+
+// a wait for the tensor core that ran past its bound in any training launch since the last check
+int check_train_status(dbox_mlp* m) {
+    int st = 0;
+    int r = cuerr(cudaMemcpy(&st, m->status, sizeof(int), cudaMemcpyDeviceToHost), "training status");
+    if (r) return r;
+    if (st) {
+        cudaMemset(m->status, 0, sizeof(int));
+        return dbox_set_error(DBOX_ERR_TIMEOUT, "k_mlp_train: a tensor-core wait ran past its bound");
+    }
+    return DBOX_OK;
 }
 
 // n host samples (features n x 32, targets n x 4) interleaved into one device buffer
@@ -399,7 +511,8 @@ int32_t dbox_mlp_create(dbox_mlp** out) {
               cudaMalloc(&m->vel, sizeof(float) * dg::kNParams) == cudaSuccess &&
               cudaMalloc(&m->norm, sizeof(float) * kNorm) == cudaSuccess &&
               cudaMalloc(&m->wbuf, sizeof(__nv_bfloat16) * 2 * (dg::kW1 + dg::kW2 + dg::kW3)) == cudaSuccess &&
-              cudaMalloc(&m->loss, sizeof(float)) == cudaSuccess;
+              cudaMalloc(&m->loss, sizeof(float)) == cudaSuccess &&
+              cudaMalloc(&m->status, sizeof(int)) == cudaSuccess;
     if (!ok) {
         dbox_mlp_destroy(m);
         return dbox_set_error(DBOX_ERR_CUDA, "dbox_mlp_create: device allocation failed");
@@ -412,7 +525,10 @@ int32_t dbox_mlp_create(dbox_mlp** out) {
     for (int i = 0; i < dg::kFeat; ++i) norm[dg::kFeat + i] = 1.0f;
     for (int i = 0; i < dg::kOut; ++i) norm[2 * dg::kFeat + dg::kOut + i] = 1.0f;
     cudaMemcpy(m->norm, norm.data(), sizeof(float) * kNorm, cudaMemcpyHostToDevice);
-    cudaFuncSetAttribute(dg::k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)train_smem());
+    cudaMemset(m->status, 0, sizeof(int));
+    cudaDeviceGetAttribute(&m->nsm, cudaDevAttrMultiProcessorCount, m->device);
+    if (m->nsm < 1) m->nsm = 1;
+    cudaFuncSetAttribute(dg::k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dg::kTcSmemBytes);
     int r = refresh(m);
     if (r) { dbox_mlp_destroy(m); return r; }
     *out = m;
@@ -422,7 +538,7 @@ int32_t dbox_mlp_create(dbox_mlp** out) {
 int32_t dbox_mlp_destroy(dbox_mlp* m) {
     if (!m) return DBOX_OK;
     cudaFree(m->p); cudaFree(m->grad); cudaFree(m->mom); cudaFree(m->vel);
-    cudaFree(m->norm); cudaFree(m->wbuf); cudaFree(m->loss);
+    cudaFree(m->norm); cudaFree(m->wbuf); cudaFree(m->loss); cudaFree(m->status);
     delete m;
     return DBOX_OK;
 }
@@ -511,6 +627,7 @@ int32_t dbox_mlp_gradient(dbox_mlp* m, int32_t n, const float* feats, const floa
     cudaMemset(m->loss, 0, sizeof(float));
     r = run_batch(m, drows, di, n);
     if (!r) r = cuerr(cudaDeviceSynchronize(), "dbox_mlp_gradient");
+    if (!r) r = check_train_status(m);
     if (!r && grad) r = cuerr(cudaMemcpy(grad, m->grad, sizeof(float) * dg::kNParams, cudaMemcpyDeviceToHost), "grad");
     float l = 0.0f;
     if (!r) r = cuerr(cudaMemcpy(&l, m->loss, sizeof(float), cudaMemcpyDeviceToHost), "loss");
@@ -552,6 +669,7 @@ int32_t dbox_mlp_train_device(dbox_mlp* m, int32_t n, const float* rows, int32_t
             if (!r) r = refresh(m);
         }
         if (!r) r = cuerr(cudaDeviceSynchronize(), "dbox_mlp_train_device");
+        if (!r) r = check_train_status(m);
         if (!r && epoch_loss) {
             float l = 0.0f;
             cudaMemcpy(&l, m->loss, sizeof(float), cudaMemcpyDeviceToHost);

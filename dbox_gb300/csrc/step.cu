@@ -3666,10 +3666,15 @@ DG void solve_world(const Ctx& x, int w, float* sbp, bool sb_smem, float* stage_
                         if (x.ws_mode == 3 && x.start_ct) {
                             // given start: the impulses another handle's step from the same state
                             // ended with at this contact slot (clamped as a prediction is)
+                            // (the point with the same feature id: the source's SolveTOI may have
+                            // re-evaluated the manifold after its solve)
                             const dbox_contact_state& g = x.start_ct[item];
                             for (int j = 0; j < pc.pointCount; ++j) {
                                 if (!(fr & (j == 0 ? kContactNew0 : kContactNew1))) continue;
-                                float ln = g.points[j].normal_impulse, lt = g.points[j].tangent_impulse;
+                                const uint32_t id = x.ct[item].points[j].id;
+                                float ln = 0.0f, lt = 0.0f;
+                                for (int q = 0; q < g.point_count && q < 2; ++q)
+                                    if (g.points[q].id == id) { ln = g.points[q].normal_impulse; lt = g.points[q].tangent_impulse; }
                                 ln = ln > 0.0f ? ln : 0.0f;
                                 const float mf = vr.K.w * ln;
                                 lt = lt < -mf ? -mf : (lt > mf ? mf : lt);

@@ -56,13 +56,22 @@ def test_batch_4096_exact(oracle_lib, gpu_lib):
     assert not bad, "%d worlds differ, first: %s" % (len(bad), bad[:3])
 
 
+def _beyond_tolerance(a, b):
+    """(bodies, bodies beyond 1e-5 m / 1e-5 rad / 1e-4 m/s) between two exported states."""
+    ba, bb = a["bodies"], b["bodies"]
+    dp = np.abs(ba["xf"][:, :2].astype(np.float64) - bb["xf"][:, :2]).max(1)
+    da = np.abs(ba["sweep"][:, 7].astype(np.float64) - bb["sweep"][:, 7])
+    dv = np.abs(ba["vel"].astype(np.float64) - bb["vel"]).max(1)
+    return len(ba), int(((dp > 1e-5) | (da > 1e-5) | (dv > 1e-4)).sum())
+
+
 def _reference_trig_run(oracle_lib, gpu_lib, worlds, pre_steps, steps):
     """Re-seeded one-step check against the host libm trig.
 
     Every step: the GPU is re-seeded from the libm oracle, both take one step, and the pair
     set, contact order, point counts and feature ids must be identical.  Positions, angles and
-    velocities must agree within 1e-5 m, 1e-5 rad and 1e-4 m/s on at least 98 % of the
-    (world, step) pairs.  A pair beyond that tolerance must be explained by the sin/cos alone:
+    velocities must agree within 1e-5 m, 1e-5 rad and 1e-4 m/s for at least 99.5 % of the
+    body-steps.  A (world, step) with a body beyond that tolerance must be explained by the sin/cos alone:
     the oracle, stepped from the same state with the device's sin/cos instead of the libm's,
     reproduces the GPU's state bit for bit (the reference's block solver and position solver
     switch cases on last-bit differences of a rotation).  Returns (worst errors, outliers)."""
@@ -75,6 +84,7 @@ def _reference_trig_run(oracle_lib, gpu_lib, worlds, pre_steps, steps):
         gw = gpu_lib.World(worlds)
         worst = [0.0, 0.0, 0.0]
         outliers = []
+        body_steps = bad_bodies = 0
         for t in range(steps):
             for i, ow in enumerate(ows):
                 gw.import_state(ow.export_state(), i)
@@ -87,11 +97,13 @@ def _reference_trig_run(oracle_lib, gpu_lib, worlds, pre_steps, steps):
                 assert not sd, "world %d step %d: %s" % (i, pre_steps + t + 1, sd[:4])
                 e = body_error(a, b)
                 worst = [max(u, v) for u, v in zip(worst, e)]
-                if not (e[0] <= 1e-5 and e[1] <= 1e-5 and e[2] <= 1e-4):
+                nb, nbad = _beyond_tolerance(a, b)
+                body_steps += nb
+                bad_bodies += nbad
+                if nbad:
                     outliers.append((i, pre_steps + t + 1, e, b))
-        total = steps * len(worlds)
-        assert len(outliers) <= 0.02 * total, "%d of %d (world, step) pairs beyond tolerance: %s" % (
-            len(outliers), total, [o[:3] for o in outliers[:4]])
+        assert bad_bodies <= 0.005 * body_steps, "%d of %d body-steps beyond tolerance: %s" % (
+            bad_bodies, body_steps, [o[:3] for o in outliers[:4]])
         for i, step, e, b in outliers[:3]:
             x = oracle_lib.OracleWorld(worlds[i])
             x.step(steps=step - 1)                         # the libm trajectory up to the step
@@ -154,3 +166,23 @@ def test_features_exact(oracle_lib, gpu_lib, flags):
         assert toi_total == 0
     else:
         assert toi_total > 0
+
+
+@pytest.mark.parametrize("per_pile", [300, 1100], ids=["warp_path", "large_world_path"])
+def test_stress_reduced_exact(oracle_lib, gpu_lib, per_pile):
+    # the large-island stress world at reduced size: 4 container piles of mixed bodies with 4
+    # revolute chains of 16 links hanging into each (with 1,100 bodies a pile the world has over
+    # 4,096 fixtures and takes the large-world kernels)
+    oracle_lib.set_trig_mode(1)
+    s = scenes.stress(piles=4, per_pile=per_pile, chains_per_pile=4, links=16)
+    ow = oracle_lib.OracleWorld(s)
+    gw = gpu_lib.World(s)
+    for t in range(120):
+        ow.step()
+        gw.step()
+        if (t + 1) % 30 == 0:
+            d = exact_diff(ow.export_state(), gw.export_state())
+            assert not d, "step %d: %s" % (t + 1, d[:6])
+    st = gw.export_state()
+    assert st["header"][0]["contact_count"] > 4 * per_pile
+    assert np.abs(st["joints"]["impulse"]).max() > 0

@@ -57,6 +57,26 @@ def test_gpu_gradient_matches_oracle(gpu_lib):
 
 
 @pytest.mark.gpu
+def test_gpu_gradient_many_tiles_matches_oracle(gpu_lib):
+    # more 128-sample tiles than the GPU has SMs: each CTA keeps its gradients in tensor memory
+    # across several tiles; the last tile is partial
+    feats, targets = _data(152 * 128 * 2 + 77, 6)
+    params = mlp_ref.init_params(7)
+    norm = _norm(feats, targets)
+    m = gpu_lib.Mlp()
+    m.set_params(params, norm)
+    g_gpu, loss_gpu = m.gradient(feats, targets)
+    loss_ref, g_ref = mlp_ref.loss_and_grad(params, norm, feats, targets, bf16=True)
+    assert abs(loss_gpu - loss_ref) <= 1e-3 * abs(loss_ref)
+    o = np.cumsum([0, mlp_ref.NW1, mlp_ref.NW2, mlp_ref.NW3, 128, 128, 8])
+    for a, b in zip(o[:-1], o[1:]):
+        d, r = g_gpu[a:b].astype(np.float64), g_ref[a:b]
+        if np.linalg.norm(r) == 0:
+            continue
+        assert np.linalg.norm(d - r) <= 2e-2 * np.linalg.norm(r), (a, b)
+
+
+@pytest.mark.gpu
 def test_gpu_forward_matches_oracle(gpu_lib):
     feats, targets = _data(200, 6)
     params = mlp_ref.init_params(7)
