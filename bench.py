@@ -62,6 +62,9 @@ def parse():
     p.add_argument("--no-queries", action="store_true", help="skip the world-query measurement")
     p.add_argument("--learned-worlds", type=int, default=1024)
     p.add_argument("--learned-log-steps", type=int, default=2000)
+    p.add_argument("--stress-warmup", type=int, default=60, help="steps before the stress world is measured")
+    p.add_argument("--stress-steps", type=int, default=3)
+    p.add_argument("--no-stress", action="store_true", help="skip the large-island stress world")
     return p.parse_args()
 
 
@@ -550,6 +553,7 @@ def learned_leg(args):
         src.close()
     p8, l5 = res["plain_8"], res["learned_5"]
     u5 = res["perfect_5"]
+    args._model = model                        # for the large-island stress leg
     return {
         "config": "%d scatter worlds x 256 bodies (40 m containers), dt 1/60, %d position iterations; "
                   "samples from %d plain steps, evaluation on new-seed worlds after 100 steps, 30 steps"
@@ -566,6 +570,51 @@ def learned_leg(args):
         "perfect_start_5_reaches_plain_8_residual": bool(u5["residual_rms"] <= p8["residual_rms"] and
                                                          u5["residual_max"] <= p8["residual_max"]),
     }
+
+
+def stress_leg(args, model):
+    """The large-island stress world: one world of 64 container piles x 2,048 mixed circles /
+    polygons (one large island per pile) and 256 revolute chains x 32 links hanging into them.
+    Plain 8/3 iterations and the learned start with 5 velocity iterations, each from the same
+    warmed-up state: body-steps/s (CUDA events), velocity residual and penetration, and the
+    algorithmic bandwidth of the solve phase."""
+    import dbox_gb300
+    from dbox_gb300 import scenes
+    s = scenes.stress(seed=args.seed)
+    nd = scenes.dynamic_body_count(s)
+    base = dbox_gb300.World(s)
+    base.step(DT, VI, PI, steps=args.stress_warmup, graph=True)
+    res = {"config": "1 world: 64 piles x 2,048 bodies + 256 chains x 32 links, %d dynamic bodies; steps %d..%d"
+                     % (nd, args.stress_warmup + 1, args.stress_warmup + args.stress_steps), "dynamic_bodies": nd}
+    runs = [("plain_8", 0, VI), ("learned_5", 2, 5)] if model is not None else [("plain_8", 0, VI)]
+    for label, mode, vi in runs:
+        w = dbox_gb300.World(s)
+        w.step()                                  # on the device, then the same state as `base`
+        w.copy_state_from(base)
+        w.set_warmstart(mode, model if mode == 2 else None, 0)
+        w.set_measure(True)
+        rms, mx, pen = [], [], []
+        for _ in range(2):
+            w.step(DT, vi, PI)
+            q = w.quality()
+            rms.append(float(np.sqrt(q[:, 0].sum() / max(q[:, 2].sum(), 1.0))))
+            mx.append(float(q[:, 1].max()))
+            pen.append(float(-q[:, 3].min()))
+        w.set_measure(False)
+        c0 = w.counters()
+        tot_ms, ph = w.step_timed(args.stress_steps, DT, vi, PI)
+        c1 = w.counters()
+        cd = {k: (c1[k] - c0[k]) / args.stress_steps for k in c1}
+        solve_ms = ph[1] / args.stress_steps
+        res[label] = {"velocity_iterations": vi, "body_steps_per_s": nd * args.stress_steps / (tot_ms / 1e3),
+                      "ms_per_step": tot_ms / args.stress_steps, "residual_rms": float(np.mean(rms)),
+                      "residual_max": float(np.mean(mx)), "penetration_max_m": float(np.max(pen)),
+                      "phases_ms_per_step": {"collide": ph[0] / args.stress_steps, "solve_and_toi": solve_ms},
+                      "solve_algorithmic_gbs": algorithmic_solve_bytes(cd) / (solve_ms / 1e3) / 1e9,
+                      "collide_contacts_per_step": cd["contacts"]}
+        w.close()
+    base.close()
+    return res
 
 
 def mapping_report(mapping, how):
@@ -611,6 +660,8 @@ def main():
             lw["train_tflops_peak"] = bf or 1900.0
             lw["train_tflops_peak_source"] = "measured (MEASURED_PEAKS.json bf16_tflops)" if bf else "fallback 1900"
             lw["train_tflops_frac"] = lw["train_tflops"] / lw["train_tflops_peak"]
+        if world_size == 1 and not args.no_stress and args.workload == "batch":
+            out["large_island_stress"] = stress_leg(args, getattr(args, "_model", None))
         if world_size == 1 and not args.no_cpu:
             rate, cores, sample = cpu_leg(args, worlds)
             out["cpu_baseline"] = {"value": rate, "unit": "body-steps/s", "cores": cores, "kind": "port",

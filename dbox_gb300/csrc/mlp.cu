@@ -55,6 +55,35 @@ constexpr uint32_t kTcSmemBytes = 225280 + 1024;   // + slack to align the base 
 constexpr uint32_t kTZ = 0, kTdW2 = 128, kTdW3 = 256, kTdW1 = 320, kTY = 384, kTdb2 = 400, kTdb1 = 416;
 constexpr uint32_t kTCols = 512;
 
+// A bijection of [0, n) standing in for a shuffled index array: a four-round Feistel network
+// over the smallest even number of bits covering n, walked along its cycle until it lands
+// back in [0, n) (each try lands there with probability above 1/4).
+struct Perm {
+    uint32_t half_bits, mask, n;
+    uint32_t key[4];
+};
+__device__ __forceinline__ uint32_t perm_round(uint32_t r, uint32_t k) {
+    uint32_t h = (r * 0x9E3779B1u) ^ k;
+    h ^= h >> 15;
+    h *= 0x2C1B3C6Du;
+    h ^= h >> 12;
+    return h;
+}
+__device__ __forceinline__ uint32_t perm_apply(const Perm& p, uint32_t x) {
+    for (int walk = 0; walk < 128; ++walk) {
+        uint32_t l = x >> p.half_bits, r = x & p.mask;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const uint32_t t = l ^ (perm_round(r, p.key[i]) & p.mask);
+            l = r;
+            r = t;
+        }
+        x = (l << p.half_bits) | r;
+        if (x < p.n) return x;
+    }
+    return x % p.n;                                       // bounded: a repeat sample at worst
+}
+
 __device__ __forceinline__ void gelu_both(float x, float& h, float& g) {
     const float k0 = 0.7978845608028654f, k1 = 0.044715f;
     float t = tanhf(k0 * (x + k1 * x * x * x));
@@ -83,12 +112,13 @@ __device__ __forceinline__ void get16_rows(const uint8_t* buf, int row, int c0, 
     for (int j = 0; j < 16; ++j) v[j] = __bfloat162float(p[j]);
 }
 
-// Forward + backward of MSE(MLP(x), t) / (n * 4) over the samples idx[0 .. n) of `rows`
-// (kSampleFloats per sample: features, then targets), normalised with the model's
-// statistics; gradients added into grad (kNParams), the sum of squared errors into *loss.
-// *status gets 1 if a wait for the tensor core ran past its bound.
+// Forward + backward of MSE(MLP(x), t) / (n * 4) over n samples of `rows` (kSampleFloats per
+// sample: features, then targets): samples idx[0 .. n), or, with idx NULL, the samples
+// perm(offset + 0 .. n) of a shuffle; normalised with the model's statistics; gradients
+// added into grad (kNParams), the sum of squared errors into *loss.  *status gets 1 if a wait
+// for the tensor core ran past its bound.
 __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_train(MlpDev m, float* grad, const float* rows, const int* idx,
-                                                             int n, float* loss, int* status) {
+                                                             int n, Perm perm, int offset, float* loss, int* status) {
     extern __shared__ uint8_t tc_smem_raw[];
     uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(tc_smem_raw) + 1023) & ~uintptr_t(1023));
     __shared__ uint64_t bar;
@@ -166,7 +196,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_train(MlpDev m, float* gr
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int r0 = tile * 128;
         const bool valid = r0 + row < n;
-        const float* sample = valid ? rows + (size_t)idx[r0 + row] * kSampleFloats : nullptr;
+        const int sid = !valid ? 0 : (idx ? idx[r0 + row] : (int)perm_apply(perm, (uint32_t)(offset + r0 + row)));
+        const float* sample = valid ? rows + (size_t)sid * kSampleFloats : nullptr;
         {   // inputs: half 0 writes features 0..15 of its row, half 1 features 16..31
             float v[16];
 #pragma unroll
@@ -359,8 +390,11 @@ __global__ void k_mlp_refresh(const float* p, __nv_bfloat16* wt1, __nv_bfloat16*
     }
 }
 
-// Adam (beta1 0.9, beta2 0.999, eps 1e-8) on the flat parameter vector; clears grad
-__global__ void k_mlp_adam(float* p, float* grad, float* mom, float* vel, int n, float lr, float bc1, float bc2) {
+// Adam (beta1 0.9, beta2 0.999, eps 1e-8) on the flat parameter vector, clearing grad, and the
+// BF16 copies of the updated weights (as k_mlp_refresh writes them)
+__global__ void k_mlp_adam(float* p, float* grad, float* mom, float* vel, int n, float lr, float bc1, float bc2,
+                           __nv_bfloat16* wt1, __nv_bfloat16* wt2, __nv_bfloat16* wt3, __nv_bfloat16* wb1,
+                           __nv_bfloat16* wb2, __nv_bfloat16* wb3) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float gi = grad[i];
         grad[i] = 0.0f;
@@ -372,7 +406,23 @@ __global__ void k_mlp_adam(float* p, float* grad, float* mom, float* vel, int n,
         float vi = 0.999f * vel[i] + 0.001f * gi * gi;
         mom[i] = mi;
         vel[i] = vi;
-        p[i] -= lr * (mi / bc1) / (sqrtf(vi / bc2) + 1e-8f);
+        const float pi = p[i] - lr * (mi / bc1) / (sqrtf(vi / bc2) + 1e-8f);
+        p[i] = pi;
+        if (i >= kW1 + kW2 + kW3) continue;
+        const __nv_bfloat16 v = __float2bfloat16_rn(pi);
+        if (i < kW1) {
+            const int r = i / kHid, c = i % kHid;
+            wb1[i] = v;
+            wt1[c * kFeat + r] = v;
+        } else if (i < kW1 + kW2) {
+            const int j = i - kW1, r = j / kHid, c = j % kHid;
+            wb2[j] = v;
+            wt2[c * kHid + r] = v;
+        } else {
+            const int j = i - kW1 - kW2, r = j / kOutPad, c = j % kOutPad;
+            wb3[j] = v;
+            wt3[c * kHid + r] = v;
+        }
     }
 }
 
@@ -460,12 +510,32 @@ int refresh(dbox_mlp* m) {
 
 // gradient of one batch (rows idx[0..n)) added into m->grad; loss sum into m->loss: one CTA per
 // SM at most, each taking 128-sample tiles in turn
-int run_batch(dbox_mlp* m, const float* rows, const int* idx, int n) {
+int run_batch(dbox_mlp* m, const float* rows, const int* idx, int n, const dg::Perm& perm = dg::Perm(), int offset = 0) {
     if (n <= 0) return DBOX_OK;
     const int tiles = (n + 127) / 128;
     const int blocks = tiles < m->nsm ? tiles : m->nsm;
-    dg::k_mlp_train<<<blocks, dg::kTcThreads, dg::kTcSmemBytes>>>(mlp_dev(m), m->grad, rows, idx, n, m->loss, m->status);
+    dg::k_mlp_train<<<blocks, dg::kTcThreads, dg::kTcSmemBytes>>>(mlp_dev(m), m->grad, rows, idx, n, perm, offset, m->loss,
+                                                                 m->status);
     return cuerr(cudaGetLastError(), "k_mlp_train");
+}
+
+// the shuffle of epoch e of n samples (dg::Perm), keyed from the training seed
+dg::Perm make_perm(uint32_t n, uint64_t seed, int epoch) {
+    dg::Perm p;
+    int bits = 2;
+    while (bits < 32 && (1ull << bits) < n) bits += 2;
+    p.half_bits = (uint32_t)(bits / 2);
+    p.mask = (1u << p.half_bits) - 1u;
+    p.n = n;
+    uint64_t s = seed ^ (0x9E3779B97F4A7C15ull * (uint64_t)(epoch + 1));
+    for (int i = 0; i < 4; ++i) {                     // SplitMix64
+        s += 0x9E3779B97F4A7C15ull;
+        uint64_t z = s;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        p.key[i] = (uint32_t)(z ^ (z >> 31));
+    }
+    return p;
 }
 
 // a wait for the tensor core that ran past its bound in any training launch since the last check
@@ -644,29 +714,22 @@ int32_t dbox_mlp_train_device(dbox_mlp* m, int32_t n, const float* rows, int32_t
                               uint64_t seed, float* epoch_loss) {
     if (!m || n <= 0 || !rows || epochs <= 0 || batch <= 0)
         return dbox_set_error(DBOX_ERR_INVALID, "dbox_mlp_train_device: bad arguments");
-    int* di = nullptr;
-    MCU(cudaMalloc(&di, sizeof(int) * (size_t)n));
-    std::vector<int> idx(n);
-    for (int i = 0; i < n; ++i) idx[i] = i;
-    uint64_t s = seed ^ 0x2545F4914F6CDD1Dull;
     int r = DBOX_OK;
+    dg::MlpDev d = mlp_dev(m);
     for (int e = 0; e < epochs && !r; ++e) {
-        for (int i = n - 1; i > 0; --i) {          // Fisher-Yates with an xorshift64 stream
-            s ^= s << 13; s ^= s >> 7; s ^= s << 17;
-            int j = (int)(s % (uint64_t)(i + 1));
-            std::swap(idx[i], idx[j]);
-        }
-        cudaMemcpy(di, idx.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice);
+        const dg::Perm perm = make_perm((uint32_t)n, seed, e);   // this epoch's shuffle, applied on the device
         cudaMemset(m->loss, 0, sizeof(float));
         for (int b0 = 0; b0 < n && !r; b0 += batch) {
             int nb = std::min(batch, n - b0);
-            r = run_batch(m, rows, di + b0, nb);
+            r = run_batch(m, rows, nullptr, nb, perm, b0);
             if (r) break;
             ++m->step;
             float bc1 = 1.0f - powf(0.9f, (float)m->step), bc2 = 1.0f - powf(0.999f, (float)m->step);
-            dg::k_mlp_adam<<<64, 256>>>(m->p, m->grad, m->mom, m->vel, dg::kNParams, lr, bc1, bc2);
+            dg::k_mlp_adam<<<86, 256>>>(m->p, m->grad, m->mom, m->vel, dg::kNParams, lr, bc1, bc2,
+                                        const_cast<__nv_bfloat16*>(d.wt1), const_cast<__nv_bfloat16*>(d.wt2),
+                                        const_cast<__nv_bfloat16*>(d.wt3), const_cast<__nv_bfloat16*>(d.wb1),
+                                        const_cast<__nv_bfloat16*>(d.wb2), const_cast<__nv_bfloat16*>(d.wb3));
             r = cuerr(cudaGetLastError(), "k_mlp_adam");
-            if (!r) r = refresh(m);
         }
         if (!r) r = cuerr(cudaDeviceSynchronize(), "dbox_mlp_train_device");
         if (!r) r = check_train_status(m);
@@ -677,7 +740,6 @@ int32_t dbox_mlp_train_device(dbox_mlp* m, int32_t n, const float* rows, int32_t
             epoch_loss[e] = l / (4.0f * (float)n);
         }
     }
-    cudaFree(di);
     return r;
 }
 

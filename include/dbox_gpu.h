@@ -432,10 +432,13 @@ typedef void (*dbox_presolve_fn)(dbox_presolve_contact* contacts, int32_t count,
  * a PreSolve edit only touches its own contact and nothing later in Collide reads it.  One
  * difference: b2World.SolveTOI also calls b2Contact.Update (and PreSolve) on the contacts it
  * moves to a time of impact, those with a static, kinematic or bullet body
- * (b2world.d:1194-1208, 1287, 1345-1372); there the library keeps the window's decision (a
- * contact disabled in the window stays disabled through the step's sub-steps, one the window
- * did not see stays enabled) and reports those calls only as recorded PRESOLVE events to the
- * listener of dbox_world_set_listener.  fn = NULL removes it.
+ * (b2world.d:1194-1208, 1287, 1345-1372); there the library keeps the window's decisions (a
+ * contact disabled in the window stays disabled through the step's sub-steps; a contact that
+ * first touches inside a sub-step gets no PreSolve call and so no edit) and reports those
+ * calls only as recorded PRESOLVE events to the listener of dbox_world_set_listener.  Edits of
+ * contacts between dynamic, non-bullet bodies therefore match the reference exactly; edits of
+ * contacts with a static, kinematic or bullet body match unless such a contact first touches
+ * during a step's time-of-impact sub-steps.  fn = NULL removes it.
  * The window costs one device synchronisation and a download of the affected worlds'
  * contacts per step. */
 int32_t dbox_world_set_presolve(dbox_world* w, dbox_presolve_fn fn, void* user);

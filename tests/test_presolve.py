@@ -14,20 +14,20 @@ pytestmark = pytest.mark.gpu
 
 
 def make_rule(static_fixtures):
-    """A user's PreSolve: decisions from the fixtures of each contact.  It disables only
-    contacts between two non-bullet dynamic bodies: b2World.SolveTOI calls b2Contact.Update
-    (and so PreSolve) again only for contacts with a static, kinematic or bullet body
-    (b2world.d:1194-1208, 1287, 1345-1372), where the library keeps the window's decision
-    instead of calling back."""
+    """A user's PreSolve: decisions from the fixtures of each contact.  It edits only contacts
+    between two non-bullet dynamic bodies: b2World.SolveTOI calls b2Contact.Update (and so
+    PreSolve) again only for contacts with a static, kinematic or bullet body
+    (b2world.d:1194-1208, 1287, 1345-1372), where the library keeps the window's decisions
+    instead of calling back (a contact that first touches inside a sub-step gets none)."""
     static = np.asarray(static_fixtures, bool)
 
     def rule(r):
         fa, fb = r["contact"]["fixture_a"], r["contact"]["fixture_b"]
         dyn = ~static[fa] & ~static[fb]
         r["enabled"][((fa % 7 == 3) | (fb % 7 == 3)) & dyn] = 0     # SetEnabled(false): this step only
-        r["friction"][(fa + fb) % 5 == 1] = np.float32(0.05)           # SetFriction
-        r["restitution"][(fa + fb) % 9 == 4] = np.float32(0.6)         # SetRestitution
-        r["tangent_speed"][(fa == 0) & (fb % 4 == 2)] = np.float32(1.5)   # SetTangentSpeed: a conveyor
+        r["friction"][((fa + fb) % 5 == 1) & dyn] = np.float32(0.05)           # SetFriction
+        r["restitution"][((fa + fb) % 9 == 4) & dyn] = np.float32(0.6)         # SetRestitution
+        r["tangent_speed"][((fa + fb) % 4 == 2) & dyn] = np.float32(1.5)       # SetTangentSpeed
     return rule
 
 
