@@ -31,7 +31,7 @@ namespace dg {
 // units) 32 (w % 4) .. +31, and split the columns between them.
 //
 //   forward   Z1 = X W1, H1 = gelu(Z1 + b1)            X: 128 x 32 (padded to 64), W1: 32 x 128
-//             Z2 = H1 W2, H2 = gelu(Z2 + b2)           W2: 128 x 128
+//             Z2 = H1 W2, H2 = gelu(Z2 + b2)           W2: 128 x 128 (gelu' kept for the backward)
 //             Y = H2 W3 + b3, dY = 2 (Y - T) / (4 n)   W3: 128 x 4 (padded to 16)
 //   backward  dW3 += H2^T dY, db3 += colsum dY
 //             dZ2 = (dY W3^T) * gelu'(P2),  dW2 += H1^T dZ2,  db2 += colsum dZ2
@@ -47,8 +47,8 @@ constexpr uint32_t kOffX = 57344;       // X [128 samples][64] (features 32..63 
 constexpr uint32_t kOffH1 = 73728;      // H1 [128][128], then dZ1                            32 KB
 constexpr uint32_t kOffH2 = 106496;     // H2 [128][128], then dZ2                            32 KB
 constexpr uint32_t kOffDY = 139264;     // dY [128][64] (columns 4..63 zero)                  16 KB
-constexpr uint32_t kOffP1 = 155648;     // P1 = Z1 + b1 (bf16, 272-byte rows)                 34 KB
-constexpr uint32_t kOffP2 = 190464;     // P2 = Z2 + b2                                       34 KB
+constexpr uint32_t kOffP1 = 155648;     // gelu'(Z1 + b1) (bf16, 272-byte rows)               34 KB
+constexpr uint32_t kOffP2 = 190464;     // gelu'(Z2 + b2)                                     34 KB
 constexpr uint32_t kPRow = 272;
 constexpr uint32_t kTcSmemBytes = 225280 + 1024;   // + slack to align the base to 1024 bytes
 // tensor-memory columns
@@ -217,10 +217,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_train(MlpDev m, float* gr
             float z[16], h[16];
             tc::ld16(T + lane_off + kTZ + c0, z);
 #pragma unroll
-            for (int j = 0; j < 16; ++j) {
-                z[j] += b1[c0 + j];
-                h[j] = gelu_f(z[j]);
-            }
+            for (int j = 0; j < 16; ++j) gelu_both(z[j] + b1[c0 + j], h[j], z[j]);   // z becomes gelu'
             put16(H1, row, c0, h);
             put16_rows(P1, row, c0, z);
         }
@@ -234,10 +231,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_train(MlpDev m, float* gr
             float z[16], h[16];
             tc::ld16(T + lane_off + kTZ + c0, z);
 #pragma unroll
-            for (int j = 0; j < 16; ++j) {
-                z[j] += b2[c0 + j];
-                h[j] = gelu_f(z[j]);
-            }
+            for (int j = 0; j < 16; ++j) gelu_both(z[j] + b2[c0 + j], h[j], z[j]);   // z becomes gelu'
             put16(H2, row, c0, h);
             put16_rows(P2, row, c0, z);
         }
@@ -282,7 +276,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_train(MlpDev m, float* gr
             tc::ld16(T + lane_off + kTZ + c0, z);
             get16_rows(P2, row, c0, p);
 #pragma unroll
-            for (int j = 0; j < 16; ++j) z[j] *= gelu_grad(p[j]);
+            for (int j = 0; j < 16; ++j) z[j] *= p[j];
             put16(H2, row, c0, z);
         }
         sync_for_mma();
@@ -301,7 +295,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_train(MlpDev m, float* gr
             tc::ld16(T + lane_off + kTZ + c0, z);
             get16_rows(P1, row, c0, p);
 #pragma unroll
-            for (int j = 0; j < 16; ++j) z[j] *= gelu_grad(p[j]);
+            for (int j = 0; j < 16; ++j) z[j] *= p[j];
             put16(H1, row, c0, z);
         }
         sync_for_mma();

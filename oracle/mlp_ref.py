@@ -84,13 +84,13 @@ def loss_and_grad(params, norm, feats, targets, bf16=True):
     dy = r(d)
     gb3 = d.sum(0)
     gw3 = h2.T @ dy
-    p2 = r(pre2)
-    dh2 = (dy @ w3r.T) * gelu_grad(p2)
+    g2 = r(gelu_grad(pre2))            # the GELU derivative, kept in BF16 from the forward pass
+    dh2 = (dy @ w3r.T) * g2
     d2 = r(dh2)
     gb2 = d2.sum(0)                    # column sums of the rounded operand (a tensor-core product with ones)
     gw2 = h1.T @ d2
-    p1 = r(pre1)
-    dh1 = (d2 @ w2r.T) * gelu_grad(p1)
+    g1 = r(gelu_grad(pre1))
+    dh1 = (d2 @ w2r.T) * g1
     d1 = r(dh1)
     gb1 = d1.sum(0)
     gw1 = x.T @ d1
