@@ -686,7 +686,7 @@ __global__ void __launch_bounds__(kPairThreads) k_pairs_block(const __grid_const
     WorldDyn& wd = x.wd[w];
     const int tid = threadIdx.x, nt = blockDim.x;
     if (!(wd.step_complete && x.dt > 0.0f) || wd.error != 0) {        // solve_world did not reach its broad-phase
-        if (tid == 0) wd.pair_total = 0;
+        if (tid == 0) { wd.pair_total = 0; wd.g_valid = 0; }
         return;
     }
     // SynchronizeFixtures of the island bodies (b2world.d:1099-1116), the solve warp's last step
@@ -724,8 +724,8 @@ __global__ void __launch_bounds__(kPairThreads) k_pairs_block(const __grid_const
     cnt = block_reduce(cnt, isum, shi);
     nm = block_reduce(nm, isum, shi);
     sum = block_reduce(sum, fsum, shf);
-    if (nm == 0) {
-        if (tid == 0) wd.pair_total = 0;
+    if (nm == 0 && !x.continuous) {                                     // no pairs, and no SolveTOI to serve
+        if (tid == 0) { wd.pair_total = 0; wd.g_valid = 0; }
         return;
     }
     const float cut = 4.0f * sum / (float)(cnt > 0 ? cnt : 1);
@@ -808,6 +808,14 @@ __global__ void __launch_bounds__(kPairThreads) k_pairs_block(const __grid_const
     s.wide = wide;
     s.nwide = n_wide;
     s.cstart = cstart;
+    if (tid == 0) {                                                      // the grid, for SolveTOI's pair searches
+        wd.g_ox = s.ox; wd.g_oy = s.oy; wd.g_inv = s.inv;
+        wd.g_ncx = s.ncx; wd.g_ncy = s.ncy; wd.g_nv = nv; wd.g_nwide = n_wide; wd.g_valid = 1;
+    }
+    if (nm == 0) {
+        if (tid == 0) wd.pair_total = 0;
+        return;
+    }
     for (int a = tid; a < nf; a += nt) {                                 // partners per proxy
         int c = 0;
         const dbox_proxy_state& p = x.px[f0 + PX(a)];
@@ -841,6 +849,102 @@ __global__ void __launch_bounds__(kPairThreads) k_pairs_block(const __grid_const
         wd.acc_pairs += (unsigned long long)total;
         wd.pair_total = total;
     }
+}
+
+// FindNewContacts inside SolveTOI for a large world (one warp): the move buffer holds the
+// proxies this event's SynchronizeFixtures moved (ranks now[0 .. nnow)); their pairs with every
+// overlapping proxy (b2BroadPhase.UpdatePairs, b2broadphase.d:139-195) come from the grid
+// k_pairs_block left (its boxes are those after the solve) for proxies that have not moved
+// since, and from a direct test against all[0 .. nall), the proxies moved during this SolveTOI
+// (whose grid boxes are stale; toimv[rank] marks them).  Pairs are sorted into (idA, idB) order
+// and left in the world's pair buffer; returns their count, or -1 when they overflow it.
+DG int toi_pairs_big(const Ctx& x, int w, const int* now, int nnow, const int* all, int nall, const int* toimv) {
+    const WorldInfo& wi = x.wi[w];
+    const WorldDyn& wd = x.wd[w];
+    const int lane = lane_id();
+    const int f0 = wi.fix_start;
+    const int* cstart = x.s_sapcell + 8 * f0 + 130 * w;
+    const int* sidx = x.s_sapi[1] + f0;
+    const int* wide = x.s_sapi[0] + f0;
+    const float4* gbox = x.s_sapbox + f0;
+    const float cs = wd.g_inv > 0.0f ? 1.0f / wd.g_inv : 0.0f;
+    int2* out = x.pairs + wi.pair_start;
+    int total = 0;
+    auto emit = [&](bool hit, int ra, int rb) {                          // warp-collective append
+        const unsigned bal = __ballot_sync(0xffffffffu, hit);
+        if (hit) {
+            const int slot = total + __popc(bal & ((1u << lane) - 1u));
+            if (slot < wi.pair_cap) out[slot] = make_int2(ra < rb ? ra : rb, ra < rb ? rb : ra);
+        }
+        total += __popc(bal);
+    };
+    for (int q = 0; q < nnow; ++q) {
+        const int ra = now[q];
+        const AABB fa = proxy_fat(x, f0 + ra);
+        // ordinary proxies by cell: lower corners within [lo - cell, hi] in both axes
+        const int cx0 = sap_cell(fa.lo.x - cs, wd.g_ox, wd.g_inv, wd.g_ncx), cx1 = sap_cell(fa.hi.x, wd.g_ox, wd.g_inv, wd.g_ncx);
+        const int cy0 = sap_cell(fa.lo.y - cs, wd.g_oy, wd.g_inv, wd.g_ncy), cy1 = sap_cell(fa.hi.y, wd.g_oy, wd.g_inv, wd.g_ncy);
+        for (int cy = cy0; cy <= cy1; ++cy) {
+            const int e0 = cstart[cy * wd.g_ncx + cx0], e1 = cstart[cy * wd.g_ncx + cx1 + 1];
+            for (int base = e0; base < e1; base += kWarp) {
+                const int e = base + lane;
+                bool hit = false;
+                int rb = 0;
+                if (e < e1) {
+                    rb = sidx[e] & 0x7fffffff;
+                    if (rb != ra && !toimv[rb]) {
+                        const float4 b = gbox[e];
+                        AABB bb;
+                        bb.lo = v2(b.x, b.y);
+                        bb.hi = v2(b.z, b.w);
+                        hit = aabb_overlap(fa, bb);
+                    }
+                }
+                emit(hit, ra, rb);
+            }
+        }
+        for (int base = 0; base < wd.g_nwide; base += kWarp) {            // wide proxies
+            const int e = base + lane;
+            bool hit = false;
+            int rb = 0;
+            if (e < wd.g_nwide) {
+                rb = wide[e] & 0x7fffffff;
+                if (rb != ra && !toimv[rb] && x.px[f0 + rb].proxy_id >= 0) hit = aabb_overlap(fa, proxy_fat(x, f0 + rb));
+            }
+            emit(hit, ra, rb);
+        }
+        for (int base = 0; base < nall; base += kWarp) {                  // proxies moved during SolveTOI
+            const int e = base + lane;
+            bool hit = false;
+            int rb = 0;
+            if (e < nall) {
+                rb = all[e];
+                // a pair of two proxies moved by this event is found from the lower one only
+                bool both_now = false;
+                for (int k = 0; k < nnow; ++k) both_now |= now[k] == rb;
+                if (rb != ra && (!both_now || ra < rb)) hit = aabb_overlap(fa, proxy_fat(x, f0 + rb));
+            }
+            emit(hit, ra, rb);
+        }
+    }
+    tsync();
+    if (total > wi.pair_cap) {
+        if (lane == 0) set_error(x, w, DBOX_ERR_CAPACITY);
+        return -1;
+    }
+    if (lane == 0) {                                                     // (idA, idB) order
+        for (int i = 1; i < total; ++i) {
+            const int2 v = out[i];
+            int j = i - 1;
+            while (j >= 0 && (out[j].x > v.x || (out[j].x == v.x && out[j].y > v.y))) { out[j + 1] = out[j]; --j; }
+            out[j + 1] = v;
+        }
+    }
+    tsync();
+    for (int i = lane; i < total; i += kWarp) out[i] = make_int2(f0 + out[i].x, f0 + out[i].y);
+    for (int k = lane; k < nnow; k += kWarp) x.px[f0 + now[k]].moved = 0;          // the move buffer is consumed
+    tsync();
+    return total;
 }
 
 // AddPair for the block's pairs, then the world's SolveTOI (one warp per large world)
@@ -4190,6 +4294,17 @@ DG void toi_world(const Ctx& x, int w, float* sbp) {
         // island as a neighbour or carry the TOI / island flags that an event clears
         int* cand = x.s_tcand + c0;
         int ncand = toi_collect(x, c0, b0, 0, wd.contact_count, cand, 0);
+        // a large world's event pair searches use the grid of its end-of-solve pair search and
+        // the proxies moved since (toi_pairs_big); without destruction a proxy's rank is its
+        // fixture index
+        const bool big_toi = wi.pair_block && wd.g_valid && !wi.proxy_order;
+        const int f0 = wi.fix_start;
+        int* toimv = reinterpret_cast<int*>(x.s_sapk[0] + f0);           // moved during this SolveTOI
+        int* pnow = x.s_pcount + f0;                                     // moved by this event
+        int* pall = x.s_moved + f0;                                      // moved during this SolveTOI
+        int nall = 0;
+        if (big_toi)
+            for (int i = lane; i < wi.fix_count; i += kWarp) toimv[i] = 0;
         tsync();
         int events = 0;
         const int max_events = 9 * wi.contact_cap + 16;   // each contact takes at most 9 events
@@ -4359,6 +4474,7 @@ DG void toi_world(const Ctx& x, int w, float* sbp) {
                     ncI = __shfl_sync(0xffffffffu, ncI, 0);
                 }
                 mark(4);
+                int nnow = 0;
                 if (lane == 0) {
                     float subDt = (1.0f - minAlpha) * x.dt;
                     solve_toi_island(x, w, wi, sb, nbI, ncI, mcb.x, mcb.y, subDt);
@@ -4370,8 +4486,18 @@ DG void toi_world(const Ctx& x, int w, float* sbp) {
                         if (Bd.type != kDynamicBody) continue;
                         x.s_bfl[b0 + body] = kBfMark;
                         sync_fixtures(x, b0 + body);
+                        if (!big_toi) continue;
+                        const BodyStatic& st = x.bst[b0 + body];                 // the proxies it moved
+                        for (int e = 0; e < st.fix_count; ++e) {
+                            const int r = x.body_fix[st.fix_start + e] - f0;
+                            if (!x.px[f0 + r].moved || x.px[f0 + r].proxy_id < 0) continue;
+                            pnow[nnow++] = r;
+                            if (!toimv[r]) { toimv[r] = 1; pall[nall++] = r; }
+                        }
                     }
                 }
+                nnow = __shfl_sync(0xffffffffu, nnow, 0);
+                nall = __shfl_sync(0xffffffffu, nall, 0);
                 tsync();
                 // invalidate the TOIs of every contact on a displaced dynamic body (only
                 // candidates carry the two flags)
@@ -4385,7 +4511,12 @@ DG void toi_world(const Ctx& x, int w, float* sbp) {
                 if (lane == 0)
                     for (int i = 0; i < nbI; ++i) x.s_bfl[b0 + x.s_isl_body[b0 + i]] = 0;
                 tsync();
-                find_new_contacts(x, w);
+                if (big_toi) {
+                    const int total = nnow > 0 ? toi_pairs_big(x, w, pnow, nnow, pall, nall, toimv) : 0;
+                    if (total > 0) add_pairs(x, w, total);
+                } else {
+                    find_new_contacts(x, w);
+                }
                 ncand = toi_collect(x, c0, b0, n, wd.contact_count, cand, ncand);
                 tsync();
                 mark(6);

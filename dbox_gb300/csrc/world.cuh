@@ -61,6 +61,11 @@ struct WorldDyn {
     float q_minsep;                // minimum separation over points after the step (<= 0)
     int ev_count;                  // contact-listener events recorded in the last step
     int ev_pad;
+    // the grid of a large world's end-of-solve pair search (k_pairs_block), kept for the pair
+    // searches of its SolveTOI events: origin, 1 / cell size, cells per row and column,
+    // ordinary and wide proxies, and whether it describes this step's boxes
+    float g_ox, g_oy, g_inv;
+    int g_ncx, g_ncy, g_nv, g_nwide, g_valid;
 };
 
 struct BodyStatic {
