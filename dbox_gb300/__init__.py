@@ -114,6 +114,7 @@ def lib():
     L.dbox_world_clear_samples.argtypes = [vp]
     L.dbox_world_set_measure.argtypes = [vp, i32]
     L.dbox_world_set_wait_limit.argtypes = [vp, i32]
+    L.dbox_world_set_island_solver.argtypes = [vp, i32]
     L.dbox_world_set_listener.argtypes = [vp, vp, vp]
     L.dbox_world_set_presolve.argtypes = [vp, vp, vp]
     L.dbox_fixture_set_filter.argtypes = [vp, i32, i32, ctypes.c_uint16, ctypes.c_uint16, ctypes.c_int16]
@@ -583,6 +584,10 @@ class World:
     def set_wait_limit(self, polls=1 << 20):
         """Polls a bounded device wait may take before the step reports DBOX_ERR_TIMEOUT."""
         _check(lib().dbox_world_set_wait_limit(self.h, polls), "dbox_world_set_wait_limit")
+
+    def set_island_solver(self, mode=0):
+        """Large worlds' Solve on a block (0, default) or on a warp (1); the same results."""
+        _check(lib().dbox_world_set_island_solver(self.h, mode), "dbox_world_set_island_solver")
 
     def set_measure(self, on=True):
         _check(lib().dbox_world_set_measure(self.h, 1 if on else 0), "dbox_world_set_measure")

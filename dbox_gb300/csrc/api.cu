@@ -199,6 +199,7 @@ struct dbox_world {
     DBuf<int> s_slog, s_pend;
     int measure = 0;
     int wait_polls = 1 << 20;   // budget of one mbarrier wait in the solve kernel (polls)
+    int island_solver = 0;      // 0: a large world's Solve on a block (k_solve_big), 1: on a warp
     // contact listener
     DBuf<dbox_contact_event> d_events;
     DBuf<unsigned> s_sapk0, s_sapk1;
@@ -807,6 +808,7 @@ dg::Ctx make_ctx(dbox_world* w, float dt, int vi, int pi) {
     x.s_sapcell = w->s_sapcell.p;
     x.big_worlds = w->d_big.p;
     x.n_big = w->n_big;
+    x.big_block = (w->n_big > 0 && w->ws_mode == 0 && w->island_solver == 0) ? 1 : 0;
     x.s_cevt = w->s_cevt.p;
     return x;
 }
@@ -2257,6 +2259,14 @@ int32_t dbox_mlp_train_world(dbox_mlp* m, dbox_world* w, int32_t epochs, int32_t
 int32_t dbox_world_set_wait_limit(dbox_world* w, int32_t polls) {
     if (!w || polls < 0) return fail(DBOX_ERR_INVALID, "dbox_world_set_wait_limit: bad arguments");
     w->wait_polls = polls < (1 << 20) ? polls : (1 << 20);
+    if (w->graph) { cudaGraphExecDestroy(w->graph); w->graph = nullptr; }
+    if (w->tgraph) { cudaGraphExecDestroy(w->tgraph); w->tgraph = nullptr; }
+    return DBOX_OK;
+}
+
+int32_t dbox_world_set_island_solver(dbox_world* w, int32_t mode) {
+    if (!w || mode < 0 || mode > 1) return fail(DBOX_ERR_INVALID, "dbox_world_set_island_solver: bad arguments");
+    w->island_solver = mode;
     if (w->graph) { cudaGraphExecDestroy(w->graph); w->graph = nullptr; }
     if (w->tgraph) { cudaGraphExecDestroy(w->tgraph); w->tgraph = nullptr; }
     return DBOX_OK;

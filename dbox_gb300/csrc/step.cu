@@ -4547,6 +4547,609 @@ DG void toi_world(const Ctx& x, int w, float* sbp) {
     }
 }
 
+// ------------------------------------------------------------ b2World.Solve of a large world on a block
+// A world of 4,096+ fixtures is one warp's dependent walk in solve_world; here a block of
+// kBigThreads threads does the same step: the same islands in the same order, the same
+// constraint order inside each island, the same arithmetic, so the same bits.
+//   islands: the island graph's components (contacts that are enabled, touching and not a
+//     sensor, joints between active bodies; static bodies do not connect) by a lock-free
+//     union-find; the reference's depth-first search (b2world.d:959-1095) seeds islands in body
+//     list order (descending index), so an island's seed is the highest-index awake, active,
+//     non-static body of its component and islands are numbered by descending seed; a prefix sum
+//     of the components' body / contact / joint counts places each island's lists, and each
+//     island's own search (the reference's, from its seed) runs on a warp of its own.  A static
+//     body is never pushed: popping one changes nothing but its island mark, which is the
+//     last island (in order) that reached it.
+//   schedules: each island's constraints get their levels on one lane (islands share no
+//     dynamic body), then the block buckets all constraints by level.
+//   rows, sweeps (levels in order, a level's constraints over the block, a block barrier
+//     between levels), integration, copy back and sleep over the block.
+// The learned-start modes keep the warp path.
+constexpr int kBigThreads = 1024;
+
+DG int ld_volatile_int(const int* p) { return *reinterpret_cast<const volatile int*>(p); }
+DG int uf_find(int* parent, int i) {
+    // parents only ever point to lower indices, so the walk ends; path halving
+    for (;;) {
+        const int p = ld_volatile_int(&parent[i]);
+        if (p == i) return i;
+        const int g = ld_volatile_int(&parent[p]);
+        if (g != p) parent[i] = g;
+        i = p;
+    }
+}
+DG void uf_union(int* parent, int a, int b) {
+    for (;;) {
+        a = uf_find(parent, a);
+        b = uf_find(parent, b);
+        if (a == b) return;
+        if (a < b) { const int t = a; a = b; b = t; }                     // the larger root under the smaller
+        if (atomicCAS(&parent[a], a, b) == a) return;
+    }
+}
+
+__global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant__ Ctx x) {
+    __shared__ int shi[32];
+    __shared__ float shf[32];
+    __shared__ int s_next, s_maxv, s_maxp;
+    const int w = x.big_worlds[blockIdx.x];
+    const WorldInfo& wi = x.wi[w];
+    WorldDyn& wd = x.wd[w];
+    const int tid = threadIdx.x, nt = blockDim.x;
+    if (!(wd.step_complete && x.dt > 0.0f)) return;
+    const int b0 = wi.body_start, nb = wi.body_count;
+    const int c0 = wi.contact_start, n = wd.contact_count;
+    const int j0 = wi.joint_start, nj = wi.joint_count;
+    const int bx = wi.bx_start, kx = wi.kx_start;
+    const float h = x.dt;
+    const bool warm = x.warm_starting != 0;
+    const float dtRatio = wd.inv_dt0 * x.dt;                            // b2world.d:392
+    auto stampb = [&](int slot) { if (x.prof && tid == 0) x.prof[kProfSlots * (size_t)w + slot] = clock64(); };
+    stampb(0);
+    if (x.measure && tid == 0) { wd.q_sumsq = 0.0f; wd.q_max = 0.0f; wd.q_points = 0; wd.q_minsep = 0.0f; }
+    SB sb;
+    sb.p = x.s_sbody + 6 * (size_t)b0;
+    int* iflags = x.s_isl_flags + b0;
+    unsigned* iminsep = x.s_isl_minsep + b0;
+    unsigned char* bfl = x.s_bfl + b0;
+    int* body_island = x.s_body_island + b0;
+    int* adj = x.s_adj_start + bx;                                       // nb + 1
+    int* isl_body = x.s_isl_body + b0;
+    int* isl_contact = x.s_isl_contact + c0;
+    int2* isl_pair = x.s_isl_pair + c0;
+    int* isl_joint = x.s_isl_joint + j0;
+    unsigned char* cvis = x.s_cvis + c0;
+    int2* items = x.s_adj_items + 2 * (size_t)c0;
+    // compact per-body / per-contact data; island flags cleared (b2world.d:944-957)
+    for (int i = tid; i < nb; i += nt) {
+        dbox_body_state& B = x.bs[b0 + i];
+        B.flags &= ~(uint32_t)kBodyIsland;
+        bfl[i] = body_flag_byte(B);
+        body_island[i] = -1;
+        sb_load(sb, i, B);
+        adj[i] = 0;
+    }
+    for (int k = tid; k < n; k += nt) {
+        x.ct[c0 + k].flags &= ~(uint32_t)kContactIsland;
+        contact_compact(x, c0 + k, b0);
+        cvis[k] = 0;
+    }
+    for (int j = tid; j < nj; j += nt) x.jt[j0 + j].island_flag = 0;
+    __syncthreads();
+    // contact edges of the island graph per body, newest contact first (b2world.d:1026-1062)
+    for (int k = tid; k < n; k += nt) {
+        if (x.s_cq[c0 + k] & 1) {
+            const int2 cb = x.s_cbody[c0 + k];
+            atomicAdd(&adj[cb.x], 1);
+            atomicAdd(&adj[cb.y], 1);
+        }
+    }
+    __syncthreads();
+    {
+        const int tot = block_exclusive_scan(adj, nb, shi);
+        if (tid == 0) adj[nb] = tot;
+    }
+    int* cursor = x.s_cursor + b0;
+    for (int i = tid; i < nb; i += nt) cursor[i] = adj[i];
+    __syncthreads();
+    for (int k = tid; k < n; k += nt) {
+        if (x.s_cq[c0 + k] & 1) {
+            const int2 cb = x.s_cbody[c0 + k];
+            items[atomicAdd(&cursor[cb.x], 1)] = make_int2(k, cb.y);
+            items[atomicAdd(&cursor[cb.y], 1)] = make_int2(k, cb.x);
+        }
+    }
+    __syncthreads();
+    for (int i = tid; i < nb; i += nt) {                                 // each list by descending contact
+        const int e0 = adj[i], e1 = adj[i + 1];
+        for (int a = e0 + 1; a < e1; ++a) {
+            const int2 v = items[a];
+            int b = a - 1;
+            while (b >= e0 && items[b].x < v.x) { items[b + 1] = items[b]; --b; }
+            items[b + 1] = v;
+        }
+    }
+    __syncthreads();
+    stampb(1);
+    // ---- islands: components, seeds, order, sizes
+    int* parent = x.s_stack + b0;
+    int* root = x.s_cursor + b0;
+    int* seedmax = x.s_last + b0;
+    int* rid = x.s_woken + b0;                                           // island of a component root
+    int* seedf = reinterpret_cast<int*>(x.s_isl_sleep + b0);
+    int* seed_of = reinterpret_cast<int*>(x.s_isl_minsep + b0);
+    int* cntb = x.s_isl_bstart + bx;
+    int* cntc = x.s_isl_cstart + bx;
+    int* cntj = x.s_isl_jstart + bx;
+    auto nonstatic = [&](int i) { return (bfl[i] & kBfStatic) == 0; };
+    auto active = [&](int i) { return (bfl[i] & kBfActive) != 0; };
+    for (int i = tid; i < nb; i += nt) { parent[i] = i; seedmax[i] = -1; rid[i] = -1; }
+    __syncthreads();
+    for (int k = tid; k < n; k += nt) {
+        if (!(x.s_cq[c0 + k] & 1)) continue;
+        const int2 cb = x.s_cbody[c0 + k];
+        if (nonstatic(cb.x) && nonstatic(cb.y)) uf_union(parent, cb.x, cb.y);
+    }
+    for (int j = tid; j < nj; j += nt) {
+        const DJoint& jj = x.jt[j0 + j];
+        if (jj.type < 0) continue;
+        const int A = jj.body_a - b0, B = jj.body_b - b0;
+        if (nonstatic(A) && nonstatic(B) && active(A) && active(B)) uf_union(parent, A, B);
+    }
+    __syncthreads();
+    for (int i = tid; i < nb; i += nt) {
+        const int r = uf_find(parent, i);
+        root[i] = r;
+        const unsigned char f = bfl[i];
+        if ((f & kBfAwake) && (f & kBfActive) && !(f & kBfStatic)) atomicMax(&seedmax[r], i);
+    }
+    __syncthreads();
+    for (int i = tid; i < nb; i += nt) {                                 // islands by descending seed
+        const int d = nb - 1 - i;
+        seedf[i] = seedmax[root[d]] == d ? 1 : 0;
+    }
+    __syncthreads();
+    const int nIsl = block_exclusive_scan(seedf, nb, shi);
+    for (int i = tid; i < nb; i += nt) {
+        const int d = nb - 1 - i;
+        if (seedmax[root[d]] == d) { rid[root[d]] = seedf[i]; seed_of[seedf[i]] = d; }
+    }
+    for (int k = tid; k <= nIsl; k += nt) { cntb[k] = 0; cntc[k] = 0; cntj[k] = 0; }
+    __syncthreads();
+    for (int i = tid; i < nb; i += nt)
+        if (nonstatic(i) && rid[root[i]] >= 0) atomicAdd(&cntb[rid[root[i]]], 1);
+    for (int k = tid; k < n; k += nt) {
+        if (!(x.s_cq[c0 + k] & 1)) continue;
+        const int2 cb = x.s_cbody[c0 + k];
+        const int d = nonstatic(cb.x) ? cb.x : cb.y;
+        if (rid[root[d]] >= 0) atomicAdd(&cntc[rid[root[d]]], 1);
+    }
+    for (int j = tid; j < nj; j += nt) {
+        const DJoint& jj = x.jt[j0 + j];
+        if (jj.type < 0) continue;
+        const int A = jj.body_a - b0, B = jj.body_b - b0;
+        if (!active(A) || !active(B)) continue;
+        const int d = nonstatic(A) ? A : (nonstatic(B) ? B : -1);
+        if (d >= 0 && rid[root[d]] >= 0) atomicAdd(&cntj[rid[root[d]]], 1);
+    }
+    __syncthreads();
+    const int nbI = block_exclusive_scan(cntb, nIsl, shi);
+    const int ncI = block_exclusive_scan(cntc, nIsl, shi);
+    const int njI = block_exclusive_scan(cntj, nIsl, shi);
+    if (tid == 0) { cntb[nIsl] = nbI; cntc[nIsl] = ncI; cntj[nIsl] = njI; wd.islands = nIsl; s_next = 0; }
+    __syncthreads();
+    // ---- each island's depth-first search (b2world.d:988-1076), an island per thread
+    // (islands handed out one at a time; they share no non-static body, contact or joint)
+    for (;;) {
+        const int k = atomicAdd(&s_next, 1);
+        if (k >= nIsl) break;
+        const int seed = seed_of[k];
+        int* stack = parent + cntb[k];                                   // this island's own stack rows
+        int nB = cntb[k], nC = cntc[k], nJ = cntj[k];
+        int top = 0;
+        stack[top++] = seed;
+        bfl[seed] |= kBfVisited;
+        while (top > 0) {
+            const int b = stack[--top];
+            body_island[b] = k;
+            isl_body[nB++] = b;
+            for (int e = adj[b], ee = adj[b + 1]; e < ee; ++e) {
+                const int2 it = items[e];
+                if (cvis[it.x]) continue;
+                isl_contact[nC] = c0 + it.x;
+                isl_pair[nC] = make_int2(b, it.y);
+                ++nC;
+                cvis[it.x] = 1;
+                const unsigned char fo = bfl[it.y];
+                if (fo & kBfStatic) { atomicMax(&body_island[it.y], k); continue; }
+                if (fo & kBfVisited) continue;
+                stack[top++] = it.y;
+                bfl[it.y] = fo | kBfVisited;
+            }
+            if (nj == 0) continue;
+            const BodyStatic& st = x.bst[b0 + b];
+            for (int e = 0; e < st.jadj_count; ++e) {
+                const int j = x.jadj_joint[st.jadj_start + e];
+                if (x.jt[j].island_flag) continue;
+                const int other = x.jadj_other[st.jadj_start + e] - b0;
+                const unsigned char fo = bfl[other];
+                if ((fo & kBfActive) == 0) continue;
+                isl_joint[nJ++] = j;
+                x.jt[j].island_flag = 1;
+                if (fo & kBfStatic) { atomicMax(&body_island[other], k); continue; }
+                if (fo & kBfVisited) continue;
+                stack[top++] = other;
+                bfl[other] = fo | kBfVisited;
+            }
+        }
+    }
+    __syncthreads();
+    stampb(2);
+    for (int k = tid; k < n; k += nt)
+        if (cvis[k]) x.ct[c0 + k].flags |= kContactIsland;
+    // ---- level schedules: each island's walk on one lane, then the block buckets by level
+    int* last = x.s_last + b0;
+    for (int i = tid; i < nb; i += nt) last[i] = 0;
+    if (tid == 0) { s_maxv = 0; s_maxp = 0; }
+    __syncthreads();
+    auto walk = [&](int k, bool contacts_first, int* maxl) {           // one lane: island k
+        int ml = 0;
+        for (int pass = 0; pass < 2; ++pass) {
+            const bool doContacts = (pass == 0) == contacts_first;
+            const int t0 = doContacts ? x.s_isl_cstart[bx + k] : x.s_isl_jstart[bx + k];
+            const int t1 = doContacts ? x.s_isl_cstart[bx + k + 1] : x.s_isl_jstart[bx + k + 1];
+            // the position of the walk in the all-contacts-then-all-joints order of build_schedule
+            const int at = doContacts ? (contacts_first ? 0 : njI) : (contacts_first ? ncI : 0);
+            for (int t = t0; t < t1; ++t) {
+                int item, A, B, C = -1, D = -1;
+                if (doContacts) {
+                    item = isl_contact[t];
+                    const int2 pr = isl_pair[t];
+                    A = pr.x;
+                    B = pr.y;
+                } else {
+                    item = -(isl_joint[t] + 1);
+                    item_bodies(x, item, b0, A, B);
+                    const DJoint& jj = x.jt[-item - 1];
+                    if (jj.type == kGearJoint) { C = jj.body_c - b0; D = jj.body_d - b0; }
+                }
+                const bool dA = (bfl[A] & kBfDynamic) != 0, dB = (bfl[B] & kBfDynamic) != 0;
+                int l = bmax(dA ? last[A] : 0, dB ? last[B] : 0);
+                const bool dC = C >= 0 && (bfl[C] & kBfDynamic) != 0, dD = D >= 0 && (bfl[D] & kBfDynamic) != 0;
+                if (dC && last[C] > l) l = last[C];
+                if (dD && last[D] > l) l = last[D];
+                l += 1;
+                if (dA) last[A] = l;
+                if (dB) last[B] = l;
+                if (dC) last[C] = l;
+                if (dD) last[D] = l;
+                ml = l > ml ? l : ml;
+                x.s_level[kx + at + t] = l;
+                x.s_tmp[kx + at + t] = item;
+            }
+        }
+        atomicMax(maxl, ml);
+    };
+    const int nItems = ncI + njI;
+    auto bucket = [&](int maxL, int* sched, int* lvl) {
+        for (int l = tid; l <= maxL + 1; l += nt) lvl[kx + l] = 0;
+        __syncthreads();
+        for (int i = tid; i < nItems; i += nt) atomicAdd(&lvl[kx + x.s_level[kx + i]], 1);
+        __syncthreads();
+        block_exclusive_scan(lvl + kx, maxL + 2, shi);
+        for (int l = tid; l <= maxL + 1; l += nt) x.s_lcur[kx + l] = lvl[kx + l];
+        __syncthreads();
+        for (int i = tid; i < nItems; i += nt) {
+            const int pos = atomicAdd(&x.s_lcur[kx + x.s_level[kx + i]], 1);
+            sched[kx + pos] = x.s_tmp[kx + i];
+        }
+        __syncthreads();
+    };
+    for (int k = tid; k < nIsl; k += nt) walk(k, false, &s_maxv);
+    __syncthreads();
+    const int maxLv = s_maxv;
+    bucket(maxLv, x.s_sched_v, x.s_lvl_v);
+    int* sched_p = x.s_sched_v;
+    int* lvl_p = x.s_lvl_v;
+    int maxLp = maxLv;
+    if (njI) {
+        for (int i = tid; i < nb; i += nt) last[i] = 0;
+        __syncthreads();
+        for (int k = tid; k < nIsl; k += nt) walk(k, true, &s_maxp);
+        __syncthreads();
+        maxLp = s_maxp;
+        sched_p = x.s_sched_p;
+        lvl_p = x.s_lvl_p;
+        bucket(maxLp, sched_p, lvl_p);
+    }
+    if (x.prof && tid == 0) { x.prof[kProfSlots * (size_t)w + 12] = maxLv; x.prof[kProfSlots * (size_t)w + 13] = n; x.prof[kProfSlots * (size_t)w + 14] = nb; }
+    stampb(3);
+    if (tid == 0) {
+        wd.acc_isl_bodies += (unsigned long long)nbI;
+        wd.acc_isl_contacts += (unsigned long long)ncI;
+        wd.acc_vsolve += (unsigned long long)ncI * (unsigned long long)x.vel_iters;
+    }
+    // island flags and SetAwake(true) of the search (b2world.d:985-1004), applied after it
+    for (int i = tid; i < nb; i += nt) {
+        dbox_body_state& B = x.bs[b0 + i];
+        if ((bfl[i] & kBfVisited) && !(bfl[i] & kBfStatic)) B.flags |= kBodyIsland;
+        if (body_island[i] >= 0) b_set_awake(B, true);
+    }
+    // integrate velocities (b2island.d:82-116)
+    for (int t = tid; t < nbI; t += nt) {
+        const int i = isl_body[t];
+        dbox_body_state& B = x.bs[b0 + i];
+        B.sweep[2] = B.sweep[4];
+        B.sweep[3] = B.sweep[5];
+        B.sweep[6] = B.sweep[7];
+        if (B.type == kDynamicBody) {
+            const BodyStatic& st = x.bst[b0 + i];
+            float2 v = sb.v(i);
+            float wv = sb.w(i);
+            float2 g = st.gravity_scale * x.gravity + B.mass[1] * v2(B.force[0], B.force[1]);
+            v += h * g;
+            wv += (h * B.mass[3]) * B.force[2];
+            v *= fdiv(1.0f, 1.0f + h * st.lin_damping);
+            wv *= fdiv(1.0f, 1.0f + h * st.ang_damping);
+            sb.set_v(i, v, wv);
+        }
+    }
+    __syncthreads();
+    // constraint rows in schedule order (b2contactsolver.d:244-450)
+    VRow* vrow = x.vr + kx;
+    PRow* prow = x.pr + kx;
+    for (int idx = tid; idx < nItems; idx += nt) {
+        const int item = x.s_sched_v[kx + idx];
+        bool pdone = false;
+        if (item >= 0) {
+            VC vc;
+            PC pc;
+            constraint_ctor(x, item, b0, warm, dtRatio, vc, pc);
+            float sep[2] = {0.0f, 0.0f};
+            constraint_init_velocity(vc, pc, sb, sep);
+            vrow[idx] = pack_v(vc, item);
+            if (njI || x.record_events) x.s_vpos[item] = idx;
+            if (!njI) {
+                prow[idx] = pack_p(pc, body_island[(bfl[vc.bodyA] & kBfStatic) ? vc.bodyB : vc.bodyA]);
+                pdone = true;
+            }
+        } else {
+            vrow[idx].ids = make_int4(0, 0, 0, item);
+        }
+        if (!pdone) {
+            const int pitem = sched_p[kx + idx];
+            const int is = item_island(x, pitem, b0);
+            if (pitem >= 0) {
+                VC vc;
+                PC pc;
+                constraint_ctor(x, pitem, b0, warm, dtRatio, vc, pc);
+                prow[idx] = pack_p(pc, is);
+            } else {
+                prow[idx].ids = make_int4(0, 0, pitem, is);
+            }
+        }
+    }
+    __syncthreads();
+    stampb(4);
+    auto sweep = [&](const int* lvl, int maxL, auto&& f) {             // levels in order over the block
+        for (int L = 1; L <= maxL; ++L) {
+            const int e = lvl[L + 1];
+            for (int idx = lvl[L] + tid; idx < e; idx += nt) f(idx);
+            __syncthreads();
+        }
+    };
+    // warm start contacts, then joints' InitVelocityConstraints (b2island.d:133-146)
+    if (njI == 0) {
+        if (warm) sweep(x.s_lvl_v + kx, maxLv, [&](int idx) { warm_start(unpack_v(load_v(vrow + idx)), sb); });
+    } else {
+        sweep(lvl_p + kx, maxLp, [&](int idx) {
+            const int item = sched_p[kx + idx];
+            if (item >= 0) { if (warm) warm_start(unpack_v(load_v(vrow + x.s_vpos[item])), sb); }
+            else joint_init(x, -item - 1, b0, sb, warm, dtRatio);
+        });
+    }
+    stampb(5);
+    // velocity iterations (b2island.d:153-161)
+    for (int it = 0; it < x.vel_iters; ++it) {
+        sweep(x.s_lvl_v + kx, maxLv, [&](int idx) {
+            const VRow r = load_v(vrow + idx);
+            if (r.ids.w >= 0) {
+                VC vc = unpack_v(r);
+                BodyVel q = load_vel(sb, vc.bodyA, vc.bodyB);
+                if (vc.pointCount == 2) solve_velocity_two(vc, q);
+                else solve_velocity(vc, q);
+                store_vel(sb, vc.bodyA, vc.bodyB, q);
+                vrow[idx].imp = make_float4(vc.p[0].normalImpulse, vc.p[0].tangentImpulse, vc.p[1].normalImpulse,
+                                            vc.p[1].tangentImpulse);
+            } else {
+                joint_solve_velocity(x, -r.ids.w - 1, b0, sb);
+            }
+        });
+    }
+    stampb(6);
+    if (x.measure) {
+        // one extra velocity sweep that changes nothing: velocities kept aside and put back,
+        // impulses not written, joints left out
+        for (int t = tid; t < nbI; t += nt) {
+            const int i = isl_body[t];
+            const float2 v = sb.v(i);
+            x.s_vsave[3 * (size_t)(b0 + i)] = v.x;
+            x.s_vsave[3 * (size_t)(b0 + i) + 1] = v.y;
+            x.s_vsave[3 * (size_t)(b0 + i) + 2] = sb.w(i);
+        }
+        __syncthreads();
+        float ssq = 0.0f, smax = 0.0f;
+        int npts = 0;
+        sweep(x.s_lvl_v + kx, maxLv, [&](int idx) {
+            const VRow r = load_v(vrow + idx);
+            if (r.ids.w < 0) return;
+            VC vc = unpack_v(r);
+            const VC before = vc;
+            solve_velocity(vc, sb);
+            for (int j = 0; j < vc.pointCount; ++j) {
+                const float dn = vc.p[j].normalImpulse - before.p[j].normalImpulse;
+                const float dt = vc.p[j].tangentImpulse - before.p[j].tangentImpulse;
+                const float d2 = dn * dn + dt * dt;
+                ssq += d2;
+                smax = bmax(smax, sqrtf(d2));
+                ++npts;
+            }
+        });
+        auto fsum = [](float a, float b) { return a + b; };
+        auto fmx = [](float a, float b) { return bmax(a, b); };
+        auto isum = [](int a, int b) { return a + b; };
+        ssq = block_reduce(ssq, fsum, shf);
+        smax = block_reduce(smax, fmx, shf);
+        npts = block_reduce(npts, isum, shi);
+        if (tid == 0) { wd.q_sumsq = ssq; wd.q_max = smax; wd.q_points = npts; }
+        __syncthreads();
+        for (int t = tid; t < nbI; t += nt) {
+            const int i = isl_body[t];
+            const float* sv = x.s_vsave + 3 * (size_t)(b0 + i);
+            sb.set_v(i, v2(sv[0], sv[1]), sv[2]);
+        }
+        __syncthreads();
+    }
+    for (int idx = tid; idx < nItems; idx += nt) {                       // StoreImpulses (b2contactsolver.d:774-787)
+        const VRow r = load_v(vrow + idx);
+        if (r.ids.w >= 0) store_impulses(x, r);
+    }
+    // integrate positions (b2island.d:168-200)
+    for (int t = tid; t < nbI; t += nt) {
+        const int i = isl_body[t];
+        float2 c = sb.c(i);
+        float a = sb.a(i);
+        float2 v = sb.v(i);
+        float wv = sb.w(i);
+        float2 translation = h * v;
+        if (dot(translation, translation) > kMaxTranslationSquared) {
+            float ratio = fdiv(kMaxTranslation, length(translation));
+            v *= ratio;
+        }
+        float rotation = h * wv;
+        if (rotation * rotation > kMaxRotationSquared) {
+            float ratio = fdiv(kMaxRotation, babs(rotation));
+            wv *= ratio;
+        }
+        c += h * v;
+        a += h * wv;
+        sb.set_c(i, c, a);
+        sb.set_v(i, v, wv);
+    }
+    for (int is = tid; is < nIsl; is += nt) iflags[is] = 0;
+    __syncthreads();
+    stampb(7);
+    // position iterations with per-island early exit (b2island.d:206-224)
+    for (int it = 0; it < x.pos_iters; ++it) {
+        for (int is = tid; is < nIsl; is += nt) {
+            iminsep[is] = fkey(0.0f);
+            iflags[is] &= ~4;
+        }
+        __syncthreads();
+        sweep(lvl_p + kx, maxLp, [&](int idx) {
+            const PRow r = load_p(prow + idx);
+            const int is = r.ids.w;
+            if (iflags[is] & 1) return;
+            if (r.ids.z >= 0) {
+                const float ms = solve_position_row(unpack_p(r), sb);
+                atomicMin(&iminsep[is], fkey(ms));
+            } else if (!joint_solve_position(x, -r.ids.z - 1, b0, sb)) {
+                atomicOr(&iflags[is], 4);
+            }
+        });
+        int psolved = 0;
+        bool remaining = false;
+        for (int is = tid; is < nIsl; is += nt) {
+            const int f = iflags[is];
+            if (f & 1) continue;
+            psolved += x.s_isl_cstart[bx + is + 1] - x.s_isl_cstart[bx + is];
+            const bool contactsOkay = funkey(iminsep[is]) >= -3.0f * kLinearSlop;
+            const bool jointsOkay = (f & 4) == 0;
+            if (contactsOkay && jointsOkay) iflags[is] = f | 1 | 2;
+            else remaining = true;
+        }
+        auto isum = [](int a, int b) { return a + b; };
+        psolved = block_reduce(psolved, isum, shi);
+        if (tid == 0) wd.acc_psolve += (unsigned long long)psolved;
+        if (!__syncthreads_or(remaining)) break;
+    }
+    __syncthreads();
+    if (x.measure) {
+        float ms = 0.0f;
+        for (int idx = tid; idx < nItems; idx += nt) {
+            const PRow r = load_p(prow + idx);
+            if (r.ids.z >= 0) ms = bmin(ms, position_min_separation(unpack_p(r), sb));
+        }
+        auto fmn = [](float a, float b) { return bmin(a, b); };
+        ms = block_reduce(ms, fmn, shf);
+        if (tid == 0) wd.q_minsep = ms;
+    }
+    if (x.record_events) {
+        // b2Island.Report (b2island.d:419-438): PostSolve per island contact in island order
+        const int e0 = wd.ev_count;
+        for (int t = tid; t < ncI; t += nt) {
+            const int item = isl_contact[t];
+            const VRow r = load_v(vrow + x.s_vpos[item]);
+            float ni[2] = {r.imp.x, r.imp.z}, ti[2] = {r.imp.y, r.imp.w};
+            put_event(x, wi, w, e0 + t, DBOX_EVENT_POSTSOLVE, x.ct[item], r.ids.z & 0xff, ni, ti);
+        }
+        __syncthreads();
+        if (tid == 0) wd.ev_count = e0 + ncI;
+    }
+    stampb(8);
+    // copy back + SynchronizeTransform (b2island.d:227-235)
+    bool nonfinite = false;
+    for (int t = tid; t < nbI; t += nt) {
+        const int i = isl_body[t];
+        dbox_body_state& B = x.bs[b0 + i];
+        const float2 c = sb.c(i), v = sb.v(i);
+        B.sweep[4] = c.x; B.sweep[5] = c.y; B.sweep[7] = sb.a(i);
+        B.vel[0] = v.x; B.vel[1] = v.y; B.vel[2] = sb.w(i);
+        b_sync_transform(B);
+        nonfinite |= !(isfinite(c.x) && isfinite(c.y) && isfinite(B.sweep[7]) && isfinite(v.x) && isfinite(v.y) &&
+                       isfinite(B.vel[2]));
+    }
+    if (__syncthreads_or(nonfinite) && tid == 0) set_error(x, w, DBOX_ERR_NAN);
+    // sleep (b2island.d:241-279)
+    if (x.allow_sleep) {
+        const float linTolSqr = kLinearSleepTolerance * kLinearSleepTolerance;
+        const float angTolSqr = kAngularSleepTolerance * kAngularSleepTolerance;
+        for (int is = tid; is < nIsl; is += nt) x.s_isl_sleep[b0 + is] = fkey(kMaxFloat);
+        __syncthreads();
+        for (int t = tid; t < nbI; t += nt) {
+            const int i = isl_body[t];
+            dbox_body_state& B = x.bs[b0 + i];
+            const int is = body_island[i];
+            if ((B.flags & kBodyAutoSleep) == 0 || B.vel[2] * B.vel[2] > angTolSqr || dot(b_v(B), b_v(B)) > linTolSqr) {
+                B.sleep_time = 0.0f;
+                atomicMin(&x.s_isl_sleep[b0 + is], fkey(0.0f));
+            } else {
+                B.sleep_time += h;
+                atomicMin(&x.s_isl_sleep[b0 + is], fkey(B.sleep_time));
+            }
+        }
+        __syncthreads();
+        for (int is = tid; is < nIsl; is += nt) {
+            const int f = iflags[is];
+            if (funkey(x.s_isl_sleep[b0 + is]) >= kTimeToSleep && (f & 2)) iflags[is] = f | 8;
+        }
+        __syncthreads();
+        for (int t = tid; t < nbI; t += nt) {
+            const int i = isl_body[t];
+            if (iflags[body_island[i]] & 8) b_set_awake(x.bs[b0 + i], false);
+        }
+        // a static body ends in the state its last island left it in
+        for (int i = tid; i < nb; i += nt) {
+            if ((bfl[i] & kBfStatic) && body_island[i] >= 0 && (iflags[body_island[i]] & 8))
+                b_set_awake(x.bs[b0 + i], false);
+        }
+    }
+    __syncthreads();
+    stampb(9);
+    stampb(10);
+    stampb(11);
+}
+
 // The solve phase and the TOI phase of one step, one warp per world: each world goes
 // from its island solve straight to its TOI events, so a world that is slow in one phase
 // overlaps with worlds that are slow in the other.  Worlds reach warps in one of two ways:
@@ -4631,7 +5234,7 @@ __global__ void __launch_bounds__(kSolveWarps * 32, 3) k_solve_toi(const __grid_
         }
         unsigned long long g0 = 0;
         if (x.prof) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(g0));
-        solve_world(x, w, sbp, in_smem, stage_f, ring);
+        if (!(x.big_block && x.wi[w].pair_block)) solve_world(x, w, sbp, in_smem, stage_f, ring);   // else k_solve_big
         tsync();
         if (!x.wi[w].pair_block) toi_world(x, w, sbp);                   // large worlds: k_finish_big
         tsync();
@@ -4669,17 +5272,18 @@ extern "C" int dbox_launch_collide(const dg::Ctx* x, cudaStream_t stream) {
     return (int)cudaGetLastError();
 }
 
-// part 2 of a step: Solve and SolveTOI (1 launch, 3 with a large world); *launches = all of the step's
+// part 2 of a step: Solve and SolveTOI (1 launch, 3 or 4 with a large world); *launches = all of the step's
 extern "C" int dbox_launch_solve(const dg::Ctx* x, cudaStream_t stream, int* launches) {
     const int threads = 128;
     if (x->solve_blocks < 1) return (int)cudaErrorInvalidValue;
     if (x->solve_queue) cudaMemsetAsync(x->solve_queue, 0, sizeof(int) * (2 + 4 * (size_t)x->solve_nsm), stream);
+    if (x->big_block) dg::k_solve_big<<<x->n_big, dg::kBigThreads, 0, stream>>>(*x);   // large worlds' Solve
     dg::k_solve_toi<<<x->solve_blocks, x->solve_wpb * dg::kWarp, x->solve_smem_floats * sizeof(float), stream>>>(*x);
     if (x->n_big > 0) {                             // large worlds: their pairs on a block each, then AddPair + TOI
         dg::k_pairs_block<<<x->n_big, dg::kPairThreads, 0, stream>>>(*x);
         dg::k_finish_big<<<(x->n_big * dg::kWarp + threads - 1) / threads, threads, 0, stream>>>(*x);
     }
-    if (launches) *launches = x->n_big > 0 ? 6 : 4;
+    if (launches) *launches = x->n_big > 0 ? 6 + x->big_block : 4;
     return (int)cudaGetLastError();
 }
 
@@ -4696,6 +5300,7 @@ extern "C" int dbox_launch_step_ev(const dg::Ctx* x, cudaStream_t stream, int* l
     dg::k_collide_finish<<<team_blocks, threads, 0, stream>>>(*x);
     if (ev) cudaEventRecordWithFlags(ev[1], stream, cudaEventRecordExternal);
     if (x->solve_queue) cudaMemsetAsync(x->solve_queue, 0, sizeof(int) * (2 + 4 * (size_t)x->solve_nsm), stream);
+    if (x->big_block) dg::k_solve_big<<<x->n_big, dg::kBigThreads, 0, stream>>>(*x);   // large worlds' Solve
     dg::k_solve_toi<<<x->solve_blocks, x->solve_wpb * dg::kWarp, x->solve_smem_floats * sizeof(float), stream>>>(*x);
     if (x->n_big > 0) {                             // large worlds: their pairs on a block each, then AddPair + TOI
         dg::k_pairs_block<<<x->n_big, dg::kPairThreads, 0, stream>>>(*x);
@@ -4703,7 +5308,7 @@ extern "C" int dbox_launch_step_ev(const dg::Ctx* x, cudaStream_t stream, int* l
     }
     if (ev) cudaEventRecordWithFlags(ev[2], stream, cudaEventRecordExternal);
     if (ev) cudaEventRecordWithFlags(ev[3], stream, cudaEventRecordExternal);
-    if (launches) *launches = x->n_big > 0 ? 6 : 4;
+    if (launches) *launches = x->n_big > 0 ? 6 + x->big_block : 4;
     return (int)cudaGetLastError();
 }
 

@@ -224,6 +224,7 @@ struct Ctx {
     int* s_sapcell;                // per world 8 * fixtures + 130 from 8 * fix_start + 130 * world: cell tables
     const int* big_worlds;         // the worlds whose end-of-Solve pairs a block generates
     int n_big;
+    int big_block;                 // 1: large worlds run b2World.Solve on a block (k_solve_big), not a warp
     const int* proxy_order;        // fixture-indexed: world-local fixture of each proxy-id rank
     // scratch (contact-indexed)
     int* s_cstate;                 // 0 processed, 1 inactive, 2 destroyed

@@ -802,6 +802,36 @@ def stress(piles=64, per_pile=2048, chains_per_pile=4, links=32, width=40.0, see
     return out
 
 
+def _shifted(scene, dx):
+    """The scene moved by dx along x (bodies, pulley ground anchors, mouse targets)."""
+    out = dict(scene)
+    out["bodies"] = scene["bodies"].copy()
+    out["bodies"]["position"][:, 0] += F32(dx)
+    for key, fields in (("pulley_joints", ("ground_anchor_a", "ground_anchor_b")), ("mouse_joints", ("target",))):
+        d = scene.get(key)
+        if d is not None and len(d):
+            d = d.copy()
+            for f in fields:
+                d[f][:, 0] += F32(dx)
+            out[key] = d
+    return out
+
+
+def large_mixed(seed=11, n=4000):
+    """One world of over 4,096 fixtures holding every joint scene side by side, 110 m apart
+    (revolute chains, distance ropes, welded beams, friction / motor joints of the table top,
+    wheel-joint cars, prismatic sliders, pulleys and a mouse joint, gears, edge and chain
+    grounds; under gravity), and a 60 m container of `n` scattered mixed bodies."""
+    parts = [chains(), ropes(), welded(), top_down(), cars(), sliders(), pulleys(), gears(), edge_ground(),
+             chain_ground()]
+    parts = [_shifted(p, 110.0 * (k + 1)) for k, p in enumerate(parts)]
+    rng = np.random.default_rng(seed)
+    parts.append(_concat([container(60.0, 60.0), scatter(n, 58.0, 58.0, rng)]))
+    out = _concat(parts)
+    out["name"] = "large_mixed"
+    return out
+
+
 def batch(n_worlds=4096, seed=3, lo=8, hi=512):
     """Batched workload: per-world body counts log-uniform in [lo, hi]; thirds of
     pyramids, 40 m-container scatters and box stacks."""

@@ -168,15 +168,17 @@ def test_features_exact(oracle_lib, gpu_lib, flags):
         assert toi_total > 0
 
 
-@pytest.mark.parametrize("per_pile", [300, 1100], ids=["warp_path", "large_world_path"])
-def test_stress_reduced_exact(oracle_lib, gpu_lib, per_pile):
+@pytest.mark.parametrize("per_pile,solver", [(300, 0), (1100, 0), (1100, 1)],
+                         ids=["warp_path", "large_world_path", "large_world_warp_solve"])
+def test_stress_reduced_exact(oracle_lib, gpu_lib, per_pile, solver):
     # the large-island stress world at reduced size: 4 container piles of mixed bodies with 4
     # revolute chains of 16 links hanging into each (with 1,100 bodies a pile the world has over
-    # 4,096 fixtures and takes the large-world kernels)
+    # 4,096 fixtures and takes the large-world kernels; its Solve on a block, or on a warp)
     oracle_lib.set_trig_mode(1)
     s = scenes.stress(piles=4, per_pile=per_pile, chains_per_pile=4, links=16)
     ow = oracle_lib.OracleWorld(s)
     gw = gpu_lib.World(s)
+    gw.set_island_solver(solver)
     for t in range(120):
         ow.step()
         gw.step()
@@ -186,3 +188,34 @@ def test_stress_reduced_exact(oracle_lib, gpu_lib, per_pile):
     st = gw.export_state()
     assert st["header"][0]["contact_count"] > 4 * per_pile
     assert np.abs(st["joints"]["impulse"]).max() > 0
+
+
+@pytest.mark.parametrize("solver", [0, 1], ids=["block_solve", "warp_solve"])
+def test_large_mixed_world_exact(oracle_lib, gpu_lib, solver):
+    # every joint type (gears with dynamic C / D bodies included), edge and chain grounds and a
+    # 4,000-body pile in one world of over 4,096 fixtures: b2World.Solve on a block (union-find
+    # islands, one search per thread, levels over the block) and on a warp; states and listener
+    # events bit for bit against the oracle for 240 steps, bodies falling asleep on the way
+    oracle_lib.set_trig_mode(1)
+    s = scenes.large_mixed()
+    assert len(s["fixtures"]) >= 4096
+    ow = oracle_lib.OracleWorld(s)
+    ow.record_events(True)
+    gw = gpu_lib.World(s)
+    gw.set_island_solver(solver)
+    got = []
+    gw.set_listener(lambda ev: got.append(ev))
+    for t in range(240):
+        got.clear()
+        ow.step()
+        gw.step()
+        ref = ow.events()
+        ev = np.concatenate(got) if got else np.zeros(0, abi.CONTACT_EVENT)
+        assert ev.tobytes() == ref.tobytes(), "step %d: events differ (%d vs %d)" % (t + 1, len(ev), len(ref))
+        if (t + 1) % 60 == 0:
+            d = exact_diff(ow.export_state(), gw.export_state())
+            assert not d, "step %d: %s" % (t + 1, d[:6])
+    st = gw.export_state()
+    dyn = st["bodies"]["type"] == abi.DYNAMIC
+    assert ((st["bodies"]["flags"][dyn] & abi.BODY_AWAKE) == 0).any()
+    assert st["header"][0]["joint_count"] == sum(len(s[k]) for k in scenes.JOINT_KINDS)
