@@ -947,17 +947,7 @@ DG int toi_pairs_big(const Ctx& x, int w, const int* now, int nnow, const int* a
     return total;
 }
 
-// AddPair for the block's pairs, then the world's SolveTOI (one warp per large world)
 DG void toi_world(const Ctx& x, int w, float* sbp);
-__global__ void k_finish_big(const __grid_constant__ Ctx x) {
-    const int i = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
-    if (i >= x.n_big) return;
-    const int w = x.big_worlds[i];
-    const int total = x.wd[w].pair_total;
-    if (total > 0) add_pairs(x, w, total);
-    tsync();
-    toi_world(x, w, x.s_sbody + 6 * (size_t)x.wi[w].body_start);
-}
 
 // ------------------------------------------------------------ kernels
 __global__ void k_step_begin(const __grid_constant__ Ctx x) {
@@ -4115,7 +4105,7 @@ DG void solve_world(const Ctx& x, int w, float* sbp, bool sb_smem, float* stage_
         }
     tsync();
     stamp(x, w, 10);
-    if (!wi.pair_block) {                                               // else k_pairs_block + k_finish_big
+    if (!wi.pair_block) {                                               // else k_pairs_block + k_finish_big_block
         hash_rebuild(x, w);
         find_new_contacts(x, w);
     }
@@ -4152,20 +4142,6 @@ DG bool toi_candidate(const Ctx& x, int ci, int b0) {
     bool collideA = (bA.flags & kBodyBullet) || bA.type != kDynamicBody;
     bool collideB = (bB.flags & kBodyBullet) || bB.type != kDynamicBody;
     return collideA || collideB;
-}
-
-// append the candidates among contact slots [k0, k1) (world-local) to list[cnt ..] in
-// ascending order; returns the new count (all lanes)
-DG int toi_collect(const Ctx& x, int c0, int b0, int k0, int k1, int* list, int cnt) {
-    const int lane = lane_id();
-    for (int base = k0; base < k1; base += kWarp) {
-        int k = base + lane;
-        bool cand = k < k1 && toi_candidate(x, c0 + k, b0);
-        unsigned bal = __ballot_sync(0xffffffffu, cand);
-        if (cand) list[cnt + __popc(bal & ((1u << lane) - 1u))] = k;
-        cnt += __popc(bal);
-    }
-    return cnt;
 }
 
 // b2Contact.Update inside the TOI loop: wakes are applied immediately (out of line: TOI events
@@ -4255,11 +4231,149 @@ __device__ __noinline__ void solve_toi_island(const Ctx& x, int w, const WorldIn
     }
 }
 
+// The threads that run one world's SolveTOI together: a warp (every world with the rest of its
+// step) or a block (a large world, after its pair search).  The lead (rank 0) does the serial
+// parts of the event loop; the passes over the contact list are spread over the team, and
+// the ones whose hits must be handled in list order hand them to the lead in that order.
+struct WarpTeam {
+    DG int rank() const { return lane_id(); }
+    DG int size() const { return kWarp; }
+    DG bool lead() const { return lane_id() == 0; }
+    DG void sync() const { __syncwarp(); }
+    DG int bcast(int v) const { return __shfl_sync(0xffffffffu, v, 0); }
+    // smallest (a, l) over the team: smallest a, then smallest l
+    DG void argmin(float& a, int& l) const {
+        for (int o = 16; o > 0; o >>= 1) {
+            const float oa = __shfl_xor_sync(0xffffffffu, a, o);
+            const int ol = __shfl_xor_sync(0xffffffffu, l, o);
+            if (oa < a || (oa == a && ol < l)) { a = oa; l = ol; }
+        }
+    }
+    // the lead calls f(t) for every t in [0, n) with pred(t), in descending t, until f returns
+    // false; pred must not depend on what f changes
+    template <class P, class F>
+    DG void scan_desc(int n, P&& pred, F&& f) const {
+        const int lane = lane_id();
+        bool stop = false;
+        for (int base = n - 1; base >= 0 && !stop; base -= kWarp) {
+            const int t = base - lane;
+            unsigned bal = __ballot_sync(0xffffffffu, t >= 0 && pred(t));
+            if (lane == 0) {
+                while (bal) {
+                    const int l = __ffs(bal) - 1;
+                    bal &= bal - 1;
+                    if (!f(base - l)) { stop = true; break; }
+                }
+            }
+            __syncwarp();
+            stop = __shfl_sync(0xffffffffu, stop, 0);
+        }
+    }
+    // append every k in [k0, k1) with pred(k) to list[cnt ..] in ascending order; the new count
+    template <class P>
+    DG int collect(int k0, int k1, int* list, int cnt, P&& pred) const {
+        const int lane = lane_id();
+        for (int base = k0; base < k1; base += kWarp) {
+            const int k = base + lane;
+            const bool hit = k < k1 && pred(k);
+            const unsigned bal = __ballot_sync(0xffffffffu, hit);
+            if (hit) list[cnt + __popc(bal & ((1u << lane) - 1u))] = k;
+            cnt += __popc(bal);
+        }
+        return cnt;
+    }
+    // f() is warp-collective and returns the same int on every lane
+    template <class F>
+    DG int first_warp(F&& f) const { return f(); }
+};
+
+struct BlockTeam {
+    unsigned* bal;                 // shared: one ballot per warp
+    int* box;                      // shared: a broadcast slot
+    float* ra;                     // shared: per-warp partial minima
+    int* rl;
+    DG int rank() const { return threadIdx.x; }
+    DG int size() const { return blockDim.x; }
+    DG bool lead() const { return threadIdx.x == 0; }
+    DG void sync() const { __syncthreads(); }
+    DG int bcast(int v) const {
+        __syncthreads();
+        if (threadIdx.x == 0) box[0] = v;
+        __syncthreads();
+        return box[0];
+    }
+    DG void argmin(float& a, int& l) const {
+        for (int o = 16; o > 0; o >>= 1) {
+            const float oa = __shfl_xor_sync(0xffffffffu, a, o);
+            const int ol = __shfl_xor_sync(0xffffffffu, l, o);
+            if (oa < a || (oa == a && ol < l)) { a = oa; l = ol; }
+        }
+        __syncthreads();
+        if (lane_id() == 0) { ra[threadIdx.x >> 5] = a; rl[threadIdx.x >> 5] = l; }
+        __syncthreads();
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k)
+            if (ra[k] < a || (ra[k] == a && rl[k] < l)) { a = ra[k]; l = rl[k]; }
+    }
+    template <class P, class F>
+    DG void scan_desc(int n, P&& pred, F&& f) const {
+        const int nt = blockDim.x, nw = nt >> 5, warp = threadIdx.x >> 5;
+        bool stop = false;
+        for (int base = n - 1; base >= 0 && !stop; base -= nt) {
+            const int t = base - (int)threadIdx.x;
+            const unsigned b = __ballot_sync(0xffffffffu, t >= 0 && pred(t));
+            if (lane_id() == 0) bal[warp] = b;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                for (int q = 0; q < nw && !stop; ++q) {
+                    unsigned m = bal[q];
+                    while (m) {
+                        const int l = __ffs(m) - 1;
+                        m &= m - 1;
+                        if (!f(base - 32 * q - l)) { stop = true; break; }
+                    }
+                }
+                box[1] = stop;
+            }
+            __syncthreads();
+            stop = box[1] != 0;
+        }
+        __syncthreads();
+    }
+    template <class P>
+    DG int collect(int k0, int k1, int* list, int cnt, P&& pred) const {
+        const int nt = blockDim.x, nw = nt >> 5, warp = threadIdx.x >> 5, lane = lane_id();
+        for (int base = k0; base < k1; base += nt) {
+            const int k = base + (int)threadIdx.x;
+            const bool hit = k < k1 && pred(k);
+            const unsigned b = __ballot_sync(0xffffffffu, hit);
+            if (lane == 0) bal[warp] = b;
+            __syncthreads();
+            int before = 0, all = 0;
+            for (int q = 0; q < nw; ++q) {
+                const int c = __popc(bal[q]);
+                before += q < warp ? c : 0;
+                all += c;
+            }
+            if (hit) list[cnt + before + __popc(b & ((1u << lane) - 1u))] = k;
+            cnt += all;
+            __syncthreads();
+        }
+        return cnt;
+    }
+    template <class F>
+    DG int first_warp(F&& f) const {
+        int r = 0;
+        if (threadIdx.x < kWarp) r = f();
+        return bcast(r);
+    }
+};
+
 // b2World.SolveTOI (b2world.d:1127-1452) for world w, then the end of b2World.Step
-DG void toi_world(const Ctx& x, int w, float* sbp) {
+template <class Team>
+DG void toi_world_t(const Ctx& x, int w, float* sbp, const Team& tm) {
     const WorldInfo& wi = x.wi[w];
     WorldDyn& wd = x.wd[w];
-    int lane = lane_id();
+    const int rk = tm.rank(), ts = tm.size();
     const int b0 = wi.body_start, nb = wi.body_count, c0 = wi.contact_start;
     // optional profile: slot 16 total cycles, 17 events, 18.. cycles per part of the event loop
     long long tlast = clock64(), t_start = tlast;
@@ -4273,27 +4387,28 @@ DG void toi_world(const Ctx& x, int w, float* sbp) {
         sb.p = sbp;
         {
             int n = wd.contact_count;
-            for (int k = lane; k < n; k += kWarp) contact_compact(x, c0 + k, b0);
+            for (int k = rk; k < n; k += ts) contact_compact(x, c0 + k, b0);
         }
         if (wd.step_complete) {                                          // b2world.d:1131-1146
-            for (int i = lane; i < nb; i += kWarp) {
+            for (int i = rk; i < nb; i += ts) {
                 x.bs[b0 + i].flags &= ~(uint32_t)kBodyIsland;
                 x.bs[b0 + i].sweep[8] = 0.0f;
             }
             int n = wd.contact_count;
-            for (int k = lane; k < n; k += kWarp) {
+            for (int k = rk; k < n; k += ts) {
                 dbox_contact_state& c = x.ct[c0 + k];
                 c.flags &= ~(uint32_t)(kContactToi | kContactIsland);
                 c.toi_count = 0;
                 c.toi = 1.0f;
             }
         }
-        for (int i = lane; i < nb; i += kWarp) x.s_bfl[b0 + i] = 0;
-        tsync();
+        for (int i = rk; i < nb; i += ts) x.s_bfl[b0 + i] = 0;
+        tm.sync();
         // TOI candidates in list order (ascending slot): only these can get a TOI, join a TOI
         // island as a neighbour or carry the TOI / island flags that an event clears
         int* cand = x.s_tcand + c0;
-        int ncand = toi_collect(x, c0, b0, 0, wd.contact_count, cand, 0);
+        auto is_cand = [&](int k) { return toi_candidate(x, c0 + k, b0); };
+        int ncand = tm.collect(0, wd.contact_count, cand, 0, is_cand);
         // a large world's event pair searches use the grid of its end-of-solve pair search and
         // the proxies moved since (toi_pairs_big); without destruction a proxy's rank is its
         // fixture index
@@ -4304,49 +4419,40 @@ DG void toi_world(const Ctx& x, int w, float* sbp) {
         int* pall = x.s_moved + f0;                                      // moved during this SolveTOI
         int nall = 0;
         if (big_toi)
-            for (int i = lane; i < wi.fix_count; i += kWarp) toimv[i] = 0;
-        tsync();
+            for (int i = rk; i < wi.fix_count; i += ts) toimv[i] = 0;
+        tm.sync();
         int events = 0;
         const int max_events = 9 * wi.contact_cap + 16;   // each contact takes at most 9 events
         for (int iter = 0;; ++iter) {
             if (iter >= max_events) {
-                if (lane == 0) set_error(x, w, DBOX_ERR_TIMEOUT);
+                if (tm.lead()) set_error(x, w, DBOX_ERR_TIMEOUT);
                 break;
             }
             int n = wd.contact_count;
             // sweeps are put onto a common time in list order (b2world.d:1212-1226)
             if (advanced) {
-                for (int base = ncand - 1; base >= 0; base -= kWarp) {
-                    int t = base - lane;
-                    bool need = t >= 0 && toi_needs(x, c0 + cand[t], b0);
-                    unsigned bal = __ballot_sync(0xffffffffu, need);
-                    if (lane == 0) {
-                        while (bal) {
-                            int l = __ffs(bal) - 1;
-                            bal &= bal - 1;
-                            int kk = cand[base - l];
-                            int2 cb = x.s_cbody[c0 + kk];
-                            dbox_body_state& bA = x.bs[b0 + cb.x];
-                            dbox_body_state& bB = x.bs[b0 + cb.y];
-                            float alpha0 = bA.sweep[8];
-                            if (bA.sweep[8] < bB.sweep[8]) {
-                                alpha0 = bB.sweep[8];
-                                Sweep s = b_sweep(bA); sweep_advance(s, alpha0); b_set_sweep(bA, s);
-                            } else if (bB.sweep[8] < bA.sweep[8]) {
-                                alpha0 = bA.sweep[8];
-                                Sweep s = b_sweep(bB); sweep_advance(s, alpha0); b_set_sweep(bB, s);
-                            }
-                            SweepSnap& sn = x.snap[c0 + kk];
-                            sn.a = b_sweep(bA);
-                            sn.b = b_sweep(bB);
-                            sn.alpha0 = alpha0;
-                        }
+                tm.scan_desc(ncand, [&](int t) { return toi_needs(x, c0 + cand[t], b0); }, [&](int t) {
+                    const int kk = cand[t];
+                    const int2 cb = x.s_cbody[c0 + kk];
+                    dbox_body_state& bA = x.bs[b0 + cb.x];
+                    dbox_body_state& bB = x.bs[b0 + cb.y];
+                    float alpha0 = bA.sweep[8];
+                    if (bA.sweep[8] < bB.sweep[8]) {
+                        alpha0 = bB.sweep[8];
+                        Sweep s = b_sweep(bA); sweep_advance(s, alpha0); b_set_sweep(bA, s);
+                    } else if (bB.sweep[8] < bA.sweep[8]) {
+                        alpha0 = bA.sweep[8];
+                        Sweep s = b_sweep(bB); sweep_advance(s, alpha0); b_set_sweep(bB, s);
                     }
-                    tsync();
-                }
+                    SweepSnap& sn = x.snap[c0 + kk];
+                    sn.a = b_sweep(bA);
+                    sn.b = b_sweep(bB);
+                    sn.alpha0 = alpha0;
+                    return true;
+                });
             }
             mark(0);
-            for (int t = lane; t < ncand; t += kWarp) {
+            for (int t = rk; t < ncand; t += ts) {
                 int k = cand[t];
                 if (!toi_needs(x, c0 + k, b0)) continue;
                 dbox_contact_state& c = x.ct[c0 + k];
@@ -4362,12 +4468,12 @@ DG void toi_world(const Ctx& x, int w, float* sbp) {
                 c.toi = alpha;
                 c.flags |= kContactToi;
             }
-            tsync();
+            tm.sync();
             mark(1);
             // minimum TOI, first in list order on ties
             float bestA = 1.0f;
             int bestLp = 0x7fffffff;
-            for (int t = lane; t < ncand; t += kWarp) {
+            for (int t = rk; t < ncand; t += ts) {
                 int k = cand[t];
                 const dbox_contact_state& c = x.ct[c0 + k];
                 if ((c.flags & kContactEnabled) == 0 || c.toi_count > kMaxSubSteps) continue;
@@ -4375,21 +4481,17 @@ DG void toi_world(const Ctx& x, int w, float* sbp) {
                 int lp = n - 1 - k;
                 if (c.toi < bestA || (c.toi == bestA && lp < bestLp && c.toi < 1.0f)) { bestA = c.toi; bestLp = lp; }
             }
-            for (int o = 16; o > 0; o >>= 1) {
-                float oa = __shfl_xor_sync(0xffffffffu, bestA, o);
-                int ol = __shfl_xor_sync(0xffffffffu, bestLp, o);
-                if (oa < bestA || (oa == bestA && ol < bestLp)) { bestA = oa; bestLp = ol; }
-            }
+            tm.argmin(bestA, bestLp);
             mark(2);
             if (bestLp == 0x7fffffff || 1.0f - 10.0f * kEpsilon < bestA) {
-                if (lane == 0) wd.step_complete = 1;
+                if (tm.lead()) wd.step_complete = 1;
                 break;
             }
             const float minAlpha = bestA;
             const int mk = n - 1 - bestLp;
             const int2 mcb = x.s_cbody[c0 + mk];
             int solved = 0, nbI = 0, ncI = 0;
-            if (lane == 0) {
+            if (tm.lead()) {
                 ++events;
                 dbox_contact_state& mc = x.ct[c0 + mk];
                 dbox_body_state& bA = x.bs[b0 + mcb.x];
@@ -4420,62 +4522,50 @@ DG void toi_world(const Ctx& x, int w, float* sbp) {
                     mc.flags |= kContactIsland;
                 }
             }
-            solved = __shfl_sync(0xffffffffu, solved, 0);
-            nbI = __shfl_sync(0xffffffffu, nbI, 0);
-            ncI = __shfl_sync(0xffffffffu, ncI, 0);
+            solved = tm.bcast(solved);
             mark(3);
             if (solved) {
                 // contacts of each dynamic event body, in its edge-list order (b2world.d:1306-1411)
                 for (int q = 0; q < 2; ++q) {
                     const int body = q == 0 ? mcb.x : mcb.y;
                     if (x.bs[b0 + body].type != kDynamicBody) continue;
-                    bool stop = false;
                     // every contact that can join (b2world.d:1330-1346) is a candidate
-                    for (int base = ncand - 1; base >= 0 && !stop; base -= kWarp) {
-                        int t = base - lane;
-                        bool hit = false;
-                        if (t >= 0) { int2 cb = x.s_cbody[c0 + cand[t]]; hit = cb.x == body || cb.y == body; }
-                        unsigned bal = __ballot_sync(0xffffffffu, hit);
-                        if (lane == 0) {
-                            dbox_body_state& Bd = x.bs[b0 + body];
-                            while (bal) {
-                                int l = __ffs(bal) - 1;
-                                bal &= bal - 1;
-                                int kk = cand[base - l];
-                                if (nbI == 2 * kMaxTOIContacts || ncI == kMaxTOIContacts) { stop = true; break; }
-                                dbox_contact_state& c = x.ct[c0 + kk];
-                                if (c.flags & kContactIsland) continue;
-                                int2 cb = x.s_cbody[c0 + kk];
-                                int other = cb.x == body ? cb.y : cb.x;
-                                dbox_body_state& O = x.bs[b0 + other];
-                                if (O.type == kDynamicBody && (Bd.flags & kBodyBullet) == 0 && (O.flags & kBodyBullet) == 0) continue;
-                                if (x.s_cq[c0 + kk] & 2) continue;
-                                Sweep backup = b_sweep(O);
-                                if ((O.flags & kBodyIsland) == 0) b_advance(O, minAlpha);
-                                unsigned evt = 0;
-                                toi_update(x, c, &evt);
-                                if (x.record_events) put_update_events(x, wi, w, wd, evt, c);
-                                if ((c.flags & kContactEnabled) == 0 || (c.flags & kContactTouching) == 0) {
-                                    b_set_sweep(O, backup);
-                                    b_sync_transform(O);
-                                    continue;
-                                }
-                                c.flags |= kContactIsland;
-                                x.s_isl_contact[c0 + ncI++] = c0 + kk;
-                                if (O.flags & kBodyIsland) continue;
-                                O.flags |= kBodyIsland;
-                                if (O.type != kStaticBody) b_set_awake(O, true);
-                                x.s_isl_body[b0 + nbI++] = other;
-                            }
+                    tm.scan_desc(ncand, [&](int t) {
+                        const int2 cb = x.s_cbody[c0 + cand[t]];
+                        return cb.x == body || cb.y == body;
+                    }, [&](int t) {
+                        const int kk = cand[t];
+                        if (nbI == 2 * kMaxTOIContacts || ncI == kMaxTOIContacts) return false;
+                        dbox_body_state& Bd = x.bs[b0 + body];
+                        dbox_contact_state& c = x.ct[c0 + kk];
+                        if (c.flags & kContactIsland) return true;
+                        const int2 cb = x.s_cbody[c0 + kk];
+                        const int other = cb.x == body ? cb.y : cb.x;
+                        dbox_body_state& O = x.bs[b0 + other];
+                        if (O.type == kDynamicBody && (Bd.flags & kBodyBullet) == 0 && (O.flags & kBodyBullet) == 0) return true;
+                        if (x.s_cq[c0 + kk] & 2) return true;
+                        Sweep backup = b_sweep(O);
+                        if ((O.flags & kBodyIsland) == 0) b_advance(O, minAlpha);
+                        unsigned evt = 0;
+                        toi_update(x, c, &evt);
+                        if (x.record_events) put_update_events(x, wi, w, wd, evt, c);
+                        if ((c.flags & kContactEnabled) == 0 || (c.flags & kContactTouching) == 0) {
+                            b_set_sweep(O, backup);
+                            b_sync_transform(O);
+                            return true;
                         }
-                        stop = __shfl_sync(0xffffffffu, stop, 0);
-                    }
-                    nbI = __shfl_sync(0xffffffffu, nbI, 0);
-                    ncI = __shfl_sync(0xffffffffu, ncI, 0);
+                        c.flags |= kContactIsland;
+                        x.s_isl_contact[c0 + ncI++] = c0 + kk;
+                        if (O.flags & kBodyIsland) return true;
+                        O.flags |= kBodyIsland;
+                        if (O.type != kStaticBody) b_set_awake(O, true);
+                        x.s_isl_body[b0 + nbI++] = other;
+                        return true;
+                    });
                 }
                 mark(4);
                 int nnow = 0;
-                if (lane == 0) {
+                if (tm.lead()) {
                     float subDt = (1.0f - minAlpha) * x.dt;
                     solve_toi_island(x, w, wi, sb, nbI, ncI, mcb.x, mcb.y, subDt);
                     mark(5);
@@ -4496,41 +4586,40 @@ DG void toi_world(const Ctx& x, int w, float* sbp) {
                         }
                     }
                 }
-                nnow = __shfl_sync(0xffffffffu, nnow, 0);
-                nall = __shfl_sync(0xffffffffu, nall, 0);
-                tsync();
+                nnow = tm.bcast(nnow);
+                nall = tm.bcast(nall);
+                nbI = tm.bcast(nbI);
                 // invalidate the TOIs of every contact on a displaced dynamic body (only
                 // candidates carry the two flags)
-                for (int t = lane; t < ncand; t += kWarp) {
+                for (int t = rk; t < ncand; t += ts) {
                     int k = cand[t];
                     int2 cb = x.s_cbody[c0 + k];
                     if ((x.s_bfl[b0 + cb.x] | x.s_bfl[b0 + cb.y]) & kBfMark)
                         x.ct[c0 + k].flags &= ~(uint32_t)(kContactToi | kContactIsland);
                 }
-                tsync();
-                if (lane == 0)
-                    for (int i = 0; i < nbI; ++i) x.s_bfl[b0 + x.s_isl_body[b0 + i]] = 0;
-                tsync();
+                tm.sync();
+                for (int i = rk; i < nbI; i += ts) x.s_bfl[b0 + x.s_isl_body[b0 + i]] = 0;
+                tm.sync();
                 if (big_toi) {
-                    const int total = nnow > 0 ? toi_pairs_big(x, w, pnow, nnow, pall, nall, toimv) : 0;
-                    if (total > 0) add_pairs(x, w, total);
+                    const int total = nnow > 0 ? tm.first_warp([&]() { return toi_pairs_big(x, w, pnow, nnow, pall, nall, toimv); }) : 0;
+                    if (total > 0) tm.first_warp([&]() { add_pairs(x, w, total); return 0; });
                 } else {
-                    find_new_contacts(x, w);
+                    tm.first_warp([&]() { find_new_contacts(x, w); return 0; });
                 }
-                ncand = toi_collect(x, c0, b0, n, wd.contact_count, cand, ncand);
-                tsync();
+                ncand = tm.collect(n, wd.contact_count, cand, ncand, is_cand);
+                tm.sync();
                 mark(6);
             }
             advanced = true;
             if (solved && x.sub_stepping) {
-                if (lane == 0) wd.step_complete = 0;
+                if (tm.lead()) wd.step_complete = 0;
                 break;
             }
         }
-        if (lane == 0) { wd.toi_events = events; wd.acc_toi_events += (unsigned long long)events; }
+        if (tm.lead()) { wd.toi_events = events; wd.acc_toi_events += (unsigned long long)events; }
     }
-    tsync();
-    if (x.prof && lane == 0) {
+    tm.sync();
+    if (x.prof && tm.lead()) {
         unsigned long long* pr = x.prof + kProfSlots * (size_t)w;
         pr[16] = clock64() - t_start;
         pr[17] = wd.toi_events;
@@ -4538,13 +4627,29 @@ DG void toi_world(const Ctx& x, int w, float* sbp) {
         for (int i = 0; i < 7; ++i) pr[18 + i] = tacc[i];
     }
     // b2World.Step epilogue (b2world.d:421-429)
-    if (lane == 0 && x.dt > 0.0f) wd.inv_dt0 = x.inv_dt;
+    if (tm.lead() && x.dt > 0.0f) wd.inv_dt0 = x.inv_dt;
     if (wd.flags & 4u) {
-        for (int i = lane; i < nb; i += kWarp) {
+        for (int i = rk; i < nb; i += ts) {
             dbox_body_state& B = x.bs[b0 + i];
             B.force[0] = 0.0f; B.force[1] = 0.0f; B.force[2] = 0.0f;
         }
     }
+}
+
+DG void toi_world(const Ctx& x, int w, float* sbp) { toi_world_t(x, w, sbp, WarpTeam()); }
+
+// AddPair for a large world's pairs, then its SolveTOI, on a block
+__global__ void __launch_bounds__(kPairThreads) k_finish_big_block(const __grid_constant__ Ctx x) {
+    __shared__ unsigned s_bal[32];
+    __shared__ int s_box[2];
+    __shared__ float s_ra[32];
+    __shared__ int s_rl[32];
+    const int w = x.big_worlds[blockIdx.x];
+    const int total = x.wd[w].pair_total;
+    if (threadIdx.x < kWarp && total > 0) add_pairs(x, w, total);
+    __syncthreads();
+    BlockTeam tm{s_bal, s_box, s_ra, s_rl};
+    toi_world_t(x, w, x.s_sbody + 6 * (size_t)x.wi[w].body_start, tm);
 }
 
 // ------------------------------------------------------------ b2World.Solve of a large world on a block
@@ -5236,7 +5341,7 @@ __global__ void __launch_bounds__(kSolveWarps * 32, 3) k_solve_toi(const __grid_
         if (x.prof) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(g0));
         if (!(x.big_block && x.wi[w].pair_block)) solve_world(x, w, sbp, in_smem, stage_f, ring);   // else k_solve_big
         tsync();
-        if (!x.wi[w].pair_block) toi_world(x, w, sbp);                   // large worlds: k_finish_big
+        if (!x.wi[w].pair_block) toi_world(x, w, sbp);                   // large worlds: k_finish_big_block
         tsync();
         if (heavy && lane == 0) atomicExch(&x.solve_queue[2 + sub], 0);
         if (x.prof && lane == 0) {
@@ -5274,14 +5379,13 @@ extern "C" int dbox_launch_collide(const dg::Ctx* x, cudaStream_t stream) {
 
 // part 2 of a step: Solve and SolveTOI (1 launch, 3 or 4 with a large world); *launches = all of the step's
 extern "C" int dbox_launch_solve(const dg::Ctx* x, cudaStream_t stream, int* launches) {
-    const int threads = 128;
     if (x->solve_blocks < 1) return (int)cudaErrorInvalidValue;
     if (x->solve_queue) cudaMemsetAsync(x->solve_queue, 0, sizeof(int) * (2 + 4 * (size_t)x->solve_nsm), stream);
     if (x->big_block) dg::k_solve_big<<<x->n_big, dg::kBigThreads, 0, stream>>>(*x);   // large worlds' Solve
     dg::k_solve_toi<<<x->solve_blocks, x->solve_wpb * dg::kWarp, x->solve_smem_floats * sizeof(float), stream>>>(*x);
     if (x->n_big > 0) {                             // large worlds: their pairs on a block each, then AddPair + TOI
         dg::k_pairs_block<<<x->n_big, dg::kPairThreads, 0, stream>>>(*x);
-        dg::k_finish_big<<<(x->n_big * dg::kWarp + threads - 1) / threads, threads, 0, stream>>>(*x);
+        dg::k_finish_big_block<<<x->n_big, dg::kPairThreads, 0, stream>>>(*x);
     }
     if (launches) *launches = x->n_big > 0 ? 6 + x->big_block : 4;
     return (int)cudaGetLastError();
@@ -5304,7 +5408,7 @@ extern "C" int dbox_launch_step_ev(const dg::Ctx* x, cudaStream_t stream, int* l
     dg::k_solve_toi<<<x->solve_blocks, x->solve_wpb * dg::kWarp, x->solve_smem_floats * sizeof(float), stream>>>(*x);
     if (x->n_big > 0) {                             // large worlds: their pairs on a block each, then AddPair + TOI
         dg::k_pairs_block<<<x->n_big, dg::kPairThreads, 0, stream>>>(*x);
-        dg::k_finish_big<<<(x->n_big * dg::kWarp + threads - 1) / threads, threads, 0, stream>>>(*x);
+        dg::k_finish_big_block<<<x->n_big, dg::kPairThreads, 0, stream>>>(*x);
     }
     if (ev) cudaEventRecordWithFlags(ev[2], stream, cudaEventRecordExternal);
     if (ev) cudaEventRecordWithFlags(ev[3], stream, cudaEventRecordExternal);
