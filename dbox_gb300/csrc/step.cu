@@ -1012,6 +1012,7 @@ __global__ void k_collide_finish(Ctx x) {
     int w = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
     if (w >= x.W) return;
     const WorldInfo& wi = x.wi[w];
+    if (wi.pair_block) return;                                          // k_collide_finish_big
     WorldDyn& wd = x.wd[w];
     int lane = lane_id();
     int n = wd.contact_count;
@@ -4638,6 +4639,138 @@ DG void toi_world_t(const Ctx& x, int w, float* sbp, const Team& tm) {
 
 DG void toi_world(const Ctx& x, int w, float* sbp) { toi_world_t(x, w, sbp, WarpTeam()); }
 
+// exclusive prefix of v over the block in thread order; *total gets the sum (all threads)
+DG int block_scan_value(int v, int* sh, int* total) {
+    const int lane = lane_id(), warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    __syncthreads();
+    if (lane == 31) sh[warp] = incl;
+    __syncthreads();
+    int before = 0, all = 0;
+    for (int q = 0; q < nw; ++q) {
+        before += q < warp ? sh[q] : 0;
+        all += sh[q];
+    }
+    *total = all;
+    return before + incl - v;
+}
+
+// k_collide_finish for a large world on a block of kPairThreads threads: the same steps, the
+// passes over its contacts spread over the block, the inactive contacts that a wake may
+// revive handed to one thread in list order, and the stable compaction done as a prefix
+// sum of destinations and a chunked in-place move (every destination is at or before its
+// source, and a chunk is read completely before any of it is written)
+__global__ void __launch_bounds__(kPairThreads) k_collide_finish_big(const __grid_constant__ Ctx x) {
+    __shared__ int shi[32];
+    __shared__ unsigned s_bal[32];
+    __shared__ int s_box[2];
+    __shared__ float s_ra[32];
+    __shared__ int s_rl[32];
+    const int w = x.big_worlds[blockIdx.x];
+    const WorldInfo& wi = x.wi[w];
+    WorldDyn& wd = x.wd[w];
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int n = wd.contact_count, c0 = wi.contact_start;
+    BlockTeam tm{s_bal, s_box, s_ra, s_rl};
+    bool need = false;
+    for (int k = tid; k < n; k += nt) {
+        if (x.s_cstate[c0 + k] == 1) {
+            const dbox_contact_state& c = x.ct[c0 + k];
+            const int A = x.fx[c.fixture_a].body, B = x.fx[c.fixture_b].body;
+            if (x.s_woken[A] != kNoWake || x.s_woken[B] != kNoWake) need = true;
+        }
+    }
+    if (__syncthreads_or(need)) {
+        tm.scan_desc(n, [&](int k) { return x.s_cstate[c0 + k] == 1; }, [&](int k) {
+            const int lp = n - 1 - k;
+            dbox_contact_state& c = x.ct[c0 + k];
+            const int A = x.fx[c.fixture_a].body, B = x.fx[c.fixture_b].body;
+            const dbox_body_state& ba = x.bs[A];
+            const dbox_body_state& bb = x.bs[B];
+            const bool awA = (ba.flags & kBodyAwake) || x.s_woken[A] < lp;
+            const bool awB = (bb.flags & kBodyAwake) || x.s_woken[B] < lp;
+            const bool activeA = awA && ba.type != kStaticBody;
+            const bool activeB = awB && bb.type != kStaticBody;
+            if (!activeA && !activeB) return true;
+            unsigned evt = 0;
+            x.s_cstate[c0 + k] = collide_one(x, c, lp, false, &evt);
+            if (x.record_events) x.s_cevt[c0 + k] = (unsigned char)evt;
+            return true;
+        });
+    }
+    __syncthreads();
+    // listener events of this Collide, in list order (newest contact first)
+    if (x.record_events) {
+        int base = 0;
+        for (int top = n - 1; top >= 0; top -= nt) {
+            const int k = top - tid;
+            const unsigned evt = k >= 0 ? x.s_cevt[c0 + k] : 0u;
+            int all;
+            int slot = base + block_scan_value(__popc(evt), shi, &all);
+            if (evt) {
+                const dbox_contact_state& c = x.ct[c0 + k];
+                if (evt & 1u) put_event(x, wi, w, slot++, DBOX_EVENT_BEGIN, c, c.point_count, nullptr, nullptr);
+                if (evt & 2u) put_event(x, wi, w, slot++, DBOX_EVENT_END, c, c.point_count, nullptr, nullptr);
+                if (evt & 4u) put_event(x, wi, w, slot++, DBOX_EVENT_PRESOLVE, c, c.point_count, nullptr, nullptr);
+            }
+            base += all;
+        }
+        if (tid == 0) wd.ev_count = base;
+    }
+    // apply wakes
+    for (int i = tid; i < wi.body_count; i += nt) {
+        const int b = wi.body_start + i;
+        if (x.s_woken[b] != kNoWake) b_set_awake(x.bs[b], true);
+    }
+    // stable compaction of surviving contacts: destinations, then the move
+    int* dst = x.s_tcand + c0;
+    int out = 0;
+    for (int base = 0; base < n; base += nt) {
+        const int k = base + tid;
+        const int keep = k < n && x.s_cstate[c0 + k] != 2;
+        int all;
+        const int d = out + block_scan_value(keep, shi, &all);
+        if (k < n) dst[k] = keep ? d : -1;
+        out += all;
+    }
+    __syncthreads();
+    if (out < n) {
+        constexpr int kWords = (int)(sizeof(dbox_contact_state) / sizeof(int4));
+        static_assert(sizeof(dbox_contact_state) % sizeof(int4) == 0, "contacts move as 16-byte words");
+        int4* words = reinterpret_cast<int4*>(x.ct + c0);
+        const int chunk = 4 * nt / kWords;                               // contacts a pass reads at once
+        for (int base = 0; base < n; base += chunk) {
+            const int cnt = n - base < chunk ? n - base : chunk;
+            int4 v[4];
+            int to[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int q = tid + j * nt;                              // word of this chunk
+                to[j] = -1;
+                if (q < cnt * kWords) {
+                    const int k = base + q / kWords;
+                    const int dk = dst[k];
+                    if (dk >= 0 && dk != k) {
+                        to[j] = dk * kWords + q % kWords;
+                        v[j] = words[(size_t)base * kWords + q];
+                    }
+                }
+            }
+            __syncthreads();
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (to[j] >= 0) words[to[j]] = v[j];
+            __syncthreads();
+        }
+    }
+    if (tid == 0) { wd.contact_count = out; wd.acc_contacts += (unsigned long long)n; wd.acc_steps += 1; }
+}
+
+
 // AddPair for a large world's pairs, then its SolveTOI, on a block
 __global__ void __launch_bounds__(kPairThreads) k_finish_big_block(const __grid_constant__ Ctx x) {
     __shared__ unsigned s_bal[32];
@@ -4741,12 +4874,14 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
     }
     for (int j = tid; j < nj; j += nt) x.jt[j0 + j].island_flag = 0;
     __syncthreads();
-    // contact edges of the island graph per body, newest contact first (b2world.d:1026-1062)
+    // contact edges of the island graph per body, newest contact first (b2world.d:1026-1062);
+    // a static body's list is never walked (the search does not continue through it), so
+    // it gets none
     for (int k = tid; k < n; k += nt) {
         if (x.s_cq[c0 + k] & 1) {
             const int2 cb = x.s_cbody[c0 + k];
-            atomicAdd(&adj[cb.x], 1);
-            atomicAdd(&adj[cb.y], 1);
+            if (!(bfl[cb.x] & kBfStatic)) atomicAdd(&adj[cb.x], 1);
+            if (!(bfl[cb.y] & kBfStatic)) atomicAdd(&adj[cb.y], 1);
         }
     }
     __syncthreads();
@@ -4760,19 +4895,22 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
     for (int k = tid; k < n; k += nt) {
         if (x.s_cq[c0 + k] & 1) {
             const int2 cb = x.s_cbody[c0 + k];
-            items[atomicAdd(&cursor[cb.x], 1)] = make_int2(k, cb.y);
-            items[atomicAdd(&cursor[cb.y], 1)] = make_int2(k, cb.x);
+            if (!(bfl[cb.x] & kBfStatic)) items[atomicAdd(&cursor[cb.x], 1)] = make_int2(k, cb.y);
+            if (!(bfl[cb.y] & kBfStatic)) items[atomicAdd(&cursor[cb.y], 1)] = make_int2(k, cb.x);
         }
     }
     __syncthreads();
     for (int i = tid; i < nb; i += nt) {                                 // each list by descending contact
-        const int e0 = adj[i], e1 = adj[i + 1];
-        for (int a = e0 + 1; a < e1; ++a) {
-            const int2 v = items[a];
-            int b = a - 1;
-            while (b >= e0 && items[b].x < v.x) { items[b + 1] = items[b]; --b; }
-            items[b + 1] = v;
-        }
+        const int e0 = adj[i], d = adj[i + 1] - e0;
+        int gap = 1;                                                     // Shell sort, gaps 1, 4, 13, 40, ...
+        while (3 * gap + 1 < d) gap = 3 * gap + 1;
+        for (; gap > 0; gap /= 3)
+            for (int a = e0 + gap; a < e0 + d; ++a) {
+                const int2 v = items[a];
+                int b = a - gap;
+                while (b >= e0 && items[b].x < v.x) { items[b + gap] = items[b]; b -= gap; }
+                items[b + gap] = v;
+            }
     }
     __syncthreads();
     stampb(1);
@@ -5374,10 +5512,12 @@ extern "C" int dbox_launch_collide(const dg::Ctx* x, cudaStream_t stream) {
     dg::k_step_begin<<<team_blocks, threads, 0, stream>>>(*x);
     dg::k_collide<<<flat_blocks, 256, 0, stream>>>(*x);
     dg::k_collide_finish<<<team_blocks, threads, 0, stream>>>(*x);
+    if (x->n_big > 0) dg::k_collide_finish_big<<<x->n_big, dg::kPairThreads, 0, stream>>>(*x);
     return (int)cudaGetLastError();
 }
 
 // part 2 of a step: Solve and SolveTOI (1 launch, 3 or 4 with a large world); *launches = all of the step's
+// (part 1 is 3 launches, 4 with a large world)
 extern "C" int dbox_launch_solve(const dg::Ctx* x, cudaStream_t stream, int* launches) {
     if (x->solve_blocks < 1) return (int)cudaErrorInvalidValue;
     if (x->solve_queue) cudaMemsetAsync(x->solve_queue, 0, sizeof(int) * (2 + 4 * (size_t)x->solve_nsm), stream);
@@ -5387,7 +5527,7 @@ extern "C" int dbox_launch_solve(const dg::Ctx* x, cudaStream_t stream, int* lau
         dg::k_pairs_block<<<x->n_big, dg::kPairThreads, 0, stream>>>(*x);
         dg::k_finish_big_block<<<x->n_big, dg::kPairThreads, 0, stream>>>(*x);
     }
-    if (launches) *launches = x->n_big > 0 ? 6 + x->big_block : 4;
+    if (launches) *launches = x->n_big > 0 ? 7 + x->big_block : 4;
     return (int)cudaGetLastError();
 }
 
@@ -5402,6 +5542,7 @@ extern "C" int dbox_launch_step_ev(const dg::Ctx* x, cudaStream_t stream, int* l
     dg::k_step_begin<<<team_blocks, threads, 0, stream>>>(*x);
     dg::k_collide<<<flat_blocks, 256, 0, stream>>>(*x);
     dg::k_collide_finish<<<team_blocks, threads, 0, stream>>>(*x);
+    if (x->n_big > 0) dg::k_collide_finish_big<<<x->n_big, dg::kPairThreads, 0, stream>>>(*x);
     if (ev) cudaEventRecordWithFlags(ev[1], stream, cudaEventRecordExternal);
     if (x->solve_queue) cudaMemsetAsync(x->solve_queue, 0, sizeof(int) * (2 + 4 * (size_t)x->solve_nsm), stream);
     if (x->big_block) dg::k_solve_big<<<x->n_big, dg::kBigThreads, 0, stream>>>(*x);   // large worlds' Solve
@@ -5412,7 +5553,7 @@ extern "C" int dbox_launch_step_ev(const dg::Ctx* x, cudaStream_t stream, int* l
     }
     if (ev) cudaEventRecordWithFlags(ev[2], stream, cudaEventRecordExternal);
     if (ev) cudaEventRecordWithFlags(ev[3], stream, cudaEventRecordExternal);
-    if (launches) *launches = x->n_big > 0 ? 6 + x->big_block : 4;
+    if (launches) *launches = x->n_big > 0 ? 7 + x->big_block : 4;
     return (int)cudaGetLastError();
 }
 
