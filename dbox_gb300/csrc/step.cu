@@ -685,8 +685,11 @@ __global__ void __launch_bounds__(kPairThreads) k_pairs_block(const __grid_const
     const WorldInfo& wi = x.wi[w];
     WorldDyn& wd = x.wd[w];
     const int tid = threadIdx.x, nt = blockDim.x;
+    const long long t_in = clock64();
+    auto prof_out = [&]() { if (x.prof && tid == 0) x.prof[kProfSlots * (size_t)w + 30] = clock64() - t_in; };
     if (!(wd.step_complete && x.dt > 0.0f) || wd.error != 0) {        // solve_world did not reach its broad-phase
         if (tid == 0) { wd.pair_total = 0; wd.g_valid = 0; }
+        prof_out();
         return;
     }
     // SynchronizeFixtures of the island bodies (b2world.d:1099-1116), the solve warp's last step
@@ -726,6 +729,7 @@ __global__ void __launch_bounds__(kPairThreads) k_pairs_block(const __grid_const
     sum = block_reduce(sum, fsum, shf);
     if (nm == 0 && !x.continuous) {                                     // no pairs, and no SolveTOI to serve
         if (tid == 0) { wd.pair_total = 0; wd.g_valid = 0; }
+        prof_out();
         return;
     }
     const float cut = 4.0f * sum / (float)(cnt > 0 ? cnt : 1);
@@ -814,6 +818,7 @@ __global__ void __launch_bounds__(kPairThreads) k_pairs_block(const __grid_const
     }
     if (nm == 0) {
         if (tid == 0) wd.pair_total = 0;
+        prof_out();
         return;
     }
     for (int a = tid; a < nf; a += nt) {                                 // partners per proxy
@@ -827,6 +832,7 @@ __global__ void __launch_bounds__(kPairThreads) k_pairs_block(const __grid_const
     const int total = block_exclusive_scan(x.s_pcount + f0, nf, shi);
     if (total > wi.pair_cap) {
         if (tid == 0) { set_error(x, w, DBOX_ERR_CAPACITY); wd.pair_total = 0; }
+        prof_out();
         return;
     }
     for (int a = tid; a < nf; a += nt) {                                 // the pairs, partners by rank
@@ -849,6 +855,7 @@ __global__ void __launch_bounds__(kPairThreads) k_pairs_block(const __grid_const
         wd.acc_pairs += (unsigned long long)total;
         wd.pair_total = total;
     }
+    prof_out();
 }
 
 // FindNewContacts inside SolveTOI for a large world (one warp): the move buffer holds the
@@ -4237,6 +4244,7 @@ __device__ __noinline__ void solve_toi_island(const Ctx& x, int w, const WorldIn
 // parts of the event loop; the passes over the contact list are spread over the team, and
 // the ones whose hits must be handled in list order hand them to the lead in that order.
 struct WarpTeam {
+    static constexpr bool kLists = false;        // joins and invalidations scan the candidate list
     DG int rank() const { return lane_id(); }
     DG int size() const { return kWarp; }
     DG bool lead() const { return lane_id() == 0; }
@@ -4253,12 +4261,12 @@ struct WarpTeam {
     // the lead calls f(t) for every t in [0, n) with pred(t), in descending t, until f returns
     // false; pred must not depend on what f changes
     template <class P, class F>
-    DG void scan_desc(int n, P&& pred, F&& f) const {
+    DG void scan_desc(int n, P&& pred, F&& f, int lo = 0) const {
         const int lane = lane_id();
         bool stop = false;
-        for (int base = n - 1; base >= 0 && !stop; base -= kWarp) {
+        for (int base = n - 1; base >= lo && !stop; base -= kWarp) {
             const int t = base - lane;
-            unsigned bal = __ballot_sync(0xffffffffu, t >= 0 && pred(t));
+            unsigned bal = __ballot_sync(0xffffffffu, t >= lo && pred(t));
             if (lane == 0) {
                 while (bal) {
                     const int l = __ffs(bal) - 1;
@@ -4289,10 +4297,12 @@ struct WarpTeam {
 };
 
 struct BlockTeam {
+    static constexpr bool kLists = true;         // joins and invalidations walk per-body candidate lists
     unsigned* bal;                 // shared: one ballot per warp
     int* box;                      // shared: a broadcast slot
     float* ra;                     // shared: per-warp partial minima
     int* rl;
+    unsigned* words;               // shared: one ballot per 32 positions of a scan (blockDim.x of them)
     DG int rank() const { return threadIdx.x; }
     DG int size() const { return blockDim.x; }
     DG bool lead() const { return threadIdx.x == 0; }
@@ -4315,22 +4325,41 @@ struct BlockTeam {
         for (int k = 0; k < (int)(blockDim.x >> 5); ++k)
             if (ra[k] < a || (ra[k] == a && rl[k] < l)) { a = ra[k]; l = rl[k]; }
     }
+    // positions [lo, n): 32 * blockDim.x at a time, every position's pred evaluated first (one
+    // ballot word per 32 positions, each warp a share of the words, loads of consecutive words
+    // in flight together), then a summary ballot per 32 words; the lead walks the non-empty
+    // words in order
     template <class P, class F>
-    DG void scan_desc(int n, P&& pred, F&& f) const {
-        const int nt = blockDim.x, nw = nt >> 5, warp = threadIdx.x >> 5;
+    DG void scan_desc(int n, P&& pred, F&& f, int lo = 0) const {
+        const int nt = blockDim.x, nw = nt >> 5, warp = threadIdx.x >> 5, lane = lane_id();
         bool stop = false;
-        for (int base = n - 1; base >= 0 && !stop; base -= nt) {
-            const int t = base - (int)threadIdx.x;
-            const unsigned b = __ballot_sync(0xffffffffu, t >= 0 && pred(t));
-            if (lane_id() == 0) bal[warp] = b;
+        for (int top = n - 1; top >= lo && !stop; top -= 32 * nt) {
+            const int nq = (top - lo) / 32 + 1 < nt ? (top - lo) / 32 + 1 : nt;    // words in use
+#pragma unroll 4
+            for (int q = warp; q < nq; q += nw) {
+                const int t = top - 32 * q - lane;
+                const unsigned b = __ballot_sync(0xffffffffu, t >= lo && pred(t));
+                if (lane == 0) words[q] = b;
+            }
+            __syncthreads();
+            for (int g = warp; 32 * g < nq; g += nw) {
+                const int q = 32 * g + lane;
+                const unsigned any = __ballot_sync(0xffffffffu, q < nq && words[q] != 0u);
+                if (lane == 0) bal[g] = any;
+            }
             __syncthreads();
             if (threadIdx.x == 0) {
-                for (int q = 0; q < nw && !stop; ++q) {
-                    unsigned m = bal[q];
-                    while (m) {
-                        const int l = __ffs(m) - 1;
-                        m &= m - 1;
-                        if (!f(base - 32 * q - l)) { stop = true; break; }
+                for (int g = 0; 32 * g < nq && !stop; ++g) {
+                    unsigned sm = bal[g];
+                    while (sm && !stop) {
+                        const int q = 32 * g + __ffs(sm) - 1;
+                        sm &= sm - 1;
+                        unsigned m = words[q];
+                        while (m) {
+                            const int l = __ffs(m) - 1;
+                            m &= m - 1;
+                            if (!f(top - 32 * q - l)) { stop = true; break; }
+                        }
                     }
                 }
                 box[1] = stop;
@@ -4410,6 +4439,47 @@ DG void toi_world_t(const Ctx& x, int w, float* sbp, const Team& tm) {
         int* cand = x.s_tcand + c0;
         auto is_cand = [&](int k) { return toi_candidate(x, c0 + k, b0); };
         int ncand = tm.collect(0, wd.contact_count, cand, 0, is_cand);
+        // block teams: the candidates of each dynamic body (positions in cand, descending), so
+        // that an event's joins and invalidations visit only its bodies' candidates; those
+        // collected after this point (from the events' new pairs) are scanned apart
+        const int ncand0 = ncand;
+        int* lstart = x.s_adj_start + wi.bx_start;                       // nb + 1
+        int* lent = reinterpret_cast<int*>(x.s_adj_items + 2 * (size_t)c0);
+        if constexpr (Team::kLists) {
+            int* lcur = x.s_cursor + b0;
+            auto dyn = [&](int b) { return x.bs[b0 + b].type == kDynamicBody; };
+            for (int i = rk; i < nb; i += ts) lstart[i] = 0;
+            tm.sync();
+            for (int t = rk; t < ncand; t += ts) {
+                const int2 cb = x.s_cbody[c0 + cand[t]];
+                if (dyn(cb.x)) atomicAdd(&lstart[cb.x], 1);
+                if (dyn(cb.y)) atomicAdd(&lstart[cb.y], 1);
+            }
+            tm.sync();
+            const int tot = block_exclusive_scan(lstart, nb, tm.rl);
+            if (tm.lead()) lstart[nb] = tot;
+            for (int i = rk; i < nb; i += ts) lcur[i] = lstart[i];
+            tm.sync();
+            for (int t = rk; t < ncand; t += ts) {
+                const int2 cb = x.s_cbody[c0 + cand[t]];
+                if (dyn(cb.x)) lent[atomicAdd(&lcur[cb.x], 1)] = t;
+                if (dyn(cb.y)) lent[atomicAdd(&lcur[cb.y], 1)] = t;
+            }
+            tm.sync();
+            for (int i = rk; i < nb; i += ts) {                          // each list by descending position
+                const int e0 = lstart[i], d = lstart[i + 1] - e0;
+                int gap = 1;
+                while (3 * gap + 1 < d) gap = 3 * gap + 1;
+                for (; gap > 0; gap /= 3)
+                    for (int a = e0 + gap; a < e0 + d; ++a) {
+                        const int v = lent[a];
+                        int q = a - gap;
+                        while (q >= e0 && lent[q] < v) { lent[q + gap] = lent[q]; q -= gap; }
+                        lent[q + gap] = v;
+                    }
+            }
+            tm.sync();
+        }
         // a large world's event pair searches use the grid of its end-of-solve pair search and
         // the proxies moved since (toi_pairs_big); without destruction a proxy's rank is its
         // fixture index
@@ -4453,35 +4523,35 @@ DG void toi_world_t(const Ctx& x, int w, float* sbp, const Team& tm) {
                 });
             }
             mark(0);
-            for (int t = rk; t < ncand; t += ts) {
-                int k = cand[t];
-                if (!toi_needs(x, c0 + k, b0)) continue;
-                dbox_contact_state& c = x.ct[c0 + k];
-                const DFixture& fa = x.fx[c.fixture_a];
-                const DFixture& fb = x.fx[c.fixture_b];
-                Sweep sA, sB;
-                float alpha0;
-                if (advanced) { sA = x.snap[c0 + k].a; sB = x.snap[c0 + k].b; alpha0 = x.snap[c0 + k].alpha0; }
-                else { sA = b_sweep(x.bs[fa.body]); sB = b_sweep(x.bs[fb.body]); alpha0 = sA.alpha0; }
-                float beta;
-                int state = time_of_impact(make_proxy(fa), make_proxy(fb), sA, sB, 1.0f, &beta);
-                float alpha = state == kToiTouching ? bmin(alpha0 + (1.0f - alpha0) * beta, 1.0f) : 1.0f;
-                c.toi = alpha;
-                c.flags |= kContactToi;
-            }
-            tm.sync();
-            mark(1);
-            // minimum TOI, first in list order on ties
+            // the TOI of every contact that needs one (b2world.d:1159-1236), and in the same
+            // pass the minimum TOI, first in list order on ties (each contact's TOI is
+            // written only by its own iteration)
             float bestA = 1.0f;
             int bestLp = 0x7fffffff;
             for (int t = rk; t < ncand; t += ts) {
                 int k = cand[t];
-                const dbox_contact_state& c = x.ct[c0 + k];
-                if ((c.flags & kContactEnabled) == 0 || c.toi_count > kMaxSubSteps) continue;
-                if ((c.flags & kContactToi) == 0) continue;
+                dbox_contact_state& c = x.ct[c0 + k];
+                if (toi_needs(x, c0 + k, b0)) {
+                    const DFixture& fa = x.fx[c.fixture_a];
+                    const DFixture& fb = x.fx[c.fixture_b];
+                    Sweep sA, sB;
+                    float alpha0;
+                    if (advanced) { sA = x.snap[c0 + k].a; sB = x.snap[c0 + k].b; alpha0 = x.snap[c0 + k].alpha0; }
+                    else { sA = b_sweep(x.bs[fa.body]); sB = b_sweep(x.bs[fb.body]); alpha0 = sA.alpha0; }
+                    float beta;
+                    int state = time_of_impact(make_proxy(fa), make_proxy(fb), sA, sB, 1.0f, &beta);
+                    float alpha = state == kToiTouching ? bmin(alpha0 + (1.0f - alpha0) * beta, 1.0f) : 1.0f;
+                    c.toi = alpha;
+                    c.flags |= kContactToi;
+                }
+                const uint32_t fl = c.flags;
+                if ((fl & kContactEnabled) == 0 || c.toi_count > kMaxSubSteps) continue;
+                if ((fl & kContactToi) == 0) continue;
+                const float toi = c.toi;
                 int lp = n - 1 - k;
-                if (c.toi < bestA || (c.toi == bestA && lp < bestLp && c.toi < 1.0f)) { bestA = c.toi; bestLp = lp; }
+                if (toi < bestA || (toi == bestA && lp < bestLp && toi < 1.0f)) { bestA = toi; bestLp = lp; }
             }
+            mark(1);
             tm.argmin(bestA, bestLp);
             mark(2);
             if (bestLp == 0x7fffffff || 1.0f - 10.0f * kEpsilon < bestA) {
@@ -4531,10 +4601,11 @@ DG void toi_world_t(const Ctx& x, int w, float* sbp, const Team& tm) {
                     const int body = q == 0 ? mcb.x : mcb.y;
                     if (x.bs[b0 + body].type != kDynamicBody) continue;
                     // every contact that can join (b2world.d:1330-1346) is a candidate
-                    tm.scan_desc(ncand, [&](int t) {
+                    auto touches = [&](int t) {
                         const int2 cb = x.s_cbody[c0 + cand[t]];
                         return cb.x == body || cb.y == body;
-                    }, [&](int t) {
+                    };
+                    auto join = [&](int t) {
                         const int kk = cand[t];
                         if (nbI == 2 * kMaxTOIContacts || ncI == kMaxTOIContacts) return false;
                         dbox_body_state& Bd = x.bs[b0 + body];
@@ -4562,7 +4633,17 @@ DG void toi_world_t(const Ctx& x, int w, float* sbp, const Team& tm) {
                         if (O.type != kStaticBody) b_set_awake(O, true);
                         x.s_isl_body[b0 + nbI++] = other;
                         return true;
-                    });
+                    };
+                    if (Team::kLists) {
+                        // the newer candidates first (higher positions), then the body's list
+                        tm.scan_desc(ncand, touches, join, ncand0);
+                        if (tm.lead()) {
+                            for (int e = lstart[body], ee = lstart[body + 1]; e < ee; ++e)
+                                if (!join(lent[e])) break;
+                        }
+                    } else {
+                        tm.scan_desc(ncand, touches, join);
+                    }
                 }
                 mark(4);
                 int nnow = 0;
@@ -4592,11 +4673,22 @@ DG void toi_world_t(const Ctx& x, int w, float* sbp, const Team& tm) {
                 nbI = tm.bcast(nbI);
                 // invalidate the TOIs of every contact on a displaced dynamic body (only
                 // candidates carry the two flags)
-                for (int t = rk; t < ncand; t += ts) {
+                if (Team::kLists) {
+                    const int warp = rk >> 5, lane = rk & 31, nw = ts >> 5;
+                    for (int i = warp; i < nbI; i += nw) {
+                        const int body = x.s_isl_body[b0 + i];
+                        if (!(x.s_bfl[b0 + body] & kBfMark)) continue;
+                        for (int e = lstart[body] + lane, ee = lstart[body + 1]; e < ee; e += 32)
+                            atomicAnd(&x.ct[c0 + cand[lent[e]]].flags, ~(uint32_t)(kContactToi | kContactIsland));
+                    }
+                }
+                for (int t = (Team::kLists ? ncand0 : 0) + rk; t < ncand; t += ts) {
                     int k = cand[t];
                     int2 cb = x.s_cbody[c0 + k];
-                    if ((x.s_bfl[b0 + cb.x] | x.s_bfl[b0 + cb.y]) & kBfMark)
-                        x.ct[c0 + k].flags &= ~(uint32_t)(kContactToi | kContactIsland);
+                    if ((x.s_bfl[b0 + cb.x] | x.s_bfl[b0 + cb.y]) & kBfMark) {
+                        if (Team::kLists) atomicAnd(&x.ct[c0 + k].flags, ~(uint32_t)(kContactToi | kContactIsland));
+                        else x.ct[c0 + k].flags &= ~(uint32_t)(kContactToi | kContactIsland);
+                    }
                 }
                 tm.sync();
                 for (int i = rk; i < nbI; i += ts) x.s_bfl[b0 + x.s_isl_body[b0 + i]] = 0;
@@ -4670,12 +4762,14 @@ __global__ void __launch_bounds__(kPairThreads) k_collide_finish_big(const __gri
     __shared__ int s_box[2];
     __shared__ float s_ra[32];
     __shared__ int s_rl[32];
+    __shared__ unsigned s_words[kPairThreads];
     const int w = x.big_worlds[blockIdx.x];
     const WorldInfo& wi = x.wi[w];
     WorldDyn& wd = x.wd[w];
     const int tid = threadIdx.x, nt = blockDim.x;
     const int n = wd.contact_count, c0 = wi.contact_start;
-    BlockTeam tm{s_bal, s_box, s_ra, s_rl};
+    const long long t_in = clock64();
+    BlockTeam tm{s_bal, s_box, s_ra, s_rl, s_words};
     bool need = false;
     for (int k = tid; k < n; k += nt) {
         if (x.s_cstate[c0 + k] == 1) {
@@ -4768,6 +4862,7 @@ __global__ void __launch_bounds__(kPairThreads) k_collide_finish_big(const __gri
         }
     }
     if (tid == 0) { wd.contact_count = out; wd.acc_contacts += (unsigned long long)n; wd.acc_steps += 1; }
+    if (x.prof && tid == 0) x.prof[kProfSlots * (size_t)w + 15] = clock64() - t_in;
 }
 
 
@@ -4777,11 +4872,14 @@ __global__ void __launch_bounds__(kPairThreads) k_finish_big_block(const __grid_
     __shared__ int s_box[2];
     __shared__ float s_ra[32];
     __shared__ int s_rl[32];
+    __shared__ unsigned s_words[kPairThreads];
     const int w = x.big_worlds[blockIdx.x];
     const int total = x.wd[w].pair_total;
+    const long long t_in = clock64();
     if (threadIdx.x < kWarp && total > 0) add_pairs(x, w, total);
     __syncthreads();
-    BlockTeam tm{s_bal, s_box, s_ra, s_rl};
+    if (x.prof && threadIdx.x == 0) x.prof[kProfSlots * (size_t)w + 31] = clock64() - t_in;
+    BlockTeam tm{s_bal, s_box, s_ra, s_rl, s_words};
     toi_world_t(x, w, x.s_sbody + 6 * (size_t)x.wi[w].body_start, tm);
 }
 

@@ -503,7 +503,9 @@ int32_t dbox_world_get_transforms(dbox_world* w, float* xya);
  * SolveTOI kernel, 17 its TOI events, 18..24 its cycles per part of the event loop (sweep
  * advance, TOI, minimum, event contact, neighbours, sub-step solve, fixture sync and pairs),
  * 25..26 the global timer (ns) when the world's warp started and ended the solve + SolveTOI
- * kernel, 27 its warp slot, 28..29 the SM and the warp's slot on the SM (%smid, %warpid). */
+ * kernel, 27 its warp slot, 28..29 the SM and the warp's slot on the SM (%smid, %warpid);
+ * for a large world (4,096+ fixtures) also 15 the cycles of its block's end of Collide, 30 of
+ * its block's SynchronizeFixtures + pair search, 31 of its AddPair pass. */
 int32_t dbox_world_set_phase_profile(dbox_world* w, int32_t enable);
 int32_t dbox_world_get_phase_profile(dbox_world* w, unsigned long long* out);
 
