@@ -545,14 +545,203 @@ __device__ __forceinline__ int gen_pairs_warp(const Ctx& x, int w) {
 
 // b2ContactManager.AddPair (b2contactmanager.d:52-176) for the world's `total` pairs in x.pairs,
 // in pair order (one warp)
-__device__ __noinline__ void add_pairs(const Ctx& x, int w, int total) {
+// exclusive prefix of v over the block in thread order; *total gets the sum (all threads)
+DG int block_scan_value(int v, int* sh, int* total) {
+    const int lane = lane_id(), warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    __syncthreads();
+    if (lane == 31) sh[warp] = incl;
+    __syncthreads();
+    int before = 0, all = 0;
+    for (int q = 0; q < nw; ++q) {
+        before += q < warp ? sh[q] : 0;
+        all += sh[q];
+    }
+    *total = all;
+    return before + incl - v;
+}
+
+// The threads that run one world's SolveTOI together: a warp (every world with the rest of its
+// step) or a block (a large world, after its pair search).  The lead (rank 0) does the serial
+// parts of the event loop; the passes over the contact list are spread over the team, and
+// the ones whose hits must be handled in list order hand them to the lead in that order.
+struct WarpTeam {
+    static constexpr bool kLists = false;        // joins and invalidations scan the candidate list
+    DG int rank() const { return lane_id(); }
+    DG int size() const { return kWarp; }
+    DG bool lead() const { return lane_id() == 0; }
+    DG void sync() const { __syncwarp(); }
+    DG int bcast(int v) const { return __shfl_sync(0xffffffffu, v, 0); }
+    // smallest (a, l) over the team: smallest a, then smallest l
+    DG void argmin(float& a, int& l) const {
+        for (int o = 16; o > 0; o >>= 1) {
+            const float oa = __shfl_xor_sync(0xffffffffu, a, o);
+            const int ol = __shfl_xor_sync(0xffffffffu, l, o);
+            if (oa < a || (oa == a && ol < l)) { a = oa; l = ol; }
+        }
+    }
+    // the lead calls f(t) for every t in [0, n) with pred(t), in descending t, until f returns
+    // false; pred must not depend on what f changes
+    template <class P, class F>
+    DG void scan_desc(int n, P&& pred, F&& f, int lo = 0) const {
+        const int lane = lane_id();
+        bool stop = false;
+        for (int base = n - 1; base >= lo && !stop; base -= kWarp) {
+            const int t = base - lane;
+            unsigned bal = __ballot_sync(0xffffffffu, t >= lo && pred(t));
+            if (lane == 0) {
+                while (bal) {
+                    const int l = __ffs(bal) - 1;
+                    bal &= bal - 1;
+                    if (!f(base - l)) { stop = true; break; }
+                }
+            }
+            __syncwarp();
+            stop = __shfl_sync(0xffffffffu, stop, 0);
+        }
+    }
+    // append every k in [k0, k1) with pred(k) to list[cnt ..] in ascending order; the new count
+    template <class P>
+    DG int collect(int k0, int k1, int* list, int cnt, P&& pred) const {
+        const int lane = lane_id();
+        for (int base = k0; base < k1; base += kWarp) {
+            const int k = base + lane;
+            const bool hit = k < k1 && pred(k);
+            const unsigned bal = __ballot_sync(0xffffffffu, hit);
+            if (hit) list[cnt + __popc(bal & ((1u << lane) - 1u))] = k;
+            cnt += __popc(bal);
+        }
+        return cnt;
+    }
+    // f() is warp-collective and returns the same int on every lane
+    template <class F>
+    DG int first_warp(F&& f) const { return f(); }
+    // exclusive prefix of a flag in rank order; *all gets the team's count
+    DG int prefix(bool v, int* all) const {
+        const unsigned bal = __ballot_sync(0xffffffffu, v);
+        *all = __popc(bal);
+        return __popc(bal & ((1u << lane_id()) - 1u));
+    }
+};
+
+struct BlockTeam {
+    static constexpr bool kLists = true;         // joins and invalidations walk per-body candidate lists
+    unsigned* bal;                 // shared: one ballot per warp
+    int* box;                      // shared: a broadcast slot
+    float* ra;                     // shared: per-warp partial minima
+    int* rl;
+    unsigned* words;               // shared: one ballot per 32 positions of a scan (blockDim.x of them)
+    DG int rank() const { return threadIdx.x; }
+    DG int size() const { return blockDim.x; }
+    DG bool lead() const { return threadIdx.x == 0; }
+    DG void sync() const { __syncthreads(); }
+    DG int bcast(int v) const {
+        __syncthreads();
+        if (threadIdx.x == 0) box[0] = v;
+        __syncthreads();
+        return box[0];
+    }
+    DG void argmin(float& a, int& l) const {
+        for (int o = 16; o > 0; o >>= 1) {
+            const float oa = __shfl_xor_sync(0xffffffffu, a, o);
+            const int ol = __shfl_xor_sync(0xffffffffu, l, o);
+            if (oa < a || (oa == a && ol < l)) { a = oa; l = ol; }
+        }
+        __syncthreads();
+        if (lane_id() == 0) { ra[threadIdx.x >> 5] = a; rl[threadIdx.x >> 5] = l; }
+        __syncthreads();
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k)
+            if (ra[k] < a || (ra[k] == a && rl[k] < l)) { a = ra[k]; l = rl[k]; }
+    }
+    // positions [lo, n): 32 * blockDim.x at a time, every position's pred evaluated first (one
+    // ballot word per 32 positions, each warp a share of the words, loads of consecutive words
+    // in flight together), then a summary ballot per 32 words; the lead walks the non-empty
+    // words in order
+    template <class P, class F>
+    DG void scan_desc(int n, P&& pred, F&& f, int lo = 0) const {
+        const int nt = blockDim.x, nw = nt >> 5, warp = threadIdx.x >> 5, lane = lane_id();
+        bool stop = false;
+        for (int top = n - 1; top >= lo && !stop; top -= 32 * nt) {
+            const int nq = (top - lo) / 32 + 1 < nt ? (top - lo) / 32 + 1 : nt;    // words in use
+#pragma unroll 4
+            for (int q = warp; q < nq; q += nw) {
+                const int t = top - 32 * q - lane;
+                const unsigned b = __ballot_sync(0xffffffffu, t >= lo && pred(t));
+                if (lane == 0) words[q] = b;
+            }
+            __syncthreads();
+            for (int g = warp; 32 * g < nq; g += nw) {
+                const int q = 32 * g + lane;
+                const unsigned any = __ballot_sync(0xffffffffu, q < nq && words[q] != 0u);
+                if (lane == 0) bal[g] = any;
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                for (int g = 0; 32 * g < nq && !stop; ++g) {
+                    unsigned sm = bal[g];
+                    while (sm && !stop) {
+                        const int q = 32 * g + __ffs(sm) - 1;
+                        sm &= sm - 1;
+                        unsigned m = words[q];
+                        while (m) {
+                            const int l = __ffs(m) - 1;
+                            m &= m - 1;
+                            if (!f(top - 32 * q - l)) { stop = true; break; }
+                        }
+                    }
+                }
+                box[1] = stop;
+            }
+            __syncthreads();
+            stop = box[1] != 0;
+        }
+        __syncthreads();
+    }
+    template <class P>
+    DG int collect(int k0, int k1, int* list, int cnt, P&& pred) const {
+        const int nt = blockDim.x, nw = nt >> 5, warp = threadIdx.x >> 5, lane = lane_id();
+        for (int base = k0; base < k1; base += nt) {
+            const int k = base + (int)threadIdx.x;
+            const bool hit = k < k1 && pred(k);
+            const unsigned b = __ballot_sync(0xffffffffu, hit);
+            if (lane == 0) bal[warp] = b;
+            __syncthreads();
+            int before = 0, all = 0;
+            for (int q = 0; q < nw; ++q) {
+                const int c = __popc(bal[q]);
+                before += q < warp ? c : 0;
+                all += c;
+            }
+            if (hit) list[cnt + before + __popc(b & ((1u << lane) - 1u))] = k;
+            cnt += all;
+            __syncthreads();
+        }
+        return cnt;
+    }
+    template <class F>
+    DG int first_warp(F&& f) const {
+        int r = 0;
+        if (threadIdx.x < kWarp) r = f();
+        return bcast(r);
+    }
+    DG int prefix(bool v, int* all) const { return block_scan_value(v ? 1 : 0, rl, all); }
+};
+
+// b2ContactManager.AddPair (b2contactmanager.d:52-176) for the pairs in order, new contacts
+// appended in that order; a team of threads (a warp, or the block of a large world)
+template <class Team>
+__device__ __noinline__ void add_pairs_t(const Ctx& x, int w, int total, const Team& tm) {
     const WorldInfo& wi = x.wi[w];
     WorldDyn& wd = x.wd[w];
-    const int lane = lane_id();
+    const int rk = tm.rank(), ts = tm.size();
     int n = wd.contact_count;
     int added = 0;
-    for (int base = 0; base < total; base += kWarp) {
-        int i = base + lane;
+    for (int base = 0; base < total; base += ts) {
+        int i = base + rk;
         bool acc = false;
         int2 pr = make_int2(0, 0);
         if (i < total) {
@@ -565,9 +754,10 @@ __device__ __noinline__ void add_pairs(const Ctx& x, int w, int total) {
             if (acc) acc = body_should_collide(x, fB.body, fA.body);
             if (acc) acc = filter_should_collide(x, w, fA, fB);
         }
-        unsigned bal = __ballot_sync(0xffffffffu, acc);
+        int all;
+        const int before = tm.prefix(acc, &all);
         if (acc) {
-            int slot = n + added + __popc(bal & ((1u << lane) - 1));
+            int slot = n + added + before;
             if (slot < wi.contact_cap) {
                 // b2Contact.Create: the registry's primary order puts the polygon before a circle and
                 // an edge before a circle or a polygon (b2contact.d:358-400)
@@ -606,17 +796,18 @@ __device__ __noinline__ void add_pairs(const Ctx& x, int w, int total) {
                 }
             }
         }
-        added += __popc(bal);
-        tsync();
+        added += all;
+        tm.sync();
     }
     if (n + added > wi.contact_cap) {
-        if (lane == 0) set_error(x, w, DBOX_ERR_CAPACITY);
+        if (tm.lead()) set_error(x, w, DBOX_ERR_CAPACITY);
         added = wi.contact_cap - n;
     }
-    tsync();
-    if (lane == 0) wd.contact_count = n + added;
-    tsync();
+    tm.sync();
+    if (tm.lead()) wd.contact_count = n + added;
+    tm.sync();
 }
+DG void add_pairs(const Ctx& x, int w, int total) { add_pairs_t(x, w, total, WarpTeam()); }
 
 // b2ContactManager.FindNewContacts (b2contactmanager.d:320-323) on one warp
 __device__ __noinline__ void find_new_contacts(const Ctx& x, int w) {
@@ -4122,11 +4313,16 @@ DG void solve_world(const Ctx& x, int w, float* sbp, bool sb_smem, float* stage_
 
 // ------------------------------------------------------------ TOI
 // contact needs a fresh TOI (b2world.d:1159-1210); bodies from the compact arrays
+DG bool toi_needs_bodies(const Ctx& x, int ci, int b0);
 DG bool toi_needs(const Ctx& x, int ci, int b0) {
     const dbox_contact_state& c = x.ct[ci];
     if ((c.flags & kContactEnabled) == 0) return false;
     if (c.toi_count > kMaxSubSteps) return false;
     if (c.flags & kContactToi) return false;
+    return toi_needs_bodies(x, ci, b0);
+}
+// the part of toi_needs past the contact's own flags and sub-step count
+DG bool toi_needs_bodies(const Ctx& x, int ci, int b0) {
     if (x.s_cq[ci] & 2) return false;
     int2 cb = x.s_cbody[ci];
     const dbox_body_state& bA = x.bs[b0 + cb.x];
@@ -4238,165 +4434,6 @@ __device__ __noinline__ void solve_toi_island(const Ctx& x, int w, const WorldIn
         }
     }
 }
-
-// The threads that run one world's SolveTOI together: a warp (every world with the rest of its
-// step) or a block (a large world, after its pair search).  The lead (rank 0) does the serial
-// parts of the event loop; the passes over the contact list are spread over the team, and
-// the ones whose hits must be handled in list order hand them to the lead in that order.
-struct WarpTeam {
-    static constexpr bool kLists = false;        // joins and invalidations scan the candidate list
-    DG int rank() const { return lane_id(); }
-    DG int size() const { return kWarp; }
-    DG bool lead() const { return lane_id() == 0; }
-    DG void sync() const { __syncwarp(); }
-    DG int bcast(int v) const { return __shfl_sync(0xffffffffu, v, 0); }
-    // smallest (a, l) over the team: smallest a, then smallest l
-    DG void argmin(float& a, int& l) const {
-        for (int o = 16; o > 0; o >>= 1) {
-            const float oa = __shfl_xor_sync(0xffffffffu, a, o);
-            const int ol = __shfl_xor_sync(0xffffffffu, l, o);
-            if (oa < a || (oa == a && ol < l)) { a = oa; l = ol; }
-        }
-    }
-    // the lead calls f(t) for every t in [0, n) with pred(t), in descending t, until f returns
-    // false; pred must not depend on what f changes
-    template <class P, class F>
-    DG void scan_desc(int n, P&& pred, F&& f, int lo = 0) const {
-        const int lane = lane_id();
-        bool stop = false;
-        for (int base = n - 1; base >= lo && !stop; base -= kWarp) {
-            const int t = base - lane;
-            unsigned bal = __ballot_sync(0xffffffffu, t >= lo && pred(t));
-            if (lane == 0) {
-                while (bal) {
-                    const int l = __ffs(bal) - 1;
-                    bal &= bal - 1;
-                    if (!f(base - l)) { stop = true; break; }
-                }
-            }
-            __syncwarp();
-            stop = __shfl_sync(0xffffffffu, stop, 0);
-        }
-    }
-    // append every k in [k0, k1) with pred(k) to list[cnt ..] in ascending order; the new count
-    template <class P>
-    DG int collect(int k0, int k1, int* list, int cnt, P&& pred) const {
-        const int lane = lane_id();
-        for (int base = k0; base < k1; base += kWarp) {
-            const int k = base + lane;
-            const bool hit = k < k1 && pred(k);
-            const unsigned bal = __ballot_sync(0xffffffffu, hit);
-            if (hit) list[cnt + __popc(bal & ((1u << lane) - 1u))] = k;
-            cnt += __popc(bal);
-        }
-        return cnt;
-    }
-    // f() is warp-collective and returns the same int on every lane
-    template <class F>
-    DG int first_warp(F&& f) const { return f(); }
-};
-
-struct BlockTeam {
-    static constexpr bool kLists = true;         // joins and invalidations walk per-body candidate lists
-    unsigned* bal;                 // shared: one ballot per warp
-    int* box;                      // shared: a broadcast slot
-    float* ra;                     // shared: per-warp partial minima
-    int* rl;
-    unsigned* words;               // shared: one ballot per 32 positions of a scan (blockDim.x of them)
-    DG int rank() const { return threadIdx.x; }
-    DG int size() const { return blockDim.x; }
-    DG bool lead() const { return threadIdx.x == 0; }
-    DG void sync() const { __syncthreads(); }
-    DG int bcast(int v) const {
-        __syncthreads();
-        if (threadIdx.x == 0) box[0] = v;
-        __syncthreads();
-        return box[0];
-    }
-    DG void argmin(float& a, int& l) const {
-        for (int o = 16; o > 0; o >>= 1) {
-            const float oa = __shfl_xor_sync(0xffffffffu, a, o);
-            const int ol = __shfl_xor_sync(0xffffffffu, l, o);
-            if (oa < a || (oa == a && ol < l)) { a = oa; l = ol; }
-        }
-        __syncthreads();
-        if (lane_id() == 0) { ra[threadIdx.x >> 5] = a; rl[threadIdx.x >> 5] = l; }
-        __syncthreads();
-        for (int k = 0; k < (int)(blockDim.x >> 5); ++k)
-            if (ra[k] < a || (ra[k] == a && rl[k] < l)) { a = ra[k]; l = rl[k]; }
-    }
-    // positions [lo, n): 32 * blockDim.x at a time, every position's pred evaluated first (one
-    // ballot word per 32 positions, each warp a share of the words, loads of consecutive words
-    // in flight together), then a summary ballot per 32 words; the lead walks the non-empty
-    // words in order
-    template <class P, class F>
-    DG void scan_desc(int n, P&& pred, F&& f, int lo = 0) const {
-        const int nt = blockDim.x, nw = nt >> 5, warp = threadIdx.x >> 5, lane = lane_id();
-        bool stop = false;
-        for (int top = n - 1; top >= lo && !stop; top -= 32 * nt) {
-            const int nq = (top - lo) / 32 + 1 < nt ? (top - lo) / 32 + 1 : nt;    // words in use
-#pragma unroll 4
-            for (int q = warp; q < nq; q += nw) {
-                const int t = top - 32 * q - lane;
-                const unsigned b = __ballot_sync(0xffffffffu, t >= lo && pred(t));
-                if (lane == 0) words[q] = b;
-            }
-            __syncthreads();
-            for (int g = warp; 32 * g < nq; g += nw) {
-                const int q = 32 * g + lane;
-                const unsigned any = __ballot_sync(0xffffffffu, q < nq && words[q] != 0u);
-                if (lane == 0) bal[g] = any;
-            }
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                for (int g = 0; 32 * g < nq && !stop; ++g) {
-                    unsigned sm = bal[g];
-                    while (sm && !stop) {
-                        const int q = 32 * g + __ffs(sm) - 1;
-                        sm &= sm - 1;
-                        unsigned m = words[q];
-                        while (m) {
-                            const int l = __ffs(m) - 1;
-                            m &= m - 1;
-                            if (!f(top - 32 * q - l)) { stop = true; break; }
-                        }
-                    }
-                }
-                box[1] = stop;
-            }
-            __syncthreads();
-            stop = box[1] != 0;
-        }
-        __syncthreads();
-    }
-    template <class P>
-    DG int collect(int k0, int k1, int* list, int cnt, P&& pred) const {
-        const int nt = blockDim.x, nw = nt >> 5, warp = threadIdx.x >> 5, lane = lane_id();
-        for (int base = k0; base < k1; base += nt) {
-            const int k = base + (int)threadIdx.x;
-            const bool hit = k < k1 && pred(k);
-            const unsigned b = __ballot_sync(0xffffffffu, hit);
-            if (lane == 0) bal[warp] = b;
-            __syncthreads();
-            int before = 0, all = 0;
-            for (int q = 0; q < nw; ++q) {
-                const int c = __popc(bal[q]);
-                before += q < warp ? c : 0;
-                all += c;
-            }
-            if (hit) list[cnt + before + __popc(b & ((1u << lane) - 1u))] = k;
-            cnt += all;
-            __syncthreads();
-        }
-        return cnt;
-    }
-    template <class F>
-    DG int first_warp(F&& f) const {
-        int r = 0;
-        if (threadIdx.x < kWarp) r = f();
-        return bcast(r);
-    }
-};
 
 // b2World.SolveTOI (b2world.d:1127-1452) for world w, then the end of b2World.Step
 template <class Team>
@@ -4526,30 +4563,54 @@ DG void toi_world_t(const Ctx& x, int w, float* sbp, const Team& tm) {
             // the TOI of every contact that needs one (b2world.d:1159-1236), and in the same
             // pass the minimum TOI, first in list order on ties (each contact's TOI is
             // written only by its own iteration)
+            // (four candidates of a rank at a time: their slots, then their flags, counts and
+            // TOIs are loaded together, and the bodies are read only when the flags leave a
+            // fresh TOI possible)
             float bestA = 1.0f;
             int bestLp = 0x7fffffff;
-            for (int t = rk; t < ncand; t += ts) {
-                int k = cand[t];
-                dbox_contact_state& c = x.ct[c0 + k];
-                if (toi_needs(x, c0 + k, b0)) {
-                    const DFixture& fa = x.fx[c.fixture_a];
-                    const DFixture& fb = x.fx[c.fixture_b];
-                    Sweep sA, sB;
-                    float alpha0;
-                    if (advanced) { sA = x.snap[c0 + k].a; sB = x.snap[c0 + k].b; alpha0 = x.snap[c0 + k].alpha0; }
-                    else { sA = b_sweep(x.bs[fa.body]); sB = b_sweep(x.bs[fb.body]); alpha0 = sA.alpha0; }
-                    float beta;
-                    int state = time_of_impact(make_proxy(fa), make_proxy(fb), sA, sB, 1.0f, &beta);
-                    float alpha = state == kToiTouching ? bmin(alpha0 + (1.0f - alpha0) * beta, 1.0f) : 1.0f;
-                    c.toi = alpha;
-                    c.flags |= kContactToi;
+            for (int t0 = rk; t0 < ncand; t0 += 4 * ts) {
+                int kk[4];
+                uint32_t fl[4];
+                int tc[4];
+                float tv[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) kk[j] = t0 + j * ts < ncand ? cand[t0 + j * ts] : -1;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    fl[j] = 0u;
+                    tc[j] = 0;
+                    tv[j] = 1.0f;
+                    if (kk[j] >= 0) {
+                        const dbox_contact_state& c = x.ct[c0 + kk[j]];
+                        fl[j] = c.flags;
+                        tc[j] = c.toi_count;
+                        tv[j] = c.toi;
+                    }
                 }
-                const uint32_t fl = c.flags;
-                if ((fl & kContactEnabled) == 0 || c.toi_count > kMaxSubSteps) continue;
-                if ((fl & kContactToi) == 0) continue;
-                const float toi = c.toi;
-                int lp = n - 1 - k;
-                if (toi < bestA || (toi == bestA && lp < bestLp && toi < 1.0f)) { bestA = toi; bestLp = lp; }
+#pragma unroll 1
+                for (int j = 0; j < 4; ++j) {
+                    const int k = kk[j];
+                    if (k < 0 || (fl[j] & kContactEnabled) == 0 || tc[j] > kMaxSubSteps) continue;
+                    if ((fl[j] & kContactToi) == 0) {
+                        if (!toi_needs_bodies(x, c0 + k, b0)) continue;
+                        dbox_contact_state& c = x.ct[c0 + k];
+                        const DFixture& fa = x.fx[c.fixture_a];
+                        const DFixture& fb = x.fx[c.fixture_b];
+                        Sweep sA, sB;
+                        float alpha0;
+                        if (advanced) { sA = x.snap[c0 + k].a; sB = x.snap[c0 + k].b; alpha0 = x.snap[c0 + k].alpha0; }
+                        else { sA = b_sweep(x.bs[fa.body]); sB = b_sweep(x.bs[fb.body]); alpha0 = sA.alpha0; }
+                        float beta;
+                        int state = time_of_impact(make_proxy(fa), make_proxy(fb), sA, sB, 1.0f, &beta);
+                        float alpha = state == kToiTouching ? bmin(alpha0 + (1.0f - alpha0) * beta, 1.0f) : 1.0f;
+                        c.toi = alpha;
+                        c.flags |= kContactToi;
+                        tv[j] = alpha;
+                    }
+                    const float toi = tv[j];
+                    int lp = n - 1 - k;
+                    if (toi < bestA || (toi == bestA && lp < bestLp && toi < 1.0f)) { bestA = toi; bestLp = lp; }
+                }
             }
             mark(1);
             tm.argmin(bestA, bestLp);
@@ -4695,7 +4756,7 @@ DG void toi_world_t(const Ctx& x, int w, float* sbp, const Team& tm) {
                 tm.sync();
                 if (big_toi) {
                     const int total = nnow > 0 ? tm.first_warp([&]() { return toi_pairs_big(x, w, pnow, nnow, pall, nall, toimv); }) : 0;
-                    if (total > 0) tm.first_warp([&]() { add_pairs(x, w, total); return 0; });
+                    if (total > 0) add_pairs_t(x, w, total, tm);
                 } else {
                     tm.first_warp([&]() { find_new_contacts(x, w); return 0; });
                 }
@@ -4730,26 +4791,6 @@ DG void toi_world_t(const Ctx& x, int w, float* sbp, const Team& tm) {
 }
 
 DG void toi_world(const Ctx& x, int w, float* sbp) { toi_world_t(x, w, sbp, WarpTeam()); }
-
-// exclusive prefix of v over the block in thread order; *total gets the sum (all threads)
-DG int block_scan_value(int v, int* sh, int* total) {
-    const int lane = lane_id(), warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    int incl = v;
-    for (int o = 1; o < 32; o <<= 1) {
-        const int t = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += t;
-    }
-    __syncthreads();
-    if (lane == 31) sh[warp] = incl;
-    __syncthreads();
-    int before = 0, all = 0;
-    for (int q = 0; q < nw; ++q) {
-        before += q < warp ? sh[q] : 0;
-        all += sh[q];
-    }
-    *total = all;
-    return before + incl - v;
-}
 
 // k_collide_finish for a large world on a block of kPairThreads threads: the same steps, the
 // passes over its contacts spread over the block, the inactive contacts that a wake may
@@ -4876,10 +4917,9 @@ __global__ void __launch_bounds__(kPairThreads) k_finish_big_block(const __grid_
     const int w = x.big_worlds[blockIdx.x];
     const int total = x.wd[w].pair_total;
     const long long t_in = clock64();
-    if (threadIdx.x < kWarp && total > 0) add_pairs(x, w, total);
-    __syncthreads();
-    if (x.prof && threadIdx.x == 0) x.prof[kProfSlots * (size_t)w + 31] = clock64() - t_in;
     BlockTeam tm{s_bal, s_box, s_ra, s_rl, s_words};
+    if (total > 0) add_pairs_t(x, w, total, tm);
+    if (x.prof && threadIdx.x == 0) x.prof[kProfSlots * (size_t)w + 31] = clock64() - t_in;
     toi_world_t(x, w, x.s_sbody + 6 * (size_t)x.wi[w].body_start, tm);
 }
 
