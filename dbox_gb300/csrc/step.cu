@@ -1012,33 +1012,123 @@ __global__ void __launch_bounds__(kPairThreads) k_pairs_block(const __grid_const
         prof_out();
         return;
     }
-    for (int a = tid; a < nf; a += nt) {                                 // partners per proxy
-        int c = 0;
-        const dbox_proxy_state& p = x.px[f0 + PX(a)];
-        if (p.proxy_id >= 0)
-            sap_partners(s, proxy_fat(x, f0 + PX(a)), a, p.moved != 0, [&](int) { ++c; });
-        x.s_pcount[f0 + a] = c;
+    // partners per proxy.  An ordinary proxy finds its ordinary partners in the cells (a
+    // pair is listed under its lower-ranked proxy, and needs one of the two moved); a wide
+    // proxy finds its ordinary partners in the cells its box reaches (one thread per row of
+    // cells) and its wide partners in the wide list, so no proxy tests the wide list.  Counts,
+    // offsets, then the same passes fill the segments and each segment is sorted by partner.
+    int* pcount = x.s_pcount + f0;
+    int* pcur = x.s_moved + f0;
+    const int nwd = n_wide;
+    // rows of cells per wide proxy, for the row jobs
+    int* wrow = x.s_sapi[0] + f0 + nwd;                                  // nwd + 1 entries after the wide list
+    for (int q = tid; q <= nwd; q += nt) {
+        int rows = 0;
+        if (q < nwd) {
+            const float4 wb = box[nv + q];
+            const int cy0 = sap_cell(wb.y, s.oy, s.inv, s.ncy), cy1 = sap_cell(wb.w, s.oy, s.inv, s.ncy);
+            rows = cy1 - (cy0 > 0 ? cy0 - 1 : 0) + 1;
+        }
+        wrow[q] = rows;
     }
     __syncthreads();
-    const int total = block_exclusive_scan(x.s_pcount + f0, nf, shi);
+    const int njobs = block_exclusive_scan(wrow, nwd + 1, shi);
+    auto wide_row = [&](int job, auto&& emit) {                          // job: one row of one wide proxy
+        int q = 0, lo = 0, hi = nwd;                                     // the last q with wrow[q] <= job
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (wrow[mid] <= job) lo = mid; else hi = mid - 1;
+        }
+        q = lo;
+        const int wi_ = wide[q];
+        const int wr = wi_ & 0x7fffffff;
+        const bool wmoved = wi_ < 0;
+        const float4 wb = box[nv + q];
+        AABB fw;
+        fw.lo = v2(wb.x, wb.y);
+        fw.hi = v2(wb.z, wb.w);
+        const int cx0 = sap_cell(wb.x, s.ox, s.inv, s.ncx), cx1 = sap_cell(wb.z, s.ox, s.inv, s.ncx);
+        const int cy0 = sap_cell(wb.y, s.oy, s.inv, s.ncy);
+        const int cy = (cy0 > 0 ? cy0 - 1 : 0) + (job - wrow[q]);
+        const int xa = cx0 > 0 ? cx0 - 1 : 0;
+        const int qe = s.cstart[cy * s.ncx + cx1 + 1];
+        for (int e = s.cstart[cy * s.ncx + xa]; e < qe; ++e) {
+            const int bi = s.idx[e];
+            if (!wmoved && bi >= 0) continue;
+            const float4 bb = s.box[e];
+            AABB fb;
+            fb.lo = v2(bb.x, bb.y);
+            fb.hi = v2(bb.z, bb.w);
+            if (!aabb_overlap(fw, fb)) continue;
+            const int b = bi & 0x7fffffff;
+            emit(wr < b ? wr : b, wr < b ? b : wr);
+        }
+    };
+    auto wide_wide = [&](int q, auto&& emit) {                           // wide q with wide v, ranks above q's
+        const int wi_ = wide[q];
+        const int wr = wi_ & 0x7fffffff;
+        const float4 wb = box[nv + q];
+        AABB fw;
+        fw.lo = v2(wb.x, wb.y);
+        fw.hi = v2(wb.z, wb.w);
+        for (int v = 0; v < nwd; ++v) {
+            const int vi = wide[v];
+            const int vr = vi & 0x7fffffff;
+            if (vr <= wr || (wi_ >= 0 && vi >= 0)) continue;
+            const float4 vb = box[nv + v];
+            AABB fv;
+            fv.lo = v2(vb.x, vb.y);
+            fv.hi = v2(vb.z, vb.w);
+            if (aabb_overlap(fw, fv)) emit(wr, vr);
+        }
+    };
+    Sap sc = s;                                                          // the cells alone
+    sc.nwide = 0;
+    for (int a = tid; a < nf; a += nt) {
+        int c = 0;
+        const dbox_proxy_state& p = x.px[f0 + PX(a)];
+        if (p.proxy_id >= 0 && extent(p) <= cut)
+            sap_partners(sc, proxy_fat(x, f0 + PX(a)), a, p.moved != 0, [&](int) { ++c; });
+        pcount[a] = c;
+    }
+    __syncthreads();
+    for (int job = tid; job < njobs; job += nt) wide_row(job, [&](int own, int) { atomicAdd(&pcount[own], 1); });
+    for (int q = tid; q < nwd; q += nt) wide_wide(q, [&](int own, int) { atomicAdd(&pcount[own], 1); });
+    __syncthreads();
+    const int total = block_exclusive_scan(pcount, nf, shi);
     if (total > wi.pair_cap) {
         if (tid == 0) { set_error(x, w, DBOX_ERR_CAPACITY); wd.pair_total = 0; }
         prof_out();
         return;
     }
-    for (int a = tid; a < nf; a += nt) {                                 // the pairs, partners by rank
+    int2* seg0 = x.pairs + wi.pair_start;
+    for (int a = tid; a < nf; a += nt) {                                 // ordinary partners first
         const dbox_proxy_state& p = x.px[f0 + PX(a)];
-        if (p.proxy_id < 0) continue;
-        int2* seg = x.pairs + wi.pair_start + x.s_pcount[f0 + a];
         int c = 0;
-        sap_partners(s, proxy_fat(x, f0 + PX(a)), a, p.moved != 0, [&](int b) { seg[c++] = make_int2(a, b); });
-        for (int i = 1; i < c; ++i) {
-            int2 v = seg[i];
-            int j = i - 1;
-            while (j >= 0 && seg[j].y > v.y) { seg[j + 1] = seg[j]; --j; }
-            seg[j + 1] = v;
+        if (p.proxy_id >= 0 && extent(p) <= cut) {
+            int2* seg = seg0 + pcount[a];
+            sap_partners(sc, proxy_fat(x, f0 + PX(a)), a, p.moved != 0, [&](int b) { seg[c++] = make_int2(a, b); });
         }
-        for (int i = 0; i < c; ++i) seg[i] = make_int2(f0 + PX(seg[i].x), f0 + PX(seg[i].y));
+        pcur[a] = pcount[a] + c;
+    }
+    __syncthreads();
+    auto put = [&](int own, int other) { seg0[atomicAdd(&pcur[own], 1)] = make_int2(own, other); };
+    for (int job = tid; job < njobs; job += nt) wide_row(job, put);
+    for (int q = tid; q < nwd; q += nt) wide_wide(q, put);
+    __syncthreads();
+    for (int a = tid; a < nf; a += nt) {                                 // each segment by partner rank
+        int2* seg = seg0 + pcount[a];
+        const int d = (a + 1 < nf ? pcount[a + 1] : total) - pcount[a];
+        int gap = 1;
+        while (3 * gap + 1 < d) gap = 3 * gap + 1;
+        for (; gap > 0; gap /= 3)
+            for (int i = gap; i < d; ++i) {
+                const int2 v = seg[i];
+                int j = i - gap;
+                while (j >= 0 && seg[j].y > v.y) { seg[j + gap] = seg[j]; j -= gap; }
+                seg[j + gap] = v;
+            }
+        for (int i = 0; i < d; ++i) seg[i] = make_int2(f0 + PX(seg[i].x), f0 + PX(seg[i].y));
     }
     __syncthreads();
     for (int i = tid; i < nf; i += nt) x.px[f0 + i].moved = 0;          // the move buffer is consumed
