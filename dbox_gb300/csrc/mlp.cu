@@ -114,10 +114,12 @@ __device__ __forceinline__ void get16_rows(const uint8_t* buf, int row, int c0, 
 
 // Forward + backward of MSE(MLP(x), t) / (n * 4) over n samples of `rows` (kSampleFloats per
 // sample: features, then targets): samples idx[0 .. n), or, with idx NULL, the samples
-// perm(offset + 0 .. n) of a shuffle; normalised with the model's statistics; gradients
-// added into grad (kNParams), the sum of squared errors into *loss.  *status gets 1 if a wait
-// for the tensor core ran past its bound.
-__global__ void __launch_bounds__(kTcThreads, 1) k_mlp_train(MlpDev m, float* grad, const float* rows, const int* idx,
+// perm(offset + 0 .. n) of a shuffle; normalised with the model's statistics.  CTA b writes
+// the gradient of its tiles to gpart[b * kNParams ..] (every entry, padding as zero; the
+// partial rows are summed by the consumer), the sum of squared errors is added into *loss.
+// *status gets 1 if a wait for the tensor core ran past its bound.  The next tile's samples
+// are loaded while the current tile is in the tensor core.
+__global__ void __launch_bounds__(kTcThreads, 1) k_mlp_train(MlpDev m, float* gpart, const float* rows, const int* idx,
                                                              int n, Perm perm, int offset, float* loss, int* status) {
     extern __shared__ uint8_t tc_smem_raw[];
     uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(tc_smem_raw) + 1023) & ~uintptr_t(1023));
@@ -193,20 +195,33 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_train(MlpDev m, float* gr
     const int cbeg = half * 64;
     float lsum = 0.0f, db3[4] = {0.0f, 0.0f, 0.0f, 0.0f};
     bool first = true;
+    // this thread's row of a tile: half 0 features 0..15 and the targets, half 1 features 16..31
+    auto fetch = [&](int tile, float* fv, float* tv) {
+        const int r0 = tile * 128;
+        const bool valid = tile < ntiles && r0 + row < n;
+        const int sid = !valid ? 0 : (idx ? idx[r0 + row] : (int)perm_apply(perm, (uint32_t)(offset + r0 + row)));
+        const float* sample = rows + (size_t)sid * kSampleFloats;
+#pragma unroll
+        for (int j = 0; j < 16; ++j) fv[j] = valid ? sample[half * 16 + j] : 0.0f;
+#pragma unroll
+        for (int o = 0; o < kOut; ++o) tv[o] = valid && half == 0 ? sample[kFeat + o] : 0.0f;
+    };
+    float fcur[16], tcur[kOut];
+    fetch(blockIdx.x, fcur, tcur);
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int r0 = tile * 128;
         const bool valid = r0 + row < n;
-        const int sid = !valid ? 0 : (idx ? idx[r0 + row] : (int)perm_apply(perm, (uint32_t)(offset + r0 + row)));
-        const float* sample = valid ? rows + (size_t)sid * kSampleFloats : nullptr;
         {   // inputs: half 0 writes features 0..15 of its row, half 1 features 16..31
             float v[16];
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
                 const int f = half * 16 + j;
-                v[j] = valid ? (sample[f] - m.fmean[f]) / m.fstd[f] : 0.0f;
+                v[j] = valid ? (fcur[j] - m.fmean[f]) / m.fstd[f] : 0.0f;
             }
             put16(X, row, half * 16, v);
         }
+        float fnext[16], tnext[kOut];
+        fetch(tile + gridDim.x, fnext, tnext);
         sync_for_mma();
         if (tid == 0) {                                   // Z1 = X W1 (K = 32)
             for (int ks = 0; ks < 2; ++ks) tc::mma(T + kTZ, tc::desc_k(aX, ks, 16384), tc::desc_k(aW1, ks, 16384), kKK128, ks > 0);
@@ -249,7 +264,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_train(MlpDev m, float* gr
             for (int o = 0; o < kOut; ++o) {
                 d[o] = 0.0f;
                 if (valid) {
-                    const float tv = (sample[kFeat + o] - m.tmean[o]) / m.tstd[o];
+                    const float tv = (tcur[o] - m.tmean[o]) / m.tstd[o];
                     const float diff = y[o] + b3[o] - tv;
                     lsum += diff * diff;
                     d[o] = 2.0f * diff * inv;
@@ -309,6 +324,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_train(MlpDev m, float* gr
         }
         wait_mma();
         first = false;
+#pragma unroll
+        for (int j = 0; j < 16; ++j) fcur[j] = fnext[j];
+#pragma unroll
+        for (int o = 0; o < kOut; ++o) tcur[o] = tnext[o];
         __syncthreads();                                  // the next tile rewrites X and the activations
     }
     // loss and db3: warp sums, then the block's
@@ -323,8 +342,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_train(MlpDev m, float* gr
 #pragma unroll
         for (int q = 0; q < kOut; ++q) atomicAdd(&s_db3[q], db3[q]);
     }
-    // the CTA's gradients: this thread's lane is hidden unit `row`
-    float* gw1 = grad;
+    // the CTA's gradients, this thread's lane being hidden unit `row`, into the CTA's partial row
+    float* gw1 = gpart + (size_t)blockIdx.x * kNParams;
     float* gw2 = gw1 + kW1;
     float* gw3 = gw2 + kW2;
     float* gb1 = gw3 + kW3;
@@ -334,28 +353,29 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_train(MlpDev m, float* gr
         float v[16];
         tc::ld16(T + lane_off + kTdW2 + c0, v);
 #pragma unroll
-        for (int j = 0; j < 16; ++j) atomicAdd(gw2 + row * kHid + c0 + j, v[j]);
+        for (int j = 0; j < 16; j += 4)
+            *reinterpret_cast<float4*>(gw2 + row * kHid + c0 + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
     }
     if (half == 0) {
         float v[16];
-        tc::ld16(T + lane_off + kTdW3, v);                // dW3[hidden = row][0..3]
+        tc::ld16(T + lane_off + kTdW3, v);                // dW3[hidden = row][0..3], padding zero
 #pragma unroll
-        for (int j = 0; j < kOut; ++j) atomicAdd(gw3 + row * kOutPad + j, v[j]);
+        for (int j = 0; j < kOutPad; ++j) gw3[row * kOutPad + j] = j < kOut ? v[j] : 0.0f;
         for (int c0 = 0; c0 < kFeat; c0 += 16) {          // dW1[feature][hidden = row]
             tc::ld16(T + lane_off + kTdW1 + c0, v);
 #pragma unroll
-            for (int j = 0; j < 16; ++j) atomicAdd(gw1 + (c0 + j) * kHid + row, v[j]);
+            for (int j = 0; j < 16; ++j) gw1[(c0 + j) * kHid + row] = v[j];
         }
         tc::ld16(T + lane_off + kTdb2, v);
-        atomicAdd(gb2 + row, v[0]);
+        gb2[row] = v[0];
     } else {
         float v[16];
         tc::ld16(T + lane_off + kTdb1, v);
-        atomicAdd(gb1 + row, v[0]);
+        gb1[row] = v[0];
     }
     tc::fence_before_sync();
     __syncthreads();
-    if (tid < kOut) atomicAdd(gb3 + tid, s_db3[tid]);
+    if (tid < kOutPad) gb3[tid] = tid < kOut ? s_db3[tid] : 0.0f;
     if (tid == 0) atomicAdd(loss, s_loss);
     if (!ok && lane == 0) atomicExch(status, 1);
     if (warp == 0) tc::tmem_free(T, kTCols);
@@ -384,14 +404,25 @@ __global__ void k_mlp_refresh(const float* p, __nv_bfloat16* wt1, __nv_bfloat16*
     }
 }
 
-// Adam (beta1 0.9, beta2 0.999, eps 1e-8) on the flat parameter vector, clearing grad, and the
-// BF16 copies of the updated weights (as k_mlp_refresh writes them)
-__global__ void k_mlp_adam(float* p, float* grad, float* mom, float* vel, int n, float lr, float bc1, float bc2,
-                           __nv_bfloat16* wt1, __nv_bfloat16* wt2, __nv_bfloat16* wt3, __nv_bfloat16* wb1,
+// the gradient of a batch: the sum of the `parts` partial rows k_mlp_train wrote
+__device__ __forceinline__ float grad_sum(const float* gpart, int parts, int i) {
+    float g = 0.0f;
+    for (int b = 0; b < parts; ++b) g += gpart[(size_t)b * kNParams + i];
+    return g;
+}
+__global__ void k_mlp_reduce(const float* gpart, int parts, float* grad) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kNParams; i += gridDim.x * blockDim.x)
+        grad[i] = grad_sum(gpart, parts, i);
+}
+
+// Adam (beta1 0.9, beta2 0.999, eps 1e-8) on the flat parameter vector, its gradient the sum of
+// the batch's partial rows, and the BF16 copies of the updated weights (as k_mlp_refresh
+// writes them)
+__global__ void k_mlp_adam(float* p, const float* gpart, int parts, float* mom, float* vel, int n, float lr, float bc1,
+                           float bc2, __nv_bfloat16* wt1, __nv_bfloat16* wt2, __nv_bfloat16* wt3, __nv_bfloat16* wb1,
                            __nv_bfloat16* wb2, __nv_bfloat16* wb3) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        float gi = grad[i];
-        grad[i] = 0.0f;
+        float gi = grad_sum(gpart, parts, i);
         bool pad = false;
         if (i >= kW1 + kW2 && i < kW1 + kW2 + kW3) pad = ((i - kW1 - kW2) % kOutPad) >= kOut;
         if (i >= kW1 + kW2 + kW3 + 2 * kHid) pad = (i - (kW1 + kW2 + kW3 + 2 * kHid)) >= kOut;
@@ -455,7 +486,8 @@ __global__ void __launch_bounds__(128) k_mlp_forward(MlpDev m, const float* feat
 struct dbox_mlp {
     int device = 0;
     float* p = nullptr;           // kNParams
-    float* grad = nullptr;
+    float* grad = nullptr;        // kNParams: a batch's gradient, for dbox_mlp_gradient
+    float* gpart = nullptr;       // nsm x kNParams: per-CTA partial gradients of a batch
     float* mom = nullptr;
     float* vel = nullptr;
     float* norm = nullptr;        // fmean 32, fstd 32, tmean 4, tstd 4
@@ -502,14 +534,17 @@ int refresh(dbox_mlp* m) {
     return cuerr(cudaGetLastError(), "k_mlp_refresh");
 }
 
-// gradient of one batch (rows idx[0..n)) added into m->grad; loss sum into m->loss: one CTA per
-// SM at most, each taking 128-sample tiles in turn
-int run_batch(dbox_mlp* m, const float* rows, const int* idx, int n, const dg::Perm& perm = dg::Perm(), int offset = 0) {
+// gradient of one batch (rows idx[0..n)) as partial rows in m->gpart (*parts of them); loss sum
+// added into m->loss: one CTA per SM at most, each taking 128-sample tiles in turn
+int run_batch(dbox_mlp* m, const float* rows, const int* idx, int n, int* parts, const dg::Perm& perm = dg::Perm(),
+              int offset = 0) {
+    *parts = 0;
     if (n <= 0) return DBOX_OK;
     const int tiles = (n + 127) / 128;
     const int blocks = tiles < m->nsm ? tiles : m->nsm;
-    dg::k_mlp_train<<<blocks, dg::kTcThreads, dg::kTcSmemBytes>>>(mlp_dev(m), m->grad, rows, idx, n, perm, offset, m->loss,
-                                                                 m->status);
+    dg::k_mlp_train<<<blocks, dg::kTcThreads, dg::kTcSmemBytes>>>(mlp_dev(m), m->gpart, rows, idx, n, perm, offset,
+                                                                 m->loss, m->status);
+    *parts = blocks;
     return cuerr(cudaGetLastError(), "k_mlp_train");
 }
 
@@ -592,6 +627,10 @@ int32_t dbox_mlp_create(dbox_mlp** out) {
     cudaMemset(m->status, 0, sizeof(int));
     cudaDeviceGetAttribute(&m->nsm, cudaDevAttrMultiProcessorCount, m->device);
     if (m->nsm < 1) m->nsm = 1;
+    if (cudaMalloc(&m->gpart, sizeof(float) * dg::kNParams * (size_t)m->nsm) != cudaSuccess) {
+        dbox_mlp_destroy(m);
+        return dbox_set_error(DBOX_ERR_CUDA, "dbox_mlp_create: device allocation failed");
+    }
     cudaFuncSetAttribute(dg::k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dg::kTcSmemBytes);
     int r = refresh(m);
     if (r) { dbox_mlp_destroy(m); return r; }
@@ -601,7 +640,7 @@ int32_t dbox_mlp_create(dbox_mlp** out) {
 
 int32_t dbox_mlp_destroy(dbox_mlp* m) {
     if (!m) return DBOX_OK;
-    cudaFree(m->p); cudaFree(m->grad); cudaFree(m->mom); cudaFree(m->vel);
+    cudaFree(m->p); cudaFree(m->grad); cudaFree(m->gpart); cudaFree(m->mom); cudaFree(m->vel);
     cudaFree(m->norm); cudaFree(m->wbuf); cudaFree(m->loss); cudaFree(m->status);
     delete m;
     return DBOX_OK;
@@ -687,16 +726,19 @@ int32_t dbox_mlp_gradient(dbox_mlp* m, int32_t n, const float* feats, const floa
     std::vector<int> idx(n);
     for (int i = 0; i < n; ++i) idx[i] = i;
     cudaMemcpy(di, idx.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice);
-    cudaMemset(m->grad, 0, sizeof(float) * dg::kNParams);
     cudaMemset(m->loss, 0, sizeof(float));
-    r = run_batch(m, drows, di, n);
+    int parts = 0;
+    r = run_batch(m, drows, di, n, &parts);
+    if (!r) {
+        dg::k_mlp_reduce<<<(dg::kNParams + 255) / 256, 256>>>(m->gpart, parts, m->grad);
+        r = cuerr(cudaGetLastError(), "k_mlp_reduce");
+    }
     if (!r) r = cuerr(cudaDeviceSynchronize(), "dbox_mlp_gradient");
     if (!r) r = check_train_status(m);
     if (!r && grad) r = cuerr(cudaMemcpy(grad, m->grad, sizeof(float) * dg::kNParams, cudaMemcpyDeviceToHost), "grad");
     float l = 0.0f;
     if (!r) r = cuerr(cudaMemcpy(&l, m->loss, sizeof(float), cudaMemcpyDeviceToHost), "loss");
     if (loss) *loss = l / (4.0f * (float)n);
-    cudaMemset(m->grad, 0, sizeof(float) * dg::kNParams);
     cudaFree(drows); cudaFree(di);
     return r;
 }
@@ -715,11 +757,12 @@ int32_t dbox_mlp_train_device(dbox_mlp* m, int32_t n, const float* rows, int32_t
         cudaMemset(m->loss, 0, sizeof(float));
         for (int b0 = 0; b0 < n && !r; b0 += batch) {
             int nb = std::min(batch, n - b0);
-            r = run_batch(m, rows, nullptr, nb, perm, b0);
+            int parts = 0;
+            r = run_batch(m, rows, nullptr, nb, &parts, perm, b0);
             if (r) break;
             ++m->step;
             float bc1 = 1.0f - powf(0.9f, (float)m->step), bc2 = 1.0f - powf(0.999f, (float)m->step);
-            dg::k_mlp_adam<<<86, 256>>>(m->p, m->grad, m->mom, m->vel, dg::kNParams, lr, bc1, bc2,
+            dg::k_mlp_adam<<<(dg::kNParams + 255) / 256, 256>>>(m->p, m->gpart, parts, m->mom, m->vel, dg::kNParams, lr, bc1, bc2,
                                         const_cast<__nv_bfloat16*>(d.wt1), const_cast<__nv_bfloat16*>(d.wt2),
                                         const_cast<__nv_bfloat16*>(d.wt3), const_cast<__nv_bfloat16*>(d.wb1),
                                         const_cast<__nv_bfloat16*>(d.wb2), const_cast<__nv_bfloat16*>(d.wb3));
