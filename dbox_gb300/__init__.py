@@ -115,6 +115,7 @@ def lib():
     L.dbox_world_set_measure.argtypes = [vp, i32]
     L.dbox_world_set_wait_limit.argtypes = [vp, i32]
     L.dbox_world_set_island_solver.argtypes = [vp, i32]
+    L.dbox_world_get_island_solver.argtypes = [vp, vp]
     L.dbox_world_set_listener.argtypes = [vp, vp, vp]
     L.dbox_world_set_presolve.argtypes = [vp, vp, vp]
     L.dbox_fixture_set_filter.argtypes = [vp, i32, i32, ctypes.c_uint16, ctypes.c_uint16, ctypes.c_int16]
@@ -163,6 +164,9 @@ def collide_manifolds_noalloc(shapes_a, xfs_a, shapes_b, xfs_b):
 
 
 MLP_PARAMS, MLP_NORM, MLP_SAMPLE, MLP_FEAT = 21768, 72, 36, 32
+# a world with this many fixtures or more runs the large-world kernels (block pair search, Solve,
+# Collide end and SolveTOI on a 1,024-thread block each)
+LARGE_WORLD_FIXTURES = 4096
 
 
 class Mlp:
@@ -279,6 +283,7 @@ class World:
                 for d in s.get(kind + "_joints", ()):
                     self.create_joint(i, kind, d)
         self.body_counts = [len(s["bodies"]) for s in scenes]
+        self.large_worlds = sum(1 for s in scenes if len(s["fixtures"]) >= LARGE_WORLD_FIXTURES)
         if flags is not None:
             self.set_flags(**flags)
 
@@ -567,10 +572,11 @@ class World:
         else:
             self.set_mapping(choice[0], choice[1], choice[2])
 
-    @staticmethod
-    def autotune_steps(steps):
-        """Steps the worlds advance during autotune(steps)."""
-        return 1 + 20 * (steps + 1)
+    def autotune_steps(self, steps):
+        """Steps the worlds advance during autotune(steps): two rounds over 10 mappings, and
+        with large worlds two rounds over the 2 island solvers, each trial a graph build step
+        plus `steps`, after one profiled step."""
+        return 1 + 20 * (steps + 1) + (4 * (steps + 1) if self.large_worlds else 0)
 
     def autotune(self, steps=3, dt=1.0 / 60.0, vel_iters=8, pos_iters=3):
         """Time the candidate mappings of worlds onto the solve kernel on the live worlds and
@@ -588,6 +594,11 @@ class World:
     def set_island_solver(self, mode=0):
         """Large worlds' Solve on a block (0, default) or on a warp (1); the same results."""
         _check(lib().dbox_world_set_island_solver(self.h, mode), "dbox_world_set_island_solver")
+
+    def island_solver(self):
+        out = ctypes.c_int32()
+        _check(lib().dbox_world_get_island_solver(self.h, ctypes.byref(out)), "dbox_world_get_island_solver")
+        return out.value
 
     def set_measure(self, on=True):
         _check(lib().dbox_world_set_measure(self.h, 1 if on else 0), "dbox_world_set_measure")

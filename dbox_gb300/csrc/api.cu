@@ -2264,6 +2264,12 @@ int32_t dbox_world_set_wait_limit(dbox_world* w, int32_t polls) {
     return DBOX_OK;
 }
 
+int32_t dbox_world_get_island_solver(dbox_world* w, int32_t* mode) {
+    if (!w || !mode) return fail(DBOX_ERR_INVALID, "dbox_world_get_island_solver: bad arguments");
+    *mode = w->island_solver;
+    return DBOX_OK;
+}
+
 int32_t dbox_world_set_island_solver(dbox_world* w, int32_t mode) {
     if (!w || mode < 0 || mode > 1) return fail(DBOX_ERR_INVALID, "dbox_world_set_island_solver: bad arguments");
     w->island_solver = mode;
@@ -2411,10 +2417,29 @@ int32_t dbox_world_autotune(dbox_world* w, float dt, int32_t velocity_iterations
             if (round == 1 && ms < best) { best = ms; bi = c; }
         }
     }
+    if (rc) { cudaEventDestroy(e0); cudaEventDestroy(e1); return rc; }
+    rc = apply(bi);
+    // large worlds: their Solve on a block or on a warp, timed the same way under the mapping kept
+    if (!rc && w->n_big > 0 && w->ws_mode == 0) {
+        float tbest[2] = {3.4e38f, 3.4e38f};
+        for (int round = 0; round < 2 && !rc; ++round)
+            for (int mode = 0; mode < 2 && !rc; ++mode) {
+                rc = dbox_world_set_island_solver(w, mode);
+                if (!rc) rc = dbox_world_step_n(w, dt, velocity_iterations, position_iterations, 1);
+                if (rc) break;
+                CU(cudaEventRecord(e0, w->stream));
+                rc = dbox_world_step_n(w, dt, velocity_iterations, position_iterations, steps);
+                CU(cudaEventRecord(e1, w->stream));
+                CU(cudaEventSynchronize(e1));
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (round == 1) tbest[mode] = ms;
+            }
+        if (!rc) rc = dbox_world_set_island_solver(w, tbest[1] < tbest[0] ? 1 : 0);
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (rc) return rc;
-    rc = apply(bi);
     if (choice) {
         if (cand[bi][0]) { choice[0] = 0; choice[1] = 0; choice[2] = 0; choice[3] = 1; choice[4] = cand[bi][1]; choice[5] = cand[bi][2]; }
         else { choice[0] = cand[bi][1]; choice[1] = cand[bi][2]; choice[2] = cand[bi][3]; choice[3] = 0; choice[4] = 0; choice[5] = 0; }

@@ -665,7 +665,9 @@ int32_t dbox_world_get_world_costs(dbox_world* w, float* out);
  * costs), then times `steps` steps (the simulation advances) under each candidate mapping,
  * twice, and keeps the fastest; choice[6] receives (warps per block, body budget, isolated,
  * queue, heavy, exclusive): the first three for a block packing (queue = 0), the last two
- * for a queue mapping (queue = 1). */
+ * for a queue mapping (queue = 1).  With large worlds (4,096+ fixtures) it then times their
+ * Solve on a block and on a warp the same way and keeps the faster island solver
+ * (dbox_world_get_island_solver). */
 int32_t dbox_world_autotune(dbox_world* w, float dt, int32_t velocity_iterations, int32_t position_iterations,
                             int32_t steps, int32_t* choice);
 
@@ -683,6 +685,8 @@ int32_t dbox_world_set_wait_limit(dbox_world* w, int32_t polls);
  * (dbox_world_set_warmstart 1..3) always take the warp.  Replaces no reference call: the
  * reference solves islands one after another on the calling thread (dynamics/b2world.d:930-1124). */
 int32_t dbox_world_set_island_solver(dbox_world* w, int32_t mode);
+/* The mode in use (set by the call above or chosen by dbox_world_autotune). */
+int32_t dbox_world_get_island_solver(dbox_world* w, int32_t* mode);
 
 /* Device kernels launched by the last step (for launch accounting). */
 int32_t dbox_world_last_launches(dbox_world* w, int32_t* out);

@@ -81,3 +81,4 @@ def test_invalid_arguments_rejected_without_device(gpu_lib):
     assert L.dbox_world_step(None, ctypes.c_float(0.016), 8, 3) == -1
     assert L.dbox_world_set_wait_limit(None, 0) == -1
     assert L.dbox_world_set_island_solver(None, 0) == -1
+    assert L.dbox_world_get_island_solver(None, None) == -1
