@@ -22,6 +22,7 @@
 
 extern "C" int dbox_launch_step(const dg::Ctx* x, cudaStream_t stream, int* launches);
 extern "C" const void* dbox_solve_kernel();
+extern "C" int dbox_big_solve_init();
 const dg::MlpDev* dbox_mlp_device_view(const dbox_mlp* m, dg::MlpDev* out);
 extern "C" int dbox_launch_step_ev(const dg::Ctx* x, cudaStream_t stream, int* launches, cudaEvent_t* ev);
 extern "C" int dbox_launch_collide(const dg::Ctx* x, cudaStream_t stream);
@@ -695,6 +696,7 @@ int ensure_device(dbox_world* w) {
         if (rc) return rc;
         rc = upload(w);
         if (rc) return rc;
+        if (w->n_big > 0) CU((cudaError_t)dbox_big_solve_init());
     }
     return sync_filter(w);
 }
@@ -808,7 +810,7 @@ dg::Ctx make_ctx(dbox_world* w, float dt, int vi, int pi) {
     x.s_sapcell = w->s_sapcell.p;
     x.big_worlds = w->d_big.p;
     x.n_big = w->n_big;
-    x.big_block = (w->n_big > 0 && w->ws_mode == 0 && w->island_solver == 0) ? 1 : 0;
+    x.big_block = (w->n_big > 0 && w->island_solver == 0) ? 1 : 0;
     x.s_cevt = w->s_cevt.p;
     return x;
 }
@@ -2420,7 +2422,7 @@ int32_t dbox_world_autotune(dbox_world* w, float dt, int32_t velocity_iterations
     if (rc) { cudaEventDestroy(e0); cudaEventDestroy(e1); return rc; }
     rc = apply(bi);
     // large worlds: their Solve on a block or on a warp, timed the same way under the mapping kept
-    if (!rc && w->n_big > 0 && w->ws_mode == 0) {
+    if (!rc && w->n_big > 0) {
         float tbest[2] = {3.4e38f, 3.4e38f};
         for (int round = 0; round < 2 && !rc; ++round)
             for (int mode = 0; mode < 2 && !rc; ++mode) {

@@ -126,6 +126,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_train(MlpDev m, float* gp
     __shared__ uint64_t bar;
     __shared__ uint32_t tbase;
     __shared__ float s_db3[4], s_loss;
+    __shared__ float s_bias[2 * kHid];                  // b1, b2
+    __shared__ float s_fnorm[2 * kFeat];                // feature means, standard deviations
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int quad = warp & 3, half = warp >> 2;
     const int row = quad * 32 + lane;                    // sample (or hidden unit) of this thread's lane
@@ -144,23 +146,32 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_train(MlpDev m, float* gp
     const float* b1 = m.p + kW1 + kW2 + kW3;
     const float* b2 = b1 + kHid;
     const float* b3 = b2 + kHid;
-    // weights and constant tiles (the zero padding of X and dY stays zero for every tile)
-    const __nv_bfloat16 zero = __float2bfloat16_rn(0.0f), one = __float2bfloat16_rn(1.0f);
-    for (int i = tid; i < 128 * 64; i += kTcThreads) {
-        const int r = i >> 6, c = i & 63;
-        *reinterpret_cast<__nv_bfloat16*>(W1 + tc::sw128_offset(r, c, 128)) = c < kFeat ? m.wt1[r * kFeat + c] : zero;
-        *reinterpret_cast<__nv_bfloat16*>(X + tc::sw128_offset(r, c, 128)) = zero;
-        *reinterpret_cast<__nv_bfloat16*>(DY + tc::sw128_offset(r, c, 128)) = zero;
+    // weights and constant tiles (the zero padding of X and dY stays zero for every tile), 16
+    // bytes at a time: eight consecutive columns of a row are one 16-byte chunk of the swizzle
+    const uint4 z4 = make_uint4(0u, 0u, 0u, 0u);
+    const uint32_t one2 = pack_bf16x2(1.0f, 1.0f);
+    const uint4 ones4 = make_uint4(one2, one2, one2, one2);
+#pragma unroll 4
+    for (int i = tid; i < 128 * 8; i += kTcThreads) {
+        const int r = i >> 3, c = (i & 7) * 8;
+        const uint4 v = c < kFeat ? *reinterpret_cast<const uint4*>(m.wt1 + r * kFeat + c) : z4;
+        *reinterpret_cast<uint4*>(W1 + tc::sw128_offset(r, c, 128)) = v;
+        *reinterpret_cast<uint4*>(X + tc::sw128_offset(r, c, 128)) = z4;
+        *reinterpret_cast<uint4*>(DY + tc::sw128_offset(r, c, 128)) = z4;
     }
-    for (int i = tid; i < 128 * 128; i += kTcThreads) {
-        const int r = i >> 7, c = i & 127;
-        *reinterpret_cast<__nv_bfloat16*>(W2 + tc::sw128_offset(r, c, 128)) = m.wt2[r * kHid + c];
+#pragma unroll 8
+    for (int i = tid; i < 128 * 16; i += kTcThreads) {
+        const int r = i >> 4, c = (i & 15) * 8;
+        *reinterpret_cast<uint4*>(W2 + tc::sw128_offset(r, c, 128)) = *reinterpret_cast<const uint4*>(m.wt2 + r * kHid + c);
     }
-    for (int i = tid; i < 16 * 128; i += kTcThreads) {
-        const int r = i >> 7, c = i & 127;
-        *reinterpret_cast<__nv_bfloat16*>(W3 + tc::sw128_offset(r, c, 16)) = r < kOutPad ? m.wt3[r * kHid + c] : zero;
-        *reinterpret_cast<__nv_bfloat16*>(ONES + tc::sw128_offset(r, c, 16)) = one;
+    for (int i = tid; i < 16 * 16; i += kTcThreads) {
+        const int r = i >> 4, c = (i & 15) * 8;
+        *reinterpret_cast<uint4*>(W3 + tc::sw128_offset(r, c, 16)) =
+            r < kOutPad ? *reinterpret_cast<const uint4*>(m.wt3 + r * kHid + c) : z4;
+        *reinterpret_cast<uint4*>(ONES + tc::sw128_offset(r, c, 16)) = ones4;
     }
+    for (int i = tid; i < 2 * kHid; i += kTcThreads) s_bias[i] = b1[i];             // b1 then b2
+    for (int i = tid; i < 2 * kFeat; i += kTcThreads) s_fnorm[i] = i < kFeat ? m.fmean[i] : m.fstd[i - kFeat];
     if (tid == 0) {
         tc::mbar_init(&bar);
         s_loss = 0.0f;
@@ -216,7 +227,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_train(MlpDev m, float* gp
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
                 const int f = half * 16 + j;
-                v[j] = valid ? (fcur[j] - m.fmean[f]) / m.fstd[f] : 0.0f;
+                v[j] = valid ? (fcur[j] - s_fnorm[f]) / s_fnorm[kFeat + f] : 0.0f;
             }
             put16(X, row, half * 16, v);
         }
@@ -232,7 +243,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_train(MlpDev m, float* gp
             float z[16], h[16];
             tc::ld16(T + lane_off + kTZ + c0, z);
 #pragma unroll
-            for (int j = 0; j < 16; ++j) gelu_both(z[j] + b1[c0 + j], h[j], z[j]);   // z becomes gelu'
+            for (int j = 0; j < 16; ++j) gelu_both(z[j] + s_bias[c0 + j], h[j], z[j]);   // z becomes gelu'
             put16(H1, row, c0, h);
             put16_rows(P1, row, c0, z);
         }
@@ -246,7 +257,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_train(MlpDev m, float* gp
             float z[16], h[16];
             tc::ld16(T + lane_off + kTZ + c0, z);
 #pragma unroll
-            for (int j = 0; j < 16; ++j) gelu_both(z[j] + b2[c0 + j], h[j], z[j]);   // z becomes gelu'
+            for (int j = 0; j < 16; ++j) gelu_both(z[j] + s_bias[kHid + c0 + j], h[j], z[j]);   // z becomes gelu'
             put16(H2, row, c0, h);
             put16_rows(P2, row, c0, z);
         }

@@ -3553,6 +3553,103 @@ __device__ __noinline__ void solve_velocity_learned(const VRow& r, SB sb, float4
     *imp = make_float4(ch.p[0].normalImpulse, ch.p[0].tangentImpulse, ch.p[1].normalImpulse, ch.p[1].tangentImpulse);
 }
 
+// The warm-start modes' part of a contact row (modes 1..3, b2contactsolver.d:244-450 itself
+// unchanged): the points whose impulse started from zero (no feature-id match in Collide) are
+// marked in the row; mode 1 logs the contact's features as a training sample (its targets
+// follow at StoreImpulses), mode 2 stores them for a prediction, mode 3 sets those points to
+// the given start.  Returns whether the row waits for a prediction.
+DG bool row_start_modes(const Ctx& x, int item, int slog_at, const VC& vc, const PC& pc, const float* sep, SB sb,
+                        float h, VRow& vr) {
+    unsigned fr = x.ct[item].flags & (kContactNew0 | kContactNew1);
+    if (pc.pointCount < 2) fr &= ~(unsigned)kContactNew1;
+    if (x.ws_mode == 1) x.s_slog[slog_at] = -1;
+    if (!fr) return false;
+    vr.ids.z |= (fr & kContactNew0 ? 0x200 : 0) | (fr & kContactNew1 ? 0x400 : 0);
+    float* f = x.ws_mode == 1 ? nullptr : x.s_feat + (size_t)kFeat * item;
+    if (x.ws_mode == 1) {
+        unsigned slot = atomicAdd(x.sample_count, 1u);
+        if ((int)slot < x.sample_cap) {
+            f = x.samples + (size_t)kSampleFloats * slot;
+            x.s_slog[slog_at] = (int)slot;
+        }
+    }
+    if (f) {
+        float fv[kFeat];
+        contact_features(vc, sep, pc.pointCount, sb, x.gravity, h, fv);
+#pragma unroll
+        for (int q = 0; q < kFeat; ++q) f[q] = fv[q];
+    }
+    if (x.ws_mode == 3 && x.start_ct) {
+        // given start: the impulses another handle's step from the same state ended with at
+        // this contact slot (clamped as a prediction is), from the point with the same feature
+        // id (the source's SolveTOI may have re-evaluated the manifold after its solve)
+        const dbox_contact_state& g = x.start_ct[item];
+        for (int j = 0; j < pc.pointCount; ++j) {
+            if (!(fr & (j == 0 ? kContactNew0 : kContactNew1))) continue;
+            const uint32_t id = x.ct[item].points[j].id;
+            float ln = 0.0f, lt = 0.0f;
+            for (int q = 0; q < g.point_count && q < 2; ++q)
+                if (g.points[q].id == id) { ln = g.points[q].normal_impulse; lt = g.points[q].tangent_impulse; }
+            ln = ln > 0.0f ? ln : 0.0f;
+            const float mf = vr.K.w * ln;
+            lt = lt < -mf ? -mf : (lt > mf ? mf : lt);
+            if (j == 0) { vr.imp.x = ln; vr.imp.y = lt; }
+            else { vr.imp.z = ln; vr.imp.w = lt; }
+        }
+    }
+    return x.ws_mode == 2;
+}
+
+// Predicted start impulses for pending rows pend[p0 .. p0 + 16) (of npend), one warp, one
+// tensor-core pass: features normalised into X (16 x kFeat bf16), the network's hidden layers
+// in H1 / H2 (16 x kHid bf16 each), the new points' impulses clamped as the solver could reach
+// them (normal >= 0, |tangent| <= friction * normal) and the rows marked predicted (0x100)
+DG void infer_pending16(const Ctx& x, const int* pend, int p0, int npend, VRow* vrow, __nv_bfloat16* X,
+                        __nv_bfloat16* H1, __nv_bfloat16* H2) {
+    const int lane = lane_id();
+    for (int e = lane; e < 16 * kFeat; e += kWarp) {
+        int r = e / kFeat, q = e % kFeat;
+        float v = 0.0f;
+        if (p0 + r < npend) {
+            int item = vrow[pend[p0 + r]].ids.w;
+            v = (x.s_feat[(size_t)kFeat * item + q] - x.mlp.fmean[q]) / x.mlp.fstd[q];
+        }
+        X[e] = __float2bfloat16_rn(v);
+    }
+    __syncwarp();
+    float y[4];
+    mlp_infer16(x.mlp, X, H1, H2, y, lane);
+    __syncwarp();
+    const int g = lane >> 2, t = lane & 3;
+    if (t < 2) {
+#pragma unroll
+        for (int hrow = 0; hrow < 2; ++hrow) {
+            const int r = g + 8 * hrow;
+            if (p0 + r >= npend) continue;
+            const int idx = pend[p0 + r];
+            VRow* vr = vrow + idx;
+            const int ids = vr->ids.z;
+            const int j = t;                              // lane t predicts point t
+            if (!(ids & (0x200 << j)) || j >= (ids & 0xff)) continue;
+            const int c = 2 * t;
+            float ln = y[2 * hrow] * x.mlp.tstd[c] + x.mlp.tmean[c];
+            float lt = y[2 * hrow + 1] * x.mlp.tstd[c + 1] + x.mlp.tmean[c + 1];
+            ln = ln > 0.0f ? ln : 0.0f;                   // a start the solver itself could reach
+            float mf = vr->K.w * ln;
+            lt = lt < -mf ? -mf : (lt > mf ? mf : lt);
+            if (j == 0) { vr->imp.x = ln; vr->imp.y = lt; }
+            else { vr->imp.z = ln; vr->imp.w = lt; }
+        }
+    }
+    if (t == 0) {
+        for (int hrow = 0; hrow < 2; ++hrow) {
+            const int r = g + 8 * hrow;
+            if (p0 + r < npend) atomicOr(&vrow[pend[p0 + r]].ids.z, 0x100);
+        }
+    }
+    __syncwarp();
+}
+
 // deepest separation over the points of a contact at the current positions
 // (b2PositionSolverManifold, b2contactsolver.d:816-851); 0 when none is below 0
 DG float position_min_separation(const PC& pc, SB sb) {
@@ -4024,49 +4121,7 @@ DG void solve_world(const Ctx& x, int w, float* sbp, bool sb_smem, float* stage_
                 float sep[2] = {0.0f, 0.0f};
                 constraint_init_velocity(vc, pc, sb, sep);
                 VRow vr = pack_v(vc, item);
-                if (x.ws_mode) {
-                    // points whose impulse started from zero (no feature-id match in Collide)
-                    unsigned fr = x.ct[item].flags & (kContactNew0 | kContactNew1);
-                    if (pc.pointCount < 2) fr &= ~(unsigned)kContactNew1;
-                    if (x.ws_mode == 1) x.s_slog[kx + idx] = -1;
-                    if (fr) {
-                        vr.ids.z |= (fr & kContactNew0 ? 0x200 : 0) | (fr & kContactNew1 ? 0x400 : 0);
-                        float* f = x.ws_mode == 1 ? nullptr : x.s_feat + (size_t)kFeat * item;
-                        if (x.ws_mode == 1) {
-                            unsigned slot = atomicAdd(x.sample_count, 1u);
-                            if ((int)slot < x.sample_cap) {
-                                f = x.samples + (size_t)kSampleFloats * slot;
-                                x.s_slog[kx + idx] = (int)slot;
-                            }
-                        }
-                        if (f) {
-                            float fv[kFeat];
-                            contact_features(vc, sep, pc.pointCount, sb, x.gravity, h, fv);
-#pragma unroll
-                            for (int q = 0; q < kFeat; ++q) f[q] = fv[q];
-                        }
-                        pend = x.ws_mode == 2;
-                        if (x.ws_mode == 3 && x.start_ct) {
-                            // given start: the impulses another handle's step from the same state
-                            // ended with at this contact slot (clamped as a prediction is)
-                            // (the point with the same feature id: the source's SolveTOI may have
-                            // re-evaluated the manifold after its solve)
-                            const dbox_contact_state& g = x.start_ct[item];
-                            for (int j = 0; j < pc.pointCount; ++j) {
-                                if (!(fr & (j == 0 ? kContactNew0 : kContactNew1))) continue;
-                                const uint32_t id = x.ct[item].points[j].id;
-                                float ln = 0.0f, lt = 0.0f;
-                                for (int q = 0; q < g.point_count && q < 2; ++q)
-                                    if (g.points[q].id == id) { ln = g.points[q].normal_impulse; lt = g.points[q].tangent_impulse; }
-                                ln = ln > 0.0f ? ln : 0.0f;
-                                const float mf = vr.K.w * ln;
-                                lt = lt < -mf ? -mf : (lt > mf ? mf : lt);
-                                if (j == 0) { vr.imp.x = ln; vr.imp.y = lt; }
-                                else { vr.imp.z = ln; vr.imp.w = lt; }
-                            }
-                        }
-                    }
-                }
+                if (x.ws_mode) pend = row_start_modes(x, item, kx + idx, vc, pc, sep, sb, h, vr);
                 vrow[idx] = vr;
                 if (njI || x.record_events) x.s_vpos[item] = idx;
                 if (!njI) {
@@ -4102,49 +4157,7 @@ DG void solve_world(const Ctx& x, int w, float* sbp, bool sb_smem, float* stage_
     // in this warp's staging area (free until the sweeps)
     for (int p0 = 0; p0 < npend; p0 += 16) {
         __nv_bfloat16* X = reinterpret_cast<__nv_bfloat16*>(stage_f);
-        __nv_bfloat16* H1 = X + 16 * kFeat;
-        __nv_bfloat16* H2 = H1 + 16 * kHid;
-        for (int e = lane; e < 16 * kFeat; e += kWarp) {
-            int r = e / kFeat, q = e % kFeat;
-            float v = 0.0f;
-            if (p0 + r < npend) {
-                int item = vrow[x.s_pend[c0 + p0 + r]].ids.w;
-                v = (x.s_feat[(size_t)kFeat * item + q] - x.mlp.fmean[q]) / x.mlp.fstd[q];
-            }
-            X[e] = __float2bfloat16_rn(v);
-        }
-        tsync();
-        float y[4];
-        mlp_infer16(x.mlp, X, H1, H2, y, lane);
-        tsync();
-        const int g = lane >> 2, t = lane & 3;
-        if (t < 2) {
-#pragma unroll
-            for (int hrow = 0; hrow < 2; ++hrow) {
-                const int r = g + 8 * hrow;
-                if (p0 + r >= npend) continue;
-                const int idx = x.s_pend[c0 + p0 + r];
-                VRow* vr = vrow + idx;
-                const int ids = vr->ids.z;
-                const int j = t;                              // lane t predicts point t
-                if (!(ids & (0x200 << j)) || j >= (ids & 0xff)) continue;
-                const int c = 2 * t;
-                float ln = y[2 * hrow] * x.mlp.tstd[c] + x.mlp.tmean[c];
-                float lt = y[2 * hrow + 1] * x.mlp.tstd[c + 1] + x.mlp.tmean[c + 1];
-                ln = ln > 0.0f ? ln : 0.0f;                   // a start the solver itself could reach
-                float mf = vr->K.w * ln;
-                lt = lt < -mf ? -mf : (lt > mf ? mf : lt);
-                if (j == 0) { vr->imp.x = ln; vr->imp.y = lt; }
-                else { vr->imp.z = ln; vr->imp.w = lt; }
-            }
-        }
-        if (t == 0) {
-            for (int hrow = 0; hrow < 2; ++hrow) {
-                const int r = g + 8 * hrow;
-                if (p0 + r < npend) atomicOr(&vrow[x.s_pend[c0 + p0 + r]].ids.z, 0x100);
-            }
-        }
-        tsync();
+        infer_pending16(x, x.s_pend + c0, p0, npend, vrow, X, X + 16 * kFeat, X + 16 * kFeat + 16 * kHid);
     }
     tsync();
     stamp(x, w, 4);
@@ -5030,8 +5043,11 @@ __global__ void __launch_bounds__(kPairThreads) k_finish_big_block(const __grid_
 //     dynamic body), then the block buckets all constraints by level.
 //   rows, sweeps (levels in order, a level's constraints over the block, a block barrier
 //     between levels), integration, copy back and sleep over the block.
-// The learned-start modes keep the warp path.
+// Every warm-start mode runs here too: the predictions of mode 2 on kInferWarps warps, 16 rows a pass.
 constexpr int kBigThreads = 1024;
+constexpr int kInferWarps = 8;
+constexpr int kInferStage = 16 * kFeat + 2 * 16 * kHid;               // bf16 per warp: X, H1, H2
+constexpr int kBigSmemInfer = kInferWarps * kInferStage * 2;          // bytes
 
 DG int ld_volatile_int(const int* p) { return *reinterpret_cast<const volatile int*>(p); }
 DG int uf_find(int* parent, int i) {
@@ -5055,6 +5071,7 @@ DG void uf_union(int* parent, int a, int b) {
 }
 
 __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant__ Ctx x) {
+    extern __shared__ __align__(16) float big_smem[];                  // ws mode 2: the inference staging
     __shared__ int shi[32];
     __shared__ float shf[32];
     __shared__ int s_next, s_maxv, s_maxp;
@@ -5366,9 +5383,12 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
         }
     }
     __syncthreads();
-    // constraint rows in schedule order (b2contactsolver.d:244-450)
+    // constraint rows in schedule order (b2contactsolver.d:244-450), with the warm-start modes'
+    // part of each contact row; rows waiting for a prediction listed in s_pend
     VRow* vrow = x.vr + kx;
     PRow* prow = x.pr + kx;
+    if (tid == 0) s_next = 0;
+    __syncthreads();
     for (int idx = tid; idx < nItems; idx += nt) {
         const int item = x.s_sched_v[kx + idx];
         bool pdone = false;
@@ -5378,7 +5398,10 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
             constraint_ctor(x, item, b0, warm, dtRatio, vc, pc);
             float sep[2] = {0.0f, 0.0f};
             constraint_init_velocity(vc, pc, sb, sep);
-            vrow[idx] = pack_v(vc, item);
+            VRow vr = pack_v(vc, item);
+            if (x.ws_mode && row_start_modes(x, item, kx + idx, vc, pc, sep, sb, h, vr))
+                x.s_pend[c0 + atomicAdd(&s_next, 1)] = idx;
+            vrow[idx] = vr;
             if (njI || x.record_events) x.s_vpos[item] = idx;
             if (!njI) {
                 prow[idx] = pack_p(pc, body_island[(bfl[vc.bodyA] & kBfStatic) ? vc.bodyB : vc.bodyA]);
@@ -5386,6 +5409,7 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
             }
         } else {
             vrow[idx].ids = make_int4(0, 0, 0, item);
+            if (x.ws_mode == 1) x.s_slog[kx + idx] = -1;
         }
         if (!pdone) {
             const int pitem = sched_p[kx + idx];
@@ -5401,6 +5425,17 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
         }
     }
     __syncthreads();
+    if (x.ws_mode == 2) {
+        // predicted starts, 16 pending rows per tensor-core pass, kInferWarps warps
+        const int npend = s_next;
+        const int warp = tid >> 5;
+        if (warp < kInferWarps) {
+            __nv_bfloat16* X = reinterpret_cast<__nv_bfloat16*>(big_smem) + (size_t)warp * kInferStage;
+            for (int p0 = 16 * warp; p0 < npend; p0 += 16 * kInferWarps)
+                infer_pending16(x, x.s_pend + c0, p0, npend, vrow, X, X + 16 * kFeat, X + 16 * kFeat + 16 * kHid);
+        }
+        __syncthreads();
+    }
     stampb(4);
     auto sweep = [&](const int* lvl, int maxL, auto&& f) {             // levels in order over the block
         for (int L = 1; L <= maxL; ++L) {
@@ -5425,6 +5460,12 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
         sweep(x.s_lvl_v + kx, maxLv, [&](int idx) {
             const VRow r = load_v(vrow + idx);
             if (r.ids.w >= 0) {
+                if (it == 0 && (r.ids.z & 0x100)) {                      // a predicted start (ws mode 2)
+                    float4 im;
+                    solve_velocity_learned(r, sb, &im);
+                    vrow[idx].imp = im;
+                    return;
+                }
                 VC vc = unpack_v(r);
                 BodyVel q = load_vel(sb, vc.bodyA, vc.bodyB);
                 if (vc.pointCount == 2) solve_velocity_two(vc, q);
@@ -5484,6 +5525,13 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
     for (int idx = tid; idx < nItems; idx += nt) {                       // StoreImpulses (b2contactsolver.d:774-787)
         const VRow r = load_v(vrow + idx);
         if (r.ids.w >= 0) store_impulses(x, r);
+        if (x.ws_mode == 1) {                                            // a logged sample's targets
+            const int slot = x.s_slog[kx + idx];
+            if (slot >= 0) {
+                float* tg = x.samples + (size_t)kSampleFloats * slot + kFeat;
+                tg[0] = r.imp.x; tg[1] = r.imp.y; tg[2] = r.imp.z; tg[3] = r.imp.w;
+            }
+        }
     }
     // integrate positions (b2island.d:168-200)
     for (int t = tid; t < nbI; t += nt) {
@@ -5749,7 +5797,8 @@ extern "C" int dbox_launch_collide(const dg::Ctx* x, cudaStream_t stream) {
 extern "C" int dbox_launch_solve(const dg::Ctx* x, cudaStream_t stream, int* launches) {
     if (x->solve_blocks < 1) return (int)cudaErrorInvalidValue;
     if (x->solve_queue) cudaMemsetAsync(x->solve_queue, 0, sizeof(int) * (2 + 4 * (size_t)x->solve_nsm), stream);
-    if (x->big_block) dg::k_solve_big<<<x->n_big, dg::kBigThreads, 0, stream>>>(*x);   // large worlds' Solve
+    if (x->big_block)                               // large worlds' Solve
+        dg::k_solve_big<<<x->n_big, dg::kBigThreads, x->ws_mode == 2 ? dg::kBigSmemInfer : 0, stream>>>(*x);
     dg::k_solve_toi<<<x->solve_blocks, x->solve_wpb * dg::kWarp, x->solve_smem_floats * sizeof(float), stream>>>(*x);
     if (x->n_big > 0) {                             // large worlds: their pairs on a block each, then AddPair + TOI
         dg::k_pairs_block<<<x->n_big, dg::kPairThreads, 0, stream>>>(*x);
@@ -5773,7 +5822,8 @@ extern "C" int dbox_launch_step_ev(const dg::Ctx* x, cudaStream_t stream, int* l
     if (x->n_big > 0) dg::k_collide_finish_big<<<x->n_big, dg::kPairThreads, 0, stream>>>(*x);
     if (ev) cudaEventRecordWithFlags(ev[1], stream, cudaEventRecordExternal);
     if (x->solve_queue) cudaMemsetAsync(x->solve_queue, 0, sizeof(int) * (2 + 4 * (size_t)x->solve_nsm), stream);
-    if (x->big_block) dg::k_solve_big<<<x->n_big, dg::kBigThreads, 0, stream>>>(*x);   // large worlds' Solve
+    if (x->big_block)                               // large worlds' Solve
+        dg::k_solve_big<<<x->n_big, dg::kBigThreads, x->ws_mode == 2 ? dg::kBigSmemInfer : 0, stream>>>(*x);
     dg::k_solve_toi<<<x->solve_blocks, x->solve_wpb * dg::kWarp, x->solve_smem_floats * sizeof(float), stream>>>(*x);
     if (x->n_big > 0) {                             // large worlds: their pairs on a block each, then AddPair + TOI
         dg::k_pairs_block<<<x->n_big, dg::kPairThreads, 0, stream>>>(*x);
@@ -5786,6 +5836,9 @@ extern "C" int dbox_launch_step_ev(const dg::Ctx* x, cudaStream_t stream, int* l
 }
 
 extern "C" const void* dbox_solve_kernel() { return reinterpret_cast<const void*>(&dg::k_solve_toi); }
+extern "C" int dbox_big_solve_init() {
+    return (int)cudaFuncSetAttribute(dg::k_solve_big, cudaFuncAttributeMaxDynamicSharedMemorySize, dg::kBigSmemInfer);
+}
 
 extern "C" int dbox_launch_step(const dg::Ctx* x, cudaStream_t stream, int* launches) {
     return dbox_launch_step_ev(x, stream, launches, nullptr);

@@ -681,8 +681,8 @@ int32_t dbox_world_set_wait_limit(dbox_world* w, int32_t polls);
 /* How b2World.Solve runs for the large worlds of the handle (4,096 fixtures or more): mode 0
  * (default) on a block of 1,024 threads each (islands found by a union-find, each island's
  * search on a thread of its own, constraint levels swept by the whole block), mode 1 on one warp
- * each like every other world.  Both give the same results bit for bit; the learned-start modes
- * (dbox_world_set_warmstart 1..3) always take the warp.  Replaces no reference call: the
+ * each like every other world.  Both give the same results bit for bit, in every warm-start mode
+ * (dbox_world_set_warmstart 0..3).  Replaces no reference call: the
  * reference solves islands one after another on the calling thread (dynamics/b2world.d:930-1124). */
 int32_t dbox_world_set_island_solver(dbox_world* w, int32_t mode);
 /* The mode in use (set by the call above or chosen by dbox_world_autotune). */

@@ -137,3 +137,53 @@ def test_given_start_slots_line_up(gpu_lib):
     given.step(vel_iters=4)
     plain.step(vel_iters=4)
     assert any(exact_diff(plain.export_state(i), given.export_state(i)) for i in range(len(worlds)))
+
+
+def _large_world():
+    rng = np.random.default_rng(27)
+    big = scenes._concat([scenes.container(90.0, 90.0), scenes.scatter(4500, 88.0, 88.0, rng)])
+    assert len(big["fixtures"]) >= 4096
+    return big
+
+
+def test_warm_start_modes_on_a_large_world(gpu_lib):
+    # a world of 4,096+ fixtures runs its Solve on a block: every warm-start mode gives there the
+    # same bits as on a warp (mode 2 with an untrained network, whose predictions are far from
+    # zero; mode 1's logged samples as a set, their slots being taken in any order; mode 3 from
+    # a source handle's step)
+    from compare import exact_diff
+    big = _large_world()
+    m = gpu_lib.Mlp(seed=5)
+    hs = {}
+    for solver in (0, 1):
+        w = gpu_lib.World(big)
+        w.set_island_solver(solver)
+        w.step(steps=40, graph=True)
+        w.set_warmstart(2, m)
+        w.step(steps=20)
+        hs[solver] = w
+    d = exact_diff(hs[0].export_state(), hs[1].export_state())
+    assert not d, d[:6]
+    samples = {}
+    for solver in (0, 1):
+        w = hs[solver]
+        w.set_warmstart(1, None, 200000)
+        w.step(steps=5)
+        n = w.sample_count()
+        f, t = w.samples(0, n)
+        rows = np.concatenate([f, t], 1)
+        samples[solver] = rows[np.lexsort(rows.T[::-1])]
+    assert len(samples[0]) > 100 and samples[0].tobytes() == samples[1].tobytes()
+    src = gpu_lib.World(big)
+    src.step()
+    for solver in (0, 1):
+        w = hs[solver]
+        w.set_warmstart(3)
+        w.set_start_source(src)
+    for _ in range(3):
+        src.copy_state_from(hs[0])
+        src.step(vel_iters=8)
+        hs[0].step(vel_iters=4)
+        hs[1].step(vel_iters=4)
+    d = exact_diff(hs[0].export_state(), hs[1].export_state())
+    assert not d, d[:6]
