@@ -211,11 +211,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_train(MlpDev m, float* gp
         const int r0 = tile * 128;
         const bool valid = tile < ntiles && r0 + row < n;
         const int sid = !valid ? 0 : (idx ? idx[r0 + row] : (int)perm_apply(perm, (uint32_t)(offset + r0 + row)));
-        const float* sample = rows + (size_t)sid * kSampleFloats;
+        // a sample row is 144 bytes, so its four-float groups are 16-byte aligned
+        const float4* sample = reinterpret_cast<const float4*>(rows + (size_t)sid * kSampleFloats);
+        const float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 #pragma unroll
-        for (int j = 0; j < 16; ++j) fv[j] = valid ? sample[half * 16 + j] : 0.0f;
-#pragma unroll
-        for (int o = 0; o < kOut; ++o) tv[o] = valid && half == 0 ? sample[kFeat + o] : 0.0f;
+        for (int q = 0; q < 4; ++q) {
+            const float4 v = valid ? sample[half * 4 + q] : z;
+            fv[4 * q] = v.x; fv[4 * q + 1] = v.y; fv[4 * q + 2] = v.z; fv[4 * q + 3] = v.w;
+        }
+        const float4 t4 = valid && half == 0 ? sample[kFeat / 4] : z;
+        tv[0] = t4.x; tv[1] = t4.y; tv[2] = t4.z; tv[3] = t4.w;
     };
     float fcur[16], tcur[kOut];
     fetch(blockIdx.x, fcur, tcur);
@@ -761,6 +766,8 @@ int32_t dbox_mlp_train_device(dbox_mlp* m, int32_t n, const float* rows, int32_t
                               uint64_t seed, float* epoch_loss) {
     if (!m || n <= 0 || !rows || epochs <= 0 || batch <= 0)
         return dbox_set_error(DBOX_ERR_INVALID, "dbox_mlp_train_device: bad arguments");
+    if (reinterpret_cast<uintptr_t>(rows) & 15u)
+        return dbox_set_error(DBOX_ERR_INVALID, "dbox_mlp_train_device: rows must be 16-byte aligned");
     int r = DBOX_OK;
     dg::MlpDev d = mlp_dev(m);
     for (int e = 0; e < epochs && !r; ++e) {

@@ -612,6 +612,7 @@ int32_t dbox_mlp_gradient(dbox_mlp* m, int32_t n, const float* feats, const floa
 /* Adam (beta 0.9 / 0.999, eps 1e-8) over shuffled batches; epoch_loss[epochs] (may be NULL) */
 int32_t dbox_mlp_train(dbox_mlp* m, int32_t n, const float* feats, const float* targets, int32_t epochs,
                        int32_t batch, float lr, uint64_t seed, float* epoch_loss);
+/* The same on n device rows of 36 floats (32 features, 4 targets); device_rows 16-byte aligned. */
 int32_t dbox_mlp_train_device(dbox_mlp* m, int32_t n, const float* device_rows, int32_t epochs, int32_t batch,
                               float lr, uint64_t seed, float* epoch_loss);
 int32_t dbox_mlp_train_world(dbox_mlp* m, dbox_world* w, int32_t epochs, int32_t batch, float lr, uint64_t seed,
