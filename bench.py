@@ -1,6 +1,6 @@
 """Benchmark: body-steps/s of b2World.Step on one GB300 (plain solver, batched worlds).
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload batch|scatter|pyramid|stress]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload batch|scatter|pyramid|stress|train]
 
 Workload (default "batch"): 4,096 independent worlds in one handle, body counts
 log-uniform in [8, 512], one third each pyramid / scatter in a 40 m container /
@@ -50,7 +50,10 @@ def parse():
     p.add_argument("--steps", type=int, default=60)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--workload", default="batch", choices=["batch", "scatter", "pyramid", "stress"])
+    p.add_argument("--workload", default="batch", choices=["batch", "scatter", "pyramid", "stress", "train"],
+                   help="train: the learned warm-start MLP's Adam training alone, on synthetic device rows")
+    p.add_argument("--train-rows", type=int, default=1 << 20)
+    p.add_argument("--train-epochs", type=int, default=3)
     p.add_argument("--worlds", type=int, default=4096)
     p.add_argument("--seed", type=int, default=3)
     p.add_argument("--no-cpu", action="store_true")
@@ -628,10 +631,47 @@ def mapping_report(mapping, how):
             "chosen_by": by}
 
 
+def train_only(args):
+    """The MLP trainer alone: --train-rows normal random rows (32 features, 4 targets) resident
+    in device memory, one untimed epoch, then --train-epochs epochs of Adam in batches of
+    65,536 (dbox_mlp_train_device), timed on the host around the synchronous call."""
+    import torch
+    import dbox_gb300
+    rng = np.random.default_rng(args.seed)
+    n = args.train_rows
+    f = rng.normal(size=(n, 32)).astype(np.float32)
+    t = rng.normal(size=(n, 4)).astype(np.float32)
+    m = dbox_gb300.Mlp(seed=args.seed)
+    m.fit_normalization(f, t)
+    rows = torch.from_numpy(np.concatenate([f, t], 1)).cuda()
+    m.train_device(rows.data_ptr(), n, epochs=1, batch=65536, lr=1e-3, seed=args.seed)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    loss = m.train_device(rows.data_ptr(), n, epochs=args.train_epochs, batch=65536, lr=1e-3, seed=args.seed)
+    dt = time.perf_counter() - t0
+    flop = 3.0 * 41984.0 * n * args.train_epochs
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    bf = json.load(open(pk)).get("bf16_tflops") if os.path.exists(pk) else None
+    out = {"metric": "MLP training TFLOP/s (learned warm-start network, Adam, batch 65,536)",
+           "value": flop / dt / 1e12, "unit": "TFLOP/s", "n_gpus": 1, "higher_is_better": True, "dtype": "bf16",
+           "data": "synthetic normal rows (seed %d), device resident" % args.seed,
+           "config": {"workload": "MLP 32-128-128-4 training", "rows": n, "epochs": args.train_epochs},
+           "seconds": dt, "loss": [float(v) for v in loss],
+           "peak": bf or 1900.0, "peak_source": "measured (MEASURED_PEAKS.json bf16_tflops)" if bf else "fallback 1900"}
+    out["frac"] = out["value"] / out["peak"]
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     world_size = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
+    if args.workload == "train":
+        if rank == 0 and args.impl == "ours":
+            train_only(args)
+        elif rank == 0:
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no trainer for this network"}))
+        return
     if args.impl == "reference":
         if rank != 0:
             return

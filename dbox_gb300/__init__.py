@@ -104,6 +104,7 @@ def lib():
     L.dbox_mlp_fit_normalization.argtypes = [vp, i32, vp, vp]
     L.dbox_mlp_gradient.argtypes = [vp, i32, vp, vp, vp, vp]
     L.dbox_mlp_train.argtypes = [vp, i32, vp, vp, i32, i32, f32, u64, vp]
+    L.dbox_mlp_train_device.argtypes = [vp, i32, vp, i32, i32, f32, u64, vp]
     L.dbox_mlp_train_world.argtypes = [vp, vp, i32, i32, f32, u64, vp]
     L.dbox_mlp_forward.argtypes = [vp, i32, vp, vp]
     L.dbox_world_set_warmstart.argtypes = [vp, i32, vp, i32]
@@ -224,6 +225,13 @@ class Mlp:
         losses = np.zeros(epochs, np.float32)
         _check(lib().dbox_mlp_train(self.h, len(f), abi.ptr(f), abi.ptr(t), epochs, batch, ctypes.c_float(lr),
                                     ctypes.c_uint64(seed), abi.ptr(losses)), "dbox_mlp_train")
+        return losses
+
+    def train_device(self, rows_ptr, n, epochs=1, batch=65536, lr=1e-3, seed=0):
+        """Adam on n device rows of 36 floats (features, targets) at a 16-byte aligned device address."""
+        losses = np.zeros(epochs, np.float32)
+        _check(lib().dbox_mlp_train_device(self.h, n, ctypes.c_void_p(rows_ptr), epochs, batch, ctypes.c_float(lr),
+                                           ctypes.c_uint64(seed), abi.ptr(losses)), "dbox_mlp_train_device")
         return losses
 
     def train_world(self, world, epochs=1, batch=65536, lr=1e-3, seed=0):
