@@ -206,15 +206,18 @@ def cpu_leg(args, worlds=None):
     # per-world cost from an untimed calibration pass over all worlds (the cost per body differs
     # between pyramids, stacks and scatter worlds), then a largest-first assignment
     nb = min(cores, len(worlds))
-    chunks = [list(range(i, len(worlds), 4 * nb)) for i in range(4 * nb)]
-    chunks = [c for c in chunks if c]
-    with ctx.Pool(nb) as pool:
-        timed = pool.map(_cpu_cost_worker, [([worlds[i] for i in c], args.warmup, args.steps) for c in chunks])
-    costs = [0.0] * len(worlds)
-    for c, t in zip(chunks, timed):
-        for i, v in zip(c, t):
-            costs[i] = v
-    shares = lpt_shares(costs, nb)
+    if len(worlds) == 1:
+        shares = [[0]]                            # one world: one core, nothing to balance
+    else:
+        chunks = [list(range(i, len(worlds), 4 * nb)) for i in range(4 * nb)]
+        chunks = [c for c in chunks if c]
+        with ctx.Pool(nb) as pool:
+            timed = pool.map(_cpu_cost_worker, [([worlds[i] for i in c], args.warmup, args.steps) for c in chunks])
+        costs = [0.0] * len(worlds)
+        for c, t in zip(chunks, timed):
+            for i, v in zip(c, t):
+                costs[i] = v
+        shares = lpt_shares(costs, nb)
     barrier = ctx.Barrier(len(shares))
     out = ctx.Queue()
     procs = [ctx.Process(target=_cpu_worker, args=([worlds[i] for i in sh], args.warmup, args.steps, barrier, out))
@@ -229,11 +232,15 @@ def cpu_leg(args, worlds=None):
     wall = max(r[1] for r in res) - min(r[0] for r in res)
     work = sum(r[2] for r in res)
     busy = [r[1] - r[0] for r in res]
-    sample = ("%d of %d worlds, steps %d..%d, %d processes (worlds spread costliest first over the cores, "
-              "costs from an untimed calibration pass), "
-              "wall clock of the pool; per-process busy %.2f-%.2f s; oracle with host libm trig"
-              % (len(worlds), len(worlds), args.warmup + 1, args.warmup + args.steps, len(shares), min(busy),
-                 max(busy)))
+    if len(worlds) == 1:
+        sample = ("the one world, steps %d..%d, one process (one core); wall clock %.2f s; oracle with host libm trig"
+                  % (args.warmup + 1, args.warmup + args.steps, wall))
+    else:
+        sample = ("%d of %d worlds, steps %d..%d, %d processes (worlds spread costliest first over the cores, "
+                  "costs from an untimed calibration pass), "
+                  "wall clock of the pool; per-process busy %.2f-%.2f s; oracle with host libm trig"
+                  % (len(worlds), len(worlds), args.warmup + 1, args.warmup + args.steps, len(shares), min(busy),
+                     max(busy)))
     return work / wall, len(shares), sample
 
 

@@ -3368,48 +3368,65 @@ DG int build_schedule(const Ctx& x, const WorldInfo& wi, int nIsl, bool contacts
     for (int i = lane; i < wi.body_count; i += kWarp) last[i] = 0;
     tsync();
     int maxL = 0, n = 0;
-    if (lane == 0) {
-        // islands share no dynamic body, so the levels are the same whether each island's
-        // constraints are walked island by island or all contacts (in island order) are walked
-        // before all joints (or after, for the velocity order): no per-island loop is needed
-        {
-            const int ncT = x.s_isl_cstart[wi.bx_start + nIsl], njT = x.s_isl_jstart[wi.bx_start + nIsl];
-            for (int pass = 0; pass < 2; ++pass) {
-                bool doContacts = (pass == 0) == contacts_first;
-                int e = doContacts ? ncT : njT;
-                for (int t = 0; t < e; ++t) {
-                    int item, A, B, C = -1, D = -1;
-                    if (doContacts) {
-                        item = x.s_isl_contact[c0 + t];
-                        int2 pr = x.s_isl_pair[c0 + t];
-                        A = pr.x;
-                        B = pr.y;
-                    } else {
-                        item = -(x.s_isl_joint[wi.joint_start + t] + 1);
-                        item_bodies(x, item, b0, A, B);
-                        const DJoint& jj = x.jt[-item - 1];
-                        if (jj.type == kGearJoint) {                    // a gear also moves C and D
-                            C = jj.body_c - b0;
-                            D = jj.body_d - b0;
-                        }
+    // islands share no dynamic body, so the levels are the same whether each island's
+    // constraints are walked island by island or all contacts (in island order) are walked
+    // before all joints (or after, for the velocity order): no per-island loop is needed.
+    // 32 constraints at a time: each lane loads one constraint's bodies and their dynamic
+    // flags, then the warp walks the 32 in order with the bodies passed by shuffles (the
+    // walk's only carried state is `last`, read by every lane and written by lane 0)
+    const int ncT = x.s_isl_cstart[wi.bx_start + nIsl], njT = x.s_isl_jstart[wi.bx_start + nIsl];
+    for (int pass = 0; pass < 2; ++pass) {
+        const bool doContacts = (pass == 0) == contacts_first;
+        const int e = doContacts ? ncT : njT;
+        for (int base = 0; base < e; base += kWarp) {
+            const int t = base + lane;
+            int item = 0, A = 0, B = 0, C = 0, D = 0;
+            unsigned dm = 0;                           // dynamic A, B, C, D in bits 0..3
+            if (t < e) {
+                if (doContacts) {
+                    item = x.s_isl_contact[c0 + t];
+                    const int2 pr = x.s_isl_pair[c0 + t];
+                    A = pr.x;
+                    B = pr.y;
+                } else {
+                    item = -(x.s_isl_joint[wi.joint_start + t] + 1);
+                    item_bodies(x, item, b0, A, B);
+                    const DJoint& jj = x.jt[-item - 1];
+                    if (jj.type == kGearJoint) {                    // a gear also moves C and D
+                        C = jj.body_c - b0;
+                        D = jj.body_d - b0;
+                        dm |= ((vbf[C] & kBfDynamic) ? 4u : 0u) | ((vbf[D] & kBfDynamic) ? 8u : 0u);
                     }
-                    bool dA = (vbf[A] & kBfDynamic) != 0, dB = (vbf[B] & kBfDynamic) != 0;
-                    int la = dA ? last[A] : 0, lb = dB ? last[B] : 0;
-                    int l = (la > lb ? la : lb);
-                    const bool dC = C >= 0 && (vbf[C] & kBfDynamic) != 0, dD = D >= 0 && (vbf[D] & kBfDynamic) != 0;
-                    if (dC && last[C] > l) l = last[C];
-                    if (dD && last[D] > l) l = last[D];
-                    l += 1;
-                    if (dA) last[A] = l;
-                    if (dB) last[B] = l;
-                    if (dC) last[C] = l;
-                    if (dD) last[D] = l;
-                    if (l > maxL) maxL = l;
-                    x.s_level[kx + n] = l;
-                    x.s_tmp[kx + n] = item;
-                    ++n;
                 }
+                dm |= ((vbf[A] & kBfDynamic) ? 1u : 0u) | ((vbf[B] & kBfDynamic) ? 2u : 0u);
             }
+            const int cnt = e - base < kWarp ? e - base : kWarp;
+            int myl = 0;
+            for (int j = 0; j < cnt; ++j) {
+                const int a = __shfl_sync(0xffffffffu, A, j), bb = __shfl_sync(0xffffffffu, B, j);
+                const int c = __shfl_sync(0xffffffffu, C, j), d = __shfl_sync(0xffffffffu, D, j);
+                const unsigned m = __shfl_sync(0xffffffffu, dm, j);
+                int la = (m & 1u) ? last[a] : 0, lb = (m & 2u) ? last[bb] : 0;
+                int l = (la > lb ? la : lb);
+                if ((m & 4u) && last[c] > l) l = last[c];
+                if ((m & 8u) && last[d] > l) l = last[d];
+                l += 1;
+                __syncwarp();
+                if (lane == 0) {
+                    if (m & 1u) last[a] = l;
+                    if (m & 2u) last[bb] = l;
+                    if (m & 4u) last[c] = l;
+                    if (m & 8u) last[d] = l;
+                }
+                __syncwarp();
+                if (lane == j) myl = l;
+                if (l > maxL) maxL = l;
+            }
+            if (t < e) {
+                x.s_level[kx + n + lane] = myl;
+                x.s_tmp[kx + n + lane] = item;
+            }
+            n += cnt;
         }
     }
     maxL = __shfl_sync(0xffffffffu, maxL, 0);
@@ -3954,55 +3971,90 @@ DG void solve_world(const Ctx& x, int w, float* sbp, bool sb_smem, float* stage_
         int* isl_contact = x.s_isl_contact + c0;
         int2* isl_pair = x.s_isl_pair + c0;
         int* body_island = x.s_body_island + b0;
-        // depth-first island search (b2world.d:959-1095), seeds in list order (descending index)
+        // depth-first island search (b2world.d:959-1095), seeds in list order (descending index).
+        // The whole warp runs it: a popped body's edges are taken 32 at a time, each lane one
+        // edge; the contacts not yet in an island are appended in edge order, and the bodies
+        // they reach that are not yet marked are pushed in edge order (a body reached twice in
+        // the same 32 edges by its first edge only), which is what the reference's one-edge-
+        // at-a-time loop does.  Joint edges (rarer) are walked by lane 0.
+        const unsigned lt = (1u << lane) - 1u;
         auto dfs_seed = [&](int seed) {
             unsigned char fs = vbf[seed];
             if (fs & kBfVisited) return;
             if ((fs & kBfAwake) == 0 || (fs & kBfActive) == 0) return;
             if (fs & kBfStatic) return;
-            x.s_isl_bstart[bx + nIsl] = nbI;
-            x.s_isl_cstart[bx + nIsl] = ncI;
-            x.s_isl_jstart[bx + nIsl] = njI;
-            int top = 0, nStatic = 0;
-            stack[top++] = seed;
-            vbf[seed] = fs | kBfVisited;
+            if (lane == 0) {
+                x.s_isl_bstart[bx + nIsl] = nbI;
+                x.s_isl_cstart[bx + nIsl] = ncI;
+                x.s_isl_jstart[bx + nIsl] = njI;
+                stack[0] = seed;
+                vbf[seed] = fs | kBfVisited;
+            }
+            int top = 1, nStatic = 0;
+            tsync();
             while (top > 0) {
-                int b = stack[--top];
-                body_island[b] = nIsl;
-                unsigned char fb = vbf[b];
+                const int b = stack[--top];
+                const unsigned char fb = vbf[b];
+                tsync();
+                if (lane == 0) body_island[b] = nIsl;
                 if (fb & kBfStatic) {
-                    statics[nStatic++] = b;
+                    if (lane == 0) statics[nStatic] = b;
+                    ++nStatic;
                     continue;
                 }
-                isl_body[nbI++] = b;
-                for (int e = adj[b], ee = adj[b + 1]; e < ee; ++e) {
-                    int2 it = items[e];
-                    if (cvis[it.x]) continue;
-                    isl_contact[ncI] = c0 + it.x;
-                    isl_pair[ncI] = make_int2(b, it.y);
-                    ++ncI;
-                    cvis[it.x] = 1;
-                    unsigned char fo = vbf[it.y];
-                    if (fo & kBfVisited) continue;
-                    stack[top++] = it.y;
-                    vbf[it.y] = fo | kBfVisited;
+                if (lane == 0) isl_body[nbI] = b;
+                ++nbI;
+                for (int e0 = adj[b], ee = adj[b + 1]; e0 < ee; e0 += kWarp) {
+                    const int e = e0 + lane;
+                    int2 it = make_int2(0, 0);
+                    bool newc = false;
+                    if (e < ee) {
+                        it = items[e];
+                        newc = !cvis[it.x];
+                    }
+                    const unsigned cm = __ballot_sync(0xffffffffu, newc);
+                    unsigned char fo = kBfVisited;
+                    if (newc) {
+                        const int pos = ncI + __popc(cm & lt);
+                        isl_contact[pos] = c0 + it.x;
+                        isl_pair[pos] = make_int2(b, it.y);
+                        cvis[it.x] = 1;
+                        fo = vbf[it.y];
+                    }
+                    ncI += __popc(cm);
+                    const bool cand = newc && !(fo & kBfVisited);
+                    const unsigned same = __match_any_sync(0xffffffffu, cand ? it.y : -1 - lane);
+                    const bool push = cand && (__ffs(same) - 1) == lane;
+                    const unsigned pm = __ballot_sync(0xffffffffu, push);
+                    if (push) {
+                        stack[top + __popc(pm & lt)] = it.y;
+                        vbf[it.y] = fo | kBfVisited;
+                    }
+                    top += __popc(pm);
+                    tsync();
                 }
                 if (nj == 0) continue;
-                const BodyStatic& st = x.bst[b0 + b];
-                for (int e = 0; e < st.jadj_count; ++e) {
-                    int j = x.jadj_joint[st.jadj_start + e];
-                    if (x.jt[j].island_flag) continue;
-                    int other = x.jadj_other[st.jadj_start + e] - b0;
-                    unsigned char fo = vbf[other];
-                    if ((fo & kBfActive) == 0) continue;
-                    x.s_isl_joint[j0 + njI++] = j;
-                    x.jt[j].island_flag = 1;
-                    if (fo & kBfVisited) continue;
-                    stack[top++] = other;
-                    vbf[other] = fo | kBfVisited;
+                if (lane == 0) {
+                    const BodyStatic& st = x.bst[b0 + b];
+                    for (int e = 0; e < st.jadj_count; ++e) {
+                        int j = x.jadj_joint[st.jadj_start + e];
+                        if (x.jt[j].island_flag) continue;
+                        int other = x.jadj_other[st.jadj_start + e] - b0;
+                        unsigned char fo = vbf[other];
+                        if ((fo & kBfActive) == 0) continue;
+                        x.s_isl_joint[j0 + njI++] = j;
+                        x.jt[j].island_flag = 1;
+                        if (fo & kBfVisited) continue;
+                        stack[top++] = other;
+                        vbf[other] = fo | kBfVisited;
+                    }
                 }
+                top = __shfl_sync(0xffffffffu, top, 0);
+                njI = __shfl_sync(0xffffffffu, njI, 0);
+                tsync();
             }
-            for (int i = 0; i < nStatic; ++i) vbf[statics[i]] &= ~kBfVisited;
+            for (int i = lane; i < nStatic; i += kWarp) vbf[statics[i]] &= ~kBfVisited;
+            tsync();
             ++nIsl;
         };
         // 32 seeds at a time: a seed with no island contact and no joint is an island of its
@@ -4031,12 +4083,7 @@ DG void solve_world(const Ctx& x, int w, float* sbp, bool sb_smem, float* stage_
                 continue;
             }
             tsync();
-            if (lane == 0)
-                for (int seed = base; seed > base - kWarp && seed >= 0; --seed) dfs_seed(seed);
-            nIsl = __shfl_sync(0xffffffffu, nIsl, 0);
-            nbI = __shfl_sync(0xffffffffu, nbI, 0);
-            ncI = __shfl_sync(0xffffffffu, ncI, 0);
-            njI = __shfl_sync(0xffffffffu, njI, 0);
+            for (int seed = base; seed > base - kWarp && seed >= 0; --seed) dfs_seed(seed);
             tsync();
         }
         if (lane == 0) {
@@ -5769,6 +5816,7 @@ __global__ void __launch_bounds__(kSolveWarps * 32, 3) k_solve_toi(const __grid_
             asm volatile("mov.u32 %0, %%warpid;" : "=r"(warpid));
             x.prof[kProfSlots * (size_t)w + 28] = smid;
             x.prof[kProfSlots * (size_t)w + 29] = warpid;
+            if (!x.wi[w].pair_block) x.prof[kProfSlots * (size_t)w + 15] = in_smem ? 1 : 0;
         }
     }
 }
