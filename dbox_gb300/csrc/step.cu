@@ -635,6 +635,7 @@ struct BlockTeam {
     float* ra;                     // shared: per-warp partial minima
     int* rl;
     unsigned* words;               // shared: one ballot per 32 positions of a scan (blockDim.x of them)
+    int* aux;                      // shared: 4 counters of the incremental SolveTOI
     DG int rank() const { return threadIdx.x; }
     DG int size() const { return blockDim.x; }
     DG bool lead() const { return threadIdx.x == 0; }
@@ -868,27 +869,28 @@ DG int block_exclusive_scan(int* a, int n, int* sh) {
 }
 
 DG void sync_fixtures(const Ctx& x, int b);
-__global__ void __launch_bounds__(kPairThreads) k_pairs_block(const __grid_constant__ Ctx x) {
-    __shared__ float shf[32];
-    __shared__ int shi[32];
-    __shared__ int n_wide;
-    const int w = x.big_worlds[blockIdx.x];
+// A large world's pair table and pair search on a block (pairs into x.pairs, their count into
+// wd.pair_total).  At the end of Solve (b2world.d:1099-1120) after SynchronizeFixtures of the
+// island bodies; at the start of a step (`at_begin`: FindNewContacts after fixtures were
+// created, b2world.d:372-376) with the proxies as they stand.
+DG void pairs_block(const Ctx& x, int w, bool at_begin, float* shf, int* shi, int& n_wide) {
     const WorldInfo& wi = x.wi[w];
     WorldDyn& wd = x.wd[w];
     const int tid = threadIdx.x, nt = blockDim.x;
     const long long t_in = clock64();
-    auto prof_out = [&]() { if (x.prof && tid == 0) x.prof[kProfSlots * (size_t)w + 30] = clock64() - t_in; };
-    if (!(wd.step_complete && x.dt > 0.0f) || wd.error != 0) {        // solve_world did not reach its broad-phase
+    auto prof_out = [&]() { if (x.prof && tid == 0 && !at_begin) x.prof[kProfSlots * (size_t)w + 30] = clock64() - t_in; };
+    if (!at_begin && (!(wd.step_complete && x.dt > 0.0f) || wd.error != 0)) {   // Solve did not reach its broad-phase
         if (tid == 0) { wd.pair_total = 0; wd.g_valid = 0; }
         prof_out();
         return;
     }
-    // SynchronizeFixtures of the island bodies (b2world.d:1099-1116), the solve warp's last step
-    for (int i = tid; i < wi.body_count; i += nt) {
-        const int b = wi.body_start + i;
-        if ((x.bs[b].flags & kBodyIsland) == 0 || x.bs[b].type == kStaticBody) continue;
-        sync_fixtures(x, b);
-    }
+    // SynchronizeFixtures of the island bodies (b2world.d:1099-1116), the solve's last step
+    if (!at_begin)
+        for (int i = tid; i < wi.body_count; i += nt) {
+            const int b = wi.body_start + i;
+            if ((x.bs[b].flags & kBodyIsland) == 0 || x.bs[b].type == kStaticBody) continue;
+            sync_fixtures(x, b);
+        }
     // the contact pair table, rebuilt from the live contacts (hash_rebuild)
     for (int i = tid; i < wi.hash_cap; i += nt) x.hash[wi.hash_start + i] = kHashEmpty;
     __syncthreads();
@@ -1139,6 +1141,35 @@ __global__ void __launch_bounds__(kPairThreads) k_pairs_block(const __grid_const
     prof_out();
 }
 
+__global__ void __launch_bounds__(kPairThreads) k_pairs_block(const __grid_constant__ Ctx x) {
+    __shared__ float shf[32];
+    __shared__ int shi[32];
+    __shared__ int n_wide;
+    pairs_block(x, x.big_worlds[blockIdx.x], false, shf, shi, n_wide);
+}
+
+// FindNewContacts of a large world whose fixtures were just created (e_newFixture), on its
+// block: the pair search, then AddPair (k_step_begin does it on a warp for the other worlds)
+__global__ void __launch_bounds__(kPairThreads) k_begin_big(const __grid_constant__ Ctx x) {
+    __shared__ float shf[32];
+    __shared__ int shi[32];
+    __shared__ int n_wide;
+    __shared__ unsigned s_bal[32];
+    __shared__ int s_box[2];
+    __shared__ float s_ra[32];
+    __shared__ int s_rl[32];
+    __shared__ int s_aux[4];
+    const int w = x.big_worlds[blockIdx.x];
+    if (!(x.wd[w].flags & 1u)) return;
+    pairs_block(x, w, true, shf, shi, n_wide);
+    __syncthreads();
+    BlockTeam tm{s_bal, s_box, s_ra, s_rl, nullptr, s_aux};
+    const int total = x.wd[w].pair_total;
+    if (total > 0) add_pairs_t(x, w, total, tm);
+    __syncthreads();
+    if (threadIdx.x == 0) x.wd[w].flags &= ~1u;
+}
+
 // FindNewContacts inside SolveTOI for a large world (one warp): the move buffer holds the
 // proxies this event's SynchronizeFixtures moved (ranks now[0 .. nnow)); their pairs with every
 // overlapping proxy (b2BroadPhase.UpdatePairs, b2broadphase.d:139-195) come from the grid
@@ -1247,7 +1278,7 @@ __global__ void k_step_begin(const __grid_constant__ Ctx x) {
     if (lane == 0) { wd.error = 0; wd.islands = 0; wd.toi_events = 0; wd.ev_count = 0; }
     for (int i = lane; i < wi.body_count; i += kWarp) x.s_woken[wi.body_start + i] = kNoWake;
     tsync();
-    if (wd.flags & 1u) {                                                // e_newFixture
+    if ((wd.flags & 1u) && !wi.pair_block) {                            // e_newFixture (large worlds: k_begin_big)
         hash_rebuild(x, w);
         find_new_contacts(x, w);
         if (lane == 0) wd.flags &= ~1u;
@@ -4626,15 +4657,15 @@ DG void toi_world_t(const Ctx& x, int w, float* sbp, const Team& tm) {
         int* cand = x.s_tcand + c0;
         auto is_cand = [&](int k) { return toi_candidate(x, c0 + k, b0); };
         int ncand = tm.collect(0, wd.contact_count, cand, 0, is_cand);
-        // block teams: the candidates of each dynamic body (positions in cand, descending), so
-        // that an event's joins and invalidations visit only its bodies' candidates; those
+        // block teams: the candidates of each non-static body (positions in cand, descending),
+        // so that an event's joins and invalidations visit only its bodies' candidates; those
         // collected after this point (from the events' new pairs) are scanned apart
         const int ncand0 = ncand;
         int* lstart = x.s_adj_start + wi.bx_start;                       // nb + 1
         int* lent = reinterpret_cast<int*>(x.s_adj_items + 2 * (size_t)c0);
         if constexpr (Team::kLists) {
             int* lcur = x.s_cursor + b0;
-            auto dyn = [&](int b) { return x.bs[b0 + b].type == kDynamicBody; };
+            auto dyn = [&](int b) { return x.bs[b0 + b].type != kStaticBody; };
             for (int i = rk; i < nb; i += ts) lstart[i] = 0;
             tm.sync();
             for (int t = rk; t < ncand; t += ts) {
@@ -4667,6 +4698,24 @@ DG void toi_world_t(const Ctx& x, int w, float* sbp, const Team& tm) {
             }
             tm.sync();
         }
+        // Block teams revisit, after an event, only the candidates whose TOI inputs the event
+        // can have changed: those of every body it touched (the event's two bodies, each
+        // neighbour a join visited, accepted or not, and both bodies of each new contact, whose
+        // AddPair may wake them) and every candidate added since SolveTOI began.  Nothing else
+        // changes a candidate's flags, sub-step count or TOI, or the awake state of its bodies.
+        // The minimum TOI is kept per 32 consecutive candidates (smallest TOI, then the newest
+        // contact slot, which is first in list order) and the chunks holding a revisited
+        // candidate are recomputed.  The first event, and any whose revisit list would overflow,
+        // take the full passes.
+        int* dset = reinterpret_cast<int*>(x.s_isl_pair + c0);          // revisit list (positions)
+        const int dcap = 2 * wi.contact_cap;
+        int* nlist = x.s_cstate + c0;                                    // the revisited that need a TOI
+        unsigned* wmin_a = reinterpret_cast<unsigned*>(x.s_level + wi.kx_start);   // per chunk: TOI bits
+        int* wmin_k = x.s_tmp + wi.kx_start;                             // and contact slot (-1: none)
+        int* wdirty = x.s_lcur + wi.kx_start;
+        int* tbody = x.s_stack + b0;                                     // bodies an event touched
+        bool full = true;
+        int nd = 0;
         // a large world's event pair searches use the grid of its end-of-solve pair search and
         // the proxies moved since (toi_pairs_big); without destruction a proxy's rank is its
         // fixture index
@@ -4687,8 +4736,108 @@ DG void toi_world_t(const Ctx& x, int w, float* sbp, const Team& tm) {
                 break;
             }
             int n = wd.contact_count;
+            auto advance_one = [&](int t) {
+                const int kk = cand[t];
+                const int2 cb = x.s_cbody[c0 + kk];
+                dbox_body_state& bA = x.bs[b0 + cb.x];
+                dbox_body_state& bB = x.bs[b0 + cb.y];
+                float alpha0 = bA.sweep[8];
+                if (bA.sweep[8] < bB.sweep[8]) {
+                    alpha0 = bB.sweep[8];
+                    Sweep s = b_sweep(bA); sweep_advance(s, alpha0); b_set_sweep(bA, s);
+                } else if (bB.sweep[8] < bA.sweep[8]) {
+                    alpha0 = bA.sweep[8];
+                    Sweep s = b_sweep(bB); sweep_advance(s, alpha0); b_set_sweep(bB, s);
+                }
+                SweepSnap& sn = x.snap[c0 + kk];
+                sn.a = b_sweep(bA);
+                sn.b = b_sweep(bB);
+                sn.alpha0 = alpha0;
+            };
+            auto compute_toi = [&](int k) {                              // the TOI of a contact that needs one
+                dbox_contact_state& c = x.ct[c0 + k];
+                const DFixture& fa = x.fx[c.fixture_a];
+                const DFixture& fb = x.fx[c.fixture_b];
+                Sweep sA, sB;
+                float alpha0;
+                if (advanced) { sA = x.snap[c0 + k].a; sB = x.snap[c0 + k].b; alpha0 = x.snap[c0 + k].alpha0; }
+                else { sA = b_sweep(x.bs[fa.body]); sB = b_sweep(x.bs[fb.body]); alpha0 = sA.alpha0; }
+                float beta;
+                int state = time_of_impact(make_proxy(fa), make_proxy(fb), sA, sB, 1.0f, &beta);
+                float alpha = state == kToiTouching ? bmin(alpha0 + (1.0f - alpha0) * beta, 1.0f) : 1.0f;
+                c.toi = alpha;
+                c.flags |= kContactToi;
+                return alpha;
+            };
+            float bestA = 1.0f;
+            int bestLp = 0x7fffffff;
+            bool incremental = false;
+            if constexpr (Team::kLists) incremental = !full && advanced;
+            if constexpr (Team::kLists) {
+              if (incremental) {
+                // the revisited candidates that need a TOI, in list order (descending position,
+                // repeats dropped) on the lead: sweeps advanced, then their TOIs over the block
+                if (tm.lead()) tm.aux[0] = 0;
+                tm.sync();
+                for (int i = rk; i < nd; i += ts) {
+                    const int t = dset[i];
+                    if (toi_needs(x, c0 + cand[t], b0)) nlist[atomicAdd(&tm.aux[0], 1)] = t;
+                }
+                tm.sync();
+                int nn = tm.aux[0];
+                if (tm.lead()) {
+                    for (int a = 1; a < nn; ++a) {                       // descending, few entries
+                        const int v = nlist[a];
+                        int q = a - 1;
+                        while (q >= 0 && nlist[q] < v) { nlist[q + 1] = nlist[q]; --q; }
+                        nlist[q + 1] = v;
+                    }
+                    int m = 0;
+                    for (int a = 0; a < nn; ++a)
+                        if (m == 0 || nlist[m - 1] != nlist[a]) nlist[m++] = nlist[a];
+                    for (int a = 0; a < m; ++a) advance_one(nlist[a]);
+                    tm.aux[1] = m;
+                }
+                tm.sync();
+                nn = tm.aux[1];
+                mark(0);
+                for (int i = rk; i < nn; i += ts) compute_toi(cand[nlist[i]]);
+                for (int i = rk; i < nd; i += ts) wdirty[dset[i] >> 5] = 1;
+                tm.sync();
+                // recompute the chunks that hold a revisited candidate, a warp a chunk
+                const int nch = (ncand + 31) >> 5, warp = rk >> 5, lane = rk & 31, nw = ts >> 5;
+                for (int q = warp; q < nch; q += nw) {
+                    if (!wdirty[q]) continue;
+                    const int t = 32 * q + lane;
+                    float a = 1.0f;
+                    int kb = -1;
+                    if (t < ncand) {
+                        const int k = cand[t];
+                        const dbox_contact_state& c = x.ct[c0 + k];
+                        if ((c.flags & kContactEnabled) && c.toi_count <= kMaxSubSteps && (c.flags & kContactToi) &&
+                            c.toi < 1.0f) { a = c.toi; kb = k; }
+                    }
+                    for (int o = 16; o > 0; o >>= 1) {
+                        const float oa = __shfl_xor_sync(0xffffffffu, a, o);
+                        const int ok = __shfl_xor_sync(0xffffffffu, kb, o);
+                        if (oa < a || (oa == a && ok > kb)) { a = oa; kb = ok; }
+                    }
+                    if (lane == 0) { wmin_a[q] = __float_as_uint(a); wmin_k[q] = kb; wdirty[q] = 0; }
+                }
+                tm.sync();
+                // the minimum over the chunks (a slot's list position is n - 1 - slot)
+                for (int q = rk; q < nch; q += ts) {
+                    const int kb = wmin_k[q];
+                    if (kb < 0) continue;
+                    const float a = __uint_as_float(wmin_a[q]);
+                    const int lp = n - 1 - kb;
+                    if (a < bestA || (a == bestA && lp < bestLp)) { bestA = a; bestLp = lp; }
+                }
+                mark(1);
+              }
+            }
             // sweeps are put onto a common time in list order (b2world.d:1212-1226)
-            if (advanced) {
+            if (advanced && !incremental) {
                 tm.scan_desc(ncand, [&](int t) { return toi_needs(x, c0 + cand[t], b0); }, [&](int t) {
                     const int kk = cand[t];
                     const int2 cb = x.s_cbody[c0 + kk];
@@ -4709,16 +4858,14 @@ DG void toi_world_t(const Ctx& x, int w, float* sbp, const Team& tm) {
                     return true;
                 });
             }
-            mark(0);
+            if (!incremental) mark(0);
             // the TOI of every contact that needs one (b2world.d:1159-1236), and in the same
             // pass the minimum TOI, first in list order on ties (each contact's TOI is
             // written only by its own iteration)
             // (four candidates of a rank at a time: their slots, then their flags, counts and
             // TOIs are loaded together, and the bodies are read only when the flags leave a
-            // fresh TOI possible)
-            float bestA = 1.0f;
-            int bestLp = 0x7fffffff;
-            for (int t0 = rk; t0 < ncand; t0 += 4 * ts) {
+            // fresh TOI possible; block teams also keep each 32-candidate chunk's minimum)
+            for (int t0 = rk; (t0 & ~31) < (incremental ? 0 : ncand); t0 += 4 * ts) {
                 int kk[4];
                 uint32_t fl[4];
                 int tc[4];
@@ -4740,29 +4887,32 @@ DG void toi_world_t(const Ctx& x, int w, float* sbp, const Team& tm) {
 #pragma unroll 1
                 for (int j = 0; j < 4; ++j) {
                     const int k = kk[j];
-                    if (k < 0 || (fl[j] & kContactEnabled) == 0 || tc[j] > kMaxSubSteps) continue;
-                    if ((fl[j] & kContactToi) == 0) {
-                        if (!toi_needs_bodies(x, c0 + k, b0)) continue;
-                        dbox_contact_state& c = x.ct[c0 + k];
-                        const DFixture& fa = x.fx[c.fixture_a];
-                        const DFixture& fb = x.fx[c.fixture_b];
-                        Sweep sA, sB;
-                        float alpha0;
-                        if (advanced) { sA = x.snap[c0 + k].a; sB = x.snap[c0 + k].b; alpha0 = x.snap[c0 + k].alpha0; }
-                        else { sA = b_sweep(x.bs[fa.body]); sB = b_sweep(x.bs[fb.body]); alpha0 = sA.alpha0; }
-                        float beta;
-                        int state = time_of_impact(make_proxy(fa), make_proxy(fb), sA, sB, 1.0f, &beta);
-                        float alpha = state == kToiTouching ? bmin(alpha0 + (1.0f - alpha0) * beta, 1.0f) : 1.0f;
-                        c.toi = alpha;
-                        c.flags |= kContactToi;
-                        tv[j] = alpha;
+                    bool in = false;
+                    if (k >= 0 && (fl[j] & kContactEnabled) && tc[j] <= kMaxSubSteps) {
+                        in = true;
+                        if ((fl[j] & kContactToi) == 0) {
+                            if (toi_needs_bodies(x, c0 + k, b0)) tv[j] = compute_toi(k);
+                            else in = false;
+                        }
                     }
                     const float toi = tv[j];
                     int lp = n - 1 - k;
-                    if (toi < bestA || (toi == bestA && lp < bestLp && toi < 1.0f)) { bestA = toi; bestLp = lp; }
+                    if (in && (toi < bestA || (toi == bestA && lp < bestLp && toi < 1.0f))) { bestA = toi; bestLp = lp; }
+                    if constexpr (Team::kLists) {
+                        // this chunk's minimum (all 32 lanes of the warp hold the chunk's candidates)
+                        float a = in && toi < 1.0f ? toi : 1.0f;
+                        int kb = in && toi < 1.0f ? k : -1;
+                        for (int o = 16; o > 0; o >>= 1) {
+                            const float oa = __shfl_xor_sync(0xffffffffu, a, o);
+                            const int ok = __shfl_xor_sync(0xffffffffu, kb, o);
+                            if (oa < a || (oa == a && ok > kb)) { a = oa; kb = ok; }
+                        }
+                        const int t = t0 + j * ts;
+                        if ((rk & 31) == 0 && t < ncand) { wmin_a[t >> 5] = __float_as_uint(a); wmin_k[t >> 5] = kb; wdirty[t >> 5] = 0; }
+                    }
                 }
             }
-            mark(1);
+            if (!incremental) mark(1);
             tm.argmin(bestA, bestLp);
             mark(2);
             if (bestLp == 0x7fffffff || 1.0f - 10.0f * kEpsilon < bestA) {
@@ -4773,8 +4923,10 @@ DG void toi_world_t(const Ctx& x, int w, float* sbp, const Team& tm) {
             const int mk = n - 1 - bestLp;
             const int2 mcb = x.s_cbody[c0 + mk];
             int solved = 0, nbI = 0, ncI = 0;
+            int ntb = 0;                                                 // bodies this event touched (lead)
             if (tm.lead()) {
                 ++events;
+                if constexpr (Team::kLists) { tbody[ntb++] = mcb.x; tbody[ntb++] = mcb.y; }
                 dbox_contact_state& mc = x.ct[c0 + mk];
                 dbox_body_state& bA = x.bs[b0 + mcb.x];
                 dbox_body_state& bB = x.bs[b0 + mcb.y];
@@ -4827,6 +4979,7 @@ DG void toi_world_t(const Ctx& x, int w, float* sbp, const Team& tm) {
                         dbox_body_state& O = x.bs[b0 + other];
                         if (O.type == kDynamicBody && (Bd.flags & kBodyBullet) == 0 && (O.flags & kBodyBullet) == 0) return true;
                         if (x.s_cq[c0 + kk] & 2) return true;
+                        if constexpr (Team::kLists) { if (ntb < nb) tbody[ntb] = other; ++ntb; }
                         Sweep backup = b_sweep(O);
                         if ((O.flags & kBodyIsland) == 0) b_advance(O, minAlpha);
                         unsigned evt = 0;
@@ -4919,6 +5072,40 @@ DG void toi_world_t(const Ctx& x, int w, float* sbp, const Team& tm) {
                 if (tm.lead()) wd.step_complete = 0;
                 break;
             }
+            if constexpr (Team::kLists) {
+                // the next event's revisit list: the candidates of the bodies this event touched
+                // (the new contacts' bodies included) and every candidate added since SolveTOI began
+                ntb = tm.bcast(ntb);
+                const int nnew = wd.contact_count - n;
+                const bool over = ntb > nb || ntb + 2 * nnew > nb;
+                if (!over)
+                    for (int i = rk; i < nnew; i += ts) {
+                        const int2 cb = x.s_cbody[c0 + n + i];
+                        tbody[ntb + 2 * i] = cb.x;
+                        tbody[ntb + 2 * i + 1] = cb.y;
+                    }
+                if (tm.lead()) tm.aux[2] = 0;
+                tm.sync();
+                if (!over) {
+                    const int warp = rk >> 5, lane = rk & 31, nw = ts >> 5;
+                    for (int i = warp; i < ntb + 2 * nnew; i += nw) {
+                        const int bd = tbody[i];
+                        if (x.bs[b0 + bd].type == kStaticBody) continue;
+                        for (int e = lstart[bd] + lane, ee = lstart[bd + 1]; e < ee; e += 32) {
+                            const int q = atomicAdd(&tm.aux[2], 1);
+                            if (q < dcap) dset[q] = lent[e];
+                        }
+                    }
+                    for (int t = ncand0 + rk; t < ncand; t += ts) {
+                        const int q = atomicAdd(&tm.aux[2], 1);
+                        if (q < dcap) dset[q] = t;
+                    }
+                }
+                tm.sync();
+                nd = tm.aux[2];
+                full = over || nd > 1024 || nd > wi.contact_cap;
+                tm.sync();
+            }
         }
         if (tm.lead()) { wd.toi_events = events; wd.acc_toi_events += (unsigned long long)events; }
     }
@@ -4954,13 +5141,14 @@ __global__ void __launch_bounds__(kPairThreads) k_collide_finish_big(const __gri
     __shared__ float s_ra[32];
     __shared__ int s_rl[32];
     __shared__ unsigned s_words[kPairThreads];
+    __shared__ int s_aux[4];
     const int w = x.big_worlds[blockIdx.x];
     const WorldInfo& wi = x.wi[w];
     WorldDyn& wd = x.wd[w];
     const int tid = threadIdx.x, nt = blockDim.x;
     const int n = wd.contact_count, c0 = wi.contact_start;
     const long long t_in = clock64();
-    BlockTeam tm{s_bal, s_box, s_ra, s_rl, s_words};
+    BlockTeam tm{s_bal, s_box, s_ra, s_rl, s_words, s_aux};
     bool need = false;
     for (int k = tid; k < n; k += nt) {
         if (x.s_cstate[c0 + k] == 1) {
@@ -5064,10 +5252,11 @@ __global__ void __launch_bounds__(kPairThreads) k_finish_big_block(const __grid_
     __shared__ float s_ra[32];
     __shared__ int s_rl[32];
     __shared__ unsigned s_words[kPairThreads];
+    __shared__ int s_aux[4];
     const int w = x.big_worlds[blockIdx.x];
     const int total = x.wd[w].pair_total;
     const long long t_in = clock64();
-    BlockTeam tm{s_bal, s_box, s_ra, s_rl, s_words};
+    BlockTeam tm{s_bal, s_box, s_ra, s_rl, s_words, s_aux};
     if (total > 0) add_pairs_t(x, w, total, tm);
     if (x.prof && threadIdx.x == 0) x.prof[kProfSlots * (size_t)w + 31] = clock64() - t_in;
     toi_world_t(x, w, x.s_sbody + 6 * (size_t)x.wi[w].body_start, tm);
@@ -5834,6 +6023,7 @@ extern "C" int dbox_launch_collide(const dg::Ctx* x, cudaStream_t stream) {
     if (flat_blocks < 1) flat_blocks = 1;
     if (flat_blocks > 152 * 16) flat_blocks = 152 * 16;
     dg::k_step_begin<<<team_blocks, threads, 0, stream>>>(*x);
+    if (x->n_big > 0) dg::k_begin_big<<<x->n_big, dg::kPairThreads, 0, stream>>>(*x);
     dg::k_collide<<<flat_blocks, 256, 0, stream>>>(*x);
     dg::k_collide_finish<<<team_blocks, threads, 0, stream>>>(*x);
     if (x->n_big > 0) dg::k_collide_finish_big<<<x->n_big, dg::kPairThreads, 0, stream>>>(*x);
@@ -5841,7 +6031,7 @@ extern "C" int dbox_launch_collide(const dg::Ctx* x, cudaStream_t stream) {
 }
 
 // part 2 of a step: Solve and SolveTOI (1 launch, 3 or 4 with a large world); *launches = all of the step's
-// (part 1 is 3 launches, 4 with a large world)
+// (part 1 is 3 launches, 5 with a large world)
 extern "C" int dbox_launch_solve(const dg::Ctx* x, cudaStream_t stream, int* launches) {
     if (x->solve_blocks < 1) return (int)cudaErrorInvalidValue;
     if (x->solve_queue) cudaMemsetAsync(x->solve_queue, 0, sizeof(int) * (2 + 4 * (size_t)x->solve_nsm), stream);
@@ -5852,7 +6042,7 @@ extern "C" int dbox_launch_solve(const dg::Ctx* x, cudaStream_t stream, int* lau
         dg::k_pairs_block<<<x->n_big, dg::kPairThreads, 0, stream>>>(*x);
         dg::k_finish_big_block<<<x->n_big, dg::kPairThreads, 0, stream>>>(*x);
     }
-    if (launches) *launches = x->n_big > 0 ? 7 + x->big_block : 4;
+    if (launches) *launches = x->n_big > 0 ? 8 + x->big_block : 4;
     return (int)cudaGetLastError();
 }
 
@@ -5865,6 +6055,7 @@ extern "C" int dbox_launch_step_ev(const dg::Ctx* x, cudaStream_t stream, int* l
     if (flat_blocks > 152 * 16) flat_blocks = 152 * 16;
     if (ev) cudaEventRecordWithFlags(ev[0], stream, cudaEventRecordExternal);
     dg::k_step_begin<<<team_blocks, threads, 0, stream>>>(*x);
+    if (x->n_big > 0) dg::k_begin_big<<<x->n_big, dg::kPairThreads, 0, stream>>>(*x);
     dg::k_collide<<<flat_blocks, 256, 0, stream>>>(*x);
     dg::k_collide_finish<<<team_blocks, threads, 0, stream>>>(*x);
     if (x->n_big > 0) dg::k_collide_finish_big<<<x->n_big, dg::kPairThreads, 0, stream>>>(*x);
@@ -5879,7 +6070,7 @@ extern "C" int dbox_launch_step_ev(const dg::Ctx* x, cudaStream_t stream, int* l
     }
     if (ev) cudaEventRecordWithFlags(ev[2], stream, cudaEventRecordExternal);
     if (ev) cudaEventRecordWithFlags(ev[3], stream, cudaEventRecordExternal);
-    if (launches) *launches = x->n_big > 0 ? 7 + x->big_block : 4;
+    if (launches) *launches = x->n_big > 0 ? 8 + x->big_block : 4;
     return (int)cudaGetLastError();
 }
 

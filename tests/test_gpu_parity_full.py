@@ -179,15 +179,19 @@ def test_stress_reduced_exact(oracle_lib, gpu_lib, per_pile, solver):
     ow = oracle_lib.OracleWorld(s)
     gw = gpu_lib.World(s)
     gw.set_island_solver(solver)
+    toi = 0
     for t in range(120):
         ow.step()
         gw.step()
+        toi += gw.stats(0)[1]
+        assert gw.stats(0)[1] == ow.last_toi_events(), "step %d: TOI events" % (t + 1)
         if (t + 1) % 30 == 0:
             d = exact_diff(ow.export_state(), gw.export_state())
             assert not d, "step %d: %s" % (t + 1, d[:6])
     st = gw.export_state()
     assert st["header"][0]["contact_count"] > 4 * per_pile
     assert np.abs(st["joints"]["impulse"]).max() > 0
+    assert toi > 100                     # SolveTOI's event loop runs many events a step
 
 
 @pytest.mark.parametrize("solver", [0, 1], ids=["block_solve", "warp_solve"])
@@ -205,10 +209,13 @@ def test_large_mixed_world_exact(oracle_lib, gpu_lib, solver):
     gw.set_island_solver(solver)
     got = []
     gw.set_listener(lambda ev: got.append(ev))
+    toi = 0
     for t in range(240):
         got.clear()
         ow.step()
         gw.step()
+        toi += gw.stats(0)[1]
+        assert gw.stats(0)[1] == ow.last_toi_events(), "step %d: TOI events" % (t + 1)
         ref = ow.events()
         ev = np.concatenate(got) if got else np.zeros(0, abi.CONTACT_EVENT)
         assert ev.tobytes() == ref.tobytes(), "step %d: events differ (%d vs %d)" % (t + 1, len(ev), len(ref))
@@ -219,3 +226,4 @@ def test_large_mixed_world_exact(oracle_lib, gpu_lib, solver):
     dyn = st["bodies"]["type"] == abi.DYNAMIC
     assert ((st["bodies"]["flags"][dyn] & abi.BODY_AWAKE) == 0).any()
     assert st["header"][0]["joint_count"] == sum(len(s[k]) for k in scenes.JOINT_KINDS)
+    assert toi > 100
