@@ -22,7 +22,7 @@
 
 extern "C" int dbox_launch_step(const dg::Ctx* x, cudaStream_t stream, int* launches);
 extern "C" const void* dbox_solve_kernel();
-extern "C" int dbox_big_solve_init();
+extern "C" int dbox_big_solve_init(int* cluster);
 const dg::MlpDev* dbox_mlp_device_view(const dbox_mlp* m, dg::MlpDev* out);
 extern "C" int dbox_launch_step_ev(const dg::Ctx* x, cudaStream_t stream, int* launches, cudaEvent_t* ev);
 extern "C" int dbox_launch_collide(const dg::Ctx* x, cudaStream_t stream);
@@ -201,6 +201,7 @@ struct dbox_world {
     int measure = 0;
     int wait_polls = 1 << 20;   // budget of one mbarrier wait in the solve kernel (polls)
     int island_solver = 0;      // 0: a large world's Solve on a block (k_solve_big), 1: on a warp
+    int big_cluster = 1;        // blocks of k_solve_big's cluster per large world (its level sweeps)
     // contact listener
     DBuf<dbox_contact_event> d_events;
     DBuf<unsigned> s_sapk0, s_sapk1;
@@ -696,7 +697,7 @@ int ensure_device(dbox_world* w) {
         if (rc) return rc;
         rc = upload(w);
         if (rc) return rc;
-        if (w->n_big > 0) CU((cudaError_t)dbox_big_solve_init());
+        if (w->n_big > 0) CU((cudaError_t)dbox_big_solve_init(&w->big_cluster));
     }
     return sync_filter(w);
 }
@@ -811,6 +812,7 @@ dg::Ctx make_ctx(dbox_world* w, float dt, int vi, int pi) {
     x.big_worlds = w->d_big.p;
     x.n_big = w->n_big;
     x.big_block = (w->n_big > 0 && w->island_solver == 0) ? 1 : 0;
+    x.big_cluster = w->big_cluster;
     x.s_cevt = w->s_cevt.p;
     return x;
 }

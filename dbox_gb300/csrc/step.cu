@@ -5306,16 +5306,141 @@ DG void uf_union(int* parent, int a, int b) {
     }
 }
 
+// ---- the level sweeps of a large world's Solve, spread over a thread-block cluster
+DG unsigned cluster_rank() { unsigned r; asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r)); return r; }
+DG unsigned cluster_blocks() { unsigned r; asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r)); return r; }
+// every thread of every block of the cluster arrives (release) and waits (acquire): the
+// global-memory writes made before it by any block are seen by the loads made after it
+DG void cluster_sync() { asm volatile("barrier.cluster.arrive;\n\tbarrier.cluster.wait;" ::: "memory"); }
+DG int ld_volatile_i(const int* p) { return *reinterpret_cast<const volatile int*>(p); }
+
+// What a row of a sweep needs (the same for every block of the cluster)
+struct BigSweep {
+    int b0, kx;
+    VRow* vrow;
+    PRow* prow;
+    SB sb;
+    bool warm;
+    float dtRatio;
+    int njI, maxLv, maxLp;
+    const int* lvl_v;
+    const int* lvl_p;
+    const int* sched_p;
+    int* iflags;
+    unsigned* iminsep;
+};
+// warm start of a contact, or a joint's InitVelocityConstraints (b2island.d:133-146)
+DG void big_warm_row(const Ctx& x, const BigSweep& s, int idx) {
+    if (s.njI == 0) { warm_start(unpack_v(load_v(s.vrow + idx)), s.sb); return; }
+    const int item = s.sched_p[s.kx + idx];
+    if (item >= 0) { if (s.warm) warm_start(unpack_v(load_v(s.vrow + x.s_vpos[item])), s.sb); }
+    else joint_init(x, -item - 1, s.b0, s.sb, s.warm, s.dtRatio);
+}
+// one row of a velocity iteration (b2contactsolver.d:492-772, the joints' SolveVelocityConstraints)
+DG void big_vel_row(const Ctx& x, const BigSweep& s, int idx, int it) {
+    const VRow r = load_v(s.vrow + idx);
+    if (r.ids.w >= 0) {
+        if (it == 0 && (r.ids.z & 0x100)) {                          // a predicted start (ws mode 2)
+            float4 im;
+            solve_velocity_learned(r, s.sb, &im);
+            s.vrow[idx].imp = im;
+            return;
+        }
+        VC vc = unpack_v(r);
+        BodyVel q = load_vel(s.sb, vc.bodyA, vc.bodyB);
+        if (vc.pointCount == 2) solve_velocity_two(vc, q);
+        else solve_velocity(vc, q);
+        store_vel(s.sb, vc.bodyA, vc.bodyB, q);
+        s.vrow[idx].imp = make_float4(vc.p[0].normalImpulse, vc.p[0].tangentImpulse, vc.p[1].normalImpulse,
+                                      vc.p[1].tangentImpulse);
+    } else {
+        joint_solve_velocity(x, -r.ids.w - 1, s.b0, s.sb);
+    }
+}
+// one row of a position iteration, skipping islands already solved (b2island.d:206-224)
+DG void big_pos_row(const Ctx& x, const BigSweep& s, int idx) {
+    const PRow r = load_p(s.prow + idx);
+    const int is = r.ids.w;
+    if (s.iflags[is] & 1) return;
+    if (r.ids.z >= 0) {
+        const float ms = solve_position_row(unpack_p(r), s.sb);
+        atomicMin(&s.iminsep[is], fkey(ms));
+    } else if (!joint_solve_position(x, -r.ids.z - 1, s.b0, s.sb)) {
+        atomicOr(&s.iflags[is], 4);
+    }
+}
+// levels 1..maxL in order, a level's rows over the cluster's threads, a barrier between levels
+template <class F>
+DG void cluster_levels(const int* lvl, int maxL, int gtid, int gsize, bool clustered, F&& f) {
+    for (int L = 1; L <= maxL; ++L) {
+        const int e = lvl[L + 1];
+        for (int idx = lvl[L] + gtid; idx < e; idx += gsize) f(idx);
+        if (clustered) cluster_sync();
+        else __syncthreads();
+    }
+}
+// The part of a large world's Solve the cluster's other blocks run: the same barriers in the
+// same order as the first block (published parameters after the first, the continue flag of
+// each position iteration after its check).
+DG void big_sweep_helper(const Ctx& x, int w, int crank, int csize) {
+    const WorldInfo& wi = x.wi[w];
+    WorldDyn& wd = x.wd[w];
+    const int b0 = wi.body_start, kx = wi.kx_start;
+    cluster_sync();                                                  // the rows are built
+    BigSweep s;
+    s.b0 = b0;
+    s.kx = kx;
+    s.vrow = x.vr + kx;
+    s.prow = x.pr + kx;
+    s.sb.p = x.s_sbody + 6 * (size_t)b0;
+    s.warm = x.warm_starting != 0;
+    s.dtRatio = wd.inv_dt0 * x.dt;
+    s.njI = ld_volatile_i(&wd.sw_njI);
+    s.maxLv = ld_volatile_i(&wd.sw_maxv);
+    s.maxLp = ld_volatile_i(&wd.sw_maxp);
+    s.lvl_v = x.s_lvl_v + kx;
+    s.lvl_p = (s.njI ? x.s_lvl_p : x.s_lvl_v) + kx;
+    s.sched_p = s.njI ? x.s_sched_p : x.s_sched_v;
+    s.iflags = x.s_isl_flags + b0;
+    s.iminsep = x.s_isl_minsep + b0;
+    // rows of a level dealt round-robin over the blocks (each block a share of every level)
+    const int gtid = (int)threadIdx.x * csize + crank, gsize = csize * (int)blockDim.x;
+    if (s.njI == 0) {
+        if (s.warm) cluster_levels(s.lvl_v, s.maxLv, gtid, gsize, true, [&](int idx) { big_warm_row(x, s, idx); });
+    } else {
+        cluster_levels(s.lvl_p, s.maxLp, gtid, gsize, true, [&](int idx) { big_warm_row(x, s, idx); });
+    }
+    for (int it = 0; it < x.vel_iters; ++it)
+        cluster_levels(s.lvl_v, s.maxLv, gtid, gsize, true, [&](int idx) { big_vel_row(x, s, idx, it); });
+    cluster_sync();                                                  // positions integrated
+    for (int it = 0; it < x.pos_iters; ++it) {
+        cluster_sync();                                              // this iteration's island marks reset
+        cluster_levels(s.lvl_p, s.maxLp, gtid, gsize, true, [&](int idx) { big_pos_row(x, s, idx); });
+        cluster_sync();                                              // the first block's check
+        if (!ld_volatile_i(&wd.sw_go)) break;
+    }
+}
+
 __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant__ Ctx x) {
     extern __shared__ __align__(16) float big_smem[];                  // ws mode 2: the inference staging
     __shared__ int shi[32];
     __shared__ float shf[32];
     __shared__ int s_next, s_maxv, s_maxp;
-    const int w = x.big_worlds[blockIdx.x];
+    const int csize = x.big_cluster > 1 ? (int)cluster_blocks() : 1;
+    const int crank = csize > 1 ? (int)cluster_rank() : 0;
+    const bool clustered = csize > 1;
+    const int w = x.big_worlds[blockIdx.x / csize];
     const WorldInfo& wi = x.wi[w];
     WorldDyn& wd = x.wd[w];
     const int tid = threadIdx.x, nt = blockDim.x;
-    if (!(wd.step_complete && x.dt > 0.0f)) return;
+    if (!(wd.step_complete && x.dt > 0.0f)) return;                    // the same decision in every block
+    if (crank != 0) { big_sweep_helper(x, w, crank, csize); return; }
+    if (x.prof && tid == 0) {
+        unsigned smid;
+        asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+        x.prof[kProfSlots * (size_t)w + 27] = csize;
+        x.prof[kProfSlots * (size_t)w + 28] = smid;
+    }
     const int b0 = wi.body_start, nb = wi.body_count;
     const int c0 = wi.contact_start, n = wd.contact_count;
     const int j0 = wi.joint_start, nj = wi.joint_count;
@@ -5680,40 +5805,37 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
             __syncthreads();
         }
     };
+    BigSweep bs_;
+    bs_.b0 = b0;
+    bs_.kx = kx;
+    bs_.vrow = vrow;
+    bs_.prow = prow;
+    bs_.sb = sb;
+    bs_.warm = warm;
+    bs_.dtRatio = dtRatio;
+    bs_.njI = njI;
+    bs_.maxLv = maxLv;
+    bs_.maxLp = maxLp;
+    bs_.lvl_v = x.s_lvl_v + kx;
+    bs_.lvl_p = lvl_p + kx;
+    bs_.sched_p = sched_p;
+    bs_.iflags = iflags;
+    bs_.iminsep = iminsep;
+    if (clustered) {                                                   // the other blocks' parameters
+        if (tid == 0) { wd.sw_maxv = maxLv; wd.sw_maxp = maxLp; wd.sw_njI = njI; }
+        cluster_sync();
+    }
+    const int gtid = tid * csize, gsize = csize * nt;                  // this block is rank 0; rows dealt round-robin
     // warm start contacts, then joints' InitVelocityConstraints (b2island.d:133-146)
     if (njI == 0) {
-        if (warm) sweep(x.s_lvl_v + kx, maxLv, [&](int idx) { warm_start(unpack_v(load_v(vrow + idx)), sb); });
+        if (warm) cluster_levels(bs_.lvl_v, maxLv, gtid, gsize, clustered, [&](int idx) { big_warm_row(x, bs_, idx); });
     } else {
-        sweep(lvl_p + kx, maxLp, [&](int idx) {
-            const int item = sched_p[kx + idx];
-            if (item >= 0) { if (warm) warm_start(unpack_v(load_v(vrow + x.s_vpos[item])), sb); }
-            else joint_init(x, -item - 1, b0, sb, warm, dtRatio);
-        });
+        cluster_levels(bs_.lvl_p, maxLp, gtid, gsize, clustered, [&](int idx) { big_warm_row(x, bs_, idx); });
     }
     stampb(5);
     // velocity iterations (b2island.d:153-161)
-    for (int it = 0; it < x.vel_iters; ++it) {
-        sweep(x.s_lvl_v + kx, maxLv, [&](int idx) {
-            const VRow r = load_v(vrow + idx);
-            if (r.ids.w >= 0) {
-                if (it == 0 && (r.ids.z & 0x100)) {                      // a predicted start (ws mode 2)
-                    float4 im;
-                    solve_velocity_learned(r, sb, &im);
-                    vrow[idx].imp = im;
-                    return;
-                }
-                VC vc = unpack_v(r);
-                BodyVel q = load_vel(sb, vc.bodyA, vc.bodyB);
-                if (vc.pointCount == 2) solve_velocity_two(vc, q);
-                else solve_velocity(vc, q);
-                store_vel(sb, vc.bodyA, vc.bodyB, q);
-                vrow[idx].imp = make_float4(vc.p[0].normalImpulse, vc.p[0].tangentImpulse, vc.p[1].normalImpulse,
-                                            vc.p[1].tangentImpulse);
-            } else {
-                joint_solve_velocity(x, -r.ids.w - 1, b0, sb);
-            }
-        });
-    }
+    for (int it = 0; it < x.vel_iters; ++it)
+        cluster_levels(bs_.lvl_v, maxLv, gtid, gsize, clustered, [&](int idx) { big_vel_row(x, bs_, idx, it); });
     stampb(6);
     if (x.measure) {
         // one extra velocity sweep that changes nothing: velocities kept aside and put back,
@@ -5793,6 +5915,7 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
     }
     for (int is = tid; is < nIsl; is += nt) iflags[is] = 0;
     __syncthreads();
+    if (clustered) cluster_sync();                                     // positions integrated
     stampb(7);
     // position iterations with per-island early exit (b2island.d:206-224)
     for (int it = 0; it < x.pos_iters; ++it) {
@@ -5801,17 +5924,8 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
             iflags[is] &= ~4;
         }
         __syncthreads();
-        sweep(lvl_p + kx, maxLp, [&](int idx) {
-            const PRow r = load_p(prow + idx);
-            const int is = r.ids.w;
-            if (iflags[is] & 1) return;
-            if (r.ids.z >= 0) {
-                const float ms = solve_position_row(unpack_p(r), sb);
-                atomicMin(&iminsep[is], fkey(ms));
-            } else if (!joint_solve_position(x, -r.ids.z - 1, b0, sb)) {
-                atomicOr(&iflags[is], 4);
-            }
-        });
+        if (clustered) cluster_sync();
+        cluster_levels(bs_.lvl_p, maxLp, gtid, gsize, clustered, [&](int idx) { big_pos_row(x, bs_, idx); });
         int psolved = 0;
         bool remaining = false;
         for (int is = tid; is < nIsl; is += nt) {
@@ -5826,7 +5940,12 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
         auto isum = [](int a, int b) { return a + b; };
         psolved = block_reduce(psolved, isum, shi);
         if (tid == 0) wd.acc_psolve += (unsigned long long)psolved;
-        if (!__syncthreads_or(remaining)) break;
+        const bool go = __syncthreads_or(remaining) != 0;
+        if (clustered) {                                               // the other blocks follow
+            if (tid == 0) wd.sw_go = go ? 1 : 0;
+            cluster_sync();
+        }
+        if (!go) break;
     }
     __syncthreads();
     if (x.measure) {
@@ -5994,7 +6113,7 @@ __global__ void __launch_bounds__(kSolveWarps * 32, 3) k_solve_toi(const __grid_
         if (!x.wi[w].pair_block) toi_world(x, w, sbp);                   // large worlds: k_finish_big_block
         tsync();
         if (heavy && lane == 0) atomicExch(&x.solve_queue[2 + sub], 0);
-        if (x.prof && lane == 0) {
+        if (x.prof && lane == 0 && !(x.big_block && x.wi[w].pair_block)) {
             unsigned long long g1;
             asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(g1));
             x.prof[kProfSlots * (size_t)w + 25] = g0;
@@ -6030,13 +6149,31 @@ extern "C" int dbox_launch_collide(const dg::Ctx* x, cudaStream_t stream) {
     return (int)cudaGetLastError();
 }
 
+// a large world's Solve: a cluster of x->big_cluster blocks per world (the level sweeps spread
+// over them), or one block
+static void launch_solve_big(const dg::Ctx* x, cudaStream_t stream) {
+    const int c = x->big_cluster > 1 ? x->big_cluster : 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(x->n_big * c));
+    cfg.blockDim = dim3(dg::kBigThreads);
+    cfg.dynamicSmemBytes = x->ws_mode == 2 ? dg::kBigSmemInfer : 0;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)c;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = c > 1 ? 1 : 0;
+    cudaLaunchKernelEx(&cfg, dg::k_solve_big, *x);
+}
+
 // part 2 of a step: Solve and SolveTOI (1 launch, 3 or 4 with a large world); *launches = all of the step's
 // (part 1 is 3 launches, 5 with a large world)
 extern "C" int dbox_launch_solve(const dg::Ctx* x, cudaStream_t stream, int* launches) {
     if (x->solve_blocks < 1) return (int)cudaErrorInvalidValue;
     if (x->solve_queue) cudaMemsetAsync(x->solve_queue, 0, sizeof(int) * (2 + 4 * (size_t)x->solve_nsm), stream);
-    if (x->big_block)                               // large worlds' Solve
-        dg::k_solve_big<<<x->n_big, dg::kBigThreads, x->ws_mode == 2 ? dg::kBigSmemInfer : 0, stream>>>(*x);
+    if (x->big_block) launch_solve_big(x, stream);  // large worlds' Solve
     dg::k_solve_toi<<<x->solve_blocks, x->solve_wpb * dg::kWarp, x->solve_smem_floats * sizeof(float), stream>>>(*x);
     if (x->n_big > 0) {                             // large worlds: their pairs on a block each, then AddPair + TOI
         dg::k_pairs_block<<<x->n_big, dg::kPairThreads, 0, stream>>>(*x);
@@ -6061,8 +6198,7 @@ extern "C" int dbox_launch_step_ev(const dg::Ctx* x, cudaStream_t stream, int* l
     if (x->n_big > 0) dg::k_collide_finish_big<<<x->n_big, dg::kPairThreads, 0, stream>>>(*x);
     if (ev) cudaEventRecordWithFlags(ev[1], stream, cudaEventRecordExternal);
     if (x->solve_queue) cudaMemsetAsync(x->solve_queue, 0, sizeof(int) * (2 + 4 * (size_t)x->solve_nsm), stream);
-    if (x->big_block)                               // large worlds' Solve
-        dg::k_solve_big<<<x->n_big, dg::kBigThreads, x->ws_mode == 2 ? dg::kBigSmemInfer : 0, stream>>>(*x);
+    if (x->big_block) launch_solve_big(x, stream);  // large worlds' Solve
     dg::k_solve_toi<<<x->solve_blocks, x->solve_wpb * dg::kWarp, x->solve_smem_floats * sizeof(float), stream>>>(*x);
     if (x->n_big > 0) {                             // large worlds: their pairs on a block each, then AddPair + TOI
         dg::k_pairs_block<<<x->n_big, dg::kPairThreads, 0, stream>>>(*x);
@@ -6075,8 +6211,28 @@ extern "C" int dbox_launch_step_ev(const dg::Ctx* x, cudaStream_t stream, int* l
 }
 
 extern "C" const void* dbox_solve_kernel() { return reinterpret_cast<const void*>(&dg::k_solve_toi); }
-extern "C" int dbox_big_solve_init() {
-    return (int)cudaFuncSetAttribute(dg::k_solve_big, cudaFuncAttributeMaxDynamicSharedMemorySize, dg::kBigSmemInfer);
+// the largest cluster (8, 4, 2 or 1 blocks) that k_solve_big can run on this device
+extern "C" int dbox_big_solve_init(int* cluster) {
+    int rc = (int)cudaFuncSetAttribute(dg::k_solve_big, cudaFuncAttributeMaxDynamicSharedMemorySize, dg::kBigSmemInfer);
+    *cluster = 1;
+    if (rc) return rc;
+    for (int c = 8; c > 1; c /= 2) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)c);
+        cfg.blockDim = dim3(dg::kBigThreads);
+        cfg.dynamicSmemBytes = dg::kBigSmemInfer;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = (unsigned)c;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        int n = 0;
+        if (cudaOccupancyMaxActiveClusters(&n, dg::k_solve_big, &cfg) == cudaSuccess && n >= 1) { *cluster = c; break; }
+        cudaGetLastError();
+    }
+    return 0;
 }
 
 extern "C" int dbox_launch_step(const dg::Ctx* x, cudaStream_t stream, int* launches) {

@@ -66,6 +66,9 @@ struct WorldDyn {
     // ordinary and wide proxies, and whether it describes this step's boxes
     float g_ox, g_oy, g_inv;
     int g_ncx, g_ncy, g_nv, g_nwide, g_valid;
+    // a large world's Solve on a cluster: what its first block tells the others before the
+    // level sweeps (velocity / position levels, island joints) and after each position iteration
+    int sw_maxv, sw_maxp, sw_njI, sw_go;
 };
 
 struct BodyStatic {
@@ -225,6 +228,7 @@ struct Ctx {
     const int* big_worlds;         // the worlds whose end-of-Solve pairs a block generates
     int n_big;
     int big_block;                 // 1: large worlds run b2World.Solve on a block (k_solve_big), not a warp
+    int big_cluster;               // blocks per large world in k_solve_big's level sweeps (a thread-block cluster)
     const int* proxy_order;        // fixture-indexed: world-local fixture of each proxy-id rank
     // scratch (contact-indexed)
     int* s_cstate;                 // 0 processed, 1 inactive, 2 destroyed
