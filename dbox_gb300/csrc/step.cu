@@ -5379,48 +5379,6 @@ DG void cluster_levels(const int* lvl, int maxL, int gtid, int gsize, bool clust
         else __syncthreads();
     }
 }
-// The part of a large world's Solve the cluster's other blocks run: the same barriers in the
-// same order as the first block (published parameters after the first, the continue flag of
-// each position iteration after its check).
-DG void big_sweep_helper(const Ctx& x, int w, int crank, int csize) {
-    const WorldInfo& wi = x.wi[w];
-    WorldDyn& wd = x.wd[w];
-    const int b0 = wi.body_start, kx = wi.kx_start;
-    cluster_sync();                                                  // the rows are built
-    BigSweep s;
-    s.b0 = b0;
-    s.kx = kx;
-    s.vrow = x.vr + kx;
-    s.prow = x.pr + kx;
-    s.sb.p = x.s_sbody + 6 * (size_t)b0;
-    s.warm = x.warm_starting != 0;
-    s.dtRatio = wd.inv_dt0 * x.dt;
-    s.njI = ld_volatile_i(&wd.sw_njI);
-    s.maxLv = ld_volatile_i(&wd.sw_maxv);
-    s.maxLp = ld_volatile_i(&wd.sw_maxp);
-    s.lvl_v = x.s_lvl_v + kx;
-    s.lvl_p = (s.njI ? x.s_lvl_p : x.s_lvl_v) + kx;
-    s.sched_p = s.njI ? x.s_sched_p : x.s_sched_v;
-    s.iflags = x.s_isl_flags + b0;
-    s.iminsep = x.s_isl_minsep + b0;
-    // rows of a level dealt round-robin over the blocks (each block a share of every level)
-    const int gtid = (int)threadIdx.x * csize + crank, gsize = csize * (int)blockDim.x;
-    if (s.njI == 0) {
-        if (s.warm) cluster_levels(s.lvl_v, s.maxLv, gtid, gsize, true, [&](int idx) { big_warm_row(x, s, idx); });
-    } else {
-        cluster_levels(s.lvl_p, s.maxLp, gtid, gsize, true, [&](int idx) { big_warm_row(x, s, idx); });
-    }
-    for (int it = 0; it < x.vel_iters; ++it)
-        cluster_levels(s.lvl_v, s.maxLv, gtid, gsize, true, [&](int idx) { big_vel_row(x, s, idx, it); });
-    cluster_sync();                                                  // positions integrated
-    for (int it = 0; it < x.pos_iters; ++it) {
-        cluster_sync();                                              // this iteration's island marks reset
-        cluster_levels(s.lvl_p, s.maxLp, gtid, gsize, true, [&](int idx) { big_pos_row(x, s, idx); });
-        cluster_sync();                                              // the first block's check
-        if (!ld_volatile_i(&wd.sw_go)) break;
-    }
-}
-
 __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant__ Ctx x) {
     extern __shared__ __align__(16) float big_smem[];                  // ws mode 2: the inference staging
     __shared__ int shi[32];
@@ -5434,8 +5392,12 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
     WorldDyn& wd = x.wd[w];
     const int tid = threadIdx.x, nt = blockDim.x;
     if (!(wd.step_complete && x.dt > 0.0f)) return;                    // the same decision in every block
-    if (crank != 0) { big_sweep_helper(x, w, crank, csize); return; }
-    if (x.prof && tid == 0) {
+    // the first block (r0) runs the serial phases; the parallel ones are dealt round-robin over
+    // the cluster's threads, a cluster barrier (a block barrier without a cluster) between phases
+    const bool r0 = crank == 0;
+    const int gtid = tid * csize + crank, gsize = nt * csize;
+    auto csync = [&]() { if (clustered) cluster_sync(); else __syncthreads(); };
+    if (r0 && x.prof && tid == 0) {
         unsigned smid;
         asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
         x.prof[kProfSlots * (size_t)w + 27] = csize;
@@ -5448,9 +5410,9 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
     const float h = x.dt;
     const bool warm = x.warm_starting != 0;
     const float dtRatio = wd.inv_dt0 * x.dt;                            // b2world.d:392
-    auto stampb = [&](int slot) { if (x.prof && tid == 0) x.prof[kProfSlots * (size_t)w + slot] = clock64(); };
+    auto stampb = [&](int slot) { if (r0 && x.prof && tid == 0) x.prof[kProfSlots * (size_t)w + slot] = clock64(); };
     stampb(0);
-    if (x.measure && tid == 0) { wd.q_sumsq = 0.0f; wd.q_max = 0.0f; wd.q_points = 0; wd.q_minsep = 0.0f; }
+    if (r0 && x.measure && tid == 0) { wd.q_sumsq = 0.0f; wd.q_max = 0.0f; wd.q_points = 0; wd.q_minsep = 0.0f; }
     SB sb;
     sb.p = x.s_sbody + 6 * (size_t)b0;
     int* iflags = x.s_isl_flags + b0;
@@ -5465,7 +5427,7 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
     unsigned char* cvis = x.s_cvis + c0;
     int2* items = x.s_adj_items + 2 * (size_t)c0;
     // compact per-body / per-contact data; island flags cleared (b2world.d:944-957)
-    for (int i = tid; i < nb; i += nt) {
+    for (int i = gtid; i < nb; i += gsize) {
         dbox_body_state& B = x.bs[b0 + i];
         B.flags &= ~(uint32_t)kBodyIsland;
         bfl[i] = body_flag_byte(B);
@@ -5473,13 +5435,15 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
         sb_load(sb, i, B);
         adj[i] = 0;
     }
-    for (int k = tid; k < n; k += nt) {
+    for (int k = gtid; k < n; k += gsize) {
         x.ct[c0 + k].flags &= ~(uint32_t)kContactIsland;
         contact_compact(x, c0 + k, b0);
         cvis[k] = 0;
     }
-    for (int j = tid; j < nj; j += nt) x.jt[j0 + j].island_flag = 0;
-    __syncthreads();
+    for (int j = gtid; j < nj; j += gsize) x.jt[j0 + j].island_flag = 0;
+    csync();
+    int nIsl = 0, nbI = 0, ncI = 0, njI = 0, maxLv = 0, maxLp = 0, nItems = 0;
+    if (r0) {
     // contact edges of the island graph per body, newest contact first (b2world.d:1026-1062);
     // a static body's list is never walked (the search does not continue through it), so
     // it gets none
@@ -5558,7 +5522,7 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
         seedf[i] = seedmax[root[d]] == d ? 1 : 0;
     }
     __syncthreads();
-    const int nIsl = block_exclusive_scan(seedf, nb, shi);
+    nIsl = block_exclusive_scan(seedf, nb, shi);
     for (int i = tid; i < nb; i += nt) {
         const int d = nb - 1 - i;
         if (seedmax[root[d]] == d) { rid[root[d]] = seedf[i]; seed_of[seedf[i]] = d; }
@@ -5582,9 +5546,9 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
         if (d >= 0 && rid[root[d]] >= 0) atomicAdd(&cntj[rid[root[d]]], 1);
     }
     __syncthreads();
-    const int nbI = block_exclusive_scan(cntb, nIsl, shi);
-    const int ncI = block_exclusive_scan(cntc, nIsl, shi);
-    const int njI = block_exclusive_scan(cntj, nIsl, shi);
+    nbI = block_exclusive_scan(cntb, nIsl, shi);
+    ncI = block_exclusive_scan(cntc, nIsl, shi);
+    njI = block_exclusive_scan(cntj, nIsl, shi);
     if (tid == 0) { cntb[nIsl] = nbI; cntc[nIsl] = ncI; cntj[nIsl] = njI; wd.islands = nIsl; s_next = 0; }
     __syncthreads();
     // ---- each island's depth-first search (b2world.d:988-1076), an island per thread
@@ -5679,7 +5643,7 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
         }
         atomicMax(maxl, ml);
     };
-    const int nItems = ncI + njI;
+    nItems = ncI + njI;
     auto bucket = [&](int maxL, int* sched, int* lvl) {
         for (int l = tid; l <= maxL + 1; l += nt) lvl[kx + l] = 0;
         __syncthreads();
@@ -5696,20 +5660,16 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
     };
     for (int k = tid; k < nIsl; k += nt) walk(k, false, &s_maxv);
     __syncthreads();
-    const int maxLv = s_maxv;
+    maxLv = s_maxv;
     bucket(maxLv, x.s_sched_v, x.s_lvl_v);
-    int* sched_p = x.s_sched_v;
-    int* lvl_p = x.s_lvl_v;
-    int maxLp = maxLv;
+    maxLp = maxLv;
     if (njI) {
         for (int i = tid; i < nb; i += nt) last[i] = 0;
         __syncthreads();
         for (int k = tid; k < nIsl; k += nt) walk(k, true, &s_maxp);
         __syncthreads();
         maxLp = s_maxp;
-        sched_p = x.s_sched_p;
-        lvl_p = x.s_lvl_p;
-        bucket(maxLp, sched_p, lvl_p);
+        bucket(maxLp, x.s_sched_p, x.s_lvl_p);
     }
     if (x.prof && tid == 0) { x.prof[kProfSlots * (size_t)w + 12] = maxLv; x.prof[kProfSlots * (size_t)w + 13] = n; x.prof[kProfSlots * (size_t)w + 14] = nb; }
     stampb(3);
@@ -5717,15 +5677,31 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
         wd.acc_isl_bodies += (unsigned long long)nbI;
         wd.acc_isl_contacts += (unsigned long long)ncI;
         wd.acc_vsolve += (unsigned long long)ncI * (unsigned long long)x.vel_iters;
+        // what the other blocks of the cluster need
+        wd.sw_maxv = maxLv; wd.sw_maxp = maxLp; wd.sw_njI = njI;
+        wd.sw_nisl = nIsl; wd.sw_nbi = nbI; wd.sw_nci = ncI; wd.sw_npend = 0;
     }
+    }                                                                    // r0
+    csync();
+    if (!r0) {
+        maxLv = ld_volatile_i(&wd.sw_maxv);
+        maxLp = ld_volatile_i(&wd.sw_maxp);
+        njI = ld_volatile_i(&wd.sw_njI);
+        nIsl = ld_volatile_i(&wd.sw_nisl);
+        nbI = ld_volatile_i(&wd.sw_nbi);
+        ncI = ld_volatile_i(&wd.sw_nci);
+        nItems = ncI + njI;
+    }
+    int* sched_p = njI ? x.s_sched_p : x.s_sched_v;
+    int* lvl_p = njI ? x.s_lvl_p : x.s_lvl_v;
     // island flags and SetAwake(true) of the search (b2world.d:985-1004), applied after it
-    for (int i = tid; i < nb; i += nt) {
+    for (int i = gtid; i < nb; i += gsize) {
         dbox_body_state& B = x.bs[b0 + i];
         if ((bfl[i] & kBfVisited) && !(bfl[i] & kBfStatic)) B.flags |= kBodyIsland;
         if (body_island[i] >= 0) b_set_awake(B, true);
     }
     // integrate velocities (b2island.d:82-116)
-    for (int t = tid; t < nbI; t += nt) {
+    for (int t = gtid; t < nbI; t += gsize) {
         const int i = isl_body[t];
         dbox_body_state& B = x.bs[b0 + i];
         B.sweep[2] = B.sweep[4];
@@ -5743,14 +5719,12 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
             sb.set_v(i, v, wv);
         }
     }
-    __syncthreads();
+    csync();
     // constraint rows in schedule order (b2contactsolver.d:244-450), with the warm-start modes'
     // part of each contact row; rows waiting for a prediction listed in s_pend
     VRow* vrow = x.vr + kx;
     PRow* prow = x.pr + kx;
-    if (tid == 0) s_next = 0;
-    __syncthreads();
-    for (int idx = tid; idx < nItems; idx += nt) {
+    for (int idx = gtid; idx < nItems; idx += gsize) {
         const int item = x.s_sched_v[kx + idx];
         bool pdone = false;
         if (item >= 0) {
@@ -5761,7 +5735,7 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
             constraint_init_velocity(vc, pc, sb, sep);
             VRow vr = pack_v(vc, item);
             if (x.ws_mode && row_start_modes(x, item, kx + idx, vc, pc, sep, sb, h, vr))
-                x.s_pend[c0 + atomicAdd(&s_next, 1)] = idx;
+                x.s_pend[c0 + atomicAdd(&wd.sw_npend, 1)] = idx;
             vrow[idx] = vr;
             if (njI || x.record_events) x.s_vpos[item] = idx;
             if (!njI) {
@@ -5785,17 +5759,17 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
             }
         }
     }
-    __syncthreads();
+    csync();
     if (x.ws_mode == 2) {
-        // predicted starts, 16 pending rows per tensor-core pass, kInferWarps warps
-        const int npend = s_next;
+        // predicted starts, 16 pending rows per tensor-core pass, kInferWarps warps of the first block
         const int warp = tid >> 5;
-        if (warp < kInferWarps) {
+        if (r0 && warp < kInferWarps) {
+            const int npend = ld_volatile_i(&wd.sw_npend);
             __nv_bfloat16* X = reinterpret_cast<__nv_bfloat16*>(big_smem) + (size_t)warp * kInferStage;
             for (int p0 = 16 * warp; p0 < npend; p0 += 16 * kInferWarps)
                 infer_pending16(x, x.s_pend + c0, p0, npend, vrow, X, X + 16 * kFeat, X + 16 * kFeat + 16 * kHid);
         }
-        __syncthreads();
+        csync();
     }
     stampb(4);
     auto sweep = [&](const int* lvl, int maxL, auto&& f) {             // levels in order over the block
@@ -5821,11 +5795,6 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
     bs_.sched_p = sched_p;
     bs_.iflags = iflags;
     bs_.iminsep = iminsep;
-    if (clustered) {                                                   // the other blocks' parameters
-        if (tid == 0) { wd.sw_maxv = maxLv; wd.sw_maxp = maxLp; wd.sw_njI = njI; }
-        cluster_sync();
-    }
-    const int gtid = tid * csize, gsize = csize * nt;                  // this block is rank 0; rows dealt round-robin
     // warm start contacts, then joints' InitVelocityConstraints (b2island.d:133-146)
     if (njI == 0) {
         if (warm) cluster_levels(bs_.lvl_v, maxLv, gtid, gsize, clustered, [&](int idx) { big_warm_row(x, bs_, idx); });
@@ -5837,7 +5806,7 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
     for (int it = 0; it < x.vel_iters; ++it)
         cluster_levels(bs_.lvl_v, maxLv, gtid, gsize, clustered, [&](int idx) { big_vel_row(x, bs_, idx, it); });
     stampb(6);
-    if (x.measure) {
+    if (x.measure && r0) {
         // one extra velocity sweep that changes nothing: velocities kept aside and put back,
         // impulses not written, joints left out
         for (int t = tid; t < nbI; t += nt) {
@@ -5880,7 +5849,8 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
         }
         __syncthreads();
     }
-    for (int idx = tid; idx < nItems; idx += nt) {                       // StoreImpulses (b2contactsolver.d:774-787)
+    if (x.measure) csync();
+    for (int idx = gtid; idx < nItems; idx += gsize) {                   // StoreImpulses (b2contactsolver.d:774-787)
         const VRow r = load_v(vrow + idx);
         if (r.ids.w >= 0) store_impulses(x, r);
         if (x.ws_mode == 1) {                                            // a logged sample's targets
@@ -5892,7 +5862,7 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
         }
     }
     // integrate positions (b2island.d:168-200)
-    for (int t = tid; t < nbI; t += nt) {
+    for (int t = gtid; t < nbI; t += gsize) {
         const int i = isl_body[t];
         float2 c = sb.c(i);
         float a = sb.a(i);
@@ -5913,19 +5883,19 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
         sb.set_c(i, c, a);
         sb.set_v(i, v, wv);
     }
-    for (int is = tid; is < nIsl; is += nt) iflags[is] = 0;
-    __syncthreads();
-    if (clustered) cluster_sync();                                     // positions integrated
+    for (int is = gtid; is < nIsl; is += gsize) iflags[is] = 0;
+    csync();                                                           // positions integrated
     stampb(7);
     // position iterations with per-island early exit (b2island.d:206-224)
     for (int it = 0; it < x.pos_iters; ++it) {
-        for (int is = tid; is < nIsl; is += nt) {
+        for (int is = gtid; is < nIsl; is += gsize) {
             iminsep[is] = fkey(0.0f);
             iflags[is] &= ~4;
         }
-        __syncthreads();
-        if (clustered) cluster_sync();
+        csync();
         cluster_levels(bs_.lvl_p, maxLp, gtid, gsize, clustered, [&](int idx) { big_pos_row(x, bs_, idx); });
+        bool go = false;
+        if (r0) {                                                      // the islands' checks
         int psolved = 0;
         bool remaining = false;
         for (int is = tid; is < nIsl; is += nt) {
@@ -5940,15 +5910,15 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
         auto isum = [](int a, int b) { return a + b; };
         psolved = block_reduce(psolved, isum, shi);
         if (tid == 0) wd.acc_psolve += (unsigned long long)psolved;
-        const bool go = __syncthreads_or(remaining) != 0;
-        if (clustered) {                                               // the other blocks follow
-            if (tid == 0) wd.sw_go = go ? 1 : 0;
-            cluster_sync();
-        }
+        go = __syncthreads_or(remaining) != 0;
+        if (tid == 0) wd.sw_go = go ? 1 : 0;
+        }                                                              // r0
+        csync();
+        if (!r0) go = ld_volatile_i(&wd.sw_go) != 0;
         if (!go) break;
     }
-    __syncthreads();
-    if (x.measure) {
+    csync();
+    if (x.measure && r0) {
         float ms = 0.0f;
         for (int idx = tid; idx < nItems; idx += nt) {
             const PRow r = load_p(prow + idx);
@@ -5958,7 +5928,7 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
         ms = block_reduce(ms, fmn, shf);
         if (tid == 0) wd.q_minsep = ms;
     }
-    if (x.record_events) {
+    if (x.record_events && r0) {
         // b2Island.Report (b2island.d:419-438): PostSolve per island contact in island order
         const int e0 = wd.ev_count;
         for (int t = tid; t < ncI; t += nt) {
@@ -5973,7 +5943,7 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
     stampb(8);
     // copy back + SynchronizeTransform (b2island.d:227-235)
     bool nonfinite = false;
-    for (int t = tid; t < nbI; t += nt) {
+    for (int t = gtid; t < nbI; t += gsize) {
         const int i = isl_body[t];
         dbox_body_state& B = x.bs[b0 + i];
         const float2 c = sb.c(i), v = sb.v(i);
@@ -5983,14 +5953,15 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
         nonfinite |= !(isfinite(c.x) && isfinite(c.y) && isfinite(B.sweep[7]) && isfinite(v.x) && isfinite(v.y) &&
                        isfinite(B.vel[2]));
     }
-    if (__syncthreads_or(nonfinite) && tid == 0) set_error(x, w, DBOX_ERR_NAN);
+    if (nonfinite) set_error(x, w, DBOX_ERR_NAN);
+    csync();
     // sleep (b2island.d:241-279)
     if (x.allow_sleep) {
         const float linTolSqr = kLinearSleepTolerance * kLinearSleepTolerance;
         const float angTolSqr = kAngularSleepTolerance * kAngularSleepTolerance;
-        for (int is = tid; is < nIsl; is += nt) x.s_isl_sleep[b0 + is] = fkey(kMaxFloat);
-        __syncthreads();
-        for (int t = tid; t < nbI; t += nt) {
+        for (int is = gtid; is < nIsl; is += gsize) x.s_isl_sleep[b0 + is] = fkey(kMaxFloat);
+        csync();
+        for (int t = gtid; t < nbI; t += gsize) {
             const int i = isl_body[t];
             dbox_body_state& B = x.bs[b0 + i];
             const int is = body_island[i];
@@ -6002,23 +5973,22 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
                 atomicMin(&x.s_isl_sleep[b0 + is], fkey(B.sleep_time));
             }
         }
-        __syncthreads();
-        for (int is = tid; is < nIsl; is += nt) {
+        csync();
+        for (int is = gtid; is < nIsl; is += gsize) {
             const int f = iflags[is];
             if (funkey(x.s_isl_sleep[b0 + is]) >= kTimeToSleep && (f & 2)) iflags[is] = f | 8;
         }
-        __syncthreads();
-        for (int t = tid; t < nbI; t += nt) {
+        csync();
+        for (int t = gtid; t < nbI; t += gsize) {
             const int i = isl_body[t];
             if (iflags[body_island[i]] & 8) b_set_awake(x.bs[b0 + i], false);
         }
         // a static body ends in the state its last island left it in
-        for (int i = tid; i < nb; i += nt) {
+        for (int i = gtid; i < nb; i += gsize) {
             if ((bfl[i] & kBfStatic) && body_island[i] >= 0 && (iflags[body_island[i]] & 8))
                 b_set_awake(x.bs[b0 + i], false);
         }
     }
-    __syncthreads();
     stampb(9);
     stampb(10);
     stampb(11);

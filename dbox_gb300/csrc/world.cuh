@@ -66,9 +66,10 @@ struct WorldDyn {
     // ordinary and wide proxies, and whether it describes this step's boxes
     float g_ox, g_oy, g_inv;
     int g_ncx, g_ncy, g_nv, g_nwide, g_valid;
-    // a large world's Solve on a cluster: what its first block tells the others before the
-    // level sweeps (velocity / position levels, island joints) and after each position iteration
-    int sw_maxv, sw_maxp, sw_njI, sw_go;
+    // a large world's Solve on a cluster: what its first block tells the others after the island
+    // search (levels, island joints, islands, island bodies and contacts), the count of rows
+    // waiting for a prediction, and the continue flag of each position iteration
+    int sw_maxv, sw_maxp, sw_njI, sw_go, sw_nisl, sw_nbi, sw_nci, sw_npend;
 };
 
 struct BodyStatic {
