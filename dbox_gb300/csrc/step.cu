@@ -822,6 +822,14 @@ __device__ __noinline__ void find_new_contacts(const Ctx& x, int w) {
 // least as large as any ordinary proxy) by a counting sort whose order inside a cell does not
 // matter (each proxy's partners are sorted by rank), the wide ones into a list every proxy
 // tests; partner counts, a block scan, then the fill.
+// ---- thread-block clusters (a large world's block and its helpers)
+DG unsigned cluster_rank() { unsigned r; asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r)); return r; }
+DG unsigned cluster_blocks() { unsigned r; asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r)); return r; }
+// every thread of every block of the cluster arrives (release) and waits (acquire): the
+// global-memory writes made before it by any block are seen by the loads made after it
+DG void cluster_sync() { asm volatile("barrier.cluster.arrive;\n\tbarrier.cluster.wait;" ::: "memory"); }
+DG int ld_volatile_i(const int* p) { return *reinterpret_cast<const volatile int*>(p); }
+
 constexpr int kPairThreads = 1024;
 
 template <class T, class Op>
@@ -873,32 +881,37 @@ DG void sync_fixtures(const Ctx& x, int b);
 // wd.pair_total).  At the end of Solve (b2world.d:1099-1120) after SynchronizeFixtures of the
 // island bodies; at the start of a step (`at_begin`: FindNewContacts after fixtures were
 // created, b2world.d:372-376) with the proxies as they stand.
-DG void pairs_block(const Ctx& x, int w, bool at_begin, float* shf, int* shi, int& n_wide) {
+DG void pairs_block(const Ctx& x, int w, bool at_begin, float* shf, int* shi, int csize, int crank) {
     const WorldInfo& wi = x.wi[w];
     WorldDyn& wd = x.wd[w];
     const int tid = threadIdx.x, nt = blockDim.x;
+    // with a cluster (csize > 1) every block takes its round-robin share of the passes, the
+    // first block the scans; block partials of the reductions are combined in block order
+    const bool clustered = csize > 1, r0 = crank == 0;
+    const int gtid = tid * csize + crank, gsize = nt * csize;
+    auto csync = [&]() { if (clustered) cluster_sync(); else __syncthreads(); };
     const long long t_in = clock64();
-    auto prof_out = [&]() { if (x.prof && tid == 0 && !at_begin) x.prof[kProfSlots * (size_t)w + 30] = clock64() - t_in; };
+    auto prof_out = [&]() { if (r0 && x.prof && tid == 0 && !at_begin) x.prof[kProfSlots * (size_t)w + 30] = clock64() - t_in; };
     if (!at_begin && (!(wd.step_complete && x.dt > 0.0f) || wd.error != 0)) {   // Solve did not reach its broad-phase
-        if (tid == 0) { wd.pair_total = 0; wd.g_valid = 0; }
+        if (r0 && tid == 0) { wd.pair_total = 0; wd.g_valid = 0; }
         prof_out();
         return;
     }
     // SynchronizeFixtures of the island bodies (b2world.d:1099-1116), the solve's last step
     if (!at_begin)
-        for (int i = tid; i < wi.body_count; i += nt) {
+        for (int i = gtid; i < wi.body_count; i += gsize) {
             const int b = wi.body_start + i;
             if ((x.bs[b].flags & kBodyIsland) == 0 || x.bs[b].type == kStaticBody) continue;
             sync_fixtures(x, b);
         }
     // the contact pair table, rebuilt from the live contacts (hash_rebuild)
-    for (int i = tid; i < wi.hash_cap; i += nt) x.hash[wi.hash_start + i] = kHashEmpty;
-    __syncthreads();
-    for (int k = tid; k < wd.contact_count; k += nt) {
+    for (int i = gtid; i < wi.hash_cap; i += gsize) x.hash[wi.hash_start + i] = kHashEmpty;
+    csync();
+    for (int k = gtid; k < wd.contact_count; k += gsize) {
         const dbox_contact_state& c = x.ct[wi.contact_start + k];
         hash_insert(x, wi, pair_key(c.fixture_a, c.fixture_b));
     }
-    __syncthreads();
+    csync();
     const int f0 = wi.fix_start, nf = wi.fix_count;
     const int* ord = wi.proxy_order ? x.proxy_order + f0 : nullptr;
     auto PX = [ord](int r) { return ord ? ord[r] : r; };
@@ -910,7 +923,8 @@ DG void pairs_block(const Ctx& x, int w, bool at_begin, float* shf, int* shi, in
     // live proxies, moved ones, mean extent (the wide cut of sap_build)
     int cnt = 0, nm = 0;
     float sum = 0.0f;
-    for (int r = tid; r < nf; r += nt) {
+    int* part = x.s_pcount + f0;                                         // 16 partials per block (cluster)
+    for (int r = gtid; r < nf; r += gsize) {
         const dbox_proxy_state& p = x.px[f0 + PX(r)];
         if (p.proxy_id < 0) continue;
         ++cnt;
@@ -920,15 +934,25 @@ DG void pairs_block(const Ctx& x, int w, bool at_begin, float* shf, int* shi, in
     cnt = block_reduce(cnt, isum, shi);
     nm = block_reduce(nm, isum, shi);
     sum = block_reduce(sum, fsum, shf);
+    if (clustered) {
+        if (tid == 0) { part[16 * crank] = cnt; part[16 * crank + 1] = nm; part[16 * crank + 2] = __float_as_int(sum); }
+        cluster_sync();
+        cnt = 0; nm = 0; sum = 0.0f;
+        for (int q = 0; q < csize; ++q) {
+            cnt += ld_volatile_i(&part[16 * q]);
+            nm += ld_volatile_i(&part[16 * q + 1]);
+            sum += __int_as_float(ld_volatile_i(&part[16 * q + 2]));
+        }
+    }
     if (nm == 0 && !x.continuous) {                                     // no pairs, and no SolveTOI to serve
-        if (tid == 0) { wd.pair_total = 0; wd.g_valid = 0; }
+        if (r0 && tid == 0) { wd.pair_total = 0; wd.g_valid = 0; }
         prof_out();
         return;
     }
     const float cut = 4.0f * sum / (float)(cnt > 0 ? cnt : 1);
     float ext = 0.0f, lo0 = 3.4e38f, lo1 = 3.4e38f, hi0 = -3.4e38f, hi1 = -3.4e38f;
     int nv = 0;
-    for (int r = tid; r < nf; r += nt) {
+    for (int r = gtid; r < nf; r += gsize) {
         const dbox_proxy_state& p = x.px[f0 + PX(r)];
         if (p.proxy_id < 0 || extent(p) > cut) continue;
         ++nv;
@@ -944,6 +968,26 @@ DG void pairs_block(const Ctx& x, int w, bool at_begin, float* shf, int* shi, in
     lo1 = block_reduce(lo1, fmn, shf);
     hi0 = block_reduce(hi0, fmx, shf);
     hi1 = block_reduce(hi1, fmx, shf);
+    if (clustered) {
+        if (tid == 0) {
+            part[16 * crank + 3] = nv;
+            part[16 * crank + 4] = __float_as_int(ext);
+            part[16 * crank + 5] = __float_as_int(lo0);
+            part[16 * crank + 6] = __float_as_int(lo1);
+            part[16 * crank + 7] = __float_as_int(hi0);
+            part[16 * crank + 8] = __float_as_int(hi1);
+        }
+        cluster_sync();
+        nv = 0;
+        for (int q = 0; q < csize; ++q) {
+            nv += ld_volatile_i(&part[16 * q + 3]);
+            ext = bmax(ext, __int_as_float(ld_volatile_i(&part[16 * q + 4])));
+            lo0 = bmin(lo0, __int_as_float(ld_volatile_i(&part[16 * q + 5])));
+            lo1 = bmin(lo1, __int_as_float(ld_volatile_i(&part[16 * q + 6])));
+            hi0 = bmax(hi0, __int_as_float(ld_volatile_i(&part[16 * q + 7])));
+            hi1 = bmax(hi1, __int_as_float(ld_volatile_i(&part[16 * q + 8])));
+        }
+    }
     // the grid (as sap_build sizes it)
     Sap s;
     float cellsz = ext > 1e-6f ? ext * 1.001f : 1.0f;
@@ -970,14 +1014,15 @@ DG void pairs_block(const Ctx& x, int w, bool at_begin, float* shf, int* shi, in
     int* sidx = x.s_sapi[1] + f0;                                        // ordinary proxies by cell
     int* wide = x.s_sapi[0] + f0;                                        // wide proxies
     float4* box = x.s_sapbox + f0;                                       // their boxes, the wide ones after nv
-    for (int c = tid; c <= ncell; c += nt) cstart[c] = 0;
-    if (tid == 0) n_wide = 0;
-    __syncthreads();
-    for (int r = tid; r < nf; r += nt) {                                 // counts per cell; the wide list
+    for (int c = gtid; c <= ncell; c += gsize) cstart[c] = 0;
+    int* n_wide = &wd.g_nwide;                                           // counted here, then kept for SolveTOI
+    if (r0 && tid == 0) *n_wide = 0;
+    csync();
+    for (int r = gtid; r < nf; r += gsize) {                             // counts per cell; the wide list
         const dbox_proxy_state& p = x.px[f0 + PX(r)];
         if (p.proxy_id < 0) continue;
         if (extent(p) > cut) {
-            const int k = atomicAdd(&n_wide, 1);
+            const int k = atomicAdd(n_wide, 1);
             wide[k] = p.moved ? (r | (int)0x80000000) : r;
             box[nv + k] = make_float4(p.fat_aabb[0], p.fat_aabb[1], p.fat_aabb[2], p.fat_aabb[3]);
         } else {
@@ -985,11 +1030,12 @@ DG void pairs_block(const Ctx& x, int w, bool at_begin, float* shf, int* shi, in
             atomicAdd(&cstart[cy * s.ncx + cx], 1);
         }
     }
-    __syncthreads();
-    block_exclusive_scan(cstart, ncell + 1, shi);
-    for (int c = tid; c < ncell; c += nt) cursor[c] = cstart[c];
-    __syncthreads();
-    for (int r = tid; r < nf; r += nt) {                                 // counting-sort scatter
+    csync();
+    if (r0) block_exclusive_scan(cstart, ncell + 1, shi);
+    csync();
+    for (int c = gtid; c < ncell; c += gsize) cursor[c] = cstart[c];
+    csync();
+    for (int r = gtid; r < nf; r += gsize) {                             // counting-sort scatter
         const dbox_proxy_state& p = x.px[f0 + PX(r)];
         if (p.proxy_id < 0 || extent(p) > cut) continue;
         const int cx = sap_cell(p.fat_aabb[0], s.ox, s.inv, s.ncx), cy = sap_cell(p.fat_aabb[1], s.oy, s.inv, s.ncy);
@@ -997,20 +1043,21 @@ DG void pairs_block(const Ctx& x, int w, bool at_begin, float* shf, int* shi, in
         sidx[slot] = p.moved ? (r | (int)0x80000000) : r;
         box[slot] = make_float4(p.fat_aabb[0], p.fat_aabb[1], p.fat_aabb[2], p.fat_aabb[3]);
     }
-    __syncthreads();
+    csync();
+    const int nwd = ld_volatile_i(n_wide);
     s.key = nullptr;
     s.box = box;
     s.idx = sidx;
     s.n = nv;
     s.wide = wide;
-    s.nwide = n_wide;
+    s.nwide = nwd;
     s.cstart = cstart;
-    if (tid == 0) {                                                      // the grid, for SolveTOI's pair searches
+    if (r0 && tid == 0) {                                                // the grid, for SolveTOI's pair searches
         wd.g_ox = s.ox; wd.g_oy = s.oy; wd.g_inv = s.inv;
-        wd.g_ncx = s.ncx; wd.g_ncy = s.ncy; wd.g_nv = nv; wd.g_nwide = n_wide; wd.g_valid = 1;
+        wd.g_ncx = s.ncx; wd.g_ncy = s.ncy; wd.g_nv = nv; wd.g_valid = 1;
     }
     if (nm == 0) {
-        if (tid == 0) wd.pair_total = 0;
+        if (r0 && tid == 0) wd.pair_total = 0;
         prof_out();
         return;
     }
@@ -1021,10 +1068,9 @@ DG void pairs_block(const Ctx& x, int w, bool at_begin, float* shf, int* shi, in
     // offsets, then the same passes fill the segments and each segment is sorted by partner.
     int* pcount = x.s_pcount + f0;
     int* pcur = x.s_moved + f0;
-    const int nwd = n_wide;
     // rows of cells per wide proxy, for the row jobs
     int* wrow = x.s_sapi[0] + f0 + nwd;                                  // nwd + 1 entries after the wide list
-    for (int q = tid; q <= nwd; q += nt) {
+    for (int q = gtid; q <= nwd; q += gsize) {
         int rows = 0;
         if (q < nwd) {
             const float4 wb = box[nv + q];
@@ -1033,8 +1079,10 @@ DG void pairs_block(const Ctx& x, int w, bool at_begin, float* shf, int* shi, in
         }
         wrow[q] = rows;
     }
-    __syncthreads();
-    const int njobs = block_exclusive_scan(wrow, nwd + 1, shi);
+    csync();
+    if (r0) block_exclusive_scan(wrow, nwd + 1, shi);
+    csync();
+    const int njobs = ld_volatile_i(&wrow[nwd]);
     auto wide_row = [&](int job, auto&& emit) {                          // job: one row of one wide proxy
         int q = 0, lo = 0, hi = nwd;                                     // the last q with wrow[q] <= job
         while (lo < hi) {
@@ -1086,25 +1134,30 @@ DG void pairs_block(const Ctx& x, int w, bool at_begin, float* shf, int* shi, in
     };
     Sap sc = s;                                                          // the cells alone
     sc.nwide = 0;
-    for (int a = tid; a < nf; a += nt) {
+    for (int a = gtid; a < nf; a += gsize) {
         int c = 0;
         const dbox_proxy_state& p = x.px[f0 + PX(a)];
         if (p.proxy_id >= 0 && extent(p) <= cut)
             sap_partners(sc, proxy_fat(x, f0 + PX(a)), a, p.moved != 0, [&](int) { ++c; });
         pcount[a] = c;
     }
-    __syncthreads();
-    for (int job = tid; job < njobs; job += nt) wide_row(job, [&](int own, int) { atomicAdd(&pcount[own], 1); });
-    for (int q = tid; q < nwd; q += nt) wide_wide(q, [&](int own, int) { atomicAdd(&pcount[own], 1); });
-    __syncthreads();
-    const int total = block_exclusive_scan(pcount, nf, shi);
+    csync();
+    for (int job = gtid; job < njobs; job += gsize) wide_row(job, [&](int own, int) { atomicAdd(&pcount[own], 1); });
+    for (int q = gtid; q < nwd; q += gsize) wide_wide(q, [&](int own, int) { atomicAdd(&pcount[own], 1); });
+    csync();
+    if (r0) {
+        const int t = block_exclusive_scan(pcount, nf, shi);
+        if (tid == 0) wd.pair_total = t;
+    }
+    csync();
+    const int total = ld_volatile_i(&wd.pair_total);
     if (total > wi.pair_cap) {
-        if (tid == 0) { set_error(x, w, DBOX_ERR_CAPACITY); wd.pair_total = 0; }
+        if (r0 && tid == 0) { set_error(x, w, DBOX_ERR_CAPACITY); wd.pair_total = 0; }
         prof_out();
         return;
     }
     int2* seg0 = x.pairs + wi.pair_start;
-    for (int a = tid; a < nf; a += nt) {                                 // ordinary partners first
+    for (int a = gtid; a < nf; a += gsize) {                             // ordinary partners first
         const dbox_proxy_state& p = x.px[f0 + PX(a)];
         int c = 0;
         if (p.proxy_id >= 0 && extent(p) <= cut) {
@@ -1113,12 +1166,12 @@ DG void pairs_block(const Ctx& x, int w, bool at_begin, float* shf, int* shi, in
         }
         pcur[a] = pcount[a] + c;
     }
-    __syncthreads();
+    csync();
     auto put = [&](int own, int other) { seg0[atomicAdd(&pcur[own], 1)] = make_int2(own, other); };
-    for (int job = tid; job < njobs; job += nt) wide_row(job, put);
-    for (int q = tid; q < nwd; q += nt) wide_wide(q, put);
-    __syncthreads();
-    for (int a = tid; a < nf; a += nt) {                                 // each segment by partner rank
+    for (int job = gtid; job < njobs; job += gsize) wide_row(job, put);
+    for (int q = gtid; q < nwd; q += gsize) wide_wide(q, put);
+    csync();
+    for (int a = gtid; a < nf; a += gsize) {                             // each segment by partner rank
         int2* seg = seg0 + pcount[a];
         const int d = (a + 1 < nf ? pcount[a + 1] : total) - pcount[a];
         int gap = 1;
@@ -1132,20 +1185,18 @@ DG void pairs_block(const Ctx& x, int w, bool at_begin, float* shf, int* shi, in
             }
         for (int i = 0; i < d; ++i) seg[i] = make_int2(f0 + PX(seg[i].x), f0 + PX(seg[i].y));
     }
-    __syncthreads();
-    for (int i = tid; i < nf; i += nt) x.px[f0 + i].moved = 0;          // the move buffer is consumed
-    if (tid == 0) {
-        wd.acc_pairs += (unsigned long long)total;
-        wd.pair_total = total;
-    }
+    csync();
+    for (int i = gtid; i < nf; i += gsize) x.px[f0 + i].moved = 0;      // the move buffer is consumed
+    if (r0 && tid == 0) wd.acc_pairs += (unsigned long long)total;
     prof_out();
 }
 
 __global__ void __launch_bounds__(kPairThreads) k_pairs_block(const __grid_constant__ Ctx x) {
     __shared__ float shf[32];
     __shared__ int shi[32];
-    __shared__ int n_wide;
-    pairs_block(x, x.big_worlds[blockIdx.x], false, shf, shi, n_wide);
+    const int csize = x.big_cluster > 1 ? (int)cluster_blocks() : 1;
+    const int crank = csize > 1 ? (int)cluster_rank() : 0;
+    pairs_block(x, x.big_worlds[blockIdx.x / csize], false, shf, shi, csize, crank);
 }
 
 // FindNewContacts of a large world whose fixtures were just created (e_newFixture), on its
@@ -1153,7 +1204,6 @@ __global__ void __launch_bounds__(kPairThreads) k_pairs_block(const __grid_const
 __global__ void __launch_bounds__(kPairThreads) k_begin_big(const __grid_constant__ Ctx x) {
     __shared__ float shf[32];
     __shared__ int shi[32];
-    __shared__ int n_wide;
     __shared__ unsigned s_bal[32];
     __shared__ int s_box[2];
     __shared__ float s_ra[32];
@@ -1161,7 +1211,7 @@ __global__ void __launch_bounds__(kPairThreads) k_begin_big(const __grid_constan
     __shared__ int s_aux[4];
     const int w = x.big_worlds[blockIdx.x];
     if (!(x.wd[w].flags & 1u)) return;
-    pairs_block(x, w, true, shf, shi, n_wide);
+    pairs_block(x, w, true, shf, shi, 1, 0);
     __syncthreads();
     BlockTeam tm{s_bal, s_box, s_ra, s_rl, nullptr, s_aux};
     const int total = x.wd[w].pair_total;
@@ -5307,12 +5357,6 @@ DG void uf_union(int* parent, int a, int b) {
 }
 
 // ---- the level sweeps of a large world's Solve, spread over a thread-block cluster
-DG unsigned cluster_rank() { unsigned r; asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r)); return r; }
-DG unsigned cluster_blocks() { unsigned r; asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r)); return r; }
-// every thread of every block of the cluster arrives (release) and waits (acquire): the
-// global-memory writes made before it by any block are seen by the loads made after it
-DG void cluster_sync() { asm volatile("barrier.cluster.arrive;\n\tbarrier.cluster.wait;" ::: "memory"); }
-DG int ld_volatile_i(const int* p) { return *reinterpret_cast<const volatile int*>(p); }
 
 // What a row of a sweep needs (the same for every block of the cluster)
 struct BigSweep {
@@ -6119,14 +6163,15 @@ extern "C" int dbox_launch_collide(const dg::Ctx* x, cudaStream_t stream) {
     return (int)cudaGetLastError();
 }
 
-// a large world's Solve: a cluster of x->big_cluster blocks per world (the level sweeps spread
-// over them), or one block
-static void launch_solve_big(const dg::Ctx* x, cudaStream_t stream) {
+// a large-world kernel on a cluster of x->big_cluster blocks per world (its passes spread over
+// them), or on one block
+template <class K>
+static void launch_big(K kernel, const dg::Ctx* x, unsigned threads, size_t smem, cudaStream_t stream) {
     const int c = x->big_cluster > 1 ? x->big_cluster : 1;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)(x->n_big * c));
-    cfg.blockDim = dim3(dg::kBigThreads);
-    cfg.dynamicSmemBytes = x->ws_mode == 2 ? dg::kBigSmemInfer : 0;
+    cfg.blockDim = dim3(threads);
+    cfg.dynamicSmemBytes = smem;
     cfg.stream = stream;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -6135,7 +6180,10 @@ static void launch_solve_big(const dg::Ctx* x, cudaStream_t stream) {
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = c > 1 ? 1 : 0;
-    cudaLaunchKernelEx(&cfg, dg::k_solve_big, *x);
+    cudaLaunchKernelEx(&cfg, kernel, *x);
+}
+static void launch_solve_big(const dg::Ctx* x, cudaStream_t stream) {
+    launch_big(dg::k_solve_big, x, dg::kBigThreads, x->ws_mode == 2 ? dg::kBigSmemInfer : 0, stream);
 }
 
 // part 2 of a step: Solve and SolveTOI (1 launch, 3 or 4 with a large world); *launches = all of the step's
@@ -6146,7 +6194,7 @@ extern "C" int dbox_launch_solve(const dg::Ctx* x, cudaStream_t stream, int* lau
     if (x->big_block) launch_solve_big(x, stream);  // large worlds' Solve
     dg::k_solve_toi<<<x->solve_blocks, x->solve_wpb * dg::kWarp, x->solve_smem_floats * sizeof(float), stream>>>(*x);
     if (x->n_big > 0) {                             // large worlds: their pairs on a block each, then AddPair + TOI
-        dg::k_pairs_block<<<x->n_big, dg::kPairThreads, 0, stream>>>(*x);
+        launch_big(dg::k_pairs_block, x, dg::kPairThreads, 0, stream);
         dg::k_finish_big_block<<<x->n_big, dg::kPairThreads, 0, stream>>>(*x);
     }
     if (launches) *launches = x->n_big > 0 ? 8 + x->big_block : 4;
@@ -6171,7 +6219,7 @@ extern "C" int dbox_launch_step_ev(const dg::Ctx* x, cudaStream_t stream, int* l
     if (x->big_block) launch_solve_big(x, stream);  // large worlds' Solve
     dg::k_solve_toi<<<x->solve_blocks, x->solve_wpb * dg::kWarp, x->solve_smem_floats * sizeof(float), stream>>>(*x);
     if (x->n_big > 0) {                             // large worlds: their pairs on a block each, then AddPair + TOI
-        dg::k_pairs_block<<<x->n_big, dg::kPairThreads, 0, stream>>>(*x);
+        launch_big(dg::k_pairs_block, x, dg::kPairThreads, 0, stream);
         dg::k_finish_big_block<<<x->n_big, dg::kPairThreads, 0, stream>>>(*x);
     }
     if (ev) cudaEventRecordWithFlags(ev[2], stream, cudaEventRecordExternal);
