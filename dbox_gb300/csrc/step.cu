@@ -732,6 +732,57 @@ struct BlockTeam {
     DG int prefix(bool v, int* all) const { return block_scan_value(v ? 1 : 0, rl, all); }
 };
 
+// b2ContactManager.AddPair's filters (b2contactmanager.d:52-120): same body, edge-edge (no such
+// contact type), an existing contact, b2Body.ShouldCollide, the contact filter
+DG bool pair_accept(const Ctx& x, int w, const WorldInfo& wi, int2 pr) {
+    const DFixture& fA = x.fx[pr.x];
+    const DFixture& fB = x.fx[pr.y];
+    bool acc = fA.body != fB.body;
+    if (acc) acc = !(fA.type == kShapeEdge && fB.type == kShapeEdge);
+    if (acc) acc = !hash_contains(x, wi, pair_key(pr.x, pr.y));
+    if (acc) acc = body_should_collide(x, fB.body, fA.body);
+    if (acc) acc = filter_should_collide(x, w, fA, fB);
+    return acc;
+}
+// b2Contact.Create and the rest of AddPair (b2contactmanager.d:120-176) into contact slot `slot`
+DG void pair_create(const Ctx& x, const WorldInfo& wi, int2 pr, int slot) {
+    // the registry's primary order puts the polygon before a circle and an edge before a circle
+    // or a polygon (b2contact.d:358-400)
+    int fa = pr.x, fb = pr.y;
+    const int ta = x.fx[fa].type, tb = x.fx[fb].type;
+    if ((ta == kShapeCircle && tb == kShapePolygon) || (ta != kShapeEdge && tb == kShapeEdge)) { int t = fa; fa = fb; fb = t; }
+    const DFixture& FA = x.fx[fa];
+    const DFixture& FB = x.fx[fb];
+    dbox_contact_state& c = x.ct[wi.contact_start + slot];
+    c.fixture_a = fa;
+    c.fixture_b = fb;
+    c.flags = kContactEnabled;
+    c.toi_count = 0;
+    c.toi = 0.0f;
+    c.friction = fsqrt(FA.friction * FB.friction);                       // b2MixFriction
+    c.restitution = FA.restitution > FB.restitution ? FA.restitution : FB.restitution;
+    c.tangent_speed = 0.0f;
+    c.point_count = 0;
+    c.type = 0;
+    c.local_normal[0] = c.local_normal[1] = 0.0f;
+    c.local_point[0] = c.local_point[1] = 0.0f;
+    for (int k = 0; k < 2; ++k) {
+        c.points[k].local_point[0] = c.points[k].local_point[1] = 0.0f;
+        c.points[k].normal_impulse = c.points[k].tangent_impulse = 0.0f;
+        c.points[k].id = 0;
+    }
+    hash_insert(x, wi, pair_key(fa, fb));
+    x.s_cbody[wi.contact_start + slot] = make_int2(FA.body - wi.body_start, FB.body - wi.body_start);
+    x.s_cq[wi.contact_start + slot] = (unsigned char)((FA.sensor || FB.sensor) ? 2 : 0);
+    if (!FA.sensor && !FB.sensor) {
+        // SetAwake(true) on both bodies; concurrent writers store identical values
+        dbox_body_state& ba = x.bs[FA.body];
+        dbox_body_state& bb = x.bs[FB.body];
+        if ((ba.flags & kBodyAwake) == 0) { atomicOr(&ba.flags, (unsigned)kBodyAwake); ba.sleep_time = 0.0f; }
+        if ((bb.flags & kBodyAwake) == 0) { atomicOr(&bb.flags, (unsigned)kBodyAwake); bb.sleep_time = 0.0f; }
+    }
+}
+
 // b2ContactManager.AddPair (b2contactmanager.d:52-176) for the pairs in order, new contacts
 // appended in that order; a team of threads (a warp, or the block of a large world)
 template <class Team>
@@ -747,55 +798,13 @@ __device__ __noinline__ void add_pairs_t(const Ctx& x, int w, int total, const T
         int2 pr = make_int2(0, 0);
         if (i < total) {
             pr = x.pairs[wi.pair_start + i];
-            const DFixture& fA = x.fx[pr.x];
-            const DFixture& fB = x.fx[pr.y];
-            acc = fA.body != fB.body;
-            if (acc) acc = !(fA.type == kShapeEdge && fB.type == kShapeEdge);   // no edge-edge contact type
-            if (acc) acc = !hash_contains(x, wi, pair_key(pr.x, pr.y));
-            if (acc) acc = body_should_collide(x, fB.body, fA.body);
-            if (acc) acc = filter_should_collide(x, w, fA, fB);
+            acc = pair_accept(x, w, wi, pr);
         }
         int all;
         const int before = tm.prefix(acc, &all);
         if (acc) {
             int slot = n + added + before;
-            if (slot < wi.contact_cap) {
-                // b2Contact.Create: the registry's primary order puts the polygon before a circle and
-                // an edge before a circle or a polygon (b2contact.d:358-400)
-                int fa = pr.x, fb = pr.y;
-                const int ta = x.fx[fa].type, tb = x.fx[fb].type;
-                if ((ta == kShapeCircle && tb == kShapePolygon) || (ta != kShapeEdge && tb == kShapeEdge)) { int t = fa; fa = fb; fb = t; }
-                const DFixture& FA = x.fx[fa];
-                const DFixture& FB = x.fx[fb];
-                dbox_contact_state& c = x.ct[wi.contact_start + slot];
-                c.fixture_a = fa;
-                c.fixture_b = fb;
-                c.flags = kContactEnabled;
-                c.toi_count = 0;
-                c.toi = 0.0f;
-                c.friction = fsqrt(FA.friction * FB.friction);                       // b2MixFriction
-                c.restitution = FA.restitution > FB.restitution ? FA.restitution : FB.restitution;
-                c.tangent_speed = 0.0f;
-                c.point_count = 0;
-                c.type = 0;
-                c.local_normal[0] = c.local_normal[1] = 0.0f;
-                c.local_point[0] = c.local_point[1] = 0.0f;
-                for (int k = 0; k < 2; ++k) {
-                    c.points[k].local_point[0] = c.points[k].local_point[1] = 0.0f;
-                    c.points[k].normal_impulse = c.points[k].tangent_impulse = 0.0f;
-                    c.points[k].id = 0;
-                }
-                hash_insert(x, wi, pair_key(fa, fb));
-                x.s_cbody[wi.contact_start + slot] = make_int2(FA.body - wi.body_start, FB.body - wi.body_start);
-                x.s_cq[wi.contact_start + slot] = (unsigned char)((FA.sensor || FB.sensor) ? 2 : 0);
-                if (!FA.sensor && !FB.sensor) {
-                    // SetAwake(true) on both bodies; concurrent writers store identical values
-                    dbox_body_state& ba = x.bs[FA.body];
-                    dbox_body_state& bb = x.bs[FB.body];
-                    if ((ba.flags & kBodyAwake) == 0) { atomicOr(&ba.flags, (unsigned)kBodyAwake); ba.sleep_time = 0.0f; }
-                    if ((bb.flags & kBodyAwake) == 0) { atomicOr(&bb.flags, (unsigned)kBodyAwake); bb.sleep_time = 0.0f; }
-                }
-            }
+            if (slot < wi.contact_cap) pair_create(x, wi, pr, slot);
         }
         added += all;
         tm.sync();
@@ -808,6 +817,7 @@ __device__ __noinline__ void add_pairs_t(const Ctx& x, int w, int total, const T
     if (tm.lead()) wd.contact_count = n + added;
     tm.sync();
 }
+
 DG void add_pairs(const Ctx& x, int w, int total) { add_pairs_t(x, w, total, WarpTeam()); }
 
 // b2ContactManager.FindNewContacts (b2contactmanager.d:320-323) on one warp
@@ -877,6 +887,57 @@ DG int block_exclusive_scan(int* a, int n, int* sh) {
 }
 
 DG void sync_fixtures(const Ctx& x, int b);
+// The same for a large world's end-of-step pairs on a cluster of csize blocks: each block takes
+// chunks of blockDim.x pairs round-robin and counts the accepted ones (a rejected pair's first
+// fixture gets its sign bit), the first block turns the chunk counts into offsets, then each
+// chunk creates its accepted pairs at their places.  No pair occurs twice, so a pair's filters
+// give the same answer whichever pairs were created before it.
+DG void add_pairs_cluster(const Ctx& x, int w, int total, int csize, int crank, int* shi) {
+    const WorldInfo& wi = x.wi[w];
+    WorldDyn& wd = x.wd[w];
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int n = wd.contact_count;
+    int2* pairs = x.pairs + wi.pair_start;
+    int* chunk = x.s_pcount + wi.fix_start;                             // per chunk: count, then offset
+    const int nch = (total + nt - 1) / nt;
+    auto csync = [&]() { if (csize > 1) cluster_sync(); else __syncthreads(); };
+    for (int c = crank; c < nch; c += csize) {
+        const int i = c * nt + tid;
+        bool acc = false;
+        if (i < total) {
+            const int2 pr = pairs[i];
+            acc = pair_accept(x, w, wi, pr);
+            if (!acc) pairs[i].x = pr.x | (int)0x80000000;
+        }
+        int all;
+        block_scan_value(acc ? 1 : 0, shi, &all);
+        if (tid == 0) chunk[c] = all;
+    }
+    if (crank == 0 && tid == 0) chunk[nch] = 0;
+    csync();
+    if (crank == 0) block_exclusive_scan(chunk, nch + 1, shi);
+    csync();
+    for (int c = crank; c < nch; c += csize) {
+        const int i = c * nt + tid;
+        int2 pr = make_int2(-1, 0);
+        if (i < total) pr = pairs[i];
+        const bool acc = i < total && pr.x >= 0;
+        int all;
+        const int before = block_scan_value(acc ? 1 : 0, shi, &all);
+        const int slot = n + ld_volatile_i(&chunk[c]) + before;
+        if (acc && slot < wi.contact_cap) pair_create(x, wi, pr, slot);
+    }
+    csync();
+    if (crank == 0 && tid == 0) {
+        int added = ld_volatile_i(&chunk[nch]);
+        if (n + added > wi.contact_cap) {
+            set_error(x, w, DBOX_ERR_CAPACITY);
+            added = wi.contact_cap - n;
+        }
+        wd.contact_count = n + added;
+    }
+    __syncthreads();
+}
 // A large world's pair table and pair search on a block (pairs into x.pairs, their count into
 // wd.pair_total).  At the end of Solve (b2world.d:1099-1120) after SynchronizeFixtures of the
 // island bodies; at the start of a step (`at_begin`: FindNewContacts after fixtures were
@@ -5295,7 +5356,7 @@ __global__ void __launch_bounds__(kPairThreads) k_collide_finish_big(const __gri
 }
 
 
-// AddPair for a large world's pairs, then its SolveTOI, on a block
+// AddPair for a large world's pairs on its cluster, then its SolveTOI on the first block
 __global__ void __launch_bounds__(kPairThreads) k_finish_big_block(const __grid_constant__ Ctx x) {
     __shared__ unsigned s_bal[32];
     __shared__ int s_box[2];
@@ -5303,11 +5364,14 @@ __global__ void __launch_bounds__(kPairThreads) k_finish_big_block(const __grid_
     __shared__ int s_rl[32];
     __shared__ unsigned s_words[kPairThreads];
     __shared__ int s_aux[4];
-    const int w = x.big_worlds[blockIdx.x];
+    const int csize = x.big_cluster > 1 ? (int)cluster_blocks() : 1;
+    const int crank = csize > 1 ? (int)cluster_rank() : 0;
+    const int w = x.big_worlds[blockIdx.x / csize];
     const int total = x.wd[w].pair_total;
     const long long t_in = clock64();
     BlockTeam tm{s_bal, s_box, s_ra, s_rl, s_words, s_aux};
-    if (total > 0) add_pairs_t(x, w, total, tm);
+    if (total > 0) add_pairs_cluster(x, w, total, csize, crank, s_rl);   // the same decision in every block
+    if (crank != 0) return;                                              // SolveTOI: the first block
     if (x.prof && threadIdx.x == 0) x.prof[kProfSlots * (size_t)w + 31] = clock64() - t_in;
     toi_world_t(x, w, x.s_sbody + 6 * (size_t)x.wi[w].body_start, tm);
 }
@@ -6195,7 +6259,7 @@ extern "C" int dbox_launch_solve(const dg::Ctx* x, cudaStream_t stream, int* lau
     dg::k_solve_toi<<<x->solve_blocks, x->solve_wpb * dg::kWarp, x->solve_smem_floats * sizeof(float), stream>>>(*x);
     if (x->n_big > 0) {                             // large worlds: their pairs on a block each, then AddPair + TOI
         launch_big(dg::k_pairs_block, x, dg::kPairThreads, 0, stream);
-        dg::k_finish_big_block<<<x->n_big, dg::kPairThreads, 0, stream>>>(*x);
+        launch_big(dg::k_finish_big_block, x, dg::kPairThreads, 0, stream);
     }
     if (launches) *launches = x->n_big > 0 ? 8 + x->big_block : 4;
     return (int)cudaGetLastError();
@@ -6220,7 +6284,7 @@ extern "C" int dbox_launch_step_ev(const dg::Ctx* x, cudaStream_t stream, int* l
     dg::k_solve_toi<<<x->solve_blocks, x->solve_wpb * dg::kWarp, x->solve_smem_floats * sizeof(float), stream>>>(*x);
     if (x->n_big > 0) {                             // large worlds: their pairs on a block each, then AddPair + TOI
         launch_big(dg::k_pairs_block, x, dg::kPairThreads, 0, stream);
-        dg::k_finish_big_block<<<x->n_big, dg::kPairThreads, 0, stream>>>(*x);
+        launch_big(dg::k_finish_big_block, x, dg::kPairThreads, 0, stream);
     }
     if (ev) cudaEventRecordWithFlags(ev[2], stream, cudaEventRecordExternal);
     if (ev) cudaEventRecordWithFlags(ev[3], stream, cudaEventRecordExternal);
