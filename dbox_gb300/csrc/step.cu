@@ -4653,31 +4653,38 @@ __device__ __noinline__ void toi_update(const Ctx& x, dbox_contact_state& c, uns
 // and s_isl_contact; one lane.  sb holds the island bodies' state for the solve.
 __device__ __noinline__ void solve_toi_island(const Ctx& x, int w, const WorldInfo& wi, SB sb, int nbI, int ncI, int toiA, int toiB,
                          float subDt) {
+    // one warp: the per-body and per-contact set-up, integration and report over its lanes, the
+    // position and velocity iterations (Gauss-Seidel over the island's contacts) on lane 0
+    const int lane = lane_id();
     const int b0 = wi.body_start, c0 = wi.contact_start;
     VRow* tv = x.tvr + (size_t)kMaxTOIContacts * w;
     PRow* tp = x.tpr + (size_t)kMaxTOIContacts * w;
-    for (int i = 0; i < nbI; ++i) {
+    for (int i = lane; i < nbI; i += kWarp) {
         int b = x.s_isl_body[b0 + i];
         sb_load(sb, b, x.bs[b0 + b]);
     }
-    for (int t = 0; t < ncI; ++t) {
+    for (int t = lane; t < ncI; t += kWarp) {
         VC vc;
         PC pc;
         constraint_ctor(x, x.s_isl_contact[c0 + t], b0, false, 1.0f, vc, pc);
         tp[t] = pack_p(pc, 0);
     }
-    for (int it = 0; it < 20; ++it) {
-        float minSep = 0.0f;
-        for (int t = 0; t < ncI; ++t)
-            minSep = bmin(minSep, solve_position(unpack_p(load_p(tp + t)), sb, true, toiA, toiB));
-        if (minSep >= -1.5f * kLinearSlop) break;
+    __syncwarp();
+    if (lane == 0) {
+        for (int it = 0; it < 20; ++it) {
+            float minSep = 0.0f;
+            for (int t = 0; t < ncI; ++t)
+                minSep = bmin(minSep, solve_position(unpack_p(load_p(tp + t)), sb, true, toiA, toiB));
+            if (minSep >= -1.5f * kLinearSlop) break;
+        }
+        dbox_body_state& A = x.bs[b0 + toiA];
+        dbox_body_state& B = x.bs[b0 + toiB];
+        float2 cA = sb.c(toiA), cB = sb.c(toiB);
+        A.sweep[2] = cA.x; A.sweep[3] = cA.y; A.sweep[6] = sb.a(toiA);
+        B.sweep[2] = cB.x; B.sweep[3] = cB.y; B.sweep[6] = sb.a(toiB);
     }
-    dbox_body_state& A = x.bs[b0 + toiA];
-    dbox_body_state& B = x.bs[b0 + toiB];
-    float2 cA = sb.c(toiA), cB = sb.c(toiB);
-    A.sweep[2] = cA.x; A.sweep[3] = cA.y; A.sweep[6] = sb.a(toiA);
-    B.sweep[2] = cB.x; B.sweep[3] = cB.y; B.sweep[6] = sb.a(toiB);
-    for (int t = 0; t < ncI; ++t) {
+    __syncwarp();
+    for (int t = lane; t < ncI; t += kWarp) {
         int ci = x.s_isl_contact[c0 + t];
         VC vc;
         PC pc;
@@ -4685,15 +4692,18 @@ __device__ __noinline__ void solve_toi_island(const Ctx& x, int w, const WorldIn
         constraint_init_velocity(vc, pc, sb);
         tv[t] = pack_v(vc, ci);
     }
-    for (int it = 0; it < x.vel_iters; ++it)
-        for (int t = 0; t < ncI; ++t) {
-            VC vc = unpack_v(load_v(tv + t));
-            solve_velocity(vc, sb);
-            tv[t].imp = make_float4(vc.p[0].normalImpulse, vc.p[0].tangentImpulse, vc.p[1].normalImpulse,
-                                    vc.p[1].tangentImpulse);
-        }
+    __syncwarp();
+    if (lane == 0)
+        for (int it = 0; it < x.vel_iters; ++it)
+            for (int t = 0; t < ncI; ++t) {
+                VC vc = unpack_v(load_v(tv + t));
+                solve_velocity(vc, sb);
+                tv[t].imp = make_float4(vc.p[0].normalImpulse, vc.p[0].tangentImpulse, vc.p[1].normalImpulse,
+                                        vc.p[1].tangentImpulse);
+            }
+    __syncwarp();
     float h = subDt;
-    for (int i = 0; i < nbI; ++i) {
+    for (int i = lane; i < nbI; i += kWarp) {
         int b = x.s_isl_body[b0 + i];
         dbox_body_state& Bd = x.bs[b0 + b];
         float2 c = sb.c(b);
@@ -4719,12 +4729,16 @@ __device__ __noinline__ void solve_toi_island(const Ctx& x, int w, const WorldIn
     if (x.record_events) {
         // b2Island.Report at the end of b2Island.SolveTOI (b2island.d:411-416)
         WorldDyn& wd = x.wd[w];
-        for (int q = 0; q < ncI; ++q) {
+        const int e0 = wd.ev_count;
+        for (int q = lane; q < ncI; q += kWarp) {
             VRow r = load_v(tv + q);
             float ni[2] = {r.imp.x, r.imp.z}, ti[2] = {r.imp.y, r.imp.w};
-            put_event(x, wi, w, wd.ev_count++, DBOX_EVENT_POSTSOLVE, x.ct[x.s_isl_contact[c0 + q]], r.ids.z & 0xff, ni, ti);
+            put_event(x, wi, w, e0 + q, DBOX_EVENT_POSTSOLVE, x.ct[x.s_isl_contact[c0 + q]], r.ids.z & 0xff, ni, ti);
         }
+        __syncwarp();
+        if (lane == 0) wd.ev_count = e0 + ncI;
     }
+    __syncwarp();
 }
 
 // b2World.SolveTOI (b2world.d:1127-1452) for world w, then the end of b2World.Step
@@ -5121,10 +5135,12 @@ DG void toi_world_t(const Ctx& x, int w, float* sbp, const Team& tm) {
                     }
                 }
                 mark(4);
+                nbI = tm.bcast(nbI);
+                ncI = tm.bcast(ncI);
+                if (rk < kWarp) solve_toi_island(x, w, wi, sb, nbI, ncI, mcb.x, mcb.y, (1.0f - minAlpha) * x.dt);
+                tm.sync();
                 int nnow = 0;
                 if (tm.lead()) {
-                    float subDt = (1.0f - minAlpha) * x.dt;
-                    solve_toi_island(x, w, wi, sb, nbI, ncI, mcb.x, mcb.y, subDt);
                     mark(5);
                     for (int i = 0; i < nbI; ++i) {
                         int body = x.s_isl_body[b0 + i];
@@ -5253,22 +5269,38 @@ __global__ void __launch_bounds__(kPairThreads) k_collide_finish_big(const __gri
     __shared__ int s_rl[32];
     __shared__ unsigned s_words[kPairThreads];
     __shared__ int s_aux[4];
-    const int w = x.big_worlds[blockIdx.x];
+    // on the world's cluster: every block a round-robin share of the passes over contacts and
+    // bodies; the first block the revived contacts, the listener events and the scans
+    const int csize = x.big_cluster > 1 ? (int)cluster_blocks() : 1;
+    const int crank = csize > 1 ? (int)cluster_rank() : 0;
+    const bool r0 = crank == 0;
+    const int w = x.big_worlds[blockIdx.x / csize];
     const WorldInfo& wi = x.wi[w];
     WorldDyn& wd = x.wd[w];
     const int tid = threadIdx.x, nt = blockDim.x;
+    const int gtid = tid * csize + crank, gsize = nt * csize;
+    auto csync = [&]() { if (csize > 1) cluster_sync(); else __syncthreads(); };
     const int n = wd.contact_count, c0 = wi.contact_start;
+    int* part = x.s_pcount + wi.fix_start;                               // per-block flags, per-chunk counts
     const long long t_in = clock64();
     BlockTeam tm{s_bal, s_box, s_ra, s_rl, s_words, s_aux};
     bool need = false;
-    for (int k = tid; k < n; k += nt) {
+    for (int k = gtid; k < n; k += gsize) {
         if (x.s_cstate[c0 + k] == 1) {
             const dbox_contact_state& c = x.ct[c0 + k];
             const int A = x.fx[c.fixture_a].body, B = x.fx[c.fixture_b].body;
             if (x.s_woken[A] != kNoWake || x.s_woken[B] != kNoWake) need = true;
         }
     }
-    if (__syncthreads_or(need)) {
+    need = __syncthreads_or(need) != 0;
+    if (csize > 1) {
+        if (tid == 0) part[crank] = need ? 1 : 0;
+        cluster_sync();
+        need = false;
+        for (int q = 0; q < csize; ++q) need |= ld_volatile_i(&part[q]) != 0;
+        cluster_sync();                                                  // before `part` is reused
+    }
+    if (need && r0) {
         tm.scan_desc(n, [&](int k) { return x.s_cstate[c0 + k] == 1; }, [&](int k) {
             const int lp = n - 1 - k;
             dbox_contact_state& c = x.ct[c0 + k];
@@ -5286,9 +5318,9 @@ __global__ void __launch_bounds__(kPairThreads) k_collide_finish_big(const __gri
             return true;
         });
     }
-    __syncthreads();
     // listener events of this Collide, in list order (newest contact first)
-    if (x.record_events) {
+    if (x.record_events && r0) {
+        __syncthreads();
         int base = 0;
         for (int top = n - 1; top >= 0; top -= nt) {
             const int k = top - tid;
@@ -5305,30 +5337,45 @@ __global__ void __launch_bounds__(kPairThreads) k_collide_finish_big(const __gri
         }
         if (tid == 0) wd.ev_count = base;
     }
+    csync();
     // apply wakes
-    for (int i = tid; i < wi.body_count; i += nt) {
+    for (int i = gtid; i < wi.body_count; i += gsize) {
         const int b = wi.body_start + i;
         if (x.s_woken[b] != kNoWake) b_set_awake(x.bs[b], true);
     }
-    // stable compaction of surviving contacts: destinations, then the move
+    // stable compaction of surviving contacts: kept contacts per chunk of nt, the chunks'
+    // offsets (first block), each contact's destination, then the move
     int* dst = x.s_tcand + c0;
-    int out = 0;
-    for (int base = 0; base < n; base += nt) {
-        const int k = base + tid;
+    const int nch = (n + nt - 1) / nt;
+    for (int c = crank; c < nch; c += csize) {
+        const int k = c * nt + tid;
+        int all;
+        block_scan_value(k < n && x.s_cstate[c0 + k] != 2 ? 1 : 0, shi, &all);
+        if (tid == 0) part[c] = all;
+    }
+    if (r0 && tid == 0) part[nch] = 0;
+    csync();
+    if (r0) block_exclusive_scan(part, nch + 1, shi);
+    csync();
+    const int out = ld_volatile_i(&part[nch]);
+    for (int c = crank; c < nch; c += csize) {
+        const int k = c * nt + tid;
         const int keep = k < n && x.s_cstate[c0 + k] != 2;
         int all;
-        const int d = out + block_scan_value(keep, shi, &all);
+        const int d = ld_volatile_i(&part[c]) + block_scan_value(keep, shi, &all);
         if (k < n) dst[k] = keep ? d : -1;
-        out += all;
     }
-    __syncthreads();
+    csync();
     if (out < n) {
+        // every destination is at or before its source, so the blocks move csize chunks at a
+        // time: all of them read their chunk, then all of them write it
         constexpr int kWords = (int)(sizeof(dbox_contact_state) / sizeof(int4));
         static_assert(sizeof(dbox_contact_state) % sizeof(int4) == 0, "contacts move as 16-byte words");
         int4* words = reinterpret_cast<int4*>(x.ct + c0);
-        const int chunk = 4 * nt / kWords;                               // contacts a pass reads at once
-        for (int base = 0; base < n; base += chunk) {
-            const int cnt = n - base < chunk ? n - base : chunk;
+        const int chunk = 4 * nt / kWords;                               // contacts a block reads at once
+        for (int wave = 0; wave * chunk * csize < n; ++wave) {
+            const int base = (wave * csize + crank) * chunk;
+            const int cnt = base >= n ? 0 : (n - base < chunk ? n - base : chunk);
             int4 v[4];
             int to[4];
 #pragma unroll
@@ -5344,15 +5391,15 @@ __global__ void __launch_bounds__(kPairThreads) k_collide_finish_big(const __gri
                     }
                 }
             }
-            __syncthreads();
+            csync();
 #pragma unroll
             for (int j = 0; j < 4; ++j)
                 if (to[j] >= 0) words[to[j]] = v[j];
-            __syncthreads();
+            csync();
         }
     }
-    if (tid == 0) { wd.contact_count = out; wd.acc_contacts += (unsigned long long)n; wd.acc_steps += 1; }
-    if (x.prof && tid == 0) x.prof[kProfSlots * (size_t)w + 15] = clock64() - t_in;
+    if (r0 && tid == 0) { wd.contact_count = out; wd.acc_contacts += (unsigned long long)n; wd.acc_steps += 1; }
+    if (r0 && x.prof && tid == 0) x.prof[kProfSlots * (size_t)w + 15] = clock64() - t_in;
 }
 
 
@@ -6213,20 +6260,6 @@ __global__ void __launch_bounds__(kSolveWarps * 32, 3) k_solve_toi(const __grid_
 // Launch one step.  ev, when not NULL, holds 4 events recorded at the phase
 // boundaries: [0] before Collide, [1] before Solve, [2] and [3] after Solve + SolveTOI (one kernel).
 // part 1 of a step: FindNewContacts for new fixtures, then Collide (3 launches)
-extern "C" int dbox_launch_collide(const dg::Ctx* x, cudaStream_t stream) {
-    const int threads = 128;                       // four worlds per block, one warp each
-    int team_blocks = (x->W * dg::kWarp + threads - 1) / threads;
-    int flat_blocks = (x->total_contacts + 255) / 256;
-    if (flat_blocks < 1) flat_blocks = 1;
-    if (flat_blocks > 152 * 16) flat_blocks = 152 * 16;
-    dg::k_step_begin<<<team_blocks, threads, 0, stream>>>(*x);
-    if (x->n_big > 0) dg::k_begin_big<<<x->n_big, dg::kPairThreads, 0, stream>>>(*x);
-    dg::k_collide<<<flat_blocks, 256, 0, stream>>>(*x);
-    dg::k_collide_finish<<<team_blocks, threads, 0, stream>>>(*x);
-    if (x->n_big > 0) dg::k_collide_finish_big<<<x->n_big, dg::kPairThreads, 0, stream>>>(*x);
-    return (int)cudaGetLastError();
-}
-
 // a large-world kernel on a cluster of x->big_cluster blocks per world (its passes spread over
 // them), or on one block
 template <class K>
@@ -6249,6 +6282,21 @@ static void launch_big(K kernel, const dg::Ctx* x, unsigned threads, size_t smem
 static void launch_solve_big(const dg::Ctx* x, cudaStream_t stream) {
     launch_big(dg::k_solve_big, x, dg::kBigThreads, x->ws_mode == 2 ? dg::kBigSmemInfer : 0, stream);
 }
+
+extern "C" int dbox_launch_collide(const dg::Ctx* x, cudaStream_t stream) {
+    const int threads = 128;                       // four worlds per block, one warp each
+    int team_blocks = (x->W * dg::kWarp + threads - 1) / threads;
+    int flat_blocks = (x->total_contacts + 255) / 256;
+    if (flat_blocks < 1) flat_blocks = 1;
+    if (flat_blocks > 152 * 16) flat_blocks = 152 * 16;
+    dg::k_step_begin<<<team_blocks, threads, 0, stream>>>(*x);
+    if (x->n_big > 0) dg::k_begin_big<<<x->n_big, dg::kPairThreads, 0, stream>>>(*x);
+    dg::k_collide<<<flat_blocks, 256, 0, stream>>>(*x);
+    dg::k_collide_finish<<<team_blocks, threads, 0, stream>>>(*x);
+    if (x->n_big > 0) launch_big(dg::k_collide_finish_big, x, dg::kPairThreads, 0, stream);
+    return (int)cudaGetLastError();
+}
+
 
 // part 2 of a step: Solve and SolveTOI (1 launch, 3 or 4 with a large world); *launches = all of the step's
 // (part 1 is 3 launches, 5 with a large world)
@@ -6277,7 +6325,7 @@ extern "C" int dbox_launch_step_ev(const dg::Ctx* x, cudaStream_t stream, int* l
     if (x->n_big > 0) dg::k_begin_big<<<x->n_big, dg::kPairThreads, 0, stream>>>(*x);
     dg::k_collide<<<flat_blocks, 256, 0, stream>>>(*x);
     dg::k_collide_finish<<<team_blocks, threads, 0, stream>>>(*x);
-    if (x->n_big > 0) dg::k_collide_finish_big<<<x->n_big, dg::kPairThreads, 0, stream>>>(*x);
+    if (x->n_big > 0) launch_big(dg::k_collide_finish_big, x, dg::kPairThreads, 0, stream);
     if (ev) cudaEventRecordWithFlags(ev[1], stream, cudaEventRecordExternal);
     if (x->solve_queue) cudaMemsetAsync(x->solve_queue, 0, sizeof(int) * (2 + 4 * (size_t)x->solve_nsm), stream);
     if (x->big_block) launch_solve_big(x, stream);  // large worlds' Solve
