@@ -600,7 +600,7 @@ class World:
         _check(lib().dbox_world_set_wait_limit(self.h, polls), "dbox_world_set_wait_limit")
 
     def set_island_solver(self, mode=0):
-        """Large worlds' Solve on a block (0, default) or on a warp (1); the same results."""
+        """Large worlds' Solve on a thread-block cluster (0, default) or on a warp (1); the same results."""
         _check(lib().dbox_world_set_island_solver(self.h, mode), "dbox_world_set_island_solver")
 
     def island_solver(self):

@@ -5423,36 +5423,38 @@ __global__ void __launch_bounds__(kPairThreads) k_finish_big_block(const __grid_
     toi_world_t(x, w, x.s_sbody + 6 * (size_t)x.wi[w].body_start, tm);
 }
 
-// ------------------------------------------------------------ b2World.Solve of a large world on a block
-// A world of 4,096+ fixtures is one warp's dependent walk in solve_world; here a block of
-// kBigThreads threads does the same step: the same islands in the same order, the same
-// constraint order inside each island, the same arithmetic, so the same bits.
+// ------------------------------------------------------------ b2World.Solve of a large world on a cluster
+// A world of 4,096+ fixtures is one warp's dependent walk in solve_world; here a thread-block
+// cluster (k_solve_big, up to 8 blocks of kBigThreads threads) does the same step: the same
+// islands in the same order, the same constraint order inside each island, the same
+// arithmetic, so the same bits.  The first block runs the serial phases:
 //   islands: the island graph's components (contacts that are enabled, touching and not a
 //     sensor, joints between active bodies; static bodies do not connect) by a lock-free
 //     union-find; the reference's depth-first search (b2world.d:959-1095) seeds islands in body
 //     list order (descending index), so an island's seed is the highest-index awake, active,
 //     non-static body of its component and islands are numbered by descending seed; a prefix sum
 //     of the components' body / contact / joint counts places each island's lists, and each
-//     island's own search (the reference's, from its seed) runs on a warp of its own.  A static
-//     body is never pushed: popping one changes nothing but its island mark, which is the
+//     island's own search (the reference's, from its seed) runs on a thread of its own.  A
+//     static body is never pushed: popping one changes nothing but its island mark, which is the
 //     last island (in order) that reached it.
-//   schedules: each island's constraints get their levels on one lane (islands share no
+//   schedules: each island's constraints get their levels on one thread (islands share no
 //     dynamic body), then the block buckets all constraints by level.
-//   rows, sweeps (levels in order, a level's constraints over the block, a block barrier
-//     between levels), integration, copy back and sleep over the block.
-// Every warm-start mode runs here too: the predictions of mode 2 on kInferWarps warps, 16 rows a pass.
+// Every block runs the parallel phases, items dealt round-robin over the cluster's threads:
+// compaction, integration, constraint rows, the sweeps (levels in order, a level's rows over
+// the cluster, a cluster barrier between levels), StoreImpulses, copy back and sleep.
+// Every warm-start mode runs here too: the predictions of mode 2 on kInferWarps warps of the
+// first block, 16 rows a pass.
 constexpr int kBigThreads = 1024;
 constexpr int kInferWarps = 8;
 constexpr int kInferStage = 16 * kFeat + 2 * 16 * kHid;               // bf16 per warp: X, H1, H2
 constexpr int kBigSmemInfer = kInferWarps * kInferStage * 2;          // bytes
 
-DG int ld_volatile_int(const int* p) { return *reinterpret_cast<const volatile int*>(p); }
 DG int uf_find(int* parent, int i) {
     // parents only ever point to lower indices, so the walk ends; path halving
     for (;;) {
-        const int p = ld_volatile_int(&parent[i]);
+        const int p = ld_volatile_i(&parent[i]);
         if (p == i) return i;
-        const int g = ld_volatile_int(&parent[p]);
+        const int g = ld_volatile_i(&parent[p]);
         if (g != p) parent[i] = g;
         i = p;
     }

@@ -682,9 +682,10 @@ int32_t dbox_world_autotune(dbox_world* w, float dt, int32_t velocity_iterations
 int32_t dbox_world_set_wait_limit(dbox_world* w, int32_t polls);
 
 /* How b2World.Solve runs for the large worlds of the handle (4,096 fixtures or more): mode 0
- * (default) on a block of 1,024 threads each (islands found by a union-find, each island's
- * search on a thread of its own, constraint levels swept by the whole block), mode 1 on one warp
- * each like every other world.  Both give the same results bit for bit, in every warm-start mode
+ * (default) on a thread-block cluster of up to 8 blocks of 1,024 threads each (islands found by
+ * a union-find, each island's search on a thread of its own, the parallel phases and the
+ * constraint level sweeps spread over the cluster), mode 1 on one warp each like every other
+ * world.  Both give the same results bit for bit, in every warm-start mode
  * (dbox_world_set_warmstart 0..3).  Replaces no reference call: the
  * reference solves islands one after another on the calling thread (dynamics/b2world.d:930-1124). */
 int32_t dbox_world_set_island_solver(dbox_world* w, int32_t mode);
