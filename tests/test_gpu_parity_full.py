@@ -227,3 +227,24 @@ def test_large_mixed_world_exact(oracle_lib, gpu_lib, solver):
     assert ((st["bodies"]["flags"][dyn] & abi.BODY_AWAKE) == 0).any()
     assert st["header"][0]["joint_count"] == sum(len(s[k]) for k in scenes.JOINT_KINDS)
     assert toi > 100
+
+
+def test_two_large_worlds_and_small_ones_exact(oracle_lib, gpu_lib):
+    # two worlds of 4,096+ fixtures in one handle (each on its own cluster of blocks) beside
+    # small worlds on warps: every world bit for bit against the oracle
+    oracle_lib.set_trig_mode(1)
+    rng = np.random.default_rng(29)
+    big_a = scenes._concat([scenes.container(90.0, 90.0), scenes.scatter(4300, 88.0, 88.0, rng)])
+    big_b = scenes.stress(piles=4, per_pile=1100, chains_per_pile=2, links=12, seed=8)
+    worlds = [scenes.pyramid(rows=8), big_a, scenes.chains(n_chains=2, links=8), big_b]
+    assert len(big_a["fixtures"]) >= 4096 and len(big_b["fixtures"]) >= 4096
+    gw = gpu_lib.World(worlds)
+    ows = [oracle_lib.OracleWorld(s) for s in worlds]
+    for t in range(90):
+        gw.step()
+        for ow in ows:
+            ow.step()
+        if (t + 1) % 30 == 0:
+            for i, ow in enumerate(ows):
+                d = exact_diff(ow.export_state(), gw.export_state(i))
+                assert not d, "world %d step %d: %s" % (i, t + 1, d[:6])
