@@ -1260,8 +1260,9 @@ __global__ void __launch_bounds__(kPairThreads) k_pairs_block(const __grid_const
     pairs_block(x, x.big_worlds[blockIdx.x / csize], false, shf, shi, csize, crank);
 }
 
-// FindNewContacts of a large world whose fixtures were just created (e_newFixture), on its
-// block: the pair search, then AddPair (k_step_begin does it on a warp for the other worlds)
+// The start of a large world's step on its block: the wake marks of Collide cleared, and
+// FindNewContacts when fixtures were just created (e_newFixture): the pair search, then AddPair
+// (k_step_begin does both on a warp for the other worlds)
 __global__ void __launch_bounds__(kPairThreads) k_begin_big(const __grid_constant__ Ctx x) {
     __shared__ float shf[32];
     __shared__ int shi[32];
@@ -1271,7 +1272,10 @@ __global__ void __launch_bounds__(kPairThreads) k_begin_big(const __grid_constan
     __shared__ int s_rl[32];
     __shared__ int s_aux[4];
     const int w = x.big_worlds[blockIdx.x];
+    const WorldInfo& wi = x.wi[w];
+    for (int i = threadIdx.x; i < wi.body_count; i += blockDim.x) x.s_woken[wi.body_start + i] = kNoWake;
     if (!(x.wd[w].flags & 1u)) return;
+    __syncthreads();
     pairs_block(x, w, true, shf, shi, 1, 0);
     __syncthreads();
     BlockTeam tm{s_bal, s_box, s_ra, s_rl, nullptr, s_aux};
@@ -1387,7 +1391,8 @@ __global__ void k_step_begin(const __grid_constant__ Ctx x) {
     const WorldInfo& wi = x.wi[w];
     int lane = lane_id();
     if (lane == 0) { wd.error = 0; wd.islands = 0; wd.toi_events = 0; wd.ev_count = 0; }
-    for (int i = lane; i < wi.body_count; i += kWarp) x.s_woken[wi.body_start + i] = kNoWake;
+    if (!wi.pair_block)                                                 // large worlds: k_begin_big
+        for (int i = lane; i < wi.body_count; i += kWarp) x.s_woken[wi.body_start + i] = kNoWake;
     tsync();
     if ((wd.flags & 1u) && !wi.pair_block) {                            // e_newFixture (large worlds: k_begin_big)
         hash_rebuild(x, w);
