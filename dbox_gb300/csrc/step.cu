@@ -4747,8 +4747,11 @@ __device__ __noinline__ void solve_toi_island(const Ctx& x, int w, const WorldIn
 }
 
 // b2World.SolveTOI (b2world.d:1127-1452) for world w, then the end of b2World.Step
+// `prepared`: a large world whose cluster already ran the passes at the start of SolveTOI
+// (toi_begin_cluster): the compaction and flag clears, the candidate list (its length in
+// WorldDyn.toi_ncand) and the per-body candidate lists
 template <class Team>
-DG void toi_world_t(const Ctx& x, int w, float* sbp, const Team& tm) {
+DG void toi_world_t(const Ctx& x, int w, float* sbp, const Team& tm, bool prepared = false) {
     const WorldInfo& wi = x.wi[w];
     WorldDyn& wd = x.wd[w];
     const int rk = tm.rank(), ts = tm.size();
@@ -4763,11 +4766,11 @@ DG void toi_world_t(const Ctx& x, int w, float* sbp, const Team& tm) {
         bool advanced = wd.step_complete == 0;
         SB sb;
         sb.p = sbp;
-        {
+        if (!prepared) {
             int n = wd.contact_count;
             for (int k = rk; k < n; k += ts) contact_compact(x, c0 + k, b0);
         }
-        if (wd.step_complete) {                                          // b2world.d:1131-1146
+        if (wd.step_complete && !prepared) {                             // b2world.d:1131-1146
             for (int i = rk; i < nb; i += ts) {
                 x.bs[b0 + i].flags &= ~(uint32_t)kBodyIsland;
                 x.bs[b0 + i].sweep[8] = 0.0f;
@@ -4780,20 +4783,21 @@ DG void toi_world_t(const Ctx& x, int w, float* sbp, const Team& tm) {
                 c.toi = 1.0f;
             }
         }
-        for (int i = rk; i < nb; i += ts) x.s_bfl[b0 + i] = 0;
+        if (!prepared)
+            for (int i = rk; i < nb; i += ts) x.s_bfl[b0 + i] = 0;
         tm.sync();
         // TOI candidates in list order (ascending slot): only these can get a TOI, join a TOI
         // island as a neighbour or carry the TOI / island flags that an event clears
         int* cand = x.s_tcand + c0;
         auto is_cand = [&](int k) { return toi_candidate(x, c0 + k, b0); };
-        int ncand = tm.collect(0, wd.contact_count, cand, 0, is_cand);
+        int ncand = prepared ? wd.toi_ncand : tm.collect(0, wd.contact_count, cand, 0, is_cand);
         // block teams: the candidates of each non-static body (positions in cand, descending),
         // so that an event's joins and invalidations visit only its bodies' candidates; those
         // collected after this point (from the events' new pairs) are scanned apart
         const int ncand0 = ncand;
         int* lstart = x.s_adj_start + wi.bx_start;                       // nb + 1
         int* lent = reinterpret_cast<int*>(x.s_adj_items + 2 * (size_t)c0);
-        if constexpr (Team::kLists) {
+        if constexpr (Team::kLists) if (!prepared) {
             int* lcur = x.s_cursor + b0;
             auto dyn = [&](int b) { return x.bs[b0 + b].type != kStaticBody; };
             for (int i = rk; i < nb; i += ts) lstart[i] = 0;
@@ -4855,7 +4859,7 @@ DG void toi_world_t(const Ctx& x, int w, float* sbp, const Team& tm) {
         int* pnow = x.s_pcount + f0;                                     // moved by this event
         int* pall = x.s_moved + f0;                                      // moved during this SolveTOI
         int nall = 0;
-        if (big_toi)
+        if (big_toi && !prepared)
             for (int i = rk; i < wi.fix_count; i += ts) toimv[i] = 0;
         tm.sync();
         int events = 0;
@@ -5408,24 +5412,151 @@ __global__ void __launch_bounds__(kPairThreads) k_collide_finish_big(const __gri
 }
 
 
-// AddPair for a large world's pairs on its cluster, then its SolveTOI on the first block
+// The passes at the start of a large world's SolveTOI (b2world.d:1131-1146, and the candidate
+// filter of :1172-1188) on its cluster, each block a round-robin share: every body's island
+// flag and alpha0 cleared, every contact compacted and its TOI state cleared, the candidates
+// marked in one ballot word per 32 contact slots; then the first block lists the candidates in
+// slot order from the words while every block counts each dynamic body's candidates, a scan
+// of the counts (each block a contiguous range of bodies, then the ranges' offsets), the lists
+// filled with candidate positions and each list sorted by descending position.  The same lists
+// as the single-block passes in toi_world_t (a list's order comes from its sort alone).
+DG void toi_begin_cluster(const Ctx& x, int w, int csize, int crank, int* shi) {
+    const WorldInfo& wi = x.wi[w];
+    WorldDyn& wd = x.wd[w];
+    if (!(x.continuous && x.dt > 0.0f)) return;                          // no SolveTOI
+    const int tid = threadIdx.x, nt = blockDim.x, lane = lane_id();
+    const int gtid = tid * csize + crank, gsize = nt * csize;
+    const int gwarp = (tid >> 5) * csize + crank, gnw = (nt >> 5) * csize;
+    auto csync = [&]() { if (csize > 1) cluster_sync(); else __syncthreads(); };
+    const int b0 = wi.body_start, nb = wi.body_count, c0 = wi.contact_start, f0 = wi.fix_start;
+    const int n = ld_volatile_i(&wd.contact_count);                     // after AddPair
+    const bool clear = wd.step_complete != 0;
+    const bool big_toi = wi.pair_block && wd.g_valid && !wi.proxy_order;
+    int* cand = x.s_tcand + c0;
+    unsigned* words = reinterpret_cast<unsigned*>(x.s_cstate + c0);     // candidate bits per 32 slots
+    int* lstart = x.s_adj_start + wi.bx_start;                          // nb + 1
+    int* lcur = x.s_cursor + b0;
+    int* lent = reinterpret_cast<int*>(x.s_adj_items + 2 * (size_t)c0);
+    int* part = x.s_pcount + f0;                                         // per block: its range's total
+    auto dyn = [&](int b) { return x.bs[b0 + b].type != kStaticBody; };
+    for (int i = gtid; i < nb; i += gsize) {
+        if (clear) {
+            x.bs[b0 + i].flags &= ~(uint32_t)kBodyIsland;
+            x.bs[b0 + i].sweep[8] = 0.0f;
+        }
+        x.s_bfl[b0 + i] = 0;
+        lstart[i] = 0;
+    }
+    if (big_toi)
+        for (int i = gtid; i < wi.fix_count; i += gsize) x.s_sapk[0][f0 + i] = 0;   // moved during this SolveTOI
+    const int nwd = (n + 31) >> 5;
+    for (int q = gwarp; q < nwd; q += gnw) {
+        const int k = 32 * q + lane;
+        bool hit = false;
+        if (k < n) {
+            contact_compact(x, c0 + k, b0);
+            if (clear) {
+                dbox_contact_state& c = x.ct[c0 + k];
+                c.flags &= ~(uint32_t)(kContactToi | kContactIsland);
+                c.toi_count = 0;
+                c.toi = 1.0f;
+            }
+            hit = toi_candidate(x, c0 + k, b0);
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, hit);
+        if (lane == 0) words[q] = bal;
+    }
+    csync();
+    for (int q = gwarp; q < nwd; q += gnw) {                             // candidates per dynamic body
+        if (!((words[q] >> lane) & 1u)) continue;
+        const int2 cb = x.s_cbody[c0 + 32 * q + lane];
+        if (dyn(cb.x)) atomicAdd(&lstart[cb.x], 1);
+        if (dyn(cb.y)) atomicAdd(&lstart[cb.y], 1);
+    }
+    if (crank == 0) {                                                    // the candidate list
+        int cnt = 0;
+        for (int base = 0; base < nwd; base += nt) {
+            const int q = base + tid;
+            const unsigned m = q < nwd ? words[q] : 0u;
+            int all;
+            int pos = cnt + block_scan_value(__popc(m), shi, &all);
+            for (unsigned b = m; b; b &= b - 1u) cand[pos++] = 32 * q + __ffs(b) - 1;
+            cnt += all;
+        }
+        if (tid == 0) wd.toi_ncand = cnt;
+    }
+    csync();
+    const int chunk = (nb + csize - 1) / csize;                          // this block's bodies
+    const int lo = min(nb, crank * chunk), hi = min(nb, lo + chunk);
+    const int tot = block_exclusive_scan(lstart + lo, hi - lo, shi);
+    if (tid == 0) part[crank] = tot;
+    csync();
+    int off = 0, all = 0;
+    for (int r = 0; r < csize; ++r) {
+        const int v = ld_volatile_i(&part[r]);
+        off += r < crank ? v : 0;
+        all += v;
+    }
+    for (int i = lo + tid; i < hi; i += nt) {
+        const int v = lstart[i] + off;
+        lstart[i] = v;
+        lcur[i] = v;
+    }
+    if (crank == 0 && tid == 0) lstart[nb] = all;
+    csync();
+    const int ncand = ld_volatile_i(&wd.toi_ncand);
+    for (int t = gtid; t < ncand; t += gsize) {
+        const int2 cb = x.s_cbody[c0 + cand[t]];
+        if (dyn(cb.x)) lent[atomicAdd(&lcur[cb.x], 1)] = t;
+        if (dyn(cb.y)) lent[atomicAdd(&lcur[cb.y], 1)] = t;
+    }
+    csync();
+    for (int i = gtid; i < nb; i += gsize) {                             // each list by descending position
+        const int e0 = lstart[i], d = lstart[i + 1] - e0;
+        int gap = 1;
+        while (3 * gap + 1 < d) gap = 3 * gap + 1;
+        for (; gap > 0; gap /= 3)
+            for (int a = e0 + gap; a < e0 + d; ++a) {
+                const int v = lent[a];
+                int q = a - gap;
+                while (q >= e0 && lent[q] < v) { lent[q + gap] = lent[q]; q -= gap; }
+                lent[q + gap] = v;
+            }
+    }
+}
+
+// AddPair for a large world's pairs on its cluster, then the passes at the start of its SolveTOI
 __global__ void __launch_bounds__(kPairThreads) k_finish_big_block(const __grid_constant__ Ctx x) {
-    __shared__ unsigned s_bal[32];
-    __shared__ int s_box[2];
-    __shared__ float s_ra[32];
     __shared__ int s_rl[32];
-    __shared__ unsigned s_words[kPairThreads];
-    __shared__ int s_aux[4];
     const int csize = x.big_cluster > 1 ? (int)cluster_blocks() : 1;
     const int crank = csize > 1 ? (int)cluster_rank() : 0;
     const int w = x.big_worlds[blockIdx.x / csize];
     const int total = x.wd[w].pair_total;
     const long long t_in = clock64();
-    BlockTeam tm{s_bal, s_box, s_ra, s_rl, s_words, s_aux};
     if (total > 0) add_pairs_cluster(x, w, total, csize, crank, s_rl);   // the same decision in every block
-    if (crank != 0) return;                                              // SolveTOI: the first block
-    if (x.prof && threadIdx.x == 0) x.prof[kProfSlots * (size_t)w + 31] = clock64() - t_in;
-    toi_world_t(x, w, x.s_sbody + 6 * (size_t)x.wi[w].body_start, tm);
+    const long long t_add = clock64();
+    if (csize > 1) cluster_sync();                                       // the contact count and new contacts
+    toi_begin_cluster(x, w, csize, crank, s_rl);
+    if (x.prof && crank == 0 && threadIdx.x == 0) {
+        x.prof[kProfSlots * (size_t)w + 31] = t_add - t_in;
+        x.prof[kProfSlots * (size_t)w + 29] = clock64() - t_add;
+    }
+}
+
+// A large world's SolveTOI event loop on a block of its own: kToiThreads threads, so that the
+// serial parts (the lead's event contact, the sub-step solve, the TOI computations) keep their
+// values in registers
+constexpr int kToiThreads = 512;
+__global__ void __launch_bounds__(kToiThreads, 1) k_toi_big(const __grid_constant__ Ctx x) {
+    __shared__ unsigned s_bal[32];
+    __shared__ int s_box[2];
+    __shared__ float s_ra[32];
+    __shared__ int s_rl[32];
+    __shared__ unsigned s_words[kToiThreads];
+    __shared__ int s_aux[4];
+    const int w = x.big_worlds[blockIdx.x];
+    BlockTeam tm{s_bal, s_box, s_ra, s_rl, s_words, s_aux};
+    toi_world_t(x, w, x.s_sbody + 6 * (size_t)x.wi[w].body_start, tm, true);
 }
 
 // ------------------------------------------------------------ b2World.Solve of a large world on a cluster
@@ -5713,11 +5844,21 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
     njI = block_exclusive_scan(cntj, nIsl, shi);
     if (tid == 0) { cntb[nIsl] = nbI; cntc[nIsl] = ncI; cntj[nIsl] = njI; wd.islands = nIsl; s_next = 0; }
     __syncthreads();
-    // ---- each island's depth-first search (b2world.d:988-1076), an island per thread
-    // (islands handed out one at a time; they share no non-static body, contact or joint)
-    for (;;) {
-        const int k = atomicAdd(&s_next, 1);
-        if (k >= nIsl) break;
+    if (tid == 0) wd.sw_nisl = nIsl;
+    }                                                                    // r0
+    csync();
+    if (!r0) nIsl = ld_volatile_i(&wd.sw_nisl);
+    // ---- each island's depth-first search (b2world.d:988-1076), an island per thread, the
+    // islands dealt round-robin over the cluster's blocks (they share no non-static body,
+    // contact or joint; spread over the blocks, the searches' scattered loads and stores are
+    // spread over as many SMs' load/store units)
+    {
+    int* parent = x.s_stack + b0;
+    const int* seed_of = reinterpret_cast<const int*>(x.s_isl_minsep + b0);
+    const int* cntb = x.s_isl_bstart + bx;
+    const int* cntc = x.s_isl_cstart + bx;
+    const int* cntj = x.s_isl_jstart + bx;
+    for (int k = crank + csize * tid; k < nIsl; k += csize * nt) {
         const int seed = seed_of[k];
         int* stack = parent + cntb[k];                                   // this island's own stack rows
         int nB = cntb[k], nC = cntc[k], nJ = cntj[k];
@@ -5758,6 +5899,9 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
             }
         }
     }
+    }
+    csync();
+    if (r0) {
     __syncthreads();
     stampb(2);
     for (int k = tid; k < n; k += nt)
@@ -6305,18 +6449,19 @@ extern "C" int dbox_launch_collide(const dg::Ctx* x, cudaStream_t stream) {
 }
 
 
-// part 2 of a step: Solve and SolveTOI (1 launch, 3 or 4 with a large world); *launches = all of the step's
+// part 2 of a step: Solve and SolveTOI (1 launch, 4 or 5 with a large world); *launches = all of the step's
 // (part 1 is 3 launches, 5 with a large world)
 extern "C" int dbox_launch_solve(const dg::Ctx* x, cudaStream_t stream, int* launches) {
     if (x->solve_blocks < 1) return (int)cudaErrorInvalidValue;
     if (x->solve_queue) cudaMemsetAsync(x->solve_queue, 0, sizeof(int) * (2 + 4 * (size_t)x->solve_nsm), stream);
     if (x->big_block) launch_solve_big(x, stream);  // large worlds' Solve
     dg::k_solve_toi<<<x->solve_blocks, x->solve_wpb * dg::kWarp, x->solve_smem_floats * sizeof(float), stream>>>(*x);
-    if (x->n_big > 0) {                             // large worlds: their pairs on a block each, then AddPair + TOI
+    if (x->n_big > 0) {                             // large worlds: pairs and AddPair on their clusters, then TOI
         launch_big(dg::k_pairs_block, x, dg::kPairThreads, 0, stream);
         launch_big(dg::k_finish_big_block, x, dg::kPairThreads, 0, stream);
+        dg::k_toi_big<<<x->n_big, dg::kToiThreads, 0, stream>>>(*x);
     }
-    if (launches) *launches = x->n_big > 0 ? 8 + x->big_block : 4;
+    if (launches) *launches = x->n_big > 0 ? 9 + x->big_block : 4;
     return (int)cudaGetLastError();
 }
 
@@ -6337,13 +6482,14 @@ extern "C" int dbox_launch_step_ev(const dg::Ctx* x, cudaStream_t stream, int* l
     if (x->solve_queue) cudaMemsetAsync(x->solve_queue, 0, sizeof(int) * (2 + 4 * (size_t)x->solve_nsm), stream);
     if (x->big_block) launch_solve_big(x, stream);  // large worlds' Solve
     dg::k_solve_toi<<<x->solve_blocks, x->solve_wpb * dg::kWarp, x->solve_smem_floats * sizeof(float), stream>>>(*x);
-    if (x->n_big > 0) {                             // large worlds: their pairs on a block each, then AddPair + TOI
+    if (x->n_big > 0) {                             // large worlds: pairs and AddPair on their clusters, then TOI
         launch_big(dg::k_pairs_block, x, dg::kPairThreads, 0, stream);
         launch_big(dg::k_finish_big_block, x, dg::kPairThreads, 0, stream);
+        dg::k_toi_big<<<x->n_big, dg::kToiThreads, 0, stream>>>(*x);
     }
     if (ev) cudaEventRecordWithFlags(ev[2], stream, cudaEventRecordExternal);
     if (ev) cudaEventRecordWithFlags(ev[3], stream, cudaEventRecordExternal);
-    if (launches) *launches = x->n_big > 0 ? 8 + x->big_block : 4;
+    if (launches) *launches = x->n_big > 0 ? 9 + x->big_block : 4;
     return (int)cudaGetLastError();
 }
 

@@ -70,6 +70,8 @@ struct WorldDyn {
     // search (levels, island joints, islands, island bodies and contacts), the count of rows
     // waiting for a prediction, and the continue flag of each position iteration
     int sw_maxv, sw_maxp, sw_njI, sw_go, sw_nisl, sw_nbi, sw_nci, sw_npend;
+    // a large world's SolveTOI candidates, counted by its cluster before the event loop
+    int toi_ncand, toi_pad;
 };
 
 struct BodyStatic {
