@@ -1547,7 +1547,9 @@ DG void sb_load(SB sb, int i, const dbox_body_state& b) {
 }
 
 // flags of the compact per-body byte (s_bfl)
-enum { kBfAwake = 1, kBfActive = 2, kBfStatic = 4, kBfDynamic = 8, kBfVisited = 16, kBfMark = 32 };
+// (kBfPopped: the island search has walked the body's contacts, so every contact between it and
+// a non-static body is already in an island)
+enum { kBfAwake = 1, kBfActive = 2, kBfStatic = 4, kBfDynamic = 8, kBfVisited = 16, kBfMark = 32, kBfPopped = 64 };
 
 // ------------------------------------------------------------ contact solver pieces (contacts/b2contactsolver.d)
 // b2ContactSolver ctor (:244-329) for one contact; body indices are world-local.
@@ -4149,24 +4151,26 @@ DG void solve_world(const Ctx& x, int w, float* sbp, bool sb_smem, float* stage_
                     ++nStatic;
                     continue;
                 }
-                if (lane == 0) isl_body[nbI] = b;
+                if (lane == 0) { isl_body[nbI] = b; vbf[b] = fb | kBfPopped; }
                 ++nbI;
                 for (int e0 = adj[b], ee = adj[b + 1]; e0 < ee; e0 += kWarp) {
                     const int e = e0 + lane;
                     int2 it = make_int2(0, 0);
                     bool newc = false;
+                    unsigned char fo = kBfVisited;
                     if (e < ee) {
                         it = items[e];
-                        newc = !cvis[it.x];
+                        // in an island already exactly when the other body is non-static and
+                        // was popped before (its walk added the contact)
+                        fo = vbf[it.y];
+                        newc = (fo & (kBfPopped | kBfStatic)) != kBfPopped;
                     }
                     const unsigned cm = __ballot_sync(0xffffffffu, newc);
-                    unsigned char fo = kBfVisited;
                     if (newc) {
                         const int pos = ncI + __popc(cm & lt);
                         isl_contact[pos] = c0 + it.x;
                         isl_pair[pos] = make_int2(b, it.y);
                         cvis[it.x] = 1;
-                        fo = vbf[it.y];
                     }
                     ncI += __popc(cm);
                     const bool cand = newc && !(fo & kBfVisited);
@@ -5869,14 +5873,17 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
             const int b = stack[--top];
             body_island[b] = k;
             isl_body[nB++] = b;
+            bfl[b] |= kBfPopped;
             for (int e = adj[b], ee = adj[b + 1]; e < ee; ++e) {
                 const int2 it = items[e];
-                if (cvis[it.x]) continue;
+                // the contact is in an island already exactly when its other body is non-static
+                // and was popped before (its walk added it): one load instead of the contact's mark
+                const unsigned char fo = bfl[it.y];
+                if ((fo & (kBfPopped | kBfStatic)) == kBfPopped) continue;
                 isl_contact[nC] = c0 + it.x;
                 isl_pair[nC] = make_int2(b, it.y);
                 ++nC;
                 cvis[it.x] = 1;
-                const unsigned char fo = bfl[it.y];
                 if (fo & kBfStatic) { atomicMax(&body_island[it.y], k); continue; }
                 if (fo & kBfVisited) continue;
                 stack[top++] = it.y;
