@@ -506,8 +506,9 @@ int32_t dbox_world_get_transforms(dbox_world* w, float* xya);
  * kernel, 27 its warp slot, 28..29 the SM and the warp's slot on the SM (%smid, %warpid);
  * 15 for a world solved on a warp 1 when its solver body rows were in shared memory; for a
  * large world (4,096+ fixtures) 15 the cycles of its block's end of Collide, 27 the blocks of
- * its Solve's cluster, 28 the SM of the first, 30 the cycles of its block's SynchronizeFixtures
- * + pair search, 31 of its AddPair pass (25..26 and 29 unused). */
+ * its Solve's cluster, 28 the SM of the first, 29 the cycles of SolveTOI's setup passes on its
+ * cluster, 30 of its block's SynchronizeFixtures + pair search, 31 of its AddPair pass (25..26
+ * unused). */
 int32_t dbox_world_set_phase_profile(dbox_world* w, int32_t enable);
 int32_t dbox_world_get_phase_profile(dbox_world* w, unsigned long long* out);
 
