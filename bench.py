@@ -68,6 +68,8 @@ def parse():
     p.add_argument("--stress-warmup", type=int, default=60, help="steps before the stress world is measured")
     p.add_argument("--stress-steps", type=int, default=3)
     p.add_argument("--no-stress", action="store_true", help="skip the large-island stress world")
+    p.add_argument("--fused-step", action="store_true",
+                   help="whole steps in one launch (dbox_world_set_fused_step) instead of four launches a step")
     return p.parse_args()
 
 
@@ -292,6 +294,7 @@ def gpu_leg(args, rank, world_size):
         costs = None
     elif not args.no_autotune and args.mapping == "auto":
         wt = dbox_gb300.World(worlds)
+        wt.set_fused_step(args.fused_step)
         wt.step(DT, VI, PI, steps=args.warmup, graph=True)
         mapping = wt.autotune(steps=3, dt=DT, vel_iters=VI, pos_iters=PI)
         costs = wt.world_costs()
@@ -300,6 +303,8 @@ def gpu_leg(args, rank, world_size):
     # twin handle for the end-to-end leg: the same scenes and warm-up, so it replays exactly
     # the steps the device-timed leg measures
     we = dbox_gb300.World(worlds)
+    for h in (w, we):
+        h.set_fused_step(args.fused_step)
     if mapping:
         for h in (w, we):
             if costs is not None:
@@ -324,7 +329,8 @@ def gpu_leg(args, rank, world_size):
     cdiff = {k: c1[k] - c0[k] for k in c1}
     total_ms_max = max_over_ranks(total_ms, "cuda")
     value = nbody_dyn * args.steps * world_size / (total_ms_max / 1e3)
-    launches = w.last_launches() * args.steps
+    launches = w.last_launches()                 # kernels of the timed call, all its steps
+    fused = w.fused_step() and phase_ms[0] == 0.0
     # end to end through the C ABI with pinned host buffers
     forces = torch.zeros((nbody, 3), dtype=torch.float32).pin_memory().numpy()
     xya = torch.zeros((nbody, 3), dtype=torch.float32).pin_memory().numpy()
@@ -340,7 +346,7 @@ def gpu_leg(args, rank, world_size):
     e2e = nbody_dyn * args.steps * world_size / max_over_ranks(e2e_s, "cuda")
     assert np.isfinite(xya).all()
     solve_bytes = algorithmic_solve_bytes(cdiff) / args.steps
-    solve_ms = phase_ms[1] / args.steps          # the fused solve + SolveTOI kernel
+    solve_ms = phase_ms[1] / args.steps          # the solve + SolveTOI kernel (the whole step when fused)
     achieved = solve_bytes / (solve_ms / 1e3) / 1e9
     hbm = peaks.get("hbm_gbs")
     chain = solver_chain(w)
@@ -353,21 +359,24 @@ def gpu_leg(args, rank, world_size):
                        parallelism="replicas: one batch of worlds per GPU",
                        mapping=mapping_report(mapping, args.mapping),
                        l2="working set (bodies, contacts, constraint rows) larger than the 129 MB L2",
-                       timing="one CUDA graph of K steps with per-phase CUDA events"),
+                       timing=("one launch of K whole steps (k_step_fused), CUDA events around it" if fused else
+                               "one CUDA graph of K steps with per-phase CUDA events")),
         "e2e": {"value": e2e, "unit": "body-steps/s", "h2d_bytes_per_step": int(forces.nbytes),
                 "d2h_bytes_per_step": int(xya.nbytes)},
         "gpu_launches": launches,
-        "phases_ms_per_step": {"collide": phase_ms[0] / args.steps, "solve_and_toi": solve_ms},
+        "phases_ms_per_step": ({"whole_step_kernel": solve_ms} if fused else
+                               {"collide": phase_ms[0] / args.steps, "solve_and_toi": solve_ms}),
         "work_per_step": {k: v / args.steps for k, v in cdiff.items()},
         # The fused solve + SolveTOI kernel is bound by the dependent Gauss-Seidel chain of the
         # deepest worlds (levels in sequence, each level a few hundred cycles of dependent
         # arithmetic), not by HBM: the bandwidth fraction below is what that chain leaves.
-        "roofline": {"bound": "latency", "kernel": "k_solve_toi", "achieved": achieved,
+        "roofline": {"bound": "latency", "kernel": "k_step_fused" if fused else "k_solve_toi", "achieved": achieved,
                      "peak": hbm, "unit": "GB/s", "frac": (achieved / hbm) if hbm else None,
                      "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if hbm else "fallback 6800",
                      "algorithmic_bytes_per_launch": solve_bytes,
                      "algorithmic_bytes_cover": "the island solve only (bodies, constraint build, velocity and "
-                                                "position solves, impulse store); SolveTOI and Collide not counted",
+                                                "position solves, impulse store); SolveTOI and Collide not counted"
+                                                + ("; the kernel time is the whole step" if fused else ""),
                      "solve_share_of_step": solve_ms / (total_ms_max / args.steps),
                      "traffic": None,
                      "traffic_note": "DRAM bytes come from a separate ncu capture of this kernel, not from the "

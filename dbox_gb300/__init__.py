@@ -117,6 +117,8 @@ def lib():
     L.dbox_world_set_wait_limit.argtypes = [vp, i32]
     L.dbox_world_set_island_solver.argtypes = [vp, i32]
     L.dbox_world_get_island_solver.argtypes = [vp, vp]
+    L.dbox_world_set_fused_step.argtypes = [vp, i32]
+    L.dbox_world_get_fused_step.argtypes = [vp, vp]
     L.dbox_world_set_listener.argtypes = [vp, vp, vp]
     L.dbox_world_set_presolve.argtypes = [vp, vp, vp]
     L.dbox_fixture_set_filter.argtypes = [vp, i32, i32, ctypes.c_uint16, ctypes.c_uint16, ctypes.c_int16]
@@ -607,6 +609,15 @@ class World:
         out = ctypes.c_int32()
         _check(lib().dbox_world_get_island_solver(self.h, ctypes.byref(out)), "dbox_world_get_island_solver")
         return out.value
+
+    def set_fused_step(self, on=True):
+        """Whole steps in one launch, or four launches a step (default); the same results."""
+        _check(lib().dbox_world_set_fused_step(self.h, 1 if on else 0), "dbox_world_set_fused_step")
+
+    def fused_step(self):
+        out = ctypes.c_int32()
+        _check(lib().dbox_world_get_fused_step(self.h, ctypes.byref(out)), "dbox_world_get_fused_step")
+        return bool(out.value)
 
     def set_measure(self, on=True):
         _check(lib().dbox_world_set_measure(self.h, 1 if on else 0), "dbox_world_set_measure")

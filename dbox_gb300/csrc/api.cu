@@ -22,6 +22,8 @@
 
 extern "C" int dbox_launch_step(const dg::Ctx* x, cudaStream_t stream, int* launches);
 extern "C" const void* dbox_solve_kernel();
+extern "C" const void* dbox_step_fused_kernel();
+extern "C" int dbox_launch_steps_fused(const dg::Ctx* x, cudaStream_t stream, int* launches);
 extern "C" int dbox_big_solve_init(int* cluster);
 const dg::MlpDev* dbox_mlp_device_view(const dbox_mlp* m, dg::MlpDev* out);
 extern "C" int dbox_launch_step_ev(const dg::Ctx* x, cudaStream_t stream, int* launches, cudaEvent_t* ev);
@@ -202,6 +204,7 @@ struct dbox_world {
     int wait_polls = 1 << 20;   // budget of one mbarrier wait in the solve kernel (polls)
     int island_solver = 0;      // 0: a large world's Solve on a block (k_solve_big), 1: on a warp
     int big_cluster = 1;        // blocks of k_solve_big's cluster per large world (its level sweeps)
+    int fused_step = 0;         // 1: whole steps in one launch (k_step_fused) where the handle allows
     // contact listener
     DBuf<dbox_contact_event> d_events;
     DBuf<unsigned> s_sapk0, s_sapk1;
@@ -220,8 +223,9 @@ struct dbox_world {
     float g_dt = -1.0f;
     int g_vi = -1, g_pi = -1;
     int graph_flags = -1;
+    int g_launches = 0;                 // kernels of one captured step
     dbox_profile profile;
-    int last_launches = 0;
+    int last_launches = 0;              // kernels launched by the last stepping call (all its steps)
     dbox_event_fn listener = nullptr;
     void* listener_user = nullptr;
     // table contact filters (b2World.SetContactFilter): per world a mode and 64 class rows
@@ -242,6 +246,7 @@ struct dbox_world {
     int t_steps = -1;
     float t_dt = -1.0f;
     int t_vi = -1, t_pi = -1, t_flags = -1;
+    int t_launches = 0;                 // kernels of the timed graph
     // world queries: the device index of the broad-phase's fat AABBs
     unsigned long long gen = 0;         // bumped before any device work that may move proxies
     unsigned long long q_gen = ~0ull;   // gen the index was built at
@@ -326,11 +331,13 @@ int pack_solve_queue(dbox_world* w) {
     w->solve_cap = std::min(max_nb, cap_max);
     w->solve_wpb = dg::kSolveWarps;
     w->solve_smem_floats = dg::kSolveWarps * (dg::kWarpSmemFloats + 8 * w->solve_cap);
-    CU(cudaFuncSetAttribute(dbox_solve_kernel(), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                            (int)(sizeof(float) * w->solve_smem_floats)));
-    int occ = 0;
-    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, dbox_solve_kernel(), dg::kSolveWarps * 32,
-                                                     sizeof(float) * w->solve_smem_floats));
+    int occ = 1 << 30;
+    for (const void* k : {dbox_solve_kernel(), dbox_step_fused_kernel()}) {   // the queue's wave fits both
+        CU(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(sizeof(float) * w->solve_smem_floats)));
+        int o = 0;
+        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k, dg::kSolveWarps * 32, sizeof(float) * w->solve_smem_floats));
+        occ = std::min(occ, o);
+    }
     if (occ < 1) return fail(DBOX_ERR_CUDA, "solve kernel does not fit on an SM");
     if (w->solve_bps > 0) occ = std::min(occ, w->solve_bps);
     w->solve_blocks = std::max(1, std::min(w->nsm * occ, (W + dg::kSolveWarps - 1) / dg::kSolveWarps));
@@ -423,8 +430,8 @@ int pack_solve_slots(dbox_world* w) {
         return fail(DBOX_ERR_CUDA, "device allocation failed (solve slots)");
     CU(cudaMemcpy(w->d_solve_world.p, slot_world.data(), sizeof(int) * slot_world.size(), cudaMemcpyHostToDevice));
     CU(cudaMemcpy(w->d_solve_smem.p, slot_off.data(), sizeof(int) * slot_off.size(), cudaMemcpyHostToDevice));
-    CU(cudaFuncSetAttribute(dbox_solve_kernel(), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                            (int)(sizeof(float) * w->solve_smem_floats)));
+    for (const void* k : {dbox_solve_kernel(), dbox_step_fused_kernel()})
+        CU(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(sizeof(float) * w->solve_smem_floats)));
     return DBOX_OK;
 }
 
@@ -2007,6 +2014,10 @@ static int deliver_events(dbox_world* w) {
     return DBOX_OK;
 }
 
+// whole steps in one launch: asked for, and no large world (their steps span clusters) and no
+// PreSolve window (the host acts between Collide and Solve)
+static bool fused_ok(const dbox_world* w) { return w->fused_step && w->n_big == 0 && !w->presolve; }
+
 int32_t dbox_world_step(dbox_world* w, float dt, int32_t velocity_iterations, int32_t position_iterations) {
     if (!w || velocity_iterations < 0 || position_iterations < 0) return fail(DBOX_ERR_INVALID, "dbox_world_step: bad arguments");
     int rc = ensure_device(w);
@@ -2026,6 +2037,9 @@ int32_t dbox_world_step(dbox_world* w, float dt, int32_t velocity_iterations, in
             if (rc) return rc;
             err = dbox_launch_solve(&x, w->stream, &launches);
         }
+    } else if (fused_ok(w)) {
+        x.steps = 1;
+        err = dbox_launch_steps_fused(&x, w->stream, &launches);
     } else {
         err = dbox_launch_step(&x, w->stream, &launches);
     }
@@ -2051,6 +2065,16 @@ int32_t dbox_world_step_n(dbox_world* w, float dt, int32_t velocity_iterations, 
         for (int i = 0; i < steps && !rc; ++i) rc = dbox_world_step(w, dt, velocity_iterations, position_iterations);
         return rc;
     }
+    if (fused_ok(w)) {                      // every step of every world in one launch
+        if (steps == 0) return DBOX_OK;
+        dg::Ctx x = make_ctx(w, dt, velocity_iterations, position_iterations);
+        x.steps = steps;
+        int launches = 0;
+        int err = dbox_launch_steps_fused(&x, w->stream, &launches);
+        if (err) return fail(DBOX_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString((cudaError_t)err));
+        w->last_launches = launches;
+        return check_status(w);
+    }
     int flags = w->warm | (w->continuous << 1) | (w->substep << 2) | (w->allow_sleep << 3) | (w->autoclear << 4);
     if (!w->graph || w->g_dt != dt || w->g_vi != velocity_iterations || w->g_pi != position_iterations ||
         w->graph_flags != flags) {
@@ -2065,9 +2089,10 @@ int32_t dbox_world_step_n(dbox_world* w, float dt, int32_t velocity_iterations, 
         CU(cudaGraphInstantiate(&w->graph, g, 0));
         cudaGraphDestroy(g);
         w->g_dt = dt; w->g_vi = velocity_iterations; w->g_pi = position_iterations; w->graph_flags = flags;
-        w->last_launches = launches;
+        w->g_launches = launches;
     }
     for (int i = 0; i < steps; ++i) CU(cudaGraphLaunch(w->graph, w->stream));
+    w->last_launches = w->g_launches * steps;
     return check_status(w);
 }
 
@@ -2078,6 +2103,30 @@ int32_t dbox_world_step_n_timed(dbox_world* w, float dt, int32_t velocity_iterat
     if (w->presolve) return fail(DBOX_ERR_UNSUPPORTED, "dbox_world_step_n_timed: a PreSolve window needs dbox_world_step");
     int rc = ensure_device(w);
     if (rc) return rc;
+    if (fused_ok(w)) {                      // one launch: the whole step is phase 1
+        if (w->tev.size() < 2) {
+            for (auto& e : w->tev) cudaEventDestroy(e);
+            w->tev.assign(2, nullptr);
+            for (auto& e : w->tev) CU(cudaEventCreate(&e));
+            if (w->tgraph) { cudaGraphExecDestroy(w->tgraph); w->tgraph = nullptr; }
+        }
+        dg::Ctx x = make_ctx(w, dt, velocity_iterations, position_iterations);
+        x.steps = steps;
+        int launches = 0;
+        CU(cudaEventRecord(w->tev[0], w->stream));
+        int err = dbox_launch_steps_fused(&x, w->stream, &launches);
+        CU(cudaEventRecord(w->tev[1], w->stream));
+        if (err) return fail(DBOX_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString((cudaError_t)err));
+        w->last_launches = launches;
+        rc = check_status(w);
+        float tot = 0.0f;
+        CU(cudaEventElapsedTime(&tot, w->tev[0], w->tev[1]));
+        if (total_ms) *total_ms = tot;
+        if (phase_ms) { phase_ms[0] = 0.0f; phase_ms[1] = tot; phase_ms[2] = 0.0f; }
+        memset(&w->profile, 0, sizeof(w->profile));
+        w->profile.step = tot / steps;
+        return rc;
+    }
     int flags = w->warm | (w->continuous << 1) | (w->substep << 2) | (w->allow_sleep << 3) | (w->autoclear << 4);
     if (!w->tgraph || w->t_steps != steps || w->t_dt != dt || w->t_vi != velocity_iterations ||
         w->t_pi != position_iterations || w->t_flags != flags) {
@@ -2096,9 +2145,10 @@ int32_t dbox_world_step_n_timed(dbox_world* w, float dt, int32_t velocity_iterat
         cudaGraphDestroy(g);
         w->t_steps = steps; w->t_dt = dt; w->t_vi = velocity_iterations; w->t_pi = position_iterations;
         w->t_flags = flags;
-        w->last_launches = launches;
+        w->t_launches = launches * steps;
     }
     CU(cudaGraphLaunch(w->tgraph, w->stream));
+    w->last_launches = w->t_launches;
     rc = check_status(w);
     float tot = 0.0f, ph[3] = {0.0f, 0.0f, 0.0f};
     CU(cudaEventElapsedTime(&tot, w->tev[0], w->tev[4 * (size_t)steps - 1]));
@@ -2265,6 +2315,18 @@ int32_t dbox_world_set_wait_limit(dbox_world* w, int32_t polls) {
     w->wait_polls = polls < (1 << 20) ? polls : (1 << 20);
     if (w->graph) { cudaGraphExecDestroy(w->graph); w->graph = nullptr; }
     if (w->tgraph) { cudaGraphExecDestroy(w->tgraph); w->tgraph = nullptr; }
+    return DBOX_OK;
+}
+
+int32_t dbox_world_set_fused_step(dbox_world* w, int32_t enable) {
+    if (!w || enable < 0 || enable > 1) return fail(DBOX_ERR_INVALID, "dbox_world_set_fused_step: bad arguments");
+    w->fused_step = enable;
+    return DBOX_OK;
+}
+
+int32_t dbox_world_get_fused_step(dbox_world* w, int32_t* enable) {
+    if (!w || !enable) return fail(DBOX_ERR_INVALID, "dbox_world_get_fused_step: bad arguments");
+    *enable = w->fused_step;
     return DBOX_OK;
 }
 

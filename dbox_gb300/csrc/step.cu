@@ -1384,9 +1384,9 @@ DG int toi_pairs_big(const Ctx& x, int w, const int* now, int nnow, const int* a
 DG void toi_world(const Ctx& x, int w, float* sbp);
 
 // ------------------------------------------------------------ kernels
-__global__ void k_step_begin(const __grid_constant__ Ctx x) {
-    int w = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
-    if (w >= x.W) return;
+// the start of b2World.Step (b2world.d:367-376) for world w on one warp: per-step records
+// reset, wake marks cleared, FindNewContacts after fixtures were created
+DG void step_begin_world(const Ctx& x, int w) {
     WorldDyn& wd = x.wd[w];
     const WorldInfo& wi = x.wi[w];
     int lane = lane_id();
@@ -1401,53 +1401,63 @@ __global__ void k_step_begin(const __grid_constant__ Ctx x) {
     }
 }
 
-__global__ void k_collide(Ctx x) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < x.total_contacts; i += gridDim.x * blockDim.x) {
-        int w = x.c_world[i];
-        const WorldInfo& wi = x.wi[w];
-        int k = i - wi.contact_start;
-        int n = x.wd[w].contact_count;
-        if (k >= n) continue;
-        int lp = n - 1 - k;
-        dbox_contact_state c = x.ct[i];
-        const DFixture& fa = x.fx[c.fixture_a];
-        const DFixture& fb = x.fx[c.fixture_b];
-        int A = fa.body, B = fb.body;
-        int state = 0;
-        unsigned evt = 0;
-        if (c.flags & kContactFilter) {                                // b2contactmanager.d:266-288
-            if (!body_should_collide(x, B, A) || !filter_should_collide(x, w, fa, fb)) {
-                state = 2;
-                evt = (c.flags & kContactTouching) ? 2u : 0u;
-                if (c.point_count > 0 && !fa.sensor && !fb.sensor) {
-                    atomicMin(&x.s_woken[A], lp);
-                    atomicMin(&x.s_woken[B], lp);
-                }
-            } else {
-                c.flags &= ~(uint32_t)kContactFilter;
+__global__ void k_step_begin(const __grid_constant__ Ctx x) {
+    int w = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+    if (w >= x.W) return;
+    step_begin_world(x, w);
+}
+
+// b2ContactManager.Collide (b2contactmanager.d:251-317) for contact slot i of world w: the
+// contact filter, the active test and the narrow phase; the contacts of a world are
+// independent here (wakes are only marked, in s_woken, and applied by the finish)
+DG void collide_contact(const Ctx& x, int w, int i) {
+    const WorldInfo& wi = x.wi[w];
+    int k = i - wi.contact_start;
+    int n = x.wd[w].contact_count;
+    if (k >= n) return;
+    int lp = n - 1 - k;
+    dbox_contact_state c = x.ct[i];
+    const DFixture& fa = x.fx[c.fixture_a];
+    const DFixture& fb = x.fx[c.fixture_b];
+    int A = fa.body, B = fb.body;
+    int state = 0;
+    unsigned evt = 0;
+    if (c.flags & kContactFilter) {                                // b2contactmanager.d:266-288
+        if (!body_should_collide(x, B, A) || !filter_should_collide(x, w, fa, fb)) {
+            state = 2;
+            evt = (c.flags & kContactTouching) ? 2u : 0u;
+            if (c.point_count > 0 && !fa.sensor && !fb.sensor) {
+                atomicMin(&x.s_woken[A], lp);
+                atomicMin(&x.s_woken[B], lp);
             }
+        } else {
+            c.flags &= ~(uint32_t)kContactFilter;
         }
-        if (state == 0) {
-            const dbox_body_state& ba = x.bs[A];
-            const dbox_body_state& bb = x.bs[B];
-            bool activeA = (ba.flags & kBodyAwake) && ba.type != kStaticBody;
-            bool activeB = (bb.flags & kBodyAwake) && bb.type != kStaticBody;
-            if (!activeA && !activeB) state = 1;
-            else state = collide_one(x, c, lp, true, &evt);
-        }
-        x.s_cstate[i] = state;
-        if (x.record_events) x.s_cevt[i] = (unsigned char)evt;
-        if (state != 2) x.ct[i] = c;
     }
+    if (state == 0) {
+        const dbox_body_state& ba = x.bs[A];
+        const dbox_body_state& bb = x.bs[B];
+        bool activeA = (ba.flags & kBodyAwake) && ba.type != kStaticBody;
+        bool activeB = (bb.flags & kBodyAwake) && bb.type != kStaticBody;
+        if (!activeA && !activeB) state = 1;
+        else state = collide_one(x, c, lp, true, &evt);
+    }
+    x.s_cstate[i] = state;
+    if (x.record_events) x.s_cevt[i] = (unsigned char)evt;
+    if (state != 2) x.ct[i] = c;
+}
+
+__global__ void k_collide(Ctx x) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < x.total_contacts; i += gridDim.x * blockDim.x)
+        collide_contact(x, x.c_world[i], i);
 }
 
 // Contacts skipped as inactive may become active when an earlier contact in list
 // order woke one of their bodies (Collide walks the list and wakes as it goes).
-__global__ void k_collide_finish(Ctx x) {
-    int w = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
-    if (w >= x.W) return;
+// the end of b2ContactManager.Collide for world w on one warp: contacts revived by a wake,
+// listener events, wakes, compaction
+DG void collide_finish_world(const Ctx& x, int w) {
     const WorldInfo& wi = x.wi[w];
-    if (wi.pair_block) return;                                          // k_collide_finish_big
     WorldDyn& wd = x.wd[w];
     int lane = lane_id();
     int n = wd.contact_count;
@@ -1525,6 +1535,24 @@ __global__ void k_collide_finish(Ctx x) {
     }
     if (lane == 0) { wd.contact_count = out; wd.acc_contacts += (unsigned long long)n; wd.acc_steps += 1; }
     tsync();
+}
+
+__global__ void k_collide_finish(Ctx x) {
+    int w = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+    if (w >= x.W) return;
+    if (x.wi[w].pair_block) return;                                     // k_collide_finish_big
+    collide_finish_world(x, w);
+}
+
+// the Collide part of one step of world w on one warp (k_step_fused): the step's start, every
+// contact's narrow phase over the lanes, the finish
+__device__ __noinline__ void collide_world(const Ctx& x, int w) {
+    step_begin_world(x, w);
+    tsync();
+    const int c0 = x.wi[w].contact_start, n = x.wd[w].contact_count;
+    for (int k = lane_id(); k < n; k += kWarp) collide_contact(x, w, c0 + k);
+    tsync();
+    collide_finish_world(x, w);
 }
 
 // ------------------------------------------------------------ solver body state
@@ -6319,7 +6347,9 @@ constexpr int kQueueWaitLimit = 1 << 16;      // bounded wait of the exclusive q
 
 DG int ld_acquire_int(const int* p) { return *reinterpret_cast<const volatile int*>(p); }
 
-__global__ void __launch_bounds__(kSolveWarps * 32, 3) k_solve_toi(const __grid_constant__ Ctx x) {
+// kFused: the whole step, x.steps times over, for each world the warp takes (k_step_fused)
+template <bool kFused>
+DG void solve_warps(const Ctx& x) {
     extern __shared__ float smem_sb[];
     const int warp = threadIdx.x >> 5, lane = lane_id();
     const int slot = blockIdx.x * x.solve_wpb + warp;
@@ -6391,10 +6421,20 @@ __global__ void __launch_bounds__(kSolveWarps * 32, 3) k_solve_toi(const __grid_
         }
         unsigned long long g0 = 0;
         if (x.prof) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(g0));
-        if (!(x.big_block && x.wi[w].pair_block)) solve_world(x, w, sbp, in_smem, stage_f, ring);   // else k_solve_big
-        tsync();
-        if (!x.wi[w].pair_block) toi_world(x, w, sbp);                   // large worlds: k_finish_big_block
-        tsync();
+        if constexpr (kFused) {                                          // no large worlds in this launch
+            for (int st = 0; st < x.steps; ++st) {
+                collide_world(x, w);
+                solve_world(x, w, sbp, in_smem, stage_f, ring);
+                tsync();
+                toi_world(x, w, sbp);
+                tsync();
+            }
+        } else {
+            if (!(x.big_block && x.wi[w].pair_block)) solve_world(x, w, sbp, in_smem, stage_f, ring);   // else k_solve_big
+            tsync();
+            if (!x.wi[w].pair_block) toi_world(x, w, sbp);               // large worlds: k_toi_big
+            tsync();
+        }
         if (heavy && lane == 0) atomicExch(&x.solve_queue[2 + sub], 0);
         if (x.prof && lane == 0 && !(x.big_block && x.wi[w].pair_block)) {
             unsigned long long g1;
@@ -6411,6 +6451,14 @@ __global__ void __launch_bounds__(kSolveWarps * 32, 3) k_solve_toi(const __grid_
         }
     }
 }
+
+__global__ void __launch_bounds__(kSolveWarps * 32, 3) k_solve_toi(const __grid_constant__ Ctx x) { solve_warps<false>(x); }
+
+// One launch for x.steps whole steps of every world (a handle without large worlds): each warp
+// takes its worlds through their steps one after the other (b2World.Step of separate worlds
+// shares nothing), so a world never waits at a step boundary for the others, and the deep
+// worlds start their solve right after their own Collide
+__global__ void __launch_bounds__(kSolveWarps * 32, 3) k_step_fused(const __grid_constant__ Ctx x) { solve_warps<true>(x); }
 
 }  // namespace dg
 
@@ -6501,6 +6549,17 @@ extern "C" int dbox_launch_step_ev(const dg::Ctx* x, cudaStream_t stream, int* l
 }
 
 extern "C" const void* dbox_solve_kernel() { return reinterpret_cast<const void*>(&dg::k_solve_toi); }
+extern "C" const void* dbox_step_fused_kernel() { return reinterpret_cast<const void*>(&dg::k_step_fused); }
+
+// x->steps whole steps of every world in one launch (k_step_fused; a handle without large
+// worlds); *launches = 1
+extern "C" int dbox_launch_steps_fused(const dg::Ctx* x, cudaStream_t stream, int* launches) {
+    if (x->solve_blocks < 1 || x->n_big > 0 || x->steps < 1) return (int)cudaErrorInvalidValue;
+    if (x->solve_queue) cudaMemsetAsync(x->solve_queue, 0, sizeof(int) * (2 + 4 * (size_t)x->solve_nsm), stream);
+    dg::k_step_fused<<<x->solve_blocks, x->solve_wpb * dg::kWarp, x->solve_smem_floats * sizeof(float), stream>>>(*x);
+    if (launches) *launches = 1;
+    return (int)cudaGetLastError();
+}
 // the largest cluster (8, 4, 2 or 1 blocks) that k_solve_big can run on this device
 extern "C" int dbox_big_solve_init(int* cluster) {
     int rc = (int)cudaFuncSetAttribute(dg::k_solve_big, cudaFuncAttributeMaxDynamicSharedMemorySize, dg::kBigSmemInfer);

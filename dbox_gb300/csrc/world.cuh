@@ -232,6 +232,7 @@ struct Ctx {
     int n_big;
     int big_block;                 // 1: large worlds run b2World.Solve on a block (k_solve_big), not a warp
     int big_cluster;               // blocks per large world in k_solve_big's level sweeps (a thread-block cluster)
+    int steps;                     // steps each world takes in one launch of k_step_fused
     const int* proxy_order;        // fixture-indexed: world-local fixture of each proxy-id rank
     // scratch (contact-indexed)
     int* s_cstate;                 // 0 processed, 1 inactive, 2 destroyed

@@ -693,7 +693,20 @@ int32_t dbox_world_set_island_solver(dbox_world* w, int32_t mode);
 /* The mode in use (set by the call above or chosen by dbox_world_autotune). */
 int32_t dbox_world_get_island_solver(dbox_world* w, int32_t* mode);
 
-/* Device kernels launched by the last step (for launch accounting). */
+/* Whole steps in one launch (no counterpart in the reference, which steps one world on the
+ * calling thread: dynamics/b2world.d:367-434): with enable = 1 (default 0) a handle without large
+ * worlds (4,096+ fixtures) and without a PreSolve window runs each step as one kernel in which
+ * every world's warp goes from its Collide straight to its Solve and SolveTOI, and
+ * dbox_world_step_n / dbox_world_step_n_timed run all their steps in one such launch (each world
+ * takes its steps one after the other; separate worlds share nothing, so no world waits at a
+ * step boundary for the others).  The results are the same bits as the per-phase launches
+ * (enable = 0: 4 launches a step).  With the fused launch dbox_world_step_n_timed reports the
+ * whole step as its phase 1 and dbox_world_get_profile only the step time. */
+int32_t dbox_world_set_fused_step(dbox_world* w, int32_t enable);
+int32_t dbox_world_get_fused_step(dbox_world* w, int32_t* enable);
+
+/* Device kernels launched by the last stepping call (dbox_world_step, dbox_world_step_n or
+ * dbox_world_step_n_timed, all of its steps; for launch accounting). */
 int32_t dbox_world_last_launches(dbox_world* w, int32_t* out);
 
 /* Text of the last error on the calling thread (never NULL). */

@@ -82,3 +82,5 @@ def test_invalid_arguments_rejected_without_device(gpu_lib):
     assert L.dbox_world_set_wait_limit(None, 0) == -1
     assert L.dbox_world_set_island_solver(None, 0) == -1
     assert L.dbox_world_get_island_solver(None, None) == -1
+    assert L.dbox_world_set_fused_step(None, 1) == -1
+    assert L.dbox_world_get_fused_step(None, None) == -1

@@ -150,6 +150,38 @@ def test_queue_mapping_with_more_worlds_than_warps_exact(oracle_lib, gpu_lib):
         assert not d, "world %d: %s" % (i, d[:6])
 
 
+def test_fused_and_split_steps_exact(oracle_lib, gpu_lib):
+    # one launch per step (each world's warp from its Collide straight to its Solve and TOI), all
+    # the steps of a step_n call in one launch, and four launches a step: the same bits, on
+    # both mappings (packed blocks and the world queue, where warps take several worlds)
+    from dbox_gb300 import scenes
+    oracle_lib.set_trig_mode(1)
+    worlds = scenes.batch(n_worlds=600, seed=15, lo=8, hi=160)
+    gw = gpu_lib.World(worlds)
+    ows = [oracle_lib.OracleWorld(s) for s in worlds]
+    assert not gw.fused_step()
+    steps = 0
+    for queue in (False, True):
+        if queue:
+            gw.set_mapping_queue(16, False)
+        for fused in (True, False):
+            gw.set_fused_step(fused)
+            gw.step(steps=7, graph=True)
+            for _ in range(3):
+                gw.step()
+            steps += 10
+            assert gw.last_launches() == (1 if fused else 4)
+            tot, ph = gw.step_timed(5)
+            steps += 5
+            assert gw.last_launches() == (1 if fused else 20)
+            assert tot > 0.0 and (ph[0] == 0.0) == fused
+    for ow in ows:
+        ow.step(steps=steps)
+    for i, ow in enumerate(ows):
+        d = exact_diff(ow.export_state(), gw.export_state(i))
+        assert not d, "world %d: %s" % (i, d[:6])
+
+
 def test_graph_replay_matches_single_steps(oracle_lib, gpu_lib):
     from dbox_gb300 import scenes
     s = scenes.scatter(200, 25.0, 30.0, np.random.default_rng(3))
