@@ -4970,10 +4970,15 @@ DG void toi_world_t(const Ctx& x, int w, float* sbp, const Team& tm, bool prepar
                 for (int i = rk; i < nn; i += ts) compute_toi(cand[nlist[i]]);
                 for (int i = rk; i < nd; i += ts) wdirty[dset[i] >> 5] = 1;
                 tm.sync();
-                // recompute the chunks that hold a revisited candidate, a warp a chunk
+                // recompute the chunks that hold a revisited candidate, a warp a chunk: the warps
+                // walk the revisit list and the first to claim a chunk's mark recomputes it (the
+                // marked chunks are found from the list, not by a walk over every chunk)
                 const int nch = (ncand + 31) >> 5, warp = rk >> 5, lane = rk & 31, nw = ts >> 5;
-                for (int q = warp; q < nch; q += nw) {
-                    if (!wdirty[q]) continue;
+                for (int i = warp; i < nd; i += nw) {
+                    const int q = dset[i] >> 5;
+                    int claim = 0;
+                    if (lane == 0) claim = atomicExch(&wdirty[q], 0);
+                    if (!__shfl_sync(0xffffffffu, claim, 0)) continue;
                     const int t = 32 * q + lane;
                     float a = 1.0f;
                     int kb = -1;
@@ -4988,7 +4993,7 @@ DG void toi_world_t(const Ctx& x, int w, float* sbp, const Team& tm, bool prepar
                         const int ok = __shfl_xor_sync(0xffffffffu, kb, o);
                         if (oa < a || (oa == a && ok > kb)) { a = oa; kb = ok; }
                     }
-                    if (lane == 0) { wmin_a[q] = __float_as_uint(a); wmin_k[q] = kb; wdirty[q] = 0; }
+                    if (lane == 0) { wmin_a[q] = __float_as_uint(a); wmin_k[q] = kb; }
                 }
                 tm.sync();
                 // the minimum over the chunks (a slot's list position is n - 1 - slot)
