@@ -11,6 +11,11 @@
 //                     at once in reference constraint order, SynchronizeFixtures,
 //                     FindNewContacts), then b2World.SolveTOI (toi_world:
 //                     b2world.d:1127-1452), inv_dt0 and ClearForces
+//   k_step_fused      option (dbox_world_set_fused_step): the four phases above for each
+//                     world on its warp, x.steps whole steps in one launch
+// Large worlds (4,096+ fixtures) take kernels of their own: k_begin_big, k_collide_finish_big,
+// k_solve_big, k_pairs_block and k_finish_big_block (AddPair, SolveTOI's setup passes) on
+// thread-block clusters, k_toi_big (SolveTOI's event loop) on a 512-thread block.
 //
 // Gauss-Seidel order: inside an island every constraint reads the velocities
 // (positions) its predecessors in island order wrote.  The kernels assign each
