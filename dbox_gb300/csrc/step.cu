@@ -5704,14 +5704,29 @@ DG void big_pos_row(const Ctx& x, const BigSweep& s, int idx) {
         atomicOr(&s.iflags[is], 4);
     }
 }
-// levels 1..maxL in order, a level's rows over the cluster's threads, a barrier between levels
+// levels 1..maxL in order with a barrier between levels.  On a cluster, a level of more than
+// kNarrowRows rows is dealt over the cluster's threads and ends in a cluster barrier; a run of
+// narrower levels is swept by the first block alone (r0), with block barriers between its
+// levels, while the other blocks wait at the cluster barrier after the run: a cluster barrier
+// costs thousands of cycles however few the level's rows.  Rows and body state live in global
+// memory, so any block may sweep any level; every block finds the same runs.
+constexpr int kNarrowRows = 128;
 template <class F>
-DG void cluster_levels(const int* lvl, int maxL, int gtid, int gsize, bool clustered, F&& f) {
-    for (int L = 1; L <= maxL; ++L) {
-        const int e = lvl[L + 1];
-        for (int idx = lvl[L] + gtid; idx < e; idx += gsize) f(idx);
-        if (clustered) cluster_sync();
-        else __syncthreads();
+DG void cluster_levels(const int* lvl, int maxL, int gtid, int gsize, bool clustered, bool r0, F&& f) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int L = 1; L <= maxL;) {
+        const int s = lvl[L], e = lvl[L + 1];
+        const bool wide = !clustered || e - s > kNarrowRows;
+        if (!wide && !r0) {                                             // a run of narrow levels: wait after it
+            while (L <= maxL && lvl[L + 1] - lvl[L] <= kNarrowRows) ++L;
+            cluster_sync();
+            continue;
+        }
+        for (int idx = wide ? s + gtid : s + tid; idx < e; idx += wide ? gsize : nt) f(idx);   // one call site
+        ++L;
+        if (!clustered) __syncthreads();
+        else if (wide || L > maxL || lvl[L + 1] - lvl[L] > kNarrowRows) cluster_sync();   // the cluster meets
+        else __syncthreads();                                           // the first block's next narrow level
     }
 }
 __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant__ Ctx x) {
@@ -6148,14 +6163,14 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
     bs_.iminsep = iminsep;
     // warm start contacts, then joints' InitVelocityConstraints (b2island.d:133-146)
     if (njI == 0) {
-        if (warm) cluster_levels(bs_.lvl_v, maxLv, gtid, gsize, clustered, [&](int idx) { big_warm_row(x, bs_, idx); });
+        if (warm) cluster_levels(bs_.lvl_v, maxLv, gtid, gsize, clustered, r0, [&](int idx) { big_warm_row(x, bs_, idx); });
     } else {
-        cluster_levels(bs_.lvl_p, maxLp, gtid, gsize, clustered, [&](int idx) { big_warm_row(x, bs_, idx); });
+        cluster_levels(bs_.lvl_p, maxLp, gtid, gsize, clustered, r0, [&](int idx) { big_warm_row(x, bs_, idx); });
     }
     stampb(5);
     // velocity iterations (b2island.d:153-161)
     for (int it = 0; it < x.vel_iters; ++it)
-        cluster_levels(bs_.lvl_v, maxLv, gtid, gsize, clustered, [&](int idx) { big_vel_row(x, bs_, idx, it); });
+        cluster_levels(bs_.lvl_v, maxLv, gtid, gsize, clustered, r0, [&](int idx) { big_vel_row(x, bs_, idx, it); });
     stampb(6);
     if (x.measure && r0) {
         // one extra velocity sweep that changes nothing: velocities kept aside and put back,
@@ -6244,7 +6259,7 @@ __global__ void __launch_bounds__(kBigThreads) k_solve_big(const __grid_constant
             iflags[is] &= ~4;
         }
         csync();
-        cluster_levels(bs_.lvl_p, maxLp, gtid, gsize, clustered, [&](int idx) { big_pos_row(x, bs_, idx); });
+        cluster_levels(bs_.lvl_p, maxLp, gtid, gsize, clustered, r0, [&](int idx) { big_pos_row(x, bs_, idx); });
         bool go = false;
         if (r0) {                                                      // the islands' checks
         int psolved = 0;
